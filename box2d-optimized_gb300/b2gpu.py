@@ -1,0 +1,348 @@
+"""Python binding of libb2g.so (the GB300 Step engine) through its C ABI (include/b2g_capi.h).
+
+The records below mirror the C structs field for field (ctypes applies the same alignment rules
+as the C compiler). ``Lib`` loads the shared library built in-tree by ``build.py``; there is no
+fallback path: if the library is missing, loading fails with an error that says how to build it.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+import numpy as np
+
+PKG_DIR = Path(__file__).resolve().parent
+LIB_PATH = PKG_DIR / "_build" / "libb2g.so"
+
+B2G_OK = 0
+STATUS = {0: "OK", 1: "INVALID_ARG", 2: "OUT_OF_MEMORY", 3: "TIMEOUT", 4: "WORLD_FAULT", 5: "CUDA",
+          6: "LOCKED", 7: "CAPACITY"}
+
+STATIC, KINEMATIC, DYNAMIC = 0, 1, 2
+SHAPE_CIRCLE, SHAPE_EDGE, SHAPE_POLYGON = 0, 1, 2
+JOINT_REVOLUTE, JOINT_PRISMATIC, JOINT_DISTANCE = 1, 2, 3
+POLY_HULL, POLY_BOX, POLY_BOX_ORIENTED, POLY_RAW = 0, 1, 2, 3
+SCENE_PYRAMID, SCENE_MIXED_DROP, SCENE_CHAINS, SCENE_BATCH_WORLD = 0, 1, 2, 3
+EVENT_BEGIN, EVENT_END, EVENT_PRESOLVE, EVENT_POSTSOLVE = 1, 2, 3, 4
+CONTACT_TOUCHING, CONTACT_ENABLED = 2, 4
+
+F2 = C.c_float * 2
+
+
+class Shape(C.Structure):
+    _fields_ = [("type", C.c_int32), ("count", C.c_int32), ("radius", C.c_float),
+                ("one_sided", C.c_int32), ("vertices", F2 * 8), ("normals", F2 * 8),
+                ("centroid", F2)]
+
+
+class ManifoldPoint(C.Structure):
+    _fields_ = [("local_point", F2), ("normal_impulse", C.c_float),
+                ("tangent_impulse", C.c_float), ("id", C.c_uint32)]
+
+
+class Manifold(C.Structure):
+    _fields_ = [("points", ManifoldPoint * 2), ("local_normal", F2), ("local_point", F2),
+                ("type", C.c_int32), ("point_count", C.c_int32)]
+
+
+class BodyDef(C.Structure):
+    _fields_ = [("type", C.c_int32), ("position", F2), ("angle", C.c_float),
+                ("linear_velocity", F2), ("angular_velocity", C.c_float),
+                ("linear_damping", C.c_float), ("angular_damping", C.c_float),
+                ("gravity_scale", C.c_float), ("allow_sleep", C.c_int32), ("awake", C.c_int32),
+                ("fixed_rotation", C.c_int32), ("bullet", C.c_int32), ("enabled", C.c_int32),
+                ("user_data", C.c_uint64)]
+
+
+class FixtureDef(C.Structure):
+    _fields_ = [("body", C.c_int32), ("shape_type", C.c_int32), ("poly_mode", C.c_int32),
+                ("count", C.c_int32), ("verts", F2 * 8), ("box", C.c_float * 5),
+                ("radius", C.c_float), ("center", F2), ("one_sided", C.c_int32),
+                ("friction", C.c_float), ("restitution", C.c_float),
+                ("restitution_threshold", C.c_float), ("density", C.c_float),
+                ("is_sensor", C.c_int32), ("category_bits", C.c_uint16),
+                ("mask_bits", C.c_uint16), ("group_index", C.c_int16), ("pad0", C.c_int16),
+                ("user_data", C.c_uint64), ("shape", Shape)]
+
+
+class JointDef(C.Structure):
+    _fields_ = [("type", C.c_int32), ("body_a", C.c_int32), ("body_b", C.c_int32),
+                ("collide_connected", C.c_int32), ("local_anchor_a", F2),
+                ("local_anchor_b", F2), ("reference_angle", C.c_float),
+                ("local_axis_a", F2), ("enable_limit", C.c_int32), ("lower", C.c_float),
+                ("upper", C.c_float), ("enable_motor", C.c_int32), ("max_motor", C.c_float),
+                ("motor_speed", C.c_float), ("length", C.c_float), ("min_length", C.c_float),
+                ("max_length", C.c_float), ("stiffness", C.c_float), ("damping", C.c_float),
+                ("user_data", C.c_uint64)]
+
+
+class Body(C.Structure):
+    _fields_ = [("xf", C.c_float * 4), ("c", F2), ("a", C.c_float), ("v", F2),
+                ("w", C.c_float), ("local_center", F2), ("mass", C.c_float),
+                ("inv_mass", C.c_float), ("inertia", C.c_float), ("inv_inertia", C.c_float),
+                ("linear_damping", C.c_float), ("angular_damping", C.c_float),
+                ("gravity_scale", C.c_float), ("force", F2), ("torque", C.c_float),
+                ("type", C.c_int32), ("flags", C.c_uint32)]
+
+
+class Fixture(C.Structure):
+    _fields_ = [("shape", Shape), ("body", C.c_int32), ("density", C.c_float),
+                ("friction", C.c_float), ("restitution", C.c_float),
+                ("restitution_threshold", C.c_float), ("category_bits", C.c_uint16),
+                ("mask_bits", C.c_uint16), ("group_index", C.c_int16), ("is_sensor", C.c_uint8),
+                ("pad0", C.c_uint8)]
+
+
+class Joint(C.Structure):
+    _fields_ = [("def_", JointDef), ("impulse", C.c_float * 3), ("motor_impulse", C.c_float),
+                ("lower_impulse", C.c_float), ("upper_impulse", C.c_float),
+                ("reaction_force", F2), ("reaction_torque", C.c_float)]
+
+
+class Contact(C.Structure):
+    _fields_ = [("fixture_a", C.c_int32), ("fixture_b", C.c_int32), ("flags", C.c_uint32),
+                ("friction", C.c_float), ("restitution", C.c_float),
+                ("restitution_threshold", C.c_float), ("tangent_speed", C.c_float),
+                ("manifold", Manifold)]
+
+
+class Event(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("world", C.c_int32), ("fixture_a", C.c_int32),
+                ("fixture_b", C.c_int32), ("point_count", C.c_int32),
+                ("normal_impulses", F2), ("tangent_impulses", F2), ("old_manifold", Manifold)]
+
+
+class Profile(C.Structure):
+    _fields_ = [("step", C.c_float), ("collide", C.c_float), ("solve", C.c_float),
+                ("broadphase", C.c_float), ("solve_toi", C.c_float), ("bodies", C.c_int64),
+                ("fixtures", C.c_int64), ("contacts", C.c_int64), ("touching", C.c_int64),
+                ("joints", C.c_int64), ("colors_max", C.c_int64)]
+
+
+class RequestResult(C.Structure):
+    _fields_ = [("request_id", C.c_int64), ("status", C.c_int32), ("bodies", C.c_int32),
+                ("steps", C.c_int32), ("submit_time_s", C.c_double),
+                ("admit_time_s", C.c_double), ("finish_time_s", C.c_double),
+                ("checksum", C.c_float * 4)]
+
+
+RECORD_SIZES = {"b2g_shape": 152, "b2g_manifold_point": 20, "b2g_manifold": 64,
+                "b2g_body": 100}
+
+
+def body_array_to_numpy(arr) -> dict:
+    """Body records -> dict of numpy arrays (xf[n,4], c[n,2], a[n], v[n,2], w[n], type[n])."""
+    n = len(arr)
+    raw = np.frombuffer(arr, dtype=np.uint8).reshape(n, C.sizeof(Body))
+    f = raw[:, :92].copy().view(np.float32).reshape(n, 23)
+    t = raw[:, 92:96].copy().view(np.int32).reshape(n)
+    return {"xf": f[:, 0:4], "c": f[:, 4:6], "a": f[:, 6], "v": f[:, 7:9], "w": f[:, 9],
+            "local_center": f[:, 10:12], "mass": f[:, 12], "inv_mass": f[:, 13],
+            "inertia": f[:, 14], "inv_inertia": f[:, 15], "type": t}
+
+
+class B2GError(RuntimeError):
+    pass
+
+
+def _check(status: int, what: str, lib=None):
+    if status != B2G_OK:
+        detail = ""
+        if lib is not None:
+            try:
+                detail = lib.b2g_last_error().decode()
+            except Exception:  # noqa: BLE001 - the message is best effort
+                detail = ""
+        raise B2GError(f"{what} failed: {STATUS.get(status, status)} {detail}")
+
+
+class Lib:
+    """The loaded libb2g.so with argument types declared for every C-ABI entry point."""
+
+    SYMBOLS = [
+        "b2g_batch_create", "b2g_batch_destroy", "b2g_world_add", "b2g_world_count",
+        "b2g_world_set_gravity", "b2g_world_set_flags", "b2g_bodies_add", "b2g_fixtures_add",
+        "b2g_joints_add", "b2g_world_sizes", "b2g_step", "b2g_step_n", "b2g_reserve",
+        "b2g_bodies_read", "b2g_bodies_write", "b2g_batch_read_states", "b2g_fixtures_read",
+        "b2g_joints_read", "b2g_contacts_read", "b2g_events_enable", "b2g_events_drain",
+        "b2g_profile_get", "b2g_solver_order", "b2g_collide", "b2g_pairs", "b2g_scene_build",
+        "b2g_batch_world_params", "b2g_server_create", "b2g_server_destroy", "b2g_server_submit",
+        "b2g_server_tick", "b2g_server_poll", "b2g_server_stats", "b2g_status_string",
+        "b2g_last_error", "b2g_device_count",
+    ]
+
+    def __init__(self, path: os.PathLike | str | None = None):
+        p = Path(path) if path else LIB_PATH
+        if not p.exists():
+            raise B2GError(f"{p} is missing: build it with `python -c 'import __graft_entry__ as g; "
+                           f"g.build()'` (the engine has no CPU fallback)")
+        self.path = p
+        self.lib = C.CDLL(str(p))
+        L = self.lib
+        vp, i32, u32, f32, i64 = C.c_void_p, C.c_int32, C.c_uint32, C.c_float, C.c_int64
+        P = C.POINTER
+        sig = {
+            "b2g_batch_create": ([C.c_int, C.c_uint64, P(vp)], C.c_int),
+            "b2g_batch_destroy": ([vp], C.c_int),
+            "b2g_world_add": ([vp, f32, f32, P(i32)], C.c_int),
+            "b2g_world_count": ([vp, P(i32)], C.c_int),
+            "b2g_world_set_gravity": ([vp, i32, f32, f32], C.c_int),
+            "b2g_world_set_flags": ([vp, i32, i32, i32, i32, i32], C.c_int),
+            "b2g_bodies_add": ([vp, i32, P(BodyDef), i32, P(i32)], C.c_int),
+            "b2g_fixtures_add": ([vp, i32, P(FixtureDef), i32, P(i32)], C.c_int),
+            "b2g_joints_add": ([vp, i32, P(JointDef), i32, P(i32)], C.c_int),
+            "b2g_world_sizes": ([vp, i32, P(i32), P(i32), P(i32), P(i32)], C.c_int),
+            "b2g_step": ([vp, f32, i32, i32, P(C.c_uint8)], C.c_int),
+            "b2g_step_n": ([vp, f32, i32, i32, i32, i32], C.c_int),
+            "b2g_reserve": ([vp, i64], C.c_int),
+            "b2g_bodies_read": ([vp, i32, i32, i32, P(Body)], C.c_int),
+            "b2g_bodies_write": ([vp, i32, i32, i32, P(Body)], C.c_int),
+            "b2g_batch_read_states": ([vp, P(f32), P(f32), i64, P(i64)], C.c_int),
+            "b2g_fixtures_read": ([vp, i32, i32, i32, P(Fixture)], C.c_int),
+            "b2g_joints_read": ([vp, i32, i32, i32, P(Joint)], C.c_int),
+            "b2g_contacts_read": ([vp, i32, P(Contact), i32, P(i32)], C.c_int),
+            "b2g_events_enable": ([vp, i32], C.c_int),
+            "b2g_events_drain": ([vp, P(Event), i32, P(i32)], C.c_int),
+            "b2g_profile_get": ([vp, P(Profile)], C.c_int),
+            "b2g_solver_order": ([vp, i32, P(i32), P(u32), i32, P(i32), P(u32), i32], C.c_int),
+            "b2g_collide": ([vp, vp, vp, vp, i32, vp, vp], C.c_int),
+            "b2g_pairs": ([vp, i32, vp, i64, P(i64), vp], C.c_int),
+            "b2g_scene_build": ([vp, i32, i32, u32, i32, f32, f32, P(i32)], C.c_int),
+            "b2g_batch_world_params": ([u32, P(i32), P(f32), P(f32)], C.c_int),
+            "b2g_server_create": ([C.c_int, C.c_uint64, i32, f32, i32, i32, P(vp)], C.c_int),
+            "b2g_server_destroy": ([vp], C.c_int),
+            "b2g_server_submit": ([vp, u32, i32, i32, P(i64)], C.c_int),
+            "b2g_server_tick": ([vp, P(i32), P(C.c_double)], C.c_int),
+            "b2g_server_poll": ([vp, P(RequestResult), i32, P(i32)], C.c_int),
+            "b2g_server_stats": ([vp, P(i64), P(i64), P(i64), P(i64), P(i64)], C.c_int),
+            "b2g_status_string": ([C.c_int], C.c_char_p),
+            "b2g_last_error": ([], C.c_char_p),
+            "b2g_device_count": ([P(i32)], C.c_int),
+        }
+        for name, (args, res) in sig.items():
+            fn = getattr(L, name)
+            fn.argtypes = args
+            fn.restype = res
+
+    def __getattr__(self, name):
+        return getattr(self.lib, name)
+
+    def check(self, status: int, what: str):
+        _check(status, what, self.lib)
+
+
+class Batch:
+    """A batch of worlds on one GPU (b2g_batch)."""
+
+    def __init__(self, lib: Lib, device: int = 0, budget_bytes: int = 0):
+        self.lib = lib
+        h = C.c_void_p()
+        lib.check(lib.b2g_batch_create(device, budget_bytes, C.byref(h)), "b2g_batch_create")
+        self.h = h
+
+    def close(self):
+        if self.h:
+            self.lib.b2g_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:  # noqa: BLE001 - interpreter shutdown
+            pass
+
+    def add_world(self, gx=0.0, gy=-10.0) -> int:
+        w = C.c_int32()
+        self.lib.check(self.lib.b2g_world_add(self.h, gx, gy, C.byref(w)), "b2g_world_add")
+        return w.value
+
+    def set_flags(self, world, allow_sleep=False, warm_starting=True, continuous=False,
+                  auto_clear_forces=True):
+        self.lib.check(self.lib.b2g_world_set_flags(self.h, world, int(allow_sleep),
+                                                    int(warm_starting), int(continuous),
+                                                    int(auto_clear_forces)),
+                       "b2g_world_set_flags")
+
+    def scene(self, world, kind, seed=1, n=20, p0=1.0, p1=0.6):
+        counts = (C.c_int32 * 3)()
+        self.lib.check(self.lib.b2g_scene_build(self.h, world, kind, seed, n, p0, p1, counts),
+                       "b2g_scene_build")
+        return tuple(counts)
+
+    def sizes(self, world):
+        v = [C.c_int32() for _ in range(4)]
+        self.lib.check(self.lib.b2g_world_sizes(self.h, world, *[C.byref(x) for x in v]),
+                       "b2g_world_sizes")
+        return tuple(x.value for x in v)
+
+    def step(self, dt=1 / 60, vi=8, pi=3, mask=None):
+        m = None
+        if mask is not None:
+            arr = (C.c_uint8 * len(mask))(*[1 if x else 0 for x in mask])
+            m = C.cast(arr, C.POINTER(C.c_uint8))
+        self.lib.check(self.lib.b2g_step(self.h, dt, vi, pi, m), "b2g_step")
+
+    def step_n(self, n, dt=1 / 60, vi=8, pi=3, use_graph=False):
+        self.lib.check(self.lib.b2g_step_n(self.h, dt, vi, pi, n, int(use_graph)), "b2g_step_n")
+
+    def bodies(self, world):
+        nb = self.sizes(world)[0]
+        arr = (Body * max(nb, 1))()
+        self.lib.check(self.lib.b2g_bodies_read(self.h, world, 0, nb, arr), "b2g_bodies_read")
+        return arr[:nb] if nb else []
+
+    def bodies_np(self, world):
+        nb = self.sizes(world)[0]
+        arr = (Body * max(nb, 1))()
+        self.lib.check(self.lib.b2g_bodies_read(self.h, world, 0, nb, arr), "b2g_bodies_read")
+        return body_array_to_numpy((Body * nb).from_buffer(arr)) if nb else None
+
+    def write_bodies(self, world, recs):
+        arr = (Body * len(recs))(*recs)
+        self.lib.check(self.lib.b2g_bodies_write(self.h, world, 0, len(recs), arr),
+                       "b2g_bodies_write")
+
+    def fixtures(self, world):
+        nf = self.sizes(world)[1]
+        arr = (Fixture * max(nf, 1))()
+        self.lib.check(self.lib.b2g_fixtures_read(self.h, world, 0, nf, arr), "b2g_fixtures_read")
+        return arr[:nf] if nf else []
+
+    def joints(self, world):
+        nj = self.sizes(world)[2]
+        arr = (Joint * max(nj, 1))()
+        self.lib.check(self.lib.b2g_joints_read(self.h, world, 0, nj, arr), "b2g_joints_read")
+        return arr[:nj] if nj else []
+
+    def contacts(self, world):
+        n = C.c_int32()
+        self.lib.check(self.lib.b2g_contacts_read(self.h, world, None, 0, C.byref(n)),
+                       "b2g_contacts_read")
+        arr = (Contact * max(n.value, 1))()
+        self.lib.check(self.lib.b2g_contacts_read(self.h, world, arr, n.value, C.byref(n)),
+                       "b2g_contacts_read")
+        return arr[:n.value]
+
+    def solver_order(self, world, nc, nj):
+        cc = (C.c_int32 * max(nc, 1))()
+        cp = (C.c_uint32 * max(nc, 1))()
+        jc = (C.c_int32 * max(nj, 1))()
+        jp = (C.c_uint32 * max(nj, 1))()
+        self.lib.check(self.lib.b2g_solver_order(self.h, world, cc, cp, nc, jc, jp, nj),
+                       "b2g_solver_order")
+        return list(cc[:nc]), list(cp[:nc]), list(jc[:nj]), list(jp[:nj])
+
+    def events(self, enable=None, cap=1 << 20):
+        if enable is not None:
+            self.lib.check(self.lib.b2g_events_enable(self.h, int(enable)), "b2g_events_enable")
+            return None
+        n = C.c_int32()
+        arr = (Event * cap)()
+        self.lib.check(self.lib.b2g_events_drain(self.h, arr, cap, C.byref(n)), "b2g_events_drain")
+        return arr[:n.value]
+
+    def profile(self) -> Profile:
+        p = Profile()
+        self.lib.check(self.lib.b2g_profile_get(self.h, C.byref(p)), "b2g_profile_get")
+        return p

@@ -1,0 +1,389 @@
+/*
+ * b2g_capi.h - C ABI of the GB300 Step engine (box2d-optimized_gb300).
+ *
+ * One shared library, libb2g.so, steps batches of Box2D worlds on one GPU. The ABI takes plain
+ * pointers, sizes and POD structs; no C++ or torch types cross it; every entry point returns an
+ * int status (B2G_OK or a B2G_E* code) and never throws.
+ *
+ * Each entry point replaces one piece of the reference's public C++ API (file:line cited beside
+ * it). The C++ facade in box2d-optimized_gb300/include/box2d/ (b2World, b2Body, b2Fixture,
+ * b2Joint, b2Contact) is written on top of these calls.
+ *
+ * Threading: one host thread per batch handle. A batch may hold many independent worlds; a world
+ * is addressed by (batch, world index). Bodies, fixtures and joints are addressed by their
+ * creation index inside their world.
+ */
+#ifndef B2G_CAPI_H
+#define B2G_CAPI_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(_WIN32)
+#define B2G_API __declspec(dllexport)
+#else
+#define B2G_API __attribute__((visibility("default")))
+#endif
+
+/* ---- status codes ------------------------------------------------------------------------ */
+#define B2G_OK 0
+#define B2G_E_INVALID_ARG 1   /* bad handle, index, size or malformed definition            */
+#define B2G_E_OUT_OF_MEMORY 2 /* host or device allocation failed / budget exceeded          */
+#define B2G_E_TIMEOUT 3       /* a bounded device wait ran out (the step did not complete)   */
+#define B2G_E_WORLD_FAULT 4   /* a world produced a non-finite state and was frozen          */
+#define B2G_E_CUDA 5          /* a CUDA runtime call failed (no device, launch error, ...)    */
+#define B2G_E_LOCKED 6        /* world is locked (inside a step)                              */
+#define B2G_E_CAPACITY 7      /* a fixed-size buffer is too small for the request            */
+
+/* ---- enums mirroring the reference's values ---------------------------------------------- */
+/* b2BodyType, include/box2d/b2_body.h:44-49 */
+#define B2G_STATIC 0
+#define B2G_KINEMATIC 1
+#define B2G_DYNAMIC 2
+/* b2Shape::Type, include/box2d/b2_shape.h:52-59 */
+#define B2G_SHAPE_CIRCLE 0
+#define B2G_SHAPE_EDGE 1
+#define B2G_SHAPE_POLYGON 2
+/* b2JointType, include/box2d/b2_joint.h:35-49 (the three supported kinds) */
+#define B2G_JOINT_REVOLUTE 1
+#define B2G_JOINT_PRISMATIC 2
+#define B2G_JOINT_DISTANCE 3
+/* b2Manifold::Type, include/box2d/b2_collision.h:105-110 */
+#define B2G_MANIFOLD_CIRCLES 0
+#define B2G_MANIFOLD_FACE_A 1
+#define B2G_MANIFOLD_FACE_B 2
+
+#define B2G_MAX_POLYGON_VERTICES 8 /* b2_maxPolygonVertices, b2_settings.h:54 */
+
+/* ---- geometry ----------------------------------------------------------------------------- */
+/* A processed shape in its body frame (b2CircleShape / b2EdgeShape / b2PolygonShape state).
+ *   circle : vertices[0] = m_p, radius = m_radius
+ *   edge   : vertices[0] = m_vertex1, [1] = m_vertex2, [2] = m_vertex0, [3] = m_vertex3,
+ *            one_sided = m_oneSided, radius = b2_polygonRadius
+ *   polygon: vertices/normals[0..count), centroid = m_centroid, radius = b2_polygonRadius   */
+typedef struct b2g_shape {
+  int32_t type;
+  int32_t count;
+  float radius;
+  int32_t one_sided;
+  float vertices[B2G_MAX_POLYGON_VERTICES][2];
+  float normals[B2G_MAX_POLYGON_VERTICES][2];
+  float centroid[2];
+} b2g_shape; /* 152 bytes */
+
+/* b2ManifoldPoint (b2_collision.h:75-85): 20 bytes. id = b2ContactID.key, i.e.
+ * indexA | indexB << 8 | typeA << 16 | typeB << 24. */
+typedef struct b2g_manifold_point {
+  float local_point[2];
+  float normal_impulse;
+  float tangent_impulse;
+  uint32_t id;
+} b2g_manifold_point;
+
+/* b2Manifold (b2_collision.h:103-117): 64 bytes, same field meaning and order. */
+typedef struct b2g_manifold {
+  b2g_manifold_point points[2];
+  float local_normal[2];
+  float local_point[2];
+  int32_t type;
+  int32_t point_count;
+} b2g_manifold;
+
+/* ---- definitions (inputs) ------------------------------------------------------------------ */
+/* b2BodyDef, include/box2d/b2_body.h:52-130 */
+typedef struct b2g_body_def {
+  int32_t type;
+  float position[2];
+  float angle;
+  float linear_velocity[2];
+  float angular_velocity;
+  float linear_damping;
+  float angular_damping;
+  float gravity_scale;
+  int32_t allow_sleep;
+  int32_t awake;
+  int32_t fixed_rotation;
+  int32_t bullet;
+  int32_t enabled;
+  uint64_t user_data;
+} b2g_body_def;
+
+/* How a polygon fixture's geometry is given. */
+#define B2G_POLY_HULL 0       /* b2PolygonShape::Set(vertices, count)          b2_polygon_shape.cpp:113 */
+#define B2G_POLY_BOX 1        /* b2PolygonShape::SetAsBox(hx, hy)               b2_polygon_shape.cpp:36  */
+#define B2G_POLY_BOX_ORIENTED 2 /* SetAsBox(hx, hy, center, angle)              b2_polygon_shape.cpp:50  */
+#define B2G_POLY_RAW 3        /* already-processed b2g_shape given in `shape`                           */
+
+/* b2FixtureDef (include/box2d/b2_fixture.h:60-110) with its shape given inline. */
+typedef struct b2g_fixture_def {
+  int32_t body;         /* creation index of the owning body in the same world */
+  int32_t shape_type;   /* B2G_SHAPE_* */
+  int32_t poly_mode;    /* B2G_POLY_* for polygons */
+  int32_t count;        /* raw vertex count for B2G_POLY_HULL */
+  float verts[B2G_MAX_POLYGON_VERTICES][2]; /* hull input; edge: v1, v2, v0, v3 */
+  float box[5];         /* hx, hy, center.x, center.y, angle */
+  float radius;         /* circle radius */
+  float center[2];      /* circle m_p */
+  int32_t one_sided;    /* edge */
+  float friction;
+  float restitution;
+  float restitution_threshold;
+  float density;
+  int32_t is_sensor;
+  uint16_t category_bits;
+  uint16_t mask_bits;
+  int16_t group_index;
+  int16_t pad0;
+  uint64_t user_data;
+  b2g_shape shape;      /* B2G_POLY_RAW input */
+} b2g_fixture_def;
+
+/* b2RevoluteJointDef / b2PrismaticJointDef / b2DistanceJointDef in one record
+ * (b2_revolute_joint.h:39-88, b2_prismatic_joint.h:35-88, b2_distance_joint.h:33-70). */
+typedef struct b2g_joint_def {
+  int32_t type;             /* B2G_JOINT_* */
+  int32_t body_a;
+  int32_t body_b;
+  int32_t collide_connected;
+  float local_anchor_a[2];
+  float local_anchor_b[2];
+  float reference_angle;    /* revolute, prismatic */
+  float local_axis_a[2];    /* prismatic (normalised on creation) */
+  int32_t enable_limit;
+  float lower;              /* lowerAngle / lowerTranslation */
+  float upper;              /* upperAngle / upperTranslation */
+  int32_t enable_motor;
+  float max_motor;          /* maxMotorTorque / maxMotorForce */
+  float motor_speed;
+  float length;             /* distance */
+  float min_length;
+  float max_length;
+  float stiffness;
+  float damping;
+  uint64_t user_data;
+} b2g_joint_def;
+
+/* ---- state records (outputs / snapshot) ------------------------------------------------------ */
+/* Body state and mass data (b2Body members, include/box2d/b2_body.h:480-560). */
+#define B2G_BODY_ENABLED 1u
+#define B2G_BODY_FIXED_ROTATION 2u
+#define B2G_BODY_BULLET 4u
+#define B2G_BODY_AWAKE 8u
+#define B2G_BODY_AUTO_SLEEP 16u
+typedef struct b2g_body {
+  float xf[4];             /* m_xf: p.x, p.y, q.s, q.c */
+  float c[2];              /* m_sweep.c */
+  float a;                 /* m_sweep.a */
+  float v[2];              /* m_linearVelocity */
+  float w;                 /* m_angularVelocity */
+  float local_center[2];   /* m_sweep.localCenter */
+  float mass, inv_mass, inertia, inv_inertia;
+  float linear_damping, angular_damping, gravity_scale;
+  float force[2];
+  float torque;
+  int32_t type;
+  uint32_t flags;
+} b2g_body; /* 100 bytes */
+
+typedef struct b2g_fixture {
+  b2g_shape shape;
+  int32_t body;
+  float density, friction, restitution, restitution_threshold;
+  uint16_t category_bits, mask_bits;
+  int16_t group_index;
+  uint8_t is_sensor;
+  uint8_t pad0;
+} b2g_fixture;
+
+/* Joint parameters and warm-start state. impulse[0..2]: revolute m_impulse (x, y), prismatic
+ * m_impulse (x, y), distance m_impulse in [0]. */
+typedef struct b2g_joint {
+  b2g_joint_def def;
+  float impulse[3];
+  float motor_impulse, lower_impulse, upper_impulse;
+  float reaction_force[2]; /* GetReactionForce(inv_dt of the last step) */
+  float reaction_torque;   /* GetReactionTorque(inv_dt of the last step) */
+} b2g_joint;
+
+/* b2Contact (include/box2d/b2_contact.h:155-173 flags) */
+#define B2G_CONTACT_TOUCHING 2u
+#define B2G_CONTACT_ENABLED 4u
+typedef struct b2g_contact {
+  int32_t fixture_a;       /* creation index of fixture A in its world */
+  int32_t fixture_b;
+  uint32_t flags;
+  float friction, restitution, restitution_threshold, tangent_speed;
+  b2g_manifold manifold;
+} b2g_contact;
+
+/* Listener events (b2ContactListener, b2_world_callbacks.h:133-209), delivered as a batch after
+ * each step in the order: End (contacts destroyed by the broadphase), Begin, End, PreSolve
+ * (from the narrowphase), PostSolve (from the solver). */
+#define B2G_EVENT_BEGIN 1
+#define B2G_EVENT_END 2
+#define B2G_EVENT_PRESOLVE 3
+#define B2G_EVENT_POSTSOLVE 4
+typedef struct b2g_event {
+  int32_t kind;
+  int32_t world;
+  int32_t fixture_a;
+  int32_t fixture_b;
+  int32_t point_count;     /* PostSolve: b2ContactImpulse::count */
+  float normal_impulses[2];
+  float tangent_impulses[2];
+  b2g_manifold old_manifold; /* PreSolve: the manifold before this step's update */
+} b2g_event;
+
+/* b2Profile (include/box2d/b2_time_step.h:29-36), milliseconds of the last step (device time). */
+typedef struct b2g_profile {
+  float step, collide, solve, broadphase, solve_toi;
+  int64_t bodies, fixtures, contacts, touching, joints, colors_max;
+} b2g_profile;
+
+/* ---- batch lifecycle ------------------------------------------------------------------------ */
+typedef struct b2g_batch b2g_batch;
+
+/* Device memory budget in bytes (0 = no limit). Allocation beyond it fails with
+ * B2G_E_OUT_OF_MEMORY instead of reaching cudaMalloc. */
+B2G_API int b2g_batch_create(int device, uint64_t budget_bytes, b2g_batch** out);
+B2G_API int b2g_batch_destroy(b2g_batch* b);
+
+/* b2World::b2World(gravity), include/box2d/b2_world.h:54 */
+B2G_API int b2g_world_add(b2g_batch* b, float gx, float gy, int32_t* out_world);
+B2G_API int b2g_world_count(b2g_batch* b, int32_t* out_n);
+/* b2World::SetGravity / SetAllowSleeping / SetWarmStarting / SetContinuousPhysics /
+ * SetAutoClearForces, include/box2d/b2_world.h:195-235 */
+B2G_API int b2g_world_set_gravity(b2g_batch* b, int32_t world, float gx, float gy);
+B2G_API int b2g_world_set_flags(b2g_batch* b, int32_t world, int32_t allow_sleep,
+                                int32_t warm_starting, int32_t continuous, int32_t auto_clear_forces);
+
+/* b2World::CreateBody, include/box2d/b2_world.h:80 (bulk). out_ids may be NULL. */
+B2G_API int b2g_bodies_add(b2g_batch* b, int32_t world, const b2g_body_def* defs, int32_t n,
+                           int32_t* out_ids);
+/* b2Body::CreateFixture, src/dynamics/b2_body.cpp:230 (bulk; runs ResetMassData per body). */
+B2G_API int b2g_fixtures_add(b2g_batch* b, int32_t world, const b2g_fixture_def* defs, int32_t n,
+                             int32_t* out_ids);
+/* b2World::CreateJoint, src/dynamics/b2_world.cpp:268 (bulk). */
+B2G_API int b2g_joints_add(b2g_batch* b, int32_t world, const b2g_joint_def* defs, int32_t n,
+                           int32_t* out_ids);
+
+/* Counts of one world. */
+B2G_API int b2g_world_sizes(b2g_batch* b, int32_t world, int32_t* bodies, int32_t* fixtures,
+                            int32_t* joints, int32_t* contacts);
+
+/* ---- stepping ------------------------------------------------------------------------------- */
+/* b2World::Step(dt, velocityIterations, positionIterations), include/box2d/b2_world.h:127-141,
+ * for every world of the batch whose world_mask entry is non-zero (world_mask NULL = all).
+ * Returns after the step's device work has been enqueued and completed. */
+B2G_API int b2g_step(b2g_batch* b, float dt, int32_t velocity_iterations,
+                     int32_t position_iterations, const uint8_t* world_mask);
+/* n steps back to back; with use_graph != 0 the whole Step is captured once in a CUDA graph and
+ * replayed (buffers are sized on the first step; see b2g_reserve). */
+B2G_API int b2g_step_n(b2g_batch* b, float dt, int32_t velocity_iterations,
+                       int32_t position_iterations, int32_t n, int32_t use_graph);
+/* Pre-size the pair/contact buffers to at least `contacts` entries in total. */
+B2G_API int b2g_reserve(b2g_batch* b, int64_t contacts);
+
+/* ---- reading and writing state ---------------------------------------------------------------- */
+/* b2Body getters (GetPosition, GetAngle, GetLinearVelocity, ...), include/box2d/b2_body.h:141-260 */
+B2G_API int b2g_bodies_read(b2g_batch* b, int32_t world, int32_t first, int32_t n, b2g_body* out);
+/* b2Body::SetTransform / SetLinearVelocity / SetAngularVelocity / ApplyForce...,
+ * src/dynamics/b2_body.cpp:482 (writes xf, sweep, velocities, force and torque of each record) */
+B2G_API int b2g_bodies_write(b2g_batch* b, int32_t world, int32_t first, int32_t n,
+                             const b2g_body* in);
+/* All body states of all worlds as packed arrays (device order = world, then creation order).
+ * Any pointer may be NULL. */
+B2G_API int b2g_batch_read_states(b2g_batch* b, float* xf4, float* v3, int64_t cap_bodies,
+                                  int64_t* n_bodies);
+B2G_API int b2g_fixtures_read(b2g_batch* b, int32_t world, int32_t first, int32_t n,
+                              b2g_fixture* out);
+B2G_API int b2g_joints_read(b2g_batch* b, int32_t world, int32_t first, int32_t n, b2g_joint* out);
+/* b2World::GetContactList / b2Contact::GetManifold / IsTouching, b2_world.h:187-191,
+ * b2_contact.h:71-143. Contacts are listed in the engine's canonical order. */
+B2G_API int b2g_contacts_read(b2g_batch* b, int32_t world, b2g_contact* out, int32_t cap,
+                              int32_t* n);
+/* b2ContactListener callbacks of the last step, as a batch (see b2g_event). enable != 0 turns
+ * event recording on for the batch (off by default; recording costs device time). */
+B2G_API int b2g_events_enable(b2g_batch* b, int32_t enable);
+B2G_API int b2g_events_drain(b2g_batch* b, b2g_event* out, int32_t cap, int32_t* n);
+/* b2World::GetProfile, include/box2d/b2_world.h:249 */
+B2G_API int b2g_profile_get(b2g_batch* b, b2g_profile* out);
+/* The constraint colour and solve-order record of the last step of one world, for replaying the
+ * same Gauss-Seidel order on a CPU solver: contact_color[i] for contact i in b2g_contacts_read
+ * order (-1 if not solved), joint_color[j] per joint, and the priority keys. */
+B2G_API int b2g_solver_order(b2g_batch* b, int32_t world, int32_t* contact_color,
+                             uint32_t* contact_priority, int32_t nc, int32_t* joint_color,
+                             uint32_t* joint_priority, int32_t nj);
+
+/* ---- standalone kernels over caller buffers (device pointers) ------------------------------ */
+/* Narrowphase: manifolds for n shape pairs (b2CollidePolygons / b2CollideCircles /
+ * b2CollidePolygonAndCircle / b2CollideEdgeAndCircle / b2CollideEdgeAndPolygon,
+ * include/box2d/b2_collision.h:225-259). Shapes must be ordered like b2Contact::Create's
+ * dispatch (src/dynamics/b2_contact.cpp:46-56): A's type >= B's type, edge-edge unsupported.
+ * All pointers are device pointers; xf records are (p.x, p.y, q.s, q.c). */
+B2G_API int b2g_collide(const b2g_shape* d_shape_a, const float* d_xf_a, const b2g_shape* d_shape_b,
+                        const float* d_xf_b, int32_t n, b2g_manifold* d_out, void* stream);
+/* Broadphase: every pair (i < j) of the n AABBs (lo.x, lo.y, hi.x, hi.y) that overlap with the
+ * reference's inclusive test (include/box2d/b2_collision.h:270-276), sorted by (i, j), written
+ * as i << 32 | j into d_pairs (capacity cap). *n_pairs receives the total, which may exceed cap
+ * (then nothing beyond cap is written and B2G_E_CAPACITY is returned).
+ * Replaces b2BroadPhase::UpdateAndQuery's pair report (include/box2d/b2_broad_phase.h:252-343). */
+B2G_API int b2g_pairs(const float* d_aabbs, int32_t n, uint64_t* d_pairs, int64_t cap,
+                      int64_t* n_pairs, void* stream);
+
+/* ---- scenes ------------------------------------------------------------------------------------ */
+/* Builds one of the seeded benchmark scenes into `world` through the b2World facade calls
+ * (box2d-optimized_gb300/scenes/scenes.h). kind: 0 pyramid(rows=n, density=p0, friction=p1),
+ * 1 mixed drop(n bodies), 2 chains over pile(n chains, 20 links, p0 circles),
+ * 3 batch world(n bodies), with `seed`. counts[3] = bodies, fixtures, joints. */
+#define B2G_SCENE_PYRAMID 0
+#define B2G_SCENE_MIXED_DROP 1
+#define B2G_SCENE_CHAINS 2
+#define B2G_SCENE_BATCH_WORLD 3
+B2G_API int b2g_scene_build(b2g_batch* b, int32_t world, int32_t kind, uint32_t seed, int32_t n,
+                            float p0, float p1, int32_t* counts);
+B2G_API int b2g_batch_world_params(uint32_t seed, int32_t* n_bodies, float* gx, float* gy);
+
+/* ---- serving ------------------------------------------------------------------------------------ */
+typedef struct b2g_server b2g_server;
+typedef struct b2g_request_result {
+  int64_t request_id;
+  int32_t status;           /* B2G_OK, B2G_E_OUT_OF_MEMORY (rejected), ... */
+  int32_t bodies;
+  int32_t steps;
+  double submit_time_s;     /* host monotonic clock */
+  double admit_time_s;
+  double finish_time_s;
+  float checksum[4];        /* sum of x, y, angle, |v| over the world's bodies at the end */
+} b2g_request_result;
+/* A continuous-batching server: rollout requests (a seeded scene + K steps) are admitted as
+ * slots and device memory free up, packed into one batched Step with every other active
+ * world, and retired when their K steps are done. */
+B2G_API int b2g_server_create(int device, uint64_t budget_bytes, int32_t max_worlds,
+                              float dt, int32_t velocity_iterations, int32_t position_iterations,
+                              b2g_server** out);
+B2G_API int b2g_server_destroy(b2g_server* s);
+/* Queue a request: scene B2G_SCENE_BATCH_WORLD with `seed`, `bodies` bodies, `steps` steps. */
+B2G_API int b2g_server_submit(b2g_server* s, uint32_t seed, int32_t bodies, int32_t steps,
+                              int64_t* out_request_id);
+/* Admit what fits, run one batched step of all active worlds, retire finished ones.
+ * *active receives the number of worlds stepped; *step_ms the step's wall time. */
+B2G_API int b2g_server_tick(b2g_server* s, int32_t* active, double* step_ms);
+B2G_API int b2g_server_poll(b2g_server* s, b2g_request_result* out, int32_t cap, int32_t* n);
+B2G_API int b2g_server_stats(b2g_server* s, int64_t* queued, int64_t* active,
+                             int64_t* completed, int64_t* rejected, int64_t* hbm_bytes);
+
+/* ---- misc ---------------------------------------------------------------------------------------- */
+B2G_API const char* b2g_status_string(int status);
+B2G_API const char* b2g_last_error(void);
+B2G_API int b2g_device_count(int32_t* n);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* B2G_CAPI_H */

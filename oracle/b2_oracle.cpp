@@ -1,0 +1,2341 @@
+// b2_oracle.cpp - CPU ORACLE for the GB300 Step engine. TEST INFRASTRUCTURE ONLY.
+//
+// A plain, single-threaded restatement of box2d-optimized's per-step hot path
+// (b2World::Step, src/dynamics/b2_world.cpp:1108-1171) in the canonical order the GPU engine
+// uses, so that the engine's results can be checked against it value for value:
+//   * contacts are kept sorted by (emitter fixture, partner fixture) instead of the reference's
+//     broadphase traversal order;
+//   * Gauss-Seidel constraint order is colour by colour (a greedy colouring in hashed-priority
+//     order, identical to the engine's) instead of island DFS order, and the position solver's
+//     early exit is per world instead of per island;
+//   * sine/cosine come from a portable routine (Cody-Waite reduction + Taylor polynomials) that
+//     the engine evaluates identically on the GPU; `orc_set_libm_trig(1)` switches the oracle to
+//     libm sinf/cosf like the reference.
+// Everything else restates the reference's arithmetic in the reference's operation order; each
+// function cites the reference file:line it follows.
+//
+// Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg load this library; the
+// product never links or calls it. Pinned against the reference engine compiled from its own
+// sources (oracle/_ref, see Makefile) and against committed golden vectors in tests/golden/.
+
+#include <algorithm>
+#include <atomic>
+#include <cfloat>
+#include <chrono>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <thread>
+#include <vector>
+
+#include "../include/b2g_capi.h"
+
+namespace orc {
+
+// ------------------------------------------------------------------------------------------------
+// Constants (include/box2d/b2_common.h:39-41, 110-182; b2_settings.h:45-54)
+static const float kMaxFloat = FLT_MAX;
+static const float kEpsilon = FLT_EPSILON;
+static const float kPi = 3.14159265359f;
+static const float kLinearSlop = 0.005f;
+static const float kAngularSlop = (2.0f / 180.0f * kPi);
+static const float kPolygonRadius = (2.0f * kLinearSlop);
+static const float kMaxLinearCorrection = 0.2f;
+static const float kMaxAngularCorrection = (8.0f / 180.0f * kPi);
+static const float kMaxTranslation = 2.0f;
+static const float kMaxTranslationSquared = (kMaxTranslation * kMaxTranslation);
+static const float kMaxRotation = (0.5f * kPi);
+static const float kMaxRotationSquared = (kMaxRotation * kMaxRotation);
+static const float kBaumgarte = 0.2f;
+
+// ------------------------------------------------------------------------------------------------
+// Vector algebra with the reference's expression order (include/box2d/b2_math.h:56-735).
+struct V2 {
+  float x, y;
+};
+static inline V2 v2(float x, float y) { V2 r; r.x = x; r.y = y; return r; }
+static inline V2 operator+(V2 a, V2 b) { return v2(a.x + b.x, a.y + b.y); }
+static inline V2 operator-(V2 a, V2 b) { return v2(a.x - b.x, a.y - b.y); }
+static inline V2 operator-(V2 a) { return v2(-a.x, -a.y); }
+static inline V2 operator*(float s, V2 a) { return v2(s * a.x, s * a.y); }
+static inline void addTo(V2& a, V2 b) { a.x += b.x; a.y += b.y; }
+static inline void subFrom(V2& a, V2 b) { a.x -= b.x; a.y -= b.y; }
+static inline float dot(V2 a, V2 b) { return a.x * b.x + a.y * b.y; }
+static inline float cross(V2 a, V2 b) { return a.x * b.y - a.y * b.x; }
+static inline V2 cross(V2 a, float s) { return v2(s * a.y, -s * a.x); }
+static inline V2 cross(float s, V2 a) { return v2(-s * a.y, s * a.x); }
+static inline float lengthOf(V2 a) { return sqrtf(a.x * a.x + a.y * a.y); }
+static inline float lengthSq(V2 a) { return a.x * a.x + a.y * a.y; }
+static inline float distSq(V2 a, V2 b) { V2 c = a - b; return c.x * c.x + c.y * c.y; }
+// b2Vec2::Normalize, b2_math.h:117-130
+static inline float normalize(V2& a) {
+  float length = lengthOf(a);
+  if (length < kEpsilon) return 0.0f;
+  float inv = 1.0f / length;
+  a.x *= inv;
+  a.y *= inv;
+  return length;
+}
+template <typename T> static inline T bmin(T a, T b) { return a < b ? a : b; }
+template <typename T> static inline T bmax(T a, T b) { return a > b ? a : b; }
+template <typename T> static inline T bclamp(T a, T lo, T hi) { return bmax(lo, bmin(a, hi)); }
+static inline float babs(float a) { return a > 0.0f ? a : -a; }
+static inline V2 vmin(V2 a, V2 b) { return v2(bmin(a.x, b.x), bmin(a.y, b.y)); }
+static inline V2 vmax(V2 a, V2 b) { return v2(bmax(a.x, b.x), bmax(a.y, b.y)); }
+
+struct Rot { float s, c; };
+struct Xf { V2 p; Rot q; };
+static inline V2 mul(Rot q, V2 v) { return v2(q.c * v.x - q.s * v.y, q.s * v.x + q.c * v.y); }
+static inline V2 mulT(Rot q, V2 v) { return v2(q.c * v.x + q.s * v.y, -q.s * v.x + q.c * v.y); }
+static inline V2 mul(const Xf& T, V2 v) {
+  float x = (T.q.c * v.x - T.q.s * v.y) + T.p.x;
+  float y = (T.q.s * v.x + T.q.c * v.y) + T.p.y;
+  return v2(x, y);
+}
+static inline V2 mulT(const Xf& T, V2 v) {
+  float px = v.x - T.p.x;
+  float py = v.y - T.p.y;
+  float x = (T.q.c * px + T.q.s * py);
+  float y = (-T.q.s * px + T.q.c * py);
+  return v2(x, y);
+}
+static inline Rot mulT(Rot q, Rot r) {
+  Rot o;
+  o.s = q.c * r.s - q.s * r.c;
+  o.c = q.c * r.c + q.s * r.s;
+  return o;
+}
+static inline Xf mulT(const Xf& A, const Xf& B) {
+  Xf C;
+  C.q = mulT(A.q, B.q);
+  C.p = mulT(A.q, B.p - A.p);
+  return C;
+}
+
+// b2Mat22 (b2_math.h:184-256)
+struct M22 { V2 ex, ey; };
+static inline M22 inverse(const M22& m) {
+  float a = m.ex.x, b = m.ey.x, c = m.ex.y, d = m.ey.y;
+  M22 B;
+  float det = a * d - b * c;
+  if (det != 0.0f) det = 1.0f / det;
+  B.ex.x = det * d;  B.ey.x = -det * b;
+  B.ex.y = -det * c; B.ey.y = det * a;
+  return B;
+}
+static inline V2 solve(const M22& m, V2 b) {
+  float a11 = m.ex.x, a12 = m.ey.x, a21 = m.ex.y, a22 = m.ey.y;
+  float det = a11 * a22 - a12 * a21;
+  if (det != 0.0f) det = 1.0f / det;
+  V2 x;
+  x.x = det * (a22 * b.x - a12 * b.y);
+  x.y = det * (a11 * b.y - a21 * b.x);
+  return x;
+}
+static inline V2 mul(const M22& A, V2 v) { return v2(A.ex.x * v.x + A.ey.x * v.y, A.ex.y * v.x + A.ey.y * v.y); }
+
+// b2Vec3 / b2Mat33::Solve33 (b2_math.h:493-520, src/common/b2_math.cpp:28-40)
+struct V3 { float x, y, z; };
+static inline float dot3(V3 a, V3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+static inline V3 cross3(V3 a, V3 b) {
+  V3 r; r.x = a.y * b.z - a.z * b.y; r.y = a.z * b.x - a.x * b.z; r.z = a.x * b.y - a.y * b.x; return r;
+}
+static inline V3 solve33(V3 ex, V3 ey, V3 ez, V3 b) {
+  float det = dot3(ex, cross3(ey, ez));
+  if (det != 0.0f) det = 1.0f / det;
+  V3 x;
+  x.x = det * dot3(b, cross3(ey, ez));
+  x.y = det * dot3(ex, cross3(b, ez));
+  x.z = det * dot3(ex, cross3(ey, b));
+  return x;
+}
+
+// ------------------------------------------------------------------------------------------------
+// Portable sine/cosine (the engine's trig; libm on request).
+// Method: Cody & Waite argument reduction by pi/2 with a three-part split of pi/2 whose two
+// leading parts carry 12 significant bits (so k*part is exact for |k| < 4096), followed by the
+// Taylor series of sin (to r^9) and cos (to r^10) on |r| <= pi/4, evaluated by Horner's rule.
+// Truncation error < 3e-9 relative on that interval, well under float's 6e-8 ulp.
+static int g_libm_trig = 0;
+static const float kTwoOverPi = 0.636619772367581343f;
+static const float kPio2A = 1.5703125f;                 // pi/2 to 12 bits
+static const float kPio2B = 4.8351287841796875e-04f;    // next 12 bits of pi/2
+static const float kPio2C = 3.13916473e-07f;            // remainder of pi/2 (rounded to float)
+static inline void sincos_portable(float x, float* s_out, float* c_out) {
+  float k = rintf(x * kTwoOverPi);
+  float r = x - k * kPio2A;
+  r = r - k * kPio2B;
+  r = r - k * kPio2C;
+  float z = r * r;
+  float s = r + (r * z) * (-1.66666667e-01f + z * (8.33333333e-03f + z * (-1.98412698e-04f + z * 2.75573192e-06f)));
+  float c = 1.0f + z * (-0.5f + z * (4.16666667e-02f + z * (-1.38888889e-03f + z * (2.48015873e-05f + z * -2.75573192e-07f))));
+  long long ki = (long long)k;
+  int q = (int)(ki & 3);
+  if (q == 0) { *s_out = s; *c_out = c; }
+  else if (q == 1) { *s_out = c; *c_out = -s; }
+  else if (q == 2) { *s_out = -s; *c_out = -c; }
+  else { *s_out = -c; *c_out = s; }
+}
+static inline Rot rotOf(float angle) {
+  Rot q;
+  if (g_libm_trig) { q.s = sinf(angle); q.c = cosf(angle); }
+  else sincos_portable(angle, &q.s, &q.c);
+  return q;
+}
+
+// ------------------------------------------------------------------------------------------------
+// Shapes (src/collision/b2_polygon_shape.cpp, b2_circle_shape.cpp, b2_edge_shape.cpp)
+struct Shape {
+  int type;       // 0 circle, 1 edge, 2 polygon
+  int count;
+  float radius;
+  bool oneSided;
+  V2 v[8];        // polygon vertices / circle p in v[0] / edge v1, v2, v0, v3
+  V2 n[8];
+  V2 centroid;
+};
+
+static Shape shapeFrom(const b2g_shape& s) {
+  Shape o;
+  memset(&o, 0, sizeof(o));
+  o.type = s.type; o.count = s.count; o.radius = s.radius; o.oneSided = s.one_sided != 0;
+  for (int i = 0; i < 8; ++i) {
+    o.v[i] = v2(s.vertices[i][0], s.vertices[i][1]);
+    o.n[i] = v2(s.normals[i][0], s.normals[i][1]);
+  }
+  o.centroid = v2(s.centroid[0], s.centroid[1]);
+  return o;
+}
+static void shapeTo(const Shape& o, b2g_shape* s) {
+  memset(s, 0, sizeof(*s));
+  s->type = o.type; s->count = o.count; s->radius = o.radius; s->one_sided = o.oneSided ? 1 : 0;
+  for (int i = 0; i < 8; ++i) {
+    s->vertices[i][0] = o.v[i].x; s->vertices[i][1] = o.v[i].y;
+    s->normals[i][0] = o.n[i].x; s->normals[i][1] = o.n[i].y;
+  }
+  s->centroid[0] = o.centroid.x; s->centroid[1] = o.centroid.y;
+}
+
+// b2PolygonShape::SetAsBox (b2_polygon_shape.cpp:36-48, 50-75)
+static void setAsBox(Shape* p, float hx, float hy, bool oriented, V2 center, float angle) {
+  memset(p, 0, sizeof(*p));
+  p->type = 2; p->radius = kPolygonRadius; p->count = 4;
+  p->v[0] = v2(-hx, -hy); p->v[1] = v2(hx, -hy); p->v[2] = v2(hx, hy); p->v[3] = v2(-hx, hy);
+  p->n[0] = v2(0.0f, -1.0f); p->n[1] = v2(1.0f, 0.0f); p->n[2] = v2(0.0f, 1.0f); p->n[3] = v2(-1.0f, 0.0f);
+  p->centroid = v2(0.0f, 0.0f);
+  if (oriented) {
+    p->centroid = center;
+    Xf xf;
+    xf.p = center;
+    xf.q.s = sinf(angle);   // b2Rot::Set on the host uses libm (b2_math.h:313-318)
+    xf.q.c = cosf(angle);
+    for (int i = 0; i < 4; ++i) {
+      p->v[i] = mul(xf, p->v[i]);
+      p->n[i] = mul(xf.q, p->n[i]);
+    }
+  }
+}
+
+// ComputeCentroid (b2_polygon_shape.cpp:77-111)
+static V2 computeCentroid(const V2* vs, int count) {
+  V2 c = v2(0.0f, 0.0f);
+  float area = 0.0f;
+  V2 s = vs[0];
+  const float inv3 = 1.0f / 3.0f;
+  for (int i = 0; i < count; ++i) {
+    V2 p1 = vs[0] - s;
+    V2 p2 = vs[i] - s;
+    V2 p3 = i + 1 < count ? vs[i + 1] - s : vs[0] - s;
+    V2 e1 = p2 - p1;
+    V2 e2 = p3 - p1;
+    float D = cross(e1, e2);
+    float triangleArea = 0.5f * D;
+    area += triangleArea;
+    addTo(c, (triangleArea * inv3) * ((p1 + p2) + p3));
+  }
+  c = (1.0f / area) * c + s;
+  return c;
+}
+
+// b2PolygonShape::Set (b2_polygon_shape.cpp:113-243): weld, gift-wrap hull, normals, centroid.
+static void polygonSet(Shape* p, const V2* vertices, int count) {
+  if (count < 3) { setAsBox(p, 1.0f, 1.0f, false, v2(0, 0), 0); return; }
+  int n = bmin(count, 8);
+  V2 ps[8];
+  int tempCount = 0;
+  for (int i = 0; i < n; ++i) {
+    V2 v = vertices[i];
+    bool unique = true;
+    for (int j = 0; j < tempCount; ++j) {
+      if (distSq(v, ps[j]) < ((0.5f * kLinearSlop) * (0.5f * kLinearSlop))) { unique = false; break; }
+    }
+    if (unique) ps[tempCount++] = v;
+  }
+  n = tempCount;
+  if (n < 3) { setAsBox(p, 1.0f, 1.0f, false, v2(0, 0), 0); return; }
+  int i0 = 0;
+  float x0 = ps[0].x;
+  for (int i = 1; i < n; ++i) {
+    float x = ps[i].x;
+    if (x > x0 || (x == x0 && ps[i].y < ps[i0].y)) { i0 = i; x0 = x; }
+  }
+  int hull[8];
+  int m = 0;
+  int ih = i0;
+  for (;;) {
+    if (m >= 8) break;
+    hull[m] = ih;
+    int ie = 0;
+    for (int j = 1; j < n; ++j) {
+      if (ie == ih) { ie = j; continue; }
+      V2 r = ps[ie] - ps[hull[m]];
+      V2 v = ps[j] - ps[hull[m]];
+      float c = cross(r, v);
+      if (c < 0.0f) ie = j;
+      if (c == 0.0f && lengthSq(v) > lengthSq(r)) ie = j;
+    }
+    ++m;
+    ih = ie;
+    if (ie == i0) break;
+  }
+  if (m < 3) { setAsBox(p, 1.0f, 1.0f, false, v2(0, 0), 0); return; }
+  memset(p, 0, sizeof(*p));
+  p->type = 2; p->radius = kPolygonRadius; p->count = m;
+  for (int i = 0; i < m; ++i) p->v[i] = ps[hull[i]];
+  for (int i = 0; i < m; ++i) {
+    int i1 = i;
+    int i2 = i + 1 < m ? i + 1 : 0;
+    V2 edge = p->v[i2] - p->v[i1];
+    p->n[i] = cross(edge, 1.0f);
+    normalize(p->n[i]);
+  }
+  p->centroid = computeCentroid(p->v, m);
+}
+
+struct MassData { float mass; V2 center; float I; };
+
+// ComputeMass for polygon (b2_polygon_shape.cpp:390-464), circle (b2_circle_shape.cpp:98-104),
+// edge (b2_edge_shape.cpp:169-176).
+static MassData computeMass(const Shape& s, float density) {
+  MassData md;
+  if (s.type == 0) {
+    md.mass = density * kPi * s.radius * s.radius;
+    md.center = s.v[0];
+    md.I = md.mass * (0.5f * s.radius * s.radius + dot(s.v[0], s.v[0]));
+    return md;
+  }
+  if (s.type == 1) {
+    md.mass = 0.0f;
+    md.center = 0.5f * (s.v[0] + s.v[1]);
+    md.I = 0.0f;
+    return md;
+  }
+  V2 center = v2(0.0f, 0.0f);
+  float area = 0.0f;
+  float I = 0.0f;
+  V2 sref = s.v[0];
+  const float k_inv3 = 1.0f / 3.0f;
+  for (int i = 0; i < s.count; ++i) {
+    V2 e1 = s.v[i] - sref;
+    V2 e2 = i + 1 < s.count ? s.v[i + 1] - sref : s.v[0] - sref;
+    float D = cross(e1, e2);
+    float triangleArea = 0.5f * D;
+    area += triangleArea;
+    addTo(center, (triangleArea * k_inv3) * (e1 + e2));
+    float ex1 = e1.x, ey1 = e1.y;
+    float ex2 = e2.x, ey2 = e2.y;
+    float intx2 = ex1 * ex1 + ex2 * ex1 + ex2 * ex2;
+    float inty2 = ey1 * ey1 + ey2 * ey1 + ey2 * ey2;
+    I += (0.25f * k_inv3 * D) * (intx2 + inty2);
+  }
+  md.mass = density * area;
+  float inv = 1.0f / area;
+  center.x *= inv;
+  center.y *= inv;
+  md.center = center + sref;
+  md.I = density * I;
+  md.I += md.mass * (dot(md.center, md.center) - dot(center, center));
+  return md;
+}
+
+struct AABB { V2 lo, hi; };
+
+// ComputeAABB: polygon (b2_polygon_shape.cpp:373-388), circle (b2_circle_shape.cpp:91-96),
+// edge (b2_edge_shape.cpp:156-167).
+static AABB computeAABB(const Shape& s, const Xf& xf) {
+  AABB bb;
+  if (s.type == 0) {
+    V2 p = xf.p + mul(xf.q, s.v[0]);
+    bb.lo = v2(p.x - s.radius, p.y - s.radius);
+    bb.hi = v2(p.x + s.radius, p.y + s.radius);
+    return bb;
+  }
+  if (s.type == 1) {
+    V2 a = mul(xf, s.v[0]);
+    V2 b = mul(xf, s.v[1]);
+    V2 lower = vmin(a, b);
+    V2 upper = vmax(a, b);
+    V2 r = v2(s.radius, s.radius);
+    bb.lo = lower - r;
+    bb.hi = upper + r;
+    return bb;
+  }
+  V2 lower = mul(xf, s.v[0]);
+  V2 upper = lower;
+  for (int i = 1; i < s.count; ++i) {
+    V2 v = mul(xf, s.v[i]);
+    lower = vmin(lower, v);
+    upper = vmax(upper, v);
+  }
+  V2 r = v2(s.radius, s.radius);
+  bb.lo = lower - r;
+  bb.hi = upper + r;
+  return bb;
+}
+
+// b2TestOverlap(AABB, AABB), include/box2d/b2_collision.h:270-276 (inclusive)
+static inline bool overlap(const AABB& a, const AABB& b) {
+  return (a.hi.x >= b.lo.x) & (a.lo.x <= b.hi.x) & (a.hi.y >= b.lo.y) & (a.lo.y <= b.hi.y);
+}
+
+// ------------------------------------------------------------------------------------------------
+// Narrowphase (src/collision/b2_collide_*.cpp, b2_collision.cpp)
+struct MPoint { V2 localPoint; float normalImpulse, tangentImpulse; uint32_t id; };
+struct Manifold { MPoint points[2]; V2 localNormal; V2 localPoint; int type; int pointCount; };
+
+static inline uint32_t makeId(int indexA, int indexB, int typeA, int typeB) {
+  return (uint32_t)(uint8_t)indexA | ((uint32_t)(uint8_t)indexB << 8) |
+         ((uint32_t)(uint8_t)typeA << 16) | ((uint32_t)(uint8_t)typeB << 24);
+}
+static inline int idIndexA(uint32_t id) { return (int)(id & 0xff); }
+static inline int idIndexB(uint32_t id) { return (int)((id >> 8) & 0xff); }
+static inline int idTypeA(uint32_t id) { return (int)((id >> 16) & 0xff); }
+static inline int idTypeB(uint32_t id) { return (int)((id >> 24) & 0xff); }
+static inline uint32_t swapId(uint32_t id) {
+  return makeId(idIndexB(id), idIndexA(id), idTypeB(id), idTypeA(id));
+}
+enum { kVertex = 0, kFace = 1 };
+
+struct ClipVertex { V2 v; uint32_t id; };
+
+// b2ClipSegmentToLine (b2_collision.cpp:205-237)
+static int clipSegmentToLine(ClipVertex vOut[2], const ClipVertex vIn[2], V2 normal, float offset,
+                             int vertexIndexA) {
+  int count = 0;
+  float distance0 = dot(normal, vIn[0].v) - offset;
+  float distance1 = dot(normal, vIn[1].v) - offset;
+  if (distance0 <= 0.0f) vOut[count++] = vIn[0];
+  if (distance1 <= 0.0f) vOut[count++] = vIn[1];
+  if (distance0 * distance1 < 0.0f) {
+    float interp = distance0 / (distance0 - distance1);
+    vOut[count].v = vIn[0].v + interp * (vIn[1].v - vIn[0].v);
+    vOut[count].id = makeId(vertexIndexA, idIndexB(vIn[0].id), kVertex, kFace);
+    ++count;
+  }
+  return count;
+}
+
+// b2CollideCircles (b2_collide_circle.cpp:27-53)
+static void collideCircles(Manifold* m, const Shape& A, const Xf& xfA, const Shape& B, const Xf& xfB) {
+  m->pointCount = 0;
+  V2 pA = mul(xfA, A.v[0]);
+  V2 pB = mul(xfB, B.v[0]);
+  V2 d = pB - pA;
+  float distSqr = dot(d, d);
+  float rA = A.radius, rB = B.radius;
+  float radius = rA + rB;
+  if (distSqr > radius * radius) return;
+  m->type = 0;
+  m->localPoint = A.v[0];
+  m->localNormal = v2(0.0f, 0.0f);
+  m->pointCount = 1;
+  m->points[0].localPoint = B.v[0];
+  m->points[0].id = 0;
+}
+
+// b2CollidePolygonAndCircle (b2_collide_circle.cpp:55-158)
+static void collidePolygonAndCircle(Manifold* m, const Shape& P, const Xf& xfA, const Shape& Cs,
+                                    const Xf& xfB) {
+  m->pointCount = 0;
+  V2 c = mul(xfB, Cs.v[0]);
+  V2 cLocal = mulT(xfA, c);
+  int normalIndex = 0;
+  float separation = -kMaxFloat;
+  float radius = P.radius + Cs.radius;
+  int vertexCount = P.count;
+  for (int i = 0; i < vertexCount; ++i) {
+    float s = dot(P.n[i], cLocal - P.v[i]);
+    if (s > radius) return;
+    if (s > separation) { separation = s; normalIndex = i; }
+  }
+  int vertIndex1 = normalIndex;
+  int vertIndex2 = vertIndex1 + 1 < vertexCount ? vertIndex1 + 1 : 0;
+  V2 v1 = P.v[vertIndex1];
+  V2 v2_ = P.v[vertIndex2];
+  if (separation < kEpsilon) {
+    m->pointCount = 1;
+    m->type = 1;
+    m->localNormal = P.n[normalIndex];
+    m->localPoint = 0.5f * (v1 + v2_);
+    m->points[0].localPoint = Cs.v[0];
+    m->points[0].id = 0;
+    return;
+  }
+  float u1 = dot(cLocal - v1, v2_ - v1);
+  float u2 = dot(cLocal - v2_, v1 - v2_);
+  if (u1 <= 0.0f) {
+    if (distSq(cLocal, v1) > radius * radius) return;
+    m->pointCount = 1;
+    m->type = 1;
+    m->localNormal = cLocal - v1;
+    normalize(m->localNormal);
+    m->localPoint = v1;
+    m->points[0].localPoint = Cs.v[0];
+    m->points[0].id = 0;
+  } else if (u2 <= 0.0f) {
+    if (distSq(cLocal, v2_) > radius * radius) return;
+    m->pointCount = 1;
+    m->type = 1;
+    m->localNormal = cLocal - v2_;
+    normalize(m->localNormal);
+    m->localPoint = v2_;
+    m->points[0].localPoint = Cs.v[0];
+    m->points[0].id = 0;
+  } else {
+    V2 faceCenter = 0.5f * (v1 + v2_);
+    float s = dot(cLocal - faceCenter, P.n[vertIndex1]);
+    if (s > radius) return;
+    m->pointCount = 1;
+    m->type = 1;
+    m->localNormal = P.n[vertIndex1];
+    m->localPoint = faceCenter;
+    m->points[0].localPoint = Cs.v[0];
+    m->points[0].id = 0;
+  }
+}
+
+// b2FindMaxSeparation (b2_collide_polygon.cpp:27-66)
+static float findMaxSeparation(int* edgeIndex, const Shape& p1, const Xf& xf1, const Shape& p2, const Xf& xf2) {
+  int count1 = p1.count;
+  int count2 = p2.count;
+  Xf xf = mulT(xf2, xf1);
+  int bestIndex = 0;
+  float maxSeparation = -kMaxFloat;
+  for (int i = 0; i < count1; ++i) {
+    V2 n = mul(xf.q, p1.n[i]);
+    V2 v1 = mul(xf, p1.v[i]);
+    float si = kMaxFloat;
+    for (int j = 0; j < count2; ++j) {
+      float sij = dot(n, p2.v[j] - v1);
+      if (sij < si) si = sij;
+    }
+    if (si > maxSeparation) { maxSeparation = si; bestIndex = i; }
+  }
+  *edgeIndex = bestIndex;
+  return maxSeparation;
+}
+
+// b2FindIncidentEdge (b2_collide_polygon.cpp:68-111)
+static void findIncidentEdge(ClipVertex c[2], const Shape& p1, const Xf& xf1, int edge1, const Shape& p2,
+                             const Xf& xf2) {
+  V2 normal1 = mulT(xf2.q, mul(xf1.q, p1.n[edge1]));
+  int index = 0;
+  float minDot = kMaxFloat;
+  for (int i = 0; i < p2.count; ++i) {
+    float d = dot(normal1, p2.n[i]);
+    if (d < minDot) { minDot = d; index = i; }
+  }
+  int i1 = index;
+  int i2 = i1 + 1 < p2.count ? i1 + 1 : 0;
+  c[0].v = mul(xf2, p2.v[i1]);
+  c[0].id = makeId(edge1, i1, kFace, kVertex);
+  c[1].v = mul(xf2, p2.v[i2]);
+  c[1].id = makeId(edge1, i2, kFace, kVertex);
+}
+
+// b2CollidePolygons (b2_collide_polygon.cpp:120-243)
+static void collidePolygons(Manifold* m, const Shape& A, const Xf& xfA, const Shape& B, const Xf& xfB) {
+  m->pointCount = 0;
+  float totalRadius = A.radius + B.radius;
+  int edgeA = 0;
+  float separationA = findMaxSeparation(&edgeA, A, xfA, B, xfB);
+  if (separationA > totalRadius) return;
+  int edgeB = 0;
+  float separationB = findMaxSeparation(&edgeB, B, xfB, A, xfA);
+  if (separationB > totalRadius) return;
+  const Shape* poly1;
+  const Shape* poly2;
+  Xf xf1, xf2;
+  int edge1;
+  int flip;
+  const float k_tol = 0.1f * kLinearSlop;
+  if (separationB > separationA + k_tol) {
+    poly1 = &B; poly2 = &A; xf1 = xfB; xf2 = xfA; edge1 = edgeB; m->type = 2; flip = 1;
+  } else {
+    poly1 = &A; poly2 = &B; xf1 = xfA; xf2 = xfB; edge1 = edgeA; m->type = 1; flip = 0;
+  }
+  ClipVertex incidentEdge[2];
+  findIncidentEdge(incidentEdge, *poly1, xf1, edge1, *poly2, xf2);
+  int count1 = poly1->count;
+  int iv1 = edge1;
+  int iv2 = edge1 + 1 < count1 ? edge1 + 1 : 0;
+  V2 v11 = poly1->v[iv1];
+  V2 v12 = poly1->v[iv2];
+  V2 localTangent = v12 - v11;
+  normalize(localTangent);
+  V2 localNormal = cross(localTangent, 1.0f);
+  V2 planePoint = 0.5f * (v11 + v12);
+  V2 tangent = mul(xf1.q, localTangent);
+  V2 normal = cross(tangent, 1.0f);
+  v11 = mul(xf1, v11);
+  v12 = mul(xf1, v12);
+  float frontOffset = dot(normal, v11);
+  float sideOffset1 = -dot(tangent, v11) + totalRadius;
+  float sideOffset2 = dot(tangent, v12) + totalRadius;
+  ClipVertex clipPoints1[2];
+  ClipVertex clipPoints2[2];
+  int np = clipSegmentToLine(clipPoints1, incidentEdge, -tangent, sideOffset1, iv1);
+  if (np < 2) return;
+  np = clipSegmentToLine(clipPoints2, clipPoints1, tangent, sideOffset2, iv2);
+  if (np < 2) return;
+  m->localNormal = localNormal;
+  m->localPoint = planePoint;
+  int pointCount = 0;
+  for (int i = 0; i < 2; ++i) {
+    float separation = dot(normal, clipPoints2[i].v) - frontOffset;
+    if (separation <= totalRadius) {
+      MPoint* cp = m->points + pointCount;
+      cp->localPoint = mulT(xf2, clipPoints2[i].v);
+      cp->id = flip ? swapId(clipPoints2[i].id) : clipPoints2[i].id;
+      ++pointCount;
+    }
+  }
+  m->pointCount = pointCount;
+}
+
+// b2CollideEdgeAndCircle (b2_collide_edge.cpp:31-165)
+static void collideEdgeAndCircle(Manifold* m, const Shape& E, const Xf& xfA, const Shape& Cs, const Xf& xfB) {
+  m->pointCount = 0;
+  V2 Q = mulT(xfA, mul(xfB, Cs.v[0]));
+  V2 A = E.v[0], B = E.v[1];
+  V2 e = B - A;
+  V2 n = v2(e.y, -e.x);
+  float offset = dot(n, Q - A);
+  bool oneSided = E.oneSided;
+  if (oneSided && offset < 0.0f) return;
+  float u = dot(e, B - Q);
+  float v = dot(e, Q - A);
+  float radius = E.radius + Cs.radius;
+  if (v <= 0.0f) {
+    V2 P = A;
+    V2 d = Q - P;
+    float dd = dot(d, d);
+    if (dd > radius * radius) return;
+    if (E.oneSided) {
+      V2 A1 = E.v[2];
+      V2 B1 = A;
+      V2 e1 = B1 - A1;
+      float u1 = dot(e1, B1 - Q);
+      if (u1 > 0.0f) return;
+    }
+    m->pointCount = 1;
+    m->type = 0;
+    m->localNormal = v2(0.0f, 0.0f);
+    m->localPoint = P;
+    m->points[0].id = makeId(0, 0, kVertex, kVertex);
+    m->points[0].localPoint = Cs.v[0];
+    return;
+  }
+  if (u <= 0.0f) {
+    V2 P = B;
+    V2 d = Q - P;
+    float dd = dot(d, d);
+    if (dd > radius * radius) return;
+    if (E.oneSided) {
+      V2 B2 = E.v[3];
+      V2 A2 = B;
+      V2 e2 = B2 - A2;
+      float v2v = dot(e2, Q - A2);
+      if (v2v > 0.0f) return;
+    }
+    m->pointCount = 1;
+    m->type = 0;
+    m->localNormal = v2(0.0f, 0.0f);
+    m->localPoint = P;
+    m->points[0].id = makeId(1, 0, kVertex, kVertex);
+    m->points[0].localPoint = Cs.v[0];
+    return;
+  }
+  float den = dot(e, e);
+  V2 P = (1.0f / den) * (u * A + v * B);
+  V2 d = Q - P;
+  float dd = dot(d, d);
+  if (dd > radius * radius) return;
+  if (offset < 0.0f) n = v2(-n.x, -n.y);
+  normalize(n);
+  m->pointCount = 1;
+  m->type = 1;
+  m->localNormal = n;
+  m->localPoint = A;
+  m->points[0].id = makeId(0, 0, kFace, kVertex);
+  m->points[0].localPoint = Cs.v[0];
+}
+
+// b2EPAxis, b2TempPolygon, b2ReferenceFace and b2CollideEdgeAndPolygon (b2_collide_edge.cpp:167-524)
+struct EPAxis { V2 normal; int type; int index; float separation; };  // type 0 unknown 1 edgeA 2 edgeB
+struct TempPoly { V2 v[8]; V2 n[8]; int count; };
+
+static EPAxis computeEdgeSeparation(const TempPoly& pb, V2 v1, V2 normal1) {
+  EPAxis axis;
+  axis.type = 1; axis.index = -1; axis.separation = -FLT_MAX; axis.normal = v2(0.0f, 0.0f);
+  V2 axes[2] = {normal1, -normal1};
+  for (int j = 0; j < 2; ++j) {
+    float sj = FLT_MAX;
+    for (int i = 0; i < pb.count; ++i) {
+      float si = dot(axes[j], pb.v[i] - v1);
+      if (si < sj) sj = si;
+    }
+    if (sj > axis.separation) { axis.index = j; axis.separation = sj; axis.normal = axes[j]; }
+  }
+  return axis;
+}
+
+static EPAxis computePolygonSeparation(const TempPoly& pb, V2 v1, V2 v2_) {
+  EPAxis axis;
+  axis.type = 0; axis.index = -1; axis.separation = -FLT_MAX; axis.normal = v2(0.0f, 0.0f);
+  for (int i = 0; i < pb.count; ++i) {
+    V2 n = -pb.n[i];
+    float s1 = dot(n, pb.v[i] - v1);
+    float s2 = dot(n, pb.v[i] - v2_);
+    float s = bmin(s1, s2);
+    if (s > axis.separation) { axis.type = 2; axis.index = i; axis.separation = s; axis.normal = n; }
+  }
+  return axis;
+}
+
+static void collideEdgeAndPolygon(Manifold* m, const Shape& E, const Xf& xfA, const Shape& PB, const Xf& xfB) {
+  m->pointCount = 0;
+  Xf xf = mulT(xfA, xfB);
+  V2 centroidB = mul(xf, PB.centroid);
+  V2 v1 = E.v[0];
+  V2 v2_ = E.v[1];
+  V2 edge1 = v2_ - v1;
+  normalize(edge1);
+  V2 normal1 = v2(edge1.y, -edge1.x);
+  float offset1 = dot(normal1, centroidB - v1);
+  bool oneSided = E.oneSided;
+  if (oneSided && offset1 < 0.0f) return;
+  TempPoly tp;
+  tp.count = PB.count;
+  for (int i = 0; i < PB.count; ++i) {
+    tp.v[i] = mul(xf, PB.v[i]);
+    tp.n[i] = mul(xf.q, PB.n[i]);
+  }
+  float radius = PB.radius + E.radius;
+  EPAxis edgeAxis = computeEdgeSeparation(tp, v1, normal1);
+  if (edgeAxis.separation > radius) return;
+  EPAxis polygonAxis = computePolygonSeparation(tp, v1, v2_);
+  if (polygonAxis.separation > radius) return;
+  const float k_relativeTol = 0.98f;
+  const float k_absoluteTol = 0.001f;
+  EPAxis primaryAxis;
+  if (polygonAxis.separation - radius > k_relativeTol * (edgeAxis.separation - radius) + k_absoluteTol)
+    primaryAxis = polygonAxis;
+  else
+    primaryAxis = edgeAxis;
+  if (oneSided) {
+    V2 edge0 = v1 - E.v[2];
+    normalize(edge0);
+    V2 normal0 = v2(edge0.y, -edge0.x);
+    bool convex1 = cross(edge0, edge1) >= 0.0f;
+    V2 edge2 = E.v[3] - v2_;
+    normalize(edge2);
+    V2 normal2 = v2(edge2.y, -edge2.x);
+    bool convex2 = cross(edge1, edge2) >= 0.0f;
+    const float sinTol = 0.1f;
+    bool side1 = dot(primaryAxis.normal, edge1) <= 0.0f;
+    if (side1) {
+      if (convex1) {
+        if (cross(primaryAxis.normal, normal0) > sinTol) return;
+      } else {
+        primaryAxis = edgeAxis;
+      }
+    } else {
+      if (convex2) {
+        if (cross(normal2, primaryAxis.normal) > sinTol) return;
+      } else {
+        primaryAxis = edgeAxis;
+      }
+    }
+  }
+  ClipVertex clipPoints[2];
+  int ri1, ri2;
+  V2 rv1, rv2, rnormal, sideNormal1, sideNormal2;
+  if (primaryAxis.type == 1) {
+    m->type = 1;
+    int bestIndex = 0;
+    float bestValue = dot(primaryAxis.normal, tp.n[0]);
+    for (int i = 1; i < tp.count; ++i) {
+      float value = dot(primaryAxis.normal, tp.n[i]);
+      if (value < bestValue) { bestValue = value; bestIndex = i; }
+    }
+    int i1 = bestIndex;
+    int i2 = i1 + 1 < tp.count ? i1 + 1 : 0;
+    clipPoints[0].v = tp.v[i1];
+    clipPoints[0].id = makeId(0, i1, kFace, kVertex);
+    clipPoints[1].v = tp.v[i2];
+    clipPoints[1].id = makeId(0, i2, kFace, kVertex);
+    ri1 = 0; ri2 = 1; rv1 = v1; rv2 = v2_;
+    rnormal = primaryAxis.normal;
+    sideNormal1 = -edge1;
+    sideNormal2 = edge1;
+  } else {
+    m->type = 2;
+    clipPoints[0].v = v2_;
+    clipPoints[0].id = makeId(1, primaryAxis.index, kVertex, kFace);
+    clipPoints[1].v = v1;
+    clipPoints[1].id = makeId(0, primaryAxis.index, kVertex, kFace);
+    ri1 = primaryAxis.index;
+    ri2 = ri1 + 1 < tp.count ? ri1 + 1 : 0;
+    rv1 = tp.v[ri1];
+    rv2 = tp.v[ri2];
+    rnormal = tp.n[ri1];
+    sideNormal1 = v2(rnormal.y, -rnormal.x);
+    sideNormal2 = -sideNormal1;
+  }
+  float sideOffset1 = dot(sideNormal1, rv1);
+  float sideOffset2 = dot(sideNormal2, rv2);
+  ClipVertex clipPoints1[2];
+  ClipVertex clipPoints2[2];
+  int np = clipSegmentToLine(clipPoints1, clipPoints, sideNormal1, sideOffset1, ri1);
+  if (np < 2) return;
+  np = clipSegmentToLine(clipPoints2, clipPoints1, sideNormal2, sideOffset2, ri2);
+  if (np < 2) return;
+  if (primaryAxis.type == 1) {
+    m->localNormal = rnormal;
+    m->localPoint = rv1;
+  } else {
+    m->localNormal = PB.n[ri1];
+    m->localPoint = PB.v[ri1];
+  }
+  int pointCount = 0;
+  for (int i = 0; i < 2; ++i) {
+    float separation = dot(rnormal, clipPoints2[i].v - rv1);
+    if (separation <= radius) {
+      MPoint* cp = m->points + pointCount;
+      if (primaryAxis.type == 1) {
+        cp->localPoint = mulT(xf, clipPoints2[i].v);
+        cp->id = clipPoints2[i].id;
+      } else {
+        cp->localPoint = clipPoints2[i].v;
+        cp->id = swapId(clipPoints2[i].id);
+      }
+      ++pointCount;
+    }
+  }
+  m->pointCount = pointCount;
+}
+
+// Dispatch in b2Contact's table order (src/dynamics/b2_contact.cpp:46-56); A's shape first.
+static bool hasCollider(int ta, int tb) {
+  return (ta == 0 && tb == 0) || (ta == 2 && tb == 0) || (ta == 2 && tb == 2) || (ta == 1 && tb == 0) ||
+         (ta == 1 && tb == 2);
+}
+static void evaluate(Manifold* m, const Shape& A, const Xf& xfA, const Shape& B, const Xf& xfB) {
+  if (A.type == 0 && B.type == 0) collideCircles(m, A, xfA, B, xfB);
+  else if (A.type == 2 && B.type == 0) collidePolygonAndCircle(m, A, xfA, B, xfB);
+  else if (A.type == 2 && B.type == 2) collidePolygons(m, A, xfA, B, xfB);
+  else if (A.type == 1 && B.type == 0) collideEdgeAndCircle(m, A, xfA, B, xfB);
+  else if (A.type == 1 && B.type == 2) collideEdgeAndPolygon(m, A, xfA, B, xfB);
+  else m->pointCount = 0;
+}
+
+// b2WorldManifold::Initialize (b2_collision.cpp:26-90)
+struct WorldManifold { V2 normal; V2 points[2]; float separations[2]; };
+static void worldManifold(WorldManifold* wm, const Manifold& m, const Xf& xfA, float radiusA, const Xf& xfB,
+                          float radiusB) {
+  if (m.pointCount == 0) return;
+  if (m.type == 0) {
+    wm->normal = v2(1.0f, 0.0f);
+    V2 pointA = mul(xfA, m.localPoint);
+    V2 pointB = mul(xfB, m.points[0].localPoint);
+    if (distSq(pointA, pointB) > kEpsilon * kEpsilon) {
+      wm->normal = pointB - pointA;
+      normalize(wm->normal);
+    }
+    V2 cA = pointA + radiusA * wm->normal;
+    V2 cB = pointB - radiusB * wm->normal;
+    wm->points[0] = 0.5f * (cA + cB);
+    wm->separations[0] = dot(cB - cA, wm->normal);
+  } else if (m.type == 1) {
+    wm->normal = mul(xfA.q, m.localNormal);
+    V2 planePoint = mul(xfA, m.localPoint);
+    for (int i = 0; i < m.pointCount; ++i) {
+      V2 clipPoint = mul(xfB, m.points[i].localPoint);
+      V2 cA = clipPoint + (radiusA - dot(clipPoint - planePoint, wm->normal)) * wm->normal;
+      V2 cB = clipPoint - radiusB * wm->normal;
+      wm->points[i] = 0.5f * (cA + cB);
+      wm->separations[i] = dot(cB - cA, wm->normal);
+    }
+  } else {
+    wm->normal = mul(xfB.q, m.localNormal);
+    V2 planePoint = mul(xfB, m.localPoint);
+    for (int i = 0; i < m.pointCount; ++i) {
+      V2 clipPoint = mul(xfA, m.points[i].localPoint);
+      V2 cB = clipPoint + (radiusB - dot(clipPoint - planePoint, wm->normal)) * wm->normal;
+      V2 cA = clipPoint - radiusA * wm->normal;
+      wm->points[i] = 0.5f * (cA + cB);
+      wm->separations[i] = dot(cA - cB, wm->normal);
+    }
+    wm->normal = -wm->normal;
+  }
+}
+
+static Manifold manifoldFrom(const b2g_manifold& s) {
+  Manifold m;
+  memset(&m, 0, sizeof(m));
+  for (int i = 0; i < 2; ++i) {
+    m.points[i].localPoint = v2(s.points[i].local_point[0], s.points[i].local_point[1]);
+    m.points[i].normalImpulse = s.points[i].normal_impulse;
+    m.points[i].tangentImpulse = s.points[i].tangent_impulse;
+    m.points[i].id = s.points[i].id;
+  }
+  m.localNormal = v2(s.local_normal[0], s.local_normal[1]);
+  m.localPoint = v2(s.local_point[0], s.local_point[1]);
+  m.type = s.type;
+  m.pointCount = s.point_count;
+  return m;
+}
+static void manifoldTo(const Manifold& m, b2g_manifold* s) {
+  memset(s, 0, sizeof(*s));
+  for (int i = 0; i < 2; ++i) {
+    s->points[i].local_point[0] = m.points[i].localPoint.x;
+    s->points[i].local_point[1] = m.points[i].localPoint.y;
+    s->points[i].normal_impulse = m.points[i].normalImpulse;
+    s->points[i].tangent_impulse = m.points[i].tangentImpulse;
+    s->points[i].id = m.points[i].id;
+  }
+  s->local_normal[0] = m.localNormal.x; s->local_normal[1] = m.localNormal.y;
+  s->local_point[0] = m.localPoint.x; s->local_point[1] = m.localPoint.y;
+  s->type = m.type;
+  s->point_count = m.pointCount;
+}
+
+// ------------------------------------------------------------------------------------------------
+// World model
+struct Body {
+  Xf xf;
+  V2 c; float a;
+  V2 v; float w;
+  V2 localCenter;
+  float mass, invMass, I, invI;
+  float linearDamping, angularDamping, gravityScale;
+  V2 force; float torque;
+  int type;
+  uint32_t flags;
+};
+
+struct Fixture {
+  Shape shape;
+  int body;
+  float density, friction, restitution, threshold;
+  uint16_t category, mask; int16_t group;
+  bool sensor;
+};
+
+struct Joint {
+  b2g_joint_def d;
+  // state (b2RevoluteJoint / b2PrismaticJoint / b2DistanceJoint members)
+  V2 impulse2;       // revolute / prismatic m_impulse
+  float impulse1;    // distance m_impulse
+  float motorImpulse, lowerImpulse, upperImpulse;
+  // solver temporaries
+  int iA, iB;
+  V2 lcA, lcB;
+  float mA, mB, invIA, invIB;
+  V2 rA, rB;
+  M22 K;
+  float axialMass, angle;
+  V2 localXAxisA, localYAxisA, axis, perp;
+  float a1, a2, s1, s2, translation;
+  V2 u; float currentLength, mass, softMass, gamma, bias;
+};
+
+struct Contact {
+  uint64_t key;   // emitter << 32 | partner
+  int fA, fB;     // oriented per the dispatch table
+  uint32_t flags;
+  float friction, restitution, threshold, tangentSpeed;
+  Manifold m;
+};
+
+struct VCPoint { V2 rA, rB; float normalImpulse, tangentImpulse, normalMass, tangentMass, velocityBias; };
+struct VC {
+  VCPoint points[2];
+  V2 normal;
+  M22 normalMass, K;
+  int indexA, indexB;
+  float invMassA, invMassB, invIA, invIB;
+  float friction, restitution, threshold, tangentSpeed;
+  int pointCount;
+  int contact;
+};
+struct PC {
+  V2 localPoints[2];
+  V2 localNormal, localPoint;
+  int indexA, indexB;
+  float invMassA, invMassB;
+  V2 localCenterA, localCenterB;
+  float invIA, invIB;
+  int type;
+  float radiusA, radiusB;
+  int pointCount;
+};
+
+// Hash of a constraint's stable identity, the colouring priority (lower first).
+static inline uint32_t fmix32(uint32_t h) {
+  h ^= h >> 16; h *= 0x85ebca6bu; h ^= h >> 13; h *= 0xc2b2ae35u; h ^= h >> 16; return h;
+}
+static inline uint32_t contactPriority(uint64_t key) {
+  uint32_t e = (uint32_t)(key >> 32), p = (uint32_t)key;
+  return fmix32(e * 0x9e3779b1u ^ fmix32(p + 0x7f4a7c15u));
+}
+static inline uint32_t jointPriority(uint32_t j) { return fmix32(j * 0x9e3779b1u + 0x632be5abu); }
+
+static const int kColors = 64;          // colours 0..62 regular, 63 = overflow (solved serially)
+static const int kOverflow = kColors - 1;
+
+struct World {
+  V2 gravity;
+  bool warmStarting = true;
+  bool autoClearForces = true;
+  bool newContacts = true;
+  float inv_dt0 = 0.0f;
+  std::vector<Body> bodies;
+  std::vector<Fixture> fixtures;
+  std::vector<Joint> joints;
+  std::vector<Contact> contacts;           // sorted by key
+  std::vector<uint64_t> noCollide;         // sorted body pairs joined by collideConnected=false joints
+  // last step's solver order record
+  std::vector<int> contactColor;           // per contact (-1 not solved)
+  std::vector<uint32_t> contactPrio;
+  std::vector<int> jointColor;
+  std::vector<uint32_t> jointPrioV;
+  std::vector<int32_t> lastContactOrder;   // (fixture A, fixture B) pairs in solve order
+  std::vector<int32_t> lastJointOrder;     // joint indices in solve order
+};
+
+static void rebuildNoCollide(World* w) {
+  w->noCollide.clear();
+  for (const Joint& j : w->joints) {
+    if (j.d.collide_connected) continue;
+    uint32_t a = (uint32_t)j.d.body_a, b = (uint32_t)j.d.body_b;
+    if (a > b) std::swap(a, b);
+    w->noCollide.push_back(((uint64_t)a << 32) | b);
+  }
+  std::sort(w->noCollide.begin(), w->noCollide.end());
+}
+
+// b2Body::ShouldCollide (src/dynamics/b2_body.cpp:459-480) + b2ContactFilter::ShouldCollide
+// (src/dynamics/b2_world_callbacks.cpp:28-39).
+static bool shouldCollide(const World& w, int fi, int fj) {
+  const Fixture& a = w.fixtures[fi];
+  const Fixture& b = w.fixtures[fj];
+  if (a.body == b.body) return false;
+  const Body& ba = w.bodies[a.body];
+  const Body& bb = w.bodies[b.body];
+  if (ba.type != 2 && bb.type != 2) return false;
+  uint32_t x = (uint32_t)a.body, y = (uint32_t)b.body;
+  if (x > y) std::swap(x, y);
+  if (std::binary_search(w.noCollide.begin(), w.noCollide.end(), ((uint64_t)x << 32) | y)) return false;
+  if (a.group == b.group && a.group != 0) return a.group > 0;
+  return (a.mask & b.category) != 0 && (a.category & b.mask) != 0;
+}
+
+// Broadphase: the set of overlapping fixture AABB pairs (reference pair set:
+// include/box2d/b2_broad_phase.h:252-343 reports every overlapping pair, QueryCallback
+// src/dynamics/b2_contact_manager.cpp:136-188 filters it) in canonical (emitter, partner) order.
+// Emitter: the non-static fixture of a static/non-static pair, else the lower index.
+static void findPairs(const World& w, const std::vector<AABB>& bb, std::vector<uint64_t>* out) {
+  int n = (int)w.fixtures.size();
+  std::vector<int> order(n);
+  for (int i = 0; i < n; ++i) order[i] = i;
+  std::sort(order.begin(), order.end(), [&](int a, int b) {
+    if (bb[a].lo.x != bb[b].lo.x) return bb[a].lo.x < bb[b].lo.x;
+    return a < b;
+  });
+  out->clear();
+  for (int oi = 0; oi < n; ++oi) {
+    int i = order[oi];
+    for (int oj = oi + 1; oj < n; ++oj) {
+      int j = order[oj];
+      if (bb[j].lo.x > bb[i].hi.x) break;
+      if (!overlap(bb[i], bb[j])) continue;
+      bool si = w.bodies[w.fixtures[i].body].type == 0;
+      bool sj = w.bodies[w.fixtures[j].body].type == 0;
+      if (si && sj) continue;
+      int e, p;
+      if (si) { e = j; p = i; }
+      else if (sj) { e = i; p = j; }
+      else { e = bmin(i, j); p = bmax(i, j); }
+      if (!shouldCollide(w, e, p)) continue;
+      if (!hasCollider(w.fixtures[e].shape.type, w.fixtures[p].shape.type) &&
+          !hasCollider(w.fixtures[p].shape.type, w.fixtures[e].shape.type))
+        continue;
+      out->push_back(((uint64_t)(uint32_t)e << 32) | (uint32_t)p);
+    }
+  }
+  std::sort(out->begin(), out->end());
+}
+
+// b2Contact::b2Contact (src/dynamics/b2_contact.cpp:96-122) with b2Contact::Create's orientation
+// (:58-77); mixing laws include/box2d/b2_contact.h:42-60.
+static Contact makeContact(const World& w, uint64_t key) {
+  Contact c;
+  memset(&c, 0, sizeof(c));
+  int e = (int)(key >> 32), p = (int)(uint32_t)key;
+  int te = w.fixtures[e].shape.type, tp = w.fixtures[p].shape.type;
+  if (hasCollider(te, tp)) { c.fA = e; c.fB = p; }
+  else { c.fA = p; c.fB = e; }
+  c.key = key;
+  c.flags = B2G_CONTACT_ENABLED;
+  c.m.pointCount = 0;
+  const Fixture& fa = w.fixtures[c.fA];
+  const Fixture& fb = w.fixtures[c.fB];
+  c.friction = sqrtf(fa.friction * fb.friction);
+  c.restitution = fa.restitution > fb.restitution ? fa.restitution : fb.restitution;
+  c.threshold = fa.threshold < fb.threshold ? fa.threshold : fb.threshold;
+  c.tangentSpeed = 0.0f;
+  return c;
+}
+
+// FindNewContacts + RemoveDeadContacts (src/dynamics/b2_contact_manager.cpp:118-134): the new
+// contact list is the pair list; persisting contacts keep their state.
+static void updatePairs(World* w) {
+  int nf = (int)w->fixtures.size();
+  std::vector<AABB> bb(nf);
+  for (int i = 0; i < nf; ++i) bb[i] = computeAABB(w->fixtures[i].shape, w->bodies[w->fixtures[i].body].xf);
+  std::vector<uint64_t> pairs;
+  findPairs(*w, bb, &pairs);
+  std::vector<Contact> next;
+  next.reserve(pairs.size());
+  size_t k = 0;
+  for (uint64_t key : pairs) {
+    while (k < w->contacts.size() && w->contacts[k].key < key) ++k;
+    if (k < w->contacts.size() && w->contacts[k].key == key) next.push_back(w->contacts[k]);
+    else next.push_back(makeContact(*w, key));
+  }
+  w->contacts.swap(next);
+}
+
+// b2Contact::Update (src/dynamics/b2_contact.cpp:126-210) for every contact (sensors excluded).
+static void collide(World* w) {
+  for (Contact& c : w->contacts) {
+    Manifold old = c.m;
+    c.flags |= B2G_CONTACT_ENABLED;
+    const Fixture& fa = w->fixtures[c.fA];
+    const Fixture& fb = w->fixtures[c.fB];
+    bool touching = false;
+    if (fa.sensor || fb.sensor) {
+      c.m.pointCount = 0;
+    } else {
+      evaluate(&c.m, fa.shape, w->bodies[fa.body].xf, fb.shape, w->bodies[fb.body].xf);
+      touching = c.m.pointCount > 0;
+      for (int i = 0; i < c.m.pointCount; ++i) {
+        MPoint* mp2 = c.m.points + i;
+        mp2->normalImpulse = 0.0f;
+        mp2->tangentImpulse = 0.0f;
+        for (int j = 0; j < old.pointCount; ++j) {
+          if (old.points[j].id == mp2->id) {
+            mp2->normalImpulse = old.points[j].normalImpulse;
+            mp2->tangentImpulse = old.points[j].tangentImpulse;
+            break;
+          }
+        }
+      }
+    }
+    if (touching) c.flags |= B2G_CONTACT_TOUCHING;
+    else c.flags &= ~B2G_CONTACT_TOUCHING;
+  }
+}
+
+// Greedy colouring in priority order: each constraint takes the lowest colour not used by an
+// earlier (higher-priority) constraint sharing a non-static body; 63 = overflow (serial).
+static void colorConstraints(int n, const int* bodyA, const int* bodyB, const uint32_t* prio,
+                             const std::vector<Body>& bodies, std::vector<int>* color) {
+  std::vector<int> order(n);
+  for (int i = 0; i < n; ++i) order[i] = i;
+  std::sort(order.begin(), order.end(), [&](int a, int b) {
+    if (prio[a] != prio[b]) return prio[a] < prio[b];
+    return a < b;
+  });
+  std::vector<uint64_t> mask(bodies.size(), 0);
+  color->assign(n, -1);
+  for (int idx : order) {
+    int a = bodyA[idx], b = bodyB[idx];
+    bool sa = bodies[a].type == 0, sb = bodies[b].type == 0;
+    uint64_t used = (sa ? 0 : mask[a]) | (sb ? 0 : mask[b]);
+    uint64_t freeBits = ~used & ((1ull << kOverflow) - 1);
+    int col;
+    if (freeBits == 0) col = kOverflow;
+    else {
+      col = __builtin_ctzll(freeBits);
+      if (!sa) mask[a] |= 1ull << col;
+      if (!sb) mask[b] |= 1ull << col;
+    }
+    (*color)[idx] = col;
+  }
+}
+
+// Solve order: colour by colour; within a colour by (priority, index).
+static std::vector<int> solveOrder(int n, const std::vector<int>& color, const uint32_t* prio) {
+  std::vector<int> order(n);
+  for (int i = 0; i < n; ++i) order[i] = i;
+  std::sort(order.begin(), order.end(), [&](int a, int b) {
+    if (color[a] != color[b]) return color[a] < color[b];
+    if (prio[a] != prio[b]) return prio[a] < prio[b];
+    return a < b;
+  });
+  return order;
+}
+
+struct SolverBody { V2 c; float a; V2 v; float w; };
+
+// ---- joints (src/dynamics/b2_revolute_joint.cpp, b2_prismatic_joint.cpp, b2_distance_joint.cpp)
+struct Step { float dt, inv_dt, dtRatio; int vi, pi; bool warm; };
+
+static void jointInit(Joint& J, const std::vector<Body>& bodies, std::vector<SolverBody>& sb, const Step& st) {
+  const Body& bA = bodies[J.d.body_a];
+  const Body& bB = bodies[J.d.body_b];
+  J.iA = J.d.body_a; J.iB = J.d.body_b;
+  J.lcA = bA.localCenter; J.lcB = bB.localCenter;
+  J.mA = bA.invMass; J.mB = bB.invMass; J.invIA = bA.invI; J.invIB = bB.invI;
+  V2 cA = sb[J.iA].c; float aA = sb[J.iA].a; V2 vA = sb[J.iA].v; float wA = sb[J.iA].w;
+  V2 cB = sb[J.iB].c; float aB = sb[J.iB].a; V2 vB = sb[J.iB].v; float wB = sb[J.iB].w;
+  Rot qA = rotOf(aA), qB = rotOf(aB);
+  V2 la = v2(J.d.local_anchor_a[0], J.d.local_anchor_a[1]);
+  V2 lb = v2(J.d.local_anchor_b[0], J.d.local_anchor_b[1]);
+  float mA = J.mA, mB = J.mB, iA = J.invIA, iB = J.invIB;
+  if (J.d.type == B2G_JOINT_REVOLUTE) {
+    // b2RevoluteJoint::InitVelocityConstraints (b2_revolute_joint.cpp:73-165)
+    J.rA = mul(qA, la - J.lcA);
+    J.rB = mul(qB, lb - J.lcB);
+    J.K.ex.x = mA + mB + J.rA.y * J.rA.y * iA + J.rB.y * J.rB.y * iB;
+    J.K.ey.x = -J.rA.y * J.rA.x * iA - J.rB.y * J.rB.x * iB;
+    J.K.ex.y = J.K.ey.x;
+    J.K.ey.y = mA + mB + J.rA.x * J.rA.x * iA + J.rB.x * J.rB.x * iB;
+    J.axialMass = iA + iB;
+    bool fixedRotation;
+    if (J.axialMass > 0.0f) { J.axialMass = 1.0f / J.axialMass; fixedRotation = false; }
+    else fixedRotation = true;
+    J.angle = aB - aA - J.d.reference_angle;
+    if (J.d.enable_limit == 0 || fixedRotation) { J.lowerImpulse = 0.0f; J.upperImpulse = 0.0f; }
+    if (J.d.enable_motor == 0 || fixedRotation) J.motorImpulse = 0.0f;
+    if (st.warm) {
+      J.impulse2.x *= st.dtRatio; J.impulse2.y *= st.dtRatio;
+      J.motorImpulse *= st.dtRatio; J.lowerImpulse *= st.dtRatio; J.upperImpulse *= st.dtRatio;
+      float axialImpulse = J.motorImpulse + J.lowerImpulse - J.upperImpulse;
+      V2 P = v2(J.impulse2.x, J.impulse2.y);
+      subFrom(vA, mA * P);
+      wA -= iA * (cross(J.rA, P) + axialImpulse);
+      addTo(vB, mB * P);
+      wB += iB * (cross(J.rB, P) + axialImpulse);
+    } else {
+      J.impulse2 = v2(0.0f, 0.0f); J.motorImpulse = 0.0f; J.lowerImpulse = 0.0f; J.upperImpulse = 0.0f;
+    }
+  } else if (J.d.type == B2G_JOINT_PRISMATIC) {
+    // b2PrismaticJoint::InitVelocityConstraints (b2_prismatic_joint.cpp:114-224)
+    V2 rA = mul(qA, la - J.lcA);
+    V2 rB = mul(qB, lb - J.lcB);
+    V2 d = ((cB - cA) + rB) - rA;
+    J.axis = mul(qA, J.localXAxisA);
+    J.a1 = cross(d + rA, J.axis);
+    J.a2 = cross(rB, J.axis);
+    J.axialMass = mA + mB + iA * J.a1 * J.a1 + iB * J.a2 * J.a2;
+    if (J.axialMass > 0.0f) J.axialMass = 1.0f / J.axialMass;
+    J.perp = mul(qA, J.localYAxisA);
+    J.s1 = cross(d + rA, J.perp);
+    J.s2 = cross(rB, J.perp);
+    float k11 = mA + mB + iA * J.s1 * J.s1 + iB * J.s2 * J.s2;
+    float k12 = iA * J.s1 + iB * J.s2;
+    float k22 = iA + iB;
+    if (k22 == 0.0f) k22 = 1.0f;
+    J.K.ex = v2(k11, k12);
+    J.K.ey = v2(k12, k22);
+    if (J.d.enable_limit) J.translation = dot(J.axis, d);
+    else { J.lowerImpulse = 0.0f; J.upperImpulse = 0.0f; }
+    if (J.d.enable_motor == 0) J.motorImpulse = 0.0f;
+    if (st.warm) {
+      J.impulse2.x *= st.dtRatio; J.impulse2.y *= st.dtRatio;
+      J.motorImpulse *= st.dtRatio; J.lowerImpulse *= st.dtRatio; J.upperImpulse *= st.dtRatio;
+      float axialImpulse = J.motorImpulse + J.lowerImpulse - J.upperImpulse;
+      V2 P = J.impulse2.x * J.perp + axialImpulse * J.axis;
+      float LA = J.impulse2.x * J.s1 + J.impulse2.y + axialImpulse * J.a1;
+      float LB = J.impulse2.x * J.s2 + J.impulse2.y + axialImpulse * J.a2;
+      subFrom(vA, mA * P);
+      wA -= iA * LA;
+      addTo(vB, mB * P);
+      wB += iB * LB;
+    } else {
+      J.impulse2 = v2(0.0f, 0.0f); J.motorImpulse = 0.0f; J.lowerImpulse = 0.0f; J.upperImpulse = 0.0f;
+    }
+  } else {
+    // b2DistanceJoint::InitVelocityConstraints (b2_distance_joint.cpp:76-173)
+    J.rA = mul(qA, la - J.lcA);
+    J.rB = mul(qB, lb - J.lcB);
+    J.u = ((cB + J.rB) - cA) - J.rA;
+    J.currentLength = lengthOf(J.u);
+    if (J.currentLength > kLinearSlop) {
+      J.u = (1.0f / J.currentLength) * J.u;
+    } else {
+      J.u = v2(0.0f, 0.0f);
+      J.mass = 0.0f; J.impulse1 = 0.0f; J.lowerImpulse = 0.0f; J.upperImpulse = 0.0f;
+    }
+    float crAu = cross(J.rA, J.u);
+    float crBu = cross(J.rB, J.u);
+    float invMass = J.mA + J.invIA * crAu * crAu + J.mB + J.invIB * crBu * crBu;
+    J.mass = invMass != 0.0f ? 1.0f / invMass : 0.0f;
+    if (J.d.stiffness > 0.0f && J.d.min_length < J.d.max_length) {
+      float C = J.currentLength - J.d.length;
+      float d = J.d.damping;
+      float k = J.d.stiffness;
+      float h = st.dt;
+      J.gamma = h * (d + h * k);
+      J.gamma = J.gamma != 0.0f ? 1.0f / J.gamma : 0.0f;
+      J.bias = C * h * k * J.gamma;
+      invMass += J.gamma;
+      J.softMass = invMass != 0.0f ? 1.0f / invMass : 0.0f;
+    } else {
+      J.gamma = 0.0f; J.bias = 0.0f; J.softMass = J.mass;
+    }
+    if (st.warm) {
+      J.impulse1 *= st.dtRatio; J.lowerImpulse *= st.dtRatio; J.upperImpulse *= st.dtRatio;
+      V2 P = ((J.impulse1 + J.lowerImpulse) - J.upperImpulse) * J.u;
+      subFrom(vA, J.mA * P);
+      wA -= J.invIA * cross(J.rA, P);
+      addTo(vB, J.mB * P);
+      wB += J.invIB * cross(J.rB, P);
+    } else {
+      J.impulse1 = 0.0f;
+    }
+  }
+  sb[J.iA].v = vA; sb[J.iA].w = wA;
+  sb[J.iB].v = vB; sb[J.iB].w = wB;
+}
+
+static void jointSolveVelocity(Joint& J, std::vector<SolverBody>& sb, const Step& st) {
+  V2 vA = sb[J.iA].v; float wA = sb[J.iA].w;
+  V2 vB = sb[J.iB].v; float wB = sb[J.iB].w;
+  float mA = J.mA, mB = J.mB, iA = J.invIA, iB = J.invIB;
+  if (J.d.type == B2G_JOINT_REVOLUTE) {
+    // b2RevoluteJoint::SolveVelocityConstraints (b2_revolute_joint.cpp:167-243)
+    bool fixedRotation = (iA + iB == 0.0f);
+    if (J.d.enable_motor && fixedRotation == false) {
+      float Cdot = wB - wA - J.d.motor_speed;
+      float impulse = -J.axialMass * Cdot;
+      float oldImpulse = J.motorImpulse;
+      float maxImpulse = st.dt * J.d.max_motor;
+      J.motorImpulse = bclamp(J.motorImpulse + impulse, -maxImpulse, maxImpulse);
+      impulse = J.motorImpulse - oldImpulse;
+      wA -= iA * impulse;
+      wB += iB * impulse;
+    }
+    if (J.d.enable_limit && fixedRotation == false) {
+      {
+        float C = J.angle - J.d.lower;
+        float Cdot = wB - wA;
+        float impulse = -J.axialMass * (Cdot + bmax(C, 0.0f) * st.inv_dt);
+        float oldImpulse = J.lowerImpulse;
+        J.lowerImpulse = bmax(J.lowerImpulse + impulse, 0.0f);
+        impulse = J.lowerImpulse - oldImpulse;
+        wA -= iA * impulse;
+        wB += iB * impulse;
+      }
+      {
+        float C = J.d.upper - J.angle;
+        float Cdot = wA - wB;
+        float impulse = -J.axialMass * (Cdot + bmax(C, 0.0f) * st.inv_dt);
+        float oldImpulse = J.upperImpulse;
+        J.upperImpulse = bmax(J.upperImpulse + impulse, 0.0f);
+        impulse = J.upperImpulse - oldImpulse;
+        wA += iA * impulse;
+        wB -= iB * impulse;
+      }
+    }
+    {
+      V2 Cdot = ((vB + cross(wB, J.rB)) - vA) - cross(wA, J.rA);
+      V2 impulse = solve(J.K, -Cdot);
+      J.impulse2.x += impulse.x;
+      J.impulse2.y += impulse.y;
+      subFrom(vA, mA * impulse);
+      wA -= iA * cross(J.rA, impulse);
+      addTo(vB, mB * impulse);
+      wB += iB * cross(J.rB, impulse);
+    }
+  } else if (J.d.type == B2G_JOINT_PRISMATIC) {
+    // b2PrismaticJoint::SolveVelocityConstraints (b2_prismatic_joint.cpp:226-330)
+    if (J.d.enable_motor) {
+      float Cdot = (dot(J.axis, vB - vA) + J.a2 * wB) - J.a1 * wA;
+      float impulse = J.axialMass * (J.d.motor_speed - Cdot);
+      float oldImpulse = J.motorImpulse;
+      float maxImpulse = st.dt * J.d.max_motor;
+      J.motorImpulse = bclamp(J.motorImpulse + impulse, -maxImpulse, maxImpulse);
+      impulse = J.motorImpulse - oldImpulse;
+      V2 P = impulse * J.axis;
+      float LA = impulse * J.a1;
+      float LB = impulse * J.a2;
+      subFrom(vA, mA * P); wA -= iA * LA;
+      addTo(vB, mB * P); wB += iB * LB;
+    }
+    if (J.d.enable_limit) {
+      {
+        float C = J.translation - J.d.lower;
+        float Cdot = (dot(J.axis, vB - vA) + J.a2 * wB) - J.a1 * wA;
+        float impulse = -J.axialMass * (Cdot + bmax(C, 0.0f) * st.inv_dt);
+        float oldImpulse = J.lowerImpulse;
+        J.lowerImpulse = bmax(J.lowerImpulse + impulse, 0.0f);
+        impulse = J.lowerImpulse - oldImpulse;
+        V2 P = impulse * J.axis;
+        float LA = impulse * J.a1;
+        float LB = impulse * J.a2;
+        subFrom(vA, mA * P); wA -= iA * LA;
+        addTo(vB, mB * P); wB += iB * LB;
+      }
+      {
+        float C = J.d.upper - J.translation;
+        float Cdot = (dot(J.axis, vA - vB) + J.a1 * wA) - J.a2 * wB;
+        float impulse = -J.axialMass * (Cdot + bmax(C, 0.0f) * st.inv_dt);
+        float oldImpulse = J.upperImpulse;
+        J.upperImpulse = bmax(J.upperImpulse + impulse, 0.0f);
+        impulse = J.upperImpulse - oldImpulse;
+        V2 P = impulse * J.axis;
+        float LA = impulse * J.a1;
+        float LB = impulse * J.a2;
+        addTo(vA, mA * P); wA += iA * LA;
+        subFrom(vB, mB * P); wB -= iB * LB;
+      }
+    }
+    {
+      V2 Cdot;
+      Cdot.x = (dot(J.perp, vB - vA) + J.s2 * wB) - J.s1 * wA;
+      Cdot.y = wB - wA;
+      V2 df = solve(J.K, -Cdot);
+      addTo(J.impulse2, df);
+      V2 P = df.x * J.perp;
+      float LA = df.x * J.s1 + df.y;
+      float LB = df.x * J.s2 + df.y;
+      subFrom(vA, mA * P); wA -= iA * LA;
+      addTo(vB, mB * P); wB += iB * LB;
+    }
+  } else {
+    // b2DistanceJoint::SolveVelocityConstraints (b2_distance_joint.cpp:175-266)
+    if (J.d.min_length < J.d.max_length) {
+      if (J.d.stiffness > 0.0f) {
+        V2 vpA = vA + cross(wA, J.rA);
+        V2 vpB = vB + cross(wB, J.rB);
+        float Cdot = dot(J.u, vpB - vpA);
+        float impulse = -J.softMass * ((Cdot + J.bias) + J.gamma * J.impulse1);
+        J.impulse1 += impulse;
+        V2 P = impulse * J.u;
+        subFrom(vA, J.mA * P); wA -= J.invIA * cross(J.rA, P);
+        addTo(vB, J.mB * P); wB += J.invIB * cross(J.rB, P);
+      }
+      {
+        float C = J.currentLength - J.d.min_length;
+        float bias = bmax(0.0f, C) * st.inv_dt;
+        V2 vpA = vA + cross(wA, J.rA);
+        V2 vpB = vB + cross(wB, J.rB);
+        float Cdot = dot(J.u, vpB - vpA);
+        float impulse = -J.mass * (Cdot + bias);
+        float oldImpulse = J.lowerImpulse;
+        J.lowerImpulse = bmax(0.0f, J.lowerImpulse + impulse);
+        impulse = J.lowerImpulse - oldImpulse;
+        V2 P = impulse * J.u;
+        subFrom(vA, J.mA * P); wA -= J.invIA * cross(J.rA, P);
+        addTo(vB, J.mB * P); wB += J.invIB * cross(J.rB, P);
+      }
+      {
+        float C = J.d.max_length - J.currentLength;
+        float bias = bmax(0.0f, C) * st.inv_dt;
+        V2 vpA = vA + cross(wA, J.rA);
+        V2 vpB = vB + cross(wB, J.rB);
+        float Cdot = dot(J.u, vpA - vpB);
+        float impulse = -J.mass * (Cdot + bias);
+        float oldImpulse = J.upperImpulse;
+        J.upperImpulse = bmax(0.0f, J.upperImpulse + impulse);
+        impulse = J.upperImpulse - oldImpulse;
+        V2 P = -impulse * J.u;
+        subFrom(vA, J.mA * P); wA -= J.invIA * cross(J.rA, P);
+        addTo(vB, J.mB * P); wB += J.invIB * cross(J.rB, P);
+      }
+    } else {
+      V2 vpA = vA + cross(wA, J.rA);
+      V2 vpB = vB + cross(wB, J.rB);
+      float Cdot = dot(J.u, vpB - vpA);
+      float impulse = -J.mass * Cdot;
+      J.impulse1 += impulse;
+      V2 P = impulse * J.u;
+      subFrom(vA, J.mA * P); wA -= J.invIA * cross(J.rA, P);
+      addTo(vB, J.mB * P); wB += J.invIB * cross(J.rB, P);
+    }
+  }
+  sb[J.iA].v = vA; sb[J.iA].w = wA;
+  sb[J.iB].v = vB; sb[J.iB].w = wB;
+}
+
+static bool jointSolvePosition(Joint& J, std::vector<SolverBody>& sb) {
+  V2 cA = sb[J.iA].c; float aA = sb[J.iA].a;
+  V2 cB = sb[J.iB].c; float aB = sb[J.iB].a;
+  Rot qA = rotOf(aA), qB = rotOf(aB);
+  V2 la = v2(J.d.local_anchor_a[0], J.d.local_anchor_a[1]);
+  V2 lb = v2(J.d.local_anchor_b[0], J.d.local_anchor_b[1]);
+  bool ok;
+  if (J.d.type == B2G_JOINT_REVOLUTE) {
+    // b2RevoluteJoint::SolvePositionConstraints (b2_revolute_joint.cpp:245-321)
+    float angularError = 0.0f;
+    float positionError = 0.0f;
+    bool fixedRotation = (J.invIA + J.invIB == 0.0f);
+    if (J.d.enable_limit && fixedRotation == false) {
+      float angle = aB - aA - J.d.reference_angle;
+      float C = 0.0f;
+      if (babs(J.d.upper - J.d.lower) < 2.0f * kAngularSlop)
+        C = bclamp(angle - J.d.lower, -kMaxAngularCorrection, kMaxAngularCorrection);
+      else if (angle <= J.d.lower)
+        C = bclamp(angle - J.d.lower + kAngularSlop, -kMaxAngularCorrection, 0.0f);
+      else if (angle >= J.d.upper)
+        C = bclamp(angle - J.d.upper - kAngularSlop, 0.0f, kMaxAngularCorrection);
+      float limitImpulse = -J.axialMass * C;
+      aA -= J.invIA * limitImpulse;
+      aB += J.invIB * limitImpulse;
+      angularError = babs(C);
+    }
+    {
+      qA = rotOf(aA);
+      qB = rotOf(aB);
+      V2 rA = mul(qA, la - J.lcA);
+      V2 rB = mul(qB, lb - J.lcB);
+      V2 C = ((cB + rB) - cA) - rA;
+      positionError = lengthOf(C);
+      float mA = J.mA, mB = J.mB, iA = J.invIA, iB = J.invIB;
+      M22 K;
+      K.ex.x = mA + mB + iA * rA.y * rA.y + iB * rB.y * rB.y;
+      K.ex.y = -iA * rA.x * rA.y - iB * rB.x * rB.y;
+      K.ey.x = K.ex.y;
+      K.ey.y = mA + mB + iA * rA.x * rA.x + iB * rB.x * rB.x;
+      V2 impulse = -solve(K, C);
+      subFrom(cA, mA * impulse);
+      aA -= iA * cross(rA, impulse);
+      addTo(cB, mB * impulse);
+      aB += iB * cross(rB, impulse);
+    }
+    ok = positionError <= kLinearSlop && angularError <= kAngularSlop;
+  } else if (J.d.type == B2G_JOINT_PRISMATIC) {
+    // b2PrismaticJoint::SolvePositionConstraints (b2_prismatic_joint.cpp:340-459)
+    float mA = J.mA, mB = J.mB, iA = J.invIA, iB = J.invIB;
+    V2 rA = mul(qA, la - J.lcA);
+    V2 rB = mul(qB, lb - J.lcB);
+    V2 d = ((cB + rB) - cA) - rA;
+    V2 axis = mul(qA, J.localXAxisA);
+    float a1 = cross(d + rA, axis);
+    float a2 = cross(rB, axis);
+    V2 perp = mul(qA, J.localYAxisA);
+    float s1 = cross(d + rA, perp);
+    float s2 = cross(rB, perp);
+    V3 impulse;
+    V2 C1;
+    C1.x = dot(perp, d);
+    C1.y = aB - aA - J.d.reference_angle;
+    float linearError = babs(C1.x);
+    float angularError = babs(C1.y);
+    bool active = false;
+    float C2 = 0.0f;
+    if (J.d.enable_limit) {
+      float translation = dot(axis, d);
+      if (babs(J.d.upper - J.d.lower) < 2.0f * kLinearSlop) {
+        C2 = translation;
+        linearError = bmax(linearError, babs(translation));
+        active = true;
+      } else if (translation <= J.d.lower) {
+        C2 = bmin(translation - J.d.lower, 0.0f);
+        linearError = bmax(linearError, J.d.lower - translation);
+        active = true;
+      } else if (translation >= J.d.upper) {
+        C2 = bmax(translation - J.d.upper, 0.0f);
+        linearError = bmax(linearError, translation - J.d.upper);
+        active = true;
+      }
+    }
+    if (active) {
+      float k11 = mA + mB + iA * s1 * s1 + iB * s2 * s2;
+      float k12 = iA * s1 + iB * s2;
+      float k13 = iA * s1 * a1 + iB * s2 * a2;
+      float k22 = iA + iB;
+      if (k22 == 0.0f) k22 = 1.0f;
+      float k23 = iA * a1 + iB * a2;
+      float k33 = mA + mB + iA * a1 * a1 + iB * a2 * a2;
+      V3 ex = {k11, k12, k13}, ey = {k12, k22, k23}, ez = {k13, k23, k33};
+      V3 Cn = {-C1.x, -C1.y, -C2};
+      impulse = solve33(ex, ey, ez, Cn);
+    } else {
+      float k11 = mA + mB + iA * s1 * s1 + iB * s2 * s2;
+      float k12 = iA * s1 + iB * s2;
+      float k22 = iA + iB;
+      if (k22 == 0.0f) k22 = 1.0f;
+      M22 K;
+      K.ex = v2(k11, k12);
+      K.ey = v2(k12, k22);
+      V2 impulse1 = solve(K, -C1);
+      impulse.x = impulse1.x; impulse.y = impulse1.y; impulse.z = 0.0f;
+    }
+    V2 P = impulse.x * perp + impulse.z * axis;
+    float LA = (impulse.x * s1 + impulse.y) + impulse.z * a1;
+    float LB = (impulse.x * s2 + impulse.y) + impulse.z * a2;
+    subFrom(cA, mA * P); aA -= iA * LA;
+    addTo(cB, mB * P); aB += iB * LB;
+    ok = linearError <= kLinearSlop && angularError <= kAngularSlop;
+  } else {
+    // b2DistanceJoint::SolvePositionConstraints (b2_distance_joint.cpp:268-314)
+    V2 rA = mul(qA, la - J.lcA);
+    V2 rB = mul(qB, lb - J.lcB);
+    V2 u = ((cB + rB) - cA) - rA;
+    float length = normalize(u);
+    float C;
+    if (J.d.min_length == J.d.max_length) C = length - J.d.min_length;
+    else if (length < J.d.min_length) C = length - J.d.min_length;
+    else if (J.d.max_length < length) C = length - J.d.max_length;
+    else return true;
+    float impulse = -J.mass * C;
+    V2 P = impulse * u;
+    subFrom(cA, J.mA * P); aA -= J.invIA * cross(rA, P);
+    addTo(cB, J.mB * P); aB += J.invIB * cross(rB, P);
+    ok = babs(C) < kLinearSlop;
+  }
+  sb[J.iA].c = cA; sb[J.iA].a = aA;
+  sb[J.iB].c = cB; sb[J.iB].a = aB;
+  return ok;
+}
+
+// Reaction force/torque after the step (GetReactionForce/Torque of each joint type).
+static void jointReaction(const Joint& J, float inv_dt, float* F, float* T) {
+  if (J.d.type == B2G_JOINT_REVOLUTE) {
+    F[0] = inv_dt * J.impulse2.x; F[1] = inv_dt * J.impulse2.y;
+    *T = inv_dt * ((J.motorImpulse + J.lowerImpulse) - J.upperImpulse);
+  } else if (J.d.type == B2G_JOINT_PRISMATIC) {
+    V2 f = inv_dt * (J.impulse2.x * J.perp + ((J.motorImpulse + J.lowerImpulse) - J.upperImpulse) * J.axis);
+    F[0] = f.x; F[1] = f.y;
+    *T = inv_dt * J.impulse2.y;
+  } else {
+    V2 f = (inv_dt * ((J.impulse1 + J.lowerImpulse) - J.upperImpulse)) * J.u;
+    F[0] = f.x; F[1] = f.y;
+    *T = 0.0f;
+  }
+}
+
+// ---- the contact solver (src/dynamics/b2_contact_solver.cpp)
+static void prepareContacts(World* w, const std::vector<int>& solverContacts, std::vector<SolverBody>& sb,
+                            const Step& st, std::vector<VC>& vcs, std::vector<PC>& pcs) {
+  int n = (int)solverContacts.size();
+  vcs.assign(n, VC());
+  pcs.assign(n, PC());
+  for (int i = 0; i < n; ++i) {
+    // b2ContactSolver::Initialize (:65-152)
+    Contact& c = w->contacts[solverContacts[i]];
+    const Fixture& fa = w->fixtures[c.fA];
+    const Fixture& fb = w->fixtures[c.fB];
+    const Body& bA = w->bodies[fa.body];
+    const Body& bB = w->bodies[fb.body];
+    VC& vc = vcs[i];
+    PC& pc = pcs[i];
+    memset(&vc, 0, sizeof(vc));
+    memset(&pc, 0, sizeof(pc));
+    vc.friction = c.friction; vc.restitution = c.restitution; vc.threshold = c.threshold;
+    vc.tangentSpeed = c.tangentSpeed;
+    vc.indexA = fa.body; vc.indexB = fb.body;
+    vc.invMassA = bA.invMass; vc.invMassB = bB.invMass; vc.invIA = bA.invI; vc.invIB = bB.invI;
+    vc.contact = solverContacts[i];
+    vc.pointCount = c.m.pointCount;
+    pc.indexA = fa.body; pc.indexB = fb.body;
+    pc.invMassA = bA.invMass; pc.invMassB = bB.invMass;
+    pc.localCenterA = bA.localCenter; pc.localCenterB = bB.localCenter;
+    pc.invIA = bA.invI; pc.invIB = bB.invI;
+    pc.localNormal = c.m.localNormal; pc.localPoint = c.m.localPoint;
+    pc.pointCount = c.m.pointCount;
+    pc.radiusA = fa.shape.radius; pc.radiusB = fb.shape.radius;
+    pc.type = c.m.type;
+    for (int j = 0; j < c.m.pointCount; ++j) {
+      if (st.warm) {
+        vc.points[j].normalImpulse = st.dtRatio * c.m.points[j].normalImpulse;
+        vc.points[j].tangentImpulse = st.dtRatio * c.m.points[j].tangentImpulse;
+      } else {
+        vc.points[j].normalImpulse = 0.0f;
+        vc.points[j].tangentImpulse = 0.0f;
+      }
+      pc.localPoints[j] = c.m.points[j].localPoint;
+    }
+  }
+  for (int i = 0; i < n; ++i) {
+    // b2ContactSolver::InitializeVelocityConstraints (:155-258)
+    VC& vc = vcs[i];
+    PC& pc = pcs[i];
+    const Manifold& manifold = w->contacts[vc.contact].m;
+    float mA = vc.invMassA, mB = vc.invMassB, iA = vc.invIA, iB = vc.invIB;
+    V2 cA = sb[vc.indexA].c; float aA = sb[vc.indexA].a; V2 vA = sb[vc.indexA].v; float wA = sb[vc.indexA].w;
+    V2 cB = sb[vc.indexB].c; float aB = sb[vc.indexB].a; V2 vB = sb[vc.indexB].v; float wB = sb[vc.indexB].w;
+    Xf xfA, xfB;
+    xfA.q = rotOf(aA);
+    xfB.q = rotOf(aB);
+    xfA.p = cA - mul(xfA.q, pc.localCenterA);
+    xfB.p = cB - mul(xfB.q, pc.localCenterB);
+    WorldManifold wm;
+    memset(&wm, 0, sizeof(wm));
+    worldManifold(&wm, manifold, xfA, pc.radiusA, xfB, pc.radiusB);
+    vc.normal = wm.normal;
+    V2 tangent = cross(vc.normal, 1.0f);
+    for (int j = 0; j < vc.pointCount; ++j) {
+      VCPoint& vcp = vc.points[j];
+      vcp.rA = wm.points[j] - cA;
+      vcp.rB = wm.points[j] - cB;
+      float rnA = cross(vcp.rA, vc.normal);
+      float rnB = cross(vcp.rB, vc.normal);
+      float kNormal = mA + mB + iA * rnA * rnA + iB * rnB * rnB;
+      vcp.normalMass = kNormal > 0.0f ? 1.0f / kNormal : 0.0f;
+      float rtA = cross(vcp.rA, tangent);
+      float rtB = cross(vcp.rB, tangent);
+      float kTangent = mA + mB + iA * rtA * rtA + iB * rtB * rtB;
+      vcp.tangentMass = kTangent > 0.0f ? 1.0f / kTangent : 0.0f;
+      vcp.velocityBias = 0.0f;
+      float vRel = dot(vc.normal, (vB + cross(wB, vcp.rB)) - (vA + cross(wA, vcp.rA)));
+      if (vRel < -vc.threshold) vcp.velocityBias = -vc.restitution * vRel;
+    }
+    if (vc.pointCount == 2) {
+      VCPoint& vcp1 = vc.points[0];
+      VCPoint& vcp2 = vc.points[1];
+      float rn1A = cross(vcp1.rA, vc.normal);
+      float rn1B = cross(vcp1.rB, vc.normal);
+      float rn2A = cross(vcp2.rA, vc.normal);
+      float rn2B = cross(vcp2.rB, vc.normal);
+      float k11 = mA + mB + iA * rn1A * rn1A + iB * rn1B * rn1B;
+      float k22 = mA + mB + iA * rn2A * rn2A + iB * rn2B * rn2B;
+      float k12 = mA + mB + iA * rn1A * rn2A + iB * rn1B * rn2B;
+      const float k_maxConditionNumber = 1000.0f;
+      if (k11 * k11 < k_maxConditionNumber * (k11 * k22 - k12 * k12)) {
+        vc.K.ex = v2(k11, k12);
+        vc.K.ey = v2(k12, k22);
+        vc.normalMass = inverse(vc.K);
+      } else {
+        vc.pointCount = 1;
+      }
+    }
+  }
+}
+
+// b2ContactSolver::WarmStart (:260-299) for one constraint.
+static void warmStartOne(VC& vc, std::vector<SolverBody>& sb) {
+  float mA = vc.invMassA, iA = vc.invIA, mB = vc.invMassB, iB = vc.invIB;
+  V2 vA = sb[vc.indexA].v; float wA = sb[vc.indexA].w;
+  V2 vB = sb[vc.indexB].v; float wB = sb[vc.indexB].w;
+  V2 normal = vc.normal;
+  V2 tangent = cross(normal, 1.0f);
+  for (int j = 0; j < vc.pointCount; ++j) {
+    VCPoint& vcp = vc.points[j];
+    V2 P = vcp.normalImpulse * normal + vcp.tangentImpulse * tangent;
+    wA -= iA * cross(vcp.rA, P);
+    subFrom(vA, mA * P);
+    wB += iB * cross(vcp.rB, P);
+    addTo(vB, mB * P);
+  }
+  sb[vc.indexA].v = vA; sb[vc.indexA].w = wA;
+  sb[vc.indexB].v = vB; sb[vc.indexB].w = wB;
+}
+
+// b2ContactSolver::SolveVelocityConstraints (:301-639) for one constraint.
+static void solveVelocityOne(VC& vc, std::vector<SolverBody>& sb) {
+  float mA = vc.invMassA, iA = vc.invIA, mB = vc.invMassB, iB = vc.invIB;
+  int pointCount = vc.pointCount;
+  V2 vA = sb[vc.indexA].v; float wA = sb[vc.indexA].w;
+  V2 vB = sb[vc.indexB].v; float wB = sb[vc.indexB].w;
+  V2 normal = vc.normal;
+  V2 tangent = cross(normal, 1.0f);
+  for (int j = 0; j < pointCount; ++j) {
+    VCPoint& vcp = vc.points[j];
+    V2 dv = (vB + cross(wB, vcp.rB)) - (vA + cross(wA, vcp.rA));
+    float vt = dot(dv, tangent) - vc.tangentSpeed;
+    float lambda = vcp.tangentMass * (-vt);
+    float maxFriction = vc.friction * vcp.normalImpulse;
+    float newImpulse = bclamp(vcp.tangentImpulse + lambda, -maxFriction, maxFriction);
+    lambda = newImpulse - vcp.tangentImpulse;
+    vcp.tangentImpulse = newImpulse;
+    V2 P = lambda * tangent;
+    subFrom(vA, mA * P);
+    wA -= iA * cross(vcp.rA, P);
+    addTo(vB, mB * P);
+    wB += iB * cross(vcp.rB, P);
+  }
+  if (pointCount == 1) {
+    VCPoint& vcp = vc.points[0];
+    V2 dv = (vB + cross(wB, vcp.rB)) - (vA + cross(wA, vcp.rA));
+    float vn = dot(dv, normal);
+    float lambda = -vcp.normalMass * (vn - vcp.velocityBias);
+    float newImpulse = bmax(vcp.normalImpulse + lambda, 0.0f);
+    lambda = newImpulse - vcp.normalImpulse;
+    vcp.normalImpulse = newImpulse;
+    V2 P = lambda * normal;
+    subFrom(vA, mA * P);
+    wA -= iA * cross(vcp.rA, P);
+    addTo(vB, mB * P);
+    wB += iB * cross(vcp.rB, P);
+  } else {
+    VCPoint& cp1 = vc.points[0];
+    VCPoint& cp2 = vc.points[1];
+    V2 a = v2(cp1.normalImpulse, cp2.normalImpulse);
+    V2 dv1 = (vB + cross(wB, cp1.rB)) - (vA + cross(wA, cp1.rA));
+    V2 dv2 = (vB + cross(wB, cp2.rB)) - (vA + cross(wA, cp2.rA));
+    float vn1 = dot(dv1, normal);
+    float vn2 = dot(dv2, normal);
+    V2 b;
+    b.x = vn1 - cp1.velocityBias;
+    b.y = vn2 - cp2.velocityBias;
+    subFrom(b, mul(vc.K, a));
+    for (;;) {
+      V2 x = -mul(vc.normalMass, b);
+      if (x.x >= 0.0f && x.y >= 0.0f) {
+        V2 d = x - a;
+        V2 P1 = d.x * normal;
+        V2 P2 = d.y * normal;
+        subFrom(vA, mA * (P1 + P2));
+        wA -= iA * (cross(cp1.rA, P1) + cross(cp2.rA, P2));
+        addTo(vB, mB * (P1 + P2));
+        wB += iB * (cross(cp1.rB, P1) + cross(cp2.rB, P2));
+        cp1.normalImpulse = x.x;
+        cp2.normalImpulse = x.y;
+        break;
+      }
+      x.x = -cp1.normalMass * b.x;
+      x.y = 0.0f;
+      vn1 = 0.0f;
+      vn2 = vc.K.ex.y * x.x + b.y;
+      if (x.x >= 0.0f && vn2 >= 0.0f) {
+        V2 d = x - a;
+        V2 P1 = d.x * normal;
+        V2 P2 = d.y * normal;
+        subFrom(vA, mA * (P1 + P2));
+        wA -= iA * (cross(cp1.rA, P1) + cross(cp2.rA, P2));
+        addTo(vB, mB * (P1 + P2));
+        wB += iB * (cross(cp1.rB, P1) + cross(cp2.rB, P2));
+        cp1.normalImpulse = x.x;
+        cp2.normalImpulse = x.y;
+        break;
+      }
+      x.x = 0.0f;
+      x.y = -cp2.normalMass * b.y;
+      vn1 = vc.K.ey.x * x.y + b.x;
+      vn2 = 0.0f;
+      if (x.y >= 0.0f && vn1 >= 0.0f) {
+        V2 d = x - a;
+        V2 P1 = d.x * normal;
+        V2 P2 = d.y * normal;
+        subFrom(vA, mA * (P1 + P2));
+        wA -= iA * (cross(cp1.rA, P1) + cross(cp2.rA, P2));
+        addTo(vB, mB * (P1 + P2));
+        wB += iB * (cross(cp1.rB, P1) + cross(cp2.rB, P2));
+        cp1.normalImpulse = x.x;
+        cp2.normalImpulse = x.y;
+        break;
+      }
+      x.x = 0.0f;
+      x.y = 0.0f;
+      vn1 = b.x;
+      vn2 = b.y;
+      if (vn1 >= 0.0f && vn2 >= 0.0f) {
+        V2 d = x - a;
+        V2 P1 = d.x * normal;
+        V2 P2 = d.y * normal;
+        subFrom(vA, mA * (P1 + P2));
+        wA -= iA * (cross(cp1.rA, P1) + cross(cp2.rA, P2));
+        addTo(vB, mB * (P1 + P2));
+        wB += iB * (cross(cp1.rB, P1) + cross(cp2.rB, P2));
+        cp1.normalImpulse = x.x;
+        cp2.normalImpulse = x.y;
+        break;
+      }
+      break;
+    }
+  }
+  sb[vc.indexA].v = vA; sb[vc.indexA].w = wA;
+  sb[vc.indexB].v = vB; sb[vc.indexB].w = wB;
+}
+
+// b2PositionSolverManifold::Initialize (:659-708) + SolvePositionConstraints (:711-787) for one
+// constraint; returns this constraint's minimum separation (starting from 0).
+static float solvePositionOne(const PC& pc, std::vector<SolverBody>& sb) {
+  float minSeparation = 0.0f;
+  V2 localCenterA = pc.localCenterA, localCenterB = pc.localCenterB;
+  float mA = pc.invMassA, iA = pc.invIA, mB = pc.invMassB, iB = pc.invIB;
+  V2 cA = sb[pc.indexA].c; float aA = sb[pc.indexA].a;
+  V2 cB = sb[pc.indexB].c; float aB = sb[pc.indexB].a;
+  for (int j = 0; j < pc.pointCount; ++j) {
+    Xf xfA, xfB;
+    xfA.q = rotOf(aA);
+    xfB.q = rotOf(aB);
+    xfA.p = cA - mul(xfA.q, localCenterA);
+    xfB.p = cB - mul(xfB.q, localCenterB);
+    V2 normal, point;
+    float separation;
+    if (pc.type == 0) {
+      V2 pointA = mul(xfA, pc.localPoint);
+      V2 pointB = mul(xfB, pc.localPoints[0]);
+      normal = pointB - pointA;
+      normalize(normal);
+      point = 0.5f * (pointA + pointB);
+      separation = (dot(pointB - pointA, normal) - pc.radiusA) - pc.radiusB;
+    } else if (pc.type == 1) {
+      normal = mul(xfA.q, pc.localNormal);
+      V2 planePoint = mul(xfA, pc.localPoint);
+      V2 clipPoint = mul(xfB, pc.localPoints[j]);
+      separation = (dot(clipPoint - planePoint, normal) - pc.radiusA) - pc.radiusB;
+      point = clipPoint;
+    } else {
+      normal = mul(xfB.q, pc.localNormal);
+      V2 planePoint = mul(xfB, pc.localPoint);
+      V2 clipPoint = mul(xfA, pc.localPoints[j]);
+      separation = (dot(clipPoint - planePoint, normal) - pc.radiusA) - pc.radiusB;
+      point = clipPoint;
+      normal = -normal;
+    }
+    V2 rA = point - cA;
+    V2 rB = point - cB;
+    minSeparation = bmin(minSeparation, separation);
+    float C = bclamp(kBaumgarte * (separation + kLinearSlop), -kMaxLinearCorrection, 0.0f);
+    float rnA = cross(rA, normal);
+    float rnB = cross(rB, normal);
+    float K = mA + mB + iA * rnA * rnA + iB * rnB * rnB;
+    float impulse = K > 0.0f ? -C / K : 0.0f;
+    V2 P = impulse * normal;
+    subFrom(cA, mA * P);
+    aA -= iA * cross(rA, P);
+    addTo(cB, mB * P);
+    aB += iB * cross(rB, P);
+  }
+  sb[pc.indexA].c = cA; sb[pc.indexA].a = aA;
+  sb[pc.indexB].c = cB; sb[pc.indexB].a = aB;
+  return minSeparation;
+}
+
+// One b2World::Step (src/dynamics/b2_world.cpp:1108-1171) with sleeping and CCD off.
+static void stepWorld(World* w, float dt, int vi, int pi) {
+  if (w->newContacts) {
+    updatePairs(w);
+    w->newContacts = false;
+  }
+  Step st;
+  st.dt = dt;
+  st.inv_dt = (dt > 0.0f) ? 1.0f / dt : 0.0f;
+  st.dtRatio = w->inv_dt0 * dt;
+  st.vi = vi;
+  st.pi = pi;
+  st.warm = w->warmStarting;
+  collide(w);
+  if (dt > 0.0f) {
+    int nb = (int)w->bodies.size();
+    float h = st.dt;
+    std::vector<SolverBody> sb(nb);
+    // b2Island::Solve velocity integration (src/dynamics/b2_island.cpp:256-293) / SolveOrphan
+    for (int i = 0; i < nb; ++i) {
+      Body& b = w->bodies[i];
+      V2 v = b.v;
+      float wv = b.w;
+      if (b.type == 2) {
+        addTo(v, (h * b.invMass) * (b.gravityScale * b.mass * w->gravity + b.force));
+        wv += h * b.invI * b.torque;
+        v.x /= (1.0f + h * b.linearDamping);
+        v.y /= (1.0f + h * b.linearDamping);
+        wv /= (1.0f + h * b.angularDamping);
+      }
+      sb[i].c = b.c; sb[i].a = b.a; sb[i].v = v; sb[i].w = wv;
+    }
+    // solver contact set: touching, enabled, no sensor, enabled bodies (b2_world.cpp:567-599)
+    std::vector<int> solverContacts;
+    for (int i = 0; i < (int)w->contacts.size(); ++i) {
+      const Contact& c = w->contacts[i];
+      if ((c.flags & B2G_CONTACT_TOUCHING) == 0 || (c.flags & B2G_CONTACT_ENABLED) == 0) continue;
+      if (w->fixtures[c.fA].sensor || w->fixtures[c.fB].sensor) continue;
+      solverContacts.push_back(i);
+    }
+    int nc = (int)solverContacts.size();
+    int nj = (int)w->joints.size();
+    std::vector<VC> vcs;
+    std::vector<PC> pcs;
+    prepareContacts(w, solverContacts, sb, st, vcs, pcs);
+    // colouring
+    std::vector<int> cA(nc), cB(nc), jA(nj), jB(nj);
+    std::vector<uint32_t> cp(nc), jp(nj);
+    for (int i = 0; i < nc; ++i) {
+      cA[i] = vcs[i].indexA; cB[i] = vcs[i].indexB;
+      cp[i] = contactPriority(w->contacts[solverContacts[i]].key);
+    }
+    for (int j = 0; j < nj; ++j) {
+      jA[j] = w->joints[j].d.body_a; jB[j] = w->joints[j].d.body_b;
+      jp[j] = jointPriority((uint32_t)j);
+    }
+    std::vector<int> ccol, jcol;
+    colorConstraints(nc, cA.data(), cB.data(), cp.data(), w->bodies, &ccol);
+    colorConstraints(nj, jA.data(), jB.data(), jp.data(), w->bodies, &jcol);
+    std::vector<int> corder = solveOrder(nc, ccol, cp.data());
+    std::vector<int> jorder = solveOrder(nj, jcol, jp.data());
+    w->contactColor.assign(w->contacts.size(), -1);
+    w->contactPrio.assign(w->contacts.size(), 0);
+    for (int i = 0; i < nc; ++i) {
+      w->contactColor[solverContacts[i]] = ccol[i];
+      w->contactPrio[solverContacts[i]] = cp[i];
+    }
+    w->jointColor = jcol;
+    w->jointPrioV = jp;
+    w->lastContactOrder.clear();
+    for (int i : corder) {
+      w->lastContactOrder.push_back(w->contacts[solverContacts[i]].fA);
+      w->lastContactOrder.push_back(w->contacts[solverContacts[i]].fB);
+    }
+    w->lastJointOrder.assign(jorder.begin(), jorder.end());
+    // warm start (b2_island.cpp:304-325): contacts, then joint init
+    if (st.warm)
+      for (int i : corder) warmStartOne(vcs[i], sb);
+    for (int j : jorder) jointInit(w->joints[j], w->bodies, sb, st);
+    // velocity iterations (b2_island.cpp:327-346): joints then contacts
+    for (int it = 0; it < vi; ++it) {
+      for (int j : jorder) jointSolveVelocity(w->joints[j], sb, st);
+      for (int i : corder) solveVelocityOne(vcs[i], sb);
+    }
+    // StoreImpulses (b2_contact_solver.cpp:641-657)
+    for (int i = 0; i < nc; ++i) {
+      Manifold& m = w->contacts[vcs[i].contact].m;
+      for (int j = 0; j < vcs[i].pointCount; ++j) {
+        m.points[j].normalImpulse = vcs[i].points[j].normalImpulse;
+        m.points[j].tangentImpulse = vcs[i].points[j].tangentImpulse;
+      }
+    }
+    // integrate positions (b2_island.cpp:349-385)
+    for (int i = 0; i < nb; ++i) {
+      if (w->bodies[i].type == 0) continue;
+      V2 c = sb[i].c; float a = sb[i].a; V2 v = sb[i].v; float wv = sb[i].w;
+      V2 translation = h * v;
+      if (dot(translation, translation) > kMaxTranslationSquared) {
+        float ratio = kMaxTranslation / lengthOf(translation);
+        v.x *= ratio; v.y *= ratio;
+      }
+      float rotation = h * wv;
+      if (rotation * rotation > kMaxRotationSquared) {
+        float ratio = kMaxRotation / babs(rotation);
+        wv *= ratio;
+      }
+      addTo(c, h * v);
+      a += h * wv;
+      sb[i].c = c; sb[i].a = a; sb[i].v = v; sb[i].w = wv;
+    }
+    // position iterations (b2_island.cpp:387-428): contacts then joints, early exit per world
+    for (int it = 0; it < pi; ++it) {
+      float minSep = 0.0f;
+      for (int i : corder) minSep = bmin(minSep, solvePositionOne(pcs[i], sb));
+      bool contactsOkay = minSep >= -3.0f * kLinearSlop;
+      bool jointsOkay = true;
+      for (int j : jorder) {
+        bool ok = jointSolvePosition(w->joints[j], sb);
+        jointsOkay = jointsOkay && ok;
+      }
+      if (contactsOkay && jointsOkay) break;
+    }
+    // write back + SynchronizeTransform (b2_island.cpp:430-438, include/box2d/b2_body.h:957-961)
+    for (int i = 0; i < nb; ++i) {
+      Body& b = w->bodies[i];
+      if (b.type == 0) continue;
+      b.c = sb[i].c; b.a = sb[i].a; b.v = sb[i].v; b.w = sb[i].w;
+      b.xf.q = rotOf(b.a);
+      b.xf.p = b.c - mul(b.xf.q, b.localCenter);
+    }
+    // broadphase at the end of Solve (b2_world.cpp:663-669)
+    updatePairs(w);
+    w->inv_dt0 = st.inv_dt;
+    for (Joint& j : w->joints) {
+      float F[2], T;
+      jointReaction(j, st.inv_dt, F, &T);
+      (void)F; (void)T;
+    }
+  }
+  if (w->autoClearForces) {
+    for (Body& b : w->bodies) { b.force = v2(0.0f, 0.0f); b.torque = 0.0f; }
+  }
+}
+
+}  // namespace orc
+
+// ================================================================================================
+// C ABI of the oracle (loaded by tests through ctypes)
+using namespace orc;
+
+extern "C" {
+
+void orc_set_libm_trig(int32_t on) { g_libm_trig = on; }
+
+void orc_sincos(float x, float* s, float* c) { sincos_portable(x, s, c); }
+
+int orc_polygon_set(const float* xy, int32_t n, b2g_shape* out) {
+  V2 v[8];
+  for (int i = 0; i < n && i < 8; ++i) v[i] = v2(xy[2 * i], xy[2 * i + 1]);
+  Shape p;
+  polygonSet(&p, v, n);
+  shapeTo(p, out);
+  return 0;
+}
+
+int orc_polygon_box(float hx, float hy, float cx, float cy, float angle, int32_t oriented, b2g_shape* out) {
+  Shape p;
+  setAsBox(&p, hx, hy, oriented != 0, v2(cx, cy), angle);
+  shapeTo(p, out);
+  return 0;
+}
+
+int orc_shape_mass(const b2g_shape* s, float density, float* out4) {
+  MassData md = computeMass(shapeFrom(*s), density);
+  out4[0] = md.mass; out4[1] = md.center.x; out4[2] = md.center.y; out4[3] = md.I;
+  return 0;
+}
+
+int orc_shape_aabb(const b2g_shape* s, const float* xf, float* out4) {
+  Xf t;
+  t.p = v2(xf[0], xf[1]); t.q.s = xf[2]; t.q.c = xf[3];
+  AABB bb = computeAABB(shapeFrom(*s), t);
+  out4[0] = bb.lo.x; out4[1] = bb.lo.y; out4[2] = bb.hi.x; out4[3] = bb.hi.y;
+  return 0;
+}
+
+int orc_collide(const b2g_shape* sa, const float* xfa, const b2g_shape* sb, const float* xfb, b2g_manifold* out) {
+  Shape A = shapeFrom(*sa), B = shapeFrom(*sb);
+  Xf ta, tb;
+  ta.p = v2(xfa[0], xfa[1]); ta.q.s = xfa[2]; ta.q.c = xfa[3];
+  tb.p = v2(xfb[0], xfb[1]); tb.q.s = xfb[2]; tb.q.c = xfb[3];
+  Manifold m;
+  memset(&m, 0, sizeof(m));
+  if (!hasCollider(A.type, B.type)) return 1;
+  evaluate(&m, A, ta, B, tb);
+  manifoldTo(m, out);
+  return 0;
+}
+
+int orc_world_manifold(const b2g_manifold* mi, const float* xfa, float ra, const float* xfb, float rb, float* out8) {
+  Manifold m = manifoldFrom(*mi);
+  Xf ta, tb;
+  ta.p = v2(xfa[0], xfa[1]); ta.q.s = xfa[2]; ta.q.c = xfa[3];
+  tb.p = v2(xfb[0], xfb[1]); tb.q.s = xfb[2]; tb.q.c = xfb[3];
+  WorldManifold wm;
+  memset(&wm, 0, sizeof(wm));
+  worldManifold(&wm, m, ta, ra, tb, rb);
+  out8[0] = wm.normal.x; out8[1] = wm.normal.y;
+  out8[2] = wm.points[0].x; out8[3] = wm.points[0].y;
+  out8[4] = wm.points[1].x; out8[5] = wm.points[1].y;
+  out8[6] = wm.separations[0]; out8[7] = wm.separations[1];
+  return 0;
+}
+
+// All pairs i < j of n AABBs that overlap (inclusive), sorted, as i << 32 | j.
+int64_t orc_pairs(const float* aabbs, int32_t n, uint64_t* out, int64_t cap) {
+  std::vector<int> order(n);
+  for (int i = 0; i < n; ++i) order[i] = i;
+  auto lo = [&](int i) { return aabbs[4 * i]; };
+  std::sort(order.begin(), order.end(), [&](int a, int b) { return lo(a) != lo(b) ? lo(a) < lo(b) : a < b; });
+  std::vector<uint64_t> pairs;
+  for (int oi = 0; oi < n; ++oi) {
+    int i = order[oi];
+    AABB a = {{aabbs[4 * i], aabbs[4 * i + 1]}, {aabbs[4 * i + 2], aabbs[4 * i + 3]}};
+    for (int oj = oi + 1; oj < n; ++oj) {
+      int j = order[oj];
+      if (aabbs[4 * j] > a.hi.x) break;
+      AABB b = {{aabbs[4 * j], aabbs[4 * j + 1]}, {aabbs[4 * j + 2], aabbs[4 * j + 3]}};
+      if (!overlap(a, b)) continue;
+      uint32_t x = (uint32_t)bmin(i, j), y = (uint32_t)bmax(i, j);
+      pairs.push_back(((uint64_t)x << 32) | y);
+    }
+  }
+  std::sort(pairs.begin(), pairs.end());
+  for (int64_t k = 0; k < (int64_t)pairs.size() && k < cap; ++k) out[k] = pairs[k];
+  return (int64_t)pairs.size();
+}
+
+void* orc_world_new(float gx, float gy) {
+  World* w = new World();
+  w->gravity = v2(gx, gy);
+  return w;
+}
+
+void orc_world_free(void* h) { delete (World*)h; }
+
+// Loads a world from exported records (bodies/fixtures/joints in creation order; contacts with
+// their fixture indices, flags and manifolds). With no contacts given, the first step finds them
+// (like b2World::Step after CreateFixture, b2_world.cpp:1113-1116).
+int orc_world_load(void* h, const b2g_body* bodies, int32_t nb, const b2g_fixture* fixtures, int32_t nf,
+                   const b2g_joint* joints, int32_t nj, const b2g_contact* contacts, int32_t nc, float inv_dt0) {
+  World* w = (World*)h;
+  w->bodies.resize(nb);
+  for (int i = 0; i < nb; ++i) {
+    const b2g_body& s = bodies[i];
+    Body& b = w->bodies[i];
+    b.xf.p = v2(s.xf[0], s.xf[1]); b.xf.q.s = s.xf[2]; b.xf.q.c = s.xf[3];
+    b.c = v2(s.c[0], s.c[1]); b.a = s.a;
+    b.v = v2(s.v[0], s.v[1]); b.w = s.w;
+    b.localCenter = v2(s.local_center[0], s.local_center[1]);
+    b.mass = s.mass; b.invMass = s.inv_mass; b.I = s.inertia; b.invI = s.inv_inertia;
+    b.linearDamping = s.linear_damping; b.angularDamping = s.angular_damping; b.gravityScale = s.gravity_scale;
+    b.force = v2(s.force[0], s.force[1]); b.torque = s.torque;
+    b.type = s.type; b.flags = s.flags;
+  }
+  w->fixtures.resize(nf);
+  for (int i = 0; i < nf; ++i) {
+    const b2g_fixture& s = fixtures[i];
+    Fixture& f = w->fixtures[i];
+    f.shape = shapeFrom(s.shape);
+    f.body = s.body;
+    if (f.body < 0 || f.body >= nb) return 1;
+    f.density = s.density; f.friction = s.friction; f.restitution = s.restitution;
+    f.threshold = s.restitution_threshold;
+    f.category = s.category_bits; f.mask = s.mask_bits; f.group = s.group_index;
+    f.sensor = s.is_sensor != 0;
+  }
+  w->joints.resize(nj);
+  for (int i = 0; i < nj; ++i) {
+    Joint& J = w->joints[i];
+    memset(&J, 0, sizeof(J));
+    J.d = joints[i].def;
+    J.impulse2 = v2(joints[i].impulse[0], joints[i].impulse[1]);
+    J.impulse1 = joints[i].impulse[0];
+    J.motorImpulse = joints[i].motor_impulse;
+    J.lowerImpulse = joints[i].lower_impulse;
+    J.upperImpulse = joints[i].upper_impulse;
+    if (J.d.type == B2G_JOINT_PRISMATIC) {
+      J.localXAxisA = v2(J.d.local_axis_a[0], J.d.local_axis_a[1]);
+      J.localYAxisA = cross(1.0f, J.localXAxisA);
+    }
+    if (J.d.body_a < 0 || J.d.body_a >= nb || J.d.body_b < 0 || J.d.body_b >= nb) return 1;
+  }
+  rebuildNoCollide(w);
+  w->contacts.clear();
+  for (int i = 0; i < nc; ++i) {
+    const b2g_contact& s = contacts[i];
+    int a = s.fixture_a, b = s.fixture_b;
+    bool sa = w->bodies[w->fixtures[a].body].type == 0;
+    bool sbb = w->bodies[w->fixtures[b].body].type == 0;
+    int e, p;
+    if (sa) { e = b; p = a; } else if (sbb) { e = a; p = b; } else { e = bmin(a, b); p = bmax(a, b); }
+    Contact c = makeContact(*w, ((uint64_t)(uint32_t)e << 32) | (uint32_t)p);
+    c.fA = a;  // a loaded contact keeps its orientation: its manifold was computed for it
+    c.fB = b;
+    c.flags = s.flags;
+    c.friction = s.friction; c.restitution = s.restitution; c.threshold = s.restitution_threshold;
+    c.tangentSpeed = s.tangent_speed;
+    c.m = manifoldFrom(s.manifold);
+    w->contacts.push_back(c);
+  }
+  std::sort(w->contacts.begin(), w->contacts.end(), [](const Contact& x, const Contact& y) { return x.key < y.key; });
+  w->newContacts = (nc == 0);
+  w->inv_dt0 = inv_dt0;
+  return 0;
+}
+
+double orc_world_step(void* h, float dt, int32_t vi, int32_t pi, int32_t n) {
+  World* w = (World*)h;
+  auto t0 = std::chrono::steady_clock::now();
+  for (int i = 0; i < n; ++i) stepWorld(w, dt, vi, pi);
+  return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+}
+
+int32_t orc_world_sizes(void* h, int32_t* out4) {
+  World* w = (World*)h;
+  out4[0] = (int32_t)w->bodies.size();
+  out4[1] = (int32_t)w->fixtures.size();
+  out4[2] = (int32_t)w->joints.size();
+  out4[3] = (int32_t)w->contacts.size();
+  return 0;
+}
+
+void orc_world_bodies(void* h, b2g_body* out) {
+  World* w = (World*)h;
+  for (size_t i = 0; i < w->bodies.size(); ++i) {
+    const Body& b = w->bodies[i];
+    b2g_body& s = out[i];
+    memset(&s, 0, sizeof(s));
+    s.xf[0] = b.xf.p.x; s.xf[1] = b.xf.p.y; s.xf[2] = b.xf.q.s; s.xf[3] = b.xf.q.c;
+    s.c[0] = b.c.x; s.c[1] = b.c.y; s.a = b.a;
+    s.v[0] = b.v.x; s.v[1] = b.v.y; s.w = b.w;
+    s.local_center[0] = b.localCenter.x; s.local_center[1] = b.localCenter.y;
+    s.mass = b.mass; s.inv_mass = b.invMass; s.inertia = b.I; s.inv_inertia = b.invI;
+    s.linear_damping = b.linearDamping; s.angular_damping = b.angularDamping; s.gravity_scale = b.gravityScale;
+    s.force[0] = b.force.x; s.force[1] = b.force.y; s.torque = b.torque;
+    s.type = b.type; s.flags = b.flags;
+  }
+}
+
+void orc_world_joints(void* h, b2g_joint* out) {
+  World* w = (World*)h;
+  for (size_t i = 0; i < w->joints.size(); ++i) {
+    const Joint& J = w->joints[i];
+    b2g_joint& s = out[i];
+    memset(&s, 0, sizeof(s));
+    s.def = J.d;
+    if (J.d.type == B2G_JOINT_DISTANCE) s.impulse[0] = J.impulse1;
+    else { s.impulse[0] = J.impulse2.x; s.impulse[1] = J.impulse2.y; }
+    s.motor_impulse = J.motorImpulse; s.lower_impulse = J.lowerImpulse; s.upper_impulse = J.upperImpulse;
+    float F[2], T;
+    jointReaction(J, w->inv_dt0, F, &T);
+    s.reaction_force[0] = F[0]; s.reaction_force[1] = F[1]; s.reaction_torque = T;
+  }
+}
+
+int32_t orc_world_contacts(void* h, b2g_contact* out, int32_t cap) {
+  World* w = (World*)h;
+  int32_t n = (int32_t)w->contacts.size();
+  for (int32_t i = 0; i < n && i < cap; ++i) {
+    const Contact& c = w->contacts[i];
+    b2g_contact& s = out[i];
+    memset(&s, 0, sizeof(s));
+    s.fixture_a = c.fA; s.fixture_b = c.fB; s.flags = c.flags;
+    s.friction = c.friction; s.restitution = c.restitution; s.restitution_threshold = c.threshold;
+    s.tangent_speed = c.tangentSpeed;
+    manifoldTo(c.m, &s.manifold);
+  }
+  return n;
+}
+
+int orc_world_solver_order(void* h, int32_t* ccol, uint32_t* cprio, int32_t nc, int32_t* jcol, uint32_t* jprio,
+                           int32_t nj) {
+  World* w = (World*)h;
+  for (int i = 0; i < nc && i < (int)w->contactColor.size(); ++i) { ccol[i] = w->contactColor[i]; cprio[i] = w->contactPrio[i]; }
+  for (int j = 0; j < nj && j < (int)w->jointColor.size(); ++j) { jcol[j] = w->jointColor[j]; jprio[j] = w->jointPrioV[j]; }
+  return 0;
+}
+
+// The Gauss-Seidel order of the last step: (fixture A, fixture B) per solved contact and joint
+// indices, both in solve order. Returns the number of solved contacts.
+int32_t orc_world_last_order(void* h, int32_t* pairs, int32_t cap_pairs, int32_t* joints, int32_t cap_joints,
+                             int32_t* n_joints) {
+  World* w = (World*)h;
+  int32_t nc = (int32_t)(w->lastContactOrder.size() / 2);
+  for (int32_t i = 0; i < 2 * nc && i < 2 * cap_pairs; ++i) pairs[i] = w->lastContactOrder[i];
+  int32_t nj = (int32_t)w->lastJointOrder.size();
+  for (int32_t j = 0; j < nj && j < cap_joints; ++j) joints[j] = w->lastJointOrder[j];
+  if (n_joints) *n_joints = nj;
+  return nc;
+}
+
+// Steps n worlds on `threads` host threads (disjoint subsets); returns wall seconds.
+double orc_worlds_step_parallel(void** hs, int32_t n, float dt, int32_t vi, int32_t pi, int32_t nsteps,
+                                int32_t threads) {
+  auto t0 = std::chrono::steady_clock::now();
+  std::vector<std::thread> th;
+  for (int t = 0; t < threads; ++t) {
+    th.emplace_back([=]() {
+      for (int i = t; i < n; i += threads)
+        for (int s = 0; s < nsteps; ++s) stepWorld((World*)hs[i], dt, vi, pi);
+    });
+  }
+  for (auto& x : th) x.join();
+  return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+}
+
+}  // extern "C"

@@ -1,0 +1,210 @@
+"""ctypes bindings of the oracle libraries (test infrastructure only).
+
+* ``Ref``    - oracle/_ref/libb2ref.so: the reference engine compiled from its own sources plus
+               oracle/ref_shim.cpp. It exists only where the reference sources are checked out.
+* ``Oracle`` - oracle/_build/libb2oracle.so: the CPU restatement of the Step path that the GPU
+               engine is checked against everywhere (it is built from the repository alone).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import sys
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parents[1]
+sys.path.insert(0, str(ROOT / "box2d-optimized_gb300"))
+import b2gpu as G  # noqa: E402
+
+REF_PATH = ROOT / "oracle" / "_ref" / "libb2ref.so"
+ORACLE_PATH = ROOT / "oracle" / "_build" / "libb2oracle.so"
+
+P = C.POINTER
+vp, i32, u32, f32 = C.c_void_p, C.c_int32, C.c_uint32, C.c_float
+
+
+class Ref:
+    def __init__(self, path=REF_PATH):
+        self.lib = L = C.CDLL(str(path))
+        sig = {
+            "ref_polygon_set": ([P(f32), i32, P(G.Shape)], C.c_int),
+            "ref_polygon_box": ([f32, f32, f32, f32, f32, i32, P(G.Shape)], C.c_int),
+            "ref_shape_mass": ([P(G.Shape), f32, P(f32)], C.c_int),
+            "ref_shape_aabb": ([P(G.Shape), P(f32), P(f32)], C.c_int),
+            "ref_collide": ([P(G.Shape), P(f32), P(G.Shape), P(f32), P(G.Manifold)], C.c_int),
+            "ref_world_manifold": ([P(G.Manifold), P(f32), f32, P(f32), f32, P(f32)], C.c_int),
+            "ref_scene_world": ([i32, u32, i32, f32, f32, f32, f32, P(i32)], vp),
+            "ref_world_free": ([vp], None),
+            "ref_world_set_flags": ([vp, i32, i32, i32], None),
+            "ref_world_step": ([vp, f32, i32, i32, i32], C.c_double),
+            "ref_world_sizes": ([vp, P(i32)], i32),
+            "ref_world_bodies": ([vp, P(G.Body)], None),
+            "ref_world_fixtures": ([vp, P(G.Fixture)], None),
+            "ref_world_joints": ([vp, P(G.Joint)], None),
+            "ref_world_contacts": ([vp, P(G.Contact), i32], i32),
+            "ref_world_set_bodies": ([vp, P(G.Body)], None),
+            "ref_replay_step": ([vp, f32, i32, i32, P(i32), i32, P(i32), i32], C.c_int),
+            "ref_worlds_step_parallel": ([P(vp), i32, f32, i32, i32, i32, i32], C.c_double),
+        }
+        for name, (a, r) in sig.items():
+            fn = getattr(L, name)
+            fn.argtypes = a
+            fn.restype = r
+
+    def __getattr__(self, name):
+        return getattr(self.lib, name)
+
+
+class RefWorld:
+    """A reference b2World built by one of the shared scene recipes."""
+
+    def __init__(self, ref: Ref, kind, seed=1, n=20, p0=1.0, p1=0.6, gravity=(0.0, -10.0),
+                 allow_sleep=False, warm=True, continuous=False):
+        self.ref = ref
+        counts = (i32 * 3)()
+        self.h = ref.ref_scene_world(kind, seed, n, p0, p1, gravity[0], gravity[1], counts)
+        self.counts = tuple(counts)
+        ref.ref_world_set_flags(self.h, int(allow_sleep), int(warm), int(continuous))
+
+    def close(self):
+        if self.h:
+            self.ref.ref_world_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def sizes(self):
+        s = (i32 * 4)()
+        self.ref.ref_world_sizes(self.h, s)
+        return tuple(s)
+
+    def step(self, n=1, dt=1 / 60, vi=8, pi=3):
+        return self.ref.ref_world_step(self.h, dt, vi, pi, n)
+
+    def bodies(self):
+        nb = self.sizes()[0]
+        arr = (G.Body * nb)()
+        self.ref.ref_world_bodies(self.h, arr)
+        return arr
+
+    def fixtures(self):
+        nf = self.sizes()[1]
+        arr = (G.Fixture * nf)()
+        self.ref.ref_world_fixtures(self.h, arr)
+        return arr
+
+    def joints(self):
+        nj = self.sizes()[2]
+        arr = (G.Joint * max(nj, 1))()
+        self.ref.ref_world_joints(self.h, arr)
+        return arr[:nj]
+
+    def contacts(self):
+        n = self.ref.ref_world_contacts(self.h, None, 0)
+        arr = (G.Contact * max(n, 1))()
+        self.ref.ref_world_contacts(self.h, arr, n)
+        return arr[:n]
+
+
+class Oracle:
+    def __init__(self, path=ORACLE_PATH):
+        self.lib = L = C.CDLL(str(path))
+        sig = {
+            "orc_polygon_set": ([P(f32), i32, P(G.Shape)], C.c_int),
+            "orc_polygon_box": ([f32, f32, f32, f32, f32, i32, P(G.Shape)], C.c_int),
+            "orc_shape_mass": ([P(G.Shape), f32, P(f32)], C.c_int),
+            "orc_shape_aabb": ([P(G.Shape), P(f32), P(f32)], C.c_int),
+            "orc_collide": ([P(G.Shape), P(f32), P(G.Shape), P(f32), P(G.Manifold)], C.c_int),
+            "orc_world_manifold": ([P(G.Manifold), P(f32), f32, P(f32), f32, P(f32)], C.c_int),
+            "orc_sincos": ([f32, P(f32), P(f32)], None),
+            "orc_world_new": ([f32, f32], vp),
+            "orc_world_free": ([vp], None),
+            "orc_world_load": ([vp, P(G.Body), i32, P(G.Fixture), i32, P(G.Joint), i32,
+                                P(G.Contact), i32, f32], C.c_int),
+            "orc_world_step": ([vp, f32, i32, i32, i32], C.c_double),
+            "orc_world_sizes": ([vp, P(i32)], i32),
+            "orc_world_bodies": ([vp, P(G.Body)], None),
+            "orc_world_joints": ([vp, P(G.Joint)], None),
+            "orc_world_contacts": ([vp, P(G.Contact), i32], i32),
+            "orc_world_solver_order": ([vp, P(i32), P(u32), i32, P(i32), P(u32), i32], C.c_int),
+            "orc_world_last_order": ([vp, P(i32), i32, P(i32), i32, P(i32)], i32),
+            "orc_set_libm_trig": ([i32], None),
+            "orc_pairs": ([P(f32), i32, P(C.c_uint64), C.c_int64], C.c_int64),
+            "orc_worlds_step_parallel": ([P(vp), i32, f32, i32, i32, i32, i32], C.c_double),
+        }
+        for name, (a, r) in sig.items():
+            fn = getattr(L, name)
+            fn.argtypes = a
+            fn.restype = r
+
+    def __getattr__(self, name):
+        return getattr(self.lib, name)
+
+
+class OracleWorld:
+    """A world of the CPU restatement loaded from exported records."""
+
+    def __init__(self, orc: Oracle, gravity, bodies, fixtures, joints=(), contacts=(),
+                 inv_dt0=0.0):
+        self.orc = orc
+        self.h = orc.orc_world_new(gravity[0], gravity[1])
+        nb, nf, nj, nc = len(bodies), len(fixtures), len(joints), len(contacts)
+        B = (G.Body * max(nb, 1))(*bodies)
+        F = (G.Fixture * max(nf, 1))(*fixtures)
+        J = (G.Joint * max(nj, 1))(*joints)
+        Cc = (G.Contact * max(nc, 1))(*contacts)
+        st = orc.orc_world_load(self.h, B, nb, F, nf, J, nj, Cc, nc, inv_dt0)
+        if st != 0:
+            raise RuntimeError(f"orc_world_load failed: {st}")
+
+    def close(self):
+        if self.h:
+            self.orc.orc_world_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def sizes(self):
+        s = (i32 * 4)()
+        self.orc.orc_world_sizes(self.h, s)
+        return tuple(s)
+
+    def step(self, n=1, dt=1 / 60, vi=8, pi=3, new_contacts=False):
+        return self.orc.orc_world_step(self.h, dt, vi, pi, n)
+
+    def bodies(self):
+        nb = self.sizes()[0]
+        arr = (G.Body * max(nb, 1))()
+        self.orc.orc_world_bodies(self.h, arr)
+        return arr[:nb]
+
+    def joints(self):
+        nj = self.sizes()[2]
+        arr = (G.Joint * max(nj, 1))()
+        self.orc.orc_world_joints(self.h, arr)
+        return arr[:nj]
+
+    def contacts(self):
+        n = self.orc.orc_world_contacts(self.h, None, 0)
+        arr = (G.Contact * max(n, 1))()
+        self.orc.orc_world_contacts(self.h, arr, n)
+        return arr[:n]
+
+    def last_order(self):
+        nj = C.c_int32()
+        nc = self.orc.orc_world_last_order(self.h, None, 0, None, 0, C.byref(nj))
+        pairs = (i32 * max(2 * nc, 1))()
+        joints = (i32 * max(nj.value, 1))()
+        self.orc.orc_world_last_order(self.h, pairs, nc, joints, nj.value, C.byref(nj))
+        return list(pairs[:2 * nc]), list(joints[:nj.value])
+
+    def solver_order(self):
+        nc = self.sizes()[3]
+        nj = self.sizes()[2]
+        cc = (i32 * max(nc, 1))()
+        cp = (u32 * max(nc, 1))()
+        jc = (i32 * max(nj, 1))()
+        jp = (u32 * max(nj, 1))()
+        self.orc.orc_world_solver_order(self.h, cc, cp, nc, jc, jp, nj)
+        return list(cc[:nc]), list(cp[:nc]), list(jc[:nj]), list(jp[:nj])
