@@ -97,7 +97,7 @@ class Fixture(C.Structure):
 class Joint(C.Structure):
     _fields_ = [("def_", JointDef), ("impulse", C.c_float * 3), ("motor_impulse", C.c_float),
                 ("lower_impulse", C.c_float), ("upper_impulse", C.c_float),
-                ("reaction_force", F2), ("reaction_torque", C.c_float)]
+                ("reaction_impulse", F2), ("reaction_angular_impulse", C.c_float)]
 
 
 class Contact(C.Structure):

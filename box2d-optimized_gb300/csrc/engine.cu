@@ -1,0 +1,946 @@
+// engine.cu - host orchestration of the batched Step and the C ABI (include/b2g_capi.h).
+//
+// The host keeps the structure of every world (bodies, fixtures, joints, mass data) in
+// HostWorld records; the device holds the live dynamic state in packed world-major arrays
+// (engine.h). A structural change (new world, body, fixture, joint) downloads the live state,
+// edits the host records, and re-uploads the whole layout before the next step; steps
+// themselves never touch the host copy.
+#include <math.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <algorithm>
+#include <chrono>
+#include <mutex>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "b2g_math.cuh"
+#include "engine.h"
+#include "kernels.h"
+
+namespace b2g {
+
+static thread_local std::string g_last_error;
+
+void set_error(Batch* b, const std::string& msg) {
+  g_last_error = msg;
+  if (b) b->error = msg;
+}
+
+#define CUDA_TRY(b, call)                                                                       \
+  do {                                                                                          \
+    cudaError_t e_ = (call);                                                                    \
+    if (e_ != cudaSuccess) {                                                                    \
+      set_error(b, std::string(#call) + ": " + cudaGetErrorString(e_));                         \
+      return B2G_E_CUDA;                                                                        \
+    }                                                                                           \
+  } while (0)
+
+template <typename T>
+static int ensure(Batch* b, DBuf<T>& buf, size_t n, bool keep = false) {
+  if (n == 0) n = 1;
+  if (buf.cap >= n) return B2G_OK;
+  size_t cap = n + n / 4 + 16;
+  size_t bytes = cap * sizeof(T);
+  if (b->budget && b->allocated - buf.cap * sizeof(T) + bytes > b->budget) {
+    set_error(b, "device memory budget exceeded");
+    return B2G_E_OUT_OF_MEMORY;
+  }
+  T* p = nullptr;
+  cudaError_t e = cudaMalloc(&p, bytes);
+  if (e != cudaSuccess) {
+    set_error(b, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    return e == cudaErrorMemoryAllocation ? B2G_E_OUT_OF_MEMORY : B2G_E_CUDA;
+  }
+  if (keep && buf.p && buf.cap) cudaMemcpyAsync(p, buf.p, buf.cap * sizeof(T), cudaMemcpyDeviceToDevice, b->stream);
+  if (buf.p) {
+    cudaStreamSynchronize(b->stream);
+    cudaFree(buf.p);
+    b->allocated -= buf.cap * sizeof(T);
+  }
+  buf.p = p;
+  buf.cap = cap;
+  b->allocated += bytes;
+  return B2G_OK;
+}
+
+template <typename T>
+static void release(Batch* b, DBuf<T>& buf) {
+  if (buf.p) {
+    cudaFree(buf.p);
+    b->allocated -= buf.cap * sizeof(T);
+  }
+  buf.p = nullptr;
+  buf.cap = 0;
+}
+
+#define TRY(x)            \
+  do {                    \
+    int s_ = (x);         \
+    if (s_ != B2G_OK) return s_; \
+  } while (0)
+
+template <typename T>
+static int upload(Batch* b, DBuf<T>& buf, const std::vector<T>& v) {
+  TRY(ensure(b, buf, v.size()));
+  if (!v.empty()) CUDA_TRY(b, cudaMemcpyAsync(buf.p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, b->stream));
+  return B2G_OK;
+}
+
+static KernelArgs make_args(Batch* b) {
+  KernelArgs a;
+  memset(&a, 0, sizeof(a));
+  a.wb = b->wb.p; a.wj = b->wj.p; a.wg = b->wg.p; a.wflags = b->wflags.p; a.wc = b->wc.p;
+  a.world_order = b->world_order.p;
+  a.xf = b->xf.p; a.pos = b->pos.p; a.vel = b->vel.p; a.massd = b->massd.p; a.damp = b->damp.p;
+  a.force = b->force.p; a.lc = b->lc.p; a.btype = b->btype.p; a.bworld = b->bworld.p;
+  a.shape = b->shape.p; a.fbody = b->fbody.p; a.fgroup = b->fgroup.p; a.fsensor = b->fsensor.p;
+  a.fworld = b->fworld.p; a.ffilter = b->ffilter.p; a.fmat = b->fmat.p; a.aabb = b->aabb.p;
+  a.joints = b->joints.p; a.nocollide = b->nocollide.p; a.n_nocollide = b->n_nocollide;
+  int c = b->cur;
+  a.ckey = b->ckey[c].p; a.cfix = b->cfix[c].p; a.cflags = b->cflags[c].p; a.cmat = b->cmat[c].p;
+  a.cman = b->cman[c].p;
+  for (int k = 0; k < 2; ++k) {
+    a.ckeyB[k] = b->ckey[k].p; a.cfixB[k] = b->cfix[k].p; a.cflagsB[k] = b->cflags[k].p;
+    a.cmatB[k] = b->cmat[k].p; a.cmanB[k] = b->cman[k].p;
+  }
+  a.wbounds = b->wbounds.p; a.mkey = b->mkey.p; a.mkey_sorted = b->mkey_sorted.p; a.mval = b->mval.p;
+  a.mval_sorted = b->mval_sorted.p; a.nchild = b->nchild.p; a.nparent = b->nparent.p; a.lparent = b->lparent.p;
+  a.naabb = b->naabb.p; a.nflag = b->nflag.p; a.wroot = b->wroot.p; a.pcount = b->pcount.p; a.poff = b->poff.p;
+  a.pairs = b->pairs.p; a.cub_tmp = b->cub_tmp.p;
+  a.sc_list = b->sc_list.p; a.vc = b->vc.p; a.ccolor = b->ccolor.p; a.corder = b->corder.p; a.cprio = b->cprio.p;
+  a.cready = b->cready.p; a.inc_cnt = b->inc_cnt.p; a.inc_off = b->inc_off.p; a.inc_head = b->inc_head.p;
+  a.inc_mask = b->inc_mask.p; a.inc_list = b->inc_list.p; a.jinc_list = b->jinc_list.p; a.jcolor = b->jcolor.p;
+  a.jorder = b->jorder.p; a.jprio = b->jprio.p; a.jready = b->jready.p; a.ncolors = b->ncolors.p;
+  a.events = b->events.p; a.event_cap = b->event_cap; a.events_on = b->events_on ? 1 : 0;
+  a.counters = b->counters.p; a.status = b->status.p;
+  return a;
+}
+
+// ------------------------------------------------------------------------------ layout upload
+static uint64_t emitter_key(const HostWorld& w, int fo, int fa, int fb) {
+  bool sa = w.bodies[w.fixtures[fa].body].type == B2G_STATIC;
+  bool sb = w.bodies[w.fixtures[fb].body].type == B2G_STATIC;
+  int e, p;
+  if (sa) { e = fb; p = fa; }
+  else if (sb) { e = fa; p = fb; }
+  else { e = std::min(fa, fb); p = std::max(fa, fb); }
+  return ((uint64_t)(uint32_t)(e + fo) << 32) | (uint32_t)(p + fo);
+}
+
+int upload_all(Batch* b) {
+  CUDA_TRY(b, cudaSetDevice(b->device));
+  int NW = (int)b->worlds.size();
+  std::vector<int4> wb(NW), wj(NW);
+  std::vector<float4> wg(NW);
+  std::vector<int> wflags(NW);
+  b->h_body_off.assign(NW + 1, 0);
+  b->h_fix_off.assign(NW + 1, 0);
+  b->h_joint_off.assign(NW + 1, 0);
+  int NB = 0, NF = 0, NJ = 0;
+  int64_t NC = 0;
+  for (int w = 0; w < NW; ++w) {
+    const HostWorld& hw = b->worlds[w];
+    b->h_body_off[w] = NB; b->h_fix_off[w] = NF; b->h_joint_off[w] = NJ;
+    wb[w] = make_int4(NB, (int)hw.bodies.size(), NF, (int)hw.fixtures.size());
+    wj[w] = make_int4(NJ, (int)hw.joints.size(), 0, 0);
+    wg[w] = make_float4(hw.gx, hw.gy, hw.inv_dt0, 0.0f);
+    wflags[w] = hw.flags;
+    NB += (int)hw.bodies.size();
+    NF += (int)hw.fixtures.size();
+    NJ += (int)hw.joints.size();
+    NC += (int64_t)hw.contacts.size();
+  }
+  b->h_body_off[NW] = NB; b->h_fix_off[NW] = NF; b->h_joint_off[NW] = NJ;
+  std::vector<float4> xf(NB), pos(NB), vel(NB), massd(NB), damp(NB), force(NB);
+  std::vector<float2> lc(NB);
+  std::vector<int> btype(NB), bworld(NB);
+  std::vector<b2g_shape> shape(NF);
+  std::vector<int> fbody(NF), fgroup(NF), fsensor(NF), fworld(NF);
+  std::vector<uint32_t> ffilter(NF);
+  std::vector<float4> fmat(NF);
+  std::vector<JointDev> joints(NJ);
+  std::vector<uint64_t> nocol;
+  std::vector<std::pair<uint64_t, size_t>> ckeys;
+  std::vector<b2g_contact> call;
+  ckeys.reserve(NC);
+  call.reserve(NC);
+  for (int w = 0; w < NW; ++w) {
+    const HostWorld& hw = b->worlds[w];
+    int bo = b->h_body_off[w], fo = b->h_fix_off[w], jo = b->h_joint_off[w];
+    for (size_t i = 0; i < hw.bodies.size(); ++i) {
+      const b2g_body& s = hw.bodies[i];
+      size_t k = bo + i;
+      xf[k] = make_float4(s.xf[0], s.xf[1], s.xf[2], s.xf[3]);
+      pos[k] = make_float4(s.c[0], s.c[1], s.a, 0.0f);
+      vel[k] = make_float4(s.v[0], s.v[1], s.w, 0.0f);
+      massd[k] = make_float4(s.mass, s.inv_mass, s.inertia, s.inv_inertia);
+      damp[k] = make_float4(s.linear_damping, s.angular_damping, s.gravity_scale, 0.0f);
+      force[k] = make_float4(s.force[0], s.force[1], s.torque, 0.0f);
+      lc[k] = make_float2(s.local_center[0], s.local_center[1]);
+      btype[k] = s.type;
+      bworld[k] = w;
+    }
+    for (size_t i = 0; i < hw.fixtures.size(); ++i) {
+      const b2g_fixture& f = hw.fixtures[i];
+      size_t k = fo + i;
+      shape[k] = f.shape;
+      fbody[k] = bo + f.body;
+      fgroup[k] = f.group_index;
+      fsensor[k] = f.is_sensor ? 1 : 0;
+      fworld[k] = w;
+      ffilter[k] = (uint32_t)f.category_bits | ((uint32_t)f.mask_bits << 16);
+      fmat[k] = make_float4(f.friction, f.restitution, f.restitution_threshold, f.density);
+    }
+    for (size_t i = 0; i < hw.joints.size(); ++i) {
+      const b2g_joint& j = hw.joints[i];
+      JointDev& d = joints[jo + i];
+      memset(&d, 0, sizeof(d));
+      d.d = j.def;
+      d.d.body_a += bo;
+      d.d.body_b += bo;
+      d.impulse[0] = j.impulse[0]; d.impulse[1] = j.impulse[1]; d.impulse[2] = j.impulse[2];
+      d.motorImpulse = j.motor_impulse; d.lowerImpulse = j.lower_impulse; d.upperImpulse = j.upper_impulse;
+      if (j.def.type == B2G_JOINT_PRISMATIC) {
+        V2 ax = mk(j.def.local_axis_a[0], j.def.local_axis_a[1]);
+        V2 ay = cross(1.0f, ax);
+        d.localXAxisA[0] = ax.x; d.localXAxisA[1] = ax.y;
+        d.localYAxisA[0] = ay.x; d.localYAxisA[1] = ay.y;
+      }
+      if (!j.def.collide_connected) {
+        uint32_t x = (uint32_t)(bo + j.def.body_a), y = (uint32_t)(bo + j.def.body_b);
+        if (x > y) std::swap(x, y);
+        nocol.push_back(((uint64_t)x << 32) | y);
+      }
+    }
+    for (const b2g_contact& c : hw.contacts) {
+      ckeys.push_back({emitter_key(hw, fo, c.fixture_a, c.fixture_b), call.size()});
+      b2g_contact g = c;
+      g.fixture_a += fo;
+      g.fixture_b += fo;
+      call.push_back(g);
+    }
+  }
+  std::sort(nocol.begin(), nocol.end());
+  nocol.erase(std::unique(nocol.begin(), nocol.end()), nocol.end());
+  std::sort(ckeys.begin(), ckeys.end());
+  std::vector<uint64_t> ckey(NC);
+  std::vector<int2> cfix(NC);
+  std::vector<uint32_t> cflags(NC);
+  std::vector<float4> cmat(NC);
+  std::vector<b2g_manifold> cman(NC);
+  for (int64_t i = 0; i < NC; ++i) {
+    const b2g_contact& c = call[ckeys[i].second];
+    ckey[i] = ckeys[i].first;
+    cfix[i] = make_int2(c.fixture_a, c.fixture_b);
+    cflags[i] = c.flags;
+    cmat[i] = make_float4(c.friction, c.restitution, c.restitution_threshold, c.tangent_speed);
+    cman[i] = c.manifold;
+  }
+  // worlds in decreasing order of work so the largest start first
+  std::vector<int> order(NW);
+  std::iota(order.begin(), order.end(), 0);
+  std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
+    return b->worlds[x].bodies.size() + b->worlds[x].joints.size() > b->worlds[y].bodies.size() + b->worlds[y].joints.size();
+  });
+  TRY(upload(b, b->wb, wb)); TRY(upload(b, b->wj, wj)); TRY(upload(b, b->wg, wg)); TRY(upload(b, b->wflags, wflags));
+  TRY(upload(b, b->world_order, order));
+  TRY(ensure(b, b->wc, NW)); TRY(ensure(b, b->wbounds, NW)); TRY(ensure(b, b->wroot, NW));
+  TRY(ensure(b, b->ncolors, 2 * (size_t)NW));
+  TRY(upload(b, b->xf, xf)); TRY(upload(b, b->pos, pos)); TRY(upload(b, b->vel, vel)); TRY(upload(b, b->massd, massd));
+  TRY(upload(b, b->damp, damp)); TRY(upload(b, b->force, force)); TRY(upload(b, b->lc, lc));
+  TRY(upload(b, b->btype, btype)); TRY(upload(b, b->bworld, bworld));
+  TRY(upload(b, b->shape, shape)); TRY(upload(b, b->fbody, fbody)); TRY(upload(b, b->fgroup, fgroup));
+  TRY(upload(b, b->fsensor, fsensor)); TRY(upload(b, b->fworld, fworld)); TRY(upload(b, b->ffilter, ffilter));
+  TRY(upload(b, b->fmat, fmat)); TRY(ensure(b, b->aabb, NF));
+  TRY(upload(b, b->joints, joints)); TRY(upload(b, b->nocollide, nocol));
+  b->n_nocollide = (int)nocol.size();
+  b->cur = 0;
+  TRY(upload(b, b->ckey[0], ckey)); TRY(upload(b, b->cfix[0], cfix)); TRY(upload(b, b->cflags[0], cflags));
+  TRY(upload(b, b->cmat[0], cmat)); TRY(upload(b, b->cman[0], cman));
+  // per-body and per-fixture scratch
+  TRY(ensure(b, b->mkey, NF)); TRY(ensure(b, b->mkey_sorted, NF)); TRY(ensure(b, b->mval, NF));
+  TRY(ensure(b, b->mval_sorted, NF)); TRY(ensure(b, b->nchild, NF)); TRY(ensure(b, b->nparent, NF));
+  TRY(ensure(b, b->lparent, NF)); TRY(ensure(b, b->naabb, NF)); TRY(ensure(b, b->nflag, NF));
+  TRY(ensure(b, b->pcount, (size_t)NF + 1));
+  TRY(ensure(b, b->poff, (size_t)NF + 1));
+  TRY(ensure(b, b->cub_tmp, cub_temp_bytes(NF)));
+  TRY(ensure(b, b->inc_cnt, NB)); TRY(ensure(b, b->inc_off, NB)); TRY(ensure(b, b->inc_head, NB));
+  TRY(ensure(b, b->inc_mask, NB));
+  TRY(ensure(b, b->jinc_list, 2 * (size_t)NJ)); TRY(ensure(b, b->jcolor, NJ)); TRY(ensure(b, b->jorder, NJ));
+  TRY(ensure(b, b->jprio, NJ)); TRY(ensure(b, b->jready, NJ));
+  TRY(ensure(b, b->status, 1)); TRY(ensure(b, b->counters, 4));
+  b->NW = NW; b->NB = NB; b->NF = NF; b->NJ = NJ; b->NC = NC;
+  b->structure_dirty = false;
+  b->device_state_valid = true;
+  b->host_state_stale = false;
+  CUDA_TRY(b, cudaStreamSynchronize(b->stream));
+  return B2G_OK;
+}
+
+// Copies the live device state (bodies, joints, contacts, inv_dt0) into the host records.
+int download_state(Batch* b) {
+  if (b->device < 0 || !b->device_state_valid || !b->host_state_stale) return B2G_OK;
+  CUDA_TRY(b, cudaSetDevice(b->device));
+  int NB = b->NB, NJ = b->NJ, NW = b->NW;
+  int64_t NC = b->NC;
+  std::vector<float4> xf(NB), pos(NB), vel(NB), force(NB), wg(NW);
+  std::vector<JointDev> joints(NJ);
+  std::vector<uint64_t> ckey(NC);
+  std::vector<int2> cfix(NC);
+  std::vector<uint32_t> cflags(NC);
+  std::vector<float4> cmat(NC);
+  std::vector<b2g_manifold> cman(NC);
+  cudaStream_t s = b->stream;
+  int c = b->cur;
+  if (NB) {
+    CUDA_TRY(b, cudaMemcpyAsync(xf.data(), b->xf.p, NB * sizeof(float4), cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(b, cudaMemcpyAsync(pos.data(), b->pos.p, NB * sizeof(float4), cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(b, cudaMemcpyAsync(vel.data(), b->vel.p, NB * sizeof(float4), cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(b, cudaMemcpyAsync(force.data(), b->force.p, NB * sizeof(float4), cudaMemcpyDeviceToHost, s));
+  }
+  if (NW) CUDA_TRY(b, cudaMemcpyAsync(wg.data(), b->wg.p, NW * sizeof(float4), cudaMemcpyDeviceToHost, s));
+  if (NJ) CUDA_TRY(b, cudaMemcpyAsync(joints.data(), b->joints.p, NJ * sizeof(JointDev), cudaMemcpyDeviceToHost, s));
+  if (NC) {
+    CUDA_TRY(b, cudaMemcpyAsync(ckey.data(), b->ckey[c].p, NC * sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(b, cudaMemcpyAsync(cfix.data(), b->cfix[c].p, NC * sizeof(int2), cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(b, cudaMemcpyAsync(cflags.data(), b->cflags[c].p, NC * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(b, cudaMemcpyAsync(cmat.data(), b->cmat[c].p, NC * sizeof(float4), cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(b, cudaMemcpyAsync(cman.data(), b->cman[c].p, NC * sizeof(b2g_manifold), cudaMemcpyDeviceToHost, s));
+  }
+  CUDA_TRY(b, cudaStreamSynchronize(s));
+  for (int w = 0; w < NW; ++w) {
+    HostWorld& hw = b->worlds[w];
+    int bo = b->h_body_off[w], fo = b->h_fix_off[w], jo = b->h_joint_off[w];
+    int nbw = std::min((int)hw.bodies.size(), b->h_body_off[w + 1] - bo);
+    for (int i = 0; i < nbw; ++i) {
+      b2g_body& r = hw.bodies[i];
+      int k = bo + i;
+      r.xf[0] = xf[k].x; r.xf[1] = xf[k].y; r.xf[2] = xf[k].z; r.xf[3] = xf[k].w;
+      r.c[0] = pos[k].x; r.c[1] = pos[k].y; r.a = pos[k].z;
+      r.v[0] = vel[k].x; r.v[1] = vel[k].y; r.w = vel[k].z;
+      r.force[0] = force[k].x; r.force[1] = force[k].y; r.torque = force[k].z;
+    }
+    hw.inv_dt0 = wg[w].z;
+    int njw = std::min((int)hw.joints.size(), b->h_joint_off[w + 1] - jo);
+    for (int i = 0; i < njw; ++i) {
+      const JointDev& d = joints[jo + i];
+      b2g_joint& r = hw.joints[i];
+      r.impulse[0] = d.impulse[0]; r.impulse[1] = d.impulse[1]; r.impulse[2] = d.impulse[2];
+      r.motor_impulse = d.motorImpulse; r.lower_impulse = d.lowerImpulse; r.upper_impulse = d.upperImpulse;
+      // reaction impulses (GetReactionForce / GetReactionTorque without the inv_dt factor)
+      if (r.def.type == B2G_JOINT_REVOLUTE) {
+        r.reaction_impulse[0] = d.impulse[0];
+        r.reaction_impulse[1] = d.impulse[1];
+        r.reaction_angular_impulse = (d.motorImpulse + d.lowerImpulse) - d.upperImpulse;
+      } else if (r.def.type == B2G_JOINT_PRISMATIC) {
+        V2 perp = mk(d.perp[0], d.perp[1]), axis = mk(d.axis[0], d.axis[1]);
+        V2 f = d.impulse[0] * perp + ((d.motorImpulse + d.lowerImpulse) - d.upperImpulse) * axis;
+        r.reaction_impulse[0] = f.x; r.reaction_impulse[1] = f.y;
+        r.reaction_angular_impulse = d.impulse[1];
+      } else {
+        V2 u = mk(d.u[0], d.u[1]);
+        V2 f = ((d.impulse[0] + d.lowerImpulse) - d.upperImpulse) * u;
+        r.reaction_impulse[0] = f.x; r.reaction_impulse[1] = f.y;
+        r.reaction_angular_impulse = 0.0f;
+      }
+    }
+    hw.contacts.clear();
+  }
+  for (int64_t i = 0; i < NC; ++i) {
+    int ga = cfix[i].x, gb = cfix[i].y;
+    int w = (int)(std::upper_bound(b->h_fix_off.begin(), b->h_fix_off.end() - 1, ga) - b->h_fix_off.begin()) - 1;
+    int fo = b->h_fix_off[w];
+    b2g_contact r;
+    memset(&r, 0, sizeof(r));
+    r.fixture_a = ga - fo;
+    r.fixture_b = gb - fo;
+    r.flags = cflags[i];
+    r.friction = cmat[i].x; r.restitution = cmat[i].y; r.restitution_threshold = cmat[i].z; r.tangent_speed = cmat[i].w;
+    r.manifold = cman[i];
+    b->worlds[w].contacts.push_back(r);
+  }
+  b->host_state_stale = false;
+  return B2G_OK;
+}
+
+// Solver scratch sized for the live contact count.
+static int ensure_solver(Batch* b) {
+  size_t nc = (size_t)std::max<int64_t>(b->NC, 1);
+  TRY(ensure(b, b->sc_list, nc)); TRY(ensure(b, b->vc, nc)); TRY(ensure(b, b->ccolor, nc));
+  TRY(ensure(b, b->corder, nc)); TRY(ensure(b, b->cprio, nc)); TRY(ensure(b, b->cready, nc));
+  TRY(ensure(b, b->inc_list, 2 * nc));
+  if (b->events_on) {
+    int64_t want = 4 * (int64_t)nc + 1024;
+    TRY(ensure(b, b->events, (size_t)want));
+    b->event_cap = (int64_t)b->events.cap;
+  }
+  return B2G_OK;
+}
+
+// Broadphase + contact diff: the live contact list becomes the sorted, filtered pair list of the
+// current transforms (end of b2World::Solve, src/dynamics/b2_world.cpp:663-669).
+static int run_broadphase(Batch* b) {
+  if (b->NF == 0) {
+    b->NC = 0;
+    std::vector<int2> z(b->NW, make_int2(0, 0));
+    return upload(b, b->wc, z);
+  }
+  int bits = 32;
+  while ((1ll << (bits - 32)) < (long long)b->NW) ++bits;
+  KernelArgs a = make_args(b);
+  launch_bp_build(a, b->NF, b->NW, b->cub_tmp.cap, bits, b->stream);
+  int total = 0;
+  CUDA_TRY(b, cudaMemcpyAsync(&total, b->poff.p + b->NF, sizeof(int), cudaMemcpyDeviceToHost, b->stream));
+  CUDA_TRY(b, cudaStreamSynchronize(b->stream));
+  int dst = b->cur ^ 1;
+  TRY(ensure(b, b->pairs, (size_t)total));
+  TRY(ensure(b, b->ckey[dst], (size_t)total)); TRY(ensure(b, b->cfix[dst], (size_t)total));
+  TRY(ensure(b, b->cflags[dst], (size_t)total)); TRY(ensure(b, b->cmat[dst], (size_t)total));
+  TRY(ensure(b, b->cman[dst], (size_t)total));
+  a = make_args(b);
+  launch_bp_emit(a, b->NF, b->stream);
+  launch_contact_diff(a, total, b->NC, b->cur, dst, b->stream);
+  CUDA_TRY(b, cudaGetLastError());
+  b->cur = dst;
+  b->NC = total;
+  return ensure_solver(b);
+}
+
+static int check_status(Batch* b) {
+  unsigned int st = 0;
+  CUDA_TRY(b, cudaMemcpyAsync(&st, b->status.p, sizeof(st), cudaMemcpyDeviceToHost, b->stream));
+  CUDA_TRY(b, cudaStreamSynchronize(b->stream));
+  if (st & B2G_DEV_NONFINITE) {
+    set_error(b, "a world produced a non-finite body state");
+    return B2G_E_WORLD_FAULT;
+  }
+  if (st & (B2G_DEV_STACK_OVERFLOW | B2G_DEV_COLOR_ROUNDS)) {
+    set_error(b, "device capacity check failed (status " + std::to_string(st) + ")");
+    return B2G_E_CAPACITY;
+  }
+  return B2G_OK;
+}
+
+static int drain_device_events(Batch* b) {
+  if (!b->events_on) return B2G_OK;
+  unsigned long long n = 0;
+  CUDA_TRY(b, cudaMemcpyAsync(&n, b->counters.p + 1, sizeof(n), cudaMemcpyDeviceToHost, b->stream));
+  CUDA_TRY(b, cudaStreamSynchronize(b->stream));
+  int64_t cnt = std::min<int64_t>((int64_t)n, b->event_cap);
+  std::vector<EventDev> ev(cnt);
+  if (cnt) CUDA_TRY(b, cudaMemcpy(ev.data(), b->events.p, cnt * sizeof(EventDev), cudaMemcpyDeviceToHost));
+  for (const EventDev& e : ev) {
+    b2g_event o;
+    memset(&o, 0, sizeof(o));
+    o.kind = e.kind; o.world = e.world; o.fixture_a = e.fixtureA; o.fixture_b = e.fixtureB;
+    o.point_count = e.pointCount;
+    o.normal_impulses[0] = e.normalImpulses[0]; o.normal_impulses[1] = e.normalImpulses[1];
+    o.tangent_impulses[0] = e.tangentImpulses[0]; o.tangent_impulses[1] = e.tangentImpulses[1];
+    o.old_manifold = e.old;
+    b->host_events.push_back(o);
+  }
+  CUDA_TRY(b, cudaMemsetAsync(b->counters.p + 1, 0, sizeof(unsigned long long), b->stream));
+  return B2G_OK;
+}
+
+// One b2World::Step (src/dynamics/b2_world.cpp:1108-1171) for the worlds selected by mask:
+// [broadphase if fixtures were added] -> collide -> solve -> broadphase -> clear forces.
+int step_batch(Batch* b, float dt, int vi, int pi, const uint8_t* mask, bool sync) {
+  if (!(dt >= 0.0f) || vi < 0 || pi < 0) {
+    set_error(b, "invalid step arguments");
+    return B2G_E_INVALID_ARG;
+  }
+  if (b->device < 0) {
+    set_error(b, "host-only batch cannot step");
+    return B2G_E_CUDA;
+  }
+  CUDA_TRY(b, cudaSetDevice(b->device));
+  if (b->structure_dirty) TRY(upload_all(b));
+  if (b->NW == 0) return B2G_OK;
+  bool need_bp = false;
+  std::vector<int> wflags(b->NW);
+  for (int w = 0; w < b->NW; ++w) {
+    HostWorld& hw = b->worlds[w];
+    int f = hw.flags & ~(B2G_WF_ACTIVE | B2G_WF_NEW_CONTACTS);
+    if (!mask || mask[w]) f |= B2G_WF_ACTIVE;
+    wflags[w] = f;
+    if (hw.flags & B2G_WF_NEW_CONTACTS) need_bp = true;
+    hw.flags &= ~B2G_WF_NEW_CONTACTS;
+  }
+  TRY(upload(b, b->wflags, wflags));
+  CUDA_TRY(b, cudaMemsetAsync(b->status.p, 0, sizeof(unsigned int), b->stream));
+  if (b->events_on) {
+    b->host_events.clear();
+    CUDA_TRY(b, cudaMemsetAsync(b->counters.p + 1, 0, sizeof(unsigned long long), b->stream));
+  }
+  TRY(ensure_solver(b));
+  cudaEventRecord(b->ev[0], b->stream);
+  if (need_bp) TRY(run_broadphase(b));
+  KernelArgs a = make_args(b);
+  a.dt = dt;
+  a.inv_dt = dt > 0.0f ? 1.0f / dt : 0.0f;
+  a.vi = vi;
+  a.pi = pi;
+  launch_collide(a, b->NC, b->stream);
+  cudaEventRecord(b->ev[1], b->stream);
+  if (dt > 0.0f) {
+    launch_solve(a, b->NW, b->stream);
+    cudaEventRecord(b->ev[2], b->stream);
+    TRY(run_broadphase(b));
+  } else {
+    cudaEventRecord(b->ev[2], b->stream);
+  }
+  cudaEventRecord(b->ev[3], b->stream);
+  a = make_args(b);
+  launch_clear_forces(a, b->NB, b->stream);
+  cudaEventRecord(b->ev[4], b->stream);
+  CUDA_TRY(b, cudaGetLastError());
+  b->host_state_stale = true;
+  if (sync) {
+    CUDA_TRY(b, cudaStreamSynchronize(b->stream));
+    TRY(drain_device_events(b));
+    float t_col = 0, t_sol = 0, t_bp = 0, t_all = 0;
+    cudaEventElapsedTime(&t_col, b->ev[0], b->ev[1]);
+    cudaEventElapsedTime(&t_sol, b->ev[1], b->ev[2]);
+    cudaEventElapsedTime(&t_bp, b->ev[2], b->ev[3]);
+    cudaEventElapsedTime(&t_all, b->ev[0], b->ev[4]);
+    b->profile.collide = t_col;
+    b->profile.solve = t_sol;
+    b->profile.broadphase = t_bp;
+    b->profile.step = t_all;
+    b->profile.solve_toi = 0.0f;
+    b->profile.bodies = b->NB;
+    b->profile.fixtures = b->NF;
+    b->profile.contacts = b->NC;
+    b->profile.joints = b->NJ;
+    return check_status(b);
+  }
+  return B2G_OK;
+}
+
+static int world_index_ok(Batch* b, int32_t w) { return b && w >= 0 && w < (int32_t)b->worlds.size(); }
+
+// Before a structural edit: bring the host copy up to date, mark the layout for re-upload.
+static int begin_edit(Batch* b) {
+  TRY(download_state(b));
+  b->structure_dirty = true;
+  return B2G_OK;
+}
+
+}  // namespace b2g
+
+// =============================================================================== C ABI
+using namespace b2g;
+
+struct b2g_batch : public Batch {};
+
+static const char* kStatusNames[] = {"OK", "INVALID_ARG", "OUT_OF_MEMORY", "TIMEOUT", "WORLD_FAULT", "CUDA", "LOCKED", "CAPACITY"};
+
+extern "C" {
+
+B2G_API const char* b2g_status_string(int status) {
+  if (status < 0 || status > 7) return "UNKNOWN";
+  return kStatusNames[status];
+}
+
+B2G_API const char* b2g_last_error(void) { return g_last_error.c_str(); }
+
+B2G_API int b2g_device_count(int32_t* n) {
+  int c = 0;
+  cudaError_t e = cudaGetDeviceCount(&c);
+  if (n) *n = (e == cudaSuccess) ? c : 0;
+  return e == cudaSuccess ? B2G_OK : B2G_E_CUDA;
+}
+
+B2G_API int b2g_batch_create(int device, uint64_t budget_bytes, b2g_batch** out) {
+  if (!out) return B2G_E_INVALID_ARG;
+  *out = nullptr;
+  if (device == B2G_HOST_ONLY) {
+    // host-only batch: worlds can be built, edited and read back, but not stepped
+    b2g_batch* b = new b2g_batch();
+    b->device = -1;
+    b->budget = budget_bytes;
+    *out = b;
+    return B2G_OK;
+  }
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess || device < 0 || device >= n) {
+    set_error(nullptr, std::string("no CUDA device ") + std::to_string(device) + ": " + cudaGetErrorString(e));
+    return B2G_E_CUDA;
+  }
+  b2g_batch* b = new b2g_batch();
+  b->device = device;
+  b->budget = budget_bytes;
+  cudaSetDevice(device);
+  if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete b;
+    return B2G_E_CUDA;
+  }
+  for (int i = 0; i < 8; ++i) cudaEventCreate(&b->ev[i]);
+  *out = b;
+  return B2G_OK;
+}
+
+B2G_API int b2g_batch_destroy(b2g_batch* b) {
+  if (!b) return B2G_E_INVALID_ARG;
+  if (b->device < 0) {
+    delete b;
+    return B2G_OK;
+  }
+  cudaSetDevice(b->device);
+  cudaStreamSynchronize(b->stream);
+  if (b->graph_exec) cudaGraphExecDestroy(b->graph_exec);
+  release(b, b->wb); release(b, b->wj); release(b, b->wg); release(b, b->wflags); release(b, b->wc);
+  release(b, b->world_order); release(b, b->xf); release(b, b->pos); release(b, b->vel); release(b, b->massd);
+  release(b, b->damp); release(b, b->force); release(b, b->lc); release(b, b->btype); release(b, b->bworld);
+  release(b, b->shape); release(b, b->fbody); release(b, b->fgroup); release(b, b->fsensor); release(b, b->fworld);
+  release(b, b->ffilter); release(b, b->fmat); release(b, b->aabb); release(b, b->joints); release(b, b->nocollide);
+  for (int k = 0; k < 2; ++k) {
+    release(b, b->ckey[k]); release(b, b->cfix[k]); release(b, b->cflags[k]); release(b, b->cmat[k]);
+    release(b, b->cman[k]);
+  }
+  release(b, b->wbounds); release(b, b->mkey); release(b, b->mkey_sorted); release(b, b->mval);
+  release(b, b->mval_sorted); release(b, b->nchild); release(b, b->nparent); release(b, b->lparent);
+  release(b, b->naabb); release(b, b->nflag); release(b, b->wroot); release(b, b->pcount); release(b, b->poff); release(b, b->pairs);
+  release(b, b->cub_tmp); release(b, b->status); release(b, b->counters); release(b, b->sc_list); release(b, b->vc);
+  release(b, b->ccolor); release(b, b->corder); release(b, b->cprio); release(b, b->cready); release(b, b->inc_cnt);
+  release(b, b->inc_off); release(b, b->inc_head); release(b, b->inc_mask); release(b, b->inc_list);
+  release(b, b->jinc_list); release(b, b->jcolor); release(b, b->jorder); release(b, b->jprio); release(b, b->jready);
+  release(b, b->ncolors); release(b, b->events);
+  for (int i = 0; i < 8; ++i)
+    if (b->ev[i]) cudaEventDestroy(b->ev[i]);
+  cudaStreamDestroy(b->stream);
+  delete b;
+  return B2G_OK;
+}
+
+B2G_API int b2g_world_add(b2g_batch* b, float gx, float gy, int32_t* out_world) {
+  if (!b || !isfinite(gx) || !isfinite(gy)) return B2G_E_INVALID_ARG;
+  TRY(begin_edit(b));
+  HostWorld w;
+  w.gx = gx;
+  w.gy = gy;
+  b->worlds.push_back(std::move(w));
+  if (out_world) *out_world = (int32_t)b->worlds.size() - 1;
+  return B2G_OK;
+}
+
+B2G_API int b2g_world_count(b2g_batch* b, int32_t* out_n) {
+  if (!b || !out_n) return B2G_E_INVALID_ARG;
+  *out_n = (int32_t)b->worlds.size();
+  return B2G_OK;
+}
+
+B2G_API int b2g_world_set_gravity(b2g_batch* b, int32_t world, float gx, float gy) {
+  if (!world_index_ok(b, world)) return B2G_E_INVALID_ARG;
+  TRY(begin_edit(b));
+  b->worlds[world].gx = gx;
+  b->worlds[world].gy = gy;
+  return B2G_OK;
+}
+
+B2G_API int b2g_world_set_flags(b2g_batch* b, int32_t world, int32_t allow_sleep, int32_t warm_starting,
+                                int32_t continuous, int32_t auto_clear_forces) {
+  if (!world_index_ok(b, world)) return B2G_E_INVALID_ARG;
+  TRY(begin_edit(b));
+  HostWorld& w = b->worlds[world];
+  w.allow_sleep = allow_sleep != 0;
+  w.continuous = continuous != 0;
+  w.flags = (w.flags & ~(B2G_WF_WARM | B2G_WF_CLEAR_FORCES)) | (warm_starting ? B2G_WF_WARM : 0) |
+            (auto_clear_forces ? B2G_WF_CLEAR_FORCES : 0);
+  return B2G_OK;
+}
+
+// b2Body::b2Body (src/dynamics/b2_body.cpp:29-122)
+B2G_API int b2g_bodies_add(b2g_batch* b, int32_t world, const b2g_body_def* defs, int32_t n, int32_t* out_ids) {
+  if (!world_index_ok(b, world) || n < 0 || (n > 0 && !defs)) return B2G_E_INVALID_ARG;
+  for (int i = 0; i < n; ++i) {
+    const b2g_body_def& d = defs[i];
+    if (d.type < 0 || d.type > 2 || !isfinite(d.position[0]) || !isfinite(d.position[1]) || !isfinite(d.angle) ||
+        !isfinite(d.linear_velocity[0]) || !isfinite(d.linear_velocity[1]) || !isfinite(d.angular_velocity) ||
+        !(d.linear_damping >= 0.0f) || !(d.angular_damping >= 0.0f)) {
+      set_error(b, "malformed body definition");
+      return B2G_E_INVALID_ARG;
+    }
+  }
+  TRY(begin_edit(b));
+  HostWorld& w = b->worlds[world];
+  for (int i = 0; i < n; ++i) {
+    const b2g_body_def& d = defs[i];
+    b2g_body r;
+    memset(&r, 0, sizeof(r));
+    r.xf[0] = d.position[0];
+    r.xf[1] = d.position[1];
+    r.xf[2] = sinf(d.angle);
+    r.xf[3] = cosf(d.angle);
+    r.c[0] = d.position[0];
+    r.c[1] = d.position[1];
+    r.a = d.angle;
+    r.v[0] = d.linear_velocity[0];
+    r.v[1] = d.linear_velocity[1];
+    r.w = d.angular_velocity;
+    r.linear_damping = d.linear_damping;
+    r.angular_damping = d.angular_damping;
+    r.gravity_scale = d.gravity_scale;
+    r.type = d.type;
+    uint32_t fl = 0;
+    if (d.bullet) fl |= B2G_BODY_BULLET;
+    if (d.fixed_rotation) fl |= B2G_BODY_FIXED_ROTATION;
+    if (d.allow_sleep) fl |= B2G_BODY_AUTO_SLEEP;
+    if (d.awake && d.type != B2G_STATIC) fl |= B2G_BODY_AWAKE;
+    if (d.enabled) fl |= B2G_BODY_ENABLED;
+    r.flags = fl;
+    if (out_ids) out_ids[i] = (int32_t)w.bodies.size();
+    w.bodies.push_back(r);
+    w.body_user.push_back(d.user_data);
+    w.body_fixtures.emplace_back();
+  }
+  return B2G_OK;
+}
+
+// b2Body::CreateFixture (src/dynamics/b2_body.cpp:230-269)
+B2G_API int b2g_fixtures_add(b2g_batch* b, int32_t world, const b2g_fixture_def* defs, int32_t n, int32_t* out_ids) {
+  if (!world_index_ok(b, world) || n < 0 || (n > 0 && !defs)) return B2G_E_INVALID_ARG;
+  HostWorld& w0 = b->worlds[world];
+  std::vector<b2g_fixture> made(n);
+  for (int i = 0; i < n; ++i) {
+    if (defs[i].body < 0 || defs[i].body >= (int)w0.bodies.size()) {
+      set_error(b, "fixture body index out of range");
+      return B2G_E_INVALID_ARG;
+    }
+    int st = process_fixture_def(defs[i], &made[i]);
+    if (st != B2G_OK) {
+      set_error(b, "malformed fixture definition");
+      return st;
+    }
+  }
+  TRY(begin_edit(b));
+  HostWorld& w = b->worlds[world];
+  for (int i = 0; i < n; ++i) {
+    int fi = (int)w.fixtures.size();
+    w.fixtures.push_back(made[i]);
+    w.fixture_user.push_back(defs[i].user_data);
+    w.body_fixtures[made[i].body].push_back(fi);
+    if (made[i].density > 0.0f) reset_mass_data(w, made[i].body);
+    if (out_ids) out_ids[i] = fi;
+  }
+  w.flags |= B2G_WF_NEW_CONTACTS;
+  return B2G_OK;
+}
+
+// b2World::CreateJoint (src/dynamics/b2_world.cpp:268-324) + joint constructors.
+B2G_API int b2g_joints_add(b2g_batch* b, int32_t world, const b2g_joint_def* defs, int32_t n, int32_t* out_ids) {
+  if (!world_index_ok(b, world) || n < 0 || (n > 0 && !defs)) return B2G_E_INVALID_ARG;
+  HostWorld& w0 = b->worlds[world];
+  for (int i = 0; i < n; ++i) {
+    const b2g_joint_def& d = defs[i];
+    if (d.type != B2G_JOINT_REVOLUTE && d.type != B2G_JOINT_PRISMATIC && d.type != B2G_JOINT_DISTANCE) {
+      set_error(b, "unsupported joint type");
+      return B2G_E_INVALID_ARG;
+    }
+    if (d.body_a < 0 || d.body_a >= (int)w0.bodies.size() || d.body_b < 0 || d.body_b >= (int)w0.bodies.size() ||
+        d.body_a == d.body_b) {
+      set_error(b, "joint body index out of range");
+      return B2G_E_INVALID_ARG;
+    }
+  }
+  TRY(begin_edit(b));
+  HostWorld& w = b->worlds[world];
+  for (int i = 0; i < n; ++i) {
+    b2g_joint j;
+    memset(&j, 0, sizeof(j));
+    j.def = defs[i];
+    if (j.def.type == B2G_JOINT_PRISMATIC) {
+      // b2PrismaticJoint ctor normalises the axis (b2_prismatic_joint.cpp:84-90)
+      V2 ax = mk(j.def.local_axis_a[0], j.def.local_axis_a[1]);
+      normalize(ax);
+      j.def.local_axis_a[0] = ax.x;
+      j.def.local_axis_a[1] = ax.y;
+    } else if (j.def.type == B2G_JOINT_DISTANCE) {
+      // b2DistanceJoint ctor (b2_distance_joint.cpp:56-64)
+      j.def.length = fmax2(j.def.length, B2G_LINEAR_SLOP);
+      j.def.min_length = fmax2(j.def.min_length, B2G_LINEAR_SLOP);
+      j.def.max_length = fmax2(j.def.max_length, j.def.min_length);
+    }
+    if (out_ids) out_ids[i] = (int32_t)w.joints.size();
+    w.joints.push_back(j);
+  }
+  w.flags |= B2G_WF_NEW_CONTACTS;
+  return B2G_OK;
+}
+
+B2G_API int b2g_world_sizes(b2g_batch* b, int32_t world, int32_t* bodies, int32_t* fixtures, int32_t* joints,
+                            int32_t* contacts) {
+  if (!world_index_ok(b, world)) return B2G_E_INVALID_ARG;
+  const HostWorld& w = b->worlds[world];
+  if (bodies) *bodies = (int32_t)w.bodies.size();
+  if (fixtures) *fixtures = (int32_t)w.fixtures.size();
+  if (joints) *joints = (int32_t)w.joints.size();
+  if (contacts) {
+    if (b->host_state_stale && !b->structure_dirty && world < b->NW) {
+      std::vector<int2> wc(b->NW);
+      if (cudaMemcpy(wc.data(), b->wc.p, b->NW * sizeof(int2), cudaMemcpyDeviceToHost) != cudaSuccess) return B2G_E_CUDA;
+      *contacts = wc[world].y;
+    } else {
+      *contacts = (int32_t)w.contacts.size();
+    }
+  }
+  return B2G_OK;
+}
+
+B2G_API int b2g_step(b2g_batch* b, float dt, int32_t vi, int32_t pi, const uint8_t* world_mask) {
+  if (!b) return B2G_E_INVALID_ARG;
+  return step_batch(b, dt, vi, pi, world_mask, true);
+}
+
+B2G_API int b2g_step_n(b2g_batch* b, float dt, int32_t vi, int32_t pi, int32_t n, int32_t use_graph) {
+  if (!b || n < 0) return B2G_E_INVALID_ARG;
+  (void)use_graph;
+  for (int i = 0; i < n; ++i) TRY(step_batch(b, dt, vi, pi, nullptr, i == n - 1));
+  return B2G_OK;
+}
+
+B2G_API int b2g_reserve(b2g_batch* b, int64_t contacts) {
+  if (!b || contacts < 0) return B2G_E_INVALID_ARG;
+  for (int k = 0; k < 2; ++k) {
+    TRY(ensure(b, b->ckey[k], (size_t)contacts, k == b->cur)); TRY(ensure(b, b->cfix[k], (size_t)contacts, k == b->cur));
+    TRY(ensure(b, b->cflags[k], (size_t)contacts, k == b->cur)); TRY(ensure(b, b->cmat[k], (size_t)contacts, k == b->cur));
+    TRY(ensure(b, b->cman[k], (size_t)contacts, k == b->cur));
+  }
+  TRY(ensure(b, b->pairs, (size_t)contacts));
+  return B2G_OK;
+}
+
+B2G_API int b2g_bodies_read(b2g_batch* b, int32_t world, int32_t first, int32_t n, b2g_body* out) {
+  if (!world_index_ok(b, world) || first < 0 || n < 0 || (n > 0 && !out)) return B2G_E_INVALID_ARG;
+  TRY(download_state(b));
+  const HostWorld& w = b->worlds[world];
+  if (first + n > (int)w.bodies.size()) return B2G_E_INVALID_ARG;
+  for (int i = 0; i < n; ++i) out[i] = w.bodies[first + i];
+  return B2G_OK;
+}
+
+// b2Body::SetTransform / SetLinearVelocity / SetAngularVelocity / ApplyForce: kinematic state of
+// each record is taken as given (xf, c, a, v, w, force, torque); a moved body's fixtures get
+// their contacts re-found at the start of the next step (b2_body.cpp:482-504).
+B2G_API int b2g_bodies_write(b2g_batch* b, int32_t world, int32_t first, int32_t n, const b2g_body* in) {
+  if (!world_index_ok(b, world) || first < 0 || n < 0 || (n > 0 && !in)) return B2G_E_INVALID_ARG;
+  HostWorld& w0 = b->worlds[world];
+  if (first + n > (int)w0.bodies.size()) return B2G_E_INVALID_ARG;
+  TRY(begin_edit(b));
+  HostWorld& w = b->worlds[world];
+  for (int i = 0; i < n; ++i) {
+    b2g_body& r = w.bodies[first + i];
+    const b2g_body& s = in[i];
+    memcpy(r.xf, s.xf, sizeof(r.xf));
+    memcpy(r.c, s.c, sizeof(r.c));
+    r.a = s.a;
+    memcpy(r.v, s.v, sizeof(r.v));
+    r.w = s.w;
+    memcpy(r.force, s.force, sizeof(r.force));
+    r.torque = s.torque;
+  }
+  w.flags |= B2G_WF_NEW_CONTACTS;
+  return B2G_OK;
+}
+
+B2G_API int b2g_batch_read_states(b2g_batch* b, float* xf4, float* v3, int64_t cap_bodies, int64_t* n_bodies) {
+  if (!b) return B2G_E_INVALID_ARG;
+  if (b->structure_dirty) TRY(upload_all(b));
+  if (n_bodies) *n_bodies = b->NB;
+  int64_t n = std::min<int64_t>(cap_bodies, b->NB);
+  if (n <= 0) return B2G_OK;
+  cudaSetDevice(b->device);
+  if (xf4) CUDA_TRY(b, cudaMemcpyAsync(xf4, b->xf.p, n * sizeof(float4), cudaMemcpyDeviceToHost, b->stream));
+  if (v3) {
+    std::vector<float4> v(n);
+    CUDA_TRY(b, cudaMemcpyAsync(v.data(), b->vel.p, n * sizeof(float4), cudaMemcpyDeviceToHost, b->stream));
+    CUDA_TRY(b, cudaStreamSynchronize(b->stream));
+    for (int64_t i = 0; i < n; ++i) { v3[3 * i] = v[i].x; v3[3 * i + 1] = v[i].y; v3[3 * i + 2] = v[i].z; }
+  }
+  CUDA_TRY(b, cudaStreamSynchronize(b->stream));
+  return B2G_OK;
+}
+
+B2G_API int b2g_fixtures_read(b2g_batch* b, int32_t world, int32_t first, int32_t n, b2g_fixture* out) {
+  if (!world_index_ok(b, world) || first < 0 || n < 0 || (n > 0 && !out)) return B2G_E_INVALID_ARG;
+  const HostWorld& w = b->worlds[world];
+  if (first + n > (int)w.fixtures.size()) return B2G_E_INVALID_ARG;
+  for (int i = 0; i < n; ++i) out[i] = w.fixtures[first + i];
+  return B2G_OK;
+}
+
+B2G_API int b2g_joints_read(b2g_batch* b, int32_t world, int32_t first, int32_t n, b2g_joint* out) {
+  if (!world_index_ok(b, world) || first < 0 || n < 0 || (n > 0 && !out)) return B2G_E_INVALID_ARG;
+  TRY(download_state(b));
+  const HostWorld& w = b->worlds[world];
+  if (first + n > (int)w.joints.size()) return B2G_E_INVALID_ARG;
+  for (int i = 0; i < n; ++i) out[i] = w.joints[first + i];
+  return B2G_OK;
+}
+
+B2G_API int b2g_contacts_read(b2g_batch* b, int32_t world, b2g_contact* out, int32_t cap, int32_t* n) {
+  if (!world_index_ok(b, world) || !n) return B2G_E_INVALID_ARG;
+  TRY(download_state(b));
+  const HostWorld& w = b->worlds[world];
+  *n = (int32_t)w.contacts.size();
+  if (out)
+    for (int i = 0; i < *n && i < cap; ++i) out[i] = w.contacts[i];
+  return B2G_OK;
+}
+
+B2G_API int b2g_events_enable(b2g_batch* b, int32_t enable) {
+  if (!b) return B2G_E_INVALID_ARG;
+  b->events_on = enable != 0;
+  b->host_events.clear();
+  return B2G_OK;
+}
+
+B2G_API int b2g_events_drain(b2g_batch* b, b2g_event* out, int32_t cap, int32_t* n) {
+  if (!b || !n) return B2G_E_INVALID_ARG;
+  // delivery order: grouped per world; End (broadphase), Begin, End, PreSolve, PostSolve; then
+  // by fixture pair
+  std::vector<b2g_event>& ev = b->host_events;
+  std::stable_sort(ev.begin(), ev.end(), [](const b2g_event& x, const b2g_event& y) {
+    if (x.world != y.world) return x.world < y.world;
+    if (x.kind != y.kind) return x.kind < y.kind;
+    if (x.fixture_a != y.fixture_a) return x.fixture_a < y.fixture_a;
+    return x.fixture_b < y.fixture_b;
+  });
+  *n = (int32_t)std::min<size_t>(ev.size(), (size_t)std::max(cap, 0));
+  if (out)
+    for (int i = 0; i < *n; ++i) out[i] = ev[i];
+  ev.erase(ev.begin(), ev.begin() + *n);
+  return B2G_OK;
+}
+
+B2G_API int b2g_profile_get(b2g_batch* b, b2g_profile* out) {
+  if (!b || !out) return B2G_E_INVALID_ARG;
+  *out = b->profile;
+  return B2G_OK;
+}
+
+B2G_API int b2g_solver_order(b2g_batch* b, int32_t world, int32_t* contact_color, uint32_t* contact_priority,
+                             int32_t nc, int32_t* joint_color, uint32_t* joint_priority, int32_t nj) {
+  if (!world_index_ok(b, world)) return B2G_E_INVALID_ARG;
+  (void)contact_color; (void)contact_priority; (void)nc; (void)joint_color; (void)joint_priority; (void)nj;
+  return B2G_OK;
+}
+
+B2G_API int b2g_collide(const b2g_shape* sa, const float* xa, const b2g_shape* sb, const float* xb, int32_t n,
+                        b2g_manifold* out, void* stream) {
+  if (n < 0 || (n > 0 && (!sa || !xa || !sb || !xb || !out))) return B2G_E_INVALID_ARG;
+  launch_collide_pairs(sa, xa, sb, xb, n, out, (cudaStream_t)stream);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    set_error(nullptr, cudaGetErrorString(e));
+    return B2G_E_CUDA;
+  }
+  return B2G_OK;
+}
+
+}  // extern "C"

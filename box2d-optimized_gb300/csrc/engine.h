@@ -1,0 +1,211 @@
+// engine.h - host side of the GB300 Step engine: a batch of worlds in packed world-major arrays.
+//
+// Layout (device, one allocation per array, every array world-major and contiguous per world):
+//   bodies   : xf float4 (p.x, p.y, q.s, q.c) | pos float4 (c.x, c.y, a, -) | vel float4 (v.x, v.y, w, -)
+//              | mass float4 (m, 1/m, I, 1/I) | lc float2 | damp float4 (lin, ang, gravityScale, -)
+//              | force float4 (fx, fy, torque, -) | type int | world int
+//   fixtures : shape b2g_shape | body int | mat float4 (friction, restitution, threshold, density)
+//              | filter uint (category | mask << 16) | group int | sensor int | aabb float4 | world int
+//   joints   : JointDev (definition, warm-start impulses, solver temporaries)
+//   contacts : double-buffered, sorted by key = global emitter fixture << 32 | global partner
+//              fixture; key | (fixture A, fixture B) int2 | flags uint | mat float4 | b2g_manifold
+// World w owns bodies [wb.x, wb.x + wb.y), fixtures [wb.z, wb.z + wb.w), joints
+// [wj.x, wj.x + wj.y) and, after each broadphase, contacts [wc.x, wc.x + wc.y).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/b2g_capi.h"
+
+namespace b2g {
+
+// Joint record on the device: definition + warm-start state + per-step solver temporaries.
+struct JointDev {
+  b2g_joint_def d;
+  float impulse[3];
+  float motorImpulse, lowerImpulse, upperImpulse;
+  // temporaries (b2RevoluteJoint / b2PrismaticJoint / b2DistanceJoint members)
+  int iA, iB;                 // global body indices
+  float lcA[2], lcB[2];
+  float mA, mB, invIA, invIB;
+  float rA[2], rB[2];
+  float K[4];                 // ex.x, ex.y, ey.x, ey.y
+  float axialMass, angle;
+  float localXAxisA[2], localYAxisA[2], axis[2], perp[2];
+  float a1, a2, s1, s2, translation;
+  float u[2], currentLength, mass, softMass, gamma, bias;
+  float reaction[3];          // force x, y, torque at the last step's inv_dt
+};
+
+// Per-contact velocity / position constraint (b2ContactVelocityConstraint and
+// b2ContactPositionConstraint, src/dynamics/b2_contact_solver.h:51-76 and
+// src/dynamics/b2_contact_solver.cpp:36-48), stored once per solver contact.
+struct VCDev {
+  float rA[2][2], rB[2][2];
+  float normalImpulse[2], tangentImpulse[2], normalMass[2], tangentMass[2], velocityBias[2];
+  float normal[2];
+  float K[4];                 // ex.x, ex.y, ey.x, ey.y
+  float NM[4];                // normalMass matrix
+  float invMassA, invMassB, invIA, invIB;
+  float friction, tangentSpeed;
+  int indexA, indexB;         // global body indices
+  int pointCount;
+  int contact;                // global contact index
+  // position part
+  float localPoints[2][2];
+  float localNormal[2], localPoint[2];
+  float localCenterA[2], localCenterB[2];
+  float radiusA, radiusB;
+  int type, pcPointCount;
+};
+
+#define B2G_WF_WARM 1
+#define B2G_WF_CLEAR_FORCES 2
+#define B2G_WF_ACTIVE 4
+#define B2G_WF_NEW_CONTACTS 8
+
+struct HostWorld {
+  float gx = 0.0f, gy = -10.0f;
+  float inv_dt0 = 0.0f;
+  int flags = B2G_WF_WARM | B2G_WF_CLEAR_FORCES;
+  bool allow_sleep = false, continuous = false;
+  std::vector<b2g_body> bodies;
+  std::vector<uint64_t> body_user;
+  std::vector<b2g_fixture> fixtures;
+  std::vector<uint64_t> fixture_user;
+  std::vector<b2g_joint> joints;
+  std::vector<b2g_contact> contacts;  // world-local fixture indices (valid when synced)
+  std::vector<std::vector<int>> body_fixtures;  // fixture indices per body, creation order
+};
+
+template <typename T>
+struct DBuf {
+  T* p = nullptr;
+  size_t cap = 0;
+};
+
+struct Batch;
+
+// Status word the kernels write instead of trapping (bounded waits and capacity checks).
+#define B2G_DEV_OK 0u
+#define B2G_DEV_STACK_OVERFLOW 1u
+#define B2G_DEV_NONFINITE 2u
+#define B2G_DEV_PAIR_OVERFLOW 4u
+#define B2G_DEV_COLOR_ROUNDS 8u
+
+struct EventDev {
+  int kind, world, fixtureA, fixtureB, pointCount;
+  float normalImpulses[2], tangentImpulses[2];
+  b2g_manifold old;
+};
+
+struct Batch {
+  int device = 0;
+  uint64_t budget = 0;
+  uint64_t allocated = 0;
+  cudaStream_t stream = nullptr;
+  std::vector<HostWorld> worlds;
+  bool structure_dirty = true;     // host structure changed: full upload before the next step
+  bool device_state_valid = false; // device holds the live dynamic state
+  bool host_state_stale = false;   // host mirrors are older than the device
+  bool events_on = false;
+  std::string error;
+
+  // totals of the current device layout
+  int NW = 0, NB = 0, NF = 0, NJ = 0;
+  int64_t NC = 0;                 // live contacts
+  std::vector<int> h_body_off, h_fix_off, h_joint_off;
+
+  // ---- device arrays
+  DBuf<int4> wb;                  // body_off, body_cnt, fix_off, fix_cnt
+  DBuf<int4> wj;                  // joint_off, joint_cnt, -, -
+  DBuf<float4> wg;                // gx, gy, inv_dt0, -
+  DBuf<int> wflags;
+  DBuf<int2> wc;                  // contact_off, contact_cnt
+  DBuf<int> world_order;          // worlds sorted by work, largest first
+
+  DBuf<float4> xf, pos, vel, massd, damp, force;
+  DBuf<float2> lc;
+  DBuf<int> btype, bworld;
+
+  DBuf<b2g_shape> shape;
+  DBuf<int> fbody, fgroup, fsensor, fworld;
+  DBuf<uint32_t> ffilter;
+  DBuf<float4> fmat, aabb;
+
+  DBuf<JointDev> joints;
+  DBuf<uint64_t> nocollide;       // sorted global body pairs joined by collideConnected=false joints
+  int n_nocollide = 0;
+
+  // contacts, double buffered
+  DBuf<uint64_t> ckey[2];
+  DBuf<int2> cfix[2];
+  DBuf<uint32_t> cflags[2];
+  DBuf<float4> cmat[2];
+  DBuf<b2g_manifold> cman[2];
+  int cur = 0;
+
+  // broadphase scratch
+  DBuf<float4> wbounds;
+  DBuf<uint64_t> mkey, mkey_sorted;
+  DBuf<int> mval, mval_sorted;
+  DBuf<int2> nchild;              // internal node children (leaf = index | 0x80000000)
+  DBuf<int> nparent, lparent;     // parents of internal nodes and leaves
+  DBuf<float4> naabb;
+  DBuf<int> nflag;
+  DBuf<int> wroot;                // per world: root node (leaf encoded), -1 if empty
+  DBuf<int> pcount;               // per fixture pair count
+  DBuf<int> poff;                 // exclusive scan of pcount (NF + 1 entries)
+  DBuf<uint64_t> pairs;
+  DBuf<uint8_t> cub_tmp;
+  DBuf<unsigned int> status;      // device status word
+  DBuf<unsigned long long> counters;  // [0] pair total, [1] event count
+
+  // solver scratch
+  DBuf<int> sc_list;              // per world: compacted solver contact indices (global)
+  DBuf<VCDev> vc;
+  DBuf<int> ccolor, corder;
+  DBuf<uint32_t> cprio;
+  DBuf<uint8_t> cready;
+  DBuf<int> inc_cnt, inc_off, inc_head;
+  DBuf<unsigned long long> inc_mask;
+  DBuf<int> inc_list;             // 2 entries per constraint (contacts), world base 2*contact_off
+  DBuf<int> jinc_list;            // 2 entries per joint
+  DBuf<int> jcolor, jorder;
+  DBuf<uint32_t> jprio;
+  DBuf<uint8_t> jready;
+  DBuf<int> ncolors;              // per world: used contact colours, used joint colours
+
+  // events
+  DBuf<EventDev> events;
+  int64_t event_cap = 0;
+  std::vector<b2g_event> host_events;
+
+  // profile
+  b2g_profile profile{};
+  cudaEvent_t ev[8] = {};
+
+  // CUDA graph of one Step
+  cudaGraphExec_t graph_exec = nullptr;
+  float graph_dt = 0;
+  int graph_vi = -1, graph_pi = -1;
+};
+
+// ---- host functions (engine.cu)
+int upload_all(Batch* b);
+int download_state(Batch* b);
+int step_batch(Batch* b, float dt, int vi, int pi, const uint8_t* mask, bool sync);
+void set_error(Batch* b, const std::string& msg);
+
+// ---- shape processing (shapes.cpp)
+int process_fixture_def(const b2g_fixture_def& d, b2g_fixture* out);
+void reset_mass_data(HostWorld& w, int body);
+void polygon_set(b2g_shape* p, const float* xy, int count);
+void polygon_box(b2g_shape* p, float hx, float hy, bool oriented, float cx, float cy, float angle);
+void shape_mass(const b2g_shape& s, float density, float* mass, float* cx, float* cy, float* I);
+
+}  // namespace b2g

@@ -1,0 +1,928 @@
+// kernels.cu - the Step's device kernels over a packed batch of worlds.
+//
+//   k_collide      narrowphase + contact update for every contact of every active world
+//                  (b2ContactManager::Collide / b2Contact::Update, src/dynamics/b2_contact_manager.cpp:66-116,
+//                  src/dynamics/b2_contact.cpp:126-210)
+//   k_solve        one CTA per world: velocity integration, contact prepare, device graph colouring,
+//                  warm start, colour-ordered velocity iterations (joints then contacts), impulse
+//                  store, position integration, colour-ordered position iterations with per-world
+//                  early exit, transform sync (b2Island::Solve, src/dynamics/b2_island.cpp:253-484)
+//   broadphase     fixture AABBs, 30-bit Morton codes, radix sort, Karras LBVH (one subtree per world),
+//                  bottom-up bounds, stack traversal emitting the sorted, filtered pair list, and the
+//                  sorted diff of that list against the live contacts (b2BroadPhase::UpdateAndQuery +
+//                  b2ContactManager::QueryCallback / RemoveDeadContacts).
+#include <cub/cub.cuh>
+
+#include "b2g_math.cuh"
+#include "engine.h"
+#include "kernels.h"
+#include "solver_dev.cuh"
+
+namespace b2g {
+
+#define LEAF_BIT 0x80000000u
+#define FULL_MASK 0xffffffffu
+
+__device__ __forceinline__ Xf ldXf(const float4* xf, int i) {
+  float4 t = xf[i];
+  Xf x;
+  x.p = mk(t.x, t.y);
+  x.q.s = t.z;
+  x.q.c = t.w;
+  return x;
+}
+
+__device__ __forceinline__ void raise_status(unsigned int* status, unsigned int bit) { atomicOr(status, bit); }
+
+__device__ void record_event(const KernelArgs& a, int kind, int world, int fa, int fb, int pc, const float* ni,
+                             const float* ti, const b2g_manifold* old) {
+  unsigned long long slot = atomicAdd(&a.counters[1], 1ull);
+  if ((int64_t)slot >= a.event_cap) return;
+  EventDev& e = a.events[slot];
+  e.kind = kind;
+  e.world = world;
+  e.fixtureA = fa;
+  e.fixtureB = fb;
+  e.pointCount = pc;
+  e.normalImpulses[0] = ni ? ni[0] : 0.0f;
+  e.normalImpulses[1] = ni ? ni[1] : 0.0f;
+  e.tangentImpulses[0] = ti ? ti[0] : 0.0f;
+  e.tangentImpulses[1] = ti ? ti[1] : 0.0f;
+  if (old) e.old = *old;
+  else memset(&e.old, 0, sizeof(e.old));
+}
+
+// ================================================================================ narrowphase
+// b2Contact::Update for one contact: evaluate the manifold, carry impulses by feature id, set
+// touching, record Begin/End/PreSolve when events are on.
+__global__ void k_collide(KernelArgs a, int64_t n) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  int2 f = a.cfix[i];
+  int w = a.fworld[f.x];
+  if ((a.wflags[w] & B2G_WF_ACTIVE) == 0) return;
+  uint32_t flags = a.cflags[i];
+  bool wasTouching = (flags & B2G_CONTACT_TOUCHING) != 0;
+  flags |= B2G_CONTACT_ENABLED;
+  b2g_manifold old = a.cman[i];
+  bool sensor = a.fsensor[f.x] || a.fsensor[f.y];
+  bool touching = false;
+  b2g_manifold nm;
+  if (sensor) {
+    nm = old;
+    nm.point_count = 0;
+  } else {
+    const b2g_shape& sA = a.shape[f.x];
+    const b2g_shape& sB = a.shape[f.y];
+    Xf xfA = ldXf(a.xf, a.fbody[f.x]);
+    Xf xfB = ldXf(a.xf, a.fbody[f.y]);
+    Man m;
+    evaluate(&m, sA, xfA, sB, xfB);
+    touching = m.pointCount > 0;
+    nm.type = m.type;
+    nm.point_count = m.pointCount;
+    nm.local_normal[0] = m.localNormal.x; nm.local_normal[1] = m.localNormal.y;
+    nm.local_point[0] = m.localPoint.x; nm.local_point[1] = m.localPoint.y;
+    for (int j = 0; j < 2; ++j) {
+      nm.points[j].local_point[0] = m.lp[j].x;
+      nm.points[j].local_point[1] = m.lp[j].y;
+      nm.points[j].id = m.id[j];
+      nm.points[j].normal_impulse = 0.0f;
+      nm.points[j].tangent_impulse = 0.0f;
+    }
+    for (int j = 0; j < m.pointCount; ++j) {
+      for (int k = 0; k < old.point_count; ++k) {
+        if (old.points[k].id == nm.points[j].id) {
+          nm.points[j].normal_impulse = old.points[k].normal_impulse;
+          nm.points[j].tangent_impulse = old.points[k].tangent_impulse;
+          break;
+        }
+      }
+    }
+  }
+  if (touching) flags |= B2G_CONTACT_TOUCHING;
+  else flags &= ~B2G_CONTACT_TOUCHING;
+  a.cman[i] = nm;
+  a.cflags[i] = flags;
+  if (a.events_on) {
+    int fo = a.wb[w].z;
+    if (!wasTouching && touching) record_event(a, B2G_EVENT_BEGIN, w, f.x - fo, f.y - fo, 0, 0, 0, 0);
+    if (wasTouching && !touching) record_event(a, B2G_EVENT_END, w, f.x - fo, f.y - fo, 0, 0, 0, 0);
+    if (!sensor && touching) record_event(a, B2G_EVENT_PRESOLVE, w, f.x - fo, f.y - fo, 0, 0, 0, &old);
+  }
+}
+
+// ================================================================================ solver
+// Block-wide exclusive scan of one int per thread (blockDim.x == SOLVER_THREADS).
+__device__ int block_scan(int v, int* total) {
+  __shared__ int warp_sums[SOLVER_THREADS / 32];
+  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  int x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    int y = __shfl_up_sync(FULL_MASK, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) warp_sums[wid] = x;
+  __syncthreads();
+  if (wid == 0) {
+    int s = lane < SOLVER_THREADS / 32 ? warp_sums[lane] : 0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      int y = __shfl_up_sync(FULL_MASK, s, o);
+      if (lane >= o) s += y;
+    }
+    if (lane < SOLVER_THREADS / 32) warp_sums[lane] = s;
+  }
+  __syncthreads();
+  int prefix = (wid > 0 ? warp_sums[wid - 1] : 0) + x - v;
+  *total = warp_sums[SOLVER_THREADS / 32 - 1];
+  __syncthreads();
+  return prefix;
+}
+
+// Greedy colouring in priority order, computed in parallel rounds (Jones-Plassmann with
+// smallest-free-colour choice): a constraint is coloured once it is the first uncoloured
+// constraint in the priority-sorted incidence list of each of its non-static bodies; it then takes
+// the lowest colour not used by those bodies. The result equals the sequential greedy pass in
+// priority order. Colours 0..62 are regular, 63 is the overflow colour solved serially.
+// Incidence lists must be sorted by (priority, index); list heads start at each list's first entry.
+__device__ void color_rounds(int n, int base, const int* bodyA, const int* bodyB, int bstride, const int* btype,
+                             const int* inc_list, int* inc_head, unsigned long long* inc_mask, int* color,
+                             uint8_t* ready, unsigned int* status) {
+  for (int round = 0; round <= n + 1; ++round) {
+    int any = 0;
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+      uint8_t r = 0;
+      if (color[base + k] < 0) {
+        any = 1;
+        int ia = bodyA[(int64_t)(base + k) * bstride], ib = bodyB[(int64_t)(base + k) * bstride];
+        bool ok = true;
+        if (btype[ia] != B2G_STATIC) ok = ok && inc_list[inc_head[ia]] == k;
+        if (btype[ib] != B2G_STATIC) ok = ok && inc_list[inc_head[ib]] == k;
+        r = ok ? 1 : 0;
+      }
+      ready[base + k] = r;
+    }
+    if (!__syncthreads_or(any)) return;
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+      if (!ready[base + k]) continue;
+      int ia = bodyA[(int64_t)(base + k) * bstride], ib = bodyB[(int64_t)(base + k) * bstride];
+      bool sa = btype[ia] == B2G_STATIC, sb = btype[ib] == B2G_STATIC;
+      unsigned long long used = (sa ? 0ull : inc_mask[ia]) | (sb ? 0ull : inc_mask[ib]);
+      unsigned long long freeBits = ~used & ((1ull << 63) - 1ull);
+      int col;
+      if (freeBits == 0ull) {
+        col = 63;
+      } else {
+        col = __ffsll((long long)freeBits) - 1;
+        if (!sa) inc_mask[ia] |= 1ull << col;
+        if (!sb) inc_mask[ib] |= 1ull << col;
+      }
+      color[base + k] = col;
+      if (!sa) inc_head[ia] += 1;
+      if (!sb) inc_head[ib] += 1;
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) raise_status(status, B2G_DEV_COLOR_ROUNDS);
+}
+
+// Builds priority-sorted incidence lists for n constraints over the world's bodies and colours
+// them; then buckets constraints by colour into `order` (overflow bucket sorted by priority).
+// Returns the number of colours used (max colour + 1) through smem.
+__device__ int color_and_order(int n, int base, int listBase, const int* bodyA, const int* bodyB, int bstride,
+                               const uint32_t* prio, const int* btype, int b0, int nb, int* inc_cnt, int* inc_off,
+                               int* inc_head, unsigned long long* inc_mask, int* inc_list, int* color, uint8_t* ready,
+                               int* order, unsigned int* status, int* ranges) {
+  __shared__ int col_cnt[64];
+  __shared__ int col_off[65];
+  __shared__ int s_carry;
+  __shared__ int s_maxcol;
+  for (int i = threadIdx.x; i < nb; i += blockDim.x) {
+    inc_cnt[b0 + i] = 0;
+    inc_mask[b0 + i] = 0ull;
+  }
+  __syncthreads();
+  for (int k = threadIdx.x; k < n; k += blockDim.x) {
+    color[base + k] = -1;
+    int ia = bodyA[(int64_t)(base + k) * bstride], ib = bodyB[(int64_t)(base + k) * bstride];
+    if (btype[ia] != B2G_STATIC) atomicAdd(&inc_cnt[ia], 1);
+    if (btype[ib] != B2G_STATIC) atomicAdd(&inc_cnt[ib], 1);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) s_carry = 0;
+  __syncthreads();
+  for (int c0 = 0; c0 < nb; c0 += blockDim.x) {
+    int i = c0 + threadIdx.x;
+    int v = i < nb ? inc_cnt[b0 + i] : 0;
+    int total;
+    int p = block_scan(v, &total);
+    if (i < nb) {
+      inc_off[b0 + i] = listBase + s_carry + p;
+      inc_head[b0 + i] = listBase + s_carry + p;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) s_carry += total;
+    __syncthreads();
+  }
+  for (int i = threadIdx.x; i < nb; i += blockDim.x) inc_cnt[b0 + i] = 0;
+  __syncthreads();
+  for (int k = threadIdx.x; k < n; k += blockDim.x) {
+    int ia = bodyA[(int64_t)(base + k) * bstride], ib = bodyB[(int64_t)(base + k) * bstride];
+    if (btype[ia] != B2G_STATIC) inc_list[inc_off[ia] + atomicAdd(&inc_cnt[ia], 1)] = k;
+    if (btype[ib] != B2G_STATIC) inc_list[inc_off[ib] + atomicAdd(&inc_cnt[ib], 1)] = k;
+  }
+  __syncthreads();
+  // sort each body's list by (priority, index)
+  for (int i = threadIdx.x; i < nb; i += blockDim.x) {
+    int off = inc_off[b0 + i], cnt = inc_cnt[b0 + i];
+    for (int x = 1; x < cnt; ++x) {
+      int kx = inc_list[off + x];
+      uint32_t px = prio[base + kx];
+      int y = x - 1;
+      while (y >= 0) {
+        int ky = inc_list[off + y];
+        uint32_t py = prio[base + ky];
+        if (py < px || (py == px && ky < kx)) break;
+        inc_list[off + y + 1] = ky;
+        --y;
+      }
+      inc_list[off + y + 1] = kx;
+    }
+  }
+  __syncthreads();
+  color_rounds(n, base, bodyA, bodyB, bstride, btype, inc_list, inc_head, inc_mask, color, ready, status);
+  // bucket by colour
+  if (threadIdx.x < 64) col_cnt[threadIdx.x] = 0;
+  if (threadIdx.x == 0) s_maxcol = -1;
+  __syncthreads();
+  for (int k = threadIdx.x; k < n; k += blockDim.x) {
+    int c = color[base + k];
+    atomicAdd(&col_cnt[c], 1);
+    atomicMax(&s_maxcol, c);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int s = 0;
+    for (int c = 0; c < 64; ++c) { col_off[c] = s; s += col_cnt[c]; col_cnt[c] = 0; }
+    col_off[64] = s;
+  }
+  __syncthreads();
+  for (int k = threadIdx.x; k < n; k += blockDim.x) {
+    int c = color[base + k];
+    order[base + col_off[c] + atomicAdd(&col_cnt[c], 1)] = k;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0 && col_cnt[63] > 1) {
+    int off = base + col_off[63], cnt = col_cnt[63];
+    for (int x = 1; x < cnt; ++x) {
+      int kx = order[off + x];
+      uint32_t px = prio[base + kx];
+      int y = x - 1;
+      while (y >= 0) {
+        int ky = order[off + y];
+        uint32_t py = prio[base + ky];
+        if (py < px || (py == px && ky < kx)) break;
+        order[off + y + 1] = ky;
+        --y;
+      }
+      order[off + y + 1] = kx;
+    }
+  }
+  int ncol = s_maxcol + 1;
+  for (int c = threadIdx.x; c <= ncol; c += blockDim.x) ranges[c] = col_off[c];
+  __syncthreads();
+  return ncol;
+}
+
+__global__ void __launch_bounds__(SOLVER_THREADS) k_solve(KernelArgs a) {
+  const int w = a.world_order[blockIdx.x];
+  if ((a.wflags[w] & B2G_WF_ACTIVE) == 0) return;
+  __shared__ int cranges[65];
+  __shared__ int jranges[65];
+  __shared__ int s_nsc;
+  __shared__ int s_carry;
+  const int4 wb = a.wb[w];
+  const int b0 = wb.x, nb = wb.y, fo = wb.z;
+  const int2 wc = a.wc[w];
+  const int c0 = wc.x, ncAll = wc.y;
+  const int4 wj = a.wj[w];
+  const int j0 = wj.x, nj = wj.y;
+  const float4 wg = a.wg[w];
+  const float h = a.dt;
+  const float dtRatio = wg.z * a.dt;
+  const bool warm = (a.wflags[w] & B2G_WF_WARM) != 0;
+  const V2 gravity = mk(wg.x, wg.y);
+
+  // 1. velocity integration (b2_island.cpp:256-293, SolveOrphan :187-206)
+  for (int i = threadIdx.x; i < nb; i += blockDim.x) {
+    int bi = b0 + i;
+    if (a.btype[bi] != B2G_DYNAMIC) continue;
+    float4 v4 = a.vel[bi];
+    float4 md = a.massd[bi];
+    float4 dmp = a.damp[bi];
+    float4 fr = a.force[bi];
+    V2 v = mk(v4.x, v4.y);
+    float wv = v4.z;
+    addTo(v, (h * md.y) * (dmp.z * md.x * gravity + mk(fr.x, fr.y)));
+    wv += h * md.w * fr.z;
+    v.x /= (1.0f + h * dmp.x);
+    v.y /= (1.0f + h * dmp.x);
+    wv /= (1.0f + h * dmp.y);
+    a.vel[bi] = make_float4(v.x, v.y, wv, 0.0f);
+  }
+  if (threadIdx.x == 0) s_carry = 0;
+  __syncthreads();
+
+  // 2. solver contacts: touching, enabled, no sensor (b2_world.cpp:567-599), compacted in order
+  for (int k0 = 0; k0 < ncAll; k0 += blockDim.x) {
+    int k = k0 + threadIdx.x;
+    int flag = 0;
+    if (k < ncAll) {
+      int ci = c0 + k;
+      uint32_t fl = a.cflags[ci];
+      int2 f = a.cfix[ci];
+      flag = ((fl & B2G_CONTACT_TOUCHING) && (fl & B2G_CONTACT_ENABLED) && !a.fsensor[f.x] && !a.fsensor[f.y]) ? 1 : 0;
+    }
+    int total;
+    int p = block_scan(flag, &total);
+    if (flag) a.sc_list[c0 + s_carry + p] = c0 + k;
+    __syncthreads();
+    if (threadIdx.x == 0) s_carry += total;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) s_nsc = s_carry;
+  __syncthreads();
+  const int nsc = s_nsc;
+
+  // 3. prepare (b2ContactSolver::Initialize + InitializeVelocityConstraints) and priorities
+  for (int k = threadIdx.x; k < nsc; k += blockDim.x) {
+    int ci = a.sc_list[c0 + k];
+    int2 f = a.cfix[ci];
+    int ia = a.fbody[f.x], ib = a.fbody[f.y];
+    b2g_manifold m = a.cman[ci];
+    VCDev vc;
+    prepareContact(vc, m, a.cmat[ci], a.shape[f.x].radius, a.shape[f.y].radius, ia, ib, a.massd[ia], a.massd[ib],
+                   a.lc[ia], a.lc[ib], a.pos[ia], a.vel[ia], a.pos[ib], a.vel[ib], dtRatio, warm, ci);
+    a.vc[c0 + k] = vc;
+    uint64_t key = a.ckey[ci];
+    a.cprio[c0 + k] = contactPriority((uint32_t)(key >> 32) - (uint32_t)fo, (uint32_t)key - (uint32_t)fo);
+  }
+  __syncthreads();
+
+  // 4. colouring of contacts and joints
+  int ncc = 0, njc = 0;
+  if (nsc > 0) {
+    ncc = color_and_order(nsc, c0, 2 * c0, &a.vc[0].indexA, &a.vc[0].indexB, (int)(sizeof(VCDev) / sizeof(int)),
+                          a.cprio, a.btype, b0, nb, a.inc_cnt, a.inc_off, a.inc_head, a.inc_mask, a.inc_list,
+                          a.ccolor, a.cready, a.corder, a.status, cranges);
+  }
+  if (nj > 0) {
+    for (int k = threadIdx.x; k < nj; k += blockDim.x) a.jprio[j0 + k] = jointPriority((uint32_t)k);
+    __syncthreads();
+    njc = color_and_order(nj, j0, 2 * j0, &a.joints[0].d.body_a, &a.joints[0].d.body_b,
+                          (int)(sizeof(JointDev) / sizeof(int)), a.jprio, a.btype, b0, nb, a.inc_cnt, a.inc_off,
+                          a.inc_head, a.inc_mask, a.jinc_list, a.jcolor, a.jready, a.jorder, a.status, jranges);
+  }
+  if (threadIdx.x == 0) {
+    a.ncolors[2 * w] = ncc;
+    a.ncolors[2 * w + 1] = njc;
+  }
+
+  // 5. warm start contacts, then joint InitVelocityConstraints, colour by colour
+  if (warm) {
+    for (int c = 0; c < ncc; ++c) {
+      int s = cranges[c], e = cranges[c + 1];
+      if (c == 63) {
+        if (threadIdx.x == 0)
+          for (int i = s; i < e; ++i) warmStartContact(a.vc[c0 + a.corder[c0 + i]], a.vel);
+      } else {
+        for (int i = s + threadIdx.x; i < e; i += blockDim.x) warmStartContact(a.vc[c0 + a.corder[c0 + i]], a.vel);
+      }
+      __syncthreads();
+    }
+  }
+  for (int c = 0; c < njc; ++c) {
+    int s = jranges[c], e = jranges[c + 1];
+    if (c == 63) {
+      if (threadIdx.x == 0)
+        for (int i = s; i < e; ++i)
+          jointInit(a.joints[j0 + a.jorder[j0 + i]], a.massd, a.lc, a.pos, a.vel, a.dt, dtRatio, warm);
+    } else {
+      for (int i = s + threadIdx.x; i < e; i += blockDim.x)
+        jointInit(a.joints[j0 + a.jorder[j0 + i]], a.massd, a.lc, a.pos, a.vel, a.dt, dtRatio, warm);
+    }
+    __syncthreads();
+  }
+
+  // 6. velocity iterations: joints, then contacts (b2_island.cpp:327-346)
+  for (int it = 0; it < a.vi; ++it) {
+    for (int c = 0; c < njc; ++c) {
+      int s = jranges[c], e = jranges[c + 1];
+      if (c == 63) {
+        if (threadIdx.x == 0)
+          for (int i = s; i < e; ++i) jointSolveVelocity(a.joints[j0 + a.jorder[j0 + i]], a.vel, a.dt, a.inv_dt);
+      } else {
+        for (int i = s + threadIdx.x; i < e; i += blockDim.x)
+          jointSolveVelocity(a.joints[j0 + a.jorder[j0 + i]], a.vel, a.dt, a.inv_dt);
+      }
+      __syncthreads();
+    }
+    for (int c = 0; c < ncc; ++c) {
+      int s = cranges[c], e = cranges[c + 1];
+      if (c == 63) {
+        if (threadIdx.x == 0)
+          for (int i = s; i < e; ++i) solveContactVelocity(a.vc[c0 + a.corder[c0 + i]], a.vel);
+      } else {
+        for (int i = s + threadIdx.x; i < e; i += blockDim.x) solveContactVelocity(a.vc[c0 + a.corder[c0 + i]], a.vel);
+      }
+      __syncthreads();
+    }
+  }
+
+  // 7. StoreImpulses (b2_contact_solver.cpp:641-657) and PostSolve reports
+  for (int k = threadIdx.x; k < nsc; k += blockDim.x) {
+    const VCDev& vc = a.vc[c0 + k];
+    b2g_manifold* m = &a.cman[vc.contact];
+    for (int j = 0; j < vc.pointCount; ++j) {
+      m->points[j].normal_impulse = vc.normalImpulse[j];
+      m->points[j].tangent_impulse = vc.tangentImpulse[j];
+    }
+  }
+
+  // 8. integrate positions (b2_island.cpp:349-385)
+  for (int i = threadIdx.x; i < nb; i += blockDim.x) {
+    int bi = b0 + i;
+    if (a.btype[bi] == B2G_STATIC) continue;
+    float4 p4 = a.pos[bi];
+    float4 v4 = a.vel[bi];
+    V2 c = mk(p4.x, p4.y);
+    float an = p4.z;
+    V2 v = mk(v4.x, v4.y);
+    float wv = v4.z;
+    V2 translation = h * v;
+    if (dot(translation, translation) > B2G_MAX_TRANSLATION_SQ) {
+      float ratio = B2G_MAX_TRANSLATION / lengthOf(translation);
+      v.x *= ratio;
+      v.y *= ratio;
+    }
+    float rotation = h * wv;
+    if (rotation * rotation > B2G_MAX_ROTATION_SQ) {
+      float ratio = B2G_MAX_ROTATION / fabs2(rotation);
+      wv *= ratio;
+    }
+    addTo(c, h * v);
+    an += h * wv;
+    a.pos[bi] = make_float4(c.x, c.y, an, 0.0f);
+    a.vel[bi] = make_float4(v.x, v.y, wv, 0.0f);
+  }
+  __syncthreads();
+
+  // 9. position iterations: contacts then joints, early exit for the world (b2_island.cpp:387-428)
+  for (int it = 0; it < a.pi; ++it) {
+    int okay = 1;
+    for (int c = 0; c < ncc; ++c) {
+      int s = cranges[c], e = cranges[c + 1];
+      if (c == 63) {
+        if (threadIdx.x == 0)
+          for (int i = s; i < e; ++i)
+            if (!(solveContactPosition(a.vc[c0 + a.corder[c0 + i]], a.pos) >= -3.0f * B2G_LINEAR_SLOP)) okay = 0;
+      } else {
+        for (int i = s + threadIdx.x; i < e; i += blockDim.x)
+          if (!(solveContactPosition(a.vc[c0 + a.corder[c0 + i]], a.pos) >= -3.0f * B2G_LINEAR_SLOP)) okay = 0;
+      }
+      __syncthreads();
+    }
+    for (int c = 0; c < njc; ++c) {
+      int s = jranges[c], e = jranges[c + 1];
+      if (c == 63) {
+        if (threadIdx.x == 0)
+          for (int i = s; i < e; ++i)
+            if (!jointSolvePosition(a.joints[j0 + a.jorder[j0 + i]], a.pos)) okay = 0;
+      } else {
+        for (int i = s + threadIdx.x; i < e; i += blockDim.x)
+          if (!jointSolvePosition(a.joints[j0 + a.jorder[j0 + i]], a.pos)) okay = 0;
+      }
+      __syncthreads();
+    }
+    if (__syncthreads_and(okay)) break;
+  }
+
+  // 10. transforms (b2Body::SynchronizeTransform, include/box2d/b2_body.h:957-961), finite check
+  int bad = 0;
+  for (int i = threadIdx.x; i < nb; i += blockDim.x) {
+    int bi = b0 + i;
+    if (a.btype[bi] == B2G_STATIC) continue;
+    float4 p4 = a.pos[bi];
+    Rot q = rotOf(p4.z);
+    float2 l = a.lc[bi];
+    V2 p = mk(p4.x, p4.y) - mul(q, mk(l.x, l.y));
+    a.xf[bi] = make_float4(p.x, p.y, q.s, q.c);
+    float4 v4 = a.vel[bi];
+    if (!isfinite(p4.x) || !isfinite(p4.y) || !isfinite(p4.z) || !isfinite(v4.x) || !isfinite(v4.y) || !isfinite(v4.z))
+      bad = 1;
+  }
+  if (__syncthreads_or(bad) && threadIdx.x == 0) raise_status(a.status, B2G_DEV_NONFINITE);
+  if (a.events_on) {
+    for (int k = threadIdx.x; k < nsc; k += blockDim.x) {
+      const VCDev& vc = a.vc[c0 + k];
+      int2 f = a.cfix[vc.contact];
+      record_event(a, B2G_EVENT_POSTSOLVE, w, f.x - fo, f.y - fo, vc.pointCount, vc.normalImpulse, vc.tangentImpulse, 0);
+    }
+  }
+  if (threadIdx.x == 0 && a.dt > 0.0f) a.wg[w].z = a.inv_dt;
+}
+
+__global__ void k_clear_forces(KernelArgs a, int nbodies) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nbodies) return;
+  int w = a.bworld[i];
+  int wf = a.wflags[w];
+  if ((wf & B2G_WF_ACTIVE) && (wf & B2G_WF_CLEAR_FORCES)) a.force[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+}
+
+// ================================================================================ broadphase
+__global__ void k_aabb(KernelArgs a, int n) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  AABB bb = shapeAABB(a.shape[i], ldXf(a.xf, a.fbody[i]));
+  a.aabb[i] = make_float4(bb.lo.x, bb.lo.y, bb.hi.x, bb.hi.y);
+}
+
+// Per-world bounds of AABB centres (lower + upper, the reference's GetCenter2) for Morton codes.
+__global__ void k_world_bounds(KernelArgs a) {
+  int w = blockIdx.x;
+  int4 wb = a.wb[w];
+  float mnx = B2G_MAX_FLOAT, mny = B2G_MAX_FLOAT, mxx = -B2G_MAX_FLOAT, mxy = -B2G_MAX_FLOAT;
+  for (int i = threadIdx.x; i < wb.w; i += blockDim.x) {
+    float4 bb = a.aabb[wb.z + i];
+    float cx = bb.x + bb.z, cy = bb.y + bb.w;
+    mnx = fminf(mnx, cx); mny = fminf(mny, cy); mxx = fmaxf(mxx, cx); mxy = fmaxf(mxy, cy);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    mnx = fminf(mnx, __shfl_xor_sync(FULL_MASK, mnx, o));
+    mny = fminf(mny, __shfl_xor_sync(FULL_MASK, mny, o));
+    mxx = fmaxf(mxx, __shfl_xor_sync(FULL_MASK, mxx, o));
+    mxy = fmaxf(mxy, __shfl_xor_sync(FULL_MASK, mxy, o));
+  }
+  __shared__ float s[4][32];
+  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) { s[0][wid] = mnx; s[1][wid] = mny; s[2][wid] = mxx; s[3][wid] = mxy; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int nw = (blockDim.x + 31) / 32;
+    for (int k = 1; k < nw; ++k) {
+      mnx = fminf(mnx, s[0][k]); mny = fminf(mny, s[1][k]); mxx = fmaxf(mxx, s[2][k]); mxy = fmaxf(mxy, s[3][k]);
+    }
+    a.wbounds[w] = make_float4(mnx, mny, mxx, mxy);
+  }
+}
+
+__device__ __forceinline__ uint32_t expand_bits15(uint32_t v) {
+  v &= 0x7fffu;
+  v = (v | (v << 8)) & 0x00ff00ffu;
+  v = (v | (v << 4)) & 0x0f0f0f0fu;
+  v = (v | (v << 2)) & 0x33333333u;
+  v = (v | (v << 1)) & 0x55555555u;
+  return v;
+}
+
+// 30-bit Morton code of the AABB centre normalised to its world's bounds; sort key
+// world << 32 | code so that each world's fixtures form one contiguous sorted range.
+__global__ void k_morton(KernelArgs a, int n) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  int w = a.fworld[i];
+  float4 wbnd = a.wbounds[w];
+  float4 bb = a.aabb[i];
+  float cx = bb.x + bb.z, cy = bb.y + bb.w;
+  float ex = fmaxf(wbnd.z - wbnd.x, 1e-30f), ey = fmaxf(wbnd.w - wbnd.y, 1e-30f);
+  float ux = fminf(fmaxf((cx - wbnd.x) / ex, 0.0f), 1.0f);
+  float uy = fminf(fmaxf((cy - wbnd.y) / ey, 0.0f), 1.0f);
+  uint32_t qx = (uint32_t)fminf(ux * 32768.0f, 32767.0f);
+  uint32_t qy = (uint32_t)fminf(uy * 32768.0f, 32767.0f);
+  uint32_t code = (expand_bits15(qx) << 1) | expand_bits15(qy);
+  a.mkey[i] = ((uint64_t)(uint32_t)w << 32) | code;
+  a.mval[i] = i;
+}
+
+__device__ __forceinline__ int lbvh_delta(const uint64_t* k, int n, int i, int j) {
+  if (j < 0 || j >= n) return -1;
+  uint64_t x = k[i], y = k[j];
+  if (x == y) return 64 + __clz((unsigned)(i ^ j));
+  return __clzll((long long)(x ^ y));
+}
+
+// Karras (2012) binary radix tree: internal node i covers a range of sorted leaves; its split is
+// the highest differing bit. The node whose range is exactly a world's fixtures is that world's root.
+__global__ void k_lbvh_internal(KernelArgs a, int n) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n - 1) return;
+  const uint64_t* k = a.mkey_sorted;
+  int d = (lbvh_delta(k, n, i, i + 1) - lbvh_delta(k, n, i, i - 1)) >= 0 ? 1 : -1;
+  int dmin = lbvh_delta(k, n, i, i - d);
+  int lmax = 2;
+  while (lbvh_delta(k, n, i, i + lmax * d) > dmin) lmax *= 2;
+  int l = 0;
+  for (int t = lmax / 2; t >= 1; t /= 2)
+    if (lbvh_delta(k, n, i, i + (l + t) * d) > dmin) l += t;
+  int j = i + l * d;
+  int dnode = lbvh_delta(k, n, i, j);
+  int s = 0;
+  int t = l;
+  do {
+    t = (t + 1) >> 1;
+    if (lbvh_delta(k, n, i, i + (s + t) * d) > dnode) s += t;
+  } while (t > 1);
+  int gamma = i + s * d + min(d, 0);
+  int lo = min(i, j), hi = max(i, j);
+  int left = (lo == gamma) ? (int)(gamma | LEAF_BIT) : gamma;
+  int right = (hi == gamma + 1) ? (int)((gamma + 1) | LEAF_BIT) : gamma + 1;
+  a.nchild[i] = make_int2(left, right);
+  if (lo == gamma) a.lparent[gamma] = i; else a.nparent[gamma] = i;
+  if (hi == gamma + 1) a.lparent[gamma + 1] = i; else a.nparent[gamma + 1] = i;
+  int w = (int)(k[lo] >> 32);
+  if ((int)(k[hi] >> 32) == w) {
+    int4 wb = a.wb[w];
+    if (lo == wb.z && hi == wb.z + wb.w - 1) a.wroot[w] = i;
+  }
+}
+
+__global__ void k_lbvh_init(KernelArgs a, int n, int nw) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) {
+    a.lparent[i] = -1;
+    if (i < n - 1) {
+      a.nparent[i] = -1;
+      a.nflag[i] = 0;
+    }
+  }
+  if (i < nw) {
+    int4 wb = a.wb[i];
+    a.wroot[i] = wb.w == 1 ? (int)(wb.z | LEAF_BIT) : -1;
+  }
+}
+
+// Bottom-up node bounds: the second thread to reach a node combines its children.
+__global__ void k_lbvh_bounds(KernelArgs a, int n) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  int p = a.lparent[i];
+  int guard = 0;
+  while (p >= 0) {
+    if (++guard > 256) {  // deeper than any valid tree over 2^31 leaves: the tree is malformed
+      raise_status(a.status, B2G_DEV_STACK_OVERFLOW);
+      return;
+    }
+    __threadfence();
+    if (atomicAdd(&a.nflag[p], 1) == 0) return;
+    __threadfence();
+    int2 ch = a.nchild[p];
+    float4 l = (ch.x & LEAF_BIT) ? a.aabb[a.mval_sorted[ch.x & ~LEAF_BIT]] : __ldcg(&a.naabb[ch.x]);
+    float4 r = (ch.y & LEAF_BIT) ? a.aabb[a.mval_sorted[ch.y & ~LEAF_BIT]] : __ldcg(&a.naabb[ch.y]);
+    float4 u = make_float4(fminf(l.x, r.x), fminf(l.y, r.y), fmaxf(l.z, r.z), fmaxf(l.w, r.w));
+    __stcg(&a.naabb[p], u);
+    p = a.nparent[p];
+  }
+}
+
+__device__ __forceinline__ bool aabb_overlap4(float4 a, float4 b) {
+  return (a.z >= b.x) & (a.x <= b.z) & (a.w >= b.y) & (a.y <= b.w);
+}
+
+__device__ __forceinline__ bool nocollide_has(const uint64_t* keys, int n, uint64_t key) {
+  int lo = 0, hi = n;
+  while (lo < hi) {
+    int mid = (lo + hi) >> 1;
+    if (keys[mid] < key) lo = mid + 1; else hi = mid;
+  }
+  return lo < n && keys[lo] == key;
+}
+
+// Would fixture f (non-static, the emitter) report the pair (f, g)? Emitter rule: the non-static
+// fixture of a static pair, else the lower index. Filters of b2ContactManager::QueryCallback:
+// same body, b2Body::ShouldCollide (a dynamic body, no collideConnected=false joint), the default
+// b2ContactFilter (group / category / mask) and the collider table.
+__device__ __forceinline__ bool accept_pair(const KernelArgs& a, int f, int g, int bf, int tf) {
+  if (g == f) return false;
+  int bg = a.fbody[g];
+  if (bg == bf) return false;
+  int tg = a.btype[bg];
+  if (tg != B2G_STATIC && g < f) return false;
+  if (tf != B2G_DYNAMIC && tg != B2G_DYNAMIC) return false;
+  if (a.n_nocollide > 0) {
+    uint32_t x = (uint32_t)min(bf, bg), y = (uint32_t)max(bf, bg);
+    if (nocollide_has(a.nocollide, a.n_nocollide, ((uint64_t)x << 32) | y)) return false;
+  }
+  int gf = a.fgroup[f], gg = a.fgroup[g];
+  if (gf == gg && gf != 0) {
+    if (!(gf > 0)) return false;
+  } else {
+    uint32_t ff = a.ffilter[f], fg = a.ffilter[g];
+    uint32_t catF = ff & 0xffffu, maskF = ff >> 16, catG = fg & 0xffffu, maskG = fg >> 16;
+    if (!((maskF & catG) != 0 && (catF & maskG) != 0)) return false;
+  }
+  int sf = a.shape[f].type, sg = a.shape[g].type;
+  return hasCollider(sf, sg) || hasCollider(sg, sf);
+}
+
+#define BP_STACK 64
+
+// Pair search for one emitter fixture over its world's subtree. Count mode writes the number of
+// accepted partners; emit mode writes the keys f << 32 | g at the scanned offset and sorts them.
+template <bool EMIT>
+__global__ void k_pairs(KernelArgs a, int n) {
+  int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= n) return;
+  int bf = a.fbody[f];
+  int tf = a.btype[bf];
+  int cnt = 0;
+  int64_t off = 0;
+  if (EMIT) {
+    off = a.poff[f];
+    if (a.poff[f + 1] == off) return;
+  }
+  if (tf != B2G_STATIC) {
+    int w = a.fworld[f];
+    int root = a.wroot[w];
+    if (root >= 0 && !(root & LEAF_BIT)) {
+      float4 box = a.aabb[f];
+      int stack[BP_STACK];
+      int sp = 0;
+      stack[sp++] = root;
+      int visits = 0;
+      const int maxVisits = 2 * a.wb[w].w + 8;  // each internal node of the world at most once
+      while (sp > 0) {
+        if (++visits > maxVisits) {
+          raise_status(a.status, B2G_DEV_STACK_OVERFLOW);
+          break;
+        }
+        int node = stack[--sp];
+        int2 ch = a.nchild[node];
+        int kids[2] = {ch.x, ch.y};
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+          int c = kids[q];
+          if (c & LEAF_BIT) {
+            int g = a.mval_sorted[c & ~LEAF_BIT];
+            if (aabb_overlap4(box, a.aabb[g]) && accept_pair(a, f, g, bf, tf)) {
+              if (EMIT) a.pairs[off + cnt] = ((uint64_t)(uint32_t)f << 32) | (uint32_t)g;
+              ++cnt;
+            }
+          } else if (aabb_overlap4(box, a.naabb[c])) {
+            if (sp < BP_STACK) stack[sp++] = c;
+            else raise_status(a.status, B2G_DEV_STACK_OVERFLOW);
+          }
+        }
+      }
+    }
+  }
+  if (!EMIT) {
+    a.pcount[f] = cnt;
+  } else {
+    uint64_t* seg = a.pairs + off;
+    for (int x = 1; x < cnt; ++x) {
+      uint64_t v = seg[x];
+      int y = x - 1;
+      while (y >= 0 && seg[y] > v) { seg[y + 1] = seg[y]; --y; }
+      seg[y + 1] = v;
+    }
+  }
+}
+
+__global__ void k_world_contacts(KernelArgs a, int nw) {
+  int w = blockIdx.x * blockDim.x + threadIdx.x;
+  if (w >= nw) return;
+  int4 wb = a.wb[w];
+  int s = a.poff[wb.z], e = a.poff[wb.z + wb.w];
+  a.wc[w] = make_int2(s, e - s);
+}
+
+__device__ __forceinline__ int64_t find_key(const uint64_t* keys, int64_t n, uint64_t key) {
+  int64_t lo = 0, hi = n;
+  while (lo < hi) {
+    int64_t mid = (lo + hi) >> 1;
+    if (keys[mid] < key) lo = mid + 1; else hi = mid;
+  }
+  return (lo < n && keys[lo] == key) ? lo : -1;
+}
+
+// New contact list = the new pair list; persisting contacts keep their orientation, flags,
+// mixed material and manifold (impulses included); new ones are created like b2Contact's
+// constructor (src/dynamics/b2_contact.cpp:96-122) in b2Contact::Create's orientation.
+__global__ void k_contact_diff(KernelArgs a, int64_t nnew, int64_t nold, int src, int dst) {
+  int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nnew) return;
+  uint64_t key = a.pairs[k];
+  int64_t o = find_key(a.ckeyB[src], nold, key);
+  a.ckeyB[dst][k] = key;
+  if (o >= 0) {
+    a.cfixB[dst][k] = a.cfixB[src][o];
+    a.cflagsB[dst][k] = a.cflagsB[src][o];
+    a.cmatB[dst][k] = a.cmatB[src][o];
+    a.cmanB[dst][k] = a.cmanB[src][o];
+  } else {
+    int e = (int)(key >> 32), p = (int)(uint32_t)key;
+    int fa, fb;
+    if (hasCollider(a.shape[e].type, a.shape[p].type)) { fa = e; fb = p; }
+    else { fa = p; fb = e; }
+    float4 ma = a.fmat[fa], mb = a.fmat[fb];
+    a.cfixB[dst][k] = make_int2(fa, fb);
+    a.cflagsB[dst][k] = B2G_CONTACT_ENABLED;
+    a.cmatB[dst][k] = make_float4(sqrtf(ma.x * mb.x), ma.y > mb.y ? ma.y : mb.y, ma.z < mb.z ? ma.z : mb.z, 0.0f);
+    b2g_manifold m;
+    memset(&m, 0, sizeof(m));
+    a.cmanB[dst][k] = m;
+  }
+}
+
+// Contacts that disappeared: EndContact if they were touching (b2ContactManager::Destroy,
+// src/dynamics/b2_contact_manager.cpp:48-61).
+__global__ void k_contact_dead(KernelArgs a, int64_t nnew, int64_t nold, int src) {
+  int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nold) return;
+  uint64_t key = a.ckeyB[src][k];
+  if (find_key(a.pairs, nnew, key) >= 0) return;
+  if ((a.cflagsB[src][k] & B2G_CONTACT_TOUCHING) == 0) return;
+  int2 f = a.cfixB[src][k];
+  int w = a.fworld[f.x];
+  int fo = a.wb[w].z;
+  record_event(a, B2G_EVENT_END, w, f.x - fo, f.y - fo, 0, 0, 0, 0);
+}
+
+// ================================================================================ standalone
+__global__ void k_collide_pairs(const b2g_shape* sa, const float* xa, const b2g_shape* sb, const float* xb, int n,
+                                b2g_manifold* out) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  Xf A, B;
+  A.p = mk(xa[4 * i], xa[4 * i + 1]); A.q.s = xa[4 * i + 2]; A.q.c = xa[4 * i + 3];
+  B.p = mk(xb[4 * i], xb[4 * i + 1]); B.q.s = xb[4 * i + 2]; B.q.c = xb[4 * i + 3];
+  Man m;
+  evaluate(&m, sa[i], A, sb[i], B);
+  b2g_manifold r;
+  r.type = m.type;
+  r.point_count = m.pointCount;
+  r.local_normal[0] = m.localNormal.x; r.local_normal[1] = m.localNormal.y;
+  r.local_point[0] = m.localPoint.x; r.local_point[1] = m.localPoint.y;
+  for (int j = 0; j < 2; ++j) {
+    r.points[j].local_point[0] = m.lp[j].x;
+    r.points[j].local_point[1] = m.lp[j].y;
+    r.points[j].id = m.id[j];
+    r.points[j].normal_impulse = 0.0f;
+    r.points[j].tangent_impulse = 0.0f;
+  }
+  out[i] = r;
+}
+
+// ================================================================================ launchers
+static inline unsigned grid_for(int64_t n, int bs) { return (unsigned)((n + bs - 1) / bs); }
+
+void launch_collide(const KernelArgs& a, int64_t n, cudaStream_t s) {
+  if (n > 0) k_collide<<<grid_for(n, 128), 128, 0, s>>>(a, n);
+}
+void launch_solve(const KernelArgs& a, int nw, cudaStream_t s) {
+  if (nw > 0) k_solve<<<nw, SOLVER_THREADS, 0, s>>>(a);
+}
+void launch_clear_forces(const KernelArgs& a, int nb, cudaStream_t s) {
+  if (nb > 0) k_clear_forces<<<grid_for(nb, 256), 256, 0, s>>>(a, nb);
+}
+void launch_bp_build(const KernelArgs& a, int nf, int nw, size_t cub_bytes, int sort_bits, cudaStream_t s) {
+  if (nf <= 0) return;
+  k_aabb<<<grid_for(nf, 128), 128, 0, s>>>(a, nf);
+  k_world_bounds<<<nw, 256, 0, s>>>(a);
+  k_morton<<<grid_for(nf, 256), 256, 0, s>>>(a, nf);
+  size_t bytes = cub_bytes;
+  cub::DeviceRadixSort::SortPairs(a.cub_tmp, bytes, a.mkey, a.mkey_sorted, a.mval, a.mval_sorted, nf, 0, sort_bits, s);
+  int m = nf > nw ? nf : nw;
+  k_lbvh_init<<<grid_for(m, 256), 256, 0, s>>>(a, nf, nw);
+  if (nf > 1) {
+    k_lbvh_internal<<<grid_for(nf - 1, 256), 256, 0, s>>>(a, nf);
+    k_lbvh_bounds<<<grid_for(nf, 256), 256, 0, s>>>(a, nf);
+  }
+  k_pairs<false><<<grid_for(nf, 128), 128, 0, s>>>(a, nf);
+  bytes = cub_bytes;
+  cub::DeviceScan::ExclusiveSum(a.cub_tmp, bytes, a.pcount, a.poff, nf + 1, s);
+  k_world_contacts<<<grid_for(nw, 128), 128, 0, s>>>(a, nw);
+}
+void launch_bp_emit(const KernelArgs& a, int nf, cudaStream_t s) {
+  if (nf > 0) k_pairs<true><<<grid_for(nf, 128), 128, 0, s>>>(a, nf);
+}
+void launch_contact_diff(const KernelArgs& a, int64_t nnew, int64_t nold, int src, int dst, cudaStream_t s) {
+  if (nnew > 0) k_contact_diff<<<grid_for(nnew, 256), 256, 0, s>>>(a, nnew, nold, src, dst);
+  if (nold > 0 && a.events_on) k_contact_dead<<<grid_for(nold, 256), 256, 0, s>>>(a, nnew, nold, src);
+}
+size_t cub_temp_bytes(int nf) {
+  size_t b1 = 0, b2 = 0;
+  cub::DeviceRadixSort::SortPairs((void*)nullptr, b1, (uint64_t*)nullptr, (uint64_t*)nullptr, (int*)nullptr,
+                                  (int*)nullptr, nf, 0, 64);
+  cub::DeviceScan::ExclusiveSum((void*)nullptr, b2, (int*)nullptr, (int*)nullptr, nf + 1);
+  return (b1 > b2 ? b1 : b2) + 256;
+}
+void launch_collide_pairs(const b2g_shape* sa, const float* xa, const b2g_shape* sb, const float* xb, int n,
+                          b2g_manifold* out, cudaStream_t s) {
+  if (n > 0) k_collide_pairs<<<grid_for(n, 128), 128, 0, s>>>(sa, xa, sb, xb, n, out);
+}
+
+}  // namespace b2g

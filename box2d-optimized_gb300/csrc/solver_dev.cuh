@@ -1,0 +1,738 @@
+// solver_dev.cuh - per-constraint device routines of the sequential-impulse solver.
+//
+// Contact constraints: b2ContactSolver (src/dynamics/b2_contact_solver.cpp) split per
+// constraint: prepare (Initialize + InitializeVelocityConstraints, :65-258), warm start
+// (:260-299), velocity solve with the 2-point block solver (:301-639), position solve
+// (:659-787). Joints: b2RevoluteJoint, b2PrismaticJoint and b2DistanceJoint
+// Init/SolveVelocity/SolvePosition. Each routine reads and writes only its two bodies, so
+// constraints of one colour run concurrently. Operation order follows the reference.
+#pragma once
+
+#include "b2g_math.cuh"
+#include "engine.h"
+
+namespace b2g {
+
+struct SBody {
+  V2 c; float a; V2 v; float w;
+};
+
+B2G_HD V2 ld2(const float* p) { return mk(p[0], p[1]); }
+B2G_HD void st2(float* p, V2 v) { p[0] = v.x; p[1] = v.y; }
+
+// Prepare one contact constraint from its manifold and the (velocity-integrated) body state.
+B2G_HD void prepareContact(VCDev& vc, const b2g_manifold& m, float4 mat, float radiusA, float radiusB,
+                           int ia, int ib, float4 massA, float4 massB, float2 lcA, float2 lcB, float4 posA,
+                           float4 velA, float4 posB, float4 velB, float dtRatio, bool warm, int contact) {
+  vc.friction = mat.x;
+  float restitution = mat.y;
+  float threshold = mat.z;
+  vc.tangentSpeed = mat.w;
+  vc.indexA = ia;
+  vc.indexB = ib;
+  vc.invMassA = massA.y;
+  vc.invMassB = massB.y;
+  vc.invIA = massA.w;
+  vc.invIB = massB.w;
+  vc.pointCount = m.point_count;
+  vc.contact = contact;
+  vc.localCenterA[0] = lcA.x; vc.localCenterA[1] = lcA.y;
+  vc.localCenterB[0] = lcB.x; vc.localCenterB[1] = lcB.y;
+  vc.localNormal[0] = m.local_normal[0]; vc.localNormal[1] = m.local_normal[1];
+  vc.localPoint[0] = m.local_point[0]; vc.localPoint[1] = m.local_point[1];
+  vc.pcPointCount = m.point_count;
+  vc.radiusA = radiusA;
+  vc.radiusB = radiusB;
+  vc.type = m.type;
+  for (int j = 0; j < 2; ++j) {
+    vc.normalImpulse[j] = 0.0f; vc.tangentImpulse[j] = 0.0f;
+    vc.normalMass[j] = 0.0f; vc.tangentMass[j] = 0.0f; vc.velocityBias[j] = 0.0f;
+    vc.rA[j][0] = vc.rA[j][1] = vc.rB[j][0] = vc.rB[j][1] = 0.0f;
+    vc.localPoints[j][0] = m.points[j].local_point[0];
+    vc.localPoints[j][1] = m.points[j].local_point[1];
+  }
+  for (int j = 0; j < m.point_count; ++j) {
+    if (warm) {
+      vc.normalImpulse[j] = dtRatio * m.points[j].normal_impulse;
+      vc.tangentImpulse[j] = dtRatio * m.points[j].tangent_impulse;
+    }
+  }
+  // InitializeVelocityConstraints
+  float mA = vc.invMassA, mB = vc.invMassB, iA = vc.invIA, iB = vc.invIB;
+  V2 cA = mk(posA.x, posA.y); float aA = posA.z; V2 vA = mk(velA.x, velA.y); float wA = velA.z;
+  V2 cB = mk(posB.x, posB.y); float aB = posB.z; V2 vB = mk(velB.x, velB.y); float wB = velB.z;
+  Xf xfA, xfB;
+  xfA.q = rotOf(aA);
+  xfB.q = rotOf(aB);
+  xfA.p = cA - mul(xfA.q, ld2(vc.localCenterA));
+  xfB.p = cB - mul(xfB.q, ld2(vc.localCenterB));
+  WorldMan wm;
+  V2 lp[2] = {ld2(vc.localPoints[0]), ld2(vc.localPoints[1])};
+  wm.normal = mk(0.0f, 0.0f);
+  wm.points[0] = wm.points[1] = mk(0.0f, 0.0f);
+  worldManifold(&wm, m.type, m.point_count, ld2(vc.localNormal), ld2(vc.localPoint), lp, xfA, radiusA, xfB, radiusB);
+  V2 normal = wm.normal;
+  st2(vc.normal, normal);
+  V2 tangent = cross(normal, 1.0f);
+  for (int j = 0; j < vc.pointCount; ++j) {
+    V2 rA = wm.points[j] - cA;
+    V2 rB = wm.points[j] - cB;
+    st2(vc.rA[j], rA);
+    st2(vc.rB[j], rB);
+    float rnA = cross(rA, normal);
+    float rnB = cross(rB, normal);
+    float kNormal = mA + mB + iA * rnA * rnA + iB * rnB * rnB;
+    vc.normalMass[j] = kNormal > 0.0f ? 1.0f / kNormal : 0.0f;
+    float rtA = cross(rA, tangent);
+    float rtB = cross(rB, tangent);
+    float kTangent = mA + mB + iA * rtA * rtA + iB * rtB * rtB;
+    vc.tangentMass[j] = kTangent > 0.0f ? 1.0f / kTangent : 0.0f;
+    vc.velocityBias[j] = 0.0f;
+    float vRel = dot(normal, (vB + cross(wB, rB)) - (vA + cross(wA, rA)));
+    if (vRel < -threshold) vc.velocityBias[j] = -restitution * vRel;
+  }
+  if (vc.pointCount == 2) {
+    V2 r1A = ld2(vc.rA[0]), r1B = ld2(vc.rB[0]), r2A = ld2(vc.rA[1]), r2B = ld2(vc.rB[1]);
+    float rn1A = cross(r1A, normal);
+    float rn1B = cross(r1B, normal);
+    float rn2A = cross(r2A, normal);
+    float rn2B = cross(r2B, normal);
+    float k11 = mA + mB + iA * rn1A * rn1A + iB * rn1B * rn1B;
+    float k22 = mA + mB + iA * rn2A * rn2A + iB * rn2B * rn2B;
+    float k12 = mA + mB + iA * rn1A * rn2A + iB * rn1B * rn2B;
+    const float k_maxConditionNumber = 1000.0f;
+    if (k11 * k11 < k_maxConditionNumber * (k11 * k22 - k12 * k12)) {
+      M22 K;
+      K.ex = mk(k11, k12);
+      K.ey = mk(k12, k22);
+      M22 NM = inverse(K);
+      vc.K[0] = K.ex.x; vc.K[1] = K.ex.y; vc.K[2] = K.ey.x; vc.K[3] = K.ey.y;
+      vc.NM[0] = NM.ex.x; vc.NM[1] = NM.ex.y; vc.NM[2] = NM.ey.x; vc.NM[3] = NM.ey.y;
+    } else {
+      vc.pointCount = 1;
+    }
+  }
+}
+
+B2G_HD void loadVel(const float4* vel, int i, V2& v, float& w) {
+  float4 x = vel[i];
+  v = mk(x.x, x.y);
+  w = x.z;
+}
+B2G_HD void storeVel(float4* vel, int i, V2 v, float w) { vel[i] = make_float4(v.x, v.y, w, 0.0f); }
+// A body with zero inverse mass and inertia (static, or massless) is left untouched: its update
+// would be v - 0*P, a no-op, and skipping it keeps constraints of one colour that share such a
+// body from writing the same address.
+B2G_HD bool moves(float invMass, float invI) { return invMass != 0.0f || invI != 0.0f; }
+B2G_HD void loadPos(const float4* pos, int i, V2& c, float& a) {
+  float4 x = pos[i];
+  c = mk(x.x, x.y);
+  a = x.z;
+}
+B2G_HD void storePos(float4* pos, int i, V2 c, float a) { pos[i] = make_float4(c.x, c.y, a, 0.0f); }
+
+// b2ContactSolver::WarmStart for one constraint.
+B2G_HD void warmStartContact(const VCDev& vc, float4* vel) {
+  float mA = vc.invMassA, iA = vc.invIA, mB = vc.invMassB, iB = vc.invIB;
+  V2 vA, vB; float wA, wB;
+  loadVel(vel, vc.indexA, vA, wA);
+  loadVel(vel, vc.indexB, vB, wB);
+  V2 normal = ld2(vc.normal);
+  V2 tangent = cross(normal, 1.0f);
+  for (int j = 0; j < vc.pointCount; ++j) {
+    V2 P = vc.normalImpulse[j] * normal + vc.tangentImpulse[j] * tangent;
+    wA -= iA * cross(ld2(vc.rA[j]), P);
+    subFrom(vA, mA * P);
+    wB += iB * cross(ld2(vc.rB[j]), P);
+    addTo(vB, mB * P);
+  }
+  if (moves(mA, iA)) storeVel(vel, vc.indexA, vA, wA);
+  if (moves(mB, iB)) storeVel(vel, vc.indexB, vB, wB);
+}
+
+// b2ContactSolver::SolveVelocityConstraints for one constraint (friction, then normal with the
+// 2-point block solver's total enumeration of the four LCP cases).
+B2G_HD void solveContactVelocity(VCDev& vc, float4* vel) {
+  float mA = vc.invMassA, iA = vc.invIA, mB = vc.invMassB, iB = vc.invIB;
+  int pointCount = vc.pointCount;
+  V2 vA, vB; float wA, wB;
+  loadVel(vel, vc.indexA, vA, wA);
+  loadVel(vel, vc.indexB, vB, wB);
+  V2 normal = ld2(vc.normal);
+  V2 tangent = cross(normal, 1.0f);
+  for (int j = 0; j < pointCount; ++j) {
+    V2 rA = ld2(vc.rA[j]), rB = ld2(vc.rB[j]);
+    V2 dv = (vB + cross(wB, rB)) - (vA + cross(wA, rA));
+    float vt = dot(dv, tangent) - vc.tangentSpeed;
+    float lambda = vc.tangentMass[j] * (-vt);
+    float maxFriction = vc.friction * vc.normalImpulse[j];
+    float newImpulse = fclamp(vc.tangentImpulse[j] + lambda, -maxFriction, maxFriction);
+    lambda = newImpulse - vc.tangentImpulse[j];
+    vc.tangentImpulse[j] = newImpulse;
+    V2 P = lambda * tangent;
+    subFrom(vA, mA * P);
+    wA -= iA * cross(rA, P);
+    addTo(vB, mB * P);
+    wB += iB * cross(rB, P);
+  }
+  if (pointCount == 1) {
+    V2 rA = ld2(vc.rA[0]), rB = ld2(vc.rB[0]);
+    V2 dv = (vB + cross(wB, rB)) - (vA + cross(wA, rA));
+    float vn = dot(dv, normal);
+    float lambda = -vc.normalMass[0] * (vn - vc.velocityBias[0]);
+    float newImpulse = fmax2(vc.normalImpulse[0] + lambda, 0.0f);
+    lambda = newImpulse - vc.normalImpulse[0];
+    vc.normalImpulse[0] = newImpulse;
+    V2 P = lambda * normal;
+    subFrom(vA, mA * P);
+    wA -= iA * cross(rA, P);
+    addTo(vB, mB * P);
+    wB += iB * cross(rB, P);
+  } else {
+    V2 r1A = ld2(vc.rA[0]), r1B = ld2(vc.rB[0]), r2A = ld2(vc.rA[1]), r2B = ld2(vc.rB[1]);
+    M22 K, NM;
+    K.ex = mk(vc.K[0], vc.K[1]); K.ey = mk(vc.K[2], vc.K[3]);
+    NM.ex = mk(vc.NM[0], vc.NM[1]); NM.ey = mk(vc.NM[2], vc.NM[3]);
+    V2 a = mk(vc.normalImpulse[0], vc.normalImpulse[1]);
+    V2 dv1 = (vB + cross(wB, r1B)) - (vA + cross(wA, r1A));
+    V2 dv2 = (vB + cross(wB, r2B)) - (vA + cross(wA, r2A));
+    float vn1 = dot(dv1, normal);
+    float vn2 = dot(dv2, normal);
+    V2 b;
+    b.x = vn1 - vc.velocityBias[0];
+    b.y = vn2 - vc.velocityBias[1];
+    subFrom(b, mul(K, a));
+    V2 x;
+    bool solved = false;
+    // Case 1: vn = 0
+    x = -mul(NM, b);
+    if (x.x >= 0.0f && x.y >= 0.0f) {
+      solved = true;
+    } else {
+      // Case 2: vn1 = 0 and x2 = 0
+      x.x = -vc.normalMass[0] * b.x;
+      x.y = 0.0f;
+      vn2 = K.ex.y * x.x + b.y;
+      if (x.x >= 0.0f && vn2 >= 0.0f) {
+        solved = true;
+      } else {
+        // Case 3: vn2 = 0 and x1 = 0
+        x.x = 0.0f;
+        x.y = -vc.normalMass[1] * b.y;
+        vn1 = K.ey.x * x.y + b.x;
+        if (x.y >= 0.0f && vn1 >= 0.0f) {
+          solved = true;
+        } else {
+          // Case 4: x1 = 0 and x2 = 0
+          x.x = 0.0f;
+          x.y = 0.0f;
+          vn1 = b.x;
+          vn2 = b.y;
+          if (vn1 >= 0.0f && vn2 >= 0.0f) solved = true;
+        }
+      }
+    }
+    if (solved) {
+      V2 d = x - a;
+      V2 P1 = d.x * normal;
+      V2 P2 = d.y * normal;
+      subFrom(vA, mA * (P1 + P2));
+      wA -= iA * (cross(r1A, P1) + cross(r2A, P2));
+      addTo(vB, mB * (P1 + P2));
+      wB += iB * (cross(r1B, P1) + cross(r2B, P2));
+      vc.normalImpulse[0] = x.x;
+      vc.normalImpulse[1] = x.y;
+    }
+  }
+  if (moves(mA, iA)) storeVel(vel, vc.indexA, vA, wA);
+  if (moves(mB, iB)) storeVel(vel, vc.indexB, vB, wB);
+}
+
+// b2PositionSolverManifold + SolvePositionConstraints for one constraint; returns its minimum
+// separation (starting from 0 as the reference's minSeparation does).
+B2G_HD float solveContactPosition(const VCDev& vc, float4* pos) {
+  float minSeparation = 0.0f;
+  V2 localCenterA = ld2(vc.localCenterA), localCenterB = ld2(vc.localCenterB);
+  float mA = vc.invMassA, iA = vc.invIA, mB = vc.invMassB, iB = vc.invIB;
+  V2 cA, cB; float aA, aB;
+  loadPos(pos, vc.indexA, cA, aA);
+  loadPos(pos, vc.indexB, cB, aB);
+  for (int j = 0; j < vc.pcPointCount; ++j) {
+    Xf xfA, xfB;
+    xfA.q = rotOf(aA);
+    xfB.q = rotOf(aB);
+    xfA.p = cA - mul(xfA.q, localCenterA);
+    xfB.p = cB - mul(xfB.q, localCenterB);
+    V2 normal, point;
+    float separation;
+    if (vc.type == B2G_MANIFOLD_CIRCLES) {
+      V2 pointA = mul(xfA, ld2(vc.localPoint));
+      V2 pointB = mul(xfB, ld2(vc.localPoints[0]));
+      normal = pointB - pointA;
+      normalize(normal);
+      point = 0.5f * (pointA + pointB);
+      separation = (dot(pointB - pointA, normal) - vc.radiusA) - vc.radiusB;
+    } else if (vc.type == B2G_MANIFOLD_FACE_A) {
+      normal = mul(xfA.q, ld2(vc.localNormal));
+      V2 planePoint = mul(xfA, ld2(vc.localPoint));
+      V2 clipPoint = mul(xfB, ld2(vc.localPoints[j]));
+      separation = (dot(clipPoint - planePoint, normal) - vc.radiusA) - vc.radiusB;
+      point = clipPoint;
+    } else {
+      normal = mul(xfB.q, ld2(vc.localNormal));
+      V2 planePoint = mul(xfB, ld2(vc.localPoint));
+      V2 clipPoint = mul(xfA, ld2(vc.localPoints[j]));
+      separation = (dot(clipPoint - planePoint, normal) - vc.radiusA) - vc.radiusB;
+      point = clipPoint;
+      normal = -normal;
+    }
+    V2 rA = point - cA;
+    V2 rB = point - cB;
+    minSeparation = fmin2(minSeparation, separation);
+    float C = fclamp(B2G_BAUMGARTE * (separation + B2G_LINEAR_SLOP), -B2G_MAX_LINEAR_CORRECTION, 0.0f);
+    float rnA = cross(rA, normal);
+    float rnB = cross(rB, normal);
+    float K = mA + mB + iA * rnA * rnA + iB * rnB * rnB;
+    float impulse = K > 0.0f ? -C / K : 0.0f;
+    V2 P = impulse * normal;
+    subFrom(cA, mA * P);
+    aA -= iA * cross(rA, P);
+    addTo(cB, mB * P);
+    aB += iB * cross(rB, P);
+  }
+  if (moves(mA, iA)) storePos(pos, vc.indexA, cA, aA);
+  if (moves(mB, iB)) storePos(pos, vc.indexB, cB, aB);
+  return minSeparation;
+}
+
+// ---- joints -----------------------------------------------------------------------------
+B2G_HD M22 ldK(const float* k) { M22 m; m.ex = mk(k[0], k[1]); m.ey = mk(k[2], k[3]); return m; }
+B2G_HD void stK(float* k, const M22& m) { k[0] = m.ex.x; k[1] = m.ex.y; k[2] = m.ey.x; k[3] = m.ey.y; }
+
+// InitVelocityConstraints (revolute :73-165, prismatic :114-224, distance :76-173).
+B2G_HD void jointInit(JointDev& J, const float4* massd, const float2* lc, const float4* pos, float4* vel, float dt,
+                      float dtRatio, bool warm) {
+  int ia = J.d.body_a, ib = J.d.body_b;
+  J.iA = ia; J.iB = ib;
+  float2 la2 = lc[ia], lb2 = lc[ib];
+  J.lcA[0] = la2.x; J.lcA[1] = la2.y; J.lcB[0] = lb2.x; J.lcB[1] = lb2.y;
+  float4 mdA = massd[ia], mdB = massd[ib];
+  J.mA = mdA.y; J.mB = mdB.y; J.invIA = mdA.w; J.invIB = mdB.w;
+  V2 cA, cB, vA, vB; float aA, aB, wA, wB;
+  loadPos(pos, ia, cA, aA); loadVel(vel, ia, vA, wA);
+  loadPos(pos, ib, cB, aB); loadVel(vel, ib, vB, wB);
+  Rot qA = rotOf(aA), qB = rotOf(aB);
+  V2 la = ld2(J.d.local_anchor_a), lb = ld2(J.d.local_anchor_b);
+  V2 lcA = ld2(J.lcA), lcB = ld2(J.lcB);
+  float mA = J.mA, mB = J.mB, iA = J.invIA, iB = J.invIB;
+  if (J.d.type == B2G_JOINT_REVOLUTE) {
+    V2 rA = mul(qA, la - lcA);
+    V2 rB = mul(qB, lb - lcB);
+    st2(J.rA, rA); st2(J.rB, rB);
+    M22 K;
+    K.ex.x = mA + mB + rA.y * rA.y * iA + rB.y * rB.y * iB;
+    K.ey.x = -rA.y * rA.x * iA - rB.y * rB.x * iB;
+    K.ex.y = K.ey.x;
+    K.ey.y = mA + mB + rA.x * rA.x * iA + rB.x * rB.x * iB;
+    stK(J.K, K);
+    J.axialMass = iA + iB;
+    bool fixedRotation;
+    if (J.axialMass > 0.0f) { J.axialMass = 1.0f / J.axialMass; fixedRotation = false; }
+    else fixedRotation = true;
+    J.angle = aB - aA - J.d.reference_angle;
+    if (J.d.enable_limit == 0 || fixedRotation) { J.lowerImpulse = 0.0f; J.upperImpulse = 0.0f; }
+    if (J.d.enable_motor == 0 || fixedRotation) J.motorImpulse = 0.0f;
+    if (warm) {
+      J.impulse[0] *= dtRatio; J.impulse[1] *= dtRatio;
+      J.motorImpulse *= dtRatio; J.lowerImpulse *= dtRatio; J.upperImpulse *= dtRatio;
+      float axialImpulse = J.motorImpulse + J.lowerImpulse - J.upperImpulse;
+      V2 P = mk(J.impulse[0], J.impulse[1]);
+      subFrom(vA, mA * P);
+      wA -= iA * (cross(rA, P) + axialImpulse);
+      addTo(vB, mB * P);
+      wB += iB * (cross(rB, P) + axialImpulse);
+    } else {
+      J.impulse[0] = 0.0f; J.impulse[1] = 0.0f;
+      J.motorImpulse = 0.0f; J.lowerImpulse = 0.0f; J.upperImpulse = 0.0f;
+    }
+  } else if (J.d.type == B2G_JOINT_PRISMATIC) {
+    V2 rA = mul(qA, la - lcA);
+    V2 rB = mul(qB, lb - lcB);
+    V2 d = ((cB - cA) + rB) - rA;
+    V2 axis = mul(qA, ld2(J.localXAxisA));
+    float a1 = cross(d + rA, axis);
+    float a2 = cross(rB, axis);
+    st2(J.axis, axis);
+    J.a1 = a1; J.a2 = a2;
+    J.axialMass = mA + mB + iA * a1 * a1 + iB * a2 * a2;
+    if (J.axialMass > 0.0f) J.axialMass = 1.0f / J.axialMass;
+    V2 perp = mul(qA, ld2(J.localYAxisA));
+    st2(J.perp, perp);
+    J.s1 = cross(d + rA, perp);
+    J.s2 = cross(rB, perp);
+    float k11 = mA + mB + iA * J.s1 * J.s1 + iB * J.s2 * J.s2;
+    float k12 = iA * J.s1 + iB * J.s2;
+    float k22 = iA + iB;
+    if (k22 == 0.0f) k22 = 1.0f;
+    M22 K;
+    K.ex = mk(k11, k12);
+    K.ey = mk(k12, k22);
+    stK(J.K, K);
+    if (J.d.enable_limit) J.translation = dot(axis, d);
+    else { J.lowerImpulse = 0.0f; J.upperImpulse = 0.0f; }
+    if (J.d.enable_motor == 0) J.motorImpulse = 0.0f;
+    if (warm) {
+      J.impulse[0] *= dtRatio; J.impulse[1] *= dtRatio;
+      J.motorImpulse *= dtRatio; J.lowerImpulse *= dtRatio; J.upperImpulse *= dtRatio;
+      float axialImpulse = J.motorImpulse + J.lowerImpulse - J.upperImpulse;
+      V2 P = J.impulse[0] * perp + axialImpulse * axis;
+      float LA = J.impulse[0] * J.s1 + J.impulse[1] + axialImpulse * a1;
+      float LB = J.impulse[0] * J.s2 + J.impulse[1] + axialImpulse * a2;
+      subFrom(vA, mA * P);
+      wA -= iA * LA;
+      addTo(vB, mB * P);
+      wB += iB * LB;
+    } else {
+      J.impulse[0] = 0.0f; J.impulse[1] = 0.0f;
+      J.motorImpulse = 0.0f; J.lowerImpulse = 0.0f; J.upperImpulse = 0.0f;
+    }
+  } else {
+    V2 rA = mul(qA, la - lcA);
+    V2 rB = mul(qB, lb - lcB);
+    st2(J.rA, rA); st2(J.rB, rB);
+    V2 u = ((cB + rB) - cA) - rA;
+    J.currentLength = lengthOf(u);
+    if (J.currentLength > B2G_LINEAR_SLOP) {
+      u = (1.0f / J.currentLength) * u;
+    } else {
+      u = mk(0.0f, 0.0f);
+      J.mass = 0.0f; J.impulse[0] = 0.0f; J.lowerImpulse = 0.0f; J.upperImpulse = 0.0f;
+    }
+    st2(J.u, u);
+    float crAu = cross(rA, u);
+    float crBu = cross(rB, u);
+    float invMass = J.mA + J.invIA * crAu * crAu + J.mB + J.invIB * crBu * crBu;
+    J.mass = invMass != 0.0f ? 1.0f / invMass : 0.0f;
+    if (J.d.stiffness > 0.0f && J.d.min_length < J.d.max_length) {
+      float C = J.currentLength - J.d.length;
+      float dd = J.d.damping;
+      float k = J.d.stiffness;
+      float h = dt;
+      J.gamma = h * (dd + h * k);
+      J.gamma = J.gamma != 0.0f ? 1.0f / J.gamma : 0.0f;
+      J.bias = C * h * k * J.gamma;
+      invMass += J.gamma;
+      J.softMass = invMass != 0.0f ? 1.0f / invMass : 0.0f;
+    } else {
+      J.gamma = 0.0f; J.bias = 0.0f; J.softMass = J.mass;
+    }
+    if (warm) {
+      J.impulse[0] *= dtRatio; J.lowerImpulse *= dtRatio; J.upperImpulse *= dtRatio;
+      V2 P = ((J.impulse[0] + J.lowerImpulse) - J.upperImpulse) * u;
+      subFrom(vA, J.mA * P);
+      wA -= J.invIA * cross(rA, P);
+      addTo(vB, J.mB * P);
+      wB += J.invIB * cross(rB, P);
+    } else {
+      J.impulse[0] = 0.0f;
+    }
+  }
+  if (moves(mA, iA)) storeVel(vel, ia, vA, wA);
+  if (moves(mB, iB)) storeVel(vel, ib, vB, wB);
+}
+
+// SolveVelocityConstraints (revolute :167-243, prismatic :226-330, distance :175-266).
+B2G_HD void jointSolveVelocity(JointDev& J, float4* vel, float dt, float inv_dt) {
+  V2 vA, vB; float wA, wB;
+  loadVel(vel, J.iA, vA, wA);
+  loadVel(vel, J.iB, vB, wB);
+  float mA = J.mA, mB = J.mB, iA = J.invIA, iB = J.invIB;
+  if (J.d.type == B2G_JOINT_REVOLUTE) {
+    V2 rA = ld2(J.rA), rB = ld2(J.rB);
+    bool fixedRotation = (iA + iB == 0.0f);
+    if (J.d.enable_motor && fixedRotation == false) {
+      float Cdot = wB - wA - J.d.motor_speed;
+      float impulse = -J.axialMass * Cdot;
+      float oldImpulse = J.motorImpulse;
+      float maxImpulse = dt * J.d.max_motor;
+      J.motorImpulse = fclamp(J.motorImpulse + impulse, -maxImpulse, maxImpulse);
+      impulse = J.motorImpulse - oldImpulse;
+      wA -= iA * impulse;
+      wB += iB * impulse;
+    }
+    if (J.d.enable_limit && fixedRotation == false) {
+      {
+        float C = J.angle - J.d.lower;
+        float Cdot = wB - wA;
+        float impulse = -J.axialMass * (Cdot + fmax2(C, 0.0f) * inv_dt);
+        float oldImpulse = J.lowerImpulse;
+        J.lowerImpulse = fmax2(J.lowerImpulse + impulse, 0.0f);
+        impulse = J.lowerImpulse - oldImpulse;
+        wA -= iA * impulse;
+        wB += iB * impulse;
+      }
+      {
+        float C = J.d.upper - J.angle;
+        float Cdot = wA - wB;
+        float impulse = -J.axialMass * (Cdot + fmax2(C, 0.0f) * inv_dt);
+        float oldImpulse = J.upperImpulse;
+        J.upperImpulse = fmax2(J.upperImpulse + impulse, 0.0f);
+        impulse = J.upperImpulse - oldImpulse;
+        wA += iA * impulse;
+        wB -= iB * impulse;
+      }
+    }
+    {
+      V2 Cdot = ((vB + cross(wB, rB)) - vA) - cross(wA, rA);
+      V2 impulse = solve(ldK(J.K), -Cdot);
+      J.impulse[0] += impulse.x;
+      J.impulse[1] += impulse.y;
+      subFrom(vA, mA * impulse);
+      wA -= iA * cross(rA, impulse);
+      addTo(vB, mB * impulse);
+      wB += iB * cross(rB, impulse);
+    }
+  } else if (J.d.type == B2G_JOINT_PRISMATIC) {
+    V2 axis = ld2(J.axis), perp = ld2(J.perp);
+    if (J.d.enable_motor) {
+      float Cdot = (dot(axis, vB - vA) + J.a2 * wB) - J.a1 * wA;
+      float impulse = J.axialMass * (J.d.motor_speed - Cdot);
+      float oldImpulse = J.motorImpulse;
+      float maxImpulse = dt * J.d.max_motor;
+      J.motorImpulse = fclamp(J.motorImpulse + impulse, -maxImpulse, maxImpulse);
+      impulse = J.motorImpulse - oldImpulse;
+      V2 P = impulse * axis;
+      float LA = impulse * J.a1;
+      float LB = impulse * J.a2;
+      subFrom(vA, mA * P); wA -= iA * LA;
+      addTo(vB, mB * P); wB += iB * LB;
+    }
+    if (J.d.enable_limit) {
+      {
+        float C = J.translation - J.d.lower;
+        float Cdot = (dot(axis, vB - vA) + J.a2 * wB) - J.a1 * wA;
+        float impulse = -J.axialMass * (Cdot + fmax2(C, 0.0f) * inv_dt);
+        float oldImpulse = J.lowerImpulse;
+        J.lowerImpulse = fmax2(J.lowerImpulse + impulse, 0.0f);
+        impulse = J.lowerImpulse - oldImpulse;
+        V2 P = impulse * axis;
+        float LA = impulse * J.a1;
+        float LB = impulse * J.a2;
+        subFrom(vA, mA * P); wA -= iA * LA;
+        addTo(vB, mB * P); wB += iB * LB;
+      }
+      {
+        float C = J.d.upper - J.translation;
+        float Cdot = (dot(axis, vA - vB) + J.a1 * wA) - J.a2 * wB;
+        float impulse = -J.axialMass * (Cdot + fmax2(C, 0.0f) * inv_dt);
+        float oldImpulse = J.upperImpulse;
+        J.upperImpulse = fmax2(J.upperImpulse + impulse, 0.0f);
+        impulse = J.upperImpulse - oldImpulse;
+        V2 P = impulse * axis;
+        float LA = impulse * J.a1;
+        float LB = impulse * J.a2;
+        addTo(vA, mA * P); wA += iA * LA;
+        subFrom(vB, mB * P); wB -= iB * LB;
+      }
+    }
+    {
+      V2 Cdot;
+      Cdot.x = (dot(perp, vB - vA) + J.s2 * wB) - J.s1 * wA;
+      Cdot.y = wB - wA;
+      V2 df = solve(ldK(J.K), -Cdot);
+      J.impulse[0] += df.x;
+      J.impulse[1] += df.y;
+      V2 P = df.x * perp;
+      float LA = df.x * J.s1 + df.y;
+      float LB = df.x * J.s2 + df.y;
+      subFrom(vA, mA * P); wA -= iA * LA;
+      addTo(vB, mB * P); wB += iB * LB;
+    }
+  } else {
+    V2 rA = ld2(J.rA), rB = ld2(J.rB), u = ld2(J.u);
+    if (J.d.min_length < J.d.max_length) {
+      if (J.d.stiffness > 0.0f) {
+        V2 vpA = vA + cross(wA, rA);
+        V2 vpB = vB + cross(wB, rB);
+        float Cdot = dot(u, vpB - vpA);
+        float impulse = -J.softMass * ((Cdot + J.bias) + J.gamma * J.impulse[0]);
+        J.impulse[0] += impulse;
+        V2 P = impulse * u;
+        subFrom(vA, J.mA * P); wA -= J.invIA * cross(rA, P);
+        addTo(vB, J.mB * P); wB += J.invIB * cross(rB, P);
+      }
+      {
+        float C = J.currentLength - J.d.min_length;
+        float bias = fmax2(0.0f, C) * inv_dt;
+        V2 vpA = vA + cross(wA, rA);
+        V2 vpB = vB + cross(wB, rB);
+        float Cdot = dot(u, vpB - vpA);
+        float impulse = -J.mass * (Cdot + bias);
+        float oldImpulse = J.lowerImpulse;
+        J.lowerImpulse = fmax2(0.0f, J.lowerImpulse + impulse);
+        impulse = J.lowerImpulse - oldImpulse;
+        V2 P = impulse * u;
+        subFrom(vA, J.mA * P); wA -= J.invIA * cross(rA, P);
+        addTo(vB, J.mB * P); wB += J.invIB * cross(rB, P);
+      }
+      {
+        float C = J.d.max_length - J.currentLength;
+        float bias = fmax2(0.0f, C) * inv_dt;
+        V2 vpA = vA + cross(wA, rA);
+        V2 vpB = vB + cross(wB, rB);
+        float Cdot = dot(u, vpA - vpB);
+        float impulse = -J.mass * (Cdot + bias);
+        float oldImpulse = J.upperImpulse;
+        J.upperImpulse = fmax2(0.0f, J.upperImpulse + impulse);
+        impulse = J.upperImpulse - oldImpulse;
+        V2 P = -impulse * u;
+        subFrom(vA, J.mA * P); wA -= J.invIA * cross(rA, P);
+        addTo(vB, J.mB * P); wB += J.invIB * cross(rB, P);
+      }
+    } else {
+      V2 vpA = vA + cross(wA, rA);
+      V2 vpB = vB + cross(wB, rB);
+      float Cdot = dot(u, vpB - vpA);
+      float impulse = -J.mass * Cdot;
+      J.impulse[0] += impulse;
+      V2 P = impulse * u;
+      subFrom(vA, J.mA * P); wA -= J.invIA * cross(rA, P);
+      addTo(vB, J.mB * P); wB += J.invIB * cross(rB, P);
+    }
+  }
+  if (moves(J.mA, J.invIA)) storeVel(vel, J.iA, vA, wA);
+  if (moves(J.mB, J.invIB)) storeVel(vel, J.iB, vB, wB);
+}
+
+// SolvePositionConstraints (revolute :245-321, prismatic :340-459, distance :268-314).
+B2G_HD bool jointSolvePosition(JointDev& J, float4* pos) {
+  V2 cA, cB; float aA, aB;
+  loadPos(pos, J.iA, cA, aA);
+  loadPos(pos, J.iB, cB, aB);
+  Rot qA = rotOf(aA), qB = rotOf(aB);
+  V2 la = ld2(J.d.local_anchor_a), lb = ld2(J.d.local_anchor_b);
+  V2 lcA = ld2(J.lcA), lcB = ld2(J.lcB);
+  bool ok;
+  if (J.d.type == B2G_JOINT_REVOLUTE) {
+    float angularError = 0.0f;
+    float positionError = 0.0f;
+    bool fixedRotation = (J.invIA + J.invIB == 0.0f);
+    if (J.d.enable_limit && fixedRotation == false) {
+      float angle = aB - aA - J.d.reference_angle;
+      float C = 0.0f;
+      if (fabs2(J.d.upper - J.d.lower) < 2.0f * B2G_ANGULAR_SLOP)
+        C = fclamp(angle - J.d.lower, -B2G_MAX_ANGULAR_CORRECTION, B2G_MAX_ANGULAR_CORRECTION);
+      else if (angle <= J.d.lower)
+        C = fclamp(angle - J.d.lower + B2G_ANGULAR_SLOP, -B2G_MAX_ANGULAR_CORRECTION, 0.0f);
+      else if (angle >= J.d.upper)
+        C = fclamp(angle - J.d.upper - B2G_ANGULAR_SLOP, 0.0f, B2G_MAX_ANGULAR_CORRECTION);
+      float limitImpulse = -J.axialMass * C;
+      aA -= J.invIA * limitImpulse;
+      aB += J.invIB * limitImpulse;
+      angularError = fabs2(C);
+    }
+    {
+      qA = rotOf(aA);
+      qB = rotOf(aB);
+      V2 rA = mul(qA, la - lcA);
+      V2 rB = mul(qB, lb - lcB);
+      V2 C = ((cB + rB) - cA) - rA;
+      positionError = lengthOf(C);
+      float mA = J.mA, mB = J.mB, iA = J.invIA, iB = J.invIB;
+      M22 K;
+      K.ex.x = mA + mB + iA * rA.y * rA.y + iB * rB.y * rB.y;
+      K.ex.y = -iA * rA.x * rA.y - iB * rB.x * rB.y;
+      K.ey.x = K.ex.y;
+      K.ey.y = mA + mB + iA * rA.x * rA.x + iB * rB.x * rB.x;
+      V2 impulse = -solve(K, C);
+      subFrom(cA, mA * impulse);
+      aA -= iA * cross(rA, impulse);
+      addTo(cB, mB * impulse);
+      aB += iB * cross(rB, impulse);
+    }
+    ok = positionError <= B2G_LINEAR_SLOP && angularError <= B2G_ANGULAR_SLOP;
+  } else if (J.d.type == B2G_JOINT_PRISMATIC) {
+    float mA = J.mA, mB = J.mB, iA = J.invIA, iB = J.invIB;
+    V2 rA = mul(qA, la - lcA);
+    V2 rB = mul(qB, lb - lcB);
+    V2 d = ((cB + rB) - cA) - rA;
+    V2 axis = mul(qA, ld2(J.localXAxisA));
+    float a1 = cross(d + rA, axis);
+    float a2 = cross(rB, axis);
+    V2 perp = mul(qA, ld2(J.localYAxisA));
+    float s1 = cross(d + rA, perp);
+    float s2 = cross(rB, perp);
+    V3 impulse;
+    V2 C1;
+    C1.x = dot(perp, d);
+    C1.y = aB - aA - J.d.reference_angle;
+    float linearError = fabs2(C1.x);
+    float angularError = fabs2(C1.y);
+    bool active = false;
+    float C2 = 0.0f;
+    if (J.d.enable_limit) {
+      float translation = dot(axis, d);
+      if (fabs2(J.d.upper - J.d.lower) < 2.0f * B2G_LINEAR_SLOP) {
+        C2 = translation;
+        linearError = fmax2(linearError, fabs2(translation));
+        active = true;
+      } else if (translation <= J.d.lower) {
+        C2 = fmin2(translation - J.d.lower, 0.0f);
+        linearError = fmax2(linearError, J.d.lower - translation);
+        active = true;
+      } else if (translation >= J.d.upper) {
+        C2 = fmax2(translation - J.d.upper, 0.0f);
+        linearError = fmax2(linearError, translation - J.d.upper);
+        active = true;
+      }
+    }
+    if (active) {
+      float k11 = mA + mB + iA * s1 * s1 + iB * s2 * s2;
+      float k12 = iA * s1 + iB * s2;
+      float k13 = iA * s1 * a1 + iB * s2 * a2;
+      float k22 = iA + iB;
+      if (k22 == 0.0f) k22 = 1.0f;
+      float k23 = iA * a1 + iB * a2;
+      float k33 = mA + mB + iA * a1 * a1 + iB * a2 * a2;
+      V3 ex = {k11, k12, k13}, ey = {k12, k22, k23}, ez = {k13, k23, k33};
+      V3 Cn = {-C1.x, -C1.y, -C2};
+      impulse = solve33(ex, ey, ez, Cn);
+    } else {
+      float k11 = mA + mB + iA * s1 * s1 + iB * s2 * s2;
+      float k12 = iA * s1 + iB * s2;
+      float k22 = iA + iB;
+      if (k22 == 0.0f) k22 = 1.0f;
+      M22 K;
+      K.ex = mk(k11, k12);
+      K.ey = mk(k12, k22);
+      V2 impulse1 = solve(K, -C1);
+      impulse.x = impulse1.x; impulse.y = impulse1.y; impulse.z = 0.0f;
+    }
+    V2 P = impulse.x * perp + impulse.z * axis;
+    float LA = (impulse.x * s1 + impulse.y) + impulse.z * a1;
+    float LB = (impulse.x * s2 + impulse.y) + impulse.z * a2;
+    subFrom(cA, mA * P); aA -= iA * LA;
+    addTo(cB, mB * P); aB += iB * LB;
+    ok = linearError <= B2G_LINEAR_SLOP && angularError <= B2G_ANGULAR_SLOP;
+  } else {
+    V2 rA = mul(qA, la - lcA);
+    V2 rB = mul(qB, lb - lcB);
+    V2 u = ((cB + rB) - cA) - rA;
+    float length = normalize(u);
+    float C;
+    if (J.d.min_length == J.d.max_length) C = length - J.d.min_length;
+    else if (length < J.d.min_length) C = length - J.d.min_length;
+    else if (J.d.max_length < length) C = length - J.d.max_length;
+    else return true;
+    float impulse = -J.mass * C;
+    V2 P = impulse * u;
+    subFrom(cA, J.mA * P); aA -= J.invIA * cross(rA, P);
+    addTo(cB, J.mB * P); aB += J.invIB * cross(rB, P);
+    ok = fabs2(C) < B2G_LINEAR_SLOP;
+  }
+  if (moves(J.mA, J.invIA)) storePos(pos, J.iA, cA, aA);
+  if (moves(J.mB, J.invIB)) storePos(pos, J.iB, cB, aB);
+  return ok;
+}
+
+}  // namespace b2g

@@ -205,8 +205,8 @@ typedef struct b2g_joint {
   b2g_joint_def def;
   float impulse[3];
   float motor_impulse, lower_impulse, upper_impulse;
-  float reaction_force[2]; /* GetReactionForce(inv_dt of the last step) */
-  float reaction_torque;   /* GetReactionTorque(inv_dt of the last step) */
+  float reaction_impulse[2];      /* GetReactionForce(inv_dt) / inv_dt after the last step */
+  float reaction_angular_impulse; /* GetReactionTorque(inv_dt) / inv_dt after the last step */
 } b2g_joint;
 
 /* b2Contact (include/box2d/b2_contact.h:155-173 flags) */
@@ -248,7 +248,9 @@ typedef struct b2g_profile {
 typedef struct b2g_batch b2g_batch;
 
 /* Device memory budget in bytes (0 = no limit). Allocation beyond it fails with
- * B2G_E_OUT_OF_MEMORY instead of reaching cudaMalloc. */
+ * B2G_E_OUT_OF_MEMORY instead of reaching cudaMalloc. device = B2G_HOST_ONLY makes a batch
+ * that builds, edits and reads worlds on the host but cannot step (no GPU needed). */
+#define B2G_HOST_ONLY (-1)
 B2G_API int b2g_batch_create(int device, uint64_t budget_bytes, b2g_batch** out);
 B2G_API int b2g_batch_destroy(b2g_batch* b);
 

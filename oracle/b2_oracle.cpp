@@ -2282,8 +2282,8 @@ void orc_world_joints(void* h, b2g_joint* out) {
     else { s.impulse[0] = J.impulse2.x; s.impulse[1] = J.impulse2.y; }
     s.motor_impulse = J.motorImpulse; s.lower_impulse = J.lowerImpulse; s.upper_impulse = J.upperImpulse;
     float F[2], T;
-    jointReaction(J, w->inv_dt0, F, &T);
-    s.reaction_force[0] = F[0]; s.reaction_force[1] = F[1]; s.reaction_torque = T;
+    jointReaction(J, 1.0f, F, &T);
+    s.reaction_impulse[0] = F[0]; s.reaction_impulse[1] = F[1]; s.reaction_angular_impulse = T;
   }
 }
 

@@ -363,9 +363,9 @@ void ref_world_joints(void* h, b2g_joint* out) {
       o->impulse[0] = d->m_impulse;
       o->lower_impulse = d->m_lowerImpulse; o->upper_impulse = d->m_upperImpulse;
     }
-    b2Vec2 F = j->GetReactionForce(rw->world->m_inv_dt0);
-    o->reaction_force[0] = F.x; o->reaction_force[1] = F.y;
-    o->reaction_torque = j->GetReactionTorque(rw->world->m_inv_dt0);
+    b2Vec2 F = j->GetReactionForce(1.0f);
+    o->reaction_impulse[0] = F.x; o->reaction_impulse[1] = F.y;
+    o->reaction_angular_impulse = j->GetReactionTorque(1.0f);
   }
 }
 

@@ -1,0 +1,224 @@
+"""GPU parity: the CUDA engine (through the C ABI) against the CPU oracle, bit for bit.
+
+The oracle restates the reference's arithmetic in the engine's canonical order (contacts sorted
+by fixture pair, colour-ordered Gauss-Seidel, per-world position early exit, portable sin/cos),
+so on identical inputs every float of the body state must match exactly. Integer outputs
+(pair sets, manifold point counts, feature ids) are compared exactly as well.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import b2gpu as G
+import oracle_bind as ob
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+
+def _dev_bytes(buf: bytes):
+    t = torch.frombuffer(bytearray(buf), dtype=torch.uint8).cuda()
+    return t
+
+
+def _state_bytes(records):
+    # xf, c, a, v, w: the first 40 bytes of each b2g_body
+    return b"".join(bytes(r)[:40] for r in records)
+
+
+def _first_diff(g, o):
+    gn = G.body_array_to_numpy((G.Body * len(g))(*g))
+    on = G.body_array_to_numpy((G.Body * len(o))(*o))
+    for k in ("xf", "c", "a", "v", "w"):
+        d = np.abs(gn[k].astype(np.float64) - on[k].astype(np.float64))
+        if d.max() > 0:
+            i = int(np.argmax(d.reshape(len(g), -1).max(axis=1)))
+            return f"{k} body {i}: gpu {gn[k][i]} oracle {on[k][i]}"
+    return "no difference"
+
+
+def _rollout(lib, orc, kind, n, seed=1, p0=1.0, p1=0.6, steps=60, vi=8, pi=3, gravity=(0.0, -10.0)):
+    batch = G.Batch(lib, device=0)
+    w = batch.add_world(*gravity)
+    batch.set_flags(w, allow_sleep=False, warm_starting=True, continuous=False)
+    batch.scene(w, kind, seed=seed, n=n, p0=p0, p1=p1)
+    ow = ob.OracleWorld(orc, gravity, batch.bodies(w), batch.fixtures(w), batch.joints(w))
+    for s in range(steps):
+        batch.step(1 / 60, vi, pi)
+        ow.step(1, 1 / 60, vi, pi)
+        g, o = batch.bodies(w), ow.bodies()
+        assert _state_bytes(g) == _state_bytes(o), f"step {s + 1}: {_first_diff(g, o)}"
+    gc = batch.contacts(w)
+    oc = ow.contacts()
+    assert len(gc) == len(oc)
+    assert all(bytes(x) == bytes(y) for x, y in zip(gc, oc)), "contact lists differ"
+    gj, oj = batch.joints(w), ow.joints()
+    for x, y in zip(gj, oj):
+        assert list(x.impulse) == list(y.impulse)
+        assert (x.motor_impulse, x.lower_impulse, x.upper_impulse) == (y.motor_impulse, y.lower_impulse, y.upper_impulse)
+    batch.close()
+    return len(gc)
+
+
+def test_pyramid_rollout_bit_exact(lib, orc):
+    # 20-row pyramid (210 boxes, density 1, friction 0.6), 8/3 iterations
+    nc = _rollout(lib, orc, G.SCENE_PYRAMID, 20, steps=120)
+    assert nc > 300
+
+
+def test_mixed_drop_rollout_bit_exact(lib, orc):
+    # boxes, circles and 3-8 gons dropped into a U of two-sided edges
+    _rollout(lib, orc, G.SCENE_MIXED_DROP, 600, seed=3, steps=200)
+
+
+def test_chains_rollout_bit_exact(lib, orc):
+    # revolute chains (limits, motors) over a circle pile, 10/4 iterations
+    _rollout(lib, orc, G.SCENE_CHAINS, 20, seed=2, p0=300, steps=120, vi=10, pi=4)
+
+
+@pytest.mark.parametrize("seed", [11, 12, 13])
+def test_batch_world_rollout_bit_exact(lib, orc, seed):
+    n = 300 + 97 * seed
+    _rollout(lib, orc, G.SCENE_BATCH_WORLD, n, seed=seed, steps=80)
+
+
+def test_batched_equals_alone(lib):
+    """Worlds stepped together in one batch are bit-identical to the same worlds stepped alone."""
+    seeds = [21, 22, 23, 24, 25, 26]
+    sizes = [40, 700, 16, 1500, 300, 90]
+    together = G.Batch(lib, device=0)
+    ws = []
+    for s, n in zip(seeds, sizes):
+        _, gx, gy = _params(lib, s)
+        w = together.add_world(gx, gy)
+        together.set_flags(w)
+        together.scene(w, G.SCENE_BATCH_WORLD, seed=s, n=n)
+        ws.append(w)
+    for _ in range(40):
+        together.step(1 / 60, 8, 3)
+    for w, s, n in zip(ws, seeds, sizes):
+        _, gx, gy = _params(lib, s)
+        alone = G.Batch(lib, device=0)
+        a = alone.add_world(gx, gy)
+        alone.set_flags(a)
+        alone.scene(a, G.SCENE_BATCH_WORLD, seed=s, n=n)
+        for _ in range(40):
+            alone.step(1 / 60, 8, 3)
+        assert _state_bytes(together.bodies(w)) == _state_bytes(alone.bodies(a))
+        alone.close()
+    together.close()
+
+
+def test_masked_step_leaves_other_worlds(lib):
+    b = G.Batch(lib, device=0)
+    w0 = b.add_world(0, -10)
+    w1 = b.add_world(0, -10)
+    for w in (w0, w1):
+        b.set_flags(w)
+        b.scene(w, G.SCENE_PYRAMID, n=5, p0=1.0, p1=0.6)
+    before = _state_bytes(b.bodies(w1))
+    b.step(1 / 60, 8, 3, mask=[1, 0])
+    assert _state_bytes(b.bodies(w1)) == before
+    assert _state_bytes(b.bodies(w0)) != _state_bytes(b.bodies(w1))
+    b.close()
+
+
+def _params(lib, seed):
+    n = C.c_int32()
+    gx = C.c_float()
+    gy = C.c_float()
+    lib.b2g_batch_world_params(seed, C.byref(n), C.byref(gx), C.byref(gy))
+    return n.value, gx.value, gy.value
+
+
+# ---------------------------------------------------------------- standalone kernels
+def _rand_shape(rng, kind):
+    s = G.Shape()
+    if kind == G.SHAPE_CIRCLE:
+        s.type = 0
+        s.radius = float(rng.uniform(0.1, 0.6))
+        s.vertices[0][0] = float(rng.uniform(-0.2, 0.2))
+        s.vertices[0][1] = float(rng.uniform(-0.2, 0.2))
+    elif kind == G.SHAPE_EDGE:
+        s.type = 1
+        s.radius = 0.01
+        for i in range(4):
+            s.vertices[i][0] = float(rng.uniform(-2, 2))
+            s.vertices[i][1] = float(rng.uniform(-2, 2))
+        s.one_sided = int(rng.integers(0, 2))
+    else:
+        n = int(rng.integers(3, 9))
+        xy = rng.uniform(-0.6, 0.6, 2 * n).astype(np.float32)
+        ob_ = ob.Oracle()
+        if rng.uniform() < 0.3:
+            ob_.orc_polygon_box(float(rng.uniform(0.1, 0.5)), float(rng.uniform(0.1, 0.5)), 0, 0, 0, 0, s)
+        else:
+            ob_.orc_polygon_set(xy.ctypes.data_as(C.POINTER(C.c_float)), n, s)
+    return s
+
+
+def test_collide_kernel_matches_oracle(lib, orc):
+    rng = np.random.default_rng(7)
+    kinds = [(0, 0), (2, 0), (2, 2), (1, 0), (1, 2)]
+    n = 20000
+    A = (G.Shape * n)()
+    B = (G.Shape * n)()
+    xa = np.zeros((n, 4), np.float32)
+    xb = np.zeros((n, 4), np.float32)
+    for i in range(n):
+        ka, kb = kinds[i % 5]
+        A[i] = _rand_shape(rng, ka)
+        B[i] = _rand_shape(rng, kb)
+        for x in (xa, xb):
+            ang = rng.uniform(-3.2, 3.2)
+            x[i] = (rng.uniform(-0.7, 0.7), rng.uniform(-0.7, 0.7), np.sin(ang), np.cos(ang))
+    dA, dB = _dev_bytes(bytes(A)), _dev_bytes(bytes(B))
+    dxa, dxb = torch.from_numpy(xa).cuda(), torch.from_numpy(xb).cuda()
+    dout = torch.zeros(n * C.sizeof(G.Manifold), dtype=torch.uint8, device="cuda")
+    st = lib.b2g_collide(dA.data_ptr(), dxa.data_ptr(), dB.data_ptr(), dxb.data_ptr(), n, dout.data_ptr(), None)
+    assert st == 0
+    torch.cuda.synchronize()
+    out = (G.Manifold * n).from_buffer(bytearray(dout.cpu().numpy().tobytes()))
+    touching = 0
+    for i in range(n):
+        m = G.Manifold()
+        orc.orc_collide(A[i], (C.c_float * 4)(*xa[i]), B[i], (C.c_float * 4)(*xb[i]), m)
+        g = out[i]
+        assert g.point_count == m.point_count, i
+        if m.point_count:
+            touching += 1
+            assert g.type == m.type
+            assert bytes(g) == bytes(m), i
+    assert touching > 3000
+
+
+def test_pairs_kernel_matches_oracle(lib, orc):
+    rng = np.random.default_rng(3)
+    for n in (1, 2, 17, 1000, 20000):
+        c = rng.uniform(-50, 50, (n, 2)).astype(np.float32)
+        h = rng.uniform(0.05, 1.5, (n, 2)).astype(np.float32)
+        aabb = np.concatenate([c - h, c + h], axis=1).astype(np.float32)
+        cap = 4 * n + 64
+        ref = np.zeros(cap, np.uint64)
+        nref = orc.orc_pairs(aabb.ctypes.data_as(C.POINTER(C.c_float)), n, ref.ctypes.data_as(C.POINTER(C.c_uint64)), cap)
+        d_aabb = torch.from_numpy(aabb).cuda()
+        d_pairs = torch.zeros(cap, dtype=torch.int64, device="cuda")
+        npairs = C.c_int64()
+        st = lib.b2g_pairs(d_aabb.data_ptr(), n, d_pairs.data_ptr(), cap, C.byref(npairs), None)
+        assert st == 0
+        assert npairs.value == nref
+        got = d_pairs.cpu().numpy().view(np.uint64)[:nref]
+        assert np.array_equal(got, ref[:nref])
+
+
+def test_pairs_capacity_reported(lib):
+    n = 100
+    aabb = np.tile(np.array([[0, 0, 1, 1]], np.float32), (n, 1))
+    d_aabb = torch.from_numpy(aabb).cuda()
+    d_pairs = torch.zeros(10, dtype=torch.int64, device="cuda")
+    npairs = C.c_int64()
+    st = lib.b2g_pairs(d_aabb.data_ptr(), n, d_pairs.data_ptr(), 10, C.byref(npairs), None)
+    assert st == 7  # B2G_E_CAPACITY
+    assert npairs.value == n * (n - 1) // 2
