@@ -1,0 +1,312 @@
+"""Benchmark of the batched b2World::Step on one GB300 (and N GPUs as independent shards).
+
+Workload (one "step" = one batched Step of every world): 4096 independent worlds per GPU, body
+counts log-uniform in [16, 8192] by seed, each a pyramid, a mixed grid drop or revolute chains
+over a circle pile, gravity and friction jittered +-10%, dt 1/60, 8 velocity / 3 position
+iterations, sleeping and CCD off. Synthetic scenes from seeded generators; all state stays in
+HBM (far larger than the 129 MB L2, so no L2 flush is needed between steps).
+
+Prints one JSON line. `value` is whole-job body-steps/s (bodies x steps / max-over-ranks device
+time of the timed steps). `e2e` is the same metric through the public C ABI with host buffers:
+every step copies the bodies' forces host->device (pinned) and reads the transforms back.
+`--impl reference` times the reference algorithm on the host cores instead (the CPU oracle
+restatement of the reference's Step, run on all host threads over a bounded sample of worlds).
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT / "box2d-optimized_gb300"))
+sys.path.insert(0, str(ROOT / "tests"))
+
+import b2gpu as G  # noqa: E402
+
+METRIC = "batched body-steps/s vs plain GPU b2World::Step; served p50/p99 step latency"
+DT, VI, PI = 1.0 / 60.0, 8, 3
+
+
+def _peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d.get("hbm_gbs", 6800.0)), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons, sampled every 200 ms while running."""
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], 0.0, set()
+        try:
+            for line in open(self.path):
+                f = [x.strip() for x in line.split(",")]
+                if len(f) < 9 or not f[1].replace(".", "").isdigit():
+                    continue
+                sm.append(float(f[1]))
+                mx = max(mx, float(f[2]))
+                for name, v in zip(("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"),
+                                   f[5:9]):
+                    if v.lower().startswith("active"):
+                        reasons.add(name)
+        except OSError:
+            pass
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx or None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def world_params(lib, seed):
+    n = C.c_int32()
+    gx = C.c_float()
+    gy = C.c_float()
+    lib.b2g_batch_world_params(seed, C.byref(n), C.byref(gx), C.byref(gy))
+    return n.value, gx.value, gy.value
+
+
+def build_batch(lib, seeds, device):
+    batch = G.Batch(lib, device=device)
+    nb = 0
+    for s in seeds:
+        n, gx, gy = world_params(lib, s)
+        w = batch.add_world(gx, gy)
+        batch.set_flags(w, allow_sleep=False, warm_starting=True, continuous=False)
+        c = batch.scene(w, G.SCENE_BATCH_WORLD, seed=s, n=n)
+        nb += c[0]
+    return batch, nb
+
+
+def step_bytes(nb, nf, np_, nc, nj, vi=VI, pi=PI):
+    """Algorithmic bytes of one Step (fixed accounting): bodies 96/body, broadphase 144/fixture +
+    8/pair, per touching contact 524 + 192 vi + 144 pi, per joint 160 + 128 vi + 96 pi."""
+    return 96 * nb + 144 * nf + 8 * np_ + nc * (524 + 192 * vi + 144 * pi) + nj * (160 + 128 * vi + 96 * pi)
+
+
+def solve_bytes(nb, nc, nj, vi=VI, pi=PI):
+    """Algorithmic bytes of the solver kernel alone: body state read/write (64/body), contact
+    prepare 208 + store 16, velocity 192 vi and position 144 pi per touching contact, joints."""
+    return 64 * nb + nc * (208 + 16 + 192 * vi + 144 * pi) + nj * (160 + 128 * vi + 96 * pi)
+
+
+def cpu_sample(lib, seeds, warmup, steps, threads):
+    """Steps the CPU oracle (restatement of the reference Step) over a sample of worlds."""
+    import oracle_bind as ob  # noqa: PLC0415 - CPU baseline leg only
+
+    orc = ob.Oracle()
+    host = G.Batch.__new__(G.Batch)
+    host.lib = lib
+    h = C.c_void_p()
+    lib.check(lib.b2g_batch_create(-1, 0, C.byref(h)), "host batch")
+    host.h = h
+    worlds = []
+    nb = 0
+    for s in seeds:
+        n, gx, gy = world_params(lib, s)
+        w = host.add_world(gx, gy)
+        host.scene(w, G.SCENE_BATCH_WORLD, seed=s, n=n)
+        bodies = host.bodies(w)
+        nb += len(bodies)
+        worlds.append(ob.OracleWorld(orc, (gx, gy), bodies, host.fixtures(w), host.joints(w)))
+    hs = (C.c_void_p * len(worlds))(*[w.h for w in worlds])
+    orc.orc_worlds_step_parallel(hs, len(worlds), DT, VI, PI, warmup, threads)  # untimed, like the GPU warm-up
+    secs = orc.orc_worlds_step_parallel(hs, len(worlds), DT, VI, PI, steps, threads)
+    host.close()
+    return nb * steps / secs, nb, secs
+
+
+def run_reference(args, rank):
+    lib = G.Lib()
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    seeds = list(range(0, args.worlds, max(1, args.worlds // args.ref_worlds)))[: args.ref_worlds]
+    import oracle_bind as ob  # noqa: PLC0415 - the reference arm runs the oracle port
+
+    orc = ob.Oracle()
+    host = G.Batch.__new__(G.Batch)
+    host.lib = lib
+    h = C.c_void_p()
+    lib.check(lib.b2g_batch_create(-1, 0, C.byref(h)), "host batch")
+    host.h = h
+    worlds, nb = [], 0
+    for s in seeds:
+        n, gx, gy = world_params(lib, s)
+        w = host.add_world(gx, gy)
+        host.scene(w, G.SCENE_BATCH_WORLD, seed=s, n=n)
+        bodies = host.bodies(w)
+        nb += len(bodies)
+        worlds.append(ob.OracleWorld(orc, (gx, gy), bodies, host.fixtures(w), host.joints(w)))
+    hs = (C.c_void_p * len(worlds))(*[w.h for w in worlds])
+    orc.orc_worlds_step_parallel(hs, len(worlds), DT, VI, PI, args.warmup, threads)
+    secs = orc.orc_worlds_step_parallel(hs, len(worlds), DT, VI, PI, args.steps, threads)
+    value = nb * args.steps / secs
+    sample = f"{len(worlds)} of the {args.worlds} worlds (every {args.worlds // len(worlds)}th seed), {nb} bodies"
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "body-steps/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": secs * 1e3 / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"batched {args.worlds} worlds, 16-8192 bodies log-uniform, 8/3 iterations, dt 1/60",
+                   "worlds": args.worlds, "l2": "state larger than L2"},
+        "cpu_baseline": {"value": value, "unit": "body-steps/s", "cores": threads, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": "body-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, rank, world_size):
+    import torch  # noqa: PLC0415 - device selection and pinned host buffers
+
+    lib = G.Lib()
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    seeds = [rank * args.worlds + i for i in range(args.worlds)]
+    t0 = time.time()
+    batch, nb = build_batch(lib, seeds, dev)
+    build_s = time.time() - t0
+    # warm-up (includes the first upload and contact creation)
+    batch.step_timed(args.warmup, DT, VI, PI)
+    prof_w = batch.profile()
+    if world_size > 1:
+        torch.distributed.barrier()
+    with ClockSampler(dev) as clocks:
+        ms = batch.step_timed(args.steps, DT, VI, PI)
+    prof = batch.profile()
+    ms_per_step = ms / args.steps
+    if world_size > 1:
+        t = torch.tensor([ms_per_step], device=f"cuda:{dev}")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms_per_step = float(t.item())
+        n_total = torch.tensor([nb], device=f"cuda:{dev}", dtype=torch.float64)
+        torch.distributed.all_reduce(n_total)
+        nb_all = float(n_total.item())
+    else:
+        nb_all = float(nb)
+    value = nb_all / (ms_per_step / 1e3)
+
+    # end to end through the C ABI with pinned host buffers: forces in, transforms out
+    nbody = prof.bodies
+    forces = torch.zeros((nbody, 4), dtype=torch.float32).pin_memory()
+    xf_out = torch.empty((nbody, 4), dtype=torch.float32).pin_memory()
+    n_out = C.c_int64()
+    e2e_steps = max(3, args.steps // 2)
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    for _ in range(e2e_steps):
+        lib.check(lib.b2g_batch_set_forces(batch.h, forces.data_ptr(), nbody), "set_forces")
+        lib.check(lib.b2g_step(batch.h, DT, VI, PI, None), "step")
+        lib.check(lib.b2g_batch_read_states(batch.h, C.cast(xf_out.data_ptr(), C.POINTER(C.c_float)), None,
+                                            nbody, C.byref(n_out)), "read_states")
+    e2e_s = time.perf_counter() - t1
+    e2e_value = nb * e2e_steps / e2e_s * world_size
+
+    # roofline of the dominant kernel (the per-world solver CTA), from the last timed step
+    peak, peak_kind = _peaks()
+    sb = solve_bytes(prof.bodies, prof.touching, prof.joints)
+    achieved = sb / (prof.solve / 1e3) / 1e9 if prof.solve > 0 else None
+    step_b = step_bytes(prof.bodies, prof.fixtures, prof.contacts, prof.touching, prof.joints)
+
+    line = None
+    if rank == 0:
+        cpu = None
+        if world_size == 1 and not args.no_cpu:
+            threads = os.cpu_count() or 1
+            cpu_seeds = seeds[:: max(1, len(seeds) // args.cpu_worlds)][: args.cpu_worlds]
+            v, cnb, secs = cpu_sample(lib, cpu_seeds, args.warmup, args.steps, threads)
+            cpu = {"value": v, "unit": "body-steps/s", "cores": threads, "kind": "port",
+                   "sample": f"{len(cpu_seeds)} of the worlds ({cnb} bodies), steps {args.warmup + 1}-"
+                             f"{args.warmup + args.steps} of the same rollout, {secs:.1f} s on {threads} threads"}
+        kernels_per_step = 13
+        line = {
+            "metric": METRIC, "value": value, "unit": "body-steps/s", "n_gpus": world_size, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": f"batched {args.worlds} worlds per GPU, 16-8192 bodies log-uniform (pyramid / "
+                                   f"mixed drop / chains), 8/3 iterations, dt 1/60",
+                       "worlds": args.worlds * world_size, "bodies": int(nb_all), "fixtures_per_gpu": prof.fixtures,
+                       "contacts_per_gpu": prof.contacts, "touching_per_gpu": prof.touching,
+                       "joints_per_gpu": prof.joints, "l2": "state larger than L2 (no flush needed)",
+                       "parallelism": f"{world_size} independent world shards", "build_s": round(build_s, 1)},
+            "breakdown_ms": {"collide": prof.collide, "solve": prof.solve, "broadphase": prof.broadphase,
+                             "step": prof.step},
+            "step_bytes": step_b, "step_gbs": step_b / (ms_per_step / 1e3) / 1e9,
+            "roofline": {"kernel": "k_solve", "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": (achieved / peak) if achieved else None, "traffic": None,
+                         "peak_kind": f"{peak_kind} hbm_gbs", "bytes_per_launch": sb},
+            "cpu_baseline": cpu,
+            "e2e": {"value": e2e_value, "unit": "body-steps/s", "h2d_bytes_per_step": 16 * nbody,
+                    "d2h_bytes_per_step": 16 * nbody, "steps": e2e_steps},
+            "gpu_launches": kernels_per_step * args.steps,
+            "clocks": clocks.summary(),
+        }
+    batch.close()
+    if line:
+        print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=256)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--worlds", type=int, default=4096)
+    ap.add_argument("--ref-worlds", type=int, default=128)
+    ap.add_argument("--cpu-worlds", type=int, default=128)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    rank = int(os.environ.get("RANK", "0"))
+    world_size = int(os.environ.get("WORLD_SIZE", "1"))
+    if args.impl == "reference":
+        run_reference(args, rank)
+        return
+    if world_size > 1:
+        import torch  # noqa: PLC0415
+
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        torch.distributed.init_process_group("nccl")
+    run_ours(args, rank, world_size)
+    if world_size > 1:
+        import torch  # noqa: PLC0415
+
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

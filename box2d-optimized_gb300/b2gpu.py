@@ -163,7 +163,8 @@ class Lib:
     SYMBOLS = [
         "b2g_batch_create", "b2g_batch_destroy", "b2g_world_add", "b2g_world_count",
         "b2g_world_set_gravity", "b2g_world_set_flags", "b2g_bodies_add", "b2g_fixtures_add",
-        "b2g_joints_add", "b2g_world_sizes", "b2g_step", "b2g_step_n", "b2g_reserve",
+        "b2g_joints_add", "b2g_world_sizes", "b2g_step", "b2g_step_n", "b2g_step_timed",
+        "b2g_batch_set_forces", "b2g_reserve",
         "b2g_bodies_read", "b2g_bodies_write", "b2g_batch_read_states", "b2g_fixtures_read",
         "b2g_joints_read", "b2g_contacts_read", "b2g_events_enable", "b2g_events_drain",
         "b2g_profile_get", "b2g_solver_order", "b2g_collide", "b2g_pairs", "b2g_scene_build",
@@ -195,6 +196,8 @@ class Lib:
             "b2g_world_sizes": ([vp, i32, P(i32), P(i32), P(i32), P(i32)], C.c_int),
             "b2g_step": ([vp, f32, i32, i32, P(C.c_uint8)], C.c_int),
             "b2g_step_n": ([vp, f32, i32, i32, i32, i32], C.c_int),
+            "b2g_step_timed": ([vp, f32, i32, i32, i32, P(f32)], C.c_int),
+            "b2g_batch_set_forces": ([vp, vp, i64], C.c_int),
             "b2g_reserve": ([vp, i64], C.c_int),
             "b2g_bodies_read": ([vp, i32, i32, i32, P(Body)], C.c_int),
             "b2g_bodies_write": ([vp, i32, i32, i32, P(Body)], C.c_int),
@@ -285,6 +288,11 @@ class Batch:
 
     def step_n(self, n, dt=1 / 60, vi=8, pi=3, use_graph=False):
         self.lib.check(self.lib.b2g_step_n(self.h, dt, vi, pi, n, int(use_graph)), "b2g_step_n")
+
+    def step_timed(self, n, dt=1 / 60, vi=8, pi=3) -> float:
+        ms = C.c_float()
+        self.lib.check(self.lib.b2g_step_timed(self.h, dt, vi, pi, n, C.byref(ms)), "b2g_step_timed")
+        return ms.value
 
     def bodies(self, world):
         nb = self.sizes(world)[0]

@@ -477,6 +477,7 @@ int step_batch(Batch* b, float dt, int vi, int pi, const uint8_t* mask, bool syn
     CUDA_TRY(b, cudaMemsetAsync(b->counters.p + 1, 0, sizeof(unsigned long long), b->stream));
   }
   TRY(ensure_solver(b));
+  CUDA_TRY(b, cudaMemsetAsync(b->counters.p + 2, 0, sizeof(unsigned long long), b->stream));
   cudaEventRecord(b->ev[0], b->stream);
   if (need_bp) TRY(run_broadphase(b));
   KernelArgs a = make_args(b);
@@ -516,6 +517,9 @@ int step_batch(Batch* b, float dt, int vi, int pi, const uint8_t* mask, bool syn
     b->profile.fixtures = b->NF;
     b->profile.contacts = b->NC;
     b->profile.joints = b->NJ;
+    unsigned long long touching = 0;
+    cudaMemcpy(&touching, b->counters.p + 2, sizeof(touching), cudaMemcpyDeviceToHost);
+    b->profile.touching = (int64_t)touching;
     return check_status(b);
   }
   return B2G_OK;
@@ -801,6 +805,35 @@ B2G_API int b2g_step_n(b2g_batch* b, float dt, int32_t vi, int32_t pi, int32_t n
   if (!b || n < 0) return B2G_E_INVALID_ARG;
   (void)use_graph;
   for (int i = 0; i < n; ++i) TRY(step_batch(b, dt, vi, pi, nullptr, i == n - 1));
+  return B2G_OK;
+}
+
+B2G_API int b2g_step_timed(b2g_batch* b, float dt, int32_t vi, int32_t pi, int32_t n, float* device_ms) {
+  if (!b || n < 0 || b->device < 0) return B2G_E_INVALID_ARG;
+  if (b->structure_dirty) TRY(upload_all(b));
+  cudaEvent_t e0, e1;
+  cudaSetDevice(b->device);
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  cudaEventRecord(e0, b->stream);
+  int st = B2G_OK;
+  for (int i = 0; i < n && st == B2G_OK; ++i) st = step_batch(b, dt, vi, pi, nullptr, i == n - 1);
+  cudaEventRecord(e1, b->stream);
+  cudaEventSynchronize(e1);
+  float ms = 0.0f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (device_ms) *device_ms = ms;
+  return st;
+}
+
+B2G_API int b2g_batch_set_forces(b2g_batch* b, const float* f4, int64_t n_bodies) {
+  if (!b || !f4 || n_bodies < 0 || b->device < 0) return B2G_E_INVALID_ARG;
+  if (b->structure_dirty) TRY(upload_all(b));
+  if (n_bodies != b->NB) return B2G_E_INVALID_ARG;
+  if (n_bodies) CUDA_TRY(b, cudaMemcpyAsync(b->force.p, f4, n_bodies * sizeof(float4), cudaMemcpyHostToDevice, b->stream));
+  b->host_state_stale = true;
   return B2G_OK;
 }
 

@@ -388,6 +388,7 @@ __global__ void __launch_bounds__(SOLVER_THREADS) k_solve(KernelArgs a) {
   if (threadIdx.x == 0) {
     a.ncolors[2 * w] = ncc;
     a.ncolors[2 * w + 1] = njc;
+    atomicAdd(&a.counters[2], (unsigned long long)nsc);
   }
 
   // 5. warm start contacts, then joint InitVelocityConstraints, colour by colour

@@ -287,6 +287,14 @@ B2G_API int b2g_step(b2g_batch* b, float dt, int32_t velocity_iterations,
  * replayed (buffers are sized on the first step; see b2g_reserve). */
 B2G_API int b2g_step_n(b2g_batch* b, float dt, int32_t velocity_iterations,
                        int32_t position_iterations, int32_t n, int32_t use_graph);
+/* n steps back to back, timed with CUDA events recorded on the engine's stream around them;
+ * *device_ms receives the elapsed device time (all n steps). */
+B2G_API int b2g_step_timed(b2g_batch* b, float dt, int32_t velocity_iterations,
+                           int32_t position_iterations, int32_t n, float* device_ms);
+/* Host -> device copy of the force and torque of every body of the batch (device order = world,
+ * then creation order): f4 holds (fx, fy, torque, unused) per body, n_bodies records. The
+ * per-step input of an end-to-end loop (b2Body::ApplyForce / ApplyTorque on every body). */
+B2G_API int b2g_batch_set_forces(b2g_batch* b, const float* f4, int64_t n_bodies);
 /* Pre-size the pair/contact buffers to at least `contacts` entries in total. */
 B2G_API int b2g_reserve(b2g_batch* b, int64_t contacts);
 

@@ -39,6 +39,17 @@ def _first_diff(g, o):
     return "no difference"
 
 
+def _contact_key(c):
+    """The meaningful content of a contact record: slots beyond point_count (and the local
+    normal/point of an empty manifold) are left over from earlier steps and never read."""
+    m = c.manifold
+    pts = tuple((m.points[j].local_point[0], m.points[j].local_point[1], m.points[j].normal_impulse,
+                 m.points[j].tangent_impulse, m.points[j].id) for j in range(m.point_count))
+    geo = (m.type, tuple(m.local_normal), tuple(m.local_point)) if m.point_count else ()
+    return (c.fixture_a, c.fixture_b, c.flags, c.friction, c.restitution, c.restitution_threshold,
+            c.tangent_speed, m.point_count, geo, pts)
+
+
 def _rollout(lib, orc, kind, n, seed=1, p0=1.0, p1=0.6, steps=60, vi=8, pi=3, gravity=(0.0, -10.0)):
     batch = G.Batch(lib, device=0)
     w = batch.add_world(*gravity)
@@ -53,7 +64,7 @@ def _rollout(lib, orc, kind, n, seed=1, p0=1.0, p1=0.6, steps=60, vi=8, pi=3, gr
     gc = batch.contacts(w)
     oc = ow.contacts()
     assert len(gc) == len(oc)
-    assert all(bytes(x) == bytes(y) for x, y in zip(gc, oc)), "contact lists differ"
+    assert [_contact_key(x) for x in gc] == [_contact_key(y) for y in oc], "contact lists differ"
     gj, oj = batch.joints(w), ow.joints()
     for x, y in zip(gj, oj):
         assert list(x.impulse) == list(y.impulse)
