@@ -211,9 +211,10 @@ def test_pairs_kernel_matches_oracle(lib, orc):
         c = rng.uniform(-50, 50, (n, 2)).astype(np.float32)
         h = rng.uniform(0.05, 1.5, (n, 2)).astype(np.float32)
         aabb = np.concatenate([c - h, c + h], axis=1).astype(np.float32)
-        cap = 4 * n + 64
+        fp = aabb.ctypes.data_as(C.POINTER(C.c_float))
+        cap = int(orc.orc_pairs(fp, n, None, 0)) + 16
         ref = np.zeros(cap, np.uint64)
-        nref = orc.orc_pairs(aabb.ctypes.data_as(C.POINTER(C.c_float)), n, ref.ctypes.data_as(C.POINTER(C.c_uint64)), cap)
+        nref = orc.orc_pairs(fp, n, ref.ctypes.data_as(C.POINTER(C.c_uint64)), cap)
         d_aabb = torch.from_numpy(aabb).cuda()
         d_pairs = torch.zeros(cap, dtype=torch.int64, device="cuda")
         npairs = C.c_int64()
