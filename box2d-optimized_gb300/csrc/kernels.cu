@@ -728,7 +728,7 @@ __device__ __forceinline__ bool accept_pair(const KernelArgs& a, int f, int g, i
   return hasCollider(sf, sg) || hasCollider(sg, sf);
 }
 
-#define BP_STACK 64
+#define BP_STACK 96
 
 // Pair search for one emitter fixture over its world's subtree. Count mode writes the number of
 // accepted partners; emit mode writes the keys f << 32 | g at the scanned offset and sorts them.

@@ -136,7 +136,7 @@ __global__ void kp_traverse(const float4* aabb, const int* val, int n, const int
   }  // in the emit pass `counts` is the offsets array
   if (n > 1) {
     float4 box = aabb[f];
-    int stack[64];
+    int stack[96];
     int sp = 0;
     stack[sp++] = 0;
     int visits = 0;
@@ -158,7 +158,7 @@ __global__ void kp_traverse(const float4* aabb, const int* val, int n, const int
             ++cnt;
           }
         } else if (p_overlap(box, naabb[c])) {
-          if (sp < 64) stack[sp++] = c;
+          if (sp < 96) stack[sp++] = c;
           else atomicOr(status, 1u);
         }
       }
@@ -275,4 +275,61 @@ extern "C" B2G_API int b2g_pairs(const float* d_aabbs, int32_t n, uint64_t* d_pa
   cudaStreamSynchronize((cudaStream_t)stream);
   cudaFree(base);
   return st;
+}
+
+// ------------------------------------------------------------------------------------------
+// Allocation-free variant of b2g_pairs.
+//
+// Its scratch is one file-scope device array, so a call allocates nothing. Every GPU that loads
+// the library holds this array (B2G_PAIRS_STATIC_SCRATCH_BYTES) until the process exits, and
+// every call shares it: calls that overlap on the GPU (different streams, or host threads)
+// race on it and must be serialised by the caller. Each call re-initialises the parts that must
+// start at zero (status word, arrival counters, the count terminator) before using them.
+#include <mutex>
+
+namespace b2g {
+
+#define B2G_PAIRS_STATIC_SCRATCH_BYTES (16u << 20)
+static __device__ __align__(256) unsigned char g_pairs_static_scratch[B2G_PAIRS_STATIC_SCRATCH_BYTES];
+
+// Device address of the array, looked up once per device with that device current (the array's
+// name on the host is only a stand-in, not a device address). The first call on a device does
+// this set-up.
+static std::mutex g_static_mutex;
+static void* g_static_ptr[64] = {};
+
+static int static_scratch_for_current_device(void** out) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return B2G_E_CUDA;
+  std::lock_guard<std::mutex> lock(g_static_mutex);
+  if (!g_static_ptr[dev]) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_pairs_static_scratch);
+    if (e != cudaSuccess || !p) return B2G_E_CUDA;
+    g_static_ptr[dev] = p;
+  }
+  *out = g_static_ptr[dev];
+  return B2G_OK;
+}
+
+}  // namespace b2g
+
+extern "C" B2G_API int b2g_pairs_static(const float* d_aabbs, int32_t n, uint64_t* d_pairs, int64_t cap,
+                                        int64_t* n_pairs, void* stream) {
+  if (n < 0 || cap < 0 || (n > 0 && !d_aabbs) || (cap > 0 && !d_pairs)) return B2G_E_INVALID_ARG;
+  if (n > B2G_PAIRS_STATIC_MAX) return B2G_E_CAPACITY;
+  if (n == 0) {
+    if (n_pairs) *n_pairs = 0;
+    return B2G_OK;
+  }
+  void* base = nullptr;
+  int st = b2g::static_scratch_for_current_device(&base);
+  if (st != B2G_OK) return st;
+  size_t cub_bytes = 0, cub_scan = 0;
+  cub::DeviceRadixSort::SortPairs((void*)nullptr, cub_bytes, (uint32_t*)nullptr, (uint32_t*)nullptr, (int*)nullptr,
+                                  (int*)nullptr, n, 0, 30);
+  cub::DeviceScan::ExclusiveSum((void*)nullptr, cub_scan, (int*)nullptr, (int*)nullptr, n + 1);
+  b2g::PairsScratch s = b2g::pairs_scratch_layout(base, n, cub_bytes > cub_scan ? cub_bytes : cub_scan);
+  if (s.total_bytes > B2G_PAIRS_STATIC_SCRATCH_BYTES) return B2G_E_CAPACITY;
+  return b2g::pairs_run((const float4*)d_aabbs, n, d_pairs, cap, n_pairs, s, (cudaStream_t)stream);
 }

@@ -345,6 +345,21 @@ B2G_API int b2g_collide(const b2g_shape* d_shape_a, const float* d_xf_a, const b
 B2G_API int b2g_pairs(const float* d_aabbs, int32_t n, uint64_t* d_pairs, int64_t cap,
                       int64_t* n_pairs, void* stream);
 
+/* The same pair search as b2g_pairs, for callers that cannot allocate device memory when they
+ * call it: a game or robotics loop that must not call cudaMalloc/cudaFree inside its frame (the
+ * calls synchronise the device and can stall for milliseconds), or a plug-in running inside a host
+ * application that owns the device's memory budget. No counterpart in the reference (its
+ * broadphase runs on the CPU and allocates from its own pools).
+ * Its scratch is a fixed 16 MiB array in device memory that every GPU loading the library keeps
+ * until the process exits; n may be at most B2G_PAIRS_STATIC_MAX (larger n returns
+ * B2G_E_CAPACITY without touching anything). The first call on a device looks up that array's
+ * device address, so make it before any stream capture. All calls share the array: calls that
+ * overlap on the GPU (two streams, or two host threads) race and must be serialised by the caller.
+ * Same outputs, capacity rule and status codes as b2g_pairs. */
+#define B2G_PAIRS_STATIC_MAX 131072
+B2G_API int b2g_pairs_static(const float* d_aabbs, int32_t n, uint64_t* d_pairs, int64_t cap,
+                             int64_t* n_pairs, void* stream);
+
 /* ---- scenes ------------------------------------------------------------------------------------ */
 /* Builds one of the seeded benchmark scenes into `world` through the b2World facade calls
  * (box2d-optimized_gb300/scenes/scenes.h). kind: 0 pyramid(rows=n, density=p0, friction=p1),
