@@ -127,16 +127,15 @@ class RequestResult(C.Structure):
                 ("checksum", C.c_float * 4)]
 
 
-RECORD_SIZES = {"b2g_shape": 152, "b2g_manifold_point": 20, "b2g_manifold": 64,
-                "b2g_body": 100}
+RECORD_SIZES = {"b2g_shape": 152, "b2g_manifold_point": 20, "b2g_manifold": 64, "b2g_body": 96}
 
 
 def body_array_to_numpy(arr) -> dict:
     """Body records -> dict of numpy arrays (xf[n,4], c[n,2], a[n], v[n,2], w[n], type[n])."""
     n = len(arr)
     raw = np.frombuffer(arr, dtype=np.uint8).reshape(n, C.sizeof(Body))
-    f = raw[:, :92].copy().view(np.float32).reshape(n, 23)
-    t = raw[:, 92:96].copy().view(np.int32).reshape(n)
+    f = raw[:, :88].copy().view(np.float32).reshape(n, 22)
+    t = raw[:, 88:92].copy().view(np.int32).reshape(n)
     return {"xf": f[:, 0:4], "c": f[:, 4:6], "a": f[:, 6], "v": f[:, 7:9], "w": f[:, 9],
             "local_center": f[:, 10:12], "mass": f[:, 12], "inv_mass": f[:, 13],
             "inertia": f[:, 14], "inv_inertia": f[:, 15], "type": t}

@@ -187,7 +187,7 @@ typedef struct b2g_body {
   float torque;
   int32_t type;
   uint32_t flags;
-} b2g_body; /* 100 bytes */
+} b2g_body; /* 96 bytes */
 
 typedef struct b2g_fixture {
   b2g_shape shape;

@@ -1,0 +1,143 @@
+"""Generates the golden vectors in tests/golden/ from the reference engine.
+
+Run where the reference sources are checked out and oracle/_ref/libb2ref.so is built
+(`make -C oracle ref`):
+
+    python tests/golden/make_golden.py
+
+Every vector is an output of the reference's own code (compiled from its sources) on seeded
+inputs: polygon hulls and mass data (b2PolygonShape::Set / SetAsBox / ComputeMass), manifolds of
+the five collide functions, one replayed solver step (b2Island::Solve in a given constraint
+order) on exported world states, and the final state of 256-step reference rollouts.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import sys
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+sys.path.insert(0, str(HERE.parent))
+import oracle_bind as ob  # noqa: E402
+
+G = ob.G
+
+
+def rec_bytes(arr):
+    return np.frombuffer(b"".join(bytes(x) for x in arr), dtype=np.uint8)
+
+
+def shapes(ref, rng):
+    n = 400
+    counts = rng.integers(3, 9, n)
+    verts = rng.uniform(-1, 1, (n, 16)).astype(np.float32)
+    hulls, masses = [], []
+    for i in range(n):
+        s = G.Shape()
+        ref.ref_polygon_set(verts[i].ctypes.data_as(C.POINTER(C.c_float)), int(counts[i]), s)
+        m = (C.c_float * 4)()
+        ref.ref_shape_mass(s, 1.7, m)
+        hulls.append(s)
+        masses.append(list(m))
+    boxes = rng.uniform(0.05, 2.0, (100, 5)).astype(np.float32)
+    boxes[:, 2:4] = rng.uniform(-50, 50, (100, 2))
+    boxes[:, 4] = rng.uniform(-3, 3, 100)
+    box_out = []
+    for b in boxes:
+        s = G.Shape()
+        ref.ref_polygon_box(float(b[0]), float(b[1]), float(b[2]), float(b[3]), float(b[4]), 1, s)
+        box_out.append(s)
+    np.savez_compressed(HERE / "shapes.npz", counts=counts, verts=verts, hulls=rec_bytes(hulls),
+                        masses=np.array(masses, np.float32), boxes=boxes, box_shapes=rec_bytes(box_out))
+
+
+def rand_shape(ref, rng, kind):
+    s = G.Shape()
+    if kind == 0:
+        s.type = 0
+        s.radius = float(rng.uniform(0.1, 0.6))
+        s.vertices[0][0] = float(rng.uniform(-0.2, 0.2))
+        s.vertices[0][1] = float(rng.uniform(-0.2, 0.2))
+    elif kind == 1:
+        s.type = 1
+        s.radius = 0.01
+        for i in range(4):
+            s.vertices[i][0] = float(rng.uniform(-2, 2))
+            s.vertices[i][1] = float(rng.uniform(-2, 2))
+        s.one_sided = int(rng.integers(0, 2))
+    else:
+        n = int(rng.integers(3, 9))
+        xy = rng.uniform(-0.6, 0.6, 2 * n).astype(np.float32)
+        if rng.uniform() < 0.3:
+            ref.ref_polygon_box(float(rng.uniform(0.1, 0.5)), float(rng.uniform(0.1, 0.5)), 0, 0, 0, 0, s)
+        else:
+            ref.ref_polygon_set(xy.ctypes.data_as(C.POINTER(C.c_float)), n, s)
+    return s
+
+
+def collide(ref, rng):
+    kinds = [(0, 0), (2, 0), (2, 2), (1, 0), (1, 2)]
+    n = 1500
+    A, B, M = [], [], []
+    xa = np.zeros((n, 4), np.float32)
+    xb = np.zeros((n, 4), np.float32)
+    for i in range(n):
+        ka, kb = kinds[i % 5]
+        a, b = rand_shape(ref, rng, ka), rand_shape(ref, rng, kb)
+        for x in (xa, xb):
+            ang = rng.uniform(-3.2, 3.2)
+            x[i] = (rng.uniform(-0.7, 0.7), rng.uniform(-0.7, 0.7), np.sin(ang), np.cos(ang))
+        m = G.Manifold()
+        ref.ref_collide(a, (C.c_float * 4)(*xa[i]), b, (C.c_float * 4)(*xb[i]), m)
+        A.append(a)
+        B.append(b)
+        M.append(m)
+    np.savez_compressed(HERE / "collide.npz", a=rec_bytes(A), b=rec_bytes(B), xa=xa, xb=xb, m=rec_bytes(M))
+
+
+def replay(ref, orc, name, kind, n, seed, p0, warm, vi, pi):
+    """World state after `warm` reference steps, and the reference's next step replayed in the
+    oracle's constraint order (the oracle runs with libm trig, like the reference)."""
+    rw = ob.RefWorld(ref, kind, seed=seed, n=n, p0=p0, p1=0.6)
+    rw.step(warm, vi=vi, pi=pi)
+    bodies, fixtures, joints, contacts = rw.bodies(), rw.fixtures(), rw.joints(), rw.contacts()
+    orc.orc_set_libm_trig(1)
+    ow = ob.OracleWorld(orc, (0.0, -10.0), list(bodies), list(fixtures), list(joints), list(contacts), inv_dt0=60.0)
+    ow.step(1, 1 / 60, vi, pi)
+    orc.orc_set_libm_trig(0)
+    pairs, jorder = ow.last_order()
+    arr = (C.c_int32 * max(len(pairs), 1))(*pairs)
+    jar = (C.c_int32 * max(len(jorder), 1))(*jorder)
+    assert ref.ref_replay_step(rw.h, 1 / 60, vi, pi, arr, len(pairs) // 2, jar, len(jorder)) == 0
+    after = rw.bodies()
+    np.savez_compressed(HERE / f"replay_{name}.npz", bodies=rec_bytes(bodies), fixtures=rec_bytes(fixtures),
+                        joints=rec_bytes(joints) if joints else np.zeros(0, np.uint8), contacts=rec_bytes(contacts),
+                        order_pairs=np.array(pairs, np.int32), order_joints=np.array(jorder, np.int32),
+                        after=rec_bytes(after), vi=vi, pi=pi)
+
+
+def rollout(ref, name, kind, n, seed, p0, steps, vi, pi):
+    rw = ob.RefWorld(ref, kind, seed=seed, n=n, p0=p0, p1=0.6)
+    start = rw.bodies()
+    rw.step(steps, vi=vi, pi=pi)
+    np.savez_compressed(HERE / f"rollout_{name}.npz", start=rec_bytes(start), final=rec_bytes(rw.bodies()),
+                        steps=steps, vi=vi, pi=pi)
+
+
+def main():
+    ref = ob.Ref()
+    orc = ob.Oracle()
+    rng = np.random.default_rng(20261203)
+    shapes(ref, rng)
+    collide(ref, rng)
+    replay(ref, orc, "pyramid", G.SCENE_PYRAMID, 20, 1, 1.0, 40, 8, 3)
+    replay(ref, orc, "mixed", G.SCENE_MIXED_DROP, 300, 3, 0.0, 150, 8, 3)
+    replay(ref, orc, "chains", G.SCENE_CHAINS, 10, 2, 150.0, 100, 10, 4)
+    rollout(ref, "pyramid", G.SCENE_PYRAMID, 20, 1, 1.0, 256, 8, 3)
+    print("golden vectors written to", HERE)
+
+
+if __name__ == "__main__":
+    main()

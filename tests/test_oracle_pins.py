@@ -1,0 +1,172 @@
+"""Pins of the CPU oracle (and of the engine's host-side set-up) to the reference.
+
+Two sources of truth:
+* tests/golden/*.npz - outputs of the reference's own code on seeded inputs (generator:
+  tests/golden/make_golden.py), usable everywhere;
+* the reference compiled from its sources (oracle/_ref), where it is present: live comparisons
+  on fresh random inputs.
+Integer outputs (point counts, feature ids, pair sets) are compared exactly; float outputs of
+shapes and collide functions bit for bit; one replayed solver step within 1e-5 relative (bit for
+bit where the host's libm matches the reference's); rollouts by physical measures.
+"""
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import b2gpu as G
+import oracle_bind as ob
+
+GOLD = Path(__file__).resolve().parent / "golden"
+
+
+def recs(cls, raw):
+    raw = bytes(np.asarray(raw, np.uint8))
+    n = len(raw) // C.sizeof(cls)
+    return list((cls * n).from_buffer_copy(raw)) if n else []
+
+
+def test_oracle_shapes_vs_golden(orc):
+    g = np.load(GOLD / "shapes.npz")
+    hulls = recs(G.Shape, g["hulls"])
+    for i, (cnt, v) in enumerate(zip(g["counts"], g["verts"])):
+        s = G.Shape()
+        orc.orc_polygon_set(np.ascontiguousarray(v).ctypes.data_as(C.POINTER(C.c_float)), int(cnt), s)
+        assert bytes(s) == bytes(hulls[i]), i
+        m = (C.c_float * 4)()
+        orc.orc_shape_mass(s, 1.7, m)
+        assert np.array_equal(np.array(list(m), np.float32), g["masses"][i]), i
+    boxes = recs(G.Shape, g["box_shapes"])
+    for b, ref_s in zip(g["boxes"], boxes):
+        s = G.Shape()
+        orc.orc_polygon_box(*[float(x) for x in b], 1, s)
+        # oriented boxes use the host libm sinf/cosf, as b2Rot::Set does: equal up to libm ulps
+        np.testing.assert_allclose(np.frombuffer(bytes(s), np.float32)[4:], np.frombuffer(bytes(ref_s), np.float32)[4:],
+                                   rtol=2e-6, atol=2e-5)
+
+
+def test_oracle_collide_vs_golden(orc):
+    g = np.load(GOLD / "collide.npz")
+    A, B, M = recs(G.Shape, g["a"]), recs(G.Shape, g["b"]), recs(G.Manifold, g["m"])
+    touching = 0
+    for i in range(len(A)):
+        m = G.Manifold()
+        orc.orc_collide(A[i], (C.c_float * 4)(*g["xa"][i]), B[i], (C.c_float * 4)(*g["xb"][i]), m)
+        r = M[i]
+        assert m.point_count == r.point_count, i
+        if r.point_count:
+            touching += 1
+            assert m.type == r.type
+            for j in range(r.point_count):
+                assert m.points[j].id == r.points[j].id
+                assert tuple(m.points[j].local_point) == tuple(r.points[j].local_point)
+            assert tuple(m.local_normal) == tuple(r.local_normal)
+            assert tuple(m.local_point) == tuple(r.local_point)
+    assert touching > 300
+
+
+@pytest.mark.parametrize("name", ["pyramid", "mixed", "chains"])
+def test_oracle_replayed_step_vs_golden(orc, name):
+    """One step from an exported reference state; the reference's b2Island solved the constraints
+    in the order the oracle chooses, so the two steps differ only by libm rounding."""
+    g = np.load(GOLD / f"replay_{name}.npz")
+    bodies, fixtures = recs(G.Body, g["bodies"]), recs(G.Fixture, g["fixtures"])
+    joints, contacts = recs(G.Joint, g["joints"]), recs(G.Contact, g["contacts"])
+    orc.orc_set_libm_trig(1)
+    try:
+        ow = ob.OracleWorld(orc, (0.0, -10.0), bodies, fixtures, joints, contacts, inv_dt0=60.0)
+        ow.step(1, 1 / 60, int(g["vi"]), int(g["pi"]))
+        pairs, jorder = ow.last_order()
+    finally:
+        orc.orc_set_libm_trig(0)
+    assert pairs == list(g["order_pairs"]) and jorder == list(g["order_joints"])
+    got = G.body_array_to_numpy((G.Body * len(bodies))(*ow.bodies()))
+    exp = G.body_array_to_numpy((G.Body * len(bodies))(*recs(G.Body, g["after"])))
+    for k in ("c", "a", "v", "w", "xf"):
+        np.testing.assert_allclose(got[k], exp[k], rtol=1e-5, atol=1e-5, err_msg=k)
+
+
+def test_oracle_rollout_vs_reference_golden(orc):
+    """256-step pyramid (20 rows, density 1, friction 0.6): the oracle (engine order, portable
+    trig) against the reference's own rollout, by physical measures."""
+    g = np.load(GOLD / "rollout_pyramid.npz")
+    start = recs(G.Body, g["start"])
+    host_batch = _host_batch()
+    w = host_batch.add_world(0.0, -10.0)
+    host_batch.scene(w, G.SCENE_PYRAMID, n=20, p0=1.0, p1=0.6)
+    assert b"".join(bytes(b) for b in host_batch.bodies(w)) == b"".join(bytes(b) for b in start)
+    ow = ob.OracleWorld(orc, (0.0, -10.0), host_batch.bodies(w), host_batch.fixtures(w), host_batch.joints(w))
+    ow.step(int(g["steps"]), 1 / 60, int(g["vi"]), int(g["pi"]))
+    got = G.body_array_to_numpy((G.Body * len(start))(*ow.bodies()))
+    exp = G.body_array_to_numpy((G.Body * len(start))(*recs(G.Body, g["final"])))
+    dyn = exp["type"] == G.DYNAMIC
+    assert abs(got["c"][dyn, 1].max() - exp["c"][dyn, 1].max()) < 0.02  # settled stack height
+    assert np.abs(got["c"][dyn] - exp["c"][dyn]).max() < 0.1           # every box within a fifth of its size
+    assert np.abs(got["v"][dyn]).max() < 0.5 and np.abs(exp["v"][dyn]).max() < 0.5
+    host_batch.close()
+
+
+def _host_batch():
+    lib = G.Lib()
+    b = G.Batch.__new__(G.Batch)
+    b.lib = lib
+    h = C.c_void_p()
+    lib.check(lib.b2g_batch_create(-1, 0, C.byref(h)), "host batch")
+    b.h = h
+    return b
+
+
+# ------------------------------------------------------------------ live, where the reference is built
+def test_oracle_vs_reference_live(ref, orc):
+    rng = np.random.default_rng(99)
+    for _ in range(300):
+        n = int(rng.integers(3, 9))
+        xy = rng.uniform(-1, 1, 2 * n).astype(np.float32)
+        a, b = G.Shape(), G.Shape()
+        ref.ref_polygon_set(xy.ctypes.data_as(C.POINTER(C.c_float)), n, a)
+        orc.orc_polygon_set(xy.ctypes.data_as(C.POINTER(C.c_float)), n, b)
+        assert bytes(a) == bytes(b)
+
+
+@pytest.mark.parametrize("kind,n,seed,p0,warm,vi,pi", [
+    (G.SCENE_PYRAMID, 20, 1, 1.0, 30, 8, 3),
+    (G.SCENE_MIXED_DROP, 400, 5, 0.0, 200, 8, 3),
+    (G.SCENE_CHAINS, 15, 4, 200.0, 80, 10, 4),
+])
+def test_oracle_replay_vs_reference_live(ref, orc, kind, n, seed, p0, warm, vi, pi):
+    """The reference's b2Island::Solve replaying the oracle's order: bit-exact, 3 steps."""
+    rw = ob.RefWorld(ref, kind, seed=seed, n=n, p0=p0, p1=0.6)
+    rw.step(warm, vi=vi, pi=pi)
+    orc.orc_set_libm_trig(1)
+    try:
+        for _ in range(3):
+            ow = ob.OracleWorld(orc, (0.0, -10.0), list(rw.bodies()), list(rw.fixtures()), list(rw.joints()),
+                                list(rw.contacts()), inv_dt0=60.0)
+            ow.step(1, 1 / 60, vi, pi)
+            pairs, jorder = ow.last_order()
+            arr = (C.c_int32 * max(len(pairs), 1))(*pairs)
+            jar = (C.c_int32 * max(len(jorder), 1))(*jorder)
+            assert ref.ref_replay_step(rw.h, 1 / 60, vi, pi, arr, len(pairs) // 2, jar, len(jorder)) == 0
+            assert b"".join(bytes(b)[:40] for b in rw.bodies()) == b"".join(bytes(b)[:40] for b in ow.bodies())
+            rset = sorted((min(c.fixture_a, c.fixture_b), max(c.fixture_a, c.fixture_b)) for c in rw.contacts())
+            oset = sorted((min(c.fixture_a, c.fixture_b), max(c.fixture_a, c.fixture_b)) for c in ow.contacts())
+            assert rset == oset
+    finally:
+        orc.orc_set_libm_trig(0)
+
+
+@pytest.mark.parametrize("kind,n,seed,p0", [
+    (G.SCENE_PYRAMID, 20, 1, 1.0), (G.SCENE_MIXED_DROP, 500, 3, 0.0), (G.SCENE_CHAINS, 30, 2, 300.0),
+    (G.SCENE_BATCH_WORLD, 777, 5, 0.0)])
+def test_host_scene_setup_vs_reference_live(ref, kind, n, seed, p0):
+    """The engine's host-side set-up (facade -> shapes -> mass data -> joint defs) produces the
+    reference's body, fixture and joint state byte for byte."""
+    hb = _host_batch()
+    w = hb.add_world(0.0, -10.0)
+    hb.scene(w, kind, seed=seed, n=n, p0=p0, p1=0.6)
+    rw = ob.RefWorld(ref, kind, seed=seed, n=n, p0=p0, p1=0.6)
+    assert [bytes(x) for x in hb.bodies(w)] == [bytes(x) for x in rw.bodies()]
+    assert [bytes(x) for x in hb.fixtures(w)] == [bytes(x) for x in rw.fixtures()]
+    assert [bytes(x.def_)[:-8] for x in hb.joints(w)] == [bytes(x.def_)[:-8] for x in rw.joints()]
+    hb.close()
