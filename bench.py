@@ -235,7 +235,31 @@ def run_ours(args, rank, world_size):
     e2e_s = time.perf_counter() - t1
     e2e_value = nb * e2e_steps / e2e_s * world_size
 
-    # roofline of the dominant kernel (the per-world solver CTA), from the last timed step
+    # per-phase breakdown: one eager (non-graph) step after the timed region
+    lib.b2g_batch_set_graphs(batch.h, 0)
+    batch.step(DT, VI, PI)
+    lib.b2g_batch_set_graphs(batch.h, 1)
+    prof = batch.profile()
+
+    # plain per-world GPU Step: a sample of the same worlds, each stepped alone in its own batch
+    # (one world per launch sequence, no graph), over the same rollout window
+    plain = None
+    if not args.no_plain:
+        ps = seeds[:: max(1, len(seeds) // args.plain_worlds)][: args.plain_worlds]
+        p_bodies, p_ms = 0, 0.0
+        for s in ps:
+            one, nb1 = build_batch(lib, [s], dev)
+            lib.b2g_batch_set_graphs(one.h, 0)
+            one.step_timed(args.warmup, DT, VI, PI)
+            p_ms += one.step_timed(args.steps, DT, VI, PI)
+            p_bodies += nb1
+            one.close()
+        pv = p_bodies * args.steps / (p_ms / 1e3)
+        plain = {"value": pv, "unit": "body-steps/s", "sample": f"{len(ps)} of the worlds ({p_bodies} bodies), "
+                 f"each stepped alone, steps {args.warmup + 1}-{args.warmup + args.steps}",
+                 "ms_per_world_step": p_ms / (len(ps) * args.steps)}
+
+    # roofline of the dominant kernel (the per-world solver CTA), from the eager step
     peak, peak_kind = _peaks()
     sb = solve_bytes(prof.bodies, prof.touching, prof.joints)
     achieved = sb / (prof.solve / 1e3) / 1e9 if prof.solve > 0 else None
@@ -251,7 +275,7 @@ def run_ours(args, rank, world_size):
             cpu = {"value": v, "unit": "body-steps/s", "cores": threads, "kind": "port",
                    "sample": f"{len(cpu_seeds)} of the worlds ({cnb} bodies), steps {args.warmup + 1}-"
                              f"{args.warmup + args.steps} of the same rollout, {secs:.1f} s on {threads} threads"}
-        kernels_per_step = 13
+        kernels_per_step = 14  # collide, solve, 11 broadphase/diff kernels, clear forces
         line = {
             "metric": METRIC, "value": value, "unit": "body-steps/s", "n_gpus": world_size, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
@@ -269,6 +293,8 @@ def run_ours(args, rank, world_size):
                          "frac": (achieved / peak) if achieved else None, "traffic": None,
                          "peak_kind": f"{peak_kind} hbm_gbs", "bytes_per_launch": sb},
             "cpu_baseline": cpu,
+            "plain_gpu": plain,
+            "batched_over_plain": (value / world_size / plain["value"]) if plain else None,
             "e2e": {"value": e2e_value, "unit": "body-steps/s", "h2d_bytes_per_step": 16 * nbody,
                     "d2h_bytes_per_step": 16 * nbody, "steps": e2e_steps},
             "gpu_launches": kernels_per_step * args.steps,
@@ -289,6 +315,8 @@ def main():
     ap.add_argument("--ref-worlds", type=int, default=128)
     ap.add_argument("--cpu-worlds", type=int, default=128)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--plain-worlds", type=int, default=32)
+    ap.add_argument("--no-plain", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank = int(os.environ.get("RANK", "0"))

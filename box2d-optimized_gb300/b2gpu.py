@@ -163,7 +163,8 @@ class Lib:
         "b2g_batch_create", "b2g_batch_destroy", "b2g_world_add", "b2g_world_count",
         "b2g_world_set_gravity", "b2g_world_set_flags", "b2g_bodies_add", "b2g_fixtures_add",
         "b2g_joints_add", "b2g_world_sizes", "b2g_step", "b2g_step_n", "b2g_step_timed",
-        "b2g_batch_set_forces", "b2g_reserve",
+        "b2g_batch_set_forces", "b2g_batch_set_graphs", "b2g_debug_set_contact_capacity",
+        "b2g_pairs_static", "b2g_reserve",
         "b2g_bodies_read", "b2g_bodies_write", "b2g_batch_read_states", "b2g_fixtures_read",
         "b2g_joints_read", "b2g_contacts_read", "b2g_events_enable", "b2g_events_drain",
         "b2g_profile_get", "b2g_solver_order", "b2g_collide", "b2g_pairs", "b2g_scene_build",
@@ -197,6 +198,9 @@ class Lib:
             "b2g_step_n": ([vp, f32, i32, i32, i32, i32], C.c_int),
             "b2g_step_timed": ([vp, f32, i32, i32, i32, P(f32)], C.c_int),
             "b2g_batch_set_forces": ([vp, vp, i64], C.c_int),
+            "b2g_batch_set_graphs": ([vp, i32], C.c_int),
+            "b2g_debug_set_contact_capacity": ([vp, i64], C.c_int),
+            "b2g_pairs_static": ([vp, i32, vp, i64, P(i64), vp], C.c_int),
             "b2g_reserve": ([vp, i64], C.c_int),
             "b2g_bodies_read": ([vp, i32, i32, i32, P(Body)], C.c_int),
             "b2g_bodies_write": ([vp, i32, i32, i32, P(Body)], C.c_int),

@@ -66,6 +66,23 @@ static int ensure(Batch* b, DBuf<T>& buf, size_t n, bool keep = false) {
   return B2G_OK;
 }
 
+// Reallocates `buf` at exactly n elements (keeping the first min(n, old) when `keep`).
+template <typename T>
+static int resize_exact(Batch* b, DBuf<T>& buf, size_t n, bool keep) {
+  T* p = nullptr;
+  if (cudaMalloc(&p, n * sizeof(T)) != cudaSuccess) return B2G_E_OUT_OF_MEMORY;
+  if (keep && buf.p) cudaMemcpyAsync(p, buf.p, std::min(n, buf.cap) * sizeof(T), cudaMemcpyDeviceToDevice, b->stream);
+  cudaStreamSynchronize(b->stream);
+  if (buf.p) {
+    cudaFree(buf.p);
+    b->allocated -= buf.cap * sizeof(T);
+  }
+  buf.p = p;
+  buf.cap = n;
+  b->allocated += n * sizeof(T);
+  return B2G_OK;
+}
+
 template <typename T>
 static void release(Batch* b, DBuf<T>& buf) {
   if (buf.p) {
@@ -273,6 +290,13 @@ int upload_all(Batch* b) {
   TRY(ensure(b, b->jprio, NJ)); TRY(ensure(b, b->jready, NJ));
   TRY(ensure(b, b->status, 1)); TRY(ensure(b, b->counters, 4));
   b->NW = NW; b->NB = NB; b->NF = NF; b->NJ = NJ; b->NC = NC;
+  {
+    unsigned long long cnt[4] = {(unsigned long long)NC, 0, 0, 0};
+    CUDA_TRY(b, cudaMemcpyAsync(b->counters.p, cnt, sizeof(cnt), cudaMemcpyHostToDevice, b->stream));
+  }
+  b->h_wflags = wflags;
+  b->ccap = 0;
+  b->layout_version++;
   b->structure_dirty = false;
   b->device_state_valid = true;
   b->host_state_stale = false;
@@ -366,53 +390,87 @@ int download_state(Batch* b) {
   return B2G_OK;
 }
 
-// Solver scratch sized for the live contact count.
-static int ensure_solver(Batch* b) {
-  size_t nc = (size_t)std::max<int64_t>(b->NC, 1);
-  TRY(ensure(b, b->sc_list, nc)); TRY(ensure(b, b->vc, nc)); TRY(ensure(b, b->ccolor, nc));
-  TRY(ensure(b, b->corder, nc)); TRY(ensure(b, b->cprio, nc)); TRY(ensure(b, b->cready, nc));
-  TRY(ensure(b, b->inc_list, 2 * nc));
+// Contact-sized buffers (both contact lists, the pair list, solver scratch) at capacity `cap`.
+static int ensure_contact_capacity(Batch* b, int64_t want) {
+  if (want < b->ccap && b->ccap > 0) return B2G_OK;
+  int64_t cap = std::max<int64_t>(want + want / 2 + 1024, 4 * (int64_t)b->NF + 1024);
+  for (int k = 0; k < 2; ++k) {
+    bool keep = (k == b->cur);
+    TRY(ensure(b, b->ckey[k], (size_t)cap, keep)); TRY(ensure(b, b->cfix[k], (size_t)cap, keep));
+    TRY(ensure(b, b->cflags[k], (size_t)cap, keep)); TRY(ensure(b, b->cmat[k], (size_t)cap, keep));
+    TRY(ensure(b, b->cman[k], (size_t)cap, keep));
+  }
+  TRY(ensure(b, b->pairs, (size_t)cap));
+  TRY(ensure(b, b->sc_list, (size_t)cap)); TRY(ensure(b, b->vc, (size_t)cap)); TRY(ensure(b, b->ccolor, (size_t)cap));
+  TRY(ensure(b, b->corder, (size_t)cap)); TRY(ensure(b, b->cprio, (size_t)cap)); TRY(ensure(b, b->cready, (size_t)cap));
+  TRY(ensure(b, b->inc_list, 2 * (size_t)cap));
   if (b->events_on) {
-    int64_t want = 4 * (int64_t)nc + 1024;
-    TRY(ensure(b, b->events, (size_t)want));
+    TRY(ensure(b, b->events, (size_t)(4 * cap + 1024)));
     b->event_cap = (int64_t)b->events.cap;
   }
+  b->ccap = cap;
+  b->layout_version++;
   return B2G_OK;
 }
 
-// Broadphase + contact diff: the live contact list becomes the sorted, filtered pair list of the
-// current transforms (end of b2World::Solve, src/dynamics/b2_world.cpp:663-669).
-static int run_broadphase(Batch* b) {
-  if (b->NF == 0) {
-    b->NC = 0;
-    std::vector<int2> z(b->NW, make_int2(0, 0));
-    return upload(b, b->wc, z);
-  }
-  int bits = 32;
-  while ((1ll << (bits - 32)) < (long long)b->NW) ++bits;
+static KernelArgs step_args(Batch* b, float dt, int vi, int pi) {
   KernelArgs a = make_args(b);
-  launch_bp_build(a, b->NF, b->NW, b->cub_tmp.cap, bits, b->stream);
-  int total = 0;
-  CUDA_TRY(b, cudaMemcpyAsync(&total, b->poff.p + b->NF, sizeof(int), cudaMemcpyDeviceToHost, b->stream));
-  CUDA_TRY(b, cudaStreamSynchronize(b->stream));
-  int dst = b->cur ^ 1;
-  TRY(ensure(b, b->pairs, (size_t)total));
-  TRY(ensure(b, b->ckey[dst], (size_t)total)); TRY(ensure(b, b->cfix[dst], (size_t)total));
-  TRY(ensure(b, b->cflags[dst], (size_t)total)); TRY(ensure(b, b->cmat[dst], (size_t)total));
-  TRY(ensure(b, b->cman[dst], (size_t)total));
-  a = make_args(b);
-  launch_bp_emit(a, b->NF, b->stream);
-  launch_contact_diff(a, total, b->NC, b->cur, dst, b->stream);
-  CUDA_TRY(b, cudaGetLastError());
-  b->cur = dst;
-  b->NC = total;
-  return ensure_solver(b);
+  a.dt = dt;
+  a.inv_dt = dt > 0.0f ? 1.0f / dt : 0.0f;
+  a.vi = vi;
+  a.pi = pi;
+  a.nf = b->NF;
+  a.nw = b->NW;
+  a.ccap = b->ccap;
+  return a;
 }
 
-static int check_status(Batch* b) {
-  unsigned int st = 0;
-  CUDA_TRY(b, cudaMemcpyAsync(&st, b->status.p, sizeof(st), cudaMemcpyDeviceToHost, b->stream));
-  CUDA_TRY(b, cudaStreamSynchronize(b->stream));
+static int sort_bits(Batch* b) {
+  int bits = 32;
+  while ((1ll << (bits - 32)) < (long long)b->NW) ++bits;
+  return bits;
+}
+
+// Broadphase + contact diff enqueued on the stream with no host synchronisation: pair counts,
+// scan, emission and the diff read their sizes from device memory; when the pairs exceed the
+// buffers, emission and diff are skipped and the needed size is left in the overflow counter.
+// The live contact list moves to buffer cur ^ 1.
+static void enqueue_broadphase(Batch* b, const KernelArgs& a0, int src) {
+  KernelArgs a = a0;
+  launch_bp_build(a, b->NF, b->NW, b->cub_tmp.cap, sort_bits(b), b->stream);
+  launch_bp_emit(a, b->NF, b->stream);
+  launch_contact_diff(a, src, src ^ 1, b->stream);
+}
+
+// One Step enqueued: [broadphase if fixtures were added] -> collide -> solve -> broadphase ->
+// clear forces. `src` is the live contact buffer at entry; it flips once per broadphase.
+static void enqueue_step(Batch* b, float dt, int vi, int pi, bool initial_bp, int src, bool record_profile) {
+  KernelArgs a = step_args(b, dt, vi, pi);
+  if (record_profile) cudaEventRecord(b->ev[0], b->stream);
+  if (initial_bp) {
+    b->cur = src;
+    enqueue_broadphase(b, step_args(b, dt, vi, pi), src);
+    src ^= 1;
+  }
+  b->cur = src;
+  a = step_args(b, dt, vi, pi);
+  launch_collide(a, b->stream);
+  if (record_profile) cudaEventRecord(b->ev[1], b->stream);
+  if (dt > 0.0f) {
+    launch_solve(a, b->NW, b->stream);
+    if (record_profile) cudaEventRecord(b->ev[2], b->stream);
+    enqueue_broadphase(b, a, src);
+    src ^= 1;
+  } else if (record_profile) {
+    cudaEventRecord(b->ev[2], b->stream);
+  }
+  if (record_profile) cudaEventRecord(b->ev[3], b->stream);
+  b->cur = src;
+  launch_clear_forces(step_args(b, dt, vi, pi), b->NB, b->stream);
+  if (record_profile) cudaEventRecord(b->ev[4], b->stream);
+}
+
+static int check_status(Batch* b, unsigned int st) {
   if (st & B2G_DEV_NONFINITE) {
     set_error(b, "a world produced a non-finite body state");
     return B2G_E_WORLD_FAULT;
@@ -424,11 +482,8 @@ static int check_status(Batch* b) {
   return B2G_OK;
 }
 
-static int drain_device_events(Batch* b) {
+static int drain_device_events(Batch* b, unsigned long long n) {
   if (!b->events_on) return B2G_OK;
-  unsigned long long n = 0;
-  CUDA_TRY(b, cudaMemcpyAsync(&n, b->counters.p + 1, sizeof(n), cudaMemcpyDeviceToHost, b->stream));
-  CUDA_TRY(b, cudaStreamSynchronize(b->stream));
   int64_t cnt = std::min<int64_t>((int64_t)n, b->event_cap);
   std::vector<EventDev> ev(cnt);
   if (cnt) CUDA_TRY(b, cudaMemcpy(ev.data(), b->events.p, cnt * sizeof(EventDev), cudaMemcpyDeviceToHost));
@@ -442,13 +497,74 @@ static int drain_device_events(Batch* b) {
     o.old_manifold = e.old;
     b->host_events.push_back(o);
   }
-  CUDA_TRY(b, cudaMemsetAsync(b->counters.p + 1, 0, sizeof(unsigned long long), b->stream));
   return B2G_OK;
 }
 
-// One b2World::Step (src/dynamics/b2_world.cpp:1108-1171) for the worlds selected by mask:
-// [broadphase if fixtures were added] -> collide -> solve -> broadphase -> clear forces.
+// Reads the step's counters and status word (one small copy), and recovers from a pair-buffer
+// overflow: the overflowing broadphase skipped its emission, so the live list is still the
+// pre-broadphase one (with this step's manifolds); grow the buffers and redo the broadphase.
+static int finish_step(Batch* b, int live_before_last_bp) {
+  b->h_readback[4] = 0;
+  CUDA_TRY(b, cudaMemcpyAsync(b->h_readback, b->counters.p, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                              b->stream));
+  CUDA_TRY(b, cudaMemcpyAsync(b->h_readback + 4, b->status.p, sizeof(unsigned int), cudaMemcpyDeviceToHost, b->stream));
+  CUDA_TRY(b, cudaStreamSynchronize(b->stream));
+  unsigned long long* r = b->h_readback;
+  unsigned long long overflow = r[B2G_CNT_OVERFLOW];
+  unsigned int status_word = (unsigned int)(r[4] & 0xffffffffull);
+  int guard = 0;
+  while (overflow) {
+    if (++guard > 8) {
+      set_error(b, "pair buffer kept overflowing");
+      return B2G_E_CAPACITY;
+    }
+    b->cur = live_before_last_bp;
+    TRY(ensure_contact_capacity(b, (int64_t)overflow));
+    CUDA_TRY(b, cudaMemsetAsync(b->counters.p + B2G_CNT_OVERFLOW, 0, sizeof(unsigned long long), b->stream));
+    KernelArgs a = step_args(b, b->last_dt, b->last_vi, b->last_pi);
+    enqueue_broadphase(b, a, b->cur);
+    b->cur ^= 1;
+    CUDA_TRY(b, cudaMemcpyAsync(b->h_readback, b->counters.p, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                                b->stream));
+    CUDA_TRY(b, cudaStreamSynchronize(b->stream));
+    overflow = r[B2G_CNT_OVERFLOW];
+  }
+  b->NC = (int64_t)r[B2G_CNT_CONTACTS];
+  TRY(drain_device_events(b, r[B2G_CNT_EVENTS]));
+  b->profile.touching = (int64_t)r[B2G_CNT_TOUCHING];
+  return check_status(b, status_word);
+}
+
+static void invalidate_graphs(Batch* b) {
+  for (int k = 0; k < 2; ++k) {
+    if (b->graph_exec[k]) cudaGraphExecDestroy(b->graph_exec[k]);
+    b->graph_exec[k] = nullptr;
+  }
+}
+
+// Captures one Step per live-buffer parity; a replay does the whole Step with no host work.
+static int capture_graphs(Batch* b, float dt, int vi, int pi) {
+  invalidate_graphs(b);
+  int saved = b->cur;
+  for (int parity = 0; parity < 2; ++parity) {
+    cudaGraph_t g = nullptr;
+    CUDA_TRY(b, cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+    enqueue_step(b, dt, vi, pi, false, parity, false);
+    CUDA_TRY(b, cudaStreamEndCapture(b->stream, &g));
+    CUDA_TRY(b, cudaGraphInstantiate(&b->graph_exec[parity], g, 0));
+    cudaGraphDestroy(g);
+  }
+  b->cur = saved;
+  b->graph_dt = dt;
+  b->graph_vi = vi;
+  b->graph_pi = pi;
+  b->graph_version = b->layout_version;
+  return B2G_OK;
+}
+
+// One b2World::Step (src/dynamics/b2_world.cpp:1108-1171) for the worlds selected by mask.
 int step_batch(Batch* b, float dt, int vi, int pi, const uint8_t* mask, bool sync) {
+  (void)sync;
   if (!(dt >= 0.0f) || vi < 0 || pi < 0) {
     set_error(b, "invalid step arguments");
     return B2G_E_INVALID_ARG;
@@ -458,71 +574,80 @@ int step_batch(Batch* b, float dt, int vi, int pi, const uint8_t* mask, bool syn
     return B2G_E_CUDA;
   }
   CUDA_TRY(b, cudaSetDevice(b->device));
-  if (b->structure_dirty) TRY(upload_all(b));
+  if (b->structure_dirty) {
+    TRY(upload_all(b));
+    invalidate_graphs(b);
+  }
   if (b->NW == 0) return B2G_OK;
+  if (!b->h_readback) CUDA_TRY(b, cudaMallocHost(&b->h_readback, 8 * sizeof(unsigned long long)));
   bool need_bp = false;
+  bool all_active = true;
   std::vector<int> wflags(b->NW);
   for (int w = 0; w < b->NW; ++w) {
     HostWorld& hw = b->worlds[w];
     int f = hw.flags & ~(B2G_WF_ACTIVE | B2G_WF_NEW_CONTACTS);
     if (!mask || mask[w]) f |= B2G_WF_ACTIVE;
+    else all_active = false;
     wflags[w] = f;
     if (hw.flags & B2G_WF_NEW_CONTACTS) need_bp = true;
     hw.flags &= ~B2G_WF_NEW_CONTACTS;
   }
-  TRY(upload(b, b->wflags, wflags));
+  if (wflags != b->h_wflags) {
+    TRY(upload(b, b->wflags, wflags));
+    b->h_wflags = wflags;
+  }
+  TRY(ensure_contact_capacity(b, b->NC));
   CUDA_TRY(b, cudaMemsetAsync(b->status.p, 0, sizeof(unsigned int), b->stream));
-  if (b->events_on) {
-    b->host_events.clear();
-    CUDA_TRY(b, cudaMemsetAsync(b->counters.p + 1, 0, sizeof(unsigned long long), b->stream));
+  CUDA_TRY(b, cudaMemsetAsync(b->counters.p + 1, 0, 3 * sizeof(unsigned long long), b->stream));
+  if (b->events_on) b->host_events.clear();
+  b->last_dt = dt;
+  b->last_vi = vi;
+  b->last_pi = pi;
+  int entry = b->cur;
+  bool graph = b->use_graphs && !need_bp && !b->events_on && all_active && dt > 0.0f;
+  if (graph && (!b->graph_exec[0] || b->graph_version != b->layout_version || b->graph_dt != dt ||
+                b->graph_vi != vi || b->graph_pi != pi))
+    TRY(capture_graphs(b, dt, vi, pi));
+  if (need_bp) {
+    // fixtures were added or bodies moved: find contacts first (b2_world.cpp:1113-1122), and
+    // make sure the list is complete before any kernel reads it
+    KernelArgs a = step_args(b, dt, vi, pi);
+    enqueue_broadphase(b, a, b->cur);
+    b->cur ^= 1;
+    TRY(finish_step(b, b->cur ^ 1));
+    CUDA_TRY(b, cudaMemsetAsync(b->counters.p + 1, 0, 3 * sizeof(unsigned long long), b->stream));
+    entry = b->cur;
   }
-  TRY(ensure_solver(b));
-  CUDA_TRY(b, cudaMemsetAsync(b->counters.p + 2, 0, sizeof(unsigned long long), b->stream));
-  cudaEventRecord(b->ev[0], b->stream);
-  if (need_bp) TRY(run_broadphase(b));
-  KernelArgs a = make_args(b);
-  a.dt = dt;
-  a.inv_dt = dt > 0.0f ? 1.0f / dt : 0.0f;
-  a.vi = vi;
-  a.pi = pi;
-  launch_collide(a, b->NC, b->stream);
-  cudaEventRecord(b->ev[1], b->stream);
-  if (dt > 0.0f) {
-    launch_solve(a, b->NW, b->stream);
-    cudaEventRecord(b->ev[2], b->stream);
-    TRY(run_broadphase(b));
+  if (graph) {
+    cudaEventRecord(b->ev[0], b->stream);
+    CUDA_TRY(b, cudaGraphLaunch(b->graph_exec[entry], b->stream));
+    cudaEventRecord(b->ev[4], b->stream);
+    b->cur = entry ^ 1;
   } else {
-    cudaEventRecord(b->ev[2], b->stream);
+    enqueue_step(b, dt, vi, pi, false, entry, true);
   }
-  cudaEventRecord(b->ev[3], b->stream);
-  a = make_args(b);
-  launch_clear_forces(a, b->NB, b->stream);
-  cudaEventRecord(b->ev[4], b->stream);
   CUDA_TRY(b, cudaGetLastError());
   b->host_state_stale = true;
-  if (sync) {
-    CUDA_TRY(b, cudaStreamSynchronize(b->stream));
-    TRY(drain_device_events(b));
-    float t_col = 0, t_sol = 0, t_bp = 0, t_all = 0;
+  int live_before_last_bp = b->cur ^ 1;
+  int st = finish_step(b, live_before_last_bp);
+  if (!graph) {
+    float t_col = 0, t_sol = 0, t_bp = 0;
     cudaEventElapsedTime(&t_col, b->ev[0], b->ev[1]);
     cudaEventElapsedTime(&t_sol, b->ev[1], b->ev[2]);
     cudaEventElapsedTime(&t_bp, b->ev[2], b->ev[3]);
-    cudaEventElapsedTime(&t_all, b->ev[0], b->ev[4]);
     b->profile.collide = t_col;
     b->profile.solve = t_sol;
     b->profile.broadphase = t_bp;
-    b->profile.step = t_all;
-    b->profile.solve_toi = 0.0f;
-    b->profile.bodies = b->NB;
-    b->profile.fixtures = b->NF;
-    b->profile.contacts = b->NC;
-    b->profile.joints = b->NJ;
-    unsigned long long touching = 0;
-    cudaMemcpy(&touching, b->counters.p + 2, sizeof(touching), cudaMemcpyDeviceToHost);
-    b->profile.touching = (int64_t)touching;
-    return check_status(b);
   }
-  return B2G_OK;
+  float t_all = 0;
+  cudaEventElapsedTime(&t_all, b->ev[0], b->ev[4]);
+  b->profile.step = t_all;
+  b->profile.solve_toi = 0.0f;
+  b->profile.bodies = b->NB;
+  b->profile.fixtures = b->NF;
+  b->profile.contacts = b->NC;
+  b->profile.joints = b->NJ;
+  return st;
 }
 
 static int world_index_ok(Batch* b, int32_t w) { return b && w >= 0 && w < (int32_t)b->worlds.size(); }
@@ -597,7 +722,9 @@ B2G_API int b2g_batch_destroy(b2g_batch* b) {
   }
   cudaSetDevice(b->device);
   cudaStreamSynchronize(b->stream);
-  if (b->graph_exec) cudaGraphExecDestroy(b->graph_exec);
+  for (int k = 0; k < 2; ++k)
+    if (b->graph_exec[k]) cudaGraphExecDestroy(b->graph_exec[k]);
+  if (b->h_readback) cudaFreeHost(b->h_readback);
   release(b, b->wb); release(b, b->wj); release(b, b->wg); release(b, b->wflags); release(b, b->wc);
   release(b, b->world_order); release(b, b->xf); release(b, b->pos); release(b, b->vel); release(b, b->massd);
   release(b, b->damp); release(b, b->force); release(b, b->lc); release(b, b->btype); release(b, b->bworld);
@@ -803,8 +930,34 @@ B2G_API int b2g_step(b2g_batch* b, float dt, int32_t vi, int32_t pi, const uint8
 
 B2G_API int b2g_step_n(b2g_batch* b, float dt, int32_t vi, int32_t pi, int32_t n, int32_t use_graph) {
   if (!b || n < 0) return B2G_E_INVALID_ARG;
-  (void)use_graph;
-  for (int i = 0; i < n; ++i) TRY(step_batch(b, dt, vi, pi, nullptr, i == n - 1));
+  bool saved = b->use_graphs;
+  b->use_graphs = use_graph != 0;
+  int st = B2G_OK;
+  for (int i = 0; i < n && st == B2G_OK; ++i) st = step_batch(b, dt, vi, pi, nullptr, i == n - 1);
+  b->use_graphs = saved;
+  return st;
+}
+
+B2G_API int b2g_debug_set_contact_capacity(b2g_batch* b, int64_t cap) {
+  if (!b || cap < 1 || b->device < 0) return B2G_E_INVALID_ARG;
+  if (b->structure_dirty) TRY(upload_all(b));
+  if (cap < b->NC) return B2G_E_INVALID_ARG;
+  // shrink: reallocate every contact-sized buffer at exactly `cap` (the live list is kept)
+  for (int k = 0; k < 2; ++k) {
+    bool keep = (k == b->cur);
+    TRY(resize_exact(b, b->ckey[k], (size_t)cap, keep)); TRY(resize_exact(b, b->cfix[k], (size_t)cap, keep));
+    TRY(resize_exact(b, b->cflags[k], (size_t)cap, keep)); TRY(resize_exact(b, b->cmat[k], (size_t)cap, keep));
+    TRY(resize_exact(b, b->cman[k], (size_t)cap, keep));
+  }
+  TRY(resize_exact(b, b->pairs, (size_t)cap, false));
+  b->ccap = cap;
+  b->layout_version++;
+  return B2G_OK;
+}
+
+B2G_API int b2g_batch_set_graphs(b2g_batch* b, int32_t enable) {
+  if (!b) return B2G_E_INVALID_ARG;
+  b->use_graphs = enable != 0;
   return B2G_OK;
 }
 
@@ -838,14 +991,9 @@ B2G_API int b2g_batch_set_forces(b2g_batch* b, const float* f4, int64_t n_bodies
 }
 
 B2G_API int b2g_reserve(b2g_batch* b, int64_t contacts) {
-  if (!b || contacts < 0) return B2G_E_INVALID_ARG;
-  for (int k = 0; k < 2; ++k) {
-    TRY(ensure(b, b->ckey[k], (size_t)contacts, k == b->cur)); TRY(ensure(b, b->cfix[k], (size_t)contacts, k == b->cur));
-    TRY(ensure(b, b->cflags[k], (size_t)contacts, k == b->cur)); TRY(ensure(b, b->cmat[k], (size_t)contacts, k == b->cur));
-    TRY(ensure(b, b->cman[k], (size_t)contacts, k == b->cur));
-  }
-  TRY(ensure(b, b->pairs, (size_t)contacts));
-  return B2G_OK;
+  if (!b || contacts < 0 || b->device < 0) return B2G_E_INVALID_ARG;
+  if (b->structure_dirty) TRY(upload_all(b));
+  return ensure_contact_capacity(b, contacts);
 }
 
 B2G_API int b2g_bodies_read(b2g_batch* b, int32_t world, int32_t first, int32_t n, b2g_body* out) {

@@ -189,8 +189,18 @@ struct Batch {
   b2g_profile profile{};
   cudaEvent_t ev[8] = {};
 
-  // CUDA graph of one Step
-  cudaGraphExec_t graph_exec = nullptr;
+  // contact / pair buffer capacity and a version bumped whenever a kernel-visible buffer moves
+  int64_t ccap = 0;
+  uint64_t layout_version = 1;
+  std::vector<int> h_wflags;
+  unsigned long long* h_readback = nullptr;  // pinned: device counters + status after each step
+  float last_dt = 0.0f;
+  int last_vi = 0, last_pi = 0;
+
+  // CUDA graphs of one Step (one per parity of the live contact buffer)
+  bool use_graphs = true;
+  cudaGraphExec_t graph_exec[2] = {nullptr, nullptr};
+  uint64_t graph_version = 0;
   float graph_dt = 0;
   int graph_vi = -1, graph_pi = -1;
 };

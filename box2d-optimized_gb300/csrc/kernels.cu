@@ -55,9 +55,9 @@ __device__ void record_event(const KernelArgs& a, int kind, int world, int fa, i
 // ================================================================================ narrowphase
 // b2Contact::Update for one contact: evaluate the manifold, carry impulses by feature id, set
 // touching, record Begin/End/PreSolve when events are on.
-__global__ void k_collide(KernelArgs a, int64_t n) {
+__global__ void k_collide(KernelArgs a) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
+  if (i >= (int64_t)a.counters[B2G_CNT_CONTACTS]) return;
   int2 f = a.cfix[i];
   int w = a.fworld[f.x];
   if ((a.wflags[w] & B2G_WF_ACTIVE) == 0) return;
@@ -741,6 +741,7 @@ __global__ void k_pairs(KernelArgs a, int n) {
   int cnt = 0;
   int64_t off = 0;
   if (EMIT) {
+    if ((int64_t)a.poff[a.nf] > a.ccap) return;  // overflow: the host grows the buffers and redoes this pass
     off = a.poff[f];
     if (a.poff[f + 1] == off) return;
   }
@@ -812,9 +813,11 @@ __device__ __forceinline__ int64_t find_key(const uint64_t* keys, int64_t n, uin
 // New contact list = the new pair list; persisting contacts keep their orientation, flags,
 // mixed material and manifold (impulses included); new ones are created like b2Contact's
 // constructor (src/dynamics/b2_contact.cpp:96-122) in b2Contact::Create's orientation.
-__global__ void k_contact_diff(KernelArgs a, int64_t nnew, int64_t nold, int src, int dst) {
+__global__ void k_contact_diff(KernelArgs a, int src, int dst) {
   int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= nnew) return;
+  int64_t nnew = a.poff[a.nf];
+  int64_t nold = (int64_t)a.counters[B2G_CNT_CONTACTS];
+  if (nnew > a.ccap || k >= nnew) return;
   uint64_t key = a.pairs[k];
   int64_t o = find_key(a.ckeyB[src], nold, key);
   a.ckeyB[dst][k] = key;
@@ -840,9 +843,11 @@ __global__ void k_contact_diff(KernelArgs a, int64_t nnew, int64_t nold, int src
 
 // Contacts that disappeared: EndContact if they were touching (b2ContactManager::Destroy,
 // src/dynamics/b2_contact_manager.cpp:48-61).
-__global__ void k_contact_dead(KernelArgs a, int64_t nnew, int64_t nold, int src) {
+__global__ void k_contact_dead(KernelArgs a, int src) {
   int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= nold) return;
+  int64_t nnew = a.poff[a.nf];
+  int64_t nold = (int64_t)a.counters[B2G_CNT_CONTACTS];
+  if (nnew > a.ccap || k >= nold) return;
   uint64_t key = a.ckeyB[src][k];
   if (find_key(a.pairs, nnew, key) >= 0) return;
   if ((a.cflagsB[src][k] & B2G_CONTACT_TOUCHING) == 0) return;
@@ -850,6 +855,13 @@ __global__ void k_contact_dead(KernelArgs a, int64_t nnew, int64_t nold, int src
   int w = a.fworld[f.x];
   int fo = a.wb[w].z;
   record_event(a, B2G_EVENT_END, w, f.x - fo, f.y - fo, 0, 0, 0, 0);
+}
+
+// The new list becomes the live one, or the needed capacity is recorded for the host.
+__global__ void k_commit_contacts(KernelArgs a) {
+  unsigned long long total = (unsigned long long)a.poff[a.nf];
+  if ((int64_t)total > a.ccap) a.counters[B2G_CNT_OVERFLOW] = total;
+  else a.counters[B2G_CNT_CONTACTS] = total;
 }
 
 // ================================================================================ standalone
@@ -880,8 +892,8 @@ __global__ void k_collide_pairs(const b2g_shape* sa, const float* xa, const b2g_
 // ================================================================================ launchers
 static inline unsigned grid_for(int64_t n, int bs) { return (unsigned)((n + bs - 1) / bs); }
 
-void launch_collide(const KernelArgs& a, int64_t n, cudaStream_t s) {
-  if (n > 0) k_collide<<<grid_for(n, 128), 128, 0, s>>>(a, n);
+void launch_collide(const KernelArgs& a, cudaStream_t s) {
+  if (a.ccap > 0) k_collide<<<grid_for(a.ccap, 128), 128, 0, s>>>(a);
 }
 void launch_solve(const KernelArgs& a, int nw, cudaStream_t s) {
   if (nw > 0) k_solve<<<nw, SOLVER_THREADS, 0, s>>>(a);
@@ -890,7 +902,11 @@ void launch_clear_forces(const KernelArgs& a, int nb, cudaStream_t s) {
   if (nb > 0) k_clear_forces<<<grid_for(nb, 256), 256, 0, s>>>(a, nb);
 }
 void launch_bp_build(const KernelArgs& a, int nf, int nw, size_t cub_bytes, int sort_bits, cudaStream_t s) {
-  if (nf <= 0) return;
+  if (nf <= 0) {
+    cudaMemsetAsync(a.poff, 0, sizeof(int), s);
+    k_world_contacts<<<grid_for(nw, 128), 128, 0, s>>>(a, nw);
+    return;
+  }
   k_aabb<<<grid_for(nf, 128), 128, 0, s>>>(a, nf);
   k_world_bounds<<<nw, 256, 0, s>>>(a);
   k_morton<<<grid_for(nf, 256), 256, 0, s>>>(a, nf);
@@ -910,9 +926,10 @@ void launch_bp_build(const KernelArgs& a, int nf, int nw, size_t cub_bytes, int 
 void launch_bp_emit(const KernelArgs& a, int nf, cudaStream_t s) {
   if (nf > 0) k_pairs<true><<<grid_for(nf, 128), 128, 0, s>>>(a, nf);
 }
-void launch_contact_diff(const KernelArgs& a, int64_t nnew, int64_t nold, int src, int dst, cudaStream_t s) {
-  if (nnew > 0) k_contact_diff<<<grid_for(nnew, 256), 256, 0, s>>>(a, nnew, nold, src, dst);
-  if (nold > 0 && a.events_on) k_contact_dead<<<grid_for(nold, 256), 256, 0, s>>>(a, nnew, nold, src);
+void launch_contact_diff(const KernelArgs& a, int src, int dst, cudaStream_t s) {
+  k_contact_diff<<<grid_for(a.ccap, 256), 256, 0, s>>>(a, src, dst);
+  if (a.events_on) k_contact_dead<<<grid_for(a.ccap, 256), 256, 0, s>>>(a, src);
+  k_commit_contacts<<<1, 1, 0, s>>>(a);
 }
 size_t cub_temp_bytes(int nf) {
   size_t b1 = 0, b2 = 0;

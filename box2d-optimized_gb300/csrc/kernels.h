@@ -85,14 +85,22 @@ struct KernelArgs {
 
   float dt, inv_dt;
   int vi, pi;
+  int nf, nw;        // fixture and world counts of the layout
+  int64_t ccap;      // contact / pair buffer capacity
 };
 
-void launch_collide(const KernelArgs& a, int64_t n, cudaStream_t s);
+// device counters (KernelArgs::counters)
+#define B2G_CNT_CONTACTS 0   // live contacts
+#define B2G_CNT_EVENTS 1     // recorded events
+#define B2G_CNT_TOUCHING 2   // solver contacts of the last step
+#define B2G_CNT_OVERFLOW 3   // pair capacity needed when the last broadphase overflowed (else 0)
+
+void launch_collide(const KernelArgs& a, cudaStream_t s);
 void launch_solve(const KernelArgs& a, int nw, cudaStream_t s);
 void launch_clear_forces(const KernelArgs& a, int nb, cudaStream_t s);
 void launch_bp_build(const KernelArgs& a, int nf, int nw, size_t cub_bytes, int sort_bits, cudaStream_t s);
 void launch_bp_emit(const KernelArgs& a, int nf, cudaStream_t s);
-void launch_contact_diff(const KernelArgs& a, int64_t nnew, int64_t nold, int src, int dst, cudaStream_t s);
+void launch_contact_diff(const KernelArgs& a, int src, int dst, cudaStream_t s);
 size_t cub_temp_bytes(int nf);
 void launch_collide_pairs(const b2g_shape* sa, const float* xa, const b2g_shape* sb, const float* xb, int n,
                           b2g_manifold* out, cudaStream_t s);

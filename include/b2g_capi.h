@@ -295,6 +295,12 @@ B2G_API int b2g_step_timed(b2g_batch* b, float dt, int32_t velocity_iterations,
  * then creation order): f4 holds (fx, fy, torque, unused) per body, n_bodies records. The
  * per-step input of an end-to-end loop (b2Body::ApplyForce / ApplyTorque on every body). */
 B2G_API int b2g_batch_set_forces(b2g_batch* b, const float* f4, int64_t n_bodies);
+/* Whether b2g_step replays the Step as a captured CUDA graph (default on). A graph is used for
+ * unmasked steps with dt > 0 and events off; it is re-captured when buffers move. */
+B2G_API int b2g_batch_set_graphs(b2g_batch* b, int32_t enable);
+/* Testing knob: sets the contact/pair buffer capacity to exactly `cap` (>= live contacts), so
+ * that a later broadphase overflows and exercises the recovery path. */
+B2G_API int b2g_debug_set_contact_capacity(b2g_batch* b, int64_t cap);
 /* Pre-size the pair/contact buffers to at least `contacts` entries in total. */
 B2G_API int b2g_reserve(b2g_batch* b, int64_t contacts);
 

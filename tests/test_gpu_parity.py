@@ -234,3 +234,40 @@ def test_pairs_capacity_reported(lib):
     st = lib.b2g_pairs(d_aabb.data_ptr(), n, d_pairs.data_ptr(), 10, C.byref(npairs), None)
     assert st == 7  # B2G_E_CAPACITY
     assert npairs.value == n * (n - 1) // 2
+
+
+# ---------------------------------------------------------------- graphs and capacity recovery
+def test_graph_replay_equals_eager(lib):
+    """The Step replayed as a captured CUDA graph is bit-identical to the eagerly launched Step."""
+    out = []
+    for graphs in (0, 1):
+        b = G.Batch(lib, device=0)
+        for s, n in ((31, 900), (32, 200), (33, 2500)):
+            _, gx, gy = _params(lib, s)
+            w = b.add_world(gx, gy)
+            b.set_flags(w)
+            b.scene(w, G.SCENE_BATCH_WORLD, seed=s, n=n)
+        lib.b2g_batch_set_graphs(b.h, graphs)
+        for _ in range(60):
+            b.step(1 / 60, 8, 3)
+        out.append([_state_bytes(b.bodies(w)) for w in range(3)])
+        b.close()
+    assert out[0] == out[1]
+
+
+def test_pair_overflow_recovery_bit_exact(lib, orc):
+    """Contact buffers far too small: every overflowing broadphase is redone with larger buffers
+    and the rollout still matches the oracle bit for bit."""
+    b = G.Batch(lib, device=0)
+    w = b.add_world(0.0, -10.0)
+    b.set_flags(w)
+    b.scene(w, G.SCENE_PYRAMID, n=12, p0=1.0, p1=0.6)
+    ow = ob.OracleWorld(orc, (0.0, -10.0), b.bodies(w), b.fixtures(w), b.joints(w))
+    for s in range(40):
+        if s % 10 == 0:
+            nc = b.sizes(w)[3]
+            assert lib.b2g_debug_set_contact_capacity(b.h, max(nc, 1)) == 0
+        b.step(1 / 60, 8, 3)
+        ow.step(1, 1 / 60, 8, 3)
+        assert _state_bytes(b.bodies(w)) == _state_bytes(ow.bodies()), f"step {s + 1}"
+    b.close()
