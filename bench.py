@@ -101,6 +101,73 @@ def world_params(lib, seed):
     return n.value, gx.value, gy.value
 
 
+def shard_seeds(rank, world_size, worlds_per_rank):
+    """World seeds of one rank: disjoint contiguous shards, the same count on every rank."""
+    return [rank * worlds_per_rank + i for i in range(worlds_per_rank)]
+
+
+def reduce_over_ranks(ms_per_step, bodies, device):
+    """(max over ranks of the step time, sum over ranks of the bodies) through torch.distributed."""
+    import torch  # noqa: PLC0415
+
+    if not torch.distributed.is_initialized() or torch.distributed.get_world_size() == 1:
+        return float(ms_per_step), float(bodies)
+    t = torch.tensor([float(ms_per_step)], dtype=torch.float64, device=device)
+    n = torch.tensor([float(bodies)], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    torch.distributed.all_reduce(n, op=torch.distributed.ReduceOp.SUM)
+    return float(t.item()), float(n.item())
+
+
+def serve(lib, dev, seconds, rate, seed0, budget=120 << 30):
+    """Poisson stream of rollout requests (32-4096 bodies log-uniform, K ~ U[16, 512]) at `rate`
+    requests/s (rate=None: closed loop, the queue is kept full). Returns tick and request
+    latencies and the served body-steps/s."""
+    import numpy as np  # noqa: PLC0415
+
+    rng = np.random.default_rng(seed0)
+    srv = G.Server(lib, device=dev, budget_bytes=budget, max_worlds=4096)
+    t0 = time.perf_counter()
+    next_arrival = 0.0
+    steps_ms, lat, body_steps = [], [], 0
+    sizes = {}
+    k = 0
+    while True:
+        now = time.perf_counter() - t0
+        if now > seconds:
+            break
+        if rate is None:
+            st = srv.stats()
+            while st["queued"] < 8:
+                n = int(round(2 ** rng.uniform(5, 12)))
+                rid = srv.submit(seed0 + k, n, int(rng.integers(16, 513)))
+                sizes[rid] = n
+                k += 1
+                st["queued"] += 1
+        else:
+            while next_arrival <= now:
+                n = int(round(2 ** rng.uniform(5, 12)))
+                rid = srv.submit(seed0 + k, n, int(rng.integers(16, 513)))
+                sizes[rid] = n
+                k += 1
+                next_arrival += rng.exponential(1.0 / rate)
+        active, ms = srv.tick()
+        if active:
+            steps_ms.append(ms)
+        for r in srv.poll():
+            if r.status == 0:
+                lat.append((r.finish_time_s - r.submit_time_s) * 1e3)
+                body_steps += r.bodies * r.steps
+    elapsed = time.perf_counter() - t0
+    st = srv.stats()
+    srv.close()
+    q = lambda a, p: float(np.percentile(a, p)) if len(a) else None  # noqa: E731
+    return {"rate_req_s": rate, "seconds": round(elapsed, 1), "completed": st["completed"],
+            "throughput_req_s": st["completed"] / elapsed, "body_steps_s": body_steps / elapsed,
+            "step_ms_p50": q(steps_ms, 50), "step_ms_p99": q(steps_ms, 99),
+            "request_ms_p50": q(lat, 50), "request_ms_p99": q(lat, 99), "ticks": len(steps_ms)}
+
+
 def build_batch(lib, seeds, device):
     batch = G.Batch(lib, device=device)
     nb = 0
@@ -195,7 +262,7 @@ def run_ours(args, rank, world_size):
 
     lib = G.Lib()
     dev = int(os.environ.get("LOCAL_RANK", "0"))
-    seeds = [rank * args.worlds + i for i in range(args.worlds)]
+    seeds = shard_seeds(rank, world_size, args.worlds)
     t0 = time.time()
     batch, nb = build_batch(lib, seeds, dev)
     build_s = time.time() - t0
@@ -208,15 +275,7 @@ def run_ours(args, rank, world_size):
         ms = batch.step_timed(args.steps, DT, VI, PI)
     prof = batch.profile()
     ms_per_step = ms / args.steps
-    if world_size > 1:
-        t = torch.tensor([ms_per_step], device=f"cuda:{dev}")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms_per_step = float(t.item())
-        n_total = torch.tensor([nb], device=f"cuda:{dev}", dtype=torch.float64)
-        torch.distributed.all_reduce(n_total)
-        nb_all = float(n_total.item())
-    else:
-        nb_all = float(nb)
+    ms_per_step, nb_all = reduce_over_ranks(ms_per_step, nb, f"cuda:{dev}")
     value = nb_all / (ms_per_step / 1e3)
 
     # end to end through the C ABI with pinned host buffers: forces in, transforms out
@@ -265,6 +324,18 @@ def run_ours(args, rank, world_size):
     achieved = sb / (prof.solve / 1e3) / 1e9 if prof.solve > 0 else None
     step_b = step_bytes(prof.bodies, prof.fixtures, prof.contacts, prof.touching, prof.joints)
 
+    # served: closed-loop saturation, then a Poisson stream at 70% of it
+    served = None
+    if rank == 0 and not args.no_serve:
+        sat = serve(lib, dev, args.serve_seconds, None, 1_000_000)
+        rate = 0.7 * sat["throughput_req_s"]
+        at70 = serve(lib, dev, args.serve_seconds, rate, 2_000_000)
+        served = {"saturation": sat, "at_70pct": at70,
+                  "step_ms_p50": at70["step_ms_p50"], "step_ms_p99": at70["step_ms_p99"],
+                  "request_ms_p50": at70["request_ms_p50"], "request_ms_p99": at70["request_ms_p99"],
+                  "workload": "Poisson rollout requests, 32-4096 bodies log-uniform, K ~ U[16,512] steps, "
+                              "120 GB HBM budget; rate = 0.7 x closed-loop saturation throughput"}
+
     line = None
     if rank == 0:
         cpu = None
@@ -293,6 +364,7 @@ def run_ours(args, rank, world_size):
                          "frac": (achieved / peak) if achieved else None, "traffic": None,
                          "peak_kind": f"{peak_kind} hbm_gbs", "bytes_per_launch": sb},
             "cpu_baseline": cpu,
+            "served": served,
             "plain_gpu": plain,
             "batched_over_plain": (value / world_size / plain["value"]) if plain else None,
             "e2e": {"value": e2e_value, "unit": "body-steps/s", "h2d_bytes_per_step": 16 * nbody,
@@ -317,6 +389,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--plain-worlds", type=int, default=32)
     ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--serve-seconds", type=float, default=12.0)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank = int(os.environ.get("RANK", "0"))

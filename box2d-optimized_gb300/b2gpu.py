@@ -141,6 +141,50 @@ def body_array_to_numpy(arr) -> dict:
             "inertia": f[:, 14], "inv_inertia": f[:, 15], "type": t}
 
 
+class Server:
+    """Continuous-batching rollout server (b2g_server)."""
+
+    def __init__(self, lib, device=0, budget_bytes=120 << 30, max_worlds=4096, dt=1 / 60, vi=8, pi=3):
+        self.lib = lib
+        h = C.c_void_p()
+        lib.check(lib.b2g_server_create(device, budget_bytes, max_worlds, dt, vi, pi, C.byref(h)),
+                  "b2g_server_create")
+        self.h = h
+
+    def close(self):
+        if self.h:
+            self.lib.b2g_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:  # noqa: BLE001 - interpreter shutdown
+            pass
+
+    def submit(self, seed, bodies, steps) -> int:
+        rid = C.c_int64()
+        self.lib.check(self.lib.b2g_server_submit(self.h, seed, bodies, steps, C.byref(rid)), "submit")
+        return rid.value
+
+    def tick(self):
+        active = C.c_int32()
+        ms = C.c_double()
+        self.lib.check(self.lib.b2g_server_tick(self.h, C.byref(active), C.byref(ms)), "tick")
+        return active.value, ms.value
+
+    def poll(self, cap=4096):
+        arr = (RequestResult * cap)()
+        n = C.c_int32()
+        self.lib.check(self.lib.b2g_server_poll(self.h, arr, cap, C.byref(n)), "poll")
+        return arr[:n.value]
+
+    def stats(self):
+        v = [C.c_int64() for _ in range(5)]
+        self.lib.check(self.lib.b2g_server_stats(self.h, *[C.byref(x) for x in v]), "stats")
+        return dict(zip(("queued", "active", "completed", "rejected", "hbm_bytes"), (x.value for x in v)))
+
+
 class B2GError(RuntimeError):
     pass
 
@@ -163,7 +207,7 @@ class Lib:
         "b2g_batch_create", "b2g_batch_destroy", "b2g_world_add", "b2g_world_count",
         "b2g_world_set_gravity", "b2g_world_set_flags", "b2g_bodies_add", "b2g_fixtures_add",
         "b2g_joints_add", "b2g_world_sizes", "b2g_step", "b2g_step_n", "b2g_step_timed",
-        "b2g_batch_set_forces", "b2g_batch_set_graphs", "b2g_debug_set_contact_capacity",
+        "b2g_batch_set_forces", "b2g_batch_set_graphs", "b2g_world_retire", "b2g_compact", "b2g_debug_set_contact_capacity",
         "b2g_pairs_static", "b2g_reserve",
         "b2g_bodies_read", "b2g_bodies_write", "b2g_batch_read_states", "b2g_fixtures_read",
         "b2g_joints_read", "b2g_contacts_read", "b2g_events_enable", "b2g_events_drain",
@@ -199,6 +243,8 @@ class Lib:
             "b2g_step_timed": ([vp, f32, i32, i32, i32, P(f32)], C.c_int),
             "b2g_batch_set_forces": ([vp, vp, i64], C.c_int),
             "b2g_batch_set_graphs": ([vp, i32], C.c_int),
+            "b2g_world_retire": ([vp, i32], C.c_int),
+            "b2g_compact": ([vp, P(i32), i32], C.c_int),
             "b2g_debug_set_contact_capacity": ([vp, i64], C.c_int),
             "b2g_pairs_static": ([vp, i32, vp, i64, P(i64), vp], C.c_int),
             "b2g_reserve": ([vp, i64], C.c_int),

@@ -304,6 +304,129 @@ int upload_all(Batch* b) {
   return B2G_OK;
 }
 
+// Copies v into buf at element offset `off`, growing buf (keeping its contents) as needed.
+template <typename T>
+static int upload_at(Batch* b, DBuf<T>& buf, size_t off, const std::vector<T>& v) {
+  TRY(ensure(b, buf, off + v.size(), true));
+  if (!v.empty()) CUDA_TRY(b, cudaMemcpyAsync(buf.p + off, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, b->stream));
+  return B2G_OK;
+}
+
+// Appends the worlds [NW, worlds.size()) that are not on the device yet after the existing
+// layout, without touching the live state of the others: body / fixture / joint arrays grow in
+// place and only the new segments are copied; the world table is rewritten (small); the new
+// worlds' contacts are found by the next step's broadphase.
+int upload_tail(Batch* b) {
+  CUDA_TRY(b, cudaSetDevice(b->device));
+  int w0 = b->NW, NW = (int)b->worlds.size();
+  int NB0 = b->NB, NF0 = b->NF, NJ0 = b->NJ;
+  std::vector<float4> xf, pos, vel, massd, damp, force;
+  std::vector<float2> lc;
+  std::vector<int> btype, bworld, fbody, fgroup, fsensor, fworld;
+  std::vector<b2g_shape> shape;
+  std::vector<uint32_t> ffilter;
+  std::vector<float4> fmat, wg_tail;
+  std::vector<JointDev> joints;
+  std::vector<uint64_t> nocol;
+  b->h_body_off.resize(NW + 1);
+  b->h_fix_off.resize(NW + 1);
+  b->h_joint_off.resize(NW + 1);
+  int NB = NB0, NF = NF0, NJ = NJ0;
+  for (int w = w0; w < NW; ++w) {
+    const HostWorld& hw = b->worlds[w];
+    int bo = NB, fo = NF, jo = NJ;
+    b->h_body_off[w] = bo; b->h_fix_off[w] = fo; b->h_joint_off[w] = jo;
+    wg_tail.push_back(make_float4(hw.gx, hw.gy, hw.inv_dt0, 0.0f));
+    for (const b2g_body& s : hw.bodies) {
+      xf.push_back(make_float4(s.xf[0], s.xf[1], s.xf[2], s.xf[3]));
+      pos.push_back(make_float4(s.c[0], s.c[1], s.a, 0.0f));
+      vel.push_back(make_float4(s.v[0], s.v[1], s.w, 0.0f));
+      massd.push_back(make_float4(s.mass, s.inv_mass, s.inertia, s.inv_inertia));
+      damp.push_back(make_float4(s.linear_damping, s.angular_damping, s.gravity_scale, 0.0f));
+      force.push_back(make_float4(s.force[0], s.force[1], s.torque, 0.0f));
+      lc.push_back(make_float2(s.local_center[0], s.local_center[1]));
+      btype.push_back(s.type);
+      bworld.push_back(w);
+    }
+    for (const b2g_fixture& f : hw.fixtures) {
+      shape.push_back(f.shape);
+      fbody.push_back(bo + f.body);
+      fgroup.push_back(f.group_index);
+      fsensor.push_back(f.is_sensor ? 1 : 0);
+      fworld.push_back(w);
+      ffilter.push_back((uint32_t)f.category_bits | ((uint32_t)f.mask_bits << 16));
+      fmat.push_back(make_float4(f.friction, f.restitution, f.restitution_threshold, f.density));
+    }
+    for (const b2g_joint& j : hw.joints) {
+      JointDev d;
+      memset(&d, 0, sizeof(d));
+      d.d = j.def;
+      d.d.body_a += bo;
+      d.d.body_b += bo;
+      d.impulse[0] = j.impulse[0]; d.impulse[1] = j.impulse[1]; d.impulse[2] = j.impulse[2];
+      d.motorImpulse = j.motor_impulse; d.lowerImpulse = j.lower_impulse; d.upperImpulse = j.upper_impulse;
+      if (j.def.type == B2G_JOINT_PRISMATIC) {
+        V2 ax = mk(j.def.local_axis_a[0], j.def.local_axis_a[1]);
+        V2 ay = cross(1.0f, ax);
+        d.localXAxisA[0] = ax.x; d.localXAxisA[1] = ax.y;
+        d.localYAxisA[0] = ay.x; d.localYAxisA[1] = ay.y;
+      }
+      joints.push_back(d);
+      if (!j.def.collide_connected) {
+        uint32_t x = (uint32_t)(bo + j.def.body_a), y = (uint32_t)(bo + j.def.body_b);
+        if (x > y) std::swap(x, y);
+        nocol.push_back(((uint64_t)x << 32) | y);
+      }
+    }
+    NB += (int)hw.bodies.size();
+    NF += (int)hw.fixtures.size();
+    NJ += (int)hw.joints.size();
+  }
+  b->h_body_off[NW] = NB; b->h_fix_off[NW] = NF; b->h_joint_off[NW] = NJ;
+  std::sort(nocol.begin(), nocol.end());
+  nocol.erase(std::unique(nocol.begin(), nocol.end()), nocol.end());
+  // world table: offsets are static, gravity/inv_dt0 of existing worlds stay as the device has them
+  std::vector<int4> wb(NW), wj(NW);
+  std::vector<int> wflags(NW);
+  for (int w = 0; w < NW; ++w) {
+    const HostWorld& hw = b->worlds[w];
+    wb[w] = make_int4(b->h_body_off[w], (int)hw.bodies.size(), b->h_fix_off[w], (int)hw.fixtures.size());
+    wj[w] = make_int4(b->h_joint_off[w], (int)hw.joints.size(), 0, 0);
+    wflags[w] = hw.flags & ~(B2G_WF_ACTIVE | B2G_WF_NEW_CONTACTS);
+  }
+  std::vector<int> order(NW);
+  std::iota(order.begin(), order.end(), 0);
+  std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
+    return b->worlds[x].bodies.size() + b->worlds[x].joints.size() > b->worlds[y].bodies.size() + b->worlds[y].joints.size();
+  });
+  std::vector<int2> wc_tail(NW - w0, make_int2(0, 0));
+  TRY(upload(b, b->wb, wb)); TRY(upload(b, b->wj, wj)); TRY(upload_at(b, b->wg, w0, wg_tail));
+  TRY(upload(b, b->wflags, wflags)); TRY(upload(b, b->world_order, order)); TRY(upload_at(b, b->wc, w0, wc_tail));
+  b->h_wflags = wflags;
+  TRY(ensure(b, b->wbounds, NW)); TRY(ensure(b, b->wroot, NW)); TRY(ensure(b, b->ncolors, 2 * (size_t)NW));
+  TRY(upload_at(b, b->xf, NB0, xf)); TRY(upload_at(b, b->pos, NB0, pos)); TRY(upload_at(b, b->vel, NB0, vel));
+  TRY(upload_at(b, b->massd, NB0, massd)); TRY(upload_at(b, b->damp, NB0, damp)); TRY(upload_at(b, b->force, NB0, force));
+  TRY(upload_at(b, b->lc, NB0, lc)); TRY(upload_at(b, b->btype, NB0, btype)); TRY(upload_at(b, b->bworld, NB0, bworld));
+  TRY(upload_at(b, b->shape, NF0, shape)); TRY(upload_at(b, b->fbody, NF0, fbody)); TRY(upload_at(b, b->fgroup, NF0, fgroup));
+  TRY(upload_at(b, b->fsensor, NF0, fsensor)); TRY(upload_at(b, b->fworld, NF0, fworld));
+  TRY(upload_at(b, b->ffilter, NF0, ffilter)); TRY(upload_at(b, b->fmat, NF0, fmat));
+  TRY(upload_at(b, b->joints, NJ0, joints)); TRY(upload_at(b, b->nocollide, b->n_nocollide, nocol));
+  b->n_nocollide += (int)nocol.size();
+  TRY(ensure(b, b->aabb, NF)); TRY(ensure(b, b->mkey, NF)); TRY(ensure(b, b->mkey_sorted, NF));
+  TRY(ensure(b, b->mval, NF)); TRY(ensure(b, b->mval_sorted, NF)); TRY(ensure(b, b->nchild, NF));
+  TRY(ensure(b, b->nparent, NF)); TRY(ensure(b, b->lparent, NF)); TRY(ensure(b, b->naabb, NF));
+  TRY(ensure(b, b->nflag, NF)); TRY(ensure(b, b->pcount, (size_t)NF + 1)); TRY(ensure(b, b->poff, (size_t)NF + 1));
+  TRY(ensure(b, b->cub_tmp, cub_temp_bytes(NF)));
+  TRY(ensure(b, b->inc_cnt, NB)); TRY(ensure(b, b->inc_off, NB)); TRY(ensure(b, b->inc_head, NB));
+  TRY(ensure(b, b->inc_mask, NB));
+  TRY(ensure(b, b->jinc_list, 2 * (size_t)NJ)); TRY(ensure(b, b->jcolor, NJ)); TRY(ensure(b, b->jorder, NJ));
+  TRY(ensure(b, b->jprio, NJ)); TRY(ensure(b, b->jready, NJ));
+  b->NW = NW; b->NB = NB; b->NF = NF; b->NJ = NJ;
+  b->layout_version++;
+  CUDA_TRY(b, cudaStreamSynchronize(b->stream));
+  return B2G_OK;
+}
+
 // Copies the live device state (bodies, joints, contacts, inv_dt0) into the host records.
 int download_state(Batch* b) {
   if (b->device < 0 || !b->device_state_valid || !b->host_state_stale) return B2G_OK;
@@ -577,6 +700,9 @@ int step_batch(Batch* b, float dt, int vi, int pi, const uint8_t* mask, bool syn
   if (b->structure_dirty) {
     TRY(upload_all(b));
     invalidate_graphs(b);
+  } else if ((int)b->worlds.size() > b->NW) {
+    TRY(upload_tail(b));
+    invalidate_graphs(b);
   }
   if (b->NW == 0) return B2G_OK;
   if (!b->h_readback) CUDA_TRY(b, cudaMallocHost(&b->h_readback, 8 * sizeof(unsigned long long)));
@@ -586,8 +712,8 @@ int step_batch(Batch* b, float dt, int vi, int pi, const uint8_t* mask, bool syn
   for (int w = 0; w < b->NW; ++w) {
     HostWorld& hw = b->worlds[w];
     int f = hw.flags & ~(B2G_WF_ACTIVE | B2G_WF_NEW_CONTACTS);
-    if (!mask || mask[w]) f |= B2G_WF_ACTIVE;
-    else all_active = false;
+    if ((!mask || mask[w]) && !(hw.flags & B2G_WF_RETIRED)) f |= B2G_WF_ACTIVE;
+    if (mask && !mask[w]) all_active = false;
     wflags[w] = f;
     if (hw.flags & B2G_WF_NEW_CONTACTS) need_bp = true;
     hw.flags &= ~B2G_WF_NEW_CONTACTS;
@@ -665,6 +791,8 @@ static int begin_edit(Batch* b) {
 using namespace b2g;
 
 struct b2g_batch : public Batch {};
+
+uint64_t b2g::batch_allocated_bytes(const b2g_batch* b) { return b ? b->allocated : 0; }
 
 static const char* kStatusNames[] = {"OK", "INVALID_ARG", "OUT_OF_MEMORY", "TIMEOUT", "WORLD_FAULT", "CUDA", "LOCKED", "CAPACITY"};
 
@@ -751,7 +879,7 @@ B2G_API int b2g_batch_destroy(b2g_batch* b) {
 
 B2G_API int b2g_world_add(b2g_batch* b, float gx, float gy, int32_t* out_world) {
   if (!b || !isfinite(gx) || !isfinite(gy)) return B2G_E_INVALID_ARG;
-  TRY(begin_edit(b));
+  // a new world goes after the device layout: the next step uploads only the new worlds
   HostWorld w;
   w.gx = gx;
   w.gy = gy;
@@ -767,17 +895,48 @@ B2G_API int b2g_world_count(b2g_batch* b, int32_t* out_n) {
 }
 
 B2G_API int b2g_world_set_gravity(b2g_batch* b, int32_t world, float gx, float gy) {
-  if (!world_index_ok(b, world)) return B2G_E_INVALID_ARG;
-  TRY(begin_edit(b));
+  if (!world_index_ok(b, world) || !isfinite(gx) || !isfinite(gy)) return B2G_E_INVALID_ARG;
   b->worlds[world].gx = gx;
   b->worlds[world].gy = gy;
+  if (world < b->NW && b->device_state_valid && !b->structure_dirty) {
+    float g2[2] = {gx, gy};
+    CUDA_TRY(b, cudaMemcpyAsync((char*)(b->wg.p + world), g2, sizeof(g2), cudaMemcpyHostToDevice, b->stream));
+    CUDA_TRY(b, cudaStreamSynchronize(b->stream));
+  }
+  return B2G_OK;
+}
+
+// Retires a world: it is no longer stepped, its contacts are dropped at the next broadphase, and
+// its memory is reclaimed by the next b2g_compact.
+B2G_API int b2g_world_retire(b2g_batch* b, int32_t world) {
+  if (!world_index_ok(b, world)) return B2G_E_INVALID_ARG;
+  b->worlds[world].flags |= B2G_WF_RETIRED;
+  return B2G_OK;
+}
+
+// Removes retired worlds; old_to_new[w] receives each world's new index (-1 if removed).
+B2G_API int b2g_compact(b2g_batch* b, int32_t* old_to_new, int32_t n) {
+  if (!b || (n > 0 && !old_to_new)) return B2G_E_INVALID_ARG;
+  TRY(download_state(b));
+  std::vector<HostWorld> keep;
+  int nw = (int)b->worlds.size();
+  for (int w = 0; w < nw; ++w) {
+    int to = -1;
+    if (!(b->worlds[w].flags & B2G_WF_RETIRED)) {
+      to = (int)keep.size();
+      keep.push_back(std::move(b->worlds[w]));
+    }
+    if (w < n) old_to_new[w] = to;
+  }
+  b->worlds.swap(keep);
+  b->structure_dirty = true;
   return B2G_OK;
 }
 
 B2G_API int b2g_world_set_flags(b2g_batch* b, int32_t world, int32_t allow_sleep, int32_t warm_starting,
                                 int32_t continuous, int32_t auto_clear_forces) {
   if (!world_index_ok(b, world)) return B2G_E_INVALID_ARG;
-  TRY(begin_edit(b));
+  // flags travel with the per-step world flags upload; no re-layout
   HostWorld& w = b->worlds[world];
   w.allow_sleep = allow_sleep != 0;
   w.continuous = continuous != 0;
@@ -798,7 +957,7 @@ B2G_API int b2g_bodies_add(b2g_batch* b, int32_t world, const b2g_body_def* defs
       return B2G_E_INVALID_ARG;
     }
   }
-  TRY(begin_edit(b));
+  if (world < b->NW) TRY(begin_edit(b));
   HostWorld& w = b->worlds[world];
   for (int i = 0; i < n; ++i) {
     const b2g_body_def& d = defs[i];
@@ -849,7 +1008,7 @@ B2G_API int b2g_fixtures_add(b2g_batch* b, int32_t world, const b2g_fixture_def*
       return st;
     }
   }
-  TRY(begin_edit(b));
+  if (world < b->NW) TRY(begin_edit(b));
   HostWorld& w = b->worlds[world];
   for (int i = 0; i < n; ++i) {
     int fi = (int)w.fixtures.size();
@@ -879,7 +1038,7 @@ B2G_API int b2g_joints_add(b2g_batch* b, int32_t world, const b2g_joint_def* def
       return B2G_E_INVALID_ARG;
     }
   }
-  TRY(begin_edit(b));
+  if (world < b->NW) TRY(begin_edit(b));
   HostWorld& w = b->worlds[world];
   for (int i = 0; i < n; ++i) {
     b2g_joint j;
@@ -998,10 +1157,26 @@ B2G_API int b2g_reserve(b2g_batch* b, int64_t contacts) {
 
 B2G_API int b2g_bodies_read(b2g_batch* b, int32_t world, int32_t first, int32_t n, b2g_body* out) {
   if (!world_index_ok(b, world) || first < 0 || n < 0 || (n > 0 && !out)) return B2G_E_INVALID_ARG;
-  TRY(download_state(b));
   const HostWorld& w = b->worlds[world];
   if (first + n > (int)w.bodies.size()) return B2G_E_INVALID_ARG;
   for (int i = 0; i < n; ++i) out[i] = w.bodies[first + i];
+  if (n > 0 && b->host_state_stale && b->device_state_valid && world < b->NW) {
+    // the host copy is older than the device: fetch this world's slice only
+    int bo = b->h_body_off[world] + first;
+    std::vector<float4> xf(n), pos(n), vel(n), force(n);
+    CUDA_TRY(b, cudaMemcpyAsync(xf.data(), b->xf.p + bo, n * sizeof(float4), cudaMemcpyDeviceToHost, b->stream));
+    CUDA_TRY(b, cudaMemcpyAsync(pos.data(), b->pos.p + bo, n * sizeof(float4), cudaMemcpyDeviceToHost, b->stream));
+    CUDA_TRY(b, cudaMemcpyAsync(vel.data(), b->vel.p + bo, n * sizeof(float4), cudaMemcpyDeviceToHost, b->stream));
+    CUDA_TRY(b, cudaMemcpyAsync(force.data(), b->force.p + bo, n * sizeof(float4), cudaMemcpyDeviceToHost, b->stream));
+    CUDA_TRY(b, cudaStreamSynchronize(b->stream));
+    for (int i = 0; i < n; ++i) {
+      b2g_body& r = out[i];
+      r.xf[0] = xf[i].x; r.xf[1] = xf[i].y; r.xf[2] = xf[i].z; r.xf[3] = xf[i].w;
+      r.c[0] = pos[i].x; r.c[1] = pos[i].y; r.a = pos[i].z;
+      r.v[0] = vel[i].x; r.v[1] = vel[i].y; r.w = vel[i].z;
+      r.force[0] = force[i].x; r.force[1] = force[i].y; r.torque = force[i].z;
+    }
+  }
   return B2G_OK;
 }
 

@@ -67,6 +67,7 @@ struct VCDev {
 #define B2G_WF_CLEAR_FORCES 2
 #define B2G_WF_ACTIVE 4
 #define B2G_WF_NEW_CONTACTS 8
+#define B2G_WF_RETIRED 16
 
 struct HostWorld {
   float gx = 0.0f, gy = -10.0f;
@@ -207,6 +208,8 @@ struct Batch {
 
 // ---- host functions (engine.cu)
 int upload_all(Batch* b);
+uint64_t batch_allocated_bytes(const b2g_batch* b);
+int upload_tail(Batch* b);
 int download_state(Batch* b);
 int step_batch(Batch* b, float dt, int vi, int pi, const uint8_t* mask, bool sync);
 void set_error(Batch* b, const std::string& msg);

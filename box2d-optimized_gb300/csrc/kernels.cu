@@ -745,8 +745,9 @@ __global__ void k_pairs(KernelArgs a, int n) {
     off = a.poff[f];
     if (a.poff[f + 1] == off) return;
   }
-  if (tf != B2G_STATIC) {
-    int w = a.fworld[f];
+  int wf = a.fworld[f];
+  if (tf != B2G_STATIC && !(a.wflags[wf] & B2G_WF_RETIRED)) {
+    int w = wf;
     int root = a.wroot[w];
     if (root >= 0 && !(root & LEAF_BIT)) {
       float4 box = a.aabb[f];
@@ -853,6 +854,7 @@ __global__ void k_contact_dead(KernelArgs a, int src) {
   if ((a.cflagsB[src][k] & B2G_CONTACT_TOUCHING) == 0) return;
   int2 f = a.cfixB[src][k];
   int w = a.fworld[f.x];
+  if (a.wflags[w] & B2G_WF_RETIRED) return;
   int fo = a.wb[w].z;
   record_event(a, B2G_EVENT_END, w, f.x - fo, f.y - fo, 0, 0, 0, 0);
 }

@@ -273,6 +273,13 @@ B2G_API int b2g_fixtures_add(b2g_batch* b, int32_t world, const b2g_fixture_def*
 B2G_API int b2g_joints_add(b2g_batch* b, int32_t world, const b2g_joint_def* defs, int32_t n,
                            int32_t* out_ids);
 
+/* Retires a world (it is no longer stepped; its contacts go at the next broadphase) and
+ * b2g_compact removes retired worlds, writing each old index's new index (-1 = removed) into
+ * old_to_new. (The reference's b2World destructor, src/dynamics/b2_world.cpp:71-101, for worlds
+ * that share a batch.) */
+B2G_API int b2g_world_retire(b2g_batch* b, int32_t world);
+B2G_API int b2g_compact(b2g_batch* b, int32_t* old_to_new, int32_t n);
+
 /* Counts of one world. */
 B2G_API int b2g_world_sizes(b2g_batch* b, int32_t world, int32_t* bodies, int32_t* fixtures,
                             int32_t* joints, int32_t* contacts);
