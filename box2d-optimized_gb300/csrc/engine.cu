@@ -264,7 +264,19 @@ int upload_all(Batch* b) {
   });
   TRY(upload(b, b->wb, wb)); TRY(upload(b, b->wj, wj)); TRY(upload(b, b->wg, wg)); TRY(upload(b, b->wflags, wflags));
   TRY(upload(b, b->world_order, order));
-  TRY(ensure(b, b->wc, NW)); TRY(ensure(b, b->wbounds, NW)); TRY(ensure(b, b->wroot, NW));
+  // per-world live contact ranges: the sorted contact list groups by world (keys hold global
+  // fixture indices, and each world's fixtures are contiguous)
+  {
+    std::vector<int2> wc(NW);
+    int64_t off = 0;
+    for (int w = 0; w < NW; ++w) {
+      int cnt = (int)b->worlds[w].contacts.size();
+      wc[w] = make_int2((int)off, cnt);
+      off += cnt;
+    }
+    TRY(upload(b, b->wc, wc));
+  }
+  TRY(ensure(b, b->wbounds, NW)); TRY(ensure(b, b->wroot, NW));
   TRY(ensure(b, b->ncolors, 2 * (size_t)NW));
   TRY(upload(b, b->xf, xf)); TRY(upload(b, b->pos, pos)); TRY(upload(b, b->vel, vel)); TRY(upload(b, b->massd, massd));
   TRY(upload(b, b->damp, damp)); TRY(upload(b, b->force, force)); TRY(upload(b, b->lc, lc));
