@@ -161,17 +161,23 @@ B2G_API int b2g_server_tick(b2g_server* s, int32_t* active, double* step_ms) {
       continue;
     }
     r.admit = now_s();
+    if (r.steps == 0) {  // nothing to step: summarise the initial state and retire at once
+      float cs[4];
+      st = world_checksum(s, r.world, cs);
+      b2g_world_retire(s->batch, r.world);
+      ++s->retired;
+      ++s->completed;
+      finish(s, r, st, st == B2G_OK ? cs : nullptr);
+      continue;
+    }
     s->in_use += r.bytes;
     s->active.push_back(r);
   }
   if (active) *active = (int32_t)s->active.size();
   if (step_ms) *step_ms = 0.0;
-  if (s->active.empty()) return B2G_OK;
-  // requests with K = 0 finish without stepping
-  double t0 = now_s();
-  bool any_steps = false;
-  for (const Request& r : s->active) any_steps = any_steps || r.done < r.steps;
-  if (any_steps) {
+  if (!s->active.empty()) {
+    // every active request has at least one step left (K = 0 requests finish at admission)
+    double t0 = now_s();
     int st = b2g_step(s->batch, s->dt, s->vi, s->pi, nullptr);
     if (step_ms) *step_ms = (now_s() - t0) * 1e3;
     if (st != B2G_OK) return st;
@@ -179,7 +185,7 @@ B2G_API int b2g_server_tick(b2g_server* s, int32_t* active, double* step_ms) {
   // retire finished requests
   std::vector<Request> still;
   for (Request& r : s->active) {
-    if (r.done < r.steps) ++r.done;
+    ++r.done;
     if (r.done >= r.steps) {
       float cs[4];
       int st = world_checksum(s, r.world, cs);
