@@ -63,7 +63,9 @@ B2G_API int b2g_server_create(int device, uint64_t budget_bytes, int32_t max_wor
   if (!out || max_worlds <= 0 || !(dt > 0.0f) || velocity_iterations < 0 || position_iterations < 0)
     return B2G_E_INVALID_ARG;
   b2g_server* s = new b2g_server();
-  int st = b2g_batch_create(device, budget_bytes, &s->batch);
+  // the budget governs admission (per-body estimate); the batch itself gets no hard cap, since
+  // its fixed scratch (sort temporaries, counters) does not scale with the admitted bodies
+  int st = b2g_batch_create(device, 0, &s->batch);
   if (st != B2G_OK) {
     delete s;
     return st;
