@@ -64,6 +64,13 @@ class ClockSampler:
                                          stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
         except OSError:
             self.proc = None
+        # nvidia-smi's start-up (NVML initialisation) stalls the driver for a moment: wait for its
+        # first sample so that the stall falls before the timed region, not inside it
+        t0 = time.time()
+        while self.proc and self.proc.poll() is None and time.time() - t0 < 15.0:
+            if os.path.getsize(self.path) > 0:
+                break
+            time.sleep(0.05)
         return self
 
     def __exit__(self, *exc):

@@ -127,10 +127,15 @@ static KernelArgs make_args(Batch* b) {
   a.mval_sorted = b->mval_sorted.p; a.nchild = b->nchild.p; a.nparent = b->nparent.p; a.lparent = b->lparent.p;
   a.naabb = b->naabb.p; a.nflag = b->nflag.p; a.wroot = b->wroot.p; a.pcount = b->pcount.p; a.poff = b->poff.p;
   a.pairs = b->pairs.p; a.cub_tmp = b->cub_tmp.p;
-  a.sc_list = b->sc_list.p; a.vc = b->vc.p; a.ccolor = b->ccolor.p; a.corder = b->corder.p; a.cprio = b->cprio.p;
-  a.cready = b->cready.p; a.inc_cnt = b->inc_cnt.p; a.inc_off = b->inc_off.p; a.inc_head = b->inc_head.p;
-  a.inc_mask = b->inc_mask.p; a.inc_list = b->inc_list.p; a.jinc_list = b->jinc_list.p; a.jcolor = b->jcolor.p;
-  a.jorder = b->jorder.p; a.jprio = b->jprio.p; a.jready = b->jready.p; a.ncolors = b->ncolors.p;
+  a.sc_list = b->sc_list.p; a.scb = b->scb.p; a.ccol = b->ccol.p; a.corder = b->corder.p; a.cprio = b->cprio.p;
+  a.sp.nf = b->sp_nf.p; a.sp.mass = b->sp_mass.p; a.sp.r0 = b->sp_r0.p; a.sp.r1 = b->sp_r1.p;
+  a.sp.nmtm = b->sp_nmtm.p; a.sp.bk = b->sp_bk.p; a.sp.kn = b->sp_kn.p; a.sp.imp = b->sp_imp.p;
+  a.sp.idx = b->sp_idx.p; a.sp.lcs = b->sp_lcs.p; a.sp.lnp = b->sp_lnp.p; a.sp.lps = b->sp_lps.p;
+  a.sp.rad = b->sp_rad.p;
+  a.cready = b->cready.p; a.inc_cnt = b->inc_cnt.p; a.inc_head = b->inc_head.p;
+  a.inc_mask = b->inc_mask.p; a.inc_list = b->inc_list.p; a.jinc_list = b->jinc_list.p; a.jcb = b->jcb.p;
+  a.jcol = b->jcol.p; a.jorder = b->jorder.p; a.jranges = b->jranges.p; a.jprio = b->jprio.p;
+  a.jready = b->jready.p; a.ncolors = b->ncolors.p;
   a.events = b->events.p; a.event_cap = b->event_cap; a.events_on = b->events_on ? 1 : 0;
   a.counters = b->counters.p; a.status = b->status.p;
   return a;
@@ -145,6 +150,18 @@ static uint64_t emitter_key(const HostWorld& w, int fo, int fa, int fb) {
   else if (sb) { e = fa; p = fb; }
   else { e = std::min(fa, fb); p = std::max(fa, fb); }
   return ((uint64_t)(uint32_t)(e + fo) << 32) | (uint32_t)(p + fo);
+}
+
+// Reads the status word after the upload's joint colouring (the upload synchronises anyway).
+static int check_upload_status(Batch* b) {
+  unsigned int st = 0;
+  CUDA_TRY(b, cudaMemcpyAsync(&st, b->status.p, sizeof(st), cudaMemcpyDeviceToHost, b->stream));
+  CUDA_TRY(b, cudaStreamSynchronize(b->stream));
+  if (st & B2G_DEV_COLOR_ROUNDS) {
+    set_error(b, "joint colouring did not complete");
+    return B2G_E_CAPACITY;
+  }
+  return B2G_OK;
 }
 
 int upload_all(Batch* b) {
@@ -256,12 +273,16 @@ int upload_all(Batch* b) {
     cmat[i] = make_float4(c.friction, c.restitution, c.restitution_threshold, c.tangent_speed);
     cman[i] = c.manifold;
   }
-  // worlds in decreasing order of work so the largest start first
+  // worlds by body count, largest first: solver launch classes are contiguous ranges of it
   std::vector<int> order(NW);
   std::iota(order.begin(), order.end(), 0);
-  std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
-    return b->worlds[x].bodies.size() + b->worlds[x].joints.size() > b->worlds[y].bodies.size() + b->worlds[y].joints.size();
-  });
+  std::stable_sort(order.begin(), order.end(),
+                   [&](int x, int y) { return b->worlds[x].bodies.size() > b->worlds[y].bodies.size(); });
+  {
+    std::vector<int> nbw(NW);
+    for (int w = 0; w < NW; ++w) nbw[w] = (int)b->worlds[w].bodies.size();
+    b->solve_classes = plan_solve_classes(order, nbw);
+  }
   TRY(upload(b, b->wb, wb)); TRY(upload(b, b->wj, wj)); TRY(upload(b, b->wg, wg)); TRY(upload(b, b->wflags, wflags));
   TRY(upload(b, b->world_order, order));
   // per-world live contact ranges: the sorted contact list groups by world (keys hold global
@@ -277,7 +298,7 @@ int upload_all(Batch* b) {
     TRY(upload(b, b->wc, wc));
   }
   TRY(ensure(b, b->wbounds, NW)); TRY(ensure(b, b->wroot, NW));
-  TRY(ensure(b, b->ncolors, 2 * (size_t)NW));
+  TRY(ensure(b, b->ncolors, 4 * (size_t)NW)); TRY(ensure(b, b->jranges, 65 * (size_t)NW));
   TRY(upload(b, b->xf, xf)); TRY(upload(b, b->pos, pos)); TRY(upload(b, b->vel, vel)); TRY(upload(b, b->massd, massd));
   TRY(upload(b, b->damp, damp)); TRY(upload(b, b->force, force)); TRY(upload(b, b->lc, lc));
   TRY(upload(b, b->btype, btype)); TRY(upload(b, b->bworld, bworld));
@@ -296,10 +317,9 @@ int upload_all(Batch* b) {
   TRY(ensure(b, b->pcount, (size_t)NF + 1));
   TRY(ensure(b, b->poff, (size_t)NF + 1));
   TRY(ensure(b, b->cub_tmp, cub_temp_bytes(NF)));
-  TRY(ensure(b, b->inc_cnt, NB)); TRY(ensure(b, b->inc_off, NB)); TRY(ensure(b, b->inc_head, NB));
-  TRY(ensure(b, b->inc_mask, NB));
-  TRY(ensure(b, b->jinc_list, 2 * (size_t)NJ)); TRY(ensure(b, b->jcolor, NJ)); TRY(ensure(b, b->jorder, NJ));
-  TRY(ensure(b, b->jprio, NJ)); TRY(ensure(b, b->jready, NJ));
+  TRY(ensure(b, b->inc_cnt, NB)); TRY(ensure(b, b->inc_head, NB)); TRY(ensure(b, b->inc_mask, NB));
+  TRY(ensure(b, b->jinc_list, 2 * (size_t)NJ)); TRY(ensure(b, b->jcol, NJ)); TRY(ensure(b, b->jorder, NJ));
+  TRY(ensure(b, b->jcb, NJ)); TRY(ensure(b, b->jprio, NJ)); TRY(ensure(b, b->jready, NJ));
   TRY(ensure(b, b->status, 1)); TRY(ensure(b, b->counters, 4));
   b->NW = NW; b->NB = NB; b->NF = NF; b->NJ = NJ; b->NC = NC;
   {
@@ -308,6 +328,10 @@ int upload_all(Batch* b) {
   }
   b->h_wflags = wflags;
   b->ccap = 0;
+  // joint colours are fixed for the layout
+  CUDA_TRY(b, cudaMemsetAsync(b->status.p, 0, sizeof(unsigned int), b->stream));
+  launch_joint_colour(make_args(b), 0, NW, b->stream);
+  TRY(check_upload_status(b));
   b->layout_version++;
   b->structure_dirty = false;
   b->device_state_valid = true;
@@ -408,14 +432,19 @@ int upload_tail(Batch* b) {
   }
   std::vector<int> order(NW);
   std::iota(order.begin(), order.end(), 0);
-  std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
-    return b->worlds[x].bodies.size() + b->worlds[x].joints.size() > b->worlds[y].bodies.size() + b->worlds[y].joints.size();
-  });
+  std::stable_sort(order.begin(), order.end(),
+                   [&](int x, int y) { return b->worlds[x].bodies.size() > b->worlds[y].bodies.size(); });
+  {
+    std::vector<int> nbw(NW);
+    for (int w = 0; w < NW; ++w) nbw[w] = (int)b->worlds[w].bodies.size();
+    b->solve_classes = plan_solve_classes(order, nbw);
+  }
   std::vector<int2> wc_tail(NW - w0, make_int2(0, 0));
   TRY(upload(b, b->wb, wb)); TRY(upload(b, b->wj, wj)); TRY(upload_at(b, b->wg, w0, wg_tail));
   TRY(upload(b, b->wflags, wflags)); TRY(upload(b, b->world_order, order)); TRY(upload_at(b, b->wc, w0, wc_tail));
   b->h_wflags = wflags;
-  TRY(ensure(b, b->wbounds, NW)); TRY(ensure(b, b->wroot, NW)); TRY(ensure(b, b->ncolors, 2 * (size_t)NW));
+  TRY(ensure(b, b->wbounds, NW)); TRY(ensure(b, b->wroot, NW)); TRY(ensure(b, b->ncolors, 4 * (size_t)NW, true));
+  TRY(ensure(b, b->jranges, 65 * (size_t)NW, true));
   TRY(upload_at(b, b->xf, NB0, xf)); TRY(upload_at(b, b->pos, NB0, pos)); TRY(upload_at(b, b->vel, NB0, vel));
   TRY(upload_at(b, b->massd, NB0, massd)); TRY(upload_at(b, b->damp, NB0, damp)); TRY(upload_at(b, b->force, NB0, force));
   TRY(upload_at(b, b->lc, NB0, lc)); TRY(upload_at(b, b->btype, NB0, btype)); TRY(upload_at(b, b->bworld, NB0, bworld));
@@ -429,11 +458,13 @@ int upload_tail(Batch* b) {
   TRY(ensure(b, b->nparent, NF)); TRY(ensure(b, b->lparent, NF)); TRY(ensure(b, b->naabb, NF));
   TRY(ensure(b, b->nflag, NF)); TRY(ensure(b, b->pcount, (size_t)NF + 1)); TRY(ensure(b, b->poff, (size_t)NF + 1));
   TRY(ensure(b, b->cub_tmp, cub_temp_bytes(NF)));
-  TRY(ensure(b, b->inc_cnt, NB)); TRY(ensure(b, b->inc_off, NB)); TRY(ensure(b, b->inc_head, NB));
-  TRY(ensure(b, b->inc_mask, NB));
-  TRY(ensure(b, b->jinc_list, 2 * (size_t)NJ)); TRY(ensure(b, b->jcolor, NJ)); TRY(ensure(b, b->jorder, NJ));
-  TRY(ensure(b, b->jprio, NJ)); TRY(ensure(b, b->jready, NJ));
+  TRY(ensure(b, b->inc_cnt, NB)); TRY(ensure(b, b->inc_head, NB)); TRY(ensure(b, b->inc_mask, NB));
+  TRY(ensure(b, b->jinc_list, 2 * (size_t)NJ)); TRY(ensure(b, b->jcol, NJ, true)); TRY(ensure(b, b->jorder, NJ, true));
+  TRY(ensure(b, b->jcb, NJ, true)); TRY(ensure(b, b->jprio, NJ, true)); TRY(ensure(b, b->jready, NJ));
   b->NW = NW; b->NB = NB; b->NF = NF; b->NJ = NJ;
+  CUDA_TRY(b, cudaMemsetAsync(b->status.p, 0, sizeof(unsigned int), b->stream));
+  launch_joint_colour(make_args(b), w0, NW - w0, b->stream);
+  TRY(check_upload_status(b));
   b->layout_version++;
   CUDA_TRY(b, cudaStreamSynchronize(b->stream));
   return B2G_OK;
@@ -536,9 +567,14 @@ static int ensure_contact_capacity(Batch* b, int64_t want) {
     TRY(ensure(b, b->cman[k], (size_t)cap, keep));
   }
   TRY(ensure(b, b->pairs, (size_t)cap));
-  TRY(ensure(b, b->sc_list, (size_t)cap)); TRY(ensure(b, b->vc, (size_t)cap)); TRY(ensure(b, b->ccolor, (size_t)cap));
+  TRY(ensure(b, b->sc_list, (size_t)cap)); TRY(ensure(b, b->scb, (size_t)cap)); TRY(ensure(b, b->ccol, (size_t)cap));
   TRY(ensure(b, b->corder, (size_t)cap)); TRY(ensure(b, b->cprio, (size_t)cap)); TRY(ensure(b, b->cready, (size_t)cap));
   TRY(ensure(b, b->inc_list, 2 * (size_t)cap));
+  TRY(ensure(b, b->sp_nf, (size_t)cap)); TRY(ensure(b, b->sp_mass, (size_t)cap)); TRY(ensure(b, b->sp_r0, (size_t)cap));
+  TRY(ensure(b, b->sp_r1, (size_t)cap)); TRY(ensure(b, b->sp_nmtm, (size_t)cap)); TRY(ensure(b, b->sp_bk, (size_t)cap));
+  TRY(ensure(b, b->sp_kn, (size_t)cap)); TRY(ensure(b, b->sp_imp, (size_t)cap)); TRY(ensure(b, b->sp_idx, (size_t)cap));
+  TRY(ensure(b, b->sp_lcs, (size_t)cap)); TRY(ensure(b, b->sp_lnp, (size_t)cap)); TRY(ensure(b, b->sp_lps, (size_t)cap));
+  TRY(ensure(b, b->sp_rad, (size_t)cap));
   if (b->events_on) {
     TRY(ensure(b, b->events, (size_t)(4 * cap + 1024)));
     b->event_cap = (int64_t)b->events.cap;
@@ -592,7 +628,8 @@ static void enqueue_step(Batch* b, float dt, int vi, int pi, bool initial_bp, in
   launch_collide(a, b->stream);
   if (record_profile) cudaEventRecord(b->ev[1], b->stream);
   if (dt > 0.0f) {
-    launch_solve(a, b->NW, b->stream);
+    launch_solve(a, b->solve_classes, b->stream, b->side, b->fork_ev);
+    b->last_solve_buf = src;
     if (record_profile) cudaEventRecord(b->ev[2], b->stream);
     enqueue_broadphase(b, a, src);
     src ^= 1;
@@ -761,6 +798,7 @@ int step_batch(Batch* b, float dt, int vi, int pi, const uint8_t* mask, bool syn
     CUDA_TRY(b, cudaGraphLaunch(b->graph_exec[entry], b->stream));
     cudaEventRecord(b->ev[4], b->stream);
     b->cur = entry ^ 1;
+    b->last_solve_buf = entry;
   } else {
     enqueue_step(b, dt, vi, pi, false, entry, true);
   }
@@ -850,6 +888,9 @@ B2G_API int b2g_batch_create(int device, uint64_t budget_bytes, b2g_batch** out)
     return B2G_E_CUDA;
   }
   for (int i = 0; i < 8; ++i) cudaEventCreate(&b->ev[i]);
+  for (int i = 0; i < B2G_SOLVE_CLASSES; ++i) cudaStreamCreateWithFlags(&b->side[i], cudaStreamNonBlocking);
+  for (int i = 0; i <= B2G_SOLVE_CLASSES; ++i) cudaEventCreateWithFlags(&b->fork_ev[i], cudaEventDisableTiming);
+  solver_setup();
   *out = b;
   return B2G_OK;
 }
@@ -877,11 +918,20 @@ B2G_API int b2g_batch_destroy(b2g_batch* b) {
   release(b, b->wbounds); release(b, b->mkey); release(b, b->mkey_sorted); release(b, b->mval);
   release(b, b->mval_sorted); release(b, b->nchild); release(b, b->nparent); release(b, b->lparent);
   release(b, b->naabb); release(b, b->nflag); release(b, b->wroot); release(b, b->pcount); release(b, b->poff); release(b, b->pairs);
-  release(b, b->cub_tmp); release(b, b->status); release(b, b->counters); release(b, b->sc_list); release(b, b->vc);
-  release(b, b->ccolor); release(b, b->corder); release(b, b->cprio); release(b, b->cready); release(b, b->inc_cnt);
-  release(b, b->inc_off); release(b, b->inc_head); release(b, b->inc_mask); release(b, b->inc_list);
-  release(b, b->jinc_list); release(b, b->jcolor); release(b, b->jorder); release(b, b->jprio); release(b, b->jready);
+  release(b, b->cub_tmp); release(b, b->status); release(b, b->counters); release(b, b->sc_list); release(b, b->scb);
+  release(b, b->ccol); release(b, b->corder); release(b, b->cprio); release(b, b->cready); release(b, b->inc_cnt);
+  release(b, b->inc_head); release(b, b->inc_mask); release(b, b->inc_list);
+  release(b, b->sp_nf); release(b, b->sp_mass); release(b, b->sp_r0); release(b, b->sp_r1); release(b, b->sp_nmtm);
+  release(b, b->sp_bk); release(b, b->sp_kn); release(b, b->sp_imp); release(b, b->sp_idx); release(b, b->sp_lcs);
+  release(b, b->sp_lnp); release(b, b->sp_lps); release(b, b->sp_rad);
+  release(b, b->jinc_list); release(b, b->jcol); release(b, b->jorder); release(b, b->jcb); release(b, b->jranges);
+  release(b, b->jprio); release(b, b->jready);
   release(b, b->ncolors); release(b, b->events);
+  for (int i = 0; i < B2G_SOLVE_CLASSES; ++i) {
+    if (b->side[i]) cudaStreamDestroy(b->side[i]);
+    if (b->fork_ev[i]) cudaEventDestroy(b->fork_ev[i]);
+  }
+  if (b->fork_ev[B2G_SOLVE_CLASSES]) cudaEventDestroy(b->fork_ev[B2G_SOLVE_CLASSES]);
   for (int i = 0; i < 8; ++i)
     if (b->ev[i]) cudaEventDestroy(b->ev[i]);
   cudaStreamDestroy(b->stream);
@@ -1294,8 +1344,64 @@ B2G_API int b2g_profile_get(b2g_batch* b, b2g_profile* out) {
 
 B2G_API int b2g_solver_order(b2g_batch* b, int32_t world, int32_t* contact_color, uint32_t* contact_priority,
                              int32_t nc, int32_t* joint_color, uint32_t* joint_priority, int32_t nj) {
-  if (!world_index_ok(b, world)) return B2G_E_INVALID_ARG;
-  (void)contact_color; (void)contact_priority; (void)nc; (void)joint_color; (void)joint_priority; (void)nj;
+  if (!world_index_ok(b, world) || nc < 0 || nj < 0) return B2G_E_INVALID_ARG;
+  if (b->device < 0 || b->structure_dirty || world >= b->NW) return B2G_E_INVALID_ARG;
+  CUDA_TRY(b, cudaSetDevice(b->device));
+  cudaStream_t s = b->stream;
+  int w = world;
+  // joints: colours and priorities fixed for the layout
+  int j0 = b->h_joint_off[w], njw = b->h_joint_off[w + 1] - j0;
+  int jn = std::min(nj, njw);
+  std::vector<int8_t> jc(std::max(jn, 1));
+  if (jn > 0) {
+    CUDA_TRY(b, cudaMemcpyAsync(jc.data(), b->jcol.p + j0, jn, cudaMemcpyDeviceToHost, s));
+    if (joint_priority) CUDA_TRY(b, cudaMemcpyAsync(joint_priority, b->jprio.p + j0, jn * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+  }
+  // contacts: the last solve's solver contacts, matched by key into the current contact list
+  int info[4] = {0, 0, 0, 0};
+  int2 wcw = make_int2(0, 0);
+  CUDA_TRY(b, cudaMemcpyAsync(info, b->ncolors.p + 4 * w, sizeof(info), cudaMemcpyDeviceToHost, s));
+  CUDA_TRY(b, cudaMemcpyAsync(&wcw, b->wc.p + w, sizeof(int2), cudaMemcpyDeviceToHost, s));
+  CUDA_TRY(b, cudaStreamSynchronize(s));
+  for (int j = 0; j < jn; ++j)
+    if (joint_color) joint_color[j] = jc[j];
+  int nsc = b->last_solve_buf < 0 ? 0 : info[2], base = info[3];
+  std::vector<int> sl(std::max(nsc, 1));
+  std::vector<int8_t> cc(std::max(nsc, 1));
+  std::vector<uint32_t> cp(std::max(nsc, 1));
+  std::vector<uint64_t> cur_keys(std::max(wcw.y, 1));
+  if (nsc > 0) {
+    CUDA_TRY(b, cudaMemcpyAsync(sl.data(), b->sc_list.p + base, nsc * sizeof(int), cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(b, cudaMemcpyAsync(cc.data(), b->ccol.p + base, nsc, cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(b, cudaMemcpyAsync(cp.data(), b->cprio.p + base, nsc * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+  }
+  if (wcw.y > 0)
+    CUDA_TRY(b, cudaMemcpyAsync(cur_keys.data(), b->ckey[b->cur].p + wcw.x, wcw.y * sizeof(uint64_t),
+                                cudaMemcpyDeviceToHost, s));
+  CUDA_TRY(b, cudaStreamSynchronize(s));
+  // keys of the solved contacts in the list the solve read (their indices span one world range)
+  std::vector<uint64_t> old_keys(std::max(nsc, 1));
+  if (nsc > 0) {
+    int lo = *std::min_element(sl.begin(), sl.begin() + nsc), hi = *std::max_element(sl.begin(), sl.begin() + nsc);
+    std::vector<uint64_t> span(hi - lo + 1);
+    CUDA_TRY(b, cudaMemcpyAsync(span.data(), b->ckey[b->last_solve_buf].p + lo, span.size() * sizeof(uint64_t),
+                                cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(b, cudaStreamSynchronize(s));
+    for (int k = 0; k < nsc; ++k) old_keys[k] = span[sl[k] - lo];
+  }
+  int cn = std::min(nc, wcw.y);
+  for (int i = 0; i < cn; ++i) {
+    if (contact_color) contact_color[i] = -1;
+    if (contact_priority) contact_priority[i] = 0;
+  }
+  for (int k = 0; k < nsc; ++k) {
+    auto it = std::lower_bound(cur_keys.begin(), cur_keys.begin() + wcw.y, old_keys[k]);
+    if (it == cur_keys.begin() + wcw.y || *it != old_keys[k]) continue;
+    int i = (int)(it - cur_keys.begin());
+    if (i >= cn) continue;
+    if (contact_color) contact_color[i] = cc[k];
+    if (contact_priority) contact_priority[i] = cp[k];
+  }
   return B2G_OK;
 }
 

@@ -91,6 +91,12 @@ struct DBuf {
 
 struct Batch;
 
+// One solver launch over a contiguous range of the size-sorted world order.
+struct SolveClass {
+  int first, count, threads, smem;
+};
+#define B2G_SOLVE_CLASSES 5
+
 // Status word the kernels write instead of trapping (bounded waits and capacity checks).
 #define B2G_DEV_OK 0u
 #define B2G_DEV_STACK_OVERFLOW 1u
@@ -149,6 +155,7 @@ struct Batch {
   DBuf<float4> cmat[2];
   DBuf<b2g_manifold> cman[2];
   int cur = 0;
+  int last_solve_buf = -1;        // contact buffer the last solve read (solver order lookups)
 
   // broadphase scratch
   DBuf<float4> wbounds;
@@ -168,18 +175,27 @@ struct Batch {
 
   // solver scratch
   DBuf<int> sc_list;              // per world: compacted solver contact indices (global)
-  DBuf<VCDev> vc;
-  DBuf<int> ccolor, corder;
+  DBuf<int2> scb;                 // per solver contact: world-local non-static bodies
+  DBuf<float4> sp_nf, sp_mass, sp_r0, sp_r1, sp_nmtm, sp_bk, sp_kn, sp_imp, sp_lcs, sp_lnp, sp_lps;
+  DBuf<int4> sp_idx;
+  DBuf<float2> sp_rad;
+  DBuf<int8_t> ccol;
+  DBuf<int> corder;
   DBuf<uint32_t> cprio;
   DBuf<uint8_t> cready;
-  DBuf<int> inc_cnt, inc_off, inc_head;
+  DBuf<int> inc_cnt, inc_head;
   DBuf<unsigned long long> inc_mask;
   DBuf<int> inc_list;             // 2 entries per constraint (contacts), world base 2*contact_off
   DBuf<int> jinc_list;            // 2 entries per joint
-  DBuf<int> jcolor, jorder;
+  DBuf<int2> jcb;
+  DBuf<int8_t> jcol;
+  DBuf<int> jorder, jranges;
   DBuf<uint32_t> jprio;
   DBuf<uint8_t> jready;
-  DBuf<int> ncolors;              // per world: used contact colours, used joint colours
+  DBuf<int> ncolors;              // per world: contact colours, joint colours, solver contacts, slot base
+  std::vector<SolveClass> solve_classes;
+  cudaStream_t side[B2G_SOLVE_CLASSES] = {};
+  cudaEvent_t fork_ev[B2G_SOLVE_CLASSES + 1] = {};
 
   // events
   DBuf<EventDev> events;

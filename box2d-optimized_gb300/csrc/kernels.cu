@@ -3,10 +3,7 @@
 //   k_collide      narrowphase + contact update for every contact of every active world
 //                  (b2ContactManager::Collide / b2Contact::Update, src/dynamics/b2_contact_manager.cpp:66-116,
 //                  src/dynamics/b2_contact.cpp:126-210)
-//   k_solve        one CTA per world: velocity integration, contact prepare, device graph colouring,
-//                  warm start, colour-ordered velocity iterations (joints then contacts), impulse
-//                  store, position integration, colour-ordered position iterations with per-world
-//                  early exit, transform sync (b2Island::Solve, src/dynamics/b2_island.cpp:253-484)
+//   (the island solver, one CTA per world, is in solve.cu)
 //   broadphase     fixture AABBs, 30-bit Morton codes, radix sort, Karras LBVH (one subtree per world),
 //                  bottom-up bounds, stack traversal emitting the sorted, filtered pair list, and the
 //                  sorted diff of that list against the live contacts (b2BroadPhase::UpdateAndQuery +
@@ -15,8 +12,8 @@
 
 #include "b2g_math.cuh"
 #include "engine.h"
+#include "dev_common.cuh"
 #include "kernels.h"
-#include "solver_dev.cuh"
 
 namespace b2g {
 
@@ -30,26 +27,6 @@ __device__ __forceinline__ Xf ldXf(const float4* xf, int i) {
   x.q.s = t.z;
   x.q.c = t.w;
   return x;
-}
-
-__device__ __forceinline__ void raise_status(unsigned int* status, unsigned int bit) { atomicOr(status, bit); }
-
-__device__ void record_event(const KernelArgs& a, int kind, int world, int fa, int fb, int pc, const float* ni,
-                             const float* ti, const b2g_manifold* old) {
-  unsigned long long slot = atomicAdd(&a.counters[1], 1ull);
-  if ((int64_t)slot >= a.event_cap) return;
-  EventDev& e = a.events[slot];
-  e.kind = kind;
-  e.world = world;
-  e.fixtureA = fa;
-  e.fixtureB = fb;
-  e.pointCount = pc;
-  e.normalImpulses[0] = ni ? ni[0] : 0.0f;
-  e.normalImpulses[1] = ni ? ni[1] : 0.0f;
-  e.tangentImpulses[0] = ti ? ti[0] : 0.0f;
-  e.tangentImpulses[1] = ti ? ti[1] : 0.0f;
-  if (old) e.old = *old;
-  else memset(&e.old, 0, sizeof(e.old));
 }
 
 // ================================================================================ narrowphase
@@ -110,429 +87,6 @@ __global__ void k_collide(KernelArgs a) {
     if (wasTouching && !touching) record_event(a, B2G_EVENT_END, w, f.x - fo, f.y - fo, 0, 0, 0, 0);
     if (!sensor && touching) record_event(a, B2G_EVENT_PRESOLVE, w, f.x - fo, f.y - fo, 0, 0, 0, &old);
   }
-}
-
-// ================================================================================ solver
-// Block-wide exclusive scan of one int per thread (blockDim.x == SOLVER_THREADS).
-__device__ int block_scan(int v, int* total) {
-  __shared__ int warp_sums[SOLVER_THREADS / 32];
-  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  int x = v;
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    int y = __shfl_up_sync(FULL_MASK, x, o);
-    if (lane >= o) x += y;
-  }
-  if (lane == 31) warp_sums[wid] = x;
-  __syncthreads();
-  if (wid == 0) {
-    int s = lane < SOLVER_THREADS / 32 ? warp_sums[lane] : 0;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      int y = __shfl_up_sync(FULL_MASK, s, o);
-      if (lane >= o) s += y;
-    }
-    if (lane < SOLVER_THREADS / 32) warp_sums[lane] = s;
-  }
-  __syncthreads();
-  int prefix = (wid > 0 ? warp_sums[wid - 1] : 0) + x - v;
-  *total = warp_sums[SOLVER_THREADS / 32 - 1];
-  __syncthreads();
-  return prefix;
-}
-
-// Greedy colouring in priority order, computed in parallel rounds (Jones-Plassmann with
-// smallest-free-colour choice): a constraint is coloured once it is the first uncoloured
-// constraint in the priority-sorted incidence list of each of its non-static bodies; it then takes
-// the lowest colour not used by those bodies. The result equals the sequential greedy pass in
-// priority order. Colours 0..62 are regular, 63 is the overflow colour solved serially.
-// Incidence lists must be sorted by (priority, index); list heads start at each list's first entry.
-__device__ void color_rounds(int n, int base, const int* bodyA, const int* bodyB, int bstride, const int* btype,
-                             const int* inc_list, int* inc_head, unsigned long long* inc_mask, int* color,
-                             uint8_t* ready, unsigned int* status) {
-  for (int round = 0; round <= n + 1; ++round) {
-    int any = 0;
-    for (int k = threadIdx.x; k < n; k += blockDim.x) {
-      uint8_t r = 0;
-      if (color[base + k] < 0) {
-        any = 1;
-        int ia = bodyA[(int64_t)(base + k) * bstride], ib = bodyB[(int64_t)(base + k) * bstride];
-        bool ok = true;
-        if (btype[ia] != B2G_STATIC) ok = ok && inc_list[inc_head[ia]] == k;
-        if (btype[ib] != B2G_STATIC) ok = ok && inc_list[inc_head[ib]] == k;
-        r = ok ? 1 : 0;
-      }
-      ready[base + k] = r;
-    }
-    if (!__syncthreads_or(any)) return;
-    for (int k = threadIdx.x; k < n; k += blockDim.x) {
-      if (!ready[base + k]) continue;
-      int ia = bodyA[(int64_t)(base + k) * bstride], ib = bodyB[(int64_t)(base + k) * bstride];
-      bool sa = btype[ia] == B2G_STATIC, sb = btype[ib] == B2G_STATIC;
-      unsigned long long used = (sa ? 0ull : inc_mask[ia]) | (sb ? 0ull : inc_mask[ib]);
-      unsigned long long freeBits = ~used & ((1ull << 63) - 1ull);
-      int col;
-      if (freeBits == 0ull) {
-        col = 63;
-      } else {
-        col = __ffsll((long long)freeBits) - 1;
-        if (!sa) inc_mask[ia] |= 1ull << col;
-        if (!sb) inc_mask[ib] |= 1ull << col;
-      }
-      color[base + k] = col;
-      if (!sa) inc_head[ia] += 1;
-      if (!sb) inc_head[ib] += 1;
-    }
-    __syncthreads();
-  }
-  if (threadIdx.x == 0) raise_status(status, B2G_DEV_COLOR_ROUNDS);
-}
-
-// Builds priority-sorted incidence lists for n constraints over the world's bodies and colours
-// them; then buckets constraints by colour into `order` (overflow bucket sorted by priority).
-// Returns the number of colours used (max colour + 1) through smem.
-__device__ int color_and_order(int n, int base, int listBase, const int* bodyA, const int* bodyB, int bstride,
-                               const uint32_t* prio, const int* btype, int b0, int nb, int* inc_cnt, int* inc_off,
-                               int* inc_head, unsigned long long* inc_mask, int* inc_list, int* color, uint8_t* ready,
-                               int* order, unsigned int* status, int* ranges) {
-  __shared__ int col_cnt[64];
-  __shared__ int col_off[65];
-  __shared__ int s_carry;
-  __shared__ int s_maxcol;
-  for (int i = threadIdx.x; i < nb; i += blockDim.x) {
-    inc_cnt[b0 + i] = 0;
-    inc_mask[b0 + i] = 0ull;
-  }
-  __syncthreads();
-  for (int k = threadIdx.x; k < n; k += blockDim.x) {
-    color[base + k] = -1;
-    int ia = bodyA[(int64_t)(base + k) * bstride], ib = bodyB[(int64_t)(base + k) * bstride];
-    if (btype[ia] != B2G_STATIC) atomicAdd(&inc_cnt[ia], 1);
-    if (btype[ib] != B2G_STATIC) atomicAdd(&inc_cnt[ib], 1);
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) s_carry = 0;
-  __syncthreads();
-  for (int c0 = 0; c0 < nb; c0 += blockDim.x) {
-    int i = c0 + threadIdx.x;
-    int v = i < nb ? inc_cnt[b0 + i] : 0;
-    int total;
-    int p = block_scan(v, &total);
-    if (i < nb) {
-      inc_off[b0 + i] = listBase + s_carry + p;
-      inc_head[b0 + i] = listBase + s_carry + p;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) s_carry += total;
-    __syncthreads();
-  }
-  for (int i = threadIdx.x; i < nb; i += blockDim.x) inc_cnt[b0 + i] = 0;
-  __syncthreads();
-  for (int k = threadIdx.x; k < n; k += blockDim.x) {
-    int ia = bodyA[(int64_t)(base + k) * bstride], ib = bodyB[(int64_t)(base + k) * bstride];
-    if (btype[ia] != B2G_STATIC) inc_list[inc_off[ia] + atomicAdd(&inc_cnt[ia], 1)] = k;
-    if (btype[ib] != B2G_STATIC) inc_list[inc_off[ib] + atomicAdd(&inc_cnt[ib], 1)] = k;
-  }
-  __syncthreads();
-  // sort each body's list by (priority, index)
-  for (int i = threadIdx.x; i < nb; i += blockDim.x) {
-    int off = inc_off[b0 + i], cnt = inc_cnt[b0 + i];
-    for (int x = 1; x < cnt; ++x) {
-      int kx = inc_list[off + x];
-      uint32_t px = prio[base + kx];
-      int y = x - 1;
-      while (y >= 0) {
-        int ky = inc_list[off + y];
-        uint32_t py = prio[base + ky];
-        if (py < px || (py == px && ky < kx)) break;
-        inc_list[off + y + 1] = ky;
-        --y;
-      }
-      inc_list[off + y + 1] = kx;
-    }
-  }
-  __syncthreads();
-  color_rounds(n, base, bodyA, bodyB, bstride, btype, inc_list, inc_head, inc_mask, color, ready, status);
-  // bucket by colour
-  if (threadIdx.x < 64) col_cnt[threadIdx.x] = 0;
-  if (threadIdx.x == 0) s_maxcol = -1;
-  __syncthreads();
-  for (int k = threadIdx.x; k < n; k += blockDim.x) {
-    int c = color[base + k];
-    atomicAdd(&col_cnt[c], 1);
-    atomicMax(&s_maxcol, c);
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    int s = 0;
-    for (int c = 0; c < 64; ++c) { col_off[c] = s; s += col_cnt[c]; col_cnt[c] = 0; }
-    col_off[64] = s;
-  }
-  __syncthreads();
-  for (int k = threadIdx.x; k < n; k += blockDim.x) {
-    int c = color[base + k];
-    order[base + col_off[c] + atomicAdd(&col_cnt[c], 1)] = k;
-  }
-  __syncthreads();
-  if (threadIdx.x == 0 && col_cnt[63] > 1) {
-    int off = base + col_off[63], cnt = col_cnt[63];
-    for (int x = 1; x < cnt; ++x) {
-      int kx = order[off + x];
-      uint32_t px = prio[base + kx];
-      int y = x - 1;
-      while (y >= 0) {
-        int ky = order[off + y];
-        uint32_t py = prio[base + ky];
-        if (py < px || (py == px && ky < kx)) break;
-        order[off + y + 1] = ky;
-        --y;
-      }
-      order[off + y + 1] = kx;
-    }
-  }
-  int ncol = s_maxcol + 1;
-  for (int c = threadIdx.x; c <= ncol; c += blockDim.x) ranges[c] = col_off[c];
-  __syncthreads();
-  return ncol;
-}
-
-__global__ void __launch_bounds__(SOLVER_THREADS) k_solve(KernelArgs a) {
-  const int w = a.world_order[blockIdx.x];
-  if ((a.wflags[w] & B2G_WF_ACTIVE) == 0) return;
-  __shared__ int cranges[65];
-  __shared__ int jranges[65];
-  __shared__ int s_nsc;
-  __shared__ int s_carry;
-  const int4 wb = a.wb[w];
-  const int b0 = wb.x, nb = wb.y, fo = wb.z;
-  const int2 wc = a.wc[w];
-  const int c0 = wc.x, ncAll = wc.y;
-  const int4 wj = a.wj[w];
-  const int j0 = wj.x, nj = wj.y;
-  const float4 wg = a.wg[w];
-  const float h = a.dt;
-  const float dtRatio = wg.z * a.dt;
-  const bool warm = (a.wflags[w] & B2G_WF_WARM) != 0;
-  const V2 gravity = mk(wg.x, wg.y);
-
-  // 1. velocity integration (b2_island.cpp:256-293, SolveOrphan :187-206)
-  for (int i = threadIdx.x; i < nb; i += blockDim.x) {
-    int bi = b0 + i;
-    if (a.btype[bi] != B2G_DYNAMIC) continue;
-    float4 v4 = a.vel[bi];
-    float4 md = a.massd[bi];
-    float4 dmp = a.damp[bi];
-    float4 fr = a.force[bi];
-    V2 v = mk(v4.x, v4.y);
-    float wv = v4.z;
-    addTo(v, (h * md.y) * (dmp.z * md.x * gravity + mk(fr.x, fr.y)));
-    wv += h * md.w * fr.z;
-    v.x /= (1.0f + h * dmp.x);
-    v.y /= (1.0f + h * dmp.x);
-    wv /= (1.0f + h * dmp.y);
-    a.vel[bi] = make_float4(v.x, v.y, wv, 0.0f);
-  }
-  if (threadIdx.x == 0) s_carry = 0;
-  __syncthreads();
-
-  // 2. solver contacts: touching, enabled, no sensor (b2_world.cpp:567-599), compacted in order
-  for (int k0 = 0; k0 < ncAll; k0 += blockDim.x) {
-    int k = k0 + threadIdx.x;
-    int flag = 0;
-    if (k < ncAll) {
-      int ci = c0 + k;
-      uint32_t fl = a.cflags[ci];
-      int2 f = a.cfix[ci];
-      flag = ((fl & B2G_CONTACT_TOUCHING) && (fl & B2G_CONTACT_ENABLED) && !a.fsensor[f.x] && !a.fsensor[f.y]) ? 1 : 0;
-    }
-    int total;
-    int p = block_scan(flag, &total);
-    if (flag) a.sc_list[c0 + s_carry + p] = c0 + k;
-    __syncthreads();
-    if (threadIdx.x == 0) s_carry += total;
-    __syncthreads();
-  }
-  if (threadIdx.x == 0) s_nsc = s_carry;
-  __syncthreads();
-  const int nsc = s_nsc;
-
-  // 3. prepare (b2ContactSolver::Initialize + InitializeVelocityConstraints) and priorities
-  for (int k = threadIdx.x; k < nsc; k += blockDim.x) {
-    int ci = a.sc_list[c0 + k];
-    int2 f = a.cfix[ci];
-    int ia = a.fbody[f.x], ib = a.fbody[f.y];
-    b2g_manifold m = a.cman[ci];
-    VCDev vc;
-    prepareContact(vc, m, a.cmat[ci], a.shape[f.x].radius, a.shape[f.y].radius, ia, ib, a.massd[ia], a.massd[ib],
-                   a.lc[ia], a.lc[ib], a.pos[ia], a.vel[ia], a.pos[ib], a.vel[ib], dtRatio, warm, ci);
-    a.vc[c0 + k] = vc;
-    uint64_t key = a.ckey[ci];
-    a.cprio[c0 + k] = contactPriority((uint32_t)(key >> 32) - (uint32_t)fo, (uint32_t)key - (uint32_t)fo);
-  }
-  __syncthreads();
-
-  // 4. colouring of contacts and joints
-  int ncc = 0, njc = 0;
-  if (nsc > 0) {
-    ncc = color_and_order(nsc, c0, 2 * c0, &a.vc[0].indexA, &a.vc[0].indexB, (int)(sizeof(VCDev) / sizeof(int)),
-                          a.cprio, a.btype, b0, nb, a.inc_cnt, a.inc_off, a.inc_head, a.inc_mask, a.inc_list,
-                          a.ccolor, a.cready, a.corder, a.status, cranges);
-  }
-  if (nj > 0) {
-    for (int k = threadIdx.x; k < nj; k += blockDim.x) a.jprio[j0 + k] = jointPriority((uint32_t)k);
-    __syncthreads();
-    njc = color_and_order(nj, j0, 2 * j0, &a.joints[0].d.body_a, &a.joints[0].d.body_b,
-                          (int)(sizeof(JointDev) / sizeof(int)), a.jprio, a.btype, b0, nb, a.inc_cnt, a.inc_off,
-                          a.inc_head, a.inc_mask, a.jinc_list, a.jcolor, a.jready, a.jorder, a.status, jranges);
-  }
-  if (threadIdx.x == 0) {
-    a.ncolors[2 * w] = ncc;
-    a.ncolors[2 * w + 1] = njc;
-    atomicAdd(&a.counters[2], (unsigned long long)nsc);
-  }
-
-  // 5. warm start contacts, then joint InitVelocityConstraints, colour by colour
-  if (warm) {
-    for (int c = 0; c < ncc; ++c) {
-      int s = cranges[c], e = cranges[c + 1];
-      if (c == 63) {
-        if (threadIdx.x == 0)
-          for (int i = s; i < e; ++i) warmStartContact(a.vc[c0 + a.corder[c0 + i]], a.vel);
-      } else {
-        for (int i = s + threadIdx.x; i < e; i += blockDim.x) warmStartContact(a.vc[c0 + a.corder[c0 + i]], a.vel);
-      }
-      __syncthreads();
-    }
-  }
-  for (int c = 0; c < njc; ++c) {
-    int s = jranges[c], e = jranges[c + 1];
-    if (c == 63) {
-      if (threadIdx.x == 0)
-        for (int i = s; i < e; ++i)
-          jointInit(a.joints[j0 + a.jorder[j0 + i]], a.massd, a.lc, a.pos, a.vel, a.dt, dtRatio, warm);
-    } else {
-      for (int i = s + threadIdx.x; i < e; i += blockDim.x)
-        jointInit(a.joints[j0 + a.jorder[j0 + i]], a.massd, a.lc, a.pos, a.vel, a.dt, dtRatio, warm);
-    }
-    __syncthreads();
-  }
-
-  // 6. velocity iterations: joints, then contacts (b2_island.cpp:327-346)
-  for (int it = 0; it < a.vi; ++it) {
-    for (int c = 0; c < njc; ++c) {
-      int s = jranges[c], e = jranges[c + 1];
-      if (c == 63) {
-        if (threadIdx.x == 0)
-          for (int i = s; i < e; ++i) jointSolveVelocity(a.joints[j0 + a.jorder[j0 + i]], a.vel, a.dt, a.inv_dt);
-      } else {
-        for (int i = s + threadIdx.x; i < e; i += blockDim.x)
-          jointSolveVelocity(a.joints[j0 + a.jorder[j0 + i]], a.vel, a.dt, a.inv_dt);
-      }
-      __syncthreads();
-    }
-    for (int c = 0; c < ncc; ++c) {
-      int s = cranges[c], e = cranges[c + 1];
-      if (c == 63) {
-        if (threadIdx.x == 0)
-          for (int i = s; i < e; ++i) solveContactVelocity(a.vc[c0 + a.corder[c0 + i]], a.vel);
-      } else {
-        for (int i = s + threadIdx.x; i < e; i += blockDim.x) solveContactVelocity(a.vc[c0 + a.corder[c0 + i]], a.vel);
-      }
-      __syncthreads();
-    }
-  }
-
-  // 7. StoreImpulses (b2_contact_solver.cpp:641-657) and PostSolve reports
-  for (int k = threadIdx.x; k < nsc; k += blockDim.x) {
-    const VCDev& vc = a.vc[c0 + k];
-    b2g_manifold* m = &a.cman[vc.contact];
-    for (int j = 0; j < vc.pointCount; ++j) {
-      m->points[j].normal_impulse = vc.normalImpulse[j];
-      m->points[j].tangent_impulse = vc.tangentImpulse[j];
-    }
-  }
-
-  // 8. integrate positions (b2_island.cpp:349-385)
-  for (int i = threadIdx.x; i < nb; i += blockDim.x) {
-    int bi = b0 + i;
-    if (a.btype[bi] == B2G_STATIC) continue;
-    float4 p4 = a.pos[bi];
-    float4 v4 = a.vel[bi];
-    V2 c = mk(p4.x, p4.y);
-    float an = p4.z;
-    V2 v = mk(v4.x, v4.y);
-    float wv = v4.z;
-    V2 translation = h * v;
-    if (dot(translation, translation) > B2G_MAX_TRANSLATION_SQ) {
-      float ratio = B2G_MAX_TRANSLATION / lengthOf(translation);
-      v.x *= ratio;
-      v.y *= ratio;
-    }
-    float rotation = h * wv;
-    if (rotation * rotation > B2G_MAX_ROTATION_SQ) {
-      float ratio = B2G_MAX_ROTATION / fabs2(rotation);
-      wv *= ratio;
-    }
-    addTo(c, h * v);
-    an += h * wv;
-    a.pos[bi] = make_float4(c.x, c.y, an, 0.0f);
-    a.vel[bi] = make_float4(v.x, v.y, wv, 0.0f);
-  }
-  __syncthreads();
-
-  // 9. position iterations: contacts then joints, early exit for the world (b2_island.cpp:387-428)
-  for (int it = 0; it < a.pi; ++it) {
-    int okay = 1;
-    for (int c = 0; c < ncc; ++c) {
-      int s = cranges[c], e = cranges[c + 1];
-      if (c == 63) {
-        if (threadIdx.x == 0)
-          for (int i = s; i < e; ++i)
-            if (!(solveContactPosition(a.vc[c0 + a.corder[c0 + i]], a.pos) >= -3.0f * B2G_LINEAR_SLOP)) okay = 0;
-      } else {
-        for (int i = s + threadIdx.x; i < e; i += blockDim.x)
-          if (!(solveContactPosition(a.vc[c0 + a.corder[c0 + i]], a.pos) >= -3.0f * B2G_LINEAR_SLOP)) okay = 0;
-      }
-      __syncthreads();
-    }
-    for (int c = 0; c < njc; ++c) {
-      int s = jranges[c], e = jranges[c + 1];
-      if (c == 63) {
-        if (threadIdx.x == 0)
-          for (int i = s; i < e; ++i)
-            if (!jointSolvePosition(a.joints[j0 + a.jorder[j0 + i]], a.pos)) okay = 0;
-      } else {
-        for (int i = s + threadIdx.x; i < e; i += blockDim.x)
-          if (!jointSolvePosition(a.joints[j0 + a.jorder[j0 + i]], a.pos)) okay = 0;
-      }
-      __syncthreads();
-    }
-    if (__syncthreads_and(okay)) break;
-  }
-
-  // 10. transforms (b2Body::SynchronizeTransform, include/box2d/b2_body.h:957-961), finite check
-  int bad = 0;
-  for (int i = threadIdx.x; i < nb; i += blockDim.x) {
-    int bi = b0 + i;
-    if (a.btype[bi] == B2G_STATIC) continue;
-    float4 p4 = a.pos[bi];
-    Rot q = rotOf(p4.z);
-    float2 l = a.lc[bi];
-    V2 p = mk(p4.x, p4.y) - mul(q, mk(l.x, l.y));
-    a.xf[bi] = make_float4(p.x, p.y, q.s, q.c);
-    float4 v4 = a.vel[bi];
-    if (!isfinite(p4.x) || !isfinite(p4.y) || !isfinite(p4.z) || !isfinite(v4.x) || !isfinite(v4.y) || !isfinite(v4.z))
-      bad = 1;
-  }
-  if (__syncthreads_or(bad) && threadIdx.x == 0) raise_status(a.status, B2G_DEV_NONFINITE);
-  if (a.events_on) {
-    for (int k = threadIdx.x; k < nsc; k += blockDim.x) {
-      const VCDev& vc = a.vc[c0 + k];
-      int2 f = a.cfix[vc.contact];
-      record_event(a, B2G_EVENT_POSTSOLVE, w, f.x - fo, f.y - fo, vc.pointCount, vc.normalImpulse, vc.tangentImpulse, 0);
-    }
-  }
-  if (threadIdx.x == 0 && a.dt > 0.0f) a.wg[w].z = a.inv_dt;
 }
 
 __global__ void k_clear_forces(KernelArgs a, int nbodies) {
@@ -896,9 +450,6 @@ static inline unsigned grid_for(int64_t n, int bs) { return (unsigned)((n + bs -
 
 void launch_collide(const KernelArgs& a, cudaStream_t s) {
   if (a.ccap > 0) k_collide<<<grid_for(a.ccap, 128), 128, 0, s>>>(a);
-}
-void launch_solve(const KernelArgs& a, int nw, cudaStream_t s) {
-  if (nw > 0) k_solve<<<nw, SOLVER_THREADS, 0, s>>>(a);
 }
 void launch_clear_forces(const KernelArgs& a, int nb, cudaStream_t s) {
   if (nb > 0) k_clear_forces<<<grid_for(nb, 256), 256, 0, s>>>(a, nb);

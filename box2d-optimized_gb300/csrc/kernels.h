@@ -4,11 +4,32 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <vector>
+
 #include "engine.h"
 
 namespace b2g {
 
-#define SOLVER_THREADS 256
+// Solver contact constraints in colour order, one float4 (or int4) per plane and slot; world w
+// owns slots [contact_off, contact_off + solver contacts). Split by use so that each phase reads
+// only full, coalesced 16-byte rows: velocity (nf, mass, r0, r1, nmtm, bk, kn, imp, idx) and
+// position (mass, idx, lcs, lnp, lps, rad).
+struct SolverPlanes {
+  float4* nf;    // normal.x, normal.y, friction, tangentSpeed
+  float4* mass;  // invMassA, invIA, invMassB, invIB
+  float4* r0;    // rA.x, rA.y, rB.x, rB.y of point 0
+  float4* r1;    // ... of point 1
+  float4* nmtm;  // normalMass 0, 1, tangentMass 0, 1
+  float4* bk;    // velocityBias 0, 1, K.ex.x, K.ex.y (= K.ey.x)
+  float4* kn;    // K.ey.y, normalMass matrix ex.x, ex.y (= ey.x), ey.y
+  float4* imp;   // normalImpulse 0, 1, tangentImpulse 0, 1
+  int4* idx;     // world-local body A, body B, pointCount | pcPointCount << 4 | type << 8, contact
+  float4* lcs;   // localCenterA, localCenterB
+  float4* lnp;   // localNormal, localPoint
+  float4* lps;   // localPoints 0, 1
+  float2* rad;   // radiusA, radiusB
+};
+
 
 // Plain device pointers of one batch, passed by value to every kernel.
 struct KernelArgs {
@@ -63,18 +84,23 @@ struct KernelArgs {
   void* cub_tmp;
 
   // solver
-  int* sc_list;
-  VCDev* vc;
-  int *ccolor, *corder;
+  int* sc_list;                   // per solver contact: live contact index
+  int2* scb;                      // per solver contact: world-local non-static bodies (-1 = static)
+  SolverPlanes sp;
+  int8_t* ccol;
+  int* corder;
   uint32_t* cprio;
   uint8_t* cready;
-  int *inc_cnt, *inc_off, *inc_head;
+  int *inc_cnt, *inc_head;
   unsigned long long* inc_mask;
   int *inc_list, *jinc_list;
-  int *jcolor, *jorder;
+  int2* jcb;
+  int8_t* jcol;
+  int* jorder;
+  int* jranges;                   // per world: 65 joint colour offsets
   uint32_t* jprio;
   uint8_t* jready;
-  int* ncolors;
+  int* ncolors;                   // per world: contact colours, joint colours, solver contacts, slot base
 
   // events, status
   EventDev* events;
@@ -96,7 +122,13 @@ struct KernelArgs {
 #define B2G_CNT_OVERFLOW 3   // pair capacity needed when the last broadphase overflowed (else 0)
 
 void launch_collide(const KernelArgs& a, cudaStream_t s);
-void launch_solve(const KernelArgs& a, int nw, cudaStream_t s);
+// Solver launches per class: class 0 on `s`, the others on side streams forked from and joined
+// back to `s` with the given events (classes.size() - 1 streams, classes.size() events).
+void launch_solve(const KernelArgs& a, const std::vector<SolveClass>& classes, cudaStream_t s,
+                  const cudaStream_t* side, const cudaEvent_t* ev);
+void launch_joint_colour(const KernelArgs& a, int w0, int nw, cudaStream_t s);
+void solver_setup();
+std::vector<SolveClass> plan_solve_classes(const std::vector<int>& order, const std::vector<int>& bodies);
 void launch_clear_forces(const KernelArgs& a, int nb, cudaStream_t s);
 void launch_bp_build(const KernelArgs& a, int nf, int nw, size_t cub_bytes, int sort_bits, cudaStream_t s);
 void launch_bp_emit(const KernelArgs& a, int nf, cudaStream_t s);

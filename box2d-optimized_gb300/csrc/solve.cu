@@ -1,0 +1,721 @@
+// solve.cu - the island solver of one Step for every active world of the batch
+// (b2Island::Solve, src/dynamics/b2_island.cpp:253-484; b2ContactSolver,
+// src/dynamics/b2_contact_solver.cpp), one CTA per world.
+//
+// Per world, in order:
+//   1. solver contacts: the touching, enabled, non-sensor live contacts (b2_world.cpp:567-599),
+//      compacted in list order, with their world-local non-static bodies and priorities;
+//   2. deterministic greedy colouring of those contacts in priority order (Jones-Plassmann
+//      rounds), in shared memory when the world fits; joints keep the colouring computed once
+//      per layout by k_joint_colour;
+//   3. velocity integration into the body-state buffer (shared memory when the world fits);
+//   4. contact prepare, written straight into colour-ordered constraint planes;
+//   5. warm start, joint InitVelocityConstraints, velocity iterations (joints then contacts),
+//      StoreImpulses, position integration, position iterations (contacts then joints) with the
+//      world's early exit, transforms.
+// Constraints of one colour share no non-static body, so a colour runs in parallel; colours
+// run in order with a CTA barrier between them, which reproduces the sequential Gauss-Seidel
+// sweep in colour order. Worlds are launched in size classes (threads and shared memory per
+// class) on forked streams so that small and large worlds run side by side.
+#include "b2g_math.cuh"
+#include "dev_common.cuh"
+#include "engine.h"
+#include "kernels.h"
+#include "solver_dev.cuh"
+
+namespace b2g {
+
+#define FULL_MASK 0xffffffffu
+
+// Block-wide exclusive scan of one int per thread (blockDim.x == T).
+template <int T>
+__device__ int block_scan(int v, int* total) {
+  constexpr int NWARP = T / 32;
+  __shared__ int warp_sums[NWARP];
+  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  int x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    int y = __shfl_up_sync(FULL_MASK, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) warp_sums[wid] = x;
+  __syncthreads();
+  if (wid == 0) {
+    int s = lane < NWARP ? warp_sums[lane] : 0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      int y = __shfl_up_sync(FULL_MASK, s, o);
+      if (lane >= o) s += y;
+    }
+    if (lane < NWARP) warp_sums[lane] = s;
+  }
+  __syncthreads();
+  int prefix = (wid > 0 ? warp_sums[wid - 1] : 0) + x - v;
+  *total = warp_sums[NWARP - 1];
+  __syncthreads();
+  return prefix;
+}
+
+// Working arrays of one colouring, each in shared or global memory (generic pointers).
+struct ColourMem {
+  int* cnt;                  // per body: incidence count, then fill counter
+  int* head;                 // per body: list offset, then first uncoloured entry
+  unsigned long long* mask;  // per body: colours taken
+  int* list;                 // 2 per constraint: per-body incidence lists
+  const int2* cb;            // per constraint: world-local non-static bodies (-1 = static)
+  int8_t* col;               // per constraint: colour, -1 until coloured
+  uint8_t* rdy;              // per constraint: ready in the current round
+};
+
+// Greedy colouring in priority order, computed in parallel rounds (Jones-Plassmann with
+// smallest-free-colour choice): a constraint is coloured once it is the first uncoloured entry
+// of the priority-sorted incidence list of each of its non-static bodies; it then takes the
+// lowest colour not used at those bodies. The result equals the sequential greedy pass in
+// (priority, index) order. Colours 0..62 are regular; 63 is the overflow colour, solved
+// serially in priority order. Buckets the constraints by colour into `order` and writes the
+// colour offsets to `ranges` (ncol + 1 entries). Returns the number of colours (max + 1).
+template <int T>
+__device__ int colour_constraints(int n, int nb, const ColourMem m, const uint32_t* prio, int* order, int* ranges,
+                                  unsigned int* status) {
+  __shared__ int col_cnt[64];
+  __shared__ int col_off[65];
+  __shared__ int s_carry, s_maxcol;
+  for (int i = threadIdx.x; i < nb; i += T) {
+    m.cnt[i] = 0;
+    m.mask[i] = 0ull;
+  }
+  for (int k = threadIdx.x; k < n; k += T) m.col[k] = -1;
+  if (threadIdx.x == 0) s_carry = 0;
+  __syncthreads();
+  for (int k = threadIdx.x; k < n; k += T) {
+    int2 b = m.cb[k];
+    if (b.x >= 0) atomicAdd(&m.cnt[b.x], 1);
+    if (b.y >= 0) atomicAdd(&m.cnt[b.y], 1);
+  }
+  __syncthreads();
+  for (int i0 = 0; i0 < nb; i0 += T) {
+    int i = i0 + threadIdx.x;
+    int v = i < nb ? m.cnt[i] : 0;
+    int total;
+    int p = block_scan<T>(v, &total);
+    if (i < nb) m.head[i] = s_carry + p;
+    __syncthreads();
+    if (threadIdx.x == 0) s_carry += total;
+    __syncthreads();
+  }
+  for (int i = threadIdx.x; i < nb; i += T) m.cnt[i] = 0;
+  __syncthreads();
+  for (int k = threadIdx.x; k < n; k += T) {
+    int2 b = m.cb[k];
+    if (b.x >= 0) m.list[m.head[b.x] + atomicAdd(&m.cnt[b.x], 1)] = k;
+    if (b.y >= 0) m.list[m.head[b.y] + atomicAdd(&m.cnt[b.y], 1)] = k;
+  }
+  __syncthreads();
+  // each body's list in (priority, index) order
+  for (int i = threadIdx.x; i < nb; i += T) {
+    int off = m.head[i], cnt = m.cnt[i];
+    for (int x = 1; x < cnt; ++x) {
+      int kx = m.list[off + x];
+      uint32_t px = prio[kx];
+      int y = x - 1;
+      while (y >= 0) {
+        int ky = m.list[off + y];
+        uint32_t py = prio[ky];
+        if (py < px || (py == px && ky < kx)) break;
+        m.list[off + y + 1] = ky;
+        --y;
+      }
+      m.list[off + y + 1] = kx;
+    }
+  }
+  __syncthreads();
+  // rounds: every round colours at least the uncoloured constraint of lowest (priority, index)
+  bool done = false;
+  for (int round = 0; round <= n + 1; ++round) {
+    int any = 0;
+    for (int k = threadIdx.x; k < n; k += T) {
+      uint8_t r = 0;
+      if (m.col[k] < 0) {
+        any = 1;
+        int2 b = m.cb[k];
+        bool ok = (b.x < 0 || m.list[m.head[b.x]] == k) && (b.y < 0 || m.list[m.head[b.y]] == k);
+        r = ok ? 1 : 0;
+      }
+      m.rdy[k] = r;
+    }
+    if (!__syncthreads_or(any)) {
+      done = true;
+      break;
+    }
+    for (int k = threadIdx.x; k < n; k += T) {
+      if (!m.rdy[k]) continue;
+      int2 b = m.cb[k];
+      unsigned long long used = (b.x >= 0 ? m.mask[b.x] : 0ull) | (b.y >= 0 ? m.mask[b.y] : 0ull);
+      unsigned long long freeBits = ~used & ((1ull << 63) - 1ull);
+      int c;
+      if (freeBits == 0ull) {
+        c = 63;
+      } else {
+        c = __ffsll((long long)freeBits) - 1;
+        if (b.x >= 0) m.mask[b.x] |= 1ull << c;
+        if (b.y >= 0) m.mask[b.y] |= 1ull << c;
+      }
+      m.col[k] = (int8_t)c;
+      if (b.x >= 0) m.head[b.x] += 1;
+      if (b.y >= 0) m.head[b.y] += 1;
+    }
+    __syncthreads();
+  }
+  if (!done && threadIdx.x == 0) atomicOr(status, B2G_DEV_COLOR_ROUNDS);
+  // bucket by colour
+  if (threadIdx.x < 64) col_cnt[threadIdx.x] = 0;
+  if (threadIdx.x == 0) s_maxcol = -1;
+  __syncthreads();
+  for (int k = threadIdx.x; k < n; k += T) {
+    int c = m.col[k];
+    if (c < 0) c = 63;  // only after a failed colouring (status raised)
+    atomicAdd(&col_cnt[c], 1);
+    atomicMax(&s_maxcol, c);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int s = 0;
+    for (int c = 0; c < 64; ++c) {
+      col_off[c] = s;
+      s += col_cnt[c];
+      col_cnt[c] = 0;
+    }
+    col_off[64] = s;
+  }
+  __syncthreads();
+  for (int k = threadIdx.x; k < n; k += T) {
+    int c = m.col[k];
+    if (c < 0) c = 63;
+    order[col_off[c] + atomicAdd(&col_cnt[c], 1)] = k;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0 && col_cnt[63] > 1) {
+    int off = col_off[63], cnt = col_cnt[63];
+    for (int x = 1; x < cnt; ++x) {
+      int kx = order[off + x];
+      uint32_t px = prio[kx];
+      int y = x - 1;
+      while (y >= 0) {
+        int ky = order[off + y];
+        uint32_t py = prio[ky];
+        if (py < px || (py == px && ky < kx)) break;
+        order[off + y + 1] = ky;
+        --y;
+      }
+      order[off + y + 1] = kx;
+    }
+  }
+  int ncol = s_maxcol + 1;
+  for (int c = threadIdx.x; c <= ncol; c += T) ranges[c] = col_off[c];
+  __syncthreads();
+  return ncol;
+}
+
+// ---- constraint planes <-> the per-constraint register record
+__device__ __forceinline__ void store_planes(const SolverPlanes& P, int s, const VCDev& vc) {
+  P.nf[s] = make_float4(vc.normal[0], vc.normal[1], vc.friction, vc.tangentSpeed);
+  P.mass[s] = make_float4(vc.invMassA, vc.invIA, vc.invMassB, vc.invIB);
+  P.r0[s] = make_float4(vc.rA[0][0], vc.rA[0][1], vc.rB[0][0], vc.rB[0][1]);
+  P.r1[s] = make_float4(vc.rA[1][0], vc.rA[1][1], vc.rB[1][0], vc.rB[1][1]);
+  P.nmtm[s] = make_float4(vc.normalMass[0], vc.normalMass[1], vc.tangentMass[0], vc.tangentMass[1]);
+  P.bk[s] = make_float4(vc.velocityBias[0], vc.velocityBias[1], vc.K[0], vc.K[1]);
+  P.kn[s] = make_float4(vc.K[3], vc.NM[0], vc.NM[1], vc.NM[3]);
+  P.imp[s] = make_float4(vc.normalImpulse[0], vc.normalImpulse[1], vc.tangentImpulse[0], vc.tangentImpulse[1]);
+  P.idx[s] = make_int4(vc.indexA, vc.indexB, vc.pointCount | (vc.pcPointCount << 4) | (vc.type << 8), vc.contact);
+  P.lcs[s] = make_float4(vc.localCenterA[0], vc.localCenterA[1], vc.localCenterB[0], vc.localCenterB[1]);
+  P.lnp[s] = make_float4(vc.localNormal[0], vc.localNormal[1], vc.localPoint[0], vc.localPoint[1]);
+  P.lps[s] = make_float4(vc.localPoints[0][0], vc.localPoints[0][1], vc.localPoints[1][0], vc.localPoints[1][1]);
+  P.rad[s] = make_float2(vc.radiusA, vc.radiusB);
+}
+
+__device__ __forceinline__ void load_common(const SolverPlanes& P, int s, VCDev& vc) {
+  int4 id = P.idx[s];
+  vc.indexA = id.x;
+  vc.indexB = id.y;
+  vc.pointCount = id.z & 15;
+  vc.pcPointCount = (id.z >> 4) & 15;
+  vc.type = id.z >> 8;
+  vc.contact = id.w;
+  float4 m = P.mass[s];
+  vc.invMassA = m.x; vc.invIA = m.y; vc.invMassB = m.z; vc.invIB = m.w;
+}
+
+// Fields read by warmStartContact / solveContactVelocity.
+__device__ __forceinline__ void load_velocity(const SolverPlanes& P, int s, VCDev& vc, bool full) {
+  load_common(P, s, vc);
+  float4 nf = P.nf[s];
+  vc.normal[0] = nf.x; vc.normal[1] = nf.y; vc.friction = nf.z; vc.tangentSpeed = nf.w;
+  float4 r0 = P.r0[s];
+  vc.rA[0][0] = r0.x; vc.rA[0][1] = r0.y; vc.rB[0][0] = r0.z; vc.rB[0][1] = r0.w;
+  float4 im = P.imp[s];
+  vc.normalImpulse[0] = im.x; vc.normalImpulse[1] = im.y; vc.tangentImpulse[0] = im.z; vc.tangentImpulse[1] = im.w;
+  if (vc.pointCount == 2) {
+    float4 r1 = P.r1[s];
+    vc.rA[1][0] = r1.x; vc.rA[1][1] = r1.y; vc.rB[1][0] = r1.z; vc.rB[1][1] = r1.w;
+  }
+  if (full) {
+    float4 mm = P.nmtm[s];
+    vc.normalMass[0] = mm.x; vc.normalMass[1] = mm.y; vc.tangentMass[0] = mm.z; vc.tangentMass[1] = mm.w;
+    float4 bk = P.bk[s];
+    vc.velocityBias[0] = bk.x; vc.velocityBias[1] = bk.y;
+    if (vc.pointCount == 2) {
+      float4 kn = P.kn[s];
+      vc.K[0] = bk.z; vc.K[1] = bk.w; vc.K[2] = bk.w; vc.K[3] = kn.x;
+      vc.NM[0] = kn.y; vc.NM[1] = kn.z; vc.NM[2] = kn.z; vc.NM[3] = kn.w;
+    }
+  }
+}
+
+// Fields read by solveContactPosition.
+__device__ __forceinline__ void load_position(const SolverPlanes& P, int s, VCDev& vc) {
+  load_common(P, s, vc);
+  float4 lc = P.lcs[s];
+  vc.localCenterA[0] = lc.x; vc.localCenterA[1] = lc.y; vc.localCenterB[0] = lc.z; vc.localCenterB[1] = lc.w;
+  float4 ln = P.lnp[s];
+  vc.localNormal[0] = ln.x; vc.localNormal[1] = ln.y; vc.localPoint[0] = ln.z; vc.localPoint[1] = ln.w;
+  float4 lp = P.lps[s];
+  vc.localPoints[0][0] = lp.x; vc.localPoints[0][1] = lp.y; vc.localPoints[1][0] = lp.z; vc.localPoints[1][1] = lp.w;
+  float2 r = P.rad[s];
+  vc.radiusA = r.x; vc.radiusB = r.y;
+}
+
+// Carves 16-byte aligned pieces out of the CTA's dynamic shared memory.
+struct SmemCarver {
+  unsigned char* p;
+  size_t left;
+  __device__ void* take(size_t bytes) {
+    bytes = (bytes + 15) & ~(size_t)15;
+    if (bytes > left) return nullptr;
+    void* r = p;
+    p += bytes;
+    left -= bytes;
+    return r;
+  }
+};
+
+template <int T>
+__global__ void __launch_bounds__(T, 1024 / T) k_solve(KernelArgs a, int first, int smem_bytes) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int w = a.world_order[first + blockIdx.x];
+  if ((a.wflags[w] & B2G_WF_ACTIVE) == 0) return;
+  __shared__ int cranges[65];
+  __shared__ int jranges[65];
+  __shared__ int s_carry;
+  const int4 wb = a.wb[w];
+  const int b0 = wb.x, nb = wb.y, fo = wb.z;
+  const int2 wc = a.wc[w];
+  const int c0 = wc.x, ncAll = wc.y;
+  const int4 wj = a.wj[w];
+  const int j0 = wj.x, nj = wj.y;
+  const float4 wg = a.wg[w];
+  const float h = a.dt;
+  const float dtRatio = wg.z * a.dt;
+  const bool warm = (a.wflags[w] & B2G_WF_WARM) != 0;
+  const V2 gravity = mk(wg.x, wg.y);
+  const SolverPlanes P = a.sp;
+
+  // 1. solver contacts in list order, with local bodies (static = -1) and colouring priorities
+  if (threadIdx.x == 0) s_carry = 0;
+  __syncthreads();
+  for (int k0 = 0; k0 < ncAll; k0 += T) {
+    int k = k0 + threadIdx.x;
+    int flag = 0;
+    int2 f = make_int2(0, 0);
+    if (k < ncAll) {
+      uint32_t fl = a.cflags[c0 + k];
+      f = a.cfix[c0 + k];
+      flag = ((fl & B2G_CONTACT_TOUCHING) && (fl & B2G_CONTACT_ENABLED) && !a.fsensor[f.x] && !a.fsensor[f.y]) ? 1 : 0;
+    }
+    int total;
+    int p = block_scan<T>(flag, &total);
+    if (flag) {
+      int s = c0 + s_carry + p;
+      a.sc_list[s] = c0 + k;
+      int ia = a.fbody[f.x], ib = a.fbody[f.y];
+      a.scb[s] = make_int2(a.btype[ia] == B2G_STATIC ? -1 : ia - b0, a.btype[ib] == B2G_STATIC ? -1 : ib - b0);
+      uint64_t key = a.ckey[c0 + k];
+      a.cprio[s] = contactPriority((uint32_t)(key >> 32) - (uint32_t)fo, (uint32_t)key - (uint32_t)fo);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) s_carry += total;
+    __syncthreads();
+  }
+  const int nsc = s_carry;
+
+  // 2. colour the solver contacts (shared memory for whatever fits)
+  int ncc = 0;
+  if (nsc > 0) {
+    SmemCarver sc{smem, (size_t)smem_bytes};
+    ColourMem m;
+    m.mask = (unsigned long long*)sc.take(8 * (size_t)nb);
+    m.cnt = (int*)sc.take(4 * (size_t)nb);
+    m.head = (int*)sc.take(4 * (size_t)nb);
+    bool bodySm = m.mask && m.cnt && m.head;
+    if (!bodySm) {
+      m.mask = a.inc_mask + b0;
+      m.cnt = a.inc_cnt + b0;
+      m.head = a.inc_head + b0;
+    }
+    int* list = bodySm ? (int*)sc.take(8 * (size_t)nsc) : nullptr;
+    int2* cb = bodySm ? (int2*)sc.take(8 * (size_t)nsc) : nullptr;
+    int8_t* col = bodySm ? (int8_t*)sc.take((size_t)nsc) : nullptr;
+    uint8_t* rdy = bodySm ? (uint8_t*)sc.take((size_t)nsc) : nullptr;
+    bool conSm = list && cb && col && rdy;
+    if (conSm) {
+      for (int k = threadIdx.x; k < nsc; k += T) cb[k] = a.scb[c0 + k];
+      __syncthreads();
+      m.list = list; m.cb = cb; m.col = col; m.rdy = rdy;
+    } else {
+      m.list = a.inc_list + 2 * (int64_t)c0;
+      m.cb = a.scb + c0;
+      m.col = a.ccol + c0;
+      m.rdy = a.cready + c0;
+    }
+    ncc = colour_constraints<T>(nsc, nb, m, a.cprio + c0, a.corder + c0, cranges, a.status);
+    if (conSm) {
+      for (int k = threadIdx.x; k < nsc; k += T) a.ccol[c0 + k] = col[k];
+      __syncthreads();
+    }
+  }
+  // joints: colours fixed per layout
+  const int njc = nj > 0 ? a.ncolors[4 * w + 1] : 0;
+  for (int c = threadIdx.x; c <= njc; c += T) jranges[c] = a.jranges[65 * (int64_t)w + c];
+  if (threadIdx.x == 0) {
+    a.ncolors[4 * w] = ncc;
+    a.ncolors[4 * w + 2] = nsc;
+    a.ncolors[4 * w + 3] = c0;
+    atomicAdd(&a.counters[B2G_CNT_TOUCHING], (unsigned long long)nsc);
+  }
+
+  // 3. velocity integration (b2_island.cpp:256-293, SolveOrphan :187-206) into the body-state
+  //    buffer: shared memory when the world's bodies fit, else the global velocity array
+  const bool bsm = (size_t)nb * sizeof(float4) <= (size_t)smem_bytes;
+  float4* bs = bsm ? reinterpret_cast<float4*>(smem) : a.vel + b0;
+  for (int i = threadIdx.x; i < nb; i += T) {
+    int bi = b0 + i;
+    float4 v4 = a.vel[bi];
+    if (a.btype[bi] == B2G_DYNAMIC) {
+      float4 md = a.massd[bi];
+      float4 dmp = a.damp[bi];
+      float4 fr = a.force[bi];
+      V2 v = mk(v4.x, v4.y);
+      float wv = v4.z;
+      addTo(v, (h * md.y) * (dmp.z * md.x * gravity + mk(fr.x, fr.y)));
+      wv += h * md.w * fr.z;
+      v.x /= (1.0f + h * dmp.x);
+      v.y /= (1.0f + h * dmp.x);
+      wv /= (1.0f + h * dmp.y);
+      v4 = make_float4(v.x, v.y, wv, 0.0f);
+      bs[i] = v4;
+    } else if (bsm) {
+      bs[i] = v4;
+    }
+  }
+  __syncthreads();
+
+  // 4. prepare (b2ContactSolver::Initialize + InitializeVelocityConstraints) into colour order
+  for (int p = threadIdx.x; p < nsc; p += T) {
+    int k = a.corder[c0 + p];
+    int ci = a.sc_list[c0 + k];
+    int2 f = a.cfix[ci];
+    int ia = a.fbody[f.x], ib = a.fbody[f.y];
+    b2g_manifold m = a.cman[ci];
+    VCDev vc;
+    for (int q = 0; q < 4; ++q) vc.K[q] = vc.NM[q] = 0.0f;
+    prepareContact(vc, m, a.cmat[ci], a.shape[f.x].radius, a.shape[f.y].radius, ia - b0, ib - b0, a.massd[ia],
+                   a.massd[ib], a.lc[ia], a.lc[ib], a.pos[ia], bs[ia - b0], a.pos[ib], bs[ib - b0], dtRatio, warm, ci);
+    store_planes(P, c0 + p, vc);
+  }
+  __syncthreads();
+  float4* jb = bs - b0;  // joints address bodies by global index
+
+  // 5. warm start contacts, then joint InitVelocityConstraints, colour by colour
+  if (warm) {
+    for (int c = 0; c < ncc; ++c) {
+      int s = cranges[c], e = cranges[c + 1];
+      if (c == 63) {
+        if (threadIdx.x == 0)
+          for (int i = s; i < e; ++i) {
+            VCDev vc;
+            load_velocity(P, c0 + i, vc, false);
+            warmStartContact(vc, bs);
+          }
+      } else {
+        for (int i = s + threadIdx.x; i < e; i += T) {
+          VCDev vc;
+          load_velocity(P, c0 + i, vc, false);
+          warmStartContact(vc, bs);
+        }
+      }
+      __syncthreads();
+    }
+  }
+  for (int c = 0; c < njc; ++c) {
+    int s = jranges[c], e = jranges[c + 1];
+    if (c == 63) {
+      if (threadIdx.x == 0)
+        for (int i = s; i < e; ++i) jointInit(a.joints[j0 + a.jorder[j0 + i]], a.massd, a.lc, a.pos, jb, a.dt, dtRatio, warm);
+    } else {
+      for (int i = s + threadIdx.x; i < e; i += T)
+        jointInit(a.joints[j0 + a.jorder[j0 + i]], a.massd, a.lc, a.pos, jb, a.dt, dtRatio, warm);
+    }
+    __syncthreads();
+  }
+
+  // 6. velocity iterations: joints, then contacts (b2_island.cpp:327-346)
+  for (int it = 0; it < a.vi; ++it) {
+    for (int c = 0; c < njc; ++c) {
+      int s = jranges[c], e = jranges[c + 1];
+      if (c == 63) {
+        if (threadIdx.x == 0)
+          for (int i = s; i < e; ++i) jointSolveVelocity(a.joints[j0 + a.jorder[j0 + i]], jb, a.dt, a.inv_dt);
+      } else {
+        for (int i = s + threadIdx.x; i < e; i += T) jointSolveVelocity(a.joints[j0 + a.jorder[j0 + i]], jb, a.dt, a.inv_dt);
+      }
+      __syncthreads();
+    }
+    for (int c = 0; c < ncc; ++c) {
+      int s = cranges[c], e = cranges[c + 1];
+      if (c == 63) {
+        if (threadIdx.x == 0)
+          for (int i = s; i < e; ++i) {
+            VCDev vc;
+            load_velocity(P, c0 + i, vc, true);
+            solveContactVelocity(vc, bs);
+            P.imp[c0 + i] = make_float4(vc.normalImpulse[0], vc.normalImpulse[1], vc.tangentImpulse[0], vc.tangentImpulse[1]);
+          }
+      } else {
+        for (int i = s + threadIdx.x; i < e; i += T) {
+          VCDev vc;
+          load_velocity(P, c0 + i, vc, true);
+          solveContactVelocity(vc, bs);
+          P.imp[c0 + i] = make_float4(vc.normalImpulse[0], vc.normalImpulse[1], vc.tangentImpulse[0], vc.tangentImpulse[1]);
+        }
+      }
+      __syncthreads();
+    }
+  }
+
+  // 7. StoreImpulses (b2_contact_solver.cpp:641-657)
+  for (int p = threadIdx.x; p < nsc; p += T) {
+    int4 id = P.idx[c0 + p];
+    float4 im = P.imp[c0 + p];
+    b2g_manifold* m = &a.cman[id.w];
+    int pc = id.z & 15;
+    if (pc > 0) { m->points[0].normal_impulse = im.x; m->points[0].tangent_impulse = im.z; }
+    if (pc > 1) { m->points[1].normal_impulse = im.y; m->points[1].tangent_impulse = im.w; }
+  }
+
+  // 8. integrate positions (b2_island.cpp:349-385); the buffer switches to positions
+  for (int i = threadIdx.x; i < nb; i += T) {
+    int bi = b0 + i;
+    float4 p4 = a.pos[bi];
+    if (a.btype[bi] == B2G_STATIC) {
+      if (bsm) bs[i] = p4;
+      continue;
+    }
+    float4 v4 = bs[i];
+    V2 c = mk(p4.x, p4.y);
+    float an = p4.z;
+    V2 v = mk(v4.x, v4.y);
+    float wv = v4.z;
+    V2 translation = h * v;
+    if (dot(translation, translation) > B2G_MAX_TRANSLATION_SQ) {
+      float ratio = B2G_MAX_TRANSLATION / lengthOf(translation);
+      v.x *= ratio;
+      v.y *= ratio;
+    }
+    float rotation = h * wv;
+    if (rotation * rotation > B2G_MAX_ROTATION_SQ) {
+      float ratio = B2G_MAX_ROTATION / fabs2(rotation);
+      wv *= ratio;
+    }
+    addTo(c, h * v);
+    an += h * wv;
+    a.vel[bi] = make_float4(v.x, v.y, wv, 0.0f);
+    if (bsm) bs[i] = make_float4(c.x, c.y, an, 0.0f);
+    else a.pos[bi] = make_float4(c.x, c.y, an, 0.0f);
+  }
+  __syncthreads();
+  float4* ps = bsm ? bs : a.pos + b0;
+  float4* jp = ps - b0;
+
+  // 9. position iterations: contacts then joints, early exit for the world (b2_island.cpp:387-428)
+  for (int it = 0; it < a.pi; ++it) {
+    int okay = 1;
+    for (int c = 0; c < ncc; ++c) {
+      int s = cranges[c], e = cranges[c + 1];
+      if (c == 63) {
+        if (threadIdx.x == 0)
+          for (int i = s; i < e; ++i) {
+            VCDev vc;
+            load_position(P, c0 + i, vc);
+            if (!(solveContactPosition(vc, ps) >= -3.0f * B2G_LINEAR_SLOP)) okay = 0;
+          }
+      } else {
+        for (int i = s + threadIdx.x; i < e; i += T) {
+          VCDev vc;
+          load_position(P, c0 + i, vc);
+          if (!(solveContactPosition(vc, ps) >= -3.0f * B2G_LINEAR_SLOP)) okay = 0;
+        }
+      }
+      __syncthreads();
+    }
+    for (int c = 0; c < njc; ++c) {
+      int s = jranges[c], e = jranges[c + 1];
+      if (c == 63) {
+        if (threadIdx.x == 0)
+          for (int i = s; i < e; ++i)
+            if (!jointSolvePosition(a.joints[j0 + a.jorder[j0 + i]], jp)) okay = 0;
+      } else {
+        for (int i = s + threadIdx.x; i < e; i += T)
+          if (!jointSolvePosition(a.joints[j0 + a.jorder[j0 + i]], jp)) okay = 0;
+      }
+      __syncthreads();
+    }
+    if (__syncthreads_and(okay)) break;
+  }
+
+  // 10. transforms (b2Body::SynchronizeTransform, include/box2d/b2_body.h:957-961), finite check
+  int bad = 0;
+  for (int i = threadIdx.x; i < nb; i += T) {
+    int bi = b0 + i;
+    if (a.btype[bi] == B2G_STATIC) continue;
+    float4 p4 = ps[i];
+    if (bsm) a.pos[bi] = p4;
+    Rot q = rotOf(p4.z);
+    float2 l = a.lc[bi];
+    V2 p = mk(p4.x, p4.y) - mul(q, mk(l.x, l.y));
+    a.xf[bi] = make_float4(p.x, p.y, q.s, q.c);
+    float4 v4 = a.vel[bi];
+    if (!isfinite(p4.x) || !isfinite(p4.y) || !isfinite(p4.z) || !isfinite(v4.x) || !isfinite(v4.y) || !isfinite(v4.z))
+      bad = 1;
+  }
+  if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(a.status, B2G_DEV_NONFINITE);
+  if (a.events_on) {
+    for (int p = threadIdx.x; p < nsc; p += T) {
+      int4 id = P.idx[c0 + p];
+      float4 im = P.imp[c0 + p];
+      int2 f = a.cfix[id.w];
+      float ni[2] = {im.x, im.y}, ti[2] = {im.z, im.w};
+      record_event(a, B2G_EVENT_POSTSOLVE, w, f.x - fo, f.y - fo, id.z & 15, ni, ti, 0);
+    }
+  }
+  if (threadIdx.x == 0 && a.dt > 0.0f) a.wg[w].z = a.inv_dt;
+}
+
+// Joint colouring of worlds [w0, w0 + gridDim.x), once per layout: joints and the static flags
+// of their bodies change only through structural edits, which re-upload the layout.
+template <int T>
+__global__ void __launch_bounds__(T) k_joint_colour(KernelArgs a, int w0) {
+  __shared__ int jr[65];
+  const int w = w0 + blockIdx.x;
+  const int4 wb = a.wb[w];
+  const int b0 = wb.x, nb = wb.y;
+  const int4 wj = a.wj[w];
+  const int j0 = wj.x, nj = wj.y;
+  if (nj == 0) {
+    if (threadIdx.x == 0) a.ncolors[4 * w + 1] = 0;
+    return;
+  }
+  for (int k = threadIdx.x; k < nj; k += T) {
+    const JointDev& J = a.joints[j0 + k];
+    int ia = J.d.body_a, ib = J.d.body_b;
+    a.jcb[j0 + k] = make_int2(a.btype[ia] == B2G_STATIC ? -1 : ia - b0, a.btype[ib] == B2G_STATIC ? -1 : ib - b0);
+    a.jprio[j0 + k] = jointPriority((uint32_t)k);
+  }
+  __syncthreads();
+  ColourMem m;
+  m.cnt = a.inc_cnt + b0;
+  m.head = a.inc_head + b0;
+  m.mask = a.inc_mask + b0;
+  m.list = a.jinc_list + 2 * (int64_t)j0;
+  m.cb = a.jcb + j0;
+  m.col = a.jcol + j0;
+  m.rdy = a.jready + j0;
+  int njc = colour_constraints<T>(nj, nb, m, a.jprio + j0, a.jorder + j0, jr, a.status);
+  for (int c = threadIdx.x; c <= njc; c += T) a.jranges[65 * (int64_t)w + c] = jr[c];
+  if (threadIdx.x == 0) a.ncolors[4 * w + 1] = njc;
+}
+
+// ---- launch planning
+// Class by world body count: threads per CTA and the dynamic shared memory that holds the
+// world's body state (16 B/body) and, room permitting, its colouring arrays (about 52 B/body
+// at two contacts per body).
+static const int kClassMaxBodies[B2G_SOLVE_CLASSES] = {64, 256, 1024, 4096, 1 << 30};
+static const int kClassThreads[B2G_SOLVE_CLASSES] = {64, 128, 256, 512, 1024};
+static const int kClassSmemCap[B2G_SOLVE_CLASSES] = {16 << 10, 24 << 10, 56 << 10, 110 << 10, 200 << 10};
+
+std::vector<SolveClass> plan_solve_classes(const std::vector<int>& order, const std::vector<int>& bodies) {
+  // `order` lists worlds by body count, largest first: each class is a contiguous range
+  std::vector<SolveClass> out;
+  int n = (int)order.size();
+  int i = 0;
+  for (int c = B2G_SOLVE_CLASSES - 1; c >= 0 && i < n; --c) {
+    int lo = c > 0 ? kClassMaxBodies[c - 1] : -1;
+    int start = i;
+    int nbmax = 0;
+    while (i < n && bodies[order[i]] > lo) {
+      nbmax = nbmax > bodies[order[i]] ? nbmax : bodies[order[i]];
+      ++i;
+    }
+    if (i == start) continue;
+    int64_t need = 52ll * nbmax;
+    need = (need + 15) & ~15ll;
+    int smem = (int)(need < kClassSmemCap[c] ? need : kClassSmemCap[c]);
+    out.push_back({start, i - start, kClassThreads[c], smem});
+  }
+  return out;
+}
+
+template <int T>
+static void set_smem_attr(int c) {
+  cudaFuncSetAttribute(k_solve<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, kClassSmemCap[c]);
+}
+
+void solver_setup() {
+  set_smem_attr<64>(0);
+  set_smem_attr<128>(1);
+  set_smem_attr<256>(2);
+  set_smem_attr<512>(3);
+  set_smem_attr<1024>(4);
+}
+
+static void launch_class(const KernelArgs& a, const SolveClass& c, cudaStream_t s) {
+  switch (c.threads) {
+    case 64: k_solve<64><<<c.count, 64, c.smem, s>>>(a, c.first, c.smem); break;
+    case 128: k_solve<128><<<c.count, 128, c.smem, s>>>(a, c.first, c.smem); break;
+    case 256: k_solve<256><<<c.count, 256, c.smem, s>>>(a, c.first, c.smem); break;
+    case 512: k_solve<512><<<c.count, 512, c.smem, s>>>(a, c.first, c.smem); break;
+    default: k_solve<1024><<<c.count, 1024, c.smem, s>>>(a, c.first, c.smem); break;
+  }
+}
+
+void launch_solve(const KernelArgs& a, const std::vector<SolveClass>& classes, cudaStream_t s, const cudaStream_t* side,
+                  const cudaEvent_t* ev) {
+  if (classes.empty()) return;
+  if (classes.size() == 1) {
+    launch_class(a, classes[0], s);
+    return;
+  }
+  cudaEventRecord(ev[0], s);
+  for (size_t i = 1; i < classes.size(); ++i) {
+    cudaStreamWaitEvent(side[i - 1], ev[0], 0);
+    launch_class(a, classes[i], side[i - 1]);
+    cudaEventRecord(ev[i], side[i - 1]);
+  }
+  launch_class(a, classes[0], s);
+  for (size_t i = 1; i < classes.size(); ++i) cudaStreamWaitEvent(s, ev[i], 0);
+}
+
+void launch_joint_colour(const KernelArgs& a, int w0, int nw, cudaStream_t s) {
+  if (nw > 0) k_joint_colour<256><<<nw, 256, 0, s>>>(a, w0);
+}
+
+}  // namespace b2g

@@ -44,6 +44,7 @@ B2G_HD void prepareContact(VCDev& vc, const b2g_manifold& m, float4 mat, float r
   vc.radiusA = radiusA;
   vc.radiusB = radiusB;
   vc.type = m.type;
+#pragma unroll
   for (int j = 0; j < 2; ++j) {
     vc.normalImpulse[j] = 0.0f; vc.tangentImpulse[j] = 0.0f;
     vc.normalMass[j] = 0.0f; vc.tangentMass[j] = 0.0f; vc.velocityBias[j] = 0.0f;
@@ -51,7 +52,9 @@ B2G_HD void prepareContact(VCDev& vc, const b2g_manifold& m, float4 mat, float r
     vc.localPoints[j][0] = m.points[j].local_point[0];
     vc.localPoints[j][1] = m.points[j].local_point[1];
   }
-  for (int j = 0; j < m.point_count; ++j) {
+#pragma unroll
+  for (int j = 0; j < 2; ++j) {
+    if (j >= m.point_count) break;
     if (warm) {
       vc.normalImpulse[j] = dtRatio * m.points[j].normal_impulse;
       vc.tangentImpulse[j] = dtRatio * m.points[j].tangent_impulse;
@@ -74,7 +77,9 @@ B2G_HD void prepareContact(VCDev& vc, const b2g_manifold& m, float4 mat, float r
   V2 normal = wm.normal;
   st2(vc.normal, normal);
   V2 tangent = cross(normal, 1.0f);
-  for (int j = 0; j < vc.pointCount; ++j) {
+#pragma unroll
+  for (int j = 0; j < 2; ++j) {
+    if (j >= vc.pointCount) break;
     V2 rA = wm.points[j] - cA;
     V2 rB = wm.points[j] - cB;
     st2(vc.rA[j], rA);
@@ -139,7 +144,9 @@ B2G_HD void warmStartContact(const VCDev& vc, float4* vel) {
   loadVel(vel, vc.indexB, vB, wB);
   V2 normal = ld2(vc.normal);
   V2 tangent = cross(normal, 1.0f);
-  for (int j = 0; j < vc.pointCount; ++j) {
+#pragma unroll
+  for (int j = 0; j < 2; ++j) {
+    if (j >= vc.pointCount) break;
     V2 P = vc.normalImpulse[j] * normal + vc.tangentImpulse[j] * tangent;
     wA -= iA * cross(ld2(vc.rA[j]), P);
     subFrom(vA, mA * P);
@@ -160,7 +167,9 @@ B2G_HD void solveContactVelocity(VCDev& vc, float4* vel) {
   loadVel(vel, vc.indexB, vB, wB);
   V2 normal = ld2(vc.normal);
   V2 tangent = cross(normal, 1.0f);
-  for (int j = 0; j < pointCount; ++j) {
+#pragma unroll
+  for (int j = 0; j < 2; ++j) {
+    if (j >= pointCount) break;
     V2 rA = ld2(vc.rA[j]), rB = ld2(vc.rB[j]);
     V2 dv = (vB + cross(wB, rB)) - (vA + cross(wA, rA));
     float vt = dot(dv, tangent) - vc.tangentSpeed;
@@ -257,7 +266,9 @@ B2G_HD float solveContactPosition(const VCDev& vc, float4* pos) {
   V2 cA, cB; float aA, aB;
   loadPos(pos, vc.indexA, cA, aA);
   loadPos(pos, vc.indexB, cB, aB);
-  for (int j = 0; j < vc.pcPointCount; ++j) {
+#pragma unroll
+  for (int j = 0; j < 2; ++j) {
+    if (j >= vc.pcPointCount) break;
     Xf xfA, xfB;
     xfA.q = rotOf(aA);
     xfB.q = rotOf(aB);

@@ -95,6 +95,45 @@ def test_batch_world_rollout_bit_exact(lib, orc, seed):
     _rollout(lib, orc, G.SCENE_BATCH_WORLD, n, seed=seed, steps=80)
 
 
+@pytest.mark.parametrize("rows", [90, 161])
+def test_large_pyramid_rollout_bit_exact(lib, orc, rows):
+    # 90 rows (4096 bodies): body state and per-body colouring state in shared memory, the
+    # per-contact colouring arrays in global memory; 161 rows (13042 bodies): too large for the
+    # CTA's shared memory, every solver array in global memory
+    _rollout(lib, orc, G.SCENE_PYRAMID, rows, steps=4)
+
+
+@pytest.mark.parametrize("kind,n,p0", [(G.SCENE_PYRAMID, 20, 1.0), (G.SCENE_CHAINS, 12, 200.0)])
+def test_solver_order_matches_oracle(lib, orc, kind, n, p0):
+    """The colour and priority of every solved contact and joint equal the oracle's greedy
+    colouring (the Gauss-Seidel order up to the order inside a colour, which does not matter:
+    constraints of one colour share no non-static body)."""
+    batch = G.Batch(lib, device=0)
+    w = batch.add_world(0.0, -10.0)
+    batch.set_flags(w, allow_sleep=False, warm_starting=True, continuous=False)
+    batch.scene(w, kind, seed=2, n=n, p0=p0, p1=0.6)
+    ow = ob.OracleWorld(orc, (0.0, -10.0), batch.bodies(w), batch.fixtures(w), batch.joints(w))
+    for _ in range(40):
+        batch.step(1 / 60, 8, 3)
+        ow.step(1, 1 / 60, 8, 3)
+    before = [(c.fixture_a, c.fixture_b) for c in ow.contacts()]
+    batch.step(1 / 60, 8, 3)
+    ow.step(1, 1 / 60, 8, 3)
+    after = [(c.fixture_a, c.fixture_b) for c in ow.contacts()]
+    nb, nf, nj, nc = batch.sizes(w)
+    gc, gp, gj, gjp = batch.solver_order(w, nc, nj)
+    oc, op, oj, ojp = ow.solver_order()
+    assert gj == oj and gjp == ojp
+    if kind == G.SCENE_PYRAMID:
+        # a settled pyramid keeps its contact list, so the oracle's per-contact record (indexed by
+        # the list the solve read) lines up with the current list
+        assert before == after and len(after) == nc
+    if before == after:
+        assert gc == oc and gp == op
+        assert max(gc) >= 2
+    batch.close()
+
+
 def test_batched_equals_alone(lib):
     """Worlds stepped together in one batch are bit-identical to the same worlds stepped alone."""
     seeds = [21, 22, 23, 24, 25, 26]
