@@ -114,7 +114,7 @@ static KernelArgs make_args(Batch* b) {
   a.xf = b->xf.p; a.pos = b->pos.p; a.vel = b->vel.p; a.massd = b->massd.p; a.damp = b->damp.p;
   a.force = b->force.p; a.lc = b->lc.p; a.btype = b->btype.p; a.bworld = b->bworld.p;
   a.shape = b->shape.p; a.fbody = b->fbody.p; a.fgroup = b->fgroup.p; a.fsensor = b->fsensor.p;
-  a.fworld = b->fworld.p; a.ffilter = b->ffilter.p; a.fmat = b->fmat.p; a.aabb = b->aabb.p;
+  a.fworld = b->fworld.p; a.frad = b->frad.p; a.ffilter = b->ffilter.p; a.fmat = b->fmat.p; a.aabb = b->aabb.p;
   a.joints = b->joints.p; a.nocollide = b->nocollide.p; a.n_nocollide = b->n_nocollide;
   int c = b->cur;
   a.ckey = b->ckey[c].p; a.cfix = b->cfix[c].p; a.cflags = b->cflags[c].p; a.cmat = b->cmat[c].p;
@@ -125,10 +125,10 @@ static KernelArgs make_args(Batch* b) {
   }
   a.wbounds = b->wbounds.p; a.mkey = b->mkey.p; a.mkey_sorted = b->mkey_sorted.p; a.mval = b->mval.p;
   a.mval_sorted = b->mval_sorted.p; a.nchild = b->nchild.p; a.nparent = b->nparent.p; a.lparent = b->lparent.p;
-  a.naabb = b->naabb.p; a.nflag = b->nflag.p; a.wroot = b->wroot.p; a.pcount = b->pcount.p; a.poff = b->poff.p;
+  a.naabb = b->naabb.p; a.nflag = b->nflag.p; a.wroot = b->wroot.p; a.pcount = b->pcount.p; a.pslots = b->pslots.p; a.poff = b->poff.p;
   a.pairs = b->pairs.p; a.cub_tmp = b->cub_tmp.p;
-  a.sc_list = b->sc_list.p; a.scb = b->scb.p; a.ccol = b->ccol.p; a.corder = b->corder.p; a.cprio = b->cprio.p;
-  a.sp.nf = b->sp_nf.p; a.sp.mass = b->sp_mass.p; a.sp.r0 = b->sp_r0.p; a.sp.r1 = b->sp_r1.p;
+  a.sc_list = b->sc_list.p; a.scb = b->scb.p; a.cslot = b->cslot.p; a.ccol = b->ccol.p; a.corder = b->corder.p; a.cprio = b->cprio.p;
+  a.sp.nf = b->sp_nf.p; a.sp.cid = b->sp_cid.p; a.sp.r0 = b->sp_r0.p; a.sp.r1 = b->sp_r1.p;
   a.sp.nmtm = b->sp_nmtm.p; a.sp.bk = b->sp_bk.p; a.sp.kn = b->sp_kn.p; a.sp.imp = b->sp_imp.p;
   a.sp.idx = b->sp_idx.p; a.sp.lcs = b->sp_lcs.p; a.sp.lnp = b->sp_lnp.p; a.sp.lps = b->sp_lps.p;
   a.sp.rad = b->sp_rad.p;
@@ -151,6 +151,9 @@ static uint64_t emitter_key(const HostWorld& w, int fo, int fa, int fb) {
   else { e = std::min(fa, fb); p = std::max(fa, fb); }
   return ((uint64_t)(uint32_t)(e + fo) << 32) | (uint32_t)(p + fo);
 }
+
+// Solver constraints address bodies by a 24-bit world-local index.
+static const size_t kMaxWorldBodies = size_t(1) << 24;
 
 // Reads the status word after the upload's joint colouring (the upload synchronises anyway).
 static int check_upload_status(Batch* b) {
@@ -177,6 +180,10 @@ int upload_all(Batch* b) {
   int64_t NC = 0;
   for (int w = 0; w < NW; ++w) {
     const HostWorld& hw = b->worlds[w];
+    if (hw.bodies.size() >= kMaxWorldBodies) {
+      set_error(b, "a world has more bodies than the solver's 24-bit body index allows");
+      return B2G_E_CAPACITY;
+    }
     b->h_body_off[w] = NB; b->h_fix_off[w] = NF; b->h_joint_off[w] = NJ;
     wb[w] = make_int4(NB, (int)hw.bodies.size(), NF, (int)hw.fixtures.size());
     wj[w] = make_int4(NJ, (int)hw.joints.size(), 0, 0);
@@ -193,6 +200,7 @@ int upload_all(Batch* b) {
   std::vector<int> btype(NB), bworld(NB);
   std::vector<b2g_shape> shape(NF);
   std::vector<int> fbody(NF), fgroup(NF), fsensor(NF), fworld(NF);
+  std::vector<float> frad(NF);
   std::vector<uint32_t> ffilter(NF);
   std::vector<float4> fmat(NF);
   std::vector<JointDev> joints(NJ);
@@ -221,6 +229,7 @@ int upload_all(Batch* b) {
       const b2g_fixture& f = hw.fixtures[i];
       size_t k = fo + i;
       shape[k] = f.shape;
+      frad[k] = f.shape.radius;
       fbody[k] = bo + f.body;
       fgroup[k] = f.group_index;
       fsensor[k] = f.is_sensor ? 1 : 0;
@@ -304,6 +313,7 @@ int upload_all(Batch* b) {
   TRY(upload(b, b->btype, btype)); TRY(upload(b, b->bworld, bworld));
   TRY(upload(b, b->shape, shape)); TRY(upload(b, b->fbody, fbody)); TRY(upload(b, b->fgroup, fgroup));
   TRY(upload(b, b->fsensor, fsensor)); TRY(upload(b, b->fworld, fworld)); TRY(upload(b, b->ffilter, ffilter));
+  TRY(upload(b, b->frad, frad));
   TRY(upload(b, b->fmat, fmat)); TRY(ensure(b, b->aabb, NF));
   TRY(upload(b, b->joints, joints)); TRY(upload(b, b->nocollide, nocol));
   b->n_nocollide = (int)nocol.size();
@@ -314,13 +324,13 @@ int upload_all(Batch* b) {
   TRY(ensure(b, b->mkey, NF)); TRY(ensure(b, b->mkey_sorted, NF)); TRY(ensure(b, b->mval, NF));
   TRY(ensure(b, b->mval_sorted, NF)); TRY(ensure(b, b->nchild, NF)); TRY(ensure(b, b->nparent, NF));
   TRY(ensure(b, b->lparent, NF)); TRY(ensure(b, b->naabb, NF)); TRY(ensure(b, b->nflag, NF));
-  TRY(ensure(b, b->pcount, (size_t)NF + 1));
+  TRY(ensure(b, b->pcount, (size_t)NF + 1)); TRY(ensure(b, b->pslots, 8 * (size_t)NF));
   TRY(ensure(b, b->poff, (size_t)NF + 1));
   TRY(ensure(b, b->cub_tmp, cub_temp_bytes(NF)));
   TRY(ensure(b, b->inc_cnt, NB)); TRY(ensure(b, b->inc_head, NB)); TRY(ensure(b, b->inc_mask, NB));
   TRY(ensure(b, b->jinc_list, 2 * (size_t)NJ)); TRY(ensure(b, b->jcol, NJ)); TRY(ensure(b, b->jorder, NJ));
   TRY(ensure(b, b->jcb, NJ)); TRY(ensure(b, b->jprio, NJ)); TRY(ensure(b, b->jready, NJ));
-  TRY(ensure(b, b->status, 1)); TRY(ensure(b, b->counters, 4));
+  TRY(ensure(b, b->status, 1)); TRY(ensure(b, b->counters, 5));
   b->NW = NW; b->NB = NB; b->NF = NF; b->NJ = NJ; b->NC = NC;
   {
     unsigned long long cnt[4] = {(unsigned long long)NC, 0, 0, 0};
@@ -359,6 +369,7 @@ int upload_tail(Batch* b) {
   std::vector<float4> xf, pos, vel, massd, damp, force;
   std::vector<float2> lc;
   std::vector<int> btype, bworld, fbody, fgroup, fsensor, fworld;
+  std::vector<float> frad;
   std::vector<b2g_shape> shape;
   std::vector<uint32_t> ffilter;
   std::vector<float4> fmat, wg_tail;
@@ -370,6 +381,10 @@ int upload_tail(Batch* b) {
   int NB = NB0, NF = NF0, NJ = NJ0;
   for (int w = w0; w < NW; ++w) {
     const HostWorld& hw = b->worlds[w];
+    if (hw.bodies.size() >= kMaxWorldBodies) {
+      set_error(b, "a world has more bodies than the solver's 24-bit body index allows");
+      return B2G_E_CAPACITY;
+    }
     int bo = NB, fo = NF, jo = NJ;
     b->h_body_off[w] = bo; b->h_fix_off[w] = fo; b->h_joint_off[w] = jo;
     wg_tail.push_back(make_float4(hw.gx, hw.gy, hw.inv_dt0, 0.0f));
@@ -386,6 +401,7 @@ int upload_tail(Batch* b) {
     }
     for (const b2g_fixture& f : hw.fixtures) {
       shape.push_back(f.shape);
+      frad.push_back(f.shape.radius);
       fbody.push_back(bo + f.body);
       fgroup.push_back(f.group_index);
       fsensor.push_back(f.is_sensor ? 1 : 0);
@@ -450,6 +466,7 @@ int upload_tail(Batch* b) {
   TRY(upload_at(b, b->lc, NB0, lc)); TRY(upload_at(b, b->btype, NB0, btype)); TRY(upload_at(b, b->bworld, NB0, bworld));
   TRY(upload_at(b, b->shape, NF0, shape)); TRY(upload_at(b, b->fbody, NF0, fbody)); TRY(upload_at(b, b->fgroup, NF0, fgroup));
   TRY(upload_at(b, b->fsensor, NF0, fsensor)); TRY(upload_at(b, b->fworld, NF0, fworld));
+  TRY(upload_at(b, b->frad, NF0, frad));
   TRY(upload_at(b, b->ffilter, NF0, ffilter)); TRY(upload_at(b, b->fmat, NF0, fmat));
   TRY(upload_at(b, b->joints, NJ0, joints)); TRY(upload_at(b, b->nocollide, b->n_nocollide, nocol));
   b->n_nocollide += (int)nocol.size();
@@ -457,6 +474,7 @@ int upload_tail(Batch* b) {
   TRY(ensure(b, b->mval, NF)); TRY(ensure(b, b->mval_sorted, NF)); TRY(ensure(b, b->nchild, NF));
   TRY(ensure(b, b->nparent, NF)); TRY(ensure(b, b->lparent, NF)); TRY(ensure(b, b->naabb, NF));
   TRY(ensure(b, b->nflag, NF)); TRY(ensure(b, b->pcount, (size_t)NF + 1)); TRY(ensure(b, b->poff, (size_t)NF + 1));
+  TRY(ensure(b, b->pslots, 8 * (size_t)NF));
   TRY(ensure(b, b->cub_tmp, cub_temp_bytes(NF)));
   TRY(ensure(b, b->inc_cnt, NB)); TRY(ensure(b, b->inc_head, NB)); TRY(ensure(b, b->inc_mask, NB));
   TRY(ensure(b, b->jinc_list, 2 * (size_t)NJ)); TRY(ensure(b, b->jcol, NJ, true)); TRY(ensure(b, b->jorder, NJ, true));
@@ -567,10 +585,10 @@ static int ensure_contact_capacity(Batch* b, int64_t want) {
     TRY(ensure(b, b->cman[k], (size_t)cap, keep));
   }
   TRY(ensure(b, b->pairs, (size_t)cap));
-  TRY(ensure(b, b->sc_list, (size_t)cap)); TRY(ensure(b, b->scb, (size_t)cap)); TRY(ensure(b, b->ccol, (size_t)cap));
+  TRY(ensure(b, b->sc_list, (size_t)cap)); TRY(ensure(b, b->scb, (size_t)cap)); TRY(ensure(b, b->cslot, (size_t)cap)); TRY(ensure(b, b->ccol, (size_t)cap));
   TRY(ensure(b, b->corder, (size_t)cap)); TRY(ensure(b, b->cprio, (size_t)cap)); TRY(ensure(b, b->cready, (size_t)cap));
   TRY(ensure(b, b->inc_list, 2 * (size_t)cap));
-  TRY(ensure(b, b->sp_nf, (size_t)cap)); TRY(ensure(b, b->sp_mass, (size_t)cap)); TRY(ensure(b, b->sp_r0, (size_t)cap));
+  TRY(ensure(b, b->sp_nf, (size_t)cap)); TRY(ensure(b, b->sp_cid, (size_t)cap)); TRY(ensure(b, b->sp_r0, (size_t)cap));
   TRY(ensure(b, b->sp_r1, (size_t)cap)); TRY(ensure(b, b->sp_nmtm, (size_t)cap)); TRY(ensure(b, b->sp_bk, (size_t)cap));
   TRY(ensure(b, b->sp_kn, (size_t)cap)); TRY(ensure(b, b->sp_imp, (size_t)cap)); TRY(ensure(b, b->sp_idx, (size_t)cap));
   TRY(ensure(b, b->sp_lcs, (size_t)cap)); TRY(ensure(b, b->sp_lnp, (size_t)cap)); TRY(ensure(b, b->sp_lps, (size_t)cap));
@@ -676,14 +694,15 @@ static int drain_device_events(Batch* b, unsigned long long n) {
 // overflow: the overflowing broadphase skipped its emission, so the live list is still the
 // pre-broadphase one (with this step's manifolds); grow the buffers and redo the broadphase.
 static int finish_step(Batch* b, int live_before_last_bp) {
-  b->h_readback[4] = 0;
-  CUDA_TRY(b, cudaMemcpyAsync(b->h_readback, b->counters.p, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+  b->h_readback[5] = 0;
+  CUDA_TRY(b, cudaMemcpyAsync(b->h_readback, b->counters.p, 5 * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
                               b->stream));
-  CUDA_TRY(b, cudaMemcpyAsync(b->h_readback + 4, b->status.p, sizeof(unsigned int), cudaMemcpyDeviceToHost, b->stream));
+  CUDA_TRY(b, cudaMemcpyAsync(b->h_readback + 5, b->status.p, sizeof(unsigned int), cudaMemcpyDeviceToHost, b->stream));
   CUDA_TRY(b, cudaStreamSynchronize(b->stream));
   unsigned long long* r = b->h_readback;
   unsigned long long overflow = r[B2G_CNT_OVERFLOW];
-  unsigned int status_word = (unsigned int)(r[4] & 0xffffffffull);
+  unsigned int status_word = (unsigned int)(r[5] & 0xffffffffull);
+  b->profile.colors_max = (int64_t)r[B2G_CNT_MAXCOLORS];
   int guard = 0;
   while (overflow) {
     if (++guard > 8) {
@@ -773,7 +792,7 @@ int step_batch(Batch* b, float dt, int vi, int pi, const uint8_t* mask, bool syn
   }
   TRY(ensure_contact_capacity(b, b->NC));
   CUDA_TRY(b, cudaMemsetAsync(b->status.p, 0, sizeof(unsigned int), b->stream));
-  CUDA_TRY(b, cudaMemsetAsync(b->counters.p + 1, 0, 3 * sizeof(unsigned long long), b->stream));
+  CUDA_TRY(b, cudaMemsetAsync(b->counters.p + 1, 0, 4 * sizeof(unsigned long long), b->stream));
   if (b->events_on) b->host_events.clear();
   b->last_dt = dt;
   b->last_vi = vi;
@@ -790,7 +809,7 @@ int step_batch(Batch* b, float dt, int vi, int pi, const uint8_t* mask, bool syn
     enqueue_broadphase(b, a, b->cur);
     b->cur ^= 1;
     TRY(finish_step(b, b->cur ^ 1));
-    CUDA_TRY(b, cudaMemsetAsync(b->counters.p + 1, 0, 3 * sizeof(unsigned long long), b->stream));
+    CUDA_TRY(b, cudaMemsetAsync(b->counters.p + 1, 0, 4 * sizeof(unsigned long long), b->stream));
     entry = b->cur;
   }
   if (graph) {
@@ -917,11 +936,11 @@ B2G_API int b2g_batch_destroy(b2g_batch* b) {
   }
   release(b, b->wbounds); release(b, b->mkey); release(b, b->mkey_sorted); release(b, b->mval);
   release(b, b->mval_sorted); release(b, b->nchild); release(b, b->nparent); release(b, b->lparent);
-  release(b, b->naabb); release(b, b->nflag); release(b, b->wroot); release(b, b->pcount); release(b, b->poff); release(b, b->pairs);
-  release(b, b->cub_tmp); release(b, b->status); release(b, b->counters); release(b, b->sc_list); release(b, b->scb);
+  release(b, b->naabb); release(b, b->nflag); release(b, b->wroot); release(b, b->pcount); release(b, b->pslots); release(b, b->poff); release(b, b->pairs);
+  release(b, b->cub_tmp); release(b, b->status); release(b, b->counters); release(b, b->sc_list); release(b, b->scb); release(b, b->cslot); release(b, b->frad);
   release(b, b->ccol); release(b, b->corder); release(b, b->cprio); release(b, b->cready); release(b, b->inc_cnt);
   release(b, b->inc_head); release(b, b->inc_mask); release(b, b->inc_list);
-  release(b, b->sp_nf); release(b, b->sp_mass); release(b, b->sp_r0); release(b, b->sp_r1); release(b, b->sp_nmtm);
+  release(b, b->sp_nf); release(b, b->sp_cid); release(b, b->sp_r0); release(b, b->sp_r1); release(b, b->sp_nmtm);
   release(b, b->sp_bk); release(b, b->sp_kn); release(b, b->sp_imp); release(b, b->sp_idx); release(b, b->sp_lcs);
   release(b, b->sp_lnp); release(b, b->sp_lps); release(b, b->sp_rad);
   release(b, b->jinc_list); release(b, b->jcol); release(b, b->jorder); release(b, b->jcb); release(b, b->jranges);

@@ -141,6 +141,7 @@ struct Batch {
 
   DBuf<b2g_shape> shape;
   DBuf<int> fbody, fgroup, fsensor, fworld;
+  DBuf<float> frad;
   DBuf<uint32_t> ffilter;
   DBuf<float4> fmat, aabb;
 
@@ -167,6 +168,7 @@ struct Batch {
   DBuf<int> nflag;
   DBuf<int> wroot;                // per world: root node (leaf encoded), -1 if empty
   DBuf<int> pcount;               // per fixture pair count
+  DBuf<uint32_t> pslots;          // per fixture: first partners found by the counting pass
   DBuf<int> poff;                 // exclusive scan of pcount (NF + 1 entries)
   DBuf<uint64_t> pairs;
   DBuf<uint8_t> cub_tmp;
@@ -175,9 +177,11 @@ struct Batch {
 
   // solver scratch
   DBuf<int> sc_list;              // per world: compacted solver contact indices (global)
-  DBuf<int2> scb;                 // per solver contact: world-local non-static bodies
-  DBuf<float4> sp_nf, sp_mass, sp_r0, sp_r1, sp_nmtm, sp_bk, sp_kn, sp_imp, sp_lcs, sp_lnp, sp_lps;
-  DBuf<int4> sp_idx;
+  DBuf<int2> scb;                 // per solver contact: world-local bodies, bit 31 set = static
+  DBuf<int> cslot;                // per solver contact: colour-ordered slot
+  DBuf<float4> sp_nf, sp_r0, sp_r1, sp_nmtm, sp_bk, sp_kn, sp_imp, sp_lcs, sp_lnp, sp_lps;
+  DBuf<int2> sp_idx;
+  DBuf<int> sp_cid;
   DBuf<float2> sp_rad;
   DBuf<int8_t> ccol;
   DBuf<int> corder;

@@ -9,6 +9,7 @@
 //                  sorted diff of that list against the live contacts (b2BroadPhase::UpdateAndQuery +
 //                  b2ContactManager::QueryCallback / RemoveDeadContacts).
 #include <cub/cub.cuh>
+#include <cuda/atomic>
 
 #include "b2g_math.cuh"
 #include "engine.h"
@@ -219,10 +220,14 @@ __global__ void k_lbvh_init(KernelArgs a, int n, int nw) {
   }
 }
 
-// Bottom-up node bounds: the second thread to reach a node combines its children.
+// Bottom-up node bounds: the second thread to reach a node combines its children. Walks stop at
+// their world's root (the traversal never reads nodes above it). The arrival counter is an
+// acquire-release atomic: the first thread's child bounds are visible to the second.
 __global__ void k_lbvh_bounds(KernelArgs a, int n) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
+  const int root = a.wroot[a.fworld[a.mval_sorted[i]]];
+  if (root < 0 || (root & LEAF_BIT)) return;  // single-fixture world: the leaf is the root
   int p = a.lparent[i];
   int guard = 0;
   while (p >= 0) {
@@ -230,14 +235,14 @@ __global__ void k_lbvh_bounds(KernelArgs a, int n) {
       raise_status(a.status, B2G_DEV_STACK_OVERFLOW);
       return;
     }
-    __threadfence();
-    if (atomicAdd(&a.nflag[p], 1) == 0) return;
-    __threadfence();
+    cuda::atomic_ref<int, cuda::thread_scope_device> arrivals(a.nflag[p]);
+    if (arrivals.fetch_add(1, cuda::memory_order_acq_rel) == 0) return;
     int2 ch = a.nchild[p];
     float4 l = (ch.x & LEAF_BIT) ? a.aabb[a.mval_sorted[ch.x & ~LEAF_BIT]] : __ldcg(&a.naabb[ch.x]);
     float4 r = (ch.y & LEAF_BIT) ? a.aabb[a.mval_sorted[ch.y & ~LEAF_BIT]] : __ldcg(&a.naabb[ch.y]);
     float4 u = make_float4(fminf(l.x, r.x), fminf(l.y, r.y), fmaxf(l.z, r.z), fmaxf(l.w, r.w));
     __stcg(&a.naabb[p], u);
+    if (p == root) return;
     p = a.nparent[p];
   }
 }
@@ -283,68 +288,106 @@ __device__ __forceinline__ bool accept_pair(const KernelArgs& a, int f, int g, i
 }
 
 #define BP_STACK 96
+#define BP_SLOTS 8  // partners recorded per fixture by the counting pass
 
-// Pair search for one emitter fixture over its world's subtree. Count mode writes the number of
-// accepted partners; emit mode writes the keys f << 32 | g at the scanned offset and sorts them.
-template <bool EMIT>
-__global__ void k_pairs(KernelArgs a, int n) {
-  int f = blockIdx.x * blockDim.x + threadIdx.x;
-  if (f >= n) return;
+// Pair search for one emitter fixture over its world's subtree; calls on_pair(g, j) for the j-th
+// accepted partner (traversal order) and returns the number of partners.
+template <class OnPair>
+__device__ __forceinline__ int traverse_pairs(const KernelArgs& a, int f, OnPair&& on_pair) {
   int bf = a.fbody[f];
   int tf = a.btype[bf];
-  int cnt = 0;
-  int64_t off = 0;
-  if (EMIT) {
-    if ((int64_t)a.poff[a.nf] > a.ccap) return;  // overflow: the host grows the buffers and redoes this pass
-    off = a.poff[f];
-    if (a.poff[f + 1] == off) return;
-  }
   int wf = a.fworld[f];
-  if (tf != B2G_STATIC && !(a.wflags[wf] & B2G_WF_RETIRED)) {
-    int w = wf;
-    int root = a.wroot[w];
-    if (root >= 0 && !(root & LEAF_BIT)) {
-      float4 box = a.aabb[f];
-      int stack[BP_STACK];
-      int sp = 0;
-      stack[sp++] = root;
-      int visits = 0;
-      const int maxVisits = 2 * a.wb[w].w + 8;  // each internal node of the world at most once
-      while (sp > 0) {
-        if (++visits > maxVisits) {
-          raise_status(a.status, B2G_DEV_STACK_OVERFLOW);
-          break;
-        }
-        int node = stack[--sp];
-        int2 ch = a.nchild[node];
-        int kids[2] = {ch.x, ch.y};
+  int cnt = 0;
+  if (tf == B2G_STATIC || (a.wflags[wf] & B2G_WF_RETIRED)) return 0;
+  int root = a.wroot[wf];
+  if (root < 0 || (root & LEAF_BIT)) return 0;
+  float4 box = a.aabb[f];
+  int stack[BP_STACK];
+  int sp = 0;
+  stack[sp++] = root;
+  int visits = 0;
+  const int maxVisits = 2 * a.wb[wf].w + 8;  // each internal node of the world at most once
+  while (sp > 0) {
+    if (++visits > maxVisits) {
+      raise_status(a.status, B2G_DEV_STACK_OVERFLOW);
+      break;
+    }
+    int node = stack[--sp];
+    int2 ch = a.nchild[node];
+    int kids[2] = {ch.x, ch.y};
 #pragma unroll
-        for (int q = 0; q < 2; ++q) {
-          int c = kids[q];
-          if (c & LEAF_BIT) {
-            int g = a.mval_sorted[c & ~LEAF_BIT];
-            if (aabb_overlap4(box, a.aabb[g]) && accept_pair(a, f, g, bf, tf)) {
-              if (EMIT) a.pairs[off + cnt] = ((uint64_t)(uint32_t)f << 32) | (uint32_t)g;
-              ++cnt;
-            }
-          } else if (aabb_overlap4(box, a.naabb[c])) {
-            if (sp < BP_STACK) stack[sp++] = c;
-            else raise_status(a.status, B2G_DEV_STACK_OVERFLOW);
-          }
+    for (int q = 0; q < 2; ++q) {
+      int c = kids[q];
+      if (c & LEAF_BIT) {
+        int g = a.mval_sorted[c & ~LEAF_BIT];
+        if (aabb_overlap4(box, a.aabb[g]) && accept_pair(a, f, g, bf, tf)) {
+          on_pair(g, cnt);
+          ++cnt;
         }
+      } else if (aabb_overlap4(box, a.naabb[c])) {
+        if (sp < BP_STACK) stack[sp++] = c;
+        else raise_status(a.status, B2G_DEV_STACK_OVERFLOW);
       }
     }
   }
-  if (!EMIT) {
-    a.pcount[f] = cnt;
-  } else {
-    uint64_t* seg = a.pairs + off;
-    for (int x = 1; x < cnt; ++x) {
-      uint64_t v = seg[x];
-      int y = x - 1;
-      while (y >= 0 && seg[y] > v) { seg[y + 1] = seg[y]; --y; }
-      seg[y + 1] = v;
+  return cnt;
+}
+
+// Counting pass: partners of every emitter fixture, the first BP_SLOTS of them kept. Threads walk
+// the fixtures in Morton order, so a warp's traversals follow neighbouring tree paths.
+__global__ void k_pairs_count(KernelArgs a, int n) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  int f = a.mval_sorted[i];
+  uint32_t* slots = a.pslots + (int64_t)f * BP_SLOTS;
+  a.pcount[f] = traverse_pairs(a, f, [&](int g, int j) {
+    if (j < BP_SLOTS) slots[j] = (uint32_t)g;
+  });
+}
+
+// Emit pass: each fixture's partners, ascending, as keys f << 32 | g at its scanned offset (the
+// pair list comes out sorted). Fixtures with more partners than slots search again.
+__global__ void k_pairs_emit(KernelArgs a, int n) {
+  int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= n) return;
+  if ((int64_t)a.poff[a.nf] > a.ccap) return;  // overflow: the host grows the buffers and redoes this pass
+  int64_t off = a.poff[f];
+  int cnt = (int)(a.poff[f + 1] - off);
+  if (cnt == 0) return;
+  uint64_t* seg = a.pairs + off;
+  const uint64_t hi = (uint64_t)(uint32_t)f << 32;
+  if (cnt <= BP_SLOTS) {
+    uint32_t v[BP_SLOTS];
+    const uint32_t* slots = a.pslots + (int64_t)f * BP_SLOTS;
+#pragma unroll
+    for (int j = 0; j < BP_SLOTS; ++j) v[j] = j < cnt ? slots[j] : 0xffffffffu;
+    // odd-even transposition sort, fully unrolled so that v stays in registers
+#pragma unroll
+    for (int r = 0; r < BP_SLOTS; ++r) {
+#pragma unroll
+      for (int j = r & 1; j + 1 < BP_SLOTS; j += 2) {
+        uint32_t x = v[j], y = v[j + 1];
+        v[j] = x < y ? x : y;
+        v[j + 1] = x < y ? y : x;
+      }
     }
+#pragma unroll
+    for (int j = 0; j < BP_SLOTS; ++j)
+      if (j < cnt) seg[j] = hi | v[j];
+    return;
+  }
+  int got = traverse_pairs(a, f, [&](int g, int j) {
+    if (j < cnt) seg[j] = hi | (uint32_t)g;
+  });
+  if (got != cnt) raise_status(a.status, B2G_DEV_STACK_OVERFLOW);  // cannot happen: same tree, same test
+  for (int x = 1; x < cnt; ++x) {
+    uint64_t v = seg[x];
+    int y = x - 1;
+    while (y >= 0 && seg[y] > v) {
+      seg[y + 1] = seg[y];
+      --y;
+    }
+    seg[y + 1] = v;
   }
 }
 
@@ -471,13 +514,13 @@ void launch_bp_build(const KernelArgs& a, int nf, int nw, size_t cub_bytes, int 
     k_lbvh_internal<<<grid_for(nf - 1, 256), 256, 0, s>>>(a, nf);
     k_lbvh_bounds<<<grid_for(nf, 256), 256, 0, s>>>(a, nf);
   }
-  k_pairs<false><<<grid_for(nf, 128), 128, 0, s>>>(a, nf);
+  k_pairs_count<<<grid_for(nf, 128), 128, 0, s>>>(a, nf);
   bytes = cub_bytes;
   cub::DeviceScan::ExclusiveSum(a.cub_tmp, bytes, a.pcount, a.poff, nf + 1, s);
   k_world_contacts<<<grid_for(nw, 128), 128, 0, s>>>(a, nw);
 }
 void launch_bp_emit(const KernelArgs& a, int nf, cudaStream_t s) {
-  if (nf > 0) k_pairs<true><<<grid_for(nf, 128), 128, 0, s>>>(a, nf);
+  if (nf > 0) k_pairs_emit<<<grid_for(nf, 128), 128, 0, s>>>(a, nf);
 }
 void launch_contact_diff(const KernelArgs& a, int src, int dst, cudaStream_t s) {
   k_contact_diff<<<grid_for(a.ccap, 256), 256, 0, s>>>(a, src, dst);

@@ -10,20 +10,20 @@
 
 namespace b2g {
 
-// Solver contact constraints in colour order, one float4 (or int4) per plane and slot; world w
-// owns slots [contact_off, contact_off + solver contacts). Split by use so that each phase reads
-// only full, coalesced 16-byte rows: velocity (nf, mass, r0, r1, nmtm, bk, kn, imp, idx) and
-// position (mass, idx, lcs, lnp, lps, rad).
+// Solver contact constraints in colour order, one row per plane and slot; world w owns slots
+// [contact_off, contact_off + solver contacts). Split by use so that each phase reads only full,
+// coalesced rows: velocity (idx, nf, r0, r1, nmtm, bk, kn, imp) and position (idx, lcs, lnp, lps,
+// rad). Body inverse masses are read per body, not per constraint.
 struct SolverPlanes {
+  int2* idx;     // local body A | pointCount << 24 | pcPointCount << 28, local body B | type << 24
+  int* cid;      // live contact index (impulse store, events)
   float4* nf;    // normal.x, normal.y, friction, tangentSpeed
-  float4* mass;  // invMassA, invIA, invMassB, invIB
   float4* r0;    // rA.x, rA.y, rB.x, rB.y of point 0
   float4* r1;    // ... of point 1
   float4* nmtm;  // normalMass 0, 1, tangentMass 0, 1
   float4* bk;    // velocityBias 0, 1, K.ex.x, K.ex.y (= K.ey.x)
   float4* kn;    // K.ey.y, normalMass matrix ex.x, ex.y (= ey.x), ey.y
   float4* imp;   // normalImpulse 0, 1, tangentImpulse 0, 1
-  int4* idx;     // world-local body A, body B, pointCount | pcPointCount << 4 | type << 8, contact
   float4* lcs;   // localCenterA, localCenterB
   float4* lnp;   // localNormal, localPoint
   float4* lps;   // localPoints 0, 1
@@ -48,6 +48,7 @@ struct KernelArgs {
 
   const b2g_shape* shape;
   const int *fbody, *fgroup, *fsensor, *fworld;
+  const float* frad;              // per fixture: shape radius
   const uint32_t* ffilter;
   const float4* fmat;
   float4* aabb;
@@ -79,13 +80,15 @@ struct KernelArgs {
   int* nflag;
   int* wroot;
   int* pcount;
+  uint32_t* pslots;               // BP_SLOTS partners per fixture from the counting pass
   int* poff;
   uint64_t* pairs;
   void* cub_tmp;
 
   // solver
   int* sc_list;                   // per solver contact: live contact index
-  int2* scb;                      // per solver contact: world-local non-static bodies (-1 = static)
+  int2* scb;                      // per solver contact: world-local bodies, bit 31 set = static
+  int* cslot;                     // per solver contact: its colour-ordered slot
   SolverPlanes sp;
   int8_t* ccol;
   int* corder;
@@ -120,6 +123,7 @@ struct KernelArgs {
 #define B2G_CNT_EVENTS 1     // recorded events
 #define B2G_CNT_TOUCHING 2   // solver contacts of the last step
 #define B2G_CNT_OVERFLOW 3   // pair capacity needed when the last broadphase overflowed (else 0)
+#define B2G_CNT_MAXCOLORS 4  // most constraint colours of any world in the last solve
 
 void launch_collide(const KernelArgs& a, cudaStream_t s);
 // Solver launches per class: class 0 on `s`, the others on side streams forked from and joined

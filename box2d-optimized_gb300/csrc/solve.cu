@@ -63,7 +63,7 @@ struct ColourMem {
   int* head;                 // per body: list offset, then first uncoloured entry
   unsigned long long* mask;  // per body: colours taken
   int* list;                 // 2 per constraint: per-body incidence lists
-  const int2* cb;            // per constraint: world-local non-static bodies (-1 = static)
+  const int2* cb;            // per constraint: world-local bodies, negative (bit 31 set) = static
   int8_t* col;               // per constraint: colour, -1 until coloured
   uint8_t* rdy;              // per constraint: ready in the current round
 };
@@ -73,11 +73,12 @@ struct ColourMem {
 // of the priority-sorted incidence list of each of its non-static bodies; it then takes the
 // lowest colour not used at those bodies. The result equals the sequential greedy pass in
 // (priority, index) order. Colours 0..62 are regular; 63 is the overflow colour, solved
-// serially in priority order. Buckets the constraints by colour into `order` and writes the
-// colour offsets to `ranges` (ncol + 1 entries). Returns the number of colours (max + 1).
+// serially in priority order. Buckets the constraints by colour into `order` (and its inverse
+// into `slot` when given) and writes the colour offsets to `ranges` (ncol + 1 entries). Returns
+// the number of colours (max + 1).
 template <int T>
-__device__ int colour_constraints(int n, int nb, const ColourMem m, const uint32_t* prio, int* order, int* ranges,
-                                  unsigned int* status) {
+__device__ int colour_constraints(int n, int nb, const ColourMem m, const uint32_t* prio, int* order, int* slot,
+                                  int* ranges, unsigned int* status) {
   __shared__ int col_cnt[64];
   __shared__ int col_off[65];
   __shared__ int s_carry, s_maxcol;
@@ -192,7 +193,9 @@ __device__ int colour_constraints(int n, int nb, const ColourMem m, const uint32
   for (int k = threadIdx.x; k < n; k += T) {
     int c = m.col[k];
     if (c < 0) c = 63;
-    order[col_off[c] + atomicAdd(&col_cnt[c], 1)] = k;
+    int pos = col_off[c] + atomicAdd(&col_cnt[c], 1);
+    order[pos] = k;
+    if (slot) slot[k] = pos;
   }
   __syncthreads();
   if (threadIdx.x == 0 && col_cnt[63] > 1) {
@@ -210,6 +213,8 @@ __device__ int colour_constraints(int n, int nb, const ColourMem m, const uint32
       }
       order[off + y + 1] = kx;
     }
+    if (slot)
+      for (int x = 0; x < cnt; ++x) slot[order[off + x]] = off + x;
   }
   int ncol = s_maxcol + 1;
   for (int c = threadIdx.x; c <= ncol; c += T) ranges[c] = col_off[c];
@@ -219,36 +224,47 @@ __device__ int colour_constraints(int n, int nb, const ColourMem m, const uint32
 
 // ---- constraint planes <-> the per-constraint register record
 __device__ __forceinline__ void store_planes(const SolverPlanes& P, int s, const VCDev& vc) {
+  P.idx[s] = make_int2(vc.indexA | (vc.pointCount << 24) | (vc.pcPointCount << 28), vc.indexB | (vc.type << 24));
+  P.cid[s] = vc.contact;
   P.nf[s] = make_float4(vc.normal[0], vc.normal[1], vc.friction, vc.tangentSpeed);
-  P.mass[s] = make_float4(vc.invMassA, vc.invIA, vc.invMassB, vc.invIB);
   P.r0[s] = make_float4(vc.rA[0][0], vc.rA[0][1], vc.rB[0][0], vc.rB[0][1]);
   P.r1[s] = make_float4(vc.rA[1][0], vc.rA[1][1], vc.rB[1][0], vc.rB[1][1]);
   P.nmtm[s] = make_float4(vc.normalMass[0], vc.normalMass[1], vc.tangentMass[0], vc.tangentMass[1]);
   P.bk[s] = make_float4(vc.velocityBias[0], vc.velocityBias[1], vc.K[0], vc.K[1]);
   P.kn[s] = make_float4(vc.K[3], vc.NM[0], vc.NM[1], vc.NM[3]);
   P.imp[s] = make_float4(vc.normalImpulse[0], vc.normalImpulse[1], vc.tangentImpulse[0], vc.tangentImpulse[1]);
-  P.idx[s] = make_int4(vc.indexA, vc.indexB, vc.pointCount | (vc.pcPointCount << 4) | (vc.type << 8), vc.contact);
   P.lcs[s] = make_float4(vc.localCenterA[0], vc.localCenterA[1], vc.localCenterB[0], vc.localCenterB[1]);
   P.lnp[s] = make_float4(vc.localNormal[0], vc.localNormal[1], vc.localPoint[0], vc.localPoint[1]);
   P.lps[s] = make_float4(vc.localPoints[0][0], vc.localPoints[0][1], vc.localPoints[1][0], vc.localPoints[1][1]);
   P.rad[s] = make_float2(vc.radiusA, vc.radiusB);
 }
 
-__device__ __forceinline__ void load_common(const SolverPlanes& P, int s, VCDev& vc) {
-  int4 id = P.idx[s];
-  vc.indexA = id.x;
-  vc.indexB = id.y;
-  vc.pointCount = id.z & 15;
-  vc.pcPointCount = (id.z >> 4) & 15;
-  vc.type = id.z >> 8;
-  vc.contact = id.w;
-  float4 m = P.mass[s];
-  vc.invMassA = m.x; vc.invIA = m.y; vc.invMassB = m.z; vc.invIB = m.w;
+// Inverse mass and inertia per world-local body: (1/m, 1/I) pairs in shared memory, or the
+// global mass records (m, 1/m, I, 1/I) of the world.
+struct Masses {
+  const float2* sm;
+  const float4* g;
+  __device__ __forceinline__ float2 get(int i) const {
+    if (sm) return sm[i];
+    float4 m = g[i];
+    return make_float2(m.y, m.w);
+  }
+};
+
+__device__ __forceinline__ void load_common(const SolverPlanes& P, int s, VCDev& vc, const Masses& M) {
+  int2 id = P.idx[s];
+  vc.indexA = id.x & 0xffffff;
+  vc.indexB = id.y & 0xffffff;
+  vc.pointCount = (id.x >> 24) & 15;
+  vc.pcPointCount = (id.x >> 28) & 15;
+  vc.type = id.y >> 24;
+  float2 ma = M.get(vc.indexA), mb = M.get(vc.indexB);
+  vc.invMassA = ma.x; vc.invIA = ma.y; vc.invMassB = mb.x; vc.invIB = mb.y;
 }
 
 // Fields read by warmStartContact / solveContactVelocity.
-__device__ __forceinline__ void load_velocity(const SolverPlanes& P, int s, VCDev& vc, bool full) {
-  load_common(P, s, vc);
+__device__ __forceinline__ void load_velocity(const SolverPlanes& P, int s, VCDev& vc, const Masses& M, bool full) {
+  load_common(P, s, vc, M);
   float4 nf = P.nf[s];
   vc.normal[0] = nf.x; vc.normal[1] = nf.y; vc.friction = nf.z; vc.tangentSpeed = nf.w;
   float4 r0 = P.r0[s];
@@ -273,8 +289,8 @@ __device__ __forceinline__ void load_velocity(const SolverPlanes& P, int s, VCDe
 }
 
 // Fields read by solveContactPosition.
-__device__ __forceinline__ void load_position(const SolverPlanes& P, int s, VCDev& vc) {
-  load_common(P, s, vc);
+__device__ __forceinline__ void load_position(const SolverPlanes& P, int s, VCDev& vc, const Masses& M) {
+  load_common(P, s, vc, M);
   float4 lc = P.lcs[s];
   vc.localCenterA[0] = lc.x; vc.localCenterA[1] = lc.y; vc.localCenterB[0] = lc.z; vc.localCenterB[1] = lc.w;
   float4 ln = P.lnp[s];
@@ -338,7 +354,8 @@ __global__ void __launch_bounds__(T, 1024 / T) k_solve(KernelArgs a, int first, 
       int s = c0 + s_carry + p;
       a.sc_list[s] = c0 + k;
       int ia = a.fbody[f.x], ib = a.fbody[f.y];
-      a.scb[s] = make_int2(a.btype[ia] == B2G_STATIC ? -1 : ia - b0, a.btype[ib] == B2G_STATIC ? -1 : ib - b0);
+      a.scb[s] = make_int2((ia - b0) | (a.btype[ia] == B2G_STATIC ? (int)0x80000000 : 0),
+                           (ib - b0) | (a.btype[ib] == B2G_STATIC ? (int)0x80000000 : 0));
       uint64_t key = a.ckey[c0 + k];
       a.cprio[s] = contactPriority((uint32_t)(key >> 32) - (uint32_t)fo, (uint32_t)key - (uint32_t)fo);
     }
@@ -377,7 +394,7 @@ __global__ void __launch_bounds__(T, 1024 / T) k_solve(KernelArgs a, int first, 
       m.col = a.ccol + c0;
       m.rdy = a.cready + c0;
     }
-    ncc = colour_constraints<T>(nsc, nb, m, a.cprio + c0, a.corder + c0, cranges, a.status);
+    ncc = colour_constraints<T>(nsc, nb, m, a.cprio + c0, a.corder + c0, a.cslot + c0, cranges, a.status);
     if (conSm) {
       for (int k = threadIdx.x; k < nsc; k += T) a.ccol[c0 + k] = col[k];
       __syncthreads();
@@ -391,17 +408,22 @@ __global__ void __launch_bounds__(T, 1024 / T) k_solve(KernelArgs a, int first, 
     a.ncolors[4 * w + 2] = nsc;
     a.ncolors[4 * w + 3] = c0;
     atomicAdd(&a.counters[B2G_CNT_TOUCHING], (unsigned long long)nsc);
+    atomicMax(&a.counters[B2G_CNT_MAXCOLORS], (unsigned long long)(ncc > njc ? ncc : njc));
   }
 
   // 3. velocity integration (b2_island.cpp:256-293, SolveOrphan :187-206) into the body-state
-  //    buffer: shared memory when the world's bodies fit, else the global velocity array
-  const bool bsm = (size_t)nb * sizeof(float4) <= (size_t)smem_bytes;
+  //    buffer: shared memory (with the bodies' inverse masses) when the world's bodies fit, else
+  //    the global velocity array
+  const bool bsm = (size_t)nb * (sizeof(float4) + sizeof(float2)) <= (size_t)smem_bytes;
   float4* bs = bsm ? reinterpret_cast<float4*>(smem) : a.vel + b0;
+  float2* msm = bsm ? reinterpret_cast<float2*>(smem + sizeof(float4) * (size_t)nb) : nullptr;
+  const Masses M{msm, a.massd + b0};
   for (int i = threadIdx.x; i < nb; i += T) {
     int bi = b0 + i;
     float4 v4 = a.vel[bi];
+    float4 md = a.massd[bi];
+    if (bsm) msm[i] = make_float2(md.y, md.w);
     if (a.btype[bi] == B2G_DYNAMIC) {
-      float4 md = a.massd[bi];
       float4 dmp = a.damp[bi];
       float4 fr = a.force[bi];
       V2 v = mk(v4.x, v4.y);
@@ -419,17 +441,20 @@ __global__ void __launch_bounds__(T, 1024 / T) k_solve(KernelArgs a, int first, 
   }
   __syncthreads();
 
-  // 4. prepare (b2ContactSolver::Initialize + InitializeVelocityConstraints) into colour order
-  for (int p = threadIdx.x; p < nsc; p += T) {
-    int k = a.corder[c0 + p];
+  // 4. prepare (b2ContactSolver::Initialize + InitializeVelocityConstraints) in list order, each
+  //    constraint written to its colour-ordered slot
+  for (int k = threadIdx.x; k < nsc; k += T) {
     int ci = a.sc_list[c0 + k];
+    int p = a.cslot[c0 + k];
+    int2 lb = a.scb[c0 + k];
+    int la = lb.x & 0x7fffffff, lbb = lb.y & 0x7fffffff;
+    int ia = b0 + la, ib = b0 + lbb;
     int2 f = a.cfix[ci];
-    int ia = a.fbody[f.x], ib = a.fbody[f.y];
     b2g_manifold m = a.cman[ci];
     VCDev vc;
     for (int q = 0; q < 4; ++q) vc.K[q] = vc.NM[q] = 0.0f;
-    prepareContact(vc, m, a.cmat[ci], a.shape[f.x].radius, a.shape[f.y].radius, ia - b0, ib - b0, a.massd[ia],
-                   a.massd[ib], a.lc[ia], a.lc[ib], a.pos[ia], bs[ia - b0], a.pos[ib], bs[ib - b0], dtRatio, warm, ci);
+    prepareContact(vc, m, a.cmat[ci], a.frad[f.x], a.frad[f.y], la, lbb, a.massd[ia], a.massd[ib], a.lc[ia], a.lc[ib],
+                   a.pos[ia], bs[la], a.pos[ib], bs[lbb], dtRatio, warm, ci);
     store_planes(P, c0 + p, vc);
   }
   __syncthreads();
@@ -443,13 +468,13 @@ __global__ void __launch_bounds__(T, 1024 / T) k_solve(KernelArgs a, int first, 
         if (threadIdx.x == 0)
           for (int i = s; i < e; ++i) {
             VCDev vc;
-            load_velocity(P, c0 + i, vc, false);
+            load_velocity(P, c0 + i, vc, M, false);
             warmStartContact(vc, bs);
           }
       } else {
         for (int i = s + threadIdx.x; i < e; i += T) {
           VCDev vc;
-          load_velocity(P, c0 + i, vc, false);
+          load_velocity(P, c0 + i, vc, M, false);
           warmStartContact(vc, bs);
         }
       }
@@ -486,14 +511,14 @@ __global__ void __launch_bounds__(T, 1024 / T) k_solve(KernelArgs a, int first, 
         if (threadIdx.x == 0)
           for (int i = s; i < e; ++i) {
             VCDev vc;
-            load_velocity(P, c0 + i, vc, true);
+            load_velocity(P, c0 + i, vc, M, true);
             solveContactVelocity(vc, bs);
             P.imp[c0 + i] = make_float4(vc.normalImpulse[0], vc.normalImpulse[1], vc.tangentImpulse[0], vc.tangentImpulse[1]);
           }
       } else {
         for (int i = s + threadIdx.x; i < e; i += T) {
           VCDev vc;
-          load_velocity(P, c0 + i, vc, true);
+          load_velocity(P, c0 + i, vc, M, true);
           solveContactVelocity(vc, bs);
           P.imp[c0 + i] = make_float4(vc.normalImpulse[0], vc.normalImpulse[1], vc.tangentImpulse[0], vc.tangentImpulse[1]);
         }
@@ -504,10 +529,9 @@ __global__ void __launch_bounds__(T, 1024 / T) k_solve(KernelArgs a, int first, 
 
   // 7. StoreImpulses (b2_contact_solver.cpp:641-657)
   for (int p = threadIdx.x; p < nsc; p += T) {
-    int4 id = P.idx[c0 + p];
+    int pc = (P.idx[c0 + p].x >> 24) & 15;
     float4 im = P.imp[c0 + p];
-    b2g_manifold* m = &a.cman[id.w];
-    int pc = id.z & 15;
+    b2g_manifold* m = &a.cman[P.cid[c0 + p]];
     if (pc > 0) { m->points[0].normal_impulse = im.x; m->points[0].tangent_impulse = im.z; }
     if (pc > 1) { m->points[1].normal_impulse = im.y; m->points[1].tangent_impulse = im.w; }
   }
@@ -555,13 +579,13 @@ __global__ void __launch_bounds__(T, 1024 / T) k_solve(KernelArgs a, int first, 
         if (threadIdx.x == 0)
           for (int i = s; i < e; ++i) {
             VCDev vc;
-            load_position(P, c0 + i, vc);
+            load_position(P, c0 + i, vc, M);
             if (!(solveContactPosition(vc, ps) >= -3.0f * B2G_LINEAR_SLOP)) okay = 0;
           }
       } else {
         for (int i = s + threadIdx.x; i < e; i += T) {
           VCDev vc;
-          load_position(P, c0 + i, vc);
+          load_position(P, c0 + i, vc, M);
           if (!(solveContactPosition(vc, ps) >= -3.0f * B2G_LINEAR_SLOP)) okay = 0;
         }
       }
@@ -600,11 +624,11 @@ __global__ void __launch_bounds__(T, 1024 / T) k_solve(KernelArgs a, int first, 
   if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(a.status, B2G_DEV_NONFINITE);
   if (a.events_on) {
     for (int p = threadIdx.x; p < nsc; p += T) {
-      int4 id = P.idx[c0 + p];
+      int pc = (P.idx[c0 + p].x >> 24) & 15;
       float4 im = P.imp[c0 + p];
-      int2 f = a.cfix[id.w];
+      int2 f = a.cfix[P.cid[c0 + p]];
       float ni[2] = {im.x, im.y}, ti[2] = {im.z, im.w};
-      record_event(a, B2G_EVENT_POSTSOLVE, w, f.x - fo, f.y - fo, id.z & 15, ni, ti, 0);
+      record_event(a, B2G_EVENT_POSTSOLVE, w, f.x - fo, f.y - fo, pc, ni, ti, 0);
     }
   }
   if (threadIdx.x == 0 && a.dt > 0.0f) a.wg[w].z = a.inv_dt;
@@ -627,7 +651,8 @@ __global__ void __launch_bounds__(T) k_joint_colour(KernelArgs a, int w0) {
   for (int k = threadIdx.x; k < nj; k += T) {
     const JointDev& J = a.joints[j0 + k];
     int ia = J.d.body_a, ib = J.d.body_b;
-    a.jcb[j0 + k] = make_int2(a.btype[ia] == B2G_STATIC ? -1 : ia - b0, a.btype[ib] == B2G_STATIC ? -1 : ib - b0);
+    a.jcb[j0 + k] = make_int2((ia - b0) | (a.btype[ia] == B2G_STATIC ? (int)0x80000000 : 0),
+                              (ib - b0) | (a.btype[ib] == B2G_STATIC ? (int)0x80000000 : 0));
     a.jprio[j0 + k] = jointPriority((uint32_t)k);
   }
   __syncthreads();
@@ -639,15 +664,15 @@ __global__ void __launch_bounds__(T) k_joint_colour(KernelArgs a, int w0) {
   m.cb = a.jcb + j0;
   m.col = a.jcol + j0;
   m.rdy = a.jready + j0;
-  int njc = colour_constraints<T>(nj, nb, m, a.jprio + j0, a.jorder + j0, jr, a.status);
+  int njc = colour_constraints<T>(nj, nb, m, a.jprio + j0, a.jorder + j0, nullptr, jr, a.status);
   for (int c = threadIdx.x; c <= njc; c += T) a.jranges[65 * (int64_t)w + c] = jr[c];
   if (threadIdx.x == 0) a.ncolors[4 * w + 1] = njc;
 }
 
 // ---- launch planning
 // Class by world body count: threads per CTA and the dynamic shared memory that holds the
-// world's body state (16 B/body) and, room permitting, its colouring arrays (about 52 B/body
-// at two contacts per body).
+// world's body state and inverse masses (24 B/body) and, room permitting, its colouring arrays
+// (about 52 B/body at two contacts per body).
 static const int kClassMaxBodies[B2G_SOLVE_CLASSES] = {64, 256, 1024, 4096, 1 << 30};
 static const int kClassThreads[B2G_SOLVE_CLASSES] = {64, 128, 256, 512, 1024};
 static const int kClassSmemCap[B2G_SOLVE_CLASSES] = {16 << 10, 24 << 10, 56 << 10, 110 << 10, 200 << 10};
