@@ -125,7 +125,7 @@ static KernelArgs make_args(Batch* b) {
   }
   a.wbounds = b->wbounds.p; a.mkey = b->mkey.p; a.mkey_sorted = b->mkey_sorted.p; a.mval = b->mval.p;
   a.mval_sorted = b->mval_sorted.p; a.nchild = b->nchild.p; a.nparent = b->nparent.p; a.lparent = b->lparent.p;
-  a.naabb = b->naabb.p; a.nflag = b->nflag.p; a.wroot = b->wroot.p; a.pcount = b->pcount.p; a.pslots = b->pslots.p; a.poff = b->poff.p;
+  a.naabb = b->naabb.p; a.ncbox = b->ncbox.p; a.laabb = b->laabb.p; a.fattr = b->fattr.p; a.nflag = b->nflag.p; a.wroot = b->wroot.p; a.pcount = b->pcount.p; a.pslots = b->pslots.p; a.poff = b->poffB[b->cur ^ 1].p; a.poff_old = nullptr;
   a.pairs = b->pairs.p; a.cub_tmp = b->cub_tmp.p;
   a.sc_list = b->sc_list.p; a.scb = b->scb.p; a.cslot = b->cslot.p; a.ccol = b->ccol.p; a.corder = b->corder.p; a.cprio = b->cprio.p;
   a.sp.nf = b->sp_nf.p; a.sp.cid = b->sp_cid.p; a.sp.r0 = b->sp_r0.p; a.sp.r1 = b->sp_r1.p;
@@ -324,8 +324,10 @@ int upload_all(Batch* b) {
   TRY(ensure(b, b->mkey, NF)); TRY(ensure(b, b->mkey_sorted, NF)); TRY(ensure(b, b->mval, NF));
   TRY(ensure(b, b->mval_sorted, NF)); TRY(ensure(b, b->nchild, NF)); TRY(ensure(b, b->nparent, NF));
   TRY(ensure(b, b->lparent, NF)); TRY(ensure(b, b->naabb, NF)); TRY(ensure(b, b->nflag, NF));
+  TRY(ensure(b, b->ncbox, 2 * (size_t)NF)); TRY(ensure(b, b->laabb, NF)); TRY(ensure(b, b->fattr, NF));
   TRY(ensure(b, b->pcount, (size_t)NF + 1)); TRY(ensure(b, b->pslots, 8 * (size_t)NF));
-  TRY(ensure(b, b->poff, (size_t)NF + 1));
+  TRY(ensure(b, b->poffB[0], (size_t)NF + 1)); TRY(ensure(b, b->poffB[1], (size_t)NF + 1));
+  b->poff_valid[0] = b->poff_valid[1] = false;
   TRY(ensure(b, b->cub_tmp, cub_temp_bytes(NF)));
   TRY(ensure(b, b->inc_cnt, NB)); TRY(ensure(b, b->inc_head, NB)); TRY(ensure(b, b->inc_mask, NB));
   TRY(ensure(b, b->jinc_list, 2 * (size_t)NJ)); TRY(ensure(b, b->jcol, NJ)); TRY(ensure(b, b->jorder, NJ));
@@ -473,7 +475,10 @@ int upload_tail(Batch* b) {
   TRY(ensure(b, b->aabb, NF)); TRY(ensure(b, b->mkey, NF)); TRY(ensure(b, b->mkey_sorted, NF));
   TRY(ensure(b, b->mval, NF)); TRY(ensure(b, b->mval_sorted, NF)); TRY(ensure(b, b->nchild, NF));
   TRY(ensure(b, b->nparent, NF)); TRY(ensure(b, b->lparent, NF)); TRY(ensure(b, b->naabb, NF));
-  TRY(ensure(b, b->nflag, NF)); TRY(ensure(b, b->pcount, (size_t)NF + 1)); TRY(ensure(b, b->poff, (size_t)NF + 1));
+  TRY(ensure(b, b->ncbox, 2 * (size_t)NF)); TRY(ensure(b, b->laabb, NF)); TRY(ensure(b, b->fattr, NF));
+  TRY(ensure(b, b->nflag, NF)); TRY(ensure(b, b->pcount, (size_t)NF + 1));
+  TRY(ensure(b, b->poffB[0], (size_t)NF + 1)); TRY(ensure(b, b->poffB[1], (size_t)NF + 1));
+  b->poff_valid[0] = b->poff_valid[1] = false;
   TRY(ensure(b, b->pslots, 8 * (size_t)NF));
   TRY(ensure(b, b->cub_tmp, cub_temp_bytes(NF)));
   TRY(ensure(b, b->inc_cnt, NB)); TRY(ensure(b, b->inc_head, NB)); TRY(ensure(b, b->inc_mask, NB));
@@ -626,6 +631,11 @@ static int sort_bits(Batch* b) {
 // The live contact list moves to buffer cur ^ 1.
 static void enqueue_broadphase(Batch* b, const KernelArgs& a0, int src) {
   KernelArgs a = a0;
+  // the new list goes to buffer src ^ 1; the diff finds persisting contacts through the live
+  // list's per-fixture offsets when the last broadphase left them
+  a.poff = b->poffB[src ^ 1].p;
+  a.poff_old = b->poff_valid[src] ? b->poffB[src].p : nullptr;
+  b->poff_valid[src ^ 1] = true;
   launch_bp_build(a, b->NF, b->NW, b->cub_tmp.cap, sort_bits(b), b->stream);
   launch_bp_emit(a, b->NF, b->stream);
   launch_contact_diff(a, src, src ^ 1, b->stream);
@@ -936,7 +946,7 @@ B2G_API int b2g_batch_destroy(b2g_batch* b) {
   }
   release(b, b->wbounds); release(b, b->mkey); release(b, b->mkey_sorted); release(b, b->mval);
   release(b, b->mval_sorted); release(b, b->nchild); release(b, b->nparent); release(b, b->lparent);
-  release(b, b->naabb); release(b, b->nflag); release(b, b->wroot); release(b, b->pcount); release(b, b->pslots); release(b, b->poff); release(b, b->pairs);
+  release(b, b->naabb); release(b, b->ncbox); release(b, b->laabb); release(b, b->fattr); release(b, b->nflag); release(b, b->wroot); release(b, b->pcount); release(b, b->pslots); release(b, b->poffB[0]); release(b, b->poffB[1]); release(b, b->pairs);
   release(b, b->cub_tmp); release(b, b->status); release(b, b->counters); release(b, b->sc_list); release(b, b->scb); release(b, b->cslot); release(b, b->frad);
   release(b, b->ccol); release(b, b->corder); release(b, b->cprio); release(b, b->cready); release(b, b->inc_cnt);
   release(b, b->inc_head); release(b, b->inc_mask); release(b, b->inc_list);

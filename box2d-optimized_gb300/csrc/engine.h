@@ -164,12 +164,14 @@ struct Batch {
   DBuf<int> mval, mval_sorted;
   DBuf<int2> nchild;              // internal node children (leaf = index | 0x80000000)
   DBuf<int> nparent, lparent;     // parents of internal nodes and leaves
-  DBuf<float4> naabb;
+  DBuf<float4> naabb, ncbox, laabb;
+  DBuf<int4> fattr;
   DBuf<int> nflag;
   DBuf<int> wroot;                // per world: root node (leaf encoded), -1 if empty
   DBuf<int> pcount;               // per fixture pair count
   DBuf<uint32_t> pslots;          // per fixture: first partners found by the counting pass
-  DBuf<int> poff;                 // exclusive scan of pcount (NF + 1 entries)
+  DBuf<int> poffB[2];             // per contact buffer: exclusive scan of pcount (NF + 1 entries)
+  bool poff_valid[2] = {false, false};  // offsets describe that buffer's list (built by a broadphase)
   DBuf<uint64_t> pairs;
   DBuf<uint8_t> cub_tmp;
   DBuf<unsigned int> status;      // device status word

@@ -99,11 +99,16 @@ __global__ void k_clear_forces(KernelArgs a, int nbodies) {
 }
 
 // ================================================================================ broadphase
+// Fixture AABBs, and the packed attributes the pair filter reads for every candidate partner:
+// (body, group index, category | mask << 16, shape type | body type << 8).
 __global__ void k_aabb(KernelArgs a, int n) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  AABB bb = shapeAABB(a.shape[i], ldXf(a.xf, a.fbody[i]));
+  int body = a.fbody[i];
+  const b2g_shape& sh = a.shape[i];
+  AABB bb = shapeAABB(sh, ldXf(a.xf, body));
   a.aabb[i] = make_float4(bb.lo.x, bb.lo.y, bb.hi.x, bb.hi.y);
+  a.fattr[i] = make_int4(body, a.fgroup[i], (int)a.ffilter[i], sh.type | (a.btype[body] << 8));
 }
 
 // Per-world bounds of AABB centres (lower + upper, the reference's GetCenter2) for Morton codes.
@@ -208,6 +213,7 @@ __global__ void k_lbvh_internal(KernelArgs a, int n) {
 __global__ void k_lbvh_init(KernelArgs a, int n, int nw) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) {
+    a.laabb[i] = a.aabb[a.mval_sorted[i]];
     a.lparent[i] = -1;
     if (i < n - 1) {
       a.nparent[i] = -1;
@@ -238,10 +244,12 @@ __global__ void k_lbvh_bounds(KernelArgs a, int n) {
     cuda::atomic_ref<int, cuda::thread_scope_device> arrivals(a.nflag[p]);
     if (arrivals.fetch_add(1, cuda::memory_order_acq_rel) == 0) return;
     int2 ch = a.nchild[p];
-    float4 l = (ch.x & LEAF_BIT) ? a.aabb[a.mval_sorted[ch.x & ~LEAF_BIT]] : __ldcg(&a.naabb[ch.x]);
-    float4 r = (ch.y & LEAF_BIT) ? a.aabb[a.mval_sorted[ch.y & ~LEAF_BIT]] : __ldcg(&a.naabb[ch.y]);
+    float4 l = (ch.x & LEAF_BIT) ? a.laabb[ch.x & ~LEAF_BIT] : __ldcg(&a.naabb[ch.x]);
+    float4 r = (ch.y & LEAF_BIT) ? a.laabb[ch.y & ~LEAF_BIT] : __ldcg(&a.naabb[ch.y]);
     float4 u = make_float4(fminf(l.x, r.x), fminf(l.y, r.y), fmaxf(l.z, r.z), fmaxf(l.w, r.w));
     __stcg(&a.naabb[p], u);
+    a.ncbox[2 * (int64_t)p] = l;  // the traversal tests both children from their parent's record
+    a.ncbox[2 * (int64_t)p + 1] = r;
     if (p == root) return;
     p = a.nparent[p];
   }
@@ -263,27 +271,28 @@ __device__ __forceinline__ bool nocollide_has(const uint64_t* keys, int n, uint6
 // Would fixture f (non-static, the emitter) report the pair (f, g)? Emitter rule: the non-static
 // fixture of a static pair, else the lower index. Filters of b2ContactManager::QueryCallback:
 // same body, b2Body::ShouldCollide (a dynamic body, no collideConnected=false joint), the default
-// b2ContactFilter (group / category / mask) and the collider table.
-__device__ __forceinline__ bool accept_pair(const KernelArgs& a, int f, int g, int bf, int tf) {
+// b2ContactFilter (group / category / mask) and the collider table. fa / ga are the packed
+// attributes of f and g (k_aabb).
+__device__ __forceinline__ bool accept_pair(const KernelArgs& a, int f, int4 fa, int g, int4 ga) {
   if (g == f) return false;
-  int bg = a.fbody[g];
+  int bf = fa.x, bg = ga.x;
   if (bg == bf) return false;
-  int tg = a.btype[bg];
+  int tf = fa.w >> 8, tg = ga.w >> 8;
   if (tg != B2G_STATIC && g < f) return false;
   if (tf != B2G_DYNAMIC && tg != B2G_DYNAMIC) return false;
   if (a.n_nocollide > 0) {
     uint32_t x = (uint32_t)min(bf, bg), y = (uint32_t)max(bf, bg);
     if (nocollide_has(a.nocollide, a.n_nocollide, ((uint64_t)x << 32) | y)) return false;
   }
-  int gf = a.fgroup[f], gg = a.fgroup[g];
+  int gf = fa.y, gg = ga.y;
   if (gf == gg && gf != 0) {
     if (!(gf > 0)) return false;
   } else {
-    uint32_t ff = a.ffilter[f], fg = a.ffilter[g];
+    uint32_t ff = (uint32_t)fa.z, fg = (uint32_t)ga.z;
     uint32_t catF = ff & 0xffffu, maskF = ff >> 16, catG = fg & 0xffffu, maskG = fg >> 16;
     if (!((maskF & catG) != 0 && (catF & maskG) != 0)) return false;
   }
-  int sf = a.shape[f].type, sg = a.shape[g].type;
+  int sf = fa.w & 0xff, sg = ga.w & 0xff;
   return hasCollider(sf, sg) || hasCollider(sg, sf);
 }
 
@@ -294,11 +303,10 @@ __device__ __forceinline__ bool accept_pair(const KernelArgs& a, int f, int g, i
 // accepted partner (traversal order) and returns the number of partners.
 template <class OnPair>
 __device__ __forceinline__ int traverse_pairs(const KernelArgs& a, int f, OnPair&& on_pair) {
-  int bf = a.fbody[f];
-  int tf = a.btype[bf];
+  const int4 fa = a.fattr[f];
   int wf = a.fworld[f];
   int cnt = 0;
-  if (tf == B2G_STATIC || (a.wflags[wf] & B2G_WF_RETIRED)) return 0;
+  if ((fa.w >> 8) == B2G_STATIC || (a.wflags[wf] & B2G_WF_RETIRED)) return 0;
   int root = a.wroot[wf];
   if (root < 0 || (root & LEAF_BIT)) return 0;
   float4 box = a.aabb[f];
@@ -314,17 +322,19 @@ __device__ __forceinline__ int traverse_pairs(const KernelArgs& a, int f, OnPair
     }
     int node = stack[--sp];
     int2 ch = a.nchild[node];
+    float4 cbox[2] = {a.ncbox[2 * (int64_t)node], a.ncbox[2 * (int64_t)node + 1]};
     int kids[2] = {ch.x, ch.y};
 #pragma unroll
     for (int q = 0; q < 2; ++q) {
       int c = kids[q];
+      if (!aabb_overlap4(box, cbox[q])) continue;
       if (c & LEAF_BIT) {
         int g = a.mval_sorted[c & ~LEAF_BIT];
-        if (aabb_overlap4(box, a.aabb[g]) && accept_pair(a, f, g, bf, tf)) {
+        if (accept_pair(a, f, fa, g, a.fattr[g])) {
           on_pair(g, cnt);
           ++cnt;
         }
-      } else if (aabb_overlap4(box, a.naabb[c])) {
+      } else {
         if (sp < BP_STACK) stack[sp++] = c;
         else raise_status(a.status, B2G_DEV_STACK_OVERFLOW);
       }
@@ -417,7 +427,15 @@ __global__ void k_contact_diff(KernelArgs a, int src, int dst) {
   int64_t nold = (int64_t)a.counters[B2G_CNT_CONTACTS];
   if (nnew > a.ccap || k >= nnew) return;
   uint64_t key = a.pairs[k];
-  int64_t o = find_key(a.ckeyB[src], nold, key);
+  int64_t o;
+  if (a.poff_old) {  // the live list's entries of this emitter
+    int e = (int)(key >> 32);
+    int64_t lo = a.poff_old[e], hi = a.poff_old[e + 1];
+    int64_t r = find_key(a.ckeyB[src] + lo, hi - lo, key);
+    o = r >= 0 ? lo + r : -1;
+  } else {
+    o = find_key(a.ckeyB[src], nold, key);
+  }
   a.ckeyB[dst][k] = key;
   if (o >= 0) {
     a.cfixB[dst][k] = a.cfixB[src][o];
@@ -447,7 +465,9 @@ __global__ void k_contact_dead(KernelArgs a, int src) {
   int64_t nold = (int64_t)a.counters[B2G_CNT_CONTACTS];
   if (nnew > a.ccap || k >= nold) return;
   uint64_t key = a.ckeyB[src][k];
-  if (find_key(a.pairs, nnew, key) >= 0) return;
+  int e = (int)(key >> 32);
+  int64_t lo = a.poff[e];
+  if (find_key(a.pairs + lo, (int64_t)a.poff[e + 1] - lo, key) >= 0) return;
   if ((a.cflagsB[src][k] & B2G_CONTACT_TOUCHING) == 0) return;
   int2 f = a.cfixB[src][k];
   int w = a.fworld[f.x];

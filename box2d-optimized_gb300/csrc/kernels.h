@@ -77,11 +77,15 @@ struct KernelArgs {
   int2* nchild;
   int *nparent, *lparent;
   float4* naabb;
+  float4* ncbox;                  // per internal node: left and right child boxes
+  float4* laabb;                  // leaf boxes in sorted order
+  int4* fattr;                    // per fixture: body, group, filter, shape type | body type << 8
   int* nflag;
   int* wroot;
   int* pcount;
   uint32_t* pslots;               // BP_SLOTS partners per fixture from the counting pass
-  int* poff;
+  int* poff;                      // offsets of the pair list being built, per emitter fixture
+  const int* poff_old;            // offsets of the live (source) list, or null when unknown
   uint64_t* pairs;
   void* cub_tmp;
 

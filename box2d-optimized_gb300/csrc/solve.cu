@@ -271,20 +271,18 @@ __device__ __forceinline__ void load_velocity(const SolverPlanes& P, int s, VCDe
   vc.rA[0][0] = r0.x; vc.rA[0][1] = r0.y; vc.rB[0][0] = r0.z; vc.rB[0][1] = r0.w;
   float4 im = P.imp[s];
   vc.normalImpulse[0] = im.x; vc.normalImpulse[1] = im.y; vc.tangentImpulse[0] = im.z; vc.tangentImpulse[1] = im.w;
-  if (vc.pointCount == 2) {
-    float4 r1 = P.r1[s];
-    vc.rA[1][0] = r1.x; vc.rA[1][1] = r1.y; vc.rB[1][0] = r1.z; vc.rB[1][1] = r1.w;
-  }
+  // rows of the second point and the block solver are loaded whatever the point count, so that
+  // no load waits for the index row (1-point rows hold zeros and are not used)
+  float4 r1 = P.r1[s];
+  vc.rA[1][0] = r1.x; vc.rA[1][1] = r1.y; vc.rB[1][0] = r1.z; vc.rB[1][1] = r1.w;
   if (full) {
     float4 mm = P.nmtm[s];
     vc.normalMass[0] = mm.x; vc.normalMass[1] = mm.y; vc.tangentMass[0] = mm.z; vc.tangentMass[1] = mm.w;
     float4 bk = P.bk[s];
     vc.velocityBias[0] = bk.x; vc.velocityBias[1] = bk.y;
-    if (vc.pointCount == 2) {
-      float4 kn = P.kn[s];
-      vc.K[0] = bk.z; vc.K[1] = bk.w; vc.K[2] = bk.w; vc.K[3] = kn.x;
-      vc.NM[0] = kn.y; vc.NM[1] = kn.z; vc.NM[2] = kn.z; vc.NM[3] = kn.w;
-    }
+    float4 kn = P.kn[s];
+    vc.K[0] = bk.z; vc.K[1] = bk.w; vc.K[2] = bk.w; vc.K[3] = kn.x;
+    vc.NM[0] = kn.y; vc.NM[1] = kn.z; vc.NM[2] = kn.z; vc.NM[3] = kn.w;
   }
 }
 
