@@ -42,7 +42,7 @@ __global__ void k_collide(KernelArgs a) {
   uint32_t flags = a.cflags[i];
   bool wasTouching = (flags & B2G_CONTACT_TOUCHING) != 0;
   flags |= B2G_CONTACT_ENABLED;
-  b2g_manifold old = a.cman[i];
+  b2g_manifold old = ld_manifold(&a.cman[i]);
   bool sensor = a.fsensor[f.x] || a.fsensor[f.y];
   bool touching = false;
   b2g_manifold nm;
@@ -80,7 +80,7 @@ __global__ void k_collide(KernelArgs a) {
   }
   if (touching) flags |= B2G_CONTACT_TOUCHING;
   else flags &= ~B2G_CONTACT_TOUCHING;
-  a.cman[i] = nm;
+  st_manifold(&a.cman[i], nm);
   a.cflags[i] = flags;
   if (a.events_on) {
     int fo = a.wb[w].z;
@@ -441,7 +441,7 @@ __global__ void k_contact_diff(KernelArgs a, int src, int dst) {
     a.cfixB[dst][k] = a.cfixB[src][o];
     a.cflagsB[dst][k] = a.cflagsB[src][o];
     a.cmatB[dst][k] = a.cmatB[src][o];
-    a.cmanB[dst][k] = a.cmanB[src][o];
+    copy_manifold(&a.cmanB[dst][k], &a.cmanB[src][o]);
   } else {
     int e = (int)(key >> 32), p = (int)(uint32_t)key;
     int fa, fb;
@@ -451,9 +451,8 @@ __global__ void k_contact_diff(KernelArgs a, int src, int dst) {
     a.cfixB[dst][k] = make_int2(fa, fb);
     a.cflagsB[dst][k] = B2G_CONTACT_ENABLED;
     a.cmatB[dst][k] = make_float4(sqrtf(ma.x * mb.x), ma.y > mb.y ? ma.y : mb.y, ma.z < mb.z ? ma.z : mb.z, 0.0f);
-    b2g_manifold m;
-    memset(&m, 0, sizeof(m));
-    a.cmanB[dst][k] = m;
+    int4* m = reinterpret_cast<int4*>(&a.cmanB[dst][k]);
+    m[0] = m[1] = m[2] = m[3] = make_int4(0, 0, 0, 0);
   }
 }
 

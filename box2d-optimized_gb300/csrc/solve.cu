@@ -251,8 +251,38 @@ struct Masses {
   }
 };
 
-__device__ __forceinline__ void load_common(const SolverPlanes& P, int s, VCDev& vc, const Masses& M) {
-  int2 id = P.idx[s];
+// The rows of one constraint read by the velocity phase (warm start, velocity iterations) and by
+// the position iterations; all loads are issued together (none waits for another).
+struct VelRows {
+  int2 id;
+  float4 nf, r0, r1, nmtm, bk, kn, imp;
+};
+struct PosRows {
+  int2 id;
+  float4 lcs, lnp, lps;
+  float2 rad;
+};
+
+__device__ __forceinline__ void fetch_vel(const SolverPlanes& P, int s, VelRows& r) {
+  r.id = P.idx[s];
+  r.nf = P.nf[s];
+  r.r0 = P.r0[s];
+  r.r1 = P.r1[s];
+  r.nmtm = P.nmtm[s];
+  r.bk = P.bk[s];
+  r.kn = P.kn[s];
+  r.imp = P.imp[s];
+}
+
+__device__ __forceinline__ void fetch_pos(const SolverPlanes& P, int s, PosRows& r) {
+  r.id = P.idx[s];
+  r.lcs = P.lcs[s];
+  r.lnp = P.lnp[s];
+  r.lps = P.lps[s];
+  r.rad = P.rad[s];
+}
+
+__device__ __forceinline__ void unpack_common(int2 id, VCDev& vc, const Masses& M) {
   vc.indexA = id.x & 0xffffff;
   vc.indexB = id.y & 0xffffff;
   vc.pointCount = (id.x >> 24) & 15;
@@ -262,41 +292,53 @@ __device__ __forceinline__ void load_common(const SolverPlanes& P, int s, VCDev&
   vc.invMassA = ma.x; vc.invIA = ma.y; vc.invMassB = mb.x; vc.invIB = mb.y;
 }
 
-// Fields read by warmStartContact / solveContactVelocity.
-__device__ __forceinline__ void load_velocity(const SolverPlanes& P, int s, VCDev& vc, const Masses& M, bool full) {
-  load_common(P, s, vc, M);
-  float4 nf = P.nf[s];
-  vc.normal[0] = nf.x; vc.normal[1] = nf.y; vc.friction = nf.z; vc.tangentSpeed = nf.w;
-  float4 r0 = P.r0[s];
-  vc.rA[0][0] = r0.x; vc.rA[0][1] = r0.y; vc.rB[0][0] = r0.z; vc.rB[0][1] = r0.w;
-  float4 im = P.imp[s];
-  vc.normalImpulse[0] = im.x; vc.normalImpulse[1] = im.y; vc.tangentImpulse[0] = im.z; vc.tangentImpulse[1] = im.w;
-  // rows of the second point and the block solver are loaded whatever the point count, so that
-  // no load waits for the index row (1-point rows hold zeros and are not used)
-  float4 r1 = P.r1[s];
-  vc.rA[1][0] = r1.x; vc.rA[1][1] = r1.y; vc.rB[1][0] = r1.z; vc.rB[1][1] = r1.w;
-  if (full) {
-    float4 mm = P.nmtm[s];
-    vc.normalMass[0] = mm.x; vc.normalMass[1] = mm.y; vc.tangentMass[0] = mm.z; vc.tangentMass[1] = mm.w;
-    float4 bk = P.bk[s];
-    vc.velocityBias[0] = bk.x; vc.velocityBias[1] = bk.y;
-    float4 kn = P.kn[s];
-    vc.K[0] = bk.z; vc.K[1] = bk.w; vc.K[2] = bk.w; vc.K[3] = kn.x;
-    vc.NM[0] = kn.y; vc.NM[1] = kn.z; vc.NM[2] = kn.z; vc.NM[3] = kn.w;
-  }
+// Fields read by warmStartContact / solveContactVelocity (1-point rows of the second point and
+// the block solver hold zeros and are not used).
+__device__ __forceinline__ void unpack_vel(const VelRows& r, VCDev& vc, const Masses& M) {
+  unpack_common(r.id, vc, M);
+  vc.normal[0] = r.nf.x; vc.normal[1] = r.nf.y; vc.friction = r.nf.z; vc.tangentSpeed = r.nf.w;
+  vc.rA[0][0] = r.r0.x; vc.rA[0][1] = r.r0.y; vc.rB[0][0] = r.r0.z; vc.rB[0][1] = r.r0.w;
+  vc.rA[1][0] = r.r1.x; vc.rA[1][1] = r.r1.y; vc.rB[1][0] = r.r1.z; vc.rB[1][1] = r.r1.w;
+  vc.normalImpulse[0] = r.imp.x; vc.normalImpulse[1] = r.imp.y;
+  vc.tangentImpulse[0] = r.imp.z; vc.tangentImpulse[1] = r.imp.w;
+  vc.normalMass[0] = r.nmtm.x; vc.normalMass[1] = r.nmtm.y; vc.tangentMass[0] = r.nmtm.z; vc.tangentMass[1] = r.nmtm.w;
+  vc.velocityBias[0] = r.bk.x; vc.velocityBias[1] = r.bk.y;
+  vc.K[0] = r.bk.z; vc.K[1] = r.bk.w; vc.K[2] = r.bk.w; vc.K[3] = r.kn.x;
+  vc.NM[0] = r.kn.y; vc.NM[1] = r.kn.z; vc.NM[2] = r.kn.z; vc.NM[3] = r.kn.w;
 }
 
 // Fields read by solveContactPosition.
-__device__ __forceinline__ void load_position(const SolverPlanes& P, int s, VCDev& vc, const Masses& M) {
-  load_common(P, s, vc, M);
-  float4 lc = P.lcs[s];
-  vc.localCenterA[0] = lc.x; vc.localCenterA[1] = lc.y; vc.localCenterB[0] = lc.z; vc.localCenterB[1] = lc.w;
-  float4 ln = P.lnp[s];
-  vc.localNormal[0] = ln.x; vc.localNormal[1] = ln.y; vc.localPoint[0] = ln.z; vc.localPoint[1] = ln.w;
-  float4 lp = P.lps[s];
-  vc.localPoints[0][0] = lp.x; vc.localPoints[0][1] = lp.y; vc.localPoints[1][0] = lp.z; vc.localPoints[1][1] = lp.w;
-  float2 r = P.rad[s];
-  vc.radiusA = r.x; vc.radiusB = r.y;
+__device__ __forceinline__ void unpack_pos(const PosRows& r, VCDev& vc, const Masses& M) {
+  unpack_common(r.id, vc, M);
+  vc.localCenterA[0] = r.lcs.x; vc.localCenterA[1] = r.lcs.y; vc.localCenterB[0] = r.lcs.z; vc.localCenterB[1] = r.lcs.w;
+  vc.localNormal[0] = r.lnp.x; vc.localNormal[1] = r.lnp.y; vc.localPoint[0] = r.lnp.z; vc.localPoint[1] = r.lnp.w;
+  vc.localPoints[0][0] = r.lps.x; vc.localPoints[0][1] = r.lps.y;
+  vc.localPoints[1][0] = r.lps.z; vc.localPoints[1][1] = r.lps.w;
+  vc.radiusA = r.rad.x; vc.radiusB = r.rad.y;
+}
+
+// One pass over the contact colours: colour by colour, a CTA barrier after each; colour 63 (the
+// overflow colour) is solved serially by thread 0 in priority order.
+template <int T, class Rows, class Fetch, class Solve>
+__device__ __forceinline__ void colour_sweep(const int* ranges, int ncol, int c0, Fetch fetch, Solve solve) {
+  for (int c = 0; c < ncol; ++c) {
+    int s = ranges[c], e = ranges[c + 1];
+    if (c == 63) {
+      if (threadIdx.x == 0)
+        for (int i = s; i < e; ++i) {
+          Rows r;
+          fetch(c0 + i, r);
+          solve(c0 + i, r);
+        }
+    } else {
+      for (int i = s + threadIdx.x; i < e; i += T) {
+        Rows r;
+        fetch(c0 + i, r);
+        solve(c0 + i, r);
+      }
+    }
+    __syncthreads();
+  }
 }
 
 // Carves 16-byte aligned pieces out of the CTA's dynamic shared memory.
@@ -448,7 +490,7 @@ __global__ void __launch_bounds__(T, 1024 / T) k_solve(KernelArgs a, int first, 
     int la = lb.x & 0x7fffffff, lbb = lb.y & 0x7fffffff;
     int ia = b0 + la, ib = b0 + lbb;
     int2 f = a.cfix[ci];
-    b2g_manifold m = a.cman[ci];
+    b2g_manifold m = ld_manifold(&a.cman[ci]);
     VCDev vc;
     for (int q = 0; q < 4; ++q) vc.K[q] = vc.NM[q] = 0.0f;
     prepareContact(vc, m, a.cmat[ci], a.frad[f.x], a.frad[f.y], la, lbb, a.massd[ia], a.massd[ib], a.lc[ia], a.lc[ib],
@@ -459,25 +501,14 @@ __global__ void __launch_bounds__(T, 1024 / T) k_solve(KernelArgs a, int first, 
   float4* jb = bs - b0;  // joints address bodies by global index
 
   // 5. warm start contacts, then joint InitVelocityConstraints, colour by colour
+  auto fetchV = [&](int slot, VelRows& r) { fetch_vel(P, slot, r); };
+  auto fetchP = [&](int slot, PosRows& r) { fetch_pos(P, slot, r); };
   if (warm) {
-    for (int c = 0; c < ncc; ++c) {
-      int s = cranges[c], e = cranges[c + 1];
-      if (c == 63) {
-        if (threadIdx.x == 0)
-          for (int i = s; i < e; ++i) {
-            VCDev vc;
-            load_velocity(P, c0 + i, vc, M, false);
-            warmStartContact(vc, bs);
-          }
-      } else {
-        for (int i = s + threadIdx.x; i < e; i += T) {
-          VCDev vc;
-          load_velocity(P, c0 + i, vc, M, false);
-          warmStartContact(vc, bs);
-        }
-      }
-      __syncthreads();
-    }
+    colour_sweep<T, VelRows>(cranges, ncc, c0, fetchV, [&](int slot, const VelRows& r) {
+      VCDev vc;
+      unpack_vel(r, vc, M);
+      warmStartContact(vc, bs);
+    });
   }
   for (int c = 0; c < njc; ++c) {
     int s = jranges[c], e = jranges[c + 1];
@@ -503,26 +534,12 @@ __global__ void __launch_bounds__(T, 1024 / T) k_solve(KernelArgs a, int first, 
       }
       __syncthreads();
     }
-    for (int c = 0; c < ncc; ++c) {
-      int s = cranges[c], e = cranges[c + 1];
-      if (c == 63) {
-        if (threadIdx.x == 0)
-          for (int i = s; i < e; ++i) {
-            VCDev vc;
-            load_velocity(P, c0 + i, vc, M, true);
-            solveContactVelocity(vc, bs);
-            P.imp[c0 + i] = make_float4(vc.normalImpulse[0], vc.normalImpulse[1], vc.tangentImpulse[0], vc.tangentImpulse[1]);
-          }
-      } else {
-        for (int i = s + threadIdx.x; i < e; i += T) {
-          VCDev vc;
-          load_velocity(P, c0 + i, vc, M, true);
-          solveContactVelocity(vc, bs);
-          P.imp[c0 + i] = make_float4(vc.normalImpulse[0], vc.normalImpulse[1], vc.tangentImpulse[0], vc.tangentImpulse[1]);
-        }
-      }
-      __syncthreads();
-    }
+    colour_sweep<T, VelRows>(cranges, ncc, c0, fetchV, [&](int slot, const VelRows& r) {
+      VCDev vc;
+      unpack_vel(r, vc, M);
+      solveContactVelocity(vc, bs);
+      P.imp[slot] = make_float4(vc.normalImpulse[0], vc.normalImpulse[1], vc.tangentImpulse[0], vc.tangentImpulse[1]);
+    });
   }
 
   // 7. StoreImpulses (b2_contact_solver.cpp:641-657)
@@ -571,24 +588,11 @@ __global__ void __launch_bounds__(T, 1024 / T) k_solve(KernelArgs a, int first, 
   // 9. position iterations: contacts then joints, early exit for the world (b2_island.cpp:387-428)
   for (int it = 0; it < a.pi; ++it) {
     int okay = 1;
-    for (int c = 0; c < ncc; ++c) {
-      int s = cranges[c], e = cranges[c + 1];
-      if (c == 63) {
-        if (threadIdx.x == 0)
-          for (int i = s; i < e; ++i) {
-            VCDev vc;
-            load_position(P, c0 + i, vc, M);
-            if (!(solveContactPosition(vc, ps) >= -3.0f * B2G_LINEAR_SLOP)) okay = 0;
-          }
-      } else {
-        for (int i = s + threadIdx.x; i < e; i += T) {
-          VCDev vc;
-          load_position(P, c0 + i, vc, M);
-          if (!(solveContactPosition(vc, ps) >= -3.0f * B2G_LINEAR_SLOP)) okay = 0;
-        }
-      }
-      __syncthreads();
-    }
+    colour_sweep<T, PosRows>(cranges, ncc, c0, fetchP, [&](int slot, const PosRows& r) {
+      VCDev vc;
+      unpack_pos(r, vc, M);
+      if (!(solveContactPosition(vc, ps) >= -3.0f * B2G_LINEAR_SLOP)) okay = 0;
+    });
     for (int c = 0; c < njc; ++c) {
       int s = jranges[c], e = jranges[c + 1];
       if (c == 63) {
