@@ -187,6 +187,18 @@ def build_batch(lib, seeds, device):
     return batch, nb
 
 
+def solve_traffic(sb):
+    """DRAM bytes of the solver launches of one step, from the ncu capture of the settled
+    384-world case committed in profiles/k_solve_dram.json, scaled to this step by algorithmic
+    bytes (traffic grows with the solver's work); None when the capture is absent."""
+    try:
+        with open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "profiles", "k_solve_dram.json")) as f:
+            d = json.load(f)
+        return d["dram_bytes_per_step"] * sb / d["solve_bytes_per_step"]
+    except (OSError, KeyError, ValueError, ZeroDivisionError):
+        return None
+
+
 def step_bytes(nb, nf, np_, nc, nj, vi=VI, pi=PI):
     """Algorithmic bytes of one Step (fixed accounting): bodies 96/body, broadphase 144/fixture +
     8/pair, per touching contact 524 + 192 vi + 144 pi, per joint 160 + 128 vi + 96 pi."""
@@ -353,7 +365,10 @@ def run_ours(args, rank, world_size):
             cpu = {"value": v, "unit": "body-steps/s", "cores": threads, "kind": "port",
                    "sample": f"{len(cpu_seeds)} of the worlds ({cnb} bodies), steps {args.warmup + 1}-"
                              f"{args.warmup + args.steps} of the same rollout, {secs:.1f} s on {threads} threads"}
-        kernels_per_step = 14  # collide, solve, 11 broadphase/diff kernels, clear forces
+        # own kernels per step (CUB's sort and scan kernels not counted): collide, one solver launch
+        # per world size class (5 in this workload), aabb, world bounds, morton, lbvh init /
+        # internal / bounds, pair count, world contact ranges, pair emit, diff, commit, clear forces
+        kernels_per_step = 18
         line = {
             "metric": METRIC, "value": value, "unit": "body-steps/s", "n_gpus": world_size, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
@@ -368,7 +383,7 @@ def run_ours(args, rank, world_size):
                              "step": prof.step},
             "step_bytes": step_b, "step_gbs": step_b / (ms_per_step / 1e3) / 1e9,
             "roofline": {"kernel": "k_solve", "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": (achieved / peak) if achieved else None, "traffic": None,
+                         "frac": (achieved / peak) if achieved else None, "traffic": solve_traffic(sb),
                          "peak_kind": f"{peak_kind} hbm_gbs", "bytes_per_launch": sb},
             "cpu_baseline": cpu,
             "served": served,
@@ -382,6 +397,28 @@ def run_ours(args, rank, world_size):
     batch.close()
     if line:
         print(json.dumps(line), flush=True)
+
+
+def profile_window(args):
+    """Profiling case for ncu: builds the batch, settles it for --settle steps (CUDA graphs), then
+    runs two eager steps inside the NVTX range "profile" (select them with
+    `ncu --nvtx --nvtx-include profile/`). Prints the state sizes; no timing is reported."""
+    import torch  # noqa: PLC0415 - NVTX ranges
+
+    lib = G.Lib()
+    batch, nb = build_batch(lib, shard_seeds(0, 1, args.worlds), 0)
+    batch.step_timed(args.settle, DT, VI, PI)
+    lib.b2g_batch_set_graphs(batch.h, 0)
+    torch.cuda.nvtx.range_push("profile")
+    for _ in range(2):
+        batch.step(DT, VI, PI)
+    torch.cuda.synchronize()
+    torch.cuda.nvtx.range_pop()
+    p = batch.profile()
+    print(json.dumps({"profile_window": {"worlds": args.worlds, "settle_steps": args.settle, "bodies": nb,
+                                         "fixtures": p.fixtures, "contacts": p.contacts, "touching": p.touching,
+                                         "joints": p.joints, "colors_max": p.colors_max}}))
+    batch.close()
 
 
 def main():
@@ -398,7 +435,13 @@ def main():
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--serve-seconds", type=float, default=12.0)
+    ap.add_argument("--profile-window", action="store_true",
+                    help="ncu case: settle --settle steps, then 2 steps inside the NVTX range 'profile'")
+    ap.add_argument("--settle", type=int, default=250)
     args = ap.parse_args()
+    if args.profile_window:
+        profile_window(args)
+        return
     args.warmup = max(args.warmup, 3)
     rank = int(os.environ.get("RANK", "0"))
     world_size = int(os.environ.get("WORLD_SIZE", "1"))
