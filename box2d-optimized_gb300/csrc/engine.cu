@@ -133,7 +133,7 @@ static KernelArgs make_args(Batch* b) {
   a.sp.idx = b->sp_idx.p; a.sp.lcs = b->sp_lcs.p; a.sp.lnp = b->sp_lnp.p; a.sp.lps = b->sp_lps.p;
   a.sp.rad = b->sp_rad.p;
   a.cready = b->cready.p; a.inc_cnt = b->inc_cnt.p; a.inc_head = b->inc_head.p;
-  a.inc_mask = b->inc_mask.p; a.inc_list = b->inc_list.p; a.jinc_list = b->jinc_list.p; a.jcb = b->jcb.p;
+  a.inc_mask = b->inc_mask.p; a.inc_list = b->inc_list.p; a.jinc_list = b->jinc_list.p; a.cwork = b->cwork.p; a.jwork = b->jwork.p; a.jcb = b->jcb.p;
   a.jcol = b->jcol.p; a.jorder = b->jorder.p; a.jranges = b->jranges.p; a.jprio = b->jprio.p;
   a.jready = b->jready.p; a.ncolors = b->ncolors.p;
   a.events = b->events.p; a.event_cap = b->event_cap; a.events_on = b->events_on ? 1 : 0;
@@ -330,7 +330,7 @@ int upload_all(Batch* b) {
   b->poff_valid[0] = b->poff_valid[1] = false;
   TRY(ensure(b, b->cub_tmp, cub_temp_bytes(NF)));
   TRY(ensure(b, b->inc_cnt, NB)); TRY(ensure(b, b->inc_head, NB)); TRY(ensure(b, b->inc_mask, NB));
-  TRY(ensure(b, b->jinc_list, 2 * (size_t)NJ)); TRY(ensure(b, b->jcol, NJ)); TRY(ensure(b, b->jorder, NJ));
+  TRY(ensure(b, b->jinc_list, 2 * (size_t)NJ)); TRY(ensure(b, b->jwork, 2 * (size_t)NJ)); TRY(ensure(b, b->jcol, NJ)); TRY(ensure(b, b->jorder, NJ));
   TRY(ensure(b, b->jcb, NJ)); TRY(ensure(b, b->jprio, NJ)); TRY(ensure(b, b->jready, NJ));
   TRY(ensure(b, b->status, 1)); TRY(ensure(b, b->counters, 5));
   b->NW = NW; b->NB = NB; b->NF = NF; b->NJ = NJ; b->NC = NC;
@@ -482,7 +482,7 @@ int upload_tail(Batch* b) {
   TRY(ensure(b, b->pslots, 8 * (size_t)NF));
   TRY(ensure(b, b->cub_tmp, cub_temp_bytes(NF)));
   TRY(ensure(b, b->inc_cnt, NB)); TRY(ensure(b, b->inc_head, NB)); TRY(ensure(b, b->inc_mask, NB));
-  TRY(ensure(b, b->jinc_list, 2 * (size_t)NJ)); TRY(ensure(b, b->jcol, NJ, true)); TRY(ensure(b, b->jorder, NJ, true));
+  TRY(ensure(b, b->jinc_list, 2 * (size_t)NJ)); TRY(ensure(b, b->jwork, 2 * (size_t)NJ)); TRY(ensure(b, b->jcol, NJ, true)); TRY(ensure(b, b->jorder, NJ, true));
   TRY(ensure(b, b->jcb, NJ, true)); TRY(ensure(b, b->jprio, NJ, true)); TRY(ensure(b, b->jready, NJ));
   b->NW = NW; b->NB = NB; b->NF = NF; b->NJ = NJ;
   CUDA_TRY(b, cudaMemsetAsync(b->status.p, 0, sizeof(unsigned int), b->stream));
@@ -592,7 +592,7 @@ static int ensure_contact_capacity(Batch* b, int64_t want) {
   TRY(ensure(b, b->pairs, (size_t)cap));
   TRY(ensure(b, b->sc_list, (size_t)cap)); TRY(ensure(b, b->scb, (size_t)cap)); TRY(ensure(b, b->cslot, (size_t)cap)); TRY(ensure(b, b->ccol, (size_t)cap));
   TRY(ensure(b, b->corder, (size_t)cap)); TRY(ensure(b, b->cprio, (size_t)cap)); TRY(ensure(b, b->cready, (size_t)cap));
-  TRY(ensure(b, b->inc_list, 2 * (size_t)cap));
+  TRY(ensure(b, b->inc_list, 2 * (size_t)cap)); TRY(ensure(b, b->cwork, 2 * (size_t)cap));
   TRY(ensure(b, b->sp_nf, (size_t)cap)); TRY(ensure(b, b->sp_cid, (size_t)cap)); TRY(ensure(b, b->sp_r0, (size_t)cap));
   TRY(ensure(b, b->sp_r1, (size_t)cap)); TRY(ensure(b, b->sp_nmtm, (size_t)cap)); TRY(ensure(b, b->sp_bk, (size_t)cap));
   TRY(ensure(b, b->sp_kn, (size_t)cap)); TRY(ensure(b, b->sp_imp, (size_t)cap)); TRY(ensure(b, b->sp_idx, (size_t)cap));
@@ -949,7 +949,7 @@ B2G_API int b2g_batch_destroy(b2g_batch* b) {
   release(b, b->naabb); release(b, b->ncbox); release(b, b->laabb); release(b, b->fattr); release(b, b->nflag); release(b, b->wroot); release(b, b->pcount); release(b, b->pslots); release(b, b->poffB[0]); release(b, b->poffB[1]); release(b, b->pairs);
   release(b, b->cub_tmp); release(b, b->status); release(b, b->counters); release(b, b->sc_list); release(b, b->scb); release(b, b->cslot); release(b, b->frad);
   release(b, b->ccol); release(b, b->corder); release(b, b->cprio); release(b, b->cready); release(b, b->inc_cnt);
-  release(b, b->inc_head); release(b, b->inc_mask); release(b, b->inc_list);
+  release(b, b->inc_head); release(b, b->inc_mask); release(b, b->inc_list); release(b, b->cwork); release(b, b->jwork);
   release(b, b->sp_nf); release(b, b->sp_cid); release(b, b->sp_r0); release(b, b->sp_r1); release(b, b->sp_nmtm);
   release(b, b->sp_bk); release(b, b->sp_kn); release(b, b->sp_imp); release(b, b->sp_idx); release(b, b->sp_lcs);
   release(b, b->sp_lnp); release(b, b->sp_lps); release(b, b->sp_rad);

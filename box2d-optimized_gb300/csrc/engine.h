@@ -193,6 +193,7 @@ struct Batch {
   DBuf<unsigned long long> inc_mask;
   DBuf<int> inc_list;             // 2 entries per constraint (contacts), world base 2*contact_off
   DBuf<int> jinc_list;            // 2 entries per joint
+  DBuf<int> cwork, jwork;         // colouring worklists, 2 entries per contact / joint
   DBuf<int2> jcb;
   DBuf<int8_t> jcol;
   DBuf<int> jorder, jranges;

@@ -66,6 +66,8 @@ struct ColourMem {
   const int2* cb;            // per constraint: world-local bodies, negative (bit 31 set) = static
   int8_t* col;               // per constraint: colour, -1 until coloured
   uint8_t* rdy;              // per constraint: ready in the current round
+  int* wl0;                  // worklists of uncoloured constraints (n entries each)
+  int* wl1;
 };
 
 // Greedy colouring in priority order, computed in parallel rounds (Jones-Plassmann with
@@ -131,42 +133,69 @@ __device__ int colour_constraints(int n, int nb, const ColourMem m, const uint32
     }
   }
   __syncthreads();
-  // rounds: every round colours at least the uncoloured constraint of lowest (priority, index)
-  bool done = false;
-  for (int round = 0; round <= n + 1; ++round) {
-    int any = 0;
-    for (int k = threadIdx.x; k < n; k += T) {
-      uint8_t r = 0;
-      if (m.col[k] < 0) {
-        any = 1;
-        int2 b = m.cb[k];
-        bool ok = (b.x < 0 || m.list[m.head[b.x]] == k) && (b.y < 0 || m.list[m.head[b.y]] == k);
-        r = ok ? 1 : 0;
-      }
-      m.rdy[k] = r;
-    }
-    if (!__syncthreads_or(any)) {
-      done = true;
-      break;
-    }
-    for (int k = threadIdx.x; k < n; k += T) {
-      if (!m.rdy[k]) continue;
+  // rounds over a worklist of the uncoloured constraints: a round colours every constraint that
+  // heads the priority lists of all its non-static bodies (at least the uncoloured one of lowest
+  // (priority, index)); the others form the next round's worklist (their order is immaterial)
+  __shared__ int s_m, s_next;
+  if (threadIdx.x == 0) {
+    s_m = n;
+    s_next = 0;
+  }
+  __syncthreads();
+  int* wl = m.wl0;
+  int* wn = m.wl1;
+  bool done = (n == 0);
+  for (int round = 0; round <= n + 1 && !done; ++round) {
+    const int cnt = s_m;
+    for (int i = threadIdx.x; i < cnt; i += T) {
+      int k = round == 0 ? i : wl[i];
       int2 b = m.cb[k];
-      unsigned long long used = (b.x >= 0 ? m.mask[b.x] : 0ull) | (b.y >= 0 ? m.mask[b.y] : 0ull);
-      unsigned long long freeBits = ~used & ((1ull << 63) - 1ull);
-      int c;
-      if (freeBits == 0ull) {
-        c = 63;
-      } else {
-        c = __ffsll((long long)freeBits) - 1;
-        if (b.x >= 0) m.mask[b.x] |= 1ull << c;
-        if (b.y >= 0) m.mask[b.y] |= 1ull << c;
-      }
-      m.col[k] = (int8_t)c;
-      if (b.x >= 0) m.head[b.x] += 1;
-      if (b.y >= 0) m.head[b.y] += 1;
+      bool ok = (b.x < 0 || m.list[m.head[b.x]] == k) && (b.y < 0 || m.list[m.head[b.y]] == k);
+      m.rdy[k] = ok ? 1 : 0;
     }
     __syncthreads();
+    for (int i0 = 0; i0 < cnt; i0 += T) {  // CTA-uniform trip count: whole warps reach the ballot
+      int i = i0 + threadIdx.x;
+      int k = -1;
+      bool keep = false;
+      if (i < cnt) {
+        k = round == 0 ? i : wl[i];
+        if (m.rdy[k]) {
+          int2 b = m.cb[k];
+          unsigned long long used = (b.x >= 0 ? m.mask[b.x] : 0ull) | (b.y >= 0 ? m.mask[b.y] : 0ull);
+          unsigned long long freeBits = ~used & ((1ull << 63) - 1ull);
+          int c;
+          if (freeBits == 0ull) {
+            c = 63;
+          } else {
+            c = __ffsll((long long)freeBits) - 1;
+            if (b.x >= 0) m.mask[b.x] |= 1ull << c;
+            if (b.y >= 0) m.mask[b.y] |= 1ull << c;
+          }
+          m.col[k] = (int8_t)c;
+          if (b.x >= 0) m.head[b.x] += 1;
+          if (b.y >= 0) m.head[b.y] += 1;
+        } else {
+          keep = true;
+        }
+      }
+      unsigned bal = __ballot_sync(FULL_MASK, keep);
+      int lane = threadIdx.x & 31;
+      int base = 0;
+      if (lane == 0 && bal) base = atomicAdd(&s_next, __popc(bal));
+      base = __shfl_sync(FULL_MASK, base, 0);
+      if (keep) wn[base + __popc(bal & ((1u << lane) - 1u))] = k;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      s_m = s_next;
+      s_next = 0;
+    }
+    __syncthreads();
+    done = (s_m == 0);
+    int* t = wl;
+    wl = wn;
+    wn = t;
   }
   if (!done && threadIdx.x == 0) atomicOr(status, B2G_DEV_COLOR_ROUNDS);
   // bucket by colour
@@ -421,18 +450,22 @@ __global__ void __launch_bounds__(T, 1024 / T) k_solve(KernelArgs a, int first, 
     }
     int* list = bodySm ? (int*)sc.take(8 * (size_t)nsc) : nullptr;
     int2* cb = bodySm ? (int2*)sc.take(8 * (size_t)nsc) : nullptr;
+    int* wl = bodySm ? (int*)sc.take(8 * (size_t)nsc) : nullptr;
     int8_t* col = bodySm ? (int8_t*)sc.take((size_t)nsc) : nullptr;
     uint8_t* rdy = bodySm ? (uint8_t*)sc.take((size_t)nsc) : nullptr;
-    bool conSm = list && cb && col && rdy;
+    bool conSm = list && cb && wl && col && rdy;
     if (conSm) {
       for (int k = threadIdx.x; k < nsc; k += T) cb[k] = a.scb[c0 + k];
       __syncthreads();
       m.list = list; m.cb = cb; m.col = col; m.rdy = rdy;
+      m.wl0 = wl; m.wl1 = wl + nsc;
     } else {
       m.list = a.inc_list + 2 * (int64_t)c0;
       m.cb = a.scb + c0;
       m.col = a.ccol + c0;
       m.rdy = a.cready + c0;
+      m.wl0 = a.cwork + 2 * (int64_t)c0;
+      m.wl1 = a.cwork + 2 * (int64_t)c0 + nsc;
     }
     ncc = colour_constraints<T>(nsc, nb, m, a.cprio + c0, a.corder + c0, a.cslot + c0, cranges, a.status);
     if (conSm) {
@@ -666,6 +699,8 @@ __global__ void __launch_bounds__(T) k_joint_colour(KernelArgs a, int w0) {
   m.cb = a.jcb + j0;
   m.col = a.jcol + j0;
   m.rdy = a.jready + j0;
+  m.wl0 = a.jwork + 2 * (int64_t)j0;
+  m.wl1 = a.jwork + 2 * (int64_t)j0 + nj;
   int njc = colour_constraints<T>(nj, nb, m, a.jprio + j0, a.jorder + j0, nullptr, jr, a.status);
   for (int c = threadIdx.x; c <= njc; c += T) a.jranges[65 * (int64_t)w + c] = jr[c];
   if (threadIdx.x == 0) a.ncolors[4 * w + 1] = njc;
@@ -674,7 +709,7 @@ __global__ void __launch_bounds__(T) k_joint_colour(KernelArgs a, int w0) {
 // ---- launch planning
 // Class by world body count: threads per CTA and the dynamic shared memory that holds the
 // world's body state and inverse masses (24 B/body) and, room permitting, its colouring arrays
-// (about 52 B/body at two contacts per body).
+// (16 B/body + 26 B per contact, about 68 B/body at two contacts per body).
 static const int kClassMaxBodies[B2G_SOLVE_CLASSES] = {64, 256, 1024, 4096, 1 << 30};
 static const int kClassThreads[B2G_SOLVE_CLASSES] = {64, 128, 256, 512, 1024};
 static const int kClassSmemCap[B2G_SOLVE_CLASSES] = {16 << 10, 24 << 10, 56 << 10, 110 << 10, 200 << 10};
@@ -693,7 +728,7 @@ std::vector<SolveClass> plan_solve_classes(const std::vector<int>& order, const 
       ++i;
     }
     if (i == start) continue;
-    int64_t need = 52ll * nbmax;
+    int64_t need = 68ll * nbmax;  // colouring at two contacts per body: 16 + 2 x 26 B per body
     need = (need + 15) & ~15ll;
     int smem = (int)(need < kClassSmemCap[c] ? need : kClassSmemCap[c]);
     out.push_back({start, i - start, kClassThreads[c], smem});
