@@ -282,20 +282,40 @@ def run_ours(args, rank, world_size):
     lib = G.Lib()
     dev = int(os.environ.get("LOCAL_RANK", "0"))
     seeds = shard_seeds(rank, world_size, args.worlds)
+    # autotune the solver's threads per world on a settled sample of the same worlds (every 8th);
+    # results do not depend on the choice, so the timed batch just takes it
+    threads, tune_s = None, 0.0
+    if not args.no_autotune:
+        t0 = time.time()
+        sample, _ = build_batch(lib, seeds[::8], dev)
+        sample.step_timed(100, DT, VI, PI)
+        threads, _ = sample.autotune(steps=3, dt=DT, vi=VI, pi=PI)
+        sample.close()
+        tune_s = time.time() - t0
     t0 = time.time()
     batch, nb = build_batch(lib, seeds, dev)
+    if threads:
+        batch.solver_threads(threads)
+    batch_threads = batch.solver_threads()
     build_s = time.time() - t0
     # warm-up (includes the first upload and contact creation)
     batch.step_timed(args.warmup, DT, VI, PI)
     prof_w = batch.profile()
     if world_size > 1:
         torch.distributed.barrier()
+    touching0 = batch.profile().touching_total
     with ClockSampler(dev) as clocks:
         ms = batch.step_timed(args.steps, DT, VI, PI)
     prof = batch.profile()
+    touching_window = prof.touching_total - touching0
     ms_per_step = ms / args.steps
-    ms_per_step, nb_all = reduce_over_ranks(ms_per_step, nb, f"cuda:{dev}")
+    ms_per_step_own = ms_per_step
+    ms_per_step, nb_all = reduce_over_ranks(ms_per_step_own, nb, f"cuda:{dev}")
+    _, touching_all = reduce_over_ranks(ms_per_step_own, touching_window, f"cuda:{dev}")
     value = nb_all / (ms_per_step / 1e3)
+    # contact-constraint iterations: solver contacts of every timed step x (velocity + position
+    # iterations), per second of the whole job
+    contact_iters = touching_all * (VI + PI) / (ms_per_step * args.steps / 1e3)
 
     # end to end through the C ABI with pinned host buffers: forces in, transforms out
     nbody = prof.bodies
@@ -378,7 +398,10 @@ def run_ours(args, rank, world_size):
                        "worlds": args.worlds * world_size, "bodies": int(nb_all), "fixtures_per_gpu": prof.fixtures,
                        "contacts_per_gpu": prof.contacts, "touching_per_gpu": prof.touching,
                        "joints_per_gpu": prof.joints, "l2": "state larger than L2 (no flush needed)",
-                       "parallelism": f"{world_size} independent world shards", "build_s": round(build_s, 1)},
+                       "parallelism": f"{world_size} independent world shards", "build_s": round(build_s, 1),
+                       "solver_threads_per_class": batch_threads,
+                       "autotune": (f"threads per world for size classes <=64/256/1024/4096/more bodies, tuned on "
+                                    f"every 8th world after 100 steps in {tune_s:.1f} s") if threads else "off"},
             "breakdown_ms": {"collide": prof.collide, "solve": prof.solve, "broadphase": prof.broadphase,
                              "step": prof.step},
             "step_bytes": step_b, "step_gbs": step_b / (ms_per_step / 1e3) / 1e9,
@@ -392,6 +415,7 @@ def run_ours(args, rank, world_size):
             "e2e": {"value": e2e_value, "unit": "body-steps/s", "h2d_bytes_per_step": 16 * nbody,
                     "d2h_bytes_per_step": 16 * nbody, "steps": e2e_steps},
             "gpu_launches": kernels_per_step * args.steps,
+            "contact_constraint_iterations_per_s": contact_iters,
             "clocks": clocks.summary(),
         }
     batch.close()
@@ -435,6 +459,7 @@ def main():
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--serve-seconds", type=float, default=12.0)
+    ap.add_argument("--no-autotune", action="store_true", help="keep the default solver threads per world")
     ap.add_argument("--profile-window", action="store_true",
                     help="ncu case: settle --settle steps, then 2 steps inside the NVTX range 'profile'")
     ap.add_argument("--settle", type=int, default=250)

@@ -117,7 +117,7 @@ class Profile(C.Structure):
     _fields_ = [("step", C.c_float), ("collide", C.c_float), ("solve", C.c_float),
                 ("broadphase", C.c_float), ("solve_toi", C.c_float), ("bodies", C.c_int64),
                 ("fixtures", C.c_int64), ("contacts", C.c_int64), ("touching", C.c_int64),
-                ("joints", C.c_int64), ("colors_max", C.c_int64)]
+                ("joints", C.c_int64), ("colors_max", C.c_int64), ("touching_total", C.c_int64)]
 
 
 class RequestResult(C.Structure):
@@ -207,7 +207,8 @@ class Lib:
         "b2g_batch_create", "b2g_batch_destroy", "b2g_world_add", "b2g_world_count",
         "b2g_world_set_gravity", "b2g_world_set_flags", "b2g_bodies_add", "b2g_fixtures_add",
         "b2g_joints_add", "b2g_world_sizes", "b2g_step", "b2g_step_n", "b2g_step_timed",
-        "b2g_batch_set_forces", "b2g_batch_set_graphs", "b2g_world_retire", "b2g_compact", "b2g_debug_set_contact_capacity",
+        "b2g_batch_set_forces", "b2g_batch_set_graphs", "b2g_batch_set_solver_threads",
+        "b2g_batch_get_solver_threads", "b2g_batch_autotune", "b2g_world_retire", "b2g_compact", "b2g_debug_set_contact_capacity",
         "b2g_pairs_static", "b2g_reserve",
         "b2g_bodies_read", "b2g_bodies_write", "b2g_batch_read_states", "b2g_fixtures_read",
         "b2g_joints_read", "b2g_contacts_read", "b2g_events_enable", "b2g_events_drain",
@@ -257,6 +258,9 @@ class Lib:
             "b2g_events_enable": ([vp, i32], C.c_int),
             "b2g_events_drain": ([vp, P(Event), i32, P(i32)], C.c_int),
             "b2g_profile_get": ([vp, P(Profile)], C.c_int),
+            "b2g_batch_set_solver_threads": ([vp, P(i32)], C.c_int),
+            "b2g_batch_get_solver_threads": ([vp, P(i32)], C.c_int),
+            "b2g_batch_autotune": ([vp, i32, f32, i32, i32, P(i32), P(i32)], C.c_int),
             "b2g_solver_order": ([vp, i32, P(i32), P(u32), i32, P(i32), P(u32), i32], C.c_int),
             "b2g_collide": ([vp, vp, vp, vp, i32, vp, vp], C.c_int),
             "b2g_pairs": ([vp, i32, vp, i64, P(i64), vp], C.c_int),
@@ -380,6 +384,24 @@ class Batch:
         self.lib.check(self.lib.b2g_contacts_read(self.h, world, arr, n.value, C.byref(n)),
                        "b2g_contacts_read")
         return arr[:n.value]
+
+    def solver_threads(self, threads=None):
+        """Threads per world CTA of the solver for the five size classes (sets when given)."""
+        arr = (C.c_int32 * 5)()
+        if threads is not None:
+            arr = (C.c_int32 * 5)(*threads)
+            self.lib.check(self.lib.b2g_batch_set_solver_threads(self.h, arr), "b2g_batch_set_solver_threads")
+        self.lib.check(self.lib.b2g_batch_get_solver_threads(self.h, arr), "b2g_batch_get_solver_threads")
+        return list(arr)
+
+    def autotune(self, steps=3, dt=1 / 60, vi=8, pi=3):
+        """Picks the solver's threads per world for each size class by timing real steps;
+        returns (threads per class, steps taken)."""
+        arr = (C.c_int32 * 5)()
+        taken = C.c_int32()
+        self.lib.check(self.lib.b2g_batch_autotune(self.h, steps, dt, vi, pi, arr, C.byref(taken)),
+                       "b2g_batch_autotune")
+        return list(arr), taken.value
 
     def solver_order(self, world, nc, nj):
         cc = (C.c_int32 * max(nc, 1))()

@@ -152,6 +152,13 @@ static uint64_t emitter_key(const HostWorld& w, int fo, int fa, int fb) {
   return ((uint64_t)(uint32_t)(e + fo) << 32) | (uint32_t)(p + fo);
 }
 
+// Solver launch classes from the world order and the per-class thread counts.
+static void replan_solver(Batch* b) {
+  std::vector<int> nbw(b->worlds.size());
+  for (size_t w = 0; w < b->worlds.size(); ++w) nbw[w] = (int)b->worlds[w].bodies.size();
+  b->solve_classes = plan_solve_classes(b->h_world_order, nbw, b->class_threads);
+}
+
 // Solver constraints address bodies by a 24-bit world-local index.
 static const size_t kMaxWorldBodies = size_t(1) << 24;
 
@@ -287,11 +294,8 @@ int upload_all(Batch* b) {
   std::iota(order.begin(), order.end(), 0);
   std::stable_sort(order.begin(), order.end(),
                    [&](int x, int y) { return b->worlds[x].bodies.size() > b->worlds[y].bodies.size(); });
-  {
-    std::vector<int> nbw(NW);
-    for (int w = 0; w < NW; ++w) nbw[w] = (int)b->worlds[w].bodies.size();
-    b->solve_classes = plan_solve_classes(order, nbw);
-  }
+  b->h_world_order = order;
+  replan_solver(b);
   TRY(upload(b, b->wb, wb)); TRY(upload(b, b->wj, wj)); TRY(upload(b, b->wg, wg)); TRY(upload(b, b->wflags, wflags));
   TRY(upload(b, b->world_order, order));
   // per-world live contact ranges: the sorted contact list groups by world (keys hold global
@@ -452,11 +456,8 @@ int upload_tail(Batch* b) {
   std::iota(order.begin(), order.end(), 0);
   std::stable_sort(order.begin(), order.end(),
                    [&](int x, int y) { return b->worlds[x].bodies.size() > b->worlds[y].bodies.size(); });
-  {
-    std::vector<int> nbw(NW);
-    for (int w = 0; w < NW; ++w) nbw[w] = (int)b->worlds[w].bodies.size();
-    b->solve_classes = plan_solve_classes(order, nbw);
-  }
+  b->h_world_order = order;
+  replan_solver(b);
   std::vector<int2> wc_tail(NW - w0, make_int2(0, 0));
   TRY(upload(b, b->wb, wb)); TRY(upload(b, b->wj, wj)); TRY(upload_at(b, b->wg, w0, wg_tail));
   TRY(upload(b, b->wflags, wflags)); TRY(upload(b, b->world_order, order)); TRY(upload_at(b, b->wc, w0, wc_tail));
@@ -733,6 +734,7 @@ static int finish_step(Batch* b, int live_before_last_bp) {
   b->NC = (int64_t)r[B2G_CNT_CONTACTS];
   TRY(drain_device_events(b, r[B2G_CNT_EVENTS]));
   b->profile.touching = (int64_t)r[B2G_CNT_TOUCHING];
+  b->profile.touching_total += (int64_t)r[B2G_CNT_TOUCHING];
   return check_status(b, status_word);
 }
 
@@ -956,6 +958,13 @@ B2G_API int b2g_batch_destroy(b2g_batch* b) {
   release(b, b->jinc_list); release(b, b->jcol); release(b, b->jorder); release(b, b->jcb); release(b, b->jranges);
   release(b, b->jprio); release(b, b->jready);
   release(b, b->ncolors); release(b, b->events);
+  {
+    Batch::Spare& sp = b->spare;
+    release(b, sp.xf); release(b, sp.pos); release(b, sp.vel); release(b, sp.massd); release(b, sp.damp);
+    release(b, sp.force); release(b, sp.fmat); release(b, sp.lc); release(b, sp.btype); release(b, sp.bworld);
+    release(b, sp.fbody); release(b, sp.fgroup); release(b, sp.fsensor); release(b, sp.fworld); release(b, sp.tables);
+    release(b, sp.shape); release(b, sp.ffilter); release(b, sp.frad); release(b, sp.joints);
+  }
   for (int i = 0; i < B2G_SOLVE_CLASSES; ++i) {
     if (b->side[i]) cudaStreamDestroy(b->side[i]);
     if (b->fork_ev[i]) cudaEventDestroy(b->fork_ev[i]);
@@ -1005,9 +1014,137 @@ B2G_API int b2g_world_retire(b2g_batch* b, int32_t world) {
   return B2G_OK;
 }
 
+// Device compaction of a batch whose device layout is current: kept worlds move down in every
+// array (compact.cu), the small world table and the joint-no-collide list are rebuilt on the
+// host, and the joint colouring is recomputed; no body, fixture or contact state crosses the bus.
+static int compact_device(Batch* b, int32_t* old_to_new, int32_t n) {
+  CUDA_TRY(b, cudaSetDevice(b->device));
+  cudaStream_t s = b->stream;
+  const int NW = b->NW;
+  std::vector<int2> wc(NW);
+  std::vector<float4> wg(NW);
+  if (NW > 0) {
+    CUDA_TRY(b, cudaMemcpyAsync(wc.data(), b->wc.p, NW * sizeof(int2), cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(b, cudaMemcpyAsync(wg.data(), b->wg.p, NW * sizeof(float4), cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(b, cudaStreamSynchronize(s));
+  }
+  // per old world: new index and offsets; tables packed as off_old | off_new | wnew | con_old | con_new
+  std::vector<int> tab(11 * (size_t)std::max(NW, 1), 0);
+  int4* off_old = reinterpret_cast<int4*>(tab.data());
+  int4* off_new = off_old + NW;
+  int* wnew = tab.data() + 8 * (size_t)NW;
+  int* con_old = wnew + NW;
+  int* con_new = con_old + NW;
+  int NB2 = 0, NF2 = 0, NJ2 = 0, kept = 0;
+  int64_t NC2 = 0;
+  for (int w = 0; w < NW; ++w) {
+    const HostWorld& hw = b->worlds[w];
+    off_old[w] = make_int4(b->h_body_off[w], b->h_fix_off[w], b->h_joint_off[w], 0);
+    wnew[w] = -1;
+    if (hw.flags & B2G_WF_RETIRED) continue;
+    wnew[w] = kept++;
+    off_new[w] = make_int4(NB2, NF2, NJ2, 0);
+    con_old[w] = wc[w].x;
+    con_new[w] = (int)NC2;
+    NB2 += (int)hw.bodies.size();
+    NF2 += (int)hw.fixtures.size();
+    NJ2 += (int)hw.joints.size();
+    NC2 += wc[w].y;
+  }
+  TRY(upload(b, b->spare.tables, tab));
+  const int* tp = b->spare.tables.p;
+  CompactTables t{tp + 8 * (size_t)NW, reinterpret_cast<const int4*>(tp), reinterpret_cast<const int4*>(tp) + NW,
+                  tp + 9 * (size_t)NW, tp + 10 * (size_t)NW};
+  Batch::Spare& sp = b->spare;
+  TRY(ensure(b, sp.xf, NB2)); TRY(ensure(b, sp.pos, NB2)); TRY(ensure(b, sp.vel, NB2)); TRY(ensure(b, sp.massd, NB2));
+  TRY(ensure(b, sp.damp, NB2)); TRY(ensure(b, sp.force, NB2)); TRY(ensure(b, sp.lc, NB2));
+  TRY(ensure(b, sp.btype, NB2)); TRY(ensure(b, sp.bworld, NB2));
+  TRY(ensure(b, sp.shape, NF2)); TRY(ensure(b, sp.fbody, NF2)); TRY(ensure(b, sp.fgroup, NF2));
+  TRY(ensure(b, sp.fsensor, NF2)); TRY(ensure(b, sp.fworld, NF2)); TRY(ensure(b, sp.ffilter, NF2));
+  TRY(ensure(b, sp.fmat, NF2)); TRY(ensure(b, sp.frad, NF2)); TRY(ensure(b, sp.joints, NJ2));
+  BodyRecs sb{b->xf.p, b->pos.p, b->vel.p, b->massd.p, b->damp.p, b->force.p, b->lc.p, b->btype.p, b->bworld.p};
+  BodyRecs db{sp.xf.p, sp.pos.p, sp.vel.p, sp.massd.p, sp.damp.p, sp.force.p, sp.lc.p, sp.btype.p, sp.bworld.p};
+  FixRecs sf{b->shape.p, b->fbody.p, b->fgroup.p, b->fsensor.p, b->fworld.p, b->ffilter.p, b->fmat.p, b->frad.p};
+  FixRecs df{sp.shape.p, sp.fbody.p, sp.fgroup.p, sp.fsensor.p, sp.fworld.p, sp.ffilter.p, sp.fmat.p, sp.frad.p};
+  const int c = b->cur, d = c ^ 1;  // the live list moves into the other (scratch) contact buffer
+  ConRecs sc{b->ckey[c].p, b->cfix[c].p, b->cflags[c].p, b->cmat[c].p, b->cman[c].p};
+  ConRecs dc{b->ckey[d].p, b->cfix[d].p, b->cflags[d].p, b->cmat[d].p, b->cman[d].p};
+  launch_compact(t, b->NB, sb, db, b->NF, sf, df, b->NJ, b->joints.p, sp.joints.p, b->NC, sc, dc, s);
+  CUDA_TRY(b, cudaGetLastError());
+  std::swap(b->xf, sp.xf); std::swap(b->pos, sp.pos); std::swap(b->vel, sp.vel); std::swap(b->massd, sp.massd);
+  std::swap(b->damp, sp.damp); std::swap(b->force, sp.force); std::swap(b->lc, sp.lc);
+  std::swap(b->btype, sp.btype); std::swap(b->bworld, sp.bworld);
+  std::swap(b->shape, sp.shape); std::swap(b->fbody, sp.fbody); std::swap(b->fgroup, sp.fgroup);
+  std::swap(b->fsensor, sp.fsensor); std::swap(b->fworld, sp.fworld); std::swap(b->ffilter, sp.ffilter);
+  std::swap(b->fmat, sp.fmat); std::swap(b->frad, sp.frad); std::swap(b->joints, sp.joints);
+  b->cur = d;
+  // host records and the world table
+  std::vector<HostWorld> keep;
+  keep.reserve(kept);
+  std::vector<int4> wb(kept), wj(kept);
+  std::vector<float4> wg2(kept);
+  std::vector<int2> wc2(kept);
+  std::vector<int> wflags(kept);
+  for (int w = 0; w < (int)b->worlds.size(); ++w) {
+    int to = w < NW ? wnew[w] : -1;
+    if (w < n) old_to_new[w] = to;
+    if (to < 0) continue;
+    HostWorld& hw = b->worlds[w];
+    wb[to] = make_int4(off_new[w].x, (int)hw.bodies.size(), off_new[w].y, (int)hw.fixtures.size());
+    wj[to] = make_int4(off_new[w].z, (int)hw.joints.size(), 0, 0);
+    wg2[to] = wg[w];
+    wc2[to] = make_int2(con_new[w], wc[w].y);
+    wflags[to] = hw.flags & ~(B2G_WF_ACTIVE | B2G_WF_NEW_CONTACTS);
+    keep.push_back(std::move(hw));
+  }
+  b->worlds.swap(keep);
+  b->h_body_off.assign(kept + 1, 0);
+  b->h_fix_off.assign(kept + 1, 0);
+  b->h_joint_off.assign(kept + 1, 0);
+  std::vector<uint64_t> nocol;
+  for (int w = 0; w < kept; ++w) {
+    b->h_body_off[w] = wb[w].x; b->h_fix_off[w] = wb[w].z; b->h_joint_off[w] = wj[w].x;
+    for (const b2g_joint& j : b->worlds[w].joints) {
+      if (j.def.collide_connected) continue;
+      uint32_t x = (uint32_t)(wb[w].x + j.def.body_a), y = (uint32_t)(wb[w].x + j.def.body_b);
+      if (x > y) std::swap(x, y);
+      nocol.push_back(((uint64_t)x << 32) | y);
+    }
+  }
+  b->h_body_off[kept] = NB2; b->h_fix_off[kept] = NF2; b->h_joint_off[kept] = NJ2;
+  std::sort(nocol.begin(), nocol.end());
+  nocol.erase(std::unique(nocol.begin(), nocol.end()), nocol.end());
+  TRY(upload(b, b->wb, wb)); TRY(upload(b, b->wj, wj)); TRY(upload(b, b->wg, wg2)); TRY(upload(b, b->wc, wc2));
+  TRY(upload(b, b->wflags, wflags)); TRY(upload(b, b->nocollide, nocol));
+  b->n_nocollide = (int)nocol.size();
+  std::vector<int> order(kept);
+  std::iota(order.begin(), order.end(), 0);
+  std::stable_sort(order.begin(), order.end(),
+                   [&](int x, int y) { return b->worlds[x].bodies.size() > b->worlds[y].bodies.size(); });
+  TRY(upload(b, b->world_order, order));
+  b->h_world_order = order;
+  b->NW = kept; b->NB = NB2; b->NF = NF2; b->NJ = NJ2; b->NC = NC2;
+  replan_solver(b);
+  {
+    unsigned long long cnt = (unsigned long long)NC2;
+    CUDA_TRY(b, cudaMemcpyAsync(b->counters.p, &cnt, sizeof(cnt), cudaMemcpyHostToDevice, s));
+  }
+  b->h_wflags = wflags;
+  b->poff_valid[0] = b->poff_valid[1] = false;
+  b->last_solve_buf = -1;
+  CUDA_TRY(b, cudaMemsetAsync(b->status.p, 0, sizeof(unsigned int), s));
+  launch_joint_colour(make_args(b), 0, kept, s);
+  TRY(check_upload_status(b));
+  b->layout_version++;
+  return B2G_OK;
+}
+
 // Removes retired worlds; old_to_new[w] receives each world's new index (-1 if removed).
 B2G_API int b2g_compact(b2g_batch* b, int32_t* old_to_new, int32_t n) {
   if (!b || (n > 0 && !old_to_new)) return B2G_E_INVALID_ARG;
+  if (b->device >= 0 && b->device_state_valid && !b->structure_dirty && (int)b->worlds.size() == b->NW &&
+      b->NW > 0)
+    return compact_device(b, old_to_new, n);
   TRY(download_state(b));
   std::vector<HostWorld> keep;
   int nw = (int)b->worlds.size();
@@ -1209,6 +1346,82 @@ B2G_API int b2g_batch_set_graphs(b2g_batch* b, int32_t enable) {
   if (!b) return B2G_E_INVALID_ARG;
   b->use_graphs = enable != 0;
   return B2G_OK;
+}
+
+B2G_API int b2g_batch_set_solver_threads(b2g_batch* b, const int32_t* threads) {
+  if (!b || !threads) return B2G_E_INVALID_ARG;
+  for (int c = 0; c < B2G_SOLVE_CLASSES; ++c)
+    if (!solver_threads_valid(threads[c])) return B2G_E_INVALID_ARG;
+  for (int c = 0; c < B2G_SOLVE_CLASSES; ++c) b->class_threads[c] = threads[c];
+  if (!b->h_world_order.empty()) {
+    replan_solver(b);
+    b->layout_version++;  // captured graphs hold the old launch shapes
+  }
+  return B2G_OK;
+}
+
+B2G_API int b2g_batch_get_solver_threads(b2g_batch* b, int32_t* threads) {
+  if (!b || !threads) return B2G_E_INVALID_ARG;
+  for (int c = 0; c < B2G_SOLVE_CLASSES; ++c) threads[c] = b->class_threads[c];
+  return B2G_OK;
+}
+
+// Median device time of the solver over `steps` eager steps (real steps: the worlds advance).
+static int time_solver(Batch* b, int steps, float dt, int vi, int pi, float* ms, int* taken) {
+  std::vector<float> t;
+  for (int i = 0; i < steps; ++i) {
+    TRY(step_batch(b, dt, vi, pi, nullptr, true));
+    ++*taken;
+    t.push_back(b->profile.solve);
+  }
+  std::sort(t.begin(), t.end());
+  *ms = t.empty() ? 0.0f : t[t.size() / 2];
+  return B2G_OK;
+}
+
+B2G_API int b2g_batch_autotune(b2g_batch* b, int32_t steps, float dt, int32_t vi, int32_t pi, int32_t* threads_out,
+                               int32_t* steps_taken) {
+  if (!b || steps < 1 || !(dt > 0.0f) || vi < 0 || pi < 0 || b->device < 0) return B2G_E_INVALID_ARG;
+  bool graphs = b->use_graphs;
+  b->use_graphs = false;  // eager steps carry the per-phase events
+  int st = B2G_OK;
+  int taken = 0;
+  if (b->structure_dirty || (int)b->worlds.size() > b->NW) {
+    st = step_batch(b, dt, vi, pi, nullptr, true);
+    ++taken;
+  }
+  // coordinate descent, largest worlds first: each class tries half and double its threads
+  for (int c = B2G_SOLVE_CLASSES - 1; c >= 0 && st == B2G_OK; --c) {
+    bool present = false;
+    for (const SolveClass& k : b->solve_classes) present = present || k.cls == c;
+    if (!present) continue;
+    int best = b->class_threads[c];
+    float best_ms = 0.0f;
+    st = time_solver(b, steps, dt, vi, pi, &best_ms, &taken);
+    for (int cand : {best / 2, best * 2}) {
+      if (st != B2G_OK || !solver_threads_valid(cand)) continue;
+      int keep = b->class_threads[c];
+      b->class_threads[c] = cand;
+      replan_solver(b);
+      float ms = 0.0f;
+      st = time_solver(b, steps, dt, vi, pi, &ms, &taken);
+      if (st == B2G_OK && ms < 0.97f * best_ms) {
+        best = cand;
+        best_ms = ms;
+      } else {
+        b->class_threads[c] = keep;
+        replan_solver(b);
+      }
+    }
+    b->class_threads[c] = best;
+    replan_solver(b);
+  }
+  b->layout_version++;
+  b->use_graphs = graphs;
+  if (threads_out)
+    for (int c = 0; c < B2G_SOLVE_CLASSES; ++c) threads_out[c] = b->class_threads[c];
+  if (steps_taken) *steps_taken = taken;
+  return st;
 }
 
 B2G_API int b2g_step_timed(b2g_batch* b, float dt, int32_t vi, int32_t pi, int32_t n, float* device_ms) {

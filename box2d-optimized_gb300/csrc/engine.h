@@ -94,6 +94,7 @@ struct Batch;
 // One solver launch over a contiguous range of the size-sorted world order.
 struct SolveClass {
   int first, count, threads, smem;
+  int cls;  // size class index
 };
 #define B2G_SOLVE_CLASSES 5
 
@@ -200,7 +201,20 @@ struct Batch {
   DBuf<uint32_t> jprio;
   DBuf<uint8_t> jready;
   DBuf<int> ncolors;              // per world: contact colours, joint colours, solver contacts, slot base
+  // compaction targets: swapped with the live arrays by a device compaction, kept for the next
+  struct Spare {
+    DBuf<float4> xf, pos, vel, massd, damp, force, fmat;
+    DBuf<float2> lc;
+    DBuf<int> btype, bworld, fbody, fgroup, fsensor, fworld, tables;
+    DBuf<b2g_shape> shape;
+    DBuf<uint32_t> ffilter;
+    DBuf<float> frad;
+    DBuf<JointDev> joints;
+  } spare;
+
   std::vector<SolveClass> solve_classes;
+  std::vector<int> h_world_order;  // worlds by body count, largest first (device world_order)
+  int class_threads[B2G_SOLVE_CLASSES] = {64, 128, 256, 512, 1024};
   cudaStream_t side[B2G_SOLVE_CLASSES] = {};
   cudaEvent_t fork_ev[B2G_SOLVE_CLASSES + 1] = {};
 

@@ -136,8 +136,43 @@ void launch_collide(const KernelArgs& a, cudaStream_t s);
 void launch_solve(const KernelArgs& a, const std::vector<SolveClass>& classes, cudaStream_t s,
                   const cudaStream_t* side, const cudaEvent_t* ev);
 void launch_joint_colour(const KernelArgs& a, int w0, int nw, cudaStream_t s);
+
+// ---- batch compaction (compact.cu)
+struct CompactTables {            // per old world
+  const int* wnew;                // new world index, -1 when removed
+  const int4* off_old;            // body, fixture, joint offsets in the old layout
+  const int4* off_new;            // ... and in the new one
+  const int* con_old;             // live contact range start, old and new
+  const int* con_new;
+};
+struct BodyRecs {
+  float4 *xf, *pos, *vel, *massd, *damp, *force;
+  float2* lc;
+  int *btype, *bworld;
+};
+struct FixRecs {
+  b2g_shape* shape;
+  int *fbody, *fgroup, *fsensor, *fworld;
+  uint32_t* ffilter;
+  float4* fmat;
+  float* frad;
+};
+struct ConRecs {
+  uint64_t* key;
+  int2* fix;
+  uint32_t* flags;
+  float4* mat;
+  b2g_manifold* man;
+};
+void launch_compact(const CompactTables& t, int nb, const BodyRecs& sb, const BodyRecs& db, int nf, const FixRecs& sf,
+                    const FixRecs& df, int nj, const JointDev* sj, JointDev* dj, int64_t nc, const ConRecs& sc,
+                    const ConRecs& dc, cudaStream_t s);
 void solver_setup();
-std::vector<SolveClass> plan_solve_classes(const std::vector<int>& order, const std::vector<int>& bodies);
+// Solver launches for worlds listed by body count, largest first, with the given threads per
+// CTA for each size class (at most 64, 256, 1024, 4096 and more bodies).
+std::vector<SolveClass> plan_solve_classes(const std::vector<int>& order, const std::vector<int>& bodies,
+                                           const int* class_threads);
+bool solver_threads_valid(int t);
 void launch_clear_forces(const KernelArgs& a, int nb, cudaStream_t s);
 void launch_bp_build(const KernelArgs& a, int nf, int nw, size_t cub_bytes, int sort_bits, cudaStream_t s);
 void launch_bp_emit(const KernelArgs& a, int nf, cudaStream_t s);

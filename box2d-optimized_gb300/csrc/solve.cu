@@ -711,10 +711,20 @@ __global__ void __launch_bounds__(T) k_joint_colour(KernelArgs a, int w0) {
 // world's body state and inverse masses (24 B/body) and, room permitting, its colouring arrays
 // (16 B/body + 26 B per contact, about 68 B/body at two contacts per body).
 static const int kClassMaxBodies[B2G_SOLVE_CLASSES] = {64, 256, 1024, 4096, 1 << 30};
-static const int kClassThreads[B2G_SOLVE_CLASSES] = {64, 128, 256, 512, 1024};
-static const int kClassSmemCap[B2G_SOLVE_CLASSES] = {16 << 10, 24 << 10, 56 << 10, 110 << 10, 200 << 10};
+// Shared-memory allowance by threads per CTA (64, 128, 256, 512, 1024): at 64 registers per
+// thread the SM holds 1024 / T such CTAs, and the allowance keeps that many resident.
+static const int kSmemCapByThreads[B2G_SOLVE_CLASSES] = {16 << 10, 24 << 10, 56 << 10, 110 << 10, 200 << 10};
 
-std::vector<SolveClass> plan_solve_classes(const std::vector<int>& order, const std::vector<int>& bodies) {
+static int threads_index(int t) {
+  int k = 0;
+  while (k + 1 < B2G_SOLVE_CLASSES && (64 << k) < t) ++k;
+  return k;
+}
+
+bool solver_threads_valid(int t) { return t == 64 || t == 128 || t == 256 || t == 512 || t == 1024; }
+
+std::vector<SolveClass> plan_solve_classes(const std::vector<int>& order, const std::vector<int>& bodies,
+                                           const int* class_threads) {
   // `order` lists worlds by body count, largest first: each class is a contiguous range
   std::vector<SolveClass> out;
   int n = (int)order.size();
@@ -730,15 +740,17 @@ std::vector<SolveClass> plan_solve_classes(const std::vector<int>& order, const 
     if (i == start) continue;
     int64_t need = 68ll * nbmax;  // colouring at two contacts per body: 16 + 2 x 26 B per body
     need = (need + 15) & ~15ll;
-    int smem = (int)(need < kClassSmemCap[c] ? need : kClassSmemCap[c]);
-    out.push_back({start, i - start, kClassThreads[c], smem});
+    int t = class_threads[c];
+    int cap = kSmemCapByThreads[threads_index(t)];
+    int smem = (int)(need < cap ? need : cap);
+    out.push_back({start, i - start, t, smem, c});
   }
   return out;
 }
 
 template <int T>
 static void set_smem_attr(int c) {
-  cudaFuncSetAttribute(k_solve<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, kClassSmemCap[c]);
+  cudaFuncSetAttribute(k_solve<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemCapByThreads[c]);
 }
 
 void solver_setup() {

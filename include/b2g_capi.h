@@ -242,6 +242,7 @@ typedef struct b2g_event {
 typedef struct b2g_profile {
   float step, collide, solve, broadphase, solve_toi;
   int64_t bodies, fixtures, contacts, touching, joints, colors_max;
+  int64_t touching_total; /* solver contacts summed over every step of the batch so far */
 } b2g_profile;
 
 /* ---- batch lifecycle ------------------------------------------------------------------------ */
@@ -305,6 +306,18 @@ B2G_API int b2g_batch_set_forces(b2g_batch* b, const float* f4, int64_t n_bodies
 /* Whether b2g_step replays the Step as a captured CUDA graph (default on). A graph is used for
  * unmasked steps with dt > 0 and events off; it is re-captured when buffers move. */
 B2G_API int b2g_batch_set_graphs(b2g_batch* b, int32_t enable);
+/* Threads per world CTA of the solver for each world size class (worlds of at most 64, 256,
+ * 1024 and 4096 bodies, and larger), 5 entries each one of 64, 128, 256, 512, 1024 (defaults
+ * 64, 128, 256, 512, 1024). A tuning knob: results do not depend on it. No reference counterpart. */
+B2G_API int b2g_batch_set_solver_threads(b2g_batch* b, const int32_t* threads);
+B2G_API int b2g_batch_get_solver_threads(b2g_batch* b, int32_t* threads);
+/* Autotuner: picks each size class's threads per world by timing the solver over `steps` eager
+ * steps per candidate (the class's current count, half and double), largest worlds first. The
+ * steps are real steps of the batch (its worlds advance; their number goes to steps_taken);
+ * results are bit-identical whatever it picks. Writes the chosen counts to threads_out (5
+ * entries) when not null. No reference counterpart. */
+B2G_API int b2g_batch_autotune(b2g_batch* b, int32_t steps, float dt, int32_t velocity_iterations,
+                               int32_t position_iterations, int32_t* threads_out, int32_t* steps_taken);
 /* Testing knob: sets the contact/pair buffer capacity to exactly `cap` (>= live contacts), so
  * that a later broadphase overflows and exercises the recovery path. */
 B2G_API int b2g_debug_set_contact_capacity(b2g_batch* b, int64_t cap);

@@ -161,6 +161,78 @@ def test_batched_equals_alone(lib):
     together.close()
 
 
+def _mixed_batch(lib, seeds, sizes):
+    b = G.Batch(lib, device=0)
+    ws = []
+    for s, n in zip(seeds, sizes):
+        _, gx, gy = _params(lib, s)
+        w = b.add_world(gx, gy)
+        b.set_flags(w)
+        b.scene(w, G.SCENE_BATCH_WORLD, seed=s, n=n)
+        ws.append(w)
+    return b, ws
+
+
+# one world in every solver size class (at most 64, 256, 1024, 4096 bodies, and larger)
+CLASS_SEEDS = [31, 32, 33, 34, 35, 36]
+CLASS_SIZES = [40, 200, 900, 3000, 5000, 60]
+
+
+def test_solver_threads_do_not_change_results(lib):
+    """Every world of every size class gives the same bits with 64 or 1024 threads per world (and
+    the shared-memory allowance that goes with each)."""
+    out = []
+    for threads in ([64] * 5, [1024] * 5, [128, 256, 512, 1024, 512]):
+        b, ws = _mixed_batch(lib, CLASS_SEEDS, CLASS_SIZES)
+        assert b.solver_threads(threads) == threads
+        for _ in range(30):
+            b.step(1 / 60, 8, 3)
+        out.append([_state_bytes(b.bodies(w)) for w in ws])
+        b.close()
+    assert out[0] == out[1] == out[2]
+
+
+def test_autotune_picks_valid_threads_and_keeps_results(lib):
+    tuned, ws = _mixed_batch(lib, CLASS_SEEDS, CLASS_SIZES)
+    threads, taken = tuned.autotune(steps=2)
+    assert all(t in (64, 128, 256, 512, 1024) for t in threads)
+    assert tuned.solver_threads() == threads and taken >= 2
+    for _ in range(10):
+        tuned.step(1 / 60, 8, 3)
+    plain, ws2 = _mixed_batch(lib, CLASS_SEEDS, CLASS_SIZES)
+    for _ in range(taken + 10):
+        plain.step(1 / 60, 8, 3)
+    for w, w2 in zip(ws, ws2):
+        assert _state_bytes(tuned.bodies(w)) == _state_bytes(plain.bodies(w2))
+    tuned.close()
+    plain.close()
+
+
+def test_device_compaction_equals_fresh_batch(lib):
+    """Retiring worlds and compacting the batch on the device leaves the kept worlds exactly as a
+    batch that never held the others (bodies, contacts and the steps after)."""
+    seeds, sizes = CLASS_SEEDS, CLASS_SIZES
+    big, ws = _mixed_batch(lib, seeds, sizes)
+    for _ in range(20):
+        big.step(1 / 60, 8, 3)
+    for w in (ws[1], ws[3]):
+        lib.check(lib.b2g_world_retire(big.h, w), "retire")
+    nmap = (C.c_int32 * len(ws))()
+    lib.check(lib.b2g_compact(big.h, nmap, len(ws)), "compact")
+    assert list(nmap) == [0, -1, 1, -1, 2, 3]
+    for _ in range(20):
+        big.step(1 / 60, 8, 3)
+    kept = [0, 2, 4, 5]
+    small, ws2 = _mixed_batch(lib, [seeds[i] for i in kept], [sizes[i] for i in kept])
+    for _ in range(40):
+        small.step(1 / 60, 8, 3)
+    for new, w2 in enumerate(ws2):
+        assert _state_bytes(big.bodies(new)) == _state_bytes(small.bodies(w2))
+        assert [_contact_key(x) for x in big.contacts(new)] == [_contact_key(y) for y in small.contacts(w2)]
+    big.close()
+    small.close()
+
+
 def test_masked_step_leaves_other_worlds(lib):
     b = G.Batch(lib, device=0)
     w0 = b.add_world(0, -10)
