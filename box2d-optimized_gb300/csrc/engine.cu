@@ -364,6 +364,48 @@ static int upload_at(Batch* b, DBuf<T>& buf, size_t off, const std::vector<T>& v
   return B2G_OK;
 }
 
+// Host -> device copies of host vectors through one pinned staging buffer: the copies are
+// asynchronous (no pageable-memory staging on the copy path) and the buffer is reused only once
+// the previous batch of copies has completed.
+struct Stager {
+  struct Item {
+    void* dst;
+    const void* src;
+    size_t bytes;
+  };
+  std::vector<Item> items;
+  size_t total = 0;
+  template <typename T>
+  int add(Batch* b, DBuf<T>& buf, size_t off, const std::vector<T>& v) {
+    TRY(ensure(b, buf, off + v.size(), true));
+    if (!v.empty()) {
+      items.push_back({buf.p + off, v.data(), v.size() * sizeof(T)});
+      total += (v.size() * sizeof(T) + 15) & ~(size_t)15;
+    }
+    return B2G_OK;
+  }
+  int flush(Batch* b) {
+    if (b->stage_ev) CUDA_TRY(b, cudaEventSynchronize(b->stage_ev));
+    if (total > b->h_stage_cap) {
+      if (b->h_stage) cudaFreeHost(b->h_stage);
+      b->h_stage = nullptr;
+      b->h_stage_cap = 0;
+      size_t cap = total + total / 2 + 4096;
+      CUDA_TRY(b, cudaMallocHost(&b->h_stage, cap));
+      b->h_stage_cap = cap;
+    }
+    char* p = (char*)b->h_stage;
+    for (const Item& it : items) {
+      memcpy(p, it.src, it.bytes);
+      CUDA_TRY(b, cudaMemcpyAsync(it.dst, p, it.bytes, cudaMemcpyHostToDevice, b->stream));
+      p += (it.bytes + 15) & ~(size_t)15;
+    }
+    if (!b->stage_ev) CUDA_TRY(b, cudaEventCreateWithFlags(&b->stage_ev, cudaEventDisableTiming));
+    CUDA_TRY(b, cudaEventRecord(b->stage_ev, b->stream));
+    return B2G_OK;
+  }
+};
+
 // Appends the worlds [NW, worlds.size()) that are not on the device yet after the existing
 // layout, without touching the live state of the others: body / fixture / joint arrays grow in
 // place and only the new segments are copied; the world table is rewritten (small); the new
@@ -459,38 +501,39 @@ int upload_tail(Batch* b) {
   b->h_world_order = order;
   replan_solver(b);
   std::vector<int2> wc_tail(NW - w0, make_int2(0, 0));
-  TRY(upload(b, b->wb, wb)); TRY(upload(b, b->wj, wj)); TRY(upload_at(b, b->wg, w0, wg_tail));
-  TRY(upload(b, b->wflags, wflags)); TRY(upload(b, b->world_order, order)); TRY(upload_at(b, b->wc, w0, wc_tail));
+  Stager st;
+  TRY(st.add(b, b->wb, 0, wb)); TRY(st.add(b, b->wj, 0, wj)); TRY(st.add(b, b->wg, w0, wg_tail));
+  TRY(st.add(b, b->wflags, 0, wflags)); TRY(st.add(b, b->world_order, 0, order)); TRY(st.add(b, b->wc, w0, wc_tail));
   b->h_wflags = wflags;
   TRY(ensure(b, b->wbounds, NW)); TRY(ensure(b, b->wroot, NW)); TRY(ensure(b, b->ncolors, 4 * (size_t)NW, true));
   TRY(ensure(b, b->jranges, 65 * (size_t)NW, true));
-  TRY(upload_at(b, b->xf, NB0, xf)); TRY(upload_at(b, b->pos, NB0, pos)); TRY(upload_at(b, b->vel, NB0, vel));
-  TRY(upload_at(b, b->massd, NB0, massd)); TRY(upload_at(b, b->damp, NB0, damp)); TRY(upload_at(b, b->force, NB0, force));
-  TRY(upload_at(b, b->lc, NB0, lc)); TRY(upload_at(b, b->btype, NB0, btype)); TRY(upload_at(b, b->bworld, NB0, bworld));
-  TRY(upload_at(b, b->shape, NF0, shape)); TRY(upload_at(b, b->fbody, NF0, fbody)); TRY(upload_at(b, b->fgroup, NF0, fgroup));
-  TRY(upload_at(b, b->fsensor, NF0, fsensor)); TRY(upload_at(b, b->fworld, NF0, fworld));
-  TRY(upload_at(b, b->frad, NF0, frad));
-  TRY(upload_at(b, b->ffilter, NF0, ffilter)); TRY(upload_at(b, b->fmat, NF0, fmat));
-  TRY(upload_at(b, b->joints, NJ0, joints)); TRY(upload_at(b, b->nocollide, b->n_nocollide, nocol));
+  TRY(st.add(b, b->xf, NB0, xf)); TRY(st.add(b, b->pos, NB0, pos)); TRY(st.add(b, b->vel, NB0, vel));
+  TRY(st.add(b, b->massd, NB0, massd)); TRY(st.add(b, b->damp, NB0, damp)); TRY(st.add(b, b->force, NB0, force));
+  TRY(st.add(b, b->lc, NB0, lc)); TRY(st.add(b, b->btype, NB0, btype)); TRY(st.add(b, b->bworld, NB0, bworld));
+  TRY(st.add(b, b->shape, NF0, shape)); TRY(st.add(b, b->fbody, NF0, fbody)); TRY(st.add(b, b->fgroup, NF0, fgroup));
+  TRY(st.add(b, b->fsensor, NF0, fsensor)); TRY(st.add(b, b->fworld, NF0, fworld));
+  TRY(st.add(b, b->frad, NF0, frad));
+  TRY(st.add(b, b->ffilter, NF0, ffilter)); TRY(st.add(b, b->fmat, NF0, fmat));
+  TRY(st.add(b, b->joints, NJ0, joints)); TRY(st.add(b, b->nocollide, b->n_nocollide, nocol));
+  TRY(st.flush(b));
   b->n_nocollide += (int)nocol.size();
   TRY(ensure(b, b->aabb, NF)); TRY(ensure(b, b->mkey, NF)); TRY(ensure(b, b->mkey_sorted, NF));
   TRY(ensure(b, b->mval, NF)); TRY(ensure(b, b->mval_sorted, NF)); TRY(ensure(b, b->nchild, NF));
   TRY(ensure(b, b->nparent, NF)); TRY(ensure(b, b->lparent, NF)); TRY(ensure(b, b->naabb, NF));
   TRY(ensure(b, b->ncbox, 2 * (size_t)NF)); TRY(ensure(b, b->laabb, NF)); TRY(ensure(b, b->fattr, NF));
   TRY(ensure(b, b->nflag, NF)); TRY(ensure(b, b->pcount, (size_t)NF + 1));
-  TRY(ensure(b, b->poffB[0], (size_t)NF + 1)); TRY(ensure(b, b->poffB[1], (size_t)NF + 1));
-  b->poff_valid[0] = b->poff_valid[1] = false;
+  // the live list's per-fixture offsets stay valid for the existing fixtures; the appended
+  // fixtures' entries come from their broadphase in the next step
+  TRY(ensure(b, b->poffB[0], (size_t)NF + 1, true)); TRY(ensure(b, b->poffB[1], (size_t)NF + 1, true));
   TRY(ensure(b, b->pslots, 8 * (size_t)NF));
   TRY(ensure(b, b->cub_tmp, cub_temp_bytes(NF)));
   TRY(ensure(b, b->inc_cnt, NB)); TRY(ensure(b, b->inc_head, NB)); TRY(ensure(b, b->inc_mask, NB));
   TRY(ensure(b, b->jinc_list, 2 * (size_t)NJ)); TRY(ensure(b, b->jwork, 2 * (size_t)NJ)); TRY(ensure(b, b->jcol, NJ, true)); TRY(ensure(b, b->jorder, NJ, true));
   TRY(ensure(b, b->jcb, NJ, true)); TRY(ensure(b, b->jprio, NJ, true)); TRY(ensure(b, b->jready, NJ));
   b->NW = NW; b->NB = NB; b->NF = NF; b->NJ = NJ;
-  CUDA_TRY(b, cudaMemsetAsync(b->status.p, 0, sizeof(unsigned int), b->stream));
+  // joint colours of the appended worlds; a colouring failure reaches the step's status check
   launch_joint_colour(make_args(b), w0, NW - w0, b->stream);
-  TRY(check_upload_status(b));
   b->layout_version++;
-  CUDA_TRY(b, cudaStreamSynchronize(b->stream));
   return B2G_OK;
 }
 
@@ -738,6 +781,32 @@ static int finish_step(Batch* b, int live_before_last_bp) {
   return check_status(b, status_word);
 }
 
+// Contacts of worlds appended since the last step (b2World::Step's FindNewContacts for their new
+// fixtures, src/dynamics/b2_world.cpp:1113-1122): a broadphase over the appended fixtures only,
+// appended to the live list (the other worlds' bodies have not moved since their broadphase).
+static int tail_broadphase(Batch* b, float dt, int vi, int pi, int f0, int w0) {
+  for (int guard = 0;; ++guard) {
+    if (guard > 8) {
+      set_error(b, "pair buffer kept overflowing");
+      return B2G_E_CAPACITY;
+    }
+    KernelArgs a = step_args(b, dt, vi, pi);
+    a.poff = b->poffB[b->cur ^ 1].p;  // scratch: the next full broadphase rewrites it
+    launch_bp_tail(a, f0, b->NF, w0, b->NW, b->cub_tmp.cap, sort_bits(b), b->cur,
+                   b->poff_valid[b->cur] ? b->poffB[b->cur].p : nullptr, b->stream);
+    CUDA_TRY(b, cudaGetLastError());
+    CUDA_TRY(b, cudaMemcpyAsync(b->h_readback, b->counters.p, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                                b->stream));
+    CUDA_TRY(b, cudaStreamSynchronize(b->stream));
+    unsigned long long overflow = b->h_readback[B2G_CNT_OVERFLOW];
+    if (!overflow) break;
+    TRY(ensure_contact_capacity(b, (int64_t)overflow));
+    CUDA_TRY(b, cudaMemsetAsync(b->counters.p + B2G_CNT_OVERFLOW, 0, sizeof(unsigned long long), b->stream));
+  }
+  b->NC = (int64_t)b->h_readback[B2G_CNT_CONTACTS];
+  return B2G_OK;
+}
+
 static void invalidate_graphs(Batch* b) {
   for (int k = 0; k < 2; ++k) {
     if (b->graph_exec[k]) cudaGraphExecDestroy(b->graph_exec[k]);
@@ -777,10 +846,14 @@ int step_batch(Batch* b, float dt, int vi, int pi, const uint8_t* mask, bool syn
     return B2G_E_CUDA;
   }
   CUDA_TRY(b, cudaSetDevice(b->device));
+  int tail_w0 = -1, tail_f0 = 0;
+  if (b->status.p) CUDA_TRY(b, cudaMemsetAsync(b->status.p, 0, sizeof(unsigned int), b->stream));
   if (b->structure_dirty) {
     TRY(upload_all(b));
     invalidate_graphs(b);
   } else if ((int)b->worlds.size() > b->NW) {
+    tail_w0 = b->NW;
+    tail_f0 = b->NF;
     TRY(upload_tail(b));
     invalidate_graphs(b);
   }
@@ -795,7 +868,8 @@ int step_batch(Batch* b, float dt, int vi, int pi, const uint8_t* mask, bool syn
     if ((!mask || mask[w]) && !(hw.flags & B2G_WF_RETIRED)) f |= B2G_WF_ACTIVE;
     if (mask && !mask[w]) all_active = false;
     wflags[w] = f;
-    if (hw.flags & B2G_WF_NEW_CONTACTS) need_bp = true;
+    // appended worlds get their first contacts from the broadphase of the appended range below
+    if ((hw.flags & B2G_WF_NEW_CONTACTS) && (tail_w0 < 0 || w < tail_w0)) need_bp = true;
     hw.flags &= ~B2G_WF_NEW_CONTACTS;
   }
   if (wflags != b->h_wflags) {
@@ -803,12 +877,15 @@ int step_batch(Batch* b, float dt, int vi, int pi, const uint8_t* mask, bool syn
     b->h_wflags = wflags;
   }
   TRY(ensure_contact_capacity(b, b->NC));
-  CUDA_TRY(b, cudaMemsetAsync(b->status.p, 0, sizeof(unsigned int), b->stream));
   CUDA_TRY(b, cudaMemsetAsync(b->counters.p + 1, 0, 4 * sizeof(unsigned long long), b->stream));
   if (b->events_on) b->host_events.clear();
   b->last_dt = dt;
   b->last_vi = vi;
   b->last_pi = pi;
+  if (tail_w0 >= 0) {
+    TRY(tail_broadphase(b, dt, vi, pi, tail_f0, tail_w0));
+    CUDA_TRY(b, cudaMemsetAsync(b->counters.p + 1, 0, 4 * sizeof(unsigned long long), b->stream));
+  }
   int entry = b->cur;
   bool graph = b->use_graphs && !need_bp && !b->events_on && all_active && dt > 0.0f;
   if (graph && (!b->graph_exec[0] || b->graph_version != b->layout_version || b->graph_dt != dt ||
@@ -937,6 +1014,8 @@ B2G_API int b2g_batch_destroy(b2g_batch* b) {
   for (int k = 0; k < 2; ++k)
     if (b->graph_exec[k]) cudaGraphExecDestroy(b->graph_exec[k]);
   if (b->h_readback) cudaFreeHost(b->h_readback);
+  if (b->h_stage) cudaFreeHost(b->h_stage);
+  if (b->stage_ev) cudaEventDestroy(b->stage_ev);
   release(b, b->wb); release(b, b->wj); release(b, b->wg); release(b, b->wflags); release(b, b->wc);
   release(b, b->world_order); release(b, b->xf); release(b, b->pos); release(b, b->vel); release(b, b->massd);
   release(b, b->damp); release(b, b->force); release(b, b->lc); release(b, b->btype); release(b, b->bworld);

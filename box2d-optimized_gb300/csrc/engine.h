@@ -232,6 +232,9 @@ struct Batch {
   uint64_t layout_version = 1;
   std::vector<int> h_wflags;
   unsigned long long* h_readback = nullptr;  // pinned: device counters + status after each step
+  void* h_stage = nullptr;        // pinned staging of appended worlds' records
+  size_t h_stage_cap = 0;
+  cudaEvent_t stage_ev = nullptr; // recorded after the last staged copies
   float last_dt = 0.0f;
   int last_vi = 0, last_pi = 0;
 

@@ -102,8 +102,9 @@ __global__ void k_clear_forces(KernelArgs a, int nbodies) {
 // Fixture AABBs, and the packed attributes the pair filter reads for every candidate partner:
 // (body, group index, category | mask << 16, shape type | body type << 8).
 __global__ void k_aabb(KernelArgs a, int n) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
+  int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= n) return;
+  int i = a.bp_f0 + idx;
   int body = a.fbody[i];
   const b2g_shape& sh = a.shape[i];
   AABB bb = shapeAABB(sh, ldXf(a.xf, body));
@@ -113,7 +114,7 @@ __global__ void k_aabb(KernelArgs a, int n) {
 
 // Per-world bounds of AABB centres (lower + upper, the reference's GetCenter2) for Morton codes.
 __global__ void k_world_bounds(KernelArgs a) {
-  int w = blockIdx.x;
+  int w = a.bp_w0 + blockIdx.x;
   int4 wb = a.wb[w];
   float mnx = B2G_MAX_FLOAT, mny = B2G_MAX_FLOAT, mxx = -B2G_MAX_FLOAT, mxy = -B2G_MAX_FLOAT;
   for (int i = threadIdx.x; i < wb.w; i += blockDim.x) {
@@ -152,8 +153,9 @@ __device__ __forceinline__ uint32_t expand_bits15(uint32_t v) {
 // 30-bit Morton code of the AABB centre normalised to its world's bounds; sort key
 // world << 32 | code so that each world's fixtures form one contiguous sorted range.
 __global__ void k_morton(KernelArgs a, int n) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
+  int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= n) return;
+  int i = a.bp_f0 + idx;
   int w = a.fworld[i];
   float4 wbnd = a.wbounds[w];
   float4 bb = a.aabb[i];
@@ -180,7 +182,8 @@ __device__ __forceinline__ int lbvh_delta(const uint64_t* k, int n, int i, int j
 __global__ void k_lbvh_internal(KernelArgs a, int n) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n - 1) return;
-  const uint64_t* k = a.mkey_sorted;
+  const int f0 = a.bp_f0;  // the tree is built over sorted leaves [f0, f0 + n); ids are global
+  const uint64_t* k = a.mkey_sorted + f0;
   int d = (lbvh_delta(k, n, i, i + 1) - lbvh_delta(k, n, i, i - 1)) >= 0 ? 1 : -1;
   int dmin = lbvh_delta(k, n, i, i - d);
   int lmax = 2;
@@ -198,31 +201,34 @@ __global__ void k_lbvh_internal(KernelArgs a, int n) {
   } while (t > 1);
   int gamma = i + s * d + min(d, 0);
   int lo = min(i, j), hi = max(i, j);
-  int left = (lo == gamma) ? (int)(gamma | LEAF_BIT) : gamma;
-  int right = (hi == gamma + 1) ? (int)((gamma + 1) | LEAF_BIT) : gamma + 1;
-  a.nchild[i] = make_int2(left, right);
-  if (lo == gamma) a.lparent[gamma] = i; else a.nparent[gamma] = i;
-  if (hi == gamma + 1) a.lparent[gamma + 1] = i; else a.nparent[gamma + 1] = i;
+  const int gi = f0 + i, gg = f0 + gamma;
+  int left = (lo == gamma) ? (int)(gg | LEAF_BIT) : gg;
+  int right = (hi == gamma + 1) ? (int)((gg + 1) | LEAF_BIT) : gg + 1;
+  a.nchild[gi] = make_int2(left, right);
+  if (lo == gamma) a.lparent[gg] = gi; else a.nparent[gg] = gi;
+  if (hi == gamma + 1) a.lparent[gg + 1] = gi; else a.nparent[gg + 1] = gi;
   int w = (int)(k[lo] >> 32);
   if ((int)(k[hi] >> 32) == w) {
     int4 wb = a.wb[w];
-    if (lo == wb.z && hi == wb.z + wb.w - 1) a.wroot[w] = i;
+    if (f0 + lo == wb.z && f0 + hi == wb.z + wb.w - 1) a.wroot[w] = gi;
   }
 }
 
 __global__ void k_lbvh_init(KernelArgs a, int n, int nw) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) {
+  int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx < n) {
+    int i = a.bp_f0 + idx;
     a.laabb[i] = a.aabb[a.mval_sorted[i]];
     a.lparent[i] = -1;
-    if (i < n - 1) {
+    if (idx < n - 1) {
       a.nparent[i] = -1;
       a.nflag[i] = 0;
     }
   }
-  if (i < nw) {
-    int4 wb = a.wb[i];
-    a.wroot[i] = wb.w == 1 ? (int)(wb.z | LEAF_BIT) : -1;
+  if (idx < nw) {
+    int w = a.bp_w0 + idx;
+    int4 wb = a.wb[w];
+    a.wroot[w] = wb.w == 1 ? (int)(wb.z | LEAF_BIT) : -1;
   }
 }
 
@@ -230,8 +236,9 @@ __global__ void k_lbvh_init(KernelArgs a, int n, int nw) {
 // their world's root (the traversal never reads nodes above it). The arrival counter is an
 // acquire-release atomic: the first thread's child bounds are visible to the second.
 __global__ void k_lbvh_bounds(KernelArgs a, int n) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
+  int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= n) return;
+  int i = a.bp_f0 + idx;
   const int root = a.wroot[a.fworld[a.mval_sorted[i]]];
   if (root < 0 || (root & LEAF_BIT)) return;  // single-fixture world: the leaf is the root
   int p = a.lparent[i];
@@ -346,9 +353,9 @@ __device__ __forceinline__ int traverse_pairs(const KernelArgs& a, int f, OnPair
 // Counting pass: partners of every emitter fixture, the first BP_SLOTS of them kept. Threads walk
 // the fixtures in Morton order, so a warp's traversals follow neighbouring tree paths.
 __global__ void k_pairs_count(KernelArgs a, int n) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  int f = a.mval_sorted[i];
+  int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= n) return;
+  int f = a.mval_sorted[a.bp_f0 + idx];
   uint32_t* slots = a.pslots + (int64_t)f * BP_SLOTS;
   a.pcount[f] = traverse_pairs(a, f, [&](int g, int j) {
     if (j < BP_SLOTS) slots[j] = (uint32_t)g;
@@ -358,8 +365,9 @@ __global__ void k_pairs_count(KernelArgs a, int n) {
 // Emit pass: each fixture's partners, ascending, as keys f << 32 | g at its scanned offset (the
 // pair list comes out sorted). Fixtures with more partners than slots search again.
 __global__ void k_pairs_emit(KernelArgs a, int n) {
-  int f = blockIdx.x * blockDim.x + threadIdx.x;
-  if (f >= n) return;
+  int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= n) return;
+  int f = a.bp_f0 + idx;
   if ((int64_t)a.poff[a.nf] > a.ccap) return;  // overflow: the host grows the buffers and redoes this pass
   int64_t off = a.poff[f];
   int cnt = (int)(a.poff[f + 1] - off);
@@ -402,8 +410,9 @@ __global__ void k_pairs_emit(KernelArgs a, int n) {
 }
 
 __global__ void k_world_contacts(KernelArgs a, int nw) {
-  int w = blockIdx.x * blockDim.x + threadIdx.x;
-  if (w >= nw) return;
+  int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= nw) return;
+  int w = a.bp_w0 + idx;
   int4 wb = a.wb[w];
   int s = a.poff[wb.z], e = a.poff[wb.z + wb.w];
   a.wc[w] = make_int2(s, e - s);
@@ -418,9 +427,25 @@ __device__ __forceinline__ int64_t find_key(const uint64_t* keys, int64_t n, uin
   return (lo < n && keys[lo] == key) ? lo : -1;
 }
 
+// A new contact for pair `key` at index k of contact buffer `dst`, like b2Contact's constructor
+// (src/dynamics/b2_contact.cpp:96-122) in b2Contact::Create's orientation: fixture order by the
+// collider table, mixed friction / restitution / threshold, enabled, empty manifold.
+__device__ __forceinline__ void init_new_contact(const KernelArgs& a, int dst, int64_t k, uint64_t key) {
+  a.ckeyB[dst][k] = key;
+  int e = (int)(key >> 32), p = (int)(uint32_t)key;
+  int fa, fb;
+  if (hasCollider(a.shape[e].type, a.shape[p].type)) { fa = e; fb = p; }
+  else { fa = p; fb = e; }
+  float4 ma = a.fmat[fa], mb = a.fmat[fb];
+  a.cfixB[dst][k] = make_int2(fa, fb);
+  a.cflagsB[dst][k] = B2G_CONTACT_ENABLED;
+  a.cmatB[dst][k] = make_float4(sqrtf(ma.x * mb.x), ma.y > mb.y ? ma.y : mb.y, ma.z < mb.z ? ma.z : mb.z, 0.0f);
+  int4* m = reinterpret_cast<int4*>(&a.cmanB[dst][k]);
+  m[0] = m[1] = m[2] = m[3] = make_int4(0, 0, 0, 0);
+}
+
 // New contact list = the new pair list; persisting contacts keep their orientation, flags,
-// mixed material and manifold (impulses included); new ones are created like b2Contact's
-// constructor (src/dynamics/b2_contact.cpp:96-122) in b2Contact::Create's orientation.
+// mixed material and manifold (impulses included); new ones are created as new contacts.
 __global__ void k_contact_diff(KernelArgs a, int src, int dst) {
   int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   int64_t nnew = a.poff[a.nf];
@@ -436,24 +461,48 @@ __global__ void k_contact_diff(KernelArgs a, int src, int dst) {
   } else {
     o = find_key(a.ckeyB[src], nold, key);
   }
-  a.ckeyB[dst][k] = key;
   if (o >= 0) {
+    a.ckeyB[dst][k] = key;
     a.cfixB[dst][k] = a.cfixB[src][o];
     a.cflagsB[dst][k] = a.cflagsB[src][o];
     a.cmatB[dst][k] = a.cmatB[src][o];
     copy_manifold(&a.cmanB[dst][k], &a.cmanB[src][o]);
   } else {
-    int e = (int)(key >> 32), p = (int)(uint32_t)key;
-    int fa, fb;
-    if (hasCollider(a.shape[e].type, a.shape[p].type)) { fa = e; fb = p; }
-    else { fa = p; fb = e; }
-    float4 ma = a.fmat[fa], mb = a.fmat[fb];
-    a.cfixB[dst][k] = make_int2(fa, fb);
-    a.cflagsB[dst][k] = B2G_CONTACT_ENABLED;
-    a.cmatB[dst][k] = make_float4(sqrtf(ma.x * mb.x), ma.y > mb.y ? ma.y : mb.y, ma.z < mb.z ? ma.z : mb.z, 0.0f);
-    int4* m = reinterpret_cast<int4*>(&a.cmanB[dst][k]);
-    m[0] = m[1] = m[2] = m[3] = make_int4(0, 0, 0, 0);
+    init_new_contact(a, dst, k, key);
   }
+}
+
+// ---- broadphase of appended worlds only (fixtures [bp_f0, nf), worlds [bp_w0, nw)): their keys
+// sort after every live contact, so their pairs are appended to the live list of buffer `dst`.
+// poff holds the appended pairs' offsets relative to the first appended fixture.
+__global__ void k_tail_append(KernelArgs a, int dst) {
+  const int64_t total = (int64_t)a.poff[a.nf];
+  const int64_t nc0 = (int64_t)a.counters[B2G_CNT_CONTACTS];
+  if (nc0 + total > a.ccap) return;  // overflow: the host grows the buffers and redoes this pass
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < total; k += (int64_t)gridDim.x * blockDim.x)
+    init_new_contact(a, dst, nc0 + k, a.pairs[k]);
+}
+
+// Contact ranges of the appended worlds and, when the live list's per-fixture offsets are kept,
+// their entries for the appended fixtures.
+__global__ void k_tail_ranges(KernelArgs a, int nw, int nfix, int* poff_live) {
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t total = (int64_t)a.poff[a.nf];
+  const int nc0 = (int)a.counters[B2G_CNT_CONTACTS];
+  if (nc0 + total > a.ccap) return;
+  if (idx < nw) {
+    int4 wb = a.wb[a.bp_w0 + idx];
+    int s = a.poff[wb.z], e = a.poff[wb.z + wb.w];
+    a.wc[a.bp_w0 + idx] = make_int2(nc0 + s, e - s);
+  }
+  if (poff_live && idx <= nfix) poff_live[a.bp_f0 + idx] = nc0 + a.poff[a.bp_f0 + idx];
+}
+
+__global__ void k_tail_commit(KernelArgs a) {
+  unsigned long long total = (unsigned long long)a.poff[a.nf];
+  unsigned long long nc = a.counters[B2G_CNT_CONTACTS] + total;
+  if ((int64_t)nc > a.ccap) a.counters[B2G_CNT_OVERFLOW] = nc;
+  else a.counters[B2G_CNT_CONTACTS] = nc;
 }
 
 // Contacts that disappeared: EndContact if they were touching (b2ContactManager::Destroy,
@@ -537,6 +586,38 @@ void launch_bp_build(const KernelArgs& a, int nf, int nw, size_t cub_bytes, int 
   bytes = cub_bytes;
   cub::DeviceScan::ExclusiveSum(a.cub_tmp, bytes, a.pcount, a.poff, nf + 1, s);
   k_world_contacts<<<grid_for(nw, 128), 128, 0, s>>>(a, nw);
+}
+void launch_bp_tail(const KernelArgs& a0, int f0, int nf, int w0, int nw, size_t cub_bytes, int sort_bits, int dst,
+                    int* poff_live, cudaStream_t s) {
+  KernelArgs a = a0;
+  a.bp_f0 = f0;
+  a.bp_w0 = w0;
+  const int n = nf - f0, nwt = nw - w0;
+  if (n <= 0) {  // appended worlds without fixtures: empty ranges at the end of the live list
+    cudaMemsetAsync(a.poff + f0, 0, sizeof(int), s);
+    k_tail_ranges<<<grid_for(nwt + 1, 128), 128, 0, s>>>(a, nwt, 0, nullptr);
+    return;
+  }
+  k_aabb<<<grid_for(n, 128), 128, 0, s>>>(a, n);
+  k_world_bounds<<<nwt, 256, 0, s>>>(a);
+  k_morton<<<grid_for(n, 256), 256, 0, s>>>(a, n);
+  size_t bytes = cub_bytes;
+  cub::DeviceRadixSort::SortPairs(a.cub_tmp, bytes, a.mkey + f0, a.mkey_sorted + f0, a.mval + f0, a.mval_sorted + f0, n,
+                                  0, sort_bits, s);
+  int m = n > nwt ? n : nwt;
+  k_lbvh_init<<<grid_for(m, 256), 256, 0, s>>>(a, n, nwt);
+  if (n > 1) {
+    k_lbvh_internal<<<grid_for(n - 1, 256), 256, 0, s>>>(a, n);
+    k_lbvh_bounds<<<grid_for(n, 256), 256, 0, s>>>(a, n);
+  }
+  k_pairs_count<<<grid_for(n, 128), 128, 0, s>>>(a, n);
+  bytes = cub_bytes;
+  cub::DeviceScan::ExclusiveSum(a.cub_tmp, bytes, a.pcount + f0, a.poff + f0, n + 1, s);
+  k_pairs_emit<<<grid_for(n, 128), 128, 0, s>>>(a, n);
+  k_tail_append<<<1024, 256, 0, s>>>(a, dst);
+  int r = (n + 1 > nwt ? n + 1 : nwt);
+  k_tail_ranges<<<grid_for(r, 128), 128, 0, s>>>(a, nwt, n, poff_live);
+  k_tail_commit<<<1, 1, 0, s>>>(a);
 }
 void launch_bp_emit(const KernelArgs& a, int nf, cudaStream_t s) {
   if (nf > 0) k_pairs_emit<<<grid_for(nf, 128), 128, 0, s>>>(a, nf);

@@ -84,6 +84,7 @@ struct KernelArgs {
   int* wroot;
   int* pcount;
   uint32_t* pslots;               // BP_SLOTS partners per fixture from the counting pass
+  int bp_f0, bp_w0;               // first fixture and world of a partial broadphase (0: all)
   int* poff;                      // offsets of the pair list being built, per emitter fixture
   const int* poff_old;            // offsets of the live (source) list, or null when unknown
   uint64_t* pairs;
@@ -176,6 +177,10 @@ bool solver_threads_valid(int t);
 void launch_clear_forces(const KernelArgs& a, int nb, cudaStream_t s);
 void launch_bp_build(const KernelArgs& a, int nf, int nw, size_t cub_bytes, int sort_bits, cudaStream_t s);
 void launch_bp_emit(const KernelArgs& a, int nf, cudaStream_t s);
+// Broadphase of the appended fixtures [f0, nf) of worlds [w0, nw) only; their pairs are appended to
+// the live list (buffer dst); poff_live (may be null) gets the appended fixtures' offsets.
+void launch_bp_tail(const KernelArgs& a, int f0, int nf, int w0, int nw, size_t cub_bytes, int sort_bits, int dst,
+                    int* poff_live, cudaStream_t s);
 void launch_contact_diff(const KernelArgs& a, int src, int dst, cudaStream_t s);
 size_t cub_temp_bytes(int nf);
 void launch_collide_pairs(const b2g_shape* sa, const float* xa, const b2g_shape* sb, const float* xb, int n,

@@ -233,6 +233,31 @@ def test_device_compaction_equals_fresh_batch(lib):
     small.close()
 
 
+def test_appended_worlds_match_alone(lib):
+    """Worlds appended to a running batch get their first contacts from a broadphase over the
+    appended fixtures only; each world ends bit-identical to the same world stepped alone."""
+    first, ws = _mixed_batch(lib, [41, 42], [500, 60])
+    for _ in range(10):
+        first.step(1 / 60, 8, 3)
+    late = []
+    for s, n in ((43, 800), (44, 3000), (45, 20)):
+        _, gx, gy = _params(lib, s)
+        w = first.add_world(gx, gy)
+        first.set_flags(w)
+        first.scene(w, G.SCENE_BATCH_WORLD, seed=s, n=n)
+        late.append((w, s, n))
+    for _ in range(30):
+        first.step(1 / 60, 8, 3)
+    for w, s, n, steps in [(ws[0], 41, 500, 40), (ws[1], 42, 60, 40)] + [(w, s, n, 30) for w, s, n in late]:
+        alone, wa = _mixed_batch(lib, [s], [n])
+        for _ in range(steps):
+            alone.step(1 / 60, 8, 3)
+        assert _state_bytes(first.bodies(w)) == _state_bytes(alone.bodies(wa[0])), s
+        assert [_contact_key(x) for x in first.contacts(w)] == [_contact_key(y) for y in alone.contacts(wa[0])], s
+        alone.close()
+    first.close()
+
+
 def test_masked_step_leaves_other_worlds(lib):
     b = G.Batch(lib, device=0)
     w0 = b.add_world(0, -10)
