@@ -24,6 +24,7 @@ SHAPE_CIRCLE, SHAPE_EDGE, SHAPE_POLYGON = 0, 1, 2
 JOINT_REVOLUTE, JOINT_PRISMATIC, JOINT_DISTANCE = 1, 2, 3
 POLY_HULL, POLY_BOX, POLY_BOX_ORIENTED, POLY_RAW = 0, 1, 2, 3
 SCENE_PYRAMID, SCENE_MIXED_DROP, SCENE_CHAINS, SCENE_BATCH_WORLD = 0, 1, 2, 3
+HOST_ONLY = -1  # B2G_HOST_ONLY: a batch built and read on the host only (no device)
 EVENT_BEGIN, EVENT_END, EVENT_PRESOLVE, EVENT_POSTSOLVE = 1, 2, 3, 4
 CONTACT_TOUCHING, CONTACT_ENABLED = 2, 4
 
@@ -118,6 +119,11 @@ class Profile(C.Structure):
                 ("broadphase", C.c_float), ("solve_toi", C.c_float), ("bodies", C.c_int64),
                 ("fixtures", C.c_int64), ("contacts", C.c_int64), ("touching", C.c_int64),
                 ("joints", C.c_int64), ("colors_max", C.c_int64), ("touching_total", C.c_int64)]
+
+
+class RayHit(C.Structure):
+    _fields_ = [("fixture", C.c_int32), ("point", C.c_float * 2), ("normal", C.c_float * 2),
+                ("fraction", C.c_float)]
 
 
 class RequestResult(C.Structure):
@@ -215,7 +221,7 @@ class Lib:
         "b2g_profile_get", "b2g_solver_order", "b2g_collide", "b2g_pairs", "b2g_scene_build",
         "b2g_batch_world_params", "b2g_server_create", "b2g_server_destroy", "b2g_server_submit",
         "b2g_server_tick", "b2g_server_poll", "b2g_server_stats", "b2g_status_string",
-        "b2g_last_error", "b2g_device_count",
+        "b2g_last_error", "b2g_device_count", "b2g_query_aabb", "b2g_raycast_closest",
     ]
 
     def __init__(self, path: os.PathLike | str | None = None):
@@ -261,6 +267,8 @@ class Lib:
             "b2g_batch_set_solver_threads": ([vp, P(i32)], C.c_int),
             "b2g_batch_get_solver_threads": ([vp, P(i32)], C.c_int),
             "b2g_batch_autotune": ([vp, i32, f32, i32, i32, P(i32), P(i32)], C.c_int),
+            "b2g_query_aabb": ([vp, P(i32), P(f32), i32, P(i32), P(i32), i64, P(i64)], C.c_int),
+            "b2g_raycast_closest": ([vp, P(i32), P(f32), i32, P(RayHit)], C.c_int),
             "b2g_solver_order": ([vp, i32, P(i32), P(u32), i32, P(i32), P(u32), i32], C.c_int),
             "b2g_collide": ([vp, vp, vp, vp, i32, vp, vp], C.c_int),
             "b2g_pairs": ([vp, i32, vp, i64, P(i64), vp], C.c_int),
@@ -402,6 +410,32 @@ class Batch:
         self.lib.check(self.lib.b2g_batch_autotune(self.h, steps, dt, vi, pi, arr, C.byref(taken)),
                        "b2g_batch_autotune")
         return list(arr), taken.value
+
+    def raycast(self, worlds, rays):
+        """Closest hit of each ray (x1, y1, x2, y2) in its world: list of
+        (fixture, point, normal, fraction), fixture -1 for no hit."""
+        n = len(worlds)
+        w = (C.c_int32 * max(n, 1))(*worlds)
+        r = (C.c_float * max(4 * n, 1))(*[v for ray in rays for v in ray])
+        out = (RayHit * max(n, 1))()
+        self.lib.check(self.lib.b2g_raycast_closest(self.h, w, r, n, out), "b2g_raycast_closest")
+        return [(h.fixture, tuple(h.point), tuple(h.normal), h.fraction) if h.fixture >= 0 else (-1, None, None, None)
+                for h in out[:n]]
+
+    def query_aabb(self, worlds, boxes, cap=1 << 20):
+        """Fixtures overlapping each box (lower x, y, upper x, y) in its world, ascending."""
+        n = len(worlds)
+        w = (C.c_int32 * max(n, 1))(*worlds)
+        bx = (C.c_float * max(4 * n, 1))(*[v for box in boxes for v in box])
+        counts = (C.c_int32 * max(n, 1))()
+        out = (C.c_int32 * max(cap, 1))()
+        total = C.c_int64()
+        self.lib.check(self.lib.b2g_query_aabb(self.h, w, bx, n, counts, out, cap, C.byref(total)), "b2g_query_aabb")
+        res, k = [], 0
+        for q in range(n):
+            res.append(list(out[k:k + counts[q]]))
+            k += counts[q]
+        return res
 
     def solver_order(self, world, nc, nj):
         cc = (C.c_int32 * max(nc, 1))()

@@ -209,6 +209,114 @@ B2G_HD bool overlap(const AABB& a, const AABB& b) {
   return (a.hi.x >= b.lo.x) & (a.lo.x <= b.hi.x) & (a.hi.y >= b.lo.y) & (a.lo.y <= b.hi.y);
 }
 
+// ---- ray casts ---------------------------------------------------------------------------
+// b2RayCastOutput: where along p1 -> p2 the ray enters the shape, and the surface normal there.
+struct RayHit {
+  float fraction;
+  V2 normal;
+};
+
+// b2PolygonShape::RayCast (src/collision/b2_polygon_shape.cpp:303-364): clip the parametric
+// segment against every face's half-space in the polygon's frame; a hit needs an entering face.
+B2G_HD bool rayPolygon(const b2g_shape& s, const Xf& xf, V2 P1, V2 P2, float maxFraction, RayHit* out) {
+  V2 p1 = mulT(xf.q, P1 - xf.p);
+  V2 p2 = mulT(xf.q, P2 - xf.p);
+  V2 d = p2 - p1;
+  float lower = 0.0f, upper = maxFraction;
+  int index = -1;
+  for (int i = 0; i < s.count; ++i) {
+    float numerator = dot(sn(s, i), sv(s, i) - p1);
+    float denominator = dot(sn(s, i), d);
+    if (denominator == 0.0f) {
+      if (numerator < 0.0f) return false;
+    } else if (denominator < 0.0f && numerator < lower * denominator) {
+      lower = numerator / denominator;  // the segment enters this half-space
+      index = i;
+    } else if (denominator > 0.0f && numerator < upper * denominator) {
+      upper = numerator / denominator;  // ... and leaves this one
+    }
+    if (upper < lower) return false;
+  }
+  if (index < 0) return false;
+  out->fraction = lower;
+  out->normal = mul(xf.q, sn(s, index));
+  return true;
+}
+
+// b2CircleShape::RayCast (src/collision/b2_circle_shape.cpp:56-87): the smaller root of
+// |p1 + t r - c|^2 = radius^2, accepted on [0, maxFraction].
+B2G_HD bool rayCircle(const b2g_shape& s, const Xf& xf, V2 P1, V2 P2, float maxFraction, RayHit* out) {
+  V2 position = xf.p + mul(xf.q, sv(s, 0));
+  V2 d = P1 - position;
+  float b = dot(d, d) - s.radius * s.radius;
+  V2 r = P2 - P1;
+  float c = dot(d, r);
+  float rr = dot(r, r);
+  float sigma = c * c - rr * b;
+  if (sigma < 0.0f || rr < B2G_EPSILON) return false;
+  float a = -(c + sqrtf(sigma));
+  if (!(0.0f <= a && a <= maxFraction * rr)) return false;
+  a /= rr;
+  out->fraction = a;
+  V2 n = d + a * r;
+  normalize(n);
+  out->normal = n;
+  return true;
+}
+
+// b2EdgeShape::RayCast (src/collision/b2_edge_shape.cpp:89-149): crossing of the edge's line,
+// kept when it lies on the segment and the edge; one-sided edges ignore rays from behind.
+B2G_HD bool rayEdge(const b2g_shape& s, const Xf& xf, V2 P1, V2 P2, float maxFraction, RayHit* out) {
+  V2 p1 = mulT(xf.q, P1 - xf.p);
+  V2 p2 = mulT(xf.q, P2 - xf.p);
+  V2 d = p2 - p1;
+  V2 v1 = sv(s, 0), v2 = sv(s, 1);
+  V2 e = v2 - v1;
+  V2 normal = mk(e.y, -e.x);  // to the right, looking from v1 at v2
+  normalize(normal);
+  float numerator = dot(normal, v1 - p1);
+  if (s.one_sided && numerator > 0.0f) return false;
+  float denominator = dot(normal, d);
+  if (denominator == 0.0f) return false;
+  float t = numerator / denominator;
+  if (t < 0.0f || maxFraction < t) return false;
+  V2 q = p1 + t * d;
+  V2 r = v2 - v1;
+  float rr = dot(r, r);
+  if (rr == 0.0f) return false;
+  float sc = dot(q - v1, r) / rr;
+  if (sc < 0.0f || 1.0f < sc) return false;
+  out->fraction = t;
+  out->normal = numerator > 0.0f ? -mul(xf.q, normal) : mul(xf.q, normal);
+  return true;
+}
+
+B2G_HD bool rayShape(const b2g_shape& s, const Xf& xf, V2 p1, V2 p2, float maxFraction, RayHit* out) {
+  if (s.type == B2G_SHAPE_CIRCLE) return rayCircle(s, xf, p1, p2, maxFraction, out);
+  if (s.type == B2G_SHAPE_EDGE) return rayEdge(s, xf, p1, p2, maxFraction, out);
+  return rayPolygon(s, xf, p1, p2, maxFraction, out);
+}
+
+// The pruning tests b2BroadPhase::RayCast applies to a tree node's box
+// (include/box2d/b2_broad_phase.h:646-710): overlap with the box of the segment so far, then the
+// separating axis |dot(v, p1 - c)| > dot(|v|, h), v the segment's unit normal. True = skip.
+B2G_HD bool rayPrunes(const AABB& box, const AABB& segment, V2 p1, V2 v, V2 absV) {
+  if (!overlap(box, segment)) return true;
+  V2 c = 0.5f * (box.lo + box.hi);
+  V2 h = 0.5f * (box.hi - box.lo);
+  float separation = fabs2(dot(v, p1 - c)) - dot(absV, h);
+  return separation > 0.0f;
+}
+
+// Box of the segment p1 -> p1 + maxFraction (p2 - p1).
+B2G_HD AABB raySegmentBox(V2 p1, V2 p2, float maxFraction) {
+  V2 t = p1 + maxFraction * (p2 - p1);
+  AABB bb;
+  bb.lo = vmin(p1, t);
+  bb.hi = vmax(p1, t);
+  return bb;
+}
+
 // Collider dispatch of b2Contact::InitializeRegisters (src/dynamics/b2_contact.cpp:46-56).
 B2G_HD bool hasCollider(int ta, int tb) {
   return (ta == 0 && tb == 0) || (ta == 2 && tb == 0) || (ta == 2 && tb == 2) || (ta == 1 && tb == 0) ||

@@ -348,6 +348,7 @@ int upload_all(Batch* b) {
   CUDA_TRY(b, cudaMemsetAsync(b->status.p, 0, sizeof(unsigned int), b->stream));
   launch_joint_colour(make_args(b), 0, NW, b->stream);
   TRY(check_upload_status(b));
+  b->tree_valid = false;
   b->layout_version++;
   b->structure_dirty = false;
   b->device_state_valid = true;
@@ -912,6 +913,7 @@ int step_batch(Batch* b, float dt, int vi, int pi, const uint8_t* mask, bool syn
   }
   CUDA_TRY(b, cudaGetLastError());
   b->host_state_stale = true;
+  if (dt > 0.0f || need_bp) b->tree_valid = true;  // a full broadphase rebuilt every world's tree
   int live_before_last_bp = b->cur ^ 1;
   int st = finish_step(b, live_before_last_bp);
   if (!graph) {
@@ -1037,6 +1039,8 @@ B2G_API int b2g_batch_destroy(b2g_batch* b) {
   release(b, b->jinc_list); release(b, b->jcol); release(b, b->jorder); release(b, b->jcb); release(b, b->jranges);
   release(b, b->jprio); release(b, b->jready);
   release(b, b->ncolors); release(b, b->events);
+  release(b, b->q_world); release(b, b->q_counts); release(b, b->q_out); release(b, b->q_box); release(b, b->q_offs);
+  release(b, b->q_hits);
   {
     Batch::Spare& sp = b->spare;
     release(b, sp.xf); release(b, sp.pos); release(b, sp.vel); release(b, sp.massd); release(b, sp.damp);
@@ -1211,6 +1215,7 @@ static int compact_device(Batch* b, int32_t* old_to_new, int32_t n) {
   b->h_wflags = wflags;
   b->poff_valid[0] = b->poff_valid[1] = false;
   b->last_solve_buf = -1;
+  b->tree_valid = false;
   CUDA_TRY(b, cudaMemsetAsync(b->status.p, 0, sizeof(unsigned int), s));
   launch_joint_colour(make_args(b), 0, kept, s);
   TRY(check_upload_status(b));
@@ -1724,6 +1729,84 @@ B2G_API int b2g_solver_order(b2g_batch* b, int32_t world, int32_t* contact_color
     if (contact_priority) contact_priority[i] = cp[k];
   }
   return B2G_OK;
+}
+
+// The per-world trees for queries: pending host edits are uploaded, and when the trees are stale
+// (re-layout, compaction) the broadphase rebuilds them without touching the contact list.
+static int ensure_query_trees(Batch* b) {
+  if (b->device < 0) return B2G_E_INVALID_ARG;
+  CUDA_TRY(b, cudaSetDevice(b->device));
+  if (b->structure_dirty) {
+    TRY(upload_all(b));
+    invalidate_graphs(b);
+  } else if ((int)b->worlds.size() > b->NW) {
+    TRY(upload_tail(b));  // the appended worlds still get their contacts from the next step
+    invalidate_graphs(b);
+    b->tree_valid = false;
+  }
+  if (!b->tree_valid && b->NF > 0) {
+    KernelArgs a = step_args(b, 0.0f, 0, 0);
+    launch_bp_build(a, b->NF, b->NW, b->cub_tmp.cap, sort_bits(b), b->stream, false);
+    CUDA_TRY(b, cudaGetLastError());
+  }
+  b->tree_valid = true;
+  CUDA_TRY(b, cudaMemsetAsync(b->status.p, 0, sizeof(unsigned int), b->stream));
+  return B2G_OK;
+}
+
+static int query_status(Batch* b) {
+  unsigned int st = 0;
+  CUDA_TRY(b, cudaMemcpyAsync(&st, b->status.p, sizeof(st), cudaMemcpyDeviceToHost, b->stream));
+  CUDA_TRY(b, cudaStreamSynchronize(b->stream));
+  return check_status(b, st);
+}
+
+B2G_API int b2g_query_aabb(b2g_batch* b, const int32_t* worlds, const float* boxes, int32_t n, int32_t* counts,
+                           int32_t* fixtures, int64_t cap, int64_t* total) {
+  if (!b || n < 0 || (n > 0 && (!worlds || !boxes || !counts)) || cap < 0 || (cap > 0 && !fixtures) || !total)
+    return B2G_E_INVALID_ARG;
+  *total = 0;
+  if (n == 0) return B2G_OK;
+  TRY(ensure_query_trees(b));
+  cudaStream_t s = b->stream;
+  TRY(ensure(b, b->q_world, n)); TRY(ensure(b, b->q_box, n)); TRY(ensure(b, b->q_counts, n));
+  CUDA_TRY(b, cudaMemcpyAsync(b->q_world.p, worlds, n * sizeof(int32_t), cudaMemcpyHostToDevice, s));
+  CUDA_TRY(b, cudaMemcpyAsync(b->q_box.p, boxes, n * sizeof(float4), cudaMemcpyHostToDevice, s));
+  KernelArgs a = step_args(b, 0.0f, 0, 0);
+  launch_query_count(a, n, b->q_world.p, b->q_box.p, b->q_counts.p, s);
+  CUDA_TRY(b, cudaMemcpyAsync(counts, b->q_counts.p, n * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+  TRY(query_status(b));
+  std::vector<int64_t> offs(n);
+  int64_t t = 0;
+  for (int q = 0; q < n; ++q) {
+    offs[q] = t;
+    t += counts[q];
+  }
+  *total = t;
+  if (t > cap) {
+    set_error(b, "query result larger than the output capacity");
+    return B2G_E_CAPACITY;
+  }
+  if (t == 0) return B2G_OK;
+  TRY(upload(b, b->q_offs, offs));
+  TRY(ensure(b, b->q_out, (size_t)t));
+  launch_query_emit(a, n, b->q_world.p, b->q_box.p, b->q_counts.p, b->q_offs.p, b->q_out.p, s);
+  CUDA_TRY(b, cudaMemcpyAsync(fixtures, b->q_out.p, t * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+  return query_status(b);
+}
+
+B2G_API int b2g_raycast_closest(b2g_batch* b, const int32_t* worlds, const float* rays, int32_t n, b2g_ray_hit* hits) {
+  if (!b || n < 0 || (n > 0 && (!worlds || !rays || !hits))) return B2G_E_INVALID_ARG;
+  if (n == 0) return B2G_OK;
+  TRY(ensure_query_trees(b));
+  cudaStream_t s = b->stream;
+  TRY(ensure(b, b->q_world, n)); TRY(ensure(b, b->q_box, n)); TRY(ensure(b, b->q_hits, n));
+  CUDA_TRY(b, cudaMemcpyAsync(b->q_world.p, worlds, n * sizeof(int32_t), cudaMemcpyHostToDevice, s));
+  CUDA_TRY(b, cudaMemcpyAsync(b->q_box.p, rays, n * sizeof(float4), cudaMemcpyHostToDevice, s));
+  KernelArgs a = step_args(b, 0.0f, 0, 0);
+  launch_raycast(a, n, b->q_world.p, b->q_box.p, b->q_hits.p, s);
+  CUDA_TRY(b, cudaMemcpyAsync(hits, b->q_hits.p, n * sizeof(b2g_ray_hit), cudaMemcpyDeviceToHost, s));
+  return query_status(b);
 }
 
 B2G_API int b2g_collide(const b2g_shape* sa, const float* xa, const b2g_shape* sb, const float* xb, int32_t n,

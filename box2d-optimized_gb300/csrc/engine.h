@@ -158,6 +158,13 @@ struct Batch {
   DBuf<b2g_manifold> cman[2];
   int cur = 0;
   int last_solve_buf = -1;        // contact buffer the last solve read (solver order lookups)
+  bool tree_valid = false;        // the per-world trees match the current body transforms
+
+  // world query scratch
+  DBuf<int> q_world, q_counts, q_out;
+  DBuf<float4> q_box;
+  DBuf<int64_t> q_offs;
+  DBuf<b2g_ray_hit> q_hits;
 
   // broadphase scratch
   DBuf<float4> wbounds;

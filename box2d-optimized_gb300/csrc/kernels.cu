@@ -565,8 +565,13 @@ void launch_collide(const KernelArgs& a, cudaStream_t s) {
 void launch_clear_forces(const KernelArgs& a, int nb, cudaStream_t s) {
   if (nb > 0) k_clear_forces<<<grid_for(nb, 256), 256, 0, s>>>(a, nb);
 }
-void launch_bp_build(const KernelArgs& a, int nf, int nw, size_t cub_bytes, int sort_bits, cudaStream_t s) {
+void launch_bp_build(const KernelArgs& a, int nf, int nw, size_t cub_bytes, int sort_bits, cudaStream_t s,
+                     bool pairs) {
   if (nf <= 0) {
+    if (!pairs) {
+      k_lbvh_init<<<grid_for(nw, 256), 256, 0, s>>>(a, 0, nw);
+      return;
+    }
     cudaMemsetAsync(a.poff, 0, sizeof(int), s);
     k_world_contacts<<<grid_for(nw, 128), 128, 0, s>>>(a, nw);
     return;
@@ -582,6 +587,7 @@ void launch_bp_build(const KernelArgs& a, int nf, int nw, size_t cub_bytes, int 
     k_lbvh_internal<<<grid_for(nf - 1, 256), 256, 0, s>>>(a, nf);
     k_lbvh_bounds<<<grid_for(nf, 256), 256, 0, s>>>(a, nf);
   }
+  if (!pairs) return;
   k_pairs_count<<<grid_for(nf, 128), 128, 0, s>>>(a, nf);
   bytes = cub_bytes;
   cub::DeviceScan::ExclusiveSum(a.cub_tmp, bytes, a.pcount, a.poff, nf + 1, s);

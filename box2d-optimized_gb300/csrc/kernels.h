@@ -138,6 +138,12 @@ void launch_solve(const KernelArgs& a, const std::vector<SolveClass>& classes, c
                   const cudaStream_t* side, const cudaEvent_t* ev);
 void launch_joint_colour(const KernelArgs& a, int w0, int nw, cudaStream_t s);
 
+// ---- world queries (query.cu)
+void launch_query_count(const KernelArgs& a, int n, const int* qw, const float4* qbox, int* counts, cudaStream_t s);
+void launch_query_emit(const KernelArgs& a, int n, const int* qw, const float4* qbox, int* counts, const int64_t* offs,
+                       int* out, cudaStream_t s);
+void launch_raycast(const KernelArgs& a, int n, const int* qw, const float4* rays, b2g_ray_hit* out, cudaStream_t s);
+
 // ---- batch compaction (compact.cu)
 struct CompactTables {            // per old world
   const int* wnew;                // new world index, -1 when removed
@@ -175,7 +181,10 @@ std::vector<SolveClass> plan_solve_classes(const std::vector<int>& order, const 
                                            const int* class_threads);
 bool solver_threads_valid(int t);
 void launch_clear_forces(const KernelArgs& a, int nb, cudaStream_t s);
-void launch_bp_build(const KernelArgs& a, int nf, int nw, size_t cub_bytes, int sort_bits, cudaStream_t s);
+// Broadphase up to the tree (AABBs, Morton sort, LBVH, node boxes); with `pairs` also the pair
+// count, its scan and the per-world contact ranges of the list being built.
+void launch_bp_build(const KernelArgs& a, int nf, int nw, size_t cub_bytes, int sort_bits, cudaStream_t s,
+                     bool pairs = true);
 void launch_bp_emit(const KernelArgs& a, int nf, cudaStream_t s);
 // Broadphase of the appended fixtures [f0, nf) of worlds [w0, nw) only; their pairs are appended to
 // the live list (buffer dst); poff_live (may be null) gets the appended fixtures' offsets.

@@ -355,6 +355,29 @@ B2G_API int b2g_solver_order(b2g_batch* b, int32_t world, int32_t* contact_color
                              uint32_t* contact_priority, int32_t nc, int32_t* joint_color,
                              uint32_t* joint_priority, int32_t nj);
 
+/* ---- world queries (batched; host buffers) ------------------------------------------------- */
+/* One ray's closest hit (b2RayCastCallback::ReportFixture returning the fraction). */
+typedef struct b2g_ray_hit {
+  int32_t fixture;  /* world-local fixture index, -1 when the ray hits nothing */
+  float point[2];   /* (1 - fraction) * p1 + fraction * p2 */
+  float normal[2];
+  float fraction;
+} b2g_ray_hit; /* 24 bytes */
+
+/* b2World::QueryAABB (src/dynamics/b2_world.cpp:1193-1207) for n queries at once: query q asks
+ * world worlds[q] for the fixtures whose AABB overlaps boxes[4q..4q+3] (lower x, y, upper x, y).
+ * counts[q] receives the number of fixtures; fixtures receives them query after query, each
+ * query's ascending (world-local indices), at most cap in total; *total is the number found.
+ * Returns B2G_E_CAPACITY (counts and total filled, fixtures not) when total > cap. Like the
+ * reference, a world of one fixture reports it for every box. */
+B2G_API int b2g_query_aabb(b2g_batch* b, const int32_t* worlds, const float* boxes, int32_t n, int32_t* counts,
+                           int32_t* fixtures, int64_t cap, int64_t* total);
+/* b2World::RayCast (src/dynamics/b2_world.cpp:1228-1238) with a closest-hit callback, for n rays
+ * at once: ray q from (rays[4q], rays[4q+1]) to (rays[4q+2], rays[4q+3]) in world worlds[q].
+ * Of fixtures hit at the same fraction the lowest index is reported (the reference reports the
+ * one its tree visits last). */
+B2G_API int b2g_raycast_closest(b2g_batch* b, const int32_t* worlds, const float* rays, int32_t n, b2g_ray_hit* hits);
+
 /* ---- standalone kernels over caller buffers (device pointers) ------------------------------ */
 /* Narrowphase: manifolds for n shape pairs (b2CollidePolygons / b2CollideCircles /
  * b2CollidePolygonAndCircle / b2CollideEdgeAndCircle / b2CollideEdgeAndPolygon,

@@ -2310,6 +2310,150 @@ int orc_world_solver_order(void* h, int32_t* ccol, uint32_t* cprio, int32_t nc, 
   return 0;
 }
 
+// ---- world queries (brute force over the world's fixtures) --------------------------------
+// b2World::QueryAABB (src/dynamics/b2_world.cpp:1193-1207 over b2BroadPhase::Query,
+// include/box2d/b2_broad_phase.h:622-644): fixtures whose AABB overlaps the box, ascending; a
+// world of one fixture reports it for any box (the tree's root leaf is reported untested).
+int32_t orc_world_query_aabb(void* h, const float* box4, int32_t* out, int32_t cap) {
+  World* w = (World*)h;
+  AABB q;
+  q.lo = v2(box4[0], box4[1]);
+  q.hi = v2(box4[2], box4[3]);
+  int32_t n = 0;
+  for (size_t f = 0; f < w->fixtures.size(); ++f) {
+    const Fixture& fx = w->fixtures[f];
+    AABB bb = computeAABB(fx.shape, w->bodies[fx.body].xf);
+    if (w->fixtures.size() == 1 || overlap(bb, q)) {
+      if (n < cap) out[n] = (int32_t)f;
+      ++n;
+    }
+  }
+  return n;
+}
+
+struct RayOut {
+  float fraction;
+  V2 normal;
+};
+
+// b2PolygonShape::RayCast (src/collision/b2_polygon_shape.cpp:303-364)
+static bool rayPolygon(const Shape& s, const Xf& xf, V2 P1, V2 P2, float maxFraction, RayOut* out) {
+  V2 p1 = mulT(xf.q, P1 - xf.p), p2 = mulT(xf.q, P2 - xf.p);
+  V2 d = p2 - p1;
+  float lower = 0.0f, upper = maxFraction;
+  int index = -1;
+  for (int i = 0; i < s.count; ++i) {
+    float num = dot(s.n[i], s.v[i] - p1);
+    float den = dot(s.n[i], d);
+    if (den == 0.0f) {
+      if (num < 0.0f) return false;
+    } else if (den < 0.0f && num < lower * den) {
+      lower = num / den;
+      index = i;
+    } else if (den > 0.0f && num < upper * den) {
+      upper = num / den;
+    }
+    if (upper < lower) return false;
+  }
+  if (index < 0) return false;
+  out->fraction = lower;
+  out->normal = mul(xf.q, s.n[index]);
+  return true;
+}
+
+// b2CircleShape::RayCast (src/collision/b2_circle_shape.cpp:56-87)
+static bool rayCircle(const Shape& s, const Xf& xf, V2 P1, V2 P2, float maxFraction, RayOut* out) {
+  V2 position = xf.p + mul(xf.q, s.v[0]);
+  V2 sv = P1 - position;
+  float b = dot(sv, sv) - s.radius * s.radius;
+  V2 r = P2 - P1;
+  float c = dot(sv, r);
+  float rr = dot(r, r);
+  float sigma = c * c - rr * b;
+  if (sigma < 0.0f || rr < 1.192092896e-07f) return false;
+  float a = -(c + sqrtf(sigma));
+  if (!(0.0f <= a && a <= maxFraction * rr)) return false;
+  a /= rr;
+  out->fraction = a;
+  V2 n = sv + a * r;
+  normalize(n);
+  out->normal = n;
+  return true;
+}
+
+// b2EdgeShape::RayCast (src/collision/b2_edge_shape.cpp:89-149)
+static bool rayEdge(const Shape& s, const Xf& xf, V2 P1, V2 P2, float maxFraction, RayOut* out) {
+  V2 p1 = mulT(xf.q, P1 - xf.p), p2 = mulT(xf.q, P2 - xf.p);
+  V2 d = p2 - p1;
+  V2 v1 = s.v[0], v2_ = s.v[1];
+  V2 e = v2_ - v1;
+  V2 normal = v2(e.y, -e.x);
+  normalize(normal);
+  float num = dot(normal, v1 - p1);
+  if (s.oneSided && num > 0.0f) return false;
+  float den = dot(normal, d);
+  if (den == 0.0f) return false;
+  float t = num / den;
+  if (t < 0.0f || maxFraction < t) return false;
+  V2 q = p1 + t * d;
+  V2 r = v2_ - v1;
+  float rr = dot(r, r);
+  if (rr == 0.0f) return false;
+  float sc = dot(q - v1, r) / rr;
+  if (sc < 0.0f || 1.0f < sc) return false;
+  out->fraction = t;
+  out->normal = num > 0.0f ? -mul(xf.q, normal) : mul(xf.q, normal);
+  return true;
+}
+
+// b2World::RayCast with a closest-hit callback (src/dynamics/b2_world.cpp:1209-1238 over
+// b2BroadPhase::RayCast, include/box2d/b2_broad_phase.h:646-710): every fixture whose AABB
+// passes the segment-box and separating-axis tests is ray cast against the segment clipped to
+// the best fraction so far. Returns the fixture index (-1: no hit); out5 = point, normal,
+// fraction. A tie keeps the lower index.
+int32_t orc_world_raycast(void* h, const float* ray4, float* out5) {
+  World* w = (World*)h;
+  V2 p1 = v2(ray4[0], ray4[1]), p2 = v2(ray4[2], ray4[3]);
+  V2 r = p2 - p1;
+  if (normalize(r) == 0.0f) return -1;
+  V2 v = cross(1.0f, r);
+  V2 absV = v2(fabsf(v.x), fabsf(v.y));
+  float maxFraction = 1.0f;
+  int best = -1;
+  RayOut bo = {0.0f, v2(0.0f, 0.0f)};
+  for (size_t f = 0; f < w->fixtures.size(); ++f) {
+    const Fixture& fx = w->fixtures[f];
+    const Xf& xf = w->bodies[fx.body].xf;
+    AABB bb = computeAABB(fx.shape, xf);
+    V2 t = p1 + maxFraction * (p2 - p1);
+    AABB seg;
+    seg.lo = vmin(p1, t);
+    seg.hi = vmax(p1, t);
+    if (!overlap(bb, seg)) continue;
+    V2 c = 0.5f * (bb.lo + bb.hi);
+    V2 hh = 0.5f * (bb.hi - bb.lo);
+    float separation = fabsf(dot(v, p1 - c)) - dot(absV, hh);
+    if (separation > 0.0f) continue;
+    RayOut o;
+    bool hit = fx.shape.type == 0 ? rayCircle(fx.shape, xf, p1, p2, maxFraction, &o)
+               : fx.shape.type == 1 ? rayEdge(fx.shape, xf, p1, p2, maxFraction, &o)
+                                    : rayPolygon(fx.shape, xf, p1, p2, maxFraction, &o);
+    if (!hit) continue;
+    if (best >= 0 && o.fraction == bo.fraction) continue;  // fixtures are visited in ascending order
+    best = (int)f;
+    bo = o;
+    maxFraction = o.fraction;
+  }
+  if (best < 0) return -1;
+  V2 point = (1.0f - bo.fraction) * p1 + bo.fraction * p2;
+  out5[0] = point.x;
+  out5[1] = point.y;
+  out5[2] = bo.normal.x;
+  out5[3] = bo.normal.y;
+  out5[4] = bo.fraction;
+  return best;
+}
+
 // The Gauss-Seidel order of the last step: (fixture A, fixture B) per solved contact and joint
 // indices, both in solve order. Returns the number of solved contacts.
 int32_t orc_world_last_order(void* h, int32_t* pairs, int32_t cap_pairs, int32_t* joints, int32_t cap_joints,

@@ -409,6 +409,58 @@ void ref_world_set_bodies(void* h, const b2g_body* in) {
 // the solver contacts in the order given by (fixture_a, fixture_b) pairs, and the joints in the
 // given creation-index order; the rest follows b2World::Step (src/dynamics/b2_world.cpp:1108-1171)
 // and b2World::Solve (:492-670) with sleeping off. Contacts not listed are not solved.
+// b2World::RayCast with a closest-hit callback (ties keep the lower fixture index); returns the
+// fixture index or -1, out5 = point, normal, fraction.
+struct RefClosestHit : public b2RayCastCallback {
+  RefWorld* rw;
+  int best = -1;
+  b2Vec2 point, normal;
+  float fraction = 1.0f;
+  float ReportFixture(b2Fixture* fixture, const b2Vec2& p, const b2Vec2& n, float f) override {
+    int idx = rw->fixture_index[fixture];
+    if (best < 0 || f < fraction || (f == fraction && idx < best)) {
+      best = idx;
+      point = p;
+      normal = n;
+      fraction = f;
+    }
+    return f;
+  }
+};
+
+int32_t ref_world_raycast(void* h, const float* ray4, float* out5) {
+  RefWorld* rw = (RefWorld*)h;
+  RefClosestHit cb;
+  cb.rw = rw;
+  rw->world->RayCast(&cb, b2Vec2(ray4[0], ray4[1]), b2Vec2(ray4[2], ray4[3]));
+  if (cb.best < 0) return -1;
+  out5[0] = cb.point.x; out5[1] = cb.point.y; out5[2] = cb.normal.x; out5[3] = cb.normal.y; out5[4] = cb.fraction;
+  return cb.best;
+}
+
+// b2World::QueryAABB: the reported fixtures, ascending; returns their number.
+struct RefQuery : public b2QueryCallback {
+  RefWorld* rw;
+  std::vector<int32_t> found;
+  bool ReportFixture(b2Fixture* fixture) override {
+    found.push_back(rw->fixture_index[fixture]);
+    return true;
+  }
+};
+
+int32_t ref_world_query_aabb(void* h, const float* box4, int32_t* out, int32_t cap) {
+  RefWorld* rw = (RefWorld*)h;
+  RefQuery cb;
+  cb.rw = rw;
+  b2AABB box;
+  box.lowerBound = b2Vec2(box4[0], box4[1]);
+  box.upperBound = b2Vec2(box4[2], box4[3]);
+  rw->world->QueryAABB(&cb, box);
+  std::sort(cb.found.begin(), cb.found.end());
+  for (size_t i = 0; i < cb.found.size() && (int32_t)i < cap; ++i) out[i] = cb.found[i];
+  return (int32_t)cb.found.size();
+}
+
 int ref_replay_step(void* h, float dt, int32_t vi, int32_t pi, const int32_t* contact_pairs,
                     int32_t nc, const int32_t* joint_order, int32_t nj) {
   RefWorld* rw = (RefWorld*)h;

@@ -41,6 +41,8 @@ class Ref:
             "ref_world_fixtures": ([vp, P(G.Fixture)], None),
             "ref_world_joints": ([vp, P(G.Joint)], None),
             "ref_world_contacts": ([vp, P(G.Contact), i32], i32),
+            "ref_world_raycast": ([vp, P(f32), P(f32)], i32),
+            "ref_world_query_aabb": ([vp, P(f32), P(i32), i32], i32),
             "ref_world_set_bodies": ([vp, P(G.Body)], None),
             "ref_replay_step": ([vp, f32, i32, i32, P(i32), i32, P(i32), i32], C.c_int),
             "ref_worlds_step_parallel": ([P(vp), i32, f32, i32, i32, i32, i32], C.c_double),
@@ -54,6 +56,21 @@ class Ref:
         return getattr(self.lib, name)
 
 
+def _raycast(fn, h, ray):
+    r = (f32 * 4)(*ray)
+    o = (f32 * 5)()
+    f = fn(h, r, o)
+    return (f, tuple(o[:2]), tuple(o[2:4]), o[4]) if f >= 0 else (-1, None, None, None)
+
+
+def _query(fn, h, box, cap=4096):
+    b = (f32 * 4)(*box)
+    out = (i32 * cap)()
+    n = fn(h, b, out, cap)
+    assert n <= cap
+    return list(out[:n])
+
+
 class RefWorld:
     """A reference b2World built by one of the shared scene recipes."""
 
@@ -64,6 +81,7 @@ class RefWorld:
         self.h = ref.ref_scene_world(kind, seed, n, p0, p1, gravity[0], gravity[1], counts)
         self.counts = tuple(counts)
         ref.ref_world_set_flags(self.h, int(allow_sleep), int(warm), int(continuous))
+        self._raycast_fn, self._query_fn = ref.ref_world_raycast, ref.ref_world_query_aabb
 
     def close(self):
         if self.h:
@@ -99,6 +117,13 @@ class RefWorld:
         self.ref.ref_world_joints(self.h, arr)
         return arr[:nj]
 
+    def raycast(self, ray):
+        """Closest hit (fixture, point, normal, fraction) of the segment ray = (x1, y1, x2, y2)."""
+        return _raycast(self._raycast_fn, self.h, ray)
+
+    def query_aabb(self, box):
+        return _query(self._query_fn, self.h, box)
+
     def contacts(self):
         n = self.ref.ref_world_contacts(self.h, None, 0)
         arr = (G.Contact * max(n, 1))()
@@ -128,6 +153,8 @@ class Oracle:
             "orc_world_contacts": ([vp, P(G.Contact), i32], i32),
             "orc_world_solver_order": ([vp, P(i32), P(u32), i32, P(i32), P(u32), i32], C.c_int),
             "orc_world_last_order": ([vp, P(i32), i32, P(i32), i32, P(i32)], i32),
+            "orc_world_raycast": ([vp, P(f32), P(f32)], i32),
+            "orc_world_query_aabb": ([vp, P(f32), P(i32), i32], i32),
             "orc_set_libm_trig": ([i32], None),
             "orc_pairs": ([P(f32), i32, P(C.c_uint64), C.c_int64], C.c_int64),
             "orc_worlds_step_parallel": ([P(vp), i32, f32, i32, i32, i32, i32], C.c_double),
@@ -156,6 +183,7 @@ class OracleWorld:
         st = orc.orc_world_load(self.h, B, nb, F, nf, J, nj, Cc, nc, inv_dt0)
         if st != 0:
             raise RuntimeError(f"orc_world_load failed: {st}")
+        self._raycast_fn, self._query_fn = orc.orc_world_raycast, orc.orc_world_query_aabb
 
     def close(self):
         if self.h:
@@ -184,6 +212,13 @@ class OracleWorld:
         arr = (G.Joint * max(nj, 1))()
         self.orc.orc_world_joints(self.h, arr)
         return arr[:nj]
+
+    def raycast(self, ray):
+        """Closest hit (fixture, point, normal, fraction) of the segment ray = (x1, y1, x2, y2)."""
+        return _raycast(self._raycast_fn, self.h, ray)
+
+    def query_aabb(self, box):
+        return _query(self._query_fn, self.h, box)
 
     def contacts(self):
         n = self.orc.orc_world_contacts(self.h, None, 0)

@@ -1,0 +1,52 @@
+"""The C ABI without a GPU: libb2g.so loads, exports every entry point include/*.h declares, the
+ctypes binding declares them all, and the record layouts match the header's stated sizes."""
+import ctypes as C
+import re
+from pathlib import Path
+
+import b2gpu as G
+
+ROOT = Path(__file__).resolve().parents[1]
+
+
+def _declared():
+    names = set()
+    for h in (ROOT / "include").glob("*.h"):
+        text = h.read_text()
+        names |= set(re.findall(r"B2G_API\s+[\w\s\*]+?\b(b2g_\w+)\s*\(", text))
+    return names
+
+
+def test_library_exports_every_declared_entry_point():
+    names = _declared()
+    assert len(names) > 40
+    lib = C.CDLL(str(G.LIB_PATH))
+    missing = sorted(n for n in names if not hasattr(lib, n))
+    assert not missing, missing
+
+
+def test_binding_declares_every_entry_point():
+    assert _declared() == set(G.Lib.SYMBOLS)
+
+
+def test_record_sizes_match_the_header():
+    sizes = {"b2g_shape": G.Shape, "b2g_manifold_point": None, "b2g_manifold": G.Manifold, "b2g_body": G.Body,
+             "b2g_ray_hit": G.RayHit}
+    stated = {"b2g_shape": 152, "b2g_manifold": 64, "b2g_body": 96, "b2g_ray_hit": 24}
+    for name, n in stated.items():
+        assert C.sizeof(sizes[name]) == n, name
+    for name, n in G.RECORD_SIZES.items():
+        if sizes.get(name) is not None:
+            assert C.sizeof(sizes[name]) == n, name
+
+
+def test_host_only_batch_builds_and_reads_back():
+    lib = G.Lib()
+    b = G.Batch(lib, device=G.HOST_ONLY)
+    w = b.add_world(0.0, -10.0)
+    b.scene(w, G.SCENE_PYRAMID, n=5, p0=1.0, p1=0.6)
+    nb, nf, nj, nc = b.sizes(w)
+    assert nb == 16 and nf == 16 and nj == 0
+    bodies = b.bodies(w)
+    assert bodies[1].mass > 0 and bodies[0].type == 0
+    b.close()

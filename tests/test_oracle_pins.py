@@ -170,3 +170,45 @@ def test_host_scene_setup_vs_reference_live(ref, kind, n, seed, p0):
     assert [bytes(x) for x in hb.fixtures(w)] == [bytes(x) for x in rw.fixtures()]
     assert [bytes(x.def_)[:-8] for x in hb.joints(w)] == [bytes(x.def_)[:-8] for x in rw.joints()]
     hb.close()
+
+
+def _query_cases(bodies, rng, n_rays=300, n_boxes=120):
+    """Seeded rays and boxes over the scene's extent (bodies' centres, padded)."""
+    c = np.array([[b.c[0], b.c[1]] for b in bodies], dtype=np.float64)
+    lo, hi = c.min(axis=0) - 3.0, c.max(axis=0) + 3.0
+    rays = []
+    for _ in range(n_rays):
+        p1 = rng.uniform(lo, hi)
+        p2 = rng.uniform(lo, hi)
+        rays.append(tuple(float(np.float32(v)) for v in (*p1, *p2)))
+    boxes = []
+    for _ in range(n_boxes):
+        a = rng.uniform(lo, hi)
+        ext = rng.uniform(0.05, 4.0, size=2)
+        boxes.append(tuple(float(np.float32(v)) for v in (a[0], a[1], a[0] + ext[0], a[1] + ext[1])))
+    return rays, boxes
+
+
+@pytest.mark.parametrize("kind,n,seed,p0", [
+    (G.SCENE_PYRAMID, 20, 1, 1.0), (G.SCENE_MIXED_DROP, 400, 3, 1.0), (G.SCENE_CHAINS, 12, 2, 200.0)])
+def test_oracle_queries_vs_reference_live(ref, orc, kind, n, seed, p0):
+    """b2World::RayCast (closest hit) and QueryAABB of the reference after 40 steps, against the
+    oracle's brute force over the same bodies: identical fixtures, points, normals, fractions."""
+    rw = ob.RefWorld(ref, kind, seed=seed, n=n, p0=p0)
+    rw.step(40)
+    ow = ob.OracleWorld(orc, (0.0, -10.0), rw.bodies(), rw.fixtures(), rw.joints())
+    rays, boxes = _query_cases(rw.bodies(), np.random.default_rng(seed))
+    hits = 0
+    for ray in rays:
+        r, o = rw.raycast(ray), ow.raycast(ray)
+        assert r == o, (ray, r, o)
+        hits += r[0] >= 0
+    assert hits > len(rays) // 10
+    found = 0
+    for box in boxes:
+        r, o = rw.query_aabb(box), ow.query_aabb(box)
+        assert r == o, box
+        found += len(r)
+    assert found > 0
+    rw.close()
+    ow.close()
