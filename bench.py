@@ -175,6 +175,50 @@ def serve(lib, dev, seconds, rate, seed0, budget=120 << 30):
             "request_ms_p50": q(lat, 50), "request_ms_p99": q(lat, 99), "ticks": len(steps_ms)}
 
 
+def query_bench(batch, n_rays):
+    """Rays per second (closest hit) and AABB queries per second over all worlds of the batch,
+    timed end to end through the C ABI (inputs copied in, results copied out)."""
+    import numpy as np  # noqa: PLC0415
+
+    rng = np.random.default_rng(99)
+    count = C.c_int32()
+    batch.lib.check(batch.lib.b2g_world_count(batch.h, C.byref(count)), "world_count")
+    nw = count.value
+    worlds = rng.integers(0, nw, size=n_rays).astype(np.int32)
+    # rays over a 40 m x 40 m window around each world's origin region (the scenes start near it)
+    p1 = rng.uniform([-20.0, -2.0], [20.0, 38.0], size=(n_rays, 2))
+    p2 = p1 + rng.uniform(-15.0, 15.0, size=(n_rays, 2))
+    rays = np.concatenate([p1, p2], axis=1).astype(np.float32)
+    out = (G.RayHit * n_rays)()
+    wp = worlds.ctypes.data_as(C.POINTER(C.c_int32))
+    rp = rays.ctypes.data_as(C.POINTER(C.c_float))
+    batch.lib.check(batch.lib.b2g_raycast_closest(batch.h, wp, rp, n_rays, out), "raycast")  # warm-up
+    t0 = time.perf_counter()
+    reps = 3
+    for _ in range(reps):
+        batch.lib.check(batch.lib.b2g_raycast_closest(batch.h, wp, rp, n_rays, out), "raycast")
+    ray_s = (time.perf_counter() - t0) / reps
+    hit = int((np.frombuffer(out, dtype=np.int32).reshape(n_rays, 6)[:, 0] >= 0).sum())
+    nq = n_rays // 4
+    lo = rng.uniform([-20.0, -2.0], [20.0, 38.0], size=(nq, 2))
+    boxes = np.concatenate([lo, lo + rng.uniform(0.2, 3.0, size=(nq, 2))], axis=1).astype(np.float32)
+    qw = worlds[:nq].copy()
+    counts = (C.c_int32 * nq)()
+    cap = 64 * nq
+    found = (C.c_int32 * cap)()
+    total = C.c_int64()
+    args_q = (batch.h, qw.ctypes.data_as(C.POINTER(C.c_int32)), boxes.ctypes.data_as(C.POINTER(C.c_float)), nq,
+              counts, found, cap, C.byref(total))
+    batch.lib.check(batch.lib.b2g_query_aabb(*args_q), "query_aabb")
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        batch.lib.check(batch.lib.b2g_query_aabb(*args_q), "query_aabb")
+    q_s = (time.perf_counter() - t0) / reps
+    return {"rays": n_rays, "raycasts_per_s": n_rays / ray_s, "ray_hit_fraction": hit / n_rays,
+            "aabb_queries": nq, "aabb_queries_per_s": nq / q_s, "fixtures_reported_per_query": total.value / nq,
+            "timing": "end to end through the C ABI with host buffers, mean of 3 calls after a warm-up call"}
+
+
 def build_batch(lib, seeds, device):
     batch = G.Batch(lib, device=device)
     nb = 0
@@ -333,6 +377,12 @@ def run_ours(args, rank, world_size):
     e2e_s = time.perf_counter() - t1
     e2e_value = nb * e2e_steps / e2e_s * world_size
 
+    # world queries on the settled batch: closest-hit ray casts and AABB queries, end to end
+    # through the C ABI (host buffers in and out), seeded rays over each world's extent
+    queries = None
+    if args.rays > 0:
+        queries = query_bench(batch, args.rays)
+
     # per-phase breakdown: one eager (non-graph) step after the timed region
     lib.b2g_batch_set_graphs(batch.h, 0)
     batch.step(DT, VI, PI)
@@ -416,6 +466,7 @@ def run_ours(args, rank, world_size):
                     "d2h_bytes_per_step": 16 * nbody, "steps": e2e_steps},
             "gpu_launches": kernels_per_step * args.steps,
             "contact_constraint_iterations_per_s": contact_iters,
+            "queries": queries,
             "clocks": clocks.summary(),
         }
     batch.close()
@@ -460,6 +511,7 @@ def main():
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--serve-seconds", type=float, default=12.0)
     ap.add_argument("--no-autotune", action="store_true", help="keep the default solver threads per world")
+    ap.add_argument("--rays", type=int, default=1 << 20, help="rays of the world-query measurement (0: skip)")
     ap.add_argument("--profile-window", action="store_true",
                     help="ncu case: settle --settle steps, then 2 steps inside the NVTX range 'profile'")
     ap.add_argument("--settle", type=int, default=250)
