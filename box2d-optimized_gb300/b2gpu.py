@@ -221,7 +221,7 @@ class Lib:
         "b2g_profile_get", "b2g_solver_order", "b2g_collide", "b2g_pairs", "b2g_scene_build",
         "b2g_batch_world_params", "b2g_server_create", "b2g_server_destroy", "b2g_server_submit",
         "b2g_server_tick", "b2g_server_poll", "b2g_server_stats", "b2g_status_string",
-        "b2g_last_error", "b2g_device_count", "b2g_query_aabb", "b2g_raycast_closest",
+        "b2g_last_error", "b2g_device_count", "b2g_query_aabb", "b2g_raycast_closest", "b2g_world_status",
     ]
 
     def __init__(self, path: os.PathLike | str | None = None):
@@ -267,6 +267,7 @@ class Lib:
             "b2g_batch_set_solver_threads": ([vp, P(i32)], C.c_int),
             "b2g_batch_get_solver_threads": ([vp, P(i32)], C.c_int),
             "b2g_batch_autotune": ([vp, i32, f32, i32, i32, P(i32), P(i32)], C.c_int),
+            "b2g_world_status": ([vp, i32, P(i32)], C.c_int),
             "b2g_query_aabb": ([vp, P(i32), P(f32), i32, P(i32), P(i32), i64, P(i64)], C.c_int),
             "b2g_raycast_closest": ([vp, P(i32), P(f32), i32, P(RayHit)], C.c_int),
             "b2g_solver_order": ([vp, i32, P(i32), P(u32), i32, P(i32), P(u32), i32], C.c_int),
@@ -410,6 +411,12 @@ class Batch:
         self.lib.check(self.lib.b2g_batch_autotune(self.h, steps, dt, vi, pi, arr, C.byref(taken)),
                        "b2g_batch_autotune")
         return list(arr), taken.value
+
+    def world_status(self, world):
+        """B2G_OK, or B2G_E_WORLD_FAULT once the world was frozen after a non-finite state."""
+        st = C.c_int32()
+        self.lib.check(self.lib.b2g_world_status(self.h, world, C.byref(st)), "b2g_world_status")
+        return st.value
 
     def raycast(self, worlds, rays):
         """Closest hit of each ray (x1, y1, x2, y2) in its world: list of

@@ -109,7 +109,7 @@ static int upload(Batch* b, DBuf<T>& buf, const std::vector<T>& v) {
 static KernelArgs make_args(Batch* b) {
   KernelArgs a;
   memset(&a, 0, sizeof(a));
-  a.wb = b->wb.p; a.wj = b->wj.p; a.wg = b->wg.p; a.wflags = b->wflags.p; a.wc = b->wc.p;
+  a.wb = b->wb.p; a.wj = b->wj.p; a.wg = b->wg.p; a.wflags = b->wflags.p; a.wc = b->wc.p; a.wfault = b->wfault.p;
   a.world_order = b->world_order.p;
   a.xf = b->xf.p; a.pos = b->pos.p; a.vel = b->vel.p; a.massd = b->massd.p; a.damp = b->damp.p;
   a.force = b->force.p; a.lc = b->lc.p; a.btype = b->btype.p; a.bworld = b->bworld.p;
@@ -312,6 +312,8 @@ int upload_all(Batch* b) {
   }
   TRY(ensure(b, b->wbounds, NW)); TRY(ensure(b, b->wroot, NW));
   TRY(ensure(b, b->ncolors, 4 * (size_t)NW)); TRY(ensure(b, b->jranges, 65 * (size_t)NW));
+  TRY(ensure(b, b->wfault, NW));
+  CUDA_TRY(b, cudaMemsetAsync(b->wfault.p, 0, b->wfault.cap, b->stream));
   TRY(upload(b, b->xf, xf)); TRY(upload(b, b->pos, pos)); TRY(upload(b, b->vel, vel)); TRY(upload(b, b->massd, massd));
   TRY(upload(b, b->damp, damp)); TRY(upload(b, b->force, force)); TRY(upload(b, b->lc, lc));
   TRY(upload(b, b->btype, btype)); TRY(upload(b, b->bworld, bworld));
@@ -507,6 +509,10 @@ int upload_tail(Batch* b) {
   TRY(st.add(b, b->wflags, 0, wflags)); TRY(st.add(b, b->world_order, 0, order)); TRY(st.add(b, b->wc, w0, wc_tail));
   b->h_wflags = wflags;
   TRY(ensure(b, b->wbounds, NW)); TRY(ensure(b, b->wroot, NW)); TRY(ensure(b, b->ncolors, 4 * (size_t)NW, true));
+  if (b->wfault.cap < (size_t)NW) {  // flags are zero between steps: a grown array starts zeroed
+    TRY(ensure(b, b->wfault, NW));
+    CUDA_TRY(b, cudaMemsetAsync(b->wfault.p, 0, b->wfault.cap, b->stream));
+  }
   TRY(ensure(b, b->jranges, 65 * (size_t)NW, true));
   TRY(st.add(b, b->xf, NB0, xf)); TRY(st.add(b, b->pos, NB0, pos)); TRY(st.add(b, b->vel, NB0, vel));
   TRY(st.add(b, b->massd, NB0, massd)); TRY(st.add(b, b->damp, NB0, damp)); TRY(st.add(b, b->force, NB0, force));
@@ -715,6 +721,20 @@ static void enqueue_step(Batch* b, float dt, int vi, int pi, bool initial_bp, in
   if (record_profile) cudaEventRecord(b->ev[4], b->stream);
 }
 
+// Worlds whose state became non-finite in the last step are frozen (retired: no kernel touches
+// them again) and marked faulted; the other worlds of the batch are unaffected.
+static int freeze_faulted_worlds(Batch* b) {
+  std::vector<uint8_t> f(b->NW);
+  if (b->NW > 0) {
+    CUDA_TRY(b, cudaMemcpyAsync(f.data(), b->wfault.p, b->NW, cudaMemcpyDeviceToHost, b->stream));
+    CUDA_TRY(b, cudaMemsetAsync(b->wfault.p, 0, b->NW, b->stream));
+    CUDA_TRY(b, cudaStreamSynchronize(b->stream));
+  }
+  for (int w = 0; w < b->NW; ++w)
+    if (f[w]) b->worlds[w].flags |= B2G_WF_RETIRED | B2G_WF_FAULTED;
+  return B2G_OK;
+}
+
 static int check_status(Batch* b, unsigned int st) {
   if (st & B2G_DEV_NONFINITE) {
     set_error(b, "a world produced a non-finite body state");
@@ -776,6 +796,10 @@ static int finish_step(Batch* b, int live_before_last_bp) {
     overflow = r[B2G_CNT_OVERFLOW];
   }
   b->NC = (int64_t)r[B2G_CNT_CONTACTS];
+  if (status_word & B2G_DEV_NONFINITE) {
+    TRY(freeze_faulted_worlds(b));
+    status_word &= ~B2G_DEV_NONFINITE;
+  }
   TRY(drain_device_events(b, r[B2G_CNT_EVENTS]));
   b->profile.touching = (int64_t)r[B2G_CNT_TOUCHING];
   b->profile.touching_total += (int64_t)r[B2G_CNT_TOUCHING];
@@ -1018,7 +1042,7 @@ B2G_API int b2g_batch_destroy(b2g_batch* b) {
   if (b->h_readback) cudaFreeHost(b->h_readback);
   if (b->h_stage) cudaFreeHost(b->h_stage);
   if (b->stage_ev) cudaEventDestroy(b->stage_ev);
-  release(b, b->wb); release(b, b->wj); release(b, b->wg); release(b, b->wflags); release(b, b->wc);
+  release(b, b->wb); release(b, b->wj); release(b, b->wg); release(b, b->wflags); release(b, b->wc); release(b, b->wfault);
   release(b, b->world_order); release(b, b->xf); release(b, b->pos); release(b, b->vel); release(b, b->massd);
   release(b, b->damp); release(b, b->force); release(b, b->lc); release(b, b->btype); release(b, b->bworld);
   release(b, b->shape); release(b, b->fbody); release(b, b->fgroup); release(b, b->fsensor); release(b, b->fworld);
@@ -1220,6 +1244,12 @@ static int compact_device(Batch* b, int32_t* old_to_new, int32_t n) {
   launch_joint_colour(make_args(b), 0, kept, s);
   TRY(check_upload_status(b));
   b->layout_version++;
+  return B2G_OK;
+}
+
+B2G_API int b2g_world_status(b2g_batch* b, int32_t world, int32_t* status) {
+  if (!world_index_ok(b, world) || !status) return B2G_E_INVALID_ARG;
+  *status = (b->worlds[world].flags & B2G_WF_FAULTED) ? B2G_E_WORLD_FAULT : B2G_OK;
   return B2G_OK;
 }
 

@@ -68,6 +68,7 @@ struct VCDev {
 #define B2G_WF_ACTIVE 4
 #define B2G_WF_NEW_CONTACTS 8
 #define B2G_WF_RETIRED 16
+#define B2G_WF_FAULTED 32  // produced a non-finite state: frozen (retired) and reported
 
 struct HostWorld {
   float gx = 0.0f, gy = -10.0f;
@@ -134,6 +135,7 @@ struct Batch {
   DBuf<float4> wg;                // gx, gy, inv_dt0, -
   DBuf<int> wflags;
   DBuf<int2> wc;                  // contact_off, contact_cnt
+  DBuf<uint8_t> wfault;           // set by the solver when the world's state became non-finite
   DBuf<int> world_order;          // worlds sorted by work, largest first
 
   DBuf<float4> xf, pos, vel, massd, damp, force;

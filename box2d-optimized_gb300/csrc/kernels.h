@@ -38,6 +38,7 @@ struct KernelArgs {
   float4* wg;
   const int* wflags;
   int2* wc;
+  uint8_t* wfault;
   const int* world_order;
 
   float4 *xf, *pos, *vel;

@@ -184,10 +184,20 @@ B2G_API int b2g_server_tick(b2g_server* s, int32_t* active, double* step_ms) {
     if (step_ms) *step_ms = (now_s() - t0) * 1e3;
     if (st != B2G_OK) return st;
   }
-  // retire finished requests
+  // retire finished requests; a request whose world faulted (non-finite state) ends with that
+  // status, the others run on unaffected
   std::vector<Request> still;
   for (Request& r : s->active) {
     ++r.done;
+    int32_t wst = B2G_OK;
+    b2g_world_status(s->batch, r.world, &wst);
+    if (wst != B2G_OK) {
+      ++s->retired;
+      s->in_use -= r.bytes;
+      ++s->rejected;
+      finish(s, r, wst, nullptr);
+      continue;
+    }
     if (r.done >= r.steps) {
       float cs[4];
       int st = world_checksum(s, r.world, cs);

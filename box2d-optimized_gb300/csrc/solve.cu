@@ -656,7 +656,10 @@ __global__ void __launch_bounds__(T, 1024 / T) k_solve(KernelArgs a, int first, 
     if (!isfinite(p4.x) || !isfinite(p4.y) || !isfinite(p4.z) || !isfinite(v4.x) || !isfinite(v4.y) || !isfinite(v4.z))
       bad = 1;
   }
-  if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(a.status, B2G_DEV_NONFINITE);
+  if (__syncthreads_or(bad) && threadIdx.x == 0) {  // the host freezes this world; the others go on
+    a.wfault[w] = 1;
+    atomicOr(a.status, B2G_DEV_NONFINITE);
+  }
   if (a.events_on) {
     for (int p = threadIdx.x; p < nsc; p += T) {
       int pc = (P.idx[c0 + p].x >> 24) & 15;

@@ -274,6 +274,10 @@ B2G_API int b2g_fixtures_add(b2g_batch* b, int32_t world, const b2g_fixture_def*
 B2G_API int b2g_joints_add(b2g_batch* b, int32_t world, const b2g_joint_def* defs, int32_t n,
                            int32_t* out_ids);
 
+/* Whether a world is still stepped: *status = B2G_E_WORLD_FAULT once a step left one of its
+ * bodies with a non-finite position or velocity. Such a world is frozen (no later step touches
+ * it; its last state stays readable) while the other worlds of the batch go on. */
+B2G_API int b2g_world_status(b2g_batch* b, int32_t world, int32_t* status);
 /* Retires a world (it is no longer stepped; its contacts go at the next broadphase) and
  * b2g_compact removes retired worlds, writing each old index's new index (-1 = removed) into
  * old_to_new. (The reference's b2World destructor, src/dynamics/b2_world.cpp:71-101, for worlds

@@ -258,6 +258,34 @@ def test_appended_worlds_match_alone(lib):
     first.close()
 
 
+def test_nonfinite_world_is_frozen_alone(lib):
+    """A world driven to a non-finite state (infinite forces: a floating-point fault, nothing on
+    the device faults) is frozen and reported; the other worlds step on exactly as if it were
+    not in the batch."""
+    seeds, sizes = [71, 72, 73], [300, 500, 200]
+    b, ws = _mixed_batch(lib, seeds, sizes)
+    for _ in range(10):
+        b.step(1 / 60, 8, 3)
+    counts = [b.sizes(w)[0] for w in ws]
+    forces = np.zeros((sum(counts), 4), dtype=np.float32)
+    forces[counts[0]:counts[0] + counts[1], 1] = np.inf
+    lib.check(lib.b2g_batch_set_forces(b.h, forces.ctypes.data_as(C.POINTER(C.c_float)), len(forces)), "forces")
+    b.step(1 / 60, 8, 3)
+    assert b.world_status(ws[1]) == 4 and b.world_status(ws[0]) == 0 and b.world_status(ws[2]) == 0
+    frozen = _state_bytes(b.bodies(ws[1]))
+    assert not np.isfinite(G.body_array_to_numpy((G.Body * counts[1])(*b.bodies(ws[1])))["c"]).all()
+    for _ in range(20):
+        b.step(1 / 60, 8, 3)
+    assert _state_bytes(b.bodies(ws[1])) == frozen
+    other, wo = _mixed_batch(lib, [seeds[0], seeds[2]], [sizes[0], sizes[2]])
+    for _ in range(31):
+        other.step(1 / 60, 8, 3)
+    assert _state_bytes(b.bodies(ws[0])) == _state_bytes(other.bodies(wo[0]))
+    assert _state_bytes(b.bodies(ws[2])) == _state_bytes(other.bodies(wo[1]))
+    b.close()
+    other.close()
+
+
 def test_masked_step_leaves_other_worlds(lib):
     b = G.Batch(lib, device=0)
     w0 = b.add_world(0, -10)
