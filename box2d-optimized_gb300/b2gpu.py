@@ -222,6 +222,7 @@ class Lib:
         "b2g_batch_world_params", "b2g_server_create", "b2g_server_destroy", "b2g_server_submit",
         "b2g_server_tick", "b2g_server_poll", "b2g_server_stats", "b2g_status_string",
         "b2g_last_error", "b2g_device_count", "b2g_query_aabb", "b2g_raycast_closest", "b2g_world_status",
+        "b2g_world_snapshot", "b2g_world_restore",
     ]
 
     def __init__(self, path: os.PathLike | str | None = None):
@@ -268,6 +269,8 @@ class Lib:
             "b2g_batch_get_solver_threads": ([vp, P(i32)], C.c_int),
             "b2g_batch_autotune": ([vp, i32, f32, i32, i32, P(i32), P(i32)], C.c_int),
             "b2g_world_status": ([vp, i32, P(i32)], C.c_int),
+            "b2g_world_snapshot": ([vp, i32, vp, C.c_uint64, P(C.c_uint64)], C.c_int),
+            "b2g_world_restore": ([vp, vp, C.c_uint64, P(i32)], C.c_int),
             "b2g_query_aabb": ([vp, P(i32), P(f32), i32, P(i32), P(i32), i64, P(i64)], C.c_int),
             "b2g_raycast_closest": ([vp, P(i32), P(f32), i32, P(RayHit)], C.c_int),
             "b2g_solver_order": ([vp, i32, P(i32), P(u32), i32, P(i32), P(u32), i32], C.c_int),
@@ -411,6 +414,23 @@ class Batch:
         self.lib.check(self.lib.b2g_batch_autotune(self.h, steps, dt, vi, pi, arr, C.byref(taken)),
                        "b2g_batch_autotune")
         return list(arr), taken.value
+
+    def snapshot(self, world) -> bytes:
+        """The world's complete state (checkpoint) as bytes."""
+        size = C.c_uint64()
+        st = self.lib.lib.b2g_world_snapshot(self.h, world, None, 0, C.byref(size))
+        if st not in (0, 7):  # B2G_OK for an empty world, B2G_E_CAPACITY otherwise
+            self.lib.check(st, "b2g_world_snapshot")
+        buf = C.create_string_buffer(size.value)
+        self.lib.check(self.lib.b2g_world_snapshot(self.h, world, buf, size.value, C.byref(size)), "b2g_world_snapshot")
+        return buf.raw[:size.value]
+
+    def restore(self, blob: bytes) -> int:
+        """Appends a world from a snapshot; returns its index."""
+        w = C.c_int32()
+        buf = C.create_string_buffer(blob, len(blob))
+        self.lib.check(self.lib.b2g_world_restore(self.h, buf, len(blob), C.byref(w)), "b2g_world_restore")
+        return w.value
 
     def world_status(self, world):
         """B2G_OK, or B2G_E_WORLD_FAULT once the world was frozen after a non-finite state."""

@@ -1095,6 +1095,105 @@ B2G_API int b2g_world_add(b2g_batch* b, float gx, float gy, int32_t* out_world) 
   return B2G_OK;
 }
 
+// ---- checkpoint / resume: one world's complete state as a self-describing byte blob
+extern "C++" {
+namespace {
+const uint32_t kSnapMagic = 0x53473242u;  // "B2GS"
+const uint32_t kSnapVersion = 1;
+struct SnapshotHeader {
+  uint32_t magic, version;
+  uint32_t nb, nf, nj, nc;
+  float gx, gy, inv_dt0;
+  int32_t flags;
+  uint8_t allow_sleep, continuous, pad[2];
+  uint32_t record_size[4];  // b2g_body, b2g_fixture, b2g_joint, b2g_contact
+};
+uint64_t snapshot_bytes(const HostWorld& w) {
+  return sizeof(SnapshotHeader) + w.bodies.size() * (sizeof(b2g_body) + 8) +
+         w.fixtures.size() * (sizeof(b2g_fixture) + 8) + w.joints.size() * sizeof(b2g_joint) +
+         w.contacts.size() * sizeof(b2g_contact);
+}
+template <typename T>
+void put(uint8_t*& p, const std::vector<T>& v) {
+  if (!v.empty()) memcpy(p, v.data(), v.size() * sizeof(T));
+  p += v.size() * sizeof(T);
+}
+template <typename T>
+void get(const uint8_t*& p, std::vector<T>& v, size_t n) {
+  v.resize(n);
+  if (n) memcpy(v.data(), p, n * sizeof(T));
+  p += n * sizeof(T);
+}
+}  // namespace
+}  // extern "C++"
+
+B2G_API int b2g_world_snapshot(b2g_batch* b, int32_t world, void* buf, uint64_t cap, uint64_t* size) {
+  if (!world_index_ok(b, world) || !size || (cap > 0 && !buf)) return B2G_E_INVALID_ARG;
+  TRY(download_state(b));  // the host records hold the live state, contacts and impulses included
+  const HostWorld& w = b->worlds[world];
+  *size = snapshot_bytes(w);
+  if (cap < *size) {
+    set_error(b, "snapshot buffer too small");
+    return B2G_E_CAPACITY;
+  }
+  SnapshotHeader h;
+  memset(&h, 0, sizeof(h));
+  h.magic = kSnapMagic;
+  h.version = kSnapVersion;
+  h.nb = (uint32_t)w.bodies.size(); h.nf = (uint32_t)w.fixtures.size();
+  h.nj = (uint32_t)w.joints.size(); h.nc = (uint32_t)w.contacts.size();
+  h.gx = w.gx; h.gy = w.gy; h.inv_dt0 = w.inv_dt0;
+  h.flags = w.flags & ~(B2G_WF_ACTIVE | B2G_WF_RETIRED | B2G_WF_FAULTED);
+  h.allow_sleep = w.allow_sleep; h.continuous = w.continuous;
+  h.record_size[0] = sizeof(b2g_body); h.record_size[1] = sizeof(b2g_fixture);
+  h.record_size[2] = sizeof(b2g_joint); h.record_size[3] = sizeof(b2g_contact);
+  uint8_t* p = (uint8_t*)buf;
+  memcpy(p, &h, sizeof(h));
+  p += sizeof(h);
+  put(p, w.bodies); put(p, w.body_user); put(p, w.fixtures); put(p, w.fixture_user);
+  put(p, w.joints); put(p, w.contacts);
+  return B2G_OK;
+}
+
+B2G_API int b2g_world_restore(b2g_batch* b, const void* buf, uint64_t size, int32_t* out_world) {
+  if (!b || !buf || size < sizeof(SnapshotHeader)) return B2G_E_INVALID_ARG;
+  SnapshotHeader h;
+  memcpy(&h, buf, sizeof(h));
+  if (h.magic != kSnapMagic || h.version != kSnapVersion || h.record_size[0] != sizeof(b2g_body) ||
+      h.record_size[1] != sizeof(b2g_fixture) || h.record_size[2] != sizeof(b2g_joint) ||
+      h.record_size[3] != sizeof(b2g_contact)) {
+    set_error(b, "not a world snapshot of this format");
+    return B2G_E_INVALID_ARG;
+  }
+  HostWorld w;
+  w.gx = h.gx; w.gy = h.gy; w.inv_dt0 = h.inv_dt0; w.flags = h.flags;
+  w.allow_sleep = h.allow_sleep != 0; w.continuous = h.continuous != 0;
+  if (sizeof(SnapshotHeader) + (uint64_t)h.nb * (sizeof(b2g_body) + 8) + (uint64_t)h.nf * (sizeof(b2g_fixture) + 8) +
+          (uint64_t)h.nj * sizeof(b2g_joint) + (uint64_t)h.nc * sizeof(b2g_contact) != size) {
+    set_error(b, "snapshot size does not match its counts");
+    return B2G_E_INVALID_ARG;
+  }
+  const uint8_t* p = (const uint8_t*)buf + sizeof(SnapshotHeader);
+  get(p, w.bodies, h.nb); get(p, w.body_user, h.nb); get(p, w.fixtures, h.nf); get(p, w.fixture_user, h.nf);
+  get(p, w.joints, h.nj); get(p, w.contacts, h.nc);
+  // indices must stay inside the world
+  for (const b2g_fixture& f : w.fixtures)
+    if (f.body < 0 || f.body >= (int32_t)h.nb) return B2G_E_INVALID_ARG;
+  for (const b2g_joint& j : w.joints)
+    if (j.def.body_a < 0 || j.def.body_a >= (int32_t)h.nb || j.def.body_b < 0 || j.def.body_b >= (int32_t)h.nb)
+      return B2G_E_INVALID_ARG;
+  for (const b2g_contact& c : w.contacts)
+    if (c.fixture_a < 0 || c.fixture_a >= (int32_t)h.nf || c.fixture_b < 0 || c.fixture_b >= (int32_t)h.nf)
+      return B2G_E_INVALID_ARG;
+  w.body_fixtures.assign(h.nb, {});
+  for (uint32_t f = 0; f < h.nf; ++f) w.body_fixtures[w.fixtures[f].body].push_back((int)f);
+  // the restored contacts (with their impulses) enter through a full layout upload
+  TRY(begin_edit(b));
+  b->worlds.push_back(std::move(w));
+  if (out_world) *out_world = (int32_t)b->worlds.size() - 1;
+  return B2G_OK;
+}
+
 B2G_API int b2g_world_count(b2g_batch* b, int32_t* out_n) {
   if (!b || !out_n) return B2G_E_INVALID_ARG;
   *out_n = (int32_t)b->worlds.size();

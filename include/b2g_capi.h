@@ -274,6 +274,16 @@ B2G_API int b2g_fixtures_add(b2g_batch* b, int32_t world, const b2g_fixture_def*
 B2G_API int b2g_joints_add(b2g_batch* b, int32_t world, const b2g_joint_def* defs, int32_t n,
                            int32_t* out_ids);
 
+/* Checkpoint / resume. b2g_world_snapshot writes one world's complete state (bodies, fixtures,
+ * joints with their warm-start impulses, the live contacts with their manifolds and impulses,
+ * gravity, the previous step's inverse time step, flags) into buf as a self-describing blob of
+ * *size bytes (pass cap = 0 to learn the size: B2G_E_CAPACITY). b2g_world_restore appends such a
+ * world to a batch (any batch); stepping it continues bit-identically to the original. A
+ * restore re-lays out the batch at its next step. (The reference has b2World::Dump,
+ * src/dynamics/b2_world.cpp:1469-1531, which writes C++ code and no contacts; this is the
+ * binary resume it lacks.) */
+B2G_API int b2g_world_snapshot(b2g_batch* b, int32_t world, void* buf, uint64_t cap, uint64_t* size);
+B2G_API int b2g_world_restore(b2g_batch* b, const void* buf, uint64_t size, int32_t* out_world);
 /* Whether a world is still stepped: *status = B2G_E_WORLD_FAULT once a step left one of its
  * bodies with a non-finite position or velocity. Such a world is frozen (no later step touches
  * it; its last state stays readable) while the other worlds of the batch go on. */

@@ -50,3 +50,25 @@ def test_host_only_batch_builds_and_reads_back():
     bodies = b.bodies(w)
     assert bodies[1].mass > 0 and bodies[0].type == 0
     b.close()
+
+
+def test_snapshot_round_trip_on_the_host():
+    """A world's snapshot restores into an equal world (host-only batch: no device involved),
+    and malformed blobs are rejected with INVALID_ARG."""
+    lib = G.Lib()
+    b = G.Batch(lib, device=G.HOST_ONLY)
+    w = b.add_world(0.5, -9.0)
+    b.scene(w, G.SCENE_CHAINS, seed=3, n=6, p0=40.0, p1=0.6)
+    blob = b.snapshot(w)
+    w2 = b.restore(blob)
+    assert b.sizes(w2) == b.sizes(w)
+    assert [bytes(x) for x in b.bodies(w2)] == [bytes(x) for x in b.bodies(w)]
+    assert [bytes(x) for x in b.joints(w2)] == [bytes(x) for x in b.joints(w)]
+    assert b.snapshot(w2) == blob
+    bad = bytearray(blob)
+    bad[0] ^= 0xFF
+    st = lib.lib.b2g_world_restore(b.h, C.create_string_buffer(bytes(bad), len(bad)), len(bad), None)
+    assert st == 1
+    st = lib.lib.b2g_world_restore(b.h, C.create_string_buffer(blob[:-8], len(blob) - 8), len(blob) - 8, None)
+    assert st == 1
+    b.close()
