@@ -17,7 +17,7 @@ LIB_PATH = PKG_DIR / "_build" / "libb2g.so"
 
 B2G_OK = 0
 STATUS = {0: "OK", 1: "INVALID_ARG", 2: "OUT_OF_MEMORY", 3: "TIMEOUT", 4: "WORLD_FAULT", 5: "CUDA",
-          6: "LOCKED", 7: "CAPACITY"}
+          6: "LOCKED", 7: "CAPACITY", 8: "CANCELLED"}
 
 STATIC, KINEMATIC, DYNAMIC = 0, 1, 2
 SHAPE_CIRCLE, SHAPE_EDGE, SHAPE_POLYGON = 0, 1, 2
@@ -185,6 +185,10 @@ class Server:
         self.lib.check(self.lib.b2g_server_poll(self.h, arr, cap, C.byref(n)), "poll")
         return arr[:n.value]
 
+    def cancel(self, request_id):
+        """Cancels a queued or running request (it finishes with status B2G_E_CANCELLED)."""
+        return self.lib.b2g_server_cancel(self.h, request_id)
+
     def stats(self):
         v = [C.c_int64() for _ in range(5)]
         self.lib.check(self.lib.b2g_server_stats(self.h, *[C.byref(x) for x in v]), "stats")
@@ -213,7 +217,8 @@ class Lib:
         "b2g_batch_create", "b2g_batch_destroy", "b2g_world_add", "b2g_world_count",
         "b2g_world_set_gravity", "b2g_world_set_flags", "b2g_bodies_add", "b2g_fixtures_add",
         "b2g_joints_add", "b2g_world_sizes", "b2g_step", "b2g_step_n", "b2g_step_timed",
-        "b2g_batch_set_forces", "b2g_batch_set_graphs", "b2g_batch_set_solver_threads",
+        "b2g_batch_set_forces", "b2g_batch_set_graphs", "b2g_batch_set_debug_checks",
+        "b2g_batch_set_solver_threads",
         "b2g_batch_get_solver_threads", "b2g_batch_autotune", "b2g_world_retire", "b2g_compact", "b2g_debug_set_contact_capacity",
         "b2g_pairs_static", "b2g_reserve",
         "b2g_bodies_read", "b2g_bodies_write", "b2g_batch_read_states", "b2g_fixtures_read",
@@ -222,7 +227,7 @@ class Lib:
         "b2g_batch_world_params", "b2g_server_create", "b2g_server_destroy", "b2g_server_submit",
         "b2g_server_tick", "b2g_server_poll", "b2g_server_stats", "b2g_status_string",
         "b2g_last_error", "b2g_device_count", "b2g_query_aabb", "b2g_raycast_closest", "b2g_world_status",
-        "b2g_world_snapshot", "b2g_world_restore",
+        "b2g_world_snapshot", "b2g_world_restore", "b2g_server_cancel",
     ]
 
     def __init__(self, path: os.PathLike | str | None = None):
@@ -269,6 +274,8 @@ class Lib:
             "b2g_batch_get_solver_threads": ([vp, P(i32)], C.c_int),
             "b2g_batch_autotune": ([vp, i32, f32, i32, i32, P(i32), P(i32)], C.c_int),
             "b2g_world_status": ([vp, i32, P(i32)], C.c_int),
+            "b2g_server_cancel": ([vp, i64], C.c_int),
+            "b2g_batch_set_debug_checks": ([vp, i32], C.c_int),
             "b2g_world_snapshot": ([vp, i32, vp, C.c_uint64, P(C.c_uint64)], C.c_int),
             "b2g_world_restore": ([vp, vp, C.c_uint64, P(i32)], C.c_int),
             "b2g_query_aabb": ([vp, P(i32), P(f32), i32, P(i32), P(i32), i64, P(i64)], C.c_int),
@@ -396,6 +403,14 @@ class Batch:
         self.lib.check(self.lib.b2g_contacts_read(self.h, world, arr, n.value, C.byref(n)),
                        "b2g_contacts_read")
         return arr[:n.value]
+
+    def set_graphs(self, enable=True):
+        """Whether unmasked steps replay a captured CUDA graph (default on)."""
+        self.lib.check(self.lib.b2g_batch_set_graphs(self.h, int(enable)), "b2g_batch_set_graphs")
+
+    def set_debug_checks(self, enable=True):
+        """Verify every step's constraint colouring on the device (a violation fails the step)."""
+        self.lib.check(self.lib.b2g_batch_set_debug_checks(self.h, int(enable)), "b2g_batch_set_debug_checks")
 
     def solver_threads(self, threads=None):
         """Threads per world CTA of the solver for the five size classes (sets when given)."""

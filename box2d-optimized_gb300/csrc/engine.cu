@@ -16,11 +16,23 @@
 #include <string>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "b2g_math.cuh"
 #include "engine.h"
 #include "kernels.h"
 
 namespace b2g {
+
+// Host-side NVTX range around an engine phase (upload, tail broadphase, step, readback,
+// compaction, queries). NVTX is header-only and costs a branch when no profiler is attached;
+// under a profiler the ranges group each phase's launches on the timeline.
+struct NvtxRange {
+  explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+  NvtxRange(const NvtxRange&) = delete;
+  NvtxRange& operator=(const NvtxRange&) = delete;
+};
 
 static thread_local std::string g_last_error;
 
@@ -51,6 +63,7 @@ static int ensure(Batch* b, DBuf<T>& buf, size_t n, bool keep = false) {
   T* p = nullptr;
   cudaError_t e = cudaMalloc(&p, bytes);
   if (e != cudaSuccess) {
+    cudaGetLastError();  // a failed allocation leaves the context usable: clear the error
     set_error(b, std::string("cudaMalloc: ") + cudaGetErrorString(e));
     return e == cudaErrorMemoryAllocation ? B2G_E_OUT_OF_MEMORY : B2G_E_CUDA;
   }
@@ -69,8 +82,17 @@ static int ensure(Batch* b, DBuf<T>& buf, size_t n, bool keep = false) {
 // Reallocates `buf` at exactly n elements (keeping the first min(n, old) when `keep`).
 template <typename T>
 static int resize_exact(Batch* b, DBuf<T>& buf, size_t n, bool keep) {
+  if (b->budget && b->allocated - buf.cap * sizeof(T) + n * sizeof(T) > b->budget) {
+    set_error(b, "device memory budget exceeded");
+    return B2G_E_OUT_OF_MEMORY;
+  }
   T* p = nullptr;
-  if (cudaMalloc(&p, n * sizeof(T)) != cudaSuccess) return B2G_E_OUT_OF_MEMORY;
+  cudaError_t e = cudaMalloc(&p, n * sizeof(T));
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    set_error(b, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    return e == cudaErrorMemoryAllocation ? B2G_E_OUT_OF_MEMORY : B2G_E_CUDA;
+  }
   if (keep && buf.p) cudaMemcpyAsync(p, buf.p, std::min(n, buf.cap) * sizeof(T), cudaMemcpyDeviceToDevice, b->stream);
   cudaStreamSynchronize(b->stream);
   if (buf.p) {
@@ -708,6 +730,7 @@ static void enqueue_step(Batch* b, float dt, int vi, int pi, bool initial_bp, in
   if (record_profile) cudaEventRecord(b->ev[1], b->stream);
   if (dt > 0.0f) {
     launch_solve(a, b->solve_classes, b->stream, b->side, b->fork_ev);
+    if (b->debug_checks) launch_colour_check(a, b->NW, b->stream);
     b->last_solve_buf = src;
     if (record_profile) cudaEventRecord(b->ev[2], b->stream);
     enqueue_broadphase(b, a, src);
@@ -740,6 +763,10 @@ static int check_status(Batch* b, unsigned int st) {
     set_error(b, "a world produced a non-finite body state");
     return B2G_E_WORLD_FAULT;
   }
+  if (st & B2G_DEV_COLOUR_CONFLICT) {
+    set_error(b, "colouring check failed: a regular colour holds two constraints of one body");
+    return B2G_E_CAPACITY;
+  }
   if (st & (B2G_DEV_STACK_OVERFLOW | B2G_DEV_COLOR_ROUNDS)) {
     set_error(b, "device capacity check failed (status " + std::to_string(st) + ")");
     return B2G_E_CAPACITY;
@@ -769,6 +796,7 @@ static int drain_device_events(Batch* b, unsigned long long n) {
 // overflow: the overflowing broadphase skipped its emission, so the live list is still the
 // pre-broadphase one (with this step's manifolds); grow the buffers and redo the broadphase.
 static int finish_step(Batch* b, int live_before_last_bp) {
+  NvtxRange range("b2g.readback");
   b->h_readback[5] = 0;
   CUDA_TRY(b, cudaMemcpyAsync(b->h_readback, b->counters.p, 5 * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
                               b->stream));
@@ -810,6 +838,7 @@ static int finish_step(Batch* b, int live_before_last_bp) {
 // fixtures, src/dynamics/b2_world.cpp:1113-1122): a broadphase over the appended fixtures only,
 // appended to the live list (the other worlds' bodies have not moved since their broadphase).
 static int tail_broadphase(Batch* b, float dt, int vi, int pi, int f0, int w0) {
+  NvtxRange range("b2g.tail_broadphase");
   for (int guard = 0;; ++guard) {
     if (guard > 8) {
       set_error(b, "pair buffer kept overflowing");
@@ -862,6 +891,7 @@ static int capture_graphs(Batch* b, float dt, int vi, int pi) {
 // One b2World::Step (src/dynamics/b2_world.cpp:1108-1171) for the worlds selected by mask.
 int step_batch(Batch* b, float dt, int vi, int pi, const uint8_t* mask, bool sync) {
   (void)sync;
+  NvtxRange range("b2g.step");
   if (!(dt >= 0.0f) || vi < 0 || pi < 0) {
     set_error(b, "invalid step arguments");
     return B2G_E_INVALID_ARG;
@@ -874,9 +904,11 @@ int step_batch(Batch* b, float dt, int vi, int pi, const uint8_t* mask, bool syn
   int tail_w0 = -1, tail_f0 = 0;
   if (b->status.p) CUDA_TRY(b, cudaMemsetAsync(b->status.p, 0, sizeof(unsigned int), b->stream));
   if (b->structure_dirty) {
+    NvtxRange upload_range("b2g.upload");
     TRY(upload_all(b));
     invalidate_graphs(b);
   } else if ((int)b->worlds.size() > b->NW) {
+    NvtxRange upload_range("b2g.upload_tail");
     tail_w0 = b->NW;
     tail_f0 = b->NF;
     TRY(upload_tail(b));
@@ -978,12 +1010,13 @@ struct b2g_batch : public Batch {};
 
 uint64_t b2g::batch_allocated_bytes(const b2g_batch* b) { return b ? b->allocated : 0; }
 
-static const char* kStatusNames[] = {"OK", "INVALID_ARG", "OUT_OF_MEMORY", "TIMEOUT", "WORLD_FAULT", "CUDA", "LOCKED", "CAPACITY"};
+static const char* kStatusNames[] = {"OK",   "INVALID_ARG", "OUT_OF_MEMORY", "TIMEOUT",  "WORLD_FAULT",
+                                     "CUDA", "LOCKED",      "CAPACITY",      "CANCELLED"};
 
 extern "C" {
 
 B2G_API const char* b2g_status_string(int status) {
-  if (status < 0 || status > 7) return "UNKNOWN";
+  if (status < 0 || status >= (int)(sizeof(kStatusNames) / sizeof(kStatusNames[0]))) return "UNKNOWN";
   return kStatusNames[status];
 }
 
@@ -1224,6 +1257,7 @@ B2G_API int b2g_world_retire(b2g_batch* b, int32_t world) {
 // array (compact.cu), the small world table and the joint-no-collide list are rebuilt on the
 // host, and the joint colouring is recomputed; no body, fixture or contact state crosses the bus.
 static int compact_device(Batch* b, int32_t* old_to_new, int32_t n) {
+  NvtxRange range("b2g.compact");
   CUDA_TRY(b, cudaSetDevice(b->device));
   cudaStream_t s = b->stream;
   const int NW = b->NW;
@@ -1558,6 +1592,13 @@ B2G_API int b2g_debug_set_contact_capacity(b2g_batch* b, int64_t cap) {
 B2G_API int b2g_batch_set_graphs(b2g_batch* b, int32_t enable) {
   if (!b) return B2G_E_INVALID_ARG;
   b->use_graphs = enable != 0;
+  return B2G_OK;
+}
+
+B2G_API int b2g_batch_set_debug_checks(b2g_batch* b, int32_t enable) {
+  if (!b) return B2G_E_INVALID_ARG;
+  if (b->debug_checks != (enable != 0)) b->layout_version++;  // captured graphs lack or hold the check
+  b->debug_checks = enable != 0;
   return B2G_OK;
 }
 
@@ -1896,6 +1937,7 @@ B2G_API int b2g_query_aabb(b2g_batch* b, const int32_t* worlds, const float* box
     return B2G_E_INVALID_ARG;
   *total = 0;
   if (n == 0) return B2G_OK;
+  NvtxRange range("b2g.query_aabb");
   TRY(ensure_query_trees(b));
   cudaStream_t s = b->stream;
   TRY(ensure(b, b->q_world, n)); TRY(ensure(b, b->q_box, n)); TRY(ensure(b, b->q_counts, n));
@@ -1927,6 +1969,7 @@ B2G_API int b2g_query_aabb(b2g_batch* b, const int32_t* worlds, const float* box
 B2G_API int b2g_raycast_closest(b2g_batch* b, const int32_t* worlds, const float* rays, int32_t n, b2g_ray_hit* hits) {
   if (!b || n < 0 || (n > 0 && (!worlds || !rays || !hits))) return B2G_E_INVALID_ARG;
   if (n == 0) return B2G_OK;
+  NvtxRange range("b2g.raycast");
   TRY(ensure_query_trees(b));
   cudaStream_t s = b->stream;
   TRY(ensure(b, b->q_world, n)); TRY(ensure(b, b->q_box, n)); TRY(ensure(b, b->q_hits, n));

@@ -105,6 +105,7 @@ struct SolveClass {
 #define B2G_DEV_NONFINITE 2u
 #define B2G_DEV_PAIR_OVERFLOW 4u
 #define B2G_DEV_COLOR_ROUNDS 8u
+#define B2G_DEV_COLOUR_CONFLICT 16u  // debug check: one regular colour holds two constraints of a body
 
 struct EventDev {
   int kind, world, fixtureA, fixtureB, pointCount;
@@ -122,6 +123,7 @@ struct Batch {
   bool device_state_valid = false; // device holds the live dynamic state
   bool host_state_stale = false;   // host mirrors are older than the device
   bool events_on = false;
+  bool debug_checks = false;       // verify each step's constraint colouring on the device
   std::string error;
 
   // totals of the current device layout

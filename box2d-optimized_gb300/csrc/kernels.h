@@ -138,6 +138,10 @@ void launch_collide(const KernelArgs& a, cudaStream_t s);
 void launch_solve(const KernelArgs& a, const std::vector<SolveClass>& classes, cudaStream_t s,
                   const cudaStream_t* side, const cudaEvent_t* ev);
 void launch_joint_colour(const KernelArgs& a, int w0, int nw, cudaStream_t s);
+// Debug check of the last solve's colouring: within every regular colour (0-62) of every active
+// world, no two contact constraints and no two joints share a non-static body; a violation
+// raises B2G_DEV_COLOUR_CONFLICT. Uses the per-body colour masks as scratch.
+void launch_colour_check(const KernelArgs& a, int nw, cudaStream_t s);
 
 // ---- world queries (query.cu)
 void launch_query_count(const KernelArgs& a, int n, const int* qw, const float4* qbox, int* counts, cudaStream_t s);

@@ -265,7 +265,10 @@ extern "C" B2G_API int b2g_pairs(const float* d_aabbs, int32_t n, uint64_t* d_pa
   }
   size_t bytes = b2g::pairs_scratch_bytes(n);
   void* base = nullptr;
-  if (cudaMalloc(&base, bytes) != cudaSuccess) return B2G_E_OUT_OF_MEMORY;
+  if (cudaMalloc(&base, bytes) != cudaSuccess) {
+    cudaGetLastError();  // clear the failed allocation's error; the context stays usable
+    return B2G_E_OUT_OF_MEMORY;
+  }
   size_t cub_bytes = 0, cub_scan = 0;
   cub::DeviceRadixSort::SortPairs((void*)nullptr, cub_bytes, (uint32_t*)nullptr, (uint32_t*)nullptr, (int*)nullptr,
                                   (int*)nullptr, n, 0, 30);

@@ -192,6 +192,7 @@ B2G_API int b2g_server_tick(b2g_server* s, int32_t* active, double* step_ms) {
     int32_t wst = B2G_OK;
     b2g_world_status(s->batch, r.world, &wst);
     if (wst != B2G_OK) {
+      b2g_world_retire(s->batch, r.world);
       ++s->retired;
       s->in_use -= r.bytes;
       ++s->rejected;
@@ -222,6 +223,28 @@ B2G_API int b2g_server_tick(b2g_server* s, int32_t* active, double* step_ms) {
     s->retired = 0;
   }
   return B2G_OK;
+}
+
+B2G_API int b2g_server_cancel(b2g_server* s, int64_t request_id) {
+  if (!s) return B2G_E_INVALID_ARG;
+  for (auto it = s->queue.begin(); it != s->queue.end(); ++it) {
+    if (it->id != request_id) continue;
+    Request r = *it;
+    s->queue.erase(it);
+    finish(s, r, B2G_E_CANCELLED, nullptr);
+    return B2G_OK;
+  }
+  for (auto it = s->active.begin(); it != s->active.end(); ++it) {
+    if (it->id != request_id) continue;
+    Request r = *it;
+    s->active.erase(it);
+    b2g_world_retire(s->batch, r.world);
+    ++s->retired;
+    s->in_use -= r.bytes;
+    finish(s, r, B2G_E_CANCELLED, nullptr);
+    return B2G_OK;
+  }
+  return B2G_E_INVALID_ARG;
 }
 
 B2G_API int b2g_server_poll(b2g_server* s, b2g_request_result* out, int32_t cap, int32_t* n) {

@@ -709,6 +709,42 @@ __global__ void __launch_bounds__(T) k_joint_colour(KernelArgs a, int w0) {
   if (threadIdx.x == 0) a.ncolors[4 * w + 1] = njc;
 }
 
+// One block per world: each constraint of a regular colour sets its colour's bit in the masks of
+// its non-static bodies; a bit found already set is a conflict. Contacts first, then (masks
+// cleared) joints, since the two sets are solved in separate sweeps.
+__device__ __forceinline__ void colour_mark(unsigned long long* mask, int2 cb, int col, unsigned int* status) {
+  if (col < 0 || col >= 63) return;  // the serial colour is solved by one thread
+  const unsigned long long bit = 1ull << col;
+  const int ends[2] = {cb.x, cb.y};
+#pragma unroll
+  for (int e = 0; e < 2; ++e) {
+    if (ends[e] < 0) continue;  // static body (bit 31 set)
+    if (atomicOr(&mask[ends[e]], bit) & bit) atomicOr(status, B2G_DEV_COLOUR_CONFLICT);
+  }
+}
+
+__global__ void __launch_bounds__(256) k_colour_check(KernelArgs a) {
+  const int w = blockIdx.x;
+  if ((a.wflags[w] & B2G_WF_ACTIVE) == 0) return;
+  const int4 wb = a.wb[w];
+  const int b0 = wb.x, nb = wb.y;
+  unsigned long long* mask = a.inc_mask + b0;
+  for (int i = threadIdx.x; i < nb; i += blockDim.x) mask[i] = 0ull;
+  __syncthreads();
+  const int nsc = a.ncolors[4 * w + 2], c0 = a.ncolors[4 * w + 3];
+  for (int k = threadIdx.x; k < nsc; k += blockDim.x) colour_mark(mask, a.scb[c0 + k], a.ccol[c0 + k], a.status);
+  __syncthreads();
+  for (int i = threadIdx.x; i < nb; i += blockDim.x) mask[i] = 0ull;
+  __syncthreads();
+  const int4 wj = a.wj[w];
+  const int j0 = wj.x, nj = wj.y;
+  for (int k = threadIdx.x; k < nj; k += blockDim.x) colour_mark(mask, a.jcb[j0 + k], a.jcol[j0 + k], a.status);
+}
+
+void launch_colour_check(const KernelArgs& a, int nw, cudaStream_t s) {
+  if (nw > 0) k_colour_check<<<nw, 256, 0, s>>>(a);
+}
+
 // ---- launch planning
 // Class by world body count: threads per CTA and the dynamic shared memory that holds the
 // world's body state and inverse masses (24 B/body) and, room permitting, its colouring arrays

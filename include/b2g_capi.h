@@ -38,6 +38,7 @@ extern "C" {
 #define B2G_E_CUDA 5          /* a CUDA runtime call failed (no device, launch error, ...)    */
 #define B2G_E_LOCKED 6        /* world is locked (inside a step)                              */
 #define B2G_E_CAPACITY 7      /* a fixed-size buffer is too small for the request            */
+#define B2G_E_CANCELLED 8     /* a served request was cancelled before it finished            */
 
 /* ---- enums mirroring the reference's values ---------------------------------------------- */
 /* b2BodyType, include/box2d/b2_body.h:44-49 */
@@ -320,6 +321,11 @@ B2G_API int b2g_batch_set_forces(b2g_batch* b, const float* f4, int64_t n_bodies
 /* Whether b2g_step replays the Step as a captured CUDA graph (default on). A graph is used for
  * unmasked steps with dt > 0 and events off; it is re-captured when buffers move. */
 B2G_API int b2g_batch_set_graphs(b2g_batch* b, int32_t enable);
+/* Debug checks (default off): after every solve, a device pass verifies that no regular colour
+ * of the constraint colouring holds two contacts or two joints on the same non-static body;
+ * a violation makes the step return B2G_E_CAPACITY with a message. Costs one small launch per
+ * step. No reference counterpart (the reference solves serially). */
+B2G_API int b2g_batch_set_debug_checks(b2g_batch* b, int32_t enable);
 /* Threads per world CTA of the solver for each world size class (worlds of at most 64, 256,
  * 1024 and 4096 bodies, and larger), 5 entries each one of 64, 128, 256, 512, 1024 (defaults
  * 64, 128, 256, 512, 1024). A tuning knob: results do not depend on it. No reference counterpart. */
@@ -462,6 +468,10 @@ B2G_API int b2g_server_submit(b2g_server* s, uint32_t seed, int32_t bodies, int3
  * *active receives the number of worlds stepped; *step_ms the step's wall time. */
 B2G_API int b2g_server_tick(b2g_server* s, int32_t* active, double* step_ms);
 B2G_API int b2g_server_poll(b2g_server* s, b2g_request_result* out, int32_t cap, int32_t* n);
+/* Cancels a queued or running request: it finishes at once with status B2G_E_CANCELLED (its
+ * world, if admitted, is retired; the other requests are unaffected). B2G_E_INVALID_ARG when the
+ * request is unknown or already finished. */
+B2G_API int b2g_server_cancel(b2g_server* s, int64_t request_id);
 B2G_API int b2g_server_stats(b2g_server* s, int64_t* queued, int64_t* active,
                              int64_t* completed, int64_t* rejected, int64_t* hbm_bytes);
 

@@ -72,3 +72,21 @@ def test_snapshot_round_trip_on_the_host():
     st = lib.lib.b2g_world_restore(b.h, C.create_string_buffer(blob[:-8], len(blob) - 8), len(blob) - 8, None)
     assert st == 1
     b.close()
+
+
+def test_server_cancels_queued_requests_without_a_device():
+    """Queued requests cancel on the host: they finish with CANCELLED and zero steps; unknown or
+    already finished ids are INVALID_ARG."""
+    lib = G.Lib()
+    srv = G.Server(lib, device=G.HOST_ONLY, budget_bytes=1 << 30, max_worlds=4)
+    a = srv.submit(1, 100, 10)
+    b = srv.submit(2, 100, 10)
+    assert srv.cancel(b) == 0
+    assert srv.cancel(b) == 1
+    assert srv.cancel(12345) == 1
+    res = srv.poll()
+    assert [(r.request_id, r.status, r.steps) for r in res] == [(b, 8, 0)]
+    assert srv.stats()["queued"] == 1
+    assert srv.cancel(a) == 0
+    assert srv.stats()["queued"] == 0
+    srv.close()

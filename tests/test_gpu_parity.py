@@ -464,3 +464,50 @@ def test_snapshot_resumes_bit_identically(lib):
     fresh.close()
     twin.close()
     b.close()
+
+
+def test_colouring_check_passes_and_changes_nothing(lib):
+    """With the device colouring check on, every step of worlds in every size class (and worlds
+    with joint chains and a dense pyramid) passes it, and the results equal those without it."""
+    out = []
+    for checks in (True, False):
+        b, ws = _mixed_batch(lib, CLASS_SEEDS, CLASS_SIZES)
+        for kind, n, p0 in ((G.SCENE_CHAINS, 12, 30.0), (G.SCENE_PYRAMID, 40, 1.0)):
+            w = b.add_world(0.0, -10.0)
+            b.set_flags(w)
+            b.scene(w, kind, seed=5, n=n, p0=p0, p1=0.6)
+            ws.append(w)
+        b.set_debug_checks(checks)
+        for s in range(30):
+            b.step(1 / 60, 8, 3)
+            if s == 10:
+                b.set_graphs(False)
+        out.append([_state_bytes(b.bodies(w)) for w in ws])
+        b.close()
+    assert out[0] == out[1]
+
+
+def test_budget_exhaustion_fails_cleanly(lib):
+    """A batch whose device memory budget cannot hold its worlds fails the step with
+    OUT_OF_MEMORY and a message (no partial state is stepped); the batch closes cleanly and a
+    batch with room steps the same world to the same bits as one without a budget."""
+    _, gx, gy = _params(lib, 41)
+    tight = G.Batch(lib, device=0, budget_bytes=2 << 20)
+    w = tight.add_world(gx, gy)
+    tight.set_flags(w)
+    tight.scene(w, G.SCENE_BATCH_WORLD, seed=41, n=6000)
+    with pytest.raises(G.B2GError, match="OUT_OF_MEMORY"):
+        tight.step(1 / 60, 8, 3)
+    assert "budget" in lib.b2g_last_error().decode()
+    tight.close()
+    out = []
+    for budget in (0, 1 << 30):
+        b = G.Batch(lib, device=0, budget_bytes=budget)
+        w = b.add_world(gx, gy)
+        b.set_flags(w)
+        b.scene(w, G.SCENE_BATCH_WORLD, seed=41, n=6000)
+        for _ in range(10):
+            b.step(1 / 60, 8, 3)
+        out.append(_state_bytes(b.bodies(w)))
+        b.close()
+    assert out[0] == out[1]

@@ -67,3 +67,28 @@ def test_admission_respects_budget_and_rejects_oversize(lib):
             break
     assert {a, b, c} <= done
     srv.close()
+
+
+def test_cancel_mid_rollout_leaves_the_others_unchanged(lib):
+    """A running request cancelled mid-rollout finishes with CANCELLED after the steps it took; its
+    world's slot and budget are released and the requests served beside it end exactly as alone."""
+    alone = {}
+    for q in REQS[:3]:
+        alone.update(_run(lib, [q], [0]))
+    srv = G.Server(lib, device=0, budget_bytes=8 << 30, max_worlds=64)
+    ids = {srv.submit(seed, n, k): seed for seed, n, k in REQS[:3]}
+    victim = srv.submit(999, 1200, 500)
+    results, tick = {}, 0
+    while srv.stats()["active"] or srv.stats()["queued"]:
+        srv.tick()
+        tick += 1
+        if tick == 6:
+            assert srv.cancel(victim) == 0
+            assert srv.cancel(victim) == 1  # already finished
+        for r in srv.poll():
+            results[r.request_id] = (r.status, r.steps, tuple(r.checksum))
+        assert tick < 1000
+    assert results[victim][:2] == (8, 6)
+    for rid, seed in ids.items():
+        assert results[rid] == alone[seed], seed
+    srv.close()
