@@ -227,7 +227,8 @@ class Lib:
         "b2g_batch_world_params", "b2g_server_create", "b2g_server_destroy", "b2g_server_submit",
         "b2g_server_tick", "b2g_server_poll", "b2g_server_stats", "b2g_status_string",
         "b2g_last_error", "b2g_device_count", "b2g_query_aabb", "b2g_raycast_closest", "b2g_world_status",
-        "b2g_world_snapshot", "b2g_world_restore", "b2g_server_cancel",
+        "b2g_world_snapshot", "b2g_world_restore", "b2g_server_cancel", "b2g_body_set_awake",
+        "b2g_bodies_sleep_time_read", "b2g_world_get_flags",
     ]
 
     def __init__(self, path: os.PathLike | str | None = None):
@@ -276,6 +277,9 @@ class Lib:
             "b2g_world_status": ([vp, i32, P(i32)], C.c_int),
             "b2g_server_cancel": ([vp, i64], C.c_int),
             "b2g_batch_set_debug_checks": ([vp, i32], C.c_int),
+            "b2g_body_set_awake": ([vp, i32, i32, i32], C.c_int),
+            "b2g_world_get_flags": ([vp, i32, P(i32), P(i32), P(i32), P(i32)], C.c_int),
+            "b2g_bodies_sleep_time_read": ([vp, i32, i32, i32, P(f32)], C.c_int),
             "b2g_world_snapshot": ([vp, i32, vp, C.c_uint64, P(C.c_uint64)], C.c_int),
             "b2g_world_restore": ([vp, vp, C.c_uint64, P(i32)], C.c_int),
             "b2g_query_aabb": ([vp, P(i32), P(f32), i32, P(i32), P(i32), i64, P(i64)], C.c_int),
@@ -403,6 +407,17 @@ class Batch:
         self.lib.check(self.lib.b2g_contacts_read(self.h, world, arr, n.value, C.byref(n)),
                        "b2g_contacts_read")
         return arr[:n.value]
+
+    def set_awake(self, world, body, awake=True):
+        """b2Body::SetAwake."""
+        self.lib.check(self.lib.b2g_body_set_awake(self.h, world, body, int(awake)), "b2g_body_set_awake")
+
+    def sleep_times(self, world):
+        """The bodies' sleep timers (b2Body::m_sleepTime) in creation order."""
+        nb = self.sizes(world)[0]
+        arr = (C.c_float * max(nb, 1))()
+        self.lib.check(self.lib.b2g_bodies_sleep_time_read(self.h, world, 0, nb, arr), "b2g_bodies_sleep_time_read")
+        return list(arr[:nb])
 
     def set_graphs(self, enable=True):
         """Whether unmasked steps replay a captured CUDA graph (default on)."""

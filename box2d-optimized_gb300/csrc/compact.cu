@@ -24,6 +24,7 @@ __global__ void k_compact_bodies(CompactTables t, int n, BodyRecs s, BodyRecs d)
   d.force[nb] = s.force[ob];
   d.lc[nb] = s.lc[ob];
   d.btype[nb] = s.btype[ob];
+  d.bstate[nb] = s.bstate[ob];
   d.bworld[nb] = nw;
 }
 

@@ -135,6 +135,7 @@ static KernelArgs make_args(Batch* b) {
   a.world_order = b->world_order.p;
   a.xf = b->xf.p; a.pos = b->pos.p; a.vel = b->vel.p; a.massd = b->massd.p; a.damp = b->damp.p;
   a.force = b->force.p; a.lc = b->lc.p; a.btype = b->btype.p; a.bworld = b->bworld.p;
+  a.bstate = b->bstate.p; a.bwake = b->bwake.p; a.sl = b->sl.p; a.any_sleep = b->any_sleep ? 1 : 0;
   a.shape = b->shape.p; a.fbody = b->fbody.p; a.fgroup = b->fgroup.p; a.fsensor = b->fsensor.p;
   a.fworld = b->fworld.p; a.frad = b->frad.p; a.ffilter = b->ffilter.p; a.fmat = b->fmat.p; a.aabb = b->aabb.p;
   a.joints = b->joints.p; a.nocollide = b->nocollide.p; a.n_nocollide = b->n_nocollide;
@@ -164,6 +165,26 @@ static KernelArgs make_args(Batch* b) {
 }
 
 // ------------------------------------------------------------------------------ layout upload
+// Device world flags: the host flags without the per-step ones, plus the sleep bits.
+static int device_world_flags(const HostWorld& hw) {
+  int f = hw.flags & ~(B2G_WF_ACTIVE | B2G_WF_NEW_CONTACTS | B2G_WF_SLEEPMODE | B2G_WF_ALLOW_SLEEP);
+  if (hw.allow_sleep || hw.sleepers) f |= B2G_WF_SLEEPMODE;
+  if (hw.allow_sleep) f |= B2G_WF_ALLOW_SLEEP;
+  return f;
+}
+
+// Device sleep state of body i: awake / auto-sleep flags and the sleep timer.
+static int2 body_state(const HostWorld& hw, size_t i) {
+  const b2g_body& s = hw.bodies[i];
+  int fl = 0;
+  if ((s.flags & B2G_BODY_AWAKE) && s.type != B2G_STATIC) fl |= B2G_BS_AWAKE;
+  if (s.flags & B2G_BODY_AUTO_SLEEP) fl |= B2G_BS_AUTO_SLEEP;
+  float t = i < hw.body_sleep.size() ? hw.body_sleep[i] : 0.0f;
+  int bits;
+  memcpy(&bits, &t, sizeof(bits));
+  return make_int2(fl, bits);
+}
+
 static uint64_t emitter_key(const HostWorld& w, int fo, int fa, int fb) {
   bool sa = w.bodies[w.fixtures[fa].body].type == B2G_STATIC;
   bool sb = w.bodies[w.fixtures[fb].body].type == B2G_STATIC;
@@ -217,7 +238,7 @@ int upload_all(Batch* b) {
     wb[w] = make_int4(NB, (int)hw.bodies.size(), NF, (int)hw.fixtures.size());
     wj[w] = make_int4(NJ, (int)hw.joints.size(), 0, 0);
     wg[w] = make_float4(hw.gx, hw.gy, hw.inv_dt0, 0.0f);
-    wflags[w] = hw.flags;
+    wflags[w] = device_world_flags(hw);
     NB += (int)hw.bodies.size();
     NF += (int)hw.fixtures.size();
     NJ += (int)hw.joints.size();
@@ -227,6 +248,7 @@ int upload_all(Batch* b) {
   std::vector<float4> xf(NB), pos(NB), vel(NB), massd(NB), damp(NB), force(NB);
   std::vector<float2> lc(NB);
   std::vector<int> btype(NB), bworld(NB);
+  std::vector<int2> bstate(NB);
   std::vector<b2g_shape> shape(NF);
   std::vector<int> fbody(NF), fgroup(NF), fsensor(NF), fworld(NF);
   std::vector<float> frad(NF);
@@ -253,6 +275,7 @@ int upload_all(Batch* b) {
       lc[k] = make_float2(s.local_center[0], s.local_center[1]);
       btype[k] = s.type;
       bworld[k] = w;
+      bstate[k] = body_state(hw, i);
     }
     for (size_t i = 0; i < hw.fixtures.size(); ++i) {
       const b2g_fixture& f = hw.fixtures[i];
@@ -338,7 +361,9 @@ int upload_all(Batch* b) {
   CUDA_TRY(b, cudaMemsetAsync(b->wfault.p, 0, b->wfault.cap, b->stream));
   TRY(upload(b, b->xf, xf)); TRY(upload(b, b->pos, pos)); TRY(upload(b, b->vel, vel)); TRY(upload(b, b->massd, massd));
   TRY(upload(b, b->damp, damp)); TRY(upload(b, b->force, force)); TRY(upload(b, b->lc, lc));
-  TRY(upload(b, b->btype, btype)); TRY(upload(b, b->bworld, bworld));
+  TRY(upload(b, b->btype, btype)); TRY(upload(b, b->bworld, bworld)); TRY(upload(b, b->bstate, bstate));
+  TRY(ensure(b, b->bwake, NB)); TRY(ensure(b, b->sl, NB));
+  CUDA_TRY(b, cudaMemsetAsync(b->bwake.p, 0, b->bwake.cap, b->stream));
   TRY(upload(b, b->shape, shape)); TRY(upload(b, b->fbody, fbody)); TRY(upload(b, b->fgroup, fgroup));
   TRY(upload(b, b->fsensor, fsensor)); TRY(upload(b, b->fworld, fworld)); TRY(upload(b, b->ffilter, ffilter));
   TRY(upload(b, b->frad, frad));
@@ -442,6 +467,7 @@ int upload_tail(Batch* b) {
   std::vector<float4> xf, pos, vel, massd, damp, force;
   std::vector<float2> lc;
   std::vector<int> btype, bworld, fbody, fgroup, fsensor, fworld;
+  std::vector<int2> bstate;
   std::vector<float> frad;
   std::vector<b2g_shape> shape;
   std::vector<uint32_t> ffilter;
@@ -461,7 +487,9 @@ int upload_tail(Batch* b) {
     int bo = NB, fo = NF, jo = NJ;
     b->h_body_off[w] = bo; b->h_fix_off[w] = fo; b->h_joint_off[w] = jo;
     wg_tail.push_back(make_float4(hw.gx, hw.gy, hw.inv_dt0, 0.0f));
-    for (const b2g_body& s : hw.bodies) {
+    for (size_t i = 0; i < hw.bodies.size(); ++i) {
+      const b2g_body& s = hw.bodies[i];
+      bstate.push_back(body_state(hw, i));
       xf.push_back(make_float4(s.xf[0], s.xf[1], s.xf[2], s.xf[3]));
       pos.push_back(make_float4(s.c[0], s.c[1], s.a, 0.0f));
       vel.push_back(make_float4(s.v[0], s.v[1], s.w, 0.0f));
@@ -517,7 +545,7 @@ int upload_tail(Batch* b) {
     const HostWorld& hw = b->worlds[w];
     wb[w] = make_int4(b->h_body_off[w], (int)hw.bodies.size(), b->h_fix_off[w], (int)hw.fixtures.size());
     wj[w] = make_int4(b->h_joint_off[w], (int)hw.joints.size(), 0, 0);
-    wflags[w] = hw.flags & ~(B2G_WF_ACTIVE | B2G_WF_NEW_CONTACTS);
+    wflags[w] = device_world_flags(hw);
   }
   std::vector<int> order(NW);
   std::iota(order.begin(), order.end(), 0);
@@ -539,6 +567,7 @@ int upload_tail(Batch* b) {
   TRY(st.add(b, b->xf, NB0, xf)); TRY(st.add(b, b->pos, NB0, pos)); TRY(st.add(b, b->vel, NB0, vel));
   TRY(st.add(b, b->massd, NB0, massd)); TRY(st.add(b, b->damp, NB0, damp)); TRY(st.add(b, b->force, NB0, force));
   TRY(st.add(b, b->lc, NB0, lc)); TRY(st.add(b, b->btype, NB0, btype)); TRY(st.add(b, b->bworld, NB0, bworld));
+  TRY(st.add(b, b->bstate, NB0, bstate));
   TRY(st.add(b, b->shape, NF0, shape)); TRY(st.add(b, b->fbody, NF0, fbody)); TRY(st.add(b, b->fgroup, NF0, fgroup));
   TRY(st.add(b, b->fsensor, NF0, fsensor)); TRY(st.add(b, b->fworld, NF0, fworld));
   TRY(st.add(b, b->frad, NF0, frad));
@@ -546,6 +575,8 @@ int upload_tail(Batch* b) {
   TRY(st.add(b, b->joints, NJ0, joints)); TRY(st.add(b, b->nocollide, b->n_nocollide, nocol));
   TRY(st.flush(b));
   b->n_nocollide += (int)nocol.size();
+  TRY(ensure(b, b->bwake, NB, true)); TRY(ensure(b, b->sl, NB));  // wake marks are zero between steps
+  if (b->bwake.cap > (size_t)NB0) CUDA_TRY(b, cudaMemsetAsync(b->bwake.p + NB0, 0, b->bwake.cap - NB0, b->stream));
   TRY(ensure(b, b->aabb, NF)); TRY(ensure(b, b->mkey, NF)); TRY(ensure(b, b->mkey_sorted, NF));
   TRY(ensure(b, b->mval, NF)); TRY(ensure(b, b->mval_sorted, NF)); TRY(ensure(b, b->nchild, NF));
   TRY(ensure(b, b->nparent, NF)); TRY(ensure(b, b->lparent, NF)); TRY(ensure(b, b->naabb, NF));
@@ -573,6 +604,7 @@ int download_state(Batch* b) {
   int NB = b->NB, NJ = b->NJ, NW = b->NW;
   int64_t NC = b->NC;
   std::vector<float4> xf(NB), pos(NB), vel(NB), force(NB), wg(NW);
+  std::vector<int2> bstate(NB);
   std::vector<JointDev> joints(NJ);
   std::vector<uint64_t> ckey(NC);
   std::vector<int2> cfix(NC);
@@ -586,6 +618,7 @@ int download_state(Batch* b) {
     CUDA_TRY(b, cudaMemcpyAsync(pos.data(), b->pos.p, NB * sizeof(float4), cudaMemcpyDeviceToHost, s));
     CUDA_TRY(b, cudaMemcpyAsync(vel.data(), b->vel.p, NB * sizeof(float4), cudaMemcpyDeviceToHost, s));
     CUDA_TRY(b, cudaMemcpyAsync(force.data(), b->force.p, NB * sizeof(float4), cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(b, cudaMemcpyAsync(bstate.data(), b->bstate.p, NB * sizeof(int2), cudaMemcpyDeviceToHost, s));
   }
   if (NW) CUDA_TRY(b, cudaMemcpyAsync(wg.data(), b->wg.p, NW * sizeof(float4), cudaMemcpyDeviceToHost, s));
   if (NJ) CUDA_TRY(b, cudaMemcpyAsync(joints.data(), b->joints.p, NJ * sizeof(JointDev), cudaMemcpyDeviceToHost, s));
@@ -608,6 +641,10 @@ int download_state(Batch* b) {
       r.c[0] = pos[k].x; r.c[1] = pos[k].y; r.a = pos[k].z;
       r.v[0] = vel[k].x; r.v[1] = vel[k].y; r.w = vel[k].z;
       r.force[0] = force[k].x; r.force[1] = force[k].y; r.torque = force[k].z;
+      if (r.type != B2G_STATIC)
+        r.flags = (r.flags & ~B2G_BODY_AWAKE) | ((bstate[k].x & B2G_BS_AWAKE) ? B2G_BODY_AWAKE : 0u);
+      if (hw.body_sleep.size() < hw.bodies.size()) hw.body_sleep.resize(hw.bodies.size(), 0.0f);
+      memcpy(&hw.body_sleep[i], &bstate[k].y, sizeof(float));
     }
     hw.inv_dt0 = wg[w].z;
     int njw = std::min((int)hw.joints.size(), b->h_joint_off[w + 1] - jo);
@@ -726,7 +763,7 @@ static void enqueue_step(Batch* b, float dt, int vi, int pi, bool initial_bp, in
   }
   b->cur = src;
   a = step_args(b, dt, vi, pi);
-  launch_collide(a, b->stream);
+  launch_collide(a, b->NW, b->stream);
   if (record_profile) cudaEventRecord(b->ev[1], b->stream);
   if (dt > 0.0f) {
     launch_solve(a, b->solve_classes, b->stream, b->side, b->fork_ev);
@@ -762,6 +799,10 @@ static int check_status(Batch* b, unsigned int st) {
   if (st & B2G_DEV_NONFINITE) {
     set_error(b, "a world produced a non-finite body state");
     return B2G_E_WORLD_FAULT;
+  }
+  if (st & B2G_DEV_ISLAND_CHECK) {
+    set_error(b, "island check failed: inconsistent island labels");
+    return B2G_E_CAPACITY;
   }
   if (st & B2G_DEV_COLOUR_CONFLICT) {
     set_error(b, "colouring check failed: a regular colour holds two constraints of one body");
@@ -918,11 +959,13 @@ int step_batch(Batch* b, float dt, int vi, int pi, const uint8_t* mask, bool syn
   if (!b->h_readback) CUDA_TRY(b, cudaMallocHost(&b->h_readback, 8 * sizeof(unsigned long long)));
   bool need_bp = false;
   bool all_active = true;
+  bool any_sleep = false;
   std::vector<int> wflags(b->NW);
   for (int w = 0; w < b->NW; ++w) {
     HostWorld& hw = b->worlds[w];
-    int f = hw.flags & ~(B2G_WF_ACTIVE | B2G_WF_NEW_CONTACTS);
+    int f = device_world_flags(hw);
     if ((!mask || mask[w]) && !(hw.flags & B2G_WF_RETIRED)) f |= B2G_WF_ACTIVE;
+    if (f & B2G_WF_SLEEPMODE) any_sleep = true;
     if (mask && !mask[w]) all_active = false;
     wflags[w] = f;
     // appended worlds get their first contacts from the broadphase of the appended range below
@@ -932,6 +975,10 @@ int step_batch(Batch* b, float dt, int vi, int pi, const uint8_t* mask, bool syn
   if (wflags != b->h_wflags) {
     TRY(upload(b, b->wflags, wflags));
     b->h_wflags = wflags;
+  }
+  if (any_sleep != b->any_sleep) {
+    b->any_sleep = any_sleep;
+    b->layout_version++;  // captured graphs hold the kernel arguments
   }
   TRY(ensure_contact_capacity(b, b->NC));
   CUDA_TRY(b, cudaMemsetAsync(b->counters.p + 1, 0, 4 * sizeof(unsigned long long), b->stream));
@@ -1078,6 +1125,7 @@ B2G_API int b2g_batch_destroy(b2g_batch* b) {
   release(b, b->wb); release(b, b->wj); release(b, b->wg); release(b, b->wflags); release(b, b->wc); release(b, b->wfault);
   release(b, b->world_order); release(b, b->xf); release(b, b->pos); release(b, b->vel); release(b, b->massd);
   release(b, b->damp); release(b, b->force); release(b, b->lc); release(b, b->btype); release(b, b->bworld);
+  release(b, b->bstate); release(b, b->bwake); release(b, b->sl);
   release(b, b->shape); release(b, b->fbody); release(b, b->fgroup); release(b, b->fsensor); release(b, b->fworld);
   release(b, b->ffilter); release(b, b->fmat); release(b, b->aabb); release(b, b->joints); release(b, b->nocollide);
   for (int k = 0; k < 2; ++k) {
@@ -1101,7 +1149,7 @@ B2G_API int b2g_batch_destroy(b2g_batch* b) {
   {
     Batch::Spare& sp = b->spare;
     release(b, sp.xf); release(b, sp.pos); release(b, sp.vel); release(b, sp.massd); release(b, sp.damp);
-    release(b, sp.force); release(b, sp.fmat); release(b, sp.lc); release(b, sp.btype); release(b, sp.bworld);
+    release(b, sp.force); release(b, sp.fmat); release(b, sp.lc); release(b, sp.btype); release(b, sp.bworld); release(b, sp.bstate);
     release(b, sp.fbody); release(b, sp.fgroup); release(b, sp.fsensor); release(b, sp.fworld); release(b, sp.tables);
     release(b, sp.shape); release(b, sp.ffilter); release(b, sp.frad); release(b, sp.joints);
   }
@@ -1132,17 +1180,17 @@ B2G_API int b2g_world_add(b2g_batch* b, float gx, float gy, int32_t* out_world) 
 extern "C++" {
 namespace {
 const uint32_t kSnapMagic = 0x53473242u;  // "B2GS"
-const uint32_t kSnapVersion = 1;
+const uint32_t kSnapVersion = 2;  // 2: body sleep timers
 struct SnapshotHeader {
   uint32_t magic, version;
   uint32_t nb, nf, nj, nc;
   float gx, gy, inv_dt0;
   int32_t flags;
-  uint8_t allow_sleep, continuous, pad[2];
+  uint8_t allow_sleep, continuous, sleepers, pad;
   uint32_t record_size[4];  // b2g_body, b2g_fixture, b2g_joint, b2g_contact
 };
 uint64_t snapshot_bytes(const HostWorld& w) {
-  return sizeof(SnapshotHeader) + w.bodies.size() * (sizeof(b2g_body) + 8) +
+  return sizeof(SnapshotHeader) + w.bodies.size() * (sizeof(b2g_body) + 8 + sizeof(float)) +
          w.fixtures.size() * (sizeof(b2g_fixture) + 8) + w.joints.size() * sizeof(b2g_joint) +
          w.contacts.size() * sizeof(b2g_contact);
 }
@@ -1177,13 +1225,15 @@ B2G_API int b2g_world_snapshot(b2g_batch* b, int32_t world, void* buf, uint64_t 
   h.nj = (uint32_t)w.joints.size(); h.nc = (uint32_t)w.contacts.size();
   h.gx = w.gx; h.gy = w.gy; h.inv_dt0 = w.inv_dt0;
   h.flags = w.flags & ~(B2G_WF_ACTIVE | B2G_WF_RETIRED | B2G_WF_FAULTED);
-  h.allow_sleep = w.allow_sleep; h.continuous = w.continuous;
+  h.allow_sleep = w.allow_sleep; h.continuous = w.continuous; h.sleepers = w.sleepers;
   h.record_size[0] = sizeof(b2g_body); h.record_size[1] = sizeof(b2g_fixture);
   h.record_size[2] = sizeof(b2g_joint); h.record_size[3] = sizeof(b2g_contact);
   uint8_t* p = (uint8_t*)buf;
   memcpy(p, &h, sizeof(h));
   p += sizeof(h);
-  put(p, w.bodies); put(p, w.body_user); put(p, w.fixtures); put(p, w.fixture_user);
+  std::vector<float> sleep(w.bodies.size(), 0.0f);
+  for (size_t i = 0; i < sleep.size() && i < w.body_sleep.size(); ++i) sleep[i] = w.body_sleep[i];
+  put(p, w.bodies); put(p, w.body_user); put(p, sleep); put(p, w.fixtures); put(p, w.fixture_user);
   put(p, w.joints); put(p, w.contacts);
   return B2G_OK;
 }
@@ -1200,14 +1250,15 @@ B2G_API int b2g_world_restore(b2g_batch* b, const void* buf, uint64_t size, int3
   }
   HostWorld w;
   w.gx = h.gx; w.gy = h.gy; w.inv_dt0 = h.inv_dt0; w.flags = h.flags;
-  w.allow_sleep = h.allow_sleep != 0; w.continuous = h.continuous != 0;
-  if (sizeof(SnapshotHeader) + (uint64_t)h.nb * (sizeof(b2g_body) + 8) + (uint64_t)h.nf * (sizeof(b2g_fixture) + 8) +
+  w.allow_sleep = h.allow_sleep != 0; w.continuous = h.continuous != 0; w.sleepers = h.sleepers != 0;
+  if (sizeof(SnapshotHeader) + (uint64_t)h.nb * (sizeof(b2g_body) + 8 + sizeof(float)) + (uint64_t)h.nf * (sizeof(b2g_fixture) + 8) +
           (uint64_t)h.nj * sizeof(b2g_joint) + (uint64_t)h.nc * sizeof(b2g_contact) != size) {
     set_error(b, "snapshot size does not match its counts");
     return B2G_E_INVALID_ARG;
   }
   const uint8_t* p = (const uint8_t*)buf + sizeof(SnapshotHeader);
-  get(p, w.bodies, h.nb); get(p, w.body_user, h.nb); get(p, w.fixtures, h.nf); get(p, w.fixture_user, h.nf);
+  get(p, w.bodies, h.nb); get(p, w.body_user, h.nb); get(p, w.body_sleep, h.nb);
+  get(p, w.fixtures, h.nf); get(p, w.fixture_user, h.nf);
   get(p, w.joints, h.nj); get(p, w.contacts, h.nc);
   // indices must stay inside the world
   for (const b2g_fixture& f : w.fixtures)
@@ -1298,12 +1349,14 @@ static int compact_device(Batch* b, int32_t* old_to_new, int32_t n) {
   Batch::Spare& sp = b->spare;
   TRY(ensure(b, sp.xf, NB2)); TRY(ensure(b, sp.pos, NB2)); TRY(ensure(b, sp.vel, NB2)); TRY(ensure(b, sp.massd, NB2));
   TRY(ensure(b, sp.damp, NB2)); TRY(ensure(b, sp.force, NB2)); TRY(ensure(b, sp.lc, NB2));
-  TRY(ensure(b, sp.btype, NB2)); TRY(ensure(b, sp.bworld, NB2));
+  TRY(ensure(b, sp.btype, NB2)); TRY(ensure(b, sp.bworld, NB2)); TRY(ensure(b, sp.bstate, NB2));
   TRY(ensure(b, sp.shape, NF2)); TRY(ensure(b, sp.fbody, NF2)); TRY(ensure(b, sp.fgroup, NF2));
   TRY(ensure(b, sp.fsensor, NF2)); TRY(ensure(b, sp.fworld, NF2)); TRY(ensure(b, sp.ffilter, NF2));
   TRY(ensure(b, sp.fmat, NF2)); TRY(ensure(b, sp.frad, NF2)); TRY(ensure(b, sp.joints, NJ2));
-  BodyRecs sb{b->xf.p, b->pos.p, b->vel.p, b->massd.p, b->damp.p, b->force.p, b->lc.p, b->btype.p, b->bworld.p};
-  BodyRecs db{sp.xf.p, sp.pos.p, sp.vel.p, sp.massd.p, sp.damp.p, sp.force.p, sp.lc.p, sp.btype.p, sp.bworld.p};
+  BodyRecs sb{b->xf.p, b->pos.p, b->vel.p, b->massd.p, b->damp.p, b->force.p, b->lc.p, b->btype.p, b->bworld.p,
+              b->bstate.p};
+  BodyRecs db{sp.xf.p, sp.pos.p, sp.vel.p, sp.massd.p, sp.damp.p, sp.force.p, sp.lc.p, sp.btype.p, sp.bworld.p,
+              sp.bstate.p};
   FixRecs sf{b->shape.p, b->fbody.p, b->fgroup.p, b->fsensor.p, b->fworld.p, b->ffilter.p, b->fmat.p, b->frad.p};
   FixRecs df{sp.shape.p, sp.fbody.p, sp.fgroup.p, sp.fsensor.p, sp.fworld.p, sp.ffilter.p, sp.fmat.p, sp.frad.p};
   const int c = b->cur, d = c ^ 1;  // the live list moves into the other (scratch) contact buffer
@@ -1313,7 +1366,7 @@ static int compact_device(Batch* b, int32_t* old_to_new, int32_t n) {
   CUDA_TRY(b, cudaGetLastError());
   std::swap(b->xf, sp.xf); std::swap(b->pos, sp.pos); std::swap(b->vel, sp.vel); std::swap(b->massd, sp.massd);
   std::swap(b->damp, sp.damp); std::swap(b->force, sp.force); std::swap(b->lc, sp.lc);
-  std::swap(b->btype, sp.btype); std::swap(b->bworld, sp.bworld);
+  std::swap(b->btype, sp.btype); std::swap(b->bworld, sp.bworld); std::swap(b->bstate, sp.bstate);
   std::swap(b->shape, sp.shape); std::swap(b->fbody, sp.fbody); std::swap(b->fgroup, sp.fgroup);
   std::swap(b->fsensor, sp.fsensor); std::swap(b->fworld, sp.fworld); std::swap(b->ffilter, sp.ffilter);
   std::swap(b->fmat, sp.fmat); std::swap(b->frad, sp.frad); std::swap(b->joints, sp.joints);
@@ -1334,7 +1387,7 @@ static int compact_device(Batch* b, int32_t* old_to_new, int32_t n) {
     wj[to] = make_int4(off_new[w].z, (int)hw.joints.size(), 0, 0);
     wg2[to] = wg[w];
     wc2[to] = make_int2(con_new[w], wc[w].y);
-    wflags[to] = hw.flags & ~(B2G_WF_ACTIVE | B2G_WF_NEW_CONTACTS);
+    wflags[to] = device_world_flags(hw);
     keep.push_back(std::move(hw));
   }
   b->worlds.swap(keep);
@@ -1412,11 +1465,31 @@ B2G_API int b2g_world_set_flags(b2g_batch* b, int32_t world, int32_t allow_sleep
                                 int32_t continuous, int32_t auto_clear_forces) {
   if (!world_index_ok(b, world)) return B2G_E_INVALID_ARG;
   // flags travel with the per-step world flags upload; no re-layout
+  if (!allow_sleep && (b->worlds[world].allow_sleep || b->worlds[world].sleepers)) {
+    // b2World::SetAllowSleeping(false) wakes every body (src/dynamics/b2_world.cpp:474-488)
+    TRY(begin_edit(b));
+    HostWorld& hw = b->worlds[world];
+    for (size_t i = 0; i < hw.bodies.size(); ++i)
+      if (hw.bodies[i].type != B2G_STATIC) hw.bodies[i].flags |= B2G_BODY_AWAKE;
+    hw.body_sleep.assign(hw.bodies.size(), 0.0f);
+    hw.sleepers = false;
+  }
   HostWorld& w = b->worlds[world];
   w.allow_sleep = allow_sleep != 0;
   w.continuous = continuous != 0;
   w.flags = (w.flags & ~(B2G_WF_WARM | B2G_WF_CLEAR_FORCES)) | (warm_starting ? B2G_WF_WARM : 0) |
             (auto_clear_forces ? B2G_WF_CLEAR_FORCES : 0);
+  return B2G_OK;
+}
+
+B2G_API int b2g_world_get_flags(b2g_batch* b, int32_t world, int32_t* allow_sleep, int32_t* warm_starting,
+                                int32_t* continuous, int32_t* auto_clear_forces) {
+  if (!world_index_ok(b, world)) return B2G_E_INVALID_ARG;
+  const HostWorld& w = b->worlds[world];
+  if (allow_sleep) *allow_sleep = w.allow_sleep ? 1 : 0;
+  if (warm_starting) *warm_starting = (w.flags & B2G_WF_WARM) ? 1 : 0;
+  if (continuous) *continuous = w.continuous ? 1 : 0;
+  if (auto_clear_forces) *auto_clear_forces = (w.flags & B2G_WF_CLEAR_FORCES) ? 1 : 0;
   return B2G_OK;
 }
 
@@ -1460,7 +1533,10 @@ B2G_API int b2g_bodies_add(b2g_batch* b, int32_t world, const b2g_body_def* defs
     if (d.enabled) fl |= B2G_BODY_ENABLED;
     r.flags = fl;
     if (out_ids) out_ids[i] = (int32_t)w.bodies.size();
+    if (d.type != B2G_STATIC && !(fl & B2G_BODY_AWAKE)) w.sleepers = true;
+    w.body_sleep.resize(w.bodies.size(), 0.0f);
     w.bodies.push_back(r);
+    w.body_sleep.push_back(0.0f);
     w.body_user.push_back(d.user_data);
     w.body_fixtures.emplace_back();
   }
@@ -1722,6 +1798,8 @@ B2G_API int b2g_bodies_read(b2g_batch* b, int32_t world, int32_t first, int32_t 
     // the host copy is older than the device: fetch this world's slice only
     int bo = b->h_body_off[world] + first;
     std::vector<float4> xf(n), pos(n), vel(n), force(n);
+    std::vector<int2> bst(n);
+    CUDA_TRY(b, cudaMemcpyAsync(bst.data(), b->bstate.p + bo, n * sizeof(int2), cudaMemcpyDeviceToHost, b->stream));
     CUDA_TRY(b, cudaMemcpyAsync(xf.data(), b->xf.p + bo, n * sizeof(float4), cudaMemcpyDeviceToHost, b->stream));
     CUDA_TRY(b, cudaMemcpyAsync(pos.data(), b->pos.p + bo, n * sizeof(float4), cudaMemcpyDeviceToHost, b->stream));
     CUDA_TRY(b, cudaMemcpyAsync(vel.data(), b->vel.p + bo, n * sizeof(float4), cudaMemcpyDeviceToHost, b->stream));
@@ -1733,6 +1811,8 @@ B2G_API int b2g_bodies_read(b2g_batch* b, int32_t world, int32_t first, int32_t 
       r.c[0] = pos[i].x; r.c[1] = pos[i].y; r.a = pos[i].z;
       r.v[0] = vel[i].x; r.v[1] = vel[i].y; r.w = vel[i].z;
       r.force[0] = force[i].x; r.force[1] = force[i].y; r.torque = force[i].z;
+      if (r.type != B2G_STATIC)
+        r.flags = (r.flags & ~B2G_BODY_AWAKE) | ((bst[i].x & B2G_BS_AWAKE) ? B2G_BODY_AWAKE : 0u);
     }
   }
   return B2G_OK;
@@ -1757,8 +1837,46 @@ B2G_API int b2g_bodies_write(b2g_batch* b, int32_t world, int32_t first, int32_t
     r.w = s.w;
     memcpy(r.force, s.force, sizeof(r.force));
     r.torque = s.torque;
+    // b2Body::SetLinearVelocity / SetAngularVelocity: a non-zero velocity wakes the body and
+    // restarts its sleep timer (include/box2d/b2_body.h:580-612)
+    if (r.type != B2G_STATIC && (r.v[0] * r.v[0] + r.v[1] * r.v[1] > 0.0f || r.w * r.w > 0.0f)) {
+      r.flags |= B2G_BODY_AWAKE;
+      if ((size_t)(first + i) < w.body_sleep.size()) w.body_sleep[first + i] = 0.0f;
+    }
   }
   w.flags |= B2G_WF_NEW_CONTACTS;
+  return B2G_OK;
+}
+
+// b2Body::SetAwake (include/box2d/b2_body.h:719-740); a static body ignores it.
+B2G_API int b2g_body_set_awake(b2g_batch* b, int32_t world, int32_t body, int32_t awake) {
+  if (!world_index_ok(b, world) || body < 0 || body >= (int32_t)b->worlds[world].bodies.size())
+    return B2G_E_INVALID_ARG;
+  TRY(begin_edit(b));
+  HostWorld& w = b->worlds[world];
+  b2g_body& r = w.bodies[body];
+  if (r.type == B2G_STATIC) return B2G_OK;
+  w.body_sleep.resize(w.bodies.size(), 0.0f);
+  w.body_sleep[body] = 0.0f;
+  if (awake) {
+    r.flags |= B2G_BODY_AWAKE;
+  } else {
+    r.flags &= ~B2G_BODY_AWAKE;
+    r.v[0] = r.v[1] = r.w = 0.0f;
+    r.force[0] = r.force[1] = r.torque = 0.0f;
+    w.sleepers = true;
+  }
+  return B2G_OK;
+}
+
+// b2Body::m_sleepTime of n bodies from `first` (no public getter in the reference; exposed for
+// checkpoint tooling and tests).
+B2G_API int b2g_bodies_sleep_time_read(b2g_batch* b, int32_t world, int32_t first, int32_t n, float* out) {
+  if (!world_index_ok(b, world) || first < 0 || n < 0 || (n > 0 && !out)) return B2G_E_INVALID_ARG;
+  TRY(download_state(b));
+  HostWorld& w = b->worlds[world];
+  if (first + n > (int)w.bodies.size()) return B2G_E_INVALID_ARG;
+  for (int i = 0; i < n; ++i) out[i] = (size_t)(first + i) < w.body_sleep.size() ? w.body_sleep[first + i] : 0.0f;
   return B2G_OK;
 }
 

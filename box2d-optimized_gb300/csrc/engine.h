@@ -69,13 +69,29 @@ struct VCDev {
 #define B2G_WF_NEW_CONTACTS 8
 #define B2G_WF_RETIRED 16
 #define B2G_WF_FAULTED 32  // produced a non-finite state: frozen (retired) and reported
+#define B2G_WF_SLEEPMODE 64     // islands and awake flags are tracked (sleeping allowed or sleepers present)
+#define B2G_WF_ALLOW_SLEEP 128  // b2World::SetAllowSleeping(true): island sleep timers run
+
+// Body sleep state on the device (bstate.x) and island bits (sl.y).
+#define B2G_BS_AWAKE 1        // b2Body::e_awakeFlag
+#define B2G_BS_AUTO_SLEEP 2   // b2Body::e_autoSleepFlag
+#define B2G_ISL_AWAKE 1       // (at the island's root) some member was awake: the island is solved
+#define B2G_ISL_DONE 2        // (at the root) the island's position constraints were solved
+#define B2G_ISL_LINKED 4      // (own entry) the body has a contact or a joint: not an orphan
+
+// b2_common.h:176-182
+#define B2G_TIME_TO_SLEEP 0.5f
+#define B2G_LINEAR_SLEEP_TOL 0.01f
+#define B2G_ANGULAR_SLEEP_TOL (2.0f / 180.0f * 3.14159265359f)
 
 struct HostWorld {
   float gx = 0.0f, gy = -10.0f;
   float inv_dt0 = 0.0f;
   int flags = B2G_WF_WARM | B2G_WF_CLEAR_FORCES;
   bool allow_sleep = false, continuous = false;
+  bool sleepers = false;  // bodies may be asleep although sleeping is not allowed (created asleep)
   std::vector<b2g_body> bodies;
+  std::vector<float> body_sleep;  // b2Body::m_sleepTime per body
   std::vector<uint64_t> body_user;
   std::vector<b2g_fixture> fixtures;
   std::vector<uint64_t> fixture_user;
@@ -106,6 +122,7 @@ struct SolveClass {
 #define B2G_DEV_PAIR_OVERFLOW 4u
 #define B2G_DEV_COLOR_ROUNDS 8u
 #define B2G_DEV_COLOUR_CONFLICT 16u  // debug check: one regular colour holds two constraints of a body
+#define B2G_DEV_ISLAND_CHECK 32u     // debug check: a sleep-mode world's island labels are inconsistent
 
 struct EventDev {
   int kind, world, fixtureA, fixtureB, pointCount;
@@ -143,6 +160,10 @@ struct Batch {
   DBuf<float4> xf, pos, vel, massd, damp, force;
   DBuf<float2> lc;
   DBuf<int> btype, bworld;
+  DBuf<int2> bstate;              // awake / auto-sleep flags and sleep time per body
+  DBuf<uint8_t> bwake;            // narrowphase wake marks (zero between steps)
+  DBuf<int4> sl;                  // island scratch of sleep-mode worlds
+  bool any_sleep = false;         // some world of the layout runs in sleep mode
 
   DBuf<b2g_shape> shape;
   DBuf<int> fbody, fgroup, fsensor, fworld;
@@ -217,6 +238,7 @@ struct Batch {
     DBuf<float4> xf, pos, vel, massd, damp, force, fmat;
     DBuf<float2> lc;
     DBuf<int> btype, bworld, fbody, fgroup, fsensor, fworld, tables;
+    DBuf<int2> bstate;
     DBuf<b2g_shape> shape;
     DBuf<uint32_t> ffilter;
     DBuf<float> frad;

@@ -425,10 +425,14 @@ b2World::b2World(b2g_batch* batch, int32 index, bool attach) {
   m_batch = batch;
   m_ownsBatch = false;
   m_index = index;
-  b2g_body tmp;
-  B2_NOT_USED(tmp);
   m_gravity.Set(0.0f, -10.0f);
-  ApplyFlags();
+  // an attached world keeps the flags it has
+  int32_t sleep = 0, warm = 1, continuous = 0, clear = 1;
+  b2g_world_get_flags(m_batch, m_index, &sleep, &warm, &continuous, &clear);
+  m_allowSleep = sleep != 0;
+  m_warmStarting = warm != 0;
+  m_continuous = continuous != 0;
+  m_autoClear = clear != 0;
 }
 
 b2World::~b2World() {

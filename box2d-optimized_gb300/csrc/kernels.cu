@@ -31,17 +31,16 @@ __device__ __forceinline__ Xf ldXf(const float4* xf, int i) {
 }
 
 // ================================================================================ narrowphase
-// b2Contact::Update for one contact: evaluate the manifold, carry impulses by feature id, set
-// touching, record Begin/End/PreSolve when events are on.
-__global__ void k_collide(KernelArgs a) {
-  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= (int64_t)a.counters[B2G_CNT_CONTACTS]) return;
-  int2 f = a.cfix[i];
-  int w = a.fworld[f.x];
-  if ((a.wflags[w] & B2G_WF_ACTIVE) == 0) return;
+#define B2G_CONTACT_CLOSURE 0x40000000u  // scratch: updated by the wake closure of this step
+
+// b2Contact::Update for contact i: evaluate the manifold, carry impulses by feature id, set
+// touching, record Begin/End/PreSolve when events are on. Returns whether touching changed on a
+// non-sensor contact (which wakes both bodies, src/dynamics/b2_contact.cpp:183-188).
+__device__ __forceinline__ bool update_contact(const KernelArgs& a, int64_t i, int w, int2 f, int ba, int bb,
+                                               uint32_t extra_flags) {
   uint32_t flags = a.cflags[i];
   bool wasTouching = (flags & B2G_CONTACT_TOUCHING) != 0;
-  flags |= B2G_CONTACT_ENABLED;
+  flags |= B2G_CONTACT_ENABLED | extra_flags;
   b2g_manifold old = ld_manifold(&a.cman[i]);
   bool sensor = a.fsensor[f.x] || a.fsensor[f.y];
   bool touching = false;
@@ -52,8 +51,8 @@ __global__ void k_collide(KernelArgs a) {
   } else {
     const b2g_shape& sA = a.shape[f.x];
     const b2g_shape& sB = a.shape[f.y];
-    Xf xfA = ldXf(a.xf, a.fbody[f.x]);
-    Xf xfB = ldXf(a.xf, a.fbody[f.y]);
+    Xf xfA = ldXf(a.xf, ba);
+    Xf xfB = ldXf(a.xf, bb);
     Man m;
     evaluate(&m, sA, xfA, sB, xfB);
     touching = m.pointCount > 0;
@@ -88,6 +87,70 @@ __global__ void k_collide(KernelArgs a) {
     if (wasTouching && !touching) record_event(a, B2G_EVENT_END, w, f.x - fo, f.y - fo, 0, 0, 0, 0);
     if (!sensor && touching) record_event(a, B2G_EVENT_PRESOLVE, w, f.x - fo, f.y - fo, 0, 0, 0, &old);
   }
+  return !sensor && touching != wasTouching;
+}
+
+// Marks a non-static body woken in this step's narrowphase; returns whether the mark is new.
+__device__ __forceinline__ bool mark_wake(const KernelArgs& a, int b) {
+  if (a.btype[b] == B2G_STATIC || a.bwake[b]) return false;
+  a.bwake[b] = 1;
+  return true;
+}
+
+// b2ContactManager::Collide (src/dynamics/b2_contact_manager.cpp:66-116) over every contact of
+// every active world. In sleep-mode worlds a contact is updated only when one of its bodies is
+// awake (static bodies never are); wakes are marked, not applied, so every contact of this pass
+// sees the awake flags the step started with.
+__global__ void k_collide(KernelArgs a) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (int64_t)a.counters[B2G_CNT_CONTACTS]) return;
+  int2 f = a.cfix[i];
+  int w = a.fworld[f.x];
+  const int wf = a.wflags[w];
+  if ((wf & B2G_WF_ACTIVE) == 0) return;
+  const int ba = a.fbody[f.x], bb = a.fbody[f.y];
+  const bool sleepMode = (wf & B2G_WF_SLEEPMODE) != 0;
+  if (sleepMode && !((a.bstate[ba].x | a.bstate[bb].x) & B2G_BS_AWAKE)) return;
+  if (update_contact(a, i, w, f, ba, bb, 0u) && sleepMode) {
+    mark_wake(a, ba);
+    mark_wake(a, bb);
+  }
+}
+
+// The wake closure of a sleep-mode world (one CTA per world): a contact whose bodies were both
+// asleep at the start of the step is updated once one of them has been woken by another
+// contact's touching change in this step, and may wake further bodies, until nothing changes.
+// The reference updates its contacts in one sequential pass in which a wake takes effect for the
+// contacts after it; the closure gives that result for every order in which a waking contact
+// precedes the contacts it wakes (the reference keeps its newest contacts first), and it does not
+// depend on the order of the contact list.
+__global__ void k_collide_closure(KernelArgs a) {
+  const int w = blockIdx.x;
+  const int wf = a.wflags[w];
+  if (!(wf & B2G_WF_ACTIVE) || !(wf & B2G_WF_SLEEPMODE)) return;
+  const int2 wc = a.wc[w];
+  const int c0 = wc.x, n = wc.y;
+  for (int round = 0; round <= n; ++round) {
+    int changed = 0;
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+      const int64_t i = c0 + k;
+      if (a.cflags[i] & B2G_CONTACT_CLOSURE) continue;
+      const int2 f = a.cfix[i];
+      const int ba = a.fbody[f.x], bb = a.fbody[f.y];
+      if ((a.bstate[ba].x | a.bstate[bb].x) & B2G_BS_AWAKE) continue;  // updated by k_collide
+      if (!a.bwake[ba] && !a.bwake[bb]) continue;
+      if (update_contact(a, i, w, f, ba, bb, B2G_CONTACT_CLOSURE)) {
+        if (mark_wake(a, ba)) changed = 1;
+        if (mark_wake(a, bb)) changed = 1;
+      }
+    }
+    if (!__syncthreads_or(changed)) break;
+  }
+  for (int k = threadIdx.x; k < n; k += blockDim.x) {
+    const int64_t i = c0 + k;
+    const uint32_t fl = a.cflags[i];
+    if (fl & B2G_CONTACT_CLOSURE) a.cflags[i] = fl & ~B2G_CONTACT_CLOSURE;
+  }
 }
 
 __global__ void k_clear_forces(KernelArgs a, int nbodies) {
@@ -96,6 +159,10 @@ __global__ void k_clear_forces(KernelArgs a, int nbodies) {
   int w = a.bworld[i];
   int wf = a.wflags[w];
   if ((wf & B2G_WF_ACTIVE) && (wf & B2G_WF_CLEAR_FORCES)) a.force[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  if ((wf & B2G_WF_SLEEPMODE) && a.bwake[i]) {  // wakes of a step without a solve (dt = 0)
+    a.bwake[i] = 0;
+    if (a.btype[i] != B2G_STATIC) a.bstate[i] = make_int2(a.bstate[i].x | B2G_BS_AWAKE, 0);
+  }
 }
 
 // ================================================================================ broadphase
@@ -506,7 +573,8 @@ __global__ void k_tail_commit(KernelArgs a) {
 }
 
 // Contacts that disappeared: EndContact if they were touching (b2ContactManager::Destroy,
-// src/dynamics/b2_contact_manager.cpp:48-61).
+// src/dynamics/b2_contact_manager.cpp:48-61), and in sleep-mode worlds a destroyed contact with
+// manifold points wakes both bodies (b2Contact::Destroy, src/dynamics/b2_contact.cpp:80-91).
 __global__ void k_contact_dead(KernelArgs a, int src) {
   int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   int64_t nnew = a.poff[a.nf];
@@ -520,8 +588,15 @@ __global__ void k_contact_dead(KernelArgs a, int src) {
   int2 f = a.cfixB[src][k];
   int w = a.fworld[f.x];
   if (a.wflags[w] & B2G_WF_RETIRED) return;
-  int fo = a.wb[w].z;
-  record_event(a, B2G_EVENT_END, w, f.x - fo, f.y - fo, 0, 0, 0, 0);
+  if (a.events_on) {
+    int fo = a.wb[w].z;
+    record_event(a, B2G_EVENT_END, w, f.x - fo, f.y - fo, 0, 0, 0, 0);
+  }
+  if ((a.wflags[w] & B2G_WF_SLEEPMODE) && !a.fsensor[f.x] && !a.fsensor[f.y]) {
+    const int bodies[2] = {a.fbody[f.x], a.fbody[f.y]};
+    for (int q = 0; q < 2; ++q)
+      if (a.btype[bodies[q]] != B2G_STATIC) a.bstate[bodies[q]] = make_int2(a.bstate[bodies[q]].x | B2G_BS_AWAKE, 0);
+  }
 }
 
 // The new list becomes the live one, or the needed capacity is recorded for the host.
@@ -559,8 +634,9 @@ __global__ void k_collide_pairs(const b2g_shape* sa, const float* xa, const b2g_
 // ================================================================================ launchers
 static inline unsigned grid_for(int64_t n, int bs) { return (unsigned)((n + bs - 1) / bs); }
 
-void launch_collide(const KernelArgs& a, cudaStream_t s) {
+void launch_collide(const KernelArgs& a, int nw, cudaStream_t s) {
   if (a.ccap > 0) k_collide<<<grid_for(a.ccap, 128), 128, 0, s>>>(a);
+  if (a.ccap > 0 && a.any_sleep && nw > 0) k_collide_closure<<<nw, 256, 0, s>>>(a);
 }
 void launch_clear_forces(const KernelArgs& a, int nb, cudaStream_t s) {
   if (nb > 0) k_clear_forces<<<grid_for(nb, 256), 256, 0, s>>>(a, nb);
@@ -630,7 +706,7 @@ void launch_bp_emit(const KernelArgs& a, int nf, cudaStream_t s) {
 }
 void launch_contact_diff(const KernelArgs& a, int src, int dst, cudaStream_t s) {
   k_contact_diff<<<grid_for(a.ccap, 256), 256, 0, s>>>(a, src, dst);
-  if (a.events_on) k_contact_dead<<<grid_for(a.ccap, 256), 256, 0, s>>>(a, src);
+  if (a.events_on || a.any_sleep) k_contact_dead<<<grid_for(a.ccap, 256), 256, 0, s>>>(a, src);
   k_commit_contacts<<<1, 1, 0, s>>>(a);
 }
 size_t cub_temp_bytes(int nf) {

@@ -46,6 +46,10 @@ struct KernelArgs {
   float4* force;
   const float2* lc;
   const int *btype, *bworld;
+  int2* bstate;        // per body: x flags (B2G_BS_*), y sleep time (float bits)
+  uint8_t* bwake;      // per body: woken by a touching change in this step's narrowphase
+  int4* sl;            // per body, sleep-mode worlds: x island label (-1 static), y B2G_ISL_* bits,
+                       // z last position iteration the island failed, w island minimum sleep time bits
 
   const b2g_shape* shape;
   const int *fbody, *fgroup, *fsensor, *fworld;
@@ -116,6 +120,7 @@ struct KernelArgs {
   EventDev* events;
   int64_t event_cap;
   int events_on;
+  int any_sleep;       // some world runs in sleep mode (dead contacts may wake bodies)
   unsigned long long* counters;
   unsigned int* status;
 
@@ -132,7 +137,7 @@ struct KernelArgs {
 #define B2G_CNT_OVERFLOW 3   // pair capacity needed when the last broadphase overflowed (else 0)
 #define B2G_CNT_MAXCOLORS 4  // most constraint colours of any world in the last solve
 
-void launch_collide(const KernelArgs& a, cudaStream_t s);
+void launch_collide(const KernelArgs& a, int nw, cudaStream_t s);
 // Solver launches per class: class 0 on `s`, the others on side streams forked from and joined
 // back to `s` with the given events (classes.size() - 1 streams, classes.size() events).
 void launch_solve(const KernelArgs& a, const std::vector<SolveClass>& classes, cudaStream_t s,
@@ -161,6 +166,7 @@ struct BodyRecs {
   float4 *xf, *pos, *vel, *massd, *damp, *force;
   float2* lc;
   int *btype, *bworld;
+  int2* bstate;
 };
 struct FixRecs {
   b2g_shape* shape;

@@ -17,6 +17,8 @@
 // run in order with a CTA barrier between them, which reproduces the sequential Gauss-Seidel
 // sweep in colour order. Worlds are launched in size classes (threads and shared memory per
 // class) on forked streams so that small and large worlds run side by side.
+#include <cuda/atomic>
+
 #include "b2g_math.cuh"
 #include "dev_common.cuh"
 #include "engine.h"
@@ -384,6 +386,180 @@ struct SmemCarver {
   }
 };
 
+// ---- islands of sleep-mode worlds (b2World::Solve's depth-first search, src/dynamics/b2_world.cpp:520-650)
+// Connected components over solid contacts (touching, enabled, no sensor) and joints between
+// non-static bodies, as a lock-free union-find that always hooks the larger root under the
+// smaller: every component's root is its lowest body index, whatever the order of the unions.
+__device__ __forceinline__ int isl_load(int* p) {
+  return cuda::atomic_ref<int, cuda::thread_scope_device>(*p).load(cuda::memory_order_relaxed);
+}
+__device__ __forceinline__ void isl_store(int* p, int v) {
+  cuda::atomic_ref<int, cuda::thread_scope_device>(*p).store(v, cuda::memory_order_relaxed);
+}
+__device__ __forceinline__ void isl_or(int* p, int v) {
+  cuda::atomic_ref<int, cuda::thread_scope_device>(*p).fetch_or(v, cuda::memory_order_relaxed);
+}
+// Every access to the island records goes through device-scope atomics (never a plain load that
+// the SM's L1 could serve from a line older than an atomic performed in L2), and each phase ends
+// with a device-scope fence before the CTA barrier.
+__device__ __forceinline__ void isl_sync() {
+  __threadfence();
+  __syncthreads();
+}
+__device__ __forceinline__ int isl_label(int4* SL, int i) { return isl_load(&SL[i].x); }
+__device__ __forceinline__ int isl_bits(int4* SL, int i) { return isl_load(&SL[i].y); }
+
+// Root of x. With `halve`, path halving shortens the walk (x is no root, so no hook targets it);
+// halving stores only during the unions: a late halving store could otherwise overwrite a final
+// label with an intermediate ancestor.
+__device__ int isl_find(int4* SL, int x, bool halve, unsigned int* status) {
+  for (int guard = 0; guard < (1 << 24); ++guard) {
+    int p = isl_load(&SL[x].x);
+    if (p == x) return x;
+    int g = isl_load(&SL[p].x);
+    if (halve && g != p) isl_store(&SL[x].x, g);
+    x = g;
+  }
+  raise_status(status, B2G_DEV_STACK_OVERFLOW);
+  return x;
+}
+
+__device__ void isl_unite(int4* SL, int x, int y, unsigned int* status) {
+  for (int guard = 0; guard < (1 << 20); ++guard) {
+    x = isl_find(SL, x, true, status);
+    y = isl_find(SL, y, true, status);
+    if (x == y) return;
+    if (x < y) {
+      int t = x;
+      x = y;
+      y = t;
+    }
+    if (atomicCAS(&SL[x].x, x, y) == x) return;  // x was hooked meanwhile: retry from its root
+  }
+  raise_status(status, B2G_DEV_STACK_OVERFLOW);
+}
+
+// Applies this step's narrowphase wakes (b2Contact::Update's SetAwake(true) on a touching change,
+// src/dynamics/b2_contact.cpp:183-188), labels the islands, and wakes every member of an island
+// that holds an awake body (the search marks the bodies it reaches awake without resetting their
+// sleep timers, b2_world.cpp:565-566). Sleeping islands are neither integrated nor solved.
+template <int T>
+__device__ void build_islands(const KernelArgs& a, int b0, int nb, int c0, int ncAll, int j0, int nj) {
+  int4* SL = a.sl + b0;
+  int2* BS = a.bstate + b0;
+  for (int i = threadIdx.x; i < nb; i += T) {
+    const int bi = b0 + i;
+    const bool stat = a.btype[bi] == B2G_STATIC;
+    if (a.bwake[bi]) {
+      a.bwake[bi] = 0;
+      if (!stat) {
+        int2 st = BS[i];
+        st.x |= B2G_BS_AWAKE;
+        st.y = 0;
+        BS[i] = st;
+      }
+    }
+    isl_store(&SL[i].x, stat ? -1 : i);
+    isl_store(&SL[i].y, 0);
+    isl_store(&SL[i].z, 0);
+    isl_store(&SL[i].w, 0x7f7fffff);  // FLT_MAX: no member timed yet
+  }
+  isl_sync();
+  for (int k = threadIdx.x; k < ncAll; k += T) {
+    const int2 f = a.cfix[c0 + k];
+    const int ia = a.fbody[f.x] - b0, ib = a.fbody[f.y] - b0;
+    isl_or(&SL[ia].y, B2G_ISL_LINKED);
+    isl_or(&SL[ib].y, B2G_ISL_LINKED);
+    const uint32_t fl = a.cflags[c0 + k];
+    if ((fl & B2G_CONTACT_TOUCHING) && (fl & B2G_CONTACT_ENABLED) && !a.fsensor[f.x] && !a.fsensor[f.y] &&
+        isl_load(&SL[ia].x) >= 0 && isl_load(&SL[ib].x) >= 0)
+      isl_unite(SL, ia, ib, a.status);
+  }
+  for (int k = threadIdx.x; k < nj; k += T) {
+    const JointDev& J = a.joints[j0 + k];
+    const int ia = J.d.body_a - b0, ib = J.d.body_b - b0;
+    isl_or(&SL[ia].y, B2G_ISL_LINKED);
+    isl_or(&SL[ib].y, B2G_ISL_LINKED);
+    if (isl_load(&SL[ia].x) >= 0 && isl_load(&SL[ib].x) >= 0) isl_unite(SL, ia, ib, a.status);
+  }
+  isl_sync();
+  for (int i = threadIdx.x; i < nb; i += T)
+    if (isl_load(&SL[i].x) >= 0) isl_store(&SL[i].x, isl_find(SL, i, false, a.status));
+  isl_sync();
+  for (int i = threadIdx.x; i < nb; i += T) {
+    const int r = isl_label(SL, i);
+    if (r >= 0 && (BS[i].x & B2G_BS_AWAKE)) isl_or(&SL[r].y, B2G_ISL_AWAKE);
+  }
+  isl_sync();
+  for (int i = threadIdx.x; i < nb; i += T) {
+    const int r = isl_label(SL, i);
+    if (r >= 0 && (isl_bits(SL, r) & B2G_ISL_AWAKE)) BS[i].x |= B2G_BS_AWAKE;
+  }
+  isl_sync();
+}
+
+// Island root of a contact or joint between world-local bodies la and lb (one is non-static).
+__device__ __forceinline__ int isl_root(int4* SL, int la, int lb) {
+  const int r = isl_label(SL, la);
+  return r >= 0 ? r : isl_label(SL, lb);
+}
+
+__device__ __forceinline__ bool joint_awake(const KernelArgs& a, const JointDev& J) {
+  return ((a.bstate[J.d.body_a].x | a.bstate[J.d.body_b].x) & B2G_BS_AWAKE) != 0;
+}
+
+// Sleep timers of the bodies solved this step, then islands whose every member has rested for
+// b2_timeToSleep and whose position constraints were solved go to sleep (SetAwake(false): flags,
+// timer, velocities, force and torque cleared; include/box2d/b2_body.h:719-740). A body with no
+// contact and no joint is an orphan: it times itself, and when its timer runs out its velocity and
+// force are cleared but it stays awake (b2World::Solve marks orphans awake after solving them,
+// b2_world.cpp:545-549).
+template <int T>
+__device__ void sleep_islands(const KernelArgs& a, int b0, int nb) {
+  int4* SL = a.sl + b0;
+  int2* BS = a.bstate + b0;
+  const float linTolSqr = B2G_LINEAR_SLEEP_TOL * B2G_LINEAR_SLEEP_TOL;
+  const float angTolSqr = B2G_ANGULAR_SLEEP_TOL * B2G_ANGULAR_SLEEP_TOL;
+  const float h = a.dt;
+  for (int i = threadIdx.x; i < nb; i += T) {
+    const int ex = isl_label(SL, i), ey = isl_bits(SL, i);
+    int2 st = BS[i];
+    if (ex < 0 || !(st.x & B2G_BS_AWAKE)) continue;
+    const int bi = b0 + i;
+    const float4 v4 = a.vel[bi];
+    const bool orphan = !(ey & B2G_ISL_LINKED);
+    float t = 0.0f;
+    if ((st.x & B2G_BS_AUTO_SLEEP) == 0 || v4.z * v4.z > angTolSqr || v4.x * v4.x + v4.y * v4.y > linTolSqr) {
+      st.y = 0;
+    } else {
+      t = __int_as_float(st.y) + h;
+      st.y = __float_as_int(t);
+    }
+    if (orphan) {
+      if (t >= B2G_TIME_TO_SLEEP) {
+        st.y = 0;
+        a.vel[bi] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        a.force[bi] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+      }
+    } else {
+      // t >= 0: the bit patterns order as the floats
+      cuda::atomic_ref<int, cuda::thread_scope_device>(SL[ex].w).fetch_min(__float_as_int(t), cuda::memory_order_relaxed);
+    }
+    BS[i] = st;
+  }
+  isl_sync();
+  for (int i = threadIdx.x; i < nb; i += T) {
+    const int ex = isl_label(SL, i);
+    if (ex < 0 || !(isl_bits(SL, i) & B2G_ISL_LINKED) || !(BS[i].x & B2G_BS_AWAKE)) continue;
+    const float rmin = __int_as_float(isl_load(&SL[ex].w));
+    if (!(rmin >= B2G_TIME_TO_SLEEP) || !(isl_bits(SL, ex) & B2G_ISL_DONE)) continue;
+    const int bi = b0 + i;
+    BS[i] = make_int2(BS[i].x & ~B2G_BS_AWAKE, 0);
+    a.vel[bi] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    a.force[bi] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  }
+}
+
 template <int T>
 __global__ void __launch_bounds__(T, 1024 / T) k_solve(KernelArgs a, int first, int smem_bytes) {
   extern __shared__ __align__(16) unsigned char smem[];
@@ -401,9 +577,16 @@ __global__ void __launch_bounds__(T, 1024 / T) k_solve(KernelArgs a, int first, 
   const float4 wg = a.wg[w];
   const float h = a.dt;
   const float dtRatio = wg.z * a.dt;
-  const bool warm = (a.wflags[w] & B2G_WF_WARM) != 0;
+  const int wfl = a.wflags[w];
+  const bool warm = (wfl & B2G_WF_WARM) != 0;
+  const bool sleepMode = (wfl & B2G_WF_SLEEPMODE) != 0;
   const V2 gravity = mk(wg.x, wg.y);
   const SolverPlanes P = a.sp;
+  int4* const SL = a.sl + b0;
+  int2* const BS = a.bstate + b0;
+
+  // 0. sleep-mode worlds: wakes, islands, awake islands
+  if (sleepMode) build_islands<T>(a, b0, nb, c0, ncAll, j0, nj);
 
   // 1. solver contacts in list order, with local bodies (static = -1) and colouring priorities
   if (threadIdx.x == 0) s_carry = 0;
@@ -416,6 +599,8 @@ __global__ void __launch_bounds__(T, 1024 / T) k_solve(KernelArgs a, int first, 
       uint32_t fl = a.cflags[c0 + k];
       f = a.cfix[c0 + k];
       flag = ((fl & B2G_CONTACT_TOUCHING) && (fl & B2G_CONTACT_ENABLED) && !a.fsensor[f.x] && !a.fsensor[f.y]) ? 1 : 0;
+      if (flag && sleepMode)  // contacts of sleeping islands are not solved
+        flag = (isl_bits(SL, isl_root(SL, a.fbody[f.x] - b0, a.fbody[f.y] - b0)) & B2G_ISL_AWAKE) ? 1 : 0;
     }
     int total;
     int p = block_scan<T>(flag, &total);
@@ -496,7 +681,7 @@ __global__ void __launch_bounds__(T, 1024 / T) k_solve(KernelArgs a, int first, 
     float4 v4 = a.vel[bi];
     float4 md = a.massd[bi];
     if (bsm) msm[i] = make_float2(md.y, md.w);
-    if (a.btype[bi] == B2G_DYNAMIC) {
+    if (a.btype[bi] == B2G_DYNAMIC && (!sleepMode || (BS[i].x & B2G_BS_AWAKE))) {
       float4 dmp = a.damp[bi];
       float4 fr = a.force[bi];
       V2 v = mk(v4.x, v4.y);
@@ -545,13 +730,13 @@ __global__ void __launch_bounds__(T, 1024 / T) k_solve(KernelArgs a, int first, 
   }
   for (int c = 0; c < njc; ++c) {
     int s = jranges[c], e = jranges[c + 1];
-    if (c == 63) {
-      if (threadIdx.x == 0)
-        for (int i = s; i < e; ++i) jointInit(a.joints[j0 + a.jorder[j0 + i]], a.massd, a.lc, a.pos, jb, a.dt, dtRatio, warm);
-    } else {
-      for (int i = s + threadIdx.x; i < e; i += T)
-        jointInit(a.joints[j0 + a.jorder[j0 + i]], a.massd, a.lc, a.pos, jb, a.dt, dtRatio, warm);
-    }
+    const int step = c == 63 ? 1 : T, i0 = c == 63 ? s : s + threadIdx.x;
+    if (c != 63 || threadIdx.x == 0)
+      for (int i = i0; i < e; i += step) {
+        JointDev& J = a.joints[j0 + a.jorder[j0 + i]];
+        if (sleepMode && !joint_awake(a, J)) continue;
+        jointInit(J, a.massd, a.lc, a.pos, jb, a.dt, dtRatio, warm);
+      }
     __syncthreads();
   }
 
@@ -559,12 +744,13 @@ __global__ void __launch_bounds__(T, 1024 / T) k_solve(KernelArgs a, int first, 
   for (int it = 0; it < a.vi; ++it) {
     for (int c = 0; c < njc; ++c) {
       int s = jranges[c], e = jranges[c + 1];
-      if (c == 63) {
-        if (threadIdx.x == 0)
-          for (int i = s; i < e; ++i) jointSolveVelocity(a.joints[j0 + a.jorder[j0 + i]], jb, a.dt, a.inv_dt);
-      } else {
-        for (int i = s + threadIdx.x; i < e; i += T) jointSolveVelocity(a.joints[j0 + a.jorder[j0 + i]], jb, a.dt, a.inv_dt);
-      }
+      const int step = c == 63 ? 1 : T, i0 = c == 63 ? s : s + threadIdx.x;
+      if (c != 63 || threadIdx.x == 0)
+        for (int i = i0; i < e; i += step) {
+          JointDev& J = a.joints[j0 + a.jorder[j0 + i]];
+          if (sleepMode && !joint_awake(a, J)) continue;
+          jointSolveVelocity(J, jb, a.dt, a.inv_dt);
+        }
       __syncthreads();
     }
     colour_sweep<T, VelRows>(cranges, ncc, c0, fetchV, [&](int slot, const VelRows& r) {
@@ -588,7 +774,7 @@ __global__ void __launch_bounds__(T, 1024 / T) k_solve(KernelArgs a, int first, 
   for (int i = threadIdx.x; i < nb; i += T) {
     int bi = b0 + i;
     float4 p4 = a.pos[bi];
-    if (a.btype[bi] == B2G_STATIC) {
+    if (a.btype[bi] == B2G_STATIC || (sleepMode && !(BS[i].x & B2G_BS_AWAKE))) {
       if (bsm) bs[i] = p4;
       continue;
     }
@@ -618,34 +804,64 @@ __global__ void __launch_bounds__(T, 1024 / T) k_solve(KernelArgs a, int first, 
   float4* ps = bsm ? bs : a.pos + b0;
   float4* jp = ps - b0;
 
-  // 9. position iterations: contacts then joints, early exit for the world (b2_island.cpp:387-428)
+  // 9. position iterations: contacts then joints (b2_island.cpp:387-428). Early exit for the
+  //    world; in sleep-mode worlds per island, as the reference's island loop: an island whose
+  //    constraints were all okay in an iteration is done and no longer iterated.
   for (int it = 0; it < a.pi; ++it) {
     int okay = 1;
     colour_sweep<T, PosRows>(cranges, ncc, c0, fetchP, [&](int slot, const PosRows& r) {
       VCDev vc;
       unpack_pos(r, vc, M);
-      if (!(solveContactPosition(vc, ps) >= -3.0f * B2G_LINEAR_SLOP)) okay = 0;
+      int root = 0;
+      if (sleepMode) {
+        root = isl_root(SL, vc.indexA, vc.indexB);
+        if (isl_bits(SL, root) & B2G_ISL_DONE) return;
+      }
+      if (!(solveContactPosition(vc, ps) >= -3.0f * B2G_LINEAR_SLOP)) {
+        okay = 0;
+        if (sleepMode) isl_store(&SL[root].z, it + 1);
+      }
     });
     for (int c = 0; c < njc; ++c) {
       int s = jranges[c], e = jranges[c + 1];
-      if (c == 63) {
-        if (threadIdx.x == 0)
-          for (int i = s; i < e; ++i)
-            if (!jointSolvePosition(a.joints[j0 + a.jorder[j0 + i]], jp)) okay = 0;
-      } else {
-        for (int i = s + threadIdx.x; i < e; i += T)
-          if (!jointSolvePosition(a.joints[j0 + a.jorder[j0 + i]], jp)) okay = 0;
-      }
+      const int step = c == 63 ? 1 : T, i0 = c == 63 ? s : s + threadIdx.x;
+      if (c != 63 || threadIdx.x == 0)
+        for (int i = i0; i < e; i += step) {
+          JointDev& J = a.joints[j0 + a.jorder[j0 + i]];
+          int root = 0;
+          if (sleepMode) {
+            if (!joint_awake(a, J)) continue;
+            root = isl_root(SL, J.d.body_a - b0, J.d.body_b - b0);
+            if (isl_bits(SL, root) & B2G_ISL_DONE) continue;
+          }
+          if (!jointSolvePosition(J, jp)) {
+            okay = 0;
+            if (sleepMode) isl_store(&SL[root].z, it + 1);
+          }
+        }
       __syncthreads();
     }
-    if (__syncthreads_and(okay)) break;
+    if (sleepMode) {
+      isl_sync();
+      int pending = 0;
+      for (int i = threadIdx.x; i < nb; i += T) {
+        const int ey = isl_bits(SL, i);
+        if (isl_label(SL, i) != i || !(ey & B2G_ISL_AWAKE) || (ey & B2G_ISL_DONE)) continue;
+        if (isl_load(&SL[i].z) == it + 1) pending = 1;
+        else isl_or(&SL[i].y, B2G_ISL_DONE);
+      }
+      __threadfence();
+      if (!__syncthreads_or(pending)) break;
+    } else if (__syncthreads_and(okay)) {
+      break;
+    }
   }
 
   // 10. transforms (b2Body::SynchronizeTransform, include/box2d/b2_body.h:957-961), finite check
   int bad = 0;
   for (int i = threadIdx.x; i < nb; i += T) {
     int bi = b0 + i;
-    if (a.btype[bi] == B2G_STATIC) continue;
+    if (a.btype[bi] == B2G_STATIC || (sleepMode && !(BS[i].x & B2G_BS_AWAKE))) continue;
     float4 p4 = ps[i];
     if (bsm) a.pos[bi] = p4;
     Rot q = rotOf(p4.z);
@@ -660,6 +876,9 @@ __global__ void __launch_bounds__(T, 1024 / T) k_solve(KernelArgs a, int first, 
     a.wfault[w] = 1;
     atomicOr(a.status, B2G_DEV_NONFINITE);
   }
+
+  // 11. sleep timers (b2_island.cpp:444-483; orphans b2Island::SolveOrphan :230-249)
+  if (wfl & B2G_WF_ALLOW_SLEEP) sleep_islands<T>(a, b0, nb);
   if (a.events_on) {
     for (int p = threadIdx.x; p < nsc; p += T) {
       int pc = (P.idx[c0 + p].x >> 24) & 15;
@@ -739,6 +958,27 @@ __global__ void __launch_bounds__(256) k_colour_check(KernelArgs a) {
   const int4 wj = a.wj[w];
   const int j0 = wj.x, nj = wj.y;
   for (int k = threadIdx.x; k < nj; k += blockDim.x) colour_mark(mask, a.jcb[j0 + k], a.jcol[j0 + k], a.status);
+  if (!(a.wflags[w] & B2G_WF_SLEEPMODE)) return;
+  // the step's islands: every label is a root no larger than its body, and solid contacts and
+  // joints join bodies of one label
+  int4* SL = a.sl + b0;
+  for (int i = threadIdx.x; i < nb; i += blockDim.x) {
+    const int r = isl_label(SL, i);
+    if (r >= 0 && (r > i || isl_label(SL, r) != r)) atomicOr(a.status, B2G_DEV_ISLAND_CHECK);
+  }
+  const int2 wc = a.wc[w];
+  for (int k = threadIdx.x; k < wc.y; k += blockDim.x) {
+    const int2 f = a.cfix[wc.x + k];
+    const uint32_t fl = a.cflags[wc.x + k];
+    if (!(fl & B2G_CONTACT_TOUCHING) || !(fl & B2G_CONTACT_ENABLED) || a.fsensor[f.x] || a.fsensor[f.y]) continue;
+    const int la = isl_label(SL, a.fbody[f.x] - b0), lb = isl_label(SL, a.fbody[f.y] - b0);
+    if (la >= 0 && lb >= 0 && la != lb) atomicOr(a.status, B2G_DEV_ISLAND_CHECK);
+  }
+  for (int k = threadIdx.x; k < nj; k += blockDim.x) {
+    const JointDev& J = a.joints[j0 + k];
+    const int la = isl_label(SL, J.d.body_a - b0), lb = isl_label(SL, J.d.body_b - b0);
+    if (la >= 0 && lb >= 0 && la != lb) atomicOr(a.status, B2G_DEV_ISLAND_CHECK);
+  }
 }
 
 void launch_colour_check(const KernelArgs& a, int nw, cudaStream_t s) {

@@ -682,7 +682,8 @@ class b2World {
   bool m_ownsBatch = false;
   int32 m_index = 0;
   b2Vec2 m_gravity;
-  bool m_allowSleep = false, m_warmStarting = true, m_continuous = false, m_autoClear = true;
+  // b2World's defaults (src/dynamics/b2_world.cpp:56-62): sleeping and continuous physics on
+  bool m_allowSleep = true, m_warmStarting = true, m_continuous = true, m_autoClear = true;
   b2ContactListener* m_listener = nullptr;
   b2ContactFilter* m_filter = nullptr;
   std::deque<b2Body> m_bodies;

@@ -264,6 +264,10 @@ B2G_API int b2g_world_count(b2g_batch* b, int32_t* out_n);
 B2G_API int b2g_world_set_gravity(b2g_batch* b, int32_t world, float gx, float gy);
 B2G_API int b2g_world_set_flags(b2g_batch* b, int32_t world, int32_t allow_sleep,
                                 int32_t warm_starting, int32_t continuous, int32_t auto_clear_forces);
+/* The world's flags as b2g_world_set_flags last set them (b2World::GetAllowSleeping,
+ * GetWarmStarting, GetContinuousPhysics, GetAutoClearForces). */
+B2G_API int b2g_world_get_flags(b2g_batch* b, int32_t world, int32_t* allow_sleep, int32_t* warm_starting,
+                                int32_t* continuous, int32_t* auto_clear_forces);
 
 /* b2World::CreateBody, include/box2d/b2_world.h:80 (bulk). out_ids may be NULL. */
 B2G_API int b2g_bodies_add(b2g_batch* b, int32_t world, const b2g_body_def* defs, int32_t n,
@@ -322,9 +326,11 @@ B2G_API int b2g_batch_set_forces(b2g_batch* b, const float* f4, int64_t n_bodies
  * unmasked steps with dt > 0 and events off; it is re-captured when buffers move. */
 B2G_API int b2g_batch_set_graphs(b2g_batch* b, int32_t enable);
 /* Debug checks (default off): after every solve, a device pass verifies that no regular colour
- * of the constraint colouring holds two contacts or two joints on the same non-static body;
- * a violation makes the step return B2G_E_CAPACITY with a message. Costs one small launch per
- * step. No reference counterpart (the reference solves serially). */
+ * of the constraint colouring holds two contacts or two joints on the same non-static body, and,
+ * in worlds that track sleep, that the step's island labels are consistent (each a root, and
+ * solid contacts and joints within one island); a violation makes the step return
+ * B2G_E_CAPACITY with a message. Costs one small launch per step. No reference counterpart (the
+ * reference solves serially). */
 B2G_API int b2g_batch_set_debug_checks(b2g_batch* b, int32_t enable);
 /* Threads per world CTA of the solver for each world size class (worlds of at most 64, 256,
  * 1024 and 4096 bodies, and larger), 5 entries each one of 64, 128, 256, 512, 1024 (defaults
@@ -348,9 +354,16 @@ B2G_API int b2g_reserve(b2g_batch* b, int64_t contacts);
 /* b2Body getters (GetPosition, GetAngle, GetLinearVelocity, ...), include/box2d/b2_body.h:141-260 */
 B2G_API int b2g_bodies_read(b2g_batch* b, int32_t world, int32_t first, int32_t n, b2g_body* out);
 /* b2Body::SetTransform / SetLinearVelocity / SetAngularVelocity / ApplyForce...,
- * src/dynamics/b2_body.cpp:482 (writes xf, sweep, velocities, force and torque of each record) */
+ * src/dynamics/b2_body.cpp:482 (writes xf, sweep, velocities, force and torque of each record; a
+ * non-zero velocity wakes the body and restarts its sleep timer, as SetLinearVelocity does) */
 B2G_API int b2g_bodies_write(b2g_batch* b, int32_t world, int32_t first, int32_t n,
                              const b2g_body* in);
+/* b2Body::SetAwake (include/box2d/b2_body.h:719-740): awake = 0 puts the body to sleep (velocity,
+ * force and torque cleared); a static body ignores it. */
+B2G_API int b2g_body_set_awake(b2g_batch* b, int32_t world, int32_t body, int32_t awake);
+/* The bodies' sleep timers (b2Body::m_sleepTime, which the reference keeps private): for
+ * checkpoint tooling and tests. */
+B2G_API int b2g_bodies_sleep_time_read(b2g_batch* b, int32_t world, int32_t first, int32_t n, float* out);
 /* All body states of all worlds as packed arrays (device order = world, then creation order).
  * Any pointer may be NULL. */
 B2G_API int b2g_batch_read_states(b2g_batch* b, float* xf4, float* v3, int64_t cap_bodies,

@@ -46,6 +46,9 @@ static const float kMaxTranslation = 2.0f;
 static const float kMaxTranslationSquared = (kMaxTranslation * kMaxTranslation);
 static const float kMaxRotation = (0.5f * kPi);
 static const float kMaxRotationSquared = (kMaxRotation * kMaxRotation);
+static const float kTimeToSleep = 0.5f;                                  // b2_common.h:176
+static const float kLinearSleepTolerance = 0.01f;                        // b2_common.h:179
+static const float kAngularSleepTolerance = (2.0f / 180.0f * kPi);       // b2_common.h:182
 static const float kBaumgarte = 0.2f;
 
 // ------------------------------------------------------------------------------------------------
@@ -933,6 +936,8 @@ struct Body {
   V2 force; float torque;
   int type;
   uint32_t flags;
+  float sleepTime = 0.0f;
+  bool awake() const { return (flags & B2G_BODY_AWAKE) != 0; }
 };
 
 struct Fixture {
@@ -1007,6 +1012,8 @@ static const int kOverflow = kColors - 1;
 
 struct World {
   V2 gravity;
+  bool allowSleep = false;
+  bool sleepers = false;                   // bodies may be asleep although sleeping is not allowed
   bool warmStarting = true;
   bool autoClearForces = true;
   bool newContacts = true;
@@ -1023,7 +1030,28 @@ struct World {
   std::vector<uint32_t> jointPrioV;
   std::vector<int32_t> lastContactOrder;   // (fixture A, fixture B) pairs in solve order
   std::vector<int32_t> lastJointOrder;     // joint indices in solve order
+  // last step's islands (sleep mode): per island its root body, whether it is an orphan, its
+  // bodies, its contacts as (fixture A, fixture B) in solve order and its joints in solve order
+  std::vector<int32_t> islandRoot, islandOrphan, islandBodyOff, islandBodies;
+  std::vector<int32_t> islandContactOff, islandContacts, islandJointOff, islandJoints;
+  bool sleepMode() const { return allowSleep || sleepers; }
 };
+
+// b2Body::SetAwake (include/box2d/b2_body.h:719-740).
+static void setAwake(Body& b, bool flag) {
+  if (b.type == 0) return;
+  if (flag) {
+    b.flags |= B2G_BODY_AWAKE;
+    b.sleepTime = 0.0f;
+  } else {
+    b.flags &= ~B2G_BODY_AWAKE;
+    b.sleepTime = 0.0f;
+    b.v = v2(0.0f, 0.0f);
+    b.w = 0.0f;
+    b.force = v2(0.0f, 0.0f);
+    b.torque = 0.0f;
+  }
+}
 
 static void rebuildNoCollide(World* w) {
   w->noCollide.clear();
@@ -1119,44 +1147,98 @@ static void updatePairs(World* w) {
   findPairs(*w, bb, &pairs);
   std::vector<Contact> next;
   next.reserve(pairs.size());
+  std::vector<char> kept(w->contacts.size(), 0);
   size_t k = 0;
   for (uint64_t key : pairs) {
     while (k < w->contacts.size() && w->contacts[k].key < key) ++k;
-    if (k < w->contacts.size() && w->contacts[k].key == key) next.push_back(w->contacts[k]);
-    else next.push_back(makeContact(*w, key));
+    if (k < w->contacts.size() && w->contacts[k].key == key) {
+      next.push_back(w->contacts[k]);
+      kept[k] = 1;
+    } else {
+      next.push_back(makeContact(*w, key));
+    }
   }
+  // b2Contact::Destroy wakes both bodies of a destroyed contact with manifold points
+  // (src/dynamics/b2_contact.cpp:80-91)
+  if (w->sleepMode())
+    for (size_t i = 0; i < w->contacts.size(); ++i) {
+      const Contact& c = w->contacts[i];
+      if (kept[i] || !(c.flags & B2G_CONTACT_TOUCHING)) continue;
+      if (w->fixtures[c.fA].sensor || w->fixtures[c.fB].sensor) continue;
+      setAwake(w->bodies[w->fixtures[c.fA].body], true);
+      setAwake(w->bodies[w->fixtures[c.fB].body], true);
+    }
   w->contacts.swap(next);
 }
 
-// b2Contact::Update (src/dynamics/b2_contact.cpp:126-210) for every contact (sensors excluded).
-static void collide(World* w) {
-  for (Contact& c : w->contacts) {
-    Manifold old = c.m;
-    c.flags |= B2G_CONTACT_ENABLED;
-    const Fixture& fa = w->fixtures[c.fA];
-    const Fixture& fb = w->fixtures[c.fB];
-    bool touching = false;
-    if (fa.sensor || fb.sensor) {
-      c.m.pointCount = 0;
-    } else {
-      evaluate(&c.m, fa.shape, w->bodies[fa.body].xf, fb.shape, w->bodies[fb.body].xf);
-      touching = c.m.pointCount > 0;
-      for (int i = 0; i < c.m.pointCount; ++i) {
-        MPoint* mp2 = c.m.points + i;
-        mp2->normalImpulse = 0.0f;
-        mp2->tangentImpulse = 0.0f;
-        for (int j = 0; j < old.pointCount; ++j) {
-          if (old.points[j].id == mp2->id) {
-            mp2->normalImpulse = old.points[j].normalImpulse;
-            mp2->tangentImpulse = old.points[j].tangentImpulse;
-            break;
-          }
+// b2Contact::Update (src/dynamics/b2_contact.cpp:126-210) for one contact; returns whether
+// touching changed on a non-sensor contact (which wakes both bodies, :183-188).
+static bool updateContact(World* w, Contact& c) {
+  Manifold old = c.m;
+  const bool wasTouching = (c.flags & B2G_CONTACT_TOUCHING) != 0;
+  c.flags |= B2G_CONTACT_ENABLED;
+  const Fixture& fa = w->fixtures[c.fA];
+  const Fixture& fb = w->fixtures[c.fB];
+  bool touching = false;
+  if (fa.sensor || fb.sensor) {
+    c.m.pointCount = 0;
+  } else {
+    evaluate(&c.m, fa.shape, w->bodies[fa.body].xf, fb.shape, w->bodies[fb.body].xf);
+    touching = c.m.pointCount > 0;
+    for (int i = 0; i < c.m.pointCount; ++i) {
+      MPoint* mp2 = c.m.points + i;
+      mp2->normalImpulse = 0.0f;
+      mp2->tangentImpulse = 0.0f;
+      for (int j = 0; j < old.pointCount; ++j) {
+        if (old.points[j].id == mp2->id) {
+          mp2->normalImpulse = old.points[j].normalImpulse;
+          mp2->tangentImpulse = old.points[j].tangentImpulse;
+          break;
         }
       }
     }
-    if (touching) c.flags |= B2G_CONTACT_TOUCHING;
-    else c.flags &= ~B2G_CONTACT_TOUCHING;
   }
+  if (touching) c.flags |= B2G_CONTACT_TOUCHING;
+  else c.flags &= ~B2G_CONTACT_TOUCHING;
+  return !fa.sensor && !fb.sensor && touching != wasTouching;
+}
+
+// b2ContactManager::Collide (src/dynamics/b2_contact_manager.cpp:66-116). Sleep mode: a contact
+// is updated when one of its bodies was awake at the start of the pass (static bodies never are),
+// or, as a wake closure, once one of its bodies has been woken by another contact's touching
+// change in this pass; wakes apply after the pass. The reference's single sequential pass gives
+// the same result whenever a waking contact precedes the contacts it wakes (its list keeps the
+// newest contacts first); the closure does not depend on the list order.
+static void collide(World* w) {
+  const bool sleepMode = w->sleepMode();
+  const size_t n = w->contacts.size();
+  std::vector<char> evaluated(n, 0), wake(w->bodies.size(), 0);
+  auto mark = [&](const Contact& c) {
+    int a = w->fixtures[c.fA].body, b = w->fixtures[c.fB].body;
+    bool fresh = false;
+    if (w->bodies[a].type != 0 && !wake[a]) { wake[a] = 1; fresh = true; }
+    if (w->bodies[b].type != 0 && !wake[b]) { wake[b] = 1; fresh = true; }
+    return fresh;
+  };
+  for (size_t k = 0; k < n; ++k) {
+    Contact& c = w->contacts[k];
+    if (sleepMode && !w->bodies[w->fixtures[c.fA].body].awake() && !w->bodies[w->fixtures[c.fB].body].awake())
+      continue;
+    evaluated[k] = 1;
+    if (updateContact(w, c) && sleepMode) mark(c);
+  }
+  if (!sleepMode) return;
+  for (bool changed = true; changed;) {
+    changed = false;
+    for (size_t k = 0; k < n; ++k) {
+      Contact& c = w->contacts[k];
+      if (evaluated[k] || (!wake[w->fixtures[c.fA].body] && !wake[w->fixtures[c.fB].body])) continue;
+      evaluated[k] = 1;
+      if (updateContact(w, c) && mark(c)) changed = true;
+    }
+  }
+  for (size_t b = 0; b < wake.size(); ++b)
+    if (wake[b]) setAwake(w->bodies[b], true);
 }
 
 // Greedy colouring in priority order: each constraint takes the lowest colour not used by an
@@ -1921,7 +2003,46 @@ static float solvePositionOne(const PC& pc, std::vector<SolverBody>& sb) {
   return minSeparation;
 }
 
-// One b2World::Step (src/dynamics/b2_world.cpp:1108-1171) with sleeping and CCD off.
+// Islands of a sleep-mode world (b2World::Solve's depth-first search, src/dynamics/b2_world.cpp:
+// 520-650): connected components over solid contacts and joints between non-static bodies, each
+// labelled by its lowest body index (-1 for static bodies). `linked` marks bodies with any contact
+// or joint (the others are orphans, solved by b2Island::SolveOrphan).
+static int findRoot(std::vector<int>& parent, int x) {
+  while (parent[x] != x) x = parent[x];
+  return x;
+}
+static void buildIslands(const World& w, std::vector<int>* label, std::vector<char>* linked) {
+  const int nb = (int)w.bodies.size();
+  std::vector<int> parent(nb);
+  for (int i = 0; i < nb; ++i) parent[i] = w.bodies[i].type == 0 ? -1 : i;
+  linked->assign(nb, 0);
+  auto unite = [&](int x, int y) {
+    if (parent[x] < 0 || parent[y] < 0) return;
+    x = findRoot(parent, x);
+    y = findRoot(parent, y);
+    if (x == y) return;
+    if (x < y) std::swap(x, y);
+    parent[x] = y;  // the larger root under the smaller: roots are lowest indices
+  };
+  for (const Contact& c : w.contacts) {
+    int a = w.fixtures[c.fA].body, b = w.fixtures[c.fB].body;
+    (*linked)[a] = (*linked)[b] = 1;
+    if ((c.flags & B2G_CONTACT_TOUCHING) && (c.flags & B2G_CONTACT_ENABLED) && !w.fixtures[c.fA].sensor &&
+        !w.fixtures[c.fB].sensor)
+      unite(a, b);
+  }
+  for (const Joint& j : w.joints) {
+    (*linked)[j.d.body_a] = (*linked)[j.d.body_b] = 1;
+    unite(j.d.body_a, j.d.body_b);
+  }
+  label->assign(nb, -1);
+  for (int i = 0; i < nb; ++i)
+    if (parent[i] >= 0) (*label)[i] = findRoot(parent, i);
+}
+
+// One b2World::Step (src/dynamics/b2_world.cpp:1108-1171) with CCD off. Sleep-mode worlds
+// (sleeping allowed, or sleepers present) solve only islands holding an awake body, iterate
+// positions per island with the island's own early exit, and run the island sleep timers.
 static void stepWorld(World* w, float dt, int vi, int pi) {
   if (w->newContacts) {
     updatePairs(w);
@@ -1935,16 +2056,31 @@ static void stepWorld(World* w, float dt, int vi, int pi) {
   st.pi = pi;
   st.warm = w->warmStarting;
   collide(w);
+  const bool sleepMode = w->sleepMode();
   if (dt > 0.0f) {
     int nb = (int)w->bodies.size();
     float h = st.dt;
+    std::vector<int> label;
+    std::vector<char> linked;
+    std::vector<char> islandAwake(nb, 0);
+    if (sleepMode) {
+      buildIslands(*w, &label, &linked);
+      for (int i = 0; i < nb; ++i)
+        if (label[i] >= 0 && w->bodies[i].awake()) islandAwake[label[i]] = 1;
+      // the search marks every body it reaches awake without resetting its timer
+      for (int i = 0; i < nb; ++i)
+        if (label[i] >= 0 && islandAwake[label[i]]) w->bodies[i].flags |= B2G_BODY_AWAKE;
+    }
+    auto solved = [&](int i) { return !sleepMode || w->bodies[i].awake(); };
+    auto rootOf = [&](int a, int b) { return label[a] >= 0 ? label[a] : label[b]; };
+    auto jointActive = [&](const Joint& J) { return !sleepMode || w->bodies[J.d.body_a].awake() || w->bodies[J.d.body_b].awake(); };
     std::vector<SolverBody> sb(nb);
     // b2Island::Solve velocity integration (src/dynamics/b2_island.cpp:256-293) / SolveOrphan
     for (int i = 0; i < nb; ++i) {
       Body& b = w->bodies[i];
       V2 v = b.v;
       float wv = b.w;
-      if (b.type == 2) {
+      if (b.type == 2 && solved(i)) {
         addTo(v, (h * b.invMass) * (b.gravityScale * b.mass * w->gravity + b.force));
         wv += h * b.invI * b.torque;
         v.x /= (1.0f + h * b.linearDamping);
@@ -1959,6 +2095,7 @@ static void stepWorld(World* w, float dt, int vi, int pi) {
       const Contact& c = w->contacts[i];
       if ((c.flags & B2G_CONTACT_TOUCHING) == 0 || (c.flags & B2G_CONTACT_ENABLED) == 0) continue;
       if (w->fixtures[c.fA].sensor || w->fixtures[c.fB].sensor) continue;
+      if (sleepMode && !islandAwake[rootOf(w->fixtures[c.fA].body, w->fixtures[c.fB].body)]) continue;
       solverContacts.push_back(i);
     }
     int nc = (int)solverContacts.size();
@@ -1999,10 +2136,12 @@ static void stepWorld(World* w, float dt, int vi, int pi) {
     // warm start (b2_island.cpp:304-325): contacts, then joint init
     if (st.warm)
       for (int i : corder) warmStartOne(vcs[i], sb);
-    for (int j : jorder) jointInit(w->joints[j], w->bodies, sb, st);
+    for (int j : jorder)
+      if (jointActive(w->joints[j])) jointInit(w->joints[j], w->bodies, sb, st);
     // velocity iterations (b2_island.cpp:327-346): joints then contacts
     for (int it = 0; it < vi; ++it) {
-      for (int j : jorder) jointSolveVelocity(w->joints[j], sb, st);
+      for (int j : jorder)
+        if (jointActive(w->joints[j])) jointSolveVelocity(w->joints[j], sb, st);
       for (int i : corder) solveVelocityOne(vcs[i], sb);
     }
     // StoreImpulses (b2_contact_solver.cpp:641-657)
@@ -2015,7 +2154,7 @@ static void stepWorld(World* w, float dt, int vi, int pi) {
     }
     // integrate positions (b2_island.cpp:349-385)
     for (int i = 0; i < nb; ++i) {
-      if (w->bodies[i].type == 0) continue;
+      if (w->bodies[i].type == 0 || !solved(i)) continue;
       V2 c = sb[i].c; float a = sb[i].a; V2 v = sb[i].v; float wv = sb[i].w;
       V2 translation = h * v;
       if (dot(translation, translation) > kMaxTranslationSquared) {
@@ -2031,25 +2170,110 @@ static void stepWorld(World* w, float dt, int vi, int pi) {
       a += h * wv;
       sb[i].c = c; sb[i].a = a; sb[i].v = v; sb[i].w = wv;
     }
-    // position iterations (b2_island.cpp:387-428): contacts then joints, early exit per world
+    // position iterations (b2_island.cpp:387-428): contacts then joints, early exit per world;
+    // in sleep mode per island (an island okay in an iteration is done, as the reference's loop)
+    std::vector<int> badIt(nb, 0);
+    std::vector<char> done(nb, 0);
     for (int it = 0; it < pi; ++it) {
       float minSep = 0.0f;
-      for (int i : corder) minSep = bmin(minSep, solvePositionOne(pcs[i], sb));
+      for (int i : corder) {
+        int root = 0;
+        if (sleepMode) {
+          root = rootOf(pcs[i].indexA, pcs[i].indexB);
+          if (done[root]) continue;
+        }
+        float sep = solvePositionOne(pcs[i], sb);
+        minSep = bmin(minSep, sep);
+        if (sleepMode && !(sep >= -3.0f * kLinearSlop)) badIt[root] = it + 1;
+      }
       bool contactsOkay = minSep >= -3.0f * kLinearSlop;
       bool jointsOkay = true;
       for (int j : jorder) {
-        bool ok = jointSolvePosition(w->joints[j], sb);
+        Joint& J = w->joints[j];
+        int root = 0;
+        if (sleepMode) {
+          if (!jointActive(J)) continue;
+          root = rootOf(J.d.body_a, J.d.body_b);
+          if (done[root]) continue;
+        }
+        bool ok = jointSolvePosition(J, sb);
         jointsOkay = jointsOkay && ok;
+        if (sleepMode && !ok) badIt[root] = it + 1;
       }
-      if (contactsOkay && jointsOkay) break;
+      if (sleepMode) {
+        bool pending = false;
+        for (int i = 0; i < nb; ++i) {
+          if (label[i] != i || !islandAwake[i] || done[i]) continue;
+          if (badIt[i] == it + 1) pending = true;
+          else done[i] = 1;
+        }
+        if (!pending) break;
+      } else if (contactsOkay && jointsOkay) {
+        break;
+      }
     }
     // write back + SynchronizeTransform (b2_island.cpp:430-438, include/box2d/b2_body.h:957-961)
     for (int i = 0; i < nb; ++i) {
       Body& b = w->bodies[i];
-      if (b.type == 0) continue;
+      if (b.type == 0 || !solved(i)) continue;
       b.c = sb[i].c; b.a = sb[i].a; b.v = sb[i].v; b.w = sb[i].w;
       b.xf.q = rotOf(b.a);
       b.xf.p = b.c - mul(b.xf.q, b.localCenter);
+    }
+    // sleep timers (b2_island.cpp:444-483; orphans b2Island::SolveOrphan :230-249, which the
+    // caller marks awake again, b2_world.cpp:545-549)
+    if (w->allowSleep) {
+      const float linTolSqr = kLinearSleepTolerance * kLinearSleepTolerance;
+      const float angTolSqr = kAngularSleepTolerance * kAngularSleepTolerance;
+      std::vector<float> minSleep(nb, FLT_MAX);
+      for (int i = 0; i < nb; ++i) {
+        Body& b = w->bodies[i];
+        if (b.type == 0 || !b.awake()) continue;
+        float t = 0.0f;
+        if ((b.flags & B2G_BODY_AUTO_SLEEP) == 0 || b.w * b.w > angTolSqr || dot(b.v, b.v) > linTolSqr) {
+          b.sleepTime = 0.0f;
+        } else {
+          b.sleepTime += h;
+          t = b.sleepTime;
+        }
+        if (!linked[i]) {
+          if (t >= kTimeToSleep) {
+            setAwake(b, false);
+            b.flags |= B2G_BODY_AWAKE;
+          }
+        } else {
+          minSleep[label[i]] = bmin(minSleep[label[i]], t);
+        }
+      }
+      for (int i = 0; i < nb; ++i) {
+        Body& b = w->bodies[i];
+        if (b.type == 0 || !b.awake() || !linked[i]) continue;
+        if (minSleep[label[i]] >= kTimeToSleep && done[label[i]]) setAwake(b, false);
+      }
+    }
+    // the island structure of this step, for replaying it on the reference
+    w->islandRoot.clear(); w->islandOrphan.clear(); w->islandBodies.clear(); w->islandContacts.clear();
+    w->islandJoints.clear(); w->islandBodyOff.assign(1, 0); w->islandContactOff.assign(1, 0);
+    w->islandJointOff.assign(1, 0);
+    if (sleepMode) {
+      for (int r = 0; r < nb; ++r) {
+        if (label[r] != r || !islandAwake[r]) continue;
+        w->islandRoot.push_back(r);
+        w->islandOrphan.push_back(linked[r] ? 0 : 1);
+        for (int i = r; i < nb; ++i)
+          if (label[i] == r) w->islandBodies.push_back(i);
+        for (int i : corder) {
+          const Contact& c = w->contacts[solverContacts[i]];
+          if (rootOf(w->fixtures[c.fA].body, w->fixtures[c.fB].body) != r) continue;
+          w->islandContacts.push_back(c.fA);
+          w->islandContacts.push_back(c.fB);
+        }
+        for (int j : jorder)
+          if (rootOf(w->joints[j].d.body_a, w->joints[j].d.body_b) == r) w->islandJoints.push_back(j);
+        w->islandBodyOff.push_back((int)w->islandBodies.size());
+        w->islandContactOff.push_back((int)w->islandContacts.size() / 2);
+        w->islandJointOff.push_back((int)w->islandJoints.size());
+      }
     }
     // broadphase at the end of Solve (b2_world.cpp:663-669)
     updatePairs(w);
@@ -2185,6 +2409,8 @@ int orc_world_load(void* h, const b2g_body* bodies, int32_t nb, const b2g_fixtur
     b.linearDamping = s.linear_damping; b.angularDamping = s.angular_damping; b.gravityScale = s.gravity_scale;
     b.force = v2(s.force[0], s.force[1]); b.torque = s.torque;
     b.type = s.type; b.flags = s.flags;
+    b.sleepTime = 0.0f;
+    if (b.type != 0 && !b.awake()) w->sleepers = true;
   }
   w->fixtures.resize(nf);
   for (int i = 0; i < nf; ++i) {
@@ -2236,6 +2462,50 @@ int orc_world_load(void* h, const b2g_body* bodies, int32_t nb, const b2g_fixtur
   w->newContacts = (nc == 0);
   w->inv_dt0 = inv_dt0;
   return 0;
+}
+
+// b2World::SetAllowSleeping (src/dynamics/b2_world.cpp:474-488): turning sleep off wakes every body.
+void orc_world_set_sleep(void* h, int32_t allow_sleep) {
+  World* w = (World*)h;
+  w->allowSleep = allow_sleep != 0;
+  if (!w->allowSleep) {
+    for (Body& b : w->bodies) setAwake(b, true);
+    w->sleepers = false;
+  }
+}
+
+// Marks the world's contacts for re-finding at the start of the next step (as b2World::Step does
+// after bodies were moved or fixtures created, b2_world.cpp:1113-1122).
+void orc_world_flag_new_contacts(void* h) { ((World*)h)->newContacts = true; }
+
+void orc_world_sleep_times(void* h, float* out) {
+  World* w = (World*)h;
+  for (size_t i = 0; i < w->bodies.size(); ++i) out[i] = w->bodies[i].sleepTime;
+}
+
+void orc_world_set_sleep_times(void* h, const float* in) {
+  World* w = (World*)h;
+  for (size_t i = 0; i < w->bodies.size(); ++i) w->bodies[i].sleepTime = in[i];
+}
+
+// The last step's islands (sleep-mode worlds): counts[0..3] = islands, bodies, contacts, joints.
+// Arrays (each may be null): per island root, orphan flag, body offsets (islands + 1), contact
+// offsets (islands + 1, in contacts), joint offsets (islands + 1); then the bodies, the contacts
+// as (fixture A, fixture B) pairs in solve order, and the joints in solve order.
+void orc_world_last_islands(void* h, int32_t* counts, int32_t* root, int32_t* orphan, int32_t* body_off,
+                            int32_t* contact_off, int32_t* joint_off, int32_t* bodies, int32_t* contacts,
+                            int32_t* joints) {
+  World* w = (World*)h;
+  counts[0] = (int32_t)w->islandRoot.size();
+  counts[1] = (int32_t)w->islandBodies.size();
+  counts[2] = (int32_t)w->islandContacts.size() / 2;
+  counts[3] = (int32_t)w->islandJoints.size();
+  auto cp = [](int32_t* dst, const std::vector<int32_t>& v) {
+    if (dst && !v.empty()) memcpy(dst, v.data(), v.size() * sizeof(int32_t));
+  };
+  cp(root, w->islandRoot); cp(orphan, w->islandOrphan); cp(body_off, w->islandBodyOff);
+  cp(contact_off, w->islandContactOff); cp(joint_off, w->islandJointOff); cp(bodies, w->islandBodies);
+  cp(contacts, w->islandContacts); cp(joints, w->islandJoints);
 }
 
 double orc_world_step(void* h, float dt, int32_t vi, int32_t pi, int32_t n) {

@@ -509,6 +509,104 @@ int ref_replay_step(void* h, float dt, int32_t vi, int32_t pi, const int32_t* co
   return 0;
 }
 
+// The bodies' sleep timers (b2Body::m_sleepTime), creation order.
+void ref_world_sleep_times(void* h, float* out) {
+  RefWorld* rw = (RefWorld*)h;
+  for (size_t i = 0; i < rw->bodies.size(); ++i) out[i] = rw->bodies[i]->m_sleepTime;
+}
+
+// One Step with b2World::Solve's island loop (src/dynamics/b2_world.cpp:492-670) replayed over
+// caller-given islands: the reference's own narrowphase (b2ContactManager::Collide, with its
+// sleep rules), then per island either b2Island::SolveOrphan (orphan islands, then flagged awake
+// as b2World::Solve does) or a b2Island holding the island's bodies (marked awake without a timer
+// reset), the static bodies its contacts and joints touch, its contacts and its joints in the
+// given order, solved with the world's sleep setting; then the reference's broadphase and dead
+// contact removal. Contacts are given as (fixture A, fixture B) pairs. Returns 1 when a listed
+// contact does not exist.
+int ref_replay_step_islands(void* h, float dt, int32_t vi, int32_t pi, int32_t n_islands, const int32_t* orphan,
+                            const int32_t* body_off, const int32_t* contact_off, const int32_t* joint_off,
+                            const int32_t* bodies, const int32_t* contact_pairs, const int32_t* joints) {
+  RefWorld* rw = (RefWorld*)h;
+  b2World* w = rw->world;
+  w->m_locked = true;
+  if (w->m_newContacts) w->m_contactManager.FindNewContacts();
+  if (w->m_newContacts || w->m_removedBodies) {
+    w->RemoveDeadContacts();
+    w->m_newContacts = false;
+    w->m_removedBodies = false;
+  }
+  b2TimeStep step;
+  step.dt = dt;
+  step.inv_dt = (dt > 0.0f) ? 1.0f / dt : 0.0f;
+  step.velocityIterations = vi;
+  step.positionIterations = pi;
+  step.particleIterations = 0;
+  step.dtRatio = w->m_inv_dt0 * dt;
+  step.warmStarting = w->m_warmStarting;
+  w->m_contactManager.Collide();
+  if (dt > 0.0f) {
+    std::map<std::pair<int, int>, b2Contact*> byPair;
+    for (b2Contact* c = w->GetContactListStart(); c != w->GetContactListEnd(); c = c->GetNext())
+      byPair[{rw->fixture_index[c->m_fixtureA], rw->fixture_index[c->m_fixtureB]}] = c;
+    for (b2Body* b : rw->bodies) {
+      b->m_xf0 = b->m_xf;
+      b->m_sweep.c0 = b->m_sweep.c;
+      b->m_sweep.a0 = b->m_sweep.a;
+    }
+    int maxc = 0, maxj = 0;
+    for (int k = 0; k < n_islands; ++k) {
+      maxc = std::max(maxc, contact_off[k + 1] - contact_off[k]);
+      maxj = std::max(maxj, joint_off[k + 1] - joint_off[k]);
+    }
+    b2Island island((int32)rw->bodies.size(), std::max(maxc, 1), std::max(maxj, 1), &w->m_stackAllocator,
+                    w->m_contactManager.m_contactListener);
+    for (int k = 0; k < n_islands; ++k) {
+      if (orphan[k]) {
+        b2Body* b = rw->bodies[bodies[body_off[k]]];
+        island.SolveOrphan(b, step, w->m_gravity, w->m_allowSleep);
+        b->m_flags |= (b2Body::e_islandFlag | b2Body::e_awakeFlag);
+        continue;
+      }
+      island.Clear();
+      std::vector<b2Body*> statics;
+      auto note_static = [&](b2Body* b) {
+        if (b->GetType() == b2_staticBody && std::find(statics.begin(), statics.end(), b) == statics.end())
+          statics.push_back(b);
+      };
+      std::vector<b2Contact*> cs;
+      for (int i = contact_off[k]; i < contact_off[k + 1]; ++i) {
+        auto it = byPair.find({contact_pairs[2 * i], contact_pairs[2 * i + 1]});
+        if (it == byPair.end()) {
+          w->m_locked = false;
+          return 1;
+        }
+        cs.push_back(it->second);
+        note_static(it->second->m_fixtureA->m_body);
+        note_static(it->second->m_fixtureB->m_body);
+      }
+      for (int i = joint_off[k]; i < joint_off[k + 1]; ++i) {
+        note_static(rw->joints[joints[i]]->m_bodyA);
+        note_static(rw->joints[joints[i]]->m_bodyB);
+      }
+      for (int i = body_off[k]; i < body_off[k + 1]; ++i) {
+        b2Body* b = rw->bodies[bodies[i]];
+        b->m_flags |= b2Body::e_awakeFlag;
+        island.Add(b);
+      }
+      for (b2Body* b : statics) island.Add(b);
+      for (b2Contact* c : cs) island.Add(c);
+      for (int i = joint_off[k]; i < joint_off[k + 1]; ++i) island.Add(rw->joints[joints[i]]);
+      island.Solve(step, w->m_gravity, w->m_allowSleep);
+    }
+    w->m_contactManager.FindNewContacts();
+    w->RemoveDeadContacts();
+    w->m_inv_dt0 = step.inv_dt;
+  }
+  if (w->m_clearForces) w->ClearForces();
+  w->m_locked = false;
+  return 0;
+}
+
 // Runs `ref_world_step`-style stepping of a list of worlds on `threads` host threads (each thread
 // steps a disjoint subset); returns wall seconds. Used as the multi-core CPU baseline.
 double ref_worlds_step_parallel(void** hs, int32_t n, float dt, int32_t vi, int32_t pi,

@@ -45,6 +45,9 @@ class Ref:
             "ref_world_query_aabb": ([vp, P(f32), P(i32), i32], i32),
             "ref_world_set_bodies": ([vp, P(G.Body)], None),
             "ref_replay_step": ([vp, f32, i32, i32, P(i32), i32, P(i32), i32], C.c_int),
+            "ref_replay_step_islands": ([vp, f32, i32, i32, i32, P(i32), P(i32), P(i32), P(i32), P(i32), P(i32),
+                                         P(i32)], C.c_int),
+            "ref_world_sleep_times": ([vp, P(f32)], None),
             "ref_worlds_step_parallel": ([P(vp), i32, f32, i32, i32, i32, i32], C.c_double),
         }
         for name, (a, r) in sig.items():
@@ -124,6 +127,19 @@ class RefWorld:
     def query_aabb(self, box):
         return _query(self._query_fn, self.h, box)
 
+    def sleep_times(self):
+        nb = self.sizes()[0]
+        arr = (f32 * max(nb, 1))()
+        self.ref.ref_world_sleep_times(self.h, arr)
+        return list(arr[:nb])
+
+    def replay_islands(self, islands, dt=1 / 60, vi=8, pi=3):
+        """One Step with the reference's island solver over the oracle's islands (last_islands)."""
+        root, orphan, boff, coff, joff, bodies, pairs, joints = islands
+        arr = lambda v: (i32 * max(len(v), 1))(*v)  # noqa: E731
+        return self.ref.ref_replay_step_islands(self.h, dt, vi, pi, len(root), arr(orphan), arr(boff), arr(coff),
+                                                arr(joff), arr(bodies), arr(pairs), arr(joints))
+
     def contacts(self):
         n = self.ref.ref_world_contacts(self.h, None, 0)
         arr = (G.Contact * max(n, 1))()
@@ -155,6 +171,12 @@ class Oracle:
             "orc_world_last_order": ([vp, P(i32), i32, P(i32), i32, P(i32)], i32),
             "orc_world_raycast": ([vp, P(f32), P(f32)], i32),
             "orc_world_query_aabb": ([vp, P(f32), P(i32), i32], i32),
+            "orc_world_set_sleep": ([vp, i32], None),
+            "orc_world_flag_new_contacts": ([vp], None),
+            "orc_world_sleep_times": ([vp, P(f32)], None),
+            "orc_world_set_sleep_times": ([vp, P(f32)], None),
+            "orc_world_last_islands": ([vp, P(i32), P(i32), P(i32), P(i32), P(i32), P(i32), P(i32), P(i32),
+                                        P(i32)], None),
             "orc_set_libm_trig": ([i32], None),
             "orc_pairs": ([P(f32), i32, P(C.c_uint64), C.c_int64], C.c_int64),
             "orc_worlds_step_parallel": ([P(vp), i32, f32, i32, i32, i32, i32], C.c_double),
@@ -225,6 +247,29 @@ class OracleWorld:
         arr = (G.Contact * max(n, 1))()
         self.orc.orc_world_contacts(self.h, arr, n)
         return arr[:n]
+
+    def set_sleep(self, allow):
+        self.orc.orc_world_set_sleep(self.h, int(allow))
+
+    def sleep_times(self):
+        nb = self.sizes()[0]
+        arr = (f32 * max(nb, 1))()
+        self.orc.orc_world_sleep_times(self.h, arr)
+        return list(arr[:nb])
+
+    def set_sleep_times(self, times):
+        self.orc.orc_world_set_sleep_times(self.h, (f32 * max(len(times), 1))(*times))
+
+    def last_islands(self):
+        """The last step's islands: (roots, orphan flags, body offsets, contact offsets, joint
+        offsets, bodies, contact fixture pairs, joints)."""
+        cnt = (i32 * 4)()
+        self.orc.orc_world_last_islands(self.h, cnt, *([None] * 8))
+        ni, nb, nc, nj = cnt
+        bufs = [(i32 * max(k, 1))() for k in (ni, ni, ni + 1, ni + 1, ni + 1, nb, 2 * nc, nj)]
+        self.orc.orc_world_last_islands(self.h, cnt, *bufs)
+        sizes = (ni, ni, ni + 1, ni + 1, ni + 1, nb, 2 * nc, nj)
+        return tuple(list(b[:k]) for b, k in zip(bufs, sizes))
 
     def last_order(self):
         nj = C.c_int32()

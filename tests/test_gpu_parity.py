@@ -511,3 +511,178 @@ def test_budget_exhaustion_fails_cleanly(lib):
         out.append(_state_bytes(b.bodies(w)))
         b.close()
     assert out[0] == out[1]
+
+
+def _awake_flags(records):
+    return [r.flags & 8 for r in records]
+
+
+def _sleep_world(batch, kind, n, seed, p0):
+    w = batch.add_world(0.0, -10.0)
+    batch.set_flags(w, allow_sleep=True)
+    batch.scene(w, kind, seed=seed, n=n, p0=p0, p1=0.6)
+    return w
+
+
+@pytest.mark.parametrize("kind,n,seed,p0,steps,vi,pi", [
+    (G.SCENE_PYRAMID, 10, 1, 1.0, 160, 8, 3),
+    (G.SCENE_CHAINS, 6, 4, 100.0, 500, 10, 4),
+    (G.SCENE_MIXED_DROP, 200, 5, 0.0, 490, 8, 3),
+    (G.SCENE_BATCH_WORLD, 200, 11, 0.0, 760, 8, 3),
+])
+def test_sleep_rollout_bit_exact(lib, orc, kind, n, seed, p0, steps, vi, pi):
+    """Sleeping on: islands fall asleep, are skipped while asleep and are woken by impacts and
+    through their islands; body states, awake flags and sleep timers equal the oracle's (whose
+    sleep rules are pinned to the reference step by step) after every step."""
+    batch = G.Batch(lib, device=0)
+    batch.set_debug_checks(True)  # colouring and island labels verified on the device every step
+    w = _sleep_world(batch, kind, n, seed, p0)
+    ow = ob.OracleWorld(orc, (0.0, -10.0), batch.bodies(w), batch.fixtures(w), batch.joints(w))
+    ow.set_sleep(True)
+    asleep_max, woken = 0, 0
+    prev = _awake_flags(batch.bodies(w))
+    for s in range(steps):
+        batch.step(1 / 60, vi, pi)
+        ow.step(1, 1 / 60, vi, pi)
+        g, o = batch.bodies(w), ow.bodies()
+        assert _state_bytes(g) == _state_bytes(o), f"step {s + 1}: {_first_diff(g, o)}"
+        cur = _awake_flags(g)
+        assert cur == _awake_flags(o), f"step {s + 1}: awake flags differ"
+        woken += sum(1 for x, y in zip(prev, cur) if y and not x)
+        asleep_max = max(asleep_max, sum(1 for r in g if r.type != 0 and not r.flags & 8))
+        prev = cur
+        if s % 20 == 19 or s == steps - 1:
+            assert batch.sleep_times(w) == ow.sleep_times(), f"step {s + 1}: sleep timers differ"
+    gc, oc = batch.contacts(w), ow.contacts()
+    assert [_contact_key(x) for x in gc] == [_contact_key(y) for y in oc]
+    assert asleep_max > 0
+    if kind == G.SCENE_CHAINS:
+        assert woken > 0
+    batch.close()
+
+
+def test_sleeping_pyramid_woken_by_a_moved_box(lib, orc):
+    """A sleeping pyramid whose top box is lifted and thrown down: the lifted box's destroyed
+    contacts wake the boxes under it, its impact wakes them again, the pyramid settles and falls
+    asleep anew; every step equals the oracle."""
+    batch = G.Batch(lib, device=0)
+    w = _sleep_world(batch, G.SCENE_PYRAMID, 10, 1, 1.0)
+    for _ in range(150):
+        batch.step(1 / 60, 8, 3)
+    bodies = batch.bodies(w)
+    assert all(not r.flags & 8 for r in bodies if r.type != 0)
+    top = max(range(len(bodies)), key=lambda i: bodies[i].c[1])
+    r = bodies[top]
+    r.c[1] += 3.0
+    r.xf[1] += 3.0
+    r.v[1] = -1.0
+    recs = list(bodies)
+    recs[top] = r
+    batch.write_bodies(w, recs)
+    ow = ob.OracleWorld(orc, (0.0, -10.0), batch.bodies(w), batch.fixtures(w), batch.joints(w),
+                        batch.contacts(w), inv_dt0=60.0)
+    ow.set_sleep(True)
+    ow.set_sleep_times(batch.sleep_times(w))
+    ow.orc.orc_world_flag_new_contacts(ow.h)
+    woken, asleep_end = 0, 0
+    prev = _awake_flags(batch.bodies(w))
+    for s in range(200):
+        batch.step(1 / 60, 8, 3)
+        ow.step(1, 1 / 60, 8, 3)
+        g, o = batch.bodies(w), ow.bodies()
+        assert _state_bytes(g) == _state_bytes(o), f"step {s + 1}: {_first_diff(g, o)}"
+        cur = _awake_flags(g)
+        assert cur == _awake_flags(o), f"step {s + 1}"
+        woken += sum(1 for x, y in zip(prev, cur) if y and not x)
+        prev = cur
+    assert batch.sleep_times(w) == ow.sleep_times()
+    assert woken > 5
+    batch.close()
+
+
+def test_sleep_worlds_batched_with_others_equal_alone(lib):
+    """Sleep-mode worlds and ordinary worlds stepped together (graph replay) give each world the
+    bits it gets alone; compaction and snapshots carry the sleep state."""
+    specs = [(G.SCENE_PYRAMID, 10, 1, 1.0, True), (G.SCENE_BATCH_WORLD, 300, 7, 0.0, False),
+             (G.SCENE_BATCH_WORLD, 200, 11, 0.0, True), (G.SCENE_CHAINS, 6, 4, 100.0, True),
+             (G.SCENE_MIXED_DROP, 150, 3, 0.0, False)]
+
+    def make(batch, spec):
+        kind, n, seed, p0, sleep = spec
+        w = batch.add_world(0.0, -10.0)
+        batch.set_flags(w, allow_sleep=sleep)
+        batch.scene(w, kind, seed=seed, n=n, p0=p0, p1=0.6)
+        return w
+
+    together = G.Batch(lib, device=0)
+    together.set_debug_checks(True)
+    ws = [make(together, sp) for sp in specs]
+    for _ in range(300):
+        together.step(1 / 60, 8, 3)
+    snap = together.snapshot(ws[2])
+    # retire the second world and compact: the others keep their sleep state
+    lib.check(lib.b2g_world_retire(together.h, ws[1]), "retire")
+    nmap = (C.c_int32 * len(ws))()
+    lib.check(lib.b2g_compact(together.h, nmap, len(ws)), "compact")
+    kept = [nmap[w] for w in ws]
+    restored = together.restore(snap)
+    for _ in range(200):
+        together.step(1 / 60, 8, 3)
+    for i, sp in enumerate(specs):
+        if i == 1:
+            continue
+        alone = G.Batch(lib, device=0)
+        a = make(alone, sp)
+        alone.set_graphs(False)
+        for _ in range(500):
+            alone.step(1 / 60, 8, 3)
+        w = kept[i]
+        assert _state_bytes(together.bodies(w)) == _state_bytes(alone.bodies(a)), i
+        assert _awake_flags(together.bodies(w)) == _awake_flags(alone.bodies(a)), i
+        assert together.sleep_times(w) == alone.sleep_times(a), i
+        if i == 2:  # the restored copy went on from step 300 like the original
+            assert _state_bytes(together.bodies(restored)) == _state_bytes(alone.bodies(a))
+            assert together.sleep_times(restored) == alone.sleep_times(a)
+        alone.close()
+    together.close()
+
+
+def test_set_awake_and_disallowing_sleep(lib, orc):
+    """b2Body::SetAwake(false) on a falling body freezes it until a contact wakes it, and
+    SetAllowSleeping(false) wakes every body: both equal the oracle."""
+    batch = G.Batch(lib, device=0)
+    w = _sleep_world(batch, G.SCENE_PYRAMID, 10, 1, 1.0)
+    for _ in range(150):
+        batch.step(1 / 60, 8, 3)
+    assert all(not r.flags & 8 for r in batch.bodies(w) if r.type != 0)
+    ow = ob.OracleWorld(orc, (0.0, -10.0), batch.bodies(w), batch.fixtures(w), batch.joints(w),
+                        batch.contacts(w), inv_dt0=60.0)
+    ow.set_sleep(True)
+    ow.set_sleep_times(batch.sleep_times(w))
+    for _ in range(30):
+        batch.step(1 / 60, 8, 3)
+        ow.step(1, 1 / 60, 8, 3)
+    assert _state_bytes(batch.bodies(w)) == _state_bytes(ow.bodies())
+    batch.set_flags(w, allow_sleep=False)
+    ow.set_sleep(False)
+    assert all(r.flags & 8 for r in batch.bodies(w) if r.type != 0)
+    for s in range(30):
+        batch.step(1 / 60, 8, 3)
+        ow.step(1, 1 / 60, 8, 3)
+        assert _state_bytes(batch.bodies(w)) == _state_bytes(ow.bodies()), s
+    # a body put to sleep by hand: flags, velocity and force cleared; its island wakes it again
+    batch.set_flags(w, allow_sleep=True)
+    top = len(batch.bodies(w)) - 1
+    batch.set_awake(w, top, False)
+    r = batch.bodies(w)[top]
+    assert not r.flags & 8 and tuple(r.v) == (0.0, 0.0) and r.w == 0.0 and tuple(r.force) == (0.0, 0.0)
+    ow = ob.OracleWorld(orc, (0.0, -10.0), batch.bodies(w), batch.fixtures(w), batch.joints(w),
+                        batch.contacts(w), inv_dt0=60.0)
+    ow.set_sleep(True)
+    ow.set_sleep_times(batch.sleep_times(w))
+    for s in range(40):
+        batch.step(1 / 60, 8, 3)
+        ow.step(1, 1 / 60, 8, 3)
+        assert _state_bytes(batch.bodies(w)) == _state_bytes(ow.bodies()), s
+        assert _awake_flags(batch.bodies(w)) == _awake_flags(ow.bodies()), s
+    batch.close()

@@ -212,3 +212,49 @@ def test_oracle_queries_vs_reference_live(ref, orc, kind, n, seed, p0):
     assert found > 0
     rw.close()
     ow.close()
+
+
+@pytest.mark.parametrize("kind,n,seed,p0,warm,steps,vi,pi", [
+    (G.SCENE_PYRAMID, 10, 1, 1.0, 85, 40, 8, 3),          # the pyramid falls asleep as one island
+    (G.SCENE_CHAINS, 6, 4, 100.0, 262, 70, 10, 4),        # chains and a pile: islands fall asleep
+    (G.SCENE_CHAINS, 6, 4, 100.0, 468, 15, 10, 4),        # ... and are woken (5 bodies at step 475)
+    (G.SCENE_MIXED_DROP, 200, 5, 0.0, 300, 35, 8, 3),     # settled bodies fall asleep
+    (G.SCENE_MIXED_DROP, 200, 5, 0.0, 466, 15, 8, 3),     # a late body wakes sleeping ones (step 473)
+    (G.SCENE_BATCH_WORLD, 300, 7, 0.0, 450, 35, 8, 3),    # 144 bodies fall asleep
+    (G.SCENE_BATCH_WORLD, 200, 11, 0.0, 740, 12, 8, 3),   # 83 bodies woken through their island (748)
+])
+def test_oracle_sleep_replay_vs_reference_live(ref, orc, kind, n, seed, p0, warm, steps, vi, pi):
+    """Sleeping pinned to the reference, step by step: the reference world (sleep allowed) is
+    loaded into the oracle, the oracle steps once, and the reference replays that step with its
+    own narrowphase (awake rules, wakes on touching changes), its own b2Island::Solve or
+    SolveOrphan per island of the oracle's partition and order (sleep timers, per-island position
+    exit, SetAwake(false)) and its own broadphase (wakes of destroyed contacts). Body states, awake
+    flags and sleep timers must agree bit for bit after every step."""
+    rw = ob.RefWorld(ref, kind, seed=seed, n=n, p0=p0, p1=0.6, allow_sleep=True)
+    rw.step(warm, vi=vi, pi=pi)
+    orc.orc_set_libm_trig(1)
+    asleep_seen, transitions, woken = 0, 0, 0
+    try:
+        prev = None
+        for s in range(steps):
+            ow = ob.OracleWorld(orc, (0.0, -10.0), list(rw.bodies()), list(rw.fixtures()), list(rw.joints()),
+                                list(rw.contacts()), inv_dt0=60.0)
+            ow.set_sleep(True)
+            ow.set_sleep_times(rw.sleep_times())
+            ow.step(1, 1 / 60, vi, pi)
+            assert rw.replay_islands(ow.last_islands(), 1 / 60, vi, pi) == 0
+            rb, obd = rw.bodies(), ow.bodies()
+            for i, (x, y) in enumerate(zip(rb, obd)):
+                assert bytes(x)[:40] == bytes(y)[:40] and x.flags == y.flags, f"step {s + 1} body {i}"
+            assert rw.sleep_times() == ow.sleep_times(), f"step {s + 1}"
+            awake = tuple(b.flags & 8 for b in rb)
+            asleep_seen = max(asleep_seen, sum(1 for b in rb if b.type != 0 and not b.flags & 8))
+            if prev is not None and awake != prev:
+                transitions += 1
+                woken += sum(1 for x, y in zip(prev, awake) if y and not x)
+            prev = awake
+    finally:
+        orc.orc_set_libm_trig(0)
+    assert asleep_seen > 0 and transitions > 0
+    if warm in (468, 466, 740):
+        assert woken > 0
