@@ -219,16 +219,64 @@ def query_bench(batch, n_rays):
             "timing": "end to end through the C ABI with host buffers, mean of 3 calls after a warm-up call"}
 
 
-def build_batch(lib, seeds, device):
+def build_batch(lib, seeds, device, allow_sleep=False):
     batch = G.Batch(lib, device=device)
     nb = 0
     for s in seeds:
         n, gx, gy = world_params(lib, s)
         w = batch.add_world(gx, gy)
-        batch.set_flags(w, allow_sleep=False, warm_starting=True, continuous=False)
+        batch.set_flags(w, allow_sleep=allow_sleep, warm_starting=True, continuous=False)
         c = batch.scene(w, G.SCENE_BATCH_WORLD, seed=s, n=n)
         nb += c[0]
     return batch, nb
+
+
+def sleep_bench(lib, dev, seeds, settle, steps, cpu):
+    """Island sleep on: a sample of the same worlds settles for `settle` steps with sleeping
+    allowed, then `steps` steps are timed (CUDA events); the same sample with sleeping off is
+    timed over the same window, and, with `cpu`, the CPU oracle steps the sample with sleeping
+    allowed (the reference's default) over the same window on all host threads."""
+    out = {}
+    for sleep in (True, False):
+        batch, nb = build_batch(lib, seeds, dev, allow_sleep=sleep)
+        batch.step_timed(settle, DT, VI, PI)
+        ms = batch.step_timed(steps, DT, VI, PI)
+        asleep = 0
+        for w in range(len(seeds)):
+            asleep += sum(1 for r in batch.bodies(w) if r.type != 0 and not r.flags & G.BODY_AWAKE)
+        batch.set_graphs(False)
+        batch.step(DT, VI, PI)  # one eager step for the per-phase breakdown
+        p = batch.profile()
+        out["on" if sleep else "off"] = {"value": nb * steps / (ms / 1e3), "ms_per_step": ms / steps,
+                                         "asleep_fraction": asleep / nb,
+                                         "breakdown_ms": {"collide": p.collide, "solve": p.solve,
+                                                          "broadphase": p.broadphase}}
+        batch.close()
+    res = {"value": out["on"]["value"], "unit": "body-steps/s", "ms_per_step": out["on"]["ms_per_step"],
+           "asleep_fraction": out["on"]["asleep_fraction"], "sleep_off_value": out["off"]["value"],
+           "breakdown_ms": out["on"]["breakdown_ms"], "sleep_off_breakdown_ms": out["off"]["breakdown_ms"],
+           "sample": f"{len(seeds)} of the worlds ({nb} bodies), steps {settle + 1}-{settle + steps}"}
+    if cpu:
+        import oracle_bind as ob  # noqa: PLC0415 - CPU baseline leg only
+
+        threads = os.cpu_count() or 1
+        orc = ob.Oracle()
+        host = G.Batch(lib, device=G.HOST_ONLY)
+        worlds = []
+        for s in seeds:
+            n, gx, gy = world_params(lib, s)
+            w = host.add_world(gx, gy)
+            host.scene(w, G.SCENE_BATCH_WORLD, seed=s, n=n)
+            ow = ob.OracleWorld(orc, (gx, gy), host.bodies(w), host.fixtures(w), host.joints(w))
+            ow.set_sleep(True)
+            worlds.append(ow)
+        hs = (C.c_void_p * len(worlds))(*[w.h for w in worlds])
+        orc.orc_worlds_step_parallel(hs, len(worlds), DT, VI, PI, settle, threads)
+        secs = orc.orc_worlds_step_parallel(hs, len(worlds), DT, VI, PI, steps, threads)
+        host.close()
+        res["cpu_baseline"] = {"value": nb * steps / secs, "unit": "body-steps/s", "cores": threads, "kind": "port",
+                               "sample": "the same worlds and window, sleeping allowed"}
+    return res
 
 
 def solve_traffic(sb):
@@ -383,6 +431,13 @@ def run_ours(args, rank, world_size):
     if args.rays > 0:
         queries = query_bench(batch, args.rays)
 
+    # island sleep on a sample of the same worlds (settled, then timed), beside sleep off and the CPU
+    sleep = None
+    if args.sleep_worlds > 0:
+        ss = seeds[:: max(1, len(seeds) // args.sleep_worlds)][: args.sleep_worlds]
+        sleep = sleep_bench(lib, dev, ss, args.sleep_settle, max(3, args.steps // 2),
+                            rank == 0 and world_size == 1 and not args.no_cpu)
+
     # per-phase breakdown: one eager (non-graph) step after the timed region
     lib.b2g_batch_set_graphs(batch.h, 0)
     batch.step(DT, VI, PI)
@@ -467,6 +522,7 @@ def run_ours(args, rank, world_size):
             "gpu_launches": kernels_per_step * args.steps,
             "contact_constraint_iterations_per_s": contact_iters,
             "queries": queries,
+            "sleep": sleep,
             "clocks": clocks.summary(),
         }
     batch.close()
@@ -512,6 +568,8 @@ def main():
     ap.add_argument("--serve-seconds", type=float, default=12.0)
     ap.add_argument("--no-autotune", action="store_true", help="keep the default solver threads per world")
     ap.add_argument("--rays", type=int, default=1 << 20, help="rays of the world-query measurement (0: skip)")
+    ap.add_argument("--sleep-worlds", type=int, default=256, help="worlds of the island-sleep measurement (0: skip)")
+    ap.add_argument("--sleep-settle", type=int, default=480, help="steps before the island-sleep window")
     ap.add_argument("--profile-window", action="store_true",
                     help="ncu case: settle --settle steps, then 2 steps inside the NVTX range 'profile'")
     ap.add_argument("--settle", type=int, default=250)

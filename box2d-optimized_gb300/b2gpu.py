@@ -24,6 +24,7 @@ SHAPE_CIRCLE, SHAPE_EDGE, SHAPE_POLYGON = 0, 1, 2
 JOINT_REVOLUTE, JOINT_PRISMATIC, JOINT_DISTANCE = 1, 2, 3
 POLY_HULL, POLY_BOX, POLY_BOX_ORIENTED, POLY_RAW = 0, 1, 2, 3
 SCENE_PYRAMID, SCENE_MIXED_DROP, SCENE_CHAINS, SCENE_BATCH_WORLD = 0, 1, 2, 3
+BODY_ENABLED, BODY_FIXED_ROTATION, BODY_BULLET, BODY_AWAKE, BODY_AUTO_SLEEP = 1, 2, 4, 8, 16
 HOST_ONLY = -1  # B2G_HOST_ONLY: a batch built and read on the host only (no device)
 EVENT_BEGIN, EVENT_END, EVENT_PRESOLVE, EVENT_POSTSOLVE = 1, 2, 3, 4
 CONTACT_TOUCHING, CONTACT_ENABLED = 2, 4

@@ -128,6 +128,13 @@ __global__ void k_collide_closure(KernelArgs a) {
   const int w = blockIdx.x;
   const int wf = a.wflags[w];
   if (!(wf & B2G_WF_ACTIVE) || !(wf & B2G_WF_SLEEPMODE)) return;
+  // a contact joins only through a body that slept at the start of the step and has been woken
+  // since: nothing to do unless the world has one
+  const int4 wb = a.wb[w];
+  int trigger = 0;
+  for (int i = threadIdx.x; i < wb.y && !trigger; i += blockDim.x)
+    trigger = a.bwake[wb.x + i] && !(a.bstate[wb.x + i].x & B2G_BS_AWAKE);
+  if (!__syncthreads_or(trigger)) return;
   const int2 wc = a.wc[w];
   const int c0 = wc.x, n = wc.y;
   for (int round = 0; round <= n; ++round) {

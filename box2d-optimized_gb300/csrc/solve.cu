@@ -390,22 +390,19 @@ struct SmemCarver {
 // Connected components over solid contacts (touching, enabled, no sensor) and joints between
 // non-static bodies, as a lock-free union-find that always hooks the larger root under the
 // smaller: every component's root is its lowest body index, whatever the order of the unions.
+// A world's island records are touched by its CTA alone: every access is a CTA-scope atomic
+// (loads included, so that none is served from a line older than an atomic), and the CTA barrier
+// orders the phases.
 __device__ __forceinline__ int isl_load(int* p) {
-  return cuda::atomic_ref<int, cuda::thread_scope_device>(*p).load(cuda::memory_order_relaxed);
+  return cuda::atomic_ref<int, cuda::thread_scope_block>(*p).load(cuda::memory_order_relaxed);
 }
 __device__ __forceinline__ void isl_store(int* p, int v) {
-  cuda::atomic_ref<int, cuda::thread_scope_device>(*p).store(v, cuda::memory_order_relaxed);
+  cuda::atomic_ref<int, cuda::thread_scope_block>(*p).store(v, cuda::memory_order_relaxed);
 }
 __device__ __forceinline__ void isl_or(int* p, int v) {
-  cuda::atomic_ref<int, cuda::thread_scope_device>(*p).fetch_or(v, cuda::memory_order_relaxed);
+  cuda::atomic_ref<int, cuda::thread_scope_block>(*p).fetch_or(v, cuda::memory_order_relaxed);
 }
-// Every access to the island records goes through device-scope atomics (never a plain load that
-// the SM's L1 could serve from a line older than an atomic performed in L2), and each phase ends
-// with a device-scope fence before the CTA barrier.
-__device__ __forceinline__ void isl_sync() {
-  __threadfence();
-  __syncthreads();
-}
+__device__ __forceinline__ void isl_sync() { __syncthreads(); }
 __device__ __forceinline__ int isl_label(int4* SL, int i) { return isl_load(&SL[i].x); }
 __device__ __forceinline__ int isl_bits(int4* SL, int i) { return isl_load(&SL[i].y); }
 
@@ -434,7 +431,10 @@ __device__ void isl_unite(int4* SL, int x, int y, unsigned int* status) {
       x = y;
       y = t;
     }
-    if (atomicCAS(&SL[x].x, x, y) == x) return;  // x was hooked meanwhile: retry from its root
+    int expect = x;  // x was hooked meanwhile when this fails: retry from its root
+    if (cuda::atomic_ref<int, cuda::thread_scope_block>(SL[x].x)
+            .compare_exchange_strong(expect, y, cuda::memory_order_relaxed))
+      return;
   }
   raise_status(status, B2G_DEV_STACK_OVERFLOW);
 }
@@ -543,7 +543,7 @@ __device__ void sleep_islands(const KernelArgs& a, int b0, int nb) {
       }
     } else {
       // t >= 0: the bit patterns order as the floats
-      cuda::atomic_ref<int, cuda::thread_scope_device>(SL[ex].w).fetch_min(__float_as_int(t), cuda::memory_order_relaxed);
+      cuda::atomic_ref<int, cuda::thread_scope_block>(SL[ex].w).fetch_min(__float_as_int(t), cuda::memory_order_relaxed);
     }
     BS[i] = st;
   }
@@ -850,7 +850,6 @@ __global__ void __launch_bounds__(T, 1024 / T) k_solve(KernelArgs a, int first, 
         if (isl_load(&SL[i].z) == it + 1) pending = 1;
         else isl_or(&SL[i].y, B2G_ISL_DONE);
       }
-      __threadfence();
       if (!__syncthreads_or(pending)) break;
     } else if (__syncthreads_and(okay)) {
       break;
