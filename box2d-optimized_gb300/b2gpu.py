@@ -23,7 +23,9 @@ STATIC, KINEMATIC, DYNAMIC = 0, 1, 2
 SHAPE_CIRCLE, SHAPE_EDGE, SHAPE_POLYGON = 0, 1, 2
 JOINT_REVOLUTE, JOINT_PRISMATIC, JOINT_DISTANCE = 1, 2, 3
 POLY_HULL, POLY_BOX, POLY_BOX_ORIENTED, POLY_RAW = 0, 1, 2, 3
-SCENE_PYRAMID, SCENE_MIXED_DROP, SCENE_CHAINS, SCENE_BATCH_WORLD = 0, 1, 2, 3
+SCENE_PYRAMID, SCENE_MIXED_DROP, SCENE_CHAINS, SCENE_BATCH_WORLD, SCENE_JOINTS = 0, 1, 2, 3, 4
+JOINT_REVOLUTE, JOINT_PRISMATIC, JOINT_DISTANCE, JOINT_PULLEY, JOINT_MOUSE = 1, 2, 3, 4, 5
+JOINT_WHEEL, JOINT_WELD, JOINT_FRICTION, JOINT_MOTOR = 7, 8, 9, 11
 BODY_ENABLED, BODY_FIXED_ROTATION, BODY_BULLET, BODY_AWAKE, BODY_AUTO_SLEEP = 1, 2, 4, 8, 16
 HOST_ONLY = -1  # B2G_HOST_ONLY: a batch built and read on the host only (no device)
 EVENT_BEGIN, EVENT_END, EVENT_PRESOLVE, EVENT_POSTSOLVE = 1, 2, 3, 4
@@ -76,7 +78,10 @@ class JointDef(C.Structure):
                 ("upper", C.c_float), ("enable_motor", C.c_int32), ("max_motor", C.c_float),
                 ("motor_speed", C.c_float), ("length", C.c_float), ("min_length", C.c_float),
                 ("max_length", C.c_float), ("stiffness", C.c_float), ("damping", C.c_float),
-                ("user_data", C.c_uint64)]
+                ("linear_offset", F2), ("max_force", C.c_float), ("max_torque", C.c_float),
+                ("correction_factor", C.c_float), ("target", F2), ("ground_anchor_a", F2),
+                ("ground_anchor_b", F2), ("length_a", C.c_float), ("length_b", C.c_float),
+                ("ratio", C.c_float), ("user_data", C.c_uint64)]
 
 
 class Body(C.Structure):

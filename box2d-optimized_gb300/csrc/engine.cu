@@ -165,6 +165,20 @@ static KernelArgs make_args(Batch* b) {
 }
 
 // ------------------------------------------------------------------------------ layout upload
+// Per-joint constants set by the reference's joint constructors: the prismatic and wheel axes
+// (b2_prismatic_joint.cpp:84-90, b2_wheel_joint.cpp:44-45) and the pulley's rope constant
+// (b2_pulley_joint.cpp:67).
+static void init_joint_dev(const b2g_joint_def& def, JointDev* d) {
+  if (def.type == B2G_JOINT_PRISMATIC || def.type == B2G_JOINT_WHEEL) {
+    V2 ax = mk(def.local_axis_a[0], def.local_axis_a[1]);
+    V2 ay = cross(1.0f, ax);
+    d->localXAxisA[0] = ax.x; d->localXAxisA[1] = ax.y;
+    d->localYAxisA[0] = ay.x; d->localYAxisA[1] = ay.y;
+  } else if (def.type == B2G_JOINT_PULLEY) {
+    d->constant = def.length_a + def.ratio * def.length_b;
+  }
+}
+
 // Device world flags: the host flags without the per-step ones, plus the sleep bits.
 static int device_world_flags(const HostWorld& hw) {
   int f = hw.flags & ~(B2G_WF_ACTIVE | B2G_WF_NEW_CONTACTS | B2G_WF_SLEEPMODE | B2G_WF_ALLOW_SLEEP);
@@ -298,12 +312,7 @@ int upload_all(Batch* b) {
       d.d.body_b += bo;
       d.impulse[0] = j.impulse[0]; d.impulse[1] = j.impulse[1]; d.impulse[2] = j.impulse[2];
       d.motorImpulse = j.motor_impulse; d.lowerImpulse = j.lower_impulse; d.upperImpulse = j.upper_impulse;
-      if (j.def.type == B2G_JOINT_PRISMATIC) {
-        V2 ax = mk(j.def.local_axis_a[0], j.def.local_axis_a[1]);
-        V2 ay = cross(1.0f, ax);
-        d.localXAxisA[0] = ax.x; d.localXAxisA[1] = ax.y;
-        d.localYAxisA[0] = ay.x; d.localYAxisA[1] = ay.y;
-      }
+      init_joint_dev(j.def, &d);
       if (!j.def.collide_connected) {
         uint32_t x = (uint32_t)(bo + j.def.body_a), y = (uint32_t)(bo + j.def.body_b);
         if (x > y) std::swap(x, y);
@@ -518,12 +527,7 @@ int upload_tail(Batch* b) {
       d.d.body_b += bo;
       d.impulse[0] = j.impulse[0]; d.impulse[1] = j.impulse[1]; d.impulse[2] = j.impulse[2];
       d.motorImpulse = j.motor_impulse; d.lowerImpulse = j.lower_impulse; d.upperImpulse = j.upper_impulse;
-      if (j.def.type == B2G_JOINT_PRISMATIC) {
-        V2 ax = mk(j.def.local_axis_a[0], j.def.local_axis_a[1]);
-        V2 ay = cross(1.0f, ax);
-        d.localXAxisA[0] = ax.x; d.localXAxisA[1] = ax.y;
-        d.localYAxisA[0] = ay.x; d.localYAxisA[1] = ay.y;
-      }
+      init_joint_dev(j.def, &d);
       joints.push_back(d);
       if (!j.def.collide_connected) {
         uint32_t x = (uint32_t)(bo + j.def.body_a), y = (uint32_t)(bo + j.def.body_b);
@@ -663,11 +667,24 @@ int download_state(Batch* b) {
         V2 f = d.impulse[0] * perp + ((d.motorImpulse + d.lowerImpulse) - d.upperImpulse) * axis;
         r.reaction_impulse[0] = f.x; r.reaction_impulse[1] = f.y;
         r.reaction_angular_impulse = d.impulse[1];
-      } else {
+      } else if (r.def.type == B2G_JOINT_DISTANCE) {
         V2 u = mk(d.u[0], d.u[1]);
         V2 f = ((d.impulse[0] + d.lowerImpulse) - d.upperImpulse) * u;
         r.reaction_impulse[0] = f.x; r.reaction_impulse[1] = f.y;
         r.reaction_angular_impulse = 0.0f;
+      } else if (r.def.type == B2G_JOINT_WHEEL) {  // b2_wheel_joint.cpp:448-456
+        V2 f = d.impulse[0] * mk(d.perp[0], d.perp[1]) +
+               ((d.impulse[1] + d.lowerImpulse) - d.upperImpulse) * mk(d.axis[0], d.axis[1]);
+        r.reaction_impulse[0] = f.x; r.reaction_impulse[1] = f.y;
+        r.reaction_angular_impulse = d.motorImpulse;
+      } else if (r.def.type == B2G_JOINT_PULLEY) {  // b2_pulley_joint.cpp:276-286
+        V2 f = d.impulse[0] * mk(d.uB[0], d.uB[1]);
+        r.reaction_impulse[0] = f.x; r.reaction_impulse[1] = f.y;
+        r.reaction_angular_impulse = 0.0f;
+      } else {  // weld, motor, friction (x, y, angular), mouse (x, y)
+        r.reaction_impulse[0] = d.impulse[0];
+        r.reaction_impulse[1] = d.impulse[1];
+        r.reaction_angular_impulse = r.def.type == B2G_JOINT_MOUSE ? 0.0f : d.impulse[2];
       }
     }
     hw.contacts.clear();
@@ -1579,8 +1596,15 @@ B2G_API int b2g_joints_add(b2g_batch* b, int32_t world, const b2g_joint_def* def
   HostWorld& w0 = b->worlds[world];
   for (int i = 0; i < n; ++i) {
     const b2g_joint_def& d = defs[i];
-    if (d.type != B2G_JOINT_REVOLUTE && d.type != B2G_JOINT_PRISMATIC && d.type != B2G_JOINT_DISTANCE) {
+    const int t = d.type;
+    if (t != B2G_JOINT_REVOLUTE && t != B2G_JOINT_PRISMATIC && t != B2G_JOINT_DISTANCE && t != B2G_JOINT_PULLEY &&
+        t != B2G_JOINT_MOUSE && t != B2G_JOINT_WHEEL && t != B2G_JOINT_WELD && t != B2G_JOINT_FRICTION &&
+        t != B2G_JOINT_MOTOR) {
       set_error(b, "unsupported joint type");
+      return B2G_E_INVALID_ARG;
+    }
+    if (t == B2G_JOINT_PULLEY && !(d.ratio != 0.0f)) {  // b2PulleyJoint ctor asserts ratio != 0
+      set_error(b, "pulley ratio must be non-zero");
       return B2G_E_INVALID_ARG;
     }
     if (d.body_a < 0 || d.body_a >= (int)w0.bodies.size() || d.body_b < 0 || d.body_b >= (int)w0.bodies.size() ||
@@ -1606,6 +1630,12 @@ B2G_API int b2g_joints_add(b2g_batch* b, int32_t world, const b2g_joint_def* def
       j.def.length = fmax2(j.def.length, B2G_LINEAR_SLOP);
       j.def.min_length = fmax2(j.def.min_length, B2G_LINEAR_SLOP);
       j.def.max_length = fmax2(j.def.max_length, j.def.min_length);
+    } else if (j.def.type == B2G_JOINT_MOUSE) {
+      // b2MouseJoint ctor: the target in body B's frame (b2_mouse_joint.cpp:38-40, b2MulT)
+      const b2g_body& bB = w.bodies[j.def.body_b];
+      float px = j.def.target[0] - bB.xf[0], py = j.def.target[1] - bB.xf[1];
+      j.def.local_anchor_b[0] = bB.xf[3] * px + bB.xf[2] * py;
+      j.def.local_anchor_b[1] = -bB.xf[2] * px + bB.xf[3] * py;
     }
     if (out_ids) out_ids[i] = (int32_t)w.joints.size();
     w.joints.push_back(j);

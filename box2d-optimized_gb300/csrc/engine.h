@@ -39,6 +39,15 @@ struct JointDev {
   float a1, a2, s1, s2, translation;
   float u[2], currentLength, mass, softMass, gamma, bias;
   float reaction[3];          // force x, y, torque at the last step's inv_dt
+  // weld (b2_weld_joint.h:117-125), wheel (b2_wheel_joint.h:178-212), motor (b2_motor_joint.h:
+  // 106-122), mouse (b2_mouse_joint.h:110-127) and pulley (b2_pulley_joint.h:125-148) temporaries;
+  // the wheel keeps ax/ay in axis/perp and sAx, sBx, sAy, sBy in a1, a2, s1, s2, the motor and
+  // friction joints their linear mass in K and angular mass in axialMass, the mouse joint its
+  // mass in K, beta in bias and m_C in err, the pulley m_uA in u
+  float mass3[9];             // weld m_mass (ex, ey, ez)
+  float springMass, motorMass;
+  float err[2], angularError;
+  float uB[2], constant;
 };
 
 // Per-contact velocity / position constraint (b2ContactVelocityConstraint and

@@ -361,6 +361,54 @@ void b2PrismaticJointDef::Initialize(b2Body* bA, b2Body* bB, const b2Vec2& ancho
   localAxisA = bodyA->GetLocalVector(axis);
   referenceAngle = bodyB->GetAngle() - bodyA->GetAngle();
 }
+// b2WeldJointDef::Initialize (src/dynamics/b2_weld_joint.cpp:39-46)
+void b2WeldJointDef::Initialize(b2Body* bA, b2Body* bB, const b2Vec2& anchor) {
+  bodyA = bA;
+  bodyB = bB;
+  localAnchorA = bodyA->GetLocalPoint(anchor);
+  localAnchorB = bodyB->GetLocalPoint(anchor);
+  referenceAngle = bodyB->GetAngle() - bodyA->GetAngle();
+}
+// b2WheelJointDef::Initialize (src/dynamics/b2_wheel_joint.cpp:33-40)
+void b2WheelJointDef::Initialize(b2Body* bA, b2Body* bB, const b2Vec2& anchor, const b2Vec2& axis) {
+  bodyA = bA;
+  bodyB = bB;
+  localAnchorA = bodyA->GetLocalPoint(anchor);
+  localAnchorB = bodyB->GetLocalPoint(anchor);
+  localAxisA = bodyA->GetLocalVector(axis);
+}
+// b2MotorJointDef::Initialize (src/dynamics/b2_motor_joint.cpp:34-44)
+void b2MotorJointDef::Initialize(b2Body* bA, b2Body* bB) {
+  bodyA = bA;
+  bodyB = bB;
+  b2Vec2 xB = bodyB->GetPosition();
+  linearOffset = bodyA->GetLocalPoint(xB);
+  float angleA = bodyA->GetAngle();
+  float angleB = bodyB->GetAngle();
+  angularOffset = angleB - angleA;
+}
+// b2FrictionJointDef::Initialize (src/dynamics/b2_friction_joint.cpp:38-44)
+void b2FrictionJointDef::Initialize(b2Body* bA, b2Body* bB, const b2Vec2& anchor) {
+  bodyA = bA;
+  bodyB = bB;
+  localAnchorA = bodyA->GetLocalPoint(anchor);
+  localAnchorB = bodyB->GetLocalPoint(anchor);
+}
+// b2PulleyJointDef::Initialize (src/dynamics/b2_pulley_joint.cpp:39-58)
+void b2PulleyJointDef::Initialize(b2Body* bA, b2Body* bB, const b2Vec2& groundA, const b2Vec2& groundB,
+                                  const b2Vec2& anchorA, const b2Vec2& anchorB, float r) {
+  bodyA = bA;
+  bodyB = bB;
+  groundAnchorA = groundA;
+  groundAnchorB = groundB;
+  localAnchorA = bodyA->GetLocalPoint(anchorA);
+  localAnchorB = bodyB->GetLocalPoint(anchorB);
+  b2Vec2 dA = anchorA - groundA;
+  lengthA = dA.Length();
+  b2Vec2 dB = anchorB - groundB;
+  lengthB = dB.Length();
+  ratio = r;
+}
 void b2DistanceJointDef::Initialize(b2Body* b1, b2Body* b2, const b2Vec2& anchor1, const b2Vec2& anchor2) {
   bodyA = b1;
   bodyB = b2;
@@ -493,7 +541,7 @@ b2Joint* b2World::CreateJoint(const b2JointDef* def) {
   d.collide_connected = def->collideConnected ? 1 : 0;
   d.user_data = def->userData.pointer;
   std::unique_ptr<b2Joint> j;
-  b2Vec2 la, lb;
+  b2Vec2 la(0.0f, 0.0f), lb(0.0f, 0.0f);  // the motor and mouse joints have no local anchor A
   if (def->type == e_revoluteJoint) {
     const b2RevoluteJointDef* r = (const b2RevoluteJointDef*)def;
     d.type = B2G_JOINT_REVOLUTE;
@@ -518,6 +566,48 @@ b2Joint* b2World::CreateJoint(const b2JointDef* def) {
     d.length = q->length; d.min_length = q->minLength; d.max_length = q->maxLength;
     d.stiffness = q->stiffness; d.damping = q->damping;
     j.reset(new b2DistanceJoint());
+  } else if (def->type == e_weldJoint) {
+    const b2WeldJointDef* q = (const b2WeldJointDef*)def;
+    d.type = B2G_JOINT_WELD;
+    la = q->localAnchorA; lb = q->localAnchorB;
+    d.reference_angle = q->referenceAngle; d.stiffness = q->stiffness; d.damping = q->damping;
+    j.reset(new b2WeldJoint());
+  } else if (def->type == e_wheelJoint) {
+    const b2WheelJointDef* q = (const b2WheelJointDef*)def;
+    d.type = B2G_JOINT_WHEEL;
+    la = q->localAnchorA; lb = q->localAnchorB;
+    d.local_axis_a[0] = q->localAxisA.x; d.local_axis_a[1] = q->localAxisA.y;
+    d.enable_limit = q->enableLimit; d.lower = q->lowerTranslation; d.upper = q->upperTranslation;
+    d.enable_motor = q->enableMotor; d.max_motor = q->maxMotorTorque; d.motor_speed = q->motorSpeed;
+    d.stiffness = q->stiffness; d.damping = q->damping;
+    j.reset(new b2WheelJoint());
+  } else if (def->type == e_motorJoint) {
+    const b2MotorJointDef* q = (const b2MotorJointDef*)def;
+    d.type = B2G_JOINT_MOTOR;
+    d.linear_offset[0] = q->linearOffset.x; d.linear_offset[1] = q->linearOffset.y;
+    d.reference_angle = q->angularOffset;
+    d.max_force = q->maxForce; d.max_torque = q->maxTorque; d.correction_factor = q->correctionFactor;
+    j.reset(new b2MotorJoint());
+  } else if (def->type == e_frictionJoint) {
+    const b2FrictionJointDef* q = (const b2FrictionJointDef*)def;
+    d.type = B2G_JOINT_FRICTION;
+    la = q->localAnchorA; lb = q->localAnchorB;
+    d.max_force = q->maxForce; d.max_torque = q->maxTorque;
+    j.reset(new b2FrictionJoint());
+  } else if (def->type == e_mouseJoint) {
+    const b2MouseJointDef* q = (const b2MouseJointDef*)def;
+    d.type = B2G_JOINT_MOUSE;
+    d.target[0] = q->target.x; d.target[1] = q->target.y;
+    d.max_force = q->maxForce; d.stiffness = q->stiffness; d.damping = q->damping;
+    j.reset(new b2MouseJoint());
+  } else if (def->type == e_pulleyJoint) {
+    const b2PulleyJointDef* q = (const b2PulleyJointDef*)def;
+    d.type = B2G_JOINT_PULLEY;
+    la = q->localAnchorA; lb = q->localAnchorB;
+    d.ground_anchor_a[0] = q->groundAnchorA.x; d.ground_anchor_a[1] = q->groundAnchorA.y;
+    d.ground_anchor_b[0] = q->groundAnchorB.x; d.ground_anchor_b[1] = q->groundAnchorB.y;
+    d.length_a = q->lengthA; d.length_b = q->lengthB; d.ratio = q->ratio;
+    j.reset(new b2PulleyJoint());
   } else {
     return nullptr;
   }
@@ -525,6 +615,10 @@ b2Joint* b2World::CreateJoint(const b2JointDef* def) {
   d.local_anchor_b[0] = lb.x; d.local_anchor_b[1] = lb.y;
   int32_t id = -1;
   if (b2g_joints_add(m_batch, m_index, &d, 1, &id) != B2G_OK) return nullptr;
+  if (def->type == e_mouseJoint) {  // the engine computed the anchor on body B from the target
+    b2g_joint rec;
+    if (b2g_joints_read(m_batch, m_index, id, 1, &rec) == B2G_OK) lb.Set(rec.def.local_anchor_b[0], rec.def.local_anchor_b[1]);
+  }
   j->m_world = this;
   j->m_index = id;
   j->m_type = def->type;
@@ -673,6 +767,7 @@ extern "C" B2G_API int b2g_scene_build(b2g_batch* b, int32_t world, int32_t kind
   else if (kind == B2G_SCENE_MIXED_DROP) c = b2scenes::MixedDrop(&w, n, seed);
   else if (kind == B2G_SCENE_CHAINS) c = b2scenes::ChainsOverPile(&w, n, 20, (int)p0, seed);
   else if (kind == B2G_SCENE_BATCH_WORLD) c = b2scenes::BatchWorld(&w, seed, n);
+  else if (kind == B2G_SCENE_JOINTS) c = b2scenes::JointZoo(&w, n, seed);
   else return B2G_E_INVALID_ARG;
   if (counts) { counts[0] = c.bodies; counts[1] = c.fixtures; counts[2] = c.joints; }
   return B2G_OK;

@@ -320,6 +320,102 @@ B2G_HD float solveContactPosition(const VCDev& vc, float4* pos) {
 B2G_HD M22 ldK(const float* k) { M22 m; m.ex = mk(k[0], k[1]); m.ey = mk(k[2], k[3]); return m; }
 B2G_HD void stK(float* k, const M22& m) { k[0] = m.ex.x; k[1] = m.ex.y; k[2] = m.ey.x; k[3] = m.ey.y; }
 
+// b2Mat33 (weld): K from the anchors, and GetInverse22 / GetSymInverse33 (src/common/b2_math.cpp:
+// 55-97) into 9 floats (ex, ey, ez).
+B2G_HD void weldK(V2 rA, V2 rB, float mA, float mB, float iA, float iB, V3& ex, V3& ey, V3& ez) {
+  ex.x = mA + mB + rA.y * rA.y * iA + rB.y * rB.y * iB;
+  ey.x = -rA.y * rA.x * iA - rB.y * rB.x * iB;
+  ez.x = -rA.y * iA - rB.y * iB;
+  ex.y = ey.x;
+  ey.y = mA + mB + rA.x * rA.x * iA + rB.x * rB.x * iB;
+  ez.y = rA.x * iA + rB.x * iB;
+  ex.z = ez.x;
+  ey.z = ez.y;
+  ez.z = iA + iB;
+}
+B2G_HD void inverse22(V3 ex, V3 ey, float* M) {
+  float a = ex.x, b = ey.x, c = ex.y, d = ey.y;
+  float det = a * d - b * c;
+  if (det != 0.0f) det = 1.0f / det;
+  M[0] = det * d;  M[3] = -det * b; M[2] = 0.0f;
+  M[1] = -det * c; M[4] = det * a;  M[5] = 0.0f;
+  M[6] = 0.0f; M[7] = 0.0f; M[8] = 0.0f;
+}
+B2G_HD void symInverse33(V3 ex, V3 ey, V3 ez, float* M) {
+  float det = dot3(ex, cross3(ey, ez));
+  if (det != 0.0f) det = 1.0f / det;
+  float a11 = ex.x, a12 = ey.x, a13 = ez.x;
+  float a22 = ey.y, a23 = ez.y;
+  float a33 = ez.z;
+  M[0] = det * (a22 * a33 - a23 * a23);
+  M[1] = det * (a13 * a23 - a12 * a33);
+  M[2] = det * (a12 * a23 - a13 * a22);
+  M[3] = M[1];
+  M[4] = det * (a11 * a33 - a13 * a13);
+  M[5] = det * (a13 * a12 - a11 * a23);
+  M[6] = M[2];
+  M[7] = M[5];
+  M[8] = det * (a11 * a22 - a12 * a12);
+}
+// b2Mat33::Solve22 (b2_math.cpp:42-53)
+B2G_HD V2 solve22(V3 ex, V3 ey, V2 b) {
+  float a11 = ex.x, a12 = ey.x, a21 = ex.y, a22 = ey.y;
+  float det = a11 * a22 - a12 * a21;
+  if (det != 0.0f) det = 1.0f / det;
+  return mk(det * (a22 * b.x - a12 * b.y), det * (a11 * b.y - a21 * b.x));
+}
+// Linear/angular mass of the motor and friction joints (b2_motor_joint.cpp:91-104,
+// b2_friction_joint.cpp:88-101): K in the reference's operand order, inverted.
+B2G_HD void linearAngularMass(JointDev& J, V2 rA, V2 rB, float mA, float mB, float iA, float iB) {
+  M22 K;
+  K.ex.x = mA + mB + iA * rA.y * rA.y + iB * rB.y * rB.y;
+  K.ex.y = -iA * rA.x * rA.y - iB * rB.x * rB.y;
+  K.ey.x = K.ex.y;
+  K.ey.y = mA + mB + iA * rA.x * rA.x + iB * rB.x * rB.x;
+  stK(J.K, inverse(K));
+  J.axialMass = iA + iB;
+  if (J.axialMass > 0.0f) J.axialMass = 1.0f / J.axialMass;
+}
+// The clamped linear and angular impulses of the motor and friction joints
+// (b2_motor_joint.cpp:157-193, b2_friction_joint.cpp:144-180); the motor adds its position-error
+// feedback to both velocity errors (friction adds nothing: not even a zero, which could turn the
+// sign of a zero velocity error).
+B2G_HD void solveLinearAngular(JointDev& J, V2& vA, float& wA, V2& vB, float& wB, float h, bool feedback,
+                               float angBias, V2 linBias) {
+  float mA = J.mA, mB = J.mB, iA = J.invIA, iB = J.invIB;
+  V2 rA = ld2(J.rA), rB = ld2(J.rB);
+  {
+    float Cdot = wB - wA;
+    if (feedback) Cdot = Cdot + angBias;
+    float impulse = -J.axialMass * Cdot;
+    float oldImpulse = J.impulse[2];
+    float maxImpulse = h * J.d.max_torque;
+    J.impulse[2] = fclamp(J.impulse[2] + impulse, -maxImpulse, maxImpulse);
+    impulse = J.impulse[2] - oldImpulse;
+    wA -= iA * impulse;
+    wB += iB * impulse;
+  }
+  {
+    V2 Cdot = ((vB + cross(wB, rB)) - vA) - cross(wA, rA);
+    if (feedback) Cdot = Cdot + linBias;
+    V2 impulse = -mul(ldK(J.K), Cdot);
+    V2 oldImpulse = mk(J.impulse[0], J.impulse[1]);
+    V2 acc = oldImpulse + impulse;
+    float maxImpulse = h * J.d.max_force;
+    if (lengthSq(acc) > maxImpulse * maxImpulse) {
+      normalize(acc);
+      acc.x *= maxImpulse;
+      acc.y *= maxImpulse;
+    }
+    J.impulse[0] = acc.x; J.impulse[1] = acc.y;
+    impulse = acc - oldImpulse;
+    subFrom(vA, mA * impulse);
+    wA -= iA * cross(rA, impulse);
+    addTo(vB, mB * impulse);
+    wB += iB * cross(rB, impulse);
+  }
+}
+
 // InitVelocityConstraints (revolute :73-165, prismatic :114-224, distance :76-173).
 B2G_HD void jointInit(JointDev& J, const float4* massd, const float2* lc, const float4* pos, float4* vel, float dt,
                       float dtRatio, bool warm) {
@@ -407,7 +503,7 @@ B2G_HD void jointInit(JointDev& J, const float4* massd, const float2* lc, const 
       J.impulse[0] = 0.0f; J.impulse[1] = 0.0f;
       J.motorImpulse = 0.0f; J.lowerImpulse = 0.0f; J.upperImpulse = 0.0f;
     }
-  } else {
+  } else if (J.d.type == B2G_JOINT_DISTANCE) {
     V2 rA = mul(qA, la - lcA);
     V2 rB = mul(qB, lb - lcB);
     st2(J.rA, rA); st2(J.rB, rB);
@@ -444,6 +540,187 @@ B2G_HD void jointInit(JointDev& J, const float4* massd, const float2* lc, const 
       wA -= J.invIA * cross(rA, P);
       addTo(vB, J.mB * P);
       wB += J.invIB * cross(rB, P);
+    } else {
+      J.impulse[0] = 0.0f;
+    }
+  } else if (J.d.type == B2G_JOINT_WELD) {  // b2_weld_joint.cpp:93-187
+    V2 rA = mul(qA, la - lcA);
+    V2 rB = mul(qB, lb - lcB);
+    st2(J.rA, rA); st2(J.rB, rB);
+    V3 ex, ey, ez;
+    weldK(rA, rB, mA, mB, iA, iB, ex, ey, ez);
+    if (J.d.stiffness > 0.0f) {
+      inverse22(ex, ey, J.mass3);
+      float invM = iA + iB;
+      float C = aB - aA - J.d.reference_angle;
+      float d = J.d.damping;
+      float k = J.d.stiffness;
+      float h = dt;
+      J.gamma = h * (d + h * k);
+      J.gamma = J.gamma != 0.0f ? 1.0f / J.gamma : 0.0f;
+      J.bias = C * h * k * J.gamma;
+      invM += J.gamma;
+      J.mass3[8] = invM != 0.0f ? 1.0f / invM : 0.0f;
+    } else if (ez.z == 0.0f) {
+      inverse22(ex, ey, J.mass3);
+      J.gamma = 0.0f;
+      J.bias = 0.0f;
+    } else {
+      symInverse33(ex, ey, ez, J.mass3);
+      J.gamma = 0.0f;
+      J.bias = 0.0f;
+    }
+    if (warm) {
+      J.impulse[0] *= dtRatio; J.impulse[1] *= dtRatio; J.impulse[2] *= dtRatio;
+      V2 P = mk(J.impulse[0], J.impulse[1]);
+      subFrom(vA, mA * P);
+      wA -= iA * (cross(rA, P) + J.impulse[2]);
+      addTo(vB, mB * P);
+      wB += iB * (cross(rB, P) + J.impulse[2]);
+    } else {
+      J.impulse[0] = 0.0f; J.impulse[1] = 0.0f; J.impulse[2] = 0.0f;
+    }
+  } else if (J.d.type == B2G_JOINT_WHEEL) {  // b2_wheel_joint.cpp:89-211
+    V2 rA = mul(qA, la - lcA);
+    V2 rB = mul(qB, lb - lcB);
+    V2 d = ((cB + rB) - cA) - rA;
+    V2 ay = mul(qA, ld2(J.localYAxisA));
+    J.s1 = cross(d + rA, ay);
+    J.s2 = cross(rB, ay);
+    st2(J.perp, ay);
+    J.mass = mA + mB + iA * J.s1 * J.s1 + iB * J.s2 * J.s2;
+    if (J.mass > 0.0f) J.mass = 1.0f / J.mass;
+    V2 ax = mul(qA, ld2(J.localXAxisA));
+    st2(J.axis, ax);
+    J.a1 = cross(d + rA, ax);
+    J.a2 = cross(rB, ax);
+    const float invMass = mA + mB + iA * J.a1 * J.a1 + iB * J.a2 * J.a2;
+    J.axialMass = invMass > 0.0f ? 1.0f / invMass : 0.0f;
+    J.springMass = 0.0f;
+    J.bias = 0.0f;
+    J.gamma = 0.0f;
+    if (J.d.stiffness > 0.0f && invMass > 0.0f) {
+      J.springMass = 1.0f / invMass;
+      float C = dot(d, ax);
+      float h = dt;
+      J.gamma = h * (J.d.damping + h * J.d.stiffness);
+      if (J.gamma > 0.0f) J.gamma = 1.0f / J.gamma;
+      J.bias = C * h * J.d.stiffness * J.gamma;
+      J.springMass = invMass + J.gamma;
+      if (J.springMass > 0.0f) J.springMass = 1.0f / J.springMass;
+    } else {
+      J.impulse[1] = 0.0f;
+    }
+    if (J.d.enable_limit) J.translation = dot(ax, d);
+    else { J.lowerImpulse = 0.0f; J.upperImpulse = 0.0f; }
+    if (J.d.enable_motor) {
+      J.motorMass = iA + iB;
+      if (J.motorMass > 0.0f) J.motorMass = 1.0f / J.motorMass;
+    } else {
+      J.motorMass = 0.0f;
+      J.motorImpulse = 0.0f;
+    }
+    if (warm) {
+      J.impulse[0] *= dtRatio; J.impulse[1] *= dtRatio; J.motorImpulse *= dtRatio;
+      float axialImpulse = J.impulse[1] + J.lowerImpulse - J.upperImpulse;
+      V2 P = J.impulse[0] * ay + axialImpulse * ax;
+      float LA = J.impulse[0] * J.s1 + axialImpulse * J.a1 + J.motorImpulse;
+      float LB = J.impulse[0] * J.s2 + axialImpulse * J.a2 + J.motorImpulse;
+      subFrom(vA, mA * P);
+      wA -= iA * LA;
+      addTo(vB, mB * P);
+      wB += iB * LB;
+    } else {
+      J.impulse[0] = 0.0f; J.impulse[1] = 0.0f; J.motorImpulse = 0.0f;
+      J.lowerImpulse = 0.0f; J.upperImpulse = 0.0f;
+    }
+  } else if (J.d.type == B2G_JOINT_MOTOR) {  // b2_motor_joint.cpp:58-136
+    V2 rA = mul(qA, ld2(J.d.linear_offset) - lcA);
+    V2 rB = mul(qB, -lcB);
+    st2(J.rA, rA); st2(J.rB, rB);
+    linearAngularMass(J, rA, rB, mA, mB, iA, iB);
+    st2(J.err, ((cB + rB) - cA) - rA);
+    J.angularError = aB - aA - J.d.reference_angle;
+    if (warm) {
+      J.impulse[0] *= dtRatio; J.impulse[1] *= dtRatio; J.impulse[2] *= dtRatio;
+      V2 P = mk(J.impulse[0], J.impulse[1]);
+      subFrom(vA, mA * P);
+      wA -= iA * (cross(rA, P) + J.impulse[2]);
+      addTo(vB, mB * P);
+      wB += iB * (cross(rB, P) + J.impulse[2]);
+    } else {
+      J.impulse[0] = 0.0f; J.impulse[1] = 0.0f; J.impulse[2] = 0.0f;
+    }
+  } else if (J.d.type == B2G_JOINT_FRICTION) {  // b2_friction_joint.cpp:60-123
+    V2 rA = mul(qA, la - lcA);
+    V2 rB = mul(qB, lb - lcB);
+    st2(J.rA, rA); st2(J.rB, rB);
+    linearAngularMass(J, rA, rB, mA, mB, iA, iB);
+    if (warm) {
+      J.impulse[0] *= dtRatio; J.impulse[1] *= dtRatio; J.impulse[2] *= dtRatio;
+      V2 P = mk(J.impulse[0], J.impulse[1]);
+      subFrom(vA, mA * P);
+      wA -= iA * (cross(rA, P) + J.impulse[2]);
+      addTo(vB, mB * P);
+      wB += iB * (cross(rB, P) + J.impulse[2]);
+    } else {
+      J.impulse[0] = 0.0f; J.impulse[1] = 0.0f; J.impulse[2] = 0.0f;
+    }
+  } else if (J.d.type == B2G_JOINT_MOUSE) {  // b2_mouse_joint.cpp:75-132 (body B only)
+    float d = J.d.damping;
+    float k = J.d.stiffness;
+    float h = dt;
+    J.gamma = h * (d + h * k);
+    if (J.gamma != 0.0f) J.gamma = 1.0f / J.gamma;
+    J.bias = h * k * J.gamma;  // beta
+    V2 rB = mul(qB, lb - lcB);
+    st2(J.rB, rB);
+    M22 K;
+    K.ex.x = mB + iB * rB.y * rB.y + J.gamma;
+    K.ex.y = -iB * rB.x * rB.y;
+    K.ey.x = K.ex.y;
+    K.ey.y = mB + iB * rB.x * rB.x + J.gamma;
+    stK(J.K, inverse(K));
+    V2 C = (cB + rB) - ld2(J.d.target);
+    C.x *= J.bias;
+    C.y *= J.bias;
+    st2(J.err, C);
+    wB *= 0.98f;
+    if (warm) {
+      J.impulse[0] *= dtRatio; J.impulse[1] *= dtRatio;
+      V2 P = mk(J.impulse[0], J.impulse[1]);
+      addTo(vB, mB * P);
+      wB += iB * cross(rB, P);
+    } else {
+      J.impulse[0] = 0.0f; J.impulse[1] = 0.0f;
+    }
+  } else {  // pulley, b2_pulley_joint.cpp:78-157
+    V2 rA = mul(qA, la - lcA);
+    V2 rB = mul(qB, lb - lcB);
+    st2(J.rA, rA); st2(J.rB, rB);
+    V2 uA = (cA + rA) - ld2(J.d.ground_anchor_a);
+    V2 uB = (cB + rB) - ld2(J.d.ground_anchor_b);
+    float lengthA = lengthOf(uA);
+    float lengthB = lengthOf(uB);
+    if (lengthA > 10.0f * B2G_LINEAR_SLOP) { float s = 1.0f / lengthA; uA.x *= s; uA.y *= s; }
+    else uA = mk(0.0f, 0.0f);
+    if (lengthB > 10.0f * B2G_LINEAR_SLOP) { float s = 1.0f / lengthB; uB.x *= s; uB.y *= s; }
+    else uB = mk(0.0f, 0.0f);
+    st2(J.u, uA); st2(J.uB, uB);
+    float ruA = cross(rA, uA);
+    float ruB = cross(rB, uB);
+    float pmA = mA + iA * ruA * ruA;
+    float pmB = mB + iB * ruB * ruB;
+    J.mass = pmA + J.d.ratio * J.d.ratio * pmB;
+    if (J.mass > 0.0f) J.mass = 1.0f / J.mass;
+    if (warm) {
+      J.impulse[0] *= dtRatio;
+      V2 PA = -(J.impulse[0]) * uA;
+      V2 PB = (-J.d.ratio * J.impulse[0]) * uB;
+      addTo(vA, mA * PA);
+      wA += iA * cross(rA, PA);
+      addTo(vB, mB * PB);
+      wB += iB * cross(rB, PB);
     } else {
       J.impulse[0] = 0.0f;
     }
@@ -559,7 +836,7 @@ B2G_HD void jointSolveVelocity(JointDev& J, float4* vel, float dt, float inv_dt)
       subFrom(vA, mA * P); wA -= iA * LA;
       addTo(vB, mB * P); wB += iB * LB;
     }
-  } else {
+  } else if (J.d.type == B2G_JOINT_DISTANCE) {
     V2 rA = ld2(J.rA), rB = ld2(J.rB), u = ld2(J.u);
     if (J.d.min_length < J.d.max_length) {
       if (J.d.stiffness > 0.0f) {
@@ -610,6 +887,132 @@ B2G_HD void jointSolveVelocity(JointDev& J, float4* vel, float dt, float inv_dt)
       subFrom(vA, J.mA * P); wA -= J.invIA * cross(rA, P);
       addTo(vB, J.mB * P); wB += J.invIB * cross(rB, P);
     }
+  } else if (J.d.type == B2G_JOINT_WELD) {  // b2_weld_joint.cpp:189-250
+    V2 rA = ld2(J.rA), rB = ld2(J.rB);
+    const float* M = J.mass3;
+    if (J.d.stiffness > 0.0f) {
+      float Cdot2 = wB - wA;
+      float impulse2 = -M[8] * (Cdot2 + J.bias + J.gamma * J.impulse[2]);
+      J.impulse[2] += impulse2;
+      wA -= iA * impulse2;
+      wB += iB * impulse2;
+      V2 Cdot1 = ((vB + cross(wB, rB)) - vA) - cross(wA, rA);
+      V2 impulse1 = -mk(M[0] * Cdot1.x + M[3] * Cdot1.y, M[1] * Cdot1.x + M[4] * Cdot1.y);
+      J.impulse[0] += impulse1.x;
+      J.impulse[1] += impulse1.y;
+      V2 P = impulse1;
+      subFrom(vA, mA * P);
+      wA -= iA * cross(rA, P);
+      addTo(vB, mB * P);
+      wB += iB * cross(rB, P);
+    } else {
+      V2 Cdot1 = ((vB + cross(wB, rB)) - vA) - cross(wA, rA);
+      float Cdot2 = wB - wA;
+      V3 impulse;
+      impulse.x = -((Cdot1.x * M[0] + Cdot1.y * M[3]) + Cdot2 * M[6]);
+      impulse.y = -((Cdot1.x * M[1] + Cdot1.y * M[4]) + Cdot2 * M[7]);
+      impulse.z = -((Cdot1.x * M[2] + Cdot1.y * M[5]) + Cdot2 * M[8]);
+      J.impulse[0] += impulse.x; J.impulse[1] += impulse.y; J.impulse[2] += impulse.z;
+      V2 P = mk(impulse.x, impulse.y);
+      subFrom(vA, mA * P);
+      wA -= iA * (cross(rA, P) + impulse.z);
+      addTo(vB, mB * P);
+      wB += iB * (cross(rB, P) + impulse.z);
+    }
+  } else if (J.d.type == B2G_JOINT_WHEEL) {  // b2_wheel_joint.cpp:213-323
+    V2 ax = ld2(J.axis), ay = ld2(J.perp);
+    {
+      float Cdot = dot(ax, vB - vA) + J.a2 * wB - J.a1 * wA;
+      float impulse = -J.springMass * (Cdot + J.bias + J.gamma * J.impulse[1]);
+      J.impulse[1] += impulse;
+      V2 P = impulse * ax;
+      float LA = impulse * J.a1;
+      float LB = impulse * J.a2;
+      subFrom(vA, mA * P); wA -= iA * LA;
+      addTo(vB, mB * P); wB += iB * LB;
+    }
+    {
+      float Cdot = wB - wA - J.d.motor_speed;
+      float impulse = -J.motorMass * Cdot;
+      float oldImpulse = J.motorImpulse;
+      float maxImpulse = dt * J.d.max_motor;
+      J.motorImpulse = fclamp(J.motorImpulse + impulse, -maxImpulse, maxImpulse);
+      impulse = J.motorImpulse - oldImpulse;
+      wA -= iA * impulse;
+      wB += iB * impulse;
+    }
+    if (J.d.enable_limit) {
+      {
+        float C = J.translation - J.d.lower;
+        float Cdot = dot(ax, vB - vA) + J.a2 * wB - J.a1 * wA;
+        float impulse = -J.axialMass * (Cdot + fmax2(C, 0.0f) * inv_dt);
+        float oldImpulse = J.lowerImpulse;
+        J.lowerImpulse = fmax2(J.lowerImpulse + impulse, 0.0f);
+        impulse = J.lowerImpulse - oldImpulse;
+        V2 P = impulse * ax;
+        float LA = impulse * J.a1;
+        float LB = impulse * J.a2;
+        subFrom(vA, mA * P); wA -= iA * LA;
+        addTo(vB, mB * P); wB += iB * LB;
+      }
+      {
+        float C = J.d.upper - J.translation;
+        float Cdot = dot(ax, vA - vB) + J.a1 * wA - J.a2 * wB;
+        float impulse = -J.axialMass * (Cdot + fmax2(C, 0.0f) * inv_dt);
+        float oldImpulse = J.upperImpulse;
+        J.upperImpulse = fmax2(J.upperImpulse + impulse, 0.0f);
+        impulse = J.upperImpulse - oldImpulse;
+        V2 P = impulse * ax;
+        float LA = impulse * J.a1;
+        float LB = impulse * J.a2;
+        addTo(vA, mA * P); wA += iA * LA;
+        subFrom(vB, mB * P); wB -= iB * LB;
+      }
+    }
+    {
+      float Cdot = dot(ay, vB - vA) + J.s2 * wB - J.s1 * wA;
+      float impulse = -J.mass * Cdot;
+      J.impulse[0] += impulse;
+      V2 P = impulse * ay;
+      float LA = impulse * J.s1;
+      float LB = impulse * J.s2;
+      subFrom(vA, mA * P); wA -= iA * LA;
+      addTo(vB, mB * P); wB += iB * LB;
+    }
+  } else if (J.d.type == B2G_JOINT_MOTOR) {  // b2_motor_joint.cpp:138-196
+    float fb = inv_dt * J.d.correction_factor;
+    solveLinearAngular(J, vA, wA, vB, wB, dt, true, fb * J.angularError, fb * ld2(J.err));
+  } else if (J.d.type == B2G_JOINT_FRICTION) {  // b2_friction_joint.cpp:125-183
+    solveLinearAngular(J, vA, wA, vB, wB, dt, false, 0.0f, mk(0.0f, 0.0f));
+  } else if (J.d.type == B2G_JOINT_MOUSE) {  // b2_mouse_joint.cpp:134-160
+    V2 rB = ld2(J.rB);
+    V2 Cdot = vB + cross(wB, rB);
+    V2 old = mk(J.impulse[0], J.impulse[1]);
+    V2 impulse = mul(ldK(J.K), -((Cdot + ld2(J.err)) + J.gamma * old));
+    V2 acc = old + impulse;
+    float maxImpulse = dt * J.d.max_force;
+    if (lengthSq(acc) > maxImpulse * maxImpulse) {
+      float s = maxImpulse / lengthOf(acc);
+      acc.x *= s;
+      acc.y *= s;
+    }
+    J.impulse[0] = acc.x; J.impulse[1] = acc.y;
+    impulse = acc - old;
+    addTo(vB, mB * impulse);
+    wB += iB * cross(rB, impulse);
+  } else {  // pulley, b2_pulley_joint.cpp:159-182
+    V2 rA = ld2(J.rA), rB = ld2(J.rB), uA = ld2(J.u), uB = ld2(J.uB);
+    V2 vpA = vA + cross(wA, rA);
+    V2 vpB = vB + cross(wB, rB);
+    float Cdot = -dot(uA, vpA) - J.d.ratio * dot(uB, vpB);
+    float impulse = -J.mass * Cdot;
+    J.impulse[0] += impulse;
+    V2 PA = -impulse * uA;
+    V2 PB = -J.d.ratio * impulse * uB;
+    addTo(vA, mA * PA);
+    wA += iA * cross(rA, PA);
+    addTo(vB, mB * PB);
+    wB += iB * cross(rB, PB);
   }
   if (moves(J.mA, J.invIA)) storeVel(vel, J.iA, vA, wA);
   if (moves(J.mB, J.invIB)) storeVel(vel, J.iB, vB, wB);
@@ -725,7 +1128,7 @@ B2G_HD bool jointSolvePosition(JointDev& J, float4* pos) {
     subFrom(cA, mA * P); aA -= iA * LA;
     addTo(cB, mB * P); aB += iB * LB;
     ok = linearError <= B2G_LINEAR_SLOP && angularError <= B2G_ANGULAR_SLOP;
-  } else {
+  } else if (J.d.type == B2G_JOINT_DISTANCE) {
     V2 rA = mul(qA, la - lcA);
     V2 rB = mul(qB, lb - lcB);
     V2 u = ((cB + rB) - cA) - rA;
@@ -740,6 +1143,118 @@ B2G_HD bool jointSolvePosition(JointDev& J, float4* pos) {
     subFrom(cA, J.mA * P); aA -= J.invIA * cross(rA, P);
     addTo(cB, J.mB * P); aB += J.invIB * cross(rB, P);
     ok = fabs2(C) < B2G_LINEAR_SLOP;
+  } else if (J.d.type == B2G_JOINT_WELD) {  // b2_weld_joint.cpp:252-329
+    float mA = J.mA, mB = J.mB, iA = J.invIA, iB = J.invIB;
+    V2 rA = mul(qA, la - lcA);
+    V2 rB = mul(qB, lb - lcB);
+    float positionError, angularError;
+    V3 ex, ey, ez;
+    weldK(rA, rB, mA, mB, iA, iB, ex, ey, ez);
+    if (J.d.stiffness > 0.0f) {
+      V2 C1 = ((cB + rB) - cA) - rA;
+      positionError = lengthOf(C1);
+      angularError = 0.0f;
+      V2 P = -solve22(ex, ey, C1);
+      subFrom(cA, mA * P);
+      aA -= iA * cross(rA, P);
+      addTo(cB, mB * P);
+      aB += iB * cross(rB, P);
+    } else {
+      V2 C1 = ((cB + rB) - cA) - rA;
+      float C2 = aB - aA - J.d.reference_angle;
+      positionError = lengthOf(C1);
+      angularError = fabs2(C2);
+      V3 C = {C1.x, C1.y, C2};
+      V3 impulse;
+      if (ez.z > 0.0f) {
+        V3 x = solve33(ex, ey, ez, C);
+        impulse.x = -x.x; impulse.y = -x.y; impulse.z = -x.z;
+      } else {
+        V2 impulse2 = -solve22(ex, ey, C1);
+        impulse.x = impulse2.x; impulse.y = impulse2.y; impulse.z = 0.0f;
+      }
+      V2 P = mk(impulse.x, impulse.y);
+      subFrom(cA, mA * P);
+      aA -= iA * (cross(rA, P) + impulse.z);
+      addTo(cB, mB * P);
+      aB += iB * (cross(rB, P) + impulse.z);
+    }
+    ok = positionError <= B2G_LINEAR_SLOP && angularError <= B2G_ANGULAR_SLOP;
+  } else if (J.d.type == B2G_JOINT_WHEEL) {  // b2_wheel_joint.cpp:325-420
+    // the reference mixes this step's axis and point arms from InitVelocityConstraints (m_ax,
+    // m_sAy, m_sBy) into its position pass; kept as it is
+    float linearError = 0.0f;
+    if (J.d.enable_limit) {
+      V2 rA = mul(qA, la - lcA);
+      V2 rB = mul(qB, lb - lcB);
+      V2 d = ((cB - cA) + rB) - rA;
+      V2 ax = mul(qA, ld2(J.localXAxisA));
+      float sAx = cross(d + rA, ld2(J.axis));
+      float sBx = cross(rB, ld2(J.axis));
+      float C = 0.0f;
+      float translation = dot(ax, d);
+      if (fabs2(J.d.upper - J.d.lower) < 2.0f * B2G_LINEAR_SLOP) C = translation;
+      else if (translation <= J.d.lower) C = fmin2(translation - J.d.lower, 0.0f);
+      else if (translation >= J.d.upper) C = fmax2(translation - J.d.upper, 0.0f);
+      if (C != 0.0f) {
+        float invMass = J.mA + J.mB + J.invIA * sAx * sAx + J.invIB * sBx * sBx;
+        float impulse = 0.0f;
+        if (invMass != 0.0f) impulse = -C / invMass;
+        V2 P = impulse * ax;
+        float LA = impulse * sAx;
+        float LB = impulse * sBx;
+        subFrom(cA, J.mA * P); aA -= J.invIA * LA;
+        addTo(cB, J.mB * P); aB += J.invIB * LB;
+        linearError = fabs2(C);
+      }
+    }
+    {
+      Rot qA2 = rotOf(aA), qB2 = rotOf(aB);
+      V2 rA = mul(qA2, la - lcA);
+      V2 rB = mul(qB2, lb - lcB);
+      V2 d = ((cB - cA) + rB) - rA;
+      V2 ay = mul(qA2, ld2(J.localYAxisA));
+      float sAy = cross(d + rA, ay);
+      float sBy = cross(rB, ay);
+      float C = dot(d, ay);
+      float invMass = J.mA + J.mB + J.invIA * J.s1 * J.s1 + J.invIB * J.s2 * J.s2;
+      float impulse = 0.0f;
+      if (invMass != 0.0f) impulse = -C / invMass;
+      V2 P = impulse * ay;
+      float LA = impulse * sAy;
+      float LB = impulse * sBy;
+      subFrom(cA, J.mA * P); aA -= J.invIA * LA;
+      addTo(cB, J.mB * P); aB += J.invIB * LB;
+      linearError = fmax2(linearError, fabs2(C));
+    }
+    ok = linearError <= B2G_LINEAR_SLOP;
+  } else if (J.d.type == B2G_JOINT_PULLEY) {  // b2_pulley_joint.cpp:184-256
+    V2 rA = mul(qA, la - lcA);
+    V2 rB = mul(qB, lb - lcB);
+    V2 uA = (cA + rA) - ld2(J.d.ground_anchor_a);
+    V2 uB = (cB + rB) - ld2(J.d.ground_anchor_b);
+    float lengthA = lengthOf(uA);
+    float lengthB = lengthOf(uB);
+    if (lengthA > 10.0f * B2G_LINEAR_SLOP) { float s = 1.0f / lengthA; uA.x *= s; uA.y *= s; }
+    else uA = mk(0.0f, 0.0f);
+    if (lengthB > 10.0f * B2G_LINEAR_SLOP) { float s = 1.0f / lengthB; uB.x *= s; uB.y *= s; }
+    else uB = mk(0.0f, 0.0f);
+    float ruA = cross(rA, uA);
+    float ruB = cross(rB, uB);
+    float pmA = J.mA + J.invIA * ruA * ruA;
+    float pmB = J.mB + J.invIB * ruB * ruB;
+    float mass = pmA + J.d.ratio * J.d.ratio * pmB;
+    if (mass > 0.0f) mass = 1.0f / mass;
+    float C = J.constant - lengthA - J.d.ratio * lengthB;
+    float linearError = fabs2(C);
+    float impulse = -mass * C;
+    V2 PA = -impulse * uA;
+    V2 PB = -J.d.ratio * impulse * uB;
+    addTo(cA, J.mA * PA); aA += J.invIA * cross(rA, PA);
+    addTo(cB, J.mB * PB); aB += J.invIB * cross(rB, PB);
+    ok = linearError < B2G_LINEAR_SLOP;
+  } else {  // motor, friction, mouse: no position constraint
+    return true;
   }
   if (moves(J.mA, J.invIA)) storePos(pos, J.iA, cA, aA);
   if (moves(J.mB, J.invIB)) storePos(pos, J.iB, cB, aB);

@@ -528,6 +528,73 @@ struct b2DistanceJointDef : public b2JointDef {
   float length, minLength, maxLength, stiffness, damping;
 };
 
+// b2WeldJointDef (include/box2d/b2_weld_joint.h:31-65)
+struct b2WeldJointDef : public b2JointDef {
+  b2WeldJointDef() {
+    type = e_weldJoint; localAnchorA.Set(0.0f, 0.0f); localAnchorB.Set(0.0f, 0.0f); referenceAngle = 0.0f;
+    stiffness = 0.0f; damping = 0.0f;
+  }
+  void Initialize(b2Body* bodyA, b2Body* bodyB, const b2Vec2& anchor);
+  b2Vec2 localAnchorA, localAnchorB;
+  float referenceAngle, stiffness, damping;
+};
+
+// b2WheelJointDef (include/box2d/b2_wheel_joint.h:34-89)
+struct b2WheelJointDef : public b2JointDef {
+  b2WheelJointDef() {
+    type = e_wheelJoint; localAnchorA.SetZero(); localAnchorB.SetZero(); localAxisA.Set(1.0f, 0.0f);
+    enableLimit = false; lowerTranslation = 0.0f; upperTranslation = 0.0f; enableMotor = false;
+    maxMotorTorque = 0.0f; motorSpeed = 0.0f; stiffness = 0.0f; damping = 0.0f;
+  }
+  void Initialize(b2Body* bodyA, b2Body* bodyB, const b2Vec2& anchor, const b2Vec2& axis);
+  b2Vec2 localAnchorA, localAnchorB, localAxisA;
+  bool enableLimit;
+  float lowerTranslation, upperTranslation;
+  bool enableMotor;
+  float maxMotorTorque, motorSpeed, stiffness, damping;
+};
+
+// b2MotorJointDef (include/box2d/b2_motor_joint.h:29-59)
+struct b2MotorJointDef : public b2JointDef {
+  b2MotorJointDef() {
+    type = e_motorJoint; linearOffset.SetZero(); angularOffset = 0.0f; maxForce = 1.0f; maxTorque = 1.0f;
+    correctionFactor = 0.3f;
+  }
+  void Initialize(b2Body* bodyA, b2Body* bodyB);
+  b2Vec2 linearOffset;
+  float angularOffset, maxForce, maxTorque, correctionFactor;
+};
+
+// b2FrictionJointDef (include/box2d/b2_friction_joint.h:29-56)
+struct b2FrictionJointDef : public b2JointDef {
+  b2FrictionJointDef() {
+    type = e_frictionJoint; localAnchorA.SetZero(); localAnchorB.SetZero(); maxForce = 0.0f; maxTorque = 0.0f;
+  }
+  void Initialize(b2Body* bodyA, b2Body* bodyB, const b2Vec2& anchor);
+  b2Vec2 localAnchorA, localAnchorB;
+  float maxForce, maxTorque;
+};
+
+// b2MouseJointDef (include/box2d/b2_mouse_joint.h:30-56)
+struct b2MouseJointDef : public b2JointDef {
+  b2MouseJointDef() { type = e_mouseJoint; target.Set(0.0f, 0.0f); maxForce = 0.0f; stiffness = 0.0f; damping = 0.0f; }
+  b2Vec2 target;
+  float maxForce, stiffness, damping;
+};
+
+// b2PulleyJointDef (include/box2d/b2_pulley_joint.h:32-75)
+struct b2PulleyJointDef : public b2JointDef {
+  b2PulleyJointDef() {
+    type = e_pulleyJoint; groundAnchorA.Set(-1.0f, 1.0f); groundAnchorB.Set(1.0f, 1.0f);
+    localAnchorA.Set(-1.0f, 0.0f); localAnchorB.Set(1.0f, 0.0f); lengthA = 0.0f; lengthB = 0.0f; ratio = 1.0f;
+    collideConnected = true;
+  }
+  void Initialize(b2Body* bodyA, b2Body* bodyB, const b2Vec2& groundAnchorA, const b2Vec2& groundAnchorB,
+                  const b2Vec2& anchorA, const b2Vec2& anchorB, float ratio);
+  b2Vec2 groundAnchorA, groundAnchorB, localAnchorA, localAnchorB;
+  float lengthA, lengthB, ratio;
+};
+
 class b2Joint {
  public:
   virtual ~b2Joint() {}
@@ -557,6 +624,12 @@ class b2Joint {
 class b2RevoluteJoint : public b2Joint {};
 class b2PrismaticJoint : public b2Joint {};
 class b2DistanceJoint : public b2Joint {};
+class b2WeldJoint : public b2Joint {};
+class b2WheelJoint : public b2Joint {};
+class b2MotorJoint : public b2Joint {};
+class b2FrictionJoint : public b2Joint {};
+class b2MouseJoint : public b2Joint {};
+class b2PulleyJoint : public b2Joint {};
 
 // ---------------------------------------------------------------- contacts and listeners
 class b2Contact {

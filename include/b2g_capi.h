@@ -49,10 +49,16 @@ extern "C" {
 #define B2G_SHAPE_CIRCLE 0
 #define B2G_SHAPE_EDGE 1
 #define B2G_SHAPE_POLYGON 2
-/* b2JointType, include/box2d/b2_joint.h:35-49 (the three supported kinds) */
+/* b2JointType, include/box2d/b2_joint.h:35-49 (gear and rope joints are not supported) */
 #define B2G_JOINT_REVOLUTE 1
 #define B2G_JOINT_PRISMATIC 2
 #define B2G_JOINT_DISTANCE 3
+#define B2G_JOINT_PULLEY 4
+#define B2G_JOINT_MOUSE 5
+#define B2G_JOINT_WHEEL 7
+#define B2G_JOINT_WELD 8
+#define B2G_JOINT_FRICTION 9
+#define B2G_JOINT_MOTOR 11
 /* b2Manifold::Type, include/box2d/b2_collision.h:105-110 */
 #define B2G_MANIFOLD_CIRCLES 0
 #define B2G_MANIFOLD_FACE_A 1
@@ -143,8 +149,13 @@ typedef struct b2g_fixture_def {
   b2g_shape shape;      /* B2G_POLY_RAW input */
 } b2g_fixture_def;
 
-/* b2RevoluteJointDef / b2PrismaticJointDef / b2DistanceJointDef in one record
- * (b2_revolute_joint.h:39-88, b2_prismatic_joint.h:35-88, b2_distance_joint.h:33-70). */
+/* The joint definitions in one record: b2RevoluteJointDef (b2_revolute_joint.h:39-88),
+ * b2PrismaticJointDef (b2_prismatic_joint.h:35-88), b2DistanceJointDef (b2_distance_joint.h:33-70),
+ * b2WeldJointDef (b2_weld_joint.h:31-65), b2WheelJointDef (b2_wheel_joint.h:34-89),
+ * b2MotorJointDef (b2_motor_joint.h:29-59), b2FrictionJointDef (b2_friction_joint.h:29-56),
+ * b2MouseJointDef (b2_mouse_joint.h:30-56), b2PulleyJointDef (b2_pulley_joint.h:32-75). A mouse
+ * joint's local_anchor_b is computed from its target when it is created, as the reference's
+ * constructor does. */
 typedef struct b2g_joint_def {
   int32_t type;             /* B2G_JOINT_* */
   int32_t body_a;
@@ -152,8 +163,8 @@ typedef struct b2g_joint_def {
   int32_t collide_connected;
   float local_anchor_a[2];
   float local_anchor_b[2];
-  float reference_angle;    /* revolute, prismatic */
-  float local_axis_a[2];    /* prismatic (normalised on creation) */
+  float reference_angle;    /* revolute, prismatic, weld; motor: angularOffset */
+  float local_axis_a[2];    /* prismatic (normalised on creation), wheel (as given) */
   int32_t enable_limit;
   float lower;              /* lowerAngle / lowerTranslation */
   float upper;              /* upperAngle / upperTranslation */
@@ -163,8 +174,17 @@ typedef struct b2g_joint_def {
   float length;             /* distance */
   float min_length;
   float max_length;
-  float stiffness;
+  float stiffness;          /* distance, weld, wheel, mouse */
   float damping;
+  float linear_offset[2];   /* motor */
+  float max_force;          /* motor, friction, mouse */
+  float max_torque;         /* motor, friction */
+  float correction_factor;  /* motor */
+  float target[2];          /* mouse: world target point */
+  float ground_anchor_a[2]; /* pulley */
+  float ground_anchor_b[2];
+  float length_a, length_b; /* pulley rope lengths */
+  float ratio;              /* pulley */
   uint64_t user_data;
 } b2g_joint_def;
 
@@ -202,6 +222,9 @@ typedef struct b2g_fixture {
 
 /* Joint parameters and warm-start state. impulse[0..2]: revolute m_impulse (x, y), prismatic
  * m_impulse (x, y), distance m_impulse in [0]. */
+/* impulse[]: revolute / prismatic m_impulse (x, y), distance and pulley m_impulse in [0], weld
+ * m_impulse (x, y, z), wheel (m_impulse, m_springImpulse), motor and friction (linear x, y,
+ * angular), mouse m_impulse (x, y). */
 typedef struct b2g_joint {
   b2g_joint_def def;
   float impulse[3];
@@ -451,6 +474,7 @@ B2G_API int b2g_pairs_static(const float* d_aabbs, int32_t n, uint64_t* d_pairs,
 #define B2G_SCENE_MIXED_DROP 1
 #define B2G_SCENE_CHAINS 2
 #define B2G_SCENE_BATCH_WORLD 3
+#define B2G_SCENE_JOINTS 4      /* rigs of weld, wheel, motor, friction, mouse and pulley joints */
 B2G_API int b2g_scene_build(b2g_batch* b, int32_t world, int32_t kind, uint32_t seed, int32_t n,
                             float p0, float p1, int32_t* counts);
 B2G_API int b2g_batch_world_params(uint32_t seed, int32_t* n_bodies, float* gx, float* gy);

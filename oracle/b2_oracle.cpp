@@ -964,6 +964,15 @@ struct Joint {
   V2 localXAxisA, localYAxisA, axis, perp;
   float a1, a2, s1, s2, translation;
   V2 u; float currentLength, mass, softMass, gamma, bias;
+  // weld, wheel, motor, friction, mouse, pulley (b2_weld_joint.h:117-125, b2_wheel_joint.h:178-212,
+  // b2_motor_joint.h:106-122, b2_friction_joint.h:95-107, b2_mouse_joint.h:110-127,
+  // b2_pulley_joint.h:125-148): imp[] holds their accumulated impulses in the b2g_joint.impulse
+  // layout; the wheel keeps ax/ay in axis/perp and sAx, sBx, sAy, sBy in a1, a2, s1, s2
+  float imp[3];
+  float mass3[9];
+  float springMass, motorMass;
+  V2 err; float angularError;
+  V2 uB; float constant;
 };
 
 struct Contact {
@@ -1286,6 +1295,95 @@ struct SolverBody { V2 c; float a; V2 v; float w; };
 // ---- joints (src/dynamics/b2_revolute_joint.cpp, b2_prismatic_joint.cpp, b2_distance_joint.cpp)
 struct Step { float dt, inv_dt, dtRatio; int vi, pi; bool warm; };
 
+// b2Mat33 of the weld joint, GetInverse22 / GetSymInverse33 / Solve22 (src/common/b2_math.cpp:42-97),
+// stored as ex, ey, ez.
+static void weldK(V2 rA, V2 rB, float mA, float mB, float iA, float iB, V3& ex, V3& ey, V3& ez) {
+  ex.x = mA + mB + rA.y * rA.y * iA + rB.y * rB.y * iB;
+  ey.x = -rA.y * rA.x * iA - rB.y * rB.x * iB;
+  ez.x = -rA.y * iA - rB.y * iB;
+  ex.y = ey.x;
+  ey.y = mA + mB + rA.x * rA.x * iA + rB.x * rB.x * iB;
+  ez.y = rA.x * iA + rB.x * iB;
+  ex.z = ez.x;
+  ey.z = ez.y;
+  ez.z = iA + iB;
+}
+static void inverse22(V3 ex, V3 ey, float* M) {
+  float a = ex.x, b = ey.x, c = ex.y, d = ey.y;
+  float det = a * d - b * c;
+  if (det != 0.0f) det = 1.0f / det;
+  M[0] = det * d; M[1] = -det * c; M[2] = 0.0f;
+  M[3] = -det * b; M[4] = det * a; M[5] = 0.0f;
+  M[6] = M[7] = M[8] = 0.0f;
+}
+static void symInverse33(V3 ex, V3 ey, V3 ez, float* M) {
+  float det = dot3(ex, cross3(ey, ez));
+  if (det != 0.0f) det = 1.0f / det;
+  float a11 = ex.x, a12 = ey.x, a13 = ez.x, a22 = ey.y, a23 = ez.y, a33 = ez.z;
+  M[0] = det * (a22 * a33 - a23 * a23);
+  M[1] = det * (a13 * a23 - a12 * a33);
+  M[2] = det * (a12 * a23 - a13 * a22);
+  M[3] = M[1];
+  M[4] = det * (a11 * a33 - a13 * a13);
+  M[5] = det * (a13 * a12 - a11 * a23);
+  M[6] = M[2];
+  M[7] = M[5];
+  M[8] = det * (a11 * a22 - a12 * a12);
+}
+static V2 solve22(V3 ex, V3 ey, V2 b) {
+  float a11 = ex.x, a12 = ey.x, a21 = ex.y, a22 = ey.y;
+  float det = a11 * a22 - a12 * a21;
+  if (det != 0.0f) det = 1.0f / det;
+  return v2(det * (a22 * b.x - a12 * b.y), det * (a11 * b.y - a21 * b.x));
+}
+// Linear mass (inverse of K) and angular mass of the motor and friction joints
+// (b2_motor_joint.cpp:91-104, b2_friction_joint.cpp:88-101).
+static void linearAngularMass(Joint& J, float mA, float mB, float iA, float iB) {
+  M22 K;
+  K.ex.x = mA + mB + iA * J.rA.y * J.rA.y + iB * J.rB.y * J.rB.y;
+  K.ex.y = -iA * J.rA.x * J.rA.y - iB * J.rB.x * J.rB.y;
+  K.ey.x = K.ex.y;
+  K.ey.y = mA + mB + iA * J.rA.x * J.rA.x + iB * J.rB.x * J.rB.x;
+  J.K = inverse(K);
+  J.axialMass = iA + iB;
+  if (J.axialMass > 0.0f) J.axialMass = 1.0f / J.axialMass;
+}
+// Clamped angular then linear impulse of the motor joint (with its position feedback,
+// b2_motor_joint.cpp:157-193) and the friction joint (without, b2_friction_joint.cpp:144-180).
+static void solveLinearAngular(Joint& J, V2& vA, float& wA, V2& vB, float& wB, float h, bool motor, float inv_h) {
+  float mA = J.mA, mB = J.mB, iA = J.invIA, iB = J.invIB;
+  {
+    float Cdot = motor ? wB - wA + inv_h * J.d.correction_factor * J.angularError : wB - wA;
+    float impulse = -J.axialMass * Cdot;
+    float oldImpulse = J.imp[2];
+    float maxImpulse = h * J.d.max_torque;
+    J.imp[2] = bclamp(J.imp[2] + impulse, -maxImpulse, maxImpulse);
+    impulse = J.imp[2] - oldImpulse;
+    wA -= iA * impulse;
+    wB += iB * impulse;
+  }
+  {
+    V2 Cdot = motor ? vB + cross(wB, J.rB) - vA - cross(wA, J.rA) + inv_h * J.d.correction_factor * J.err
+                    : vB + cross(wB, J.rB) - vA - cross(wA, J.rA);
+    V2 impulse = -mul(J.K, Cdot);
+    V2 oldImpulse = v2(J.imp[0], J.imp[1]);
+    V2 li = oldImpulse;
+    addTo(li, impulse);
+    float maxImpulse = h * J.d.max_force;
+    if (lengthSq(li) > maxImpulse * maxImpulse) {
+      normalize(li);
+      li.x *= maxImpulse;
+      li.y *= maxImpulse;
+    }
+    J.imp[0] = li.x; J.imp[1] = li.y;
+    impulse = li - oldImpulse;
+    subFrom(vA, mA * impulse);
+    wA -= iA * cross(J.rA, impulse);
+    addTo(vB, mB * impulse);
+    wB += iB * cross(J.rB, impulse);
+  }
+}
+
 static void jointInit(Joint& J, const std::vector<Body>& bodies, std::vector<SolverBody>& sb, const Step& st) {
   const Body& bA = bodies[J.d.body_a];
   const Body& bB = bodies[J.d.body_b];
@@ -1361,7 +1459,7 @@ static void jointInit(Joint& J, const std::vector<Body>& bodies, std::vector<Sol
     } else {
       J.impulse2 = v2(0.0f, 0.0f); J.motorImpulse = 0.0f; J.lowerImpulse = 0.0f; J.upperImpulse = 0.0f;
     }
-  } else {
+  } else if (J.d.type == B2G_JOINT_DISTANCE) {
     // b2DistanceJoint::InitVelocityConstraints (b2_distance_joint.cpp:76-173)
     J.rA = mul(qA, la - J.lcA);
     J.rB = mul(qB, lb - J.lcB);
@@ -1399,6 +1497,161 @@ static void jointInit(Joint& J, const std::vector<Body>& bodies, std::vector<Sol
       wB += J.invIB * cross(J.rB, P);
     } else {
       J.impulse1 = 0.0f;
+    }
+  } else if (J.d.type == B2G_JOINT_WELD) {
+    // b2WeldJoint::InitVelocityConstraints (b2_weld_joint.cpp:93-187)
+    J.rA = mul(qA, la - J.lcA);
+    J.rB = mul(qB, lb - J.lcB);
+    V3 ex, ey, ez;
+    weldK(J.rA, J.rB, mA, mB, iA, iB, ex, ey, ez);
+    if (J.d.stiffness > 0.0f) {
+      inverse22(ex, ey, J.mass3);
+      float invM = iA + iB;
+      float C = aB - aA - J.d.reference_angle;
+      float d = J.d.damping, k = J.d.stiffness, h = st.dt;
+      J.gamma = h * (d + h * k);
+      J.gamma = J.gamma != 0.0f ? 1.0f / J.gamma : 0.0f;
+      J.bias = C * h * k * J.gamma;
+      invM += J.gamma;
+      J.mass3[8] = invM != 0.0f ? 1.0f / invM : 0.0f;
+    } else if (ez.z == 0.0f) {
+      inverse22(ex, ey, J.mass3);
+      J.gamma = 0.0f; J.bias = 0.0f;
+    } else {
+      symInverse33(ex, ey, ez, J.mass3);
+      J.gamma = 0.0f; J.bias = 0.0f;
+    }
+    if (st.warm) {
+      for (int k = 0; k < 3; ++k) J.imp[k] *= st.dtRatio;
+      V2 P = v2(J.imp[0], J.imp[1]);
+      subFrom(vA, mA * P);
+      wA -= iA * (cross(J.rA, P) + J.imp[2]);
+      addTo(vB, mB * P);
+      wB += iB * (cross(J.rB, P) + J.imp[2]);
+    } else {
+      J.imp[0] = J.imp[1] = J.imp[2] = 0.0f;
+    }
+  } else if (J.d.type == B2G_JOINT_WHEEL) {
+    // b2WheelJoint::InitVelocityConstraints (b2_wheel_joint.cpp:89-211)
+    V2 rA = mul(qA, la - J.lcA);
+    V2 rB = mul(qB, lb - J.lcB);
+    V2 d = cB + rB - cA - rA;
+    J.perp = mul(qA, J.localYAxisA);
+    J.s1 = cross(d + rA, J.perp);
+    J.s2 = cross(rB, J.perp);
+    J.mass = mA + mB + iA * J.s1 * J.s1 + iB * J.s2 * J.s2;
+    if (J.mass > 0.0f) J.mass = 1.0f / J.mass;
+    J.axis = mul(qA, J.localXAxisA);
+    J.a1 = cross(d + rA, J.axis);
+    J.a2 = cross(rB, J.axis);
+    const float invMass = mA + mB + iA * J.a1 * J.a1 + iB * J.a2 * J.a2;
+    J.axialMass = invMass > 0.0f ? 1.0f / invMass : 0.0f;
+    J.springMass = 0.0f; J.bias = 0.0f; J.gamma = 0.0f;
+    if (J.d.stiffness > 0.0f && invMass > 0.0f) {
+      J.springMass = 1.0f / invMass;
+      float C = dot(d, J.axis);
+      float h = st.dt;
+      J.gamma = h * (J.d.damping + h * J.d.stiffness);
+      if (J.gamma > 0.0f) J.gamma = 1.0f / J.gamma;
+      J.bias = C * h * J.d.stiffness * J.gamma;
+      J.springMass = invMass + J.gamma;
+      if (J.springMass > 0.0f) J.springMass = 1.0f / J.springMass;
+    } else {
+      J.imp[1] = 0.0f;
+    }
+    if (J.d.enable_limit) J.translation = dot(J.axis, d);
+    else { J.lowerImpulse = 0.0f; J.upperImpulse = 0.0f; }
+    if (J.d.enable_motor) {
+      J.motorMass = iA + iB;
+      if (J.motorMass > 0.0f) J.motorMass = 1.0f / J.motorMass;
+    } else {
+      J.motorMass = 0.0f; J.motorImpulse = 0.0f;
+    }
+    if (st.warm) {
+      J.imp[0] *= st.dtRatio; J.imp[1] *= st.dtRatio; J.motorImpulse *= st.dtRatio;
+      float axialImpulse = J.imp[1] + J.lowerImpulse - J.upperImpulse;
+      V2 P = J.imp[0] * J.perp + axialImpulse * J.axis;
+      float LA = J.imp[0] * J.s1 + axialImpulse * J.a1 + J.motorImpulse;
+      float LB = J.imp[0] * J.s2 + axialImpulse * J.a2 + J.motorImpulse;
+      subFrom(vA, mA * P); wA -= iA * LA;
+      addTo(vB, mB * P); wB += iB * LB;
+    } else {
+      J.imp[0] = J.imp[1] = 0.0f; J.motorImpulse = J.lowerImpulse = J.upperImpulse = 0.0f;
+    }
+  } else if (J.d.type == B2G_JOINT_MOTOR || J.d.type == B2G_JOINT_FRICTION) {
+    // b2MotorJoint::InitVelocityConstraints (b2_motor_joint.cpp:58-136) and
+    // b2FrictionJoint::InitVelocityConstraints (b2_friction_joint.cpp:60-123)
+    if (J.d.type == B2G_JOINT_MOTOR) {
+      J.rA = mul(qA, v2(J.d.linear_offset[0], J.d.linear_offset[1]) - J.lcA);
+      J.rB = mul(qB, -J.lcB);
+    } else {
+      J.rA = mul(qA, la - J.lcA);
+      J.rB = mul(qB, lb - J.lcB);
+    }
+    linearAngularMass(J, mA, mB, iA, iB);
+    if (J.d.type == B2G_JOINT_MOTOR) {
+      J.err = cB + J.rB - cA - J.rA;
+      J.angularError = aB - aA - J.d.reference_angle;
+    }
+    if (st.warm) {
+      for (int k = 0; k < 3; ++k) J.imp[k] *= st.dtRatio;
+      V2 P = v2(J.imp[0], J.imp[1]);
+      subFrom(vA, mA * P);
+      wA -= iA * (cross(J.rA, P) + J.imp[2]);
+      addTo(vB, mB * P);
+      wB += iB * (cross(J.rB, P) + J.imp[2]);
+    } else {
+      J.imp[0] = J.imp[1] = J.imp[2] = 0.0f;
+    }
+  } else if (J.d.type == B2G_JOINT_MOUSE) {
+    // b2MouseJoint::InitVelocityConstraints (b2_mouse_joint.cpp:75-132): body B only
+    float d = J.d.damping, k = J.d.stiffness, h = st.dt;
+    J.gamma = h * (d + h * k);
+    if (J.gamma != 0.0f) J.gamma = 1.0f / J.gamma;
+    J.bias = h * k * J.gamma;
+    J.rB = mul(qB, lb - J.lcB);
+    M22 K;
+    K.ex.x = mB + iB * J.rB.y * J.rB.y + J.gamma;
+    K.ex.y = -iB * J.rB.x * J.rB.y;
+    K.ey.x = K.ex.y;
+    K.ey.y = mB + iB * J.rB.x * J.rB.x + J.gamma;
+    J.K = inverse(K);
+    J.err = cB + J.rB - v2(J.d.target[0], J.d.target[1]);
+    J.err.x *= J.bias;
+    J.err.y *= J.bias;
+    wB *= 0.98f;
+    if (st.warm) {
+      J.imp[0] *= st.dtRatio; J.imp[1] *= st.dtRatio;
+      V2 P = v2(J.imp[0], J.imp[1]);
+      addTo(vB, mB * P);
+      wB += iB * cross(J.rB, P);
+    } else {
+      J.imp[0] = J.imp[1] = 0.0f;
+    }
+  } else {
+    // b2PulleyJoint::InitVelocityConstraints (b2_pulley_joint.cpp:78-157)
+    J.rA = mul(qA, la - J.lcA);
+    J.rB = mul(qB, lb - J.lcB);
+    J.u = cA + J.rA - v2(J.d.ground_anchor_a[0], J.d.ground_anchor_a[1]);
+    J.uB = cB + J.rB - v2(J.d.ground_anchor_b[0], J.d.ground_anchor_b[1]);
+    float lengthA = lengthOf(J.u), lengthB = lengthOf(J.uB);
+    if (lengthA > 10.0f * kLinearSlop) { float s = 1.0f / lengthA; J.u.x *= s; J.u.y *= s; }
+    else J.u = v2(0.0f, 0.0f);
+    if (lengthB > 10.0f * kLinearSlop) { float s = 1.0f / lengthB; J.uB.x *= s; J.uB.y *= s; }
+    else J.uB = v2(0.0f, 0.0f);
+    float ruA = cross(J.rA, J.u), ruB = cross(J.rB, J.uB);
+    float pmA = mA + iA * ruA * ruA;
+    float pmB = mB + iB * ruB * ruB;
+    J.mass = pmA + J.d.ratio * J.d.ratio * pmB;
+    if (J.mass > 0.0f) J.mass = 1.0f / J.mass;
+    if (st.warm) {
+      J.imp[0] *= st.dtRatio;
+      V2 PA = -(J.imp[0]) * J.u;
+      V2 PB = (-J.d.ratio * J.imp[0]) * J.uB;
+      addTo(vA, mA * PA); wA += iA * cross(J.rA, PA);
+      addTo(vB, mB * PB); wB += iB * cross(J.rB, PB);
+    } else {
+      J.imp[0] = 0.0f;
     }
   }
   sb[J.iA].v = vA; sb[J.iA].w = wA;
@@ -1509,7 +1762,7 @@ static void jointSolveVelocity(Joint& J, std::vector<SolverBody>& sb, const Step
       subFrom(vA, mA * P); wA -= iA * LA;
       addTo(vB, mB * P); wB += iB * LB;
     }
-  } else {
+  } else if (J.d.type == B2G_JOINT_DISTANCE) {
     // b2DistanceJoint::SolveVelocityConstraints (b2_distance_joint.cpp:175-266)
     if (J.d.min_length < J.d.max_length) {
       if (J.d.stiffness > 0.0f) {
@@ -1560,6 +1813,123 @@ static void jointSolveVelocity(Joint& J, std::vector<SolverBody>& sb, const Step
       subFrom(vA, J.mA * P); wA -= J.invIA * cross(J.rA, P);
       addTo(vB, J.mB * P); wB += J.invIB * cross(J.rB, P);
     }
+  } else if (J.d.type == B2G_JOINT_WELD) {
+    // b2WeldJoint::SolveVelocityConstraints (b2_weld_joint.cpp:189-250)
+    float mA = J.mA, mB = J.mB, iA = J.invIA, iB = J.invIB;
+    const float* M = J.mass3;
+    if (J.d.stiffness > 0.0f) {
+      float Cdot2 = wB - wA;
+      float impulse2 = -M[8] * (Cdot2 + J.bias + J.gamma * J.imp[2]);
+      J.imp[2] += impulse2;
+      wA -= iA * impulse2;
+      wB += iB * impulse2;
+      V2 Cdot1 = vB + cross(wB, J.rB) - vA - cross(wA, J.rA);
+      V2 impulse1 = -v2(M[0] * Cdot1.x + M[3] * Cdot1.y, M[1] * Cdot1.x + M[4] * Cdot1.y);
+      J.imp[0] += impulse1.x;
+      J.imp[1] += impulse1.y;
+      subFrom(vA, mA * impulse1); wA -= iA * cross(J.rA, impulse1);
+      addTo(vB, mB * impulse1); wB += iB * cross(J.rB, impulse1);
+    } else {
+      V2 Cdot1 = vB + cross(wB, J.rB) - vA - cross(wA, J.rA);
+      float Cdot2 = wB - wA;
+      // -b2Mul(m_mass, Cdot) = -(Cdot.x ex + Cdot.y ey + Cdot.z ez)
+      float ix = -(Cdot1.x * M[0] + Cdot1.y * M[3] + Cdot2 * M[6]);
+      float iy = -(Cdot1.x * M[1] + Cdot1.y * M[4] + Cdot2 * M[7]);
+      float iz = -(Cdot1.x * M[2] + Cdot1.y * M[5] + Cdot2 * M[8]);
+      J.imp[0] += ix; J.imp[1] += iy; J.imp[2] += iz;
+      V2 P = v2(ix, iy);
+      subFrom(vA, mA * P); wA -= iA * (cross(J.rA, P) + iz);
+      addTo(vB, mB * P); wB += iB * (cross(J.rB, P) + iz);
+    }
+  } else if (J.d.type == B2G_JOINT_WHEEL) {
+    // b2WheelJoint::SolveVelocityConstraints (b2_wheel_joint.cpp:213-323)
+    float mA = J.mA, mB = J.mB, iA = J.invIA, iB = J.invIB;
+    {
+      float Cdot = dot(J.axis, vB - vA) + J.a2 * wB - J.a1 * wA;
+      float impulse = -J.springMass * (Cdot + J.bias + J.gamma * J.imp[1]);
+      J.imp[1] += impulse;
+      V2 P = impulse * J.axis;
+      float LA = impulse * J.a1, LB = impulse * J.a2;
+      subFrom(vA, mA * P); wA -= iA * LA;
+      addTo(vB, mB * P); wB += iB * LB;
+    }
+    {
+      float Cdot = wB - wA - J.d.motor_speed;
+      float impulse = -J.motorMass * Cdot;
+      float oldImpulse = J.motorImpulse;
+      float maxImpulse = st.dt * J.d.max_motor;
+      J.motorImpulse = bclamp(J.motorImpulse + impulse, -maxImpulse, maxImpulse);
+      impulse = J.motorImpulse - oldImpulse;
+      wA -= iA * impulse;
+      wB += iB * impulse;
+    }
+    if (J.d.enable_limit) {
+      {
+        float C = J.translation - J.d.lower;
+        float Cdot = dot(J.axis, vB - vA) + J.a2 * wB - J.a1 * wA;
+        float impulse = -J.axialMass * (Cdot + bmax(C, 0.0f) * st.inv_dt);
+        float oldImpulse = J.lowerImpulse;
+        J.lowerImpulse = bmax(J.lowerImpulse + impulse, 0.0f);
+        impulse = J.lowerImpulse - oldImpulse;
+        V2 P = impulse * J.axis;
+        float LA = impulse * J.a1, LB = impulse * J.a2;
+        subFrom(vA, mA * P); wA -= iA * LA;
+        addTo(vB, mB * P); wB += iB * LB;
+      }
+      {
+        float C = J.d.upper - J.translation;
+        float Cdot = dot(J.axis, vA - vB) + J.a1 * wA - J.a2 * wB;
+        float impulse = -J.axialMass * (Cdot + bmax(C, 0.0f) * st.inv_dt);
+        float oldImpulse = J.upperImpulse;
+        J.upperImpulse = bmax(J.upperImpulse + impulse, 0.0f);
+        impulse = J.upperImpulse - oldImpulse;
+        V2 P = impulse * J.axis;
+        float LA = impulse * J.a1, LB = impulse * J.a2;
+        addTo(vA, mA * P); wA += iA * LA;
+        subFrom(vB, mB * P); wB -= iB * LB;
+      }
+    }
+    {
+      float Cdot = dot(J.perp, vB - vA) + J.s2 * wB - J.s1 * wA;
+      float impulse = -J.mass * Cdot;
+      J.imp[0] += impulse;
+      V2 P = impulse * J.perp;
+      float LA = impulse * J.s1, LB = impulse * J.s2;
+      subFrom(vA, mA * P); wA -= iA * LA;
+      addTo(vB, mB * P); wB += iB * LB;
+    }
+  } else if (J.d.type == B2G_JOINT_MOTOR || J.d.type == B2G_JOINT_FRICTION) {
+    // b2MotorJoint / b2FrictionJoint::SolveVelocityConstraints (b2_motor_joint.cpp:138-196,
+    // b2_friction_joint.cpp:125-183)
+    solveLinearAngular(J, vA, wA, vB, wB, st.dt, J.d.type == B2G_JOINT_MOTOR, st.inv_dt);
+  } else if (J.d.type == B2G_JOINT_MOUSE) {
+    // b2MouseJoint::SolveVelocityConstraints (b2_mouse_joint.cpp:134-160)
+    V2 Cdot = vB + cross(wB, J.rB);
+    V2 old = v2(J.imp[0], J.imp[1]);
+    V2 impulse = mul(J.K, -(Cdot + J.err + J.gamma * old));
+    V2 acc = old;
+    addTo(acc, impulse);
+    float maxImpulse = st.dt * J.d.max_force;
+    if (lengthSq(acc) > maxImpulse * maxImpulse) {
+      float s = maxImpulse / lengthOf(acc);
+      acc.x *= s;
+      acc.y *= s;
+    }
+    J.imp[0] = acc.x; J.imp[1] = acc.y;
+    impulse = acc - old;
+    addTo(vB, J.mB * impulse);
+    wB += J.invIB * cross(J.rB, impulse);
+  } else {
+    // b2PulleyJoint::SolveVelocityConstraints (b2_pulley_joint.cpp:159-182)
+    V2 vpA = vA + cross(wA, J.rA);
+    V2 vpB = vB + cross(wB, J.rB);
+    float Cdot = -dot(J.u, vpA) - J.d.ratio * dot(J.uB, vpB);
+    float impulse = -J.mass * Cdot;
+    J.imp[0] += impulse;
+    V2 PA = -impulse * J.u;
+    V2 PB = -J.d.ratio * impulse * J.uB;
+    addTo(vA, J.mA * PA); wA += J.invIA * cross(J.rA, PA);
+    addTo(vB, J.mB * PB); wB += J.invIB * cross(J.rB, PB);
   }
   sb[J.iA].v = vA; sb[J.iA].w = wA;
   sb[J.iB].v = vB; sb[J.iB].w = wB;
@@ -1675,7 +2045,7 @@ static bool jointSolvePosition(Joint& J, std::vector<SolverBody>& sb) {
     subFrom(cA, mA * P); aA -= iA * LA;
     addTo(cB, mB * P); aB += iB * LB;
     ok = linearError <= kLinearSlop && angularError <= kAngularSlop;
-  } else {
+  } else if (J.d.type == B2G_JOINT_DISTANCE) {
     // b2DistanceJoint::SolvePositionConstraints (b2_distance_joint.cpp:268-314)
     V2 rA = mul(qA, la - J.lcA);
     V2 rB = mul(qB, lb - J.lcB);
@@ -1691,6 +2061,112 @@ static bool jointSolvePosition(Joint& J, std::vector<SolverBody>& sb) {
     subFrom(cA, J.mA * P); aA -= J.invIA * cross(rA, P);
     addTo(cB, J.mB * P); aB += J.invIB * cross(rB, P);
     ok = babs(C) < kLinearSlop;
+  } else if (J.d.type == B2G_JOINT_WELD) {
+    // b2WeldJoint::SolvePositionConstraints (b2_weld_joint.cpp:252-329)
+    float mA = J.mA, mB = J.mB, iA = J.invIA, iB = J.invIB;
+    V2 rA = mul(qA, la - J.lcA);
+    V2 rB = mul(qB, lb - J.lcB);
+    float positionError, angularError;
+    V3 ex, ey, ez;
+    weldK(rA, rB, mA, mB, iA, iB, ex, ey, ez);
+    if (J.d.stiffness > 0.0f) {
+      V2 C1 = cB + rB - cA - rA;
+      positionError = lengthOf(C1);
+      angularError = 0.0f;
+      V2 P = -solve22(ex, ey, C1);
+      subFrom(cA, mA * P); aA -= iA * cross(rA, P);
+      addTo(cB, mB * P); aB += iB * cross(rB, P);
+    } else {
+      V2 C1 = cB + rB - cA - rA;
+      float C2 = aB - aA - J.d.reference_angle;
+      positionError = lengthOf(C1);
+      angularError = babs(C2);
+      V3 C = {C1.x, C1.y, C2};
+      V3 impulse;
+      if (ez.z > 0.0f) {
+        V3 x = solve33(ex, ey, ez, C);
+        impulse = V3{-x.x, -x.y, -x.z};
+      } else {
+        V2 impulse2 = -solve22(ex, ey, C1);
+        impulse = V3{impulse2.x, impulse2.y, 0.0f};
+      }
+      V2 P = v2(impulse.x, impulse.y);
+      subFrom(cA, mA * P); aA -= iA * (cross(rA, P) + impulse.z);
+      addTo(cB, mB * P); aB += iB * (cross(rB, P) + impulse.z);
+    }
+    ok = positionError <= kLinearSlop && angularError <= kAngularSlop;
+  } else if (J.d.type == B2G_JOINT_WHEEL) {
+    // b2WheelJoint::SolvePositionConstraints (b2_wheel_joint.cpp:325-420); like the reference,
+    // the limit uses the step's m_ax and the point constraint the step's m_sAy, m_sBy
+    float linearError = 0.0f;
+    if (J.d.enable_limit) {
+      V2 rA = mul(qA, la - J.lcA);
+      V2 rB = mul(qB, lb - J.lcB);
+      V2 d = (cB - cA) + rB - rA;
+      V2 ax = mul(qA, J.localXAxisA);
+      float sAx = cross(d + rA, J.axis);
+      float sBx = cross(rB, J.axis);
+      float C = 0.0f;
+      float translation = dot(ax, d);
+      if (babs(J.d.upper - J.d.lower) < 2.0f * kLinearSlop) C = translation;
+      else if (translation <= J.d.lower) C = bmin(translation - J.d.lower, 0.0f);
+      else if (translation >= J.d.upper) C = bmax(translation - J.d.upper, 0.0f);
+      if (C != 0.0f) {
+        float invMass = J.mA + J.mB + J.invIA * sAx * sAx + J.invIB * sBx * sBx;
+        float impulse = 0.0f;
+        if (invMass != 0.0f) impulse = -C / invMass;
+        V2 P = impulse * ax;
+        float LA = impulse * sAx, LB = impulse * sBx;
+        subFrom(cA, J.mA * P); aA -= J.invIA * LA;
+        addTo(cB, J.mB * P); aB += J.invIB * LB;
+        linearError = babs(C);
+      }
+    }
+    {
+      Rot qA2 = rotOf(aA), qB2 = rotOf(aB);
+      V2 rA = mul(qA2, la - J.lcA);
+      V2 rB = mul(qB2, lb - J.lcB);
+      V2 d = (cB - cA) + rB - rA;
+      V2 ay = mul(qA2, J.localYAxisA);
+      float sAy = cross(d + rA, ay);
+      float sBy = cross(rB, ay);
+      float C = dot(d, ay);
+      float invMass = J.mA + J.mB + J.invIA * J.s1 * J.s1 + J.invIB * J.s2 * J.s2;
+      float impulse = 0.0f;
+      if (invMass != 0.0f) impulse = -C / invMass;
+      V2 P = impulse * ay;
+      float LA = impulse * sAy, LB = impulse * sBy;
+      subFrom(cA, J.mA * P); aA -= J.invIA * LA;
+      addTo(cB, J.mB * P); aB += J.invIB * LB;
+      linearError = bmax(linearError, babs(C));
+    }
+    ok = linearError <= kLinearSlop;
+  } else if (J.d.type == B2G_JOINT_PULLEY) {
+    // b2PulleyJoint::SolvePositionConstraints (b2_pulley_joint.cpp:184-256)
+    V2 rA = mul(qA, la - J.lcA);
+    V2 rB = mul(qB, lb - J.lcB);
+    V2 uA = cA + rA - v2(J.d.ground_anchor_a[0], J.d.ground_anchor_a[1]);
+    V2 uB = cB + rB - v2(J.d.ground_anchor_b[0], J.d.ground_anchor_b[1]);
+    float lengthA = lengthOf(uA), lengthB = lengthOf(uB);
+    if (lengthA > 10.0f * kLinearSlop) { float s = 1.0f / lengthA; uA.x *= s; uA.y *= s; }
+    else uA = v2(0.0f, 0.0f);
+    if (lengthB > 10.0f * kLinearSlop) { float s = 1.0f / lengthB; uB.x *= s; uB.y *= s; }
+    else uB = v2(0.0f, 0.0f);
+    float ruA = cross(rA, uA), ruB = cross(rB, uB);
+    float pmA = J.mA + J.invIA * ruA * ruA;
+    float pmB = J.mB + J.invIB * ruB * ruB;
+    float mass = pmA + J.d.ratio * J.d.ratio * pmB;
+    if (mass > 0.0f) mass = 1.0f / mass;
+    float C = J.constant - lengthA - J.d.ratio * lengthB;
+    float linearError = babs(C);
+    float impulse = -mass * C;
+    V2 PA = -impulse * uA;
+    V2 PB = -J.d.ratio * impulse * uB;
+    addTo(cA, J.mA * PA); aA += J.invIA * cross(rA, PA);
+    addTo(cB, J.mB * PB); aB += J.invIB * cross(rB, PB);
+    ok = linearError < kLinearSlop;
+  } else {
+    return true;  // motor, friction and mouse joints have no position constraint
   }
   sb[J.iA].c = cA; sb[J.iA].a = aA;
   sb[J.iB].c = cB; sb[J.iB].a = aB;
@@ -1706,10 +2182,21 @@ static void jointReaction(const Joint& J, float inv_dt, float* F, float* T) {
     V2 f = inv_dt * (J.impulse2.x * J.perp + ((J.motorImpulse + J.lowerImpulse) - J.upperImpulse) * J.axis);
     F[0] = f.x; F[1] = f.y;
     *T = inv_dt * J.impulse2.y;
-  } else {
+  } else if (J.d.type == B2G_JOINT_DISTANCE) {
     V2 f = (inv_dt * ((J.impulse1 + J.lowerImpulse) - J.upperImpulse)) * J.u;
     F[0] = f.x; F[1] = f.y;
     *T = 0.0f;
+  } else if (J.d.type == B2G_JOINT_WHEEL) {  // b2_wheel_joint.cpp:448-461
+    V2 f = inv_dt * (J.imp[0] * J.perp + ((J.imp[1] + J.lowerImpulse) - J.upperImpulse) * J.axis);
+    F[0] = f.x; F[1] = f.y;
+    *T = inv_dt * J.motorImpulse;
+  } else if (J.d.type == B2G_JOINT_PULLEY) {  // b2_pulley_joint.cpp:276-286
+    V2 f = inv_dt * (J.imp[0] * J.uB);
+    F[0] = f.x; F[1] = f.y;
+    *T = 0.0f;
+  } else {  // weld, motor, friction, mouse
+    F[0] = inv_dt * J.imp[0]; F[1] = inv_dt * J.imp[1];
+    *T = J.d.type == B2G_JOINT_MOUSE ? inv_dt * 0.0f : inv_dt * J.imp[2];
   }
 }
 
@@ -2431,13 +2918,15 @@ int orc_world_load(void* h, const b2g_body* bodies, int32_t nb, const b2g_fixtur
     J.d = joints[i].def;
     J.impulse2 = v2(joints[i].impulse[0], joints[i].impulse[1]);
     J.impulse1 = joints[i].impulse[0];
+    for (int k = 0; k < 3; ++k) J.imp[k] = joints[i].impulse[k];
     J.motorImpulse = joints[i].motor_impulse;
     J.lowerImpulse = joints[i].lower_impulse;
     J.upperImpulse = joints[i].upper_impulse;
-    if (J.d.type == B2G_JOINT_PRISMATIC) {
+    if (J.d.type == B2G_JOINT_PRISMATIC || J.d.type == B2G_JOINT_WHEEL) {
       J.localXAxisA = v2(J.d.local_axis_a[0], J.d.local_axis_a[1]);
       J.localYAxisA = cross(1.0f, J.localXAxisA);
     }
+    if (J.d.type == B2G_JOINT_PULLEY) J.constant = J.d.length_a + J.d.ratio * J.d.length_b;
     if (J.d.body_a < 0 || J.d.body_a >= nb || J.d.body_b < 0 || J.d.body_b >= nb) return 1;
   }
   rebuildNoCollide(w);
@@ -2549,6 +3038,8 @@ void orc_world_joints(void* h, b2g_joint* out) {
     memset(&s, 0, sizeof(s));
     s.def = J.d;
     if (J.d.type == B2G_JOINT_DISTANCE) s.impulse[0] = J.impulse1;
+    else if (J.d.type != B2G_JOINT_REVOLUTE && J.d.type != B2G_JOINT_PRISMATIC)
+      for (int k = 0; k < 3; ++k) s.impulse[k] = J.imp[k];
     else { s.impulse[0] = J.impulse2.x; s.impulse[1] = J.impulse2.y; }
     s.motor_impulse = J.motorImpulse; s.lower_impulse = J.lowerImpulse; s.upper_impulse = J.upperImpulse;
     float F[2], T;

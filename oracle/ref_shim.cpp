@@ -244,6 +244,7 @@ void* ref_scene_world(int32_t kind, uint32_t seed, int32_t n, float p0, float p1
   else if (kind == B2G_SCENE_MIXED_DROP) c = b2scenes::MixedDrop(rw->world, n, seed);
   else if (kind == B2G_SCENE_CHAINS) c = b2scenes::ChainsOverPile(rw->world, n, 20, (int)p0, seed);
   else if (kind == B2G_SCENE_BATCH_WORLD) c = b2scenes::BatchWorld(rw->world, seed, n);
+  else if (kind == B2G_SCENE_JOINTS) c = b2scenes::JointZoo(rw->world, n, seed);
   if (counts) { counts[0] = c.bodies; counts[1] = c.fixtures; counts[2] = c.joints; }
   index_world(rw);
   return rw;
@@ -362,6 +363,60 @@ void ref_world_joints(void* h, b2g_joint* out) {
       o->def.stiffness = d->m_stiffness; o->def.damping = d->m_damping;
       o->impulse[0] = d->m_impulse;
       o->lower_impulse = d->m_lowerImpulse; o->upper_impulse = d->m_upperImpulse;
+    } else if (j->m_type == e_weldJoint) {
+      b2WeldJoint* q = (b2WeldJoint*)j;
+      o->def.type = B2G_JOINT_WELD;
+      o->def.local_anchor_a[0] = q->m_localAnchorA.x; o->def.local_anchor_a[1] = q->m_localAnchorA.y;
+      o->def.local_anchor_b[0] = q->m_localAnchorB.x; o->def.local_anchor_b[1] = q->m_localAnchorB.y;
+      o->def.reference_angle = q->m_referenceAngle;
+      o->def.stiffness = q->m_stiffness; o->def.damping = q->m_damping;
+      o->impulse[0] = q->m_impulse.x; o->impulse[1] = q->m_impulse.y; o->impulse[2] = q->m_impulse.z;
+    } else if (j->m_type == e_wheelJoint) {
+      b2WheelJoint* q = (b2WheelJoint*)j;
+      o->def.type = B2G_JOINT_WHEEL;
+      o->def.local_anchor_a[0] = q->m_localAnchorA.x; o->def.local_anchor_a[1] = q->m_localAnchorA.y;
+      o->def.local_anchor_b[0] = q->m_localAnchorB.x; o->def.local_anchor_b[1] = q->m_localAnchorB.y;
+      o->def.local_axis_a[0] = q->m_localXAxisA.x; o->def.local_axis_a[1] = q->m_localXAxisA.y;
+      o->def.enable_limit = q->m_enableLimit; o->def.lower = q->m_lowerTranslation;
+      o->def.upper = q->m_upperTranslation; o->def.enable_motor = q->m_enableMotor;
+      o->def.max_motor = q->m_maxMotorTorque; o->def.motor_speed = q->m_motorSpeed;
+      o->def.stiffness = q->m_stiffness; o->def.damping = q->m_damping;
+      o->impulse[0] = q->m_impulse; o->impulse[1] = q->m_springImpulse;
+      o->motor_impulse = q->m_motorImpulse; o->lower_impulse = q->m_lowerImpulse;
+      o->upper_impulse = q->m_upperImpulse;
+    } else if (j->m_type == e_motorJoint) {
+      b2MotorJoint* q = (b2MotorJoint*)j;
+      o->def.type = B2G_JOINT_MOTOR;
+      o->def.linear_offset[0] = q->m_linearOffset.x; o->def.linear_offset[1] = q->m_linearOffset.y;
+      o->def.reference_angle = q->m_angularOffset;
+      o->def.max_force = q->m_maxForce; o->def.max_torque = q->m_maxTorque;
+      o->def.correction_factor = q->m_correctionFactor;
+      o->impulse[0] = q->m_linearImpulse.x; o->impulse[1] = q->m_linearImpulse.y;
+      o->impulse[2] = q->m_angularImpulse;
+    } else if (j->m_type == e_frictionJoint) {
+      b2FrictionJoint* q = (b2FrictionJoint*)j;
+      o->def.type = B2G_JOINT_FRICTION;
+      o->def.local_anchor_a[0] = q->m_localAnchorA.x; o->def.local_anchor_a[1] = q->m_localAnchorA.y;
+      o->def.local_anchor_b[0] = q->m_localAnchorB.x; o->def.local_anchor_b[1] = q->m_localAnchorB.y;
+      o->def.max_force = q->m_maxForce; o->def.max_torque = q->m_maxTorque;
+      o->impulse[0] = q->m_linearImpulse.x; o->impulse[1] = q->m_linearImpulse.y;
+      o->impulse[2] = q->m_angularImpulse;
+    } else if (j->m_type == e_mouseJoint) {
+      b2MouseJoint* q = (b2MouseJoint*)j;
+      o->def.type = B2G_JOINT_MOUSE;
+      o->def.target[0] = q->m_targetA.x; o->def.target[1] = q->m_targetA.y;
+      o->def.local_anchor_b[0] = q->m_localAnchorB.x; o->def.local_anchor_b[1] = q->m_localAnchorB.y;
+      o->def.max_force = q->m_maxForce; o->def.stiffness = q->m_stiffness; o->def.damping = q->m_damping;
+      o->impulse[0] = q->m_impulse.x; o->impulse[1] = q->m_impulse.y;
+    } else if (j->m_type == e_pulleyJoint) {
+      b2PulleyJoint* q = (b2PulleyJoint*)j;
+      o->def.type = B2G_JOINT_PULLEY;
+      o->def.ground_anchor_a[0] = q->m_groundAnchorA.x; o->def.ground_anchor_a[1] = q->m_groundAnchorA.y;
+      o->def.ground_anchor_b[0] = q->m_groundAnchorB.x; o->def.ground_anchor_b[1] = q->m_groundAnchorB.y;
+      o->def.local_anchor_a[0] = q->m_localAnchorA.x; o->def.local_anchor_a[1] = q->m_localAnchorA.y;
+      o->def.local_anchor_b[0] = q->m_localAnchorB.x; o->def.local_anchor_b[1] = q->m_localAnchorB.y;
+      o->def.length_a = q->m_lengthA; o->def.length_b = q->m_lengthB; o->def.ratio = q->m_ratio;
+      o->impulse[0] = q->m_impulse;
     }
     b2Vec2 F = j->GetReactionForce(1.0f);
     o->reaction_impulse[0] = F.x; o->reaction_impulse[1] = F.y;

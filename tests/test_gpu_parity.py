@@ -134,6 +134,13 @@ def test_solver_order_matches_oracle(lib, orc, kind, n, p0):
     batch.close()
 
 
+@pytest.mark.parametrize("n,seed,vi,pi", [(4, 9, 8, 3), (2, 17, 10, 4)])
+def test_joint_zoo_rollout_bit_exact(lib, orc, n, seed, vi, pi):
+    """Weld (rigid and soft), wheel (springs, motor, limits), motor, friction, mouse and pulley
+    joints: every body state, joint impulse and contact equals the oracle's after every step."""
+    _rollout(lib, orc, G.SCENE_JOINTS, n, seed=seed, p0=0.0, steps=240, vi=vi, pi=pi)
+
+
 def test_batched_equals_alone(lib):
     """Worlds stepped together in one batch are bit-identical to the same worlds stepped alone."""
     seeds = [21, 22, 23, 24, 25, 26]
@@ -525,6 +532,7 @@ def _sleep_world(batch, kind, n, seed, p0):
 
 
 @pytest.mark.parametrize("kind,n,seed,p0,steps,vi,pi", [
+    (G.SCENE_JOINTS, 3, 9, 0.0, 400, 8, 3),
     (G.SCENE_PYRAMID, 10, 1, 1.0, 160, 8, 3),
     (G.SCENE_CHAINS, 6, 4, 100.0, 500, 10, 4),
     (G.SCENE_MIXED_DROP, 200, 5, 0.0, 490, 8, 3),

@@ -133,6 +133,9 @@ def test_oracle_vs_reference_live(ref, orc):
     (G.SCENE_PYRAMID, 20, 1, 1.0, 30, 8, 3),
     (G.SCENE_MIXED_DROP, 400, 5, 0.0, 200, 8, 3),
     (G.SCENE_CHAINS, 15, 4, 200.0, 80, 10, 4),
+    (G.SCENE_JOINTS, 3, 9, 0.0, 1, 8, 3),
+    (G.SCENE_JOINTS, 3, 9, 0.0, 40, 8, 3),
+    (G.SCENE_JOINTS, 2, 17, 0.0, 150, 10, 4),
 ])
 def test_oracle_replay_vs_reference_live(ref, orc, kind, n, seed, p0, warm, vi, pi):
     """The reference's b2Island::Solve replaying the oracle's order: bit-exact, 3 steps."""
@@ -158,7 +161,7 @@ def test_oracle_replay_vs_reference_live(ref, orc, kind, n, seed, p0, warm, vi, 
 
 @pytest.mark.parametrize("kind,n,seed,p0", [
     (G.SCENE_PYRAMID, 20, 1, 1.0), (G.SCENE_MIXED_DROP, 500, 3, 0.0), (G.SCENE_CHAINS, 30, 2, 300.0),
-    (G.SCENE_BATCH_WORLD, 777, 5, 0.0)])
+    (G.SCENE_BATCH_WORLD, 777, 5, 0.0), (G.SCENE_JOINTS, 3, 9, 0.0)])
 def test_host_scene_setup_vs_reference_live(ref, kind, n, seed, p0):
     """The engine's host-side set-up (facade -> shapes -> mass data -> joint defs) produces the
     reference's body, fixture and joint state byte for byte."""
