@@ -137,6 +137,183 @@ B2G_HD V3 solve33(V3 ex, V3 ey, V3 ez, V3 b) {
   return x;
 }
 
+// ---- GJK distance for sensors: b2TestOverlap (src/collision/b2_collision.cpp:239-258) over
+// b2Distance (src/collision/b2_distance.cpp:432-579) with an empty simplex cache and radii.
+struct SimplexVertex { V2 wA, wB, w; float a; int indexA, indexB; };
+B2G_HD int proxyCount(const b2g_shape& s) {
+  return s.type == B2G_SHAPE_CIRCLE ? 1 : (s.type == B2G_SHAPE_EDGE ? 2 : s.count);
+}
+B2G_HD V2 proxyVertex(const b2g_shape& s, int i) { return mk(s.vertices[i][0], s.vertices[i][1]); }
+// b2DistanceProxy::GetSupport (include/box2d/b2_distance.h:137-152)
+B2G_HD int proxySupport(const b2g_shape& s, V2 d) {
+  const int n = proxyCount(s);
+  int bestIndex = 0;
+  float bestValue = dot(proxyVertex(s, 0), d);
+  for (int i = 1; i < n; ++i) {
+    float value = dot(proxyVertex(s, i), d);
+    if (value > bestValue) {
+      bestIndex = i;
+      bestValue = value;
+    }
+  }
+  return bestIndex;
+}
+// b2Simplex::Solve2 (b2_distance.cpp:284-321); v holds m_v1, m_v2, m_v3
+B2G_HD void simplexSolve2(SimplexVertex* v, int& count) {
+  V2 w1 = v[0].w, w2 = v[1].w;
+  V2 e12 = w2 - w1;
+  float d12_2 = -dot(w1, e12);
+  if (d12_2 <= 0.0f) {
+    v[0].a = 1.0f;
+    count = 1;
+    return;
+  }
+  float d12_1 = dot(w2, e12);
+  if (d12_1 <= 0.0f) {
+    v[1].a = 1.0f;
+    count = 1;
+    v[0] = v[1];
+    return;
+  }
+  float inv_d12 = 1.0f / (d12_1 + d12_2);
+  v[0].a = d12_1 * inv_d12;
+  v[1].a = d12_2 * inv_d12;
+  count = 2;
+}
+// b2Simplex::Solve3 (b2_distance.cpp:323-430)
+B2G_HD void simplexSolve3(SimplexVertex* v, int& count) {
+  V2 w1 = v[0].w, w2 = v[1].w, w3 = v[2].w;
+  V2 e12 = w2 - w1;
+  float w1e12 = dot(w1, e12);
+  float w2e12 = dot(w2, e12);
+  float d12_1 = w2e12;
+  float d12_2 = -w1e12;
+  V2 e13 = w3 - w1;
+  float w1e13 = dot(w1, e13);
+  float w3e13 = dot(w3, e13);
+  float d13_1 = w3e13;
+  float d13_2 = -w1e13;
+  V2 e23 = w3 - w2;
+  float w2e23 = dot(w2, e23);
+  float w3e23 = dot(w3, e23);
+  float d23_1 = w3e23;
+  float d23_2 = -w2e23;
+  float n123 = cross(e12, e13);
+  float d123_1 = n123 * cross(w2, w3);
+  float d123_2 = n123 * cross(w3, w1);
+  float d123_3 = n123 * cross(w1, w2);
+  if (d12_2 <= 0.0f && d13_2 <= 0.0f) {
+    v[0].a = 1.0f;
+    count = 1;
+    return;
+  }
+  if (d12_1 > 0.0f && d12_2 > 0.0f && d123_3 <= 0.0f) {
+    float inv_d12 = 1.0f / (d12_1 + d12_2);
+    v[0].a = d12_1 * inv_d12;
+    v[1].a = d12_2 * inv_d12;
+    count = 2;
+    return;
+  }
+  if (d13_1 > 0.0f && d13_2 > 0.0f && d123_2 <= 0.0f) {
+    float inv_d13 = 1.0f / (d13_1 + d13_2);
+    v[0].a = d13_1 * inv_d13;
+    v[2].a = d13_2 * inv_d13;
+    count = 2;
+    v[1] = v[2];
+    return;
+  }
+  if (d12_1 <= 0.0f && d23_2 <= 0.0f) {
+    v[1].a = 1.0f;
+    count = 1;
+    v[0] = v[1];
+    return;
+  }
+  if (d13_1 <= 0.0f && d23_1 <= 0.0f) {
+    v[2].a = 1.0f;
+    count = 1;
+    v[0] = v[2];
+    return;
+  }
+  if (d23_1 > 0.0f && d23_2 > 0.0f && d123_1 <= 0.0f) {
+    float inv_d23 = 1.0f / (d23_1 + d23_2);
+    v[1].a = d23_1 * inv_d23;
+    v[2].a = d23_2 * inv_d23;
+    count = 2;
+    v[0] = v[2];
+    return;
+  }
+  float inv_d123 = 1.0f / (d123_1 + d123_2 + d123_3);
+  v[0].a = d123_1 * inv_d123;
+  v[1].a = d123_2 * inv_d123;
+  v[2].a = d123_3 * inv_d123;
+  count = 3;
+}
+// The GJK distance between the shapes' cores (radii applied as b2Distance's useRadii).
+B2G_HD float shapeDistance(const b2g_shape& A, const Xf& xfA, const b2g_shape& B, const Xf& xfB) {
+  SimplexVertex v[3];
+  v[0].indexA = 0;
+  v[0].indexB = 0;
+  v[0].wA = mul(xfA, proxyVertex(A, 0));
+  v[0].wB = mul(xfB, proxyVertex(B, 0));
+  v[0].w = v[0].wB - v[0].wA;
+  v[0].a = 1.0f;
+  int count = 1;
+  int saveA[3], saveB[3];
+  for (int iter = 0; iter < 20;) {
+    const int saveCount = count;
+    for (int i = 0; i < saveCount; ++i) {
+      saveA[i] = v[i].indexA;
+      saveB[i] = v[i].indexB;
+    }
+    if (count == 2) simplexSolve2(v, count);
+    else if (count == 3) simplexSolve3(v, count);
+    if (count == 3) break;
+    V2 d;
+    if (count == 1) {
+      d = -v[0].w;
+    } else {
+      V2 e12 = v[1].w - v[0].w;
+      float sgn = cross(e12, -v[0].w);
+      d = sgn > 0.0f ? cross(1.0f, e12) : cross(e12, 1.0f);
+    }
+    if (lengthSq(d) < B2G_EPSILON * B2G_EPSILON) break;
+    SimplexVertex& nv = v[count];
+    nv.indexA = proxySupport(A, mulT(xfA.q, -d));
+    nv.wA = mul(xfA, proxyVertex(A, nv.indexA));
+    nv.indexB = proxySupport(B, mulT(xfB.q, d));
+    nv.wB = mul(xfB, proxyVertex(B, nv.indexB));
+    nv.w = nv.wB - nv.wA;
+    ++iter;
+    bool duplicate = false;
+    for (int i = 0; i < saveCount; ++i) {
+      if (nv.indexA == saveA[i] && nv.indexB == saveB[i]) {
+        duplicate = true;
+        break;
+      }
+    }
+    if (duplicate) break;
+    ++count;
+  }
+  V2 pA, pB;
+  if (count == 1) {
+    pA = v[0].wA;
+    pB = v[0].wB;
+  } else if (count == 2) {
+    pA = v[0].a * v[0].wA + v[1].a * v[1].wA;
+    pB = v[0].a * v[0].wB + v[1].a * v[1].wB;
+  } else {
+    pA = (v[0].a * v[0].wA + v[1].a * v[1].wA) + v[2].a * v[2].wA;
+    pB = pA;
+  }
+  float distance = lengthOf(pA - pB);
+  const float rA = A.radius, rB = B.radius;
+  if (distance > rA + rB && distance > B2G_EPSILON) return distance - (rA + rB);
+  return 0.0f;
+}
+B2G_HD bool testOverlap(const b2g_shape& A, const Xf& xfA, const b2g_shape& B, const Xf& xfB) {
+  return shapeDistance(A, xfA, B, xfB) < 10.0f * B2G_EPSILON;
+}
+
 // ---- portable sine/cosine ------------------------------------------------------------------
 // Cody & Waite reduction of x by pi/2 (pi/2 split into two 12-bit parts and a float remainder,
 // so k*part is exact for |k| < 4096, i.e. |x| < ~6400 rad) and the Taylor series of sin (to

@@ -136,6 +136,7 @@ static KernelArgs make_args(Batch* b) {
   a.xf = b->xf.p; a.pos = b->pos.p; a.vel = b->vel.p; a.massd = b->massd.p; a.damp = b->damp.p;
   a.force = b->force.p; a.lc = b->lc.p; a.btype = b->btype.p; a.bworld = b->bworld.p;
   a.bstate = b->bstate.p; a.bwake = b->bwake.p; a.sl = b->sl.p; a.any_sleep = b->any_sleep ? 1 : 0;
+  a.any_sensor = b->any_sensor ? 1 : 0;
   a.shape = b->shape.p; a.fbody = b->fbody.p; a.fgroup = b->fgroup.p; a.fsensor = b->fsensor.p;
   a.fworld = b->fworld.p; a.frad = b->frad.p; a.ffilter = b->ffilter.p; a.fmat = b->fmat.p; a.aabb = b->aabb.p;
   a.joints = b->joints.p; a.nocollide = b->nocollide.p; a.n_nocollide = b->n_nocollide;
@@ -375,6 +376,7 @@ int upload_all(Batch* b) {
   CUDA_TRY(b, cudaMemsetAsync(b->bwake.p, 0, b->bwake.cap, b->stream));
   TRY(upload(b, b->shape, shape)); TRY(upload(b, b->fbody, fbody)); TRY(upload(b, b->fgroup, fgroup));
   TRY(upload(b, b->fsensor, fsensor)); TRY(upload(b, b->fworld, fworld)); TRY(upload(b, b->ffilter, ffilter));
+  b->any_sensor = std::find(fsensor.begin(), fsensor.end(), 1) != fsensor.end();
   TRY(upload(b, b->frad, frad));
   TRY(upload(b, b->fmat, fmat)); TRY(ensure(b, b->aabb, NF));
   TRY(upload(b, b->joints, joints)); TRY(upload(b, b->nocollide, nocol));
@@ -574,6 +576,7 @@ int upload_tail(Batch* b) {
   TRY(st.add(b, b->bstate, NB0, bstate));
   TRY(st.add(b, b->shape, NF0, shape)); TRY(st.add(b, b->fbody, NF0, fbody)); TRY(st.add(b, b->fgroup, NF0, fgroup));
   TRY(st.add(b, b->fsensor, NF0, fsensor)); TRY(st.add(b, b->fworld, NF0, fworld));
+  if (std::find(fsensor.begin(), fsensor.end(), 1) != fsensor.end()) b->any_sensor = true;
   TRY(st.add(b, b->frad, NF0, frad));
   TRY(st.add(b, b->ffilter, NF0, ffilter)); TRY(st.add(b, b->fmat, NF0, fmat));
   TRY(st.add(b, b->joints, NJ0, joints)); TRY(st.add(b, b->nocollide, b->n_nocollide, nocol));

@@ -173,6 +173,7 @@ struct Batch {
   DBuf<uint8_t> bwake;            // narrowphase wake marks (zero between steps)
   DBuf<int4> sl;                  // island scratch of sleep-mode worlds
   bool any_sleep = false;         // some world of the layout runs in sleep mode
+  bool any_sensor = false;        // some fixture of the layout is a sensor
 
   DBuf<b2g_shape> shape;
   DBuf<int> fbody, fgroup, fsensor, fworld;

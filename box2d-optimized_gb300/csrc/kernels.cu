@@ -33,21 +33,27 @@ __device__ __forceinline__ Xf ldXf(const float4* xf, int i) {
 // ================================================================================ narrowphase
 #define B2G_CONTACT_CLOSURE 0x40000000u  // scratch: updated by the wake closure of this step
 
+// A sensor contact is touching when the shapes overlap (b2TestOverlap); kept out of line so that
+// its GJK state does not weigh on the registers of the manifold path.
+__device__ __noinline__ bool sensor_overlap(const b2g_shape& A, Xf xfA, const b2g_shape& B, Xf xfB) {
+  return testOverlap(A, xfA, B, xfB);
+}
+
 // b2Contact::Update for contact i: evaluate the manifold, carry impulses by feature id, set
 // touching, record Begin/End/PreSolve when events are on. Returns whether touching changed on a
 // non-sensor contact (which wakes both bodies, src/dynamics/b2_contact.cpp:183-188).
 __device__ __forceinline__ bool update_contact(const KernelArgs& a, int64_t i, int w, int2 f, int ba, int bb,
-                                               uint32_t extra_flags) {
+                                               uint32_t extra_flags, bool sensor) {
   uint32_t flags = a.cflags[i];
   bool wasTouching = (flags & B2G_CONTACT_TOUCHING) != 0;
   flags |= B2G_CONTACT_ENABLED | extra_flags;
   b2g_manifold old = ld_manifold(&a.cman[i]);
-  bool sensor = a.fsensor[f.x] || a.fsensor[f.y];
   bool touching = false;
   b2g_manifold nm;
-  if (sensor) {
+  if (sensor) {  // no manifold: touching is the shapes' overlap (b2_contact.cpp:145-152)
     nm = old;
     nm.point_count = 0;
+    touching = sensor_overlap(a.shape[f.x], ldXf(a.xf, ba), a.shape[f.y], ldXf(a.xf, bb));
   } else {
     const b2g_shape& sA = a.shape[f.x];
     const b2g_shape& sB = a.shape[f.y];
@@ -100,18 +106,22 @@ __device__ __forceinline__ bool mark_wake(const KernelArgs& a, int b) {
 // b2ContactManager::Collide (src/dynamics/b2_contact_manager.cpp:66-116) over every contact of
 // every active world. In sleep-mode worlds a contact is updated only when one of its bodies is
 // awake (static bodies never are); wakes are marked, not applied, so every contact of this pass
-// sees the awake flags the step started with.
+// sees the awake flags the step started with. Sensor contacts go through a pass of their own
+// (SENSORS = true, launched only when the layout has sensors), which keeps the overlap test's
+// state out of the manifold pass's registers.
+template <bool SENSORS>
 __global__ void k_collide(KernelArgs a) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= (int64_t)a.counters[B2G_CNT_CONTACTS]) return;
   int2 f = a.cfix[i];
+  if ((a.fsensor[f.x] || a.fsensor[f.y]) != SENSORS) return;
   int w = a.fworld[f.x];
   const int wf = a.wflags[w];
   if ((wf & B2G_WF_ACTIVE) == 0) return;
   const int ba = a.fbody[f.x], bb = a.fbody[f.y];
   const bool sleepMode = (wf & B2G_WF_SLEEPMODE) != 0;
   if (sleepMode && !((a.bstate[ba].x | a.bstate[bb].x) & B2G_BS_AWAKE)) return;
-  if (update_contact(a, i, w, f, ba, bb, 0u) && sleepMode) {
+  if (update_contact(a, i, w, f, ba, bb, 0u, SENSORS) && sleepMode) {
     mark_wake(a, ba);
     mark_wake(a, bb);
   }
@@ -146,7 +156,7 @@ __global__ void k_collide_closure(KernelArgs a) {
       const int ba = a.fbody[f.x], bb = a.fbody[f.y];
       if ((a.bstate[ba].x | a.bstate[bb].x) & B2G_BS_AWAKE) continue;  // updated by k_collide
       if (!a.bwake[ba] && !a.bwake[bb]) continue;
-      if (update_contact(a, i, w, f, ba, bb, B2G_CONTACT_CLOSURE)) {
+      if (update_contact(a, i, w, f, ba, bb, B2G_CONTACT_CLOSURE, a.fsensor[f.x] || a.fsensor[f.y])) {
         if (mark_wake(a, ba)) changed = 1;
         if (mark_wake(a, bb)) changed = 1;
       }
@@ -642,7 +652,8 @@ __global__ void k_collide_pairs(const b2g_shape* sa, const float* xa, const b2g_
 static inline unsigned grid_for(int64_t n, int bs) { return (unsigned)((n + bs - 1) / bs); }
 
 void launch_collide(const KernelArgs& a, int nw, cudaStream_t s) {
-  if (a.ccap > 0) k_collide<<<grid_for(a.ccap, 128), 128, 0, s>>>(a);
+  if (a.ccap > 0) k_collide<false><<<grid_for(a.ccap, 128), 128, 0, s>>>(a);
+  if (a.ccap > 0 && a.any_sensor) k_collide<true><<<grid_for(a.ccap, 128), 128, 0, s>>>(a);
   if (a.ccap > 0 && a.any_sleep && nw > 0) k_collide_closure<<<nw, 256, 0, s>>>(a);
 }
 void launch_clear_forces(const KernelArgs& a, int nb, cudaStream_t s) {

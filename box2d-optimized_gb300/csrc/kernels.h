@@ -121,6 +121,7 @@ struct KernelArgs {
   int64_t event_cap;
   int events_on;
   int any_sleep;       // some world runs in sleep mode (dead contacts may wake bodies)
+  int any_sensor;      // the layout has sensor fixtures (their contacts get an overlap pass)
   unsigned long long* counters;
   unsigned int* status;
 

@@ -288,9 +288,10 @@ inline Counts ChainsOverPile(b2World* world, int nchains, int links, int ncircle
 
 // `rigs` rigs side by side over one ground edge, each: a cantilever of three boxes welded to a
 // static post (a rigid weld, then two soft ones); a car whose chassis rides on two sprung wheel
-// joints (rear motorised, front with translation limits) driving along the ground; a box that a
-// motor joint drives toward an offset from a static anchor; a sliding box held back by a friction
-// joint; a box pulled up toward a point by a mouse joint; two boxes hanging from a pulley.
+// joints (rear motorised, front with translation limits) driving along the ground and carrying a
+// sensor disc; a box that a motor joint drives toward an offset from a static anchor; a sliding
+// box held back by a friction joint through a static sensor gate; a box pulled up toward a point
+// by a mouse joint; two boxes hanging from a pulley.
 inline Counts JointZoo(b2World* world, int rigs, uint32_t seed, float friction = 0.6f) {
   Counts c;
   Rng rng(seed);
@@ -352,6 +353,14 @@ inline Counts JointZoo(b2World* world, int rigs, uint32_t seed, float friction =
     {
       float cx = x0 + 6.0f;
       b2Body* chassis = dynamicBox(cx, 1.4f, 0.0f);
+      b2CircleShape disc;  // a sensor reaching below the chassis: touches the ground edge
+      disc.m_radius = 1.3f;
+      b2FixtureDef sfd;
+      sfd.shape = &disc;
+      sfd.isSensor = true;
+      sfd.density = 0.0f;
+      MakeFixture(chassis, &sfd);
+      c.fixtures++;
       b2CircleShape wheel;
       wheel.m_radius = 0.35f;
       b2FixtureDef wfd;
@@ -397,8 +406,16 @@ inline Counts JointZoo(b2World* world, int rigs, uint32_t seed, float friction =
       world->CreateJoint(&jd);
       c.joints++;
     }
-    // friction joint holding back a box thrown along the ground
+    // friction joint holding back a box thrown along the ground through a sensor gate
     {
+      b2Body* gate = staticPost(x0 + 17.5f, 2.0f);
+      b2PolygonShape gs;
+      gs.SetAsBox(0.4f, 2.0f);
+      b2FixtureDef gfd;
+      gfd.shape = &gs;
+      gfd.isSensor = true;
+      MakeFixture(gate, &gfd);
+      c.fixtures++;
       b2Body* b = dynamicBox(x0 + 16.0f, 0.25f, 0.0f);
       b->SetLinearVelocity(b2Vec2(6.0f + jit, 0.0f));
       b->SetAngularVelocity(3.0f);

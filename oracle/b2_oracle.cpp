@@ -1180,6 +1180,114 @@ static void updatePairs(World* w) {
   w->contacts.swap(next);
 }
 
+// ---- GJK distance (src/collision/b2_distance.cpp:31-579) for b2TestOverlap
+// (src/collision/b2_collision.cpp:239-258): empty simplex cache, radii applied.
+struct SV { V2 wA, wB, w; float a; int iA, iB; };
+static int gjkCount(const Shape& s) { return s.type == 0 ? 1 : (s.type == 1 ? 2 : s.count); }
+static V2 gjkVertex(const Shape& s, int i) { return s.v[i]; }  // circle p, edge v1 v2, polygon vertices
+static int gjkSupport(const Shape& s, V2 d) {
+  int best = 0;
+  float bestValue = dot(gjkVertex(s, 0), d);
+  for (int i = 1; i < gjkCount(s); ++i) {
+    float value = dot(gjkVertex(s, i), d);
+    if (value > bestValue) { best = i; bestValue = value; }
+  }
+  return best;
+}
+static float gjkDistance(const Shape& A, const Xf& xfA, const Shape& B, const Xf& xfB) {
+  SV sv[3];
+  int n = 1;
+  sv[0].iA = 0; sv[0].iB = 0;
+  sv[0].wA = mul(xfA, gjkVertex(A, 0));
+  sv[0].wB = mul(xfB, gjkVertex(B, 0));
+  sv[0].w = sv[0].wB - sv[0].wA;
+  sv[0].a = 1.0f;
+  int saveA[3], saveB[3];
+  int iter = 0;
+  while (iter < 20) {
+    int saveCount = n;
+    for (int i = 0; i < saveCount; ++i) { saveA[i] = sv[i].iA; saveB[i] = sv[i].iB; }
+    if (n == 2) {  // b2Simplex::Solve2
+      V2 w1 = sv[0].w, w2 = sv[1].w, e12 = w2 - w1;
+      float d12_2 = -dot(w1, e12);
+      if (d12_2 <= 0.0f) { sv[0].a = 1.0f; n = 1; }
+      else {
+        float d12_1 = dot(w2, e12);
+        if (d12_1 <= 0.0f) { sv[1].a = 1.0f; n = 1; sv[0] = sv[1]; }
+        else {
+          float inv = 1.0f / (d12_1 + d12_2);
+          sv[0].a = d12_1 * inv; sv[1].a = d12_2 * inv; n = 2;
+        }
+      }
+    } else if (n == 3) {  // b2Simplex::Solve3
+      V2 w1 = sv[0].w, w2 = sv[1].w, w3 = sv[2].w;
+      V2 e12 = w2 - w1;
+      float d12_1 = dot(w2, e12), d12_2 = -dot(w1, e12);
+      V2 e13 = w3 - w1;
+      float d13_1 = dot(w3, e13), d13_2 = -dot(w1, e13);
+      V2 e23 = w3 - w2;
+      float d23_1 = dot(w3, e23), d23_2 = -dot(w2, e23);
+      float n123 = cross(e12, e13);
+      float d123_1 = n123 * cross(w2, w3);
+      float d123_2 = n123 * cross(w3, w1);
+      float d123_3 = n123 * cross(w1, w2);
+      if (d12_2 <= 0.0f && d13_2 <= 0.0f) { sv[0].a = 1.0f; n = 1; }
+      else if (d12_1 > 0.0f && d12_2 > 0.0f && d123_3 <= 0.0f) {
+        float inv = 1.0f / (d12_1 + d12_2);
+        sv[0].a = d12_1 * inv; sv[1].a = d12_2 * inv; n = 2;
+      } else if (d13_1 > 0.0f && d13_2 > 0.0f && d123_2 <= 0.0f) {
+        float inv = 1.0f / (d13_1 + d13_2);
+        sv[0].a = d13_1 * inv; sv[2].a = d13_2 * inv; n = 2; sv[1] = sv[2];
+      } else if (d12_1 <= 0.0f && d23_2 <= 0.0f) { sv[1].a = 1.0f; n = 1; sv[0] = sv[1]; }
+      else if (d13_1 <= 0.0f && d23_1 <= 0.0f) { sv[2].a = 1.0f; n = 1; sv[0] = sv[2]; }
+      else if (d23_1 > 0.0f && d23_2 > 0.0f && d123_1 <= 0.0f) {
+        float inv = 1.0f / (d23_1 + d23_2);
+        sv[1].a = d23_1 * inv; sv[2].a = d23_2 * inv; n = 2; sv[0] = sv[2];
+      } else {
+        float inv = 1.0f / (d123_1 + d123_2 + d123_3);
+        sv[0].a = d123_1 * inv; sv[1].a = d123_2 * inv; sv[2].a = d123_3 * inv; n = 3;
+      }
+    }
+    if (n == 3) break;
+    V2 d;
+    if (n == 1) d = -sv[0].w;
+    else {
+      V2 e12 = sv[1].w - sv[0].w;
+      float sgn = cross(e12, -sv[0].w);
+      d = sgn > 0.0f ? cross(1.0f, e12) : cross(e12, 1.0f);
+    }
+    if (lengthSq(d) < kEpsilon * kEpsilon) break;
+    SV& nv = sv[n];
+    nv.iA = gjkSupport(A, mulT(xfA.q, -d));
+    nv.wA = mul(xfA, gjkVertex(A, nv.iA));
+    nv.iB = gjkSupport(B, mulT(xfB.q, d));
+    nv.wB = mul(xfB, gjkVertex(B, nv.iB));
+    nv.w = nv.wB - nv.wA;
+    ++iter;
+    bool duplicate = false;
+    for (int i = 0; i < saveCount; ++i)
+      if (nv.iA == saveA[i] && nv.iB == saveB[i]) { duplicate = true; break; }
+    if (duplicate) break;
+    ++n;
+  }
+  V2 pA, pB;
+  if (n == 1) { pA = sv[0].wA; pB = sv[0].wB; }
+  else if (n == 2) {
+    pA = sv[0].a * sv[0].wA + sv[1].a * sv[1].wA;
+    pB = sv[0].a * sv[0].wB + sv[1].a * sv[1].wB;
+  } else {
+    pA = sv[0].a * sv[0].wA + sv[1].a * sv[1].wA + sv[2].a * sv[2].wA;
+    pB = pA;
+  }
+  float distance = lengthOf(pA - pB);
+  float rA = A.radius, rB = B.radius;
+  if (distance > rA + rB && distance > kEpsilon) return distance - (rA + rB);
+  return 0.0f;
+}
+static bool testOverlap(const Shape& A, const Xf& xfA, const Shape& B, const Xf& xfB) {
+  return gjkDistance(A, xfA, B, xfB) < 10.0f * kEpsilon;
+}
+
 // b2Contact::Update (src/dynamics/b2_contact.cpp:126-210) for one contact; returns whether
 // touching changed on a non-sensor contact (which wakes both bodies, :183-188).
 static bool updateContact(World* w, Contact& c) {
@@ -1190,6 +1298,7 @@ static bool updateContact(World* w, Contact& c) {
   const Fixture& fb = w->fixtures[c.fB];
   bool touching = false;
   if (fa.sensor || fb.sensor) {
+    touching = testOverlap(fa.shape, w->bodies[fa.body].xf, fb.shape, w->bodies[fb.body].xf);
     c.m.pointCount = 0;
   } else {
     evaluate(&c.m, fa.shape, w->bodies[fa.body].xf, fb.shape, w->bodies[fb.body].xf);
@@ -2816,6 +2925,16 @@ int orc_shape_aabb(const b2g_shape* s, const float* xf, float* out4) {
   AABB bb = computeAABB(shapeFrom(*s), t);
   out4[0] = bb.lo.x; out4[1] = bb.lo.y; out4[2] = bb.hi.x; out4[3] = bb.hi.y;
   return 0;
+}
+
+// GJK distance with radii (distance out) and b2TestOverlap (returned) of two shapes.
+int orc_test_overlap(const b2g_shape* sa, const float* xfa, const b2g_shape* sb, const float* xfb, float* distance) {
+  Shape A = shapeFrom(*sa), B = shapeFrom(*sb);
+  Xf ta, tb;
+  ta.p = v2(xfa[0], xfa[1]); ta.q.s = xfa[2]; ta.q.c = xfa[3];
+  tb.p = v2(xfb[0], xfb[1]); tb.q.s = xfb[2]; tb.q.c = xfb[3];
+  *distance = gjkDistance(A, ta, B, tb);
+  return testOverlap(A, ta, B, tb) ? 1 : 0;
 }
 
 int orc_collide(const b2g_shape* sa, const float* xfa, const b2g_shape* sb, const float* xfb, b2g_manifold* out) {

@@ -21,6 +21,7 @@
 #define private public
 #define protected public
 #include "box2d/box2d.h"
+#include "box2d/b2_distance.h"
 #include "dynamics/b2_contact_solver.h"
 #include "dynamics/b2_island.h"
 #include "box2d/b2_stack_allocator.h"
@@ -176,6 +177,25 @@ int ref_collide(const b2g_shape* sa, const float* xfa, const b2g_shape* sb, cons
     return 1;
   manifold_out(m, out);
   return 0;
+}
+
+// b2Distance with radii between two shapes (distance out) and b2TestOverlap (returned).
+int ref_test_overlap(const b2g_shape* sa, const float* xfa, const b2g_shape* sb, const float* xfb, float* distance) {
+  AnyShape a, b;
+  shape_to_ref(sa, &a);
+  shape_to_ref(sb, &b);
+  b2DistanceInput input;
+  input.proxyA.Set(a.ptr);
+  input.proxyB.Set(b.ptr);
+  input.transformA = xf_from(xfa);
+  input.transformB = xf_from(xfb);
+  input.useRadii = true;
+  b2SimplexCache cache;
+  cache.count = 0;
+  b2DistanceOutput output;
+  b2Distance(&output, &cache, &input);
+  *distance = output.distance;
+  return b2TestOverlap(a.ptr, b.ptr, xf_from(xfa), xf_from(xfb)) ? 1 : 0;
 }
 
 // b2WorldManifold::Initialize (src/collision/b2_collision.cpp:26-90): out = normal(2), points(4),

@@ -142,6 +142,7 @@ def test_oracle_replay_vs_reference_live(ref, orc, kind, n, seed, p0, warm, vi, 
     rw = ob.RefWorld(ref, kind, seed=seed, n=n, p0=p0, p1=0.6)
     rw.step(warm, vi=vi, pi=pi)
     orc.orc_set_libm_trig(1)
+    sensor_touching = 0
     try:
         for _ in range(3):
             ow = ob.OracleWorld(orc, (0.0, -10.0), list(rw.bodies()), list(rw.fixtures()), list(rw.joints()),
@@ -155,8 +156,17 @@ def test_oracle_replay_vs_reference_live(ref, orc, kind, n, seed, p0, warm, vi, 
             rset = sorted((min(c.fixture_a, c.fixture_b), max(c.fixture_a, c.fixture_b)) for c in rw.contacts())
             oset = sorted((min(c.fixture_a, c.fixture_b), max(c.fixture_a, c.fixture_b)) for c in ow.contacts())
             assert rset == oset
+            # sensor contacts: touching is the GJK overlap (b2TestOverlap) on both sides
+            sensors = {i for i, f in enumerate(rw.fixtures()) if f.is_sensor}
+            key = lambda c: (min(c.fixture_a, c.fixture_b), max(c.fixture_a, c.fixture_b))  # noqa: E731
+            rs = {key(c): c.flags & 2 for c in rw.contacts() if {c.fixture_a, c.fixture_b} & sensors}
+            os_ = {key(c): c.flags & 2 for c in ow.contacts() if {c.fixture_a, c.fixture_b} & sensors}
+            assert rs == os_
+            sensor_touching += sum(1 for v in rs.values() if v)
     finally:
         orc.orc_set_libm_trig(0)
+    if kind == G.SCENE_JOINTS and warm >= 40:  # the sensors touch once the rigs have moved
+        assert sensor_touching > 0
 
 
 @pytest.mark.parametrize("kind,n,seed,p0", [
@@ -261,3 +271,44 @@ def test_oracle_sleep_replay_vs_reference_live(ref, orc, kind, n, seed, p0, warm
     assert asleep_seen > 0 and transitions > 0
     if warm in (468, 466, 740):
         assert woken > 0
+
+
+def _random_shape(ref, rng, kind):
+    s = G.Shape()
+    if kind == 0:
+        s.type = 0
+        s.radius = float(np.float32(rng.uniform(0.05, 1.0)))
+        s.vertices[0][0], s.vertices[0][1] = (float(np.float32(v)) for v in rng.uniform(-0.3, 0.3, 2))
+    elif kind == 1:
+        s.type = 1
+        s.radius = 0.01
+        a, b = rng.uniform(-1.5, 1.5, 2), rng.uniform(-1.5, 1.5, 2)
+        s.vertices[0][0], s.vertices[0][1] = (float(np.float32(v)) for v in a)
+        s.vertices[1][0], s.vertices[1][1] = (float(np.float32(v)) for v in b)
+    else:
+        n = int(rng.integers(3, 9))
+        xy = rng.uniform(-1, 1, 2 * n).astype(np.float32)
+        ref.ref_polygon_set(xy.ctypes.data_as(C.POINTER(C.c_float)), n, s)
+    return s
+
+
+def test_oracle_overlap_vs_reference_live(ref, orc):
+    """b2TestOverlap (GJK b2Distance with radii) of the oracle against the reference on random
+    circle / edge / polygon pairs placed from well apart to interpenetrating: identical overlap
+    decisions and bit-identical distances."""
+    rng = np.random.default_rng(2024)
+    overlaps = 0
+    for k in range(3000):
+        ka, kb = int(rng.integers(0, 3)), int(rng.integers(0, 3))
+        a, b = _random_shape(ref, rng, ka), _random_shape(ref, rng, kb)
+        xa = (C.c_float * 4)(*[float(np.float32(v)) for v in (0.0, 0.0, 0.0, 1.0)])
+        ang = rng.uniform(-3.14, 3.14)
+        d = rng.uniform(0.0, 3.0)
+        th = rng.uniform(-3.14, 3.14)
+        xb = (C.c_float * 4)(*[float(np.float32(v)) for v in (d * np.cos(th), d * np.sin(th), np.sin(ang), np.cos(ang))])
+        dr, do = C.c_float(), C.c_float()
+        r = ref.ref_test_overlap(a, xa, b, xb, C.byref(dr))
+        o = orc.orc_test_overlap(a, xa, b, xb, C.byref(do))
+        assert (r, dr.value) == (o, do.value), (k, ka, kb)
+        overlaps += r
+    assert 300 < overlaps < 2700
