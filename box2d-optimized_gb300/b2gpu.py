@@ -124,7 +124,9 @@ class Profile(C.Structure):
     _fields_ = [("step", C.c_float), ("collide", C.c_float), ("solve", C.c_float),
                 ("broadphase", C.c_float), ("solve_toi", C.c_float), ("bodies", C.c_int64),
                 ("fixtures", C.c_int64), ("contacts", C.c_int64), ("touching", C.c_int64),
-                ("joints", C.c_int64), ("colors_max", C.c_int64), ("touching_total", C.c_int64)]
+                ("joints", C.c_int64), ("colors_max", C.c_int64), ("touching_total", C.c_int64),
+                ("host_step", C.c_float), ("host_admit_upload", C.c_float),
+                ("host_admit_broadphase", C.c_float), ("host_grow", C.c_float)]
 
 
 class RayHit(C.Structure):
@@ -156,12 +158,15 @@ def body_array_to_numpy(arr) -> dict:
 class Server:
     """Continuous-batching rollout server (b2g_server)."""
 
-    def __init__(self, lib, device=0, budget_bytes=120 << 30, max_worlds=4096, dt=1 / 60, vi=8, pi=3):
+    def __init__(self, lib, device=0, budget_bytes=120 << 30, max_worlds=4096, dt=1 / 60, vi=8, pi=3,
+                 builders=None):
         self.lib = lib
         h = C.c_void_p()
         lib.check(lib.b2g_server_create(device, budget_bytes, max_worlds, dt, vi, pi, C.byref(h)),
                   "b2g_server_create")
         self.h = h
+        if builders is not None:
+            lib.check(lib.b2g_server_set_builders(h, builders), "b2g_server_set_builders")
 
     def close(self):
         if self.h:
@@ -234,7 +239,8 @@ class Lib:
         "b2g_server_tick", "b2g_server_poll", "b2g_server_stats", "b2g_status_string",
         "b2g_last_error", "b2g_device_count", "b2g_query_aabb", "b2g_raycast_closest", "b2g_world_status",
         "b2g_world_snapshot", "b2g_world_restore", "b2g_server_cancel", "b2g_body_set_awake",
-        "b2g_bodies_sleep_time_read", "b2g_world_get_flags",
+        "b2g_bodies_sleep_time_read", "b2g_world_get_flags", "b2g_server_batch", "b2g_step_begin",
+        "b2g_step_poll", "b2g_step_end", "b2g_batch_stage", "b2g_server_set_builders",
     ]
 
     def __init__(self, path: os.PathLike | str | None = None):
@@ -282,6 +288,12 @@ class Lib:
             "b2g_batch_autotune": ([vp, i32, f32, i32, i32, P(i32), P(i32)], C.c_int),
             "b2g_world_status": ([vp, i32, P(i32)], C.c_int),
             "b2g_server_cancel": ([vp, i64], C.c_int),
+            "b2g_server_batch": ([vp, P(vp)], C.c_int),
+            "b2g_step_begin": ([vp, f32, i32, i32, P(C.c_uint8)], C.c_int),
+            "b2g_step_poll": ([vp, P(i32)], C.c_int),
+            "b2g_step_end": ([vp], C.c_int),
+            "b2g_batch_stage": ([vp], C.c_int),
+            "b2g_server_set_builders": ([vp, i32], C.c_int),
             "b2g_batch_set_debug_checks": ([vp, i32], C.c_int),
             "b2g_body_set_awake": ([vp, i32, i32, i32], C.c_int),
             "b2g_world_get_flags": ([vp, i32, P(i32), P(i32), P(i32), P(i32)], C.c_int),
@@ -367,6 +379,26 @@ class Batch:
             arr = (C.c_uint8 * len(mask))(*[1 if x else 0 for x in mask])
             m = C.cast(arr, C.POINTER(C.c_uint8))
         self.lib.check(self.lib.b2g_step(self.h, dt, vi, pi, m), "b2g_step")
+
+    def step_begin(self, dt=1 / 60, vi=8, pi=3, mask=None):
+        """Launches one step and returns at once (b2g_step_begin); finish it with step_end."""
+        self._mask = None
+        if mask is not None:
+            self._mask = (C.c_uint8 * len(mask))(*[1 if x else 0 for x in mask])
+        m = C.cast(self._mask, C.POINTER(C.c_uint8)) if self._mask is not None else None
+        self.lib.check(self.lib.b2g_step_begin(self.h, dt, vi, pi, m), "b2g_step_begin")
+
+    def step_done(self) -> bool:
+        d = C.c_int32()
+        self.lib.check(self.lib.b2g_step_poll(self.h, C.byref(d)), "b2g_step_poll")
+        return bool(d.value)
+
+    def step_end(self):
+        self.lib.check(self.lib.b2g_step_end(self.h), "b2g_step_end")
+
+    def stage(self):
+        """Packs the worlds not on the device yet for the next step's upload (b2g_batch_stage)."""
+        self.lib.check(self.lib.b2g_batch_stage(self.h), "b2g_batch_stage")
 
     def step_n(self, n, dt=1 / 60, vi=8, pi=3, use_graph=False):
         self.lib.check(self.lib.b2g_step_n(self.h, dt, vi, pi, n, int(use_graph)), "b2g_step_n")

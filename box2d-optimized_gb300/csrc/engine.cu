@@ -41,6 +41,11 @@ void set_error(Batch* b, const std::string& msg) {
   if (b) b->error = msg;
 }
 
+static int locked(Batch* b) {
+  set_error(b, "the batch is in a step (between b2g_step_begin and b2g_step_end)");
+  return B2G_E_LOCKED;
+}
+
 #define CUDA_TRY(b, call)                                                                       \
   do {                                                                                          \
     cudaError_t e_ = (call);                                                                    \
@@ -467,59 +472,52 @@ struct Stager {
   }
 };
 
-// Appends the worlds [NW, worlds.size()) that are not on the device yet after the existing
-// layout, without touching the live state of the others: body / fixture / joint arrays grow in
-// place and only the new segments are copied; the world table is rewritten (small); the new
-// worlds' contacts are found by the next step's broadphase.
-int upload_tail(Batch* b) {
-  CUDA_TRY(b, cudaSetDevice(b->device));
-  int w0 = b->NW, NW = (int)b->worlds.size();
-  int NB0 = b->NB, NF0 = b->NF, NJ0 = b->NJ;
-  std::vector<float4> xf, pos, vel, massd, damp, force;
-  std::vector<float2> lc;
-  std::vector<int> btype, bworld, fbody, fgroup, fsensor, fworld;
-  std::vector<int2> bstate;
-  std::vector<float> frad;
-  std::vector<b2g_shape> shape;
-  std::vector<uint32_t> ffilter;
-  std::vector<float4> fmat, wg_tail;
-  std::vector<JointDev> joints;
-  std::vector<uint64_t> nocol;
-  b->h_body_off.resize(NW + 1);
-  b->h_fix_off.resize(NW + 1);
-  b->h_joint_off.resize(NW + 1);
-  int NB = NB0, NF = NF0, NJ = NJ0;
-  for (int w = w0; w < NW; ++w) {
+// Packs the worlds [NW, worlds.size()) that are not on the device yet into device layout, after
+// the current layout: host work only, so that it can run while a step executes on the device.
+static int pack_tail(Batch* b, TailPack& P) {
+  P = TailPack();
+  P.w0 = b->NW;
+  P.w1 = (int)b->worlds.size();
+  P.NB0 = b->NB; P.NF0 = b->NF; P.NJ0 = b->NJ;
+  int NB = P.NB0, NF = P.NF0, NJ = P.NJ0;
+  size_t nb = 0, nf = 0, nj = 0;
+  for (int w = P.w0; w < P.w1; ++w) {
+    nb += b->worlds[w].bodies.size(); nf += b->worlds[w].fixtures.size(); nj += b->worlds[w].joints.size();
+  }
+  P.xf.reserve(nb); P.pos.reserve(nb); P.vel.reserve(nb); P.massd.reserve(nb); P.damp.reserve(nb);
+  P.force.reserve(nb); P.lc.reserve(nb); P.btype.reserve(nb); P.bworld.reserve(nb); P.bstate.reserve(nb);
+  P.shape.reserve(nf); P.frad.reserve(nf); P.fbody.reserve(nf); P.fgroup.reserve(nf); P.fsensor.reserve(nf);
+  P.fworld.reserve(nf); P.ffilter.reserve(nf); P.fmat.reserve(nf); P.joints.reserve(nj);
+  for (int w = P.w0; w < P.w1; ++w) {
     const HostWorld& hw = b->worlds[w];
     if (hw.bodies.size() >= kMaxWorldBodies) {
       set_error(b, "a world has more bodies than the solver's 24-bit body index allows");
       return B2G_E_CAPACITY;
     }
-    int bo = NB, fo = NF, jo = NJ;
-    b->h_body_off[w] = bo; b->h_fix_off[w] = fo; b->h_joint_off[w] = jo;
-    wg_tail.push_back(make_float4(hw.gx, hw.gy, hw.inv_dt0, 0.0f));
+    int bo = NB;
+    P.body_off.push_back(NB); P.fix_off.push_back(NF); P.joint_off.push_back(NJ);
     for (size_t i = 0; i < hw.bodies.size(); ++i) {
       const b2g_body& s = hw.bodies[i];
-      bstate.push_back(body_state(hw, i));
-      xf.push_back(make_float4(s.xf[0], s.xf[1], s.xf[2], s.xf[3]));
-      pos.push_back(make_float4(s.c[0], s.c[1], s.a, 0.0f));
-      vel.push_back(make_float4(s.v[0], s.v[1], s.w, 0.0f));
-      massd.push_back(make_float4(s.mass, s.inv_mass, s.inertia, s.inv_inertia));
-      damp.push_back(make_float4(s.linear_damping, s.angular_damping, s.gravity_scale, 0.0f));
-      force.push_back(make_float4(s.force[0], s.force[1], s.torque, 0.0f));
-      lc.push_back(make_float2(s.local_center[0], s.local_center[1]));
-      btype.push_back(s.type);
-      bworld.push_back(w);
+      P.bstate.push_back(body_state(hw, i));
+      P.xf.push_back(make_float4(s.xf[0], s.xf[1], s.xf[2], s.xf[3]));
+      P.pos.push_back(make_float4(s.c[0], s.c[1], s.a, 0.0f));
+      P.vel.push_back(make_float4(s.v[0], s.v[1], s.w, 0.0f));
+      P.massd.push_back(make_float4(s.mass, s.inv_mass, s.inertia, s.inv_inertia));
+      P.damp.push_back(make_float4(s.linear_damping, s.angular_damping, s.gravity_scale, 0.0f));
+      P.force.push_back(make_float4(s.force[0], s.force[1], s.torque, 0.0f));
+      P.lc.push_back(make_float2(s.local_center[0], s.local_center[1]));
+      P.btype.push_back(s.type);
+      P.bworld.push_back(w);
     }
     for (const b2g_fixture& f : hw.fixtures) {
-      shape.push_back(f.shape);
-      frad.push_back(f.shape.radius);
-      fbody.push_back(bo + f.body);
-      fgroup.push_back(f.group_index);
-      fsensor.push_back(f.is_sensor ? 1 : 0);
-      fworld.push_back(w);
-      ffilter.push_back((uint32_t)f.category_bits | ((uint32_t)f.mask_bits << 16));
-      fmat.push_back(make_float4(f.friction, f.restitution, f.restitution_threshold, f.density));
+      P.shape.push_back(f.shape);
+      P.frad.push_back(f.shape.radius);
+      P.fbody.push_back(bo + f.body);
+      P.fgroup.push_back(f.group_index);
+      P.fsensor.push_back(f.is_sensor ? 1 : 0);
+      P.fworld.push_back(w);
+      P.ffilter.push_back((uint32_t)f.category_bits | ((uint32_t)f.mask_bits << 16));
+      P.fmat.push_back(make_float4(f.friction, f.restitution, f.restitution_threshold, f.density));
     }
     for (const b2g_joint& j : hw.joints) {
       JointDev d;
@@ -530,20 +528,43 @@ int upload_tail(Batch* b) {
       d.impulse[0] = j.impulse[0]; d.impulse[1] = j.impulse[1]; d.impulse[2] = j.impulse[2];
       d.motorImpulse = j.motor_impulse; d.lowerImpulse = j.lower_impulse; d.upperImpulse = j.upper_impulse;
       init_joint_dev(j.def, &d);
-      joints.push_back(d);
+      P.joints.push_back(d);
       if (!j.def.collide_connected) {
         uint32_t x = (uint32_t)(bo + j.def.body_a), y = (uint32_t)(bo + j.def.body_b);
         if (x > y) std::swap(x, y);
-        nocol.push_back(((uint64_t)x << 32) | y);
+        P.nocol.push_back(((uint64_t)x << 32) | y);
       }
     }
     NB += (int)hw.bodies.size();
     NF += (int)hw.fixtures.size();
     NJ += (int)hw.joints.size();
   }
+  std::sort(P.nocol.begin(), P.nocol.end());
+  P.nocol.erase(std::unique(P.nocol.begin(), P.nocol.end()), P.nocol.end());
+  P.NB = NB; P.NF = NF; P.NJ = NJ;
+  P.valid = true;
+  return B2G_OK;
+}
+
+// Uploads the packed worlds after the existing layout without touching the live state of the
+// others: body / fixture / joint arrays grow in place and only the new segments are copied; the
+// world table is rewritten (small); the new worlds' contacts are found by a broadphase of their
+// own or by the step's closing broadphase.
+static int flush_tail(Batch* b, TailPack& P) {
+  CUDA_TRY(b, cudaSetDevice(b->device));
+  const int w0 = P.w0, NW = P.w1;
+  const int NB0 = P.NB0, NF0 = P.NF0, NJ0 = P.NJ0, NB = P.NB, NF = P.NF, NJ = P.NJ;
+  b->h_body_off.resize(NW + 1);
+  b->h_fix_off.resize(NW + 1);
+  b->h_joint_off.resize(NW + 1);
+  std::vector<float4> wg_tail;
+  for (int w = w0; w < NW; ++w) {
+    b->h_body_off[w] = P.body_off[w - w0]; b->h_fix_off[w] = P.fix_off[w - w0];
+    b->h_joint_off[w] = P.joint_off[w - w0];
+    const HostWorld& hw = b->worlds[w];
+    wg_tail.push_back(make_float4(hw.gx, hw.gy, hw.inv_dt0, 0.0f));
+  }
   b->h_body_off[NW] = NB; b->h_fix_off[NW] = NF; b->h_joint_off[NW] = NJ;
-  std::sort(nocol.begin(), nocol.end());
-  nocol.erase(std::unique(nocol.begin(), nocol.end()), nocol.end());
   // world table: offsets are static, gravity/inv_dt0 of existing worlds stay as the device has them
   std::vector<int4> wb(NW), wj(NW);
   std::vector<int> wflags(NW);
@@ -570,18 +591,18 @@ int upload_tail(Batch* b) {
     CUDA_TRY(b, cudaMemsetAsync(b->wfault.p, 0, b->wfault.cap, b->stream));
   }
   TRY(ensure(b, b->jranges, 65 * (size_t)NW, true));
-  TRY(st.add(b, b->xf, NB0, xf)); TRY(st.add(b, b->pos, NB0, pos)); TRY(st.add(b, b->vel, NB0, vel));
-  TRY(st.add(b, b->massd, NB0, massd)); TRY(st.add(b, b->damp, NB0, damp)); TRY(st.add(b, b->force, NB0, force));
-  TRY(st.add(b, b->lc, NB0, lc)); TRY(st.add(b, b->btype, NB0, btype)); TRY(st.add(b, b->bworld, NB0, bworld));
-  TRY(st.add(b, b->bstate, NB0, bstate));
-  TRY(st.add(b, b->shape, NF0, shape)); TRY(st.add(b, b->fbody, NF0, fbody)); TRY(st.add(b, b->fgroup, NF0, fgroup));
-  TRY(st.add(b, b->fsensor, NF0, fsensor)); TRY(st.add(b, b->fworld, NF0, fworld));
-  if (std::find(fsensor.begin(), fsensor.end(), 1) != fsensor.end()) b->any_sensor = true;
-  TRY(st.add(b, b->frad, NF0, frad));
-  TRY(st.add(b, b->ffilter, NF0, ffilter)); TRY(st.add(b, b->fmat, NF0, fmat));
-  TRY(st.add(b, b->joints, NJ0, joints)); TRY(st.add(b, b->nocollide, b->n_nocollide, nocol));
+  TRY(st.add(b, b->xf, NB0, P.xf)); TRY(st.add(b, b->pos, NB0, P.pos)); TRY(st.add(b, b->vel, NB0, P.vel));
+  TRY(st.add(b, b->massd, NB0, P.massd)); TRY(st.add(b, b->damp, NB0, P.damp)); TRY(st.add(b, b->force, NB0, P.force));
+  TRY(st.add(b, b->lc, NB0, P.lc)); TRY(st.add(b, b->btype, NB0, P.btype)); TRY(st.add(b, b->bworld, NB0, P.bworld));
+  TRY(st.add(b, b->bstate, NB0, P.bstate));
+  TRY(st.add(b, b->shape, NF0, P.shape)); TRY(st.add(b, b->fbody, NF0, P.fbody)); TRY(st.add(b, b->fgroup, NF0, P.fgroup));
+  TRY(st.add(b, b->fsensor, NF0, P.fsensor)); TRY(st.add(b, b->fworld, NF0, P.fworld));
+  if (std::find(P.fsensor.begin(), P.fsensor.end(), 1) != P.fsensor.end()) b->any_sensor = true;
+  TRY(st.add(b, b->frad, NF0, P.frad));
+  TRY(st.add(b, b->ffilter, NF0, P.ffilter)); TRY(st.add(b, b->fmat, NF0, P.fmat));
+  TRY(st.add(b, b->joints, NJ0, P.joints)); TRY(st.add(b, b->nocollide, b->n_nocollide, P.nocol));
   TRY(st.flush(b));
-  b->n_nocollide += (int)nocol.size();
+  b->n_nocollide += (int)P.nocol.size();
   TRY(ensure(b, b->bwake, NB, true)); TRY(ensure(b, b->sl, NB));  // wake marks are zero between steps
   if (b->bwake.cap > (size_t)NB0) CUDA_TRY(b, cudaMemsetAsync(b->bwake.p + NB0, 0, b->bwake.cap - NB0, b->stream));
   TRY(ensure(b, b->aabb, NF)); TRY(ensure(b, b->mkey, NF)); TRY(ensure(b, b->mkey_sorted, NF));
@@ -601,11 +622,28 @@ int upload_tail(Batch* b) {
   // joint colours of the appended worlds; a colouring failure reaches the step's status check
   launch_joint_colour(make_args(b), w0, NW - w0, b->stream);
   b->layout_version++;
+  P.valid = false;
+  return B2G_OK;
+}
+
+// Uploads every world not on the device yet, from a pack prepared by b2g_batch_stage when it
+// still matches the layout (it then covers the worlds that existed when it was made), else from a
+// pack made now.
+int upload_tail(Batch* b) {
+  TailPack& P = b->tail_pack;
+  if (P.valid && P.w0 == b->NW && P.NB0 == b->NB && P.NF0 == b->NF && P.NJ0 == b->NJ &&
+      P.w1 <= (int)b->worlds.size())
+    TRY(flush_tail(b, P));
+  if ((int)b->worlds.size() > b->NW) {
+    TRY(pack_tail(b, P));
+    TRY(flush_tail(b, P));
+  }
   return B2G_OK;
 }
 
 // Copies the live device state (bodies, joints, contacts, inv_dt0) into the host records.
 int download_state(Batch* b) {
+  if (b->in_step) return locked(b);
   if (b->device < 0 || !b->device_state_valid || !b->host_state_stale) return B2G_OK;
   CUDA_TRY(b, cudaSetDevice(b->device));
   int NB = b->NB, NJ = b->NJ, NW = b->NW;
@@ -950,9 +988,20 @@ static int capture_graphs(Batch* b, float dt, int vi, int pi) {
 }
 
 // One b2World::Step (src/dynamics/b2_world.cpp:1108-1171) for the worlds selected by mask.
-int step_batch(Batch* b, float dt, int vi, int pi, const uint8_t* mask, bool sync) {
-  (void)sync;
+static double host_ms_since(std::chrono::steady_clock::time_point t0) {
+  return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+}
+
+// The first half of one b2World::Step (src/dynamics/b2_world.cpp:1108-1171) for the worlds
+// selected by mask: uploads, flags, and the step's launches (or graph replay), without waiting
+// for the device; step_end waits and reads the step's counters.
+static int step_begin(Batch* b, float dt, int vi, int pi, const uint8_t* mask) {
   NvtxRange range("b2g.step");
+  if (b->in_step) return locked(b);
+  b->step_t0 = std::chrono::steady_clock::now();
+  b->profile.host_admit_upload = 0.0f;
+  b->profile.host_admit_broadphase = 0.0f;
+  b->profile.host_grow = 0.0f;
   if (!(dt >= 0.0f) || vi < 0 || pi < 0) {
     set_error(b, "invalid step arguments");
     return B2G_E_INVALID_ARG;
@@ -970,10 +1019,12 @@ int step_batch(Batch* b, float dt, int vi, int pi, const uint8_t* mask, bool syn
     invalidate_graphs(b);
   } else if ((int)b->worlds.size() > b->NW) {
     NvtxRange upload_range("b2g.upload_tail");
+    const auto t0 = std::chrono::steady_clock::now();
     tail_w0 = b->NW;
     tail_f0 = b->NF;
     TRY(upload_tail(b));
     invalidate_graphs(b);
+    b->profile.host_admit_upload = (float)host_ms_since(t0);
   }
   if (b->NW == 0) return B2G_OK;
   if (!b->h_readback) CUDA_TRY(b, cudaMallocHost(&b->h_readback, 8 * sizeof(unsigned long long)));
@@ -1000,14 +1051,33 @@ int step_batch(Batch* b, float dt, int vi, int pi, const uint8_t* mask, bool syn
     b->any_sleep = any_sleep;
     b->layout_version++;  // captured graphs hold the kernel arguments
   }
-  TRY(ensure_contact_capacity(b, b->NC));
+  // appended worlds that this step leaves out (masked) need no broadphase of their own: the
+  // end-of-step broadphase creates their contacts, as FindNewContacts would before their first
+  // step (a step without one keeps them flagged for the next step's initial broadphase)
+  bool tail_masked = false;
+  if (tail_w0 >= 0 && mask) {
+    tail_masked = true;
+    for (int w = tail_w0; w < b->NW; ++w) tail_masked = tail_masked && !mask[w];
+  }
+  if (tail_masked) {
+    b->poff_valid[b->cur] = false;  // the live list's per-fixture offsets do not cover them
+    if (!(dt > 0.0f))
+      for (int w = tail_w0; w < b->NW; ++w) b->worlds[w].flags |= B2G_WF_NEW_CONTACTS;
+  }
+  {
+    const auto t0 = std::chrono::steady_clock::now();
+    TRY(ensure_contact_capacity(b, b->NC));
+    b->profile.host_grow = (float)host_ms_since(t0);
+  }
   CUDA_TRY(b, cudaMemsetAsync(b->counters.p + 1, 0, 4 * sizeof(unsigned long long), b->stream));
   if (b->events_on) b->host_events.clear();
   b->last_dt = dt;
   b->last_vi = vi;
   b->last_pi = pi;
-  if (tail_w0 >= 0) {
+  if (tail_w0 >= 0 && !tail_masked) {
+    const auto t0 = std::chrono::steady_clock::now();
     TRY(tail_broadphase(b, dt, vi, pi, tail_f0, tail_w0));
+    b->profile.host_admit_broadphase = (float)host_ms_since(t0);
     CUDA_TRY(b, cudaMemsetAsync(b->counters.p + 1, 0, 4 * sizeof(unsigned long long), b->stream));
   }
   int entry = b->cur;
@@ -1037,9 +1107,23 @@ int step_batch(Batch* b, float dt, int vi, int pi, const uint8_t* mask, bool syn
   CUDA_TRY(b, cudaGetLastError());
   b->host_state_stale = true;
   if (dt > 0.0f || need_bp) b->tree_valid = true;  // a full broadphase rebuilt every world's tree
+  b->step_graph = graph;
+  b->in_step = true;
+  cudaEventRecord(b->ev[5], b->stream);  // b2g_step_poll's marker
+  return B2G_OK;
+}
+
+// The second half: waits for the step, reads its counters and status (recovering from a pair
+// buffer overflow), and fills the profile.
+static int step_end(Batch* b) {
+  if (!b->in_step) {
+    set_error(b, "no step in flight");
+    return B2G_E_INVALID_ARG;
+  }
+  b->in_step = false;
   int live_before_last_bp = b->cur ^ 1;
   int st = finish_step(b, live_before_last_bp);
-  if (!graph) {
+  if (!b->step_graph) {
     float t_col = 0, t_sol = 0, t_bp = 0;
     cudaEventElapsedTime(&t_col, b->ev[0], b->ev[1]);
     cudaEventElapsedTime(&t_sol, b->ev[1], b->ev[2]);
@@ -1056,13 +1140,21 @@ int step_batch(Batch* b, float dt, int vi, int pi, const uint8_t* mask, bool syn
   b->profile.fixtures = b->NF;
   b->profile.contacts = b->NC;
   b->profile.joints = b->NJ;
+  b->profile.host_step = (float)host_ms_since(b->step_t0);
   return st;
+}
+
+int step_batch(Batch* b, float dt, int vi, int pi, const uint8_t* mask, bool sync) {
+  (void)sync;
+  TRY(step_begin(b, dt, vi, pi, mask));
+  return step_end(b);
 }
 
 static int world_index_ok(Batch* b, int32_t w) { return b && w >= 0 && w < (int32_t)b->worlds.size(); }
 
 // Before a structural edit: bring the host copy up to date, mark the layout for re-upload.
 static int begin_edit(Batch* b) {
+  if (b->in_step) return locked(b);
   TRY(download_state(b));
   b->structure_dirty = true;
   return B2G_OK;
@@ -1076,6 +1168,29 @@ using namespace b2g;
 struct b2g_batch : public Batch {};
 
 uint64_t b2g::batch_allocated_bytes(const b2g_batch* b) { return b ? b->allocated : 0; }
+
+int b2g::take_world(b2g_batch* src, int32_t world, HostWorld* out) {
+  if (!world_index_ok(src, world) || !out || world < src->NW) return B2G_E_INVALID_ARG;
+  if (src->in_step) return locked(src);
+  *out = std::move(src->worlds[world]);
+  if (world + 1 == (int32_t)src->worlds.size()) {
+    src->worlds.pop_back();
+  } else {
+    src->worlds[world] = HostWorld();
+    src->worlds[world].flags |= B2G_WF_RETIRED;
+  }
+  src->tail_pack.valid = false;
+  return B2G_OK;
+}
+
+int b2g::append_world(b2g_batch* dst, HostWorld&& w, int32_t* out_world) {
+  if (!dst) return B2G_E_INVALID_ARG;
+  // after the device layout: the next step uploads it with the other new worlds
+  w.flags &= ~(B2G_WF_ACTIVE | B2G_WF_FAULTED);
+  dst->worlds.push_back(std::move(w));
+  if (out_world) *out_world = (int32_t)dst->worlds.size() - 1;
+  return B2G_OK;
+}
 
 static const char* kStatusNames[] = {"OK",   "INVALID_ARG", "OUT_OF_MEMORY", "TIMEOUT",  "WORLD_FAULT",
                                      "CUDA", "LOCKED",      "CAPACITY",      "CANCELLED"};
@@ -1306,6 +1421,7 @@ B2G_API int b2g_world_count(b2g_batch* b, int32_t* out_n) {
 
 B2G_API int b2g_world_set_gravity(b2g_batch* b, int32_t world, float gx, float gy) {
   if (!world_index_ok(b, world) || !isfinite(gx) || !isfinite(gy)) return B2G_E_INVALID_ARG;
+  if (b->in_step && world < b->NW) return locked(b);
   b->worlds[world].gx = gx;
   b->worlds[world].gy = gy;
   if (world < b->NW && b->device_state_valid && !b->structure_dirty) {
@@ -1367,12 +1483,20 @@ static int compact_device(Batch* b, int32_t* old_to_new, int32_t n) {
   CompactTables t{tp + 8 * (size_t)NW, reinterpret_cast<const int4*>(tp), reinterpret_cast<const int4*>(tp) + NW,
                   tp + 9 * (size_t)NW, tp + 10 * (size_t)NW};
   Batch::Spare& sp = b->spare;
-  TRY(ensure(b, sp.xf, NB2)); TRY(ensure(b, sp.pos, NB2)); TRY(ensure(b, sp.vel, NB2)); TRY(ensure(b, sp.massd, NB2));
-  TRY(ensure(b, sp.damp, NB2)); TRY(ensure(b, sp.force, NB2)); TRY(ensure(b, sp.lc, NB2));
-  TRY(ensure(b, sp.btype, NB2)); TRY(ensure(b, sp.bworld, NB2)); TRY(ensure(b, sp.bstate, NB2));
-  TRY(ensure(b, sp.shape, NF2)); TRY(ensure(b, sp.fbody, NF2)); TRY(ensure(b, sp.fgroup, NF2));
-  TRY(ensure(b, sp.fsensor, NF2)); TRY(ensure(b, sp.fworld, NF2)); TRY(ensure(b, sp.ffilter, NF2));
-  TRY(ensure(b, sp.fmat, NF2)); TRY(ensure(b, sp.frad, NF2)); TRY(ensure(b, sp.joints, NJ2));
+  // the spare arrays take at least the live arrays' capacity: after the swap the live layout keeps
+  // the room it had, so worlds appended after a compaction do not regrow every array
+  auto room = [](auto& spare, const auto& live, int n) { return std::max((size_t)n, live.cap); };
+  auto fit = [&](auto& spare, const auto& live, int n) -> int {
+    size_t want = room(spare, live, n);
+    return spare.cap >= want ? B2G_OK : resize_exact(b, spare, want, false);
+  };
+  TRY(fit(sp.xf, b->xf, NB2)); TRY(fit(sp.pos, b->pos, NB2)); TRY(fit(sp.vel, b->vel, NB2));
+  TRY(fit(sp.massd, b->massd, NB2)); TRY(fit(sp.damp, b->damp, NB2)); TRY(fit(sp.force, b->force, NB2));
+  TRY(fit(sp.lc, b->lc, NB2)); TRY(fit(sp.btype, b->btype, NB2)); TRY(fit(sp.bworld, b->bworld, NB2));
+  TRY(fit(sp.bstate, b->bstate, NB2));
+  TRY(fit(sp.shape, b->shape, NF2)); TRY(fit(sp.fbody, b->fbody, NF2)); TRY(fit(sp.fgroup, b->fgroup, NF2));
+  TRY(fit(sp.fsensor, b->fsensor, NF2)); TRY(fit(sp.fworld, b->fworld, NF2)); TRY(fit(sp.ffilter, b->ffilter, NF2));
+  TRY(fit(sp.fmat, b->fmat, NF2)); TRY(fit(sp.frad, b->frad, NF2)); TRY(fit(sp.joints, b->joints, NJ2));
   BodyRecs sb{b->xf.p, b->pos.p, b->vel.p, b->massd.p, b->damp.p, b->force.p, b->lc.p, b->btype.p, b->bworld.p,
               b->bstate.p};
   BodyRecs db{sp.xf.p, sp.pos.p, sp.vel.p, sp.massd.p, sp.damp.p, sp.force.p, sp.lc.p, sp.btype.p, sp.bworld.p,
@@ -1398,8 +1522,9 @@ static int compact_device(Batch* b, int32_t* old_to_new, int32_t n) {
   std::vector<float4> wg2(kept);
   std::vector<int2> wc2(kept);
   std::vector<int> wflags(kept);
-  for (int w = 0; w < (int)b->worlds.size(); ++w) {
-    int to = w < NW ? wnew[w] : -1;
+  const int trailing = (int)b->worlds.size() - NW;  // worlds not uploaded yet keep their order
+  for (int w = 0; w < NW; ++w) {
+    int to = wnew[w];
     if (w < n) old_to_new[w] = to;
     if (to < 0) continue;
     HostWorld& hw = b->worlds[w];
@@ -1409,6 +1534,10 @@ static int compact_device(Batch* b, int32_t* old_to_new, int32_t n) {
     wc2[to] = make_int2(con_new[w], wc[w].y);
     wflags[to] = device_world_flags(hw);
     keep.push_back(std::move(hw));
+  }
+  for (int k = 0; k < trailing; ++k) {
+    if (NW + k < n) old_to_new[NW + k] = kept + k;
+    keep.push_back(std::move(b->worlds[NW + k]));
   }
   b->worlds.swap(keep);
   b->h_body_off.assign(kept + 1, 0);
@@ -1462,7 +1591,8 @@ B2G_API int b2g_world_status(b2g_batch* b, int32_t world, int32_t* status) {
 // Removes retired worlds; old_to_new[w] receives each world's new index (-1 if removed).
 B2G_API int b2g_compact(b2g_batch* b, int32_t* old_to_new, int32_t n) {
   if (!b || (n > 0 && !old_to_new)) return B2G_E_INVALID_ARG;
-  if (b->device >= 0 && b->device_state_valid && !b->structure_dirty && (int)b->worlds.size() == b->NW &&
+  if (b->in_step) return locked(b);
+  if (b->device >= 0 && b->device_state_valid && !b->structure_dirty && (int)b->worlds.size() >= b->NW &&
       b->NW > 0)
     return compact_device(b, old_to_new, n);
   TRY(download_state(b));
@@ -1487,7 +1617,8 @@ B2G_API int b2g_world_set_flags(b2g_batch* b, int32_t world, int32_t allow_sleep
   // flags travel with the per-step world flags upload; no re-layout
   if (!allow_sleep && (b->worlds[world].allow_sleep || b->worlds[world].sleepers)) {
     // b2World::SetAllowSleeping(false) wakes every body (src/dynamics/b2_world.cpp:474-488)
-    TRY(begin_edit(b));
+    if (world < b->NW) TRY(begin_edit(b));
+    else b->tail_pack.valid = false;  // a staged upload of this world is stale
     HostWorld& hw = b->worlds[world];
     for (size_t i = 0; i < hw.bodies.size(); ++i)
       if (hw.bodies[i].type != B2G_STATIC) hw.bodies[i].flags |= B2G_BODY_AWAKE;
@@ -1516,6 +1647,7 @@ B2G_API int b2g_world_get_flags(b2g_batch* b, int32_t world, int32_t* allow_slee
 // b2Body::b2Body (src/dynamics/b2_body.cpp:29-122)
 B2G_API int b2g_bodies_add(b2g_batch* b, int32_t world, const b2g_body_def* defs, int32_t n, int32_t* out_ids) {
   if (!world_index_ok(b, world) || n < 0 || (n > 0 && !defs)) return B2G_E_INVALID_ARG;
+  if (world >= b->NW) b->tail_pack.valid = false;  // a staged upload of this world is stale
   for (int i = 0; i < n; ++i) {
     const b2g_body_def& d = defs[i];
     if (d.type < 0 || d.type > 2 || !isfinite(d.position[0]) || !isfinite(d.position[1]) || !isfinite(d.angle) ||
@@ -1566,6 +1698,7 @@ B2G_API int b2g_bodies_add(b2g_batch* b, int32_t world, const b2g_body_def* defs
 // b2Body::CreateFixture (src/dynamics/b2_body.cpp:230-269)
 B2G_API int b2g_fixtures_add(b2g_batch* b, int32_t world, const b2g_fixture_def* defs, int32_t n, int32_t* out_ids) {
   if (!world_index_ok(b, world) || n < 0 || (n > 0 && !defs)) return B2G_E_INVALID_ARG;
+  if (world >= b->NW) b->tail_pack.valid = false;  // a staged upload of this world is stale
   HostWorld& w0 = b->worlds[world];
   std::vector<b2g_fixture> made(n);
   for (int i = 0; i < n; ++i) {
@@ -1596,6 +1729,7 @@ B2G_API int b2g_fixtures_add(b2g_batch* b, int32_t world, const b2g_fixture_def*
 // b2World::CreateJoint (src/dynamics/b2_world.cpp:268-324) + joint constructors.
 B2G_API int b2g_joints_add(b2g_batch* b, int32_t world, const b2g_joint_def* defs, int32_t n, int32_t* out_ids) {
   if (!world_index_ok(b, world) || n < 0 || (n > 0 && !defs)) return B2G_E_INVALID_ARG;
+  if (world >= b->NW) b->tail_pack.valid = false;  // a staged upload of this world is stale
   HostWorld& w0 = b->worlds[world];
   for (int i = 0; i < n; ++i) {
     const b2g_joint_def& d = defs[i];
@@ -1669,6 +1803,38 @@ B2G_API int b2g_world_sizes(b2g_batch* b, int32_t world, int32_t* bodies, int32_
 B2G_API int b2g_step(b2g_batch* b, float dt, int32_t vi, int32_t pi, const uint8_t* world_mask) {
   if (!b) return B2G_E_INVALID_ARG;
   return step_batch(b, dt, vi, pi, world_mask, true);
+}
+
+B2G_API int b2g_step_begin(b2g_batch* b, float dt, int32_t vi, int32_t pi, const uint8_t* world_mask) {
+  if (!b) return B2G_E_INVALID_ARG;
+  return step_begin(b, dt, vi, pi, world_mask);
+}
+
+B2G_API int b2g_step_poll(b2g_batch* b, int32_t* done) {
+  if (!b || !done) return B2G_E_INVALID_ARG;
+  if (!b->in_step) {
+    *done = 1;
+    return B2G_OK;
+  }
+  cudaError_t e = cudaEventQuery(b->ev[5]);
+  if (e == cudaErrorNotReady) {
+    *done = 0;
+    return B2G_OK;
+  }
+  CUDA_TRY(b, e);
+  *done = 1;
+  return B2G_OK;
+}
+
+B2G_API int b2g_step_end(b2g_batch* b) {
+  if (!b) return B2G_E_INVALID_ARG;
+  return step_end(b);
+}
+
+B2G_API int b2g_batch_stage(b2g_batch* b) {
+  if (!b) return B2G_E_INVALID_ARG;
+  if (b->device < 0 || b->structure_dirty || (int)b->worlds.size() <= b->NW) return B2G_OK;
+  return pack_tail(b, b->tail_pack);
 }
 
 B2G_API int b2g_step_n(b2g_batch* b, float dt, int32_t vi, int32_t pi, int32_t n, int32_t use_graph) {
@@ -1809,6 +1975,7 @@ B2G_API int b2g_step_timed(b2g_batch* b, float dt, int32_t vi, int32_t pi, int32
 
 B2G_API int b2g_batch_set_forces(b2g_batch* b, const float* f4, int64_t n_bodies) {
   if (!b || !f4 || n_bodies < 0 || b->device < 0) return B2G_E_INVALID_ARG;
+  if (b->in_step) return locked(b);
   if (b->structure_dirty) TRY(upload_all(b));
   if (n_bodies != b->NB) return B2G_E_INVALID_ARG;
   if (n_bodies) CUDA_TRY(b, cudaMemcpyAsync(b->force.p, f4, n_bodies * sizeof(float4), cudaMemcpyHostToDevice, b->stream));
@@ -1826,6 +1993,7 @@ B2G_API int b2g_bodies_read(b2g_batch* b, int32_t world, int32_t first, int32_t 
   if (!world_index_ok(b, world) || first < 0 || n < 0 || (n > 0 && !out)) return B2G_E_INVALID_ARG;
   const HostWorld& w = b->worlds[world];
   if (first + n > (int)w.bodies.size()) return B2G_E_INVALID_ARG;
+  if (b->in_step && world < b->NW) return locked(b);
   for (int i = 0; i < n; ++i) out[i] = w.bodies[first + i];
   if (n > 0 && b->host_state_stale && b->device_state_valid && world < b->NW) {
     // the host copy is older than the device: fetch this world's slice only
@@ -1858,7 +2026,8 @@ B2G_API int b2g_bodies_write(b2g_batch* b, int32_t world, int32_t first, int32_t
   if (!world_index_ok(b, world) || first < 0 || n < 0 || (n > 0 && !in)) return B2G_E_INVALID_ARG;
   HostWorld& w0 = b->worlds[world];
   if (first + n > (int)w0.bodies.size()) return B2G_E_INVALID_ARG;
-  TRY(begin_edit(b));
+  if (world < b->NW) TRY(begin_edit(b));
+  else b->tail_pack.valid = false;  // not on the device yet: its host records are the state
   HostWorld& w = b->worlds[world];
   for (int i = 0; i < n; ++i) {
     b2g_body& r = w.bodies[first + i];
@@ -1885,7 +2054,8 @@ B2G_API int b2g_bodies_write(b2g_batch* b, int32_t world, int32_t first, int32_t
 B2G_API int b2g_body_set_awake(b2g_batch* b, int32_t world, int32_t body, int32_t awake) {
   if (!world_index_ok(b, world) || body < 0 || body >= (int32_t)b->worlds[world].bodies.size())
     return B2G_E_INVALID_ARG;
-  TRY(begin_edit(b));
+  if (world < b->NW) TRY(begin_edit(b));
+  else b->tail_pack.valid = false;  // not on the device yet: its host records are the state
   HostWorld& w = b->worlds[world];
   b2g_body& r = w.bodies[body];
   if (r.type == B2G_STATIC) return B2G_OK;
@@ -1906,7 +2076,7 @@ B2G_API int b2g_body_set_awake(b2g_batch* b, int32_t world, int32_t body, int32_
 // checkpoint tooling and tests).
 B2G_API int b2g_bodies_sleep_time_read(b2g_batch* b, int32_t world, int32_t first, int32_t n, float* out) {
   if (!world_index_ok(b, world) || first < 0 || n < 0 || (n > 0 && !out)) return B2G_E_INVALID_ARG;
-  TRY(download_state(b));
+  if (world < b->NW) TRY(download_state(b));  // a world not on the device yet is its host records
   HostWorld& w = b->worlds[world];
   if (first + n > (int)w.bodies.size()) return B2G_E_INVALID_ARG;
   for (int i = 0; i < n; ++i) out[i] = (size_t)(first + i) < w.body_sleep.size() ? w.body_sleep[first + i] : 0.0f;
@@ -1915,6 +2085,7 @@ B2G_API int b2g_bodies_sleep_time_read(b2g_batch* b, int32_t world, int32_t firs
 
 B2G_API int b2g_batch_read_states(b2g_batch* b, float* xf4, float* v3, int64_t cap_bodies, int64_t* n_bodies) {
   if (!b) return B2G_E_INVALID_ARG;
+  if (b->in_step) return locked(b);
   if (b->structure_dirty) TRY(upload_all(b));
   if (n_bodies) *n_bodies = b->NB;
   int64_t n = std::min<int64_t>(cap_bodies, b->NB);
@@ -1941,7 +2112,7 @@ B2G_API int b2g_fixtures_read(b2g_batch* b, int32_t world, int32_t first, int32_
 
 B2G_API int b2g_joints_read(b2g_batch* b, int32_t world, int32_t first, int32_t n, b2g_joint* out) {
   if (!world_index_ok(b, world) || first < 0 || n < 0 || (n > 0 && !out)) return B2G_E_INVALID_ARG;
-  TRY(download_state(b));
+  if (world < b->NW) TRY(download_state(b));  // a world not on the device yet is its host records
   const HostWorld& w = b->worlds[world];
   if (first + n > (int)w.joints.size()) return B2G_E_INVALID_ARG;
   for (int i = 0; i < n; ++i) out[i] = w.joints[first + i];
@@ -1950,7 +2121,7 @@ B2G_API int b2g_joints_read(b2g_batch* b, int32_t world, int32_t first, int32_t 
 
 B2G_API int b2g_contacts_read(b2g_batch* b, int32_t world, b2g_contact* out, int32_t cap, int32_t* n) {
   if (!world_index_ok(b, world) || !n) return B2G_E_INVALID_ARG;
-  TRY(download_state(b));
+  if (world < b->NW) TRY(download_state(b));  // a world not on the device yet is its host records
   const HostWorld& w = b->worlds[world];
   *n = (int32_t)w.contacts.size();
   if (out)
@@ -2056,6 +2227,7 @@ B2G_API int b2g_solver_order(b2g_batch* b, int32_t world, int32_t* contact_color
 // (re-layout, compaction) the broadphase rebuilds them without touching the contact list.
 static int ensure_query_trees(Batch* b) {
   if (b->device < 0) return B2G_E_INVALID_ARG;
+  if (b->in_step) return locked(b);
   CUDA_TRY(b, cudaSetDevice(b->device));
   if (b->structure_dirty) {
     TRY(upload_all(b));

@@ -16,6 +16,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <chrono>
 #include <string>
 #include <vector>
 
@@ -139,6 +140,23 @@ struct EventDev {
   b2g_manifold old;
 };
 
+// Appended worlds [w0, w1) packed into device layout on the host ahead of the step that uploads
+// them (b2g_batch_stage); valid while the layout it was packed against is unchanged.
+struct TailPack {
+  bool valid = false;
+  int w0 = 0, w1 = 0, NB0 = 0, NF0 = 0, NJ0 = 0, NB = 0, NF = 0, NJ = 0;
+  std::vector<int> body_off, fix_off, joint_off;  // per packed world
+  std::vector<float4> xf, pos, vel, massd, damp, force, fmat;
+  std::vector<float2> lc;
+  std::vector<int> btype, bworld, fbody, fgroup, fsensor, fworld;
+  std::vector<int2> bstate;
+  std::vector<float> frad;
+  std::vector<b2g_shape> shape;
+  std::vector<uint32_t> ffilter;
+  std::vector<JointDev> joints;
+  std::vector<uint64_t> nocol;
+};
+
 struct Batch {
   int device = 0;
   uint64_t budget = 0;
@@ -174,6 +192,10 @@ struct Batch {
   DBuf<int4> sl;                  // island scratch of sleep-mode worlds
   bool any_sleep = false;         // some world of the layout runs in sleep mode
   bool any_sensor = false;        // some fixture of the layout is a sensor
+  TailPack tail_pack;             // prepared upload of appended worlds
+  bool in_step = false;           // between b2g_step_begin and b2g_step_end
+  bool step_graph = false;        // the step in flight replays a graph
+  std::chrono::steady_clock::time_point step_t0;  // host time the step in flight began
 
   DBuf<b2g_shape> shape;
   DBuf<int> fbody, fgroup, fsensor, fworld;
@@ -292,6 +314,11 @@ struct Batch {
 // ---- host functions (engine.cu)
 int upload_all(Batch* b);
 uint64_t batch_allocated_bytes(const b2g_batch* b);
+// Moves a world that is not on the device out of `src` (host records only; the slot is dropped
+// when it is the last one, else left retired) and appends it to `dst` as a new world: how a world
+// built on another thread's host-only batch joins a device batch without copying its records.
+int take_world(b2g_batch* src, int32_t world, HostWorld* out);
+int append_world(b2g_batch* dst, HostWorld&& w, int32_t* out_world);
 int upload_tail(Batch* b);
 int download_state(Batch* b);
 int step_batch(Batch* b, float dt, int vi, int pi, const uint8_t* mask, bool sync);

@@ -267,6 +267,9 @@ typedef struct b2g_profile {
   float step, collide, solve, broadphase, solve_toi;
   int64_t bodies, fixtures, contacts, touching, joints, colors_max;
   int64_t touching_total; /* solver contacts summed over every step of the batch so far */
+  /* host wall times of the last b2g_step (ms): the whole call; uploading appended worlds; their
+   * broadphase (with its read-back); growing device buffers */
+  float host_step, host_admit_upload, host_admit_broadphase, host_grow;
 } b2g_profile;
 
 /* ---- batch lifecycle ------------------------------------------------------------------------ */
@@ -333,6 +336,19 @@ B2G_API int b2g_world_sizes(b2g_batch* b, int32_t world, int32_t* bodies, int32_
  * Returns after the step's device work has been enqueued and completed. */
 B2G_API int b2g_step(b2g_batch* b, float dt, int32_t velocity_iterations,
                      int32_t position_iterations, const uint8_t* world_mask);
+/* b2g_step in two halves, so that host work (building worlds, b2g_batch_stage) overlaps the
+ * device's step: b2g_step_begin uploads and launches the step and returns; b2g_step_poll reports
+ * whether the device has finished it (non-blocking); b2g_step_end waits and completes it (status
+ * as b2g_step). Between them only worlds that are not on the device yet may be created or edited
+ * and b2g_batch_stage called; other calls on the batch return B2G_E_LOCKED. */
+B2G_API int b2g_step_begin(b2g_batch* b, float dt, int32_t velocity_iterations, int32_t position_iterations,
+                           const uint8_t* world_mask);
+B2G_API int b2g_step_poll(b2g_batch* b, int32_t* done);
+B2G_API int b2g_step_end(b2g_batch* b);
+/* Packs the worlds added since the last step into device layout on the host (no device work), so
+ * that the next step's upload of them is a copy; call it while a step runs. Edits to those worlds
+ * afterwards discard the pack (the next step then packs them itself). */
+B2G_API int b2g_batch_stage(b2g_batch* b);
 /* n steps back to back; with use_graph != 0 the whole Step is captured once in a CUDA graph and
  * replayed (buffers are sized on the first step; see b2g_reserve). */
 B2G_API int b2g_step_n(b2g_batch* b, float dt, int32_t velocity_iterations,
@@ -493,22 +509,30 @@ typedef struct b2g_request_result {
 } b2g_request_result;
 /* A continuous-batching server: rollout requests (a seeded scene + K steps) are admitted as
  * slots and device memory free up, packed into one batched Step with every other active
- * world, and retired when their K steps are done. */
+ * world, and retired when their K steps are done. Admitted worlds are built on the host by
+ * builder threads (2 by default) while the device steps. */
 B2G_API int b2g_server_create(int device, uint64_t budget_bytes, int32_t max_worlds,
                               float dt, int32_t velocity_iterations, int32_t position_iterations,
                               b2g_server** out);
 B2G_API int b2g_server_destroy(b2g_server* s);
+/* Number of host threads that build admitted worlds (0: the tick builds them itself while the
+ * device steps). B2G_E_LOCKED while an admitted world is still to be built or joined. */
+B2G_API int b2g_server_set_builders(b2g_server* s, int32_t n);
 /* Queue a request: scene B2G_SCENE_BATCH_WORLD with `seed`, `bodies` bodies, `steps` steps. */
 B2G_API int b2g_server_submit(b2g_server* s, uint32_t seed, int32_t bodies, int32_t steps,
                               int64_t* out_request_id);
 /* Admit what fits, run one batched step of all active worlds, retire finished ones.
- * *active receives the number of worlds stepped; *step_ms the step's wall time. */
+ * *active receives the number of active worlds (stepped, or uploaded by this step); *step_ms the
+ * step's wall time, launch to completion, host work overlapped with it included. */
 B2G_API int b2g_server_tick(b2g_server* s, int32_t* active, double* step_ms);
 B2G_API int b2g_server_poll(b2g_server* s, b2g_request_result* out, int32_t cap, int32_t* n);
 /* Cancels a queued or running request: it finishes at once with status B2G_E_CANCELLED (its
  * world, if admitted, is retired; the other requests are unaffected). B2G_E_INVALID_ARG when the
  * request is unknown or already finished. */
 B2G_API int b2g_server_cancel(b2g_server* s, int64_t request_id);
+/* The batch the server steps (owned by the server): for reading its profile (b2g_profile_get),
+ * querying served worlds or reading their state between ticks. */
+B2G_API int b2g_server_batch(b2g_server* s, b2g_batch** out);
 B2G_API int b2g_server_stats(b2g_server* s, int64_t* queued, int64_t* active,
                              int64_t* completed, int64_t* rejected, int64_t* hbm_bytes);
 
