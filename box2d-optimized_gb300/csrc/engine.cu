@@ -219,7 +219,7 @@ static uint64_t emitter_key(const HostWorld& w, int fo, int fa, int fb) {
 static void replan_solver(Batch* b) {
   std::vector<int> nbw(b->worlds.size());
   for (size_t w = 0; w < b->worlds.size(); ++w) nbw[w] = (int)b->worlds[w].bodies.size();
-  b->solve_classes = plan_solve_classes(b->h_world_order, nbw, b->class_threads);
+  b->solve_classes = plan_solve_classes(b->h_world_order, nbw, b->class_threads, b->wide_waves);
 }
 
 // Solver constraints address bodies by a 24-bit world-local index.
@@ -1882,6 +1882,16 @@ B2G_API int b2g_batch_set_solver_threads(b2g_batch* b, const int32_t* threads) {
   for (int c = 0; c < B2G_SOLVE_CLASSES; ++c)
     if (!solver_threads_valid(threads[c])) return B2G_E_INVALID_ARG;
   for (int c = 0; c < B2G_SOLVE_CLASSES; ++c) b->class_threads[c] = threads[c];
+  if (!b->h_world_order.empty()) {
+    replan_solver(b);
+    b->layout_version++;  // captured graphs hold the old launch shapes
+  }
+  return B2G_OK;
+}
+
+B2G_API int b2g_batch_set_solver_waves(b2g_batch* b, float waves) {
+  if (!b || !(waves >= 0.0f)) return B2G_E_INVALID_ARG;
+  b->wide_waves = waves;
   if (!b->h_world_order.empty()) {
     replan_solver(b);
     b->layout_version++;  // captured graphs hold the old launch shapes

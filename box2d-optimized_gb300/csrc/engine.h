@@ -121,7 +121,8 @@ struct Batch;
 // One solver launch over a contiguous range of the size-sorted world order.
 struct SolveClass {
   int first, count, threads, smem;
-  int cls;  // size class index
+  int cls;    // size class index
+  bool wide;  // the 128-register build (few worlds: latency-bound) rather than the 64-register one
 };
 #define B2G_SOLVE_CLASSES 5
 
@@ -280,6 +281,7 @@ struct Batch {
   std::vector<SolveClass> solve_classes;
   std::vector<int> h_world_order;  // worlds by body count, largest first (device world_order)
   int class_threads[B2G_SOLVE_CLASSES] = {64, 128, 256, 512, 1024};
+  float wide_waves = 2.0f;  // size classes of at most this many waves run the wide solver build
   cudaStream_t side[B2G_SOLVE_CLASSES] = {};
   cudaEvent_t fork_ev[B2G_SOLVE_CLASSES + 1] = {};
 

@@ -17,878 +17,9 @@
 // run in order with a CTA barrier between them, which reproduces the sequential Gauss-Seidel
 // sweep in colour order. Worlds are launched in size classes (threads and shared memory per
 // class) on forked streams so that small and large worlds run side by side.
-#include <cuda/atomic>
-
-#include "b2g_math.cuh"
-#include "dev_common.cuh"
-#include "engine.h"
-#include "kernels.h"
-#include "solver_dev.cuh"
+#include "solve_world.cuh"
 
 namespace b2g {
-
-#define FULL_MASK 0xffffffffu
-
-// Block-wide exclusive scan of one int per thread (blockDim.x == T).
-template <int T>
-__device__ int block_scan(int v, int* total) {
-  constexpr int NWARP = T / 32;
-  __shared__ int warp_sums[NWARP];
-  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  int x = v;
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    int y = __shfl_up_sync(FULL_MASK, x, o);
-    if (lane >= o) x += y;
-  }
-  if (lane == 31) warp_sums[wid] = x;
-  __syncthreads();
-  if (wid == 0) {
-    int s = lane < NWARP ? warp_sums[lane] : 0;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      int y = __shfl_up_sync(FULL_MASK, s, o);
-      if (lane >= o) s += y;
-    }
-    if (lane < NWARP) warp_sums[lane] = s;
-  }
-  __syncthreads();
-  int prefix = (wid > 0 ? warp_sums[wid - 1] : 0) + x - v;
-  *total = warp_sums[NWARP - 1];
-  __syncthreads();
-  return prefix;
-}
-
-// Working arrays of one colouring, each in shared or global memory (generic pointers).
-struct ColourMem {
-  int* cnt;                  // per body: incidence count, then fill counter
-  int* head;                 // per body: list offset, then first uncoloured entry
-  unsigned long long* mask;  // per body: colours taken
-  int* list;                 // 2 per constraint: per-body incidence lists
-  const int2* cb;            // per constraint: world-local bodies, negative (bit 31 set) = static
-  int8_t* col;               // per constraint: colour, -1 until coloured
-  uint8_t* rdy;              // per constraint: ready in the current round
-  int* wl0;                  // worklists of uncoloured constraints (n entries each)
-  int* wl1;
-};
-
-// Greedy colouring in priority order, computed in parallel rounds (Jones-Plassmann with
-// smallest-free-colour choice): a constraint is coloured once it is the first uncoloured entry
-// of the priority-sorted incidence list of each of its non-static bodies; it then takes the
-// lowest colour not used at those bodies. The result equals the sequential greedy pass in
-// (priority, index) order. Colours 0..62 are regular; 63 is the overflow colour, solved
-// serially in priority order. Buckets the constraints by colour into `order` (and its inverse
-// into `slot` when given) and writes the colour offsets to `ranges` (ncol + 1 entries). Returns
-// the number of colours (max + 1).
-template <int T>
-__device__ int colour_constraints(int n, int nb, const ColourMem m, const uint32_t* prio, int* order, int* slot,
-                                  int* ranges, unsigned int* status) {
-  __shared__ int col_cnt[64];
-  __shared__ int col_off[65];
-  __shared__ int s_carry, s_maxcol;
-  for (int i = threadIdx.x; i < nb; i += T) {
-    m.cnt[i] = 0;
-    m.mask[i] = 0ull;
-  }
-  for (int k = threadIdx.x; k < n; k += T) m.col[k] = -1;
-  if (threadIdx.x == 0) s_carry = 0;
-  __syncthreads();
-  for (int k = threadIdx.x; k < n; k += T) {
-    int2 b = m.cb[k];
-    if (b.x >= 0) atomicAdd(&m.cnt[b.x], 1);
-    if (b.y >= 0) atomicAdd(&m.cnt[b.y], 1);
-  }
-  __syncthreads();
-  for (int i0 = 0; i0 < nb; i0 += T) {
-    int i = i0 + threadIdx.x;
-    int v = i < nb ? m.cnt[i] : 0;
-    int total;
-    int p = block_scan<T>(v, &total);
-    if (i < nb) m.head[i] = s_carry + p;
-    __syncthreads();
-    if (threadIdx.x == 0) s_carry += total;
-    __syncthreads();
-  }
-  for (int i = threadIdx.x; i < nb; i += T) m.cnt[i] = 0;
-  __syncthreads();
-  for (int k = threadIdx.x; k < n; k += T) {
-    int2 b = m.cb[k];
-    if (b.x >= 0) m.list[m.head[b.x] + atomicAdd(&m.cnt[b.x], 1)] = k;
-    if (b.y >= 0) m.list[m.head[b.y] + atomicAdd(&m.cnt[b.y], 1)] = k;
-  }
-  __syncthreads();
-  // each body's list in (priority, index) order
-  for (int i = threadIdx.x; i < nb; i += T) {
-    int off = m.head[i], cnt = m.cnt[i];
-    for (int x = 1; x < cnt; ++x) {
-      int kx = m.list[off + x];
-      uint32_t px = prio[kx];
-      int y = x - 1;
-      while (y >= 0) {
-        int ky = m.list[off + y];
-        uint32_t py = prio[ky];
-        if (py < px || (py == px && ky < kx)) break;
-        m.list[off + y + 1] = ky;
-        --y;
-      }
-      m.list[off + y + 1] = kx;
-    }
-  }
-  __syncthreads();
-  // rounds over a worklist of the uncoloured constraints: a round colours every constraint that
-  // heads the priority lists of all its non-static bodies (at least the uncoloured one of lowest
-  // (priority, index)); the others form the next round's worklist (their order is immaterial)
-  __shared__ int s_m, s_next;
-  if (threadIdx.x == 0) {
-    s_m = n;
-    s_next = 0;
-  }
-  __syncthreads();
-  int* wl = m.wl0;
-  int* wn = m.wl1;
-  bool done = (n == 0);
-  for (int round = 0; round <= n + 1 && !done; ++round) {
-    const int cnt = s_m;
-    for (int i = threadIdx.x; i < cnt; i += T) {
-      int k = round == 0 ? i : wl[i];
-      int2 b = m.cb[k];
-      bool ok = (b.x < 0 || m.list[m.head[b.x]] == k) && (b.y < 0 || m.list[m.head[b.y]] == k);
-      m.rdy[k] = ok ? 1 : 0;
-    }
-    __syncthreads();
-    for (int i0 = 0; i0 < cnt; i0 += T) {  // CTA-uniform trip count: whole warps reach the ballot
-      int i = i0 + threadIdx.x;
-      int k = -1;
-      bool keep = false;
-      if (i < cnt) {
-        k = round == 0 ? i : wl[i];
-        if (m.rdy[k]) {
-          int2 b = m.cb[k];
-          unsigned long long used = (b.x >= 0 ? m.mask[b.x] : 0ull) | (b.y >= 0 ? m.mask[b.y] : 0ull);
-          unsigned long long freeBits = ~used & ((1ull << 63) - 1ull);
-          int c;
-          if (freeBits == 0ull) {
-            c = 63;
-          } else {
-            c = __ffsll((long long)freeBits) - 1;
-            if (b.x >= 0) m.mask[b.x] |= 1ull << c;
-            if (b.y >= 0) m.mask[b.y] |= 1ull << c;
-          }
-          m.col[k] = (int8_t)c;
-          if (b.x >= 0) m.head[b.x] += 1;
-          if (b.y >= 0) m.head[b.y] += 1;
-        } else {
-          keep = true;
-        }
-      }
-      unsigned bal = __ballot_sync(FULL_MASK, keep);
-      int lane = threadIdx.x & 31;
-      int base = 0;
-      if (lane == 0 && bal) base = atomicAdd(&s_next, __popc(bal));
-      base = __shfl_sync(FULL_MASK, base, 0);
-      if (keep) wn[base + __popc(bal & ((1u << lane) - 1u))] = k;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      s_m = s_next;
-      s_next = 0;
-    }
-    __syncthreads();
-    done = (s_m == 0);
-    int* t = wl;
-    wl = wn;
-    wn = t;
-  }
-  if (!done && threadIdx.x == 0) atomicOr(status, B2G_DEV_COLOR_ROUNDS);
-  // bucket by colour
-  if (threadIdx.x < 64) col_cnt[threadIdx.x] = 0;
-  if (threadIdx.x == 0) s_maxcol = -1;
-  __syncthreads();
-  for (int k = threadIdx.x; k < n; k += T) {
-    int c = m.col[k];
-    if (c < 0) c = 63;  // only after a failed colouring (status raised)
-    atomicAdd(&col_cnt[c], 1);
-    atomicMax(&s_maxcol, c);
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    int s = 0;
-    for (int c = 0; c < 64; ++c) {
-      col_off[c] = s;
-      s += col_cnt[c];
-      col_cnt[c] = 0;
-    }
-    col_off[64] = s;
-  }
-  __syncthreads();
-  for (int k = threadIdx.x; k < n; k += T) {
-    int c = m.col[k];
-    if (c < 0) c = 63;
-    int pos = col_off[c] + atomicAdd(&col_cnt[c], 1);
-    order[pos] = k;
-    if (slot) slot[k] = pos;
-  }
-  __syncthreads();
-  if (threadIdx.x == 0 && col_cnt[63] > 1) {
-    int off = col_off[63], cnt = col_cnt[63];
-    for (int x = 1; x < cnt; ++x) {
-      int kx = order[off + x];
-      uint32_t px = prio[kx];
-      int y = x - 1;
-      while (y >= 0) {
-        int ky = order[off + y];
-        uint32_t py = prio[ky];
-        if (py < px || (py == px && ky < kx)) break;
-        order[off + y + 1] = ky;
-        --y;
-      }
-      order[off + y + 1] = kx;
-    }
-    if (slot)
-      for (int x = 0; x < cnt; ++x) slot[order[off + x]] = off + x;
-  }
-  int ncol = s_maxcol + 1;
-  for (int c = threadIdx.x; c <= ncol; c += T) ranges[c] = col_off[c];
-  __syncthreads();
-  return ncol;
-}
-
-// ---- constraint planes <-> the per-constraint register record
-__device__ __forceinline__ void store_planes(const SolverPlanes& P, int s, const VCDev& vc) {
-  P.idx[s] = make_int2(vc.indexA | (vc.pointCount << 24) | (vc.pcPointCount << 28), vc.indexB | (vc.type << 24));
-  P.cid[s] = vc.contact;
-  P.nf[s] = make_float4(vc.normal[0], vc.normal[1], vc.friction, vc.tangentSpeed);
-  P.r0[s] = make_float4(vc.rA[0][0], vc.rA[0][1], vc.rB[0][0], vc.rB[0][1]);
-  P.r1[s] = make_float4(vc.rA[1][0], vc.rA[1][1], vc.rB[1][0], vc.rB[1][1]);
-  P.nmtm[s] = make_float4(vc.normalMass[0], vc.normalMass[1], vc.tangentMass[0], vc.tangentMass[1]);
-  P.bk[s] = make_float4(vc.velocityBias[0], vc.velocityBias[1], vc.K[0], vc.K[1]);
-  P.kn[s] = make_float4(vc.K[3], vc.NM[0], vc.NM[1], vc.NM[3]);
-  P.imp[s] = make_float4(vc.normalImpulse[0], vc.normalImpulse[1], vc.tangentImpulse[0], vc.tangentImpulse[1]);
-  P.lcs[s] = make_float4(vc.localCenterA[0], vc.localCenterA[1], vc.localCenterB[0], vc.localCenterB[1]);
-  P.lnp[s] = make_float4(vc.localNormal[0], vc.localNormal[1], vc.localPoint[0], vc.localPoint[1]);
-  P.lps[s] = make_float4(vc.localPoints[0][0], vc.localPoints[0][1], vc.localPoints[1][0], vc.localPoints[1][1]);
-  P.rad[s] = make_float2(vc.radiusA, vc.radiusB);
-}
-
-// Inverse mass and inertia per world-local body: (1/m, 1/I) pairs in shared memory, or the
-// global mass records (m, 1/m, I, 1/I) of the world.
-struct Masses {
-  const float2* sm;
-  const float4* g;
-  __device__ __forceinline__ float2 get(int i) const {
-    if (sm) return sm[i];
-    float4 m = g[i];
-    return make_float2(m.y, m.w);
-  }
-};
-
-// The rows of one constraint read by the velocity phase (warm start, velocity iterations) and by
-// the position iterations; all loads are issued together (none waits for another).
-struct VelRows {
-  int2 id;
-  float4 nf, r0, r1, nmtm, bk, kn, imp;
-};
-struct PosRows {
-  int2 id;
-  float4 lcs, lnp, lps;
-  float2 rad;
-};
-
-__device__ __forceinline__ void fetch_vel(const SolverPlanes& P, int s, VelRows& r) {
-  r.id = P.idx[s];
-  r.nf = P.nf[s];
-  r.r0 = P.r0[s];
-  r.r1 = P.r1[s];
-  r.nmtm = P.nmtm[s];
-  r.bk = P.bk[s];
-  r.kn = P.kn[s];
-  r.imp = P.imp[s];
-}
-
-__device__ __forceinline__ void fetch_pos(const SolverPlanes& P, int s, PosRows& r) {
-  r.id = P.idx[s];
-  r.lcs = P.lcs[s];
-  r.lnp = P.lnp[s];
-  r.lps = P.lps[s];
-  r.rad = P.rad[s];
-}
-
-__device__ __forceinline__ void unpack_common(int2 id, VCDev& vc, const Masses& M) {
-  vc.indexA = id.x & 0xffffff;
-  vc.indexB = id.y & 0xffffff;
-  vc.pointCount = (id.x >> 24) & 15;
-  vc.pcPointCount = (id.x >> 28) & 15;
-  vc.type = id.y >> 24;
-  float2 ma = M.get(vc.indexA), mb = M.get(vc.indexB);
-  vc.invMassA = ma.x; vc.invIA = ma.y; vc.invMassB = mb.x; vc.invIB = mb.y;
-}
-
-// Fields read by warmStartContact / solveContactVelocity (1-point rows of the second point and
-// the block solver hold zeros and are not used).
-__device__ __forceinline__ void unpack_vel(const VelRows& r, VCDev& vc, const Masses& M) {
-  unpack_common(r.id, vc, M);
-  vc.normal[0] = r.nf.x; vc.normal[1] = r.nf.y; vc.friction = r.nf.z; vc.tangentSpeed = r.nf.w;
-  vc.rA[0][0] = r.r0.x; vc.rA[0][1] = r.r0.y; vc.rB[0][0] = r.r0.z; vc.rB[0][1] = r.r0.w;
-  vc.rA[1][0] = r.r1.x; vc.rA[1][1] = r.r1.y; vc.rB[1][0] = r.r1.z; vc.rB[1][1] = r.r1.w;
-  vc.normalImpulse[0] = r.imp.x; vc.normalImpulse[1] = r.imp.y;
-  vc.tangentImpulse[0] = r.imp.z; vc.tangentImpulse[1] = r.imp.w;
-  vc.normalMass[0] = r.nmtm.x; vc.normalMass[1] = r.nmtm.y; vc.tangentMass[0] = r.nmtm.z; vc.tangentMass[1] = r.nmtm.w;
-  vc.velocityBias[0] = r.bk.x; vc.velocityBias[1] = r.bk.y;
-  vc.K[0] = r.bk.z; vc.K[1] = r.bk.w; vc.K[2] = r.bk.w; vc.K[3] = r.kn.x;
-  vc.NM[0] = r.kn.y; vc.NM[1] = r.kn.z; vc.NM[2] = r.kn.z; vc.NM[3] = r.kn.w;
-}
-
-// Fields read by solveContactPosition.
-__device__ __forceinline__ void unpack_pos(const PosRows& r, VCDev& vc, const Masses& M) {
-  unpack_common(r.id, vc, M);
-  vc.localCenterA[0] = r.lcs.x; vc.localCenterA[1] = r.lcs.y; vc.localCenterB[0] = r.lcs.z; vc.localCenterB[1] = r.lcs.w;
-  vc.localNormal[0] = r.lnp.x; vc.localNormal[1] = r.lnp.y; vc.localPoint[0] = r.lnp.z; vc.localPoint[1] = r.lnp.w;
-  vc.localPoints[0][0] = r.lps.x; vc.localPoints[0][1] = r.lps.y;
-  vc.localPoints[1][0] = r.lps.z; vc.localPoints[1][1] = r.lps.w;
-  vc.radiusA = r.rad.x; vc.radiusB = r.rad.y;
-}
-
-// One pass over the contact colours: colour by colour, a CTA barrier after each; colour 63 (the
-// overflow colour) is solved serially by thread 0 in priority order.
-template <int T, class Rows, class Fetch, class Solve>
-__device__ __forceinline__ void colour_sweep(const int* ranges, int ncol, int c0, Fetch fetch, Solve solve) {
-  for (int c = 0; c < ncol; ++c) {
-    int s = ranges[c], e = ranges[c + 1];
-    if (c == 63) {
-      if (threadIdx.x == 0)
-        for (int i = s; i < e; ++i) {
-          Rows r;
-          fetch(c0 + i, r);
-          solve(c0 + i, r);
-        }
-    } else {
-      for (int i = s + threadIdx.x; i < e; i += T) {
-        Rows r;
-        fetch(c0 + i, r);
-        solve(c0 + i, r);
-      }
-    }
-    __syncthreads();
-  }
-}
-
-// Carves 16-byte aligned pieces out of the CTA's dynamic shared memory.
-struct SmemCarver {
-  unsigned char* p;
-  size_t left;
-  __device__ void* take(size_t bytes) {
-    bytes = (bytes + 15) & ~(size_t)15;
-    if (bytes > left) return nullptr;
-    void* r = p;
-    p += bytes;
-    left -= bytes;
-    return r;
-  }
-};
-
-// ---- islands of sleep-mode worlds (b2World::Solve's depth-first search, src/dynamics/b2_world.cpp:520-650)
-// Connected components over solid contacts (touching, enabled, no sensor) and joints between
-// non-static bodies, as a lock-free union-find that always hooks the larger root under the
-// smaller: every component's root is its lowest body index, whatever the order of the unions.
-// A world's island records are touched by its CTA alone: every access is a CTA-scope atomic
-// (loads included, so that none is served from a line older than an atomic), and the CTA barrier
-// orders the phases.
-__device__ __forceinline__ int isl_load(int* p) {
-  return cuda::atomic_ref<int, cuda::thread_scope_block>(*p).load(cuda::memory_order_relaxed);
-}
-__device__ __forceinline__ void isl_store(int* p, int v) {
-  cuda::atomic_ref<int, cuda::thread_scope_block>(*p).store(v, cuda::memory_order_relaxed);
-}
-__device__ __forceinline__ void isl_or(int* p, int v) {
-  cuda::atomic_ref<int, cuda::thread_scope_block>(*p).fetch_or(v, cuda::memory_order_relaxed);
-}
-__device__ __forceinline__ void isl_sync() { __syncthreads(); }
-__device__ __forceinline__ int isl_label(int4* SL, int i) { return isl_load(&SL[i].x); }
-__device__ __forceinline__ int isl_bits(int4* SL, int i) { return isl_load(&SL[i].y); }
-
-// Root of x. With `halve`, path halving shortens the walk (x is no root, so no hook targets it);
-// halving stores only during the unions: a late halving store could otherwise overwrite a final
-// label with an intermediate ancestor.
-__device__ int isl_find(int4* SL, int x, bool halve, unsigned int* status) {
-  for (int guard = 0; guard < (1 << 24); ++guard) {
-    int p = isl_load(&SL[x].x);
-    if (p == x) return x;
-    int g = isl_load(&SL[p].x);
-    if (halve && g != p) isl_store(&SL[x].x, g);
-    x = g;
-  }
-  raise_status(status, B2G_DEV_STACK_OVERFLOW);
-  return x;
-}
-
-__device__ void isl_unite(int4* SL, int x, int y, unsigned int* status) {
-  for (int guard = 0; guard < (1 << 20); ++guard) {
-    x = isl_find(SL, x, true, status);
-    y = isl_find(SL, y, true, status);
-    if (x == y) return;
-    if (x < y) {
-      int t = x;
-      x = y;
-      y = t;
-    }
-    int expect = x;  // x was hooked meanwhile when this fails: retry from its root
-    if (cuda::atomic_ref<int, cuda::thread_scope_block>(SL[x].x)
-            .compare_exchange_strong(expect, y, cuda::memory_order_relaxed))
-      return;
-  }
-  raise_status(status, B2G_DEV_STACK_OVERFLOW);
-}
-
-// Applies this step's narrowphase wakes (b2Contact::Update's SetAwake(true) on a touching change,
-// src/dynamics/b2_contact.cpp:183-188), labels the islands, and wakes every member of an island
-// that holds an awake body (the search marks the bodies it reaches awake without resetting their
-// sleep timers, b2_world.cpp:565-566). Sleeping islands are neither integrated nor solved.
-template <int T>
-__device__ void build_islands(const KernelArgs& a, int b0, int nb, int c0, int ncAll, int j0, int nj) {
-  int4* SL = a.sl + b0;
-  int2* BS = a.bstate + b0;
-  for (int i = threadIdx.x; i < nb; i += T) {
-    const int bi = b0 + i;
-    const bool stat = a.btype[bi] == B2G_STATIC;
-    if (a.bwake[bi]) {
-      a.bwake[bi] = 0;
-      if (!stat) {
-        int2 st = BS[i];
-        st.x |= B2G_BS_AWAKE;
-        st.y = 0;
-        BS[i] = st;
-      }
-    }
-    isl_store(&SL[i].x, stat ? -1 : i);
-    isl_store(&SL[i].y, 0);
-    isl_store(&SL[i].z, 0);
-    isl_store(&SL[i].w, 0x7f7fffff);  // FLT_MAX: no member timed yet
-  }
-  isl_sync();
-  for (int k = threadIdx.x; k < ncAll; k += T) {
-    const int2 f = a.cfix[c0 + k];
-    const int ia = a.fbody[f.x] - b0, ib = a.fbody[f.y] - b0;
-    isl_or(&SL[ia].y, B2G_ISL_LINKED);
-    isl_or(&SL[ib].y, B2G_ISL_LINKED);
-    const uint32_t fl = a.cflags[c0 + k];
-    if ((fl & B2G_CONTACT_TOUCHING) && (fl & B2G_CONTACT_ENABLED) && !a.fsensor[f.x] && !a.fsensor[f.y] &&
-        isl_load(&SL[ia].x) >= 0 && isl_load(&SL[ib].x) >= 0)
-      isl_unite(SL, ia, ib, a.status);
-  }
-  for (int k = threadIdx.x; k < nj; k += T) {
-    const JointDev& J = a.joints[j0 + k];
-    const int ia = J.d.body_a - b0, ib = J.d.body_b - b0;
-    isl_or(&SL[ia].y, B2G_ISL_LINKED);
-    isl_or(&SL[ib].y, B2G_ISL_LINKED);
-    if (isl_load(&SL[ia].x) >= 0 && isl_load(&SL[ib].x) >= 0) isl_unite(SL, ia, ib, a.status);
-  }
-  isl_sync();
-  for (int i = threadIdx.x; i < nb; i += T)
-    if (isl_load(&SL[i].x) >= 0) isl_store(&SL[i].x, isl_find(SL, i, false, a.status));
-  isl_sync();
-  for (int i = threadIdx.x; i < nb; i += T) {
-    const int r = isl_label(SL, i);
-    if (r >= 0 && (BS[i].x & B2G_BS_AWAKE)) isl_or(&SL[r].y, B2G_ISL_AWAKE);
-  }
-  isl_sync();
-  for (int i = threadIdx.x; i < nb; i += T) {
-    const int r = isl_label(SL, i);
-    if (r >= 0 && (isl_bits(SL, r) & B2G_ISL_AWAKE)) BS[i].x |= B2G_BS_AWAKE;
-  }
-  isl_sync();
-}
-
-// Island root of a contact or joint between world-local bodies la and lb (one is non-static).
-__device__ __forceinline__ int isl_root(int4* SL, int la, int lb) {
-  const int r = isl_label(SL, la);
-  return r >= 0 ? r : isl_label(SL, lb);
-}
-
-__device__ __forceinline__ bool joint_awake(const KernelArgs& a, const JointDev& J) {
-  return ((a.bstate[J.d.body_a].x | a.bstate[J.d.body_b].x) & B2G_BS_AWAKE) != 0;
-}
-
-// Sleep timers of the bodies solved this step, then islands whose every member has rested for
-// b2_timeToSleep and whose position constraints were solved go to sleep (SetAwake(false): flags,
-// timer, velocities, force and torque cleared; include/box2d/b2_body.h:719-740). A body with no
-// contact and no joint is an orphan: it times itself, and when its timer runs out its velocity and
-// force are cleared but it stays awake (b2World::Solve marks orphans awake after solving them,
-// b2_world.cpp:545-549).
-template <int T>
-__device__ void sleep_islands(const KernelArgs& a, int b0, int nb) {
-  int4* SL = a.sl + b0;
-  int2* BS = a.bstate + b0;
-  const float linTolSqr = B2G_LINEAR_SLEEP_TOL * B2G_LINEAR_SLEEP_TOL;
-  const float angTolSqr = B2G_ANGULAR_SLEEP_TOL * B2G_ANGULAR_SLEEP_TOL;
-  const float h = a.dt;
-  for (int i = threadIdx.x; i < nb; i += T) {
-    const int ex = isl_label(SL, i), ey = isl_bits(SL, i);
-    int2 st = BS[i];
-    if (ex < 0 || !(st.x & B2G_BS_AWAKE)) continue;
-    const int bi = b0 + i;
-    const float4 v4 = a.vel[bi];
-    const bool orphan = !(ey & B2G_ISL_LINKED);
-    float t = 0.0f;
-    if ((st.x & B2G_BS_AUTO_SLEEP) == 0 || v4.z * v4.z > angTolSqr || v4.x * v4.x + v4.y * v4.y > linTolSqr) {
-      st.y = 0;
-    } else {
-      t = __int_as_float(st.y) + h;
-      st.y = __float_as_int(t);
-    }
-    if (orphan) {
-      if (t >= B2G_TIME_TO_SLEEP) {
-        st.y = 0;
-        a.vel[bi] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-        a.force[bi] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-      }
-    } else {
-      // t >= 0: the bit patterns order as the floats
-      cuda::atomic_ref<int, cuda::thread_scope_block>(SL[ex].w).fetch_min(__float_as_int(t), cuda::memory_order_relaxed);
-    }
-    BS[i] = st;
-  }
-  isl_sync();
-  for (int i = threadIdx.x; i < nb; i += T) {
-    const int ex = isl_label(SL, i);
-    if (ex < 0 || !(isl_bits(SL, i) & B2G_ISL_LINKED) || !(BS[i].x & B2G_BS_AWAKE)) continue;
-    const float rmin = __int_as_float(isl_load(&SL[ex].w));
-    if (!(rmin >= B2G_TIME_TO_SLEEP) || !(isl_bits(SL, ex) & B2G_ISL_DONE)) continue;
-    const int bi = b0 + i;
-    BS[i] = make_int2(BS[i].x & ~B2G_BS_AWAKE, 0);
-    a.vel[bi] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-    a.force[bi] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-  }
-}
-
-template <int T>
-__global__ void __launch_bounds__(T, 1024 / T) k_solve(KernelArgs a, int first, int smem_bytes) {
-  extern __shared__ __align__(16) unsigned char smem[];
-  const int w = a.world_order[first + blockIdx.x];
-  if ((a.wflags[w] & B2G_WF_ACTIVE) == 0) return;
-  __shared__ int cranges[65];
-  __shared__ int jranges[65];
-  __shared__ int s_carry;
-  const int4 wb = a.wb[w];
-  const int b0 = wb.x, nb = wb.y, fo = wb.z;
-  const int2 wc = a.wc[w];
-  const int c0 = wc.x, ncAll = wc.y;
-  const int4 wj = a.wj[w];
-  const int j0 = wj.x, nj = wj.y;
-  const float4 wg = a.wg[w];
-  const float h = a.dt;
-  const float dtRatio = wg.z * a.dt;
-  const int wfl = a.wflags[w];
-  const bool warm = (wfl & B2G_WF_WARM) != 0;
-  const bool sleepMode = (wfl & B2G_WF_SLEEPMODE) != 0;
-  const V2 gravity = mk(wg.x, wg.y);
-  const SolverPlanes P = a.sp;
-  int4* const SL = a.sl + b0;
-  int2* const BS = a.bstate + b0;
-
-  // 0. sleep-mode worlds: wakes, islands, awake islands
-  if (sleepMode) build_islands<T>(a, b0, nb, c0, ncAll, j0, nj);
-
-  // 1. solver contacts in list order, with local bodies (static = -1) and colouring priorities
-  if (threadIdx.x == 0) s_carry = 0;
-  __syncthreads();
-  for (int k0 = 0; k0 < ncAll; k0 += T) {
-    int k = k0 + threadIdx.x;
-    int flag = 0;
-    int2 f = make_int2(0, 0);
-    if (k < ncAll) {
-      uint32_t fl = a.cflags[c0 + k];
-      f = a.cfix[c0 + k];
-      flag = ((fl & B2G_CONTACT_TOUCHING) && (fl & B2G_CONTACT_ENABLED) && !a.fsensor[f.x] && !a.fsensor[f.y]) ? 1 : 0;
-      if (flag && sleepMode)  // contacts of sleeping islands are not solved
-        flag = (isl_bits(SL, isl_root(SL, a.fbody[f.x] - b0, a.fbody[f.y] - b0)) & B2G_ISL_AWAKE) ? 1 : 0;
-    }
-    int total;
-    int p = block_scan<T>(flag, &total);
-    if (flag) {
-      int s = c0 + s_carry + p;
-      a.sc_list[s] = c0 + k;
-      int ia = a.fbody[f.x], ib = a.fbody[f.y];
-      a.scb[s] = make_int2((ia - b0) | (a.btype[ia] == B2G_STATIC ? (int)0x80000000 : 0),
-                           (ib - b0) | (a.btype[ib] == B2G_STATIC ? (int)0x80000000 : 0));
-      uint64_t key = a.ckey[c0 + k];
-      a.cprio[s] = contactPriority((uint32_t)(key >> 32) - (uint32_t)fo, (uint32_t)key - (uint32_t)fo);
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) s_carry += total;
-    __syncthreads();
-  }
-  const int nsc = s_carry;
-
-  // 2. colour the solver contacts (shared memory for whatever fits)
-  int ncc = 0;
-  if (nsc > 0) {
-    SmemCarver sc{smem, (size_t)smem_bytes};
-    ColourMem m;
-    m.mask = (unsigned long long*)sc.take(8 * (size_t)nb);
-    m.cnt = (int*)sc.take(4 * (size_t)nb);
-    m.head = (int*)sc.take(4 * (size_t)nb);
-    bool bodySm = m.mask && m.cnt && m.head;
-    if (!bodySm) {
-      m.mask = a.inc_mask + b0;
-      m.cnt = a.inc_cnt + b0;
-      m.head = a.inc_head + b0;
-    }
-    int* list = bodySm ? (int*)sc.take(8 * (size_t)nsc) : nullptr;
-    int2* cb = bodySm ? (int2*)sc.take(8 * (size_t)nsc) : nullptr;
-    int* wl = bodySm ? (int*)sc.take(8 * (size_t)nsc) : nullptr;
-    int8_t* col = bodySm ? (int8_t*)sc.take((size_t)nsc) : nullptr;
-    uint8_t* rdy = bodySm ? (uint8_t*)sc.take((size_t)nsc) : nullptr;
-    bool conSm = list && cb && wl && col && rdy;
-    if (conSm) {
-      for (int k = threadIdx.x; k < nsc; k += T) cb[k] = a.scb[c0 + k];
-      __syncthreads();
-      m.list = list; m.cb = cb; m.col = col; m.rdy = rdy;
-      m.wl0 = wl; m.wl1 = wl + nsc;
-    } else {
-      m.list = a.inc_list + 2 * (int64_t)c0;
-      m.cb = a.scb + c0;
-      m.col = a.ccol + c0;
-      m.rdy = a.cready + c0;
-      m.wl0 = a.cwork + 2 * (int64_t)c0;
-      m.wl1 = a.cwork + 2 * (int64_t)c0 + nsc;
-    }
-    ncc = colour_constraints<T>(nsc, nb, m, a.cprio + c0, a.corder + c0, a.cslot + c0, cranges, a.status);
-    if (conSm) {
-      for (int k = threadIdx.x; k < nsc; k += T) a.ccol[c0 + k] = col[k];
-      __syncthreads();
-    }
-  }
-  // joints: colours fixed per layout
-  const int njc = nj > 0 ? a.ncolors[4 * w + 1] : 0;
-  for (int c = threadIdx.x; c <= njc; c += T) jranges[c] = a.jranges[65 * (int64_t)w + c];
-  if (threadIdx.x == 0) {
-    a.ncolors[4 * w] = ncc;
-    a.ncolors[4 * w + 2] = nsc;
-    a.ncolors[4 * w + 3] = c0;
-    atomicAdd(&a.counters[B2G_CNT_TOUCHING], (unsigned long long)nsc);
-    atomicMax(&a.counters[B2G_CNT_MAXCOLORS], (unsigned long long)(ncc > njc ? ncc : njc));
-  }
-
-  // 3. velocity integration (b2_island.cpp:256-293, SolveOrphan :187-206) into the body-state
-  //    buffer: shared memory (with the bodies' inverse masses) when the world's bodies fit, else
-  //    the global velocity array
-  const bool bsm = (size_t)nb * (sizeof(float4) + sizeof(float2)) <= (size_t)smem_bytes;
-  float4* bs = bsm ? reinterpret_cast<float4*>(smem) : a.vel + b0;
-  float2* msm = bsm ? reinterpret_cast<float2*>(smem + sizeof(float4) * (size_t)nb) : nullptr;
-  const Masses M{msm, a.massd + b0};
-  for (int i = threadIdx.x; i < nb; i += T) {
-    int bi = b0 + i;
-    float4 v4 = a.vel[bi];
-    float4 md = a.massd[bi];
-    if (bsm) msm[i] = make_float2(md.y, md.w);
-    if (a.btype[bi] == B2G_DYNAMIC && (!sleepMode || (BS[i].x & B2G_BS_AWAKE))) {
-      float4 dmp = a.damp[bi];
-      float4 fr = a.force[bi];
-      V2 v = mk(v4.x, v4.y);
-      float wv = v4.z;
-      addTo(v, (h * md.y) * (dmp.z * md.x * gravity + mk(fr.x, fr.y)));
-      wv += h * md.w * fr.z;
-      v.x /= (1.0f + h * dmp.x);
-      v.y /= (1.0f + h * dmp.x);
-      wv /= (1.0f + h * dmp.y);
-      v4 = make_float4(v.x, v.y, wv, 0.0f);
-      bs[i] = v4;
-    } else if (bsm) {
-      bs[i] = v4;
-    }
-  }
-  __syncthreads();
-
-  // 4. prepare (b2ContactSolver::Initialize + InitializeVelocityConstraints) in list order, each
-  //    constraint written to its colour-ordered slot
-  for (int k = threadIdx.x; k < nsc; k += T) {
-    int ci = a.sc_list[c0 + k];
-    int p = a.cslot[c0 + k];
-    int2 lb = a.scb[c0 + k];
-    int la = lb.x & 0x7fffffff, lbb = lb.y & 0x7fffffff;
-    int ia = b0 + la, ib = b0 + lbb;
-    int2 f = a.cfix[ci];
-    b2g_manifold m = ld_manifold(&a.cman[ci]);
-    VCDev vc;
-    for (int q = 0; q < 4; ++q) vc.K[q] = vc.NM[q] = 0.0f;
-    prepareContact(vc, m, a.cmat[ci], a.frad[f.x], a.frad[f.y], la, lbb, a.massd[ia], a.massd[ib], a.lc[ia], a.lc[ib],
-                   a.pos[ia], bs[la], a.pos[ib], bs[lbb], dtRatio, warm, ci);
-    store_planes(P, c0 + p, vc);
-  }
-  __syncthreads();
-  float4* jb = bs - b0;  // joints address bodies by global index
-
-  // 5. warm start contacts, then joint InitVelocityConstraints, colour by colour
-  auto fetchV = [&](int slot, VelRows& r) { fetch_vel(P, slot, r); };
-  auto fetchP = [&](int slot, PosRows& r) { fetch_pos(P, slot, r); };
-  if (warm) {
-    colour_sweep<T, VelRows>(cranges, ncc, c0, fetchV, [&](int slot, const VelRows& r) {
-      VCDev vc;
-      unpack_vel(r, vc, M);
-      warmStartContact(vc, bs);
-    });
-  }
-  for (int c = 0; c < njc; ++c) {
-    int s = jranges[c], e = jranges[c + 1];
-    const int step = c == 63 ? 1 : T, i0 = c == 63 ? s : s + threadIdx.x;
-    if (c != 63 || threadIdx.x == 0)
-      for (int i = i0; i < e; i += step) {
-        JointDev& J = a.joints[j0 + a.jorder[j0 + i]];
-        if (sleepMode && !joint_awake(a, J)) continue;
-        jointInit(J, a.massd, a.lc, a.pos, jb, a.dt, dtRatio, warm);
-      }
-    __syncthreads();
-  }
-
-  // 6. velocity iterations: joints, then contacts (b2_island.cpp:327-346)
-  for (int it = 0; it < a.vi; ++it) {
-    for (int c = 0; c < njc; ++c) {
-      int s = jranges[c], e = jranges[c + 1];
-      const int step = c == 63 ? 1 : T, i0 = c == 63 ? s : s + threadIdx.x;
-      if (c != 63 || threadIdx.x == 0)
-        for (int i = i0; i < e; i += step) {
-          JointDev& J = a.joints[j0 + a.jorder[j0 + i]];
-          if (sleepMode && !joint_awake(a, J)) continue;
-          jointSolveVelocity(J, jb, a.dt, a.inv_dt);
-        }
-      __syncthreads();
-    }
-    colour_sweep<T, VelRows>(cranges, ncc, c0, fetchV, [&](int slot, const VelRows& r) {
-      VCDev vc;
-      unpack_vel(r, vc, M);
-      solveContactVelocity(vc, bs);
-      P.imp[slot] = make_float4(vc.normalImpulse[0], vc.normalImpulse[1], vc.tangentImpulse[0], vc.tangentImpulse[1]);
-    });
-  }
-
-  // 7. StoreImpulses (b2_contact_solver.cpp:641-657)
-  for (int p = threadIdx.x; p < nsc; p += T) {
-    int pc = (P.idx[c0 + p].x >> 24) & 15;
-    float4 im = P.imp[c0 + p];
-    b2g_manifold* m = &a.cman[P.cid[c0 + p]];
-    if (pc > 0) { m->points[0].normal_impulse = im.x; m->points[0].tangent_impulse = im.z; }
-    if (pc > 1) { m->points[1].normal_impulse = im.y; m->points[1].tangent_impulse = im.w; }
-  }
-
-  // 8. integrate positions (b2_island.cpp:349-385); the buffer switches to positions
-  for (int i = threadIdx.x; i < nb; i += T) {
-    int bi = b0 + i;
-    float4 p4 = a.pos[bi];
-    if (a.btype[bi] == B2G_STATIC || (sleepMode && !(BS[i].x & B2G_BS_AWAKE))) {
-      if (bsm) bs[i] = p4;
-      continue;
-    }
-    float4 v4 = bs[i];
-    V2 c = mk(p4.x, p4.y);
-    float an = p4.z;
-    V2 v = mk(v4.x, v4.y);
-    float wv = v4.z;
-    V2 translation = h * v;
-    if (dot(translation, translation) > B2G_MAX_TRANSLATION_SQ) {
-      float ratio = B2G_MAX_TRANSLATION / lengthOf(translation);
-      v.x *= ratio;
-      v.y *= ratio;
-    }
-    float rotation = h * wv;
-    if (rotation * rotation > B2G_MAX_ROTATION_SQ) {
-      float ratio = B2G_MAX_ROTATION / fabs2(rotation);
-      wv *= ratio;
-    }
-    addTo(c, h * v);
-    an += h * wv;
-    a.vel[bi] = make_float4(v.x, v.y, wv, 0.0f);
-    if (bsm) bs[i] = make_float4(c.x, c.y, an, 0.0f);
-    else a.pos[bi] = make_float4(c.x, c.y, an, 0.0f);
-  }
-  __syncthreads();
-  float4* ps = bsm ? bs : a.pos + b0;
-  float4* jp = ps - b0;
-
-  // 9. position iterations: contacts then joints (b2_island.cpp:387-428). Early exit for the
-  //    world; in sleep-mode worlds per island, as the reference's island loop: an island whose
-  //    constraints were all okay in an iteration is done and no longer iterated.
-  for (int it = 0; it < a.pi; ++it) {
-    int okay = 1;
-    colour_sweep<T, PosRows>(cranges, ncc, c0, fetchP, [&](int slot, const PosRows& r) {
-      VCDev vc;
-      unpack_pos(r, vc, M);
-      int root = 0;
-      if (sleepMode) {
-        root = isl_root(SL, vc.indexA, vc.indexB);
-        if (isl_bits(SL, root) & B2G_ISL_DONE) return;
-      }
-      if (!(solveContactPosition(vc, ps) >= -3.0f * B2G_LINEAR_SLOP)) {
-        okay = 0;
-        if (sleepMode) isl_store(&SL[root].z, it + 1);
-      }
-    });
-    for (int c = 0; c < njc; ++c) {
-      int s = jranges[c], e = jranges[c + 1];
-      const int step = c == 63 ? 1 : T, i0 = c == 63 ? s : s + threadIdx.x;
-      if (c != 63 || threadIdx.x == 0)
-        for (int i = i0; i < e; i += step) {
-          JointDev& J = a.joints[j0 + a.jorder[j0 + i]];
-          int root = 0;
-          if (sleepMode) {
-            if (!joint_awake(a, J)) continue;
-            root = isl_root(SL, J.d.body_a - b0, J.d.body_b - b0);
-            if (isl_bits(SL, root) & B2G_ISL_DONE) continue;
-          }
-          if (!jointSolvePosition(J, jp)) {
-            okay = 0;
-            if (sleepMode) isl_store(&SL[root].z, it + 1);
-          }
-        }
-      __syncthreads();
-    }
-    if (sleepMode) {
-      isl_sync();
-      int pending = 0;
-      for (int i = threadIdx.x; i < nb; i += T) {
-        const int ey = isl_bits(SL, i);
-        if (isl_label(SL, i) != i || !(ey & B2G_ISL_AWAKE) || (ey & B2G_ISL_DONE)) continue;
-        if (isl_load(&SL[i].z) == it + 1) pending = 1;
-        else isl_or(&SL[i].y, B2G_ISL_DONE);
-      }
-      if (!__syncthreads_or(pending)) break;
-    } else if (__syncthreads_and(okay)) {
-      break;
-    }
-  }
-
-  // 10. transforms (b2Body::SynchronizeTransform, include/box2d/b2_body.h:957-961), finite check
-  int bad = 0;
-  for (int i = threadIdx.x; i < nb; i += T) {
-    int bi = b0 + i;
-    if (a.btype[bi] == B2G_STATIC || (sleepMode && !(BS[i].x & B2G_BS_AWAKE))) continue;
-    float4 p4 = ps[i];
-    if (bsm) a.pos[bi] = p4;
-    Rot q = rotOf(p4.z);
-    float2 l = a.lc[bi];
-    V2 p = mk(p4.x, p4.y) - mul(q, mk(l.x, l.y));
-    a.xf[bi] = make_float4(p.x, p.y, q.s, q.c);
-    float4 v4 = a.vel[bi];
-    if (!isfinite(p4.x) || !isfinite(p4.y) || !isfinite(p4.z) || !isfinite(v4.x) || !isfinite(v4.y) || !isfinite(v4.z))
-      bad = 1;
-  }
-  if (__syncthreads_or(bad) && threadIdx.x == 0) {  // the host freezes this world; the others go on
-    a.wfault[w] = 1;
-    atomicOr(a.status, B2G_DEV_NONFINITE);
-  }
-
-  // 11. sleep timers (b2_island.cpp:444-483; orphans b2Island::SolveOrphan :230-249)
-  if (wfl & B2G_WF_ALLOW_SLEEP) sleep_islands<T>(a, b0, nb);
-  if (a.events_on) {
-    for (int p = threadIdx.x; p < nsc; p += T) {
-      int pc = (P.idx[c0 + p].x >> 24) & 15;
-      float4 im = P.imp[c0 + p];
-      int2 f = a.cfix[P.cid[c0 + p]];
-      float ni[2] = {im.x, im.y}, ti[2] = {im.z, im.w};
-      record_event(a, B2G_EVENT_POSTSOLVE, w, f.x - fo, f.y - fo, pc, ni, ti, 0);
-    }
-  }
-  if (threadIdx.x == 0 && a.dt > 0.0f) a.wg[w].z = a.inv_dt;
-}
 
 // Joint colouring of worlds [w0, w0 + gridDim.x), once per layout: joints and the static flags
 // of their bodies change only through structural edits, which re-upload the layout.
@@ -988,10 +119,13 @@ void launch_colour_check(const KernelArgs& a, int nw, cudaStream_t s) {
 // Class by world body count: threads per CTA and the dynamic shared memory that holds the
 // world's body state and inverse masses (24 B/body) and, room permitting, its colouring arrays
 // (16 B/body + 26 B per contact, about 68 B/body at two contacts per body).
-static const int kClassMaxBodies[B2G_SOLVE_CLASSES] = {64, 256, 1024, 4096, 1 << 30};
-// Shared-memory allowance by threads per CTA (64, 128, 256, 512, 1024): at 64 registers per
-// thread the SM holds 1024 / T such CTAs, and the allowance keeps that many resident.
-static const int kSmemCapByThreads[B2G_SOLVE_CLASSES] = {16 << 10, 24 << 10, 56 << 10, 110 << 10, 200 << 10};
+static const int kClassMaxBodies[B2G_SOLVE_CLASSES] = {64, 256, 1024, 8192, 1 << 30};
+// Shared-memory allowance by threads per CTA (64, 128, 256, 512, 1024) of the occupancy and the
+// wide builds: the SM holds kSolveBlocks<T, WIDE> such CTAs, and the allowance keeps that many
+// resident.
+static const int kSmemCapByThreads[2][B2G_SOLVE_CLASSES] = {{16 << 10, 24 << 10, 56 << 10, 110 << 10, 200 << 10},
+                                                            {27 << 10, 54 << 10, 110 << 10, 220 << 10, 220 << 10}};
+static int g_num_sms = 0;
 
 static int threads_index(int t) {
   int k = 0;
@@ -1002,7 +136,7 @@ static int threads_index(int t) {
 bool solver_threads_valid(int t) { return t == 64 || t == 128 || t == 256 || t == 512 || t == 1024; }
 
 std::vector<SolveClass> plan_solve_classes(const std::vector<int>& order, const std::vector<int>& bodies,
-                                           const int* class_threads) {
+                                           const int* class_threads, float wide_waves) {
   // `order` lists worlds by body count, largest first: each class is a contiguous range
   std::vector<SolveClass> out;
   int n = (int)order.size();
@@ -1019,16 +153,19 @@ std::vector<SolveClass> plan_solve_classes(const std::vector<int>& order, const 
     int64_t need = 68ll * nbmax;  // colouring at two contacts per body: 16 + 2 x 26 B per body
     need = (need + 15) & ~15ll;
     int t = class_threads[c];
-    int cap = kSmemCapByThreads[threads_index(t)];
+    int ti = threads_index(t);
+    // few enough worlds that the slowest one sets the class's time: the wide build
+    bool wide = g_num_sms > 0 && (double)(i - start) * t <= (double)wide_waves * 512.0 * g_num_sms;
+    int cap = kSmemCapByThreads[wide ? 1 : 0][ti];
     int smem = (int)(need < cap ? need : cap);
-    out.push_back({start, i - start, t, smem, c});
+    out.push_back({start, i - start, t, smem, c, wide});
   }
   return out;
 }
 
 template <int T>
 static void set_smem_attr(int c) {
-  cudaFuncSetAttribute(k_solve<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemCapByThreads[c]);
+  cudaFuncSetAttribute(k_solve<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemCapByThreads[0][c]);
 }
 
 void solver_setup() {
@@ -1037,15 +174,22 @@ void solver_setup() {
   set_smem_attr<256>(2);
   set_smem_attr<512>(3);
   set_smem_attr<1024>(4);
+  solve_wide_setup(kSmemCapByThreads[1]);
+  int dev = 0;
+  if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev);
 }
 
 static void launch_class(const KernelArgs& a, const SolveClass& c, cudaStream_t s) {
+  if (c.wide) {
+    launch_solve_class_wide(a, c, s);
+    return;
+  }
   switch (c.threads) {
-    case 64: k_solve<64><<<c.count, 64, c.smem, s>>>(a, c.first, c.smem); break;
-    case 128: k_solve<128><<<c.count, 128, c.smem, s>>>(a, c.first, c.smem); break;
-    case 256: k_solve<256><<<c.count, 256, c.smem, s>>>(a, c.first, c.smem); break;
-    case 512: k_solve<512><<<c.count, 512, c.smem, s>>>(a, c.first, c.smem); break;
-    default: k_solve<1024><<<c.count, 1024, c.smem, s>>>(a, c.first, c.smem); break;
+    case 64: k_solve<64, false><<<c.count, 64, c.smem, s>>>(a, c.first, c.smem); break;
+    case 128: k_solve<128, false><<<c.count, 128, c.smem, s>>>(a, c.first, c.smem); break;
+    case 256: k_solve<256, false><<<c.count, 256, c.smem, s>>>(a, c.first, c.smem); break;
+    case 512: k_solve<512, false><<<c.count, 512, c.smem, s>>>(a, c.first, c.smem); break;
+    default: k_solve<1024, false><<<c.count, 1024, c.smem, s>>>(a, c.first, c.smem); break;
   }
 }
 

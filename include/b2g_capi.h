@@ -372,10 +372,15 @@ B2G_API int b2g_batch_set_graphs(b2g_batch* b, int32_t enable);
  * reference solves serially). */
 B2G_API int b2g_batch_set_debug_checks(b2g_batch* b, int32_t enable);
 /* Threads per world CTA of the solver for each world size class (worlds of at most 64, 256,
- * 1024 and 4096 bodies, and larger), 5 entries each one of 64, 128, 256, 512, 1024 (defaults
+ * 1024 and 8192 bodies, and larger), 5 entries each one of 64, 128, 256, 512, 1024 (defaults
  * 64, 128, 256, 512, 1024). A tuning knob: results do not depend on it. No reference counterpart. */
 B2G_API int b2g_batch_set_solver_threads(b2g_batch* b, const int32_t* threads);
 B2G_API int b2g_batch_get_solver_threads(b2g_batch* b, int32_t* threads);
+/* The solver kernel comes in two builds: one for occupancy (1024 threads per SM, at most 64
+ * registers a thread) and a wide one (512 threads per SM, up to 128 registers) whose per-world
+ * solve is faster. A size class runs the wide build when its worlds fill at most `waves` waves of
+ * it (default 2; 0 never, a large value always). A tuning knob: results do not depend on it. */
+B2G_API int b2g_batch_set_solver_waves(b2g_batch* b, float waves);
 /* Autotuner: picks each size class's threads per world by timing the solver over `steps` eager
  * steps per candidate (the class's current count, half and double), largest worlds first. The
  * steps are real steps of the batch (its worlds advance; their number goes to steps_taken);
