@@ -165,6 +165,7 @@ static KernelArgs make_args(Batch* b) {
   a.inc_mask = b->inc_mask.p; a.inc_list = b->inc_list.p; a.jinc_list = b->jinc_list.p; a.cwork = b->cwork.p; a.jwork = b->jwork.p; a.jcb = b->jcb.p;
   a.jcol = b->jcol.p; a.jorder = b->jorder.p; a.jranges = b->jranges.p; a.jprio = b->jprio.p;
   a.jready = b->jready.p; a.ncolors = b->ncolors.p;
+  a.jplanes = b->jplanes.p; a.jstride = b->NJ;
   a.events = b->events.p; a.event_cap = b->event_cap; a.events_on = b->events_on ? 1 : 0;
   a.counters = b->counters.p; a.status = b->status.p;
   return a;
@@ -401,6 +402,7 @@ int upload_all(Batch* b) {
   TRY(ensure(b, b->inc_cnt, NB)); TRY(ensure(b, b->inc_head, NB)); TRY(ensure(b, b->inc_mask, NB));
   TRY(ensure(b, b->jinc_list, 2 * (size_t)NJ)); TRY(ensure(b, b->jwork, 2 * (size_t)NJ)); TRY(ensure(b, b->jcol, NJ)); TRY(ensure(b, b->jorder, NJ));
   TRY(ensure(b, b->jcb, NJ)); TRY(ensure(b, b->jprio, NJ)); TRY(ensure(b, b->jready, NJ));
+  TRY(ensure(b, b->jplanes, (size_t)B2G_JV_ROWS * NJ));
   TRY(ensure(b, b->status, 1)); TRY(ensure(b, b->counters, 5));
   b->NW = NW; b->NB = NB; b->NF = NF; b->NJ = NJ; b->NC = NC;
   {
@@ -618,6 +620,7 @@ static int flush_tail(Batch* b, TailPack& P) {
   TRY(ensure(b, b->inc_cnt, NB)); TRY(ensure(b, b->inc_head, NB)); TRY(ensure(b, b->inc_mask, NB));
   TRY(ensure(b, b->jinc_list, 2 * (size_t)NJ)); TRY(ensure(b, b->jwork, 2 * (size_t)NJ)); TRY(ensure(b, b->jcol, NJ, true)); TRY(ensure(b, b->jorder, NJ, true));
   TRY(ensure(b, b->jcb, NJ, true)); TRY(ensure(b, b->jprio, NJ, true)); TRY(ensure(b, b->jready, NJ));
+  TRY(ensure(b, b->jplanes, (size_t)B2G_JV_ROWS * NJ));
   b->NW = NW; b->NB = NB; b->NF = NF; b->NJ = NJ;
   // joint colours of the appended worlds; a colouring failure reaches the step's status check
   launch_joint_colour(make_args(b), w0, NW - w0, b->stream);
@@ -1277,7 +1280,7 @@ B2G_API int b2g_batch_destroy(b2g_batch* b) {
   release(b, b->sp_bk); release(b, b->sp_kn); release(b, b->sp_imp); release(b, b->sp_idx); release(b, b->sp_lcs);
   release(b, b->sp_lnp); release(b, b->sp_lps); release(b, b->sp_rad);
   release(b, b->jinc_list); release(b, b->jcol); release(b, b->jorder); release(b, b->jcb); release(b, b->jranges);
-  release(b, b->jprio); release(b, b->jready);
+  release(b, b->jprio); release(b, b->jready); release(b, b->jplanes);
   release(b, b->ncolors); release(b, b->events);
   release(b, b->q_world); release(b, b->q_counts); release(b, b->q_out); release(b, b->q_box); release(b, b->q_offs);
   release(b, b->q_hits);

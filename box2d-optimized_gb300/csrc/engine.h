@@ -125,6 +125,7 @@ struct SolveClass {
   bool wide;  // the 128-register build (few worlds: latency-bound) rather than the 64-register one
 };
 #define B2G_SOLVE_CLASSES 5
+#define B2G_JV_ROWS 9  // float4 rows of one joint's velocity-pass record (solver_dev.cuh)
 
 // Status word the kernels write instead of trapping (bounded waits and capacity checks).
 #define B2G_DEV_OK 0u
@@ -265,6 +266,7 @@ struct Batch {
   DBuf<int> jorder, jranges;
   DBuf<uint32_t> jprio;
   DBuf<uint8_t> jready;
+  DBuf<float4> jplanes;           // joint velocity rows, B2G_JV_ROWS planes of NJ slots (solve scratch)
   DBuf<int> ncolors;              // per world: contact colours, joint colours, solver contacts, slot base
   // compaction targets: swapped with the live arrays by a device compaction, kept for the next
   struct Spare {

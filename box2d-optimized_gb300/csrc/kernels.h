@@ -59,6 +59,8 @@ struct KernelArgs {
   float4* aabb;
 
   JointDev* joints;
+  float4* jplanes;  // joint velocity rows (B2G_JV_ROWS planes of jstride slots; solve scratch)
+  int jstride;
   const uint64_t* nocollide;
   int n_nocollide;
 

@@ -728,8 +728,12 @@ __global__ void __launch_bounds__(T, kSolveBlocks<T, WIDE>) k_solve(KernelArgs a
     if (c != 63 || threadIdx.x == 0)
       for (int i = i0; i < e; i += step) {
         JointDev& J = a.joints[j0 + a.jorder[j0 + i]];
-        if (sleepMode && !joint_awake(a, J)) continue;
+        if (sleepMode && !joint_awake(a, J)) {
+          jointPackAsleep(a.jplanes, j0 + i);
+          continue;
+        }
         jointInit(J, a.massd, a.lc, a.pos, jb, a.dt, dtRatio, warm);
+        jointPackVel(J, a.jplanes, a.jstride, j0 + i);
       }
     __syncthreads();
   }
@@ -740,11 +744,7 @@ __global__ void __launch_bounds__(T, kSolveBlocks<T, WIDE>) k_solve(KernelArgs a
       int s = jranges[c], e = jranges[c + 1];
       const int step = c == 63 ? 1 : T, i0 = c == 63 ? s : s + threadIdx.x;
       if (c != 63 || threadIdx.x == 0)
-        for (int i = i0; i < e; i += step) {
-          JointDev& J = a.joints[j0 + a.jorder[j0 + i]];
-          if (sleepMode && !joint_awake(a, J)) continue;
-          jointSolveVelocity(J, jb, a.dt, a.inv_dt);
-        }
+        for (int i = i0; i < e; i += step) jointSolveVelocitySlot(a.jplanes, a.jstride, j0 + i, jb, a.dt, a.inv_dt);
       __syncthreads();
     }
     colour_sweep<T, VelRows>(cranges, ncc, c0, fetchV, [&](int slot, const VelRows& r) {
@@ -755,7 +755,8 @@ __global__ void __launch_bounds__(T, kSolveBlocks<T, WIDE>) k_solve(KernelArgs a
     });
   }
 
-  // 7. StoreImpulses (b2_contact_solver.cpp:641-657)
+  // 7. StoreImpulses (b2_contact_solver.cpp:641-657); the joints' impulses back into their records
+  for (int i = threadIdx.x; i < nj; i += T) jointStoreImpulses(a.jplanes, a.jstride, j0 + i, a.joints[j0 + a.jorder[j0 + i]]);
   for (int p = threadIdx.x; p < nsc; p += T) {
     int pc = (P.idx[c0 + p].x >> 24) & 15;
     float4 im = P.imp[c0 + p];

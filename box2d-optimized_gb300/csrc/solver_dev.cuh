@@ -1018,6 +1018,184 @@ B2G_HD void jointSolveVelocity(JointDev& J, float4* vel, float dt, float inv_dt)
   if (moves(J.mB, J.invIB)) storeVel(vel, J.iB, vB, wB);
 }
 
+#ifdef __CUDACC__
+// ---- joint velocity rows. A joint's velocity pass reads a few dozen of its record's fields, spread
+// over the record; read from the record in global memory, each field is a separate transaction per
+// thread and the pass costs about ten contact solves. The rows hold those fields packed per type
+// (B2G_JV_ROWS float4 planes of `stride` slots, one slot per joint in colour order, so a colour's
+// threads read consecutive slots), written by the joint's init; the velocity iterations run the
+// same jointSolveVelocity on a register copy, and the accumulated impulses go back to the record
+// after the last iteration.
+//   row 0: iA, iB, type, flags (as int bits)     row 1: mA, mB, invIA, invIB
+//   rows 2-6: per type (below; row 4 holds K for the prismatic joint, motorMass, bias and gamma
+//             for the wheel joint)               row 7: impulse 0-2, motorImpulse
+//   row 8: lowerImpulse, upperImpulse
+#define B2G_JV_MOTOR 1
+#define B2G_JV_LIMIT 2
+#define B2G_JV_ASLEEP 4
+
+__device__ __forceinline__ void jointPackVel(const JointDev& J, float4* P, int stride, int slot) {
+  float4 r[B2G_JV_ROWS];
+  for (int k = 0; k < B2G_JV_ROWS; ++k) r[k] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  const int flags = (J.d.enable_motor ? B2G_JV_MOTOR : 0) | (J.d.enable_limit ? B2G_JV_LIMIT : 0);
+  r[0] = make_float4(__int_as_float(J.iA), __int_as_float(J.iB), __int_as_float(J.d.type), __int_as_float(flags));
+  r[1] = make_float4(J.mA, J.mB, J.invIA, J.invIB);
+  switch (J.d.type) {
+    case B2G_JOINT_REVOLUTE:
+      r[2] = make_float4(J.rA[0], J.rA[1], J.rB[0], J.rB[1]);
+      r[3] = make_float4(J.K[0], J.K[1], J.K[2], J.K[3]);
+      r[4] = make_float4(J.axialMass, J.angle, J.d.lower, J.d.upper);
+      r[5] = make_float4(J.d.motor_speed, J.d.max_motor, 0.0f, 0.0f);
+      break;
+    case B2G_JOINT_PRISMATIC:
+    case B2G_JOINT_WHEEL:
+      r[2] = make_float4(J.axis[0], J.axis[1], J.perp[0], J.perp[1]);
+      r[3] = make_float4(J.a1, J.a2, J.s1, J.s2);
+      r[4] = make_float4(J.K[0], J.K[1], J.K[2], J.K[3]);
+      r[5] = make_float4(J.axialMass, J.translation, J.d.lower, J.d.upper);
+      r[6] = make_float4(J.d.motor_speed, J.d.max_motor, J.mass, J.springMass);
+      r[4] = J.d.type == B2G_JOINT_WHEEL ? make_float4(J.motorMass, J.bias, J.gamma, 0.0f) : r[4];
+      break;
+    case B2G_JOINT_DISTANCE:
+      r[2] = make_float4(J.rA[0], J.rA[1], J.rB[0], J.rB[1]);
+      r[3] = make_float4(J.u[0], J.u[1], J.softMass, J.bias);
+      r[4] = make_float4(J.gamma, J.mass, J.currentLength, J.d.min_length);
+      r[5] = make_float4(J.d.max_length, J.d.stiffness, 0.0f, 0.0f);
+      break;
+    case B2G_JOINT_WELD:
+      r[2] = make_float4(J.rA[0], J.rA[1], J.rB[0], J.rB[1]);
+      r[3] = make_float4(J.mass3[0], J.mass3[1], J.mass3[2], J.mass3[3]);
+      r[4] = make_float4(J.mass3[4], J.mass3[5], J.mass3[6], J.mass3[7]);
+      r[5] = make_float4(J.mass3[8], J.bias, J.gamma, J.d.stiffness);
+      break;
+    case B2G_JOINT_MOTOR:
+    case B2G_JOINT_FRICTION:
+      r[2] = make_float4(J.rA[0], J.rA[1], J.rB[0], J.rB[1]);
+      r[3] = make_float4(J.K[0], J.K[1], J.K[2], J.K[3]);
+      r[4] = make_float4(J.axialMass, J.d.max_force, J.d.max_torque, J.d.correction_factor);
+      r[5] = make_float4(J.angularError, J.err[0], J.err[1], 0.0f);
+      break;
+    case B2G_JOINT_MOUSE:
+      r[2] = make_float4(J.rA[0], J.rA[1], J.rB[0], J.rB[1]);
+      r[3] = make_float4(J.K[0], J.K[1], J.K[2], J.K[3]);
+      r[4] = make_float4(J.err[0], J.err[1], J.gamma, J.d.max_force);
+      break;
+    default:  // pulley
+      r[2] = make_float4(J.rA[0], J.rA[1], J.rB[0], J.rB[1]);
+      r[3] = make_float4(J.u[0], J.u[1], J.uB[0], J.uB[1]);
+      r[4] = make_float4(J.mass, J.d.ratio, 0.0f, 0.0f);
+      break;
+  }
+  r[7] = make_float4(J.impulse[0], J.impulse[1], J.impulse[2], J.motorImpulse);
+  r[8] = make_float4(J.lowerImpulse, J.upperImpulse, 0.0f, 0.0f);
+#pragma unroll
+  for (int k = 0; k < B2G_JV_ROWS; ++k) P[(int64_t)k * stride + slot] = r[k];
+}
+
+// A joint left out of this step (its island sleeps): its velocity iterations skip it.
+__device__ __forceinline__ void jointPackAsleep(float4* P, int slot) {
+  P[slot] = make_float4(0.0f, 0.0f, 0.0f, __int_as_float(B2G_JV_ASLEEP));
+}
+
+// One velocity iteration of the joint in `slot`: the register copy of its rows through
+// jointSolveVelocity, its impulses written back to the rows.
+__device__ __forceinline__ void jointSolveVelocitySlot(float4* P, int stride, int slot, float4* vel, float dt,
+                                                      float inv_dt) {
+  const float4 r0 = P[slot];
+  const int flags = __float_as_int(r0.w);
+  if (flags & B2G_JV_ASLEEP) return;
+  const float4 r1 = P[(int64_t)stride + slot], r2 = P[(int64_t)2 * stride + slot], r3 = P[(int64_t)3 * stride + slot];
+  const float4 r4 = P[(int64_t)4 * stride + slot], r5 = P[(int64_t)5 * stride + slot], r6 = P[(int64_t)6 * stride + slot];
+  const float4 r7 = P[(int64_t)7 * stride + slot], r8 = P[(int64_t)8 * stride + slot];
+  // each type on its own register copy with a constant type, so that only its branch of
+  // jointSolveVelocity remains and the copy stays in registers
+#define B2G_JV_COMMON(TYPE)                                                                   \
+  JointDev J;                                                                                 \
+  J.iA = __float_as_int(r0.x); J.iB = __float_as_int(r0.y); J.d.type = TYPE;                  \
+  J.d.enable_motor = (flags & B2G_JV_MOTOR) ? 1 : 0;                                          \
+  J.d.enable_limit = (flags & B2G_JV_LIMIT) ? 1 : 0;                                          \
+  J.mA = r1.x; J.mB = r1.y; J.invIA = r1.z; J.invIB = r1.w;                                   \
+  J.impulse[0] = r7.x; J.impulse[1] = r7.y; J.impulse[2] = r7.z; J.motorImpulse = r7.w;       \
+  J.lowerImpulse = r8.x; J.upperImpulse = r8.y;                                               \
+  J.rA[0] = r2.x; J.rA[1] = r2.y; J.rB[0] = r2.z; J.rB[1] = r2.w
+#define B2G_JV_FINISH                                                                         \
+  jointSolveVelocity(J, vel, dt, inv_dt);                                                     \
+  P[(int64_t)7 * stride + slot] = make_float4(J.impulse[0], J.impulse[1], J.impulse[2], J.motorImpulse); \
+  P[(int64_t)8 * stride + slot] = make_float4(J.lowerImpulse, J.upperImpulse, 0.0f, 0.0f)
+  switch (__float_as_int(r0.z)) {
+    case B2G_JOINT_REVOLUTE: {
+      B2G_JV_COMMON(B2G_JOINT_REVOLUTE);
+      J.K[0] = r3.x; J.K[1] = r3.y; J.K[2] = r3.z; J.K[3] = r3.w;
+      J.axialMass = r4.x; J.angle = r4.y; J.d.lower = r4.z; J.d.upper = r4.w;
+      J.d.motor_speed = r5.x; J.d.max_motor = r5.y;
+      B2G_JV_FINISH;
+    } break;
+    case B2G_JOINT_PRISMATIC: {
+      B2G_JV_COMMON(B2G_JOINT_PRISMATIC);
+      J.axis[0] = r2.x; J.axis[1] = r2.y; J.perp[0] = r2.z; J.perp[1] = r2.w;
+      J.a1 = r3.x; J.a2 = r3.y; J.s1 = r3.z; J.s2 = r3.w;
+      J.K[0] = r4.x; J.K[1] = r4.y; J.K[2] = r4.z; J.K[3] = r4.w;
+      J.axialMass = r5.x; J.translation = r5.y; J.d.lower = r5.z; J.d.upper = r5.w;
+      J.d.motor_speed = r6.x; J.d.max_motor = r6.y;
+      B2G_JV_FINISH;
+    } break;
+    case B2G_JOINT_WHEEL: {
+      B2G_JV_COMMON(B2G_JOINT_WHEEL);
+      J.axis[0] = r2.x; J.axis[1] = r2.y; J.perp[0] = r2.z; J.perp[1] = r2.w;
+      J.a1 = r3.x; J.a2 = r3.y; J.s1 = r3.z; J.s2 = r3.w;
+      J.motorMass = r4.x; J.bias = r4.y; J.gamma = r4.z;
+      J.axialMass = r5.x; J.translation = r5.y; J.d.lower = r5.z; J.d.upper = r5.w;
+      J.d.motor_speed = r6.x; J.d.max_motor = r6.y; J.mass = r6.z; J.springMass = r6.w;
+      B2G_JV_FINISH;
+    } break;
+    case B2G_JOINT_DISTANCE: {
+      B2G_JV_COMMON(B2G_JOINT_DISTANCE);
+      J.u[0] = r3.x; J.u[1] = r3.y; J.softMass = r3.z; J.bias = r3.w;
+      J.gamma = r4.x; J.mass = r4.y; J.currentLength = r4.z; J.d.min_length = r4.w;
+      J.d.max_length = r5.x; J.d.stiffness = r5.y;
+      B2G_JV_FINISH;
+    } break;
+    case B2G_JOINT_WELD: {
+      B2G_JV_COMMON(B2G_JOINT_WELD);
+      J.mass3[0] = r3.x; J.mass3[1] = r3.y; J.mass3[2] = r3.z; J.mass3[3] = r3.w;
+      J.mass3[4] = r4.x; J.mass3[5] = r4.y; J.mass3[6] = r4.z; J.mass3[7] = r4.w;
+      J.mass3[8] = r5.x; J.bias = r5.y; J.gamma = r5.z; J.d.stiffness = r5.w;
+      B2G_JV_FINISH;
+    } break;
+    case B2G_JOINT_MOTOR:
+    case B2G_JOINT_FRICTION: {
+      B2G_JV_COMMON(__float_as_int(r0.z));
+      J.K[0] = r3.x; J.K[1] = r3.y; J.K[2] = r3.z; J.K[3] = r3.w;
+      J.axialMass = r4.x; J.d.max_force = r4.y; J.d.max_torque = r4.z; J.d.correction_factor = r4.w;
+      J.angularError = r5.x; J.err[0] = r5.y; J.err[1] = r5.z;
+      B2G_JV_FINISH;
+    } break;
+    case B2G_JOINT_MOUSE: {
+      B2G_JV_COMMON(B2G_JOINT_MOUSE);
+      J.K[0] = r3.x; J.K[1] = r3.y; J.K[2] = r3.z; J.K[3] = r3.w;
+      J.err[0] = r4.x; J.err[1] = r4.y; J.gamma = r4.z; J.d.max_force = r4.w;
+      B2G_JV_FINISH;
+    } break;
+    default: {  // pulley
+      B2G_JV_COMMON(B2G_JOINT_PULLEY);
+      J.u[0] = r3.x; J.u[1] = r3.y; J.uB[0] = r3.z; J.uB[1] = r3.w;
+      J.mass = r4.x; J.d.ratio = r4.y;
+      B2G_JV_FINISH;
+    } break;
+  }
+#undef B2G_JV_COMMON
+#undef B2G_JV_FINISH
+}
+
+// The accumulated impulses of the joint in `slot` back into its record.
+__device__ __forceinline__ void jointStoreImpulses(const float4* P, int stride, int slot, JointDev& J) {
+  if (__float_as_int(P[slot].w) & B2G_JV_ASLEEP) return;
+  const float4 i0 = P[(int64_t)7 * stride + slot], i1 = P[(int64_t)8 * stride + slot];
+  J.impulse[0] = i0.x; J.impulse[1] = i0.y; J.impulse[2] = i0.z; J.motorImpulse = i0.w;
+  J.lowerImpulse = i1.x; J.upperImpulse = i1.y;
+}
+#endif
+
 // SolvePositionConstraints (revolute :245-321, prismatic :340-459, distance :268-314).
 B2G_HD bool jointSolvePosition(JointDev& J, float4* pos) {
   V2 cA, cB; float aA, aB;
