@@ -125,7 +125,7 @@ struct SolveClass {
   bool wide;  // the 128-register build (few worlds: latency-bound) rather than the 64-register one
 };
 #define B2G_SOLVE_CLASSES 5
-#define B2G_JV_ROWS 9  // float4 rows of one joint's velocity-pass record (solver_dev.cuh)
+#define B2G_JV_ROWS 13  // float4 rows of one joint's solver record (solver_dev.cuh)
 
 // Status word the kernels write instead of trapping (bounded waits and capacity checks).
 #define B2G_DEV_OK 0u

@@ -727,13 +727,12 @@ __global__ void __launch_bounds__(T, kSolveBlocks<T, WIDE>) k_solve(KernelArgs a
     const int step = c == 63 ? 1 : T, i0 = c == 63 ? s : s + threadIdx.x;
     if (c != 63 || threadIdx.x == 0)
       for (int i = i0; i < e; i += step) {
-        JointDev& J = a.joints[j0 + a.jorder[j0 + i]];
+        const JointDev& J = a.joints[j0 + a.jorder[j0 + i]];
         if (sleepMode && !joint_awake(a, J)) {
           jointPackAsleep(a.jplanes, j0 + i);
           continue;
         }
-        jointInit(J, a.massd, a.lc, a.pos, jb, a.dt, dtRatio, warm);
-        jointPackVel(J, a.jplanes, a.jstride, j0 + i);
+        jointInitSlot(J, a.jplanes, a.jstride, j0 + i, a.massd, a.lc, a.pos, jb, a.dt, dtRatio, warm);
       }
     __syncthreads();
   }
@@ -822,14 +821,14 @@ __global__ void __launch_bounds__(T, kSolveBlocks<T, WIDE>) k_solve(KernelArgs a
       const int step = c == 63 ? 1 : T, i0 = c == 63 ? s : s + threadIdx.x;
       if (c != 63 || threadIdx.x == 0)
         for (int i = i0; i < e; i += step) {
-          JointDev& J = a.joints[j0 + a.jorder[j0 + i]];
           int root = 0;
           if (sleepMode) {
-            if (!joint_awake(a, J)) continue;
-            root = isl_root(SL, J.d.body_a - b0, J.d.body_b - b0);
+            const float4 h = a.jplanes[j0 + i];
+            if (__float_as_int(h.w) & B2G_JV_ASLEEP) continue;
+            root = isl_root(SL, __float_as_int(h.x) - b0, __float_as_int(h.y) - b0);
             if (isl_bits(SL, root) & B2G_ISL_DONE) continue;
           }
-          if (!jointSolvePosition(J, jp)) {
+          if (!jointSolvePositionSlot(a.jplanes, a.jstride, j0 + i, jp)) {
             okay = 0;
             if (sleepMode) isl_store(&SL[root].z, it + 1);
           }

@@ -1018,184 +1018,6 @@ B2G_HD void jointSolveVelocity(JointDev& J, float4* vel, float dt, float inv_dt)
   if (moves(J.mB, J.invIB)) storeVel(vel, J.iB, vB, wB);
 }
 
-#ifdef __CUDACC__
-// ---- joint velocity rows. A joint's velocity pass reads a few dozen of its record's fields, spread
-// over the record; read from the record in global memory, each field is a separate transaction per
-// thread and the pass costs about ten contact solves. The rows hold those fields packed per type
-// (B2G_JV_ROWS float4 planes of `stride` slots, one slot per joint in colour order, so a colour's
-// threads read consecutive slots), written by the joint's init; the velocity iterations run the
-// same jointSolveVelocity on a register copy, and the accumulated impulses go back to the record
-// after the last iteration.
-//   row 0: iA, iB, type, flags (as int bits)     row 1: mA, mB, invIA, invIB
-//   rows 2-6: per type (below; row 4 holds K for the prismatic joint, motorMass, bias and gamma
-//             for the wheel joint)               row 7: impulse 0-2, motorImpulse
-//   row 8: lowerImpulse, upperImpulse
-#define B2G_JV_MOTOR 1
-#define B2G_JV_LIMIT 2
-#define B2G_JV_ASLEEP 4
-
-__device__ __forceinline__ void jointPackVel(const JointDev& J, float4* P, int stride, int slot) {
-  float4 r[B2G_JV_ROWS];
-  for (int k = 0; k < B2G_JV_ROWS; ++k) r[k] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-  const int flags = (J.d.enable_motor ? B2G_JV_MOTOR : 0) | (J.d.enable_limit ? B2G_JV_LIMIT : 0);
-  r[0] = make_float4(__int_as_float(J.iA), __int_as_float(J.iB), __int_as_float(J.d.type), __int_as_float(flags));
-  r[1] = make_float4(J.mA, J.mB, J.invIA, J.invIB);
-  switch (J.d.type) {
-    case B2G_JOINT_REVOLUTE:
-      r[2] = make_float4(J.rA[0], J.rA[1], J.rB[0], J.rB[1]);
-      r[3] = make_float4(J.K[0], J.K[1], J.K[2], J.K[3]);
-      r[4] = make_float4(J.axialMass, J.angle, J.d.lower, J.d.upper);
-      r[5] = make_float4(J.d.motor_speed, J.d.max_motor, 0.0f, 0.0f);
-      break;
-    case B2G_JOINT_PRISMATIC:
-    case B2G_JOINT_WHEEL:
-      r[2] = make_float4(J.axis[0], J.axis[1], J.perp[0], J.perp[1]);
-      r[3] = make_float4(J.a1, J.a2, J.s1, J.s2);
-      r[4] = make_float4(J.K[0], J.K[1], J.K[2], J.K[3]);
-      r[5] = make_float4(J.axialMass, J.translation, J.d.lower, J.d.upper);
-      r[6] = make_float4(J.d.motor_speed, J.d.max_motor, J.mass, J.springMass);
-      r[4] = J.d.type == B2G_JOINT_WHEEL ? make_float4(J.motorMass, J.bias, J.gamma, 0.0f) : r[4];
-      break;
-    case B2G_JOINT_DISTANCE:
-      r[2] = make_float4(J.rA[0], J.rA[1], J.rB[0], J.rB[1]);
-      r[3] = make_float4(J.u[0], J.u[1], J.softMass, J.bias);
-      r[4] = make_float4(J.gamma, J.mass, J.currentLength, J.d.min_length);
-      r[5] = make_float4(J.d.max_length, J.d.stiffness, 0.0f, 0.0f);
-      break;
-    case B2G_JOINT_WELD:
-      r[2] = make_float4(J.rA[0], J.rA[1], J.rB[0], J.rB[1]);
-      r[3] = make_float4(J.mass3[0], J.mass3[1], J.mass3[2], J.mass3[3]);
-      r[4] = make_float4(J.mass3[4], J.mass3[5], J.mass3[6], J.mass3[7]);
-      r[5] = make_float4(J.mass3[8], J.bias, J.gamma, J.d.stiffness);
-      break;
-    case B2G_JOINT_MOTOR:
-    case B2G_JOINT_FRICTION:
-      r[2] = make_float4(J.rA[0], J.rA[1], J.rB[0], J.rB[1]);
-      r[3] = make_float4(J.K[0], J.K[1], J.K[2], J.K[3]);
-      r[4] = make_float4(J.axialMass, J.d.max_force, J.d.max_torque, J.d.correction_factor);
-      r[5] = make_float4(J.angularError, J.err[0], J.err[1], 0.0f);
-      break;
-    case B2G_JOINT_MOUSE:
-      r[2] = make_float4(J.rA[0], J.rA[1], J.rB[0], J.rB[1]);
-      r[3] = make_float4(J.K[0], J.K[1], J.K[2], J.K[3]);
-      r[4] = make_float4(J.err[0], J.err[1], J.gamma, J.d.max_force);
-      break;
-    default:  // pulley
-      r[2] = make_float4(J.rA[0], J.rA[1], J.rB[0], J.rB[1]);
-      r[3] = make_float4(J.u[0], J.u[1], J.uB[0], J.uB[1]);
-      r[4] = make_float4(J.mass, J.d.ratio, 0.0f, 0.0f);
-      break;
-  }
-  r[7] = make_float4(J.impulse[0], J.impulse[1], J.impulse[2], J.motorImpulse);
-  r[8] = make_float4(J.lowerImpulse, J.upperImpulse, 0.0f, 0.0f);
-#pragma unroll
-  for (int k = 0; k < B2G_JV_ROWS; ++k) P[(int64_t)k * stride + slot] = r[k];
-}
-
-// A joint left out of this step (its island sleeps): its velocity iterations skip it.
-__device__ __forceinline__ void jointPackAsleep(float4* P, int slot) {
-  P[slot] = make_float4(0.0f, 0.0f, 0.0f, __int_as_float(B2G_JV_ASLEEP));
-}
-
-// One velocity iteration of the joint in `slot`: the register copy of its rows through
-// jointSolveVelocity, its impulses written back to the rows.
-__device__ __forceinline__ void jointSolveVelocitySlot(float4* P, int stride, int slot, float4* vel, float dt,
-                                                      float inv_dt) {
-  const float4 r0 = P[slot];
-  const int flags = __float_as_int(r0.w);
-  if (flags & B2G_JV_ASLEEP) return;
-  const float4 r1 = P[(int64_t)stride + slot], r2 = P[(int64_t)2 * stride + slot], r3 = P[(int64_t)3 * stride + slot];
-  const float4 r4 = P[(int64_t)4 * stride + slot], r5 = P[(int64_t)5 * stride + slot], r6 = P[(int64_t)6 * stride + slot];
-  const float4 r7 = P[(int64_t)7 * stride + slot], r8 = P[(int64_t)8 * stride + slot];
-  // each type on its own register copy with a constant type, so that only its branch of
-  // jointSolveVelocity remains and the copy stays in registers
-#define B2G_JV_COMMON(TYPE)                                                                   \
-  JointDev J;                                                                                 \
-  J.iA = __float_as_int(r0.x); J.iB = __float_as_int(r0.y); J.d.type = TYPE;                  \
-  J.d.enable_motor = (flags & B2G_JV_MOTOR) ? 1 : 0;                                          \
-  J.d.enable_limit = (flags & B2G_JV_LIMIT) ? 1 : 0;                                          \
-  J.mA = r1.x; J.mB = r1.y; J.invIA = r1.z; J.invIB = r1.w;                                   \
-  J.impulse[0] = r7.x; J.impulse[1] = r7.y; J.impulse[2] = r7.z; J.motorImpulse = r7.w;       \
-  J.lowerImpulse = r8.x; J.upperImpulse = r8.y;                                               \
-  J.rA[0] = r2.x; J.rA[1] = r2.y; J.rB[0] = r2.z; J.rB[1] = r2.w
-#define B2G_JV_FINISH                                                                         \
-  jointSolveVelocity(J, vel, dt, inv_dt);                                                     \
-  P[(int64_t)7 * stride + slot] = make_float4(J.impulse[0], J.impulse[1], J.impulse[2], J.motorImpulse); \
-  P[(int64_t)8 * stride + slot] = make_float4(J.lowerImpulse, J.upperImpulse, 0.0f, 0.0f)
-  switch (__float_as_int(r0.z)) {
-    case B2G_JOINT_REVOLUTE: {
-      B2G_JV_COMMON(B2G_JOINT_REVOLUTE);
-      J.K[0] = r3.x; J.K[1] = r3.y; J.K[2] = r3.z; J.K[3] = r3.w;
-      J.axialMass = r4.x; J.angle = r4.y; J.d.lower = r4.z; J.d.upper = r4.w;
-      J.d.motor_speed = r5.x; J.d.max_motor = r5.y;
-      B2G_JV_FINISH;
-    } break;
-    case B2G_JOINT_PRISMATIC: {
-      B2G_JV_COMMON(B2G_JOINT_PRISMATIC);
-      J.axis[0] = r2.x; J.axis[1] = r2.y; J.perp[0] = r2.z; J.perp[1] = r2.w;
-      J.a1 = r3.x; J.a2 = r3.y; J.s1 = r3.z; J.s2 = r3.w;
-      J.K[0] = r4.x; J.K[1] = r4.y; J.K[2] = r4.z; J.K[3] = r4.w;
-      J.axialMass = r5.x; J.translation = r5.y; J.d.lower = r5.z; J.d.upper = r5.w;
-      J.d.motor_speed = r6.x; J.d.max_motor = r6.y;
-      B2G_JV_FINISH;
-    } break;
-    case B2G_JOINT_WHEEL: {
-      B2G_JV_COMMON(B2G_JOINT_WHEEL);
-      J.axis[0] = r2.x; J.axis[1] = r2.y; J.perp[0] = r2.z; J.perp[1] = r2.w;
-      J.a1 = r3.x; J.a2 = r3.y; J.s1 = r3.z; J.s2 = r3.w;
-      J.motorMass = r4.x; J.bias = r4.y; J.gamma = r4.z;
-      J.axialMass = r5.x; J.translation = r5.y; J.d.lower = r5.z; J.d.upper = r5.w;
-      J.d.motor_speed = r6.x; J.d.max_motor = r6.y; J.mass = r6.z; J.springMass = r6.w;
-      B2G_JV_FINISH;
-    } break;
-    case B2G_JOINT_DISTANCE: {
-      B2G_JV_COMMON(B2G_JOINT_DISTANCE);
-      J.u[0] = r3.x; J.u[1] = r3.y; J.softMass = r3.z; J.bias = r3.w;
-      J.gamma = r4.x; J.mass = r4.y; J.currentLength = r4.z; J.d.min_length = r4.w;
-      J.d.max_length = r5.x; J.d.stiffness = r5.y;
-      B2G_JV_FINISH;
-    } break;
-    case B2G_JOINT_WELD: {
-      B2G_JV_COMMON(B2G_JOINT_WELD);
-      J.mass3[0] = r3.x; J.mass3[1] = r3.y; J.mass3[2] = r3.z; J.mass3[3] = r3.w;
-      J.mass3[4] = r4.x; J.mass3[5] = r4.y; J.mass3[6] = r4.z; J.mass3[7] = r4.w;
-      J.mass3[8] = r5.x; J.bias = r5.y; J.gamma = r5.z; J.d.stiffness = r5.w;
-      B2G_JV_FINISH;
-    } break;
-    case B2G_JOINT_MOTOR:
-    case B2G_JOINT_FRICTION: {
-      B2G_JV_COMMON(__float_as_int(r0.z));
-      J.K[0] = r3.x; J.K[1] = r3.y; J.K[2] = r3.z; J.K[3] = r3.w;
-      J.axialMass = r4.x; J.d.max_force = r4.y; J.d.max_torque = r4.z; J.d.correction_factor = r4.w;
-      J.angularError = r5.x; J.err[0] = r5.y; J.err[1] = r5.z;
-      B2G_JV_FINISH;
-    } break;
-    case B2G_JOINT_MOUSE: {
-      B2G_JV_COMMON(B2G_JOINT_MOUSE);
-      J.K[0] = r3.x; J.K[1] = r3.y; J.K[2] = r3.z; J.K[3] = r3.w;
-      J.err[0] = r4.x; J.err[1] = r4.y; J.gamma = r4.z; J.d.max_force = r4.w;
-      B2G_JV_FINISH;
-    } break;
-    default: {  // pulley
-      B2G_JV_COMMON(B2G_JOINT_PULLEY);
-      J.u[0] = r3.x; J.u[1] = r3.y; J.uB[0] = r3.z; J.uB[1] = r3.w;
-      J.mass = r4.x; J.d.ratio = r4.y;
-      B2G_JV_FINISH;
-    } break;
-  }
-#undef B2G_JV_COMMON
-#undef B2G_JV_FINISH
-}
-
-// The accumulated impulses of the joint in `slot` back into its record.
-__device__ __forceinline__ void jointStoreImpulses(const float4* P, int stride, int slot, JointDev& J) {
-  if (__float_as_int(P[slot].w) & B2G_JV_ASLEEP) return;
-  const float4 i0 = P[(int64_t)7 * stride + slot], i1 = P[(int64_t)8 * stride + slot];
-  J.impulse[0] = i0.x; J.impulse[1] = i0.y; J.impulse[2] = i0.z; J.motorImpulse = i0.w;
-  J.lowerImpulse = i1.x; J.upperImpulse = i1.y;
-}
-#endif
-
 // SolvePositionConstraints (revolute :245-321, prismatic :340-459, distance :268-314).
 B2G_HD bool jointSolvePosition(JointDev& J, float4* pos) {
   V2 cA, cB; float aA, aB;
@@ -1438,5 +1260,377 @@ B2G_HD bool jointSolvePosition(JointDev& J, float4* pos) {
   if (moves(J.mB, J.invIB)) storePos(pos, J.iB, cB, aB);
   return ok;
 }
+
+#ifdef __CUDACC__
+// ---- joint velocity rows. A joint's velocity pass reads a few dozen of its record's fields, spread
+// over the record; read from the record in global memory, each field is a separate transaction per
+// thread and the pass costs about ten contact solves. The rows hold those fields packed per type
+// (B2G_JV_ROWS float4 planes of `stride` slots, one slot per joint in colour order, so a colour's
+// threads read consecutive slots), written by the joint's init; the velocity iterations run the
+// same jointSolveVelocity on a register copy, and the accumulated impulses go back to the record
+// after the last iteration.
+//   row 0: iA, iB, type, flags (as int bits)     row 1: mA, mB, invIA, invIB
+//   rows 2-6: per type (below; row 4 holds K for the prismatic joint, motorMass, bias and gamma
+//             for the wheel joint)               row 7: impulse 0-2, motorImpulse
+//   row 8: lowerImpulse, upperImpulse
+// The position iterations read rows 0-1 and the position rows 9-12 the same way:
+//   row 9: local anchors A, B                     row 10: local centres A, B
+//   rows 11-12: per type (jointPackPos)
+// The init itself runs on a per-type register copy of the record's fields it reads, so that the
+// record is only read during the step and written once, by jointStoreImpulses.
+#define B2G_JV_MOTOR 1
+#define B2G_JV_LIMIT 2
+#define B2G_JV_ASLEEP 4
+
+__device__ __forceinline__ void jointPackVel(const JointDev& J, float4* P, int stride, int slot) {
+  float4 r[B2G_JV_ROWS];
+  for (int k = 0; k < B2G_JV_ROWS; ++k) r[k] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  const int flags = (J.d.enable_motor ? B2G_JV_MOTOR : 0) | (J.d.enable_limit ? B2G_JV_LIMIT : 0);
+  r[0] = make_float4(__int_as_float(J.iA), __int_as_float(J.iB), __int_as_float(J.d.type), __int_as_float(flags));
+  r[1] = make_float4(J.mA, J.mB, J.invIA, J.invIB);
+  switch (J.d.type) {
+    case B2G_JOINT_REVOLUTE:
+      r[2] = make_float4(J.rA[0], J.rA[1], J.rB[0], J.rB[1]);
+      r[3] = make_float4(J.K[0], J.K[1], J.K[2], J.K[3]);
+      r[4] = make_float4(J.axialMass, J.angle, J.d.lower, J.d.upper);
+      r[5] = make_float4(J.d.motor_speed, J.d.max_motor, 0.0f, 0.0f);
+      break;
+    case B2G_JOINT_PRISMATIC:
+    case B2G_JOINT_WHEEL:
+      r[2] = make_float4(J.axis[0], J.axis[1], J.perp[0], J.perp[1]);
+      r[3] = make_float4(J.a1, J.a2, J.s1, J.s2);
+      r[4] = make_float4(J.K[0], J.K[1], J.K[2], J.K[3]);
+      r[5] = make_float4(J.axialMass, J.translation, J.d.lower, J.d.upper);
+      r[6] = make_float4(J.d.motor_speed, J.d.max_motor, J.mass, J.springMass);
+      r[4] = J.d.type == B2G_JOINT_WHEEL ? make_float4(J.motorMass, J.bias, J.gamma, 0.0f) : r[4];
+      break;
+    case B2G_JOINT_DISTANCE:
+      r[2] = make_float4(J.rA[0], J.rA[1], J.rB[0], J.rB[1]);
+      r[3] = make_float4(J.u[0], J.u[1], J.softMass, J.bias);
+      r[4] = make_float4(J.gamma, J.mass, J.currentLength, J.d.min_length);
+      r[5] = make_float4(J.d.max_length, J.d.stiffness, 0.0f, 0.0f);
+      break;
+    case B2G_JOINT_WELD:
+      r[2] = make_float4(J.rA[0], J.rA[1], J.rB[0], J.rB[1]);
+      r[3] = make_float4(J.mass3[0], J.mass3[1], J.mass3[2], J.mass3[3]);
+      r[4] = make_float4(J.mass3[4], J.mass3[5], J.mass3[6], J.mass3[7]);
+      r[5] = make_float4(J.mass3[8], J.bias, J.gamma, J.d.stiffness);
+      break;
+    case B2G_JOINT_MOTOR:
+    case B2G_JOINT_FRICTION:
+      r[2] = make_float4(J.rA[0], J.rA[1], J.rB[0], J.rB[1]);
+      r[3] = make_float4(J.K[0], J.K[1], J.K[2], J.K[3]);
+      r[4] = make_float4(J.axialMass, J.d.max_force, J.d.max_torque, J.d.correction_factor);
+      r[5] = make_float4(J.angularError, J.err[0], J.err[1], 0.0f);
+      break;
+    case B2G_JOINT_MOUSE:
+      r[2] = make_float4(J.rA[0], J.rA[1], J.rB[0], J.rB[1]);
+      r[3] = make_float4(J.K[0], J.K[1], J.K[2], J.K[3]);
+      r[4] = make_float4(J.err[0], J.err[1], J.gamma, J.d.max_force);
+      break;
+    default:  // pulley
+      r[2] = make_float4(J.rA[0], J.rA[1], J.rB[0], J.rB[1]);
+      r[3] = make_float4(J.u[0], J.u[1], J.uB[0], J.uB[1]);
+      r[4] = make_float4(J.mass, J.d.ratio, 0.0f, 0.0f);
+      break;
+  }
+  r[7] = make_float4(J.impulse[0], J.impulse[1], J.impulse[2], J.motorImpulse);
+  r[8] = make_float4(J.lowerImpulse, J.upperImpulse, 0.0f, 0.0f);
+#pragma unroll
+  for (int k = 0; k < B2G_JV_ROWS; ++k) P[(int64_t)k * stride + slot] = r[k];
+}
+
+// The position pass's rows of a joint whose init just ran (J holds its step temporaries).
+__device__ __forceinline__ void jointPackPos(const JointDev& J, float4* P, int stride, int slot) {
+  float4 r11 = make_float4(0.0f, 0.0f, 0.0f, 0.0f), r12 = r11;
+  switch (J.d.type) {
+    case B2G_JOINT_REVOLUTE:
+      r11 = make_float4(J.axialMass, J.d.reference_angle, J.d.lower, J.d.upper);
+      break;
+    case B2G_JOINT_PRISMATIC:
+      r11 = make_float4(J.localXAxisA[0], J.localXAxisA[1], J.localYAxisA[0], J.localYAxisA[1]);
+      r12 = make_float4(J.d.reference_angle, J.d.lower, J.d.upper, 0.0f);
+      break;
+    case B2G_JOINT_DISTANCE:
+      r11 = make_float4(J.d.max_length, J.d.min_length, J.mass, 0.0f);
+      break;
+    case B2G_JOINT_WELD:
+      r11 = make_float4(J.d.reference_angle, J.d.stiffness, 0.0f, 0.0f);
+      break;
+    case B2G_JOINT_WHEEL:
+      r11 = make_float4(J.localXAxisA[0], J.localXAxisA[1], J.localYAxisA[0], J.localYAxisA[1]);
+      r12 = make_float4(J.d.lower, J.d.upper, J.s1, J.s2);
+      break;
+    case B2G_JOINT_PULLEY:
+      r11 = make_float4(J.d.ground_anchor_a[0], J.d.ground_anchor_a[1], J.d.ground_anchor_b[0], J.d.ground_anchor_b[1]);
+      r12 = make_float4(J.constant, J.d.ratio, 0.0f, 0.0f);
+      break;
+    default:
+      break;
+  }
+  P[(int64_t)9 * stride + slot] = make_float4(J.d.local_anchor_a[0], J.d.local_anchor_a[1], J.d.local_anchor_b[0], J.d.local_anchor_b[1]);
+  P[(int64_t)10 * stride + slot] = make_float4(J.lcA[0], J.lcA[1], J.lcB[0], J.lcB[1]);
+  P[(int64_t)11 * stride + slot] = r11;
+  P[(int64_t)12 * stride + slot] = r12;
+}
+
+// InitVelocityConstraints of the joint record G into the rows of `slot`: per type, a register
+// copy of the record's fields the init and the rows read, the init on it, the rows packed.
+__device__ __forceinline__ void jointInitSlot(const JointDev& G, float4* P, int stride, int slot, const float4* massd,
+                                              const float2* lc, const float4* pos, float4* vel, float dt, float dtRatio,
+                                              bool warm) {
+#define B2G_JI_COMMON(TYPE)                                                                      \
+  JointDev J;                                                                                    \
+  J.d.type = TYPE;                                                                               \
+  J.d.body_a = G.d.body_a; J.d.body_b = G.d.body_b;                                              \
+  J.d.local_anchor_a[0] = G.d.local_anchor_a[0]; J.d.local_anchor_a[1] = G.d.local_anchor_a[1];  \
+  J.d.local_anchor_b[0] = G.d.local_anchor_b[0]; J.d.local_anchor_b[1] = G.d.local_anchor_b[1];  \
+  J.d.enable_limit = G.d.enable_limit; J.d.enable_motor = G.d.enable_motor;                      \
+  J.impulse[0] = G.impulse[0]; J.impulse[1] = G.impulse[1]; J.impulse[2] = G.impulse[2];         \
+  J.motorImpulse = G.motorImpulse; J.lowerImpulse = G.lowerImpulse; J.upperImpulse = G.upperImpulse
+#define B2G_JI_AXES                                                                              \
+  J.localXAxisA[0] = G.localXAxisA[0]; J.localXAxisA[1] = G.localXAxisA[1];                      \
+  J.localYAxisA[0] = G.localYAxisA[0]; J.localYAxisA[1] = G.localYAxisA[1]
+#define B2G_JI_FINISH                                                                            \
+  jointInit(J, massd, lc, pos, vel, dt, dtRatio, warm);                                          \
+  jointPackVel(J, P, stride, slot);                                                              \
+  jointPackPos(J, P, stride, slot)
+  switch (G.d.type) {
+    case B2G_JOINT_REVOLUTE: {
+      B2G_JI_COMMON(B2G_JOINT_REVOLUTE);
+      J.d.reference_angle = G.d.reference_angle; J.d.lower = G.d.lower; J.d.upper = G.d.upper;
+      J.d.motor_speed = G.d.motor_speed; J.d.max_motor = G.d.max_motor;
+      B2G_JI_FINISH;
+    } break;
+    case B2G_JOINT_PRISMATIC: {
+      B2G_JI_COMMON(B2G_JOINT_PRISMATIC);
+      B2G_JI_AXES;
+      J.d.reference_angle = G.d.reference_angle; J.d.lower = G.d.lower; J.d.upper = G.d.upper;
+      J.d.motor_speed = G.d.motor_speed; J.d.max_motor = G.d.max_motor;
+      B2G_JI_FINISH;
+    } break;
+    case B2G_JOINT_DISTANCE: {
+      B2G_JI_COMMON(B2G_JOINT_DISTANCE);
+      J.d.damping = G.d.damping; J.d.length = G.d.length; J.d.min_length = G.d.min_length;
+      J.d.max_length = G.d.max_length; J.d.stiffness = G.d.stiffness;
+      B2G_JI_FINISH;
+    } break;
+    case B2G_JOINT_WELD: {
+      B2G_JI_COMMON(B2G_JOINT_WELD);
+      J.d.damping = G.d.damping; J.d.reference_angle = G.d.reference_angle; J.d.stiffness = G.d.stiffness;
+      B2G_JI_FINISH;
+    } break;
+    case B2G_JOINT_WHEEL: {
+      B2G_JI_COMMON(B2G_JOINT_WHEEL);
+      B2G_JI_AXES;
+      J.d.damping = G.d.damping; J.d.stiffness = G.d.stiffness; J.d.lower = G.d.lower; J.d.upper = G.d.upper;
+      J.d.motor_speed = G.d.motor_speed; J.d.max_motor = G.d.max_motor;
+      B2G_JI_FINISH;
+    } break;
+    case B2G_JOINT_MOTOR:
+    case B2G_JOINT_FRICTION: {
+      B2G_JI_COMMON(G.d.type);
+      J.d.linear_offset[0] = G.d.linear_offset[0]; J.d.linear_offset[1] = G.d.linear_offset[1];
+      J.d.reference_angle = G.d.reference_angle; J.d.max_force = G.d.max_force; J.d.max_torque = G.d.max_torque;
+      J.d.correction_factor = G.d.correction_factor;
+      B2G_JI_FINISH;
+    } break;
+    case B2G_JOINT_MOUSE: {
+      B2G_JI_COMMON(B2G_JOINT_MOUSE);
+      J.d.damping = G.d.damping; J.d.stiffness = G.d.stiffness;
+      J.d.target[0] = G.d.target[0]; J.d.target[1] = G.d.target[1]; J.d.max_force = G.d.max_force;
+      B2G_JI_FINISH;
+    } break;
+    default: {  // pulley
+      B2G_JI_COMMON(B2G_JOINT_PULLEY);
+      J.d.ground_anchor_a[0] = G.d.ground_anchor_a[0]; J.d.ground_anchor_a[1] = G.d.ground_anchor_a[1];
+      J.d.ground_anchor_b[0] = G.d.ground_anchor_b[0]; J.d.ground_anchor_b[1] = G.d.ground_anchor_b[1];
+      J.d.ratio = G.d.ratio; J.constant = G.constant;
+      B2G_JI_FINISH;
+    } break;
+  }
+#undef B2G_JI_COMMON
+#undef B2G_JI_AXES
+#undef B2G_JI_FINISH
+}
+
+// One position iteration of the joint in `slot` (SolvePositionConstraints) on a per-type register
+// copy of its rows; returns the joint's position check. A joint of a sleeping island is not called.
+__device__ __forceinline__ bool jointSolvePositionSlot(const float4* P, int stride, int slot, float4* pos) {
+  const float4 r0 = P[slot];
+  const int type = __float_as_int(r0.z);
+  if (type == B2G_JOINT_MOTOR || type == B2G_JOINT_FRICTION || type == B2G_JOINT_MOUSE) return true;
+  const float4 r1 = P[(int64_t)stride + slot];
+  const float4 r9 = P[(int64_t)9 * stride + slot], r10 = P[(int64_t)10 * stride + slot];
+  const float4 r11 = P[(int64_t)11 * stride + slot], r12 = P[(int64_t)12 * stride + slot];
+  const int flags = __float_as_int(r0.w);
+#define B2G_JP_COMMON(TYPE)                                                                  \
+  JointDev J;                                                                                \
+  J.iA = __float_as_int(r0.x); J.iB = __float_as_int(r0.y); J.d.type = TYPE;                 \
+  J.d.enable_limit = (flags & B2G_JV_LIMIT) ? 1 : 0;                                         \
+  J.mA = r1.x; J.mB = r1.y; J.invIA = r1.z; J.invIB = r1.w;                                  \
+  J.d.local_anchor_a[0] = r9.x; J.d.local_anchor_a[1] = r9.y;                                \
+  J.d.local_anchor_b[0] = r9.z; J.d.local_anchor_b[1] = r9.w;                                \
+  J.lcA[0] = r10.x; J.lcA[1] = r10.y; J.lcB[0] = r10.z; J.lcB[1] = r10.w
+  bool ok = true;
+  switch (type) {
+    case B2G_JOINT_REVOLUTE: {
+      B2G_JP_COMMON(B2G_JOINT_REVOLUTE);
+      J.axialMass = r11.x; J.d.reference_angle = r11.y; J.d.lower = r11.z; J.d.upper = r11.w;
+      ok = jointSolvePosition(J, pos);
+    } break;
+    case B2G_JOINT_PRISMATIC: {
+      B2G_JP_COMMON(B2G_JOINT_PRISMATIC);
+      J.localXAxisA[0] = r11.x; J.localXAxisA[1] = r11.y; J.localYAxisA[0] = r11.z; J.localYAxisA[1] = r11.w;
+      J.d.reference_angle = r12.x; J.d.lower = r12.y; J.d.upper = r12.z;
+      ok = jointSolvePosition(J, pos);
+    } break;
+    case B2G_JOINT_DISTANCE: {
+      B2G_JP_COMMON(B2G_JOINT_DISTANCE);
+      J.d.max_length = r11.x; J.d.min_length = r11.y; J.mass = r11.z;
+      ok = jointSolvePosition(J, pos);
+    } break;
+    case B2G_JOINT_WELD: {
+      B2G_JP_COMMON(B2G_JOINT_WELD);
+      J.d.reference_angle = r11.x; J.d.stiffness = r11.y;
+      ok = jointSolvePosition(J, pos);
+    } break;
+    case B2G_JOINT_WHEEL: {
+      B2G_JP_COMMON(B2G_JOINT_WHEEL);
+      const float4 r2 = P[(int64_t)2 * stride + slot];
+      J.axis[0] = r2.x; J.axis[1] = r2.y;
+      J.localXAxisA[0] = r11.x; J.localXAxisA[1] = r11.y; J.localYAxisA[0] = r11.z; J.localYAxisA[1] = r11.w;
+      J.d.lower = r12.x; J.d.upper = r12.y; J.s1 = r12.z; J.s2 = r12.w;
+      ok = jointSolvePosition(J, pos);
+    } break;
+    default: {  // pulley
+      B2G_JP_COMMON(B2G_JOINT_PULLEY);
+      J.d.ground_anchor_a[0] = r11.x; J.d.ground_anchor_a[1] = r11.y;
+      J.d.ground_anchor_b[0] = r11.z; J.d.ground_anchor_b[1] = r11.w;
+      J.constant = r12.x; J.d.ratio = r12.y;
+      ok = jointSolvePosition(J, pos);
+    } break;
+  }
+#undef B2G_JP_COMMON
+  return ok;
+}
+
+// A joint left out of this step (its island sleeps): its velocity iterations skip it.
+__device__ __forceinline__ void jointPackAsleep(float4* P, int slot) {
+  P[slot] = make_float4(0.0f, 0.0f, 0.0f, __int_as_float(B2G_JV_ASLEEP));
+}
+
+// One velocity iteration of the joint in `slot`: the register copy of its rows through
+// jointSolveVelocity, its impulses written back to the rows.
+__device__ __forceinline__ void jointSolveVelocitySlot(float4* P, int stride, int slot, float4* vel, float dt,
+                                                      float inv_dt) {
+  const float4 r0 = P[slot];
+  const int flags = __float_as_int(r0.w);
+  if (flags & B2G_JV_ASLEEP) return;
+  const float4 r1 = P[(int64_t)stride + slot], r2 = P[(int64_t)2 * stride + slot], r3 = P[(int64_t)3 * stride + slot];
+  const float4 r4 = P[(int64_t)4 * stride + slot], r5 = P[(int64_t)5 * stride + slot], r6 = P[(int64_t)6 * stride + slot];
+  const float4 r7 = P[(int64_t)7 * stride + slot], r8 = P[(int64_t)8 * stride + slot];
+  // each type on its own register copy with a constant type, so that only its branch of
+  // jointSolveVelocity remains and the copy stays in registers
+#define B2G_JV_COMMON(TYPE)                                                                   \
+  JointDev J;                                                                                 \
+  J.iA = __float_as_int(r0.x); J.iB = __float_as_int(r0.y); J.d.type = TYPE;                  \
+  J.d.enable_motor = (flags & B2G_JV_MOTOR) ? 1 : 0;                                          \
+  J.d.enable_limit = (flags & B2G_JV_LIMIT) ? 1 : 0;                                          \
+  J.mA = r1.x; J.mB = r1.y; J.invIA = r1.z; J.invIB = r1.w;                                   \
+  J.impulse[0] = r7.x; J.impulse[1] = r7.y; J.impulse[2] = r7.z; J.motorImpulse = r7.w;       \
+  J.lowerImpulse = r8.x; J.upperImpulse = r8.y;                                               \
+  J.rA[0] = r2.x; J.rA[1] = r2.y; J.rB[0] = r2.z; J.rB[1] = r2.w
+#define B2G_JV_FINISH                                                                         \
+  jointSolveVelocity(J, vel, dt, inv_dt);                                                     \
+  P[(int64_t)7 * stride + slot] = make_float4(J.impulse[0], J.impulse[1], J.impulse[2], J.motorImpulse); \
+  P[(int64_t)8 * stride + slot] = make_float4(J.lowerImpulse, J.upperImpulse, 0.0f, 0.0f)
+  switch (__float_as_int(r0.z)) {
+    case B2G_JOINT_REVOLUTE: {
+      B2G_JV_COMMON(B2G_JOINT_REVOLUTE);
+      J.K[0] = r3.x; J.K[1] = r3.y; J.K[2] = r3.z; J.K[3] = r3.w;
+      J.axialMass = r4.x; J.angle = r4.y; J.d.lower = r4.z; J.d.upper = r4.w;
+      J.d.motor_speed = r5.x; J.d.max_motor = r5.y;
+      B2G_JV_FINISH;
+    } break;
+    case B2G_JOINT_PRISMATIC: {
+      B2G_JV_COMMON(B2G_JOINT_PRISMATIC);
+      J.axis[0] = r2.x; J.axis[1] = r2.y; J.perp[0] = r2.z; J.perp[1] = r2.w;
+      J.a1 = r3.x; J.a2 = r3.y; J.s1 = r3.z; J.s2 = r3.w;
+      J.K[0] = r4.x; J.K[1] = r4.y; J.K[2] = r4.z; J.K[3] = r4.w;
+      J.axialMass = r5.x; J.translation = r5.y; J.d.lower = r5.z; J.d.upper = r5.w;
+      J.d.motor_speed = r6.x; J.d.max_motor = r6.y;
+      B2G_JV_FINISH;
+    } break;
+    case B2G_JOINT_WHEEL: {
+      B2G_JV_COMMON(B2G_JOINT_WHEEL);
+      J.axis[0] = r2.x; J.axis[1] = r2.y; J.perp[0] = r2.z; J.perp[1] = r2.w;
+      J.a1 = r3.x; J.a2 = r3.y; J.s1 = r3.z; J.s2 = r3.w;
+      J.motorMass = r4.x; J.bias = r4.y; J.gamma = r4.z;
+      J.axialMass = r5.x; J.translation = r5.y; J.d.lower = r5.z; J.d.upper = r5.w;
+      J.d.motor_speed = r6.x; J.d.max_motor = r6.y; J.mass = r6.z; J.springMass = r6.w;
+      B2G_JV_FINISH;
+    } break;
+    case B2G_JOINT_DISTANCE: {
+      B2G_JV_COMMON(B2G_JOINT_DISTANCE);
+      J.u[0] = r3.x; J.u[1] = r3.y; J.softMass = r3.z; J.bias = r3.w;
+      J.gamma = r4.x; J.mass = r4.y; J.currentLength = r4.z; J.d.min_length = r4.w;
+      J.d.max_length = r5.x; J.d.stiffness = r5.y;
+      B2G_JV_FINISH;
+    } break;
+    case B2G_JOINT_WELD: {
+      B2G_JV_COMMON(B2G_JOINT_WELD);
+      J.mass3[0] = r3.x; J.mass3[1] = r3.y; J.mass3[2] = r3.z; J.mass3[3] = r3.w;
+      J.mass3[4] = r4.x; J.mass3[5] = r4.y; J.mass3[6] = r4.z; J.mass3[7] = r4.w;
+      J.mass3[8] = r5.x; J.bias = r5.y; J.gamma = r5.z; J.d.stiffness = r5.w;
+      B2G_JV_FINISH;
+    } break;
+    case B2G_JOINT_MOTOR:
+    case B2G_JOINT_FRICTION: {
+      B2G_JV_COMMON(__float_as_int(r0.z));
+      J.K[0] = r3.x; J.K[1] = r3.y; J.K[2] = r3.z; J.K[3] = r3.w;
+      J.axialMass = r4.x; J.d.max_force = r4.y; J.d.max_torque = r4.z; J.d.correction_factor = r4.w;
+      J.angularError = r5.x; J.err[0] = r5.y; J.err[1] = r5.z;
+      B2G_JV_FINISH;
+    } break;
+    case B2G_JOINT_MOUSE: {
+      B2G_JV_COMMON(B2G_JOINT_MOUSE);
+      J.K[0] = r3.x; J.K[1] = r3.y; J.K[2] = r3.z; J.K[3] = r3.w;
+      J.err[0] = r4.x; J.err[1] = r4.y; J.gamma = r4.z; J.d.max_force = r4.w;
+      B2G_JV_FINISH;
+    } break;
+    default: {  // pulley
+      B2G_JV_COMMON(B2G_JOINT_PULLEY);
+      J.u[0] = r3.x; J.u[1] = r3.y; J.uB[0] = r3.z; J.uB[1] = r3.w;
+      J.mass = r4.x; J.d.ratio = r4.y;
+      B2G_JV_FINISH;
+    } break;
+  }
+#undef B2G_JV_COMMON
+#undef B2G_JV_FINISH
+}
+
+// The accumulated impulses of the joint in `slot` back into its record, with the step's constraint
+// directions its reaction force is read along (prismatic and wheel axes, distance and pulley
+// directions).
+__device__ __forceinline__ void jointStoreImpulses(const float4* P, int stride, int slot, JointDev& J) {
+  const float4 r0 = P[slot];
+  if (__float_as_int(r0.w) & B2G_JV_ASLEEP) return;
+  const float4 i0 = P[(int64_t)7 * stride + slot], i1 = P[(int64_t)8 * stride + slot];
+  J.impulse[0] = i0.x; J.impulse[1] = i0.y; J.impulse[2] = i0.z; J.motorImpulse = i0.w;
+  J.lowerImpulse = i1.x; J.upperImpulse = i1.y;
+  const int type = __float_as_int(r0.z);
+  if (type == B2G_JOINT_PRISMATIC || type == B2G_JOINT_WHEEL) {
+    const float4 r2 = P[(int64_t)2 * stride + slot];
+    J.axis[0] = r2.x; J.axis[1] = r2.y; J.perp[0] = r2.z; J.perp[1] = r2.w;
+  } else if (type == B2G_JOINT_DISTANCE) {
+    const float4 r3 = P[(int64_t)3 * stride + slot];
+    J.u[0] = r3.x; J.u[1] = r3.y;
+  } else if (type == B2G_JOINT_PULLEY) {
+    const float4 r3 = P[(int64_t)3 * stride + slot];
+    J.u[0] = r3.x; J.u[1] = r3.y; J.uB[0] = r3.z; J.uB[1] = r3.w;
+  }
+}
+#endif
 
 }  // namespace b2g
