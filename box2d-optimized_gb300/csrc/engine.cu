@@ -227,6 +227,9 @@ static void replan_solver(Batch* b) {
 static const size_t kMaxWorldBodies = size_t(1) << 24;
 
 // Reads the status word after the upload's joint colouring (the upload synchronises anyway).
+// The broadphase forest no longer matches the fixture layout: the next broadphase builds every tree.
+static void forest_reset(Batch* b) { b->tree_nf = b->tree_nw = b->tree_age = 0; }
+
 static int check_upload_status(Batch* b) {
   unsigned int st = 0;
   CUDA_TRY(b, cudaMemcpyAsync(&st, b->status.p, sizeof(st), cudaMemcpyDeviceToHost, b->stream));
@@ -416,6 +419,7 @@ int upload_all(Batch* b) {
   launch_joint_colour(make_args(b), 0, NW, b->stream);
   TRY(check_upload_status(b));
   b->tree_valid = false;
+  forest_reset(b);
   b->layout_version++;
   b->structure_dirty = false;
   b->device_state_valid = true;
@@ -587,7 +591,9 @@ static int flush_tail(Batch* b, TailPack& P) {
   TRY(st.add(b, b->wb, 0, wb)); TRY(st.add(b, b->wj, 0, wj)); TRY(st.add(b, b->wg, w0, wg_tail));
   TRY(st.add(b, b->wflags, 0, wflags)); TRY(st.add(b, b->world_order, 0, order)); TRY(st.add(b, b->wc, w0, wc_tail));
   b->h_wflags = wflags;
-  TRY(ensure(b, b->wbounds, NW)); TRY(ensure(b, b->wroot, NW)); TRY(ensure(b, b->ncolors, 4 * (size_t)NW, true));
+  // the broadphase forest's structure (world roots, leaf order, links) survives growth: the next
+  // broadphase refits it and builds trees for the appended worlds only
+  TRY(ensure(b, b->wbounds, NW)); TRY(ensure(b, b->wroot, NW, true)); TRY(ensure(b, b->ncolors, 4 * (size_t)NW, true));
   if (b->wfault.cap < (size_t)NW) {  // flags are zero between steps: a grown array starts zeroed
     TRY(ensure(b, b->wfault, NW));
     CUDA_TRY(b, cudaMemsetAsync(b->wfault.p, 0, b->wfault.cap, b->stream));
@@ -608,8 +614,8 @@ static int flush_tail(Batch* b, TailPack& P) {
   TRY(ensure(b, b->bwake, NB, true)); TRY(ensure(b, b->sl, NB));  // wake marks are zero between steps
   if (b->bwake.cap > (size_t)NB0) CUDA_TRY(b, cudaMemsetAsync(b->bwake.p + NB0, 0, b->bwake.cap - NB0, b->stream));
   TRY(ensure(b, b->aabb, NF)); TRY(ensure(b, b->mkey, NF)); TRY(ensure(b, b->mkey_sorted, NF));
-  TRY(ensure(b, b->mval, NF)); TRY(ensure(b, b->mval_sorted, NF)); TRY(ensure(b, b->nchild, NF));
-  TRY(ensure(b, b->nparent, NF)); TRY(ensure(b, b->lparent, NF)); TRY(ensure(b, b->naabb, NF));
+  TRY(ensure(b, b->mval, NF)); TRY(ensure(b, b->mval_sorted, NF, true)); TRY(ensure(b, b->nchild, NF, true));
+  TRY(ensure(b, b->nparent, NF, true)); TRY(ensure(b, b->lparent, NF, true)); TRY(ensure(b, b->naabb, NF));
   TRY(ensure(b, b->ncbox, 2 * (size_t)NF)); TRY(ensure(b, b->laabb, NF)); TRY(ensure(b, b->fattr, NF));
   TRY(ensure(b, b->nflag, NF)); TRY(ensure(b, b->pcount, (size_t)NF + 1));
   // the live list's per-fixture offsets stay valid for the existing fixtures; the appended
@@ -796,25 +802,58 @@ static int sort_bits(Batch* b) {
   return bits;
 }
 
+// Broadphase modes: a full build sorts every fixture's Morton code and builds every world's tree;
+// a refit keeps the trees of the forest (b->tree_nf fixtures), refits their boxes and builds trees
+// only for the fixtures appended after them. Both give the same pairs; the full build restores
+// the trees' spatial order, so it runs every kTreeRebuildPeriod broadphases.
+enum { BP_FULL = 0, BP_REFIT = 1 };
+const int kTreeRebuildPeriod = 8;
+
+static int bp_mode(const Batch* b) {
+  return (b->tree_nf > 0 && b->tree_nf <= b->NF && b->tree_nw <= b->NW && b->tree_age < kTreeRebuildPeriod)
+             ? BP_REFIT : BP_FULL;
+}
+
+// The forest after a broadphase of `mode`: every fixture has a tree.
+static void bp_done(Batch* b, int mode) {
+  b->tree_age = mode == BP_FULL ? 1 : b->tree_age + 1;
+  b->tree_nf = b->NF;
+  b->tree_nw = b->NW;
+}
+
 // Broadphase + contact diff enqueued on the stream with no host synchronisation: pair counts,
 // scan, emission and the diff read their sizes from device memory; when the pairs exceed the
 // buffers, emission and diff are skipped and the needed size is left in the overflow counter.
-// The live contact list moves to buffer cur ^ 1.
-static void enqueue_broadphase(Batch* b, const KernelArgs& a0, int src) {
+// The live contact list moves to buffer cur ^ 1. `tree_nf` / `tree_nw` give the forest a refit
+// keeps (ignored by a full build).
+static void enqueue_broadphase(Batch* b, const KernelArgs& a0, int src, int mode, int tree_nf, int tree_nw) {
   KernelArgs a = a0;
   // the new list goes to buffer src ^ 1; the diff finds persisting contacts through the live
   // list's per-fixture offsets when the last broadphase left them
   a.poff = b->poffB[src ^ 1].p;
   a.poff_old = b->poff_valid[src] ? b->poffB[src].p : nullptr;
   b->poff_valid[src ^ 1] = true;
-  launch_bp_build(a, b->NF, b->NW, b->cub_tmp.cap, sort_bits(b), b->stream);
+  if (mode == BP_REFIT)
+    launch_bp_refit(a, tree_nf, tree_nw, b->NF, b->NW, b->cub_tmp.cap, sort_bits(b), b->stream);
+  else
+    launch_bp_build(a, b->NF, b->NW, b->cub_tmp.cap, sort_bits(b), b->stream);
   launch_bp_emit(a, b->NF, b->stream);
   launch_contact_diff(a, src, src ^ 1, b->stream);
 }
 
+// An eagerly launched broadphase in the mode the forest allows; the forest then covers every fixture.
+static void enqueue_broadphase(Batch* b, const KernelArgs& a0, int src) {
+  const int mode = bp_mode(b);
+  enqueue_broadphase(b, a0, src, mode, b->tree_nf, b->tree_nw);
+  bp_done(b, mode);
+}
+
 // One Step enqueued: [broadphase if fixtures were added] -> collide -> solve -> broadphase ->
-// clear forces. `src` is the live contact buffer at entry; it flips once per broadphase.
-static void enqueue_step(Batch* b, float dt, int vi, int pi, bool initial_bp, int src, bool record_profile) {
+// clear forces. `src` is the live contact buffer at entry; it flips once per broadphase. The
+// closing broadphase runs in the mode the forest allows, or (graph capture, `capture_mode` >= 0)
+// in that mode over a forest that covers every fixture.
+static void enqueue_step(Batch* b, float dt, int vi, int pi, bool initial_bp, int src, bool record_profile,
+                         int capture_mode = -1) {
   KernelArgs a = step_args(b, dt, vi, pi);
   if (record_profile) cudaEventRecord(b->ev[0], b->stream);
   if (initial_bp) {
@@ -831,7 +870,8 @@ static void enqueue_step(Batch* b, float dt, int vi, int pi, bool initial_bp, in
     if (b->debug_checks) launch_colour_check(a, b->NW, b->stream);
     b->last_solve_buf = src;
     if (record_profile) cudaEventRecord(b->ev[2], b->stream);
-    enqueue_broadphase(b, a, src);
+    if (capture_mode >= 0) enqueue_broadphase(b, a, src, capture_mode, b->NF, b->NW);
+    else enqueue_broadphase(b, a, src);
     src ^= 1;
   } else if (record_profile) {
     cudaEventRecord(b->ev[2], b->stream);
@@ -918,7 +958,8 @@ static int finish_step(Batch* b, int live_before_last_bp) {
     TRY(ensure_contact_capacity(b, (int64_t)overflow));
     CUDA_TRY(b, cudaMemsetAsync(b->counters.p + B2G_CNT_OVERFLOW, 0, sizeof(unsigned long long), b->stream));
     KernelArgs a = step_args(b, b->last_dt, b->last_vi, b->last_pi);
-    enqueue_broadphase(b, a, b->cur);
+    enqueue_broadphase(b, a, b->cur, BP_FULL, 0, 0);
+    bp_done(b, BP_FULL);
     b->cur ^= 1;
     CUDA_TRY(b, cudaMemcpyAsync(b->h_readback, b->counters.p, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
                                 b->stream));
@@ -960,28 +1001,38 @@ static int tail_broadphase(Batch* b, float dt, int vi, int pi, int f0, int w0) {
     CUDA_TRY(b, cudaMemsetAsync(b->counters.p + B2G_CNT_OVERFLOW, 0, sizeof(unsigned long long), b->stream));
   }
   b->NC = (int64_t)b->h_readback[B2G_CNT_CONTACTS];
+  // the appended fixtures' trees join the forest when it covered every fixture before them
+  if (b->tree_nf == f0 && b->tree_nw == w0) {
+    b->tree_nf = b->NF;
+    b->tree_nw = b->NW;
+  } else {
+    forest_reset(b);
+  }
   return B2G_OK;
 }
 
 static void invalidate_graphs(Batch* b) {
-  for (int k = 0; k < 2; ++k) {
-    if (b->graph_exec[k]) cudaGraphExecDestroy(b->graph_exec[k]);
-    b->graph_exec[k] = nullptr;
-  }
+  for (int m = 0; m < 2; ++m)
+    for (int k = 0; k < 2; ++k) {
+      if (b->graph_exec[m][k]) cudaGraphExecDestroy(b->graph_exec[m][k]);
+      b->graph_exec[m][k] = nullptr;
+    }
 }
 
-// Captures one Step per live-buffer parity; a replay does the whole Step with no host work.
+// Captures one Step per live-buffer parity and closing-broadphase mode; a replay does the whole
+// Step with no host work.
 static int capture_graphs(Batch* b, float dt, int vi, int pi) {
   invalidate_graphs(b);
   int saved = b->cur;
-  for (int parity = 0; parity < 2; ++parity) {
-    cudaGraph_t g = nullptr;
-    CUDA_TRY(b, cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
-    enqueue_step(b, dt, vi, pi, false, parity, false);
-    CUDA_TRY(b, cudaStreamEndCapture(b->stream, &g));
-    CUDA_TRY(b, cudaGraphInstantiate(&b->graph_exec[parity], g, 0));
-    cudaGraphDestroy(g);
-  }
+  for (int mode = 0; mode < 2; ++mode)
+    for (int parity = 0; parity < 2; ++parity) {
+      cudaGraph_t g = nullptr;
+      CUDA_TRY(b, cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+      enqueue_step(b, dt, vi, pi, false, parity, false, mode);
+      CUDA_TRY(b, cudaStreamEndCapture(b->stream, &g));
+      CUDA_TRY(b, cudaGraphInstantiate(&b->graph_exec[mode][parity], g, 0));
+      cudaGraphDestroy(g);
+    }
   b->cur = saved;
   b->graph_dt = dt;
   b->graph_vi = vi;
@@ -1085,7 +1136,7 @@ static int step_begin(Batch* b, float dt, int vi, int pi, const uint8_t* mask) {
   }
   int entry = b->cur;
   bool graph = b->use_graphs && !need_bp && !b->events_on && all_active && dt > 0.0f;
-  if (graph && (!b->graph_exec[0] || b->graph_version != b->layout_version || b->graph_dt != dt ||
+  if (graph && (!b->graph_exec[0][0] || b->graph_version != b->layout_version || b->graph_dt != dt ||
                 b->graph_vi != vi || b->graph_pi != pi))
     TRY(capture_graphs(b, dt, vi, pi));
   if (need_bp) {
@@ -1099,8 +1150,11 @@ static int step_begin(Batch* b, float dt, int vi, int pi, const uint8_t* mask) {
     entry = b->cur;
   }
   if (graph) {
+    // the refit graph assumes a forest over every fixture (captured with it)
+    const int mode = (bp_mode(b) == BP_REFIT && b->tree_nf == b->NF && b->tree_nw == b->NW) ? BP_REFIT : BP_FULL;
     cudaEventRecord(b->ev[0], b->stream);
-    CUDA_TRY(b, cudaGraphLaunch(b->graph_exec[entry], b->stream));
+    CUDA_TRY(b, cudaGraphLaunch(b->graph_exec[mode][entry], b->stream));
+    bp_done(b, mode);
     cudaEventRecord(b->ev[4], b->stream);
     b->cur = entry ^ 1;
     b->last_solve_buf = entry;
@@ -1255,8 +1309,7 @@ B2G_API int b2g_batch_destroy(b2g_batch* b) {
   }
   cudaSetDevice(b->device);
   cudaStreamSynchronize(b->stream);
-  for (int k = 0; k < 2; ++k)
-    if (b->graph_exec[k]) cudaGraphExecDestroy(b->graph_exec[k]);
+  invalidate_graphs(b);
   if (b->h_readback) cudaFreeHost(b->h_readback);
   if (b->h_stage) cudaFreeHost(b->h_stage);
   if (b->stage_ev) cudaEventDestroy(b->stage_ev);
@@ -1578,6 +1631,7 @@ static int compact_device(Batch* b, int32_t* old_to_new, int32_t n) {
   b->poff_valid[0] = b->poff_valid[1] = false;
   b->last_solve_buf = -1;
   b->tree_valid = false;
+  forest_reset(b);
   CUDA_TRY(b, cudaMemsetAsync(b->status.p, 0, sizeof(unsigned int), s));
   launch_joint_colour(make_args(b), 0, kept, s);
   TRY(check_upload_status(b));
@@ -2254,6 +2308,7 @@ static int ensure_query_trees(Batch* b) {
     KernelArgs a = step_args(b, 0.0f, 0, 0);
     launch_bp_build(a, b->NF, b->NW, b->cub_tmp.cap, sort_bits(b), b->stream, false);
     CUDA_TRY(b, cudaGetLastError());
+    bp_done(b, BP_FULL);
   }
   b->tree_valid = true;
   CUDA_TRY(b, cudaMemsetAsync(b->status.p, 0, sizeof(unsigned int), b->stream));

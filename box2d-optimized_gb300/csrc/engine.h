@@ -218,6 +218,10 @@ struct Batch {
   int cur = 0;
   int last_solve_buf = -1;        // contact buffer the last solve read (solver order lookups)
   bool tree_valid = false;        // the per-world trees match the current body transforms
+  // The broadphase forest kept between steps: trees of fixtures [0, tree_nf) (worlds [0,
+  // tree_nw)), refit by the closing broadphase and rebuilt from sorted Morton codes every
+  // kTreeRebuildPeriod broadphases (tree_age counts those since the last full build).
+  int tree_nf = 0, tree_nw = 0, tree_age = 0;
 
   // world query scratch
   DBuf<int> q_world, q_counts, q_out;
@@ -309,7 +313,7 @@ struct Batch {
 
   // CUDA graphs of one Step (one per parity of the live contact buffer)
   bool use_graphs = true;
-  cudaGraphExec_t graph_exec[2] = {nullptr, nullptr};
+  cudaGraphExec_t graph_exec[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};  // [broadphase mode][parity]
   uint64_t graph_version = 0;
   float graph_dt = 0;
   int graph_vi = -1, graph_pi = -1;

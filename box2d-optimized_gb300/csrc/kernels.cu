@@ -316,6 +316,15 @@ __global__ void k_lbvh_init(KernelArgs a, int n, int nw) {
   }
 }
 
+// Refit of existing trees: leaf boxes from the fixtures' new AABBs in the trees' leaf order, node
+// arrival counters cleared (internal nodes of every tree built over [0, n) lie in [0, n)).
+__global__ void k_lbvh_refit_init(KernelArgs a, int n) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  a.laabb[i] = a.aabb[a.mval_sorted[i]];
+  a.nflag[i] = 0;
+}
+
 // Bottom-up node bounds: the second thread to reach a node combines its children. Walks stop at
 // their world's root (the traversal never reads nodes above it). The arrival counter is an
 // acquire-release atomic: the first thread's child bounds are visible to the second.
@@ -718,6 +727,41 @@ void launch_bp_tail(const KernelArgs& a0, int f0, int nf, int w0, int nw, size_t
   int r = (n + 1 > nwt ? n + 1 : nwt);
   k_tail_ranges<<<grid_for(r, 128), 128, 0, s>>>(a, nwt, n, poff_live);
   k_tail_commit<<<1, 1, 0, s>>>(a);
+}
+void launch_bp_refit(const KernelArgs& a, int tree_nf, int tree_nw, int nf, int nw, size_t cub_bytes, int sort_bits,
+                     cudaStream_t s) {
+  if (nf <= 0) {
+    launch_bp_build(a, nf, nw, cub_bytes, sort_bits, s, true);
+    return;
+  }
+  k_aabb<<<grid_for(nf, 128), 128, 0, s>>>(a, nf);
+  if (tree_nf > 0) {
+    k_lbvh_refit_init<<<grid_for(tree_nf, 256), 256, 0, s>>>(a, tree_nf);
+    if (tree_nf > 1) k_lbvh_bounds<<<grid_for(tree_nf, 256), 256, 0, s>>>(a, tree_nf);
+  }
+  const int n = nf - tree_nf, nwt = nw - tree_nw;
+  if (nwt > 0) {  // worlds appended after the kept trees: trees of their own over [tree_nf, nf)
+    KernelArgs t = a;
+    t.bp_f0 = tree_nf;
+    t.bp_w0 = tree_nw;
+    if (n > 0) {
+      k_world_bounds<<<nwt, 256, 0, s>>>(t);
+      k_morton<<<grid_for(n, 256), 256, 0, s>>>(t, n);
+      size_t bytes = cub_bytes;
+      cub::DeviceRadixSort::SortPairs(a.cub_tmp, bytes, a.mkey + tree_nf, a.mkey_sorted + tree_nf, a.mval + tree_nf,
+                                      a.mval_sorted + tree_nf, n, 0, sort_bits, s);
+    }
+    int m = n > nwt ? n : nwt;
+    k_lbvh_init<<<grid_for(m, 256), 256, 0, s>>>(t, n, nwt);
+    if (n > 1) {
+      k_lbvh_internal<<<grid_for(n - 1, 256), 256, 0, s>>>(t, n);
+      k_lbvh_bounds<<<grid_for(n, 256), 256, 0, s>>>(t, n);
+    }
+  }
+  k_pairs_count<<<grid_for(nf, 128), 128, 0, s>>>(a, nf);
+  size_t bytes = cub_bytes;
+  cub::DeviceScan::ExclusiveSum(a.cub_tmp, bytes, a.pcount, a.poff, nf + 1, s);
+  k_world_contacts<<<grid_for(nw, 128), 128, 0, s>>>(a, nw);
 }
 void launch_bp_emit(const KernelArgs& a, int nf, cudaStream_t s) {
   if (nf > 0) k_pairs_emit<<<grid_for(nf, 128), 128, 0, s>>>(a, nf);

@@ -200,6 +200,12 @@ void launch_clear_forces(const KernelArgs& a, int nb, cudaStream_t s);
 // count, its scan and the per-world contact ranges of the list being built.
 void launch_bp_build(const KernelArgs& a, int nf, int nw, size_t cub_bytes, int sort_bits, cudaStream_t s,
                      bool pairs = true);
+// Broadphase that keeps the per-world trees of fixtures [0, tree_nf) (worlds [0, tree_nw)): their
+// leaf boxes are refreshed and the node boxes refit bottom-up, the fixtures appended after them
+// get trees of their own, then the pair count, scan and contact ranges as launch_bp_build. Any
+// tree yields the same pair set (the partners of a fixture are sorted before emission).
+void launch_bp_refit(const KernelArgs& a, int tree_nf, int tree_nw, int nf, int nw, size_t cub_bytes, int sort_bits,
+                     cudaStream_t s);
 void launch_bp_emit(const KernelArgs& a, int nf, cudaStream_t s);
 // Broadphase of the appended fixtures [f0, nf) of worlds [w0, nw) only; their pairs are appended to
 // the live list (buffer dst); poff_live (may be null) gets the appended fixtures' offsets.
