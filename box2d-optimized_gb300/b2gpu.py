@@ -240,7 +240,7 @@ class Lib:
         "b2g_last_error", "b2g_device_count", "b2g_query_aabb", "b2g_raycast_closest", "b2g_world_status",
         "b2g_world_snapshot", "b2g_world_restore", "b2g_server_cancel", "b2g_body_set_awake",
         "b2g_bodies_sleep_time_read", "b2g_world_get_flags", "b2g_server_batch", "b2g_step_begin",
-        "b2g_step_poll", "b2g_step_end", "b2g_batch_stage", "b2g_server_set_builders", "b2g_batch_set_solver_waves",
+        "b2g_step_poll", "b2g_step_end", "b2g_batch_stage", "b2g_server_set_builders", "b2g_batch_set_solver_waves", "b2g_batch_set_tree_rebuild_period",
     ]
 
     def __init__(self, path: os.PathLike | str | None = None):
@@ -295,6 +295,7 @@ class Lib:
             "b2g_batch_stage": ([vp], C.c_int),
             "b2g_server_set_builders": ([vp, i32], C.c_int),
             "b2g_batch_set_solver_waves": ([vp, f32], C.c_int),
+            "b2g_batch_set_tree_rebuild_period": ([vp, i32], C.c_int),
             "b2g_batch_set_debug_checks": ([vp, i32], C.c_int),
             "b2g_body_set_awake": ([vp, i32, i32, i32], C.c_int),
             "b2g_world_get_flags": ([vp, i32, P(i32), P(i32), P(i32), P(i32)], C.c_int),

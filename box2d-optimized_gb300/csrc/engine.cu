@@ -805,12 +805,11 @@ static int sort_bits(Batch* b) {
 // Broadphase modes: a full build sorts every fixture's Morton code and builds every world's tree;
 // a refit keeps the trees of the forest (b->tree_nf fixtures), refits their boxes and builds trees
 // only for the fixtures appended after them. Both give the same pairs; the full build restores
-// the trees' spatial order, so it runs every kTreeRebuildPeriod broadphases.
+// the trees' spatial order, so it runs every b->tree_period broadphases.
 enum { BP_FULL = 0, BP_REFIT = 1 };
-const int kTreeRebuildPeriod = 8;
 
 static int bp_mode(const Batch* b) {
-  return (b->tree_nf > 0 && b->tree_nf <= b->NF && b->tree_nw <= b->NW && b->tree_age < kTreeRebuildPeriod)
+  return (b->tree_nf > 0 && b->tree_nf <= b->NF && b->tree_nw <= b->NW && b->tree_age < b->tree_period)
              ? BP_REFIT : BP_FULL;
 }
 
@@ -1943,6 +1942,12 @@ B2G_API int b2g_batch_set_solver_threads(b2g_batch* b, const int32_t* threads) {
     replan_solver(b);
     b->layout_version++;  // captured graphs hold the old launch shapes
   }
+  return B2G_OK;
+}
+
+B2G_API int b2g_batch_set_tree_rebuild_period(b2g_batch* b, int32_t period) {
+  if (!b || period < 1) return B2G_E_INVALID_ARG;
+  b->tree_period = period;
   return B2G_OK;
 }
 

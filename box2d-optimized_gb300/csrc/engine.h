@@ -220,8 +220,9 @@ struct Batch {
   bool tree_valid = false;        // the per-world trees match the current body transforms
   // The broadphase forest kept between steps: trees of fixtures [0, tree_nf) (worlds [0,
   // tree_nw)), refit by the closing broadphase and rebuilt from sorted Morton codes every
-  // kTreeRebuildPeriod broadphases (tree_age counts those since the last full build).
+  // tree_period broadphases (tree_age counts those since the last full build).
   int tree_nf = 0, tree_nw = 0, tree_age = 0;
+  int tree_period = 16;  // broadphases per full build (1: every broadphase builds)
 
   // world query scratch
   DBuf<int> q_world, q_counts, q_out;

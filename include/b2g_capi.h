@@ -381,6 +381,11 @@ B2G_API int b2g_batch_get_solver_threads(b2g_batch* b, int32_t* threads);
  * solve is faster. A size class runs the wide build when its worlds fill at most `waves` waves of
  * it (default 2; 0 never, a large value always). A tuning knob: results do not depend on it. */
 B2G_API int b2g_batch_set_solver_waves(b2g_batch* b, float waves);
+/* The broadphase keeps each world's tree between steps and refits its boxes; every `period`
+ * broadphases (default 16; 1 = every one) it rebuilds all trees from sorted Morton codes, which
+ * restores their spatial order. A tuning knob: the pairs found, and so the results, do not
+ * depend on it. */
+B2G_API int b2g_batch_set_tree_rebuild_period(b2g_batch* b, int32_t period);
 /* Autotuner: picks each size class's threads per world by timing the solver over `steps` eager
  * steps per candidate (the class's current count, half and double), largest worlds first. The
  * steps are real steps of the batch (its worlds advance; their number goes to steps_taken);
