@@ -227,6 +227,18 @@ static void replan_solver(Batch* b) {
 static const size_t kMaxWorldBodies = size_t(1) << 24;
 
 // Reads the status word after the upload's joint colouring (the upload synchronises anyway).
+// Each world's slice of the sorted no-collide list (its bodies are contiguous, so its pairs are) in
+// the world table's joint record: z = first entry, w = count. The pair filter searches only there.
+static void nocollide_ranges(const std::vector<uint64_t>& nocol, const std::vector<int>& body_off,
+                             std::vector<int4>& wj) {
+  for (size_t w = 0; w < wj.size(); ++w) {
+    auto lo = std::lower_bound(nocol.begin(), nocol.end(), (uint64_t)(uint32_t)body_off[w] << 32);
+    auto hi = std::lower_bound(lo, nocol.end(), (uint64_t)(uint32_t)body_off[w + 1] << 32);
+    wj[w].z = (int)(lo - nocol.begin());
+    wj[w].w = (int)(hi - lo);
+  }
+}
+
 // The broadphase forest no longer matches the fixture layout: the next broadphase builds every tree.
 static void forest_reset(Batch* b) { b->tree_nf = b->tree_nw = b->tree_age = 0; }
 
@@ -360,6 +372,7 @@ int upload_all(Batch* b) {
                    [&](int x, int y) { return b->worlds[x].bodies.size() > b->worlds[y].bodies.size(); });
   b->h_world_order = order;
   replan_solver(b);
+  nocollide_ranges(nocol, b->h_body_off, wj);
   TRY(upload(b, b->wb, wb)); TRY(upload(b, b->wj, wj)); TRY(upload(b, b->wg, wg)); TRY(upload(b, b->wflags, wflags));
   TRY(upload(b, b->world_order, order));
   // per-world live contact ranges: the sorted contact list groups by world (keys hold global
@@ -390,6 +403,7 @@ int upload_all(Batch* b) {
   TRY(upload(b, b->fmat, fmat)); TRY(ensure(b, b->aabb, NF));
   TRY(upload(b, b->joints, joints)); TRY(upload(b, b->nocollide, nocol));
   b->n_nocollide = (int)nocol.size();
+  b->h_nocol.swap(nocol);
   b->cur = 0;
   TRY(upload(b, b->ckey[0], ckey)); TRY(upload(b, b->cfix[0], cfix)); TRY(upload(b, b->cflags[0], cflags));
   TRY(upload(b, b->cmat[0], cmat)); TRY(upload(b, b->cman[0], cman));
@@ -588,6 +602,8 @@ static int flush_tail(Batch* b, TailPack& P) {
   replan_solver(b);
   std::vector<int2> wc_tail(NW - w0, make_int2(0, 0));
   Stager st;
+  b->h_nocol.insert(b->h_nocol.end(), P.nocol.begin(), P.nocol.end());  // appended bodies sort last
+  nocollide_ranges(b->h_nocol, b->h_body_off, wj);
   TRY(st.add(b, b->wb, 0, wb)); TRY(st.add(b, b->wj, 0, wj)); TRY(st.add(b, b->wg, w0, wg_tail));
   TRY(st.add(b, b->wflags, 0, wflags)); TRY(st.add(b, b->world_order, 0, order)); TRY(st.add(b, b->wc, w0, wc_tail));
   b->h_wflags = wflags;
@@ -1611,9 +1627,11 @@ static int compact_device(Batch* b, int32_t* old_to_new, int32_t n) {
   b->h_body_off[kept] = NB2; b->h_fix_off[kept] = NF2; b->h_joint_off[kept] = NJ2;
   std::sort(nocol.begin(), nocol.end());
   nocol.erase(std::unique(nocol.begin(), nocol.end()), nocol.end());
+  nocollide_ranges(nocol, b->h_body_off, wj);
   TRY(upload(b, b->wb, wb)); TRY(upload(b, b->wj, wj)); TRY(upload(b, b->wg, wg2)); TRY(upload(b, b->wc, wc2));
   TRY(upload(b, b->wflags, wflags)); TRY(upload(b, b->nocollide, nocol));
   b->n_nocollide = (int)nocol.size();
+  b->h_nocol.swap(nocol);
   std::vector<int> order(kept);
   std::iota(order.begin(), order.end(), 0);
   std::stable_sort(order.begin(), order.end(),

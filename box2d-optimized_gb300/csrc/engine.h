@@ -176,6 +176,7 @@ struct Batch {
   int NW = 0, NB = 0, NF = 0, NJ = 0;
   int64_t NC = 0;                 // live contacts
   std::vector<int> h_body_off, h_fix_off, h_joint_off;
+  std::vector<uint64_t> h_nocol;  // host copy of the device no-collide list (sorted body pairs)
 
   // ---- device arrays
   DBuf<int4> wb;                  // body_off, body_cnt, fix_off, fix_cnt

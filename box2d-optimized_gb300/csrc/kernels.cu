@@ -372,17 +372,18 @@ __device__ __forceinline__ bool nocollide_has(const uint64_t* keys, int n, uint6
 // fixture of a static pair, else the lower index. Filters of b2ContactManager::QueryCallback:
 // same body, b2Body::ShouldCollide (a dynamic body, no collideConnected=false joint), the default
 // b2ContactFilter (group / category / mask) and the collider table. fa / ga are the packed
-// attributes of f and g (k_aabb).
-__device__ __forceinline__ bool accept_pair(const KernelArgs& a, int f, int4 fa, int g, int4 ga) {
+// attributes of f and g (k_aabb); `nocol` is the world's slice of the no-collide list (first,
+// count).
+__device__ __forceinline__ bool accept_pair(const KernelArgs& a, int f, int4 fa, int g, int4 ga, int2 nocol) {
   if (g == f) return false;
   int bf = fa.x, bg = ga.x;
   if (bg == bf) return false;
   int tf = fa.w >> 8, tg = ga.w >> 8;
   if (tg != B2G_STATIC && g < f) return false;
   if (tf != B2G_DYNAMIC && tg != B2G_DYNAMIC) return false;
-  if (a.n_nocollide > 0) {
+  if (nocol.y > 0) {
     uint32_t x = (uint32_t)min(bf, bg), y = (uint32_t)max(bf, bg);
-    if (nocollide_has(a.nocollide, a.n_nocollide, ((uint64_t)x << 32) | y)) return false;
+    if (nocollide_has(a.nocollide + nocol.x, nocol.y, ((uint64_t)x << 32) | y)) return false;
   }
   int gf = fa.y, gg = ga.y;
   if (gf == gg && gf != 0) {
@@ -410,6 +411,8 @@ __device__ __forceinline__ int traverse_pairs(const KernelArgs& a, int f, OnPair
   int root = a.wroot[wf];
   if (root < 0 || (root & LEAF_BIT)) return 0;
   float4 box = a.aabb[f];
+  const int4 wjw = a.wj[wf];
+  const int2 nocol = make_int2(wjw.z, wjw.w);
   int stack[BP_STACK];
   int sp = 0;
   stack[sp++] = root;
@@ -430,7 +433,7 @@ __device__ __forceinline__ int traverse_pairs(const KernelArgs& a, int f, OnPair
       if (!aabb_overlap4(box, cbox[q])) continue;
       if (c & LEAF_BIT) {
         int g = a.mval_sorted[c & ~LEAF_BIT];
-        if (accept_pair(a, f, fa, g, a.fattr[g])) {
+        if (accept_pair(a, f, fa, g, a.fattr[g], nocol)) {
           on_pair(g, cnt);
           ++cnt;
         }
