@@ -334,9 +334,18 @@ __device__ __forceinline__ void unpack_pos(const PosRows& r, VCDev& vc, const Ma
 }
 
 // One pass over the contact colours: colour by colour, a CTA barrier after each; colour 63 (the
-// overflow colour) is solved serially by thread 0 in priority order.
-template <int T, class Rows, class Fetch, class Solve>
+// overflow colour) is solved serially by thread 0 in priority order. Each thread reads the rows of
+// its first constraint of the next regular colour before the barrier, so that their round trip
+// overlaps the wait: rows do not change while a colour is solved (a constraint's impulses are
+// written only by its own solve, once per pass), only the bodies do, and those are read after.
+template <int T, class Rows, bool PREFETCH, class Fetch, class Solve>
 __device__ __forceinline__ void colour_sweep(const int* ranges, int ncol, int c0, Fetch fetch, Solve solve) {
+  Rows pre;
+  bool have = false;  // pre holds the rows of this thread's first constraint of colour c
+  if (PREFETCH && ncol > 0 && ranges[0] + (int)threadIdx.x < ranges[1]) {
+    fetch(c0 + ranges[0] + threadIdx.x, pre);
+    have = true;
+  }
   for (int c = 0; c < ncol; ++c) {
     int s = ranges[c], e = ranges[c + 1];
     if (c == 63) {
@@ -347,11 +356,21 @@ __device__ __forceinline__ void colour_sweep(const int* ranges, int ncol, int c0
           solve(c0 + i, r);
         }
     } else {
-      for (int i = s + threadIdx.x; i < e; i += T) {
+      int i = s + threadIdx.x;
+      if (have) {
+        solve(c0 + i, pre);
+        i += T;
+      }
+      for (; i < e; i += T) {
         Rows r;
         fetch(c0 + i, r);
         solve(c0 + i, r);
       }
+    }
+    have = false;
+    if (PREFETCH && c + 1 < ncol && c + 1 != 63 && ranges[c + 1] + (int)threadIdx.x < ranges[c + 2]) {
+      fetch(c0 + ranges[c + 1] + threadIdx.x, pre);
+      have = true;
     }
     __syncthreads();
   }
@@ -716,7 +735,7 @@ __global__ void __launch_bounds__(T, kSolveBlocks<T, WIDE>) k_solve(KernelArgs a
   auto fetchV = [&](int slot, VelRows& r) { fetch_vel(P, slot, r); };
   auto fetchP = [&](int slot, PosRows& r) { fetch_pos(P, slot, r); };
   if (warm) {
-    colour_sweep<T, VelRows>(cranges, ncc, c0, fetchV, [&](int slot, const VelRows& r) {
+    colour_sweep<T, VelRows, WIDE>(cranges, ncc, c0, fetchV, [&](int slot, const VelRows& r) {
       VCDev vc;
       unpack_vel(r, vc, M);
       warmStartContact(vc, bs);
@@ -746,7 +765,7 @@ __global__ void __launch_bounds__(T, kSolveBlocks<T, WIDE>) k_solve(KernelArgs a
         for (int i = i0; i < e; i += step) jointSolveVelocitySlot(a.jplanes, a.jstride, j0 + i, jb, a.dt, a.inv_dt);
       __syncthreads();
     }
-    colour_sweep<T, VelRows>(cranges, ncc, c0, fetchV, [&](int slot, const VelRows& r) {
+    colour_sweep<T, VelRows, WIDE>(cranges, ncc, c0, fetchV, [&](int slot, const VelRows& r) {
       VCDev vc;
       unpack_vel(r, vc, M);
       solveContactVelocity(vc, bs);
@@ -803,7 +822,7 @@ __global__ void __launch_bounds__(T, kSolveBlocks<T, WIDE>) k_solve(KernelArgs a
   //    constraints were all okay in an iteration is done and no longer iterated.
   for (int it = 0; it < a.pi; ++it) {
     int okay = 1;
-    colour_sweep<T, PosRows>(cranges, ncc, c0, fetchP, [&](int slot, const PosRows& r) {
+    colour_sweep<T, PosRows, WIDE>(cranges, ncc, c0, fetchP, [&](int slot, const PosRows& r) {
       VCDev vc;
       unpack_pos(r, vc, M);
       int root = 0;

@@ -199,6 +199,23 @@ def test_solver_threads_do_not_change_results(lib):
     assert out[0] == out[1] == out[2]
 
 
+def test_solver_build_and_tree_period_do_not_change_results(lib):
+    """The occupancy (64-register) and wide (128-register) builds of the solver, and broadphases
+    that rebuild every tree each step or refit kept trees for 16 steps, give the same bits, with
+    CUDA graphs and without."""
+    out = []
+    for waves, period, graphs in ((0.0, 1, False), (1e9, 16, False), (0.0, 16, True), (1e9, 3, True)):
+        b, ws = _mixed_batch(lib, CLASS_SEEDS, CLASS_SIZES)
+        lib.check(lib.b2g_batch_set_solver_waves(b.h, waves), "waves")
+        lib.check(lib.b2g_batch_set_tree_rebuild_period(b.h, period), "period")
+        b.set_graphs(graphs)
+        for _ in range(40):
+            b.step(1 / 60, 8, 3)
+        out.append([_state_bytes(b.bodies(w)) for w in ws])
+        b.close()
+    assert out[0] == out[1] == out[2] == out[3]
+
+
 def test_autotune_picks_valid_threads_and_keeps_results(lib):
     tuned, ws = _mixed_batch(lib, CLASS_SEEDS, CLASS_SIZES)
     threads, taken = tuned.autotune(steps=2)
