@@ -289,7 +289,7 @@ struct Batch {
   std::vector<SolveClass> solve_classes;
   std::vector<int> h_world_order;  // worlds by body count, largest first (device world_order)
   int class_threads[B2G_SOLVE_CLASSES] = {64, 128, 256, 512, 1024};
-  float wide_waves = 2.0f;  // size classes of at most this many waves run the wide solver build
+  float wide_waves = 1e9f;  // size classes of at most this many waves run the wide solver build (all, by default)
   cudaStream_t side[B2G_SOLVE_CLASSES] = {};
   cudaEvent_t fork_ev[B2G_SOLVE_CLASSES + 1] = {};
 

@@ -377,9 +377,9 @@ B2G_API int b2g_batch_set_debug_checks(b2g_batch* b, int32_t enable);
 B2G_API int b2g_batch_set_solver_threads(b2g_batch* b, const int32_t* threads);
 B2G_API int b2g_batch_get_solver_threads(b2g_batch* b, int32_t* threads);
 /* The solver kernel comes in two builds: one for occupancy (1024 threads per SM, at most 64
- * registers a thread) and a wide one (512 threads per SM, up to 128 registers) whose per-world
- * solve is faster. A size class runs the wide build when its worlds fill at most `waves` waves of
- * it (default 2; 0 never, a large value always). A tuning knob: results do not depend on it. */
+ * registers a thread) and a wide one (512 threads per SM, up to 128 registers, unspilled) whose
+ * per-world solve is faster. A size class runs the wide build when its worlds fill at most
+ * `waves` waves of it (default: every class; 0 never). A tuning knob: results do not depend on it. */
 B2G_API int b2g_batch_set_solver_waves(b2g_batch* b, float waves);
 /* The broadphase keeps each world's tree between steps and refits its boxes; every `period`
  * broadphases (default 16; 1 = every one) it rebuilds all trees from sorted Morton codes, which
