@@ -735,7 +735,7 @@ __global__ void __launch_bounds__(T, kSolveBlocks<T, WIDE>) k_solve(KernelArgs a
   auto fetchV = [&](int slot, VelRows& r) { fetch_vel(P, slot, r); };
   auto fetchP = [&](int slot, PosRows& r) { fetch_pos(P, slot, r); };
   if (warm) {
-    colour_sweep<T, VelRows, WIDE>(cranges, ncc, c0, fetchV, [&](int slot, const VelRows& r) {
+    colour_sweep<T, VelRows, (WIDE && T <= 512)>(cranges, ncc, c0, fetchV, [&](int slot, const VelRows& r) {
       VCDev vc;
       unpack_vel(r, vc, M);
       warmStartContact(vc, bs);
@@ -765,7 +765,7 @@ __global__ void __launch_bounds__(T, kSolveBlocks<T, WIDE>) k_solve(KernelArgs a
         for (int i = i0; i < e; i += step) jointSolveVelocitySlot(a.jplanes, a.jstride, j0 + i, jb, a.dt, a.inv_dt);
       __syncthreads();
     }
-    colour_sweep<T, VelRows, WIDE>(cranges, ncc, c0, fetchV, [&](int slot, const VelRows& r) {
+    colour_sweep<T, VelRows, (WIDE && T <= 512)>(cranges, ncc, c0, fetchV, [&](int slot, const VelRows& r) {
       VCDev vc;
       unpack_vel(r, vc, M);
       solveContactVelocity(vc, bs);
@@ -822,7 +822,7 @@ __global__ void __launch_bounds__(T, kSolveBlocks<T, WIDE>) k_solve(KernelArgs a
   //    constraints were all okay in an iteration is done and no longer iterated.
   for (int it = 0; it < a.pi; ++it) {
     int okay = 1;
-    colour_sweep<T, PosRows, WIDE>(cranges, ncc, c0, fetchP, [&](int slot, const PosRows& r) {
+    colour_sweep<T, PosRows, (WIDE && T <= 512)>(cranges, ncc, c0, fetchP, [&](int slot, const PosRows& r) {
       VCDev vc;
       unpack_pos(r, vc, M);
       int root = 0;
