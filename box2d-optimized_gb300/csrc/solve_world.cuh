@@ -14,34 +14,90 @@ namespace b2g {
 
 #define FULL_MASK 0xffffffffu
 
-// Block-wide exclusive scan of one int per thread (blockDim.x == T).
-template <int T>
-__device__ int block_scan(int v, int* total) {
+// Stable compaction of [0, n) with T / 32 warp-owned segments (multiples of 32 items, in list
+// order): `flag(k)` is evaluated twice, once to count each warp's kept items by ballots and once
+// to place them, and kept item k is handed to `emit(k, rank)` with its rank in list order. Two
+// CTA barriers in all, whatever n. Returns the number kept (in every thread).
+template <int T, class Flag, class Emit>
+__device__ __forceinline__ int block_compact(int n, Flag flag, Emit emit) {
   constexpr int NWARP = T / 32;
-  __shared__ int warp_sums[NWARP];
-  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  int x = v;
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    int y = __shfl_up_sync(FULL_MASK, x, o);
-    if (lane >= o) x += y;
+  __shared__ int wbase[NWARP + 1];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int seg = (((n + NWARP - 1) / NWARP) + 31) & ~31;
+  const int s0 = min(n, wid * seg), s1 = min(n, s0 + seg);
+  int cnt = 0;
+  for (int k0 = s0; k0 < s1; k0 += 32) {
+    const int k = k0 + lane;
+    cnt += __popc(__ballot_sync(FULL_MASK, k < s1 && flag(k)));
   }
-  if (lane == 31) warp_sums[wid] = x;
+  if (lane == 0) wbase[wid] = cnt;
   __syncthreads();
-  if (wid == 0) {
-    int s = lane < NWARP ? warp_sums[lane] : 0;
+  if (threadIdx.x == 0) {
+    int acc = 0;
+    for (int w = 0; w < NWARP; ++w) {
+      const int c = wbase[w];
+      wbase[w] = acc;
+      acc += c;
+    }
+    wbase[NWARP] = acc;
+  }
+  __syncthreads();
+  int base = wbase[wid];
+  const unsigned lt = (1u << lane) - 1u;
+  for (int k0 = s0; k0 < s1; k0 += 32) {
+    const int k = k0 + lane;
+    const bool f = k < s1 && flag(k);
+    const unsigned b = __ballot_sync(FULL_MASK, f);
+    if (f) emit(k, base + __popc(b & lt));
+    base += __popc(b);
+  }
+  const int total = wbase[NWARP];
+  __syncthreads();  // wbase is reused by the next call
+  return total;
+}
+
+// Exclusive prefix sums of get(i) over [0, n) in index order, handed to put(i, prefix), with
+// warp-owned segments: each warp sums its segment, thread 0 scans the T / 32 sums, each warp
+// scans its segment on top. Two CTA barriers in all. Returns the total (in every thread).
+template <int T, class Get, class Put>
+__device__ __forceinline__ int block_exclusive_scan(int n, Get get, Put put) {
+  constexpr int NWARP = T / 32;
+  __shared__ int wbase[NWARP + 1];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int seg = (((n + NWARP - 1) / NWARP) + 31) & ~31;
+  const int s0 = min(n, wid * seg), s1 = min(n, s0 + seg);
+  int sum = 0;
+  for (int k = s0 + lane; k < s1; k += 32) sum += get(k);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(FULL_MASK, sum, o);
+  if (lane == 0) wbase[wid] = sum;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int acc = 0;
+    for (int w = 0; w < NWARP; ++w) {
+      const int c = wbase[w];
+      wbase[w] = acc;
+      acc += c;
+    }
+    wbase[NWARP] = acc;
+  }
+  __syncthreads();
+  int base = wbase[wid];
+  for (int k0 = s0; k0 < s1; k0 += 32) {
+    const int k = k0 + lane;
+    const int v = k < s1 ? get(k) : 0;
+    int x = v;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-      int y = __shfl_up_sync(FULL_MASK, s, o);
-      if (lane >= o) s += y;
+      const int y = __shfl_up_sync(FULL_MASK, x, o);
+      if (lane >= o) x += y;
     }
-    if (lane < NWARP) warp_sums[lane] = s;
+    if (k < s1) put(k, base + x - v);
+    base += __shfl_sync(FULL_MASK, x, 31);
   }
-  __syncthreads();
-  int prefix = (wid > 0 ? warp_sums[wid - 1] : 0) + x - v;
-  *total = warp_sums[NWARP - 1];
-  __syncthreads();
-  return prefix;
+  const int total = wbase[NWARP];
+  __syncthreads();  // wbase is reused by the next call
+  return total;
 }
 
 // Working arrays of one colouring, each in shared or global memory (generic pointers).
@@ -70,13 +126,12 @@ __device__ int colour_constraints(int n, int nb, const ColourMem m, const uint32
                                   int* ranges, unsigned int* status) {
   __shared__ int col_cnt[64];
   __shared__ int col_off[65];
-  __shared__ int s_carry, s_maxcol;
+  __shared__ int s_maxcol;
   for (int i = threadIdx.x; i < nb; i += T) {
     m.cnt[i] = 0;
     m.mask[i] = 0ull;
   }
   for (int k = threadIdx.x; k < n; k += T) m.col[k] = -1;
-  if (threadIdx.x == 0) s_carry = 0;
   __syncthreads();
   for (int k = threadIdx.x; k < n; k += T) {
     int2 b = m.cb[k];
@@ -84,16 +139,7 @@ __device__ int colour_constraints(int n, int nb, const ColourMem m, const uint32
     if (b.y >= 0) atomicAdd(&m.cnt[b.y], 1);
   }
   __syncthreads();
-  for (int i0 = 0; i0 < nb; i0 += T) {
-    int i = i0 + threadIdx.x;
-    int v = i < nb ? m.cnt[i] : 0;
-    int total;
-    int p = block_scan<T>(v, &total);
-    if (i < nb) m.head[i] = s_carry + p;
-    __syncthreads();
-    if (threadIdx.x == 0) s_carry += total;
-    __syncthreads();
-  }
+  block_exclusive_scan<T>(nb, [&](int i) { return m.cnt[i]; }, [&](int i, int p) { m.head[i] = p; });
   for (int i = threadIdx.x; i < nb; i += T) m.cnt[i] = 0;
   __syncthreads();
   for (int k = threadIdx.x; k < n; k += T) {
@@ -123,23 +169,27 @@ __device__ int colour_constraints(int n, int nb, const ColourMem m, const uint32
   // rounds over a worklist of the uncoloured constraints: a round colours every constraint that
   // heads the priority lists of all its non-static bodies (at least the uncoloured one of lowest
   // (priority, index)); the others form the next round's worklist (their order is immaterial)
-  __shared__ int s_m, s_next;
+  // worklist sizes alternate between two counters: a round reads one and fills the other, which it
+  // clears before its first barrier (every thread read it two barriers ago)
+  __shared__ int s_cnt[2];
   if (threadIdx.x == 0) {
-    s_m = n;
-    s_next = 0;
+    s_cnt[0] = n;
+    s_cnt[1] = 0;
   }
   __syncthreads();
   int* wl = m.wl0;
   int* wn = m.wl1;
   bool done = (n == 0);
   for (int round = 0; round <= n + 1 && !done; ++round) {
-    const int cnt = s_m;
+    const int cur = round & 1;
+    const int cnt = s_cnt[cur];
     for (int i = threadIdx.x; i < cnt; i += T) {
       int k = round == 0 ? i : wl[i];
       int2 b = m.cb[k];
       bool ok = (b.x < 0 || m.list[m.head[b.x]] == k) && (b.y < 0 || m.list[m.head[b.y]] == k);
       m.rdy[k] = ok ? 1 : 0;
     }
+    if (round > 0 && threadIdx.x == 0) s_cnt[cur ^ 1] = 0;
     __syncthreads();
     for (int i0 = 0; i0 < cnt; i0 += T) {  // CTA-uniform trip count: whole warps reach the ballot
       int i = i0 + threadIdx.x;
@@ -169,17 +219,12 @@ __device__ int colour_constraints(int n, int nb, const ColourMem m, const uint32
       unsigned bal = __ballot_sync(FULL_MASK, keep);
       int lane = threadIdx.x & 31;
       int base = 0;
-      if (lane == 0 && bal) base = atomicAdd(&s_next, __popc(bal));
+      if (lane == 0 && bal) base = atomicAdd(&s_cnt[cur ^ 1], __popc(bal));
       base = __shfl_sync(FULL_MASK, base, 0);
       if (keep) wn[base + __popc(bal & ((1u << lane) - 1u))] = k;
     }
     __syncthreads();
-    if (threadIdx.x == 0) {
-      s_m = s_next;
-      s_next = 0;
-    }
-    __syncthreads();
-    done = (s_m == 0);
+    done = (s_cnt[cur ^ 1] == 0);
     int* t = wl;
     wl = wn;
     wn = t;
@@ -580,7 +625,6 @@ __global__ void __launch_bounds__(T, kSolveBlocks<T, WIDE>) k_solve(KernelArgs a
   if ((a.wflags[w] & B2G_WF_ACTIVE) == 0) return;
   __shared__ int cranges[65];
   __shared__ int jranges[65];
-  __shared__ int s_carry;
   const int4 wb = a.wb[w];
   const int b0 = wb.x, nb = wb.y, fo = wb.z;
   const int2 wc = a.wc[w];
@@ -602,35 +646,26 @@ __global__ void __launch_bounds__(T, kSolveBlocks<T, WIDE>) k_solve(KernelArgs a
   if (sleepMode) build_islands<T>(a, b0, nb, c0, ncAll, j0, nj);
 
   // 1. solver contacts in list order, with local bodies (static = -1) and colouring priorities
-  if (threadIdx.x == 0) s_carry = 0;
-  __syncthreads();
-  for (int k0 = 0; k0 < ncAll; k0 += T) {
-    int k = k0 + threadIdx.x;
-    int flag = 0;
-    int2 f = make_int2(0, 0);
-    if (k < ncAll) {
-      uint32_t fl = a.cflags[c0 + k];
-      f = a.cfix[c0 + k];
-      flag = ((fl & B2G_CONTACT_TOUCHING) && (fl & B2G_CONTACT_ENABLED) && !a.fsensor[f.x] && !a.fsensor[f.y]) ? 1 : 0;
-      if (flag && sleepMode)  // contacts of sleeping islands are not solved
-        flag = (isl_bits(SL, isl_root(SL, a.fbody[f.x] - b0, a.fbody[f.y] - b0)) & B2G_ISL_AWAKE) ? 1 : 0;
-    }
-    int total;
-    int p = block_scan<T>(flag, &total);
-    if (flag) {
-      int s = c0 + s_carry + p;
-      a.sc_list[s] = c0 + k;
-      int ia = a.fbody[f.x], ib = a.fbody[f.y];
-      a.scb[s] = make_int2((ia - b0) | (a.btype[ia] == B2G_STATIC ? (int)0x80000000 : 0),
-                           (ib - b0) | (a.btype[ib] == B2G_STATIC ? (int)0x80000000 : 0));
-      uint64_t key = a.ckey[c0 + k];
-      a.cprio[s] = contactPriority((uint32_t)(key >> 32) - (uint32_t)fo, (uint32_t)key - (uint32_t)fo);
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) s_carry += total;
-    __syncthreads();
-  }
-  const int nsc = s_carry;
+  const int nsc = block_compact<T>(
+      ncAll,
+      [&](int k) {
+        const uint32_t fl = a.cflags[c0 + k];
+        const int2 f = a.cfix[c0 + k];
+        bool flag = (fl & B2G_CONTACT_TOUCHING) && (fl & B2G_CONTACT_ENABLED) && !a.fsensor[f.x] && !a.fsensor[f.y];
+        if (flag && sleepMode)  // contacts of sleeping islands are not solved
+          flag = (isl_bits(SL, isl_root(SL, a.fbody[f.x] - b0, a.fbody[f.y] - b0)) & B2G_ISL_AWAKE) != 0;
+        return flag;
+      },
+      [&](int k, int r) {
+        const int s = c0 + r;
+        const int2 f = a.cfix[c0 + k];
+        a.sc_list[s] = c0 + k;
+        const int ia = a.fbody[f.x], ib = a.fbody[f.y];
+        a.scb[s] = make_int2((ia - b0) | (a.btype[ia] == B2G_STATIC ? (int)0x80000000 : 0),
+                             (ib - b0) | (a.btype[ib] == B2G_STATIC ? (int)0x80000000 : 0));
+        const uint64_t key = a.ckey[c0 + k];
+        a.cprio[s] = contactPriority((uint32_t)(key >> 32) - (uint32_t)fo, (uint32_t)key - (uint32_t)fo);
+      });
 
   // 2. colour the solver contacts (shared memory for whatever fits)
   int ncc = 0;
