@@ -8,7 +8,8 @@ HBM (far larger than the 129 MB L2, so no L2 flush is needed between steps).
 
 Prints one JSON line. `value` is whole-job body-steps/s (bodies x steps / max-over-ranks device
 time of the timed steps). `e2e` is the same metric through the public C ABI with host buffers:
-every step copies the bodies' forces host->device (pinned) and reads the transforms back.
+every step copies the bodies' forces host->device (pinned) and reads the transforms back, on a
+second batch of the same worlds over the same window of steps.
 `--impl reference` times the reference algorithm on the host cores instead (the CPU oracle
 restatement of the reference's Step, run on all host threads over a bounded sample of worlds).
 """
@@ -409,20 +410,27 @@ def run_ours(args, rank, world_size):
     # iterations), per second of the whole job
     contact_iters = touching_all * (VI + PI) / (ms_per_step * args.steps / 1e3)
 
-    # end to end through the C ABI with pinned host buffers: forces in, transforms out
+    # end to end through the C ABI with pinned host buffers: forces in, transforms out, every step,
+    # on a second batch of the same worlds over the same window of steps as the timed region (the
+    # later steps of a rollout cost more, so a later window would not be the same workload)
     nbody = prof.bodies
     forces = torch.zeros((nbody, 4), dtype=torch.float32).pin_memory()
     xf_out = torch.empty((nbody, 4), dtype=torch.float32).pin_memory()
     n_out = C.c_int64()
-    e2e_steps = max(3, args.steps // 2)
+    e2e_steps = args.steps
+    eb, _ = build_batch(lib, seeds, dev)
+    if threads:
+        eb.solver_threads(threads)
+    eb.step_timed(args.warmup, DT, VI, PI)
     torch.cuda.synchronize()
     t1 = time.perf_counter()
     for _ in range(e2e_steps):
-        lib.check(lib.b2g_batch_set_forces(batch.h, forces.data_ptr(), nbody), "set_forces")
-        lib.check(lib.b2g_step(batch.h, DT, VI, PI, None), "step")
-        lib.check(lib.b2g_batch_read_states(batch.h, C.cast(xf_out.data_ptr(), C.POINTER(C.c_float)), None,
+        lib.check(lib.b2g_batch_set_forces(eb.h, forces.data_ptr(), nbody), "set_forces")
+        lib.check(lib.b2g_step(eb.h, DT, VI, PI, None), "step")
+        lib.check(lib.b2g_batch_read_states(eb.h, C.cast(xf_out.data_ptr(), C.POINTER(C.c_float)), None,
                                             nbody, C.byref(n_out)), "read_states")
     e2e_s = time.perf_counter() - t1
+    eb.close()
     e2e_value = nb * e2e_steps / e2e_s * world_size
 
     # world queries on the settled batch: closest-hit ray casts and AABB queries, end to end
