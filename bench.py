@@ -499,9 +499,12 @@ def run_ours(args, rank, world_size):
                    "sample": f"{len(cpu_seeds)} of the worlds ({cnb} bodies), steps {args.warmup + 1}-"
                              f"{args.warmup + args.steps} of the same rollout, {secs:.1f} s on {threads} threads"}
         # own kernels per step (CUB's sort and scan kernels not counted): collide, one solver launch
-        # per world size class (5 in this workload), aabb, world bounds, morton, lbvh init /
-        # internal / bounds, pair count, world contact ranges, pair emit, diff, commit, clear forces
-        kernels_per_step = 18
+        # per world size class (5 in this workload), aabb, refit init, lbvh bounds, pair count,
+        # world contact ranges, pair emit, diff, commit, clear forces = 15 on a step whose closing
+        # broadphase refits the kept trees; a full rebuild (every 16th broadphase) launches world
+        # bounds, morton and lbvh init / internal instead of the refit init (+3)
+        kernels_per_step = 15
+        full_builds = args.steps // 16
         line = {
             "metric": METRIC, "value": value, "unit": "body-steps/s", "n_gpus": world_size, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
@@ -527,7 +530,7 @@ def run_ours(args, rank, world_size):
             "batched_over_plain": (value / world_size / plain["value"]) if plain else None,
             "e2e": {"value": e2e_value, "unit": "body-steps/s", "h2d_bytes_per_step": 16 * nbody,
                     "d2h_bytes_per_step": 16 * nbody, "steps": e2e_steps},
-            "gpu_launches": kernels_per_step * args.steps,
+            "gpu_launches": kernels_per_step * args.steps + 3 * full_builds,
             "contact_constraint_iterations_per_s": contact_iters,
             "queries": queries,
             "sleep": sleep,
