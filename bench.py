@@ -563,6 +563,39 @@ def profile_window(args):
     batch.close()
 
 
+def serve_ticks(args):
+    """Tick-driven served measurement (also the ncu case for served steps): a Poisson number of
+    rollout requests (mean --serve-per-tick; 32-4096 bodies log-uniform, K ~ U[16, 512]) arrives
+    before each of --serve-ticks ticks, so the load does not depend on the tick's own duration
+    (as it would under a profiler). Prints the percentiles of the served step and of the device
+    step and its phases over the last two thirds of the ticks."""
+    import numpy as np  # noqa: PLC0415
+
+    lib = G.Lib()
+    rng = np.random.default_rng(2_000_000)
+    srv = G.Server(lib, device=0, budget_bytes=120 << 30, max_worlds=4096)
+    bh = C.c_void_p()
+    lib.check(lib.b2g_server_batch(srv.h, C.byref(bh)), "b2g_server_batch")
+    prof = G.Profile()
+    rec, k = [], 0
+    for _ in range(args.serve_ticks):
+        for _ in range(rng.poisson(args.serve_per_tick)):
+            n = int(round(2 ** rng.uniform(5, 12)))
+            srv.submit(2_000_000 + k, n, int(rng.integers(16, 513)))
+            k += 1
+        active, ms = srv.tick()
+        lib.b2g_profile_get(bh, C.byref(prof))
+        rec.append((ms, active, prof.step, prof.collide, prof.solve, prof.broadphase))
+        list(srv.poll())
+    srv.close()
+    a = np.array(rec[len(rec) // 3:])
+    pct = lambda x: [round(float(np.percentile(x, q)), 3) for q in (50, 90, 99)]  # noqa: E731
+    print(json.dumps({"serve_ticks": {"per_tick": args.serve_per_tick, "ticks": len(rec),
+                                      "active_p50_p90_p99": pct(a[:, 1]), "step_ms": pct(a[:, 0]),
+                                      "gpu_step_ms": pct(a[:, 2]), "collide_ms": pct(a[:, 3]),
+                                      "solve_ms": pct(a[:, 4]), "broadphase_ms": pct(a[:, 5])}}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -584,9 +617,15 @@ def main():
     ap.add_argument("--profile-window", action="store_true",
                     help="ncu case: settle --settle steps, then 2 steps inside the NVTX range 'profile'")
     ap.add_argument("--settle", type=int, default=250)
+    ap.add_argument("--serve-ticks", type=int, default=0,
+                    help="tick-driven served measurement over this many ticks (see serve_ticks)")
+    ap.add_argument("--serve-per-tick", type=float, default=1.77)
     args = ap.parse_args()
     if args.profile_window:
         profile_window(args)
+        return
+    if args.serve_ticks > 0:
+        serve_ticks(args)
         return
     args.warmup = max(args.warmup, 3)
     rank = int(os.environ.get("RANK", "0"))
