@@ -4,6 +4,8 @@ import ctypes as C
 import re
 from pathlib import Path
 
+import pytest
+
 import b2gpu as G
 
 ROOT = Path(__file__).resolve().parents[1]
@@ -90,3 +92,37 @@ def test_server_cancels_queued_requests_without_a_device():
     assert srv.cancel(a) == 0
     assert srv.stats()["queued"] == 0
     srv.close()
+
+
+def test_builder_threads_build_admitted_worlds_on_the_host():
+    """Admission builds worlds on builder threads (each on a host-only batch) and moves them into
+    the served batch; with no device the tick then fails at the step, after admission."""
+    lib = G.Lib()
+    for builders in (0, 3):
+        srv = G.Server(lib, device=G.HOST_ONLY, budget_bytes=1 << 30, max_worlds=8, builders=builders)
+        ids = [srv.submit(10 + i, 50 + 30 * i, 5) for i in range(4)]
+        with pytest.raises(G.B2GError):
+            srv.tick()
+        st = srv.stats()
+        assert st["queued"] == 0 and st["active"] == 4
+        bh = C.c_void_p()
+        lib.check(lib.b2g_server_batch(srv.h, C.byref(bh)), "server_batch")
+        n = C.c_int32()
+        lib.check(lib.b2g_world_count(bh, C.byref(n)), "world_count")
+        assert n.value == 4
+        assert srv.cancel(ids[1]) == 0
+        assert srv.stats()["active"] == 3
+        srv.close()
+
+
+def test_tuning_knobs_and_split_step_on_a_host_only_batch():
+    lib = G.Lib()
+    b = G.Batch(lib, device=G.HOST_ONLY)
+    assert lib.b2g_batch_set_tree_rebuild_period(b.h, 0) == 1   # INVALID_ARG
+    assert lib.b2g_batch_set_tree_rebuild_period(b.h, 4) == 0
+    assert lib.b2g_batch_set_solver_waves(b.h, -1.0) == 1
+    assert lib.b2g_batch_set_solver_waves(b.h, 0.0) == 0
+    assert b.step_done()             # nothing in flight
+    b.stage()                        # no device: nothing to pack
+    assert lib.b2g_step_end(b.h) == 1  # no step in flight
+    b.close()
