@@ -154,7 +154,7 @@ std::vector<SolveClass> plan_solve_classes(const std::vector<int>& order, const 
     need = (need + 15) & ~15ll;
     int t = class_threads[c];
     int ti = threads_index(t);
-    // few enough worlds that the slowest one sets the class's time: the wide build
+    // the wide build unless the class holds more than wide_waves waves of it
     bool wide = g_num_sms > 0 && (double)(i - start) * t <= (double)wide_waves * 512.0 * g_num_sms;
     int cap = kSmemCapByThreads[wide ? 1 : 0][ti];
     int smem = (int)(need < cap ? need : cap);

@@ -1,7 +1,7 @@
 // solve_wide.cu - the wide build of the per-world solve kernel: 512 threads per SM at up to 128
-// registers a thread, launched for size classes whose worlds all fit on the GPU at once (the
-// step then waits for its slowest world, and the unspilled joint and contact solvers shorten
-// it). A translation unit of its own so that the two builds compile in parallel.
+// registers a thread, so the joint and contact solvers run unspilled and each thread reads its
+// next colour's rows before the barrier; the default for every size class. A translation unit of
+// its own so that the two builds compile in parallel.
 #include "solve_world.cuh"
 
 namespace b2g {

@@ -610,11 +610,11 @@ __device__ void sleep_islands(const KernelArgs& a, int b0, int nb) {
 }
 
 // Resident CTAs per SM the solve kernel is built for. The occupancy build holds 1024 threads per
-// SM at up to 64 registers a thread, for classes with more worlds than the GPU holds at once
-// (throughput-bound); the wide build holds 512 threads per SM at up to 128 registers, for
-// classes that fit on the GPU in one wave, where a world's solve time is the step's critical
-// path and the joint and contact solvers run much faster unspilled. (At 1024 threads per CTA the
-// register file allows 64 registers either way.)
+// SM at up to 64 registers a thread; the wide build holds 512 threads per SM at up to 128
+// registers, where the joint and contact solvers run unspilled and each thread can read its next
+// colour's rows before the barrier. The wide build is faster on every measured workload and is
+// the default for every size class; the occupancy build stays for b2g_batch_set_solver_waves.
+// (At 1024 threads per CTA the register file allows 64 registers either way.)
 template <int T, bool WIDE>
 constexpr int kSolveBlocks = WIDE ? (T >= 512 ? 1 : 512 / T) : 1024 / T;
 
