@@ -517,8 +517,8 @@ __device__ void build_islands(const KernelArgs& a, int b0, int nb, int c0, int n
   for (int k = threadIdx.x; k < ncAll; k += T) {
     const int2 f = a.cfix[c0 + k];
     const int ia = a.fbody[f.x] - b0, ib = a.fbody[f.y] - b0;
-    isl_or(&SL[ia].y, B2G_ISL_LINKED);
-    isl_or(&SL[ib].y, B2G_ISL_LINKED);
+    if (!(isl_bits(SL, ia) & B2G_ISL_LINKED)) isl_or(&SL[ia].y, B2G_ISL_LINKED);
+    if (!(isl_bits(SL, ib) & B2G_ISL_LINKED)) isl_or(&SL[ib].y, B2G_ISL_LINKED);
     const uint32_t fl = a.cflags[c0 + k];
     if ((fl & B2G_CONTACT_TOUCHING) && (fl & B2G_CONTACT_ENABLED) && !a.fsensor[f.x] && !a.fsensor[f.y] &&
         isl_load(&SL[ia].x) >= 0 && isl_load(&SL[ib].x) >= 0)
@@ -532,12 +532,12 @@ __device__ void build_islands(const KernelArgs& a, int b0, int nb, int c0, int n
     if (isl_load(&SL[ia].x) >= 0 && isl_load(&SL[ib].x) >= 0) isl_unite(SL, ia, ib, a.status);
   }
   isl_sync();
-  for (int i = threadIdx.x; i < nb; i += T)
-    if (isl_load(&SL[i].x) >= 0) isl_store(&SL[i].x, isl_find(SL, i, false, a.status));
-  isl_sync();
+  // labels, and the awake mark of every island with an awake member (roots no longer change)
   for (int i = threadIdx.x; i < nb; i += T) {
-    const int r = isl_label(SL, i);
-    if (r >= 0 && (BS[i].x & B2G_BS_AWAKE)) isl_or(&SL[r].y, B2G_ISL_AWAKE);
+    if (isl_load(&SL[i].x) < 0) continue;
+    const int r = isl_find(SL, i, false, a.status);
+    isl_store(&SL[i].x, r);
+    if (BS[i].x & B2G_BS_AWAKE) isl_or(&SL[r].y, B2G_ISL_AWAKE);
   }
   isl_sync();
   for (int i = threadIdx.x; i < nb; i += T) {
