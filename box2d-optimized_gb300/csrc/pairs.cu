@@ -99,14 +99,22 @@ __global__ void kp_init(int n, int* lparent, int* flag) {
   if (i < n - 1) flag[i] = 0;
 }
 
+// Status bits of a pair search (PairsScratch::status): any of them fails the call with
+// B2G_E_CAPACITY instead of returning an incomplete pair set.
+#define P_ST_STACK 1u  // a traversal outgrew its stack or its visit bound
+#define P_ST_DEPTH 2u  // a bottom-up walk passed the depth bound (node bounds left unwritten)
+
 __global__ void kp_node_bounds(const float4* aabb, const int* val, int n, const int2* child, const int* nparent,
-                               const int* lparent, float4* naabb, int* flag) {
+                               const int* lparent, float4* naabb, int* flag, unsigned int* status) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   int p = lparent[i];
   int guard = 0;
   while (p >= 0) {
-    if (++guard > 256) return;  // malformed tree: stop instead of looping
+    if (++guard > 256) {  // malformed tree: stop instead of looping, and fail the call
+      atomicOr(status, P_ST_DEPTH);
+      return;
+    }
     __threadfence();
     if (atomicAdd(&flag[p], 1) == 0) return;
     __threadfence();
@@ -122,18 +130,22 @@ __device__ __forceinline__ bool p_overlap(float4 a, float4 b) {
   return (a.z >= b.x) & (a.x <= b.z) & (a.w >= b.y) & (a.y <= b.w);
 }
 
+// Counting pass (EMIT = false): counts[f] = partners g > f of box f. Emitting pass: `counts` is
+// the 64-bit exclusive scan of the counts, and box f writes its partners to [counts[f],
+// counts[f + 1]) of `pairs` in (f, g) order. A segment outside [0, cap) is never written.
 template <bool EMIT>
 __global__ void kp_traverse(const float4* aabb, const int* val, int n, const int2* child, const float4* naabb,
-                            int* counts, uint64_t* pairs, int64_t cap, unsigned int* status) {
+                            int64_t* counts, uint64_t* pairs, int64_t cap, unsigned int* status) {
   int f = blockIdx.x * blockDim.x + threadIdx.x;
   if (f >= n) return;
-  int cnt = 0;
+  int64_t cnt = 0;
   int64_t off = 0;
   if (EMIT) {
     off = counts[f];
-    if (counts[f + 1] == off) return;
-    if ((int64_t)counts[f + 1] > cap) return;
-  }  // in the emit pass `counts` is the offsets array
+    const int64_t end = counts[f + 1];
+    if (end == off) return;
+    if (off < 0 || end > cap || end < off) return;
+  }
   if (n > 1) {
     float4 box = aabb[f];
     int stack[96];
@@ -142,7 +154,7 @@ __global__ void kp_traverse(const float4* aabb, const int* val, int n, const int
     int visits = 0;
     while (sp > 0) {
       if (++visits > 2 * n + 8) {  // each internal node at most once
-        atomicOr(status, 1u);
+        atomicOr(status, P_ST_STACK);
         break;
       }
       int node = stack[--sp];
@@ -159,7 +171,7 @@ __global__ void kp_traverse(const float4* aabb, const int* val, int n, const int
           }
         } else if (p_overlap(box, naabb[c])) {
           if (sp < 96) stack[sp++] = c;
-          else atomicOr(status, 1u);
+          else atomicOr(status, P_ST_STACK);
         }
       }
     }
@@ -181,7 +193,7 @@ size_t pairs_scratch_bytes(int n) {
   size_t cub_sort = 0, cub_scan = 0;
   cub::DeviceRadixSort::SortPairs((void*)nullptr, cub_sort, (uint32_t*)nullptr, (uint32_t*)nullptr, (int*)nullptr,
                                   (int*)nullptr, n, 0, 30);
-  cub::DeviceScan::ExclusiveSum((void*)nullptr, cub_scan, (int*)nullptr, (int*)nullptr, n + 1);
+  cub::DeviceScan::ExclusiveSum((void*)nullptr, cub_scan, (int64_t*)nullptr, (int64_t*)nullptr, n + 1);
   PairsScratch s = pairs_scratch_layout(nullptr, n, cub_sort > cub_scan ? cub_sort : cub_scan);
   return s.total_bytes;
 }
@@ -204,8 +216,8 @@ PairsScratch pairs_scratch_layout(void* base, int n, size_t cub_bytes) {
   s.lparent = (int*)take(un * 4);
   s.naabb = (float4*)take(un * 16);
   s.flag = (int*)take(un * 4);
-  s.counts = (int*)take((un + 1) * 4);
-  s.offsets = (int*)take((un + 1) * 4);
+  s.counts = (int64_t*)take((un + 1) * 8);
+  s.offsets = (int64_t*)take((un + 1) * 8);
   s.status = (unsigned int*)take(16);
   s.cub = take(cub_bytes);
   s.cub_bytes = cub_bytes;
@@ -233,21 +245,21 @@ int pairs_run(const float4* aabb, int n, uint64_t* pairs, int64_t cap, int64_t* 
   if (n > 1) {
     kp_internal<<<pgrid(n - 1, 256), 256, 0, st>>>(s.key_sorted, n, s.child, s.nparent, s.lparent);
     kp_node_bounds<<<pgrid(n, 256), 256, 0, st>>>(aabb, s.val_sorted, n, s.child, s.nparent, s.lparent, s.naabb,
-                                                  s.flag);
+                                                  s.flag, s.status);
   }
   kp_traverse<false><<<pgrid(n, 128), 128, 0, st>>>(aabb, s.val_sorted, n, s.child, s.naabb, s.counts, pairs, cap,
                                                      s.status);
-  cudaMemsetAsync(s.counts + n, 0, sizeof(int), st);
+  cudaMemsetAsync(s.counts + n, 0, sizeof(int64_t), st);
   bytes = s.cub_bytes;
-  cub::DeviceScan::ExclusiveSum(s.cub, bytes, s.counts, s.offsets, n + 1, st);
-  int total = 0;
+  cub::DeviceScan::ExclusiveSum(s.cub, bytes, s.counts, s.offsets, n + 1, st);  // 64-bit sums
+  int64_t total = 0;
   unsigned int status = 0;
-  cudaMemcpyAsync(&total, s.offsets + n, sizeof(int), cudaMemcpyDeviceToHost, st);
+  cudaMemcpyAsync(&total, s.offsets + n, sizeof(int64_t), cudaMemcpyDeviceToHost, st);
   cudaMemcpyAsync(&status, s.status, sizeof(unsigned int), cudaMemcpyDeviceToHost, st);
   if (cudaStreamSynchronize(st) != cudaSuccess) return B2G_E_CUDA;
   if (n_pairs) *n_pairs = total;
   if (status) return B2G_E_CAPACITY;
-  if ((int64_t)total > cap) return B2G_E_CAPACITY;
+  if (total > cap) return B2G_E_CAPACITY;
   kp_traverse<true><<<pgrid(n, 128), 128, 0, st>>>(aabb, s.val_sorted, n, s.child, s.naabb, s.offsets, pairs, cap,
                                                     s.status);
   if (cudaStreamSynchronize(st) != cudaSuccess) return B2G_E_CUDA;
@@ -272,7 +284,7 @@ extern "C" B2G_API int b2g_pairs(const float* d_aabbs, int32_t n, uint64_t* d_pa
   size_t cub_bytes = 0, cub_scan = 0;
   cub::DeviceRadixSort::SortPairs((void*)nullptr, cub_bytes, (uint32_t*)nullptr, (uint32_t*)nullptr, (int*)nullptr,
                                   (int*)nullptr, n, 0, 30);
-  cub::DeviceScan::ExclusiveSum((void*)nullptr, cub_scan, (int*)nullptr, (int*)nullptr, n + 1);
+  cub::DeviceScan::ExclusiveSum((void*)nullptr, cub_scan, (int64_t*)nullptr, (int64_t*)nullptr, n + 1);
   b2g::PairsScratch s = b2g::pairs_scratch_layout(base, n, cub_bytes > cub_scan ? cub_bytes : cub_scan);
   int st = b2g::pairs_run((const float4*)d_aabbs, n, d_pairs, cap, n_pairs, s, (cudaStream_t)stream);
   cudaStreamSynchronize((cudaStream_t)stream);
@@ -331,7 +343,7 @@ extern "C" B2G_API int b2g_pairs_static(const float* d_aabbs, int32_t n, uint64_
   size_t cub_bytes = 0, cub_scan = 0;
   cub::DeviceRadixSort::SortPairs((void*)nullptr, cub_bytes, (uint32_t*)nullptr, (uint32_t*)nullptr, (int*)nullptr,
                                   (int*)nullptr, n, 0, 30);
-  cub::DeviceScan::ExclusiveSum((void*)nullptr, cub_scan, (int*)nullptr, (int*)nullptr, n + 1);
+  cub::DeviceScan::ExclusiveSum((void*)nullptr, cub_scan, (int64_t*)nullptr, (int64_t*)nullptr, n + 1);
   b2g::PairsScratch s = b2g::pairs_scratch_layout(base, n, cub_bytes > cub_scan ? cub_bytes : cub_scan);
   if (s.total_bytes > B2G_PAIRS_STATIC_SCRATCH_BYTES) return B2G_E_CAPACITY;
   return b2g::pairs_run((const float4*)d_aabbs, n, d_pairs, cap, n_pairs, s, (cudaStream_t)stream);

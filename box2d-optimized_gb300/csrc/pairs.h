@@ -16,9 +16,10 @@ struct PairsScratch {
   int *nparent, *lparent;
   float4* naabb;
   int* flag;
-  int* counts;          // n + 1 entries: pairs per AABB
-  int* offsets;         // n + 1 entries: exclusive scan of counts; offsets[n] = number of pairs
-  unsigned int* status; // non-zero: traversal stack overflow
+  int64_t* counts;      // n + 1 entries: pairs per AABB (up to n - 1 each)
+  int64_t* offsets;     // n + 1 entries: exclusive scan of counts; offsets[n] = number of pairs,
+                        // which passes 2^31 for dense overlap from about 65 536 boxes
+  unsigned int* status; // non-zero: traversal stack overflow or a malformed tree
   void* cub;
   size_t cub_bytes;
   size_t total_bytes;

@@ -63,3 +63,33 @@ def test_static_scratch_rejects_oversize():
     aabb = np.zeros((131073, 4), np.float32)
     st, n, _ = _run(lib.lib.b2g_pairs_static, aabb, 16)
     assert st == 7  # B2G_E_CAPACITY
+
+
+def test_static_scratch_at_the_maximum_size():
+    """Exactly B2G_PAIRS_STATIC_MAX sparse boxes: the fixed array holds the layout and the sort's
+    temporary storage, and the result equals the allocating entry point's."""
+    lib = _lib()
+    rng = np.random.default_rng(7)
+    n = 131072
+    c = rng.uniform(-2000, 2000, (n, 2)).astype(np.float32)
+    h = rng.uniform(0.05, 1.5, (n, 2)).astype(np.float32)
+    aabb = np.concatenate([c - h, c + h], axis=1).astype(np.float32)
+    st0, n0, _ = _run(lib.lib.b2g_pairs, aabb, 1)
+    assert st0 == 7 and n0 > 0
+    st_a, na, pa = _run(lib.lib.b2g_pairs, aabb, n0)
+    st_s, ns, ps = _run(lib.lib.b2g_pairs_static, aabb, n0)
+    assert st_a == 0 and st_s == 0 and na == ns == n0
+    assert np.array_equal(pa[:na], ps[:ns])
+
+
+def test_static_scratch_counts_past_two_to_the_31():
+    """70 000 coincident boxes overlap pairwise: 2 449 965 000 pairs, more than an int32 holds.
+    The total comes back exact in 64 bits and a small capacity is refused without a write."""
+    lib = _lib()
+    n = 70000
+    aabb = np.tile(np.array([[0.0, 0.0, 1.0, 1.0]], np.float32), (n, 1))
+    for fn in (lib.lib.b2g_pairs, lib.lib.b2g_pairs_static):
+        st, total, pairs = _run(fn, aabb, 64)
+        assert st == 7  # B2G_E_CAPACITY
+        assert total == n * (n - 1) // 2
+        assert (pairs.view(np.int64) == -1).all()  # nothing written
