@@ -20,13 +20,15 @@ ROOT = PKG.parent
 CSRC = PKG / "csrc"
 OUT = PKG / "_build"
 LIB = OUT / "libb2g.so"
-REF_SOURCES = Path(os.environ.get("B2G_REF_ROOT", "/root/reference"))
+# The reference checkout the test oracle oracle/_ref is compiled from: B2G_REF_ROOT, else a
+# `reference` directory beside this repository; skipped when neither holds its sources.
+REF_SOURCES = Path(os.environ.get("B2G_REF_ROOT") or (ROOT.parent / "reference"))
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "--fmad=false", "-std=c++17", "-Xcompiler", "-fPIC",
               "-Xcompiler", "-ffp-contract=off",
               f"-I{ROOT / 'include'}", f"-I{PKG / 'include'}"]
-CU_SOURCES = ["solve.cu", "solve_wide.cu", "kernels.cu", "compact.cu", "query.cu", "engine.cu", "pairs.cu"]
+CU_SOURCES = ["solve.cu", "solve_wide.cu", "solve_cluster.cu", "kernels.cu", "compact.cu", "query.cu", "engine.cu", "pairs.cu"]
 CPP_SOURCES = ["shapes.cpp", "facade.cpp", "server.cpp"]
 
 
@@ -60,7 +62,8 @@ def build_engine(force: bool = False) -> Path:
     nvcc = _nvcc()
     OUT.mkdir(parents=True, exist_ok=True)
     headers = list(CSRC.glob("*.h")) + list(CSRC.glob("*.cuh")) + [ROOT / "include" / "b2g_capi.h",
-               PKG / "include" / "box2d" / "box2d.h", PKG / "scenes" / "scenes.h"]
+               PKG / "include" / "box2d" / "box2d.h", PKG / "scenes" / "scenes.h",
+               PKG / "scenes" / "scenes_joints.h"]
     cmds, objs = [], []
     for src in CU_SOURCES + CPP_SOURCES:
         obj = OUT / (src + ".o")
