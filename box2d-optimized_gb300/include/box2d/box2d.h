@@ -528,6 +528,13 @@ struct b2DistanceJointDef : public b2JointDef {
   float length, minLength, maxLength, stiffness, damping;
 };
 
+// Spring stiffness and damping from a frequency and damping ratio over the bodies' mass or
+// inertia (include/box2d/b2_joint.h:97-107).
+void b2LinearStiffness(float& stiffness, float& damping, float frequencyHertz, float dampingRatio,
+                       const b2Body* bodyA, const b2Body* bodyB);
+void b2AngularStiffness(float& stiffness, float& damping, float frequencyHertz, float dampingRatio,
+                        const b2Body* bodyA, const b2Body* bodyB);
+
 // b2WeldJointDef (include/box2d/b2_weld_joint.h:31-65)
 struct b2WeldJointDef : public b2JointDef {
   b2WeldJointDef() {

@@ -2,8 +2,8 @@
 //
 // Written only against the public Box2D C++ API (b2World, b2BodyDef, b2FixtureDef, b2PolygonShape,
 // b2CircleShape, b2EdgeShape, b2RevoluteJointDef), so the same source builds a world for the
-// reference engine and for this library's b2World facade: the two worlds are created by the same
-// sequence of calls with the same arguments.
+// reference engine, for this library's b2World facade and for the CPU oracle's scene builder:
+// the worlds are created by the same sequence of calls with the same arguments.
 //
 // Scene recipes:
 //   Pyramid      - testbed/tests/pyramid.cpp:33-70 layout (rows of 0.5 m half-extent boxes on a
@@ -14,9 +14,7 @@
 //                  hung above a pile of circles in the same U container.
 //   BatchWorld   - one world of a batched workload: picks one of the above by seed, scaled to a
 //                  body count, with gravity and friction jittered by +-10%.
-//   JointZoo     - rigs of the weld, wheel, motor, friction, mouse and pulley joints over a ground
-//                  edge (b2WeldJointDef, b2WheelJointDef, b2MotorJointDef, b2FrictionJointDef,
-//                  b2MouseJointDef, b2PulleyJointDef).
+//   (scenes_joints.h: JointZoo and SliderRigs, rigs of the other joint types.)
 //
 // Random numbers come from std::mt19937 (fully specified by the C++ standard) with a portable
 // 24-bit float conversion, and every draw is its own statement (argument evaluation order is
@@ -281,178 +279,6 @@ inline Counts ChainsOverPile(b2World* world, int nchains, int links, int ncircle
       world->CreateJoint(&jd);
       c.joints++;
       prev = b;
-    }
-  }
-  return c;
-}
-
-// `rigs` rigs side by side over one ground edge, each: a cantilever of three boxes welded to a
-// static post (a rigid weld, then two soft ones); a car whose chassis rides on two sprung wheel
-// joints (rear motorised, front with translation limits) driving along the ground and carrying a
-// sensor disc; a box that a motor joint drives toward an offset from a static anchor; a sliding
-// box held back by a friction joint through a static sensor gate; a box pulled up toward a point
-// by a mouse joint; two boxes hanging from a pulley.
-inline Counts JointZoo(b2World* world, int rigs, uint32_t seed, float friction = 0.6f) {
-  Counts c;
-  Rng rng(seed);
-  if (rigs < 1) rigs = 1;
-  const float pitch = 32.0f;
-  const float half = 0.5f * pitch * (float)rigs + 20.0f;
-  b2BodyDef gd;
-  b2Body* ground = MakeBody(world, &gd);
-  AddEdge(ground, -half, 0.0f, half, 0.0f, &c);
-  b2PolygonShape box;
-  box.SetAsBox(0.5f, 0.25f);
-  b2FixtureDef fd;
-  fd.shape = &box;
-  fd.density = 1.0f;
-  fd.friction = friction;
-  auto dynamicBox = [&](float x, float y, float angle) {
-    b2BodyDef bd;
-    bd.type = b2_dynamicBody;
-    bd.position.Set(x, y);
-    bd.angle = angle;
-    b2Body* b = MakeBody(world, &bd);
-    MakeFixture(b, &fd);
-    c.bodies++;
-    c.fixtures++;
-    return b;
-  };
-  auto staticPost = [&](float x, float y) {
-    b2BodyDef bd;
-    bd.position.Set(x, y);
-    b2Body* b = MakeBody(world, &bd);
-    b2PolygonShape ps;
-    ps.SetAsBox(0.2f, 0.2f);
-    MakeFixture(b, &ps, 0.0f);
-    c.fixtures++;
-    return b;
-  };
-  for (int r = 0; r < rigs; ++r) {
-    const float x0 = -0.5f * pitch * (float)rigs + pitch * (float)r + 2.0f;
-    const float jit = rng.uni(-0.1f, 0.1f);
-    // welded cantilever
-    {
-      b2Body* post = staticPost(x0, 6.0f);
-      b2Body* prev = post;
-      for (int k = 0; k < 3; ++k) {
-        float x = x0 + 0.7f + 1.0f * (float)k;
-        b2Body* b = dynamicBox(x, 6.0f + jit * (float)k, 0.0f);
-        b2WeldJointDef jd;
-        jd.Initialize(prev, b, b2Vec2(x - 0.5f, 6.0f));
-        if (k > 0) {
-          jd.stiffness = 40.0f + 20.0f * (float)k;
-          jd.damping = 2.0f;
-        }
-        world->CreateJoint(&jd);
-        c.joints++;
-        prev = b;
-      }
-    }
-    // car on two wheel joints
-    {
-      float cx = x0 + 6.0f;
-      b2Body* chassis = dynamicBox(cx, 1.4f, 0.0f);
-      b2CircleShape disc;  // a sensor reaching below the chassis: touches the ground edge
-      disc.m_radius = 1.3f;
-      b2FixtureDef sfd;
-      sfd.shape = &disc;
-      sfd.isSensor = true;
-      sfd.density = 0.0f;
-      MakeFixture(chassis, &sfd);
-      c.fixtures++;
-      b2CircleShape wheel;
-      wheel.m_radius = 0.35f;
-      b2FixtureDef wfd;
-      wfd.shape = &wheel;
-      wfd.density = 1.0f;
-      wfd.friction = 0.9f;
-      for (int k = 0; k < 2; ++k) {
-        b2BodyDef bd;
-        bd.type = b2_dynamicBody;
-        float wx = cx + (k == 0 ? -0.45f : 0.45f);
-        bd.position.Set(wx, 0.7f);
-        b2Body* w = MakeBody(world, &bd);
-        MakeFixture(w, &wfd);
-        c.bodies++;
-        c.fixtures++;
-        b2WheelJointDef jd;
-        jd.Initialize(chassis, w, w->GetPosition(), b2Vec2(0.0f, 1.0f));
-        jd.stiffness = 30.0f;
-        jd.damping = 1.5f;
-        if (k == 0) {
-          jd.enableMotor = true;
-          jd.maxMotorTorque = 8.0f;
-          jd.motorSpeed = -4.0f - 2.0f * jit;
-        } else {
-          jd.enableLimit = true;
-          jd.lowerTranslation = -0.25f;
-          jd.upperTranslation = 0.1f;
-        }
-        world->CreateJoint(&jd);
-        c.joints++;
-      }
-    }
-    // motor joint driving a box toward an offset from a static anchor
-    {
-      b2Body* anchor = staticPost(x0 + 12.0f, 3.0f);
-      b2Body* b = dynamicBox(x0 + 12.0f, 1.0f, 0.3f);
-      b2MotorJointDef jd;
-      jd.Initialize(anchor, b);
-      jd.linearOffset.Set(1.5f + jit, 2.0f);
-      jd.angularOffset = 0.5f;
-      jd.maxForce = 60.0f;
-      jd.maxTorque = 20.0f;
-      world->CreateJoint(&jd);
-      c.joints++;
-    }
-    // friction joint holding back a box thrown along the ground through a sensor gate
-    {
-      b2Body* gate = staticPost(x0 + 17.5f, 2.0f);
-      b2PolygonShape gs;
-      gs.SetAsBox(0.4f, 2.0f);
-      b2FixtureDef gfd;
-      gfd.shape = &gs;
-      gfd.isSensor = true;
-      MakeFixture(gate, &gfd);
-      c.fixtures++;
-      b2Body* b = dynamicBox(x0 + 16.0f, 0.25f, 0.0f);
-      b->SetLinearVelocity(b2Vec2(6.0f + jit, 0.0f));
-      b->SetAngularVelocity(3.0f);
-      b2FrictionJointDef jd;
-      jd.Initialize(ground, b, b->GetPosition());
-      jd.maxForce = 4.0f;
-      jd.maxTorque = 2.0f;
-      world->CreateJoint(&jd);
-      c.joints++;
-    }
-    // mouse joint pulling a box toward a point
-    {
-      b2Body* b = dynamicBox(x0 + 20.0f, 0.25f, 0.0f);
-      b2MouseJointDef jd;
-      jd.bodyA = ground;
-      jd.bodyB = b;
-      jd.target.Set(x0 + 21.0f, 4.0f + jit);
-      jd.maxForce = 30.0f;
-      jd.stiffness = 15.0f;
-      jd.damping = 0.7f;
-      world->CreateJoint(&jd);
-      c.joints++;
-    }
-    // pulley with two boxes of different mass
-    {
-      float px = x0 + 25.0f;
-      b2Body* a = dynamicBox(px - 1.5f, 4.0f, 0.0f);
-      b2Body* b = dynamicBox(px + 1.5f, 5.0f, 0.0f);
-      b2PolygonShape heavy;
-      heavy.SetAsBox(0.3f, 0.3f);
-      MakeFixture(b, &heavy, 2.0f);
-      c.fixtures++;
-      b2PulleyJointDef jd;
-      jd.Initialize(a, b, b2Vec2(px - 1.5f, 9.0f), b2Vec2(px + 1.5f, 9.0f), b2Vec2(px - 1.5f, 4.25f),
-                    b2Vec2(px + 1.5f, 5.25f), 1.5f);
-      world->CreateJoint(&jd);
-      c.joints++;
     }
   }
   return c;

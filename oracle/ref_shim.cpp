@@ -29,7 +29,7 @@
 #undef protected
 
 #include "../include/b2g_capi.h"
-#include "scenes/scenes.h"
+#include "scenes/scenes_joints.h"
 
 extern "C" {
 
@@ -265,6 +265,7 @@ void* ref_scene_world(int32_t kind, uint32_t seed, int32_t n, float p0, float p1
   else if (kind == B2G_SCENE_CHAINS) c = b2scenes::ChainsOverPile(rw->world, n, 20, (int)p0, seed);
   else if (kind == B2G_SCENE_BATCH_WORLD) c = b2scenes::BatchWorld(rw->world, seed, n);
   else if (kind == B2G_SCENE_JOINTS) c = b2scenes::JointZoo(rw->world, n, seed);
+  else if (kind == B2G_SCENE_SLIDERS) c = b2scenes::SliderRigs(rw->world, n, seed);
   if (counts) { counts[0] = c.bodies; counts[1] = c.fixtures; counts[2] = c.joints; }
   index_world(rw);
   return rw;

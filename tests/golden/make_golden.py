@@ -135,6 +135,7 @@ def main():
     replay(ref, orc, "pyramid", G.SCENE_PYRAMID, 20, 1, 1.0, 40, 8, 3)
     replay(ref, orc, "mixed", G.SCENE_MIXED_DROP, 300, 3, 0.0, 150, 8, 3)
     replay(ref, orc, "chains", G.SCENE_CHAINS, 10, 2, 150.0, 100, 10, 4)
+    replay(ref, orc, "sliders", G.SCENE_SLIDERS, 3, 9, 0.0, 60, 8, 3)
     rollout(ref, "pyramid", G.SCENE_PYRAMID, 20, 1, 1.0, 256, 8, 3)
     print("golden vectors written to", HERE)
 

@@ -66,7 +66,7 @@ def test_oracle_collide_vs_golden(orc):
     assert touching > 300
 
 
-@pytest.mark.parametrize("name", ["pyramid", "mixed", "chains"])
+@pytest.mark.parametrize("name", ["pyramid", "mixed", "chains", "sliders"])
 def test_oracle_replayed_step_vs_golden(orc, name):
     """One step from an exported reference state; the reference's b2Island solved the constraints
     in the order the oracle chooses, so the two steps differ only by libm rounding."""
@@ -136,6 +136,9 @@ def test_oracle_vs_reference_live(ref, orc):
     (G.SCENE_JOINTS, 3, 9, 0.0, 1, 8, 3),
     (G.SCENE_JOINTS, 3, 9, 0.0, 40, 8, 3),
     (G.SCENE_JOINTS, 2, 17, 0.0, 150, 10, 4),
+    (G.SCENE_SLIDERS, 3, 9, 0.0, 1, 8, 3),
+    (G.SCENE_SLIDERS, 3, 9, 0.0, 40, 8, 3),
+    (G.SCENE_SLIDERS, 2, 17, 0.0, 150, 10, 4),
 ])
 def test_oracle_replay_vs_reference_live(ref, orc, kind, n, seed, p0, warm, vi, pi):
     """The reference's b2Island::Solve replaying the oracle's order: bit-exact, 3 steps."""
@@ -171,7 +174,7 @@ def test_oracle_replay_vs_reference_live(ref, orc, kind, n, seed, p0, warm, vi, 
 
 @pytest.mark.parametrize("kind,n,seed,p0", [
     (G.SCENE_PYRAMID, 20, 1, 1.0), (G.SCENE_MIXED_DROP, 500, 3, 0.0), (G.SCENE_CHAINS, 30, 2, 300.0),
-    (G.SCENE_BATCH_WORLD, 777, 5, 0.0), (G.SCENE_JOINTS, 3, 9, 0.0)])
+    (G.SCENE_BATCH_WORLD, 777, 5, 0.0), (G.SCENE_JOINTS, 3, 9, 0.0), (G.SCENE_SLIDERS, 3, 9, 0.0)])
 def test_host_scene_setup_vs_reference_live(ref, kind, n, seed, p0):
     """The engine's host-side set-up (facade -> shapes -> mass data -> joint defs) produces the
     reference's body, fixture and joint state byte for byte."""
@@ -312,3 +315,28 @@ def test_oracle_overlap_vs_reference_live(ref, orc):
         assert (r, dr.value) == (o, do.value), (k, ka, kb)
         overlaps += r
     assert 300 < overlaps < 2700
+
+
+@pytest.mark.parametrize("kind,n,seed,p0", [
+    (G.SCENE_PYRAMID, 20, 1, 1.0), (G.SCENE_MIXED_DROP, 700, 3, 0.0), (G.SCENE_CHAINS, 30, 2, 300.0),
+    (G.SCENE_BATCH_WORLD, 0, 0, 0.0), (G.SCENE_BATCH_WORLD, 0, 1, 0.0), (G.SCENE_BATCH_WORLD, 0, 2, 0.0),
+    (G.SCENE_BATCH_WORLD, 0, 40, 0.0), (G.SCENE_BATCH_WORLD, 0, 77, 0.0)])
+def test_oracle_scene_builder_matches_engine_setup(orc, kind, n, seed, p0):
+    """The oracle's own scene builder (used by the CPU baseline and the reference arm, so that
+    neither loads the engine library) makes the engine facade's records byte for byte: bodies
+    with mass data, fixtures with hulls, revolute joints with anchors. Batch worlds take the
+    workload's body count and gravity for their seed, as the benchmark does."""
+    if kind == G.SCENE_BATCH_WORLD:
+        n, gx, gy = orc.batch_world_params(seed)
+        lib = G.Lib()
+        m, hx, hy = C.c_int32(), C.c_float(), C.c_float()
+        lib.b2g_batch_world_params(seed, C.byref(m), C.byref(hx), C.byref(hy))
+        assert (m.value, hx.value, hy.value) == (n, gx, gy)
+    hb = _host_batch()
+    w = hb.add_world(0.0, -10.0)
+    hb.scene(w, kind, seed=seed, n=n, p0=p0, p1=0.6)
+    B, F, J = orc.scene_records(kind, seed=seed, n=n, p0=p0, p1=0.6)
+    assert b"".join(bytes(b) for b in hb.bodies(w)) == b"".join(bytes(b) for b in B)
+    assert b"".join(bytes(f) for f in hb.fixtures(w)) == b"".join(bytes(f) for f in F)
+    assert b"".join(bytes(j) for j in hb.joints(w)) == b"".join(bytes(j) for j in J)
+    hb.close()
