@@ -262,22 +262,70 @@ def sleep_bench(lib, dev, seeds, settle, steps, cpu):
 
         threads = os.cpu_count() or 1
         orc = ob.Oracle()
-        host = G.Batch(lib, device=G.HOST_ONLY)
-        worlds = []
-        for s in seeds:
-            n, gx, gy = world_params(lib, s)
-            w = host.add_world(gx, gy)
-            host.scene(w, G.SCENE_BATCH_WORLD, seed=s, n=n)
-            ow = ob.OracleWorld(orc, (gx, gy), host.bodies(w), host.fixtures(w), host.joints(w))
-            ow.set_sleep(True)
-            worlds.append(ow)
+        worlds, _ = oracle_batch(orc, seeds, sleep=True)
         hs = (C.c_void_p * len(worlds))(*[w.h for w in worlds])
         orc.orc_worlds_step_parallel(hs, len(worlds), DT, VI, PI, settle, threads)
         secs = orc.orc_worlds_step_parallel(hs, len(worlds), DT, VI, PI, steps, threads)
-        host.close()
         res["cpu_baseline"] = {"value": nb * steps / secs, "unit": "body-steps/s", "cores": threads, "kind": "port",
                                "sample": "the same worlds and window, sleeping allowed"}
     return res
+
+
+# The single-world configurations: (name, scene kind, seed, n, p0, velocity / position
+# iterations, steps, workload).
+LARGE_CONFIGS = [
+    ("pyramid_210", G.SCENE_PYRAMID, 1, 20, 1.0, 8, 3, 256,
+     "20-row box pyramid (210 boxes, density 1, friction 0.6) on a 40 m edge, 8/3 iterations, 256 steps"),
+    ("mixed_20000", G.SCENE_MIXED_DROP, 1, 20000, 0.0, 8, 3, 512,
+     "single large world: 20 000 boxes / circles / 3-8-gons dropped from a 200 x 400 m grid into a U, 8/3, 512 steps"),
+    ("chains_2000x20_pile_10000", G.SCENE_CHAINS, 1, 2000, 10000.0, 10, 4, 256,
+     "2 000 chains of 20 boxes on revolute joints (limits, motors) over 10 000 circles, 10/4 iterations, 256 steps"),
+]
+
+
+def large_worlds(lib, dev, cpu, cpu_steps=16):
+    """Each single-world configuration stepped alone for its full step count (CUDA graphs, device
+    time by CUDA events): ms per step over the whole rollout and over its last `cpu_steps`
+    steps, with worlds above 8192 bodies solved by a thread-block cluster (the default) and, for
+    comparison, by one CTA. With `cpu`, the CPU oracle (restatement of the reference's Step, one
+    host thread, like the reference) is loaded with the GPU's state before the last `cpu_steps`
+    steps and times those same steps: a bounded sample of the settled workload."""
+    out = {}
+    for name, kind, seed, n, p0, vi, pi, steps, desc in LARGE_CONFIGS:
+        res = {"workload": desc}
+        for ctas in ((-1, 1) if n > 8192 else (-1,)):
+            b = G.Batch(lib, device=dev)
+            b.cluster_solve(ctas)
+            w = b.add_world(0.0, -10.0)
+            b.set_flags(w, allow_sleep=False, warm_starting=True, continuous=False)
+            counts = b.scene(w, kind, seed=seed, n=n, p0=p0, p1=0.6)
+            head = b.step_timed(steps - cpu_steps, DT, vi, pi)
+            if ctas == -1 and cpu:
+                import oracle_bind as ob  # noqa: PLC0415 - CPU baseline leg only
+
+                ow = ob.OracleWorld(ob.Oracle(), (0.0, -10.0), b.bodies(w), b.fixtures(w), b.joints(w),
+                                    b.contacts(w), inv_dt0=1.0 / DT)
+                secs = ow.step(cpu_steps, DT, vi, pi)
+                res["cpu_baseline"] = {"value": counts[0] * cpu_steps / secs, "unit": "body-steps/s", "cores": 1,
+                                       "kind": "port", "ms_per_step": secs * 1e3 / cpu_steps,
+                                       "sample": f"steps {steps - cpu_steps + 1}-{steps} from the GPU's state, one thread"}
+                ow.close()
+            tail = b.step_timed(cpu_steps, DT, vi, pi)
+            b.set_graphs(False)
+            b.step(DT, vi, pi)
+            p = b.profile()
+            key = "cluster" if ctas == -1 else "one_cta"
+            res[key] = {"ms_per_step": (head + tail) / steps, "ms_per_step_last": tail / cpu_steps,
+                        "body_steps_per_s": counts[0] * steps / ((head + tail) / 1e3),
+                        "eager_step_after_ms": {"collide": p.collide, "solve": p.solve, "broadphase": p.broadphase,
+                                                "step": p.step},
+                        "touching_at_end": p.touching, "joints": p.joints, "colors_max": p.colors_max}
+            if ctas == -1:
+                res["bodies"] = counts[0]
+                res["cluster"]["ctas_per_world"] = b.cluster_ctas() if n > 8192 else 1
+            b.close()
+        out[name] = res
+    return out
 
 
 def solve_traffic(sb):
@@ -304,65 +352,61 @@ def solve_bytes(nb, nc, nj, vi=VI, pi=PI):
     return 64 * nb + nc * (208 + 16 + 192 * vi + 144 * pi) + nj * (160 + 128 * vi + 96 * pi)
 
 
-def cpu_sample(lib, seeds, warmup, steps, threads):
+def oracle_batch(orc, seeds, sleep=False):
+    """The batched workload's worlds `seeds`, built by the CPU oracle's own scene builder (no
+    engine library involved); returns (worlds, bodies)."""
+    import oracle_bind as ob  # noqa: PLC0415 - CPU baseline and reference arm only
+
+    worlds, nb = [], 0
+    for s in seeds:
+        n, gx, gy = orc.batch_world_params(s)
+        ow = ob.OracleWorld(orc, (gx, gy), scene=(G.SCENE_BATCH_WORLD, s, n, 0.0, 0.0))
+        if sleep:
+            ow.set_sleep(True)
+        nb += ow.counts[0]  # dynamic bodies, as the GPU arm counts them
+        worlds.append(ow)
+    return worlds, nb
+
+
+def cpu_sample(seeds, warmup, steps, threads):
     """Steps the CPU oracle (restatement of the reference Step) over a sample of worlds."""
     import oracle_bind as ob  # noqa: PLC0415 - CPU baseline leg only
 
     orc = ob.Oracle()
-    host = G.Batch.__new__(G.Batch)
-    host.lib = lib
-    h = C.c_void_p()
-    lib.check(lib.b2g_batch_create(-1, 0, C.byref(h)), "host batch")
-    host.h = h
-    worlds = []
-    nb = 0
-    for s in seeds:
-        n, gx, gy = world_params(lib, s)
-        w = host.add_world(gx, gy)
-        host.scene(w, G.SCENE_BATCH_WORLD, seed=s, n=n)
-        bodies = host.bodies(w)
-        nb += len(bodies)
-        worlds.append(ob.OracleWorld(orc, (gx, gy), bodies, host.fixtures(w), host.joints(w)))
+    worlds, nb = oracle_batch(orc, seeds)
     hs = (C.c_void_p * len(worlds))(*[w.h for w in worlds])
     orc.orc_worlds_step_parallel(hs, len(worlds), DT, VI, PI, warmup, threads)  # untimed, like the GPU warm-up
     secs = orc.orc_worlds_step_parallel(hs, len(worlds), DT, VI, PI, steps, threads)
-    host.close()
     return nb * steps / secs, nb, secs
 
 
 def run_reference(args, rank):
-    lib = G.Lib()
+    """The reference arm: the reference's Step algorithm (the CPU oracle's restatement, pinned
+    to the reference's own code) on all host threads, over the same worlds, warm-up and timed
+    steps as the GPU arm. Worlds are built by the oracle's scene builder, so this arm loads no
+    engine library."""
     if rank != 0:
         return
     threads = os.cpu_count() or 1
-    seeds = list(range(0, args.worlds, max(1, args.worlds // args.ref_worlds)))[: args.ref_worlds]
     import oracle_bind as ob  # noqa: PLC0415 - the reference arm runs the oracle port
 
     orc = ob.Oracle()
-    host = G.Batch.__new__(G.Batch)
-    host.lib = lib
-    h = C.c_void_p()
-    lib.check(lib.b2g_batch_create(-1, 0, C.byref(h)), "host batch")
-    host.h = h
-    worlds, nb = [], 0
-    for s in seeds:
-        n, gx, gy = world_params(lib, s)
-        w = host.add_world(gx, gy)
-        host.scene(w, G.SCENE_BATCH_WORLD, seed=s, n=n)
-        bodies = host.bodies(w)
-        nb += len(bodies)
-        worlds.append(ob.OracleWorld(orc, (gx, gy), bodies, host.fixtures(w), host.joints(w)))
+    t0 = time.time()
+    worlds, nb = oracle_batch(orc, list(range(args.worlds)))
+    build_s = time.time() - t0
     hs = (C.c_void_p * len(worlds))(*[w.h for w in worlds])
     orc.orc_worlds_step_parallel(hs, len(worlds), DT, VI, PI, args.warmup, threads)
     secs = orc.orc_worlds_step_parallel(hs, len(worlds), DT, VI, PI, args.steps, threads)
     value = nb * args.steps / secs
-    sample = f"{len(worlds)} of the {args.worlds} worlds (every {args.worlds // len(worlds)}th seed), {nb} bodies"
+    sample = (f"all {args.worlds} worlds ({nb} bodies), steps {args.warmup + 1}-{args.warmup + args.steps} after "
+              f"{args.warmup} untimed, {threads} threads; built in {build_s:.1f} s by the oracle's scene builder")
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "body-steps/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": secs * 1e3 / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": f"batched {args.worlds} worlds, 16-8192 bodies log-uniform, 8/3 iterations, dt 1/60",
-                   "worlds": args.worlds, "l2": "state larger than L2"},
+        "config": {"workload": f"batched {args.worlds} worlds per GPU, 16-8192 bodies log-uniform (pyramid / "
+                               f"mixed drop / chains), 8/3 iterations, dt 1/60",
+                   "worlds": args.worlds, "bodies": nb, "l2": "state larger than L2 (no flush needed)"},
         "cpu_baseline": {"value": value, "unit": "body-steps/s", "cores": threads, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": "body-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -433,6 +477,21 @@ def run_ours(args, rank, world_size):
     eb.close()
     e2e_value = nb * e2e_steps / e2e_s * world_size
 
+    # the same batch after it has settled: ms/step and body-steps/s over `settled_steps` steps
+    # starting at step settle_at + 1 (graph replay, CUDA events), with the touching contacts
+    # solved per step there (piles have formed; the driver's short window is mostly free fall)
+    settled = None
+    if args.settled_at > 0:
+        batch.step_timed(max(0, args.settled_at - args.warmup - args.steps), DT, VI, PI)
+        t0c = batch.profile().touching_total
+        sms = batch.step_timed(args.settled_steps, DT, VI, PI)
+        tch = (batch.profile().touching_total - t0c) / args.settled_steps
+        sms_max, _ = reduce_over_ranks(sms / args.settled_steps, nb, f"cuda:{dev}")
+        first = max(args.settled_at, args.warmup + args.steps) + 1
+        settled = {"value": nb_all / (sms_max / 1e3), "unit": "body-steps/s", "ms_per_step": sms_max,
+                   "steps": f"{first}-{first + args.settled_steps - 1}", "touching_per_step_per_gpu": tch,
+                   "contact_constraint_iterations_per_s": tch * (VI + PI) * world_size / (sms_max / 1e3)}
+
     # world queries on the settled batch: closest-hit ray casts and AABB queries, end to end
     # through the C ABI (host buffers in and out), seeded rays over each world's extent
     queries = None
@@ -488,13 +547,18 @@ def run_ours(args, rank, world_size):
                   "workload": "Poisson rollout requests, 32-4096 bodies log-uniform, K ~ U[16,512] steps, "
                               "120 GB HBM budget; rate = 0.7 x closed-loop saturation throughput"}
 
+    # the single-world configurations (20-row pyramid, 20 000-body drop, 2 000 chains over a pile)
+    large = None
+    if rank == 0 and not args.no_large:
+        large = large_worlds(lib, dev, world_size == 1 and not args.no_cpu)
+
     line = None
     if rank == 0:
         cpu = None
         if world_size == 1 and not args.no_cpu:
             threads = os.cpu_count() or 1
             cpu_seeds = seeds[:: max(1, len(seeds) // args.cpu_worlds)][: args.cpu_worlds]
-            v, cnb, secs = cpu_sample(lib, cpu_seeds, args.warmup, args.steps, threads)
+            v, cnb, secs = cpu_sample(cpu_seeds, args.warmup, args.steps, threads)
             cpu = {"value": v, "unit": "body-steps/s", "cores": threads, "kind": "port",
                    "sample": f"{len(cpu_seeds)} of the worlds ({cnb} bodies), steps {args.warmup + 1}-"
                              f"{args.warmup + args.steps} of the same rollout, {secs:.1f} s on {threads} threads"}
@@ -532,6 +596,8 @@ def run_ours(args, rank, world_size):
                     "d2h_bytes_per_step": 16 * nbody, "steps": e2e_steps},
             "gpu_launches": kernels_per_step * args.steps + 3 * full_builds,
             "contact_constraint_iterations_per_s": contact_iters,
+            "settled": settled,
+            "large_worlds": large,
             "queries": queries,
             "sleep": sleep,
             "clocks": clocks.summary(),
@@ -611,6 +677,9 @@ def main():
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--serve-seconds", type=float, default=12.0)
     ap.add_argument("--no-autotune", action="store_true", help="keep the default solver threads per world")
+    ap.add_argument("--settled-at", type=int, default=260, help="step after which the settled window starts (0: skip)")
+    ap.add_argument("--settled-steps", type=int, default=16)
+    ap.add_argument("--no-large", action="store_true", help="skip the single-world configurations")
     ap.add_argument("--rays", type=int, default=1 << 20, help="rays of the world-query measurement (0: skip)")
     ap.add_argument("--sleep-worlds", type=int, default=256, help="worlds of the island-sleep measurement (0: skip)")
     ap.add_argument("--sleep-settle", type=int, default=480, help="steps before the island-sleep window")

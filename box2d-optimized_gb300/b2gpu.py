@@ -23,7 +23,7 @@ STATIC, KINEMATIC, DYNAMIC = 0, 1, 2
 SHAPE_CIRCLE, SHAPE_EDGE, SHAPE_POLYGON = 0, 1, 2
 JOINT_REVOLUTE, JOINT_PRISMATIC, JOINT_DISTANCE = 1, 2, 3
 POLY_HULL, POLY_BOX, POLY_BOX_ORIENTED, POLY_RAW = 0, 1, 2, 3
-SCENE_PYRAMID, SCENE_MIXED_DROP, SCENE_CHAINS, SCENE_BATCH_WORLD, SCENE_JOINTS = 0, 1, 2, 3, 4
+SCENE_PYRAMID, SCENE_MIXED_DROP, SCENE_CHAINS, SCENE_BATCH_WORLD, SCENE_JOINTS, SCENE_SLIDERS = 0, 1, 2, 3, 4, 5
 JOINT_REVOLUTE, JOINT_PRISMATIC, JOINT_DISTANCE, JOINT_PULLEY, JOINT_MOUSE = 1, 2, 3, 4, 5
 JOINT_WHEEL, JOINT_WELD, JOINT_FRICTION, JOINT_MOTOR = 7, 8, 9, 11
 BODY_ENABLED, BODY_FIXED_ROTATION, BODY_BULLET, BODY_AWAKE, BODY_AUTO_SLEEP = 1, 2, 4, 8, 16
@@ -241,6 +241,7 @@ class Lib:
         "b2g_world_snapshot", "b2g_world_restore", "b2g_server_cancel", "b2g_body_set_awake",
         "b2g_bodies_sleep_time_read", "b2g_world_get_flags", "b2g_server_batch", "b2g_step_begin",
         "b2g_step_poll", "b2g_step_end", "b2g_batch_stage", "b2g_server_set_builders", "b2g_batch_set_solver_waves", "b2g_batch_set_tree_rebuild_period",
+        "b2g_batch_set_cluster_solve", "b2g_batch_get_cluster_solve",
     ]
 
     def __init__(self, path: os.PathLike | str | None = None):
@@ -295,6 +296,8 @@ class Lib:
             "b2g_batch_stage": ([vp], C.c_int),
             "b2g_server_set_builders": ([vp, i32], C.c_int),
             "b2g_batch_set_solver_waves": ([vp, f32], C.c_int),
+            "b2g_batch_set_cluster_solve": ([vp, i32], C.c_int),
+            "b2g_batch_get_cluster_solve": ([vp, P(i32)], C.c_int),
             "b2g_batch_set_tree_rebuild_period": ([vp, i32], C.c_int),
             "b2g_batch_set_debug_checks": ([vp, i32], C.c_int),
             "b2g_body_set_awake": ([vp, i32, i32, i32], C.c_int),
@@ -462,6 +465,17 @@ class Batch:
     def set_graphs(self, enable=True):
         """Whether unmasked steps replay a captured CUDA graph (default on)."""
         self.lib.check(self.lib.b2g_batch_set_graphs(self.h, int(enable)), "b2g_batch_set_graphs")
+
+    def cluster_solve(self, ctas=-1):
+        """CTAs per world of the thread-block cluster that solves worlds above 8192 bodies (-1:
+        the device's largest; 0 or 1: one CTA per world). Results do not depend on it."""
+        self.lib.check(self.lib.b2g_batch_set_cluster_solve(self.h, int(ctas)), "b2g_batch_set_cluster_solve")
+
+    def cluster_ctas(self) -> int:
+        """CTAs per world the worlds above 8192 bodies are solved with (1: one CTA)."""
+        v = C.c_int32()
+        self.lib.check(self.lib.b2g_batch_get_cluster_solve(self.h, C.byref(v)), "b2g_batch_get_cluster_solve")
+        return v.value
 
     def set_debug_checks(self, enable=True):
         """Verify every step's constraint colouring on the device (a violation fails the step)."""

@@ -220,7 +220,8 @@ static uint64_t emitter_key(const HostWorld& w, int fo, int fa, int fb) {
 static void replan_solver(Batch* b) {
   std::vector<int> nbw(b->worlds.size());
   for (size_t w = 0; w < b->worlds.size(); ++w) nbw[w] = (int)b->worlds[w].bodies.size();
-  b->solve_classes = plan_solve_classes(b->h_world_order, nbw, b->class_threads, b->wide_waves);
+  int cl = b->cluster_ctas < 0 ? solver_max_cluster_ctas() : std::min(b->cluster_ctas, solver_max_cluster_ctas());
+  b->solve_classes = plan_solve_classes(b->h_world_order, nbw, b->class_threads, b->wide_waves, cl);
 }
 
 // Solver constraints address bodies by a 24-bit world-local index.
@@ -1976,6 +1977,25 @@ B2G_API int b2g_batch_set_solver_waves(b2g_batch* b, float waves) {
     replan_solver(b);
     b->layout_version++;  // captured graphs hold the old launch shapes
   }
+  return B2G_OK;
+}
+
+B2G_API int b2g_batch_set_cluster_solve(b2g_batch* b, int32_t ctas) {
+  if (!b || !(ctas == -1 || ctas == 0 || ctas == 1 || ctas == 2 || ctas == 4 || ctas == 8 || ctas == 16))
+    return B2G_E_INVALID_ARG;
+  b->cluster_ctas = ctas;
+  if (!b->h_world_order.empty()) {
+    replan_solver(b);
+    b->layout_version++;  // captured graphs hold the old launch shapes
+  }
+  return B2G_OK;
+}
+
+B2G_API int b2g_batch_get_cluster_solve(b2g_batch* b, int32_t* ctas) {
+  if (!b || !ctas) return B2G_E_INVALID_ARG;
+  const int dmax = solver_max_cluster_ctas();
+  const int c = b->cluster_ctas < 0 ? dmax : std::min(b->cluster_ctas, dmax);
+  *ctas = c > 1 ? c : 1;
   return B2G_OK;
 }
 

@@ -123,6 +123,7 @@ struct SolveClass {
   int first, count, threads, smem;
   int cls;    // size class index
   bool wide;  // the 128-register build (few worlds: latency-bound) rather than the 64-register one
+  int ctas;   // CTAs per world: 1, or the thread-block cluster size of the largest class
 };
 #define B2G_SOLVE_CLASSES 5
 #define B2G_JV_ROWS 13  // float4 rows of one joint's solver record (solver_dev.cuh)
@@ -289,6 +290,7 @@ struct Batch {
   std::vector<SolveClass> solve_classes;
   std::vector<int> h_world_order;  // worlds by body count, largest first (device world_order)
   int class_threads[B2G_SOLVE_CLASSES] = {64, 128, 256, 512, 1024};
+  int cluster_ctas = -1;     // CTAs per world of the largest size class (-1: the device's largest cluster)
   float wide_waves = 1e9f;  // size classes of at most this many waves run the wide solver build (all, by default)
   cudaStream_t side[B2G_SOLVE_CLASSES] = {};
   cudaEvent_t fork_ev[B2G_SOLVE_CLASSES + 1] = {};

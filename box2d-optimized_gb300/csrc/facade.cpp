@@ -8,7 +8,7 @@
 #include <stdexcept>
 
 #include "../include/box2d/box2d.h"
-#include "../scenes/scenes.h"
+#include "../scenes/scenes_joints.h"
 #include "engine.h"
 
 const b2Vec2 b2Vec2_zero(0.0f, 0.0f);
@@ -409,6 +409,27 @@ void b2PulleyJointDef::Initialize(b2Body* bA, b2Body* bB, const b2Vec2& groundA,
   lengthB = dB.Length();
   ratio = r;
 }
+// Effective mass (or inertia) of the pair: the reduced value when both are positive, else the
+// positive one; stiffness = m w^2 and damping = 2 m zeta w with w = 2 pi f, in the reference's
+// operation order (src/dynamics/b2_joint.cpp:40-88).
+static float pairValue(float a, float b) {
+  if (a > 0.0f && b > 0.0f) return a * b / (a + b);
+  return a > 0.0f ? a : b;
+}
+void b2LinearStiffness(float& stiffness, float& damping, float frequencyHertz, float dampingRatio,
+                       const b2Body* bodyA, const b2Body* bodyB) {
+  float mass = pairValue(bodyA->GetMass(), bodyB->GetMass());
+  float omega = 2.0f * b2_pi * frequencyHertz;
+  stiffness = mass * omega * omega;
+  damping = 2.0f * mass * dampingRatio * omega;
+}
+void b2AngularStiffness(float& stiffness, float& damping, float frequencyHertz, float dampingRatio,
+                        const b2Body* bodyA, const b2Body* bodyB) {
+  float inertia = pairValue(bodyA->GetInertia(), bodyB->GetInertia());
+  float omega = 2.0f * b2_pi * frequencyHertz;
+  stiffness = inertia * omega * omega;
+  damping = 2.0f * inertia * dampingRatio * omega;
+}
 void b2DistanceJointDef::Initialize(b2Body* b1, b2Body* b2, const b2Vec2& anchor1, const b2Vec2& anchor2) {
   bodyA = b1;
   bodyB = b2;
@@ -768,6 +789,7 @@ extern "C" B2G_API int b2g_scene_build(b2g_batch* b, int32_t world, int32_t kind
   else if (kind == B2G_SCENE_CHAINS) c = b2scenes::ChainsOverPile(&w, n, 20, (int)p0, seed);
   else if (kind == B2G_SCENE_BATCH_WORLD) c = b2scenes::BatchWorld(&w, seed, n);
   else if (kind == B2G_SCENE_JOINTS) c = b2scenes::JointZoo(&w, n, seed);
+  else if (kind == B2G_SCENE_SLIDERS) c = b2scenes::SliderRigs(&w, n, seed);
   else return B2G_E_INVALID_ARG;
   if (counts) { counts[0] = c.bodies; counts[1] = c.fixtures; counts[2] = c.joints; }
   return B2G_OK;

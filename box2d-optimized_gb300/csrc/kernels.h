@@ -193,7 +193,10 @@ void solver_setup();
 // CTA for each size class (at most 64, 256, 1024, 8192 and more bodies); a class runs the wide
 // build when its worlds fill at most `wide_waves` waves of it.
 std::vector<SolveClass> plan_solve_classes(const std::vector<int>& order, const std::vector<int>& bodies,
-                                           const int* class_threads, float wide_waves);
+                                           const int* class_threads, float wide_waves, int cluster_ctas);
+// Largest thread-block cluster (CTAs per world) the device runs the cluster solve with: 16 where
+// the non-portable size is available, else 8; 0 before solver_setup or when clusters are absent.
+int solver_max_cluster_ctas();
 bool solver_threads_valid(int t);
 void launch_clear_forces(const KernelArgs& a, int nb, cudaStream_t s);
 // Broadphase up to the tree (AABBs, Morton sort, LBVH, node boxes); with `pairs` also the pair

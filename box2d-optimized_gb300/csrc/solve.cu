@@ -53,7 +53,8 @@ __global__ void __launch_bounds__(T) k_joint_colour(KernelArgs a, int w0) {
   m.rdy = a.jready + j0;
   m.wl0 = a.jwork + 2 * (int64_t)j0;
   m.wl1 = a.jwork + 2 * (int64_t)j0 + nj;
-  int njc = colour_constraints<T>(nj, nb, m, a.jprio + j0, a.jorder + j0, nullptr, jr, a.status);
+  CtaTeam<T> tm;
+  int njc = colour_constraints(tm, nj, nb, m, a.jprio + j0, a.jorder + j0, nullptr, jr, a.status);
   for (int c = threadIdx.x; c <= njc; c += T) a.jranges[65 * (int64_t)w + c] = jr[c];
   if (threadIdx.x == 0) a.ncolors[4 * w + 1] = njc;
 }
@@ -136,7 +137,7 @@ static int threads_index(int t) {
 bool solver_threads_valid(int t) { return t == 64 || t == 128 || t == 256 || t == 512 || t == 1024; }
 
 std::vector<SolveClass> plan_solve_classes(const std::vector<int>& order, const std::vector<int>& bodies,
-                                           const int* class_threads, float wide_waves) {
+                                           const int* class_threads, float wide_waves, int cluster_ctas) {
   // `order` lists worlds by body count, largest first: each class is a contiguous range
   std::vector<SolveClass> out;
   int n = (int)order.size();
@@ -158,7 +159,12 @@ std::vector<SolveClass> plan_solve_classes(const std::vector<int>& order, const 
     bool wide = g_num_sms > 0 && (double)(i - start) * t <= (double)wide_waves * 512.0 * g_num_sms;
     int cap = kSmemCapByThreads[wide ? 1 : 0][ti];
     int smem = (int)(need < cap ? need : cap);
-    out.push_back({start, i - start, t, smem, c, wide});
+    // the largest class: a thread-block cluster per world when the device runs one
+    if (c == B2G_SOLVE_CLASSES - 1 && cluster_ctas > 1) {
+      out.push_back({start, i - start, kClusterThreads, 0, c, true, cluster_ctas});
+      continue;
+    }
+    out.push_back({start, i - start, t, smem, c, wide, 1});
   }
   return out;
 }
@@ -175,11 +181,16 @@ void solver_setup() {
   set_smem_attr<512>(3);
   set_smem_attr<1024>(4);
   solve_wide_setup(kSmemCapByThreads[1]);
+  solve_cluster_setup();
   int dev = 0;
   if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev);
 }
 
 static void launch_class(const KernelArgs& a, const SolveClass& c, cudaStream_t s) {
+  if (c.ctas > 1) {
+    launch_solve_class_cluster(a, c, s);
+    return;
+  }
   if (c.wide) {
     launch_solve_class_wide(a, c, s);
     return;

@@ -14,15 +14,148 @@ namespace b2g {
 
 #define FULL_MASK 0xffffffffu
 
-// Stable compaction of [0, n) with T / 32 warp-owned segments (multiples of 32 items, in list
-// order): `flag(k)` is evaluated twice, once to count each warp's kept items by ballots and once
-// to place them, and kept item k is handed to `emit(k, rank)` with its rank in list order. Two
-// CTA barriers in all, whatever n. Returns the number kept (in every thread).
-template <int T, class Flag, class Emit>
-__device__ __forceinline__ int block_compact(int n, Flag flag, Emit emit) {
-  constexpr int NWARP = T / 32;
-  __shared__ int wbase[NWARP + 1];
+// ---- teams: the threads that solve one world together
+//
+// CtaTeam<T>: one CTA of T threads; its barrier is __syncthreads.
+// ClusterTeam<T, CS>: a thread-block cluster of CS CTAs of T threads each, one world per
+// cluster, for worlds too large for one SM. Its barrier is the cluster barrier with release /
+// acquire semantics at cluster scope, which orders the team's global-memory and shared-memory
+// accesses across the cluster's SMs the way __syncthreads orders a CTA's. Team-wide counters
+// live in the shared memory of the cluster's first CTA (rank 0), which the other CTAs reach
+// through distributed shared memory.
+//
+// Every function below is written once against this interface: tid() numbers the team's
+// threads 0..kThreads-1, sync() is the team barrier, any() / all() are team-wide votes, lead(p)
+// maps a __shared__ object to the team's copy (rank 0's), rank() is the CTA's rank.
+
+__device__ __forceinline__ void cluster_barrier() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;\n" ::: "memory");
+}
+__device__ __forceinline__ unsigned cluster_rank() {
+  unsigned r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+// Generic address of `p` (a __shared__ object of this CTA) in the shared memory of CTA `rank` of
+// the cluster.
+template <class X>
+__device__ __forceinline__ X* cluster_map(X* p, unsigned rank) {
+  uint64_t out;
+  asm volatile("mapa.u64 %0, %1, %2;" : "=l"(out) : "l"((uint64_t)p), "r"(rank));
+  return reinterpret_cast<X*>(out);
+}
+
+template <int T>
+struct CtaTeam {
+  static constexpr int kThreads = T;
+  static constexpr int kCtas = 1;
+  static constexpr cuda::thread_scope kScope = cuda::thread_scope_block;
+  __device__ __forceinline__ int tid() const { return threadIdx.x; }
+  __device__ __forceinline__ int rank() const { return 0; }
+  __device__ __forceinline__ void sync() const { __syncthreads(); }
+  __device__ __forceinline__ int any(int p) { return __syncthreads_or(p); }
+  __device__ __forceinline__ int all(int p) { return __syncthreads_and(p); }
+  template <class X>
+  __device__ __forceinline__ X* lead(X* p) const { return p; }
+  __device__ __forceinline__ int next_phase() { return 0; }
+};
+
+template <int T, int CS>
+struct ClusterTeam {
+  static constexpr int kThreads = T * CS;
+  static constexpr int kCtas = CS;
+  static constexpr cuda::thread_scope kScope = cuda::thread_scope_device;
+  int r;         // this CTA's rank in the cluster
+  int* votes;    // rank 0's three vote words (team copies)
+  int vphase;    // the vote word of the next any()
+  int sphase;    // parity of the next double-buffered team scratch
+  __device__ __forceinline__ int tid() const { return r * T + (int)threadIdx.x; }
+  __device__ __forceinline__ int rank() const { return r; }
+  __device__ __forceinline__ void sync() const { cluster_barrier(); }
+  // CTA vote, then one word on rank 0: the word of a call is cleared two calls before its use
+  // (every reader of its previous use has passed a team barrier since), so one team barrier per vote
+  __device__ int any(int p) {
+    const int local = __syncthreads_or(p);
+    int* v = votes + vphase;
+    if (threadIdx.x == 0) {
+      if (r == 0) votes[vphase == 2 ? 0 : vphase + 1] = 0;
+      if (local) atomicOr(v, 1);
+    }
+    cluster_barrier();
+    const int res = *(volatile int*)v;
+    vphase = vphase == 2 ? 0 : vphase + 1;
+    return res;
+  }
+  __device__ __forceinline__ int all(int p) { return !any(!p); }
+  template <class X>
+  __device__ __forceinline__ X* lead(X* p) const { return cluster_map(p, 0); }
+  __device__ __forceinline__ int next_phase() {
+    const int s = sphase;
+    sphase ^= 1;
+    return s;
+  }
+};
+
+// Exclusive prefix of one value per warp of the team (`v`, as given by the warp's lane 0) in team
+// warp order: returns the warp's base in every lane and the team total in *total. One CTA barrier
+// pair, and in a cluster one team barrier between them: each CTA scans its own warps, rank 0
+// collects the CTA sums (double-buffered by call parity, so that a fast CTA's next call does not
+// overwrite sums that a slow one still reads).
+template <class Team>
+__device__ __forceinline__ int team_warp_scan(Team& tm, int v, int* total) {
+  constexpr int NW = (Team::kThreads / Team::kCtas) / 32;
+  __shared__ int wbase[NW + 1];
+  __shared__ int csum[2][Team::kCtas > 1 ? Team::kCtas : 1];
+  __shared__ int cbase[2];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) wbase[wid] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int acc = 0;
+    for (int w = 0; w < NW; ++w) {
+      const int c = wbase[w];
+      wbase[w] = acc;
+      acc += c;
+    }
+    wbase[NW] = acc;
+  }
+  if constexpr (Team::kCtas == 1) {
+    __syncthreads();
+    const int base = wbase[wid];
+    *total = wbase[NW];
+    __syncthreads();  // wbase is reused by the next call
+    return base;
+  } else {
+    const int ph = tm.next_phase();
+    if (threadIdx.x == 0) tm.lead(&csum[ph][0])[tm.rank()] = wbase[NW];
+    tm.sync();
+    if (threadIdx.x == 0) {
+      const int* cs = tm.lead(&csum[ph][0]);
+      int before = 0, all = 0;
+      for (int q = 0; q < Team::kCtas; ++q) {
+        const int c = cs[q];
+        if (q < tm.rank()) before += c;
+        all += c;
+      }
+      cbase[0] = before;
+      cbase[1] = all;
+    }
+    __syncthreads();
+    const int base = cbase[0] + wbase[wid];
+    *total = cbase[1];
+    __syncthreads();  // wbase and cbase are reused by the next call
+    return base;
+  }
+}
+
+// Stable compaction of [0, n) with kThreads / 32 warp-owned segments (multiples of 32 items, in
+// list order): `flag(k)` is evaluated twice, once to count each warp's kept items by ballots and
+// once to place them, and kept item k is handed to `emit(k, rank)` with its rank in list order.
+// Returns the number kept (in every thread).
+template <class Team, class Flag, class Emit>
+__device__ __forceinline__ int block_compact(Team& tm, int n, Flag flag, Emit emit) {
+  constexpr int NWARP = Team::kThreads / 32;
+  const int lane = threadIdx.x & 31, wid = tm.tid() >> 5;
   const int seg = (((n + NWARP - 1) / NWARP) + 31) & ~31;
   const int s0 = min(n, wid * seg), s1 = min(n, s0 + seg);
   int cnt = 0;
@@ -30,19 +163,8 @@ __device__ __forceinline__ int block_compact(int n, Flag flag, Emit emit) {
     const int k = k0 + lane;
     cnt += __popc(__ballot_sync(FULL_MASK, k < s1 && flag(k)));
   }
-  if (lane == 0) wbase[wid] = cnt;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    int acc = 0;
-    for (int w = 0; w < NWARP; ++w) {
-      const int c = wbase[w];
-      wbase[w] = acc;
-      acc += c;
-    }
-    wbase[NWARP] = acc;
-  }
-  __syncthreads();
-  int base = wbase[wid];
+  int total;
+  int base = team_warp_scan(tm, cnt, &total);
   const unsigned lt = (1u << lane) - 1u;
   for (int k0 = s0; k0 < s1; k0 += 32) {
     const int k = k0 + lane;
@@ -51,38 +173,25 @@ __device__ __forceinline__ int block_compact(int n, Flag flag, Emit emit) {
     if (f) emit(k, base + __popc(b & lt));
     base += __popc(b);
   }
-  const int total = wbase[NWARP];
-  __syncthreads();  // wbase is reused by the next call
+  tm.sync();  // every emit() is visible, and flag()'s inputs may change, after the call
   return total;
 }
 
 // Exclusive prefix sums of get(i) over [0, n) in index order, handed to put(i, prefix), with
-// warp-owned segments: each warp sums its segment, thread 0 scans the T / 32 sums, each warp
-// scans its segment on top. Two CTA barriers in all. Returns the total (in every thread).
-template <int T, class Get, class Put>
-__device__ __forceinline__ int block_exclusive_scan(int n, Get get, Put put) {
-  constexpr int NWARP = T / 32;
-  __shared__ int wbase[NWARP + 1];
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+// warp-owned segments: each warp sums its segment, the warp sums are scanned across the team,
+// each warp scans its segment on top. Returns the total (in every thread).
+template <class Team, class Get, class Put>
+__device__ __forceinline__ int block_exclusive_scan(Team& tm, int n, Get get, Put put) {
+  constexpr int NWARP = Team::kThreads / 32;
+  const int lane = threadIdx.x & 31, wid = tm.tid() >> 5;
   const int seg = (((n + NWARP - 1) / NWARP) + 31) & ~31;
   const int s0 = min(n, wid * seg), s1 = min(n, s0 + seg);
   int sum = 0;
   for (int k = s0 + lane; k < s1; k += 32) sum += get(k);
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(FULL_MASK, sum, o);
-  if (lane == 0) wbase[wid] = sum;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    int acc = 0;
-    for (int w = 0; w < NWARP; ++w) {
-      const int c = wbase[w];
-      wbase[w] = acc;
-      acc += c;
-    }
-    wbase[NWARP] = acc;
-  }
-  __syncthreads();
-  int base = wbase[wid];
+  int total;
+  int base = team_warp_scan(tm, sum, &total);
   for (int k0 = s0; k0 < s1; k0 += 32) {
     const int k = k0 + lane;
     const int v = k < s1 ? get(k) : 0;
@@ -95,8 +204,7 @@ __device__ __forceinline__ int block_exclusive_scan(int n, Get get, Put put) {
     if (k < s1) put(k, base + x - v);
     base += __shfl_sync(FULL_MASK, x, 31);
   }
-  const int total = wbase[NWARP];
-  __syncthreads();  // wbase is reused by the next call
+  tm.sync();  // every put() is visible, and get()'s inputs may change, after the call
   return total;
 }
 
@@ -121,35 +229,34 @@ struct ColourMem {
 // serially in priority order. Buckets the constraints by colour into `order` (and its inverse
 // into `slot` when given) and writes the colour offsets to `ranges` (ncol + 1 entries). Returns
 // the number of colours (max + 1).
-template <int T>
-__device__ int colour_constraints(int n, int nb, const ColourMem m, const uint32_t* prio, int* order, int* slot,
-                                  int* ranges, unsigned int* status) {
-  __shared__ int col_cnt[64];
-  __shared__ int col_off[65];
-  __shared__ int s_maxcol;
-  for (int i = threadIdx.x; i < nb; i += T) {
+template <class Team>
+__device__ int colour_constraints(Team& tm, int n, int nb, const ColourMem m, const uint32_t* prio, int* order,
+                                  int* slot, int* ranges, unsigned int* status) {
+  constexpr int NT = Team::kThreads;
+  const int tid = tm.tid();
+  for (int i = tid; i < nb; i += NT) {
     m.cnt[i] = 0;
     m.mask[i] = 0ull;
   }
-  for (int k = threadIdx.x; k < n; k += T) m.col[k] = -1;
-  __syncthreads();
-  for (int k = threadIdx.x; k < n; k += T) {
+  for (int k = tid; k < n; k += NT) m.col[k] = -1;
+  tm.sync();
+  for (int k = tid; k < n; k += NT) {
     int2 b = m.cb[k];
     if (b.x >= 0) atomicAdd(&m.cnt[b.x], 1);
     if (b.y >= 0) atomicAdd(&m.cnt[b.y], 1);
   }
-  __syncthreads();
-  block_exclusive_scan<T>(nb, [&](int i) { return m.cnt[i]; }, [&](int i, int p) { m.head[i] = p; });
-  for (int i = threadIdx.x; i < nb; i += T) m.cnt[i] = 0;
-  __syncthreads();
-  for (int k = threadIdx.x; k < n; k += T) {
+  tm.sync();
+  block_exclusive_scan(tm, nb, [&](int i) { return m.cnt[i]; }, [&](int i, int p) { m.head[i] = p; });
+  for (int i = tid; i < nb; i += NT) m.cnt[i] = 0;
+  tm.sync();
+  for (int k = tid; k < n; k += NT) {
     int2 b = m.cb[k];
     if (b.x >= 0) m.list[m.head[b.x] + atomicAdd(&m.cnt[b.x], 1)] = k;
     if (b.y >= 0) m.list[m.head[b.y] + atomicAdd(&m.cnt[b.y], 1)] = k;
   }
-  __syncthreads();
+  tm.sync();
   // each body's list in (priority, index) order
-  for (int i = threadIdx.x; i < nb; i += T) {
+  for (int i = tid; i < nb; i += NT) {
     int off = m.head[i], cnt = m.cnt[i];
     for (int x = 1; x < cnt; ++x) {
       int kx = m.list[off + x];
@@ -165,34 +272,34 @@ __device__ int colour_constraints(int n, int nb, const ColourMem m, const uint32
       m.list[off + y + 1] = kx;
     }
   }
-  __syncthreads();
   // rounds over a worklist of the uncoloured constraints: a round colours every constraint that
   // heads the priority lists of all its non-static bodies (at least the uncoloured one of lowest
   // (priority, index)); the others form the next round's worklist (their order is immaterial)
-  // worklist sizes alternate between two counters: a round reads one and fills the other, which it
-  // clears before its first barrier (every thread read it two barriers ago)
-  __shared__ int s_cnt[2];
-  if (threadIdx.x == 0) {
+  // worklist sizes alternate between two team counters: a round reads one and fills the other,
+  // which it clears before its first barrier (every thread read it two barriers ago)
+  __shared__ int s_cnt_own[2];
+  int* s_cnt = tm.lead(s_cnt_own);
+  if (tid == 0) {
     s_cnt[0] = n;
     s_cnt[1] = 0;
   }
-  __syncthreads();
+  tm.sync();
   int* wl = m.wl0;
   int* wn = m.wl1;
   bool done = (n == 0);
   for (int round = 0; round <= n + 1 && !done; ++round) {
     const int cur = round & 1;
-    const int cnt = s_cnt[cur];
-    for (int i = threadIdx.x; i < cnt; i += T) {
+    const int cnt = *(volatile int*)&s_cnt[cur];
+    for (int i = tid; i < cnt; i += NT) {
       int k = round == 0 ? i : wl[i];
       int2 b = m.cb[k];
       bool ok = (b.x < 0 || m.list[m.head[b.x]] == k) && (b.y < 0 || m.list[m.head[b.y]] == k);
       m.rdy[k] = ok ? 1 : 0;
     }
-    if (round > 0 && threadIdx.x == 0) s_cnt[cur ^ 1] = 0;
-    __syncthreads();
-    for (int i0 = 0; i0 < cnt; i0 += T) {  // CTA-uniform trip count: whole warps reach the ballot
-      int i = i0 + threadIdx.x;
+    if (round > 0 && tid == 0) s_cnt[cur ^ 1] = 0;
+    tm.sync();
+    for (int i0 = 0; i0 < cnt; i0 += NT) {  // team-uniform trip count: whole warps reach the ballot
+      int i = i0 + tid;
       int k = -1;
       bool keep = false;
       if (i < cnt) {
@@ -223,44 +330,76 @@ __device__ int colour_constraints(int n, int nb, const ColourMem m, const uint32
       base = __shfl_sync(FULL_MASK, base, 0);
       if (keep) wn[base + __popc(bal & ((1u << lane) - 1u))] = k;
     }
-    __syncthreads();
-    done = (s_cnt[cur ^ 1] == 0);
+    tm.sync();
+    done = (*(volatile int*)&s_cnt[cur ^ 1] == 0);
     int* t = wl;
     wl = wn;
     wn = t;
   }
-  if (!done && threadIdx.x == 0) atomicOr(status, B2G_DEV_COLOR_ROUNDS);
-  // bucket by colour
+  if (!done && tid == 0) atomicOr(status, B2G_DEV_COLOR_ROUNDS);
+  // bucket by colour: each CTA counts its constraints per colour; a colour's slots go to the CTAs
+  // in rank order (the order inside a colour does not matter), so CTA r places its constraints of
+  // colour c from off[c] = start of c + counts of c in the CTAs before it
+  __shared__ int col_cnt[64];       // this CTA's count per colour, then its fill counter
+  __shared__ int col_off[65];       // global start of each colour, then this CTA's offset
+  __shared__ int col_tot[65];       // team total per colour, then the colour offsets
+  __shared__ int cta_cnt[Team::kCtas > 1 ? 2 : 1][Team::kCtas > 1 ? Team::kCtas * 64 : 1];
   if (threadIdx.x < 64) col_cnt[threadIdx.x] = 0;
-  if (threadIdx.x == 0) s_maxcol = -1;
   __syncthreads();
-  for (int k = threadIdx.x; k < n; k += T) {
+  for (int k = tid; k < n; k += NT) {
     int c = m.col[k];
     if (c < 0) c = 63;  // only after a failed colouring (status raised)
     atomicAdd(&col_cnt[c], 1);
-    atomicMax(&s_maxcol, c);
+  }
+  __syncthreads();
+  if constexpr (Team::kCtas == 1) {
+    if (threadIdx.x < 64) col_tot[threadIdx.x] = col_cnt[threadIdx.x];
+  } else {
+    const int ph = tm.next_phase();
+    int* all = tm.lead(&cta_cnt[ph][0]);
+    if (threadIdx.x < 64) all[tm.rank() * 64 + threadIdx.x] = col_cnt[threadIdx.x];
+    tm.sync();
+    if (threadIdx.x < 64) {
+      int before = 0, tot = 0;
+      for (int q = 0; q < Team::kCtas; ++q) {
+        const int v = all[q * 64 + threadIdx.x];
+        if (q < tm.rank()) before += v;
+        tot += v;
+      }
+      col_tot[threadIdx.x] = tot;
+      col_off[threadIdx.x] = before;  // added to the colour's start below
+    }
   }
   __syncthreads();
   if (threadIdx.x == 0) {
-    int s = 0;
+    int s = 0, mx = -1;
     for (int c = 0; c < 64; ++c) {
-      col_off[c] = s;
-      s += col_cnt[c];
-      col_cnt[c] = 0;
+      const int t = col_tot[c];
+      if (t > 0) mx = c;
+      col_tot[c] = s;
+      s += t;
     }
-    col_off[64] = s;
+    col_tot[64] = s;
+    col_off[64] = mx + 1;  // the number of colours
   }
   __syncthreads();
-  for (int k = threadIdx.x; k < n; k += T) {
+  const int ncol = col_off[64];
+  if (threadIdx.x < 64) {
+    col_off[threadIdx.x] = col_tot[threadIdx.x] + (Team::kCtas == 1 ? 0 : col_off[threadIdx.x]);
+    col_cnt[threadIdx.x] = 0;
+  }
+  __syncthreads();
+  for (int k = tid; k < n; k += NT) {
     int c = m.col[k];
     if (c < 0) c = 63;
     int pos = col_off[c] + atomicAdd(&col_cnt[c], 1);
     order[pos] = k;
     if (slot) slot[k] = pos;
   }
-  __syncthreads();
-  if (threadIdx.x == 0 && col_cnt[63] > 1) {
-    int off = col_off[63], cnt = col_cnt[63];
+  tm.sync();
+  const int n63 = col_tot[64] - col_tot[63];
+  if (tid == 0 && n63 > 1) {
+    int off = col_tot[63], cnt = n63;
     for (int x = 1; x < cnt; ++x) {
       int kx = order[off + x];
       uint32_t px = prio[kx];
@@ -277,9 +416,8 @@ __device__ int colour_constraints(int n, int nb, const ColourMem m, const uint32
     if (slot)
       for (int x = 0; x < cnt; ++x) slot[order[off + x]] = off + x;
   }
-  int ncol = s_maxcol + 1;
-  for (int c = threadIdx.x; c <= ncol; c += T) ranges[c] = col_off[c];
-  __syncthreads();
+  for (int c = threadIdx.x; c <= ncol; c += Team::kThreads / Team::kCtas) ranges[c] = col_tot[c];
+  tm.sync();
   return ncol;
 }
 
@@ -383,41 +521,43 @@ __device__ __forceinline__ void unpack_pos(const PosRows& r, VCDev& vc, const Ma
 // its first constraint of the next regular colour before the barrier, so that their round trip
 // overlaps the wait: rows do not change while a colour is solved (a constraint's impulses are
 // written only by its own solve, once per pass), only the bodies do, and those are read after.
-template <int T, class Rows, bool PREFETCH, class Fetch, class Solve>
-__device__ __forceinline__ void colour_sweep(const int* ranges, int ncol, int c0, Fetch fetch, Solve solve) {
+template <class Team, class Rows, bool PREFETCH, class Fetch, class Solve>
+__device__ __forceinline__ void colour_sweep(Team& tm, const int* ranges, int ncol, int c0, Fetch fetch, Solve solve) {
+  constexpr int NT = Team::kThreads;
+  const int tid = tm.tid();
   Rows pre;
   bool have = false;  // pre holds the rows of this thread's first constraint of colour c
-  if (PREFETCH && ncol > 0 && ranges[0] + (int)threadIdx.x < ranges[1]) {
-    fetch(c0 + ranges[0] + threadIdx.x, pre);
+  if (PREFETCH && ncol > 0 && ranges[0] + tid < ranges[1]) {
+    fetch(c0 + ranges[0] + tid, pre);
     have = true;
   }
   for (int c = 0; c < ncol; ++c) {
     int s = ranges[c], e = ranges[c + 1];
     if (c == 63) {
-      if (threadIdx.x == 0)
+      if (tid == 0)
         for (int i = s; i < e; ++i) {
           Rows r;
           fetch(c0 + i, r);
           solve(c0 + i, r);
         }
     } else {
-      int i = s + threadIdx.x;
+      int i = s + tid;
       if (have) {
         solve(c0 + i, pre);
-        i += T;
+        i += NT;
       }
-      for (; i < e; i += T) {
+      for (; i < e; i += NT) {
         Rows r;
         fetch(c0 + i, r);
         solve(c0 + i, r);
       }
     }
     have = false;
-    if (PREFETCH && c + 1 < ncol && c + 1 != 63 && ranges[c + 1] + (int)threadIdx.x < ranges[c + 2]) {
-      fetch(c0 + ranges[c + 1] + threadIdx.x, pre);
+    if (PREFETCH && c + 1 < ncol && c + 1 != 63 && ranges[c + 1] + tid < ranges[c + 2]) {
+      fetch(c0 + ranges[c + 1] + tid, pre);
       have = true;
     }
-    __syncthreads();
+    tm.sync();
   }
 }
 
@@ -442,38 +582,44 @@ struct SmemCarver {
 // A world's island records are touched by its CTA alone: every access is a CTA-scope atomic
 // (loads included, so that none is served from a line older than an atomic), and the CTA barrier
 // orders the phases.
+template <cuda::thread_scope S = cuda::thread_scope_block>
 __device__ __forceinline__ int isl_load(int* p) {
-  return cuda::atomic_ref<int, cuda::thread_scope_block>(*p).load(cuda::memory_order_relaxed);
+  return cuda::atomic_ref<int, S>(*p).load(cuda::memory_order_relaxed);
 }
+template <cuda::thread_scope S = cuda::thread_scope_block>
 __device__ __forceinline__ void isl_store(int* p, int v) {
-  cuda::atomic_ref<int, cuda::thread_scope_block>(*p).store(v, cuda::memory_order_relaxed);
+  cuda::atomic_ref<int, S>(*p).store(v, cuda::memory_order_relaxed);
 }
+template <cuda::thread_scope S = cuda::thread_scope_block>
 __device__ __forceinline__ void isl_or(int* p, int v) {
-  cuda::atomic_ref<int, cuda::thread_scope_block>(*p).fetch_or(v, cuda::memory_order_relaxed);
+  cuda::atomic_ref<int, S>(*p).fetch_or(v, cuda::memory_order_relaxed);
 }
-__device__ __forceinline__ void isl_sync() { __syncthreads(); }
-__device__ __forceinline__ int isl_label(int4* SL, int i) { return isl_load(&SL[i].x); }
-__device__ __forceinline__ int isl_bits(int4* SL, int i) { return isl_load(&SL[i].y); }
+template <cuda::thread_scope S = cuda::thread_scope_block>
+__device__ __forceinline__ int isl_label(int4* SL, int i) { return isl_load<S>(&SL[i].x); }
+template <cuda::thread_scope S = cuda::thread_scope_block>
+__device__ __forceinline__ int isl_bits(int4* SL, int i) { return isl_load<S>(&SL[i].y); }
 
 // Root of x. With `halve`, path halving shortens the walk (x is no root, so no hook targets it);
 // halving stores only during the unions: a late halving store could otherwise overwrite a final
 // label with an intermediate ancestor.
+template <cuda::thread_scope S = cuda::thread_scope_block>
 __device__ inline int isl_find(int4* SL, int x, bool halve, unsigned int* status) {
   for (int guard = 0; guard < (1 << 24); ++guard) {
-    int p = isl_load(&SL[x].x);
+    int p = isl_load<S>(&SL[x].x);
     if (p == x) return x;
-    int g = isl_load(&SL[p].x);
-    if (halve && g != p) isl_store(&SL[x].x, g);
+    int g = isl_load<S>(&SL[p].x);
+    if (halve && g != p) isl_store<S>(&SL[x].x, g);
     x = g;
   }
   raise_status(status, B2G_DEV_STACK_OVERFLOW);
   return x;
 }
 
+template <cuda::thread_scope S = cuda::thread_scope_block>
 __device__ inline void isl_unite(int4* SL, int x, int y, unsigned int* status) {
   for (int guard = 0; guard < (1 << 20); ++guard) {
-    x = isl_find(SL, x, true, status);
-    y = isl_find(SL, y, true, status);
+    x = isl_find<S>(SL, x, true, status);
+    y = isl_find<S>(SL, y, true, status);
     if (x == y) return;
     if (x < y) {
       int t = x;
@@ -481,7 +627,7 @@ __device__ inline void isl_unite(int4* SL, int x, int y, unsigned int* status) {
       y = t;
     }
     int expect = x;  // x was hooked meanwhile when this fails: retry from its root
-    if (cuda::atomic_ref<int, cuda::thread_scope_block>(SL[x].x)
+    if (cuda::atomic_ref<int, S>(SL[x].x)
             .compare_exchange_strong(expect, y, cuda::memory_order_relaxed))
       return;
   }
@@ -492,11 +638,14 @@ __device__ inline void isl_unite(int4* SL, int x, int y, unsigned int* status) {
 // src/dynamics/b2_contact.cpp:183-188), labels the islands, and wakes every member of an island
 // that holds an awake body (the search marks the bodies it reaches awake without resetting their
 // sleep timers, b2_world.cpp:565-566). Sleeping islands are neither integrated nor solved.
-template <int T>
-__device__ void build_islands(const KernelArgs& a, int b0, int nb, int c0, int ncAll, int j0, int nj) {
+template <class Team>
+__device__ void build_islands(Team& tm, const KernelArgs& a, int b0, int nb, int c0, int ncAll, int j0, int nj) {
+  constexpr cuda::thread_scope S = Team::kScope;
+  constexpr int T = Team::kThreads;
+  const int tid = tm.tid();
   int4* SL = a.sl + b0;
   int2* BS = a.bstate + b0;
-  for (int i = threadIdx.x; i < nb; i += T) {
+  for (int i = tid; i < nb; i += T) {
     const int bi = b0 + i;
     const bool stat = a.btype[bi] == B2G_STATIC;
     if (a.bwake[bi]) {
@@ -508,49 +657,50 @@ __device__ void build_islands(const KernelArgs& a, int b0, int nb, int c0, int n
         BS[i] = st;
       }
     }
-    isl_store(&SL[i].x, stat ? -1 : i);
-    isl_store(&SL[i].y, 0);
-    isl_store(&SL[i].z, 0);
-    isl_store(&SL[i].w, 0x7f7fffff);  // FLT_MAX: no member timed yet
+    isl_store<S>(&SL[i].x, stat ? -1 : i);
+    isl_store<S>(&SL[i].y, 0);
+    isl_store<S>(&SL[i].z, 0);
+    isl_store<S>(&SL[i].w, 0x7f7fffff);  // FLT_MAX: no member timed yet
   }
-  isl_sync();
-  for (int k = threadIdx.x; k < ncAll; k += T) {
+  tm.sync();
+  for (int k = tid; k < ncAll; k += T) {
     const int2 f = a.cfix[c0 + k];
     const int ia = a.fbody[f.x] - b0, ib = a.fbody[f.y] - b0;
-    if (!(isl_bits(SL, ia) & B2G_ISL_LINKED)) isl_or(&SL[ia].y, B2G_ISL_LINKED);
-    if (!(isl_bits(SL, ib) & B2G_ISL_LINKED)) isl_or(&SL[ib].y, B2G_ISL_LINKED);
+    if (!(isl_bits<S>(SL, ia) & B2G_ISL_LINKED)) isl_or<S>(&SL[ia].y, B2G_ISL_LINKED);
+    if (!(isl_bits<S>(SL, ib) & B2G_ISL_LINKED)) isl_or<S>(&SL[ib].y, B2G_ISL_LINKED);
     const uint32_t fl = a.cflags[c0 + k];
     if ((fl & B2G_CONTACT_TOUCHING) && (fl & B2G_CONTACT_ENABLED) && !a.fsensor[f.x] && !a.fsensor[f.y] &&
-        isl_load(&SL[ia].x) >= 0 && isl_load(&SL[ib].x) >= 0)
-      isl_unite(SL, ia, ib, a.status);
+        isl_load<S>(&SL[ia].x) >= 0 && isl_load<S>(&SL[ib].x) >= 0)
+      isl_unite<S>(SL, ia, ib, a.status);
   }
-  for (int k = threadIdx.x; k < nj; k += T) {
+  for (int k = tid; k < nj; k += T) {
     const JointDev& J = a.joints[j0 + k];
     const int ia = J.d.body_a - b0, ib = J.d.body_b - b0;
-    isl_or(&SL[ia].y, B2G_ISL_LINKED);
-    isl_or(&SL[ib].y, B2G_ISL_LINKED);
-    if (isl_load(&SL[ia].x) >= 0 && isl_load(&SL[ib].x) >= 0) isl_unite(SL, ia, ib, a.status);
+    isl_or<S>(&SL[ia].y, B2G_ISL_LINKED);
+    isl_or<S>(&SL[ib].y, B2G_ISL_LINKED);
+    if (isl_load<S>(&SL[ia].x) >= 0 && isl_load<S>(&SL[ib].x) >= 0) isl_unite<S>(SL, ia, ib, a.status);
   }
-  isl_sync();
+  tm.sync();
   // labels, and the awake mark of every island with an awake member (roots no longer change)
-  for (int i = threadIdx.x; i < nb; i += T) {
-    if (isl_load(&SL[i].x) < 0) continue;
-    const int r = isl_find(SL, i, false, a.status);
-    isl_store(&SL[i].x, r);
-    if (BS[i].x & B2G_BS_AWAKE) isl_or(&SL[r].y, B2G_ISL_AWAKE);
+  for (int i = tid; i < nb; i += T) {
+    if (isl_load<S>(&SL[i].x) < 0) continue;
+    const int r = isl_find<S>(SL, i, false, a.status);
+    isl_store<S>(&SL[i].x, r);
+    if (BS[i].x & B2G_BS_AWAKE) isl_or<S>(&SL[r].y, B2G_ISL_AWAKE);
   }
-  isl_sync();
-  for (int i = threadIdx.x; i < nb; i += T) {
-    const int r = isl_label(SL, i);
-    if (r >= 0 && (isl_bits(SL, r) & B2G_ISL_AWAKE)) BS[i].x |= B2G_BS_AWAKE;
+  tm.sync();
+  for (int i = tid; i < nb; i += T) {
+    const int r = isl_label<S>(SL, i);
+    if (r >= 0 && (isl_bits<S>(SL, r) & B2G_ISL_AWAKE)) BS[i].x |= B2G_BS_AWAKE;
   }
-  isl_sync();
+  tm.sync();
 }
 
 // Island root of a contact or joint between world-local bodies la and lb (one is non-static).
+template <cuda::thread_scope S = cuda::thread_scope_block>
 __device__ __forceinline__ int isl_root(int4* SL, int la, int lb) {
-  const int r = isl_label(SL, la);
-  return r >= 0 ? r : isl_label(SL, lb);
+  const int r = isl_label<S>(SL, la);
+  return r >= 0 ? r : isl_label<S>(SL, lb);
 }
 
 __device__ __forceinline__ bool joint_awake(const KernelArgs& a, const JointDev& J) {
@@ -563,15 +713,18 @@ __device__ __forceinline__ bool joint_awake(const KernelArgs& a, const JointDev&
 // contact and no joint is an orphan: it times itself, and when its timer runs out its velocity and
 // force are cleared but it stays awake (b2World::Solve marks orphans awake after solving them,
 // b2_world.cpp:545-549).
-template <int T>
-__device__ void sleep_islands(const KernelArgs& a, int b0, int nb) {
+template <class Team>
+__device__ void sleep_islands(Team& tm, const KernelArgs& a, int b0, int nb) {
+  constexpr cuda::thread_scope S = Team::kScope;
+  constexpr int T = Team::kThreads;
+  const int tid = tm.tid();
   int4* SL = a.sl + b0;
   int2* BS = a.bstate + b0;
   const float linTolSqr = B2G_LINEAR_SLEEP_TOL * B2G_LINEAR_SLEEP_TOL;
   const float angTolSqr = B2G_ANGULAR_SLEEP_TOL * B2G_ANGULAR_SLEEP_TOL;
   const float h = a.dt;
-  for (int i = threadIdx.x; i < nb; i += T) {
-    const int ex = isl_label(SL, i), ey = isl_bits(SL, i);
+  for (int i = tid; i < nb; i += T) {
+    const int ex = isl_label<S>(SL, i), ey = isl_bits<S>(SL, i);
     int2 st = BS[i];
     if (ex < 0 || !(st.x & B2G_BS_AWAKE)) continue;
     const int bi = b0 + i;
@@ -592,16 +745,16 @@ __device__ void sleep_islands(const KernelArgs& a, int b0, int nb) {
       }
     } else {
       // t >= 0: the bit patterns order as the floats
-      cuda::atomic_ref<int, cuda::thread_scope_block>(SL[ex].w).fetch_min(__float_as_int(t), cuda::memory_order_relaxed);
+      cuda::atomic_ref<int, S>(SL[ex].w).fetch_min(__float_as_int(t), cuda::memory_order_relaxed);
     }
     BS[i] = st;
   }
-  isl_sync();
-  for (int i = threadIdx.x; i < nb; i += T) {
-    const int ex = isl_label(SL, i);
-    if (ex < 0 || !(isl_bits(SL, i) & B2G_ISL_LINKED) || !(BS[i].x & B2G_BS_AWAKE)) continue;
-    const float rmin = __int_as_float(isl_load(&SL[ex].w));
-    if (!(rmin >= B2G_TIME_TO_SLEEP) || !(isl_bits(SL, ex) & B2G_ISL_DONE)) continue;
+  tm.sync();
+  for (int i = tid; i < nb; i += T) {
+    const int ex = isl_label<S>(SL, i);
+    if (ex < 0 || !(isl_bits<S>(SL, i) & B2G_ISL_LINKED) || !(BS[i].x & B2G_BS_AWAKE)) continue;
+    const float rmin = __int_as_float(isl_load<S>(&SL[ex].w));
+    if (!(rmin >= B2G_TIME_TO_SLEEP) || !(isl_bits<S>(SL, ex) & B2G_ISL_DONE)) continue;
     const int bi = b0 + i;
     BS[i] = make_int2(BS[i].x & ~B2G_BS_AWAKE, 0);
     a.vel[bi] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
@@ -618,11 +771,15 @@ __device__ void sleep_islands(const KernelArgs& a, int b0, int nb) {
 template <int T, bool WIDE>
 constexpr int kSolveBlocks = WIDE ? (T >= 512 ? 1 : 512 / T) : 1024 / T;
 
-template <int T, bool WIDE>
-__global__ void __launch_bounds__(T, kSolveBlocks<T, WIDE>) k_solve(KernelArgs a, int first, int smem_bytes) {
-  extern __shared__ __align__(16) unsigned char smem[];
-  const int w = a.world_order[first + blockIdx.x];
-  if ((a.wflags[w] & B2G_WF_ACTIVE) == 0) return;
+// The island solve of world w by team tm; smem / smem_bytes: the CTA's dynamic shared memory (a
+// cluster team passes none: its world's arrays stay in global memory). PREFETCH: each thread
+// reads its next colour's rows before the colour barrier (the 128-register builds).
+template <class Team, bool PREFETCH>
+__device__ __forceinline__ void solve_world(Team& tm, const KernelArgs& a, int w, unsigned char* smem, int smem_bytes) {
+  constexpr cuda::thread_scope S = Team::kScope;
+  constexpr int NT = Team::kThreads;            // threads of the team
+  constexpr int TC = NT / Team::kCtas;          // threads of one CTA
+  const int tid = tm.tid();
   __shared__ int cranges[65];
   __shared__ int jranges[65];
   const int4 wb = a.wb[w];
@@ -643,10 +800,10 @@ __global__ void __launch_bounds__(T, kSolveBlocks<T, WIDE>) k_solve(KernelArgs a
   int2* const BS = a.bstate + b0;
 
   // 0. sleep-mode worlds: wakes, islands, awake islands
-  if (sleepMode) build_islands<T>(a, b0, nb, c0, ncAll, j0, nj);
+  if (sleepMode) build_islands(tm, a, b0, nb, c0, ncAll, j0, nj);
 
   // 1. solver contacts in list order, with local bodies (static = -1) and colouring priorities
-  const int nsc = block_compact<T>(
+  const int nsc = block_compact(tm, 
       ncAll,
       [&](int k) {
         const uint32_t fl = a.cflags[c0 + k];
@@ -690,8 +847,8 @@ __global__ void __launch_bounds__(T, kSolveBlocks<T, WIDE>) k_solve(KernelArgs a
     uint8_t* rdy = bodySm ? (uint8_t*)sc.take((size_t)nsc) : nullptr;
     bool conSm = list && cb && wl && col && rdy;
     if (conSm) {
-      for (int k = threadIdx.x; k < nsc; k += T) cb[k] = a.scb[c0 + k];
-      __syncthreads();
+      for (int k = tid; k < nsc; k += NT) cb[k] = a.scb[c0 + k];
+      tm.sync();
       m.list = list; m.cb = cb; m.col = col; m.rdy = rdy;
       m.wl0 = wl; m.wl1 = wl + nsc;
     } else {
@@ -702,16 +859,16 @@ __global__ void __launch_bounds__(T, kSolveBlocks<T, WIDE>) k_solve(KernelArgs a
       m.wl0 = a.cwork + 2 * (int64_t)c0;
       m.wl1 = a.cwork + 2 * (int64_t)c0 + nsc;
     }
-    ncc = colour_constraints<T>(nsc, nb, m, a.cprio + c0, a.corder + c0, a.cslot + c0, cranges, a.status);
+    ncc = colour_constraints(tm, nsc, nb, m, a.cprio + c0, a.corder + c0, a.cslot + c0, cranges, a.status);
     if (conSm) {
-      for (int k = threadIdx.x; k < nsc; k += T) a.ccol[c0 + k] = col[k];
-      __syncthreads();
+      for (int k = tid; k < nsc; k += NT) a.ccol[c0 + k] = col[k];
+      tm.sync();
     }
   }
   // joints: colours fixed per layout
   const int njc = nj > 0 ? a.ncolors[4 * w + 1] : 0;
-  for (int c = threadIdx.x; c <= njc; c += T) jranges[c] = a.jranges[65 * (int64_t)w + c];
-  if (threadIdx.x == 0) {
+  for (int c = threadIdx.x; c <= njc; c += TC) jranges[c] = a.jranges[65 * (int64_t)w + c];
+  if (tid == 0) {
     a.ncolors[4 * w] = ncc;
     a.ncolors[4 * w + 2] = nsc;
     a.ncolors[4 * w + 3] = c0;
@@ -726,7 +883,7 @@ __global__ void __launch_bounds__(T, kSolveBlocks<T, WIDE>) k_solve(KernelArgs a
   float4* bs = bsm ? reinterpret_cast<float4*>(smem) : a.vel + b0;
   float2* msm = bsm ? reinterpret_cast<float2*>(smem + sizeof(float4) * (size_t)nb) : nullptr;
   const Masses M{msm, a.massd + b0};
-  for (int i = threadIdx.x; i < nb; i += T) {
+  for (int i = tid; i < nb; i += NT) {
     int bi = b0 + i;
     float4 v4 = a.vel[bi];
     float4 md = a.massd[bi];
@@ -747,11 +904,11 @@ __global__ void __launch_bounds__(T, kSolveBlocks<T, WIDE>) k_solve(KernelArgs a
       bs[i] = v4;
     }
   }
-  __syncthreads();
+  tm.sync();
 
   // 4. prepare (b2ContactSolver::Initialize + InitializeVelocityConstraints) in list order, each
   //    constraint written to its colour-ordered slot
-  for (int k = threadIdx.x; k < nsc; k += T) {
+  for (int k = tid; k < nsc; k += NT) {
     int ci = a.sc_list[c0 + k];
     int p = a.cslot[c0 + k];
     int2 lb = a.scb[c0 + k];
@@ -765,14 +922,14 @@ __global__ void __launch_bounds__(T, kSolveBlocks<T, WIDE>) k_solve(KernelArgs a
                    a.pos[ia], bs[la], a.pos[ib], bs[lbb], dtRatio, warm, ci);
     store_planes(P, c0 + p, vc);
   }
-  __syncthreads();
+  tm.sync();
   float4* jb = bs - b0;  // joints address bodies by global index
 
   // 5. warm start contacts, then joint InitVelocityConstraints, colour by colour
   auto fetchV = [&](int slot, VelRows& r) { fetch_vel(P, slot, r); };
   auto fetchP = [&](int slot, PosRows& r) { fetch_pos(P, slot, r); };
   if (warm) {
-    colour_sweep<T, VelRows, (WIDE && T <= 512)>(cranges, ncc, c0, fetchV, [&](int slot, const VelRows& r) {
+    colour_sweep<Team, VelRows, PREFETCH>(tm, cranges, ncc, c0, fetchV, [&](int slot, const VelRows& r) {
       VCDev vc;
       unpack_vel(r, vc, M);
       warmStartContact(vc, bs);
@@ -780,8 +937,8 @@ __global__ void __launch_bounds__(T, kSolveBlocks<T, WIDE>) k_solve(KernelArgs a
   }
   for (int c = 0; c < njc; ++c) {
     int s = jranges[c], e = jranges[c + 1];
-    const int step = c == 63 ? 1 : T, i0 = c == 63 ? s : s + threadIdx.x;
-    if (c != 63 || threadIdx.x == 0)
+    const int step = c == 63 ? 1 : NT, i0 = c == 63 ? s : s + tid;
+    if (c != 63 || tid == 0)
       for (int i = i0; i < e; i += step) {
         const JointDev& J = a.joints[j0 + a.jorder[j0 + i]];
         if (sleepMode && !joint_awake(a, J)) {
@@ -790,19 +947,19 @@ __global__ void __launch_bounds__(T, kSolveBlocks<T, WIDE>) k_solve(KernelArgs a
         }
         jointInitSlot(J, a.jplanes, a.jstride, j0 + i, a.massd, a.lc, a.pos, jb, a.dt, dtRatio, warm);
       }
-    __syncthreads();
+    tm.sync();
   }
 
   // 6. velocity iterations: joints, then contacts (b2_island.cpp:327-346)
   for (int it = 0; it < a.vi; ++it) {
     for (int c = 0; c < njc; ++c) {
       int s = jranges[c], e = jranges[c + 1];
-      const int step = c == 63 ? 1 : T, i0 = c == 63 ? s : s + threadIdx.x;
-      if (c != 63 || threadIdx.x == 0)
+      const int step = c == 63 ? 1 : NT, i0 = c == 63 ? s : s + tid;
+      if (c != 63 || tid == 0)
         for (int i = i0; i < e; i += step) jointSolveVelocitySlot(a.jplanes, a.jstride, j0 + i, jb, a.dt, a.inv_dt);
-      __syncthreads();
+      tm.sync();
     }
-    colour_sweep<T, VelRows, (WIDE && T <= 512)>(cranges, ncc, c0, fetchV, [&](int slot, const VelRows& r) {
+    colour_sweep<Team, VelRows, PREFETCH>(tm, cranges, ncc, c0, fetchV, [&](int slot, const VelRows& r) {
       VCDev vc;
       unpack_vel(r, vc, M);
       solveContactVelocity(vc, bs);
@@ -811,8 +968,8 @@ __global__ void __launch_bounds__(T, kSolveBlocks<T, WIDE>) k_solve(KernelArgs a
   }
 
   // 7. StoreImpulses (b2_contact_solver.cpp:641-657); the joints' impulses back into their records
-  for (int i = threadIdx.x; i < nj; i += T) jointStoreImpulses(a.jplanes, a.jstride, j0 + i, a.joints[j0 + a.jorder[j0 + i]]);
-  for (int p = threadIdx.x; p < nsc; p += T) {
+  for (int i = tid; i < nj; i += NT) jointStoreImpulses(a.jplanes, a.jstride, j0 + i, a.joints[j0 + a.jorder[j0 + i]]);
+  for (int p = tid; p < nsc; p += NT) {
     int pc = (P.idx[c0 + p].x >> 24) & 15;
     float4 im = P.imp[c0 + p];
     b2g_manifold* m = &a.cman[P.cid[c0 + p]];
@@ -821,7 +978,7 @@ __global__ void __launch_bounds__(T, kSolveBlocks<T, WIDE>) k_solve(KernelArgs a
   }
 
   // 8. integrate positions (b2_island.cpp:349-385); the buffer switches to positions
-  for (int i = threadIdx.x; i < nb; i += T) {
+  for (int i = tid; i < nb; i += NT) {
     int bi = b0 + i;
     float4 p4 = a.pos[bi];
     if (a.btype[bi] == B2G_STATIC || (sleepMode && !(BS[i].x & B2G_BS_AWAKE))) {
@@ -850,7 +1007,7 @@ __global__ void __launch_bounds__(T, kSolveBlocks<T, WIDE>) k_solve(KernelArgs a
     if (bsm) bs[i] = make_float4(c.x, c.y, an, 0.0f);
     else a.pos[bi] = make_float4(c.x, c.y, an, 0.0f);
   }
-  __syncthreads();
+  tm.sync();
   float4* ps = bsm ? bs : a.pos + b0;
   float4* jp = ps - b0;
 
@@ -859,56 +1016,56 @@ __global__ void __launch_bounds__(T, kSolveBlocks<T, WIDE>) k_solve(KernelArgs a
   //    constraints were all okay in an iteration is done and no longer iterated.
   for (int it = 0; it < a.pi; ++it) {
     int okay = 1;
-    colour_sweep<T, PosRows, (WIDE && T <= 512)>(cranges, ncc, c0, fetchP, [&](int slot, const PosRows& r) {
+    colour_sweep<Team, PosRows, PREFETCH>(tm, cranges, ncc, c0, fetchP, [&](int slot, const PosRows& r) {
       VCDev vc;
       unpack_pos(r, vc, M);
       int root = 0;
       if (sleepMode) {
-        root = isl_root(SL, vc.indexA, vc.indexB);
-        if (isl_bits(SL, root) & B2G_ISL_DONE) return;
+        root = isl_root<S>(SL, vc.indexA, vc.indexB);
+        if (isl_bits<S>(SL, root) & B2G_ISL_DONE) return;
       }
       if (!(solveContactPosition(vc, ps) >= -3.0f * B2G_LINEAR_SLOP)) {
         okay = 0;
-        if (sleepMode) isl_store(&SL[root].z, it + 1);
+        if (sleepMode) isl_store<S>(&SL[root].z, it + 1);
       }
     });
     for (int c = 0; c < njc; ++c) {
       int s = jranges[c], e = jranges[c + 1];
-      const int step = c == 63 ? 1 : T, i0 = c == 63 ? s : s + threadIdx.x;
-      if (c != 63 || threadIdx.x == 0)
+      const int step = c == 63 ? 1 : NT, i0 = c == 63 ? s : s + tid;
+      if (c != 63 || tid == 0)
         for (int i = i0; i < e; i += step) {
           int root = 0;
           if (sleepMode) {
             const float4 h = a.jplanes[j0 + i];
             if (__float_as_int(h.w) & B2G_JV_ASLEEP) continue;
-            root = isl_root(SL, __float_as_int(h.x) - b0, __float_as_int(h.y) - b0);
-            if (isl_bits(SL, root) & B2G_ISL_DONE) continue;
+            root = isl_root<S>(SL, __float_as_int(h.x) - b0, __float_as_int(h.y) - b0);
+            if (isl_bits<S>(SL, root) & B2G_ISL_DONE) continue;
           }
           if (!jointSolvePositionSlot(a.jplanes, a.jstride, j0 + i, jp)) {
             okay = 0;
-            if (sleepMode) isl_store(&SL[root].z, it + 1);
+            if (sleepMode) isl_store<S>(&SL[root].z, it + 1);
           }
         }
-      __syncthreads();
+      tm.sync();
     }
     if (sleepMode) {
-      isl_sync();
+      tm.sync();
       int pending = 0;
-      for (int i = threadIdx.x; i < nb; i += T) {
-        const int ey = isl_bits(SL, i);
-        if (isl_label(SL, i) != i || !(ey & B2G_ISL_AWAKE) || (ey & B2G_ISL_DONE)) continue;
-        if (isl_load(&SL[i].z) == it + 1) pending = 1;
-        else isl_or(&SL[i].y, B2G_ISL_DONE);
+      for (int i = tid; i < nb; i += NT) {
+        const int ey = isl_bits<S>(SL, i);
+        if (isl_label<S>(SL, i) != i || !(ey & B2G_ISL_AWAKE) || (ey & B2G_ISL_DONE)) continue;
+        if (isl_load<S>(&SL[i].z) == it + 1) pending = 1;
+        else isl_or<S>(&SL[i].y, B2G_ISL_DONE);
       }
-      if (!__syncthreads_or(pending)) break;
-    } else if (__syncthreads_and(okay)) {
+      if (!tm.any(pending)) break;
+    } else if (tm.all(okay)) {
       break;
     }
   }
 
   // 10. transforms (b2Body::SynchronizeTransform, include/box2d/b2_body.h:957-961), finite check
   int bad = 0;
-  for (int i = threadIdx.x; i < nb; i += T) {
+  for (int i = tid; i < nb; i += NT) {
     int bi = b0 + i;
     if (a.btype[bi] == B2G_STATIC || (sleepMode && !(BS[i].x & B2G_BS_AWAKE))) continue;
     float4 p4 = ps[i];
@@ -921,15 +1078,15 @@ __global__ void __launch_bounds__(T, kSolveBlocks<T, WIDE>) k_solve(KernelArgs a
     if (!isfinite(p4.x) || !isfinite(p4.y) || !isfinite(p4.z) || !isfinite(v4.x) || !isfinite(v4.y) || !isfinite(v4.z))
       bad = 1;
   }
-  if (__syncthreads_or(bad) && threadIdx.x == 0) {  // the host freezes this world; the others go on
+  if (tm.any(bad) && tid == 0) {  // the host freezes this world; the others go on
     a.wfault[w] = 1;
     atomicOr(a.status, B2G_DEV_NONFINITE);
   }
 
   // 11. sleep timers (b2_island.cpp:444-483; orphans b2Island::SolveOrphan :230-249)
-  if (wfl & B2G_WF_ALLOW_SLEEP) sleep_islands<T>(a, b0, nb);
+  if (wfl & B2G_WF_ALLOW_SLEEP) sleep_islands(tm, a, b0, nb);
   if (a.events_on) {
-    for (int p = threadIdx.x; p < nsc; p += T) {
+    for (int p = tid; p < nsc; p += NT) {
       int pc = (P.idx[c0 + p].x >> 24) & 15;
       float4 im = P.imp[c0 + p];
       int2 f = a.cfix[P.cid[c0 + p]];
@@ -937,11 +1094,42 @@ __global__ void __launch_bounds__(T, kSolveBlocks<T, WIDE>) k_solve(KernelArgs a
       record_event(a, B2G_EVENT_POSTSOLVE, w, f.x - fo, f.y - fo, pc, ni, ti, 0);
     }
   }
-  if (threadIdx.x == 0 && a.dt > 0.0f) a.wg[w].z = a.inv_dt;
+  if (tid == 0 && a.dt > 0.0f) a.wg[w].z = a.inv_dt;
+}
+
+// One CTA per world: the size classes of the batch.
+template <int T, bool WIDE>
+__global__ void __launch_bounds__(T, kSolveBlocks<T, WIDE>) k_solve(KernelArgs a, int first, int smem_bytes) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int w = a.world_order[first + blockIdx.x];
+  if ((a.wflags[w] & B2G_WF_ACTIVE) == 0) return;
+  CtaTeam<T> tm;
+  solve_world<CtaTeam<T>, (WIDE && T <= 512)>(tm, a, w, smem, smem_bytes);
+}
+
+// One thread-block cluster of CS CTAs per world: the worlds above the largest CTA class. The
+// world's arrays stay in global memory; every colour barrier is a cluster barrier.
+template <int T, int CS>
+__global__ void __launch_bounds__(T, 1) k_solve_cluster(KernelArgs a, int first) {
+  __shared__ int votes[3];
+  ClusterTeam<T, CS> tm;
+  tm.r = (int)cluster_rank();
+  tm.vphase = 0;
+  tm.sphase = 0;
+  if (threadIdx.x < 3) votes[threadIdx.x] = 0;
+  tm.votes = cluster_map(votes, 0);
+  cluster_barrier();  // every CTA runs, and rank 0's votes are clear, before any remote access
+  const int w = a.world_order[first + (int)(blockIdx.x / CS)];
+  if ((a.wflags[w] & B2G_WF_ACTIVE) != 0) solve_world<ClusterTeam<T, CS>, (T <= 512)>(tm, a, w, nullptr, 0);
+  cluster_barrier();  // rank 0's shared memory outlives every remote access to it
 }
 
 // The wide build's launches and setup (solve_wide.cu).
 void launch_solve_class_wide(const KernelArgs& a, const SolveClass& c, cudaStream_t s);
 void solve_wide_setup(const int* smem_caps);
+// The cluster build (solve_cluster.cu): kClusterThreads threads per CTA, c.ctas CTAs per world.
+constexpr int kClusterThreads = 512;
+void launch_solve_class_cluster(const KernelArgs& a, const SolveClass& c, cudaStream_t s);
+void solve_cluster_setup();
 
 }  // namespace b2g

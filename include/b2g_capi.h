@@ -381,6 +381,15 @@ B2G_API int b2g_batch_get_solver_threads(b2g_batch* b, int32_t* threads);
  * per-world solve is faster. A size class runs the wide build when its worlds fill at most
  * `waves` waves of it (default: every class; 0 never). A tuning knob: results do not depend on it. */
 B2G_API int b2g_batch_set_solver_waves(b2g_batch* b, float waves);
+/* Worlds of more than 8192 bodies (single large scenes) are solved by a thread-block cluster of
+ * `ctas` CTAs of 512 threads each, one world per cluster, so that one world's colours run on
+ * that many SMs at once (the reference solves one island at a time on one core,
+ * src/dynamics/b2_world.cpp:526-647). ctas: -1 (default) the largest cluster the device runs
+ * (16, else 8); 2, 4, 8 or 16 (capped at that); 0 or 1 one CTA per world. A tuning knob: results
+ * do not depend on it. No reference counterpart. */
+B2G_API int b2g_batch_set_cluster_solve(b2g_batch* b, int32_t ctas);
+/* The CTAs per world that the batch's worlds above 8192 bodies are solved with (1: one CTA). */
+B2G_API int b2g_batch_get_cluster_solve(b2g_batch* b, int32_t* ctas);
 /* The broadphase keeps each world's tree between steps and refits its boxes; every `period`
  * broadphases (default 16; 1 = every one) it rebuilds all trees from sorted Morton codes, which
  * restores their spatial order. A tuning knob: the pairs found, and so the results, do not
@@ -470,8 +479,10 @@ B2G_API int b2g_collide(const b2g_shape* d_shape_a, const float* d_xf_a, const b
                         const float* d_xf_b, int32_t n, b2g_manifold* d_out, void* stream);
 /* Broadphase: every pair (i < j) of the n AABBs (lo.x, lo.y, hi.x, hi.y) that overlap with the
  * reference's inclusive test (include/box2d/b2_collision.h:270-276), sorted by (i, j), written
- * as i << 32 | j into d_pairs (capacity cap). *n_pairs receives the total, which may exceed cap
- * (then nothing beyond cap is written and B2G_E_CAPACITY is returned).
+ * as i << 32 | j into d_pairs (capacity cap). *n_pairs receives the total (64-bit: dense
+ * overlap passes 2^31 pairs from about 65 536 boxes), which may exceed cap (then nothing is
+ * written and B2G_E_CAPACITY is returned). A traversal that outgrows its stack also returns
+ * B2G_E_CAPACITY.
  * Replaces b2BroadPhase::UpdateAndQuery's pair report (include/box2d/b2_broad_phase.h:252-343). */
 B2G_API int b2g_pairs(const float* d_aabbs, int32_t n, uint64_t* d_pairs, int64_t cap,
                       int64_t* n_pairs, void* stream);
@@ -482,10 +493,12 @@ B2G_API int b2g_pairs(const float* d_aabbs, int32_t n, uint64_t* d_pairs, int64_
  * application that owns the device's memory budget. No counterpart in the reference (its
  * broadphase runs on the CPU and allocates from its own pools).
  * Its scratch is a fixed 16 MiB array in device memory that every GPU loading the library keeps
- * until the process exits; n may be at most B2G_PAIRS_STATIC_MAX (larger n returns
- * B2G_E_CAPACITY without touching anything). The first call on a device looks up that array's
- * device address, so make it before any stream capture. All calls share the array: calls that
- * overlap on the GPU (two streams, or two host threads) race and must be serialised by the caller.
+ * until the process exits (68 bytes per AABB plus the radix sort's temporary storage, which fits
+ * at the maximum); n may be at most B2G_PAIRS_STATIC_MAX (larger n returns B2G_E_CAPACITY without
+ * touching anything). The first call on a device looks up that array's device address, so make
+ * it before any stream capture. All calls share the array: calls that overlap on the GPU (two
+ * streams, or two host threads) race and must be serialised by the caller. Like b2g_pairs, a call
+ * waits for `stream` twice before it returns (once to read the pair total, once at the end).
  * Same outputs, capacity rule and status codes as b2g_pairs. */
 #define B2G_PAIRS_STATIC_MAX 131072
 B2G_API int b2g_pairs_static(const float* d_aabbs, int32_t n, uint64_t* d_pairs, int64_t cap,
@@ -495,12 +508,13 @@ B2G_API int b2g_pairs_static(const float* d_aabbs, int32_t n, uint64_t* d_pairs,
 /* Builds one of the seeded benchmark scenes into `world` through the b2World facade calls
  * (box2d-optimized_gb300/scenes/scenes.h). kind: 0 pyramid(rows=n, density=p0, friction=p1),
  * 1 mixed drop(n bodies), 2 chains over pile(n chains, 20 links, p0 circles),
- * 3 batch world(n bodies), with `seed`. counts[3] = bodies, fixtures, joints. */
+ * 3 batch world(n bodies), 4 joint zoo(n rigs), 5 slider rigs(n rigs), with `seed`. counts[3] = bodies, fixtures, joints. */
 #define B2G_SCENE_PYRAMID 0
 #define B2G_SCENE_MIXED_DROP 1
 #define B2G_SCENE_CHAINS 2
 #define B2G_SCENE_BATCH_WORLD 3
 #define B2G_SCENE_JOINTS 4      /* rigs of weld, wheel, motor, friction, mouse and pulley joints */
+#define B2G_SCENE_SLIDERS 5     /* rigs of distance and prismatic joints (n rigs) */
 B2G_API int b2g_scene_build(b2g_batch* b, int32_t world, int32_t kind, uint32_t seed, int32_t n,
                             float p0, float p1, int32_t* counts);
 B2G_API int b2g_batch_world_params(uint32_t seed, int32_t* n_bodies, float* gx, float* gy);

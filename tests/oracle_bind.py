@@ -182,6 +182,10 @@ class Oracle:
             "orc_set_libm_trig": ([i32], None),
             "orc_pairs": ([P(f32), i32, P(C.c_uint64), C.c_int64], C.c_int64),
             "orc_worlds_step_parallel": ([P(vp), i32, f32, i32, i32, i32, i32], C.c_double),
+            "orc_scene_world": ([i32, u32, i32, f32, f32, f32, f32, P(i32)], vp),
+            "orc_scene_records": ([i32, u32, i32, f32, f32, P(i32), P(G.Body), i32, P(G.Fixture), i32,
+                                   P(G.Joint), i32], i32),
+            "orc_batch_world_params": ([u32, P(i32), P(f32), P(f32)], C.c_int),
         }
         for name, (a, r) in sig.items():
             fn = getattr(L, name)
@@ -191,13 +195,37 @@ class Oracle:
     def __getattr__(self, name):
         return getattr(self.lib, name)
 
+    def batch_world_params(self, seed):
+        """(bodies, gx, gy) of world `seed` of the batched workload."""
+        n, gx, gy = i32(), f32(), f32()
+        self.lib.orc_batch_world_params(seed, C.byref(n), C.byref(gx), C.byref(gy))
+        return n.value, gx.value, gy.value
+
+    def scene_records(self, kind, seed=1, n=20, p0=1.0, p1=0.6):
+        """(bodies, fixtures, joints) records the oracle's scene builder makes for a recipe."""
+        sz = (i32 * 3)()
+        self.lib.orc_scene_records(kind, seed, n, p0, p1, sz, None, 0, None, 0, None, 0)
+        B, F, J = (G.Body * max(sz[0], 1))(), (G.Fixture * max(sz[1], 1))(), (G.Joint * max(sz[2], 1))()
+        self.lib.orc_scene_records(kind, seed, n, p0, p1, sz, B, sz[0], F, sz[1], J, sz[2])
+        return B[:sz[0]], F[:sz[1]], J[:sz[2]]
+
 
 class OracleWorld:
-    """A world of the CPU restatement loaded from exported records."""
+    """A world of the CPU restatement loaded from exported records (or, with `scene`, built by
+    the oracle's own scene builder: scene = (kind, seed, n, p0, p1))."""
 
-    def __init__(self, orc: Oracle, gravity, bodies, fixtures, joints=(), contacts=(),
-                 inv_dt0=0.0):
+    def __init__(self, orc: Oracle, gravity, bodies=(), fixtures=(), joints=(), contacts=(),
+                 inv_dt0=0.0, scene=None):
         self.orc = orc
+        self._raycast_fn, self._query_fn = orc.orc_world_raycast, orc.orc_world_query_aabb
+        if scene is not None:
+            kind, seed, n, p0, p1 = scene
+            counts = (i32 * 3)()
+            self.h = orc.orc_scene_world(kind, seed, n, p0, p1, gravity[0], gravity[1], counts)
+            if not self.h:
+                raise RuntimeError(f"orc_scene_world: unknown scene kind {kind}")
+            self.counts = tuple(counts)
+            return
         self.h = orc.orc_world_new(gravity[0], gravity[1])
         nb, nf, nj, nc = len(bodies), len(fixtures), len(joints), len(contacts)
         B = (G.Body * max(nb, 1))(*bodies)

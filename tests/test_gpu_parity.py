@@ -74,9 +74,67 @@ def _rollout(lib, orc, kind, n, seed=1, p0=1.0, p1=0.6, steps=60, vi=8, pi=3, gr
 
 
 def test_pyramid_rollout_bit_exact(lib, orc):
-    # 20-row pyramid (210 boxes, density 1, friction 0.6), 8/3 iterations
-    nc = _rollout(lib, orc, G.SCENE_PYRAMID, 20, steps=120)
+    # the 20-row pyramid configuration (210 boxes, density 1, friction 0.6), 8/3 iterations,
+    # its full 256 steps
+    nc = _rollout(lib, orc, G.SCENE_PYRAMID, 20, steps=256)
     assert nc > 300
+
+
+@pytest.mark.parametrize("n,seed,vi,pi", [(3, 9, 8, 3), (2, 17, 10, 4)])
+def test_slider_rigs_rollout_bit_exact(lib, orc, n, seed, vi, pi):
+    # distance joints (rigid rods, springs with min/max length, slack ropes) and prismatic joints
+    # (limits, motors, a piston between two dynamic bodies): bodies every step, joint impulses
+    # (including the limit and motor impulses) and contacts at the end
+    _rollout(lib, orc, G.SCENE_SLIDERS, n, seed=seed, steps=240, vi=vi, pi=pi)
+
+
+def _state_np(records_bytes, n):
+    return np.frombuffer(records_bytes, dtype=np.uint8).reshape(n, -1)[:, :40]
+
+
+def _rollout_large(lib, orc, kind, n, seed, p0, steps, checks, vi, pi):
+    """One large world on the GPU and in the oracle, body states compared bit for bit at the
+    `checks` steps (the whole record array at once), contact lists and joint impulses at the end."""
+    batch = G.Batch(lib, device=0)
+    w = batch.add_world(0.0, -10.0)
+    batch.set_flags(w, allow_sleep=False, warm_starting=True, continuous=False)
+    batch.scene(w, kind, seed=seed, n=n, p0=p0, p1=0.6)
+    nb = batch.sizes(w)[0]
+    ow = ob.OracleWorld(orc, (0.0, -10.0), batch.bodies(w), batch.fixtures(w), batch.joints(w))
+    done = 0
+    for at in checks:
+        batch.step_n(at - done, 1 / 60, vi, pi, use_graph=True)
+        ow.step(at - done, 1 / 60, vi, pi)
+        done = at
+        g = bytes((G.Body * nb)(*batch.bodies(w)))
+        o = bytes((G.Body * nb)(*ow.bodies()))
+        if g != o:
+            diff = np.nonzero((_state_np(g, nb) != _state_np(o, nb)).any(axis=1))[0]
+            raise AssertionError(f"step {at}: {len(diff)} bodies differ, first {diff[0]}: "
+                                 f"{_first_diff(batch.bodies(w)[diff[0]:diff[0] + 1], ow.bodies()[diff[0]:diff[0] + 1])}")
+    gc, oc = batch.contacts(w), ow.contacts()
+    assert [_contact_key(x) for x in gc] == [_contact_key(y) for y in oc], "contact lists differ"
+    for x, y in zip(batch.joints(w), ow.joints()):
+        assert list(x.impulse) == list(y.impulse)
+        assert (x.motor_impulse, x.lower_impulse, x.upper_impulse) == (y.motor_impulse, y.lower_impulse, y.upper_impulse)
+    touching = sum(1 for c in gc if c.flags & 2)
+    batch.close()
+    return touching
+
+
+def test_config_single_large_world_mixed_drop(lib, orc):
+    """The single-large-world configuration at size: 20 000 boxes, circles and 3-8-gons dropped
+    from a 200 x 400 m grid into the U container, 8/3 iterations, its full 512 steps (the bottom
+    rows have landed and piled up by then)."""
+    touching = _rollout_large(lib, orc, G.SCENE_MIXED_DROP, 20000, 1, 0.0, 512, (64, 192, 320, 512), 8, 3)
+    assert touching > 5000
+
+
+def test_config_chains_over_pile(lib, orc):
+    """The joints + dense contact configuration at size: 2 000 chains of 20 boxes on revolute
+    joints (limits, motors) over 10 000 circles, 10/4 iterations, 256 steps."""
+    touching = _rollout_large(lib, orc, G.SCENE_CHAINS, 2000, 1, 10000.0, 256, (64, 128, 256), 10, 4)
+    assert touching > 5000
 
 
 def test_mixed_drop_rollout_bit_exact(lib, orc):
@@ -197,6 +255,55 @@ def test_solver_threads_do_not_change_results(lib):
         out.append([_state_bytes(b.bodies(w)) for w in ws])
         b.close()
     assert out[0] == out[1] == out[2]
+
+
+@pytest.mark.parametrize("kind,n,p0,vi,pi", [(G.SCENE_PYRAMID, 161, 1.0, 8, 3),
+                                             (G.SCENE_CHAINS, 420, 2000.0, 10, 4)])
+def test_cluster_solve_equals_one_cta(lib, kind, n, p0, vi, pi):
+    """Worlds above 8192 bodies (a 13 041-box pyramid; 420 revolute chains over 2 000 circles)
+    solved by thread-block clusters of 16, 8 and 2 CTAs give the bits of one CTA per world, beside
+    a small world in the same batch."""
+    out = []
+    for ctas in (1, 16, 8, 2):
+        b = G.Batch(lib, device=0)
+        b.cluster_solve(ctas)
+        w = b.add_world(0.0, -10.0)
+        b.set_flags(w)
+        b.scene(w, kind, seed=3, n=n, p0=p0, p1=0.6)
+        small = b.add_world(0.0, -10.0)
+        b.set_flags(small)
+        b.scene(small, G.SCENE_PYRAMID, n=12, p0=1.0, p1=0.6)
+        for _ in range(40):
+            b.step(1 / 60, vi, pi)
+        b.step_n(20, 1 / 60, vi, pi, use_graph=True)
+        out.append((_state_bytes(b.bodies(w)), _state_bytes(b.bodies(small)),
+                    [list(j.impulse) for j in b.joints(w)]))
+        b.close()
+    assert out[0] == out[1] == out[2] == out[3]
+
+
+def test_cluster_solve_sleep_mode_bit_exact(lib, orc):
+    """A 9 000-body batch world (chains over a pile) with sleeping allowed, solved by a cluster:
+    the island union-find, the per-island position exit and the sleep timers run across the
+    cluster's SMs (device checks verify the labels every step); body states, awake flags and
+    sleep timers equal the oracle's at every check."""
+    batch = G.Batch(lib, device=0)
+    batch.set_debug_checks(True)
+    w = _sleep_world(batch, G.SCENE_BATCH_WORLD, 9000, 7, 0.0)
+    ow = ob.OracleWorld(orc, (0.0, -10.0), batch.bodies(w), batch.fixtures(w), batch.joints(w))
+    ow.set_sleep(True)
+    done = 0
+    for at in (100, 200, 300, 400):
+        batch.step_n(at - done, 1 / 60, 8, 3)
+        ow.step(at - done, 1 / 60, 8, 3)
+        done = at
+        g, o = batch.bodies(w), ow.bodies()
+        assert _state_bytes(g) == _state_bytes(o), f"step {at}: {_first_diff(g, o)}"
+        assert _awake_flags(g) == _awake_flags(o), f"step {at}: awake flags differ"
+        times = batch.sleep_times(w)
+        assert times == ow.sleep_times(), f"step {at}: sleep timers differ"
+    assert sum(1 for t in times if t > 0.0) > 100  # resting bodies are being timed
+    batch.close()
 
 
 def test_solver_build_and_tree_period_do_not_change_results(lib):
