@@ -241,7 +241,8 @@ class Lib:
         "b2g_world_snapshot", "b2g_world_restore", "b2g_server_cancel", "b2g_body_set_awake",
         "b2g_bodies_sleep_time_read", "b2g_world_get_flags", "b2g_server_batch", "b2g_step_begin",
         "b2g_step_poll", "b2g_step_end", "b2g_batch_stage", "b2g_server_set_builders", "b2g_batch_set_solver_waves", "b2g_batch_set_tree_rebuild_period",
-        "b2g_batch_set_cluster_solve", "b2g_batch_get_cluster_solve",
+        "b2g_batch_set_cluster_solve", "b2g_batch_get_cluster_solve", "b2g_events_drain_world",
+        "b2g_bodies_remove", "b2g_fixtures_remove", "b2g_joints_remove",
     ]
 
     def __init__(self, path: os.PathLike | str | None = None):
@@ -283,6 +284,10 @@ class Lib:
             "b2g_contacts_read": ([vp, i32, P(Contact), i32, P(i32)], C.c_int),
             "b2g_events_enable": ([vp, i32], C.c_int),
             "b2g_events_drain": ([vp, P(Event), i32, P(i32)], C.c_int),
+            "b2g_events_drain_world": ([vp, i32, P(Event), i32, P(i32)], C.c_int),
+            "b2g_bodies_remove": ([vp, i32, P(i32), i32, P(Event), i32, P(i32)], C.c_int),
+            "b2g_fixtures_remove": ([vp, i32, P(i32), i32, P(Event), i32, P(i32)], C.c_int),
+            "b2g_joints_remove": ([vp, i32, P(i32), i32], C.c_int),
             "b2g_profile_get": ([vp, P(Profile)], C.c_int),
             "b2g_batch_set_solver_threads": ([vp, P(i32)], C.c_int),
             "b2g_batch_get_solver_threads": ([vp, P(i32)], C.c_int),
@@ -564,6 +569,29 @@ class Batch:
         n = C.c_int32()
         arr = (Event * cap)()
         self.lib.check(self.lib.b2g_events_drain(self.h, arr, cap, C.byref(n)), "b2g_events_drain")
+        return arr[:n.value]
+
+    def remove(self, world, bodies=(), fixtures=(), joints=(), cap=1 << 16):
+        """Removes bodies, then fixtures, then joints of `world` (indices as they are before each
+        call); returns the End events of the touching contacts destroyed."""
+        ended = []
+        for fn, ids in ((self.lib.b2g_bodies_remove, bodies), (self.lib.b2g_fixtures_remove, fixtures)):
+            if ids:
+                arr = (C.c_int32 * len(ids))(*ids)
+                ev = (Event * cap)()
+                n = C.c_int32()
+                self.lib.check(fn(self.h, world, arr, len(ids), ev, cap, C.byref(n)), "remove")
+                ended += ev[:min(n.value, cap)]
+        if joints:
+            arr = (C.c_int32 * len(joints))(*joints)
+            self.lib.check(self.lib.b2g_joints_remove(self.h, world, arr, len(joints)), "b2g_joints_remove")
+        return ended
+
+    def world_events(self, world, cap=1 << 20):
+        """World `world`'s listener events of the last step (b2g_events_drain_world)."""
+        n = C.c_int32()
+        arr = (Event * cap)()
+        self.lib.check(self.lib.b2g_events_drain_world(self.h, world, arr, cap, C.byref(n)), "b2g_events_drain_world")
         return arr[:n.value]
 
     def profile(self) -> Profile:

@@ -1856,6 +1856,173 @@ B2G_API int b2g_joints_add(b2g_batch* b, int32_t world, const b2g_joint_def* def
   return B2G_OK;
 }
 
+// ---- structural removal (b2World::DestroyBody / DestroyJoint, b2Body::DestroyFixture)
+//
+// Removes the marked bodies, fixtures and joints of one world from its host records and
+// renumbers the rest (creation order is kept), as the reference's destroy calls do:
+//  * destroying a body destroys its joints, contacts and fixtures (src/dynamics/b2_world.cpp:178-266);
+//  * destroying a contact that was touching ends it (EndContact, b2_contact_manager.cpp:48-61), and
+//    one with manifold points and no sensor wakes both bodies (b2_contact.cpp:80-91);
+//  * destroying a joint wakes both bodies (b2_world.cpp:326-410);
+//  * destroying a fixture resets its body's mass data (b2_body.cpp:280-350).
+// The End callbacks of the destroyed contacts are returned at once (the reference calls them
+// inside the destroy call), with the fixture indices from before the removal. The world is
+// re-uploaded by its next step; the surviving contacts keep their manifolds and impulses.
+static void wake_body(HostWorld& w, int bi) {
+  b2g_body& r = w.bodies[bi];
+  if (r.type == B2G_STATIC) return;
+  r.flags |= B2G_BODY_AWAKE;
+  if ((size_t)bi < w.body_sleep.size()) w.body_sleep[bi] = 0.0f;
+}
+
+static int remove_structure(Batch* b, int32_t world, std::vector<char> deadBody, std::vector<char> deadFix,
+                            std::vector<char> deadJoint, b2g_event* ended, int32_t cap, int32_t* n_ended) {
+  if (world < b->NW) TRY(begin_edit(b));
+  else b->tail_pack.valid = false;  // not on the device yet: its host records are the state
+  HostWorld& w = b->worlds[world];
+  const int nb = (int)w.bodies.size(), nf = (int)w.fixtures.size(), nj = (int)w.joints.size();
+  for (int f = 0; f < nf; ++f)
+    if (deadBody[w.fixtures[f].body]) deadFix[f] = 1;
+  for (int j = 0; j < nj; ++j)
+    if (deadBody[w.joints[j].def.body_a] || deadBody[w.joints[j].def.body_b]) deadJoint[j] = 1;
+  w.body_sleep.resize(nb, 0.0f);
+  for (int j = 0; j < nj; ++j)
+    if (deadJoint[j]) {
+      wake_body(w, w.joints[j].def.body_a);
+      wake_body(w, w.joints[j].def.body_b);
+    }
+  // contacts: End for the touching ones, wakes for those with points
+  int32_t ne = 0;
+  std::vector<b2g_contact> kept;
+  kept.reserve(w.contacts.size());
+  for (const b2g_contact& c : w.contacts) {
+    if (!deadFix[c.fixture_a] && !deadFix[c.fixture_b]) {
+      kept.push_back(c);
+      continue;
+    }
+    if ((c.flags & B2G_CONTACT_TOUCHING) && ended && ne < cap) {
+      b2g_event e;
+      memset(&e, 0, sizeof(e));
+      e.kind = B2G_EVENT_END;
+      e.world = world;
+      e.fixture_a = c.fixture_a;
+      e.fixture_b = c.fixture_b;
+      ended[ne] = e;
+    }
+    if (c.flags & B2G_CONTACT_TOUCHING) ++ne;
+    const b2g_fixture& fa = w.fixtures[c.fixture_a];
+    const b2g_fixture& fb = w.fixtures[c.fixture_b];
+    if (c.manifold.point_count > 0 && !fa.is_sensor && !fb.is_sensor) {
+      wake_body(w, fa.body);
+      wake_body(w, fb.body);
+    }
+  }
+  if (n_ended) *n_ended = ne;
+  // renumbering maps (-1: removed)
+  std::vector<int> bmap(nb), fmap(nf), jmap(nj);
+  int k = 0;
+  for (int i = 0; i < nb; ++i) bmap[i] = deadBody[i] ? -1 : k++;
+  k = 0;
+  for (int i = 0; i < nf; ++i) fmap[i] = deadFix[i] ? -1 : k++;
+  k = 0;
+  for (int i = 0; i < nj; ++i) jmap[i] = deadJoint[i] ? -1 : k++;
+  std::vector<int> massReset;
+  for (int f = 0; f < nf; ++f)
+    if (deadFix[f] && !deadBody[w.fixtures[f].body] && w.fixtures[f].density > 0.0f) massReset.push_back(w.fixtures[f].body);
+  // compact every per-body, per-fixture and per-joint array
+  auto compact = [](auto& v, const std::vector<int>& map) {
+    size_t o = 0;
+    for (size_t i = 0; i < map.size() && i < v.size(); ++i) {
+      if (map[i] < 0) continue;
+      if (o != i) v[o] = std::move(v[i]);  // never self-move: it would empty a vector element
+      ++o;
+    }
+    v.resize(o);
+  };
+  compact(w.bodies, bmap);
+  compact(w.body_sleep, bmap);
+  compact(w.body_user, bmap);
+  compact(w.body_fixtures, bmap);
+  compact(w.fixtures, fmap);
+  compact(w.fixture_user, fmap);
+  compact(w.joints, jmap);
+  for (b2g_fixture& f : w.fixtures) f.body = bmap[f.body];
+  for (b2g_joint& j : w.joints) {
+    j.def.body_a = bmap[j.def.body_a];
+    j.def.body_b = bmap[j.def.body_b];
+  }
+  for (std::vector<int>& lst : w.body_fixtures) {
+    size_t o = 0;
+    for (int f : lst)
+      if (fmap[f] >= 0) lst[o++] = fmap[f];
+    lst.resize(o);
+  }
+  for (b2g_contact& c : kept) {
+    c.fixture_a = fmap[c.fixture_a];
+    c.fixture_b = fmap[c.fixture_b];
+  }
+  w.contacts.swap(kept);
+  for (int bi : massReset) reset_mass_data(w, bmap[bi]);
+  // undelivered events of this world name fixtures by their old indices
+  std::vector<b2g_event>& ev = b->host_events;
+  size_t o = 0;
+  for (size_t i = 0; i < ev.size(); ++i) {
+    b2g_event e = ev[i];
+    if (e.world == world) {
+      if (fmap[e.fixture_a] < 0 || fmap[e.fixture_b] < 0) continue;
+      e.fixture_a = fmap[e.fixture_a];
+      e.fixture_b = fmap[e.fixture_b];
+    }
+    ev[o++] = e;
+  }
+  ev.resize(o);
+  return B2G_OK;
+}
+
+static int remove_args_ok(Batch* b, int32_t world, const int32_t* ids, int32_t n, size_t count) {
+  if (!world_index_ok(b, world) || n < 0 || (n > 0 && !ids)) return B2G_E_INVALID_ARG;
+  for (int32_t i = 0; i < n; ++i)
+    if (ids[i] < 0 || (size_t)ids[i] >= count) {
+      set_error(b, "index out of range in a removal");
+      return B2G_E_INVALID_ARG;
+    }
+  return B2G_OK;
+}
+
+B2G_API int b2g_bodies_remove(b2g_batch* b, int32_t world, const int32_t* bodies, int32_t n, b2g_event* ended,
+                              int32_t cap, int32_t* n_ended) {
+  if (n_ended) *n_ended = 0;
+  if (!b || cap < 0 || (cap > 0 && !ended)) return B2G_E_INVALID_ARG;
+  TRY(remove_args_ok(b, world, bodies, n, world_index_ok(b, world) ? b->worlds[world].bodies.size() : 0));
+  if (b->in_step) return locked(b);
+  const HostWorld& w = b->worlds[world];
+  std::vector<char> db(w.bodies.size(), 0), df(w.fixtures.size(), 0), dj(w.joints.size(), 0);
+  for (int32_t i = 0; i < n; ++i) db[bodies[i]] = 1;
+  return remove_structure(b, world, std::move(db), std::move(df), std::move(dj), ended, cap, n_ended);
+}
+
+B2G_API int b2g_fixtures_remove(b2g_batch* b, int32_t world, const int32_t* fixtures, int32_t n, b2g_event* ended,
+                                int32_t cap, int32_t* n_ended) {
+  if (n_ended) *n_ended = 0;
+  if (!b || cap < 0 || (cap > 0 && !ended)) return B2G_E_INVALID_ARG;
+  TRY(remove_args_ok(b, world, fixtures, n, world_index_ok(b, world) ? b->worlds[world].fixtures.size() : 0));
+  if (b->in_step) return locked(b);
+  const HostWorld& w = b->worlds[world];
+  std::vector<char> db(w.bodies.size(), 0), df(w.fixtures.size(), 0), dj(w.joints.size(), 0);
+  for (int32_t i = 0; i < n; ++i) df[fixtures[i]] = 1;
+  return remove_structure(b, world, std::move(db), std::move(df), std::move(dj), ended, cap, n_ended);
+}
+
+B2G_API int b2g_joints_remove(b2g_batch* b, int32_t world, const int32_t* joints, int32_t n) {
+  if (!b) return B2G_E_INVALID_ARG;
+  TRY(remove_args_ok(b, world, joints, n, world_index_ok(b, world) ? b->worlds[world].joints.size() : 0));
+  if (b->in_step) return locked(b);
+  const HostWorld& w = b->worlds[world];
+  std::vector<char> db(w.bodies.size(), 0), df(w.fixtures.size(), 0), dj(w.joints.size(), 0);
+  for (int32_t i = 0; i < n; ++i) dj[joints[i]] = 1;
+  return remove_structure(b, world, std::move(db), std::move(df), std::move(dj), nullptr, 0, nullptr);
+}
+
 B2G_API int b2g_world_sizes(b2g_batch* b, int32_t world, int32_t* bodies, int32_t* fixtures, int32_t* joints,
                             int32_t* contacts) {
   if (!world_index_ok(b, world)) return B2G_E_INVALID_ARG;
@@ -2246,21 +2413,38 @@ B2G_API int b2g_events_enable(b2g_batch* b, int32_t enable) {
   return B2G_OK;
 }
 
-B2G_API int b2g_events_drain(b2g_batch* b, b2g_event* out, int32_t cap, int32_t* n) {
-  if (!b || !n) return B2G_E_INVALID_ARG;
-  // delivery order: grouped per world; End (broadphase), Begin, End, PreSolve, PostSolve; then
-  // by fixture pair
-  std::vector<b2g_event>& ev = b->host_events;
+// Delivery order of the step's events: grouped per world; Begin, End, PreSolve, PostSolve; then
+// by fixture pair.
+static void sort_events(std::vector<b2g_event>& ev) {
   std::stable_sort(ev.begin(), ev.end(), [](const b2g_event& x, const b2g_event& y) {
     if (x.world != y.world) return x.world < y.world;
     if (x.kind != y.kind) return x.kind < y.kind;
     if (x.fixture_a != y.fixture_a) return x.fixture_a < y.fixture_a;
     return x.fixture_b < y.fixture_b;
   });
+}
+
+B2G_API int b2g_events_drain(b2g_batch* b, b2g_event* out, int32_t cap, int32_t* n) {
+  if (!b || !n) return B2G_E_INVALID_ARG;
+  std::vector<b2g_event>& ev = b->host_events;
+  sort_events(ev);
   *n = (int32_t)std::min<size_t>(ev.size(), (size_t)std::max(cap, 0));
   if (out)
     for (int i = 0; i < *n; ++i) out[i] = ev[i];
   ev.erase(ev.begin(), ev.begin() + *n);
+  return B2G_OK;
+}
+
+B2G_API int b2g_events_drain_world(b2g_batch* b, int32_t world, b2g_event* out, int32_t cap, int32_t* n) {
+  if (!world_index_ok(b, world) || !n || cap < 0 || (cap > 0 && !out)) return B2G_E_INVALID_ARG;
+  std::vector<b2g_event>& ev = b->host_events;
+  sort_events(ev);
+  auto lo = std::lower_bound(ev.begin(), ev.end(), world, [](const b2g_event& e, int32_t w) { return e.world < w; });
+  auto hi = std::upper_bound(lo, ev.end(), world, [](int32_t w, const b2g_event& e) { return w < e.world; });
+  const int32_t take = (int32_t)std::min<ptrdiff_t>(hi - lo, cap);
+  for (int32_t i = 0; i < take; ++i) out[i] = lo[i];
+  ev.erase(lo, lo + take);
+  *n = take;
   return B2G_OK;
 }
 

@@ -6,6 +6,7 @@
 #include <algorithm>
 #include <map>
 #include <stdexcept>
+#include <typeinfo>
 
 #include "../include/box2d/box2d.h"
 #include "../scenes/scenes_joints.h"
@@ -540,7 +541,8 @@ b2Body* b2World::CreateBody(const b2BodyDef* def) {
   d.user_data = def->userData.pointer;
   int32_t id = -1;
   if (b2g_bodies_add(m_batch, m_index, &d, 1, &id) != B2G_OK) return nullptr;
-  b2Body* prev = m_bodies.empty() ? nullptr : &m_bodies.back();
+  b2Body* last = nullptr;  // the last live body, which links to the new one
+  for (b2Body* x = m_bodyHead; x; x = x->m_next) last = x;
   m_bodies.emplace_back();
   b2Body* b = &m_bodies.back();
   b->m_world = this;
@@ -548,10 +550,127 @@ b2Body* b2World::CreateBody(const b2BodyDef* def) {
   b->m_type = def->type;
   b->m_fixedRotation = def->fixedRotation;
   b->m_userData = def->userData;
-  if (prev) prev->m_next = b;
+  if (last) last->m_next = b;
+  else m_bodyHead = b;
+  ++m_bodyCount;
   InvalidateCaches();
   return b;
 }
+
+void b2World::SetContactFilter(b2ContactFilter* filter) {
+  m_filter = filter;
+  m_filterUnsupported = filter && typeid(*filter) != typeid(b2ContactFilter);
+}
+
+// EndContact for the contacts a removal destroyed (the engine's End records carry the fixture
+// indices from before the removal), with the contact as it was.
+void b2World::EndContacts(const std::vector<b2g_event>& ended, int32 n, const std::vector<b2Contact>& before) {
+  if (!m_listener) return;
+  std::map<std::pair<int, int>, const b2Contact*> byPair;
+  for (const b2Contact& c : before) byPair[{c.m_fixtureA->m_index, c.m_fixtureB->m_index}] = &c;
+  for (int32 i = 0; i < n && i < (int32)ended.size(); ++i) {
+    auto it = byPair.find({ended[i].fixture_a, ended[i].fixture_b});
+    if (it == byPair.end()) continue;
+    b2Contact c = *it->second;
+    c.m_next = nullptr;
+    m_listener->EndContact(&c);
+  }
+}
+
+// Indices follow the engine's renumbering: live bodies, fixtures and joints keep their creation
+// order and are numbered 0, 1, ... again; the fixture index table is rebuilt.
+void b2World::Renumber() {
+  int32 k = 0;
+  for (b2Body* b = m_bodyHead; b; b = b->m_next) b->m_index = k++;
+  m_bodyCount = k;
+  std::vector<b2Fixture*> live;
+  for (b2Fixture* f : m_fixtureIndex)
+    if (f->m_index >= 0) live.push_back(f);
+  for (size_t i = 0; i < live.size(); ++i) live[i]->m_index = (int32)i;
+  m_fixtureIndex.swap(live);
+  for (size_t i = 0; i < m_joints.size(); ++i) {
+    m_joints[i]->m_index = (int32)i;
+    m_joints[i]->m_next = i + 1 < m_joints.size() ? m_joints[i + 1].get() : nullptr;
+  }
+  InvalidateCaches();
+}
+
+void b2World::DestroyBody(b2Body* body) {
+  if (!body || body->m_index < 0 || body->m_world != this) return;
+  // the joints it takes along (SayGoodbye first, as the reference does)
+  for (auto& j : m_joints)
+    if ((j->m_bodyA == body || j->m_bodyB == body) && m_destruction) m_destruction->SayGoodbye(j.get());
+  for (b2Fixture* f = body->m_fixtureList; f; f = f->m_next)
+    if (m_destruction) m_destruction->SayGoodbye(f);
+  std::vector<b2Contact> before;
+  if (m_listener) {
+    GetContactListStart();
+    before = m_contacts;
+  }
+  std::vector<b2g_event> ended((size_t)std::max(GetContactCount(), 1));
+  int32_t ne = 0;
+  const int32_t idx = body->m_index;
+  m_lastStatus = b2g_bodies_remove(m_batch, m_index, &idx, 1, ended.data(), (int32_t)ended.size(), &ne);
+  if (m_lastStatus != B2G_OK) return;
+  EndContacts(ended, ne, before);
+  // drop the body's joints, fixtures and the body itself from the facade's lists
+  for (size_t i = 0; i < m_joints.size();) {
+    if (m_joints[i]->m_bodyA == body || m_joints[i]->m_bodyB == body) m_joints.erase(m_joints.begin() + i);
+    else ++i;
+  }
+  for (b2Fixture* f = body->m_fixtureList; f; f = f->m_next) f->m_index = -1;
+  b2Body* prev = nullptr;
+  for (b2Body* x = m_bodyHead; x && x != body; x = x->m_next) prev = x;
+  if (prev) prev->m_next = body->m_next;
+  else m_bodyHead = body->m_next;
+  body->m_next = nullptr;
+  body->m_fixtureList = nullptr;
+  body->m_index = -1;
+  Renumber();
+}
+
+void b2World::DestroyJoint(b2Joint* joint) {
+  if (!joint || joint->m_world != this) return;
+  size_t i = 0;
+  while (i < m_joints.size() && m_joints[i].get() != joint) ++i;
+  if (i == m_joints.size()) return;
+  const int32_t idx = joint->m_index;
+  m_lastStatus = b2g_joints_remove(m_batch, m_index, &idx, 1);
+  if (m_lastStatus != B2G_OK) return;
+  m_joints.erase(m_joints.begin() + i);
+  Renumber();
+}
+
+void b2Body::DestroyFixture(b2Fixture* fixture) {
+  if (!fixture || fixture->m_body != this || fixture->m_index < 0) return;
+  b2World* w = m_world;
+  std::vector<b2Contact> before;
+  if (w->m_listener) {
+    w->GetContactListStart();
+    before = w->m_contacts;
+  }
+  std::vector<b2g_event> ended((size_t)std::max(w->GetContactCount(), 1));
+  int32_t ne = 0;
+  const int32_t idx = fixture->m_index;
+  w->m_lastStatus = b2g_fixtures_remove(w->m_batch, w->m_index, &idx, 1, ended.data(), (int32_t)ended.size(), &ne);
+  if (w->m_lastStatus != B2G_OK) return;
+  w->EndContacts(ended, ne, before);
+  b2Fixture** link = &m_fixtureList;
+  while (*link && *link != fixture) link = &(*link)->m_next;
+  if (*link) *link = fixture->m_next;
+  fixture->m_next = nullptr;
+  fixture->m_index = -1;
+  w->Renumber();
+}
+
+void b2Body::SetAwake(bool flag) {
+  m_world->m_lastStatus = b2g_body_set_awake(m_world->m_batch, m_world->m_index, m_index, flag ? 1 : 0);
+  m_world->InvalidateCaches();
+}
+
+bool b2Body::IsAwake() const { return (m_world->BodyRecord(m_index).flags & B2G_BODY_AWAKE) != 0; }
+
+bool b2Body::IsSleepingAllowed() const { return (m_world->BodyRecord(m_index).flags & B2G_BODY_AUTO_SLEEP) != 0; }
 
 b2Joint* b2World::CreateJoint(const b2JointDef* def) {
   if (!def || !def->bodyA || !def->bodyB) return nullptr;
@@ -658,7 +777,7 @@ b2Joint* b2World::CreateJoint(const b2JointDef* def) {
 
 const b2g_body& b2World::BodyRecord(int32 index) const {
   if (!m_stateValid) {
-    m_state.resize(m_bodies.size());
+    m_state.resize((size_t)m_bodyCount);
     if (!m_state.empty()) b2g_bodies_read(m_batch, m_index, 0, (int32_t)m_state.size(), m_state.data());
     m_stateValid = true;
   }
@@ -681,6 +800,10 @@ const b2g_joint& b2World::JointRecord(int32 index) const {
 
 void b2World::Step(float dt, int32 vi, int32 pi, int32 particleIterations) {
   B2_NOT_USED(particleIterations);
+  if (m_filterUnsupported) {  // a custom b2ContactFilter cannot be run: nothing is stepped
+    m_lastStatus = B2G_E_INVALID_ARG;
+    return;
+  }
   int32_t nw = 0;
   b2g_world_count(m_batch, &nw);
   std::vector<uint8_t> mask(nw, 0);
@@ -696,12 +819,12 @@ void b2World::Step(float dt, int32 vi, int32 pi, int32 particleIterations) {
 }
 
 void b2World::ClearForces() {
-  for (b2Body& b : m_bodies) {
-    b2g_body r = BodyRecord(b.m_index);
+  for (b2Body* b = m_bodyHead; b; b = b->m_next) {
+    b2g_body r = BodyRecord(b->m_index);
     if (r.force[0] != 0.0f || r.force[1] != 0.0f || r.torque != 0.0f) {
       r.force[0] = r.force[1] = 0.0f;
       r.torque = 0.0f;
-      WriteBody(b.m_index, r);
+      WriteBody(b->m_index, r);
     }
   }
 }
@@ -736,7 +859,12 @@ int32 b2World::GetContactCount() const {
   return nc;
 }
 
-// Batched listener delivery after the step.
+// Batched listener delivery after the step: this world's events only (the other worlds of a
+// shared batch keep theirs for their own b2World::DeliverEvents).
+void b2World::DeliverEvents() {
+  if (m_listener) Deliver();
+}
+
 void b2World::Deliver() {
   std::vector<b2g_event> ev(1 << 16);
   b2Contact* start = GetContactListStart();
@@ -745,10 +873,9 @@ void b2World::Deliver() {
   for (b2Contact& c : m_contacts) byPair[{c.m_fixtureA->m_index, c.m_fixtureB->m_index}] = &c;
   for (;;) {
     int32_t n = 0;
-    if (b2g_events_drain(m_batch, ev.data(), (int32_t)ev.size(), &n) != B2G_OK || n == 0) break;
+    if (b2g_events_drain_world(m_batch, m_index, ev.data(), (int32_t)ev.size(), &n) != B2G_OK || n == 0) break;
     for (int32_t i = 0; i < n; ++i) {
       const b2g_event& e = ev[i];
-      if (e.world != m_index) continue;
       b2Contact tmp;
       b2Contact* c = &tmp;
       auto it = byPair.find({e.fixture_a, e.fixture_b});

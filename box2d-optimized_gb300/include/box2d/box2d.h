@@ -7,13 +7,15 @@
 // Every call goes through the C ABI in include/b2g_capi.h; the simulation runs on the GPU.
 //
 // Differences from the reference, by design:
-//  * Contact listener callbacks are delivered as a batch after each Step (End from the
-//    broadphase, Begin, End, PreSolve, PostSolve, grouped per world). A PreSolve that disables a
-//    contact takes effect from the next step.
-//  * Custom b2ContactFilter subclasses cannot run on the GPU; the default filter
-//    (group / category / mask) is applied.
-//  * DestroyBody / DestroyJoint / DestroyFixture, sleeping, TOI (bullets) and particle systems are
-//    not part of this engine; the calls return without effect (sleeping is always off).
+//  * Contact listener callbacks are delivered as a batch after each Step, grouped per world and
+//    sorted by kind (Begin, End, PreSolve, PostSolve), then fixture pair; the set of callbacks of
+//    a step is the reference's. A PreSolve that disables a contact takes effect from the next
+//    step. Worlds stepped together through b2g_step deliver with b2World::DeliverEvents.
+//  * Custom b2ContactFilter subclasses cannot run on the GPU: SetContactFilter with one makes the
+//    next Step fail (LastStatus() = B2G_E_INVALID_ARG, the world does not advance); the default
+//    filter (group / category / mask) always applies.
+//  * TOI (bullets) and particle systems are not part of this engine. Sleeping is (the world
+//    allows it by default, like the reference).
 //  * Sine/cosine inside the step come from a portable routine (identical on host and GPU), so
 //    trajectories agree with the reference to rounding, not bit for bit.
 #pragma once
@@ -410,7 +412,9 @@ class b2Body {
  public:
   b2Fixture* CreateFixture(const b2FixtureDef* def);
   b2Fixture* CreateFixture(const b2Shape* shape, float density);
-  void DestroyFixture(b2Fixture* fixture) { B2_NOT_USED(fixture); }
+  // b2Body::DestroyFixture (src/dynamics/b2_body.cpp:280-350): its contacts end (EndContact for
+  // the touching ones, before this returns) and the body's mass data is reset.
+  void DestroyFixture(b2Fixture* fixture);
   void SetTransform(const b2Vec2& position, float angle);
   const b2Transform& GetTransform() const;
   const b2Vec2& GetPosition() const { return GetTransform().p; }
@@ -441,9 +445,10 @@ class b2Body {
   void SetBullet(bool flag) { B2_NOT_USED(flag); }
   bool IsBullet() const { return false; }
   void SetSleepingAllowed(bool flag) { B2_NOT_USED(flag); }
-  bool IsSleepingAllowed() const { return false; }
-  void SetAwake(bool flag) { B2_NOT_USED(flag); }
-  bool IsAwake() const { return m_type != b2_staticBody; }
+  bool IsSleepingAllowed() const;
+  // b2Body::SetAwake / IsAwake (include/box2d/b2_body.h:719-746)
+  void SetAwake(bool flag);
+  bool IsAwake() const;
   bool IsEnabled() const { return true; }
   bool IsFixedRotation() const { return m_fixedRotation; }
   b2Fixture* GetFixtureList() { return m_fixtureList; }
@@ -689,9 +694,13 @@ class b2ContactListener {
   virtual void PostSolve(b2Contact* contact, const b2ContactImpulse* impulse) { B2_NOT_USED(contact); B2_NOT_USED(impulse); }
 };
 
+// b2DestructionListener (include/box2d/b2_world_callbacks.h:35-47): called for the joints and
+// fixtures a DestroyBody call destroys implicitly.
 class b2DestructionListener {
  public:
   virtual ~b2DestructionListener() {}
+  virtual void SayGoodbye(b2Joint* joint) = 0;
+  virtual void SayGoodbye(b2Fixture* fixture) = 0;
 };
 
 struct b2Profile {
@@ -710,16 +719,23 @@ class b2World {
   b2World(const b2World&) = delete;
   b2World& operator=(const b2World&) = delete;
 
-  void SetDestructionListener(b2DestructionListener* listener) { B2_NOT_USED(listener); }
-  void SetContactFilter(b2ContactFilter* filter) { m_filter = filter; }
+  void SetDestructionListener(b2DestructionListener* listener) { m_destruction = listener; }
+  // A b2ContactFilter subclass cannot run inside the GPU broadphase: with one set, Step returns
+  // without stepping and LastStatus() is B2G_E_INVALID_ARG. The base class (the default
+  // group / category / mask filter, which the engine applies anyway) and nullptr are accepted.
+  void SetContactFilter(b2ContactFilter* filter);
   void SetContactListener(b2ContactListener* listener);
   b2Body* CreateBody(const b2BodyDef* def);
-  void DestroyBody(b2Body* body) { B2_NOT_USED(body); }
+  // b2World::DestroyBody (src/dynamics/b2_world.cpp:178-266): its joints (SayGoodbye), contacts
+  // (EndContact for the touching ones, before this returns) and fixtures (SayGoodbye) go with it.
+  // Indices (GetIndex) of the bodies, fixtures and joints created after it shift down.
+  void DestroyBody(b2Body* body);
   b2Joint* CreateJoint(const b2JointDef* def);
-  void DestroyJoint(b2Joint* joint) { B2_NOT_USED(joint); }
+  // b2World::DestroyJoint (src/dynamics/b2_world.cpp:326-410): both bodies wake.
+  void DestroyJoint(b2Joint* joint);
   void Step(float timeStep, int32 velocityIterations, int32 positionIterations, int32 particleIterations = 1);
   void ClearForces();
-  b2Body* GetBodyList() { return m_bodies.empty() ? nullptr : &m_bodies.front(); }
+  b2Body* GetBodyList() { return m_bodyHead; }
   b2Joint* GetJointList() { return m_joints.empty() ? nullptr : m_joints.front().get(); }
   b2Contact* GetContactListStart();
   b2Contact* GetContactListEnd() { return &m_contactEnd; }
@@ -731,8 +747,8 @@ class b2World {
   bool GetContinuousPhysics() const { return m_continuous; }
   void SetSubStepping(bool flag) { B2_NOT_USED(flag); }
   bool GetSubStepping() const { return false; }
-  int32 GetProxyCount() const { return (int32)m_fixtures.size(); }
-  int32 GetBodyCount() const { return (int32)m_bodies.size(); }
+  int32 GetProxyCount() const { return (int32)m_fixtureIndex.size(); }
+  int32 GetBodyCount() const { return m_bodyCount; }
   int32 GetJointCount() const { return (int32)m_joints.size(); }
   int32 GetContactCount() const;
   void SetGravity(const b2Vec2& gravity);
@@ -743,6 +759,9 @@ class b2World {
   const b2Profile& GetProfile() const { return m_profile; }
 
   // Extensions of this engine
+  // After stepping a shared batch with b2g_step (all its worlds at once), hands this world's
+  // listener events of that step to its b2ContactListener. b2World::Step does this itself.
+  void DeliverEvents();
   b2g_batch* GetBatch() { return m_batch; }
   int32 GetWorldIndex() const { return m_index; }
   int LastStatus() const { return m_lastStatus; }
@@ -758,6 +777,9 @@ class b2World {
  private:
   void ApplyFlags();
   void Deliver();
+  // after a removal: the engine's End callbacks for the destroyed contacts, then renumbering
+  void EndContacts(const std::vector<b2g_event>& ended, int32 n, const std::vector<b2Contact>& before);
+  void Renumber();
   b2g_batch* m_batch = nullptr;
   bool m_ownsBatch = false;
   int32 m_index = 0;
@@ -766,7 +788,11 @@ class b2World {
   bool m_allowSleep = true, m_warmStarting = true, m_continuous = true, m_autoClear = true;
   b2ContactListener* m_listener = nullptr;
   b2ContactFilter* m_filter = nullptr;
-  std::deque<b2Body> m_bodies;
+  bool m_filterUnsupported = false;
+  b2DestructionListener* m_destruction = nullptr;
+  std::deque<b2Body> m_bodies;  // every body created; destroyed ones keep m_index = -1
+  b2Body* m_bodyHead = nullptr;  // first live body (creation order)
+  int32 m_bodyCount = 0;
   std::deque<b2Fixture> m_fixtures;
   std::vector<b2Fixture*> m_fixtureIndex;
   std::vector<std::unique_ptr<b2Joint>> m_joints;

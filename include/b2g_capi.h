@@ -327,6 +327,20 @@ B2G_API int b2g_world_retire(b2g_batch* b, int32_t world);
 B2G_API int b2g_compact(b2g_batch* b, int32_t* old_to_new, int32_t n);
 
 /* Counts of one world. */
+/* Structural removal: b2World::DestroyBody (src/dynamics/b2_world.cpp:178-266), b2Body::DestroyFixture
+ * (src/dynamics/b2_body.cpp:280-350), b2World::DestroyJoint (b2_world.cpp:326-410). A removed body
+ * takes its fixtures, joints and contacts along; a destroyed contact that was touching ends, and the
+ * End events are returned at once in `ended` (up to `cap`; *n_ended = their number, fixture indices
+ * from before the removal), as the reference calls EndContact inside the destroy call; a destroyed
+ * contact with manifold points wakes both bodies, a removed joint wakes its bodies, a removed fixture
+ * resets its body's mass data. The remaining bodies, fixtures and joints of the world keep their
+ * creation order and are renumbered from 0; the world is re-uploaded by its next step and its other
+ * contacts keep their manifolds and impulses. */
+B2G_API int b2g_bodies_remove(b2g_batch* b, int32_t world, const int32_t* bodies, int32_t n, b2g_event* ended,
+                              int32_t cap, int32_t* n_ended);
+B2G_API int b2g_fixtures_remove(b2g_batch* b, int32_t world, const int32_t* fixtures, int32_t n,
+                                b2g_event* ended, int32_t cap, int32_t* n_ended);
+B2G_API int b2g_joints_remove(b2g_batch* b, int32_t world, const int32_t* joints, int32_t n);
 B2G_API int b2g_world_sizes(b2g_batch* b, int32_t world, int32_t* bodies, int32_t* fixtures,
                             int32_t* joints, int32_t* contacts);
 
@@ -433,10 +447,18 @@ B2G_API int b2g_joints_read(b2g_batch* b, int32_t world, int32_t first, int32_t 
  * b2_contact.h:71-143. Contacts are listed in the engine's canonical order. */
 B2G_API int b2g_contacts_read(b2g_batch* b, int32_t world, b2g_contact* out, int32_t cap,
                               int32_t* n);
-/* b2ContactListener callbacks of the last step, as a batch (see b2g_event). enable != 0 turns
- * event recording on for the batch (off by default; recording costs device time). */
+/* b2ContactListener callbacks of the last step, as a batch (see b2g_event): the callbacks the
+ * reference makes inside one Step - Begin / End / PreSolve from b2Contact::Update
+ * (src/dynamics/b2_contact.cpp:197-209), PostSolve from b2Island::Report
+ * (src/dynamics/b2_island.cpp:621-647), End for the touching contacts the broadphase drops
+ * (src/dynamics/b2_contact_manager.cpp:48-61) - grouped per world and sorted by kind, then
+ * fixture pair. enable != 0 turns event recording on for the batch (off by default; recording
+ * costs device time). Events are kept until drained or until the next step begins.
+ * b2g_events_drain takes up to `cap` events of the whole batch; b2g_events_drain_world takes
+ * only world `world`'s (the others stay for their own drains). */
 B2G_API int b2g_events_enable(b2g_batch* b, int32_t enable);
 B2G_API int b2g_events_drain(b2g_batch* b, b2g_event* out, int32_t cap, int32_t* n);
+B2G_API int b2g_events_drain_world(b2g_batch* b, int32_t world, b2g_event* out, int32_t cap, int32_t* n);
 /* b2World::GetProfile, include/box2d/b2_world.h:249 */
 B2G_API int b2g_profile_get(b2g_batch* b, b2g_profile* out);
 /* The constraint colour and solve-order record of the last step of one world, for replaying the

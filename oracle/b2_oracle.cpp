@@ -1043,8 +1043,30 @@ struct World {
   // bodies, its contacts as (fixture A, fixture B) in solve order and its joints in solve order
   std::vector<int32_t> islandRoot, islandOrphan, islandBodyOff, islandBodies;
   std::vector<int32_t> islandContactOff, islandContacts, islandJointOff, islandJoints;
+  // listener events of the steps since the last read (b2ContactListener, src/dynamics/
+  // b2_world_callbacks.h:133-209), when recording is on: Begin / End / PreSolve from the
+  // narrowphase (b2Contact::Update), PostSolve from the solver (b2Island::Report), End for the
+  // touching contacts the broadphase drops (b2ContactManager::Destroy)
+  bool recordEvents = false;
+  std::vector<b2g_event> events;
   bool sleepMode() const { return allowSleep || sleepers; }
 };
+
+static void recordEvent(World* w, int kind, int fa, int fb, const b2g_manifold* old = nullptr, int pc = 0,
+                        const float* ni = nullptr, const float* ti = nullptr) {
+  b2g_event e;
+  memset(&e, 0, sizeof(e));
+  e.kind = kind;
+  e.fixture_a = fa;
+  e.fixture_b = fb;
+  e.point_count = pc;
+  for (int k = 0; k < 2; ++k) {
+    e.normal_impulses[k] = ni ? ni[k] : 0.0f;
+    e.tangent_impulses[k] = ti ? ti[k] : 0.0f;
+  }
+  if (old) e.old_manifold = *old;
+  w->events.push_back(e);
+}
 
 // b2Body::SetAwake (include/box2d/b2_body.h:719-740).
 static void setAwake(Body& b, bool flag) {
@@ -1167,6 +1189,13 @@ static void updatePairs(World* w) {
       next.push_back(makeContact(*w, key));
     }
   }
+  // EndContact for the touching contacts dropped (b2ContactManager::Destroy,
+  // src/dynamics/b2_contact_manager.cpp:48-61)
+  if (w->recordEvents)
+    for (size_t i = 0; i < w->contacts.size(); ++i) {
+      const Contact& c = w->contacts[i];
+      if (!kept[i] && (c.flags & B2G_CONTACT_TOUCHING)) recordEvent(w, B2G_EVENT_END, c.fA, c.fB);
+    }
   // b2Contact::Destroy wakes both bodies of a destroyed contact with manifold points
   // (src/dynamics/b2_contact.cpp:80-91)
   if (w->sleepMode())
@@ -1318,6 +1347,16 @@ static bool updateContact(World* w, Contact& c) {
   }
   if (touching) c.flags |= B2G_CONTACT_TOUCHING;
   else c.flags &= ~B2G_CONTACT_TOUCHING;
+  if (w->recordEvents) {  // b2_contact.cpp:197-209
+    const bool sensor = fa.sensor || fb.sensor;
+    if (!wasTouching && touching) recordEvent(w, B2G_EVENT_BEGIN, c.fA, c.fB);
+    if (wasTouching && !touching) recordEvent(w, B2G_EVENT_END, c.fA, c.fB);
+    if (!sensor && touching) {
+      b2g_manifold om;
+      manifoldTo(old, &om);
+      recordEvent(w, B2G_EVENT_PRESOLVE, c.fA, c.fB, &om);
+    }
+  }
   return !fa.sensor && !fb.sensor && touching != wasTouching;
 }
 
@@ -2740,6 +2779,18 @@ static void stepWorld(World* w, float dt, int vi, int pi) {
         if (jointActive(w->joints[j])) jointSolveVelocity(w->joints[j], sb, st);
       for (int i : corder) solveVelocityOne(vcs[i], sb);
     }
+    // PostSolve with the velocity impulses (b2Island::Report, src/dynamics/b2_island.cpp:621-647),
+    // recorded here (their values do not change after the velocity iterations) and delivered
+    // after the step like the engine's
+    if (w->recordEvents)
+      for (int i = 0; i < nc; ++i) {
+        const VC& vc = vcs[i];
+        const Contact& c = w->contacts[vc.contact];
+        float ni[2] = {vc.points[0].normalImpulse, vc.points[1].normalImpulse};
+        float ti[2] = {vc.points[0].tangentImpulse, vc.points[1].tangentImpulse};
+        if (vc.pointCount < 2) ni[1] = ti[1] = 0.0f;
+        recordEvent(w, B2G_EVENT_POSTSOLVE, c.fA, c.fB, nullptr, vc.pointCount, ni, ti);
+      }
     // StoreImpulses (b2_contact_solver.cpp:641-657)
     for (int i = 0; i < nc; ++i) {
       Manifold& m = w->contacts[vcs[i].contact].m;
@@ -2892,6 +2943,30 @@ static void stepWorld(World* w, float dt, int vi, int pi) {
 using namespace orc;
 
 extern "C" {
+
+// Listener-event recording (off by default) and the recorded events of the steps since the last
+// call, sorted like the engine's batch delivery (kind, then fixture pair); returns their number
+// and clears them when `out` holds them all.
+void orc_world_events_enable(void* h, int32_t on) {
+  World* w = (World*)h;
+  w->recordEvents = on != 0;
+  w->events.clear();
+}
+
+int32_t orc_world_events(void* h, b2g_event* out, int32_t cap) {
+  World* w = (World*)h;
+  std::stable_sort(w->events.begin(), w->events.end(), [](const b2g_event& x, const b2g_event& y) {
+    if (x.kind != y.kind) return x.kind < y.kind;
+    if (x.fixture_a != y.fixture_a) return x.fixture_a < y.fixture_a;
+    return x.fixture_b < y.fixture_b;
+  });
+  const int32_t n = (int32_t)w->events.size();
+  if (out && cap >= n) {
+    for (int32_t i = 0; i < n; ++i) out[i] = w->events[i];
+    w->events.clear();
+  }
+  return n;
+}
 
 void orc_set_libm_trig(int32_t on) { g_libm_trig = on; }
 

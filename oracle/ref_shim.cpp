@@ -223,6 +223,21 @@ int ref_world_manifold(const b2g_manifold* mi, const float* xfa, float ra, const
 }
 
 // ---------------------------------------------------------------- worlds
+struct RefWorld;
+
+// A b2ContactListener that records every callback of the reference's own Step as an engine
+// event record (fixtures by creation index; PreSolve with the old manifold, PostSolve with the
+// b2ContactImpulse entries the solver filled).
+struct EventRecorder : public b2ContactListener {
+  RefWorld* rw = nullptr;
+  std::vector<b2g_event> events;
+  void add(int kind, b2Contact* c, const b2Manifold* old, const b2ContactImpulse* imp);
+  void BeginContact(b2Contact* c) override { add(B2G_EVENT_BEGIN, c, nullptr, nullptr); }
+  void EndContact(b2Contact* c) override { add(B2G_EVENT_END, c, nullptr, nullptr); }
+  void PreSolve(b2Contact* c, const b2Manifold* old) override { add(B2G_EVENT_PRESOLVE, c, old, nullptr); }
+  void PostSolve(b2Contact* c, const b2ContactImpulse* imp) override { add(B2G_EVENT_POSTSOLVE, c, nullptr, imp); }
+};
+
 struct RefWorld {
   b2World* world;
   std::vector<b2Body*> bodies;      // creation order
@@ -231,7 +246,25 @@ struct RefWorld {
   std::unordered_map<const b2Body*, int> body_index;
   std::unordered_map<const b2Fixture*, int> fixture_index;
   std::unordered_map<const b2Joint*, int> joint_index;
+  EventRecorder recorder;
 };
+
+void EventRecorder::add(int kind, b2Contact* c, const b2Manifold* old, const b2ContactImpulse* imp) {
+  b2g_event e;
+  memset(&e, 0, sizeof(e));
+  e.kind = kind;
+  e.fixture_a = rw->fixture_index[c->GetFixtureA()];
+  e.fixture_b = rw->fixture_index[c->GetFixtureB()];
+  if (old) manifold_out(*old, &e.old_manifold);
+  if (imp) {
+    e.point_count = imp->count;
+    for (int k = 0; k < imp->count && k < 2; ++k) {
+      e.normal_impulses[k] = imp->normalImpulses[k];
+      e.tangent_impulses[k] = imp->tangentImpulses[k];
+    }
+  }
+  events.push_back(e);
+}
 
 static void index_world(RefWorld* rw) {
   rw->bodies.clear(); rw->fixtures.clear(); rw->joints.clear();
@@ -269,6 +302,32 @@ void* ref_scene_world(int32_t kind, uint32_t seed, int32_t n, float p0, float p1
   if (counts) { counts[0] = c.bodies; counts[1] = c.fixtures; counts[2] = c.joints; }
   index_world(rw);
   return rw;
+}
+
+// Records the reference's listener callbacks (on) or detaches the recorder (off).
+void ref_world_events_enable(void* h, int32_t on) {
+  RefWorld* rw = (RefWorld*)h;
+  rw->recorder.rw = rw;
+  rw->recorder.events.clear();
+  rw->world->SetContactListener(on ? &rw->recorder : nullptr);
+}
+
+// The callbacks recorded since the last call, sorted by (kind, fixture A, fixture B) like the
+// engine's batch delivery; returns their number and clears them when `out` holds them all.
+int32_t ref_world_events(void* h, b2g_event* out, int32_t cap) {
+  RefWorld* rw = (RefWorld*)h;
+  std::vector<b2g_event>& ev = rw->recorder.events;
+  std::stable_sort(ev.begin(), ev.end(), [](const b2g_event& x, const b2g_event& y) {
+    if (x.kind != y.kind) return x.kind < y.kind;
+    if (x.fixture_a != y.fixture_a) return x.fixture_a < y.fixture_a;
+    return x.fixture_b < y.fixture_b;
+  });
+  const int32_t n = (int32_t)ev.size();
+  if (out && cap >= n) {
+    for (int32_t i = 0; i < n; ++i) out[i] = ev[i];
+    ev.clear();
+  }
+  return n;
 }
 
 void ref_world_free(void* h) {

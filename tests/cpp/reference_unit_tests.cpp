@@ -200,6 +200,101 @@ static void sweep_transform() {
   CHECK(transform.q.s == sinf(sweep.a));
 }
 
+// b2World::DestroyBody / DestroyJoint, b2Body::DestroyFixture with a contact listener and a
+// destruction listener (the reference's semantics: src/dynamics/b2_world.cpp:178-410,
+// b2_body.cpp:280-350): EndContact for the touching contacts of a destroyed body before the call
+// returns, SayGoodbye for the joints and fixtures it takes along, counts and lists updated, the
+// world steps on without it.
+struct CountingListener : public b2ContactListener {
+  int begins = 0, ends = 0;
+  void BeginContact(b2Contact* contact) override { B2_NOT_USED(contact); ++begins; }
+  void EndContact(b2Contact* contact) override { B2_NOT_USED(contact); ++ends; }
+};
+struct Goodbyes : public b2DestructionListener {
+  int joints = 0, fixtures = 0;
+  void SayGoodbye(b2Joint* joint) override { B2_NOT_USED(joint); ++joints; }
+  void SayGoodbye(b2Fixture* fixture) override { B2_NOT_USED(fixture); ++fixtures; }
+};
+static void destroy_calls() {
+  b2World world(b2Vec2(0.0f, -10.0f));
+  world.SetAllowSleeping(false);
+  CountingListener listener;
+  Goodbyes goodbyes;
+  world.SetContactListener(&listener);
+  world.SetDestructionListener(&goodbyes);
+  b2BodyDef gd;
+  b2Body* ground = world.CreateBody(&gd);
+  b2EdgeShape edge;
+  edge.SetTwoSided(b2Vec2(-20.0f, 0.0f), b2Vec2(20.0f, 0.0f));
+  ground->CreateFixture(&edge, 0.0f);
+  b2PolygonShape box;
+  box.SetAsBox(0.5f, 0.5f);
+  b2Body* stack[3];
+  for (int i = 0; i < 3; ++i) {
+    b2BodyDef bd;
+    bd.type = b2_dynamicBody;
+    bd.position.Set(0.0f, 0.5f + 1.0f * (float)i);
+    stack[i] = world.CreateBody(&bd);
+    stack[i]->CreateFixture(&box, 1.0f);
+  }
+  b2BodyDef pd;
+  pd.type = b2_dynamicBody;
+  pd.position.Set(5.0f, 3.0f);
+  b2Body* pendulum = world.CreateBody(&pd);
+  pendulum->CreateFixture(&box, 1.0f);
+  b2RevoluteJointDef jd;
+  jd.Initialize(ground, pendulum, b2Vec2(5.0f, 5.0f));
+  b2Joint* joint = world.CreateJoint(&jd);
+  for (int i = 0; i < 60; ++i) world.Step(1.0f / 60.0f, 8, 3);
+  CHECK(listener.begins >= 3);
+  const int ends0 = listener.ends;
+  const float topY = stack[2]->GetPosition().y;
+  world.DestroyBody(stack[0]);  // touching the ground and the middle box
+  CHECK(listener.ends - ends0 == 2);
+  CHECK(goodbyes.fixtures == 1 && goodbyes.joints == 0);
+  CHECK(world.GetBodyCount() == 4);
+  int listed = 0;
+  for (b2Body* b = world.GetBodyList(); b; b = b->GetNext()) ++listed;
+  CHECK(listed == 4);
+  for (int i = 0; i < 60; ++i) world.Step(1.0f / 60.0f, 8, 3);
+  CHECK(stack[2]->GetPosition().y < topY - 0.9f);  // the two boxes above fell by a box height
+  world.DestroyJoint(joint);
+  CHECK(world.GetJointCount() == 0);
+  for (int i = 0; i < 30; ++i) world.Step(1.0f / 60.0f, 8, 3);
+  CHECK(pendulum->GetPosition().y < 3.0f - 0.5f);  // released: it falls
+  stack[2]->DestroyFixture(stack[2]->GetFixtureList());
+  CHECK(stack[2]->GetFixtureList() == nullptr);
+  CHECK(world.GetProxyCount() == 3);
+}
+
+#ifdef B2G_API
+// This engine's extension: a b2ContactFilter subclass cannot run on the GPU, so Step refuses to
+// advance with one set (LastStatus() = B2G_E_INVALID_ARG); the default filter is accepted.
+struct NoCollide : public b2ContactFilter {
+  bool ShouldCollide(b2Fixture* a, b2Fixture* b) override { B2_NOT_USED(a); B2_NOT_USED(b); return false; }
+};
+static void custom_filter_refused() {
+  b2World world(b2Vec2(0.0f, -10.0f));
+  b2BodyDef bd;
+  bd.type = b2_dynamicBody;
+  bd.position.Set(0.0f, 4.0f);
+  b2Body* body = world.CreateBody(&bd);
+  b2CircleShape c;
+  c.m_radius = 0.5f;
+  body->CreateFixture(&c, 1.0f);
+  NoCollide filter;
+  world.SetContactFilter(&filter);
+  world.Step(1.0f / 60.0f, 8, 3);
+  CHECK(world.LastStatus() == B2G_E_INVALID_ARG);
+  CHECK(body->GetPosition().y == 4.0f);
+  b2ContactFilter plain;
+  world.SetContactFilter(&plain);
+  world.Step(1.0f / 60.0f, 8, 3);
+  CHECK(world.LastStatus() == B2G_OK);
+  CHECK(body->GetPosition().y < 4.0f);
+}
+#endif
+
 int main(int argc, char** argv) {
   bool host_only = argc > 1;
   polygon_mass_data();
@@ -208,6 +303,10 @@ int main(int argc, char** argv) {
     hello_world();
     joint_reactions();
     world_begin_contact();
+    destroy_calls();
+#ifdef B2G_API
+    custom_filter_refused();
+#endif
   }
   printf("%s: %d failures\n", g_fail ? "FAILED" : "OK", g_fail);
   return g_fail ? 1 : 0;

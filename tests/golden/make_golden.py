@@ -8,7 +8,8 @@ Run where the reference sources are checked out and oracle/_ref/libb2ref.so is b
 Every vector is an output of the reference's own code (compiled from its sources) on seeded
 inputs: polygon hulls and mass data (b2PolygonShape::Set / SetAsBox / ComputeMass), manifolds of
 the five collide functions, one replayed solver step (b2Island::Solve in a given constraint
-order) on exported world states, and the final state of 256-step reference rollouts.
+order) on exported world states, the listener callbacks of one replayed step, and the final
+state of 256-step reference rollouts.
 """
 from __future__ import annotations
 
@@ -118,6 +119,31 @@ def replay(ref, orc, name, kind, n, seed, p0, warm, vi, pi):
                         after=rec_bytes(after), vi=vi, pi=pi)
 
 
+def events(ref, orc, name, kind, n, seed, p0, warm, vi, pi):
+    """World state after `warm` reference steps and the reference's listener callbacks during its
+    next step, replayed in the oracle's solver order: (kind, fixture A, fixture B, point count,
+    old manifold point count, normal impulses, tangent impulses) per callback."""
+    rw = ob.RefWorld(ref, kind, seed=seed, n=n, p0=p0, p1=0.6)
+    rw.step(warm, vi=vi, pi=pi)
+    bodies, fixtures, joints, contacts = rw.bodies(), rw.fixtures(), rw.joints(), rw.contacts()
+    orc.orc_set_libm_trig(1)
+    ow = ob.OracleWorld(orc, (0.0, -10.0), list(bodies), list(fixtures), list(joints), list(contacts), inv_dt0=60.0)
+    ow.step(1, 1 / 60, vi, pi)
+    orc.orc_set_libm_trig(0)
+    pairs, jorder = ow.last_order()
+    arr = (C.c_int32 * max(len(pairs), 1))(*pairs)
+    jar = (C.c_int32 * max(len(jorder), 1))(*jorder)
+    rw.events_enable(True)
+    assert ref.ref_replay_step(rw.h, 1 / 60, vi, pi, arr, len(pairs) // 2, jar, len(jorder)) == 0
+    ev = rw.events()
+    ints = np.array([(e.kind, e.fixture_a, e.fixture_b, e.point_count, e.old_manifold.point_count) for e in ev],
+                    np.int32)
+    imps = np.array([tuple(e.normal_impulses) + tuple(e.tangent_impulses) for e in ev], np.float32)
+    np.savez_compressed(HERE / f"events_{name}.npz", bodies=rec_bytes(bodies), fixtures=rec_bytes(fixtures),
+                        joints=rec_bytes(joints) if joints else np.zeros(0, np.uint8), contacts=rec_bytes(contacts),
+                        ints=ints, impulses=imps, vi=vi, pi=pi)
+
+
 def rollout(ref, name, kind, n, seed, p0, steps, vi, pi):
     rw = ob.RefWorld(ref, kind, seed=seed, n=n, p0=p0, p1=0.6)
     start = rw.bodies()
@@ -137,6 +163,8 @@ def main():
     replay(ref, orc, "chains", G.SCENE_CHAINS, 10, 2, 150.0, 100, 10, 4)
     replay(ref, orc, "sliders", G.SCENE_SLIDERS, 3, 9, 0.0, 60, 8, 3)
     rollout(ref, "pyramid", G.SCENE_PYRAMID, 20, 1, 1.0, 256, 8, 3)
+    events(ref, orc, "mixed", G.SCENE_MIXED_DROP, 400, 5, 0.0, 200, 8, 3)
+    events(ref, orc, "chains", G.SCENE_CHAINS, 15, 4, 200.0, 80, 10, 4)
     print("golden vectors written to", HERE)
 
 

@@ -50,6 +50,8 @@ class Ref:
                                          P(i32)], C.c_int),
             "ref_world_sleep_times": ([vp, P(f32)], None),
             "ref_worlds_step_parallel": ([P(vp), i32, f32, i32, i32, i32, i32], C.c_double),
+            "ref_world_events_enable": ([vp, i32], None),
+            "ref_world_events": ([vp, P(G.Event), i32], i32),
         }
         for name, (a, r) in sig.items():
             fn = getattr(L, name)
@@ -134,6 +136,16 @@ class RefWorld:
         self.ref.ref_world_sleep_times(self.h, arr)
         return list(arr[:nb])
 
+    def events_enable(self, on=True):
+        self.ref.ref_world_events_enable(self.h, int(on))
+
+    def events(self):
+        """Listener callbacks since the last call, sorted by (kind, fixture A, fixture B)."""
+        n = self.ref.ref_world_events(self.h, None, 0)
+        arr = (G.Event * max(n, 1))()
+        self.ref.ref_world_events(self.h, arr, n)
+        return arr[:n]
+
     def replay_islands(self, islands, dt=1 / 60, vi=8, pi=3):
         """One Step with the reference's island solver over the oracle's islands (last_islands)."""
         root, orphan, boff, coff, joff, bodies, pairs, joints = islands
@@ -186,6 +198,8 @@ class Oracle:
             "orc_scene_records": ([i32, u32, i32, f32, f32, P(i32), P(G.Body), i32, P(G.Fixture), i32,
                                    P(G.Joint), i32], i32),
             "orc_batch_world_params": ([u32, P(i32), P(f32), P(f32)], C.c_int),
+            "orc_world_events_enable": ([vp, i32], None),
+            "orc_world_events": ([vp, P(G.Event), i32], i32),
         }
         for name, (a, r) in sig.items():
             fn = getattr(L, name)
@@ -280,6 +294,16 @@ class OracleWorld:
 
     def set_sleep(self, allow):
         self.orc.orc_world_set_sleep(self.h, int(allow))
+
+    def events_enable(self, on=True):
+        self.orc.orc_world_events_enable(self.h, int(on))
+
+    def events(self):
+        """Listener events of the steps since the last call, sorted like the engine's delivery."""
+        n = self.orc.orc_world_events(self.h, None, 0)
+        arr = (G.Event * max(n, 1))()
+        self.orc.orc_world_events(self.h, arr, n)
+        return arr[:n]
 
     def sleep_times(self):
         nb = self.sizes()[0]

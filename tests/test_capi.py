@@ -126,3 +126,47 @@ def test_tuning_knobs_and_split_step_on_a_host_only_batch():
     b.stage()                        # no device: nothing to pack
     assert lib.b2g_step_end(b.h) == 1  # no step in flight
     b.close()
+
+
+def test_removal_renumbers_host_records():
+    """b2g_bodies_remove / b2g_fixtures_remove / b2g_joints_remove on a world not yet on a device:
+    a removed body takes its fixtures and joints along, the rest keep their creation order and
+    are renumbered (fixture bodies and joint bodies follow), a removed fixture resets its body's
+    mass data, and out-of-range indices are refused."""
+    lib = G.Lib()
+    b = G.Batch(lib, device=G.HOST_ONLY)
+    w = b.add_world(0.0, -10.0)
+    b.scene(w, G.SCENE_CHAINS, seed=2, n=3, p0=10, p1=0.6)
+    bodies, fixtures, joints = b.bodies(w), b.fixtures(w), b.joints(w)
+    nb, nf, nj = len(bodies), len(fixtures), len(joints)
+    # a chain link: body with one joint to its predecessor and one to its successor
+    link = joints[5].def_.body_b
+    attached = [j for j in range(nj) if link in (joints[j].def_.body_a, joints[j].def_.body_b)]
+    assert len(attached) == 2
+    assert b.remove(w, bodies=[link]) == []
+    nb2, nf2, nj2, _ = b.sizes(w)
+    assert (nb2, nf2, nj2) == (nb - 1, nf - 1, nj - 2)
+    shift = lambda i: i - 1 if i > link else i  # noqa: E731
+    kept = [j for j in range(nj) if j not in attached]
+    after = b.joints(w)
+    for k, j in enumerate(kept):
+        assert (after[k].def_.body_a, after[k].def_.body_b) == (shift(joints[j].def_.body_a), shift(joints[j].def_.body_b))
+    after_f = b.fixtures(w)
+    assert [f.body for f in after_f] == [shift(f.body) for f in fixtures if f.body != link]
+    assert bytes(b.bodies(w)[link]) == bytes(bodies[link + 1])
+    # a second fixture on a body, then its removal restores the one-fixture mass data
+    one = b.bodies(w)[1]  # the first pile circle (body 0 is the container)
+    fd = G.FixtureDef()
+    fd.body = 1
+    fd.shape_type = 0
+    fd.radius = 0.5
+    fd.density = 3.0
+    fd.friction = 0.2
+    fid = C.c_int32()
+    lib.check(lib.b2g_fixtures_add(b.h, w, C.byref(fd), 1, C.byref(fid)), "b2g_fixtures_add")
+    assert b.bodies(w)[1].mass > one.mass
+    b.remove(w, fixtures=[fid.value])
+    assert bytes(b.bodies(w)[1]) == bytes(one)
+    bad = (C.c_int32 * 1)(10 ** 6)
+    assert lib.b2g_joints_remove(b.h, w, bad, 1) == 1  # INVALID_ARG
+    b.close()

@@ -818,3 +818,88 @@ def test_set_awake_and_disallowing_sleep(lib, orc):
         assert _state_bytes(batch.bodies(w)) == _state_bytes(ow.bodies()), s
         assert _awake_flags(batch.bodies(w)) == _awake_flags(ow.bodies()), s
     batch.close()
+
+
+def test_destroy_body_fixture_joint(lib, orc):
+    """b2World::DestroyBody / b2Body::DestroyFixture / b2World::DestroyJoint through the C ABI on
+    a settled pyramid and a chain: the destroyed contacts that were touching end (End events,
+    returned at once), the rest of the world keeps its contacts and impulses, and it steps on
+    bit for bit like the oracle loaded with the same post-removal state; the boxes above the
+    removed one fall into the gap."""
+    batch = G.Batch(lib, device=0)
+    w = batch.add_world(0.0, -10.0)
+    batch.set_flags(w, allow_sleep=False)
+    batch.scene(w, G.SCENE_PYRAMID, n=10, p0=1.0, p1=0.6)
+    c = batch.add_world(0.0, -10.0)
+    batch.set_flags(c, allow_sleep=False)
+    batch.scene(c, G.SCENE_CHAINS, seed=2, n=6, p0=60, p1=0.6)
+    batch.step_n(90, 1 / 60, 8, 3)
+    bodies = batch.bodies(w)
+    nb0 = len(bodies)
+    # the bottom-row box nearest the pyramid's middle (body 0 is the ground)
+    mid = min((i for i in range(1, nb0) if bodies[i].c[1] < 1.0), key=lambda i: abs(bodies[i].c[0]))
+    fixtures = batch.fixtures(w)
+    fid = [i for i, f in enumerate(fixtures) if f.body == mid][0]
+    touching = {(x.fixture_a, x.fixture_b) for x in batch.contacts(w) if x.flags & 2 and fid in (x.fixture_a, x.fixture_b)}
+    assert len(touching) >= 3
+    above = [i for i in range(1, nb0) if abs(bodies[i].c[0] - bodies[mid].c[0]) < 0.3 and bodies[i].c[1] > 1.5]
+    ended = batch.remove(w, bodies=[mid])
+    assert {(e.fixture_a, e.fixture_b) for e in ended} == touching and all(e.kind == G.EVENT_END for e in ended)
+    assert len(batch.bodies(w)) == nb0 - 1
+    assert all(fid not in (x.fixture_a, x.fixture_b) for x in batch.contacts(w))
+    # a joint and a fixture of the chain world
+    nj0 = len(batch.joints(c))
+    batch.remove(c, joints=[3])
+    assert len(batch.joints(c)) == nj0 - 1
+    cf = batch.fixtures(c)
+    ended_f = batch.remove(c, fixtures=[len(cf) - 1])
+    assert len(batch.fixtures(c)) == len(cf) - 1
+    assert all(e.kind == G.EVENT_END for e in ended_f)
+    # both worlds step on like the oracle from the post-removal state
+    worlds = [(w, (0.0, -10.0), 8, 3), (c, (0.0, -10.0), 8, 3)]
+    ows = [ob.OracleWorld(orc, g, batch.bodies(x), batch.fixtures(x), batch.joints(x), batch.contacts(x),
+                          inv_dt0=60.0) for x, g, _, _ in worlds]
+    for s in range(60):
+        batch.step(1 / 60, 8, 3)
+        for (x, _, vi, pi), ow in zip(worlds, ows):
+            ow.step(1, 1 / 60, vi, pi)
+            g, o = batch.bodies(x), ow.bodies()
+            assert _state_bytes(g) == _state_bytes(o), f"world {x} step {s + 1}: {_first_diff(g, o)}"
+    after = batch.bodies(w)
+    shift = lambda i: i - 1 if i > mid else i  # noqa: E731
+    assert max(bodies[i].c[1] - after[shift(i)].c[1] for i in above) > 0.2  # the column dropped
+    batch.close()
+
+
+def test_listener_events_match_oracle(lib, orc):
+    """Begin / End / PreSolve / PostSolve events of every step, per world (b2g_events_drain_world)
+    for a pyramid and a chains-over-pile world stepped in one batch, equal the oracle's events
+    (whose event set is pinned to the reference's listener callbacks): kinds, fixture pairs, old
+    manifold point counts, PostSolve impulses bit for bit. Draining one world leaves the
+    other's events in place."""
+    from test_oracle_pins import event_key
+
+    batch = G.Batch(lib, device=0)
+    specs = [(G.SCENE_PYRAMID, 15, 1, 1.0), (G.SCENE_CHAINS, 8, 3, 120.0)]
+    worlds, ows = [], []
+    for kind, n, seed, p0 in specs:
+        w = batch.add_world(0.0, -10.0)
+        batch.set_flags(w, allow_sleep=False)
+        batch.scene(w, kind, seed=seed, n=n, p0=p0, p1=0.6)
+        ow = ob.OracleWorld(orc, (0.0, -10.0), batch.bodies(w), batch.fixtures(w), batch.joints(w))
+        ow.events_enable(True)
+        worlds.append(w)
+        ows.append(ow)
+    batch.events(enable=True)
+    kinds = set()
+    for s in range(150):
+        batch.step(1 / 60, 8, 3)
+        for w, ow in zip(reversed(worlds), reversed(ows)):  # the second world drained first
+            ow.step(1, 1 / 60, 8, 3)
+            got = [event_key(e) for e in batch.world_events(w)]
+            exp = [event_key(e) for e in ow.events()]
+            assert got == exp, f"world {w} step {s + 1}: {len(got)} events against {len(exp)}"
+            kinds |= {k[0] for k in got}
+        assert batch.events() == []  # nothing left once every world drained its own
+    assert kinds == {G.EVENT_BEGIN, G.EVENT_END, G.EVENT_PRESOLVE, G.EVENT_POSTSOLVE}
+    batch.close()

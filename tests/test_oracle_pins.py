@@ -340,3 +340,77 @@ def test_oracle_scene_builder_matches_engine_setup(orc, kind, n, seed, p0):
     assert b"".join(bytes(f) for f in hb.fixtures(w)) == b"".join(bytes(f) for f in F)
     assert b"".join(bytes(j) for j in hb.joints(w)) == b"".join(bytes(j) for j in J)
     hb.close()
+
+
+def event_key(e, impulses=True):
+    """The meaningful content of a listener event: kind, fixture pair (either orientation), the
+    old manifold's point count (PreSolve), the impulse entries the solver filled (PostSolve)."""
+    pc = e.point_count if e.kind == G.EVENT_POSTSOLVE else 0
+    imp = ()
+    if impulses and e.kind == G.EVENT_POSTSOLVE:
+        imp = tuple(e.normal_impulses[:pc]) + tuple(e.tangent_impulses[:pc])
+    old = e.old_manifold.point_count if e.kind == G.EVENT_PRESOLVE else 0
+    return (e.kind, min(e.fixture_a, e.fixture_b), max(e.fixture_a, e.fixture_b), pc, old, imp)
+
+
+@pytest.mark.parametrize("kind,n,seed,p0,warm,vi,pi", [
+    (G.SCENE_PYRAMID, 20, 1, 1.0, 30, 8, 3),
+    (G.SCENE_MIXED_DROP, 400, 5, 0.0, 200, 8, 3),
+    (G.SCENE_CHAINS, 15, 4, 200.0, 80, 10, 4),
+    (G.SCENE_JOINTS, 3, 9, 0.0, 40, 8, 3),
+    (G.SCENE_SLIDERS, 3, 9, 0.0, 40, 8, 3),
+])
+def test_oracle_events_vs_reference_live(ref, orc, kind, n, seed, p0, warm, vi, pi):
+    """Listener events, step by step: the reference's own Step (b2ContactListener callbacks from
+    b2Contact::Update, b2Island::Report and b2ContactManager::Destroy, replaying the oracle's
+    solver order) and the oracle's recorded events are the same set: kinds, fixture pairs, old
+    manifold point counts and PostSolve impulses bit for bit."""
+    rw = ob.RefWorld(ref, kind, seed=seed, n=n, p0=p0, p1=0.6)
+    rw.step(warm, vi=vi, pi=pi)
+    rw.events_enable(True)
+    orc.orc_set_libm_trig(1)
+    seen = set()
+    try:
+        for _ in range(4):
+            ow = ob.OracleWorld(orc, (0.0, -10.0), list(rw.bodies()), list(rw.fixtures()), list(rw.joints()),
+                                list(rw.contacts()), inv_dt0=60.0)
+            ow.events_enable(True)
+            ow.step(1, 1 / 60, vi, pi)
+            pairs, jorder = ow.last_order()
+            arr = (C.c_int32 * max(len(pairs), 1))(*pairs)
+            jar = (C.c_int32 * max(len(jorder), 1))(*jorder)
+            assert ref.ref_replay_step(rw.h, 1 / 60, vi, pi, arr, len(pairs) // 2, jar, len(jorder)) == 0
+            got = sorted(event_key(e) for e in ow.events())
+            exp = sorted(event_key(e) for e in rw.events())
+            assert got == exp
+            seen |= {k[0] for k in got}
+            ow.close()
+    finally:
+        orc.orc_set_libm_trig(0)
+    assert {G.EVENT_PRESOLVE, G.EVENT_POSTSOLVE} <= seen
+
+
+@pytest.mark.parametrize("name", ["mixed", "chains"])
+def test_oracle_events_vs_golden(orc, name):
+    """The listener callbacks of one replayed reference step (golden) equal the oracle's events
+    for the same step from the same state: kinds, pairs, point counts, impulses bit for bit."""
+    g = np.load(GOLD / f"events_{name}.npz")
+    bodies, fixtures = recs(G.Body, g["bodies"]), recs(G.Fixture, g["fixtures"])
+    joints, contacts = recs(G.Joint, g["joints"]), recs(G.Contact, g["contacts"])
+    orc.orc_set_libm_trig(1)
+    try:
+        ow = ob.OracleWorld(orc, (0.0, -10.0), bodies, fixtures, joints, contacts, inv_dt0=60.0)
+        ow.events_enable(True)
+        ow.step(1, 1 / 60, int(g["vi"]), int(g["pi"]))
+        got = sorted(event_key(e) for e in ow.events())
+    finally:
+        orc.orc_set_libm_trig(0)
+    exp = []
+    for (kind, fa, fb, pc, old), imp in zip(g["ints"].tolist(), g["impulses"]):
+        pc = pc if kind == G.EVENT_POSTSOLVE else 0
+        im = tuple(float(x) for x in imp[:pc]) + tuple(float(x) for x in imp[2:2 + pc]) if kind == G.EVENT_POSTSOLVE else ()
+        exp.append((kind, min(fa, fb), max(fa, fb), pc, old if kind == G.EVENT_PRESOLVE else 0,
+                    tuple(np.float32(x) for x in im)))
+    assert got == sorted(exp)
+    kinds = {k[0] for k in got}
+    assert {G.EVENT_BEGIN, G.EVENT_END, G.EVENT_PRESOLVE, G.EVENT_POSTSOLVE} <= kinds
