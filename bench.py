@@ -109,9 +109,27 @@ def world_params(lib, seed):
     return n.value, gx.value, gy.value
 
 
-def shard_seeds(rank, world_size, worlds_per_rank):
-    """World seeds of one rank: disjoint contiguous shards, the same count on every rank."""
-    return [rank * worlds_per_rank + i for i in range(worlds_per_rank)]
+def shard_seeds(rank, world_size, worlds_per_rank, cost=None):
+    """World seeds of one rank. The job steps seeds 0 .. world_size * worlds_per_rank - 1 (weak
+    scaling: worlds_per_rank per GPU on average), cut into contiguous ranges of about equal total
+    cost. cost(seed) is a world's cost; by default each world counts 1 (equal world counts). The
+    benchmark passes the world's body count, which its contacts and joints grow with (a world's
+    step work is about proportional to bodies + contacts)."""
+    total = world_size * worlds_per_rank
+    if world_size == 1:
+        return list(range(total))
+    w = [float(cost(s)) if cost else 1.0 for s in range(total)]
+    whole = sum(w)
+    acc, cuts = 0.0, [0]
+    for s in range(total):
+        acc += w[s]
+        # a range ends once its running cost passes the next 1/world_size of the whole
+        while len(cuts) < world_size and acc >= whole * len(cuts) / world_size:
+            cuts.append(s + 1)
+    while len(cuts) < world_size:
+        cuts.append(total)
+    cuts.append(total)
+    return list(range(cuts[rank], cuts[rank + 1]))
 
 
 def reduce_over_ranks(ms_per_step, bodies, device):
@@ -418,7 +436,7 @@ def run_ours(args, rank, world_size):
 
     lib = G.Lib()
     dev = int(os.environ.get("LOCAL_RANK", "0"))
-    seeds = shard_seeds(rank, world_size, args.worlds)
+    seeds = shard_seeds(rank, world_size, args.worlds, cost=lambda s: world_params(lib, s)[0])
     # autotune the solver's threads per world on a settled sample of the same worlds (every 8th);
     # results do not depend on the choice, so the timed batch just takes it
     threads, tune_s = None, 0.0

@@ -8,8 +8,8 @@ Run where the reference sources are checked out and oracle/_ref/libb2ref.so is b
 Every vector is an output of the reference's own code (compiled from its sources) on seeded
 inputs: polygon hulls and mass data (b2PolygonShape::Set / SetAsBox / ComputeMass), manifolds of
 the five collide functions, one replayed solver step (b2Island::Solve in a given constraint
-order) on exported world states, the listener callbacks of one replayed step, and the final
-state of 256-step reference rollouts.
+order) on exported world states, the listener callbacks of one replayed step, the final state of
+a 256-step reference rollout, and the physical measures of 256-step reference rollouts.
 """
 from __future__ import annotations
 
@@ -152,6 +152,23 @@ def rollout(ref, name, kind, n, seed, p0, steps, vi, pi):
                         steps=steps, vi=vi, pi=pi)
 
 
+MEASURE_KEYS = ("linear", "angular", "com_height", "top_height", "penetration")
+
+
+def measures(ref, orc, name, kind, n, seed, p0, steps, vi, pi, every=32):
+    """Physical measures (oracle_bind.rollout_measures) of the reference's own rollout every
+    `every` steps: linear momentum (2), angular momentum, centre-of-mass height, top height and
+    deepest penetration per row."""
+    rw = ob.RefWorld(ref, kind, seed=seed, n=n, p0=p0, p1=0.6)
+    rows = []
+    for _ in range(steps // every):
+        rw.step(every, vi=vi, pi=pi)
+        m = ob.rollout_measures(orc, list(rw.bodies()), list(rw.fixtures()), list(rw.contacts()))
+        rows.append([m["linear"][0], m["linear"][1], m["angular"], m["com_height"], m["top_height"], m["penetration"]])
+    np.savez_compressed(HERE / f"measures_{name}.npz", rows=np.array(rows, np.float64), every=every, steps=steps,
+                        vi=vi, pi=pi, kind=kind, n=n, seed=seed, p0=p0)
+
+
 def main():
     ref = ob.Ref()
     orc = ob.Oracle()
@@ -165,6 +182,9 @@ def main():
     rollout(ref, "pyramid", G.SCENE_PYRAMID, 20, 1, 1.0, 256, 8, 3)
     events(ref, orc, "mixed", G.SCENE_MIXED_DROP, 400, 5, 0.0, 200, 8, 3)
     events(ref, orc, "chains", G.SCENE_CHAINS, 15, 4, 200.0, 80, 10, 4)
+    measures(ref, orc, "pyramid", G.SCENE_PYRAMID, 20, 1, 1.0, 256, 8, 3)
+    measures(ref, orc, "mixed", G.SCENE_MIXED_DROP, 300, 3, 0.0, 256, 8, 3)
+    measures(ref, orc, "chains", G.SCENE_CHAINS, 10, 2, 150.0, 256, 10, 4)
     print("golden vectors written to", HERE)
 
 

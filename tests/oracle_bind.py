@@ -342,3 +342,74 @@ class OracleWorld:
         jp = (u32 * max(nj, 1))()
         self.orc.orc_world_solver_order(self.h, cc, cp, nc, jc, jp, nj)
         return list(cc[:nc]), list(cp[:nc]), list(jc[:nj]), list(jp[:nj])
+
+
+def rollout_measures(orc, bodies, fixtures, contacts):
+    """Physical measures of a world state, for judging rollouts whose Gauss-Seidel orders differ:
+    linear momentum per unit mass (m/s, 2-vector), angular momentum about the origin per unit mass
+    (m^2/s), height of the centre of mass and of the highest body centre (m) over the dynamic
+    bodies, and the deepest penetration (m): minus the smallest world-manifold separation over the
+    touching contacts (b2WorldManifold::Initialize, src/collision/b2_collision.cpp:26-90),
+    0 when nothing overlaps."""
+    import numpy as np  # noqa: PLC0415
+
+    b = G.body_array_to_numpy((G.Body * len(bodies))(*bodies))
+    dyn = b["type"] == G.DYNAMIC
+    m = b["mass"][dyn].astype(np.float64)
+    v = b["v"][dyn].astype(np.float64)
+    c = b["c"][dyn].astype(np.float64)
+    w = b["w"][dyn].astype(np.float64)
+    inertia = b["inertia"][dyn].astype(np.float64)
+    total = m.sum()
+    lin = (m[:, None] * v).sum(axis=0) / total
+    ang = (inertia * w + m * (c[:, 0] * v[:, 1] - c[:, 1] * v[:, 0])).sum() / total
+    pen = 0.0
+    out = (f32 * 8)()
+    for ct in contacts:
+        if not ct.flags & 2 or ct.manifold.point_count == 0:
+            continue
+        fa, fb = fixtures[ct.fixture_a], fixtures[ct.fixture_b]
+        xa = (f32 * 4)(*bodies[fa.body].xf)
+        xb = (f32 * 4)(*bodies[fb.body].xf)
+        orc.orc_world_manifold(ct.manifold, xa, fa.shape.radius, xb, fb.shape.radius, out)
+        for j in range(ct.manifold.point_count):
+            pen = max(pen, -out[6 + j])
+    return {"linear": lin, "angular": ang, "com_height": float((m * c[:, 1]).sum() / total),
+            "top_height": float(c[:, 1].max()), "penetration": pen}
+
+
+# Tolerances of a rollout judged against the reference's own rollout by physical measures (the
+# two differ in Gauss-Seidel order, so states agree to rounding at first and then diverge within
+# the physics): per measure, the largest difference allowed at any checkpoint (every 32 steps),
+# and the largest penetration either may show. Units: m/s, m^2/s, m, m, m.
+ROLLOUT_TOLERANCES = {
+    # 210 boxes settling into a stack: everything close
+    "pyramid": {"linear": 0.05, "angular": 0.3, "com_height": 0.01, "top_height": 0.02, "penetration": 0.01,
+                "max_penetration": 0.06},
+    # 300 mixed shapes landing in a U: chaotic while they land, settled by step 256
+    "mixed": {"linear": 0.75, "angular": 4.0, "com_height": 0.15, "top_height": 0.6, "penetration": 0.15,
+              "max_penetration": 0.35},
+    # 10 swinging chains over 150 circles: the chains' swing is chaotic
+    "chains": {"linear": 0.5, "angular": 5.0, "com_height": 0.1, "top_height": 0.1, "penetration": 0.05,
+               "max_penetration": 0.15},
+}
+
+
+def measure_row(m):
+    return [m["linear"][0], m["linear"][1], m["angular"], m["com_height"], m["top_height"], m["penetration"]]
+
+
+def check_rollout_measures(name, rows, golden_rows):
+    """Asserts that measure rows (one per checkpoint, as measure_row) stay within the scene's
+    tolerances of the reference's rows."""
+    import numpy as np  # noqa: PLC0415
+
+    tol = ROLLOUT_TOLERANCES[name]
+    got, exp = np.asarray(rows, np.float64), np.asarray(golden_rows, np.float64)
+    assert got.shape == exp.shape
+    lin = np.hypot(got[:, 0] - exp[:, 0], got[:, 1] - exp[:, 1])
+    checks = {"linear": lin, "angular": np.abs(got[:, 2] - exp[:, 2]), "com_height": np.abs(got[:, 3] - exp[:, 3]),
+              "top_height": np.abs(got[:, 4] - exp[:, 4]), "penetration": np.abs(got[:, 5] - exp[:, 5])}
+    for k, d in checks.items():
+        assert d.max() <= tol[k], f"{name}: {k} differs by {d.max():.4f} (> {tol[k]}) at checkpoint {int(d.argmax())}"
+    assert got[:, 5].max() <= tol["max_penetration"] and exp[:, 5].max() <= tol["max_penetration"]

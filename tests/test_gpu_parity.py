@@ -903,3 +903,26 @@ def test_listener_events_match_oracle(lib, orc):
         assert batch.events() == []  # nothing left once every world drained its own
     assert kinds == {G.EVENT_BEGIN, G.EVENT_END, G.EVENT_PRESOLVE, G.EVENT_POSTSOLVE}
     batch.close()
+
+
+@pytest.mark.parametrize("name", ["pyramid", "mixed", "chains"])
+def test_rollout_measures_vs_reference_golden(lib, orc, name):
+    """The GPU's 256-step rollouts of the pyramid, a mixed drop and chains over a pile against the
+    reference's own rollouts, by physical measures every 32 steps (momentum, centre-of-mass and
+    top height, deepest penetration), within ob.ROLLOUT_TOLERANCES."""
+    from pathlib import Path
+
+    g = np.load(Path(__file__).resolve().parent / "golden" / f"measures_{name}.npz")
+    kind, n, seed, p0 = int(g["kind"]), int(g["n"]), int(g["seed"]), float(g["p0"])
+    every, vi, pi = int(g["every"]), int(g["vi"]), int(g["pi"])
+    batch = G.Batch(lib, device=0)
+    w = batch.add_world(0.0, -10.0)
+    batch.set_flags(w, allow_sleep=False)
+    batch.scene(w, kind, seed=seed, n=n, p0=p0, p1=0.6)
+    fixtures = list(batch.fixtures(w))
+    rows = []
+    for _ in range(len(g["rows"])):
+        batch.step_n(every, 1 / 60, vi, pi, use_graph=True)
+        rows.append(ob.measure_row(ob.rollout_measures(orc, list(batch.bodies(w)), fixtures, list(batch.contacts(w)))))
+    ob.check_rollout_measures(name, rows, g["rows"])
+    batch.close()

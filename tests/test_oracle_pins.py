@@ -414,3 +414,25 @@ def test_oracle_events_vs_golden(orc, name):
     assert got == sorted(exp)
     kinds = {k[0] for k in got}
     assert {G.EVENT_BEGIN, G.EVENT_END, G.EVENT_PRESOLVE, G.EVENT_POSTSOLVE} <= kinds
+
+
+@pytest.mark.parametrize("name", ["pyramid", "mixed", "chains"])
+def test_oracle_rollout_measures_vs_reference_golden(orc, name):
+    """256-step rollouts of the pyramid (210 boxes), a 300-body mixed drop and 10 chains over 150
+    circles: the oracle (the engine's colour order) against the reference's own rollout (its own
+    order), by linear and angular momentum, centre-of-mass and top height, and the deepest
+    penetration every 32 steps, each within the tolerance ob.ROLLOUT_TOLERANCES states."""
+    g = np.load(GOLD / f"measures_{name}.npz")
+    kind, n, seed, p0 = int(g["kind"]), int(g["n"]), int(g["seed"]), float(g["p0"])
+    every, vi, pi = int(g["every"]), int(g["vi"]), int(g["pi"])
+    hb = _host_batch()
+    w = hb.add_world(0.0, -10.0)
+    hb.scene(w, kind, seed=seed, n=n, p0=p0, p1=0.6)
+    fixtures = list(hb.fixtures(w))
+    ow = ob.OracleWorld(orc, (0.0, -10.0), hb.bodies(w), fixtures, hb.joints(w))
+    rows = []
+    for _ in range(len(g["rows"])):
+        ow.step(every, 1 / 60, vi, pi)
+        rows.append(ob.measure_row(ob.rollout_measures(orc, list(ow.bodies()), fixtures, list(ow.contacts()))))
+    ob.check_rollout_measures(name, rows, g["rows"])
+    hb.close()
