@@ -23,9 +23,9 @@ STATIC, KINEMATIC, DYNAMIC = 0, 1, 2
 SHAPE_CIRCLE, SHAPE_EDGE, SHAPE_POLYGON = 0, 1, 2
 JOINT_REVOLUTE, JOINT_PRISMATIC, JOINT_DISTANCE = 1, 2, 3
 POLY_HULL, POLY_BOX, POLY_BOX_ORIENTED, POLY_RAW = 0, 1, 2, 3
-SCENE_PYRAMID, SCENE_MIXED_DROP, SCENE_CHAINS, SCENE_BATCH_WORLD, SCENE_JOINTS, SCENE_SLIDERS = 0, 1, 2, 3, 4, 5
+SCENE_PYRAMID, SCENE_MIXED_DROP, SCENE_CHAINS, SCENE_BATCH_WORLD, SCENE_JOINTS, SCENE_SLIDERS, SCENE_GEARS = 0, 1, 2, 3, 4, 5, 6
 JOINT_REVOLUTE, JOINT_PRISMATIC, JOINT_DISTANCE, JOINT_PULLEY, JOINT_MOUSE = 1, 2, 3, 4, 5
-JOINT_WHEEL, JOINT_WELD, JOINT_FRICTION, JOINT_MOTOR = 7, 8, 9, 11
+JOINT_WHEEL, JOINT_WELD, JOINT_FRICTION, JOINT_MOTOR, JOINT_GEAR = 7, 8, 9, 11, 6
 BODY_ENABLED, BODY_FIXED_ROTATION, BODY_BULLET, BODY_AWAKE, BODY_AUTO_SLEEP = 1, 2, 4, 8, 16
 HOST_ONLY = -1  # B2G_HOST_ONLY: a batch built and read on the host only (no device)
 EVENT_BEGIN, EVENT_END, EVENT_PRESOLVE, EVENT_POSTSOLVE = 1, 2, 3, 4
@@ -81,7 +81,8 @@ class JointDef(C.Structure):
                 ("linear_offset", F2), ("max_force", C.c_float), ("max_torque", C.c_float),
                 ("correction_factor", C.c_float), ("target", F2), ("ground_anchor_a", F2),
                 ("ground_anchor_b", F2), ("length_a", C.c_float), ("length_b", C.c_float),
-                ("ratio", C.c_float), ("user_data", C.c_uint64)]
+                ("ratio", C.c_float), ("user_data", C.c_uint64), ("joint_1", C.c_int32),
+                ("joint_2", C.c_int32), ("gear_constant", C.c_float), ("reserved", C.c_int32)]
 
 
 class Body(C.Structure):

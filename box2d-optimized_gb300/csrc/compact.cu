@@ -58,6 +58,10 @@ __global__ void k_compact_joints(CompactTables t, int n, const JointDev* s, cons
   J.d.body_b += db;
   J.iA += db;
   J.iB += db;
+  if (J.d.type == B2G_JOINT_GEAR) {
+    J.g.iC += db;
+    J.g.iD += db;
+  }
   d[on.z + (oj - oo.z)] = J;
 }
 

@@ -175,6 +175,26 @@ static KernelArgs make_args(Batch* b) {
 // Per-joint constants set by the reference's joint constructors: the prismatic and wheel axes
 // (b2_prismatic_joint.cpp:84-90, b2_wheel_joint.cpp:44-45) and the pulley's rope constant
 // (b2_pulley_joint.cpp:67).
+// A gear's device record from its world's two coupled joints (bo: the world's first body).
+static void init_gear_dev(const HostWorld& hw, const b2g_joint_def& def, int bo, JointDev* d) {
+  const b2g_joint_def& j1 = hw.joints[def.joint_1].def;
+  const b2g_joint_def& j2 = hw.joints[def.joint_2].def;
+  JointDev::Gear& g = d->g;
+  g.iC = bo + j1.body_a;
+  g.iD = bo + j2.body_a;
+  g.typeA = j1.type;
+  g.typeB = j2.type;
+  g.lC[0] = j1.local_anchor_a[0]; g.lC[1] = j1.local_anchor_a[1];
+  g.lA[0] = j1.local_anchor_b[0]; g.lA[1] = j1.local_anchor_b[1];
+  g.lD[0] = j2.local_anchor_a[0]; g.lD[1] = j2.local_anchor_a[1];
+  g.lB[0] = j2.local_anchor_b[0]; g.lB[1] = j2.local_anchor_b[1];
+  g.refA = j1.reference_angle;
+  g.refB = j2.reference_angle;
+  g.axC[0] = g.axC[1] = g.axD[0] = g.axD[1] = 0.0f;
+  if (j1.type == B2G_JOINT_PRISMATIC) { g.axC[0] = j1.local_axis_a[0]; g.axC[1] = j1.local_axis_a[1]; }
+  if (j2.type == B2G_JOINT_PRISMATIC) { g.axD[0] = j2.local_axis_a[0]; g.axD[1] = j2.local_axis_a[1]; }
+}
+
 static void init_joint_dev(const b2g_joint_def& def, JointDev* d) {
   if (def.type == B2G_JOINT_PRISMATIC || def.type == B2G_JOINT_WHEEL) {
     V2 ax = mk(def.local_axis_a[0], def.local_axis_a[1]);
@@ -336,6 +356,7 @@ int upload_all(Batch* b) {
       d.impulse[0] = j.impulse[0]; d.impulse[1] = j.impulse[1]; d.impulse[2] = j.impulse[2];
       d.motorImpulse = j.motor_impulse; d.lowerImpulse = j.lower_impulse; d.upperImpulse = j.upper_impulse;
       init_joint_dev(j.def, &d);
+      if (j.def.type == B2G_JOINT_GEAR) init_gear_dev(hw, j.def, bo, &d);
       if (!j.def.collide_connected) {
         uint32_t x = (uint32_t)(bo + j.def.body_a), y = (uint32_t)(bo + j.def.body_b);
         if (x > y) std::swap(x, y);
@@ -549,6 +570,7 @@ static int pack_tail(Batch* b, TailPack& P) {
       d.impulse[0] = j.impulse[0]; d.impulse[1] = j.impulse[1]; d.impulse[2] = j.impulse[2];
       d.motorImpulse = j.motor_impulse; d.lowerImpulse = j.lower_impulse; d.upperImpulse = j.upper_impulse;
       init_joint_dev(j.def, &d);
+      if (j.def.type == B2G_JOINT_GEAR) init_gear_dev(hw, j.def, bo, &d);
       P.joints.push_back(d);
       if (!j.def.collide_connected) {
         uint32_t x = (uint32_t)(bo + j.def.body_a), y = (uint32_t)(bo + j.def.body_b);
@@ -748,6 +770,10 @@ int download_state(Batch* b) {
         V2 f = d.impulse[0] * mk(d.uB[0], d.uB[1]);
         r.reaction_impulse[0] = f.x; r.reaction_impulse[1] = f.y;
         r.reaction_angular_impulse = 0.0f;
+      } else if (r.def.type == B2G_JOINT_GEAR) {  // b2_gear_joint.cpp:387-397
+        r.reaction_impulse[0] = d.impulse[0] * d.g.JvAC[0];
+        r.reaction_impulse[1] = d.impulse[0] * d.g.JvAC[1];
+        r.reaction_angular_impulse = d.impulse[0] * d.g.JwA;
       } else {  // weld, motor, friction (x, y, angular), mouse (x, y)
         r.reaction_impulse[0] = d.impulse[0];
         r.reaction_impulse[1] = d.impulse[1];
@@ -1387,7 +1413,7 @@ B2G_API int b2g_world_add(b2g_batch* b, float gx, float gy, int32_t* out_world) 
 extern "C++" {
 namespace {
 const uint32_t kSnapMagic = 0x53473242u;  // "B2GS"
-const uint32_t kSnapVersion = 2;  // 2: body sleep timers
+const uint32_t kSnapVersion = 3;  // 2: body sleep timers; 3: gear joint fields
 struct SnapshotHeader {
   uint32_t magic, version;
   uint32_t nb, nf, nj, nc;
@@ -1811,9 +1837,27 @@ B2G_API int b2g_joints_add(b2g_batch* b, int32_t world, const b2g_joint_def* def
     const int t = d.type;
     if (t != B2G_JOINT_REVOLUTE && t != B2G_JOINT_PRISMATIC && t != B2G_JOINT_DISTANCE && t != B2G_JOINT_PULLEY &&
         t != B2G_JOINT_MOUSE && t != B2G_JOINT_WHEEL && t != B2G_JOINT_WELD && t != B2G_JOINT_FRICTION &&
-        t != B2G_JOINT_MOTOR) {
+        t != B2G_JOINT_MOTOR && t != B2G_JOINT_GEAR) {
       set_error(b, "unsupported joint type");
       return B2G_E_INVALID_ARG;
+    }
+    if (t == B2G_JOINT_GEAR) {  // two earlier revolute / prismatic joints, their bodies B dynamic
+      const int have = (int)w0.joints.size() + i;
+      auto typeOf = [&](int k) { return k < (int)w0.joints.size() ? w0.joints[k].def.type : defs[k - w0.joints.size()].type; };
+      auto bodyB = [&](int k) { return k < (int)w0.joints.size() ? w0.joints[k].def.body_b : defs[k - w0.joints.size()].body_b; };
+      bool ok = d.joint_1 >= 0 && d.joint_1 < have && d.joint_2 >= 0 && d.joint_2 < have && d.joint_1 != d.joint_2 &&
+                std::isfinite(d.ratio);
+      for (int k : {d.joint_1, d.joint_2}) {
+        if (!ok) break;
+        const int tk = typeOf(k);
+        ok = (tk == B2G_JOINT_REVOLUTE || tk == B2G_JOINT_PRISMATIC) && bodyB(k) >= 0 &&
+             bodyB(k) < (int)w0.bodies.size() && w0.bodies[bodyB(k)].type == B2G_DYNAMIC;
+      }
+      if (!ok) {
+        set_error(b, "a gear joint needs two earlier revolute or prismatic joints with dynamic bodies B");
+        return B2G_E_INVALID_ARG;
+      }
+      continue;
     }
     if (t == B2G_JOINT_PULLEY && !(d.ratio != 0.0f)) {  // b2PulleyJoint ctor asserts ratio != 0
       set_error(b, "pulley ratio must be non-zero");
@@ -1842,6 +1886,27 @@ B2G_API int b2g_joints_add(b2g_batch* b, int32_t world, const b2g_joint_def* def
       j.def.length = fmax2(j.def.length, B2G_LINEAR_SLOP);
       j.def.min_length = fmax2(j.def.min_length, B2G_LINEAR_SLOP);
       j.def.max_length = fmax2(j.def.max_length, j.def.min_length);
+    } else if (j.def.type == B2G_JOINT_GEAR) {
+      // b2GearJoint ctor (src/dynamics/b2_gear_joint.cpp:48-139): bodies A, B from the joints'
+      // bodies B, C, D from their bodies A; the constant from the joints' coordinates now
+      const b2g_joint_def& j1 = w.joints[j.def.joint_1].def;
+      const b2g_joint_def& j2 = w.joints[j.def.joint_2].def;
+      auto coordinate = [&](const b2g_joint_def& jd) {
+        const b2g_body& bx = w.bodies[jd.body_b];  // the gear's A (or B)
+        const b2g_body& by = w.bodies[jd.body_a];  // the gear's C (or D)
+        if (jd.type == B2G_JOINT_REVOLUTE) return (bx.a - by.a) - jd.reference_angle;
+        Rot qx, qy;
+        qx.s = bx.xf[2]; qx.c = bx.xf[3];
+        qy.s = by.xf[2]; qy.c = by.xf[3];
+        const V2 pC = mk(jd.local_anchor_a[0], jd.local_anchor_a[1]);
+        const V2 pA = mulT(qy, mul(qx, mk(jd.local_anchor_b[0], jd.local_anchor_b[1])) +
+                                   (mk(bx.xf[0], bx.xf[1]) - mk(by.xf[0], by.xf[1])));
+        return dot(pA - pC, mk(jd.local_axis_a[0], jd.local_axis_a[1]));
+      };
+      j.def.body_a = j1.body_b;
+      j.def.body_b = j2.body_b;
+      const float coordinateA = coordinate(j1), coordinateB = coordinate(j2);
+      j.def.gear_constant = coordinateA + j.def.ratio * coordinateB;
     } else if (j.def.type == B2G_JOINT_MOUSE) {
       // b2MouseJoint ctor: the target in body B's frame (b2_mouse_joint.cpp:38-40, b2MulT)
       const b2g_body& bB = w.bodies[j.def.body_b];
@@ -1885,6 +1950,10 @@ static int remove_structure(Batch* b, int32_t world, std::vector<char> deadBody,
     if (deadBody[w.fixtures[f].body]) deadFix[f] = 1;
   for (int j = 0; j < nj; ++j)
     if (deadBody[w.joints[j].def.body_a] || deadBody[w.joints[j].def.body_b]) deadJoint[j] = 1;
+  // a gear goes with either joint it couples (gears follow their joints in creation order)
+  for (int j = 0; j < nj; ++j)
+    if (w.joints[j].def.type == B2G_JOINT_GEAR && (deadJoint[w.joints[j].def.joint_1] || deadJoint[w.joints[j].def.joint_2]))
+      deadJoint[j] = 1;
   w.body_sleep.resize(nb, 0.0f);
   for (int j = 0; j < nj; ++j)
     if (deadJoint[j]) {
@@ -1950,6 +2019,10 @@ static int remove_structure(Batch* b, int32_t world, std::vector<char> deadBody,
   for (b2g_joint& j : w.joints) {
     j.def.body_a = bmap[j.def.body_a];
     j.def.body_b = bmap[j.def.body_b];
+    if (j.def.type == B2G_JOINT_GEAR) {
+      j.def.joint_1 = jmap[j.def.joint_1];
+      j.def.joint_2 = jmap[j.def.joint_2];
+    }
   }
   for (std::vector<int>& lst : w.body_fixtures) {
     size_t o = 0;

@@ -49,6 +49,19 @@ struct JointDev {
   float springMass, motorMass;
   float err[2], angularError;
   float uB[2], constant;
+  // gear (b2_gear_joint.h:52-110): bodies C (joint 1's body A) and D (joint 2's body A), the
+  // geometry taken from the two joints on upload, and the step temporaries; A and B are d.body_a
+  // / d.body_b (the two joints' bodies B). The gear's impulse is impulse[0].
+  struct Gear {
+    int iC, iD;               // global body indices
+    int typeA, typeB;         // B2G_JOINT_REVOLUTE or B2G_JOINT_PRISMATIC (joint 1, joint 2)
+    float lA[2], lB[2], lC[2], lD[2];  // local anchors on A, B, C, D
+    float axC[2], axD[2];     // joint 1's / joint 2's local axis (prismatic)
+    float refA, refB;         // the joints' reference angles
+    float lcA[2], lcB[2], lcC[2], lcD[2];
+    float mA, mB, mC, mD, iA, iB, iC_, iD_;
+    float JvAC[2], JvBD[2], JwA, JwB, JwC, JwD, mass;
+  } g;
 };
 
 // Per-contact velocity / position constraint (b2ContactVelocityConstraint and

@@ -618,6 +618,7 @@ void b2World::DestroyBody(b2Body* body) {
     if (m_joints[i]->m_bodyA == body || m_joints[i]->m_bodyB == body) m_joints.erase(m_joints.begin() + i);
     else ++i;
   }
+  EraseOrphanGears();
   for (b2Fixture* f = body->m_fixtureList; f; f = f->m_next) f->m_index = -1;
   b2Body* prev = nullptr;
   for (b2Body* x = m_bodyHead; x && x != body; x = x->m_next) prev = x;
@@ -638,7 +639,29 @@ void b2World::DestroyJoint(b2Joint* joint) {
   m_lastStatus = b2g_joints_remove(m_batch, m_index, &idx, 1);
   if (m_lastStatus != B2G_OK) return;
   m_joints.erase(m_joints.begin() + i);
+  EraseOrphanGears();
   Renumber();
+}
+
+// The engine removes a gear together with either joint it couples; the facade follows.
+void b2World::EraseOrphanGears() {
+  for (bool again = true; again;) {
+    again = false;
+    for (size_t i = 0; i < m_joints.size(); ++i) {
+      if (m_joints[i]->m_type != e_gearJoint) continue;
+      b2GearJoint* g = (b2GearJoint*)m_joints[i].get();
+      bool alive1 = false, alive2 = false;
+      for (auto& x : m_joints) {
+        alive1 |= x.get() == g->m_joint1;
+        alive2 |= x.get() == g->m_joint2;
+      }
+      if (!alive1 || !alive2) {
+        m_joints.erase(m_joints.begin() + i);
+        again = true;
+        break;
+      }
+    }
+  }
 }
 
 void b2Body::DestroyFixture(b2Fixture* fixture) {
@@ -728,6 +751,21 @@ b2Joint* b2World::CreateJoint(const b2JointDef* def) {
     d.reference_angle = q->angularOffset;
     d.max_force = q->maxForce; d.max_torque = q->maxTorque; d.correction_factor = q->correctionFactor;
     j.reset(new b2MotorJoint());
+  } else if (def->type == e_gearJoint) {
+    const b2GearJointDef* q = (const b2GearJointDef*)def;
+    if (!q->joint1 || !q->joint2 || q->joint1->m_world != this || q->joint2->m_world != this) return nullptr;
+    d.type = B2G_JOINT_GEAR;
+    d.joint_1 = q->joint1->m_index;
+    d.joint_2 = q->joint2->m_index;
+    d.ratio = q->ratio;
+    // the gear's bodies and anchors are its joints' bodies B (b2_gear_joint.cpp:62-110)
+    la = q->joint1->m_localAnchorB;
+    lb = q->joint2->m_localAnchorB;
+    b2GearJoint* g = new b2GearJoint();
+    g->m_joint1 = q->joint1;
+    g->m_joint2 = q->joint2;
+    g->m_ratio = q->ratio;
+    j.reset(g);
   } else if (def->type == e_frictionJoint) {
     const b2FrictionJointDef* q = (const b2FrictionJointDef*)def;
     d.type = B2G_JOINT_FRICTION;
@@ -764,6 +802,11 @@ b2Joint* b2World::CreateJoint(const b2JointDef* def) {
   j->m_type = def->type;
   j->m_bodyA = def->bodyA;
   j->m_bodyB = def->bodyB;
+  if (def->type == e_gearJoint) {  // b2GearJoint::b2GearJoint replaces the def's bodies
+    const b2GearJointDef* q = (const b2GearJointDef*)def;
+    j->m_bodyA = q->joint1->m_bodyB;
+    j->m_bodyB = q->joint2->m_bodyB;
+  }
   j->m_collideConnected = def->collideConnected;
   j->m_localAnchorA = la;
   j->m_localAnchorB = lb;
@@ -917,6 +960,7 @@ extern "C" B2G_API int b2g_scene_build(b2g_batch* b, int32_t world, int32_t kind
   else if (kind == B2G_SCENE_BATCH_WORLD) c = b2scenes::BatchWorld(&w, seed, n);
   else if (kind == B2G_SCENE_JOINTS) c = b2scenes::JointZoo(&w, n, seed);
   else if (kind == B2G_SCENE_SLIDERS) c = b2scenes::SliderRigs(&w, n, seed);
+  else if (kind == B2G_SCENE_GEARS) c = b2scenes::GearRigs(&w, n, seed);
   else return B2G_E_INVALID_ARG;
   if (counts) { counts[0] = c.bodies; counts[1] = c.fixtures; counts[2] = c.joints; }
   return B2G_OK;

@@ -38,8 +38,10 @@ __global__ void __launch_bounds__(T) k_joint_colour(KernelArgs a, int w0) {
   for (int k = threadIdx.x; k < nj; k += T) {
     const JointDev& J = a.joints[j0 + k];
     int ia = J.d.body_a, ib = J.d.body_b;
-    a.jcb[j0 + k] = make_int2((ia - b0) | (a.btype[ia] == B2G_STATIC ? (int)0x80000000 : 0),
-                              (ib - b0) | (a.btype[ib] == B2G_STATIC ? (int)0x80000000 : 0));
+    a.jcb[j0 + k] = J.d.type == B2G_JOINT_GEAR
+                        ? make_int2(B2G_CB_SERIAL, B2G_CB_SERIAL)
+                        : make_int2((ia - b0) | (a.btype[ia] == B2G_STATIC ? (int)0x80000000 : 0),
+                                    (ib - b0) | (a.btype[ib] == B2G_STATIC ? (int)0x80000000 : 0));
     a.jprio[j0 + k] = jointPriority((uint32_t)k);
   }
   __syncthreads();

@@ -208,6 +208,10 @@ __device__ __forceinline__ int block_exclusive_scan(Team& tm, int n, Get get, Pu
   return total;
 }
 
+// Constraint bodies (ColourMem::cb) of a constraint that is always solved serially (colour 63):
+// a gear joint, which moves four bodies. Bits 31 and 30: no world-local body index has bit 30 set.
+#define B2G_CB_SERIAL ((int)0xC0000000)
+
 // Working arrays of one colouring, each in shared or global memory (generic pointers).
 struct ColourMem {
   int* cnt;                  // per body: incidence count, then fill counter
@@ -309,7 +313,7 @@ __device__ int colour_constraints(Team& tm, int n, int nb, const ColourMem m, co
           unsigned long long used = (b.x >= 0 ? m.mask[b.x] : 0ull) | (b.y >= 0 ? m.mask[b.y] : 0ull);
           unsigned long long freeBits = ~used & ((1ull << 63) - 1ull);
           int c;
-          if (freeBits == 0ull) {
+          if (freeBits == 0ull || b.x == B2G_CB_SERIAL) {
             c = 63;
           } else {
             c = __ffsll((long long)freeBits) - 1;
@@ -940,9 +944,14 @@ __device__ __forceinline__ void solve_world(Team& tm, const KernelArgs& a, int w
     const int step = c == 63 ? 1 : NT, i0 = c == 63 ? s : s + tid;
     if (c != 63 || tid == 0)
       for (int i = i0; i < e; i += step) {
-        const JointDev& J = a.joints[j0 + a.jorder[j0 + i]];
+        JointDev& J = a.joints[j0 + a.jorder[j0 + i]];
         if (sleepMode && !joint_awake(a, J)) {
           jointPackAsleep(a.jplanes, j0 + i);
+          continue;
+        }
+        if (c == 63 && J.d.type == B2G_JOINT_GEAR) {  // gears are coloured 63: one thread, on the record
+          gearInit(J, a.massd, a.lc, a.pos, jb, warm);
+          jointPackGear(a.jplanes, j0 + i, J.d.body_a, J.d.body_b);
           continue;
         }
         jointInitSlot(J, a.jplanes, a.jstride, j0 + i, a.massd, a.lc, a.pos, jb, a.dt, dtRatio, warm);
@@ -956,7 +965,10 @@ __device__ __forceinline__ void solve_world(Team& tm, const KernelArgs& a, int w
       int s = jranges[c], e = jranges[c + 1];
       const int step = c == 63 ? 1 : NT, i0 = c == 63 ? s : s + tid;
       if (c != 63 || tid == 0)
-        for (int i = i0; i < e; i += step) jointSolveVelocitySlot(a.jplanes, a.jstride, j0 + i, jb, a.dt, a.inv_dt);
+        for (int i = i0; i < e; i += step) {
+          if (c == 63 && jointSlotIsGear(a.jplanes, j0 + i)) gearSolveVelocity(a.joints[j0 + a.jorder[j0 + i]], jb);
+          else jointSolveVelocitySlot(a.jplanes, a.jstride, j0 + i, jb, a.dt, a.inv_dt);
+        }
       tm.sync();
     }
     colour_sweep<Team, VelRows, PREFETCH>(tm, cranges, ncc, c0, fetchV, [&](int slot, const VelRows& r) {
@@ -968,7 +980,8 @@ __device__ __forceinline__ void solve_world(Team& tm, const KernelArgs& a, int w
   }
 
   // 7. StoreImpulses (b2_contact_solver.cpp:641-657); the joints' impulses back into their records
-  for (int i = tid; i < nj; i += NT) jointStoreImpulses(a.jplanes, a.jstride, j0 + i, a.joints[j0 + a.jorder[j0 + i]]);
+  for (int i = tid; i < nj; i += NT)  // a gear's impulse is already on its record
+    if (!jointSlotIsGear(a.jplanes, j0 + i)) jointStoreImpulses(a.jplanes, a.jstride, j0 + i, a.joints[j0 + a.jorder[j0 + i]]);
   for (int p = tid; p < nsc; p += NT) {
     int pc = (P.idx[c0 + p].x >> 24) & 15;
     float4 im = P.imp[c0 + p];
@@ -1041,7 +1054,10 @@ __device__ __forceinline__ void solve_world(Team& tm, const KernelArgs& a, int w
             root = isl_root<S>(SL, __float_as_int(h.x) - b0, __float_as_int(h.y) - b0);
             if (isl_bits<S>(SL, root) & B2G_ISL_DONE) continue;
           }
-          if (!jointSolvePositionSlot(a.jplanes, a.jstride, j0 + i, jp)) {
+          const bool ok = (c == 63 && jointSlotIsGear(a.jplanes, j0 + i))
+                              ? gearSolvePosition(a.joints[j0 + a.jorder[j0 + i]], jp)
+                              : jointSolvePositionSlot(a.jplanes, a.jstride, j0 + i, jp);
+          if (!ok) {
             okay = 0;
             if (sleepMode) isl_store<S>(&SL[root].z, it + 1);
           }

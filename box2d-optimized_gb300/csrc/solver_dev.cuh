@@ -1281,6 +1281,7 @@ B2G_HD bool jointSolvePosition(JointDev& J, float4* pos) {
 #define B2G_JV_MOTOR 1
 #define B2G_JV_LIMIT 2
 #define B2G_JV_ASLEEP 4
+#define B2G_JV_GEAR 8   // the slot's joint is a gear, solved on its record (serial colour only)
 
 __device__ __forceinline__ void jointPackVel(const JointDev& J, float4* P, int stride, int slot) {
   float4 r[B2G_JV_ROWS];
@@ -1376,6 +1377,147 @@ __device__ __forceinline__ void jointPackPos(const JointDev& J, float4* P, int s
 
 // InitVelocityConstraints of the joint record G into the rows of `slot`: per type, a register
 // copy of the record's fields the init and the rows read, the init on it, the rows packed.
+// ---- gear joint (src/dynamics/b2_gear_joint.cpp:141-372). Four bodies: it runs in the serial
+// joint colour on its record, one thread. A, B are d.body_a / d.body_b; C, D are g.iC / g.iD.
+
+// The Jacobian rows and effective mass of the gear at rotations qA..qD (InitVelocityConstraints
+// :178-216 and SolvePositionConstraints :290-332 compute them alike); returns the summed mass.
+B2G_HD float gearJacobian(JointDev::Gear& g, float ratio, Rot qA, Rot qB, Rot qC, Rot qD, V2& JvAC, V2& JvBD,
+                          float& JwA, float& JwB, float& JwC, float& JwD) {
+  float mass = 0.0f;
+  if (g.typeA == B2G_JOINT_REVOLUTE) {
+    JvAC = mk(0.0f, 0.0f);
+    JwA = 1.0f;
+    JwC = 1.0f;
+    mass += g.iA + g.iC_;
+  } else {
+    V2 u = mul(qC, ld2(g.axC));
+    V2 rC = mul(qC, ld2(g.lC) - ld2(g.lcC));
+    V2 rA = mul(qA, ld2(g.lA) - ld2(g.lcA));
+    JvAC = u;
+    JwC = cross(rC, u);
+    JwA = cross(rA, u);
+    mass += g.mC + g.mA + g.iC_ * JwC * JwC + g.iA * JwA * JwA;
+  }
+  if (g.typeB == B2G_JOINT_REVOLUTE) {
+    JvBD = mk(0.0f, 0.0f);
+    JwB = ratio;
+    JwD = ratio;
+    mass += ratio * ratio * (g.iB + g.iD_);
+  } else {
+    V2 u = mul(qD, ld2(g.axD));
+    V2 rD = mul(qD, ld2(g.lD) - ld2(g.lcD));
+    V2 rB = mul(qB, ld2(g.lB) - ld2(g.lcB));
+    JvBD = ratio * u;
+    JwD = ratio * cross(rD, u);
+    JwB = ratio * cross(rB, u);
+    mass += ratio * ratio * (g.mD + g.mB) + g.iD_ * JwD * JwD + g.iB * JwB * JwB;
+  }
+  return mass;
+}
+
+// Applies `impulse` along the gear's rows to the four bodies (velocities, or positions with
+// the angular rows acting on angles).
+B2G_HD void gearApply(float4* state, int a, int b, int c, int d, const JointDev::Gear& g, float impulse, V2 JvAC,
+                      V2 JvBD, float JwA, float JwB, float JwC, float JwD) {
+  V2 xA, xB, xC, xD;
+  float tA, tB, tC, tD;
+  loadVel(state, a, xA, tA);
+  loadVel(state, b, xB, tB);
+  loadVel(state, c, xC, tC);
+  loadVel(state, d, xD, tD);
+  addTo(xA, (g.mA * impulse) * JvAC);
+  tA += g.iA * impulse * JwA;
+  addTo(xB, (g.mB * impulse) * JvBD);
+  tB += g.iB * impulse * JwB;
+  subFrom(xC, (g.mC * impulse) * JvAC);
+  tC -= g.iC_ * impulse * JwC;
+  subFrom(xD, (g.mD * impulse) * JvBD);
+  tD -= g.iD_ * impulse * JwD;
+  // the reference writes A, B, C, D in this order: a body that appears twice gets its last write
+  storeVel(state, a, xA, tA);
+  storeVel(state, b, xB, tB);
+  storeVel(state, c, xC, tC);
+  storeVel(state, d, xD, tD);
+}
+
+__device__ __forceinline__ void gearInit(JointDev& J, const float4* massd, const float2* lc, const float4* pos,
+                                         float4* vel, bool warm) {
+  JointDev::Gear& g = J.g;
+  const int a = J.d.body_a, b = J.d.body_b, c = g.iC, d = g.iD;
+  const float2 la = lc[a], lb = lc[b], lcc = lc[c], ld = lc[d];
+  g.lcA[0] = la.x; g.lcA[1] = la.y; g.lcB[0] = lb.x; g.lcB[1] = lb.y;
+  g.lcC[0] = lcc.x; g.lcC[1] = lcc.y; g.lcD[0] = ld.x; g.lcD[1] = ld.y;
+  g.mA = massd[a].y; g.mB = massd[b].y; g.mC = massd[c].y; g.mD = massd[d].y;
+  g.iA = massd[a].w; g.iB = massd[b].w; g.iC_ = massd[c].w; g.iD_ = massd[d].w;
+  const Rot qA = rotOf(pos[a].z), qB = rotOf(pos[b].z), qC = rotOf(pos[c].z), qD = rotOf(pos[d].z);
+  V2 JvAC, JvBD;
+  float JwA, JwB, JwC, JwD;
+  float mass = gearJacobian(g, J.d.ratio, qA, qB, qC, qD, JvAC, JvBD, JwA, JwB, JwC, JwD);
+  g.mass = mass > 0.0f ? 1.0f / mass : 0.0f;
+  g.JvAC[0] = JvAC.x; g.JvAC[1] = JvAC.y; g.JvBD[0] = JvBD.x; g.JvBD[1] = JvBD.y;
+  g.JwA = JwA; g.JwB = JwB; g.JwC = JwC; g.JwD = JwD;
+  if (warm) gearApply(vel, a, b, c, d, g, J.impulse[0], JvAC, JvBD, JwA, JwB, JwC, JwD);
+  else J.impulse[0] = 0.0f;
+}
+
+__device__ __forceinline__ void gearSolveVelocity(JointDev& J, float4* vel) {
+  JointDev::Gear& g = J.g;
+  const int a = J.d.body_a, b = J.d.body_b, c = g.iC, d = g.iD;
+  V2 vA, vB, vC, vD;
+  float wA, wB, wC, wD;
+  loadVel(vel, a, vA, wA);
+  loadVel(vel, b, vB, wB);
+  loadVel(vel, c, vC, wC);
+  loadVel(vel, d, vD, wD);
+  const V2 JvAC = ld2(g.JvAC), JvBD = ld2(g.JvBD);
+  float Cdot = dot(JvAC, vA - vC) + dot(JvBD, vB - vD);
+  Cdot += (g.JwA * wA - g.JwC * wC) + (g.JwB * wB - g.JwD * wD);
+  const float impulse = -g.mass * Cdot;
+  J.impulse[0] += impulse;
+  gearApply(vel, a, b, c, d, g, impulse, JvAC, JvBD, g.JwA, g.JwB, g.JwC, g.JwD);
+}
+
+// The position pass; its linear error is always zero (b2_gear_joint.cpp:370-371), so it is
+// always "okay".
+__device__ __forceinline__ bool gearSolvePosition(JointDev& J, float4* pos) {
+  JointDev::Gear& g = J.g;
+  const int a = J.d.body_a, b = J.d.body_b, c = g.iC, d = g.iD;
+  V2 cA, cB, cC, cD;
+  float aA, aB, aC, aD;
+  loadPos(pos, a, cA, aA);
+  loadPos(pos, b, cB, aB);
+  loadPos(pos, c, cC, aC);
+  loadPos(pos, d, cD, aD);
+  const Rot qA = rotOf(aA), qB = rotOf(aB), qC = rotOf(aC), qD = rotOf(aD);
+  V2 JvAC, JvBD;
+  float JwA, JwB, JwC, JwD;
+  const float ratio = J.d.ratio;
+  float mass = gearJacobian(g, ratio, qA, qB, qC, qD, JvAC, JvBD, JwA, JwB, JwC, JwD);
+  float coordinateA, coordinateB;
+  if (g.typeA == B2G_JOINT_REVOLUTE) {
+    coordinateA = aA - aC - g.refA;
+  } else {
+    V2 rA = mul(qA, ld2(g.lA) - ld2(g.lcA));
+    V2 pC = ld2(g.lC) - ld2(g.lcC);
+    V2 pA = mulT(qC, rA + (cA - cC));
+    coordinateA = dot(pA - pC, ld2(g.axC));
+  }
+  if (g.typeB == B2G_JOINT_REVOLUTE) {
+    coordinateB = aB - aD - g.refB;
+  } else {
+    V2 rB = mul(qB, ld2(g.lB) - ld2(g.lcB));
+    V2 pD = ld2(g.lD) - ld2(g.lcD);
+    V2 pB = mulT(qD, rB + (cB - cD));
+    coordinateB = dot(pB - pD, ld2(g.axD));
+  }
+  const float C = (coordinateA + ratio * coordinateB) - J.d.gear_constant;
+  float impulse = 0.0f;
+  if (mass > 0.0f) impulse = -C / mass;
+  gearApply(pos, a, b, c, d, g, impulse, JvAC, JvBD, JwA, JwB, JwC, JwD);
+  return true;
+}
+
 __device__ __forceinline__ void jointInitSlot(const JointDev& G, float4* P, int stride, int slot, const float4* massd,
                                               const float2* lc, const float4* pos, float4* vel, float dt, float dtRatio,
                                               bool warm) {
@@ -1518,6 +1660,12 @@ __device__ __forceinline__ bool jointSolvePositionSlot(const float4* P, int stri
 // A joint left out of this step (its island sleeps): its velocity iterations skip it.
 __device__ __forceinline__ void jointPackAsleep(float4* P, int slot) {
   P[slot] = make_float4(0.0f, 0.0f, 0.0f, __int_as_float(B2G_JV_ASLEEP));
+}
+__device__ __forceinline__ void jointPackGear(float4* P, int slot, int bodyA, int bodyB) {
+  P[slot] = make_float4(__int_as_float(bodyA), __int_as_float(bodyB), 0.0f, __int_as_float(B2G_JV_GEAR));
+}
+__device__ __forceinline__ bool jointSlotIsGear(const float4* P, int slot) {
+  return (__float_as_int(P[slot].w) & B2G_JV_GEAR) != 0;
 }
 
 // One velocity iteration of the joint in `slot`: the register copy of its rows through

@@ -607,6 +607,15 @@ struct b2PulleyJointDef : public b2JointDef {
   float lengthA, lengthB, ratio;
 };
 
+// b2GearJointDef (include/box2d/b2_gear_joint.h:28-45): couples two revolute or prismatic
+// joints: coordinate 1 + ratio * coordinate 2 stays constant.
+struct b2GearJointDef : public b2JointDef {
+  b2GearJointDef() { type = e_gearJoint; joint1 = nullptr; joint2 = nullptr; ratio = 1.0f; }
+  class b2Joint* joint1;
+  class b2Joint* joint2;
+  float ratio;
+};
+
 class b2Joint {
  public:
   virtual ~b2Joint() {}
@@ -642,6 +651,15 @@ class b2MotorJoint : public b2Joint {};
 class b2FrictionJoint : public b2Joint {};
 class b2MouseJoint : public b2Joint {};
 class b2PulleyJoint : public b2Joint {};
+class b2GearJoint : public b2Joint {
+ public:
+  b2Joint* GetJoint1() { return m_joint1; }
+  b2Joint* GetJoint2() { return m_joint2; }
+  float GetRatio() const { return m_ratio; }
+  b2Joint* m_joint1 = nullptr;
+  b2Joint* m_joint2 = nullptr;
+  float m_ratio = 1.0f;
+};
 
 // ---------------------------------------------------------------- contacts and listeners
 class b2Contact {
@@ -780,6 +798,7 @@ class b2World {
   // after a removal: the engine's End callbacks for the destroyed contacts, then renumbering
   void EndContacts(const std::vector<b2g_event>& ended, int32 n, const std::vector<b2Contact>& before);
   void Renumber();
+  void EraseOrphanGears();
   b2g_batch* m_batch = nullptr;
   bool m_ownsBatch = false;
   int32 m_index = 0;

@@ -6,6 +6,9 @@
 //   SliderRigs   - rigs of distance joints (rigid rods, springs from b2LinearStiffness, min/max
 //                  lengths) and prismatic joints (limits, motors, a piston between two dynamic
 //                  bodies), with loose boxes falling onto them.
+//   GearRigs     - gear joints (b2GearJointDef) coupling revolute and prismatic joints: a motor
+//                  driven wheel pair, a rack and pinion, and a double pendulum whose two hinges
+//                  are geared, with boxes falling onto them.
 // Written against the public Box2D C++ API like scenes.h, so the same source builds a world for
 // the reference engine and for this library's b2World facade.
 #pragma once
@@ -321,6 +324,125 @@ inline Counts SliderRigs(b2World* world, int rigs, uint32_t seed, float friction
       jd.motorSpeed = 1.0f;
       world->CreateJoint(&jd);
       c.joints++;
+    }
+  }
+  return c;
+}
+
+// `rigs` rigs side by side over one ground edge, each:
+//  * a wheel pair: a disc (r 1) on a motorised revolute joint to a static post and a disc (r 0.5)
+//    on a free one, geared 1 : 2 so that their rims turn together (ratio 2);
+//  * a rack and pinion: a disc (r 0.6) on a motorised revolute joint and a bar on a horizontal
+//    prismatic joint with limits, geared so that the bar moves with the disc's rim (ratio
+//    -1 / 0.6) until it reaches a limit;
+//  * a geared double pendulum: an arm hinged to a post and a second arm hinged to the first,
+//    the two hinges geared (ratio 1); the second joint's body A is the first arm, so the gear's
+//    bodies A and D are one body;
+//  * boxes dropped onto the wheels and the bar.
+inline Counts GearRigs(b2World* world, int rigs, uint32_t seed, float friction = 0.6f) {
+  Counts c;
+  Rng rng(seed);
+  if (rigs < 1) rigs = 1;
+  const float pitch = 18.0f;
+  const float half = 0.5f * pitch * (float)rigs + 20.0f;
+  b2BodyDef gd;
+  b2Body* ground = MakeBody(world, &gd);
+  AddEdge(ground, -half, 0.0f, half, 0.0f, &c);
+  auto disc = [&](float x, float y, float r) {
+    b2BodyDef bd;
+    bd.type = b2_dynamicBody;
+    bd.position.Set(x, y);
+    b2Body* b = MakeBody(world, &bd);
+    b2CircleShape cs;
+    cs.m_radius = r;
+    b2FixtureDef fd;
+    fd.shape = &cs;
+    fd.density = 1.0f;
+    fd.friction = friction;
+    MakeFixture(b, &fd);
+    c.bodies++;
+    c.fixtures++;
+    return b;
+  };
+  auto box = [&](float x, float y, float hx, float hy, float angle) {
+    b2BodyDef bd;
+    bd.type = b2_dynamicBody;
+    bd.position.Set(x, y);
+    bd.angle = angle;
+    b2Body* b = MakeBody(world, &bd);
+    b2PolygonShape ps;
+    ps.SetAsBox(hx, hy);
+    b2FixtureDef fd;
+    fd.shape = &ps;
+    fd.density = 1.0f;
+    fd.friction = friction;
+    MakeFixture(b, &fd);
+    c.bodies++;
+    c.fixtures++;
+    return b;
+  };
+  auto hinge = [&](b2Body* a, b2Body* b, b2Vec2 at) {
+    b2RevoluteJointDef jd;
+    jd.Initialize(a, b, at);
+    c.joints++;
+    return world->CreateJoint(&jd);
+  };
+  auto gear = [&](b2Joint* j1, b2Joint* j2, float ratio) {
+    b2GearJointDef jd;
+    jd.bodyA = j1->GetBodyB();
+    jd.bodyB = j2->GetBodyB();
+    jd.joint1 = j1;
+    jd.joint2 = j2;
+    jd.ratio = ratio;
+    c.joints++;
+    return world->CreateJoint(&jd);
+  };
+  for (int r = 0; r < rigs; ++r) {
+    const float x0 = -0.5f * pitch * (float)rigs + pitch * (float)r + 2.0f;
+    const float jit = rng.uni(-0.2f, 0.2f);
+    // wheel pair
+    {
+      b2Body* big = disc(x0, 5.0f, 1.0f);
+      b2Body* small = disc(x0 + 1.6f, 5.0f, 0.5f);
+      b2RevoluteJointDef jd;
+      jd.Initialize(ground, big, big->GetPosition());
+      jd.enableMotor = true;
+      jd.motorSpeed = 1.0f + jit;
+      jd.maxMotorTorque = 20.0f;
+      b2Joint* j1 = world->CreateJoint(&jd);
+      c.joints++;
+      b2Joint* j2 = hinge(ground, small, small->GetPosition());
+      gear(j1, j2, 2.0f);
+      box(x0 + 0.3f + jit, 8.0f, 0.3f, 0.3f, 0.2f);
+    }
+    // rack and pinion
+    {
+      b2Body* pinion = disc(x0 + 7.0f, 3.0f, 0.6f);
+      b2RevoluteJointDef pj;
+      pj.Initialize(ground, pinion, pinion->GetPosition());
+      pj.enableMotor = true;
+      pj.motorSpeed = -1.5f - jit;
+      pj.maxMotorTorque = 15.0f;
+      b2Joint* j3 = world->CreateJoint(&pj);
+      c.joints++;
+      b2Body* bar = box(x0 + 7.0f, 2.2f, 2.0f, 0.2f, 0.0f);
+      b2PrismaticJointDef pd;
+      pd.Initialize(ground, bar, bar->GetPosition(), b2Vec2(1.0f, 0.0f));
+      pd.enableLimit = true;
+      pd.lowerTranslation = -3.0f;
+      pd.upperTranslation = 3.0f;
+      b2Joint* j4 = world->CreateJoint(&pd);
+      c.joints++;
+      gear(j3, j4, -1.0f / 0.6f);
+      box(x0 + 8.5f, 4.0f + jit, 0.3f, 0.3f, 0.0f);
+    }
+    // geared double pendulum
+    {
+      b2Body* arm1 = box(x0 + 12.5f, 6.0f, 1.0f, 0.1f, 0.0f);
+      b2Body* arm2 = box(x0 + 14.5f, 6.0f, 1.0f, 0.1f, 0.0f);
+      b2Joint* j5 = hinge(ground, arm1, b2Vec2(x0 + 11.5f, 6.0f));
+      b2Joint* j6 = hinge(arm1, arm2, b2Vec2(x0 + 13.5f, 6.0f));
+      gear(j5, j6, 1.0f);
     }
   }
   return c;

@@ -59,6 +59,7 @@ extern "C" {
 #define B2G_JOINT_WELD 8
 #define B2G_JOINT_FRICTION 9
 #define B2G_JOINT_MOTOR 11
+#define B2G_JOINT_GEAR 6
 /* b2Manifold::Type, include/box2d/b2_collision.h:105-110 */
 #define B2G_MANIFOLD_CIRCLES 0
 #define B2G_MANIFOLD_FACE_A 1
@@ -153,9 +154,13 @@ typedef struct b2g_fixture_def {
  * b2PrismaticJointDef (b2_prismatic_joint.h:35-88), b2DistanceJointDef (b2_distance_joint.h:33-70),
  * b2WeldJointDef (b2_weld_joint.h:31-65), b2WheelJointDef (b2_wheel_joint.h:34-89),
  * b2MotorJointDef (b2_motor_joint.h:29-59), b2FrictionJointDef (b2_friction_joint.h:29-56),
- * b2MouseJointDef (b2_mouse_joint.h:30-56), b2PulleyJointDef (b2_pulley_joint.h:32-75). A mouse
- * joint's local_anchor_b is computed from its target when it is created, as the reference's
- * constructor does. */
+ * b2MouseJointDef (b2_mouse_joint.h:30-56), b2PulleyJointDef (b2_pulley_joint.h:32-75),
+ * b2GearJointDef (b2_gear_joint.h:28-45). A mouse joint's local_anchor_b is computed from its
+ * target when it is created, as the reference's constructor does. A gear joint names two earlier
+ * revolute or prismatic joints of its world (joint_1, joint_2) and a ratio; on creation the engine
+ * takes its bodies from them (body_a = joint 1's body B, body_b = joint 2's body B, as
+ * b2GearJoint::b2GearJoint does, src/dynamics/b2_gear_joint.cpp:48-139) and stores the gear's
+ * constant (coordinate 1 + ratio * coordinate 2 at creation) in gear_constant. */
 typedef struct b2g_joint_def {
   int32_t type;             /* B2G_JOINT_* */
   int32_t body_a;
@@ -184,8 +189,11 @@ typedef struct b2g_joint_def {
   float ground_anchor_a[2]; /* pulley */
   float ground_anchor_b[2];
   float length_a, length_b; /* pulley rope lengths */
-  float ratio;              /* pulley */
+  float ratio;              /* pulley, gear */
   uint64_t user_data;
+  int32_t joint_1, joint_2; /* gear: the joints it couples (indices in the world) */
+  float gear_constant;      /* gear: set on creation */
+  int32_t reserved;
 } b2g_joint_def;
 
 /* ---- state records (outputs / snapshot) ------------------------------------------------------ */
@@ -224,7 +232,7 @@ typedef struct b2g_fixture {
  * m_impulse (x, y), distance m_impulse in [0]. */
 /* impulse[]: revolute / prismatic m_impulse (x, y), distance and pulley m_impulse in [0], weld
  * m_impulse (x, y, z), wheel (m_impulse, m_springImpulse), motor and friction (linear x, y,
- * angular), mouse m_impulse (x, y). */
+ * angular), mouse m_impulse (x, y), gear m_impulse in [0]. */
 typedef struct b2g_joint {
   b2g_joint_def def;
   float impulse[3];
@@ -530,13 +538,14 @@ B2G_API int b2g_pairs_static(const float* d_aabbs, int32_t n, uint64_t* d_pairs,
 /* Builds one of the seeded benchmark scenes into `world` through the b2World facade calls
  * (box2d-optimized_gb300/scenes/scenes.h). kind: 0 pyramid(rows=n, density=p0, friction=p1),
  * 1 mixed drop(n bodies), 2 chains over pile(n chains, 20 links, p0 circles),
- * 3 batch world(n bodies), 4 joint zoo(n rigs), 5 slider rigs(n rigs), with `seed`. counts[3] = bodies, fixtures, joints. */
+ * 3 batch world(n bodies), 4 joint zoo(n rigs), 5 slider rigs(n rigs), 6 gear rigs(n rigs), with `seed`. counts[3] = bodies, fixtures, joints. */
 #define B2G_SCENE_PYRAMID 0
 #define B2G_SCENE_MIXED_DROP 1
 #define B2G_SCENE_CHAINS 2
 #define B2G_SCENE_BATCH_WORLD 3
 #define B2G_SCENE_JOINTS 4      /* rigs of weld, wheel, motor, friction, mouse and pulley joints */
 #define B2G_SCENE_SLIDERS 5     /* rigs of distance and prismatic joints (n rigs) */
+#define B2G_SCENE_GEARS 6       /* rigs of gear joints (n rigs) */
 B2G_API int b2g_scene_build(b2g_batch* b, int32_t world, int32_t kind, uint32_t seed, int32_t n,
                             float p0, float p1, int32_t* counts);
 B2G_API int b2g_batch_world_params(uint32_t seed, int32_t* n_bodies, float* gx, float* gy);

@@ -973,6 +973,15 @@ struct Joint {
   float springMass, motorMass;
   V2 err; float angularError;
   V2 uB; float constant;
+  // gear (b2_gear_joint.h:52-110): A, B = d.body_a / d.body_b (the coupled joints' bodies B),
+  // C, D = their bodies A; geometry from the two joints; m_impulse in imp[0]
+  int iC, iD, typeA, typeB;
+  V2 gLA, gLB, gLC, gLD, gAxC, gAxD;
+  float gRefA, gRefB;
+  V2 gLcA, gLcB, gLcC, gLcD;
+  float gmA, gmB, gmC, gmD, giA, giB, giC, giD;
+  V2 JvAC, JvBD;
+  float JwA, JwB, JwC, JwD, gMass;
 };
 
 struct Contact {
@@ -1412,6 +1421,10 @@ static void colorConstraints(int n, const int* bodyA, const int* bodyB, const ui
   color->assign(n, -1);
   for (int idx : order) {
     int a = bodyA[idx], b = bodyB[idx];
+    if (a < 0) {  // a constraint solved serially (gear joint): the overflow colour
+      (*color)[idx] = kOverflow;
+      continue;
+    }
     bool sa = bodies[a].type == 0, sb = bodies[b].type == 0;
     uint64_t used = (sa ? 0 : mask[a]) | (sb ? 0 : mask[b]);
     uint64_t freeBits = ~used & ((1ull << kOverflow) - 1);
@@ -1532,7 +1545,124 @@ static void solveLinearAngular(Joint& J, V2& vA, float& wA, V2& vB, float& wB, f
   }
 }
 
+// ---- gear joint (src/dynamics/b2_gear_joint.cpp:141-372), four bodies
+// Jacobian rows and summed effective mass at rotations qA..qD (:178-216, :290-332).
+static float gearRows(Joint& J, Rot qA, Rot qB, Rot qC, Rot qD, V2& JvAC, V2& JvBD, float& JwA, float& JwB,
+                      float& JwC, float& JwD) {
+  const float ratio = J.d.ratio;
+  float mass = 0.0f;
+  if (J.typeA == B2G_JOINT_REVOLUTE) {
+    JvAC = v2(0.0f, 0.0f);
+    JwA = 1.0f;
+    JwC = 1.0f;
+    mass += J.giA + J.giC;
+  } else {
+    V2 u = mul(qC, J.gAxC);
+    V2 rC = mul(qC, J.gLC - J.gLcC);
+    V2 rA = mul(qA, J.gLA - J.gLcA);
+    JvAC = u;
+    JwC = cross(rC, u);
+    JwA = cross(rA, u);
+    mass += J.gmC + J.gmA + J.giC * JwC * JwC + J.giA * JwA * JwA;
+  }
+  if (J.typeB == B2G_JOINT_REVOLUTE) {
+    JvBD = v2(0.0f, 0.0f);
+    JwB = ratio;
+    JwD = ratio;
+    mass += ratio * ratio * (J.giB + J.giD);
+  } else {
+    V2 u = mul(qD, J.gAxD);
+    V2 rD = mul(qD, J.gLD - J.gLcD);
+    V2 rB = mul(qB, J.gLB - J.gLcB);
+    JvBD = ratio * u;
+    JwD = ratio * cross(rD, u);
+    JwB = ratio * cross(rB, u);
+    mass += ratio * ratio * (J.gmD + J.gmB) + J.giD * JwD * JwD + J.giB * JwB * JwB;
+  }
+  return mass;
+}
+
+// impulse along the rows, velocities (pos = false) or positions; bodies written A, B, C, D
+static void gearApply(Joint& J, std::vector<SolverBody>& sb, bool pos, float impulse, V2 JvAC, V2 JvBD, float JwA,
+                      float JwB, float JwC, float JwD) {
+  const int a = J.d.body_a, b = J.d.body_b, c = J.iC, d = J.iD;
+  V2 xA = pos ? sb[a].c : sb[a].v, xB = pos ? sb[b].c : sb[b].v, xC = pos ? sb[c].c : sb[c].v, xD = pos ? sb[d].c : sb[d].v;
+  float tA = pos ? sb[a].a : sb[a].w, tB = pos ? sb[b].a : sb[b].w, tC = pos ? sb[c].a : sb[c].w, tD = pos ? sb[d].a : sb[d].w;
+  addTo(xA, (J.gmA * impulse) * JvAC);
+  tA += J.giA * impulse * JwA;
+  addTo(xB, (J.gmB * impulse) * JvBD);
+  tB += J.giB * impulse * JwB;
+  xC = xC - (J.gmC * impulse) * JvAC;
+  tC -= J.giC * impulse * JwC;
+  xD = xD - (J.gmD * impulse) * JvBD;
+  tD -= J.giD * impulse * JwD;
+  if (pos) {
+    sb[a].c = xA; sb[a].a = tA; sb[b].c = xB; sb[b].a = tB; sb[c].c = xC; sb[c].a = tC; sb[d].c = xD; sb[d].a = tD;
+  } else {
+    sb[a].v = xA; sb[a].w = tA; sb[b].v = xB; sb[b].w = tB; sb[c].v = xC; sb[c].w = tC; sb[d].v = xD; sb[d].w = tD;
+  }
+}
+
+static void gearInit(Joint& J, const std::vector<Body>& bodies, std::vector<SolverBody>& sb, const Step& st) {
+  const Body& bA = bodies[J.d.body_a];
+  const Body& bB = bodies[J.d.body_b];
+  const Body& bC = bodies[J.iC];
+  const Body& bD = bodies[J.iD];
+  J.gLcA = bA.localCenter; J.gLcB = bB.localCenter; J.gLcC = bC.localCenter; J.gLcD = bD.localCenter;
+  J.gmA = bA.invMass; J.gmB = bB.invMass; J.gmC = bC.invMass; J.gmD = bD.invMass;
+  J.giA = bA.invI; J.giB = bB.invI; J.giC = bC.invI; J.giD = bD.invI;
+  Rot qA = rotOf(sb[J.d.body_a].a), qB = rotOf(sb[J.d.body_b].a), qC = rotOf(sb[J.iC].a), qD = rotOf(sb[J.iD].a);
+  float mass = gearRows(J, qA, qB, qC, qD, J.JvAC, J.JvBD, J.JwA, J.JwB, J.JwC, J.JwD);
+  J.gMass = mass > 0.0f ? 1.0f / mass : 0.0f;
+  if (st.warm) gearApply(J, sb, false, J.imp[0], J.JvAC, J.JvBD, J.JwA, J.JwB, J.JwC, J.JwD);
+  else J.imp[0] = 0.0f;
+}
+
+static void gearSolveVelocity(Joint& J, std::vector<SolverBody>& sb) {
+  const SolverBody &A = sb[J.d.body_a], &B = sb[J.d.body_b], &Cb = sb[J.iC], &D = sb[J.iD];
+  float Cdot = dot(J.JvAC, A.v - Cb.v) + dot(J.JvBD, B.v - D.v);
+  Cdot += (J.JwA * A.w - J.JwC * Cb.w) + (J.JwB * B.w - J.JwD * D.w);
+  float impulse = -J.gMass * Cdot;
+  J.imp[0] += impulse;
+  gearApply(J, sb, false, impulse, J.JvAC, J.JvBD, J.JwA, J.JwB, J.JwC, J.JwD);
+}
+
+static bool gearSolvePosition(Joint& J, std::vector<SolverBody>& sb) {
+  const V2 cA = sb[J.d.body_a].c, cB = sb[J.d.body_b].c, cC = sb[J.iC].c, cD = sb[J.iD].c;
+  const float aA = sb[J.d.body_a].a, aB = sb[J.d.body_b].a, aC = sb[J.iC].a, aD = sb[J.iD].a;
+  Rot qA = rotOf(aA), qB = rotOf(aB), qC = rotOf(aC), qD = rotOf(aD);
+  V2 JvAC, JvBD;
+  float JwA, JwB, JwC, JwD;
+  float mass = gearRows(J, qA, qB, qC, qD, JvAC, JvBD, JwA, JwB, JwC, JwD);
+  float coordinateA, coordinateB;
+  if (J.typeA == B2G_JOINT_REVOLUTE) {
+    coordinateA = aA - aC - J.gRefA;
+  } else {
+    V2 rA = mul(qA, J.gLA - J.gLcA);
+    V2 pC = J.gLC - J.gLcC;
+    V2 pA = mulT(qC, rA + (cA - cC));
+    coordinateA = dot(pA - pC, J.gAxC);
+  }
+  if (J.typeB == B2G_JOINT_REVOLUTE) {
+    coordinateB = aB - aD - J.gRefB;
+  } else {
+    V2 rB = mul(qB, J.gLB - J.gLcB);
+    V2 pD = J.gLD - J.gLcD;
+    V2 pB = mulT(qD, rB + (cB - cD));
+    coordinateB = dot(pB - pD, J.gAxD);
+  }
+  float C = (coordinateA + J.d.ratio * coordinateB) - J.d.gear_constant;
+  float impulse = 0.0f;
+  if (mass > 0.0f) impulse = -C / mass;
+  gearApply(J, sb, true, impulse, JvAC, JvBD, JwA, JwB, JwC, JwD);
+  return true;  // the reference's linear error is always 0 (b2_gear_joint.cpp:370-371)
+}
+
 static void jointInit(Joint& J, const std::vector<Body>& bodies, std::vector<SolverBody>& sb, const Step& st) {
+  if (J.d.type == B2G_JOINT_GEAR) {
+    gearInit(J, bodies, sb, st);
+    return;
+  }
   const Body& bA = bodies[J.d.body_a];
   const Body& bB = bodies[J.d.body_b];
   J.iA = J.d.body_a; J.iB = J.d.body_b;
@@ -1807,6 +1937,10 @@ static void jointInit(Joint& J, const std::vector<Body>& bodies, std::vector<Sol
 }
 
 static void jointSolveVelocity(Joint& J, std::vector<SolverBody>& sb, const Step& st) {
+  if (J.d.type == B2G_JOINT_GEAR) {
+    gearSolveVelocity(J, sb);
+    return;
+  }
   V2 vA = sb[J.iA].v; float wA = sb[J.iA].w;
   V2 vB = sb[J.iB].v; float wB = sb[J.iB].w;
   float mA = J.mA, mB = J.mB, iA = J.invIA, iB = J.invIB;
@@ -2084,6 +2218,7 @@ static void jointSolveVelocity(Joint& J, std::vector<SolverBody>& sb, const Step
 }
 
 static bool jointSolvePosition(Joint& J, std::vector<SolverBody>& sb) {
+  if (J.d.type == B2G_JOINT_GEAR) return gearSolvePosition(J, sb);
   V2 cA = sb[J.iA].c; float aA = sb[J.iA].a;
   V2 cB = sb[J.iB].c; float aB = sb[J.iB].a;
   Rot qA = rotOf(aA), qB = rotOf(aB);
@@ -2323,7 +2458,11 @@ static bool jointSolvePosition(Joint& J, std::vector<SolverBody>& sb) {
 
 // Reaction force/torque after the step (GetReactionForce/Torque of each joint type).
 static void jointReaction(const Joint& J, float inv_dt, float* F, float* T) {
-  if (J.d.type == B2G_JOINT_REVOLUTE) {
+  if (J.d.type == B2G_JOINT_GEAR) {  // b2_gear_joint.cpp:387-397
+    V2 P = J.imp[0] * J.JvAC;
+    F[0] = inv_dt * P.x; F[1] = inv_dt * P.y;
+    *T = inv_dt * (J.imp[0] * J.JwA);
+  } else if (J.d.type == B2G_JOINT_REVOLUTE) {
     F[0] = inv_dt * J.impulse2.x; F[1] = inv_dt * J.impulse2.y;
     *T = inv_dt * ((J.motorImpulse + J.lowerImpulse) - J.upperImpulse);
   } else if (J.d.type == B2G_JOINT_PRISMATIC) {
@@ -2746,7 +2885,8 @@ static void stepWorld(World* w, float dt, int vi, int pi) {
       cp[i] = contactPriority(w->contacts[solverContacts[i]].key);
     }
     for (int j = 0; j < nj; ++j) {
-      jA[j] = w->joints[j].d.body_a; jB[j] = w->joints[j].d.body_b;
+      const bool gear = w->joints[j].d.type == B2G_JOINT_GEAR;
+      jA[j] = gear ? -1 : w->joints[j].d.body_a; jB[j] = gear ? -1 : w->joints[j].d.body_b;
       jp[j] = jointPriority((uint32_t)j);
     }
     std::vector<int> ccol, jcol;
@@ -3122,6 +3262,18 @@ int orc_world_load(void* h, const b2g_body* bodies, int32_t nb, const b2g_fixtur
     }
     if (J.d.type == B2G_JOINT_PULLEY) J.constant = J.d.length_a + J.d.ratio * J.d.length_b;
     if (J.d.body_a < 0 || J.d.body_a >= nb || J.d.body_b < 0 || J.d.body_b >= nb) return 1;
+    if (J.d.type == B2G_JOINT_GEAR) {  // the two earlier joints it couples
+      if (J.d.joint_1 < 0 || J.d.joint_1 >= i || J.d.joint_2 < 0 || J.d.joint_2 >= i) return 1;
+      const b2g_joint_def& j1 = joints[J.d.joint_1].def;
+      const b2g_joint_def& j2 = joints[J.d.joint_2].def;
+      J.iC = j1.body_a; J.iD = j2.body_a;
+      J.typeA = j1.type; J.typeB = j2.type;
+      J.gLC = v2(j1.local_anchor_a[0], j1.local_anchor_a[1]); J.gLA = v2(j1.local_anchor_b[0], j1.local_anchor_b[1]);
+      J.gLD = v2(j2.local_anchor_a[0], j2.local_anchor_a[1]); J.gLB = v2(j2.local_anchor_b[0], j2.local_anchor_b[1]);
+      J.gRefA = j1.reference_angle; J.gRefB = j2.reference_angle;
+      J.gAxC = j1.type == B2G_JOINT_PRISMATIC ? v2(j1.local_axis_a[0], j1.local_axis_a[1]) : v2(0.0f, 0.0f);
+      J.gAxD = j2.type == B2G_JOINT_PRISMATIC ? v2(j2.local_axis_a[0], j2.local_axis_a[1]) : v2(0.0f, 0.0f);
+    }
   }
   rebuildNoCollide(w);
   w->contacts.clear();

@@ -299,6 +299,7 @@ void* ref_scene_world(int32_t kind, uint32_t seed, int32_t n, float p0, float p1
   else if (kind == B2G_SCENE_BATCH_WORLD) c = b2scenes::BatchWorld(rw->world, seed, n);
   else if (kind == B2G_SCENE_JOINTS) c = b2scenes::JointZoo(rw->world, n, seed);
   else if (kind == B2G_SCENE_SLIDERS) c = b2scenes::SliderRigs(rw->world, n, seed);
+  else if (kind == B2G_SCENE_GEARS) c = b2scenes::GearRigs(rw->world, n, seed);
   if (counts) { counts[0] = c.bodies; counts[1] = c.fixtures; counts[2] = c.joints; }
   index_world(rw);
   return rw;
@@ -496,6 +497,16 @@ void ref_world_joints(void* h, b2g_joint* out) {
       o->def.local_anchor_a[0] = q->m_localAnchorA.x; o->def.local_anchor_a[1] = q->m_localAnchorA.y;
       o->def.local_anchor_b[0] = q->m_localAnchorB.x; o->def.local_anchor_b[1] = q->m_localAnchorB.y;
       o->def.length_a = q->m_lengthA; o->def.length_b = q->m_lengthB; o->def.ratio = q->m_ratio;
+      o->impulse[0] = q->m_impulse;
+    } else if (j->m_type == e_gearJoint) {
+      b2GearJoint* q = (b2GearJoint*)j;
+      o->def.type = B2G_JOINT_GEAR;
+      o->def.local_anchor_a[0] = q->m_localAnchorA.x; o->def.local_anchor_a[1] = q->m_localAnchorA.y;
+      o->def.local_anchor_b[0] = q->m_localAnchorB.x; o->def.local_anchor_b[1] = q->m_localAnchorB.y;
+      o->def.joint_1 = rw->joint_index[q->m_joint1];
+      o->def.joint_2 = rw->joint_index[q->m_joint2];
+      o->def.ratio = q->m_ratio;
+      o->def.gear_constant = q->m_constant;
       o->impulse[0] = q->m_impulse;
     }
     b2Vec2 F = j->GetReactionForce(1.0f);

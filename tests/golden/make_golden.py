@@ -179,6 +179,7 @@ def main():
     replay(ref, orc, "mixed", G.SCENE_MIXED_DROP, 300, 3, 0.0, 150, 8, 3)
     replay(ref, orc, "chains", G.SCENE_CHAINS, 10, 2, 150.0, 100, 10, 4)
     replay(ref, orc, "sliders", G.SCENE_SLIDERS, 3, 9, 0.0, 60, 8, 3)
+    replay(ref, orc, "gears", G.SCENE_GEARS, 3, 9, 0.0, 90, 8, 3)
     rollout(ref, "pyramid", G.SCENE_PYRAMID, 20, 1, 1.0, 256, 8, 3)
     events(ref, orc, "mixed", G.SCENE_MIXED_DROP, 400, 5, 0.0, 200, 8, 3)
     events(ref, orc, "chains", G.SCENE_CHAINS, 15, 4, 200.0, 80, 10, 4)

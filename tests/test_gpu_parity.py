@@ -88,6 +88,14 @@ def test_slider_rigs_rollout_bit_exact(lib, orc, n, seed, vi, pi):
     _rollout(lib, orc, G.SCENE_SLIDERS, n, seed=seed, steps=240, vi=vi, pi=pi)
 
 
+@pytest.mark.parametrize("n,seed,vi,pi", [(3, 9, 8, 3), (2, 17, 10, 4)])
+def test_gear_rigs_rollout_bit_exact(lib, orc, n, seed, vi, pi):
+    # gear joints (revolute-revolute with a motor, rack and pinion with prismatic limits, a double
+    # pendulum whose gear moves one body through two of its rows) in the serial joint colour:
+    # bodies every step, joint impulses (the gear's included) and contacts at the end
+    _rollout(lib, orc, G.SCENE_GEARS, n, seed=seed, steps=240, vi=vi, pi=pi)
+
+
 def _state_np(records_bytes, n):
     return np.frombuffer(records_bytes, dtype=np.uint8).reshape(n, -1)[:, :40]
 
