@@ -243,7 +243,7 @@ class Lib:
         "b2g_bodies_sleep_time_read", "b2g_world_get_flags", "b2g_server_batch", "b2g_step_begin",
         "b2g_step_poll", "b2g_step_end", "b2g_batch_stage", "b2g_server_set_builders", "b2g_batch_set_solver_waves", "b2g_batch_set_tree_rebuild_period",
         "b2g_batch_set_cluster_solve", "b2g_batch_get_cluster_solve", "b2g_events_drain_world",
-        "b2g_bodies_remove", "b2g_fixtures_remove", "b2g_joints_remove",
+        "b2g_bodies_remove", "b2g_fixtures_remove", "b2g_joints_remove", "b2g_world_dump",
     ]
 
     def __init__(self, path: os.PathLike | str | None = None):
@@ -289,6 +289,7 @@ class Lib:
             "b2g_bodies_remove": ([vp, i32, P(i32), i32, P(Event), i32, P(i32)], C.c_int),
             "b2g_fixtures_remove": ([vp, i32, P(i32), i32, P(Event), i32, P(i32)], C.c_int),
             "b2g_joints_remove": ([vp, i32, P(i32), i32], C.c_int),
+            "b2g_world_dump": ([vp, i32, C.c_char_p, C.c_uint64, P(C.c_uint64)], C.c_int),
             "b2g_profile_get": ([vp, P(Profile)], C.c_int),
             "b2g_batch_set_solver_threads": ([vp, P(i32)], C.c_int),
             "b2g_batch_get_solver_threads": ([vp, P(i32)], C.c_int),
@@ -587,6 +588,14 @@ class Batch:
             arr = (C.c_int32 * len(joints))(*joints)
             self.lib.check(self.lib.b2g_joints_remove(self.h, world, arr, len(joints)), "b2g_joints_remove")
         return ended
+
+    def dump(self, world) -> str:
+        """b2World::Dump of `world` as text (b2g_world_dump)."""
+        n = C.c_uint64()
+        self.lib.b2g_world_dump(self.h, world, None, 0, C.byref(n))
+        buf = C.create_string_buffer(n.value + 1)
+        self.lib.check(self.lib.b2g_world_dump(self.h, world, buf, n.value + 1, C.byref(n)), "b2g_world_dump")
+        return buf.value.decode()
 
     def world_events(self, world, cap=1 << 20):
         """World `world`'s listener events of the last step (b2g_events_drain_world)."""

@@ -10,6 +10,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <cstdarg>
 #include <chrono>
 #include <mutex>
 #include <numeric>
@@ -2094,6 +2095,216 @@ B2G_API int b2g_joints_remove(b2g_batch* b, int32_t world, const int32_t* joints
   std::vector<char> db(w.bodies.size(), 0), df(w.fixtures.size(), 0), dj(w.joints.size(), 0);
   for (int32_t i = 0; i < n; ++i) dj[joints[i]] = 1;
   return remove_structure(b, world, std::move(db), std::move(df), std::move(dj), nullptr, 0, nullptr);
+}
+
+// ---- b2World::Dump (src/dynamics/b2_world.cpp:1469-1531): the world as C++ source that rebuilds it
+// through the b2World API, in the reference's text format (an interchange format: the same lines,
+// numbers printed with %.9g, bodies in the reference's list order - non-static bodies newest first,
+// then static bodies oldest first - fixtures newest first, joints newest first with gears last).
+namespace {
+struct DumpText {
+  std::string s;
+  void operator()(const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    const int n = vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    if (n > 0) s.append(buf, (size_t)std::min(n, (int)sizeof(buf) - 1));
+  }
+};
+}  // namespace
+
+static void dump_world(const HostWorld& w, DumpText& D) {
+  const int nb = (int)w.bodies.size(), nj = (int)w.joints.size();
+  D("b2Vec2 g(%.9g, %.9g);\n", w.gx, w.gy);
+  D("m_world->SetGravity(g);\n");
+  D("b2Body** bodies = (b2Body**)b2Alloc(%d * sizeof(b2Body*));\n", nb);
+  D("b2Joint** joints = (b2Joint**)b2Alloc(%d * sizeof(b2Joint*));\n", nj);
+  std::vector<int> order, index(nb);
+  for (int i = nb - 1; i >= 0; --i)
+    if (w.bodies[i].type != B2G_STATIC) order.push_back(i);
+  for (int i = 0; i < nb; ++i)
+    if (w.bodies[i].type == B2G_STATIC) order.push_back(i);
+  for (int k = 0; k < nb; ++k) index[order[k]] = k;
+  // reference b2Body flags (include/box2d/b2_body.h:478-484)
+  auto flag = [](uint32_t f, uint32_t ours, int theirs) { return (f & ours) ? theirs : 0; };
+  for (int k = 0; k < nb; ++k) {
+    const b2g_body& b = w.bodies[order[k]];
+    D("{\n");
+    D("  b2BodyDef bd;\n");
+    D("  bd.type = b2BodyType(%d);\n", b.type);
+    D("  bd.position.Set(%.9g, %.9g);\n", b.xf[0], b.xf[1]);
+    D("  bd.angle = %.9g;\n", b.a);
+    D("  bd.linearVelocity.Set(%.9g, %.9g);\n", b.v[0], b.v[1]);
+    D("  bd.angularVelocity = %.9g;\n", b.w);
+    D("  bd.linearDamping = %.9g;\n", b.linear_damping);
+    D("  bd.angularDamping = %.9g;\n", b.angular_damping);
+    D("  bd.allowSleep = bool(%d);\n", flag(b.flags, B2G_BODY_AUTO_SLEEP, 0x0004));
+    D("  bd.awake = bool(%d);\n", flag(b.flags, B2G_BODY_AWAKE, 0x0002));
+    D("  bd.fixedRotation = bool(%d);\n", flag(b.flags, B2G_BODY_FIXED_ROTATION, 0x0010));
+    D("  bd.bullet = bool(%d);\n", flag(b.flags, B2G_BODY_BULLET, 0x0008));
+    D("  bd.enabled = bool(%d);\n", flag(b.flags, B2G_BODY_ENABLED, 0x0020));
+    D("  bd.gravityScale = %.9g;\n", b.gravity_scale);
+    D("  bodies[%d] = m_world->CreateBody(&bd);\n", k);
+    D("\n");
+    const std::vector<int>& fl = w.body_fixtures[order[k]];
+    for (int q = (int)fl.size() - 1; q >= 0; --q) {
+      const b2g_fixture& f = w.fixtures[fl[q]];
+      const b2g_shape& sh = f.shape;
+      D("  {\n");
+      D("    b2FixtureDef fd;\n");
+      D("    fd.friction = %.9g;\n", f.friction);
+      D("    fd.restitution = %.9g;\n", f.restitution);
+      D("    fd.restitutionThreshold = %.9g;\n", f.restitution_threshold);
+      D("    fd.density = %.9g;\n", f.density);
+      D("    fd.isSensor = bool(%d);\n", f.is_sensor ? 1 : 0);
+      D("    fd.filter.categoryBits = uint16(%d);\n", (int)f.category_bits);
+      D("    fd.filter.maskBits = uint16(%d);\n", (int)f.mask_bits);
+      D("    fd.filter.groupIndex = int16(%d);\n", (int)f.group_index);
+      if (sh.type == B2G_SHAPE_CIRCLE) {
+        D("    b2CircleShape shape;\n");
+        D("    shape.m_radius = %.9g;\n", sh.radius);
+        D("    shape.m_p.Set(%.9g, %.9g);\n", sh.vertices[0][0], sh.vertices[0][1]);
+      } else if (sh.type == B2G_SHAPE_EDGE) {  // record vertices: v1, v2, v0, v3
+        D("    b2EdgeShape shape;\n");
+        D("    shape.m_radius = %.9g;\n", sh.radius);
+        D("    shape.m_vertex0.Set(%.9g, %.9g);\n", sh.vertices[2][0], sh.vertices[2][1]);
+        D("    shape.m_vertex1.Set(%.9g, %.9g);\n", sh.vertices[0][0], sh.vertices[0][1]);
+        D("    shape.m_vertex2.Set(%.9g, %.9g);\n", sh.vertices[1][0], sh.vertices[1][1]);
+        D("    shape.m_vertex3.Set(%.9g, %.9g);\n", sh.vertices[3][0], sh.vertices[3][1]);
+        D("    shape.m_oneSided = bool(%d);\n", sh.one_sided ? 1 : 0);
+      } else {
+        D("    b2PolygonShape shape;\n");
+        D("    b2Vec2 vs[%d];\n", B2G_MAX_POLYGON_VERTICES);
+        for (int i = 0; i < sh.count; ++i) D("    vs[%d].Set(%.9g, %.9g);\n", i, sh.vertices[i][0], sh.vertices[i][1]);
+        D("    shape.Set(vs, %d);\n", sh.count);
+      }
+      D("\n");
+      D("    fd.shape = &shape;\n");
+      D("\n");
+      D("    bodies[%d]->CreateFixture(&fd);\n", k);
+      D("  }\n");
+    }
+    D("}\n");
+  }
+  auto joint = [&](int ji) {  // b2*Joint::Dump, the joint's index in the reference's list order
+    const b2g_joint_def& d = w.joints[ji].def;
+    const int jindex = nj - 1 - ji;
+    D("{\n");
+    const char* names[] = {"", "b2RevoluteJointDef", "b2PrismaticJointDef", "b2DistanceJointDef", "b2PulleyJointDef",
+                           "", "b2GearJointDef", "b2WheelJointDef", "b2WeldJointDef", "b2FrictionJointDef", "", "b2MotorJointDef"};
+    if (d.type != B2G_JOINT_MOUSE) {  // b2MouseJoint::Dump writes to the log only
+      D("  %s jd;\n", names[d.type]);
+      D("  jd.bodyA = bodies[%d];\n", index[d.body_a]);
+      D("  jd.bodyB = bodies[%d];\n", index[d.body_b]);
+      D("  jd.collideConnected = bool(%d);\n", d.collide_connected ? 1 : 0);
+    }
+    switch (d.type) {
+      case B2G_JOINT_REVOLUTE:
+        D("  jd.localAnchorA.Set(%.9g, %.9g);\n", d.local_anchor_a[0], d.local_anchor_a[1]);
+        D("  jd.localAnchorB.Set(%.9g, %.9g);\n", d.local_anchor_b[0], d.local_anchor_b[1]);
+        D("  jd.referenceAngle = %.9g;\n", d.reference_angle);
+        D("  jd.enableLimit = bool(%d);\n", d.enable_limit ? 1 : 0);
+        D("  jd.lowerAngle = %.9g;\n", d.lower);
+        D("  jd.upperAngle = %.9g;\n", d.upper);
+        D("  jd.enableMotor = bool(%d);\n", d.enable_motor ? 1 : 0);
+        D("  jd.motorSpeed = %.9g;\n", d.motor_speed);
+        D("  jd.maxMotorTorque = %.9g;\n", d.max_motor);
+        break;
+      case B2G_JOINT_PRISMATIC:
+        D("  jd.localAnchorA.Set(%.9g, %.9g);\n", d.local_anchor_a[0], d.local_anchor_a[1]);
+        D("  jd.localAnchorB.Set(%.9g, %.9g);\n", d.local_anchor_b[0], d.local_anchor_b[1]);
+        D("  jd.localAxisA.Set(%.9g, %.9g);\n", d.local_axis_a[0], d.local_axis_a[1]);
+        D("  jd.referenceAngle = %.9g;\n", d.reference_angle);
+        D("  jd.enableLimit = bool(%d);\n", d.enable_limit ? 1 : 0);
+        D("  jd.lowerTranslation = %.9g;\n", d.lower);
+        D("  jd.upperTranslation = %.9g;\n", d.upper);
+        D("  jd.enableMotor = bool(%d);\n", d.enable_motor ? 1 : 0);
+        D("  jd.motorSpeed = %.9g;\n", d.motor_speed);
+        D("  jd.maxMotorForce = %.9g;\n", d.max_motor);
+        break;
+      case B2G_JOINT_DISTANCE:
+        D("  jd.localAnchorA.Set(%.9g, %.9g);\n", d.local_anchor_a[0], d.local_anchor_a[1]);
+        D("  jd.localAnchorB.Set(%.9g, %.9g);\n", d.local_anchor_b[0], d.local_anchor_b[1]);
+        D("  jd.length = %.9g;\n", d.length);
+        D("  jd.minLength = %.9g;\n", d.min_length);
+        D("  jd.maxLength = %.9g;\n", d.max_length);
+        D("  jd.stiffness = %.9g;\n", d.stiffness);
+        D("  jd.damping = %.9g;\n", d.damping);
+        break;
+      case B2G_JOINT_WELD:
+        D("  jd.localAnchorA.Set(%.9g, %.9g);\n", d.local_anchor_a[0], d.local_anchor_a[1]);
+        D("  jd.localAnchorB.Set(%.9g, %.9g);\n", d.local_anchor_b[0], d.local_anchor_b[1]);
+        D("  jd.referenceAngle = %.9g;\n", d.reference_angle);
+        D("  jd.stiffness = %.9g;\n", d.stiffness);
+        D("  jd.damping = %.9g;\n", d.damping);
+        break;
+      case B2G_JOINT_WHEEL:
+        D("  jd.localAnchorA.Set(%.9g, %.9g);\n", d.local_anchor_a[0], d.local_anchor_a[1]);
+        D("  jd.localAnchorB.Set(%.9g, %.9g);\n", d.local_anchor_b[0], d.local_anchor_b[1]);
+        D("  jd.localAxisA.Set(%.9g, %.9g);\n", d.local_axis_a[0], d.local_axis_a[1]);
+        D("  jd.enableMotor = bool(%d);\n", d.enable_motor ? 1 : 0);
+        D("  jd.motorSpeed = %.9g;\n", d.motor_speed);
+        D("  jd.maxMotorTorque = %.9g;\n", d.max_motor);
+        D("  jd.stiffness = %.9g;\n", d.stiffness);
+        D("  jd.damping = %.9g;\n", d.damping);
+        break;
+      case B2G_JOINT_MOTOR:
+        D("  jd.linearOffset.Set(%.9g, %.9g);\n", d.linear_offset[0], d.linear_offset[1]);
+        D("  jd.angularOffset = %.9g;\n", d.reference_angle);
+        D("  jd.maxForce = %.9g;\n", d.max_force);
+        D("  jd.maxTorque = %.9g;\n", d.max_torque);
+        D("  jd.correctionFactor = %.9g;\n", d.correction_factor);
+        break;
+      case B2G_JOINT_FRICTION:
+        D("  jd.localAnchorA.Set(%.9g, %.9g);\n", d.local_anchor_a[0], d.local_anchor_a[1]);
+        D("  jd.localAnchorB.Set(%.9g, %.9g);\n", d.local_anchor_b[0], d.local_anchor_b[1]);
+        D("  jd.maxForce = %.9g;\n", d.max_force);
+        D("  jd.maxTorque = %.9g;\n", d.max_torque);
+        break;
+      case B2G_JOINT_PULLEY:
+        D("  jd.groundAnchorA.Set(%.9g, %.9g);\n", d.ground_anchor_a[0], d.ground_anchor_a[1]);
+        D("  jd.groundAnchorB.Set(%.9g, %.9g);\n", d.ground_anchor_b[0], d.ground_anchor_b[1]);
+        D("  jd.localAnchorA.Set(%.9g, %.9g);\n", d.local_anchor_a[0], d.local_anchor_a[1]);
+        D("  jd.localAnchorB.Set(%.9g, %.9g);\n", d.local_anchor_b[0], d.local_anchor_b[1]);
+        D("  jd.lengthA = %.9g;\n", d.length_a);
+        D("  jd.lengthB = %.9g;\n", d.length_b);
+        D("  jd.ratio = %.9g;\n", d.ratio);
+        break;
+      case B2G_JOINT_GEAR:
+        D("  jd.joint1 = joints[%d];\n", nj - 1 - d.joint_1);
+        D("  jd.joint2 = joints[%d];\n", nj - 1 - d.joint_2);
+        D("  jd.ratio = %.9g;\n", d.ratio);
+        break;
+      default:
+        break;
+    }
+    if (d.type != B2G_JOINT_MOUSE) D("  joints[%d] = m_world->CreateJoint(&jd);\n", jindex);
+    D("}\n");
+  };
+  for (int ji = nj - 1; ji >= 0; --ji)
+    if (w.joints[ji].def.type != B2G_JOINT_GEAR) joint(ji);
+  for (int ji = nj - 1; ji >= 0; --ji)
+    if (w.joints[ji].def.type == B2G_JOINT_GEAR) joint(ji);
+  D("b2Free(joints);\n");
+  D("b2Free(bodies);\n");
+  D("joints = nullptr;\n");
+  D("bodies = nullptr;\n");
+}
+
+B2G_API int b2g_world_dump(b2g_batch* b, int32_t world, char* out, uint64_t cap, uint64_t* n) {
+  if (!world_index_ok(b, world) || !n || (cap > 0 && !out)) return B2G_E_INVALID_ARG;
+  if (world < b->NW) TRY(download_state(b));
+  DumpText D;
+  dump_world(b->worlds[world], D);
+  *n = D.s.size();
+  if (cap > 0) {
+    const size_t k = std::min<size_t>(D.s.size(), (size_t)cap - 1);
+    memcpy(out, D.s.data(), k);
+    out[k] = 0;
+  }
+  return D.s.size() < cap ? B2G_OK : B2G_E_CAPACITY;
 }
 
 B2G_API int b2g_world_sizes(b2g_batch* b, int32_t world, int32_t* bodies, int32_t* fixtures, int32_t* joints,

@@ -1,6 +1,7 @@
 // facade.cpp - the b2World / b2Body / b2Fixture / b2Joint / b2Contact facade over the C ABI,
 // and the scene builder entry point (b2g_scene_build) that runs the shared scene recipes
 // through it.
+#include <stdio.h>
 #include <string.h>
 
 #include <algorithm>
@@ -555,6 +556,17 @@ b2Body* b2World::CreateBody(const b2BodyDef* def) {
   ++m_bodyCount;
   InvalidateCaches();
   return b;
+}
+
+void b2World::Dump() {
+  uint64_t n = 0;
+  b2g_world_dump(m_batch, m_index, nullptr, 0, &n);
+  std::vector<char> text(n + 1);
+  if (b2g_world_dump(m_batch, m_index, text.data(), n + 1, &n) != B2G_OK) return;
+  FILE* f = fopen("box2d_dump.inl", "w");
+  if (!f) return;
+  fwrite(text.data(), 1, n, f);
+  fclose(f);
 }
 
 void b2World::SetContactFilter(b2ContactFilter* filter) {

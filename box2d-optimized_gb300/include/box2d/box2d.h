@@ -775,6 +775,9 @@ class b2World {
   void SetAutoClearForces(bool flag);
   bool GetAutoClearForces() const { return m_autoClear; }
   const b2Profile& GetProfile() const { return m_profile; }
+  // b2World::Dump (src/dynamics/b2_world.cpp:1469-1531): writes the world as C++ source to
+  // box2d_dump.inl in the working directory, in the reference's format.
+  void Dump();
 
   // Extensions of this engine
   // After stepping a shared batch with b2g_step (all its worlds at once), hands this world's

@@ -335,6 +335,11 @@ B2G_API int b2g_world_retire(b2g_batch* b, int32_t world);
 B2G_API int b2g_compact(b2g_batch* b, int32_t* old_to_new, int32_t n);
 
 /* Counts of one world. */
+/* b2World::Dump (src/dynamics/b2_world.cpp:1469-1531): the world as C++ source that rebuilds it
+ * through the b2World API, in the reference's text format (same lines and order, %.9g numbers).
+ * Writes up to cap - 1 characters and a terminating zero to `out`; *n receives the text's length,
+ * and B2G_E_CAPACITY is returned when it does not fit (call with cap = 0 to size the buffer). */
+B2G_API int b2g_world_dump(b2g_batch* b, int32_t world, char* out, uint64_t cap, uint64_t* n);
 /* Structural removal: b2World::DestroyBody (src/dynamics/b2_world.cpp:178-266), b2Body::DestroyFixture
  * (src/dynamics/b2_body.cpp:280-350), b2World::DestroyJoint (b2_world.cpp:326-410). A removed body
  * takes its fixtures, joints and contacts along; a destroyed contact that was touching ends, and the

@@ -331,6 +331,12 @@ int32_t ref_world_events(void* h, b2g_event* out, int32_t cap) {
   return n;
 }
 
+// b2World::Dump of the reference world (writes box2d_dump.inl in the working directory).
+void ref_world_dump(void* h) {
+  RefWorld* rw = (RefWorld*)h;
+  rw->world->Dump();
+}
+
 void ref_world_free(void* h) {
   RefWorld* rw = (RefWorld*)h;
   delete rw->world;

@@ -52,6 +52,7 @@ class Ref:
             "ref_worlds_step_parallel": ([P(vp), i32, f32, i32, i32, i32, i32], C.c_double),
             "ref_world_events_enable": ([vp, i32], None),
             "ref_world_events": ([vp, P(G.Event), i32], i32),
+            "ref_world_dump": ([vp], None),
         }
         for name, (a, r) in sig.items():
             fn = getattr(L, name)

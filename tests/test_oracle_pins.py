@@ -448,3 +448,22 @@ def test_oracle_rollout_measures_vs_reference_golden(orc, name):
         rows.append(ob.measure_row(ob.rollout_measures(orc, list(ow.bodies()), fixtures, list(ow.contacts()))))
     ob.check_rollout_measures(name, rows, g["rows"])
     hb.close()
+
+
+@pytest.mark.parametrize("kind,n,seed,p0", [
+    (G.SCENE_PYRAMID, 6, 1, 1.0), (G.SCENE_MIXED_DROP, 60, 3, 0.0), (G.SCENE_CHAINS, 4, 2, 30.0),
+    (G.SCENE_JOINTS, 2, 9, 0.0), (G.SCENE_SLIDERS, 2, 9, 0.0), (G.SCENE_GEARS, 2, 9, 0.0)])
+def test_world_dump_text_vs_reference_live(ref, kind, n, seed, p0, tmp_path, monkeypatch):
+    """b2World::Dump: the engine's text (b2g_world_dump) equals the reference's own Dump of the
+    same scene line for line (bodies, fixtures with every shape type, every joint type, gears
+    after the other joints)."""
+    monkeypatch.chdir(tmp_path)
+    rw = ob.RefWorld(ref, kind, seed=seed, n=n, p0=p0, p1=0.6)
+    ref.ref_world_dump(rw.h)
+    expected = (tmp_path / "box2d_dump.inl").read_text()
+    hb = _host_batch()
+    w = hb.add_world(0.0, -10.0)
+    hb.scene(w, kind, seed=seed, n=n, p0=p0, p1=0.6)
+    got = hb.dump(w)
+    assert got.splitlines() == expected.splitlines()
+    hb.close()
