@@ -311,12 +311,17 @@ def large_worlds(lib, dev, cpu, cpu_steps=16):
     out = {}
     for name, kind, seed, n, p0, vi, pi, steps, desc in LARGE_CONFIGS:
         res = {"workload": desc}
-        for ctas in ((-1, 1) if n > 8192 else (-1,)):
+        big = None
+        for ctas in (-1, 1):
             b = G.Batch(lib, device=dev)
             b.cluster_solve(ctas)
             w = b.add_world(0.0, -10.0)
             b.set_flags(w, allow_sleep=False, warm_starting=True, continuous=False)
             counts = b.scene(w, kind, seed=seed, n=n, p0=p0, p1=0.6)
+            big = counts[0] > 8192  # solved by a thread-block cluster by default
+            if ctas == 1 and not big:
+                b.close()
+                break
             head = b.step_timed(steps - cpu_steps, DT, vi, pi)
             if ctas == -1 and cpu:
                 import oracle_bind as ob  # noqa: PLC0415 - CPU baseline leg only
@@ -340,7 +345,7 @@ def large_worlds(lib, dev, cpu, cpu_steps=16):
                         "touching_at_end": p.touching, "joints": p.joints, "colors_max": p.colors_max}
             if ctas == -1:
                 res["bodies"] = counts[0]
-                res["cluster"]["ctas_per_world"] = b.cluster_ctas() if n > 8192 else 1
+                res["cluster"]["ctas_per_world"] = b.cluster_ctas() if big else 1
             b.close()
         out[name] = res
     return out
@@ -485,12 +490,20 @@ def run_ours(args, rank, world_size):
         eb.solver_threads(threads)
     eb.step_timed(args.warmup, DT, VI, PI)
     torch.cuda.synchronize()
+    phase = [0.0, 0.0, 0.0]  # host time in set_forces, step, read_states
     t1 = time.perf_counter()
     for _ in range(e2e_steps):
+        ta = time.perf_counter()
         lib.check(lib.b2g_batch_set_forces(eb.h, forces.data_ptr(), nbody), "set_forces")
+        tb = time.perf_counter()
         lib.check(lib.b2g_step(eb.h, DT, VI, PI, None), "step")
+        tc = time.perf_counter()
         lib.check(lib.b2g_batch_read_states(eb.h, C.cast(xf_out.data_ptr(), C.POINTER(C.c_float)), None,
                                             nbody, C.byref(n_out)), "read_states")
+        td = time.perf_counter()
+        phase[0] += tb - ta
+        phase[1] += tc - tb
+        phase[2] += td - tc
     e2e_s = time.perf_counter() - t1
     eb.close()
     e2e_value = nb * e2e_steps / e2e_s * world_size
@@ -611,7 +624,9 @@ def run_ours(args, rank, world_size):
             "plain_gpu": plain,
             "batched_over_plain": (value / world_size / plain["value"]) if plain else None,
             "e2e": {"value": e2e_value, "unit": "body-steps/s", "h2d_bytes_per_step": 16 * nbody,
-                    "d2h_bytes_per_step": 16 * nbody, "steps": e2e_steps},
+                    "d2h_bytes_per_step": 16 * nbody, "steps": e2e_steps,
+                    "host_ms_per_step": {k: round(v * 1e3 / e2e_steps, 3)
+                                         for k, v in zip(("set_forces", "step", "read_states"), phase)}},
             "gpu_launches": kernels_per_step * args.steps + 3 * full_builds,
             "contact_constraint_iterations_per_s": contact_iters,
             "settled": settled,
@@ -645,6 +660,32 @@ def profile_window(args):
                                          "fixtures": p.fixtures, "contacts": p.contacts, "touching": p.touching,
                                          "joints": p.joints, "colors_max": p.colors_max}}))
     batch.close()
+
+
+def profile_large(args):
+    """Profiling case for ncu on one single-world configuration (--profile-large NAME): steps it
+    --settle steps (CUDA graphs), then two eager steps inside the NVTX range "profile"."""
+    import torch  # noqa: PLC0415 - NVTX ranges
+
+    cfg = {c[0]: c for c in LARGE_CONFIGS}[args.profile_large]
+    _, kind, seed, n, p0, vi, pi, _, _ = cfg
+    lib = G.Lib()
+    b = G.Batch(lib, device=0)
+    w = b.add_world(0.0, -10.0)
+    b.set_flags(w, allow_sleep=False, warm_starting=True, continuous=False)
+    counts = b.scene(w, kind, seed=seed, n=n, p0=p0, p1=0.6)
+    b.step_timed(args.settle, DT, vi, pi)
+    b.set_graphs(False)
+    torch.cuda.nvtx.range_push("profile")
+    for _ in range(2):
+        b.step(DT, vi, pi)
+    torch.cuda.synchronize()
+    torch.cuda.nvtx.range_pop()
+    p = b.profile()
+    print(json.dumps({"profile_large": {"config": args.profile_large, "settle_steps": args.settle, "bodies": counts[0],
+                                        "touching": p.touching, "joints": p.joints, "colors_max": p.colors_max,
+                                        "ctas_per_world": b.cluster_ctas()}}))
+    b.close()
 
 
 def serve_ticks(args):
@@ -704,12 +745,17 @@ def main():
     ap.add_argument("--profile-window", action="store_true",
                     help="ncu case: settle --settle steps, then 2 steps inside the NVTX range 'profile'")
     ap.add_argument("--settle", type=int, default=250)
+    ap.add_argument("--profile-large", default="", help="ncu case: one single-world configuration by name "
+                    "(pyramid_210, mixed_20000, chains_2000x20_pile_10000), settled, 2 steps in NVTX 'profile'")
     ap.add_argument("--serve-ticks", type=int, default=0,
                     help="tick-driven served measurement over this many ticks (see serve_ticks)")
     ap.add_argument("--serve-per-tick", type=float, default=1.77)
     args = ap.parse_args()
     if args.profile_window:
         profile_window(args)
+        return
+    if args.profile_large:
+        profile_large(args)
         return
     if args.serve_ticks > 0:
         serve_ticks(args)

@@ -542,8 +542,7 @@ b2Body* b2World::CreateBody(const b2BodyDef* def) {
   d.user_data = def->userData.pointer;
   int32_t id = -1;
   if (b2g_bodies_add(m_batch, m_index, &d, 1, &id) != B2G_OK) return nullptr;
-  b2Body* last = nullptr;  // the last live body, which links to the new one
-  for (b2Body* x = m_bodyHead; x; x = x->m_next) last = x;
+  b2Body* last = m_bodyTail;  // the last live body, which links to the new one
   m_bodies.emplace_back();
   b2Body* b = &m_bodies.back();
   b->m_world = this;
@@ -553,6 +552,7 @@ b2Body* b2World::CreateBody(const b2BodyDef* def) {
   b->m_userData = def->userData;
   if (last) last->m_next = b;
   else m_bodyHead = b;
+  m_bodyTail = b;
   ++m_bodyCount;
   InvalidateCaches();
   return b;
@@ -636,6 +636,7 @@ void b2World::DestroyBody(b2Body* body) {
   for (b2Body* x = m_bodyHead; x && x != body; x = x->m_next) prev = x;
   if (prev) prev->m_next = body->m_next;
   else m_bodyHead = body->m_next;
+  if (m_bodyTail == body) m_bodyTail = prev;
   body->m_next = nullptr;
   body->m_fixtureList = nullptr;
   body->m_index = -1;
@@ -832,7 +833,9 @@ b2Joint* b2World::CreateJoint(const b2JointDef* def) {
 
 const b2g_body& b2World::BodyRecord(int32 index) const {
   if (!m_stateValid) {
-    m_state.resize((size_t)m_bodyCount);
+    int32_t nb = 0;  // the engine world's bodies (an attached world may hold some made elsewhere)
+    b2g_world_sizes(m_batch, m_index, &nb, nullptr, nullptr, nullptr);
+    m_state.resize((size_t)nb);
     if (!m_state.empty()) b2g_bodies_read(m_batch, m_index, 0, (int32_t)m_state.size(), m_state.data());
     m_stateValid = true;
   }
@@ -846,7 +849,9 @@ void b2World::WriteBody(int32 index, const b2g_body& rec) {
 
 const b2g_joint& b2World::JointRecord(int32 index) const {
   if (!m_jointsValid) {
-    m_jointState.resize(m_joints.size());
+    int32_t nj = 0;
+    b2g_world_sizes(m_batch, m_index, nullptr, nullptr, &nj, nullptr);
+    m_jointState.resize((size_t)nj);
     if (!m_jointState.empty()) b2g_joints_read(m_batch, m_index, 0, (int32_t)m_jointState.size(), m_jointState.data());
     m_jointsValid = true;
   }

@@ -814,6 +814,7 @@ class b2World {
   b2DestructionListener* m_destruction = nullptr;
   std::deque<b2Body> m_bodies;  // every body created; destroyed ones keep m_index = -1
   b2Body* m_bodyHead = nullptr;  // first live body (creation order)
+  b2Body* m_bodyTail = nullptr;  // last live body
   int32 m_bodyCount = 0;
   std::deque<b2Fixture> m_fixtures;
   std::vector<b2Fixture*> m_fixtureIndex;
