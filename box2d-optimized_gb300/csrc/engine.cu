@@ -137,7 +137,7 @@ static int upload(Batch* b, DBuf<T>& buf, const std::vector<T>& v) {
 static KernelArgs make_args(Batch* b) {
   KernelArgs a;
   memset(&a, 0, sizeof(a));
-  a.wb = b->wb.p; a.wj = b->wj.p; a.wg = b->wg.p; a.wflags = b->wflags.p; a.wc = b->wc.p; a.wfault = b->wfault.p;
+  a.wb = b->wb.p; a.wj = b->wj.p; a.wg = b->wg.p; a.wflags = b->wflags.p; a.wc = b->wc.p; a.wfault = b->wfault.p; a.isl_dirty = b->isl_dirty.p;
   a.world_order = b->world_order.p;
   a.xf = b->xf.p; a.pos = b->pos.p; a.vel = b->vel.p; a.massd = b->massd.p; a.damp = b->damp.p;
   a.force = b->force.p; a.lc = b->lc.p; a.btype = b->btype.p; a.bworld = b->bworld.p;
@@ -414,6 +414,8 @@ int upload_all(Batch* b) {
   TRY(ensure(b, b->ncolors, 4 * (size_t)NW)); TRY(ensure(b, b->jranges, 65 * (size_t)NW));
   TRY(ensure(b, b->wfault, NW));
   CUDA_TRY(b, cudaMemsetAsync(b->wfault.p, 0, b->wfault.cap, b->stream));
+  TRY(ensure(b, b->isl_dirty, NW));  // a new layout labels every world's islands afresh
+  CUDA_TRY(b, cudaMemsetAsync(b->isl_dirty.p, 1, b->isl_dirty.cap, b->stream));
   TRY(upload(b, b->xf, xf)); TRY(upload(b, b->pos, pos)); TRY(upload(b, b->vel, vel)); TRY(upload(b, b->massd, massd));
   TRY(upload(b, b->damp, damp)); TRY(upload(b, b->force, force)); TRY(upload(b, b->lc, lc));
   TRY(upload(b, b->btype, btype)); TRY(upload(b, b->bworld, bworld)); TRY(upload(b, b->bstate, bstate));
@@ -634,6 +636,8 @@ static int flush_tail(Batch* b, TailPack& P) {
   // the broadphase forest's structure (world roots, leaf order, links) survives growth: the next
   // broadphase refits it and builds trees for the appended worlds only
   TRY(ensure(b, b->wbounds, NW)); TRY(ensure(b, b->wroot, NW, true)); TRY(ensure(b, b->ncolors, 4 * (size_t)NW, true));
+  TRY(ensure(b, b->isl_dirty, NW, true));  // the appended worlds label their islands afresh
+  CUDA_TRY(b, cudaMemsetAsync(b->isl_dirty.p + w0, 1, (size_t)(NW - w0), b->stream));
   if (b->wfault.cap < (size_t)NW) {  // flags are zero between steps: a grown array starts zeroed
     TRY(ensure(b, b->wfault, NW));
     CUDA_TRY(b, cudaMemsetAsync(b->wfault.p, 0, b->wfault.cap, b->stream));
@@ -1356,7 +1360,7 @@ B2G_API int b2g_batch_destroy(b2g_batch* b) {
   if (b->h_readback) cudaFreeHost(b->h_readback);
   if (b->h_stage) cudaFreeHost(b->h_stage);
   if (b->stage_ev) cudaEventDestroy(b->stage_ev);
-  release(b, b->wb); release(b, b->wj); release(b, b->wg); release(b, b->wflags); release(b, b->wc); release(b, b->wfault);
+  release(b, b->wb); release(b, b->wj); release(b, b->wg); release(b, b->wflags); release(b, b->wc); release(b, b->wfault); release(b, b->isl_dirty);
   release(b, b->world_order); release(b, b->xf); release(b, b->pos); release(b, b->vel); release(b, b->massd);
   release(b, b->damp); release(b, b->force); release(b, b->lc); release(b, b->btype); release(b, b->bworld);
   release(b, b->bstate); release(b, b->bwake); release(b, b->sl);
@@ -1680,6 +1684,7 @@ static int compact_device(Batch* b, int32_t* old_to_new, int32_t n) {
   CUDA_TRY(b, cudaMemsetAsync(b->status.p, 0, sizeof(unsigned int), s));
   launch_joint_colour(make_args(b), 0, kept, s);
   TRY(check_upload_status(b));
+  if (b->isl_dirty.p) CUDA_TRY(b, cudaMemsetAsync(b->isl_dirty.p, 1, b->isl_dirty.cap, s));  // bodies moved
   b->layout_version++;
   return B2G_OK;
 }

@@ -199,6 +199,7 @@ struct Batch {
   DBuf<int> wflags;
   DBuf<int2> wc;                  // contact_off, contact_cnt
   DBuf<uint8_t> wfault;           // set by the solver when the world's state became non-finite
+  DBuf<uint8_t> isl_dirty;        // per world: its island labels must be recomputed (sleep mode)
   DBuf<int> world_order;          // worlds sorted by work, largest first
 
   DBuf<float4> xf, pos, vel, massd, damp, force;

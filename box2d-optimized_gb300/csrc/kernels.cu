@@ -121,9 +121,12 @@ __global__ void k_collide(KernelArgs a) {
   const int ba = a.fbody[f.x], bb = a.fbody[f.y];
   const bool sleepMode = (wf & B2G_WF_SLEEPMODE) != 0;
   if (sleepMode && !((a.bstate[ba].x | a.bstate[bb].x) & B2G_BS_AWAKE)) return;
-  if (update_contact(a, i, w, f, ba, bb, 0u, SENSORS) && sleepMode) {
-    mark_wake(a, ba);
-    mark_wake(a, bb);
+  if (update_contact(a, i, w, f, ba, bb, 0u, SENSORS)) {
+    a.isl_dirty[w] = 1;  // a solid contact began or stopped touching (kept for any later sleep mode)
+    if (sleepMode) {
+      mark_wake(a, ba);
+      mark_wake(a, bb);
+    }
   }
 }
 
@@ -159,6 +162,7 @@ __global__ void k_collide_closure(KernelArgs a) {
       if (update_contact(a, i, w, f, ba, bb, B2G_CONTACT_CLOSURE, a.fsensor[f.x] || a.fsensor[f.y])) {
         if (mark_wake(a, ba)) changed = 1;
         if (mark_wake(a, bb)) changed = 1;
+        a.isl_dirty[w] = 1;
       }
     }
     if (!__syncthreads_or(changed)) break;
@@ -565,6 +569,7 @@ __global__ void k_contact_diff(KernelArgs a, int src, int dst) {
     copy_manifold(&a.cmanB[dst][k], &a.cmanB[src][o]);
   } else {
     init_new_contact(a, dst, k, key);
+    a.isl_dirty[a.fworld[(int)(key >> 32)]] = 1;  // a body may have gained its first contact
   }
 }
 
@@ -613,6 +618,7 @@ __global__ void k_contact_dead(KernelArgs a, int src) {
   int e = (int)(key >> 32);
   int64_t lo = a.poff[e];
   if (find_key(a.pairs + lo, (int64_t)a.poff[e + 1] - lo, key) >= 0) return;
+  a.isl_dirty[a.fworld[e]] = 1;  // a body may have lost its last contact, or a solid edge
   if ((a.cflagsB[src][k] & B2G_CONTACT_TOUCHING) == 0) return;
   int2 f = a.cfixB[src][k];
   int w = a.fworld[f.x];

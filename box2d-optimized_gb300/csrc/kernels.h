@@ -39,6 +39,9 @@ struct KernelArgs {
   const int* wflags;
   int2* wc;
   uint8_t* wfault;
+  // per world, sleep mode: its island graph changed since the last labelling (a solid contact
+  // began or stopped touching, a contact was created or destroyed, or the layout changed)
+  uint8_t* isl_dirty;
   const int* world_order;
 
   float4 *xf, *pos, *vel;

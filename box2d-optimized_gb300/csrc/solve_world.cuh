@@ -642,13 +642,18 @@ __device__ inline void isl_unite(int4* SL, int x, int y, unsigned int* status) {
 // src/dynamics/b2_contact.cpp:183-188), labels the islands, and wakes every member of an island
 // that holds an awake body (the search marks the bodies it reaches awake without resetting their
 // sleep timers, b2_world.cpp:565-566). Sleeping islands are neither integrated nor solved.
+// The labels are kept between steps: a world whose island graph did not change since its last
+// labelling (no solid contact began or stopped touching, no contact was created or destroyed,
+// same layout: the world's isl_dirty flag is clear) reuses them and only redoes the awake marks.
 template <class Team>
-__device__ void build_islands(Team& tm, const KernelArgs& a, int b0, int nb, int c0, int ncAll, int j0, int nj) {
+__device__ void build_islands(Team& tm, const KernelArgs& a, int w, int b0, int nb, int c0, int ncAll, int j0,
+                              int nj) {
   constexpr cuda::thread_scope S = Team::kScope;
   constexpr int T = Team::kThreads;
   const int tid = tm.tid();
   int4* SL = a.sl + b0;
   int2* BS = a.bstate + b0;
+  const bool relabel = a.isl_dirty[w] != 0;
   for (int i = tid; i < nb; i += T) {
     const int bi = b0 + i;
     const bool stat = a.btype[bi] == B2G_STATIC;
@@ -661,35 +666,46 @@ __device__ void build_islands(Team& tm, const KernelArgs& a, int b0, int nb, int
         BS[i] = st;
       }
     }
-    isl_store<S>(&SL[i].x, stat ? -1 : i);
-    isl_store<S>(&SL[i].y, 0);
+    if (relabel) {
+      isl_store<S>(&SL[i].x, stat ? -1 : i);
+      isl_store<S>(&SL[i].y, 0);
+    } else {  // the label and the body's LINKED bit stand; the island bits start over
+      isl_store<S>(&SL[i].y, isl_load<S>(&SL[i].y) & B2G_ISL_LINKED);
+    }
     isl_store<S>(&SL[i].z, 0);
     isl_store<S>(&SL[i].w, 0x7f7fffff);  // FLT_MAX: no member timed yet
   }
   tm.sync();
-  for (int k = tid; k < ncAll; k += T) {
-    const int2 f = a.cfix[c0 + k];
-    const int ia = a.fbody[f.x] - b0, ib = a.fbody[f.y] - b0;
-    if (!(isl_bits<S>(SL, ia) & B2G_ISL_LINKED)) isl_or<S>(&SL[ia].y, B2G_ISL_LINKED);
-    if (!(isl_bits<S>(SL, ib) & B2G_ISL_LINKED)) isl_or<S>(&SL[ib].y, B2G_ISL_LINKED);
-    const uint32_t fl = a.cflags[c0 + k];
-    if ((fl & B2G_CONTACT_TOUCHING) && (fl & B2G_CONTACT_ENABLED) && !a.fsensor[f.x] && !a.fsensor[f.y] &&
-        isl_load<S>(&SL[ia].x) >= 0 && isl_load<S>(&SL[ib].x) >= 0)
-      isl_unite<S>(SL, ia, ib, a.status);
+  if (relabel) {
+    for (int k = tid; k < ncAll; k += T) {
+      const int2 f = a.cfix[c0 + k];
+      const int ia = a.fbody[f.x] - b0, ib = a.fbody[f.y] - b0;
+      if (!(isl_bits<S>(SL, ia) & B2G_ISL_LINKED)) isl_or<S>(&SL[ia].y, B2G_ISL_LINKED);
+      if (!(isl_bits<S>(SL, ib) & B2G_ISL_LINKED)) isl_or<S>(&SL[ib].y, B2G_ISL_LINKED);
+      const uint32_t fl = a.cflags[c0 + k];
+      if ((fl & B2G_CONTACT_TOUCHING) && (fl & B2G_CONTACT_ENABLED) && !a.fsensor[f.x] && !a.fsensor[f.y] &&
+          isl_load<S>(&SL[ia].x) >= 0 && isl_load<S>(&SL[ib].x) >= 0)
+        isl_unite<S>(SL, ia, ib, a.status);
+    }
+    for (int k = tid; k < nj; k += T) {
+      const JointDev& J = a.joints[j0 + k];
+      const int ia = J.d.body_a - b0, ib = J.d.body_b - b0;
+      isl_or<S>(&SL[ia].y, B2G_ISL_LINKED);
+      isl_or<S>(&SL[ib].y, B2G_ISL_LINKED);
+      if (isl_load<S>(&SL[ia].x) >= 0 && isl_load<S>(&SL[ib].x) >= 0) isl_unite<S>(SL, ia, ib, a.status);
+    }
+    tm.sync();
   }
-  for (int k = tid; k < nj; k += T) {
-    const JointDev& J = a.joints[j0 + k];
-    const int ia = J.d.body_a - b0, ib = J.d.body_b - b0;
-    isl_or<S>(&SL[ia].y, B2G_ISL_LINKED);
-    isl_or<S>(&SL[ib].y, B2G_ISL_LINKED);
-    if (isl_load<S>(&SL[ia].x) >= 0 && isl_load<S>(&SL[ib].x) >= 0) isl_unite<S>(SL, ia, ib, a.status);
-  }
-  tm.sync();
   // labels, and the awake mark of every island with an awake member (roots no longer change)
   for (int i = tid; i < nb; i += T) {
     if (isl_load<S>(&SL[i].x) < 0) continue;
-    const int r = isl_find<S>(SL, i, false, a.status);
-    isl_store<S>(&SL[i].x, r);
+    int r;
+    if (relabel) {
+      r = isl_find<S>(SL, i, false, a.status);
+      isl_store<S>(&SL[i].x, r);
+    } else {
+      r = isl_load<S>(&SL[i].x);
+    }
     if (BS[i].x & B2G_BS_AWAKE) isl_or<S>(&SL[r].y, B2G_ISL_AWAKE);
   }
   tm.sync();
@@ -697,6 +713,7 @@ __device__ void build_islands(Team& tm, const KernelArgs& a, int b0, int nb, int
     const int r = isl_label<S>(SL, i);
     if (r >= 0 && (isl_bits<S>(SL, r) & B2G_ISL_AWAKE)) BS[i].x |= B2G_BS_AWAKE;
   }
+  if (tid == 0 && relabel) a.isl_dirty[w] = 0;  // every thread read the flag before the first barrier
   tm.sync();
 }
 
@@ -804,7 +821,7 @@ __device__ __forceinline__ void solve_world(Team& tm, const KernelArgs& a, int w
   int2* const BS = a.bstate + b0;
 
   // 0. sleep-mode worlds: wakes, islands, awake islands
-  if (sleepMode) build_islands(tm, a, b0, nb, c0, ncAll, j0, nj);
+  if (sleepMode) build_islands(tm, a, w, b0, nb, c0, ncAll, j0, nj);
 
   // 1. solver contacts in list order, with local bodies (static = -1) and colouring priorities
   const int nsc = block_compact(tm, 
