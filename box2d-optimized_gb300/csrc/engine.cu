@@ -143,6 +143,7 @@ static KernelArgs make_args(Batch* b) {
   a.force = b->force.p; a.lc = b->lc.p; a.btype = b->btype.p; a.bworld = b->bworld.p;
   a.bstate = b->bstate.p; a.bwake = b->bwake.p; a.sl = b->sl.p; a.any_sleep = b->any_sleep ? 1 : 0;
   a.any_sensor = b->any_sensor ? 1 : 0;
+  a.max_wfix = b->max_wfix;
   a.shape = b->shape.p; a.fbody = b->fbody.p; a.fgroup = b->fgroup.p; a.fsensor = b->fsensor.p;
   a.fworld = b->fworld.p; a.frad = b->frad.p; a.ffilter = b->ffilter.p; a.fmat = b->fmat.p; a.aabb = b->aabb.p;
   a.joints = b->joints.p; a.nocollide = b->nocollide.p; a.n_nocollide = b->n_nocollide;
@@ -155,7 +156,7 @@ static KernelArgs make_args(Batch* b) {
   }
   a.wbounds = b->wbounds.p; a.mkey = b->mkey.p; a.mkey_sorted = b->mkey_sorted.p; a.mval = b->mval.p;
   a.mval_sorted = b->mval_sorted.p; a.nchild = b->nchild.p; a.nparent = b->nparent.p; a.lparent = b->lparent.p;
-  a.naabb = b->naabb.p; a.ncbox = b->ncbox.p; a.laabb = b->laabb.p; a.fattr = b->fattr.p; a.nflag = b->nflag.p; a.wroot = b->wroot.p; a.pcount = b->pcount.p; a.pslots = b->pslots.p; a.poff = b->poffB[b->cur ^ 1].p; a.poff_old = nullptr;
+  a.naabb = b->naabb.p; a.nrec = b->nrec.p; a.nhi = b->nhi.p; a.laabb = b->laabb.p; a.lattr = b->lattr.p; a.fattr = b->fattr.p; a.nflag = b->nflag.p; a.wroot = b->wroot.p; a.pcount = b->pcount.p; a.pslots = b->pslots.p; a.poff = b->poffB[b->cur ^ 1].p; a.poff_old = nullptr;
   a.pairs = b->pairs.p; a.cub_tmp = b->cub_tmp.p;
   a.sc_list = b->sc_list.p; a.scb = b->scb.p; a.cslot = b->cslot.p; a.ccol = b->ccol.p; a.corder = b->corder.p; a.cprio = b->cprio.p;
   a.sp.nf = b->sp_nf.p; a.sp.cid = b->sp_cid.p; a.sp.r0 = b->sp_r0.p; a.sp.r1 = b->sp_r1.p;
@@ -303,6 +304,8 @@ int upload_all(Batch* b) {
     NC += (int64_t)hw.contacts.size();
   }
   b->h_body_off[NW] = NB; b->h_fix_off[NW] = NF; b->h_joint_off[NW] = NJ;
+  b->max_wfix = 0;
+  for (int w = 0; w < NW; ++w) b->max_wfix = std::max(b->max_wfix, b->h_fix_off[w + 1] - b->h_fix_off[w]);
   std::vector<float4> xf(NB), pos(NB), vel(NB), massd(NB), damp(NB), force(NB);
   std::vector<float2> lc(NB);
   std::vector<int> btype(NB), bworld(NB);
@@ -436,7 +439,7 @@ int upload_all(Batch* b) {
   TRY(ensure(b, b->mkey, NF)); TRY(ensure(b, b->mkey_sorted, NF)); TRY(ensure(b, b->mval, NF));
   TRY(ensure(b, b->mval_sorted, NF)); TRY(ensure(b, b->nchild, NF)); TRY(ensure(b, b->nparent, NF));
   TRY(ensure(b, b->lparent, NF)); TRY(ensure(b, b->naabb, NF)); TRY(ensure(b, b->nflag, NF));
-  TRY(ensure(b, b->ncbox, 2 * (size_t)NF)); TRY(ensure(b, b->laabb, NF)); TRY(ensure(b, b->fattr, NF));
+  TRY(ensure(b, b->nrec, 3 * (size_t)NF)); TRY(ensure(b, b->nhi, NF)); TRY(ensure(b, b->laabb, NF)); TRY(ensure(b, b->lattr, NF)); TRY(ensure(b, b->fattr, NF));
   TRY(ensure(b, b->pcount, (size_t)NF + 1)); TRY(ensure(b, b->pslots, 8 * (size_t)NF));
   TRY(ensure(b, b->poffB[0], (size_t)NF + 1)); TRY(ensure(b, b->poffB[1], (size_t)NF + 1));
   b->poff_valid[0] = b->poff_valid[1] = false;
@@ -611,6 +614,8 @@ static int flush_tail(Batch* b, TailPack& P) {
     wg_tail.push_back(make_float4(hw.gx, hw.gy, hw.inv_dt0, 0.0f));
   }
   b->h_body_off[NW] = NB; b->h_fix_off[NW] = NF; b->h_joint_off[NW] = NJ;
+  b->max_wfix = 0;
+  for (int w = 0; w < NW; ++w) b->max_wfix = std::max(b->max_wfix, b->h_fix_off[w + 1] - b->h_fix_off[w]);
   // world table: offsets are static, gravity/inv_dt0 of existing worlds stay as the device has them
   std::vector<int4> wb(NW), wj(NW);
   std::vector<int> wflags(NW);
@@ -660,7 +665,7 @@ static int flush_tail(Batch* b, TailPack& P) {
   TRY(ensure(b, b->aabb, NF)); TRY(ensure(b, b->mkey, NF)); TRY(ensure(b, b->mkey_sorted, NF));
   TRY(ensure(b, b->mval, NF)); TRY(ensure(b, b->mval_sorted, NF, true)); TRY(ensure(b, b->nchild, NF, true));
   TRY(ensure(b, b->nparent, NF, true)); TRY(ensure(b, b->lparent, NF, true)); TRY(ensure(b, b->naabb, NF));
-  TRY(ensure(b, b->ncbox, 2 * (size_t)NF)); TRY(ensure(b, b->laabb, NF)); TRY(ensure(b, b->fattr, NF));
+  TRY(ensure(b, b->nrec, 3 * (size_t)NF)); TRY(ensure(b, b->nhi, NF)); TRY(ensure(b, b->laabb, NF)); TRY(ensure(b, b->lattr, NF)); TRY(ensure(b, b->fattr, NF));
   TRY(ensure(b, b->nflag, NF)); TRY(ensure(b, b->pcount, (size_t)NF + 1));
   // the live list's per-fixture offsets stay valid for the existing fixtures; the appended
   // fixtures' entries come from their broadphase in the next step
@@ -1344,6 +1349,7 @@ B2G_API int b2g_batch_create(int device, uint64_t budget_bytes, b2g_batch** out)
   for (int i = 0; i < B2G_SOLVE_CLASSES; ++i) cudaStreamCreateWithFlags(&b->side[i], cudaStreamNonBlocking);
   for (int i = 0; i <= B2G_SOLVE_CLASSES; ++i) cudaEventCreateWithFlags(&b->fork_ev[i], cudaEventDisableTiming);
   solver_setup();
+  bp_setup();
   *out = b;
   return B2G_OK;
 }
@@ -1372,7 +1378,7 @@ B2G_API int b2g_batch_destroy(b2g_batch* b) {
   }
   release(b, b->wbounds); release(b, b->mkey); release(b, b->mkey_sorted); release(b, b->mval);
   release(b, b->mval_sorted); release(b, b->nchild); release(b, b->nparent); release(b, b->lparent);
-  release(b, b->naabb); release(b, b->ncbox); release(b, b->laabb); release(b, b->fattr); release(b, b->nflag); release(b, b->wroot); release(b, b->pcount); release(b, b->pslots); release(b, b->poffB[0]); release(b, b->poffB[1]); release(b, b->pairs);
+  release(b, b->naabb); release(b, b->nrec); release(b, b->nhi); release(b, b->laabb); release(b, b->lattr); release(b, b->fattr); release(b, b->nflag); release(b, b->wroot); release(b, b->pcount); release(b, b->pslots); release(b, b->poffB[0]); release(b, b->poffB[1]); release(b, b->pairs);
   release(b, b->cub_tmp); release(b, b->status); release(b, b->counters); release(b, b->sc_list); release(b, b->scb); release(b, b->cslot); release(b, b->frad);
   release(b, b->ccol); release(b, b->corder); release(b, b->cprio); release(b, b->cready); release(b, b->inc_cnt);
   release(b, b->inc_head); release(b, b->inc_mask); release(b, b->inc_list); release(b, b->cwork); release(b, b->jwork);

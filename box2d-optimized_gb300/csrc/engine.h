@@ -190,6 +190,7 @@ struct Batch {
   int NW = 0, NB = 0, NF = 0, NJ = 0;
   int64_t NC = 0;                 // live contacts
   std::vector<int> h_body_off, h_fix_off, h_joint_off;
+  int max_wfix = 0;               // fixtures of the largest world (from h_fix_off)
   std::vector<uint64_t> h_nocol;  // host copy of the device no-collide list (sorted body pairs)
 
   // ---- device arrays
@@ -252,7 +253,9 @@ struct Batch {
   DBuf<int> mval, mval_sorted;
   DBuf<int2> nchild;              // internal node children (leaf = index | 0x80000000)
   DBuf<int> nparent, lparent;     // parents of internal nodes and leaves
-  DBuf<float4> naabb, ncbox, laabb;
+  DBuf<float4> naabb, nrec, laabb;  // node boxes, node records (3 per node), sorted leaf boxes
+  DBuf<int> nhi;                  // node metas (last leaf of the range | static bit)
+  DBuf<int4> lattr;               // sorted leaf attributes
   DBuf<int4> fattr;
   DBuf<int> nflag;
   DBuf<int> wroot;                // per world: root node (leaf encoded), -1 if empty

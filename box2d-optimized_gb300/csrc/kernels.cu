@@ -302,11 +302,25 @@ __global__ void k_lbvh_internal(KernelArgs a, int n) {
   }
 }
 
+// Sorted-leaf attributes: x fixture, y body, z group << 16 | shape type | body type << 8, w filter
+// (category | mask << 16), from the fixture's packed attributes (k_aabb). The pair search reads
+// a leaf's fixture and filter data from its sorted position, with no indirection.
+__device__ __forceinline__ int4 leaf_attr(int f, int4 fa) {
+  return make_int4(f, fa.x, (int)(((uint32_t)fa.y << 16) | ((uint32_t)fa.w & 0xffffu)), fa.z);
+}
+__device__ __forceinline__ bool leaf_static(int4 la) { return ((la.z >> 8) & 0xff) == B2G_STATIC; }
+
+// A node's or leaf's meta: the last sorted leaf of its range, with the top bit set when the
+// range holds a static fixture.
+__device__ __forceinline__ int leaf_meta(int j, int4 la) { return j | (leaf_static(la) ? (int)0x80000000 : 0); }
+
 __global__ void k_lbvh_init(KernelArgs a, int n, int nw) {
   int idx = blockIdx.x * blockDim.x + threadIdx.x;
   if (idx < n) {
     int i = a.bp_f0 + idx;
-    a.laabb[i] = a.aabb[a.mval_sorted[i]];
+    const int f = a.mval_sorted[i];
+    a.laabb[i] = a.aabb[f];
+    a.lattr[i] = leaf_attr(f, a.fattr[f]);
     a.lparent[i] = -1;
     if (idx < n - 1) {
       a.nparent[i] = -1;
@@ -322,21 +336,124 @@ __global__ void k_lbvh_init(KernelArgs a, int n, int nw) {
 
 // Refit of existing trees: leaf boxes from the fixtures' new AABBs in the trees' leaf order, node
 // arrival counters cleared (internal nodes of every tree built over [0, n) lie in [0, n)).
+// Only the leaves of worlds above kRefitWorldMax fixtures: k_lbvh_refit_world refreshes the others.
 __global__ void k_lbvh_refit_init(KernelArgs a, int n) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  a.laabb[i] = a.aabb[a.mval_sorted[i]];
+  const int f = a.mval_sorted[i];
+  if (a.wb[a.fworld[f]].w <= kRefitWorldMax) return;
+  a.laabb[i] = a.aabb[f];
+  a.lattr[i] = leaf_attr(f, a.fattr[f]);
   a.nflag[i] = 0;
 }
 
-// Bottom-up node bounds: the second thread to reach a node combines its children. Walks stop at
-// their world's root (the traversal never reads nodes above it). The arrival counter is an
-// acquire-release atomic: the first thread's child bounds are visible to the second.
+// Node p's box, meta and record from its children (the second arrival at p does this).
+__device__ __forceinline__ void lbvh_combine(const KernelArgs& a, int p, int2 ch) {
+  float4 l, r;
+  int ml, mr;
+  if (ch.x & LEAF_BIT) {
+    const int j = ch.x & ~LEAF_BIT;
+    l = a.laabb[j];
+    ml = leaf_meta(j, a.lattr[j]);
+  } else {
+    l = __ldcg(&a.naabb[ch.x]);
+    ml = __ldcg(&a.nhi[ch.x]);
+  }
+  if (ch.y & LEAF_BIT) {
+    const int j = ch.y & ~LEAF_BIT;
+    r = a.laabb[j];
+    mr = leaf_meta(j, a.lattr[j]);
+  } else {
+    r = __ldcg(&a.naabb[ch.y]);
+    mr = __ldcg(&a.nhi[ch.y]);
+  }
+  float4 u = make_float4(fminf(l.x, r.x), fminf(l.y, r.y), fmaxf(l.z, r.z), fmaxf(l.w, r.w));
+  __stcg(&a.naabb[p], u);
+  // the range's last leaf is its right child's; the static bit is either child's
+  __stcg(&a.nhi[p], (mr & 0x7fffffff) | ((ml | mr) & (int)0x80000000));
+  float4* rec = a.nrec + 3 * (int64_t)p;
+  rec[0] = l;
+  rec[1] = r;
+  rec[2] = make_float4(__int_as_float(ch.x), __int_as_float(ch.y), __int_as_float(ml), __int_as_float(mr));
+}
+
+// Bottom-up node bounds of one world's tree per CTA, for worlds of 2 .. kRefitWorldMax fixtures:
+// a thread per leaf climbs towards the world's root, and the second arrival at a node combines
+// its children (lbvh_combine: box, record for the pair search, meta). The arrival counters live
+// in shared memory (a world's internal nodes are indices [first fixture, first fixture + count)
+// of the forest), so an arrival is a block-scope acquire-release atomic instead of a device-scope
+// one; the links of the next level are read while this level's children are. With INIT the leaf
+// boxes and attributes are refreshed first (a refit of a kept tree).
+constexpr int kRefitThreads = 512;
+
+template <bool INIT>
+__global__ void __launch_bounds__(kRefitThreads, 3) k_lbvh_refit_world(KernelArgs a) {
+  __shared__ int arrivals[kRefitWorldMax];
+  const int w = a.bp_w0 + blockIdx.x;
+  const int4 wb = a.wb[w];
+  const int f0 = wb.z, n = wb.w;
+  if (n < 2 || n > kRefitWorldMax) return;
+  const int root = a.wroot[w];
+  if (root < 0 || (root & LEAF_BIT)) return;
+  for (int k = threadIdx.x; k < n; k += blockDim.x) {
+    arrivals[k] = 0;
+    if (INIT) {
+      const int i = f0 + k;
+      const int f = a.mval_sorted[i];
+      a.laabb[i] = a.aabb[f];
+      a.lattr[i] = leaf_attr(f, a.fattr[f]);
+    }
+  }
+  __syncthreads();
+  int pn = threadIdx.x < n ? a.lparent[f0 + threadIdx.x] : 0;
+  for (int k = threadIdx.x; k < n; k += blockDim.x) {
+    int p = pn;
+    if (k + (int)blockDim.x < n) pn = a.lparent[f0 + k + blockDim.x];  // the next leaf's, in flight
+    if (p < f0 || p >= f0 + n) {  // every leaf of a tree has a parent inside its world's range
+      raise_status(a.status, B2G_DEV_STACK_OVERFLOW);
+      continue;
+    }
+    int2 ch = a.nchild[p];
+    int pp = a.nparent[p];
+    for (int guard = 0;; ++guard) {
+      if (guard > 256) {  // deeper than any valid tree over 2^31 leaves: the tree is malformed
+        raise_status(a.status, B2G_DEV_STACK_OVERFLOW);
+        break;
+      }
+      cuda::atomic_ref<int, cuda::thread_scope_block> arrived(arrivals[p - f0]);
+      if (arrived.fetch_add(1, cuda::memory_order_acq_rel) == 0) break;
+      const bool up = p != root;
+      if (up && (pp < f0 || pp >= f0 + n)) {
+        raise_status(a.status, B2G_DEV_STACK_OVERFLOW);
+        break;
+      }
+      int2 ch2 = ch;
+      int pp2 = pp;
+      if (up) {  // the next level's links, in flight with this level's child loads
+        ch2 = a.nchild[pp];
+        pp2 = a.nparent[pp];
+      }
+      lbvh_combine(a, p, ch);
+      if (!up) break;
+      p = pp;
+      ch = ch2;
+      pp = pp2;
+    }
+  }
+}
+
+// Bottom-up node bounds over the whole forest, for the leaves of worlds above kRefitWorldMax
+// fixtures: the second thread to reach a node combines its children (lbvh_combine). Walks stop at
+// their world's root (the traversal never reads nodes above it). The arrival counter is a
+// device-scope acquire-release atomic: the first thread's child bounds and meta are visible to
+// the second. A node's links are read before its arrival (they do not change during the pass).
 __global__ void k_lbvh_bounds(KernelArgs a, int n) {
   int idx = blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= n) return;
   int i = a.bp_f0 + idx;
-  const int root = a.wroot[a.fworld[a.mval_sorted[i]]];
+  const int w = a.fworld[a.mval_sorted[i]];
+  if (a.wb[w].w <= kRefitWorldMax) return;  // k_lbvh_refit_world's
+  const int root = a.wroot[w];
   if (root < 0 || (root & LEAF_BIT)) return;  // single-fixture world: the leaf is the root
   int p = a.lparent[i];
   int guard = 0;
@@ -345,17 +462,13 @@ __global__ void k_lbvh_bounds(KernelArgs a, int n) {
       raise_status(a.status, B2G_DEV_STACK_OVERFLOW);
       return;
     }
+    const int2 ch = a.nchild[p];
+    const int pp = a.nparent[p];
     cuda::atomic_ref<int, cuda::thread_scope_device> arrivals(a.nflag[p]);
     if (arrivals.fetch_add(1, cuda::memory_order_acq_rel) == 0) return;
-    int2 ch = a.nchild[p];
-    float4 l = (ch.x & LEAF_BIT) ? a.laabb[ch.x & ~LEAF_BIT] : __ldcg(&a.naabb[ch.x]);
-    float4 r = (ch.y & LEAF_BIT) ? a.laabb[ch.y & ~LEAF_BIT] : __ldcg(&a.naabb[ch.y]);
-    float4 u = make_float4(fminf(l.x, r.x), fminf(l.y, r.y), fmaxf(l.z, r.z), fmaxf(l.w, r.w));
-    __stcg(&a.naabb[p], u);
-    a.ncbox[2 * (int64_t)p] = l;  // the traversal tests both children from their parent's record
-    a.ncbox[2 * (int64_t)p + 1] = r;
+    lbvh_combine(a, p, ch);
     if (p == root) return;
-    p = a.nparent[p];
+    p = pp;
   }
 }
 
@@ -372,40 +485,38 @@ __device__ __forceinline__ bool nocollide_has(const uint64_t* keys, int n, uint6
   return lo < n && keys[lo] == key;
 }
 
-// Would fixture f (non-static, the emitter) report the pair (f, g)? Emitter rule: the non-static
-// fixture of a static pair, else the lower index. Filters of b2ContactManager::QueryCallback:
-// same body, b2Body::ShouldCollide (a dynamic body, no collideConnected=false joint), the default
-// b2ContactFilter (group / category / mask) and the collider table. fa / ga are the packed
-// attributes of f and g (k_aabb); `nocol` is the world's slice of the no-collide list (first,
-// count).
-__device__ __forceinline__ bool accept_pair(const KernelArgs& a, int f, int4 fa, int g, int4 ga, int2 nocol) {
-  if (g == f) return false;
-  int bf = fa.x, bg = ga.x;
-  if (bg == bf) return false;
-  int tf = fa.w >> 8, tg = ga.w >> 8;
-  if (tg != B2G_STATIC && g < f) return false;
-  if (tf != B2G_DYNAMIC && tg != B2G_DYNAMIC) return false;
+// Would the pair of sorted leaves x, y (leaf_attr records) be reported? The filters of
+// b2ContactManager::QueryCallback (src/dynamics/b2_contact_manager.cpp:136-188): same body,
+// b2Body::ShouldCollide (a dynamic body, no collideConnected=false joint: `nocol` is the world's
+// slice of the no-collide list, first and count), the default b2ContactFilter (group / category /
+// mask, src/dynamics/b2_world_callbacks.cpp:28-39) and the collider table. Symmetric in x and y;
+// which fixture emits the pair is decided by the caller.
+__device__ __forceinline__ bool accept_leaves(const KernelArgs& a, int4 x, int4 y, int2 nocol) {
+  if (x.y == y.y) return false;  // the same body (or the same fixture)
+  const int tx = (x.z >> 8) & 0xff, ty = (y.z >> 8) & 0xff;
+  if (tx != B2G_DYNAMIC && ty != B2G_DYNAMIC) return false;
   if (nocol.y > 0) {
-    uint32_t x = (uint32_t)min(bf, bg), y = (uint32_t)max(bf, bg);
-    if (nocollide_has(a.nocollide + nocol.x, nocol.y, ((uint64_t)x << 32) | y)) return false;
+    uint32_t lo = (uint32_t)min(x.y, y.y), hi = (uint32_t)max(x.y, y.y);
+    if (nocollide_has(a.nocollide + nocol.x, nocol.y, ((uint64_t)lo << 32) | hi)) return false;
   }
-  int gf = fa.y, gg = ga.y;
-  if (gf == gg && gf != 0) {
-    if (!(gf > 0)) return false;
+  const int gx = x.z >> 16, gy = y.z >> 16;
+  if (gx == gy && gx != 0) {
+    if (!(gx > 0)) return false;
   } else {
-    uint32_t ff = (uint32_t)fa.z, fg = (uint32_t)ga.z;
-    uint32_t catF = ff & 0xffffu, maskF = ff >> 16, catG = fg & 0xffffu, maskG = fg >> 16;
-    if (!((maskF & catG) != 0 && (catF & maskG) != 0)) return false;
+    const uint32_t fx = (uint32_t)x.w, fy = (uint32_t)y.w;
+    const uint32_t catX = fx & 0xffffu, maskX = fx >> 16, catY = fy & 0xffffu, maskY = fy >> 16;
+    if (!((maskX & catY) != 0 && (catX & maskY) != 0)) return false;
   }
-  int sf = fa.w & 0xff, sg = ga.w & 0xff;
-  return hasCollider(sf, sg) || hasCollider(sg, sf);
+  const int sx = x.z & 0xff, sy = y.z & 0xff;
+  return hasCollider(sx, sy) || hasCollider(sy, sx);
 }
 
 #define BP_STACK 96
 #define BP_SLOTS 8  // partners recorded per fixture by the counting pass
 
-// Pair search for one emitter fixture over its world's subtree; calls on_pair(g, j) for the j-th
-// accepted partner (traversal order) and returns the number of partners.
+// Every partner of emitter fixture f (non-static) over its world's subtree, for the emit pass of
+// fixtures with more partners than slots: f emits (f, g) when g is static or g > f. Calls
+// on_pair(g, j) for the j-th accepted partner (traversal order) and returns the number.
 template <class OnPair>
 __device__ __forceinline__ int traverse_pairs(const KernelArgs& a, int f, OnPair&& on_pair) {
   const int4 fa = a.fattr[f];
@@ -414,6 +525,7 @@ __device__ __forceinline__ int traverse_pairs(const KernelArgs& a, int f, OnPair
   if ((fa.w >> 8) == B2G_STATIC || (a.wflags[wf] & B2G_WF_RETIRED)) return 0;
   int root = a.wroot[wf];
   if (root < 0 || (root & LEAF_BIT)) return 0;
+  const int4 la = leaf_attr(f, fa);
   float4 box = a.aabb[f];
   const int4 wjw = a.wj[wf];
   const int2 nocol = make_int2(wjw.z, wjw.w);
@@ -428,16 +540,18 @@ __device__ __forceinline__ int traverse_pairs(const KernelArgs& a, int f, OnPair
       break;
     }
     int node = stack[--sp];
-    int2 ch = a.nchild[node];
-    float4 cbox[2] = {a.ncbox[2 * (int64_t)node], a.ncbox[2 * (int64_t)node + 1]};
-    int kids[2] = {ch.x, ch.y};
+    const float4* rec = a.nrec + 3 * (int64_t)node;
+    const float4 cbox[2] = {rec[0], rec[1]};
+    const float4 m4 = rec[2];
+    const int kids[2] = {__float_as_int(m4.x), __float_as_int(m4.y)};
 #pragma unroll
     for (int q = 0; q < 2; ++q) {
       int c = kids[q];
       if (!aabb_overlap4(box, cbox[q])) continue;
       if (c & LEAF_BIT) {
-        int g = a.mval_sorted[c & ~LEAF_BIT];
-        if (accept_pair(a, f, fa, g, a.fattr[g], nocol)) {
+        const int4 lg = a.lattr[c & ~LEAF_BIT];
+        const int g = lg.x;
+        if ((leaf_static(lg) || g > f) && accept_leaves(a, la, lg, nocol)) {
           on_pair(g, cnt);
           ++cnt;
         }
@@ -450,16 +564,62 @@ __device__ __forceinline__ int traverse_pairs(const KernelArgs& a, int f, OnPair
   return cnt;
 }
 
-// Counting pass: partners of every emitter fixture, the first BP_SLOTS of them kept. Threads walk
-// the fixtures in Morton order, so a warp's traversals follow neighbouring tree paths.
+// Counting pass over the sorted leaves (threads in Morton order, so that a warp's walks follow
+// neighbouring tree paths). Each overlapping pair is found once: a pair of non-static fixtures by
+// the leaf that sorts first (the walk skips every range that ends at or before its own leaf and
+// holds no static fixture), a static pair by its non-static leaf (static leaves do not walk). The
+// pair is counted for its emitter (the non-static fixture of a static pair, else the lower
+// index), whose first BP_SLOTS partners are kept in arrival order (the emit pass sorts them).
+// pcount holds zeros for the range beforehand.
 __global__ void k_pairs_count(KernelArgs a, int n) {
   int idx = blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= n) return;
-  int f = a.mval_sorted[a.bp_f0 + idx];
-  uint32_t* slots = a.pslots + (int64_t)f * BP_SLOTS;
-  a.pcount[f] = traverse_pairs(a, f, [&](int g, int j) {
-    if (j < BP_SLOTS) slots[j] = (uint32_t)g;
-  });
+  const int i = a.bp_f0 + idx;
+  const int4 la = a.lattr[i];
+  if (leaf_static(la)) return;
+  const int f = la.x;
+  const int wf = a.fworld[f];
+  if (a.wflags[wf] & B2G_WF_RETIRED) return;
+  const int root = a.wroot[wf];
+  if (root < 0 || (root & LEAF_BIT)) return;
+  const float4 box = a.laabb[i];
+  const int4 wjw = a.wj[wf];
+  const int2 nocol = make_int2(wjw.z, wjw.w);
+  int stack[BP_STACK];
+  int sp = 0;
+  stack[sp++] = root;
+  int visits = 0;
+  const int maxVisits = 2 * a.wb[wf].w + 8;  // each internal node of the world at most once
+  while (sp > 0) {
+    if (++visits > maxVisits) {
+      raise_status(a.status, B2G_DEV_STACK_OVERFLOW);
+      break;
+    }
+    const int node = stack[--sp];
+    const float4* rec = a.nrec + 3 * (int64_t)node;
+    const float4 cbox[2] = {rec[0], rec[1]};
+    const float4 m4 = rec[2];
+    const int kids[2] = {__float_as_int(m4.x), __float_as_int(m4.y)};
+    const int meta[2] = {__float_as_int(m4.z), __float_as_int(m4.w)};
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      if (meta[q] >= 0 && meta[q] <= i) continue;  // ends at or before this leaf, no static fixture
+      if (!aabb_overlap4(box, cbox[q])) continue;
+      const int c = kids[q];
+      if (c & LEAF_BIT) {
+        const int4 lg = a.lattr[c & ~LEAF_BIT];
+        if (!accept_leaves(a, la, lg, nocol)) continue;
+        const int g = lg.x;
+        const bool fe = meta[q] < 0 || f < g;  // a leaf's meta is negative when it is static
+        const int e = fe ? f : g, p = fe ? g : f;
+        const int k = atomicAdd(&a.pcount[e], 1);
+        if (k < BP_SLOTS) a.pslots[(int64_t)e * BP_SLOTS + k] = (uint32_t)p;
+      } else {
+        if (sp < BP_STACK) stack[sp++] = c;
+        else raise_status(a.status, B2G_DEV_STACK_OVERFLOW);
+      }
+    }
+  }
 }
 
 // Emit pass: each fixture's partners, ascending, as keys f << 32 | g at its scanned offset (the
@@ -674,6 +834,13 @@ void launch_collide(const KernelArgs& a, int nw, cudaStream_t s) {
   if (a.ccap > 0 && a.any_sensor) k_collide<true><<<grid_for(a.ccap, 128), 128, 0, s>>>(a);
   if (a.ccap > 0 && a.any_sleep && nw > 0) k_collide_closure<<<nw, 256, 0, s>>>(a);
 }
+void bp_setup() {
+  // the per-world refit runs three 512-thread CTAs of 32 KB shared memory per SM
+  cudaFuncSetAttribute(k_lbvh_refit_world<true>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                       cudaSharedmemCarveoutMaxShared);
+  cudaFuncSetAttribute(k_lbvh_refit_world<false>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                       cudaSharedmemCarveoutMaxShared);
+}
 void launch_clear_forces(const KernelArgs& a, int nb, cudaStream_t s) {
   if (nb > 0) k_clear_forces<<<grid_for(nb, 256), 256, 0, s>>>(a, nb);
 }
@@ -697,9 +864,11 @@ void launch_bp_build(const KernelArgs& a, int nf, int nw, size_t cub_bytes, int 
   k_lbvh_init<<<grid_for(m, 256), 256, 0, s>>>(a, nf, nw);
   if (nf > 1) {
     k_lbvh_internal<<<grid_for(nf - 1, 256), 256, 0, s>>>(a, nf);
-    k_lbvh_bounds<<<grid_for(nf, 256), 256, 0, s>>>(a, nf);
+    k_lbvh_refit_world<false><<<nw, kRefitThreads, 0, s>>>(a);
+    if (a.max_wfix > kRefitWorldMax) k_lbvh_bounds<<<grid_for(nf, 256), 256, 0, s>>>(a, nf);
   }
   if (!pairs) return;
+  cudaMemsetAsync(a.pcount, 0, sizeof(int) * (size_t)nf, s);
   k_pairs_count<<<grid_for(nf, 128), 128, 0, s>>>(a, nf);
   bytes = cub_bytes;
   cub::DeviceScan::ExclusiveSum(a.cub_tmp, bytes, a.pcount, a.poff, nf + 1, s);
@@ -726,8 +895,10 @@ void launch_bp_tail(const KernelArgs& a0, int f0, int nf, int w0, int nw, size_t
   k_lbvh_init<<<grid_for(m, 256), 256, 0, s>>>(a, n, nwt);
   if (n > 1) {
     k_lbvh_internal<<<grid_for(n - 1, 256), 256, 0, s>>>(a, n);
-    k_lbvh_bounds<<<grid_for(n, 256), 256, 0, s>>>(a, n);
+    k_lbvh_refit_world<false><<<nwt, kRefitThreads, 0, s>>>(a);
+    if (a.max_wfix > kRefitWorldMax) k_lbvh_bounds<<<grid_for(n, 256), 256, 0, s>>>(a, n);
   }
+  cudaMemsetAsync(a.pcount + f0, 0, sizeof(int) * (size_t)n, s);
   k_pairs_count<<<grid_for(n, 128), 128, 0, s>>>(a, n);
   bytes = cub_bytes;
   cub::DeviceScan::ExclusiveSum(a.cub_tmp, bytes, a.pcount + f0, a.poff + f0, n + 1, s);
@@ -745,8 +916,11 @@ void launch_bp_refit(const KernelArgs& a, int tree_nf, int tree_nw, int nf, int 
   }
   k_aabb<<<grid_for(nf, 128), 128, 0, s>>>(a, nf);
   if (tree_nf > 0) {
-    k_lbvh_refit_init<<<grid_for(tree_nf, 256), 256, 0, s>>>(a, tree_nf);
-    if (tree_nf > 1) k_lbvh_bounds<<<grid_for(tree_nf, 256), 256, 0, s>>>(a, tree_nf);
+    if (tree_nw > 0) k_lbvh_refit_world<true><<<tree_nw, kRefitThreads, 0, s>>>(a);
+    if (a.max_wfix > kRefitWorldMax) {
+      k_lbvh_refit_init<<<grid_for(tree_nf, 256), 256, 0, s>>>(a, tree_nf);
+      if (tree_nf > 1) k_lbvh_bounds<<<grid_for(tree_nf, 256), 256, 0, s>>>(a, tree_nf);
+    }
   }
   const int n = nf - tree_nf, nwt = nw - tree_nw;
   if (nwt > 0) {  // worlds appended after the kept trees: trees of their own over [tree_nf, nf)
@@ -764,9 +938,11 @@ void launch_bp_refit(const KernelArgs& a, int tree_nf, int tree_nw, int nf, int 
     k_lbvh_init<<<grid_for(m, 256), 256, 0, s>>>(t, n, nwt);
     if (n > 1) {
       k_lbvh_internal<<<grid_for(n - 1, 256), 256, 0, s>>>(t, n);
-      k_lbvh_bounds<<<grid_for(n, 256), 256, 0, s>>>(t, n);
+      k_lbvh_refit_world<false><<<nwt, kRefitThreads, 0, s>>>(t);
+      if (a.max_wfix > kRefitWorldMax) k_lbvh_bounds<<<grid_for(n, 256), 256, 0, s>>>(t, n);
     }
   }
+  cudaMemsetAsync(a.pcount, 0, sizeof(int) * (size_t)nf, s);
   k_pairs_count<<<grid_for(nf, 128), 128, 0, s>>>(a, nf);
   size_t bytes = cub_bytes;
   cub::DeviceScan::ExclusiveSum(a.cub_tmp, bytes, a.pcount, a.poff, nf + 1, s);

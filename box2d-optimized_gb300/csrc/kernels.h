@@ -87,8 +87,11 @@ struct KernelArgs {
   int2* nchild;
   int *nparent, *lparent;
   float4* naabb;
-  float4* ncbox;                  // per internal node: left and right child boxes
+  float4* nrec;                   // per internal node, 3 x 16 B: left child box, right child box,
+                                  // {left, right, left meta, right meta} (meta: lbvh_meta)
+  int* nhi;                       // per internal node: its meta (last leaf of its range, static bit)
   float4* laabb;                  // leaf boxes in sorted order
+  int4* lattr;                    // leaf attributes in sorted order (leaf_attr)
   int4* fattr;                    // per fixture: body, group, filter, shape type | body type << 8
   int* nflag;
   int* wroot;
@@ -127,6 +130,7 @@ struct KernelArgs {
   int events_on;
   int any_sleep;       // some world runs in sleep mode (dead contacts may wake bodies)
   int any_sensor;      // the layout has sensor fixtures (their contacts get an overlap pass)
+  int max_wfix;        // fixtures of the largest world (picks the tree refit kernels)
   unsigned long long* counters;
   unsigned int* status;
 
@@ -202,6 +206,10 @@ std::vector<SolveClass> plan_solve_classes(const std::vector<int>& order, const 
 int solver_max_cluster_ctas();
 bool solver_threads_valid(int t);
 void launch_clear_forces(const KernelArgs& a, int nb, cudaStream_t s);
+// Worlds of up to this many fixtures get their tree bounds from one CTA each, with the arrival
+// counters in shared memory; larger ones from the device-wide bottom-up pass.
+constexpr int kRefitWorldMax = 8192;
+void bp_setup();  // kernel attributes of the broadphase (once per device, before the first launch)
 // Broadphase up to the tree (AABBs, Morton sort, LBVH, node boxes); with `pairs` also the pair
 // count, its scan and the per-world contact ranges of the list being built.
 void launch_bp_build(const KernelArgs& a, int nf, int nw, size_t cub_bytes, int sort_bits, cudaStream_t s,

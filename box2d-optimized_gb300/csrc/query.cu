@@ -53,7 +53,7 @@ __device__ __forceinline__ void traverse_world(const KernelArgs& a, int w, bool 
     int kids[2] = {ch.x, ch.y};
 #pragma unroll
     for (int q = 0; q < 2; ++q) {
-      float4 b = a.ncbox[2 * (int64_t)node + q];
+      float4 b = a.nrec[3 * (int64_t)node + q];
       if (!keep_node(b)) continue;
       int c = kids[q];
       if (c & Q_LEAF) {
