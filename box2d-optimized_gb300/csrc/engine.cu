@@ -143,7 +143,6 @@ static KernelArgs make_args(Batch* b) {
   a.force = b->force.p; a.lc = b->lc.p; a.btype = b->btype.p; a.bworld = b->bworld.p;
   a.bstate = b->bstate.p; a.bwake = b->bwake.p; a.sl = b->sl.p; a.any_sleep = b->any_sleep ? 1 : 0;
   a.any_sensor = b->any_sensor ? 1 : 0;
-  a.max_wfix = b->max_wfix;
   a.shape = b->shape.p; a.fbody = b->fbody.p; a.fgroup = b->fgroup.p; a.fsensor = b->fsensor.p;
   a.fworld = b->fworld.p; a.frad = b->frad.p; a.ffilter = b->ffilter.p; a.fmat = b->fmat.p; a.aabb = b->aabb.p;
   a.joints = b->joints.p; a.nocollide = b->nocollide.p; a.n_nocollide = b->n_nocollide;
@@ -165,7 +164,7 @@ static KernelArgs make_args(Batch* b) {
   a.sp.rad = b->sp_rad.p;
   a.cready = b->cready.p; a.inc_cnt = b->inc_cnt.p; a.inc_head = b->inc_head.p;
   a.inc_mask = b->inc_mask.p; a.inc_list = b->inc_list.p; a.jinc_list = b->jinc_list.p; a.cwork = b->cwork.p; a.jwork = b->jwork.p; a.jcb = b->jcb.p;
-  a.jcol = b->jcol.p; a.jorder = b->jorder.p; a.jranges = b->jranges.p; a.jprio = b->jprio.p;
+  a.jcol = b->jcol.p; a.jorder = b->jorder.p; a.jranges = b->jranges.p; a.cranges = b->cranges.p; a.jprio = b->jprio.p;
   a.jready = b->jready.p; a.ncolors = b->ncolors.p;
   a.jplanes = b->jplanes.p; a.jstride = b->NJ;
   a.events = b->events.p; a.event_cap = b->event_cap; a.events_on = b->events_on ? 1 : 0;
@@ -304,8 +303,6 @@ int upload_all(Batch* b) {
     NC += (int64_t)hw.contacts.size();
   }
   b->h_body_off[NW] = NB; b->h_fix_off[NW] = NF; b->h_joint_off[NW] = NJ;
-  b->max_wfix = 0;
-  for (int w = 0; w < NW; ++w) b->max_wfix = std::max(b->max_wfix, b->h_fix_off[w + 1] - b->h_fix_off[w]);
   std::vector<float4> xf(NB), pos(NB), vel(NB), massd(NB), damp(NB), force(NB);
   std::vector<float2> lc(NB);
   std::vector<int> btype(NB), bworld(NB);
@@ -414,7 +411,7 @@ int upload_all(Batch* b) {
     TRY(upload(b, b->wc, wc));
   }
   TRY(ensure(b, b->wbounds, NW)); TRY(ensure(b, b->wroot, NW));
-  TRY(ensure(b, b->ncolors, 4 * (size_t)NW)); TRY(ensure(b, b->jranges, 65 * (size_t)NW));
+  TRY(ensure(b, b->ncolors, 4 * (size_t)NW)); TRY(ensure(b, b->jranges, 65 * (size_t)NW)); TRY(ensure(b, b->cranges, 65 * (size_t)NW));
   TRY(ensure(b, b->wfault, NW));
   CUDA_TRY(b, cudaMemsetAsync(b->wfault.p, 0, b->wfault.cap, b->stream));
   TRY(ensure(b, b->isl_dirty, NW));  // a new layout labels every world's islands afresh
@@ -614,8 +611,6 @@ static int flush_tail(Batch* b, TailPack& P) {
     wg_tail.push_back(make_float4(hw.gx, hw.gy, hw.inv_dt0, 0.0f));
   }
   b->h_body_off[NW] = NB; b->h_fix_off[NW] = NF; b->h_joint_off[NW] = NJ;
-  b->max_wfix = 0;
-  for (int w = 0; w < NW; ++w) b->max_wfix = std::max(b->max_wfix, b->h_fix_off[w + 1] - b->h_fix_off[w]);
   // world table: offsets are static, gravity/inv_dt0 of existing worlds stay as the device has them
   std::vector<int4> wb(NW), wj(NW);
   std::vector<int> wflags(NW);
@@ -647,7 +642,7 @@ static int flush_tail(Batch* b, TailPack& P) {
     TRY(ensure(b, b->wfault, NW));
     CUDA_TRY(b, cudaMemsetAsync(b->wfault.p, 0, b->wfault.cap, b->stream));
   }
-  TRY(ensure(b, b->jranges, 65 * (size_t)NW, true));
+  TRY(ensure(b, b->jranges, 65 * (size_t)NW, true)); TRY(ensure(b, b->cranges, 65 * (size_t)NW));
   TRY(st.add(b, b->xf, NB0, P.xf)); TRY(st.add(b, b->pos, NB0, P.pos)); TRY(st.add(b, b->vel, NB0, P.vel));
   TRY(st.add(b, b->massd, NB0, P.massd)); TRY(st.add(b, b->damp, NB0, P.damp)); TRY(st.add(b, b->force, NB0, P.force));
   TRY(st.add(b, b->lc, NB0, P.lc)); TRY(st.add(b, b->btype, NB0, P.btype)); TRY(st.add(b, b->bworld, NB0, P.bworld));
@@ -665,7 +660,8 @@ static int flush_tail(Batch* b, TailPack& P) {
   TRY(ensure(b, b->aabb, NF)); TRY(ensure(b, b->mkey, NF)); TRY(ensure(b, b->mkey_sorted, NF));
   TRY(ensure(b, b->mval, NF)); TRY(ensure(b, b->mval_sorted, NF, true)); TRY(ensure(b, b->nchild, NF, true));
   TRY(ensure(b, b->nparent, NF, true)); TRY(ensure(b, b->lparent, NF, true)); TRY(ensure(b, b->naabb, NF));
-  TRY(ensure(b, b->nrec, 3 * (size_t)NF)); TRY(ensure(b, b->nhi, NF)); TRY(ensure(b, b->laabb, NF)); TRY(ensure(b, b->lattr, NF)); TRY(ensure(b, b->fattr, NF));
+  TRY(ensure(b, b->nrec, 3 * (size_t)NF)); TRY(ensure(b, b->nhi, NF)); TRY(ensure(b, b->laabb, NF)); TRY(ensure(b, b->lattr, NF, true));
+  TRY(ensure(b, b->fattr, NF, true));  // kept trees keep their leaf attributes (a refit does not rewrite them)
   TRY(ensure(b, b->nflag, NF)); TRY(ensure(b, b->pcount, (size_t)NF + 1));
   // the live list's per-fixture offsets stay valid for the existing fixtures; the appended
   // fixtures' entries come from their broadphase in the next step
@@ -1081,7 +1077,12 @@ static int capture_graphs(Batch* b, float dt, int vi, int pi) {
       cudaGraph_t g = nullptr;
       CUDA_TRY(b, cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
       enqueue_step(b, dt, vi, pi, false, parity, false, mode);
+      const cudaError_t launched = cudaGetLastError();  // a launch refused during capture
       CUDA_TRY(b, cudaStreamEndCapture(b->stream, &g));
+      if (launched != cudaSuccess) {
+        cudaGraphDestroy(g);
+        CUDA_TRY(b, launched);
+      }
       CUDA_TRY(b, cudaGraphInstantiate(&b->graph_exec[mode][parity], g, 0));
       cudaGraphDestroy(g);
     }
@@ -1349,7 +1350,6 @@ B2G_API int b2g_batch_create(int device, uint64_t budget_bytes, b2g_batch** out)
   for (int i = 0; i < B2G_SOLVE_CLASSES; ++i) cudaStreamCreateWithFlags(&b->side[i], cudaStreamNonBlocking);
   for (int i = 0; i <= B2G_SOLVE_CLASSES; ++i) cudaEventCreateWithFlags(&b->fork_ev[i], cudaEventDisableTiming);
   solver_setup();
-  bp_setup();
   *out = b;
   return B2G_OK;
 }
@@ -1385,7 +1385,7 @@ B2G_API int b2g_batch_destroy(b2g_batch* b) {
   release(b, b->sp_nf); release(b, b->sp_cid); release(b, b->sp_r0); release(b, b->sp_r1); release(b, b->sp_nmtm);
   release(b, b->sp_bk); release(b, b->sp_kn); release(b, b->sp_imp); release(b, b->sp_idx); release(b, b->sp_lcs);
   release(b, b->sp_lnp); release(b, b->sp_lps); release(b, b->sp_rad);
-  release(b, b->jinc_list); release(b, b->jcol); release(b, b->jorder); release(b, b->jcb); release(b, b->jranges);
+  release(b, b->jinc_list); release(b, b->jcol); release(b, b->jorder); release(b, b->jcb); release(b, b->jranges); release(b, b->cranges);
   release(b, b->jprio); release(b, b->jready); release(b, b->jplanes);
   release(b, b->ncolors); release(b, b->events);
   release(b, b->q_world); release(b, b->q_counts); release(b, b->q_out); release(b, b->q_box); release(b, b->q_offs);

@@ -137,6 +137,7 @@ struct SolveClass {
   int cls;    // size class index
   bool wide;  // the 128-register build (few worlds: latency-bound) rather than the 64-register one
   int ctas;   // CTAs per world: 1, or the thread-block cluster size of the largest class
+  int setup_threads, setup_smem;  // the first half's launch (k_setup), for ctas == 1
 };
 #define B2G_SOLVE_CLASSES 5
 #define B2G_JV_ROWS 13  // float4 rows of one joint's solver record (solver_dev.cuh)
@@ -190,7 +191,6 @@ struct Batch {
   int NW = 0, NB = 0, NF = 0, NJ = 0;
   int64_t NC = 0;                 // live contacts
   std::vector<int> h_body_off, h_fix_off, h_joint_off;
-  int max_wfix = 0;               // fixtures of the largest world (from h_fix_off)
   std::vector<uint64_t> h_nocol;  // host copy of the device no-collide list (sorted body pairs)
 
   // ---- device arrays
@@ -288,6 +288,7 @@ struct Batch {
   DBuf<int2> jcb;
   DBuf<int8_t> jcol;
   DBuf<int> jorder, jranges;
+  DBuf<int> cranges;              // per world: 65 contact colour offsets of this step's solve
   DBuf<uint32_t> jprio;
   DBuf<uint8_t> jready;
   DBuf<float4> jplanes;           // joint velocity rows, B2G_JV_ROWS planes of NJ slots (solve scratch)

@@ -189,6 +189,9 @@ __global__ void k_clear_forces(KernelArgs a, int nbodies) {
 // ================================================================================ broadphase
 // Fixture AABBs, and the packed attributes the pair filter reads for every candidate partner:
 // (body, group index, category | mask << 16, shape type | body type << 8).
+// The attributes change only with the layout, which rebuilds every tree: ATTR is set for the
+// broadphases that build trees and clear for refits.
+template <bool ATTR>
 __global__ void k_aabb(KernelArgs a, int n) {
   int idx = blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= n) return;
@@ -197,7 +200,7 @@ __global__ void k_aabb(KernelArgs a, int n) {
   const b2g_shape& sh = a.shape[i];
   AABB bb = shapeAABB(sh, ldXf(a.xf, body));
   a.aabb[i] = make_float4(bb.lo.x, bb.lo.y, bb.hi.x, bb.hi.y);
-  a.fattr[i] = make_int4(body, a.fgroup[i], (int)a.ffilter[i], sh.type | (a.btype[body] << 8));
+  if (ATTR) a.fattr[i] = make_int4(body, a.fgroup[i], (int)a.ffilter[i], sh.type | (a.btype[body] << 8));
 }
 
 // Per-world bounds of AABB centres (lower + upper, the reference's GetCenter2) for Morton codes.
@@ -335,15 +338,12 @@ __global__ void k_lbvh_init(KernelArgs a, int n, int nw) {
 }
 
 // Refit of existing trees: leaf boxes from the fixtures' new AABBs in the trees' leaf order, node
-// arrival counters cleared (internal nodes of every tree built over [0, n) lie in [0, n)).
-// Only the leaves of worlds above kRefitWorldMax fixtures: k_lbvh_refit_world refreshes the others.
+// arrival counters cleared (internal nodes of every tree built over [0, n) lie in [0, n)). The
+// sorted leaf attributes stay those of the build: they change only with the layout.
 __global__ void k_lbvh_refit_init(KernelArgs a, int n) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  const int f = a.mval_sorted[i];
-  if (a.wb[a.fworld[f]].w <= kRefitWorldMax) return;
-  a.laabb[i] = a.aabb[f];
-  a.lattr[i] = leaf_attr(f, a.fattr[f]);
+  a.laabb[i] = a.aabb[a.mval_sorted[i]];
   a.nflag[i] = 0;
 }
 
@@ -377,82 +377,19 @@ __device__ __forceinline__ void lbvh_combine(const KernelArgs& a, int p, int2 ch
   rec[2] = make_float4(__int_as_float(ch.x), __int_as_float(ch.y), __int_as_float(ml), __int_as_float(mr));
 }
 
-// Bottom-up node bounds of one world's tree per CTA, for worlds of 2 .. kRefitWorldMax fixtures:
-// a thread per leaf climbs towards the world's root, and the second arrival at a node combines
-// its children (lbvh_combine: box, record for the pair search, meta). The arrival counters live
-// in shared memory (a world's internal nodes are indices [first fixture, first fixture + count)
-// of the forest), so an arrival is a block-scope acquire-release atomic instead of a device-scope
-// one; the links of the next level are read while this level's children are. With INIT the leaf
-// boxes and attributes are refreshed first (a refit of a kept tree).
-constexpr int kRefitThreads = 512;
-
-template <bool INIT>
-__global__ void __launch_bounds__(kRefitThreads, 3) k_lbvh_refit_world(KernelArgs a) {
-  __shared__ int arrivals[kRefitWorldMax];
-  const int w = a.bp_w0 + blockIdx.x;
-  const int4 wb = a.wb[w];
-  const int f0 = wb.z, n = wb.w;
-  if (n < 2 || n > kRefitWorldMax) return;
-  const int root = a.wroot[w];
-  if (root < 0 || (root & LEAF_BIT)) return;
-  for (int k = threadIdx.x; k < n; k += blockDim.x) {
-    arrivals[k] = 0;
-    if (INIT) {
-      const int i = f0 + k;
-      const int f = a.mval_sorted[i];
-      a.laabb[i] = a.aabb[f];
-      a.lattr[i] = leaf_attr(f, a.fattr[f]);
-    }
-  }
-  __syncthreads();
-  int pn = threadIdx.x < n ? a.lparent[f0 + threadIdx.x] : 0;
-  for (int k = threadIdx.x; k < n; k += blockDim.x) {
-    int p = pn;
-    if (k + (int)blockDim.x < n) pn = a.lparent[f0 + k + blockDim.x];  // the next leaf's, in flight
-    if (p < f0 || p >= f0 + n) {  // every leaf of a tree has a parent inside its world's range
-      raise_status(a.status, B2G_DEV_STACK_OVERFLOW);
-      continue;
-    }
-    int2 ch = a.nchild[p];
-    int pp = a.nparent[p];
-    for (int guard = 0;; ++guard) {
-      if (guard > 256) {  // deeper than any valid tree over 2^31 leaves: the tree is malformed
-        raise_status(a.status, B2G_DEV_STACK_OVERFLOW);
-        break;
-      }
-      cuda::atomic_ref<int, cuda::thread_scope_block> arrived(arrivals[p - f0]);
-      if (arrived.fetch_add(1, cuda::memory_order_acq_rel) == 0) break;
-      const bool up = p != root;
-      if (up && (pp < f0 || pp >= f0 + n)) {
-        raise_status(a.status, B2G_DEV_STACK_OVERFLOW);
-        break;
-      }
-      int2 ch2 = ch;
-      int pp2 = pp;
-      if (up) {  // the next level's links, in flight with this level's child loads
-        ch2 = a.nchild[pp];
-        pp2 = a.nparent[pp];
-      }
-      lbvh_combine(a, p, ch);
-      if (!up) break;
-      p = pp;
-      ch = ch2;
-      pp = pp2;
-    }
-  }
-}
-
-// Bottom-up node bounds over the whole forest, for the leaves of worlds above kRefitWorldMax
-// fixtures: the second thread to reach a node combines its children (lbvh_combine). Walks stop at
-// their world's root (the traversal never reads nodes above it). The arrival counter is a
-// device-scope acquire-release atomic: the first thread's child bounds and meta are visible to
-// the second. A node's links are read before its arrival (they do not change during the pass).
-__global__ void k_lbvh_bounds(KernelArgs a, int n) {
+// Bottom-up node bounds over the forest: a thread per leaf climbs towards its world's root and
+// the second thread to reach a node combines its children (lbvh_combine). Walks stop at their
+// world's root (the traversal never reads nodes above it). The arrival counter is a device-scope
+// acquire-release atomic: the first thread's child bounds and meta are visible to the second. A
+// node's links are read before its arrival (they do not change during the pass). Launched in
+// blocks of kBoundsThreads: a block's slot frees when its longest climb ends, so small blocks
+// keep the SMs filled while a few climbs go on towards the roots.
+constexpr int kBoundsThreads = 64;
+__global__ void __launch_bounds__(kBoundsThreads) k_lbvh_bounds(KernelArgs a, int n) {
   int idx = blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= n) return;
   int i = a.bp_f0 + idx;
   const int w = a.fworld[a.mval_sorted[i]];
-  if (a.wb[w].w <= kRefitWorldMax) return;  // k_lbvh_refit_world's
   const int root = a.wroot[w];
   if (root < 0 || (root & LEAF_BIT)) return;  // single-fixture world: the leaf is the root
   int p = a.lparent[i];
@@ -834,13 +771,6 @@ void launch_collide(const KernelArgs& a, int nw, cudaStream_t s) {
   if (a.ccap > 0 && a.any_sensor) k_collide<true><<<grid_for(a.ccap, 128), 128, 0, s>>>(a);
   if (a.ccap > 0 && a.any_sleep && nw > 0) k_collide_closure<<<nw, 256, 0, s>>>(a);
 }
-void bp_setup() {
-  // the per-world refit runs three 512-thread CTAs of 32 KB shared memory per SM
-  cudaFuncSetAttribute(k_lbvh_refit_world<true>, cudaFuncAttributePreferredSharedMemoryCarveout,
-                       cudaSharedmemCarveoutMaxShared);
-  cudaFuncSetAttribute(k_lbvh_refit_world<false>, cudaFuncAttributePreferredSharedMemoryCarveout,
-                       cudaSharedmemCarveoutMaxShared);
-}
 void launch_clear_forces(const KernelArgs& a, int nb, cudaStream_t s) {
   if (nb > 0) k_clear_forces<<<grid_for(nb, 256), 256, 0, s>>>(a, nb);
 }
@@ -855,7 +785,7 @@ void launch_bp_build(const KernelArgs& a, int nf, int nw, size_t cub_bytes, int 
     k_world_contacts<<<grid_for(nw, 128), 128, 0, s>>>(a, nw);
     return;
   }
-  k_aabb<<<grid_for(nf, 128), 128, 0, s>>>(a, nf);
+  k_aabb<true><<<grid_for(nf, 128), 128, 0, s>>>(a, nf);
   k_world_bounds<<<nw, 256, 0, s>>>(a);
   k_morton<<<grid_for(nf, 256), 256, 0, s>>>(a, nf);
   size_t bytes = cub_bytes;
@@ -864,8 +794,7 @@ void launch_bp_build(const KernelArgs& a, int nf, int nw, size_t cub_bytes, int 
   k_lbvh_init<<<grid_for(m, 256), 256, 0, s>>>(a, nf, nw);
   if (nf > 1) {
     k_lbvh_internal<<<grid_for(nf - 1, 256), 256, 0, s>>>(a, nf);
-    k_lbvh_refit_world<false><<<nw, kRefitThreads, 0, s>>>(a);
-    if (a.max_wfix > kRefitWorldMax) k_lbvh_bounds<<<grid_for(nf, 256), 256, 0, s>>>(a, nf);
+    k_lbvh_bounds<<<grid_for(nf, kBoundsThreads), kBoundsThreads, 0, s>>>(a, nf);
   }
   if (!pairs) return;
   cudaMemsetAsync(a.pcount, 0, sizeof(int) * (size_t)nf, s);
@@ -885,7 +814,7 @@ void launch_bp_tail(const KernelArgs& a0, int f0, int nf, int w0, int nw, size_t
     k_tail_ranges<<<grid_for(nwt + 1, 128), 128, 0, s>>>(a, nwt, 0, nullptr);
     return;
   }
-  k_aabb<<<grid_for(n, 128), 128, 0, s>>>(a, n);
+  k_aabb<true><<<grid_for(n, 128), 128, 0, s>>>(a, n);
   k_world_bounds<<<nwt, 256, 0, s>>>(a);
   k_morton<<<grid_for(n, 256), 256, 0, s>>>(a, n);
   size_t bytes = cub_bytes;
@@ -895,8 +824,7 @@ void launch_bp_tail(const KernelArgs& a0, int f0, int nf, int w0, int nw, size_t
   k_lbvh_init<<<grid_for(m, 256), 256, 0, s>>>(a, n, nwt);
   if (n > 1) {
     k_lbvh_internal<<<grid_for(n - 1, 256), 256, 0, s>>>(a, n);
-    k_lbvh_refit_world<false><<<nwt, kRefitThreads, 0, s>>>(a);
-    if (a.max_wfix > kRefitWorldMax) k_lbvh_bounds<<<grid_for(n, 256), 256, 0, s>>>(a, n);
+    k_lbvh_bounds<<<grid_for(n, kBoundsThreads), kBoundsThreads, 0, s>>>(a, n);
   }
   cudaMemsetAsync(a.pcount + f0, 0, sizeof(int) * (size_t)n, s);
   k_pairs_count<<<grid_for(n, 128), 128, 0, s>>>(a, n);
@@ -914,20 +842,18 @@ void launch_bp_refit(const KernelArgs& a, int tree_nf, int tree_nw, int nf, int 
     launch_bp_build(a, nf, nw, cub_bytes, sort_bits, s, true);
     return;
   }
-  k_aabb<<<grid_for(nf, 128), 128, 0, s>>>(a, nf);
-  if (tree_nf > 0) {
-    if (tree_nw > 0) k_lbvh_refit_world<true><<<tree_nw, kRefitThreads, 0, s>>>(a);
-    if (a.max_wfix > kRefitWorldMax) {
-      k_lbvh_refit_init<<<grid_for(tree_nf, 256), 256, 0, s>>>(a, tree_nf);
-      if (tree_nf > 1) k_lbvh_bounds<<<grid_for(tree_nf, 256), 256, 0, s>>>(a, tree_nf);
-    }
-  }
   const int n = nf - tree_nf, nwt = nw - tree_nw;
+  k_aabb<false><<<grid_for(tree_nf, 128), 128, 0, s>>>(a, tree_nf);
+  if (tree_nf > 0) {
+    k_lbvh_refit_init<<<grid_for(tree_nf, 256), 256, 0, s>>>(a, tree_nf);
+    if (tree_nf > 1) k_lbvh_bounds<<<grid_for(tree_nf, kBoundsThreads), kBoundsThreads, 0, s>>>(a, tree_nf);
+  }
   if (nwt > 0) {  // worlds appended after the kept trees: trees of their own over [tree_nf, nf)
     KernelArgs t = a;
     t.bp_f0 = tree_nf;
     t.bp_w0 = tree_nw;
     if (n > 0) {
+      k_aabb<true><<<grid_for(n, 128), 128, 0, s>>>(t, n);
       k_world_bounds<<<nwt, 256, 0, s>>>(t);
       k_morton<<<grid_for(n, 256), 256, 0, s>>>(t, n);
       size_t bytes = cub_bytes;
@@ -938,8 +864,7 @@ void launch_bp_refit(const KernelArgs& a, int tree_nf, int tree_nw, int nf, int 
     k_lbvh_init<<<grid_for(m, 256), 256, 0, s>>>(t, n, nwt);
     if (n > 1) {
       k_lbvh_internal<<<grid_for(n - 1, 256), 256, 0, s>>>(t, n);
-      k_lbvh_refit_world<false><<<nwt, kRefitThreads, 0, s>>>(t);
-      if (a.max_wfix > kRefitWorldMax) k_lbvh_bounds<<<grid_for(n, 256), 256, 0, s>>>(t, n);
+      k_lbvh_bounds<<<grid_for(n, kBoundsThreads), kBoundsThreads, 0, s>>>(t, n);
     }
   }
   cudaMemsetAsync(a.pcount, 0, sizeof(int) * (size_t)nf, s);

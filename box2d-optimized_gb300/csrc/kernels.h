@@ -120,6 +120,7 @@ struct KernelArgs {
   int8_t* jcol;
   int* jorder;
   int* jranges;                   // per world: 65 joint colour offsets
+  int* cranges;                   // per world: 65 contact colour offsets (setup -> iterations)
   uint32_t* jprio;
   uint8_t* jready;
   int* ncolors;                   // per world: contact colours, joint colours, solver contacts, slot base
@@ -130,7 +131,6 @@ struct KernelArgs {
   int events_on;
   int any_sleep;       // some world runs in sleep mode (dead contacts may wake bodies)
   int any_sensor;      // the layout has sensor fixtures (their contacts get an overlap pass)
-  int max_wfix;        // fixtures of the largest world (picks the tree refit kernels)
   unsigned long long* counters;
   unsigned int* status;
 
@@ -206,10 +206,6 @@ std::vector<SolveClass> plan_solve_classes(const std::vector<int>& order, const 
 int solver_max_cluster_ctas();
 bool solver_threads_valid(int t);
 void launch_clear_forces(const KernelArgs& a, int nb, cudaStream_t s);
-// Worlds of up to this many fixtures get their tree bounds from one CTA each, with the arrival
-// counters in shared memory; larger ones from the device-wide bottom-up pass.
-constexpr int kRefitWorldMax = 8192;
-void bp_setup();  // kernel attributes of the broadphase (once per device, before the first launch)
 // Broadphase up to the tree (AABBs, Morton sort, LBVH, node boxes); with `pairs` also the pair
 // count, its scan and the per-world contact ranges of the list being built.
 void launch_bp_build(const KernelArgs& a, int nf, int nw, size_t cub_bytes, int sort_bits, cudaStream_t s,

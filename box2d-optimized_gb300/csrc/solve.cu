@@ -129,6 +129,11 @@ static const int kClassMaxBodies[B2G_SOLVE_CLASSES] = {64, 256, 1024, 8192, 1 <<
 static const int kSmemCapByThreads[2][B2G_SOLVE_CLASSES] = {{16 << 10, 24 << 10, 56 << 10, 110 << 10, 200 << 10},
                                                             {27 << 10, 54 << 10, 110 << 10, 220 << 10, 220 << 10}};
 static int g_num_sms = 0;
+// The setup kernel (k_setup): at most 512 threads per world, 1024 threads per SM; its dynamic
+// shared memory (for the colouring) by threads per CTA (64, 128, 256, 512), so that 1024 / T
+// CTAs stay resident.
+static const int kSetupMaxThreads = 512;
+static const int kSetupSmemCap[4] = {12 << 10, 24 << 10, 48 << 10, 100 << 10};
 
 static int threads_index(int t) {
   int k = 0;
@@ -153,8 +158,11 @@ std::vector<SolveClass> plan_solve_classes(const std::vector<int>& order, const 
       ++i;
     }
     if (i == start) continue;
-    int64_t need = 68ll * nbmax;  // colouring at two contacts per body: 16 + 2 x 26 B per body
+    // the iterations hold the bodies' state and inverse masses (24 B per body); the setup as
+    // much of the colouring as fits (at two contacts per body: 16 + 2 x 26 B per body)
+    int64_t need = 24ll * nbmax + 16;
     need = (need + 15) & ~15ll;
+    const int64_t setup_need = ((68ll * nbmax) + 15) & ~15ll;
     int t = class_threads[c];
     int ti = threads_index(t);
     // the wide build unless the class holds more than wide_waves waves of it
@@ -163,10 +171,12 @@ std::vector<SolveClass> plan_solve_classes(const std::vector<int>& order, const 
     int smem = (int)(need < cap ? need : cap);
     // the largest class: a thread-block cluster per world when the device runs one
     if (c == B2G_SOLVE_CLASSES - 1 && cluster_ctas > 1) {
-      out.push_back({start, i - start, kClusterThreads, 0, c, true, cluster_ctas});
+      out.push_back({start, i - start, kClusterThreads, 0, c, true, cluster_ctas, 0, 0});
       continue;
     }
-    out.push_back({start, i - start, t, smem, c, wide, 1});
+    const int st = t < kSetupMaxThreads ? t : kSetupMaxThreads;
+    const int scap = kSetupSmemCap[threads_index(st)];
+    out.push_back({start, i - start, t, smem, c, wide, 1, st, (int)(setup_need < scap ? setup_need : scap)});
   }
   return out;
 }
@@ -176,7 +186,17 @@ static void set_smem_attr(int c) {
   cudaFuncSetAttribute(k_solve<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemCapByThreads[0][c]);
 }
 
+template <int T>
+static void set_setup_smem_attr(int c) {
+  cudaFuncSetAttribute(k_setup<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSetupSmemCap[c]);
+}
+
 void solver_setup() {
+  // the setup kernel's dynamic allowance comes on top of its static shared memory
+  set_setup_smem_attr<64>(0);
+  set_setup_smem_attr<128>(1);
+  set_setup_smem_attr<256>(2);
+  set_setup_smem_attr<512>(3);
   set_smem_attr<64>(0);
   set_smem_attr<128>(1);
   set_smem_attr<256>(2);
@@ -192,6 +212,12 @@ static void launch_class(const KernelArgs& a, const SolveClass& c, cudaStream_t 
   if (c.ctas > 1) {
     launch_solve_class_cluster(a, c, s);
     return;
+  }
+  switch (c.setup_threads) {
+    case 64: k_setup<64><<<c.count, 64, c.setup_smem, s>>>(a, c.first, c.setup_smem); break;
+    case 128: k_setup<128><<<c.count, 128, c.setup_smem, s>>>(a, c.first, c.setup_smem); break;
+    case 256: k_setup<256><<<c.count, 256, c.setup_smem, s>>>(a, c.first, c.setup_smem); break;
+    default: k_setup<512><<<c.count, 512, c.setup_smem, s>>>(a, c.first, c.setup_smem); break;
   }
   if (c.wide) {
     launch_solve_class_wide(a, c, s);

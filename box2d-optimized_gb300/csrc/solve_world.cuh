@@ -839,17 +839,19 @@ __device__ void sleep_islands(Team& tm, const KernelArgs& a, int b0, int nb) {
 template <int T, bool WIDE>
 constexpr int kSolveBlocks = WIDE ? (T >= 512 ? 1 : 512 / T) : 1024 / T;
 
-// The island solve of world w by team tm; smem / smem_bytes: the CTA's dynamic shared memory (a
-// cluster team passes none: its world's arrays stay in global memory). PREFETCH: each thread
-// reads its next colour's rows before the colour barrier (the 128-register builds).
-template <class Team, bool PREFETCH>
-__device__ __forceinline__ void solve_world(Team& tm, const KernelArgs& a, int w, unsigned char* smem, int smem_bytes) {
+// The first half of the island solve of world w by team tm: islands (sleep-mode worlds), the
+// solver contacts and their colouring, velocity integration and the contact constraints. Its
+// results are in global memory (the world's colour ranges in a.cranges, the integrated
+// velocities in a.vel, the constraint planes), so that the second half (iterate_world) can run
+// in another kernel. smem / smem_bytes: the CTA's dynamic shared memory, for whatever part of the
+// colouring's working arrays fits (a cluster team passes none).
+template <class Team>
+__device__ __forceinline__ void setup_world(Team& tm, const KernelArgs& a, int w, unsigned char* smem, int smem_bytes) {
   constexpr cuda::thread_scope S = Team::kScope;
   constexpr int NT = Team::kThreads;            // threads of the team
   constexpr int TC = NT / Team::kCtas;          // threads of one CTA
   const int tid = tm.tid();
   __shared__ int cranges[65];
-  __shared__ int jranges[65];
   const int4 wb = a.wb[w];
   const int b0 = wb.x, nb = wb.y, fo = wb.z;
   const int2 wc = a.wc[w];
@@ -933,9 +935,9 @@ __device__ __forceinline__ void solve_world(Team& tm, const KernelArgs& a, int w
       tm.sync();
     }
   }
-  // joints: colours fixed per layout
+  // the colour ranges for the iterations (joints: colours fixed per layout)
+  for (int c = tid; c <= ncc; c += NT) a.cranges[65 * (int64_t)w + c] = cranges[c];
   const int njc = nj > 0 ? a.ncolors[4 * w + 1] : 0;
-  for (int c = threadIdx.x; c <= njc; c += TC) jranges[c] = a.jranges[65 * (int64_t)w + c];
   if (tid == 0) {
     a.ncolors[4 * w] = ncc;
     a.ncolors[4 * w + 2] = nsc;
@@ -944,19 +946,13 @@ __device__ __forceinline__ void solve_world(Team& tm, const KernelArgs& a, int w
     atomicMax(&a.counters[B2G_CNT_MAXCOLORS], (unsigned long long)(ncc > njc ? ncc : njc));
   }
 
-  // 3. velocity integration (b2_island.cpp:256-293, SolveOrphan :187-206) into the body-state
-  //    buffer: shared memory (with the bodies' inverse masses) when the world's bodies fit, else
-  //    the global velocity array
-  const bool bsm = (size_t)nb * (sizeof(float4) + sizeof(float2)) <= (size_t)smem_bytes;
-  float4* bs = bsm ? reinterpret_cast<float4*>(smem) : a.vel + b0;
-  float2* msm = bsm ? reinterpret_cast<float2*>(smem + sizeof(float4) * (size_t)nb) : nullptr;
-  const Masses M{msm, a.massd + b0};
+  // 3. velocity integration (b2_island.cpp:256-293, SolveOrphan :187-206) into the global
+  //    velocity array
   for (int i = tid; i < nb; i += NT) {
     int bi = b0 + i;
-    float4 v4 = a.vel[bi];
-    float4 md = a.massd[bi];
-    if (bsm) msm[i] = make_float2(md.y, md.w);
     if (a.btype[bi] == B2G_DYNAMIC && (!sleepMode || (BS[i].x & B2G_BS_AWAKE))) {
+      float4 v4 = a.vel[bi];
+      float4 md = a.massd[bi];
       float4 dmp = a.damp[bi];
       float4 fr = a.force[bi];
       V2 v = mk(v4.x, v4.y);
@@ -966,13 +962,11 @@ __device__ __forceinline__ void solve_world(Team& tm, const KernelArgs& a, int w
       v.x /= (1.0f + h * dmp.x);
       v.y /= (1.0f + h * dmp.x);
       wv /= (1.0f + h * dmp.y);
-      v4 = make_float4(v.x, v.y, wv, 0.0f);
-      bs[i] = v4;
-    } else if (bsm) {
-      bs[i] = v4;
+      a.vel[bi] = make_float4(v.x, v.y, wv, 0.0f);
     }
   }
   tm.sync();
+  const float4* bs = a.vel + b0;
 
   // 4. prepare (b2ContactSolver::Initialize + InitializeVelocityConstraints) in list order, each
   //    constraint written to its colour-ordered slot
@@ -990,6 +984,56 @@ __device__ __forceinline__ void solve_world(Team& tm, const KernelArgs& a, int w
                    a.pos[ia], bs[la], a.pos[ib], bs[lbb], dtRatio, warm, ci);
     store_planes(P, c0 + p, vc);
   }
+}
+
+// The second half of the island solve of world w by team tm, after setup_world: warm start,
+// velocity iterations, position integration and iterations, transforms and sleep timers.
+// smem / smem_bytes: the CTA's dynamic shared memory, which holds the world's body state and
+// inverse masses when they fit (a cluster team passes none: its world's arrays stay in global
+// memory). PREFETCH: each thread reads its next colour's rows before the colour barrier (the
+// 128-register builds).
+template <class Team, bool PREFETCH>
+__device__ __forceinline__ void iterate_world(Team& tm, const KernelArgs& a, int w, unsigned char* smem, int smem_bytes) {
+  constexpr cuda::thread_scope S = Team::kScope;
+  constexpr int NT = Team::kThreads;            // threads of the team
+  constexpr int TC = NT / Team::kCtas;          // threads of one CTA
+  const int tid = tm.tid();
+  __shared__ int cranges[65];
+  __shared__ int jranges[65];
+  const int4 wb = a.wb[w];
+  const int b0 = wb.x, nb = wb.y, fo = wb.z;
+  const int2 wc = a.wc[w];
+  const int c0 = wc.x, ncAll = wc.y;
+  const int4 wj = a.wj[w];
+  const int j0 = wj.x, nj = wj.y;
+  const float4 wg = a.wg[w];
+  const float h = a.dt;
+  const float dtRatio = wg.z * a.dt;
+  const int wfl = a.wflags[w];
+  const bool warm = (wfl & B2G_WF_WARM) != 0;
+  const bool sleepMode = (wfl & B2G_WF_SLEEPMODE) != 0;
+  const V2 gravity = mk(wg.x, wg.y);
+  const SolverPlanes P = a.sp;
+  int4* const SL = a.sl + b0;
+  int2* const BS = a.bstate + b0;
+
+  const int ncc = a.ncolors[4 * w];
+  const int nsc = a.ncolors[4 * w + 2];
+  const int njc = nj > 0 ? a.ncolors[4 * w + 1] : 0;
+  for (int c = threadIdx.x; c <= ncc; c += TC) cranges[c] = a.cranges[65 * (int64_t)w + c];
+  for (int c = threadIdx.x; c <= njc; c += TC) jranges[c] = a.jranges[65 * (int64_t)w + c];
+  // the body-state buffer: shared memory (with the bodies' inverse masses) when the world's
+  // bodies fit, else the global velocity array
+  const bool bsm = (size_t)nb * (sizeof(float4) + sizeof(float2)) <= (size_t)smem_bytes;
+  float4* bs = bsm ? reinterpret_cast<float4*>(smem) : a.vel + b0;
+  float2* msm = bsm ? reinterpret_cast<float2*>(smem + sizeof(float4) * (size_t)nb) : nullptr;
+  const Masses M{msm, a.massd + b0};
+  if (bsm)
+    for (int i = tid; i < nb; i += NT) {
+      const float4 md = a.massd[b0 + i];
+      bs[i] = a.vel[b0 + i];
+      msm[i] = make_float2(md.y, md.w);
+    }
   tm.sync();
   float4* jb = bs - b0;  // joints address bodies by global index
 
@@ -1181,14 +1225,27 @@ __device__ __forceinline__ void solve_world(Team& tm, const KernelArgs& a, int w
   if (tid == 0 && a.dt > 0.0f) a.wg[w].z = a.inv_dt;
 }
 
-// One CTA per world: the size classes of the batch.
+// The first half of the solve for the size classes of the batch, one CTA per world; T is at most
+// 512 and the launch keeps 1024 threads per SM resident (64 registers a thread).
+template <int T>
+constexpr int kSetupBlocks = 1024 / T;
+template <int T>
+__global__ void __launch_bounds__(T, kSetupBlocks<T>) k_setup(KernelArgs a, int first, int smem_bytes) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int w = a.world_order[first + blockIdx.x];
+  if ((a.wflags[w] & B2G_WF_ACTIVE) == 0) return;
+  CtaTeam<T> tm;
+  setup_world(tm, a, w, smem, smem_bytes);
+}
+
+// The second half for the size classes, one CTA per world.
 template <int T, bool WIDE>
 __global__ void __launch_bounds__(T, kSolveBlocks<T, WIDE>) k_solve(KernelArgs a, int first, int smem_bytes) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int w = a.world_order[first + blockIdx.x];
   if ((a.wflags[w] & B2G_WF_ACTIVE) == 0) return;
   CtaTeam<T> tm;
-  solve_world<CtaTeam<T>, (WIDE && T <= 512)>(tm, a, w, smem, smem_bytes);
+  iterate_world<CtaTeam<T>, (WIDE && T <= 512)>(tm, a, w, smem, smem_bytes);
 }
 
 // One thread-block cluster of CS CTAs per world: the worlds above the largest CTA class. The
@@ -1204,7 +1261,11 @@ __global__ void __launch_bounds__(T, 1) k_solve_cluster(KernelArgs a, int first)
   tm.votes = cluster_map(votes, 0);
   cluster_barrier();  // every CTA runs, and rank 0's votes are clear, before any remote access
   const int w = a.world_order[first + (int)(blockIdx.x / CS)];
-  if ((a.wflags[w] & B2G_WF_ACTIVE) != 0) solve_world<ClusterTeam<T, CS>, (T <= 512)>(tm, a, w, nullptr, 0);
+  if ((a.wflags[w] & B2G_WF_ACTIVE) != 0) {
+    setup_world(tm, a, w, nullptr, 0);
+    tm.sync();  // the setup's global results are visible across the cluster
+    iterate_world<ClusterTeam<T, CS>, (T <= 512)>(tm, a, w, nullptr, 0);
+  }
   cluster_barrier();  // rank 0's shared memory outlives every remote access to it
 }
 
