@@ -157,7 +157,7 @@ static KernelArgs make_args(Batch* b) {
   a.mval_sorted = b->mval_sorted.p; a.nchild = b->nchild.p; a.nparent = b->nparent.p; a.lparent = b->lparent.p;
   a.naabb = b->naabb.p; a.nrec = b->nrec.p; a.nhi = b->nhi.p; a.laabb = b->laabb.p; a.lattr = b->lattr.p; a.fattr = b->fattr.p; a.nflag = b->nflag.p; a.wroot = b->wroot.p; a.pcount = b->pcount.p; a.pslots = b->pslots.p; a.poff = b->poffB[b->cur ^ 1].p; a.poff_old = nullptr;
   a.pairs = b->pairs.p; a.cub_tmp = b->cub_tmp.p;
-  a.sc_list = b->sc_list.p; a.scb = b->scb.p; a.cslot = b->cslot.p; a.ccol = b->ccol.p; a.corder = b->corder.p; a.cprio = b->cprio.p;
+  a.sc_list = b->sc_list.p; a.scb = b->scb.p; a.srad = b->srad.p; a.cslot = b->cslot.p; a.ccol = b->ccol.p; a.corder = b->corder.p; a.cprio = b->cprio.p;
   a.sp.nf = b->sp_nf.p; a.sp.cid = b->sp_cid.p; a.sp.r0 = b->sp_r0.p; a.sp.r1 = b->sp_r1.p;
   a.sp.nmtm = b->sp_nmtm.p; a.sp.bk = b->sp_bk.p; a.sp.kn = b->sp_kn.p; a.sp.imp = b->sp_imp.p;
   a.sp.idx = b->sp_idx.p; a.sp.lcs = b->sp_lcs.p; a.sp.lnp = b->sp_lnp.p; a.sp.lps = b->sp_lps.p;
@@ -816,7 +816,7 @@ static int ensure_contact_capacity(Batch* b, int64_t want) {
     TRY(ensure(b, b->cman[k], (size_t)cap, keep));
   }
   TRY(ensure(b, b->pairs, (size_t)cap));
-  TRY(ensure(b, b->sc_list, (size_t)cap)); TRY(ensure(b, b->scb, (size_t)cap)); TRY(ensure(b, b->cslot, (size_t)cap)); TRY(ensure(b, b->ccol, (size_t)cap));
+  TRY(ensure(b, b->sc_list, (size_t)cap)); TRY(ensure(b, b->scb, (size_t)cap)); TRY(ensure(b, b->srad, (size_t)cap)); TRY(ensure(b, b->cslot, (size_t)cap)); TRY(ensure(b, b->ccol, (size_t)cap));
   TRY(ensure(b, b->corder, (size_t)cap)); TRY(ensure(b, b->cprio, (size_t)cap)); TRY(ensure(b, b->cready, (size_t)cap));
   TRY(ensure(b, b->inc_list, 2 * (size_t)cap)); TRY(ensure(b, b->cwork, 2 * (size_t)cap));
   TRY(ensure(b, b->sp_nf, (size_t)cap)); TRY(ensure(b, b->sp_cid, (size_t)cap)); TRY(ensure(b, b->sp_r0, (size_t)cap));
@@ -1379,7 +1379,7 @@ B2G_API int b2g_batch_destroy(b2g_batch* b) {
   release(b, b->wbounds); release(b, b->mkey); release(b, b->mkey_sorted); release(b, b->mval);
   release(b, b->mval_sorted); release(b, b->nchild); release(b, b->nparent); release(b, b->lparent);
   release(b, b->naabb); release(b, b->nrec); release(b, b->nhi); release(b, b->laabb); release(b, b->lattr); release(b, b->fattr); release(b, b->nflag); release(b, b->wroot); release(b, b->pcount); release(b, b->pslots); release(b, b->poffB[0]); release(b, b->poffB[1]); release(b, b->pairs);
-  release(b, b->cub_tmp); release(b, b->status); release(b, b->counters); release(b, b->sc_list); release(b, b->scb); release(b, b->cslot); release(b, b->frad);
+  release(b, b->cub_tmp); release(b, b->status); release(b, b->counters); release(b, b->sc_list); release(b, b->scb); release(b, b->srad); release(b, b->cslot); release(b, b->frad);
   release(b, b->ccol); release(b, b->corder); release(b, b->cprio); release(b, b->cready); release(b, b->inc_cnt);
   release(b, b->inc_head); release(b, b->inc_mask); release(b, b->inc_list); release(b, b->cwork); release(b, b->jwork);
   release(b, b->sp_nf); release(b, b->sp_cid); release(b, b->sp_r0); release(b, b->sp_r1); release(b, b->sp_nmtm);

@@ -271,6 +271,7 @@ struct Batch {
   // solver scratch
   DBuf<int> sc_list;              // per world: compacted solver contact indices (global)
   DBuf<int2> scb;                 // per solver contact: world-local bodies, bit 31 set = static
+  DBuf<float2> srad;              // per solver contact: the two fixtures' radii
   DBuf<int> cslot;                // per solver contact: colour-ordered slot
   DBuf<float4> sp_nf, sp_r0, sp_r1, sp_nmtm, sp_bk, sp_kn, sp_imp, sp_lcs, sp_lnp, sp_lps;
   DBuf<int2> sp_idx;

@@ -106,6 +106,7 @@ struct KernelArgs {
   // solver
   int* sc_list;                   // per solver contact: live contact index
   int2* scb;                      // per solver contact: world-local bodies, bit 31 set = static
+  float2* srad;                   // per solver contact: the two fixtures' radii (compaction -> prepare)
   int* cslot;                     // per solver contact: its colour-ordered slot
   SolverPlanes sp;
   int8_t* ccol;

@@ -259,87 +259,137 @@ __device__ int colour_constraints(Team& tm, int n, int nb, const ColourMem m, co
     if (b.y >= 0) m.list[m.head[b.y] + atomicAdd(&m.cnt[b.y], 1)] = k;
   }
   tm.sync();
-  // each body's list in (priority, index) order
+  // each body's list in (priority, index) order: lists of up to 8 entries sorted in registers
+  // (their priorities read together), longer ones by insertion; cnt becomes the list's end
   for (int i = tid; i < nb; i += NT) {
-    int off = m.head[i], cnt = m.cnt[i];
-    for (int x = 1; x < cnt; ++x) {
-      int kx = m.list[off + x];
-      uint32_t px = prio[kx];
-      int y = x - 1;
-      while (y >= 0) {
-        int ky = m.list[off + y];
-        uint32_t py = prio[ky];
-        if (py < px || (py == px && ky < kx)) break;
-        m.list[off + y + 1] = ky;
-        --y;
+    const int off = m.head[i], cnt = m.cnt[i];
+    if (cnt <= 8) {
+      uint64_t key[8];
+#pragma unroll
+      for (int x = 0; x < 8; ++x) {
+        const int kx = x < cnt ? m.list[off + x] : 0;
+        key[x] = x < cnt ? (((uint64_t)prio[kx] << 32) | (uint32_t)kx) : ~0ull;
       }
-      m.list[off + y + 1] = kx;
+#pragma unroll
+      for (int r = 0; r < 8; ++r) {
+#pragma unroll
+        for (int x = r & 1; x + 1 < 8; x += 2) {
+          const uint64_t u = key[x], v = key[x + 1];
+          key[x] = u < v ? u : v;
+          key[x + 1] = u < v ? v : u;
+        }
+      }
+#pragma unroll
+      for (int x = 0; x < 8; ++x)
+        if (x < cnt) m.list[off + x] = (int)(uint32_t)key[x];
+    } else {
+      for (int x = 1; x < cnt; ++x) {
+        int kx = m.list[off + x];
+        uint32_t px = prio[kx];
+        int y = x - 1;
+        while (y >= 0) {
+          int ky = m.list[off + y];
+          uint32_t py = prio[ky];
+          if (py < px || (py == px && ky < kx)) break;
+          m.list[off + y + 1] = ky;
+          --y;
+        }
+        m.list[off + y + 1] = kx;
+      }
     }
+    m.cnt[i] = off + cnt;
   }
-  // rounds over a worklist of the uncoloured constraints: a round colours every constraint that
-  // heads the priority lists of all its non-static bodies (at least the uncoloured one of lowest
-  // (priority, index)); the others form the next round's worklist (their order is immaterial)
-  // worklist sizes alternate between two team counters: a round reads one and fills the other,
-  // which it clears before its first barrier (every thread read it two barriers ago)
+  // rounds: a round colours every constraint that heads the priority lists of all its
+  // non-static bodies (at least the uncoloured one of lowest (priority, index)). The frontier of
+  // a round holds exactly those: at the start, the constraints that head all their lists; after
+  // a round, the new heads of the lists its constraints left, where they head all their lists
+  // (claimed once through their rdy byte: two lists may hand over the same constraint). Each
+  // constraint is looked at a bounded number of times, whatever the number of rounds. Frontier
+  // sizes alternate between two team counters: a round reads one and fills the other, which it
+  // clears before its first barrier (every thread read it two barriers ago).
   __shared__ int s_cnt_own[2];
   int* s_cnt = tm.lead(s_cnt_own);
   if (tid == 0) {
-    s_cnt[0] = n;
+    s_cnt[0] = 0;
     s_cnt[1] = 0;
   }
+  for (int k = tid; k < n; k += NT) m.rdy[k] = 0;
   tm.sync();
   int* wl = m.wl0;
   int* wn = m.wl1;
+  const int lane = threadIdx.x & 31;
+  const unsigned lt = (1u << lane) - 1u;
+  // pushes the flagged constraints of a warp onto frontier `dst` (team counter `ctr`)
+  auto push = [&](bool f, int k, int* dst, int* ctr) {
+    const unsigned bal = __ballot_sync(FULL_MASK, f);
+    int base = 0;
+    if (lane == 0 && bal) base = atomicAdd(ctr, __popc(bal));
+    base = __shfl_sync(FULL_MASK, base, 0);
+    if (f) dst[base + __popc(bal & lt)] = k;
+  };
+  auto heads_all = [&](int k, int2 b) {
+    return (b.x < 0 || m.list[m.head[b.x]] == k) && (b.y < 0 || m.list[m.head[b.y]] == k);
+  };
+  for (int i0 = 0; i0 < n; i0 += NT) {  // team-uniform trip counts: whole warps reach the ballots
+    const int k = i0 + tid;
+    push(k < n && heads_all(k, m.cb[k]), k, wl, &s_cnt[0]);
+  }
+  tm.sync();
+  int coloured = 0;
   bool done = (n == 0);
-  for (int round = 0; round <= n + 1 && !done; ++round) {
+  for (int round = 0; round <= n && !done; ++round) {
     const int cur = round & 1;
     const int cnt = *(volatile int*)&s_cnt[cur];
-    for (int i = tid; i < cnt; i += NT) {
-      int k = round == 0 ? i : wl[i];
-      int2 b = m.cb[k];
-      bool ok = (b.x < 0 || m.list[m.head[b.x]] == k) && (b.y < 0 || m.list[m.head[b.y]] == k);
-      m.rdy[k] = ok ? 1 : 0;
-    }
+    if (cnt == 0) break;  // every thread reads the same count
     if (round > 0 && tid == 0) s_cnt[cur ^ 1] = 0;
+    for (int i = tid; i < cnt; i += NT) {
+      const int k = wl[i];
+      const int2 b = m.cb[k];
+      const unsigned long long used = (b.x >= 0 ? m.mask[b.x] : 0ull) | (b.y >= 0 ? m.mask[b.y] : 0ull);
+      const unsigned long long freeBits = ~used & ((1ull << 63) - 1ull);
+      int c;
+      if (freeBits == 0ull || b.x == B2G_CB_SERIAL) {
+        c = 63;
+      } else {
+        c = __ffsll((long long)freeBits) - 1;
+        if (b.x >= 0) m.mask[b.x] |= 1ull << c;
+        if (b.y >= 0) m.mask[b.y] |= 1ull << c;
+      }
+      m.col[k] = (int8_t)c;
+      if (b.x >= 0) m.head[b.x] += 1;
+      if (b.y >= 0) m.head[b.y] += 1;
+    }
+    coloured += cnt;
     tm.sync();
-    for (int i0 = 0; i0 < cnt; i0 += NT) {  // team-uniform trip count: whole warps reach the ballot
-      int i = i0 + tid;
-      int k = -1;
-      bool keep = false;
+    for (int i0 = 0; i0 < cnt; i0 += NT) {
+      const int i = i0 + tid;
+      int cand[2] = {-1, -1};
       if (i < cnt) {
-        k = round == 0 ? i : wl[i];
-        if (m.rdy[k]) {
-          int2 b = m.cb[k];
-          unsigned long long used = (b.x >= 0 ? m.mask[b.x] : 0ull) | (b.y >= 0 ? m.mask[b.y] : 0ull);
-          unsigned long long freeBits = ~used & ((1ull << 63) - 1ull);
-          int c;
-          if (freeBits == 0ull || b.x == B2G_CB_SERIAL) {
-            c = 63;
-          } else {
-            c = __ffsll((long long)freeBits) - 1;
-            if (b.x >= 0) m.mask[b.x] |= 1ull << c;
-            if (b.y >= 0) m.mask[b.y] |= 1ull << c;
-          }
-          m.col[k] = (int8_t)c;
-          if (b.x >= 0) m.head[b.x] += 1;
-          if (b.y >= 0) m.head[b.y] += 1;
-        } else {
-          keep = true;
+        const int2 b = m.cb[wl[i]];
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+          const int bb = q ? b.y : b.x;
+          if (bb < 0) continue;
+          const int h = m.head[bb];
+          if (h >= m.cnt[bb]) continue;  // the list is done
+          const int k2 = m.list[h];
+          if (!heads_all(k2, m.cb[k2])) continue;
+          // claim k2: set its rdy byte through the aligned word that holds it
+          const uintptr_t addr = reinterpret_cast<uintptr_t>(&m.rdy[k2]);
+          const unsigned sh = (unsigned)(addr & 3u) * 8u;
+          const unsigned old = atomicOr(reinterpret_cast<unsigned*>(addr & ~(uintptr_t)3u), 1u << sh);
+          if (!((old >> sh) & 1u)) cand[q] = k2;
         }
       }
-      unsigned bal = __ballot_sync(FULL_MASK, keep);
-      int lane = threadIdx.x & 31;
-      int base = 0;
-      if (lane == 0 && bal) base = atomicAdd(&s_cnt[cur ^ 1], __popc(bal));
-      base = __shfl_sync(FULL_MASK, base, 0);
-      if (keep) wn[base + __popc(bal & ((1u << lane) - 1u))] = k;
+      push(cand[0] >= 0, cand[0], wn, &s_cnt[cur ^ 1]);
+      push(cand[1] >= 0, cand[1], wn, &s_cnt[cur ^ 1]);
     }
     tm.sync();
-    done = (*(volatile int*)&s_cnt[cur ^ 1] == 0);
     int* t = wl;
     wl = wn;
     wn = t;
   }
+  done = (coloured == n);
   if (!done && tid == 0) atomicOr(status, B2G_DEV_COLOR_ROUNDS);
   // bucket by colour: each CTA counts its constraints per colour; a colour's slots go to the CTAs
   // in rank order (the order inside a colour does not matter), so CTA r places its constraints of
@@ -892,6 +942,7 @@ __device__ __forceinline__ void setup_world(Team& tm, const KernelArgs& a, int w
         const int ia = a.fbody[f.x], ib = a.fbody[f.y];
         a.scb[s] = make_int2((ia - b0) | (a.btype[ia] == B2G_STATIC ? (int)0x80000000 : 0),
                              (ib - b0) | (a.btype[ib] == B2G_STATIC ? (int)0x80000000 : 0));
+        a.srad[s] = make_float2(a.frad[f.x], a.frad[f.y]);
         const uint64_t key = a.ckey[c0 + k];
         a.cprio[s] = contactPriority((uint32_t)(key >> 32) - (uint32_t)fo, (uint32_t)key - (uint32_t)fo);
       });
@@ -974,13 +1025,13 @@ __device__ __forceinline__ void setup_world(Team& tm, const KernelArgs& a, int w
     int ci = a.sc_list[c0 + k];
     int p = a.cslot[c0 + k];
     int2 lb = a.scb[c0 + k];
+    const float2 rad = a.srad[c0 + k];
     int la = lb.x & 0x7fffffff, lbb = lb.y & 0x7fffffff;
     int ia = b0 + la, ib = b0 + lbb;
-    int2 f = a.cfix[ci];
     b2g_manifold m = ld_manifold(&a.cman[ci]);
     VCDev vc;
     for (int q = 0; q < 4; ++q) vc.K[q] = vc.NM[q] = 0.0f;
-    prepareContact(vc, m, a.cmat[ci], a.frad[f.x], a.frad[f.y], la, lbb, a.massd[ia], a.massd[ib], a.lc[ia], a.lc[ib],
+    prepareContact(vc, m, a.cmat[ci], rad.x, rad.y, la, lbb, a.massd[ia], a.massd[ib], a.lc[ia], a.lc[ib],
                    a.pos[ia], bs[la], a.pos[ib], bs[lbb], dtRatio, warm, ci);
     store_planes(P, c0 + p, vc);
   }
