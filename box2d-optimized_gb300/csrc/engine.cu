@@ -154,7 +154,7 @@ static KernelArgs make_args(Batch* b) {
     a.cmatB[k] = b->cmat[k].p; a.cmanB[k] = b->cman[k].p;
   }
   a.wbounds = b->wbounds.p; a.mkey = b->mkey.p; a.mkey_sorted = b->mkey_sorted.p; a.mval = b->mval.p;
-  a.mval_sorted = b->mval_sorted.p; a.nchild = b->nchild.p; a.nparent = b->nparent.p; a.lparent = b->lparent.p;
+  a.mval_sorted = b->mval_sorted.p; a.nchild = b->nchild.p; a.nrange = b->nrange.p; a.nparent = b->nparent.p; a.lparent = b->lparent.p;
   a.naabb = b->naabb.p; a.nrec = b->nrec.p; a.nhi = b->nhi.p; a.laabb = b->laabb.p; a.lattr = b->lattr.p; a.fattr = b->fattr.p; a.nflag = b->nflag.p; a.wroot = b->wroot.p; a.pcount = b->pcount.p; a.pslots = b->pslots.p; a.poff = b->poffB[b->cur ^ 1].p; a.poff_old = nullptr;
   a.pairs = b->pairs.p; a.cub_tmp = b->cub_tmp.p;
   a.sc_list = b->sc_list.p; a.scb = b->scb.p; a.srad = b->srad.p; a.cslot = b->cslot.p; a.ccol = b->ccol.p; a.corder = b->corder.p; a.cprio = b->cprio.p;
@@ -434,7 +434,7 @@ int upload_all(Batch* b) {
   TRY(upload(b, b->cmat[0], cmat)); TRY(upload(b, b->cman[0], cman));
   // per-body and per-fixture scratch
   TRY(ensure(b, b->mkey, NF)); TRY(ensure(b, b->mkey_sorted, NF)); TRY(ensure(b, b->mval, NF));
-  TRY(ensure(b, b->mval_sorted, NF)); TRY(ensure(b, b->nchild, NF)); TRY(ensure(b, b->nparent, NF));
+  TRY(ensure(b, b->mval_sorted, NF)); TRY(ensure(b, b->nchild, NF)); TRY(ensure(b, b->nrange, NF)); TRY(ensure(b, b->nparent, NF));
   TRY(ensure(b, b->lparent, NF)); TRY(ensure(b, b->naabb, NF)); TRY(ensure(b, b->nflag, NF));
   TRY(ensure(b, b->nrec, 3 * (size_t)NF)); TRY(ensure(b, b->nhi, NF)); TRY(ensure(b, b->laabb, NF)); TRY(ensure(b, b->lattr, NF)); TRY(ensure(b, b->fattr, NF));
   TRY(ensure(b, b->pcount, (size_t)NF + 1)); TRY(ensure(b, b->pslots, 8 * (size_t)NF));
@@ -658,7 +658,7 @@ static int flush_tail(Batch* b, TailPack& P) {
   TRY(ensure(b, b->bwake, NB, true)); TRY(ensure(b, b->sl, NB));  // wake marks are zero between steps
   if (b->bwake.cap > (size_t)NB0) CUDA_TRY(b, cudaMemsetAsync(b->bwake.p + NB0, 0, b->bwake.cap - NB0, b->stream));
   TRY(ensure(b, b->aabb, NF)); TRY(ensure(b, b->mkey, NF)); TRY(ensure(b, b->mkey_sorted, NF));
-  TRY(ensure(b, b->mval, NF)); TRY(ensure(b, b->mval_sorted, NF, true)); TRY(ensure(b, b->nchild, NF, true));
+  TRY(ensure(b, b->mval, NF)); TRY(ensure(b, b->mval_sorted, NF, true)); TRY(ensure(b, b->nchild, NF, true)); TRY(ensure(b, b->nrange, NF, true));
   TRY(ensure(b, b->nparent, NF, true)); TRY(ensure(b, b->lparent, NF, true)); TRY(ensure(b, b->naabb, NF));
   TRY(ensure(b, b->nrec, 3 * (size_t)NF)); TRY(ensure(b, b->nhi, NF)); TRY(ensure(b, b->laabb, NF)); TRY(ensure(b, b->lattr, NF, true));
   TRY(ensure(b, b->fattr, NF, true));  // kept trees keep their leaf attributes (a refit does not rewrite them)
@@ -1377,7 +1377,7 @@ B2G_API int b2g_batch_destroy(b2g_batch* b) {
     release(b, b->cman[k]);
   }
   release(b, b->wbounds); release(b, b->mkey); release(b, b->mkey_sorted); release(b, b->mval);
-  release(b, b->mval_sorted); release(b, b->nchild); release(b, b->nparent); release(b, b->lparent);
+  release(b, b->mval_sorted); release(b, b->nchild); release(b, b->nrange); release(b, b->nparent); release(b, b->lparent);
   release(b, b->naabb); release(b, b->nrec); release(b, b->nhi); release(b, b->laabb); release(b, b->lattr); release(b, b->fattr); release(b, b->nflag); release(b, b->wroot); release(b, b->pcount); release(b, b->pslots); release(b, b->poffB[0]); release(b, b->poffB[1]); release(b, b->pairs);
   release(b, b->cub_tmp); release(b, b->status); release(b, b->counters); release(b, b->sc_list); release(b, b->scb); release(b, b->srad); release(b, b->cslot); release(b, b->frad);
   release(b, b->ccol); release(b, b->corder); release(b, b->cprio); release(b, b->cready); release(b, b->inc_cnt);

@@ -252,6 +252,7 @@ struct Batch {
   DBuf<uint64_t> mkey, mkey_sorted;
   DBuf<int> mval, mval_sorted;
   DBuf<int2> nchild;              // internal node children (leaf = index | 0x80000000)
+  DBuf<int2> nrange;              // internal node leaf ranges (first, last sorted leaf)
   DBuf<int> nparent, lparent;     // parents of internal nodes and leaves
   DBuf<float4> naabb, nrec, laabb;  // node boxes, node records (3 per node), sorted leaf boxes
   DBuf<int> nhi;                  // node metas (last leaf of the range | static bit)

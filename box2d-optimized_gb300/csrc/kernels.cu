@@ -296,6 +296,7 @@ __global__ void k_lbvh_internal(KernelArgs a, int n) {
   int left = (lo == gamma) ? (int)(gg | LEAF_BIT) : gg;
   int right = (hi == gamma + 1) ? (int)((gg + 1) | LEAF_BIT) : gg + 1;
   a.nchild[gi] = make_int2(left, right);
+  a.nrange[gi] = make_int2(f0 + lo, f0 + hi);
   if (lo == gamma) a.lparent[gg] = gi; else a.nparent[gg] = gi;
   if (hi == gamma + 1) a.lparent[gg + 1] = gi; else a.nparent[gg + 1] = gi;
   int w = (int)(k[lo] >> 32);
@@ -379,16 +380,22 @@ __device__ __forceinline__ void lbvh_combine(const KernelArgs& a, int p, int2 ch
 
 // Bottom-up node bounds over the forest: a thread per leaf climbs towards its world's root and
 // the second thread to reach a node combines its children (lbvh_combine). Walks stop at their
-// world's root (the traversal never reads nodes above it). The arrival counter is a device-scope
-// acquire-release atomic: the first thread's child bounds and meta are visible to the second. A
-// node's links are read before its arrival (they do not change during the pass). Launched in
-// blocks of kBoundsThreads: a block's slot frees when its longest climb ends, so small blocks
-// keep the SMs filled while a few climbs go on towards the roots.
-constexpr int kBoundsThreads = 64;
+// world's root (the traversal never reads nodes above it). A block's leaves are a contiguous
+// range of the sorted leaves, so the nodes whose leaf range lies inside it are reached only by
+// its own threads: their arrival counters are block-scope acquire-release atomics in shared
+// memory (fast, and the block's threads see each other's node boxes); the nodes above them have
+// device-scope counters (nflag), through which the first arrival's child bounds and meta become
+// visible to the second. A node's links and range are read before its arrival (they do not
+// change during the pass).
+constexpr int kBoundsThreads = 256;
 __global__ void __launch_bounds__(kBoundsThreads) k_lbvh_bounds(KernelArgs a, int n) {
-  int idx = blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= n) return;
-  int i = a.bp_f0 + idx;
+  __shared__ int arrivals[kBoundsThreads];
+  const int B0 = a.bp_f0 + (int)blockIdx.x * kBoundsThreads;
+  const int B1 = min(B0 + kBoundsThreads, a.bp_f0 + n);
+  arrivals[threadIdx.x] = 0;
+  __syncthreads();
+  const int i = B0 + (int)threadIdx.x;
+  if (i >= B1) return;
   const int w = a.fworld[a.mval_sorted[i]];
   const int root = a.wroot[w];
   if (root < 0 || (root & LEAF_BIT)) return;  // single-fixture world: the leaf is the root
@@ -401,8 +408,16 @@ __global__ void __launch_bounds__(kBoundsThreads) k_lbvh_bounds(KernelArgs a, in
     }
     const int2 ch = a.nchild[p];
     const int pp = a.nparent[p];
-    cuda::atomic_ref<int, cuda::thread_scope_device> arrivals(a.nflag[p]);
-    if (arrivals.fetch_add(1, cuda::memory_order_acq_rel) == 0) return;
+    const int2 rg = a.nrange[p];
+    bool second;
+    if (rg.x >= B0 && rg.y < B1) {  // p's index is one end of its range, so p - B0 is in the block
+      cuda::atomic_ref<int, cuda::thread_scope_block> arrived(arrivals[p - B0]);
+      second = arrived.fetch_add(1, cuda::memory_order_acq_rel) != 0;
+    } else {
+      cuda::atomic_ref<int, cuda::thread_scope_device> arrived(a.nflag[p]);
+      second = arrived.fetch_add(1, cuda::memory_order_acq_rel) != 0;
+    }
+    if (!second) return;
     lbvh_combine(a, p, ch);
     if (p == root) return;
     p = pp;

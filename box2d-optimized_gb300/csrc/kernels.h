@@ -85,6 +85,7 @@ struct KernelArgs {
   uint64_t *mkey, *mkey_sorted;
   int *mval, *mval_sorted;
   int2* nchild;
+  int2* nrange;                   // per internal node: its first and last sorted leaf
   int *nparent, *lparent;
   float4* naabb;
   float4* nrec;                   // per internal node, 3 x 16 B: left child box, right child box,
