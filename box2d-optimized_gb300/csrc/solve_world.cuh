@@ -540,27 +540,6 @@ __device__ __forceinline__ void hint_vel(const SolverPlanes& P, int s) {
   prefetch_l1(P.imp + s);
 }
 
-// L1 prefetch of the rows of this thread's first joint of colour c + 1, before the barrier that
-// ends colour c: the velocity rows 0-8, or the position pass's rows 0-1 and 9-12 (no registers
-// held; the rows of colour c + 1 are not written while colour c is solved).
-template <bool POS>
-__device__ __forceinline__ void hint_next_joint(const KernelArgs& a, const int* jranges, int njc, int c, int j0,
-                                                int tid) {
-  if (c + 1 >= njc || c + 1 == 63) return;
-  const int slot = jranges[c + 1] + tid;
-  if (slot >= jranges[c + 2]) return;
-  const float4* r = a.jplanes + j0 + slot;
-  if (!POS) {
-#pragma unroll
-    for (int k = 0; k < 9; ++k) prefetch_l1(r + (int64_t)k * a.jstride);
-  } else {
-    prefetch_l1(r);
-    prefetch_l1(r + a.jstride);
-#pragma unroll
-    for (int k = 9; k < 13; ++k) prefetch_l1(r + (int64_t)k * a.jstride);
-  }
-}
-
 __device__ __forceinline__ void fetch_pos(const SolverPlanes& P, int s, PosRows& r) {
   r.id = P.idx[s];
   r.lcs = P.lcs[s];
@@ -1056,23 +1035,6 @@ __device__ __forceinline__ void setup_world(Team& tm, const KernelArgs& a, int w
                    a.pos[ia], bs[la], a.pos[ib], bs[lbb], dtRatio, warm, ci);
     store_planes(P, c0 + p, vc);
   }
-
-  // 5a. the joints' InitVelocityConstraints without the warm start (which the iterations apply
-  //     colour by colour, after the contacts' warm start): step temporaries and scaled impulses
-  //     into each joint's colour-ordered rows. Gears are initialised in the serial colour of the
-  //     iterations, on their records.
-  for (int i = tid; i < nj; i += NT) {
-    const JointDev& J = a.joints[j0 + a.jorder[j0 + i]];
-    if (sleepMode && !joint_awake(a, J)) {
-      jointPackAsleep(a.jplanes, j0 + i);
-      continue;
-    }
-    if (J.d.type == B2G_JOINT_GEAR) {
-      jointPackGear(a.jplanes, j0 + i, J.d.body_a, J.d.body_b);
-      continue;
-    }
-    jointInitSlot<false>(J, a.jplanes, a.jstride, j0 + i, a.massd, a.lc, a.pos, nullptr, a.dt, dtRatio, warm);
-  }
 }
 
 // The second half of the island solve of world w by team tm, after setup_world: warm start,
@@ -1126,8 +1088,7 @@ __device__ __forceinline__ void iterate_world(Team& tm, const KernelArgs& a, int
   tm.sync();
   float4* jb = bs - b0;  // joints address bodies by global index
 
-  // 5. warm start contacts, then the joints' warm start (their init ran in the setup), colour by
-  //    colour
+  // 5. warm start contacts, then joint InitVelocityConstraints, colour by colour
   auto fetchV = [&](int slot, VelRows& r) { fetch_vel(P, slot, r); };
   auto fetchP = [&](int slot, PosRows& r) { fetch_pos(P, slot, r); };
   auto hintV = [&](int slot) { hint_vel(P, slot); };
@@ -1144,15 +1105,18 @@ __device__ __forceinline__ void iterate_world(Team& tm, const KernelArgs& a, int
     const int step = c == 63 ? 1 : NT, i0 = c == 63 ? s : s + tid;
     if (c != 63 || tid == 0)
       for (int i = i0; i < e; i += step) {
-        if (c == 63 && jointSlotIsGear(a.jplanes, j0 + i)) {  // gears are coloured 63: one thread, on the record
-          JointDev& J = a.joints[j0 + a.jorder[j0 + i]];
+        JointDev& J = a.joints[j0 + a.jorder[j0 + i]];
+        if (sleepMode && !joint_awake(a, J)) {
+          jointPackAsleep(a.jplanes, j0 + i);
+          continue;
+        }
+        if (c == 63 && J.d.type == B2G_JOINT_GEAR) {  // gears are coloured 63: one thread, on the record
           gearInit(J, a.massd, a.lc, a.pos, jb, warm);
           jointPackGear(a.jplanes, j0 + i, J.d.body_a, J.d.body_b);
           continue;
         }
-        jointWarmStartSlot(a.jplanes, a.jstride, j0 + i, jb, warm);  // nothing for a sleeping joint
+        jointInitSlot(J, a.jplanes, a.jstride, j0 + i, a.massd, a.lc, a.pos, jb, a.dt, dtRatio, warm);
       }
-    if (PREFETCH) hint_next_joint<false>(a, jranges, njc, c, j0, tid);
     tm.sync();
   }
 
@@ -1168,7 +1132,6 @@ __device__ __forceinline__ void iterate_world(Team& tm, const KernelArgs& a, int
           if (c == 63 && jointSlotIsGear(a.jplanes, j0 + i)) gearSolveVelocity(a.joints[j0 + a.jorder[j0 + i]], jb);
           else jointSolveVelocitySlot(a.jplanes, a.jstride, j0 + i, jb, a.dt, a.inv_dt);
         }
-      if (PREFETCH) hint_next_joint<false>(a, jranges, njc, c, j0, tid);
       tm.sync();
     }
     colour_sweep<Team, VelRows, PREFETCH, 2>(tm, cranges, ncc, c0, fetchV, [&](int slot, const VelRows& r) {
@@ -1262,7 +1225,6 @@ __device__ __forceinline__ void iterate_world(Team& tm, const KernelArgs& a, int
             if (sleepMode) isl_store<S>(&SL[root].z, it + 1);
           }
         }
-      if (PREFETCH) hint_next_joint<true>(a, jranges, njc, c, j0, tid);
       tm.sync();
     }
     if (sleepMode) {

@@ -417,9 +417,6 @@ B2G_HD void solveLinearAngular(JointDev& J, V2& vA, float& wA, V2& vB, float& wB
 }
 
 // InitVelocityConstraints (revolute :73-165, prismatic :114-224, distance :76-173).
-// With VEL clear the init computes the joint's step temporaries and scaled impulses only, leaving
-// the bodies' velocities alone; jointWarmStart applies what the init would have applied to them.
-template <bool VEL = true>
 B2G_HD void jointInit(JointDev& J, const float4* massd, const float2* lc, const float4* pos, float4* vel, float dt,
                       float dtRatio, bool warm) {
   int ia = J.d.body_a, ib = J.d.body_b;
@@ -428,14 +425,9 @@ B2G_HD void jointInit(JointDev& J, const float4* massd, const float2* lc, const 
   J.lcA[0] = la2.x; J.lcA[1] = la2.y; J.lcB[0] = lb2.x; J.lcB[1] = lb2.y;
   float4 mdA = massd[ia], mdB = massd[ib];
   J.mA = mdA.y; J.mB = mdB.y; J.invIA = mdA.w; J.invIB = mdB.w;
-  V2 cA, cB, vA = mk(0.0f, 0.0f), vB = mk(0.0f, 0.0f);
-  float aA, aB, wA = 0.0f, wB = 0.0f;
-  loadPos(pos, ia, cA, aA);
-  loadPos(pos, ib, cB, aB);
-  if (VEL) {
-    loadVel(vel, ia, vA, wA);
-    loadVel(vel, ib, vB, wB);
-  }
+  V2 cA, cB, vA, vB; float aA, aB, wA, wB;
+  loadPos(pos, ia, cA, aA); loadVel(vel, ia, vA, wA);
+  loadPos(pos, ib, cB, aB); loadVel(vel, ib, vB, wB);
   Rot qA = rotOf(aA), qB = rotOf(aB);
   V2 la = ld2(J.d.local_anchor_a), lb = ld2(J.d.local_anchor_b);
   V2 lcA = ld2(J.lcA), lcB = ld2(J.lcB);
@@ -733,87 +725,8 @@ B2G_HD void jointInit(JointDev& J, const float4* massd, const float2* lc, const 
       J.impulse[0] = 0.0f;
     }
   }
-  if (VEL && moves(mA, iA)) storeVel(vel, ia, vA, wA);
-  if (VEL && moves(mB, iB)) storeVel(vel, ib, vB, wB);
-}
-
-// The velocity part of jointInit for a joint whose init ran with VEL clear (J holds its step
-// temporaries and scaled impulses): the warm start, and the mouse joint's angular damping of
-// body B, as the same operations on the same values, so that the velocities come out bit for bit
-// as from jointInit.
-B2G_HD void jointWarmStart(const JointDev& J, float4* vel, bool warm) {
-  V2 vA, vB;
-  float wA, wB;
-  loadVel(vel, J.iA, vA, wA);
-  loadVel(vel, J.iB, vB, wB);
-  const float mA = J.mA, mB = J.mB, iA = J.invIA, iB = J.invIB;
-  const V2 rA = ld2(J.rA), rB = ld2(J.rB);
-  if (J.d.type == B2G_JOINT_REVOLUTE) {
-    if (warm) {
-      float axialImpulse = J.motorImpulse + J.lowerImpulse - J.upperImpulse;
-      V2 P = mk(J.impulse[0], J.impulse[1]);
-      subFrom(vA, mA * P);
-      wA -= iA * (cross(rA, P) + axialImpulse);
-      addTo(vB, mB * P);
-      wB += iB * (cross(rB, P) + axialImpulse);
-    }
-  } else if (J.d.type == B2G_JOINT_PRISMATIC) {
-    if (warm) {
-      float axialImpulse = J.motorImpulse + J.lowerImpulse - J.upperImpulse;
-      V2 P = J.impulse[0] * ld2(J.perp) + axialImpulse * ld2(J.axis);
-      float LA = J.impulse[0] * J.s1 + J.impulse[1] + axialImpulse * J.a1;
-      float LB = J.impulse[0] * J.s2 + J.impulse[1] + axialImpulse * J.a2;
-      subFrom(vA, mA * P);
-      wA -= iA * LA;
-      addTo(vB, mB * P);
-      wB += iB * LB;
-    }
-  } else if (J.d.type == B2G_JOINT_DISTANCE) {
-    if (warm) {
-      V2 P = ((J.impulse[0] + J.lowerImpulse) - J.upperImpulse) * ld2(J.u);
-      subFrom(vA, J.mA * P);
-      wA -= J.invIA * cross(rA, P);
-      addTo(vB, J.mB * P);
-      wB += J.invIB * cross(rB, P);
-    }
-  } else if (J.d.type == B2G_JOINT_WELD || J.d.type == B2G_JOINT_MOTOR || J.d.type == B2G_JOINT_FRICTION) {
-    if (warm) {
-      V2 P = mk(J.impulse[0], J.impulse[1]);
-      subFrom(vA, mA * P);
-      wA -= iA * (cross(rA, P) + J.impulse[2]);
-      addTo(vB, mB * P);
-      wB += iB * (cross(rB, P) + J.impulse[2]);
-    }
-  } else if (J.d.type == B2G_JOINT_WHEEL) {
-    if (warm) {
-      float axialImpulse = J.impulse[1] + J.lowerImpulse - J.upperImpulse;
-      V2 P = J.impulse[0] * ld2(J.perp) + axialImpulse * ld2(J.axis);
-      float LA = J.impulse[0] * J.s1 + axialImpulse * J.a1 + J.motorImpulse;
-      float LB = J.impulse[0] * J.s2 + axialImpulse * J.a2 + J.motorImpulse;
-      subFrom(vA, mA * P);
-      wA -= iA * LA;
-      addTo(vB, mB * P);
-      wB += iB * LB;
-    }
-  } else if (J.d.type == B2G_JOINT_MOUSE) {
-    wB *= 0.98f;
-    if (warm) {
-      V2 P = mk(J.impulse[0], J.impulse[1]);
-      addTo(vB, mB * P);
-      wB += iB * cross(rB, P);
-    }
-  } else {  // pulley
-    if (warm) {
-      V2 PA = -(J.impulse[0]) * ld2(J.u);
-      V2 PB = (-J.d.ratio * J.impulse[0]) * ld2(J.uB);
-      addTo(vA, mA * PA);
-      wA += iA * cross(rA, PA);
-      addTo(vB, mB * PB);
-      wB += iB * cross(rB, PB);
-    }
-  }
-  if (moves(mA, iA)) storeVel(vel, J.iA, vA, wA);
-  if (moves(mB, iB)) storeVel(vel, J.iB, vB, wB);
+  if (moves(mA, iA)) storeVel(vel, ia, vA, wA);
+  if (moves(mB, iB)) storeVel(vel, ib, vB, wB);
 }
 
 // SolveVelocityConstraints (revolute :167-243, prismatic :226-330, distance :175-266).
@@ -1605,8 +1518,6 @@ __device__ __forceinline__ bool gearSolvePosition(JointDev& J, float4* pos) {
   return true;
 }
 
-// With VEL clear the bodies' velocities are left alone (jointWarmStartSlot applies the warm start).
-template <bool VEL = true>
 __device__ __forceinline__ void jointInitSlot(const JointDev& G, float4* P, int stride, int slot, const float4* massd,
                                               const float2* lc, const float4* pos, float4* vel, float dt, float dtRatio,
                                               bool warm) {
@@ -1623,7 +1534,7 @@ __device__ __forceinline__ void jointInitSlot(const JointDev& G, float4* P, int 
   J.localXAxisA[0] = G.localXAxisA[0]; J.localXAxisA[1] = G.localXAxisA[1];                      \
   J.localYAxisA[0] = G.localYAxisA[0]; J.localYAxisA[1] = G.localYAxisA[1]
 #define B2G_JI_FINISH                                                                            \
-  jointInit<VEL>(J, massd, lc, pos, vel, dt, dtRatio, warm);                                     \
+  jointInit(J, massd, lc, pos, vel, dt, dtRatio, warm);                                          \
   jointPackVel(J, P, stride, slot);                                                              \
   jointPackPos(J, P, stride, slot)
   switch (G.d.type) {
@@ -1867,34 +1778,6 @@ __device__ __forceinline__ void jointStoreImpulses(const float4* P, int stride, 
     const float4 r3 = P[(int64_t)3 * stride + slot];
     J.u[0] = r3.x; J.u[1] = r3.y; J.uB[0] = r3.z; J.uB[1] = r3.w;
   }
-}
-
-// The warm start of the joint in `slot` (jointWarmStart) from the rows its init packed with VEL
-// clear: a register copy of the fields the warm start reads.
-__device__ __forceinline__ void jointWarmStartSlot(const float4* P, int stride, int slot, float4* vel, bool warm) {
-  const float4 r0 = P[slot];
-  if (__float_as_int(r0.w) & B2G_JV_ASLEEP) return;
-  const float4 r1 = P[(int64_t)stride + slot], r2 = P[(int64_t)2 * stride + slot], r3 = P[(int64_t)3 * stride + slot];
-  const float4 r4 = P[(int64_t)4 * stride + slot], r7 = P[(int64_t)7 * stride + slot];
-  const float4 r8 = P[(int64_t)8 * stride + slot];
-  JointDev J;
-  J.iA = __float_as_int(r0.x);
-  J.iB = __float_as_int(r0.y);
-  J.d.type = __float_as_int(r0.z);
-  J.mA = r1.x; J.mB = r1.y; J.invIA = r1.z; J.invIB = r1.w;
-  J.impulse[0] = r7.x; J.impulse[1] = r7.y; J.impulse[2] = r7.z; J.motorImpulse = r7.w;
-  J.lowerImpulse = r8.x; J.upperImpulse = r8.y;
-  J.rA[0] = r2.x; J.rA[1] = r2.y; J.rB[0] = r2.z; J.rB[1] = r2.w;
-  if (J.d.type == B2G_JOINT_PRISMATIC || J.d.type == B2G_JOINT_WHEEL) {
-    J.axis[0] = r2.x; J.axis[1] = r2.y; J.perp[0] = r2.z; J.perp[1] = r2.w;
-    J.a1 = r3.x; J.a2 = r3.y; J.s1 = r3.z; J.s2 = r3.w;
-  } else if (J.d.type == B2G_JOINT_DISTANCE) {
-    J.u[0] = r3.x; J.u[1] = r3.y;
-  } else if (J.d.type == B2G_JOINT_PULLEY) {
-    J.u[0] = r3.x; J.u[1] = r3.y; J.uB[0] = r3.z; J.uB[1] = r3.w;
-    J.d.ratio = r4.y;
-  }
-  jointWarmStart(J, vel, warm);
 }
 #endif
 
