@@ -243,7 +243,7 @@ class Lib:
         "b2g_bodies_sleep_time_read", "b2g_world_get_flags", "b2g_server_batch", "b2g_step_begin",
         "b2g_step_poll", "b2g_step_end", "b2g_batch_stage", "b2g_server_set_builders", "b2g_batch_set_solver_waves", "b2g_batch_set_tree_rebuild_period",
         "b2g_batch_set_cluster_solve", "b2g_batch_get_cluster_solve", "b2g_events_drain_world",
-        "b2g_bodies_remove", "b2g_fixtures_remove", "b2g_joints_remove", "b2g_world_dump",
+        "b2g_bodies_remove", "b2g_fixtures_remove", "b2g_joints_remove", "b2g_world_dump", "b2g_step_io",
     ]
 
     def __init__(self, path: os.PathLike | str | None = None):
@@ -271,6 +271,7 @@ class Lib:
             "b2g_step_n": ([vp, f32, i32, i32, i32, i32], C.c_int),
             "b2g_step_timed": ([vp, f32, i32, i32, i32, P(f32)], C.c_int),
             "b2g_batch_set_forces": ([vp, vp, i64], C.c_int),
+            "b2g_step_io": ([vp, f32, i32, i32, vp, i64, vp, i64, P(i64)], C.c_int),
             "b2g_batch_set_graphs": ([vp, i32], C.c_int),
             "b2g_world_retire": ([vp, i32], C.c_int),
             "b2g_compact": ([vp, P(i32), i32], C.c_int),
@@ -468,6 +469,15 @@ class Batch:
         arr = (C.c_float * max(nb, 1))()
         self.lib.check(self.lib.b2g_bodies_sleep_time_read(self.h, world, 0, nb, arr), "b2g_bodies_sleep_time_read")
         return list(arr[:nb])
+
+    def step_io(self, forces_ptr, n_bodies, xf_ptr, cap_bodies, dt=1 / 60, vi=8, pi=3) -> int:
+        """One step with its host I/O (b2g_step_io): the forces of every body from host address
+        `forces_ptr` (0: the forces already set), the transforms to host address `xf_ptr` (0:
+        none). Returns the number of bodies."""
+        n = C.c_int64()
+        self.lib.check(self.lib.b2g_step_io(self.h, dt, vi, pi, C.c_void_p(forces_ptr or None), n_bodies,
+                                            C.c_void_p(xf_ptr or None), cap_bodies, C.byref(n)), "b2g_step_io")
+        return n.value
 
     def set_graphs(self, enable=True):
         """Whether unmasked steps replay a captured CUDA graph (default on)."""

@@ -442,7 +442,7 @@ int upload_all(Batch* b) {
   b->poff_valid[0] = b->poff_valid[1] = false;
   TRY(ensure(b, b->cub_tmp, cub_temp_bytes(NF)));
   TRY(ensure(b, b->inc_cnt, NB)); TRY(ensure(b, b->inc_head, NB)); TRY(ensure(b, b->inc_mask, NB));
-  TRY(ensure(b, b->jinc_list, 2 * (size_t)NJ)); TRY(ensure(b, b->jwork, 2 * (size_t)NJ)); TRY(ensure(b, b->jcol, NJ)); TRY(ensure(b, b->jorder, NJ));
+  TRY(ensure(b, b->jinc_list, 2 * (size_t)NJ)); TRY(ensure(b, b->jwork, 4 * (size_t)NJ)); TRY(ensure(b, b->jcol, NJ)); TRY(ensure(b, b->jorder, NJ));
   TRY(ensure(b, b->jcb, NJ)); TRY(ensure(b, b->jprio, NJ)); TRY(ensure(b, b->jready, NJ));
   TRY(ensure(b, b->jplanes, (size_t)B2G_JV_ROWS * NJ));
   TRY(ensure(b, b->status, 1)); TRY(ensure(b, b->counters, 5));
@@ -669,7 +669,7 @@ static int flush_tail(Batch* b, TailPack& P) {
   TRY(ensure(b, b->pslots, 8 * (size_t)NF));
   TRY(ensure(b, b->cub_tmp, cub_temp_bytes(NF)));
   TRY(ensure(b, b->inc_cnt, NB)); TRY(ensure(b, b->inc_head, NB)); TRY(ensure(b, b->inc_mask, NB));
-  TRY(ensure(b, b->jinc_list, 2 * (size_t)NJ)); TRY(ensure(b, b->jwork, 2 * (size_t)NJ)); TRY(ensure(b, b->jcol, NJ, true)); TRY(ensure(b, b->jorder, NJ, true));
+  TRY(ensure(b, b->jinc_list, 2 * (size_t)NJ)); TRY(ensure(b, b->jwork, 4 * (size_t)NJ)); TRY(ensure(b, b->jcol, NJ, true)); TRY(ensure(b, b->jorder, NJ, true));
   TRY(ensure(b, b->jcb, NJ, true)); TRY(ensure(b, b->jprio, NJ, true)); TRY(ensure(b, b->jready, NJ));
   TRY(ensure(b, b->jplanes, (size_t)B2G_JV_ROWS * NJ));
   b->NW = NW; b->NB = NB; b->NF = NF; b->NJ = NJ;
@@ -818,7 +818,7 @@ static int ensure_contact_capacity(Batch* b, int64_t want) {
   TRY(ensure(b, b->pairs, (size_t)cap));
   TRY(ensure(b, b->sc_list, (size_t)cap)); TRY(ensure(b, b->scb, (size_t)cap)); TRY(ensure(b, b->srad, (size_t)cap)); TRY(ensure(b, b->cslot, (size_t)cap)); TRY(ensure(b, b->ccol, (size_t)cap));
   TRY(ensure(b, b->corder, (size_t)cap)); TRY(ensure(b, b->cprio, (size_t)cap)); TRY(ensure(b, b->cready, (size_t)cap));
-  TRY(ensure(b, b->inc_list, 2 * (size_t)cap)); TRY(ensure(b, b->cwork, 2 * (size_t)cap));
+  TRY(ensure(b, b->inc_list, 2 * (size_t)cap)); TRY(ensure(b, b->cwork, 4 * (size_t)cap));
   TRY(ensure(b, b->sp_nf, (size_t)cap)); TRY(ensure(b, b->sp_cid, (size_t)cap)); TRY(ensure(b, b->sp_r0, (size_t)cap));
   TRY(ensure(b, b->sp_r1, (size_t)cap)); TRY(ensure(b, b->sp_nmtm, (size_t)cap)); TRY(ensure(b, b->sp_bk, (size_t)cap));
   TRY(ensure(b, b->sp_kn, (size_t)cap)); TRY(ensure(b, b->sp_imp, (size_t)cap)); TRY(ensure(b, b->sp_idx, (size_t)cap));
@@ -914,8 +914,12 @@ static void enqueue_step(Batch* b, float dt, int vi, int pi, bool initial_bp, in
   launch_collide(a, b->NW, b->stream);
   if (record_profile) cudaEventRecord(b->ev[1], b->stream);
   if (dt > 0.0f) {
+    // the forces' copy of b2g_step_io (an event recorded outside the graph when captured)
+    const bool captured = capture_mode >= 0;
+    cudaStreamWaitEvent(b->stream, b->io_in, captured ? cudaEventWaitExternal : 0);
     launch_solve(a, b->solve_classes, b->stream, b->side, b->fork_ev);
     if (b->debug_checks) launch_colour_check(a, b->NW, b->stream);
+    cudaEventRecordWithFlags(b->io_solved, b->stream, captured ? cudaEventRecordExternal : cudaEventRecordDefault);
     b->last_solve_buf = src;
     if (record_profile) cudaEventRecord(b->ev[2], b->stream);
     if (capture_mode >= 0) enqueue_broadphase(b, a, src, capture_mode, b->NF, b->NW);
@@ -1347,6 +1351,10 @@ B2G_API int b2g_batch_create(int device, uint64_t budget_bytes, b2g_batch** out)
     return B2G_E_CUDA;
   }
   for (int i = 0; i < 8; ++i) cudaEventCreate(&b->ev[i]);
+  cudaStreamCreateWithFlags(&b->io_stream, cudaStreamNonBlocking);
+  cudaEventCreateWithFlags(&b->io_in, cudaEventDisableTiming);
+  cudaEventCreateWithFlags(&b->io_solved, cudaEventDisableTiming);
+  cudaEventRecord(b->io_in, b->io_stream);  // complete: a step without b2g_step_io waits for nothing
   for (int i = 0; i < B2G_SOLVE_CLASSES; ++i) cudaStreamCreateWithFlags(&b->side[i], cudaStreamNonBlocking);
   for (int i = 0; i <= B2G_SOLVE_CLASSES; ++i) cudaEventCreateWithFlags(&b->fork_ev[i], cudaEventDisableTiming);
   solver_setup();
@@ -1404,6 +1412,9 @@ B2G_API int b2g_batch_destroy(b2g_batch* b) {
   if (b->fork_ev[B2G_SOLVE_CLASSES]) cudaEventDestroy(b->fork_ev[B2G_SOLVE_CLASSES]);
   for (int i = 0; i < 8; ++i)
     if (b->ev[i]) cudaEventDestroy(b->ev[i]);
+  if (b->io_in) cudaEventDestroy(b->io_in);
+  if (b->io_solved) cudaEventDestroy(b->io_solved);
+  if (b->io_stream) cudaStreamDestroy(b->io_stream);
   cudaStreamDestroy(b->stream);
   delete b;
   return B2G_OK;
@@ -2672,6 +2683,37 @@ B2G_API int b2g_batch_read_states(b2g_batch* b, float* xf4, float* v3, int64_t c
   }
   CUDA_TRY(b, cudaStreamSynchronize(b->stream));
   return B2G_OK;
+}
+
+B2G_API int b2g_step_io(b2g_batch* b, float dt, int32_t vi, int32_t pi, const float* f4, int64_t n_bodies,
+                        float* xf4_out, int64_t cap_bodies, int64_t* n_out) {
+  if (!b || b->device < 0 || (f4 && n_bodies < 0) || (xf4_out && cap_bodies < 0)) return B2G_E_INVALID_ARG;
+  if (b->in_step) return locked(b);
+  if (b->structure_dirty) TRY(upload_all(b));
+  if (f4 && n_bodies != b->NB) return B2G_E_INVALID_ARG;
+  cudaSetDevice(b->device);
+  if (f4 && n_bodies) {
+    // the previous step is complete (b2g_step_io and b2g_step return after it): nothing reads the
+    // forces while they are copied
+    CUDA_TRY(b, cudaMemcpyAsync(b->force.p, f4, n_bodies * sizeof(float4), cudaMemcpyHostToDevice, b->io_stream));
+    CUDA_TRY(b, cudaEventRecord(b->io_in, b->io_stream));
+    b->host_state_stale = true;
+  }
+  int st = step_begin(b, dt, vi, pi, nullptr);
+  if (st != B2G_OK) {
+    cudaStreamSynchronize(b->io_stream);
+    return st;
+  }
+  const int64_t n = std::min<int64_t>(cap_bodies, b->NB);
+  if (xf4_out && n > 0) {
+    // after the solve wrote the transforms; the closing broadphase only reads them
+    CUDA_TRY(b, cudaStreamWaitEvent(b->io_stream, b->io_solved, 0));
+    CUDA_TRY(b, cudaMemcpyAsync(xf4_out, b->xf.p, n * sizeof(float4), cudaMemcpyDeviceToHost, b->io_stream));
+  }
+  st = step_end(b);
+  CUDA_TRY(b, cudaStreamSynchronize(b->io_stream));
+  if (n_out) *n_out = b->NB;
+  return st;
 }
 
 B2G_API int b2g_fixtures_read(b2g_batch* b, int32_t world, int32_t first, int32_t n, b2g_fixture* out) {

@@ -286,7 +286,7 @@ struct Batch {
   DBuf<unsigned long long> inc_mask;
   DBuf<int> inc_list;             // 2 entries per constraint (contacts), world base 2*contact_off
   DBuf<int> jinc_list;            // 2 entries per joint
-  DBuf<int> cwork, jwork;         // colouring worklists, 2 entries per contact / joint
+  DBuf<int4> cwork, jwork;        // colouring list entries and frontiers, 4 per contact / joint
   DBuf<int2> jcb;
   DBuf<int8_t> jcol;
   DBuf<int> jorder, jranges;
@@ -323,6 +323,10 @@ struct Batch {
   // profile
   b2g_profile profile{};
   cudaEvent_t ev[8] = {};
+  // b2g_step_io: the host copies' stream; io_in is recorded after the forces' copy and waited for
+  // before the solve, io_solved is recorded after the solve and waited for by the transforms' copy
+  cudaStream_t io_stream = nullptr;
+  cudaEvent_t io_in = nullptr, io_solved = nullptr;
 
   // contact / pair buffer capacity and a version bumped whenever a kernel-visible buffer moves
   int64_t ccap = 0;

@@ -117,7 +117,7 @@ struct KernelArgs {
   int *inc_cnt, *inc_head;
   unsigned long long* inc_mask;
   int *inc_list, *jinc_list;
-  int *cwork, *jwork;             // colouring worklists: 2 per constraint (contacts, joints)
+  int4 *cwork, *jwork;            // colouring entries and frontiers: 4 per constraint (contacts, joints)
   int2* jcb;
   int8_t* jcol;
   int* jorder;

@@ -35,7 +35,7 @@ namespace {
 // Device bytes budgeted per body of an admitted world: body and fixture records, contact
 // buffers (about three contacts per body, both lists, pair list, solver scratch) and broadphase
 // scratch, rounded up.
-const uint64_t kBytesPerBody = 2048;
+const uint64_t kBytesPerBody = 2304;
 const int kDefaultBuilders = 2;
 
 double now_s() {

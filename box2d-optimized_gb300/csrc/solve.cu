@@ -53,8 +53,9 @@ __global__ void __launch_bounds__(T) k_joint_colour(KernelArgs a, int w0) {
   m.cb = a.jcb + j0;
   m.col = a.jcol + j0;
   m.rdy = a.jready + j0;
-  m.wl0 = a.jwork + 2 * (int64_t)j0;
-  m.wl1 = a.jwork + 2 * (int64_t)j0 + nj;
+  m.ent = a.jwork + 4 * (int64_t)j0;
+  m.wl0 = m.ent + 2 * (int64_t)nj;
+  m.wl1 = m.wl0 + nj;
   CtaTeam<T> tm;
   int njc = colour_constraints(tm, nj, nb, m, a.jprio + j0, a.jorder + j0, nullptr, jr, a.status);
   for (int c = threadIdx.x; c <= njc; c += T) a.jranges[65 * (int64_t)w + c] = jr[c];

@@ -220,9 +220,11 @@ struct ColourMem {
   int* list;                 // 2 per constraint: per-body incidence lists
   const int2* cb;            // per constraint: world-local bodies, negative (bit 31 set) = static
   int8_t* col;               // per constraint: colour, -1 until coloured
-  uint8_t* rdy;              // per constraint: ready in the current round
-  int* wl0;                  // worklists of uncoloured constraints (n entries each)
-  int* wl1;
+  uint8_t* rdy;              // per constraint: claimed for a round's frontier
+  int4* ent;                 // 2 per constraint, global: list entries {k, body x, body y, slot of
+                             // k in the list of its other body (-1: none)}
+  int4* wl0;                 // frontiers of entries (n each, global)
+  int4* wl1;
 };
 
 // Greedy colouring in priority order, computed in parallel rounds (Jones-Plassmann with
@@ -250,7 +252,7 @@ __device__ int colour_constraints(Team& tm, int n, int nb, const ColourMem m, co
     if (b.y >= 0) atomicAdd(&m.cnt[b.y], 1);
   }
   tm.sync();
-  block_exclusive_scan(tm, nb, [&](int i) { return m.cnt[i]; }, [&](int i, int p) { m.head[i] = p; });
+  const int nslots = block_exclusive_scan(tm, nb, [&](int i) { return m.cnt[i]; }, [&](int i, int p) { m.head[i] = p; });
   for (int i = tid; i < nb; i += NT) m.cnt[i] = 0;
   tm.sync();
   for (int k = tid; k < n; k += NT) {
@@ -299,6 +301,27 @@ __device__ int colour_constraints(Team& tm, int n, int nb, const ColourMem m, co
     }
     m.cnt[i] = off + cnt;
   }
+  // each list slot's entry: the constraint, its bodies and its slot in the list of its other
+  // body, so that one load of an entry tells whether its constraint heads both its lists. The
+  // constraints' slots per body go to the second frontier's space first (unused until a round).
+  // A thread per slot: the slot's body is the constraint's body whose list range holds it (the
+  // lists lie one after another in body order, heads still at their starts).
+  tm.sync();
+  int2* posk = reinterpret_cast<int2*>(m.wl1);
+  auto on_x = [&](int s2, int2 c) { return c.x >= 0 && s2 >= m.head[c.x] && s2 < m.cnt[c.x]; };
+  for (int s2 = tid; s2 < nslots; s2 += NT) {
+    const int k = m.list[s2];
+    if (on_x(s2, m.cb[k])) posk[k].x = s2;
+    else posk[k].y = s2;
+  }
+  tm.sync();
+  for (int s2 = tid; s2 < nslots; s2 += NT) {
+    const int k = m.list[s2];
+    const int2 c = m.cb[k];
+    const bool onX = on_x(s2, c);
+    const int other = onX ? c.y : c.x;
+    m.ent[s2] = make_int4(k, c.x, c.y, other < 0 ? -1 : (onX ? posk[k].y : posk[k].x));
+  }
   // rounds: a round colours every constraint that heads the priority lists of all its
   // non-static bodies (at least the uncoloured one of lowest (priority, index)). The frontier of
   // a round holds exactly those: at the start, the constraints that head all their lists; after
@@ -315,24 +338,40 @@ __device__ int colour_constraints(Team& tm, int n, int nb, const ColourMem m, co
   }
   for (int k = tid; k < n; k += NT) m.rdy[k] = 0;
   tm.sync();
-  int* wl = m.wl0;
-  int* wn = m.wl1;
+  int4* wl = m.wl0;
+  int4* wn = m.wl1;
   const int lane = threadIdx.x & 31;
   const unsigned lt = (1u << lane) - 1u;
-  // pushes the flagged constraints of a warp onto frontier `dst` (team counter `ctr`)
-  auto push = [&](bool f, int k, int* dst, int* ctr) {
+  // pushes the flagged entries of a warp onto frontier `dst` (team counter `ctr`)
+  auto push = [&](bool f, int4 e, int4* dst, int* ctr) {
     const unsigned bal = __ballot_sync(FULL_MASK, f);
     int base = 0;
     if (lane == 0 && bal) base = atomicAdd(ctr, __popc(bal));
     base = __shfl_sync(FULL_MASK, base, 0);
-    if (f) dst[base + __popc(bal & lt)] = k;
+    if (f) dst[base + __popc(bal & lt)] = e;
   };
-  auto heads_all = [&](int k, int2 b) {
-    return (b.x < 0 || m.list[m.head[b.x]] == k) && (b.y < 0 || m.list[m.head[b.y]] == k);
+  // whether the entry at the head of body bb's list heads its other body's list too
+  auto heads_other = [&](int bb, int4 e) {
+    const int other = e.y == bb ? e.z : e.y;
+    return other < 0 || m.head[other] == e.w;
   };
-  for (int i0 = 0; i0 < n; i0 += NT) {  // team-uniform trip counts: whole warps reach the ballots
+  // the first frontier: list heads that head both their lists (pushed from the x body's list when
+  // both bodies have one), and the constraints without a non-static body
+  for (int i0 = 0; i0 < nb; i0 += NT) {  // team-uniform trip counts: whole warps reach the ballots
+    const int i = i0 + tid;
+    int4 e = make_int4(0, 0, 0, 0);
+    bool f = false;
+    if (i < nb && m.head[i] < m.cnt[i]) {
+      e = m.ent[m.head[i]];
+      f = heads_other(i, e) && (e.y == i || e.y < 0);
+    }
+    push(f, e, wl, &s_cnt[0]);
+  }
+  for (int i0 = 0; i0 < n; i0 += NT) {
     const int k = i0 + tid;
-    push(k < n && heads_all(k, m.cb[k]), k, wl, &s_cnt[0]);
+    int2 c = make_int2(0, 0);
+    if (k < n) c = m.cb[k];
+    push(k < n && c.x < 0 && c.y < 0, make_int4(k, c.x, c.y, -1), wl, &s_cnt[0]);
   }
   tm.sync();
   int coloured = 0;
@@ -343,8 +382,9 @@ __device__ int colour_constraints(Team& tm, int n, int nb, const ColourMem m, co
     if (cnt == 0) break;  // every thread reads the same count
     if (round > 0 && tid == 0) s_cnt[cur ^ 1] = 0;
     for (int i = tid; i < cnt; i += NT) {
-      const int k = wl[i];
-      const int2 b = m.cb[k];
+      const int4 e = wl[i];
+      const int k = e.x;
+      const int2 b = make_int2(e.y, e.z);
       const unsigned long long used = (b.x >= 0 ? m.mask[b.x] : 0ull) | (b.y >= 0 ? m.mask[b.y] : 0ull);
       const unsigned long long freeBits = ~used & ((1ull << 63) - 1ull);
       int c;
@@ -363,29 +403,33 @@ __device__ int colour_constraints(Team& tm, int n, int nb, const ColourMem m, co
     tm.sync();
     for (int i0 = 0; i0 < cnt; i0 += NT) {
       const int i = i0 + tid;
-      int cand[2] = {-1, -1};
+      int4 cand[2] = {make_int4(0, 0, 0, 0), make_int4(0, 0, 0, 0)};
+      bool has[2] = {false, false};
       if (i < cnt) {
-        const int2 b = m.cb[wl[i]];
+        const int4 e = wl[i];
 #pragma unroll
         for (int q = 0; q < 2; ++q) {
-          const int bb = q ? b.y : b.x;
+          const int bb = q ? e.z : e.y;
           if (bb < 0) continue;
           const int h = m.head[bb];
           if (h >= m.cnt[bb]) continue;  // the list is done
-          const int k2 = m.list[h];
-          if (!heads_all(k2, m.cb[k2])) continue;
-          // claim k2: set its rdy byte through the aligned word that holds it
-          const uintptr_t addr = reinterpret_cast<uintptr_t>(&m.rdy[k2]);
+          const int4 e2 = m.ent[h];
+          if (!heads_other(bb, e2)) continue;
+          // claim the constraint: set its rdy byte through the aligned word that holds it
+          const uintptr_t addr = reinterpret_cast<uintptr_t>(&m.rdy[e2.x]);
           const unsigned sh = (unsigned)(addr & 3u) * 8u;
           const unsigned old = atomicOr(reinterpret_cast<unsigned*>(addr & ~(uintptr_t)3u), 1u << sh);
-          if (!((old >> sh) & 1u)) cand[q] = k2;
+          if (!((old >> sh) & 1u)) {
+            cand[q] = e2;
+            has[q] = true;
+          }
         }
       }
-      push(cand[0] >= 0, cand[0], wn, &s_cnt[cur ^ 1]);
-      push(cand[1] >= 0, cand[1], wn, &s_cnt[cur ^ 1]);
+      push(has[0], cand[0], wn, &s_cnt[cur ^ 1]);
+      push(has[1], cand[1], wn, &s_cnt[cur ^ 1]);
     }
     tm.sync();
-    int* t = wl;
+    int4* t = wl;
     wl = wn;
     wn = t;
   }
@@ -742,15 +786,117 @@ __device__ inline void isl_unite(int4* SL, int x, int y, unsigned int* status) {
 // The labels are kept between steps: a world whose island graph did not change since its last
 // labelling (no solid contact began or stopped touching, no contact was created or destroyed,
 // same layout: the world's isl_dirty flag is clear) reuses them and only redoes the awake marks.
+// Relabelling in shared memory (a CTA team whose shared memory holds 6 bytes per body): the labels
+// (int), linked marks and awake marks (a byte each) are worked on there with block-scope
+// atomics, and the island records are written once at the end. Same result as the global path.
+template <class Team>
+__device__ void relabel_islands_smem(Team& tm, const KernelArgs& a, int b0, int nb, int c0, int ncAll, int j0,
+                                     int nj, unsigned char* smem) {
+  constexpr int T = Team::kThreads;
+  const int tid = tm.tid();
+  int* lab = reinterpret_cast<int*>(smem);
+  uint8_t* lnk = smem + 4 * (size_t)nb;
+  uint8_t* awk = lnk + nb;
+  int4* SL = a.sl + b0;
+  int2* BS = a.bstate + b0;
+  // the same union-find as the global path (lock-free, the larger root hooked under the smaller)
+  for (int i = tid; i < nb; i += T) {
+    lab[i] = a.btype[b0 + i] == B2G_STATIC ? -1 : i;
+    lnk[i] = 0;
+    awk[i] = 0;
+  }
+  tm.sync();
+  auto find = [&](int x, bool halve) {
+    for (int guard = 0; guard < (1 << 24); ++guard) {
+      const int p = cuda::atomic_ref<int, cuda::thread_scope_block>(lab[x]).load(cuda::memory_order_relaxed);
+      if (p == x) return x;
+      const int g = cuda::atomic_ref<int, cuda::thread_scope_block>(lab[p]).load(cuda::memory_order_relaxed);
+      if (halve && g != p) cuda::atomic_ref<int, cuda::thread_scope_block>(lab[x]).store(g, cuda::memory_order_relaxed);
+      x = g;
+    }
+    raise_status(a.status, B2G_DEV_STACK_OVERFLOW);
+    return x;
+  };
+  auto unite = [&](int x, int y) {
+    for (int guard = 0; guard < (1 << 20); ++guard) {
+      x = find(x, true);
+      y = find(y, true);
+      if (x == y) return;
+      if (x < y) {
+        const int t = x;
+        x = y;
+        y = t;
+      }
+      int expect = x;  // x was hooked meanwhile when this fails: retry from its root
+      if (cuda::atomic_ref<int, cuda::thread_scope_block>(lab[x])
+              .compare_exchange_strong(expect, y, cuda::memory_order_relaxed))
+        return;
+    }
+    raise_status(a.status, B2G_DEV_STACK_OVERFLOW);
+  };
+  for (int k = tid; k < ncAll; k += T) {
+    const int2 f = a.cfix[c0 + k];
+    const int ia = a.fbody[f.x] - b0, ib = a.fbody[f.y] - b0;
+    lnk[ia] = 1;
+    lnk[ib] = 1;
+    const uint32_t fl = a.cflags[c0 + k];
+    if ((fl & B2G_CONTACT_TOUCHING) && (fl & B2G_CONTACT_ENABLED) && !a.fsensor[f.x] && !a.fsensor[f.y] &&
+        lab[ia] >= 0 && lab[ib] >= 0)
+      unite(ia, ib);
+  }
+  for (int k = tid; k < nj; k += T) {
+    const JointDev& J = a.joints[j0 + k];
+    const int ia = J.d.body_a - b0, ib = J.d.body_b - b0;
+    lnk[ia] = 1;
+    lnk[ib] = 1;
+    if (lab[ia] >= 0 && lab[ib] >= 0) unite(ia, ib);
+  }
+  tm.sync();
+  // labels (roots no longer change), and the awake mark of every island with an awake member
+  for (int i = tid; i < nb; i += T) {
+    if (lab[i] < 0) continue;
+    const int r = find(i, false);
+    if (BS[i].x & B2G_BS_AWAKE) awk[r] = 1;
+  }
+  tm.sync();
+  for (int i = tid; i < nb; i += T) {
+    const int l = lab[i];
+    const int r = l < 0 ? -1 : find(i, false);
+    if (r >= 0 && awk[r]) BS[i].x |= B2G_BS_AWAKE;
+    SL[i] = make_int4(r, (lnk[i] ? B2G_ISL_LINKED : 0) | (r == i && awk[i] ? B2G_ISL_AWAKE : 0), 0, 0x7f7fffff);
+  }
+  tm.sync();
+}
+
 template <class Team>
 __device__ void build_islands(Team& tm, const KernelArgs& a, int w, int b0, int nb, int c0, int ncAll, int j0,
-                              int nj) {
+                              int nj, unsigned char* smem = nullptr, int smem_bytes = 0) {
   constexpr cuda::thread_scope S = Team::kScope;
   constexpr int T = Team::kThreads;
   const int tid = tm.tid();
   int4* SL = a.sl + b0;
   int2* BS = a.bstate + b0;
   const bool relabel = a.isl_dirty[w] != 0;
+  if (relabel && Team::kCtas == 1 && smem && 6 * (size_t)nb <= (size_t)smem_bytes) {
+    // this step's narrowphase wakes first, as below
+    for (int i = tid; i < nb; i += T) {
+      const int bi = b0 + i;
+      if (a.bwake[bi]) {
+        a.bwake[bi] = 0;
+        if (a.btype[bi] != B2G_STATIC) {
+          int2 st = BS[i];
+          st.x |= B2G_BS_AWAKE;
+          st.y = 0;
+          BS[i] = st;
+        }
+      }
+    }
+    tm.sync();
+    relabel_islands_smem(tm, a, b0, nb, c0, ncAll, j0, nj, smem);
+    if (tid == 0) a.isl_dirty[w] = 0;  // every thread read the flag before the first barrier
+    tm.sync();
+    return;
+  }
   for (int i = tid; i < nb; i += T) {
     const int bi = b0 + i;
     const bool stat = a.btype[bi] == B2G_STATIC;
@@ -920,7 +1066,7 @@ __device__ __forceinline__ void setup_world(Team& tm, const KernelArgs& a, int w
   int2* const BS = a.bstate + b0;
 
   // 0. sleep-mode worlds: wakes, islands, awake islands
-  if (sleepMode) build_islands(tm, a, w, b0, nb, c0, ncAll, j0, nj);
+  if (sleepMode) build_islands(tm, a, w, b0, nb, c0, ncAll, j0, nj, smem, smem_bytes);
 
   // 1. solver contacts in list order, with local bodies (static = -1) and colouring priorities
   const int nsc = block_compact(tm, 
@@ -963,23 +1109,22 @@ __device__ __forceinline__ void setup_world(Team& tm, const KernelArgs& a, int w
     }
     int* list = bodySm ? (int*)sc.take(8 * (size_t)nsc) : nullptr;
     int2* cb = bodySm ? (int2*)sc.take(8 * (size_t)nsc) : nullptr;
-    int* wl = bodySm ? (int*)sc.take(8 * (size_t)nsc) : nullptr;
     int8_t* col = bodySm ? (int8_t*)sc.take((size_t)nsc) : nullptr;
     uint8_t* rdy = bodySm ? (uint8_t*)sc.take((size_t)nsc) : nullptr;
-    bool conSm = list && cb && wl && col && rdy;
+    bool conSm = list && cb && col && rdy;
     if (conSm) {
       for (int k = tid; k < nsc; k += NT) cb[k] = a.scb[c0 + k];
       tm.sync();
       m.list = list; m.cb = cb; m.col = col; m.rdy = rdy;
-      m.wl0 = wl; m.wl1 = wl + nsc;
     } else {
       m.list = a.inc_list + 2 * (int64_t)c0;
       m.cb = a.scb + c0;
       m.col = a.ccol + c0;
       m.rdy = a.cready + c0;
-      m.wl0 = a.cwork + 2 * (int64_t)c0;
-      m.wl1 = a.cwork + 2 * (int64_t)c0 + nsc;
     }
+    m.ent = a.cwork + 4 * (int64_t)c0;
+    m.wl0 = m.ent + 2 * (int64_t)nsc;
+    m.wl1 = m.wl0 + nsc;
     ncc = colour_constraints(tm, nsc, nb, m, a.cprio + c0, a.corder + c0, a.cslot + c0, cranges, a.status);
     if (conSm) {
       for (int k = tid; k < nsc; k += NT) a.ccol[c0 + k] = col[k];

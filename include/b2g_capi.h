@@ -388,6 +388,16 @@ B2G_API int b2g_step_timed(b2g_batch* b, float dt, int32_t velocity_iterations,
  * then creation order): f4 holds (fx, fy, torque, unused) per body, n_bodies records. The
  * per-step input of an end-to-end loop (b2Body::ApplyForce / ApplyTorque on every body). */
 B2G_API int b2g_batch_set_forces(b2g_batch* b, const float* f4, int64_t n_bodies);
+/* One Step of every world with its host input and output (the end-to-end loop of a driver:
+ * b2Body::ApplyForce / ApplyTorque on every body, b2World::Step src/dynamics/b2_world.cpp:1108-1171,
+ * b2Body::GetTransform on every body): f4 as b2g_batch_set_forces (NULL: the forces already set),
+ * xf4_out as b2g_batch_read_states' xf4 (NULL: none; *n_out receives the bodies). The results equal
+ * b2g_batch_set_forces + b2g_step + b2g_batch_read_states; the copies run on a stream of their own,
+ * the forces' while the contacts are updated (they are needed from the velocity integration on)
+ * and the transforms' while the closing broadphase runs. Synchronous: returns after the step and
+ * both copies. Pinned host buffers give the copies their full bandwidth. */
+B2G_API int b2g_step_io(b2g_batch* b, float dt, int32_t velocity_iterations, int32_t position_iterations,
+                        const float* f4, int64_t n_bodies, float* xf4_out, int64_t cap_bodies, int64_t* n_out);
 /* Whether b2g_step replays the Step as a captured CUDA graph (default on). A graph is used for
  * unmasked steps with dt > 0 and events off; it is re-captured when buffers move. */
 B2G_API int b2g_batch_set_graphs(b2g_batch* b, int32_t enable);

@@ -934,3 +934,38 @@ def test_rollout_measures_vs_reference_golden(lib, orc, name):
         rows.append(ob.measure_row(ob.rollout_measures(orc, list(batch.bodies(w)), fixtures, list(batch.contacts(w)))))
     ob.check_rollout_measures(name, rows, g["rows"])
     batch.close()
+
+
+def test_step_io_equals_separate_calls(lib):
+    """b2g_step_io (forces in, transforms out, the copies overlapping the step on a stream of their
+    own) gives bit for bit what b2g_batch_set_forces + b2g_step + b2g_batch_read_states give, step
+    after step, under graph replay and with forces that change every step."""
+    import torch
+
+    a, _ = _mixed_batch(lib, CLASS_SEEDS[:4], CLASS_SIZES[:4])
+    b, _ = _mixed_batch(lib, CLASS_SEEDS[:4], CLASS_SIZES[:4])
+    a.step(1 / 60, 8, 3)
+    b.step(1 / 60, 8, 3)
+    nb = a.profile().bodies
+    rng = np.random.default_rng(5)
+    forces = torch.zeros((nb, 4), dtype=torch.float32).pin_memory()
+    xa = torch.empty((nb, 4), dtype=torch.float32).pin_memory()
+    xb = torch.empty((nb, 4), dtype=torch.float32).pin_memory()
+    n_out = C.c_int64()
+    for step in range(24):
+        forces.copy_(torch.from_numpy(rng.normal(0.0, 5.0, (nb, 4)).astype(np.float32)))
+        assert a.step_io(forces.data_ptr(), nb, xa.data_ptr(), nb) == nb
+        lib.check(lib.b2g_batch_set_forces(b.h, forces.data_ptr(), nb), "set_forces")
+        b.step(1 / 60, 8, 3)
+        lib.check(lib.b2g_batch_read_states(b.h, C.cast(xb.data_ptr(), C.POINTER(C.c_float)), None, nb,
+                                            C.byref(n_out)), "read_states")
+        assert torch.equal(xa, xb), f"step {step}"
+    for w in range(4):
+        assert _state_bytes(a.bodies(w)) == _state_bytes(b.bodies(w))
+    # without host buffers it is a plain step
+    assert a.step_io(0, 0, 0, 0) == nb
+    b.step(1 / 60, 8, 3)
+    for w in range(4):
+        assert _state_bytes(a.bodies(w)) == _state_bytes(b.bodies(w))
+    a.close()
+    b.close()

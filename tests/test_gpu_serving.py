@@ -50,7 +50,7 @@ def test_results_same_alone_and_in_mix(lib, builders):
 
 
 def test_admission_respects_budget_and_rejects_oversize(lib):
-    per_body = 2048
+    per_body = 2304
     srv = G.Server(lib, device=0, budget_bytes=1000 * per_body, max_worlds=16)
     big = srv.submit(7, 5000, 5)          # larger than the whole budget: rejected
     a = srv.submit(8, 400, 50)
