@@ -540,10 +540,10 @@ B2G_API int b2g_pairs(const float* d_aabbs, int32_t n, uint64_t* d_pairs, int64_
  * Its scratch is a fixed 16 MiB array in device memory that every GPU loading the library keeps
  * until the process exits (68 bytes per AABB plus the radix sort's temporary storage, which fits
  * at the maximum); n may be at most B2G_PAIRS_STATIC_MAX (larger n returns B2G_E_CAPACITY without
- * touching anything). The first call on a device looks up that array's device address, so make
- * it before any stream capture. All calls share the array: calls that overlap on the GPU (two
- * streams, or two host threads) race and must be serialised by the caller. Like b2g_pairs, a call
- * waits for `stream` twice before it returns (once to read the pair total, once at the end).
+ * touching anything). All calls share the array: calls that overlap on the GPU (two streams, or
+ * two host threads) race and must be serialised by the caller. Like b2g_pairs, a call synchronises
+ * `stream` twice before it returns (once to read the pair total, once at the end), so it cannot be
+ * recorded into a CUDA graph or called while `stream` is being captured.
  * Same outputs, capacity rule and status codes as b2g_pairs. */
 #define B2G_PAIRS_STATIC_MAX 131072
 B2G_API int b2g_pairs_static(const float* d_aabbs, int32_t n, uint64_t* d_pairs, int64_t cap,
