@@ -152,25 +152,33 @@ __device__ __forceinline__ int team_warp_scan(Team& tm, int v, int* total) {
 // list order): `flag(k)` is evaluated twice, once to count each warp's kept items by ballots and
 // once to place them, and kept item k is handed to `emit(k, rank)` with its rank in list order.
 // Returns the number kept (in every thread).
+// The counting pass keeps each chunk's ballot in shared memory (up to kCompactChunks chunks per
+// warp), so the placing pass reads it back instead of evaluating flag() again.
+constexpr int kCompactChunks = 64;
 template <class Team, class Flag, class Emit>
 __device__ __forceinline__ int block_compact(Team& tm, int n, Flag flag, Emit emit) {
   constexpr int NWARP = Team::kThreads / 32;
-  const int lane = threadIdx.x & 31, wid = tm.tid() >> 5;
+  constexpr int CW = Team::kThreads / Team::kCtas / 32;  // warps of one CTA
+  __shared__ unsigned ballots[CW][kCompactChunks];
+  const int lane = threadIdx.x & 31, wid = tm.tid() >> 5, lw = threadIdx.x >> 5;
   const int seg = (((n + NWARP - 1) / NWARP) + 31) & ~31;
   const int s0 = min(n, wid * seg), s1 = min(n, s0 + seg);
+  const bool keep = seg / 32 <= kCompactChunks;  // the same for every warp of the team
   int cnt = 0;
-  for (int k0 = s0; k0 < s1; k0 += 32) {
+  for (int k0 = s0, c = 0; k0 < s1; k0 += 32, ++c) {
     const int k = k0 + lane;
-    cnt += __popc(__ballot_sync(FULL_MASK, k < s1 && flag(k)));
+    const unsigned b = __ballot_sync(FULL_MASK, k < s1 && flag(k));
+    if (keep && lane == 0) ballots[lw][c] = b;
+    cnt += __popc(b);
   }
+  __syncwarp();
   int total;
   int base = team_warp_scan(tm, cnt, &total);
   const unsigned lt = (1u << lane) - 1u;
-  for (int k0 = s0; k0 < s1; k0 += 32) {
+  for (int k0 = s0, c = 0; k0 < s1; k0 += 32, ++c) {
     const int k = k0 + lane;
-    const bool f = k < s1 && flag(k);
-    const unsigned b = __ballot_sync(FULL_MASK, f);
-    if (f) emit(k, base + __popc(b & lt));
+    const unsigned b = keep ? ballots[lw][c] : __ballot_sync(FULL_MASK, k < s1 && flag(k));
+    if ((b >> lane) & 1u) emit(k, base + __popc(b & lt));
     base += __popc(b);
   }
   tm.sync();  // every emit() is visible, and flag()'s inputs may change, after the call
@@ -584,6 +592,14 @@ __device__ __forceinline__ void hint_vel(const SolverPlanes& P, int s) {
   prefetch_l1(P.imp + s);
 }
 
+// L1 prefetch of a constraint's position rows (no registers held).
+__device__ __forceinline__ void hint_pos(const SolverPlanes& P, int s) {
+  prefetch_l1(P.idx + s);
+  prefetch_l1(P.lcs + s);
+  prefetch_l1(P.lnp + s);
+  prefetch_l1(P.lps + s);
+  prefetch_l1(P.rad + s);
+}
 __device__ __forceinline__ void fetch_pos(const SolverPlanes& P, int s, PosRows& r) {
   r.id = P.idx[s];
   r.lcs = P.lcs[s];
@@ -1237,7 +1253,6 @@ __device__ __forceinline__ void iterate_world(Team& tm, const KernelArgs& a, int
   auto fetchV = [&](int slot, VelRows& r) { fetch_vel(P, slot, r); };
   auto fetchP = [&](int slot, PosRows& r) { fetch_pos(P, slot, r); };
   auto hintV = [&](int slot) { hint_vel(P, slot); };
-  auto noHint = [](int) {};
   if (warm) {
     colour_sweep<Team, VelRows, PREFETCH, 2>(tm, cranges, ncc, c0, fetchV, [&](int slot, const VelRows& r) {
       VCDev vc;
@@ -1337,7 +1352,8 @@ __device__ __forceinline__ void iterate_world(Team& tm, const KernelArgs& a, int
   //    constraints were all okay in an iteration is done and no longer iterated.
   for (int it = 0; it < a.pi; ++it) {
     int okay = 1;
-    colour_sweep<Team, PosRows, PREFETCH, 1>(tm, cranges, ncc, c0, fetchP, [&](int slot, const PosRows& r) {
+    auto hintP = [&](int slot) { hint_pos(P, slot); };
+    colour_sweep<Team, PosRows, PREFETCH, 2>(tm, cranges, ncc, c0, fetchP, [&](int slot, const PosRows& r) {
       VCDev vc;
       unpack_pos(r, vc, M);
       int root = 0;
@@ -1349,7 +1365,7 @@ __device__ __forceinline__ void iterate_world(Team& tm, const KernelArgs& a, int
         okay = 0;
         if (sleepMode) isl_store<S>(&SL[root].z, it + 1);
       }
-    }, noHint);
+    }, hintP);
     for (int c = 0; c < njc; ++c) {
       int s = jranges[c], e = jranges[c + 1];
       const int step = c == 63 ? 1 : NT, i0 = c == 63 ? s : s + tid;
