@@ -602,12 +602,13 @@ def run_ours(args, rank, world_size):
             cpu = {"value": v, "unit": "body-steps/s", "cores": threads, "kind": "port",
                    "sample": f"{len(cpu_seeds)} of the worlds ({cnb} bodies), steps {args.warmup + 1}-"
                              f"{args.warmup + args.steps} of the same rollout, {secs:.1f} s on {threads} threads"}
-        # own kernels per step (CUB's sort and scan kernels not counted): collide, one solver launch
-        # per world size class (5 in this workload), aabb, refit init, lbvh bounds, pair count,
-        # world contact ranges, pair emit, diff, commit, clear forces = 15 on a step whose closing
-        # broadphase refits the kept trees; a full rebuild (every 16th broadphase) launches world
-        # bounds, morton and lbvh init / internal instead of the refit init (+3)
-        kernels_per_step = 15
+        # own kernels per step (CUB's sort and scan kernels not counted): collide, the solver's
+        # setup and iteration kernels of the four CTA size classes and the cluster kernel of the
+        # largest worlds (9), aabb, refit init, lbvh bounds, pair count, world contact ranges, pair
+        # emit, diff, commit, clear forces = 19 on a step whose closing broadphase refits the kept
+        # trees; a full rebuild (every 16th broadphase) launches world bounds, morton and lbvh
+        # init / internal instead of the refit init (+3)
+        kernels_per_step = 19
         full_builds = args.steps // 16
         line = {
             "metric": METRIC, "value": value, "unit": "body-steps/s", "n_gpus": world_size, "steps": args.steps,
