@@ -108,11 +108,12 @@ __device__ __forceinline__ bool mark_wake(const KernelArgs& a, int b) {
 // awake (static bodies never are); wakes are marked, not applied, so every contact of this pass
 // sees the awake flags the step started with. Sensor contacts go through a pass of their own
 // (SENSORS = true, launched only when the layout has sensors), which keeps the overlap test's
-// state out of the manifold pass's registers. Eight 128-thread blocks per SM (64 registers): the
+// state out of the manifold pass's registers. Four 256-thread blocks per SM (64 registers): the
 // pass waits on its shape and manifold loads, and the extra warps hide more of that than the few
-// spilled registers cost (0.8% of a settled bench step, measured).
+// spilled registers cost (against 128-thread blocks at 75 registers: -1.5% on the bench's short
+// window, the settled step unchanged; measured on the same worlds).
 template <bool SENSORS>
-__global__ void __launch_bounds__(128, 8) k_collide(KernelArgs a) {
+__global__ void __launch_bounds__(256, 4) k_collide(KernelArgs a) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= (int64_t)a.counters[B2G_CNT_CONTACTS]) return;
   int2 f = a.cfix[i];
@@ -784,7 +785,7 @@ __global__ void k_collide_pairs(const b2g_shape* sa, const float* xa, const b2g_
 static inline unsigned grid_for(int64_t n, int bs) { return (unsigned)((n + bs - 1) / bs); }
 
 void launch_collide(const KernelArgs& a, int nw, cudaStream_t s) {
-  if (a.ccap > 0) k_collide<false><<<grid_for(a.ccap, 128), 128, 0, s>>>(a);
+  if (a.ccap > 0) k_collide<false><<<grid_for(a.ccap, 256), 256, 0, s>>>(a);
   if (a.ccap > 0 && a.any_sensor) k_collide<true><<<grid_for(a.ccap, 128), 128, 0, s>>>(a);
   if (a.ccap > 0 && a.any_sleep && nw > 0) k_collide_closure<<<nw, 256, 0, s>>>(a);
 }
