@@ -606,10 +606,10 @@ def run_ours(args, rank, world_size):
         # setup and iteration kernels of the four CTA size classes and the cluster kernel of the
         # largest worlds (9), aabb, refit init, lbvh bounds, pair count, world contact ranges, pair
         # emit, diff, commit, clear forces = 19 on a step whose closing broadphase refits the kept
-        # trees; a full rebuild (every 16th broadphase) launches world bounds, morton and lbvh
+        # trees; a full rebuild (every 32nd broadphase) launches world bounds, morton and lbvh
         # init / internal instead of the refit init (+3)
         kernels_per_step = 19
-        full_builds = args.steps // 16
+        full_builds = args.steps // 32
         line = {
             "metric": METRIC, "value": value, "unit": "body-steps/s", "n_gpus": world_size, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",

@@ -239,7 +239,7 @@ struct Batch {
   // tree_nw)), refit by the closing broadphase and rebuilt from sorted Morton codes every
   // tree_period broadphases (tree_age counts those since the last full build).
   int tree_nf = 0, tree_nw = 0, tree_age = 0;
-  int tree_period = 16;  // broadphases per full build (1: every broadphase builds)
+  int tree_period = 32;  // broadphases per full build (1: every broadphase builds)
 
   // world query scratch
   DBuf<int> q_world, q_counts, q_out;

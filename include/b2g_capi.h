@@ -428,7 +428,7 @@ B2G_API int b2g_batch_set_cluster_solve(b2g_batch* b, int32_t ctas);
 /* The CTAs per world that the batch's worlds above 8192 bodies are solved with (1: one CTA). */
 B2G_API int b2g_batch_get_cluster_solve(b2g_batch* b, int32_t* ctas);
 /* The broadphase keeps each world's tree between steps and refits its boxes; every `period`
- * broadphases (default 16; 1 = every one) it rebuilds all trees from sorted Morton codes, which
+ * broadphases (default 32; 1 = every one) it rebuilds all trees from sorted Morton codes, which
  * restores their spatial order. A tuning knob: the pairs found, and so the results, do not
  * depend on it. */
 B2G_API int b2g_batch_set_tree_rebuild_period(b2g_batch* b, int32_t period);
