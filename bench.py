@@ -621,7 +621,7 @@ def run_ours(args, rank, world_size):
                        "joints_per_gpu": prof.joints, "l2": "state larger than L2 (no flush needed)",
                        "parallelism": f"{world_size} independent world shards", "build_s": round(build_s, 1),
                        "solver_threads_per_class": batch_threads,
-                       "autotune": (f"threads per world for size classes <=64/256/2048/8192/more bodies, tuned on "
+                       "autotune": (f"threads per world for size classes <=64/512/2048/8192/more bodies, tuned on "
                                     f"every 8th world after 100 steps in {tune_s:.1f} s") if threads else "off"},
             "breakdown_ms": {"collide": prof.collide, "solve": prof.solve, "broadphase": prof.broadphase,
                              "step": prof.step},

@@ -199,7 +199,7 @@ void launch_compact(const CompactTables& t, int nb, const BodyRecs& sb, const Bo
                     const ConRecs& dc, cudaStream_t s);
 void solver_setup();
 // Solver launches for worlds listed by body count, largest first, with the given threads per
-// CTA for each size class (at most 64, 256, 2048, 8192 and more bodies); a class runs the wide
+// CTA for each size class (at most 64, 512, 2048, 8192 and more bodies); a class runs the wide
 // build when its worlds fill at most `wide_waves` waves of it.
 std::vector<SolveClass> plan_solve_classes(const std::vector<int>& order, const std::vector<int>& bodies,
                                            const int* class_threads, float wide_waves, int cluster_ctas);

@@ -123,7 +123,7 @@ void launch_colour_check(const KernelArgs& a, int nw, cudaStream_t s) {
 // Class by world body count: threads per CTA and the dynamic shared memory that holds the
 // world's body state and inverse masses (24 B/body) and, room permitting, its colouring arrays
 // (16 B/body + 26 B per contact, about 68 B/body at two contacts per body).
-static const int kClassMaxBodies[B2G_SOLVE_CLASSES] = {64, 256, 2048, 8192, 1 << 30};
+static const int kClassMaxBodies[B2G_SOLVE_CLASSES] = {64, 512, 2048, 8192, 1 << 30};
 // Shared-memory allowance by threads per CTA (64, 128, 256, 512, 1024) of the occupancy and the
 // wide builds: the SM holds kSolveBlocks<T, WIDE> such CTAs, and the allowance keeps that many
 // resident.

@@ -408,7 +408,7 @@ B2G_API int b2g_batch_set_graphs(b2g_batch* b, int32_t enable);
  * B2G_E_CAPACITY with a message. Costs one small launch per step. No reference counterpart (the
  * reference solves serially). */
 B2G_API int b2g_batch_set_debug_checks(b2g_batch* b, int32_t enable);
-/* Threads per world CTA of the solver for each world size class (worlds of at most 64, 256,
+/* Threads per world CTA of the solver for each world size class (worlds of at most 64, 512,
  * 2048 and 8192 bodies, and larger), 5 entries each one of 64, 128, 256, 512, 1024 (defaults
  * 64, 128, 256, 512, 1024). A tuning knob: results do not depend on it. No reference counterpart. */
 B2G_API int b2g_batch_set_solver_threads(b2g_batch* b, const int32_t* threads);

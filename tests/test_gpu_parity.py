@@ -246,7 +246,7 @@ def _mixed_batch(lib, seeds, sizes):
     return b, ws
 
 
-# worlds in each CTA size class of the solver (at most 64, 256, 2048 and 8192 bodies)
+# worlds in each CTA size class of the solver (at most 64, 512, 2048 and 8192 bodies)
 CLASS_SEEDS = [31, 32, 33, 34, 35, 36]
 CLASS_SIZES = [40, 200, 900, 3000, 5000, 60]
 
