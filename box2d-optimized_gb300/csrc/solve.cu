@@ -1,18 +1,20 @@
 // solve.cu - the island solver of one Step for every active world of the batch
 // (b2Island::Solve, src/dynamics/b2_island.cpp:253-484; b2ContactSolver,
-// src/dynamics/b2_contact_solver.cpp), one CTA per world.
+// src/dynamics/b2_contact_solver.cpp), one CTA per world in two kernels.
 //
-// Per world, in order:
+// Per world, in order; the setup kernel (k_setup, 1024 threads per SM):
 //   1. solver contacts: the touching, enabled, non-sensor live contacts (b2_world.cpp:567-599),
 //      compacted in list order, with their world-local non-static bodies and priorities;
 //   2. deterministic greedy colouring of those contacts in priority order (Jones-Plassmann
-//      rounds), in shared memory when the world fits; joints keep the colouring computed once
-//      per layout by k_joint_colour;
-//   3. velocity integration into the body-state buffer (shared memory when the world fits);
+//      rounds), in shared memory for what fits; joints keep the colouring computed once per
+//      layout by k_joint_colour;
+//   3. velocity integration into the global velocity array;
 //   4. contact prepare, written straight into colour-ordered constraint planes;
-//   5. warm start, joint InitVelocityConstraints, velocity iterations (joints then contacts),
-//      StoreImpulses, position integration, position iterations (contacts then joints) with the
-//      world's early exit, transforms.
+// then the iteration kernel (k_solve):
+//   5. warm start, joint InitVelocityConstraints, velocity iterations (joints then contacts) on
+//      the body state in shared memory when the world fits, StoreImpulses, position
+//      integration, position iterations (contacts then joints) with the world's early exit,
+//      transforms.
 // Constraints of one colour share no non-static body, so a colour runs in parallel; colours
 // run in order with a CTA barrier between them, which reproduces the sequential Gauss-Seidel
 // sweep in colour order. Worlds are launched in size classes (threads and shared memory per

@@ -1,6 +1,8 @@
-// solve_world.cuh - the per-world island solve kernel (k_solve) and its device helpers, shared by
-// the two builds of the kernel: the occupancy build (solve.cu) and the wide build (solve_wide.cu),
-// which differ only in their register budget.
+// solve_world.cuh - the per-world island solve and its device helpers: the setup half (k_setup:
+// islands, solver contacts, colouring, velocity integration, constraint preparation) and the
+// iteration half (k_solve, in two builds that differ only in their register budget: the
+// occupancy build in solve.cu and the wide build in solve_wide.cu), and the thread-block cluster
+// kernel that runs both halves for the largest worlds (solve_cluster.cu).
 #pragma once
 #include <cuda/atomic>
 
