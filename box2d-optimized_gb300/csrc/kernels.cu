@@ -117,7 +117,8 @@ __global__ void __launch_bounds__(256, 4) k_collide(KernelArgs a) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= (int64_t)a.counters[B2G_CNT_CONTACTS]) return;
   int2 f = a.cfix[i];
-  if ((a.fsensor[f.x] || a.fsensor[f.y]) != SENSORS) return;
+  // without sensor fixtures in the layout every contact is the manifold pass's
+  if ((SENSORS || a.any_sensor) && (a.fsensor[f.x] || a.fsensor[f.y]) != SENSORS) return;
   int w = a.fworld[f.x];
   const int wf = a.wflags[w];
   if ((wf & B2G_WF_ACTIVE) == 0) return;

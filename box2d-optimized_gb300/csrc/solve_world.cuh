@@ -858,7 +858,7 @@ __device__ void relabel_islands_smem(Team& tm, const KernelArgs& a, int b0, int 
     lnk[ia] = 1;
     lnk[ib] = 1;
     const uint32_t fl = a.cflags[c0 + k];
-    if ((fl & B2G_CONTACT_TOUCHING) && (fl & B2G_CONTACT_ENABLED) && !a.fsensor[f.x] && !a.fsensor[f.y] &&
+    if ((fl & B2G_CONTACT_TOUCHING) && (fl & B2G_CONTACT_ENABLED) && (!a.any_sensor || (!a.fsensor[f.x] && !a.fsensor[f.y])) &&
         lab[ia] >= 0 && lab[ib] >= 0)
       unite(ia, ib);
   }
@@ -944,7 +944,7 @@ __device__ void build_islands(Team& tm, const KernelArgs& a, int w, int b0, int 
       if (!(isl_bits<S>(SL, ia) & B2G_ISL_LINKED)) isl_or<S>(&SL[ia].y, B2G_ISL_LINKED);
       if (!(isl_bits<S>(SL, ib) & B2G_ISL_LINKED)) isl_or<S>(&SL[ib].y, B2G_ISL_LINKED);
       const uint32_t fl = a.cflags[c0 + k];
-      if ((fl & B2G_CONTACT_TOUCHING) && (fl & B2G_CONTACT_ENABLED) && !a.fsensor[f.x] && !a.fsensor[f.y] &&
+      if ((fl & B2G_CONTACT_TOUCHING) && (fl & B2G_CONTACT_ENABLED) && (!a.any_sensor || (!a.fsensor[f.x] && !a.fsensor[f.y])) &&
           isl_load<S>(&SL[ia].x) >= 0 && isl_load<S>(&SL[ib].x) >= 0)
         isl_unite<S>(SL, ia, ib, a.status);
     }
@@ -1092,7 +1092,7 @@ __device__ __forceinline__ void setup_world(Team& tm, const KernelArgs& a, int w
       [&](int k) {
         const uint32_t fl = a.cflags[c0 + k];
         const int2 f = a.cfix[c0 + k];
-        bool flag = (fl & B2G_CONTACT_TOUCHING) && (fl & B2G_CONTACT_ENABLED) && !a.fsensor[f.x] && !a.fsensor[f.y];
+        bool flag = (fl & B2G_CONTACT_TOUCHING) && (fl & B2G_CONTACT_ENABLED) && (!a.any_sensor || (!a.fsensor[f.x] && !a.fsensor[f.y]));
         // contacts of sleeping islands are not solved: after the labelling every member of an awake
         // island is awake and no member of a sleeping one is (static bodies never are), so the
         // island's mark is its bodies' flag, one read instead of a walk to the root
