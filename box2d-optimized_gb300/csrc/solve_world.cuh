@@ -1183,8 +1183,13 @@ __device__ __forceinline__ void setup_world(Team& tm, const KernelArgs& a, int w
   const float4* bs = a.vel + b0;
 
   // 4. prepare (b2ContactSolver::Initialize + InitializeVelocityConstraints) in list order, each
-  //    constraint written to its colour-ordered slot
+  //    constraint written to its colour-ordered slot; each turn reads the next contact's index
+  //    rows up front and, after preparing the current one, prefetches the next one's gathers
+  //    (manifold, material, both bodies) into L2
   for (int k = tid; k < nsc; k += NT) {
+    const bool more = k + NT < nsc;
+    const int cin = more ? a.sc_list[c0 + k + NT] : 0;
+    const int2 lbn = more ? a.scb[c0 + k + NT] : make_int2(0, 0);
     int ci = a.sc_list[c0 + k];
     int p = a.cslot[c0 + k];
     int2 lb = a.scb[c0 + k];
@@ -1197,6 +1202,17 @@ __device__ __forceinline__ void setup_world(Team& tm, const KernelArgs& a, int w
     prepareContact(vc, m, a.cmat[ci], rad.x, rad.y, la, lbb, a.massd[ia], a.massd[ib], a.lc[ia], a.lc[ib],
                    a.pos[ia], bs[la], a.pos[ib], bs[lbb], dtRatio, warm, ci);
     store_planes(P, c0 + p, vc);
+    if (more) {
+      auto l2 = [](const void* q) { asm volatile("prefetch.global.L2 [%0];" ::"l"(q)); };  // no registers held
+      const int na = b0 + (lbn.x & 0x7fffffff), nb2 = b0 + (lbn.y & 0x7fffffff);
+      l2(&a.cman[cin]);
+      l2(reinterpret_cast<const char*>(&a.cman[cin]) + 32);
+      l2(&a.cmat[cin]);
+      l2(&a.massd[na]); l2(&a.massd[nb2]);
+      l2(&a.lc[na]); l2(&a.lc[nb2]);
+      l2(&a.pos[na]); l2(&a.pos[nb2]);
+      l2(&bs[na - b0]); l2(&bs[nb2 - b0]);
+    }
   }
 }
 
