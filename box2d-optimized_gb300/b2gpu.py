@@ -50,6 +50,23 @@ class Manifold(C.Structure):
                 ("type", C.c_int32), ("point_count", C.c_int32)]
 
 
+class Sweep(C.Structure):
+    _fields_ = [("local_center", F2), ("c0", F2), ("c", F2), ("a0", C.c_float), ("a", C.c_float),
+                ("alpha0", C.c_float)]
+
+
+class TOIInput(C.Structure):
+    _fields_ = [("shape_a", Shape), ("shape_b", Shape), ("sweep_a", Sweep), ("sweep_b", Sweep),
+                ("t_max", C.c_float)]
+
+
+class TOIOutput(C.Structure):
+    _fields_ = [("state", C.c_int32), ("t", C.c_float)]
+
+
+TOI_UNKNOWN, TOI_FAILED, TOI_OVERLAPPED, TOI_TOUCHING, TOI_SEPARATED = 0, 1, 2, 3, 4
+
+
 class BodyDef(C.Structure):
     _fields_ = [("type", C.c_int32), ("position", F2), ("angle", C.c_float),
                 ("linear_velocity", F2), ("angular_velocity", C.c_float),
@@ -235,7 +252,7 @@ class Lib:
         "b2g_pairs_static", "b2g_reserve",
         "b2g_bodies_read", "b2g_bodies_write", "b2g_batch_read_states", "b2g_fixtures_read",
         "b2g_joints_read", "b2g_contacts_read", "b2g_events_enable", "b2g_events_drain",
-        "b2g_profile_get", "b2g_solver_order", "b2g_collide", "b2g_pairs", "b2g_scene_build",
+        "b2g_profile_get", "b2g_solver_order", "b2g_collide", "b2g_time_of_impact", "b2g_pairs", "b2g_scene_build",
         "b2g_batch_world_params", "b2g_server_create", "b2g_server_destroy", "b2g_server_submit",
         "b2g_server_tick", "b2g_server_poll", "b2g_server_stats", "b2g_status_string",
         "b2g_last_error", "b2g_device_count", "b2g_query_aabb", "b2g_raycast_closest", "b2g_world_status",
@@ -317,6 +334,7 @@ class Lib:
             "b2g_raycast_closest": ([vp, P(i32), P(f32), i32, P(RayHit)], C.c_int),
             "b2g_solver_order": ([vp, i32, P(i32), P(u32), i32, P(i32), P(u32), i32], C.c_int),
             "b2g_collide": ([vp, vp, vp, vp, i32, vp, vp], C.c_int),
+            "b2g_time_of_impact": ([vp, i32, vp, vp], C.c_int),
             "b2g_pairs": ([vp, i32, vp, i64, P(i64), vp], C.c_int),
             "b2g_scene_build": ([vp, i32, i32, u32, i32, f32, f32, P(i32)], C.c_int),
             "b2g_batch_world_params": ([u32, P(i32), P(f32), P(f32)], C.c_int),

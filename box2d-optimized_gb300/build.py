@@ -28,7 +28,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "--fmad=false", "-std=c++17", "-Xcompiler", "-fPIC",
               "-Xcompiler", "-ffp-contract=off",
               f"-I{ROOT / 'include'}", f"-I{PKG / 'include'}"]
-CU_SOURCES = ["solve.cu", "solve_wide.cu", "solve_cluster.cu", "kernels.cu", "compact.cu", "query.cu", "engine.cu", "pairs.cu"]
+CU_SOURCES = ["solve.cu", "solve_wide.cu", "solve_cluster.cu", "kernels.cu", "compact.cu", "query.cu", "engine.cu", "pairs.cu", "toi.cu"]
 CPP_SOURCES = ["shapes.cpp", "facade.cpp", "server.cpp"]
 
 

@@ -2948,4 +2948,15 @@ B2G_API int b2g_collide(const b2g_shape* sa, const float* xa, const b2g_shape* s
   return B2G_OK;
 }
 
+B2G_API int b2g_time_of_impact(const b2g_toi_input* in, int32_t n, b2g_toi_output* out, void* stream) {
+  if (n < 0 || (n > 0 && (!in || !out))) return B2G_E_INVALID_ARG;
+  launch_time_of_impact(in, n, out, (cudaStream_t)stream);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    set_error(nullptr, cudaGetErrorString(e));
+    return B2G_E_CUDA;
+  }
+  return B2G_OK;
+}
+
 }  // extern "C"

@@ -225,6 +225,7 @@ void launch_bp_tail(const KernelArgs& a, int f0, int nf, int w0, int nw, size_t 
                     int* poff_live, cudaStream_t s);
 void launch_contact_diff(const KernelArgs& a, int src, int dst, cudaStream_t s);
 size_t cub_temp_bytes(int nf);
+void launch_time_of_impact(const b2g_toi_input* in, int n, b2g_toi_output* out, cudaStream_t s);
 void launch_collide_pairs(const b2g_shape* sa, const float* xa, const b2g_shape* sb, const float* xb, int n,
                           b2g_manifold* out, cudaStream_t s);
 

@@ -101,6 +101,38 @@ typedef struct b2g_manifold {
   int32_t point_count;
 } b2g_manifold;
 
+/* b2Sweep (include/box2d/b2_math.h:383-404): 36 bytes, same fields in the same order. */
+typedef struct b2g_sweep {
+  float local_center[2];
+  float c0[2];
+  float c[2];
+  float a0;
+  float a;
+  float alpha0;
+} b2g_sweep;
+
+/* b2TOIInput (include/box2d/b2_time_of_impact.h:29-36): the two b2DistanceProxy are given as
+ * their shapes (a circle's proxy is its centre, an edge's its two vertices, a polygon's its
+ * vertices; the radius is the shape's). */
+typedef struct b2g_toi_input {
+  b2g_shape shape_a;
+  b2g_shape shape_b;
+  b2g_sweep sweep_a;
+  b2g_sweep sweep_b;
+  float t_max;
+} b2g_toi_input;
+
+/* b2TOIOutput::State (include/box2d/b2_time_of_impact.h:42-49) */
+#define B2G_TOI_UNKNOWN 0
+#define B2G_TOI_FAILED 1
+#define B2G_TOI_OVERLAPPED 2
+#define B2G_TOI_TOUCHING 3
+#define B2G_TOI_SEPARATED 4
+typedef struct b2g_toi_output {
+  int32_t state;
+  float t;
+} b2g_toi_output;
+
 /* ---- definitions (inputs) ------------------------------------------------------------------ */
 /* b2BodyDef, include/box2d/b2_body.h:52-130 */
 typedef struct b2g_body_def {
@@ -522,6 +554,9 @@ B2G_API int b2g_raycast_closest(b2g_batch* b, const int32_t* worlds, const float
  * All pointers are device pointers; xf records are (p.x, p.y, q.s, q.c). */
 B2G_API int b2g_collide(const b2g_shape* d_shape_a, const float* d_xf_a, const b2g_shape* d_shape_b,
                         const float* d_xf_b, int32_t n, b2g_manifold* d_out, void* stream);
+/* Time of impact of n pairs of swept shapes (b2TimeOfImpact, src/collision/b2_time_of_impact.cpp:
+ * 258-490), one output per input, same states and times. All pointers are device pointers. */
+B2G_API int b2g_time_of_impact(const b2g_toi_input* d_in, int32_t n, b2g_toi_output* d_out, void* stream);
 /* Broadphase: every pair (i < j) of the n AABBs (lo.x, lo.y, hi.x, hi.y) that overlap with the
  * reference's inclusive test (include/box2d/b2_collision.h:270-276), sorted by (i, j), written
  * as i << 32 | j into d_pairs (capacity cap). *n_pairs receives the total (64-bit: dense

@@ -1326,6 +1326,256 @@ static bool testOverlap(const Shape& A, const Xf& xfA, const Shape& B, const Xf&
   return gjkDistance(A, xfA, B, xfB) < 10.0f * kEpsilon;
 }
 
+// ---- time of impact: b2TimeOfImpact (src/collision/b2_time_of_impact.cpp:258-490) over
+// b2Distance with a simplex cache (src/collision/b2_distance.cpp:86-135, 432-579) and the
+// separating-axis function b2SeparationFunction (b2_time_of_impact.cpp:35-251).
+struct Sweep { V2 localCenter, c0, c; float a0, a, alpha0; };
+// b2Sweep::GetTransform / Advance / Normalize (include/box2d/b2_math.h:707-733)
+static Xf sweepTransform(const Sweep& s, float beta) {
+  Xf xf;
+  xf.p = (1.0f - beta) * s.c0 + beta * s.c;
+  float angle = (1.0f - beta) * s.a0 + beta * s.a;
+  xf.q = rotOf(angle);
+  subFrom(xf.p, mul(xf.q, s.localCenter));
+  return xf;
+}
+static void sweepAdvance(Sweep& s, float alpha) {
+  float beta = (alpha - s.alpha0) / (1.0f - s.alpha0);
+  addTo(s.c0, beta * (s.c - s.c0));
+  s.a0 += beta * (s.a - s.a0);
+  s.alpha0 = alpha;
+}
+static void sweepNormalize(Sweep& s) {
+  float twoPi = 2.0f * kPi;
+  float d = twoPi * floorf(s.a0 / twoPi);
+  s.a0 -= d;
+  s.a -= d;
+}
+
+struct SimplexCache { float metric; int count; int iA[3], iB[3]; };
+
+// b2Simplex with its cache round trip; solve2/solve3 as in gjkDistance above.
+struct Simplex {
+  SV v[3];
+  int n;
+  float metric() const {
+    if (n == 2) { V2 c = v[0].w - v[1].w; return lengthOf(c); }
+    if (n == 3) return cross(v[1].w - v[0].w, v[2].w - v[0].w);
+    return 0.0f;
+  }
+  void setVertex(int i, int iA, int iB, const Shape& A, const Xf& xfA, const Shape& B, const Xf& xfB) {
+    v[i].iA = iA;
+    v[i].iB = iB;
+    v[i].wA = mul(xfA, gjkVertex(A, iA));
+    v[i].wB = mul(xfB, gjkVertex(B, iB));
+    v[i].w = v[i].wB - v[i].wA;
+  }
+  void readCache(const SimplexCache& c, const Shape& A, const Xf& xfA, const Shape& B, const Xf& xfB) {
+    n = c.count;
+    for (int i = 0; i < n; ++i) {
+      setVertex(i, c.iA[i], c.iB[i], A, xfA, B, xfB);
+      v[i].a = 0.0f;
+    }
+    if (n > 1) {
+      float m1 = c.metric, m2 = metric();
+      if (m2 < 0.5f * m1 || 2.0f * m1 < m2 || m2 < kEpsilon) n = 0;
+    }
+    if (n == 0) {
+      setVertex(0, 0, 0, A, xfA, B, xfB);
+      v[0].a = 1.0f;
+      n = 1;
+    }
+  }
+  void writeCache(SimplexCache& c) const {
+    c.metric = metric();
+    c.count = n;
+    for (int i = 0; i < n; ++i) { c.iA[i] = v[i].iA; c.iB[i] = v[i].iB; }
+  }
+  void solve2() {
+    V2 w1 = v[0].w, w2 = v[1].w, e12 = w2 - w1;
+    float d12_2 = -dot(w1, e12);
+    if (d12_2 <= 0.0f) { v[0].a = 1.0f; n = 1; return; }
+    float d12_1 = dot(w2, e12);
+    if (d12_1 <= 0.0f) { v[1].a = 1.0f; n = 1; v[0] = v[1]; return; }
+    float inv = 1.0f / (d12_1 + d12_2);
+    v[0].a = d12_1 * inv; v[1].a = d12_2 * inv; n = 2;
+  }
+  void solve3() {
+    V2 w1 = v[0].w, w2 = v[1].w, w3 = v[2].w;
+    V2 e12 = w2 - w1;
+    float d12_1 = dot(w2, e12), d12_2 = -dot(w1, e12);
+    V2 e13 = w3 - w1;
+    float d13_1 = dot(w3, e13), d13_2 = -dot(w1, e13);
+    V2 e23 = w3 - w2;
+    float d23_1 = dot(w3, e23), d23_2 = -dot(w2, e23);
+    float n123 = cross(e12, e13);
+    float d123_1 = n123 * cross(w2, w3), d123_2 = n123 * cross(w3, w1), d123_3 = n123 * cross(w1, w2);
+    if (d12_2 <= 0.0f && d13_2 <= 0.0f) { v[0].a = 1.0f; n = 1; return; }
+    if (d12_1 > 0.0f && d12_2 > 0.0f && d123_3 <= 0.0f) {
+      float inv = 1.0f / (d12_1 + d12_2);
+      v[0].a = d12_1 * inv; v[1].a = d12_2 * inv; n = 2; return;
+    }
+    if (d13_1 > 0.0f && d13_2 > 0.0f && d123_2 <= 0.0f) {
+      float inv = 1.0f / (d13_1 + d13_2);
+      v[0].a = d13_1 * inv; v[2].a = d13_2 * inv; n = 2; v[1] = v[2]; return;
+    }
+    if (d12_1 <= 0.0f && d23_2 <= 0.0f) { v[1].a = 1.0f; n = 1; v[0] = v[1]; return; }
+    if (d13_1 <= 0.0f && d23_1 <= 0.0f) { v[2].a = 1.0f; n = 1; v[0] = v[2]; return; }
+    if (d23_1 > 0.0f && d23_2 > 0.0f && d123_1 <= 0.0f) {
+      float inv = 1.0f / (d23_1 + d23_2);
+      v[1].a = d23_1 * inv; v[2].a = d23_2 * inv; n = 2; v[0] = v[2]; return;
+    }
+    float inv = 1.0f / (d123_1 + d123_2 + d123_3);
+    v[0].a = d123_1 * inv; v[1].a = d123_2 * inv; v[2].a = d123_3 * inv; n = 3;
+  }
+};
+
+// b2Distance with useRadii = false: the distance between the witness points.
+static float gjkCached(const Shape& A, const Xf& xfA, const Shape& B, const Xf& xfB, SimplexCache& cache) {
+  Simplex s;
+  s.readCache(cache, A, xfA, B, xfB);
+  int saveA[3], saveB[3];
+  int iter = 0;
+  while (iter < 20) {
+    int saveCount = s.n;
+    for (int i = 0; i < saveCount; ++i) { saveA[i] = s.v[i].iA; saveB[i] = s.v[i].iB; }
+    if (s.n == 2) s.solve2();
+    else if (s.n == 3) s.solve3();
+    if (s.n == 3) break;
+    V2 d;
+    if (s.n == 1) d = -s.v[0].w;
+    else {
+      V2 e12 = s.v[1].w - s.v[0].w;
+      d = cross(e12, -s.v[0].w) > 0.0f ? cross(1.0f, e12) : cross(e12, 1.0f);
+    }
+    if (lengthSq(d) < kEpsilon * kEpsilon) break;
+    int iA = gjkSupport(A, mulT(xfA.q, -d));
+    int iB = gjkSupport(B, mulT(xfB.q, d));
+    s.setVertex(s.n, iA, iB, A, xfA, B, xfB);
+    ++iter;
+    bool duplicate = false;
+    for (int i = 0; i < saveCount; ++i)
+      if (iA == saveA[i] && iB == saveB[i]) { duplicate = true; break; }
+    if (duplicate) break;
+    ++s.n;
+  }
+  V2 pA, pB;
+  if (s.n == 1) { pA = s.v[0].wA; pB = s.v[0].wB; }
+  else if (s.n == 2) {
+    pA = s.v[0].a * s.v[0].wA + s.v[1].a * s.v[1].wA;
+    pB = s.v[0].a * s.v[0].wB + s.v[1].a * s.v[1].wB;
+  } else {
+    pA = s.v[0].a * s.v[0].wA + s.v[1].a * s.v[1].wA + s.v[2].a * s.v[2].wA;
+    pB = pA;
+  }
+  s.writeCache(cache);
+  V2 c = pA - pB;
+  return lengthOf(c);
+}
+
+struct Separation {
+  enum Kind { kPoints, kFaceA, kFaceB };
+  const Shape *A, *B;
+  Sweep sA, sB;
+  Kind kind;
+  V2 localPoint, axis;
+
+  float init(const SimplexCache& cache, const Shape& pa, const Sweep& wa, const Shape& pb, const Sweep& wb, float t1) {
+    A = &pa; B = &pb; sA = wa; sB = wb;
+    Xf xfA = sweepTransform(sA, t1), xfB = sweepTransform(sB, t1);
+    if (cache.count == 1) {
+      kind = kPoints;
+      axis = mul(xfB, gjkVertex(*B, cache.iB[0])) - mul(xfA, gjkVertex(*A, cache.iA[0]));
+      return normalize(axis);
+    }
+    const bool faceB = cache.iA[0] == cache.iA[1];
+    const Shape& F = faceB ? *B : *A;
+    const Shape& P = faceB ? *A : *B;
+    const Xf& xfF = faceB ? xfB : xfA;
+    const Xf& xfP = faceB ? xfA : xfB;
+    const int* fi = faceB ? cache.iB : cache.iA;
+    const int pi = faceB ? cache.iA[0] : cache.iB[0];
+    kind = faceB ? kFaceB : kFaceA;
+    V2 l1 = gjkVertex(F, fi[0]), l2 = gjkVertex(F, fi[1]);
+    axis = cross(l2 - l1, 1.0f);
+    normalize(axis);
+    V2 normal = mul(xfF.q, axis);
+    localPoint = 0.5f * (l1 + l2);
+    V2 pointF = mul(xfF, localPoint);
+    V2 pointP = mul(xfP, gjkVertex(P, pi));
+    float s = dot(pointP - pointF, normal);
+    if (s < 0.0f) { axis = -axis; s = -s; }
+    return s;
+  }
+  float findMin(int* iA, int* iB, float t) const {
+    Xf xfA = sweepTransform(sA, t), xfB = sweepTransform(sB, t);
+    if (kind == kPoints) {
+      *iA = gjkSupport(*A, mulT(xfA.q, axis));
+      *iB = gjkSupport(*B, mulT(xfB.q, -axis));
+      return dot(mul(xfB, gjkVertex(*B, *iB)) - mul(xfA, gjkVertex(*A, *iA)), axis);
+    }
+    if (kind == kFaceA) {
+      V2 normal = mul(xfA.q, axis);
+      V2 pointA = mul(xfA, localPoint);
+      *iA = -1;
+      *iB = gjkSupport(*B, mulT(xfB.q, -normal));
+      return dot(mul(xfB, gjkVertex(*B, *iB)) - pointA, normal);
+    }
+    V2 normal = mul(xfB.q, axis);
+    V2 pointB = mul(xfB, localPoint);
+    *iB = -1;
+    *iA = gjkSupport(*A, mulT(xfA.q, -normal));
+    return dot(mul(xfA, gjkVertex(*A, *iA)) - pointB, normal);
+  }
+  float evaluate(int iA, int iB, float t) const {
+    Xf xfA = sweepTransform(sA, t), xfB = sweepTransform(sB, t);
+    if (kind == kPoints) return dot(mul(xfB, gjkVertex(*B, iB)) - mul(xfA, gjkVertex(*A, iA)), axis);
+    if (kind == kFaceA) return dot(mul(xfB, gjkVertex(*B, iB)) - mul(xfA, localPoint), mul(xfA.q, axis));
+    return dot(mul(xfA, gjkVertex(*A, iA)) - mul(xfB, localPoint), mul(xfB.q, axis));
+  }
+};
+
+// b2TimeOfImpact: the state (B2G_TOI_*) and the time in [0, tMax] written to *t.
+static int timeOfImpact(const Shape& A, const Shape& B, Sweep sA, Sweep sB, float tMax, float* t) {
+  *t = tMax;
+  sweepNormalize(sA);
+  sweepNormalize(sB);
+  const float target = bmax(kLinearSlop, (A.radius + B.radius) - 3.0f * kLinearSlop);
+  const float tolerance = 0.25f * kLinearSlop;
+  float t1 = 0.0f;
+  SimplexCache cache;
+  cache.count = 0;
+  cache.metric = 0.0f;
+  for (int iter = 1;; ++iter) {
+    float distance = gjkCached(A, sweepTransform(sA, t1), B, sweepTransform(sB, t1), cache);
+    if (distance <= 0.0f) { *t = 0.0f; return B2G_TOI_OVERLAPPED; }
+    if (distance < target + tolerance) { *t = t1; return B2G_TOI_TOUCHING; }
+    Separation fcn;
+    fcn.init(cache, A, sA, B, sB, t1);
+    float t2 = tMax;
+    for (int push = 1;; ++push) {
+      int iA, iB;
+      float s2 = fcn.findMin(&iA, &iB, t2);
+      if (s2 > target + tolerance) { *t = tMax; return B2G_TOI_SEPARATED; }
+      if (s2 > target - tolerance) { t1 = t2; break; }
+      float s1 = fcn.evaluate(iA, iB, t1);
+      if (s1 < target - tolerance) { *t = t1; return B2G_TOI_FAILED; }
+      if (s1 <= target + tolerance) { *t = t1; return B2G_TOI_TOUCHING; }
+      float a1 = t1, a2 = t2;
+      for (int root = 0; root < 50;) {
+        float tm = (root & 1) ? a1 + (target - s1) * (a2 - a1) / (s2 - s1) : 0.5f * (a1 + a2);
+        ++root;
+        float s = fcn.evaluate(iA, iB, tm);
+        if (babs(s - target) < tolerance) { t2 = tm; break; }
+        if (s > target) { a1 = tm; s1 = s; }
+        else { a2 = tm; s2 = s; }
+      }
+      if (push == 8) break;  // b2_maxPolygonVertices
+    }
+    if (iter == 20) { *t = t1; return B2G_TOI_FAILED; }
+  }
+}
+
 // b2Contact::Update (src/dynamics/b2_contact.cpp:126-210) for one contact; returns whether
 // touching changed on a non-sensor contact (which wakes both bodies, :183-188).
 static bool updateContact(World* w, Contact& c) {
@@ -3150,6 +3400,23 @@ int orc_test_overlap(const b2g_shape* sa, const float* xfa, const b2g_shape* sb,
   tb.p = v2(xfb[0], xfb[1]); tb.q.s = xfb[2]; tb.q.c = xfb[3];
   *distance = gjkDistance(A, ta, B, tb);
   return testOverlap(A, ta, B, tb) ? 1 : 0;
+}
+
+static Sweep sweepFrom(const b2g_sweep& s) {
+  Sweep o;
+  o.localCenter = v2(s.local_center[0], s.local_center[1]);
+  o.c0 = v2(s.c0[0], s.c0[1]);
+  o.c = v2(s.c[0], s.c[1]);
+  o.a0 = s.a0; o.a = s.a; o.alpha0 = s.alpha0;
+  return o;
+}
+
+// b2TimeOfImpact for n inputs.
+void orc_time_of_impact(const b2g_toi_input* in, int32_t n, b2g_toi_output* out) {
+  for (int32_t i = 0; i < n; ++i) {
+    Shape A = shapeFrom(in[i].shape_a), B = shapeFrom(in[i].shape_b);
+    out[i].state = timeOfImpact(A, B, sweepFrom(in[i].sweep_a), sweepFrom(in[i].sweep_b), in[i].t_max, &out[i].t);
+  }
 }
 
 int orc_collide(const b2g_shape* sa, const float* xfa, const b2g_shape* sb, const float* xfb, b2g_manifold* out) {

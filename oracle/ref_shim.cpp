@@ -22,6 +22,7 @@
 #define protected public
 #include "box2d/box2d.h"
 #include "box2d/b2_distance.h"
+#include "box2d/b2_time_of_impact.h"
 #include "dynamics/b2_contact_solver.h"
 #include "dynamics/b2_island.h"
 #include "box2d/b2_stack_allocator.h"
@@ -113,6 +114,36 @@ static void manifold_out(const b2Manifold& m, b2g_manifold* o) {
   o->local_point[0] = m.localPoint.x; o->local_point[1] = m.localPoint.y;
   o->type = (int32_t)m.type;
   o->point_count = m.pointCount;
+}
+
+static b2Sweep sweep_to_ref(const b2g_sweep& s) {
+  b2Sweep o;
+  o.localCenter.Set(s.local_center[0], s.local_center[1]);
+  o.c0.Set(s.c0[0], s.c0[1]);
+  o.c.Set(s.c[0], s.c[1]);
+  o.a0 = s.a0;
+  o.a = s.a;
+  o.alpha0 = s.alpha0;
+  return o;
+}
+
+// The reference's b2TimeOfImpact (src/collision/b2_time_of_impact.cpp:258) for n inputs.
+void ref_time_of_impact(const b2g_toi_input* in, int32_t n, b2g_toi_output* out) {
+  for (int32_t i = 0; i < n; ++i) {
+    AnyShape a, b;
+    shape_to_ref(&in[i].shape_a, &a);
+    shape_to_ref(&in[i].shape_b, &b);
+    b2TOIInput ti;
+    ti.proxyA.Set(a.ptr);
+    ti.proxyB.Set(b.ptr);
+    ti.sweepA = sweep_to_ref(in[i].sweep_a);
+    ti.sweepB = sweep_to_ref(in[i].sweep_b);
+    ti.tMax = in[i].t_max;
+    b2TOIOutput to;
+    b2TimeOfImpact(&to, &ti);
+    out[i].state = (int32_t)to.state;
+    out[i].t = to.t;
+  }
 }
 
 int ref_polygon_set(const float* xy, int32_t n, b2g_shape* out) {

@@ -9,7 +9,8 @@ Every vector is an output of the reference's own code (compiled from its sources
 inputs: polygon hulls and mass data (b2PolygonShape::Set / SetAsBox / ComputeMass), manifolds of
 the five collide functions, one replayed solver step (b2Island::Solve in a given constraint
 order) on exported world states, the listener callbacks of one replayed step, the final state of
-a 256-step reference rollout, and the physical measures of 256-step reference rollouts.
+a 256-step reference rollout, the physical measures of 256-step reference rollouts, and
+b2TimeOfImpact on swept shape pairs (`python tests/golden/make_golden.py toi` writes those alone).
 """
 from __future__ import annotations
 
@@ -169,8 +170,48 @@ def measures(ref, orc, name, kind, n, seed, p0, steps, vi, pi, every=32):
                         vi=vi, pi=pi, kind=kind, n=n, seed=seed, p0=p0)
 
 
+def toi(ref, rng, n=1500):
+    """b2TimeOfImpact on swept shape pairs: random sweeps, and sweeps where A crosses a slowly
+    moving B (touching times inside (0, 1), the root finder's work), some with alpha0 > 0 and
+    tMax < 1."""
+    kinds = [(0, 0), (2, 0), (2, 2), (1, 0), (1, 2), (0, 2), (2, 1)]
+    arr = (G.TOIInput * n)()
+    for i in range(n):
+        ka, kb = kinds[i % len(kinds)]
+        q = arr[i]
+        q.shape_a = rand_shape(ref, rng, ka)
+        q.shape_b = rand_shape(ref, rng, kb)
+        cross = i % 2 == 1
+        for k, sw in enumerate((q.sweep_a, q.sweep_b)):
+            sw.local_center[:] = rng.uniform(-0.2, 0.2, 2)
+            if cross and k == 0:
+                d = rng.uniform(1.5, 6.0)
+                th = rng.uniform(-3.2, 3.2)
+                sw.c0[:] = (-d * np.cos(th), -d * np.sin(th))
+                sw.c[:] = (d * np.cos(th) + rng.uniform(-0.5, 0.5), d * np.sin(th) + rng.uniform(-0.5, 0.5))
+            elif cross:
+                c0 = rng.uniform(-0.3, 0.3, 2)
+                sw.c0[:] = c0
+                sw.c[:] = c0 + rng.uniform(-0.2, 0.2, 2)
+            else:
+                c0 = rng.uniform(-2, 2, 2)
+                sw.c0[:] = c0
+                sw.c[:] = c0 + rng.uniform(-3, 3, 2)
+            sw.a0 = rng.uniform(-7, 7)
+            sw.a = sw.a0 + rng.uniform(-2, 2)
+            sw.alpha0 = 0.0 if i % 5 else float(rng.uniform(0.0, 0.6))
+        q.t_max = 1.0 if i % 4 else float(rng.uniform(0.3, 1.0))
+    out = (G.TOIOutput * n)()
+    ref.ref_time_of_impact(arr, n, out)
+    np.savez_compressed(HERE / "toi.npz", inputs=rec_bytes(arr), states=np.array([o.state for o in out], np.int32),
+                        t=np.array([o.t for o in out], np.float32))
+
+
 def main():
     ref = ob.Ref()
+    if sys.argv[1:] == ["toi"]:  # the time-of-impact vectors alone
+        toi(ref, np.random.default_rng(20261204))
+        return
     orc = ob.Oracle()
     rng = np.random.default_rng(20261203)
     shapes(ref, rng)
@@ -186,6 +227,7 @@ def main():
     measures(ref, orc, "pyramid", G.SCENE_PYRAMID, 20, 1, 1.0, 256, 8, 3)
     measures(ref, orc, "mixed", G.SCENE_MIXED_DROP, 300, 3, 0.0, 256, 8, 3)
     measures(ref, orc, "chains", G.SCENE_CHAINS, 10, 2, 150.0, 256, 10, 4)
+    toi(ref, np.random.default_rng(20261204))
     print("golden vectors written to", HERE)
 
 

@@ -32,6 +32,7 @@ class Ref:
             "ref_shape_aabb": ([P(G.Shape), P(f32), P(f32)], C.c_int),
             "ref_collide": ([P(G.Shape), P(f32), P(G.Shape), P(f32), P(G.Manifold)], C.c_int),
             "ref_test_overlap": ([P(G.Shape), P(f32), P(G.Shape), P(f32), P(f32)], C.c_int),
+            "ref_time_of_impact": ([P(G.TOIInput), i32, P(G.TOIOutput)], None),
             "ref_world_manifold": ([P(G.Manifold), P(f32), f32, P(f32), f32, P(f32)], C.c_int),
             "ref_scene_world": ([i32, u32, i32, f32, f32, f32, f32, P(i32)], vp),
             "ref_world_free": ([vp], None),
@@ -171,6 +172,7 @@ class Oracle:
             "orc_shape_aabb": ([P(G.Shape), P(f32), P(f32)], C.c_int),
             "orc_collide": ([P(G.Shape), P(f32), P(G.Shape), P(f32), P(G.Manifold)], C.c_int),
             "orc_test_overlap": ([P(G.Shape), P(f32), P(G.Shape), P(f32), P(f32)], C.c_int),
+            "orc_time_of_impact": ([P(G.TOIInput), i32, P(G.TOIOutput)], None),
             "orc_world_manifold": ([P(G.Manifold), P(f32), f32, P(f32), f32, P(f32)], C.c_int),
             "orc_sincos": ([f32, P(f32), P(f32)], None),
             "orc_world_new": ([f32, f32], vp),

@@ -6,6 +6,7 @@ so on identical inputs every float of the body state must match exactly. Integer
 (pair sets, manifold point counts, feature ids) are compared exactly as well.
 """
 import ctypes as C
+from pathlib import Path
 
 import numpy as np
 import pytest
@@ -506,6 +507,45 @@ def test_collide_kernel_matches_oracle(lib, orc):
             assert g.type == m.type
             assert bytes(g) == bytes(m), i
     assert touching > 3000
+
+
+def test_toi_kernel_matches_oracle(lib, orc):
+    """b2g_time_of_impact against the oracle's b2TimeOfImpact, bit for bit: the reference's own
+    input set (tests/golden/toi.npz) and 20 000 random sweeps of every shape pairing."""
+    g = np.load(Path(__file__).resolve().parent / "golden" / "toi.npz")
+    raw = bytes(np.asarray(g["inputs"], np.uint8))
+    golden = list((G.TOIInput * (len(raw) // C.sizeof(G.TOIInput))).from_buffer_copy(raw))
+    rng = np.random.default_rng(11)
+    kinds = [(0, 0), (2, 0), (2, 2), (1, 0), (1, 2), (0, 2), (2, 1)]
+    extra = []
+    for i in range(20000):
+        q = G.TOIInput()
+        ka, kb = kinds[i % len(kinds)]
+        q.shape_a, q.shape_b = _rand_shape(rng, ka), _rand_shape(rng, kb)
+        for k, sw in enumerate((q.sweep_a, q.sweep_b)):
+            sw.local_center[:] = rng.uniform(-0.2, 0.2, 2)
+            c0 = rng.uniform(-3, 3, 2) if k == 0 else rng.uniform(-0.3, 0.3, 2)
+            sw.c0[:] = c0
+            sw.c[:] = (-c0 if k == 0 else c0) + rng.uniform(-0.5, 0.5, 2)
+            sw.a0 = rng.uniform(-7, 7)
+            sw.a = sw.a0 + rng.uniform(-2, 2)
+            sw.alpha0 = 0.0 if i % 3 else float(rng.uniform(0, 0.5))
+        q.t_max = 1.0
+        extra.append(q)
+    inputs = golden + extra
+    n = len(inputs)
+    arr = (G.TOIInput * n)(*inputs)
+    din = _dev_bytes(bytes(arr))
+    dout = torch.zeros(n * C.sizeof(G.TOIOutput), dtype=torch.uint8, device="cuda")
+    assert lib.b2g_time_of_impact(din.data_ptr(), n, dout.data_ptr(), None) == 0
+    torch.cuda.synchronize()
+    got = (G.TOIOutput * n).from_buffer(bytearray(dout.cpu().numpy().tobytes()))
+    want = (G.TOIOutput * n)()
+    orc.orc_time_of_impact(arr, n, want)
+    assert bytes(got) == bytes(want)
+    states = np.array([o.state for o in want])
+    assert (states == G.TOI_TOUCHING).sum() > 3000 and (states == G.TOI_SEPARATED).sum() > 1000
+    assert lib.b2g_time_of_impact(din.data_ptr(), -1, dout.data_ptr(), None) == 1  # B2G_E_INVALID_ARG
 
 
 def test_pairs_kernel_matches_oracle(lib, orc):

@@ -66,6 +66,26 @@ def test_oracle_collide_vs_golden(orc):
     assert touching > 300
 
 
+def test_oracle_toi_vs_golden(orc):
+    """b2TimeOfImpact: the oracle, with libm trig like the reference, gives the reference's states
+    and times bit for bit on random and crossing sweeps (alpha0 > 0 and tMax < 1 included)."""
+    g = np.load(GOLD / "toi.npz")
+    inputs = recs(G.TOIInput, g["inputs"])
+    n = len(inputs)
+    arr = (G.TOIInput * n)(*inputs)
+    out = (G.TOIOutput * n)()
+    orc.orc_set_libm_trig(1)
+    try:
+        orc.orc_time_of_impact(arr, n, out)
+    finally:
+        orc.orc_set_libm_trig(0)
+    states = np.array([o.state for o in out], np.int32)
+    t = np.array([o.t for o in out], np.float32)
+    assert np.array_equal(states, g["states"])
+    assert np.array_equal(t.view(np.uint32), g["t"].view(np.uint32))
+    assert (g["states"] == G.TOI_TOUCHING).sum() > 300 and ((g["t"] > 0) & (g["t"] < 1)).sum() > 300
+
+
 @pytest.mark.parametrize("name", ["pyramid", "mixed", "chains", "sliders", "gears"])
 def test_oracle_replayed_step_vs_golden(orc, name):
     """One step from an exported reference state; the reference's b2Island solved the constraints
