@@ -24,6 +24,7 @@ SHAPE_CIRCLE, SHAPE_EDGE, SHAPE_POLYGON = 0, 1, 2
 JOINT_REVOLUTE, JOINT_PRISMATIC, JOINT_DISTANCE = 1, 2, 3
 POLY_HULL, POLY_BOX, POLY_BOX_ORIENTED, POLY_RAW = 0, 1, 2, 3
 SCENE_PYRAMID, SCENE_MIXED_DROP, SCENE_CHAINS, SCENE_BATCH_WORLD, SCENE_JOINTS, SCENE_SLIDERS, SCENE_GEARS = 0, 1, 2, 3, 4, 5, 6
+SCENE_BULLETS = 7
 JOINT_REVOLUTE, JOINT_PRISMATIC, JOINT_DISTANCE, JOINT_PULLEY, JOINT_MOUSE = 1, 2, 3, 4, 5
 JOINT_WHEEL, JOINT_WELD, JOINT_FRICTION, JOINT_MOTOR, JOINT_GEAR = 7, 8, 9, 11, 6
 BODY_ENABLED, BODY_FIXED_ROTATION, BODY_BULLET, BODY_AWAKE, BODY_AUTO_SLEEP = 1, 2, 4, 8, 16

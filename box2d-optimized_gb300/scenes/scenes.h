@@ -14,6 +14,7 @@
 //                  hung above a pile of circles in the same U container.
 //   BatchWorld   - one world of a batched workload: picks one of the above by seed, scaled to a
 //                  body count, with gravity and friction jittered by +-10%.
+//   Bullets      - bullets fired or thrown at boxes resting on the ground (continuous collision).
 //   (scenes_joints.h: JointZoo and SliderRigs, rigs of the other joint types.)
 //
 // Random numbers come from std::mt19937 (fully specified by the C++ standard) with a portable
@@ -331,6 +332,68 @@ inline Counts BatchWorld(b2World* world, uint32_t seed, int n) {
     if (ncircles < 0) ncircles = 0;
     return ChainsOverPile(world, nchains, links, ncircles, seed ^ 0x85ebca6bu, friction);
   }
+}
+
+// `n` lanes 16 m apart on a static edge ground. In each a dynamic box (half-extent 0.6-1.0 m)
+// rests on the ground and a bullet (b2BodyDef::bullet; a circle of radius 0.1-0.25 m in even
+// lanes, a square of half-extent 0.1-0.25 m in odd ones, density 3) flies at it: fired
+// horizontally at 25-70 m/s from 7 m away, or, in every third lane, thrown down at it at
+// 25-70 m/s from 7 m above. Continuous collision resolves the impacts.
+inline Counts Bullets(b2World* world, int n, uint32_t seed) {
+  Counts c;
+  Rng rng(seed);
+  b2BodyDef gd;
+  b2Body* ground = MakeBody(world, &gd);
+  AddEdge(ground, -20.0f, 0.0f, 16.0f * (float)n + 20.0f, 0.0f, &c);
+  for (int i = 0; i < n; ++i) {
+    const float x0 = 16.0f * (float)i;
+    const float half = rng.uni(0.6f, 1.0f);
+    b2BodyDef td;
+    td.type = b2_dynamicBody;
+    td.position.Set(x0 + 7.0f, half);
+    b2Body* target = MakeBody(world, &td);
+    b2PolygonShape box;
+    box.SetAsBox(half, half);
+    b2FixtureDef fd;
+    fd.shape = &box;
+    fd.density = 1.0f;
+    fd.friction = 0.6f;
+    MakeFixture(target, &fd);
+    c.bodies++;
+    c.fixtures++;
+    const float speed = rng.uni(25.0f, 70.0f);
+    const float lateral = rng.uni(-0.4f, 0.4f);
+    const float spin = rng.uni(-5.0f, 5.0f);
+    const float size = rng.uni(0.1f, 0.25f);
+    b2BodyDef bd;
+    bd.type = b2_dynamicBody;
+    bd.bullet = true;
+    if (i % 3 == 2) {
+      bd.position.Set(x0 + 7.0f + lateral, 2.0f * half + 7.0f);
+      bd.linearVelocity.Set(0.0f, -speed);
+    } else {
+      bd.position.Set(x0, half + lateral);
+      bd.linearVelocity.Set(speed, 0.0f);
+    }
+    bd.angularVelocity = spin;
+    b2Body* bullet = MakeBody(world, &bd);
+    b2FixtureDef bf;
+    bf.density = 3.0f;
+    bf.friction = 0.4f;
+    b2CircleShape circle;
+    b2PolygonShape square;
+    if (i % 2 == 0) {
+      circle.m_radius = size;
+      bf.shape = &circle;
+    } else {
+      square.SetAsBox(size, size);
+      bf.shape = &square;
+    }
+    MakeFixture(bullet, &bf);
+    c.bodies++;
+    c.fixtures++;
+  }
+  return c;
 }
 
 }  // namespace b2scenes

@@ -588,7 +588,7 @@ B2G_API int b2g_pairs_static(const float* d_aabbs, int32_t n, uint64_t* d_pairs,
 /* Builds one of the seeded benchmark scenes into `world` through the b2World facade calls
  * (box2d-optimized_gb300/scenes/scenes.h). kind: 0 pyramid(rows=n, density=p0, friction=p1),
  * 1 mixed drop(n bodies), 2 chains over pile(n chains, 20 links, p0 circles),
- * 3 batch world(n bodies), 4 joint zoo(n rigs), 5 slider rigs(n rigs), 6 gear rigs(n rigs), with `seed`. counts[3] = bodies, fixtures, joints. */
+ * 3 batch world(n bodies), 4 joint zoo(n rigs), 5 slider rigs(n rigs), 6 gear rigs(n rigs), 7 bullets(n lanes), with `seed`. counts[3] = bodies, fixtures, joints. */
 #define B2G_SCENE_PYRAMID 0
 #define B2G_SCENE_MIXED_DROP 1
 #define B2G_SCENE_CHAINS 2
@@ -596,6 +596,7 @@ B2G_API int b2g_pairs_static(const float* d_aabbs, int32_t n, uint64_t* d_pairs,
 #define B2G_SCENE_JOINTS 4      /* rigs of weld, wheel, motor, friction, mouse and pulley joints */
 #define B2G_SCENE_SLIDERS 5     /* rigs of distance and prismatic joints (n rigs) */
 #define B2G_SCENE_GEARS 6       /* rigs of gear joints (n rigs) */
+#define B2G_SCENE_BULLETS 7     /* bullets fired at boxes (n lanes), for continuous collision */
 B2G_API int b2g_scene_build(b2g_batch* b, int32_t world, int32_t kind, uint32_t seed, int32_t n,
                             float p0, float p1, int32_t* counts);
 B2G_API int b2g_batch_world_params(uint32_t seed, int32_t* n_bodies, float* gx, float* gy);

@@ -937,6 +937,8 @@ struct Body {
   int type;
   uint32_t flags;
   float sleepTime = 0.0f;
+  V2 c0;                       // b2Sweep::c0, a0, alpha0: the centre and angle at alpha0
+  float a0 = 0.0f, alpha0 = 0.0f;
   bool awake() const { return (flags & B2G_BODY_AWAKE) != 0; }
 };
 
@@ -1040,6 +1042,8 @@ struct World {
   std::vector<Fixture> fixtures;
   std::vector<Joint> joints;
   std::vector<Contact> contacts;           // sorted by key
+  bool continuous = false;                 // b2World::SetContinuousPhysics
+  std::vector<AABB> aabb;                  // per fixture: its box at the last pair update
   std::vector<uint64_t> noCollide;         // sorted body pairs joined by collideConnected=false joints
   // last step's solver order record
   std::vector<int> contactColor;           // per contact (-1 not solved)
@@ -1185,6 +1189,7 @@ static void updatePairs(World* w) {
   for (int i = 0; i < nf; ++i) bb[i] = computeAABB(w->fixtures[i].shape, w->bodies[w->fixtures[i].body].xf);
   std::vector<uint64_t> pairs;
   findPairs(*w, bb, &pairs);
+  w->aabb = bb;
   std::vector<Contact> next;
   next.reserve(pairs.size());
   std::vector<char> kept(w->contacts.size(), 0);
@@ -1330,7 +1335,7 @@ static bool testOverlap(const Shape& A, const Xf& xfA, const Shape& B, const Xf&
 // b2Distance with a simplex cache (src/collision/b2_distance.cpp:86-135, 432-579) and the
 // separating-axis function b2SeparationFunction (b2_time_of_impact.cpp:35-251).
 struct Sweep { V2 localCenter, c0, c; float a0, a, alpha0; };
-// b2Sweep::GetTransform / Advance / Normalize (include/box2d/b2_math.h:707-733)
+// b2Sweep::GetTransform / Normalize (include/box2d/b2_math.h:707-733; Advance below on bodies)
 static Xf sweepTransform(const Sweep& s, float beta) {
   Xf xf;
   xf.p = (1.0f - beta) * s.c0 + beta * s.c;
@@ -1338,12 +1343,6 @@ static Xf sweepTransform(const Sweep& s, float beta) {
   xf.q = rotOf(angle);
   subFrom(xf.p, mul(xf.q, s.localCenter));
   return xf;
-}
-static void sweepAdvance(Sweep& s, float alpha) {
-  float beta = (alpha - s.alpha0) / (1.0f - s.alpha0);
-  addTo(s.c0, beta * (s.c - s.c0));
-  s.a0 += beta * (s.a - s.a0);
-  s.alpha0 = alpha;
 }
 static void sweepNormalize(Sweep& s) {
   float twoPi = 2.0f * kPi;
@@ -3067,6 +3066,356 @@ static void buildIslands(const World& w, std::vector<int>* label, std::vector<ch
 // One b2World::Step (src/dynamics/b2_world.cpp:1108-1171) with CCD off. Sleep-mode worlds
 // (sleeping allowed, or sleepers present) solve only islands holding an awake body, iterate
 // positions per island with the island's own early exit, and run the island sleep timers.
+// ---- continuous collision: b2World::SolveTOI (src/dynamics/b2_world.cpp:859-1106) with the
+// min-heap of contact times of impact (b2TOIMinHeap, :671-850), b2Contact::CalculateTOI
+// (src/dynamics/b2_contact.cpp:212-280) and b2Island::SolveTOI (src/dynamics/b2_island.cpp:486-619).
+// Order: the heap is built over the contacts in list order, and a body's contacts are visited in
+// list order. Inside the event loop a moved body's existing contacts are kept or dropped by the
+// overlap of their stored boxes (b2BroadPhase::UpdateNoRebuild + Query); pairs that begin to
+// overlap there become contacts at the pair update that follows the loop.
+static void advanceSweep(Body& b, float alpha) {
+  float beta = (alpha - b.alpha0) / (1.0f - b.alpha0);
+  addTo(b.c0, beta * (b.c - b.c0));
+  b.a0 += beta * (b.a - b.a0);
+  b.alpha0 = alpha;
+}
+// b2Body::Advance (include/box2d/b2_body.h:963-971)
+static void advanceBody(Body& b, float alpha) {
+  advanceSweep(b, alpha);
+  b.c = b.c0;
+  b.a = b.a0;
+  b.xf.q = rotOf(b.a);
+  b.xf.p = b.c - mul(b.xf.q, b.localCenter);
+}
+static void syncTransform(Body& b) {
+  b.xf.q = rotOf(b.a);
+  b.xf.p = b.c - mul(b.xf.q, b.localCenter);
+}
+static Sweep sweepOfBody(const Body& b) {
+  Sweep s;
+  s.localCenter = b.localCenter; s.c0 = b.c0; s.c = b.c; s.a0 = b.a0; s.a = b.a; s.alpha0 = b.alpha0;
+  return s;
+}
+static bool isBullet(const Body& b) { return (b.flags & B2G_BODY_BULLET) != 0; }
+
+static float calculateTOI(World* w, int ci) {
+  Contact& c = w->contacts[ci];
+  const Fixture& fa = w->fixtures[c.fA];
+  const Fixture& fb = w->fixtures[c.fB];
+  if (fa.sensor || fb.sensor || !(c.flags & B2G_CONTACT_ENABLED)) return 1.0f;
+  Body& A = w->bodies[fa.body];
+  Body& B = w->bodies[fb.body];
+  bool active;
+  if (w->sleepMode()) active = (A.awake() && A.type != 0) && (B.awake() && B.type != 0);
+  else active = A.type != 0 && B.type != 0;
+  if (!active) return 1.0f;
+  const bool collideA = isBullet(A) || A.type != 2;
+  const bool collideB = isBullet(B) || B.type != 2;
+  if (!collideA && !collideB) return 1.0f;
+  float alpha0 = A.alpha0;
+  if (A.alpha0 < B.alpha0) {
+    alpha0 = B.alpha0;
+    advanceSweep(A, alpha0);
+  } else if (B.alpha0 < A.alpha0) {
+    alpha0 = A.alpha0;
+    advanceSweep(B, alpha0);
+  }
+  float t;
+  int state = timeOfImpact(fa.shape, fb.shape, sweepOfBody(A), sweepOfBody(B), 1.0f, &t);
+  return state == B2G_TOI_TOUCHING ? bmin(alpha0 + (1.0f - alpha0) * t, 1.0f) : 1.0f;
+}
+
+struct ToiHeap {
+  struct Node { float toi; int count; int c; };
+  World* w;
+  std::vector<Node> h;
+  std::vector<int> pos;  // per contact: its node, -1 when not in the heap
+  void swapNodes(int i, int j) {
+    std::swap(pos[h[i].c], pos[h[j].c]);
+    std::swap(h[i], h[j]);
+  }
+  void down(int i) {
+    const int n = (int)h.size();
+    for (;;) {
+      int m = i, l = 2 * i + 1, r = 2 * i + 2;
+      if (l < n && h[l].toi < h[m].toi) m = l;
+      if (r < n && h[r].toi < h[m].toi) m = r;
+      if (m == i) return;
+      swapNodes(i, m);
+      i = m;
+    }
+  }
+  void up(int i) {
+    while (i > 0 && h[i].toi < h[(i - 1) / 2].toi) {
+      swapNodes(i, (i - 1) / 2);
+      i = (i - 1) / 2;
+    }
+  }
+  void setKey(int i, float toi) {
+    const bool u = toi < h[i].toi, d = toi > h[i].toi;
+    h[i].toi = toi;
+    if (u) up(i);
+    else if (d) down(i);
+  }
+  void update(int c) {
+    const int i = pos[c];
+    setKey(i, h[i].count > 8 ? 1.0f : calculateTOI(w, c));  // b2_maxSubSteps
+  }
+  void insert(int c) {
+    float toi = calculateTOI(w, c);
+    if (toi < 1.0f) {
+      h.push_back({toi, 0, c});
+      pos[c] = (int)h.size() - 1;
+      up((int)h.size() - 1);
+    }
+  }
+};
+
+// b2ContactSolver::SolveTOIPositionConstraints (src/dynamics/b2_contact_solver.cpp:790-878) for
+// one constraint: only the two bodies of the impact move.
+static float solveTOIPositionOne(const PC& pc, std::vector<SolverBody>& sb, int toiA, int toiB) {
+  float minSeparation = 0.0f;
+  float mA = 0.0f, iA = 0.0f, mB = 0.0f, iB = 0.0f;
+  if (pc.indexA == toiA || pc.indexA == toiB) { mA = pc.invMassA; iA = pc.invIA; }
+  if (pc.indexB == toiA || pc.indexB == toiB) { mB = pc.invMassB; iB = pc.invIB; }
+  V2 cA = sb[pc.indexA].c; float aA = sb[pc.indexA].a;
+  V2 cB = sb[pc.indexB].c; float aB = sb[pc.indexB].a;
+  for (int j = 0; j < pc.pointCount; ++j) {
+    Xf xfA, xfB;
+    xfA.q = rotOf(aA);
+    xfB.q = rotOf(aB);
+    xfA.p = cA - mul(xfA.q, pc.localCenterA);
+    xfB.p = cB - mul(xfB.q, pc.localCenterB);
+    V2 normal, point;
+    float separation;
+    if (pc.type == 0) {
+      V2 pointA = mul(xfA, pc.localPoint);
+      V2 pointB = mul(xfB, pc.localPoints[0]);
+      normal = pointB - pointA;
+      normalize(normal);
+      point = 0.5f * (pointA + pointB);
+      separation = (dot(pointB - pointA, normal) - pc.radiusA) - pc.radiusB;
+    } else if (pc.type == 1) {
+      normal = mul(xfA.q, pc.localNormal);
+      V2 clipPoint = mul(xfB, pc.localPoints[j]);
+      separation = (dot(clipPoint - mul(xfA, pc.localPoint), normal) - pc.radiusA) - pc.radiusB;
+      point = clipPoint;
+    } else {
+      normal = mul(xfB.q, pc.localNormal);
+      V2 clipPoint = mul(xfA, pc.localPoints[j]);
+      separation = (dot(clipPoint - mul(xfB, pc.localPoint), normal) - pc.radiusA) - pc.radiusB;
+      point = clipPoint;
+      normal = -normal;
+    }
+    V2 rA = point - cA, rB = point - cB;
+    minSeparation = bmin(minSeparation, separation);
+    float C = bclamp(0.75f * (separation + kLinearSlop), -kMaxLinearCorrection, 0.0f);  // b2_toiBaumgarte
+    float rnA = cross(rA, normal), rnB = cross(rB, normal);
+    float K = mA + mB + iA * rnA * rnA + iB * rnB * rnB;
+    float impulse = K > 0.0f ? -C / K : 0.0f;
+    V2 P = impulse * normal;
+    subFrom(cA, mA * P);
+    aA -= iA * cross(rA, P);
+    addTo(cB, mB * P);
+    aB += iB * cross(rB, P);
+  }
+  sb[pc.indexA].c = cA; sb[pc.indexA].a = aA;
+  sb[pc.indexB].c = cB; sb[pc.indexB].a = aB;
+  return minSeparation;
+}
+
+static void solveTOI(World* w, const Step& step) {
+  const int nc = (int)w->contacts.size();
+  if (nc == 0) return;
+  const bool sleepMode = w->sleepMode();
+  const int nb = (int)w->bodies.size();
+  std::vector<char> bodyIsland(nb, 0), contactIsland(nc, 0), persist(nc, 1);
+  for (Body& b : w->bodies) b.alpha0 = 0.0f;
+  ToiHeap heap;
+  heap.w = w;
+  heap.pos.assign(nc, -1);
+  for (int i = 0; i < nc; ++i) {
+    if (!(w->contacts[i].flags & B2G_CONTACT_ENABLED)) continue;
+    float toi = calculateTOI(w, i);
+    if (toi < 1.0f) heap.h.push_back({toi, 0, i});
+  }
+  for (int i = (int)heap.h.size() / 2 - 1; i >= 0; --i) heap.down(i);
+  for (int i = 0; i < (int)heap.h.size(); ++i) heap.pos[heap.h[i].c] = i;
+  auto bodyOf = [&](int ci, int side) { return w->fixtures[side ? w->contacts[ci].fB : w->contacts[ci].fA].body; };
+  auto wakeOnChange = [&](int ci) {
+    if (updateContact(w, w->contacts[ci]) && sleepMode) {
+      setAwake(w->bodies[bodyOf(ci, 0)], true);
+      setAwake(w->bodies[bodyOf(ci, 1)], true);
+    }
+  };
+  auto awake = [&](int b) { if (sleepMode) setAwake(w->bodies[b], true); };
+  while (!heap.h.empty()) {
+    ToiHeap::Node& mn = heap.h[0];
+    ++mn.count;
+    const int mc = mn.c;
+    const float minAlpha = mn.toi;
+    if (1.0f - 10.0f * kEpsilon < minAlpha) break;
+    const int ia = bodyOf(mc, 0), ib = bodyOf(mc, 1);
+    Body& bA = w->bodies[ia];
+    Body& bB = w->bodies[ib];
+    const Body backA = bA, backB = bB;
+    advanceBody(bA, minAlpha);
+    advanceBody(bB, minAlpha);
+    wakeOnChange(mc);
+    heap.update(mc);
+    Contact& cm = w->contacts[mc];
+    if (!(cm.flags & B2G_CONTACT_ENABLED) || !(cm.flags & B2G_CONTACT_TOUCHING)) {
+      cm.flags &= ~B2G_CONTACT_ENABLED;
+      bA.c0 = backA.c0; bA.c = backA.c; bA.a0 = backA.a0; bA.a = backA.a; bA.alpha0 = backA.alpha0;
+      bB.c0 = backB.c0; bB.c = backB.c; bB.a0 = backB.a0; bB.a = backB.a; bB.alpha0 = backB.alpha0;
+      syncTransform(bA);
+      syncTransform(bB);
+      heap.update(mc);
+      continue;
+    }
+    awake(ia);
+    awake(ib);
+    std::vector<int> ibodies = {ia, ib}, icontacts = {mc};
+    bodyIsland[ia] = bodyIsland[ib] = 1;
+    contactIsland[mc] = 1;
+    for (int k = 0; k < 2; ++k) {
+      const int body = k ? ib : ia;
+      if (w->bodies[body].type != 2) continue;
+      for (int ci = 0; ci < (int)w->contacts.size(); ++ci) {
+        const int ca = bodyOf(ci, 0), cb = bodyOf(ci, 1);
+        if (ca != body && cb != body) continue;
+        if ((int)ibodies.size() == 64 || (int)icontacts.size() == 32) break;  // 2 * b2_maxTOIContacts
+        if (contactIsland[ci] || !persist[ci]) continue;
+        const int other = ca == body ? cb : ca;
+        Body& ob = w->bodies[other];
+        if (ob.type == 2 && !isBullet(w->bodies[body]) && !isBullet(ob)) continue;
+        if (w->fixtures[w->contacts[ci].fA].sensor || w->fixtures[w->contacts[ci].fB].sensor) continue;
+        const Body backup = ob;
+        if (!bodyIsland[other]) advanceBody(ob, minAlpha);
+        wakeOnChange(ci);
+        const uint32_t fl = w->contacts[ci].flags;
+        if (!(fl & B2G_CONTACT_ENABLED) || !(fl & B2G_CONTACT_TOUCHING)) {
+          ob.c0 = backup.c0; ob.c = backup.c; ob.a0 = backup.a0; ob.a = backup.a; ob.alpha0 = backup.alpha0;
+          syncTransform(ob);
+          continue;
+        }
+        contactIsland[ci] = 1;
+        icontacts.push_back(ci);
+        if (bodyIsland[other]) continue;
+        bodyIsland[other] = 1;
+        if (ob.type != 0) awake(other);
+        ibodies.push_back(other);
+      }
+    }
+    // b2Island::SolveTOI
+    Step sub;
+    sub.dt = (1.0f - minAlpha) * step.dt;
+    sub.inv_dt = 1.0f / sub.dt;
+    sub.dtRatio = 1.0f;
+    sub.vi = step.vi;
+    sub.pi = 20;
+    sub.warm = false;
+    std::vector<SolverBody> sb(nb);
+    for (int b : ibodies) {
+      const Body& bd = w->bodies[b];
+      sb[b].c = bd.c; sb[b].a = bd.a; sb[b].v = bd.v; sb[b].w = bd.w;
+    }
+    std::vector<VC> vcs;
+    std::vector<PC> pcs;
+    prepareContacts(w, icontacts, sb, sub, vcs, pcs);
+    for (int it = 0; it < sub.pi; ++it) {
+      float minSep = 0.0f;
+      for (const PC& pc : pcs) minSep = bmin(minSep, solveTOIPositionOne(pc, sb, ia, ib));
+      if (minSep >= -1.5f * kLinearSlop) break;
+    }
+    bA.c0 = sb[ia].c; bA.a0 = sb[ia].a;
+    bB.c0 = sb[ib].c; bB.a0 = sb[ib].a;
+    prepareContacts(w, icontacts, sb, sub, vcs, pcs);  // InitializeVelocityConstraints at the new positions
+    for (int it = 0; it < sub.vi; ++it)
+      for (VC& vc : vcs) solveVelocityOne(vc, sb);
+    const float h = sub.dt;
+    for (int b : ibodies) {
+      V2 c = sb[b].c; float a = sb[b].a; V2 v = sb[b].v; float wv = sb[b].w;
+      V2 translation = h * v;
+      if (dot(translation, translation) > kMaxTranslationSquared) {
+        float ratio = kMaxTranslation / lengthOf(translation);
+        v.x *= ratio; v.y *= ratio;
+      }
+      float rotation = h * wv;
+      if (rotation * rotation > kMaxRotationSquared) {
+        float ratio = kMaxRotation / babs(rotation);
+        wv *= ratio;
+      }
+      addTo(c, h * v);
+      a += h * wv;
+      Body& bd = w->bodies[b];
+      bd.c = c; bd.a = a; bd.v = v; bd.w = wv;
+      syncTransform(bd);
+    }
+    if (w->recordEvents)  // b2Island::Report (src/dynamics/b2_island.cpp:621-647)
+      for (const VC& vc : vcs) {
+        const Contact& c = w->contacts[vc.contact];
+        float ni[2] = {vc.points[0].normalImpulse, vc.points[1].normalImpulse};
+        float ti[2] = {vc.points[0].tangentImpulse, vc.points[1].tangentImpulse};
+        if (vc.pointCount < 2) ni[1] = ti[1] = 0.0f;
+        recordEvent(w, B2G_EVENT_POSTSOLVE, c.fA, c.fB, nullptr, vc.pointCount, ni, ti);
+      }
+    // reset the island flags, move the proxies of the dynamic bodies, refresh their contacts' TOIs
+    for (int b : ibodies) {
+      bodyIsland[b] = 0;
+      if (w->bodies[b].type != 2) continue;
+      for (size_t f = 0; f < w->fixtures.size(); ++f)
+        if (w->fixtures[f].body == b) w->aabb[f] = computeAABB(w->fixtures[f].shape, w->bodies[b].xf);
+      for (int ci = 0; ci < (int)w->contacts.size(); ++ci) {
+        if (bodyOf(ci, 0) != b && bodyOf(ci, 1) != b) continue;
+        if (persist[ci]) {
+          if (heap.pos[ci] == -1) heap.insert(ci);
+          else heap.update(ci);
+        }
+        contactIsland[ci] = 0;
+        persist[ci] = 0;
+      }
+    }
+    // b2BroadPhase::Query with each moved fixture's box (b2ContactManager::QueryCallback): the
+    // contacts of the overlapping fixtures persist, and overlapping pairs without one get a new
+    // contact (a fixture's partners in fixture order)
+    for (int b : ibodies) {
+      if (w->bodies[b].type != 2) continue;
+      const int nf = (int)w->fixtures.size();
+      for (int f = 0; f < nf; ++f) {
+        if (w->fixtures[f].body != b) continue;
+        for (int g = 0; g < nf; ++g) {
+          if (w->fixtures[g].body == b || !overlap(w->aabb[f], w->aabb[g])) continue;
+          int found = -1;
+          for (int ci = 0; ci < (int)w->contacts.size() && found < 0; ++ci) {
+            const Contact& c = w->contacts[ci];
+            if ((c.fA == f && c.fB == g) || (c.fA == g && c.fB == f)) found = ci;
+          }
+          if (found >= 0) {
+            persist[found] = 1;
+            if (heap.pos[found] == -1) heap.insert(found);
+            continue;
+          }
+          const bool sg = w->bodies[w->fixtures[g].body].type == 0;
+          const int e = sg ? f : bmin(f, g), pp = sg ? g : bmax(f, g);
+          if (!shouldCollide(*w, e, pp)) continue;
+          if (!hasCollider(w->fixtures[e].shape.type, w->fixtures[pp].shape.type) &&
+              !hasCollider(w->fixtures[pp].shape.type, w->fixtures[e].shape.type))
+            continue;
+          w->contacts.push_back(makeContact(*w, ((uint64_t)(uint32_t)e << 32) | (uint32_t)pp));
+          contactIsland.push_back(0);
+          persist.push_back(1);
+          heap.pos.push_back(-1);
+          heap.insert((int)w->contacts.size() - 1);
+        }
+      }
+    }
+  }
+  // the contacts made inside the loop are made again, with no touching history, by the pair
+  // update that follows (b2World::Step's next FindNewContacts finds the same pairs)
+  w->contacts.resize(nc);
+}
+
 static void stepWorld(World* w, float dt, int vi, int pi) {
   if (w->newContacts) {
     updatePairs(w);
@@ -3193,6 +3542,8 @@ static void stepWorld(World* w, float dt, int vi, int pi) {
     for (int i = 0; i < nb; ++i) {
       if (w->bodies[i].type == 0 || !solved(i)) continue;
       V2 c = sb[i].c; float a = sb[i].a; V2 v = sb[i].v; float wv = sb[i].w;
+      w->bodies[i].c0 = c;  // b2Island::Solve keeps the step's start for continuous collision
+      w->bodies[i].a0 = a;
       V2 translation = h * v;
       if (dot(translation, translation) > kMaxTranslationSquared) {
         float ratio = kMaxTranslation / lengthOf(translation);
@@ -3314,6 +3665,12 @@ static void stepWorld(World* w, float dt, int vi, int pi) {
     }
     // broadphase at the end of Solve (b2_world.cpp:663-669)
     updatePairs(w);
+    // b2World::Step's SolveTOI (b2_world.cpp:1152-1156); the pair update after it stands for
+    // the proxy moves and dead-contact removal inside SolveTOI
+    if (w->continuous) {
+      solveTOI(w, st);
+      updatePairs(w);
+    }
     w->inv_dt0 = st.inv_dt;
     for (Joint& j : w->joints) {
       float F[2], T;
@@ -3498,6 +3855,7 @@ int orc_world_load(void* h, const b2g_body* bodies, int32_t nb, const b2g_fixtur
     b.force = v2(s.force[0], s.force[1]); b.torque = s.torque;
     b.type = s.type; b.flags = s.flags;
     b.sleepTime = 0.0f;
+    b.c0 = b.c; b.a0 = b.a; b.alpha0 = 0.0f;
     if (b.type != 0 && !b.awake()) w->sleepers = true;
   }
   w->fixtures.resize(nf);
@@ -3567,6 +3925,9 @@ int orc_world_load(void* h, const b2g_body* bodies, int32_t nb, const b2g_fixtur
 }
 
 // b2World::SetAllowSleeping (src/dynamics/b2_world.cpp:474-488): turning sleep off wakes every body.
+// b2World::SetContinuousPhysics
+void orc_world_set_continuous(void* h, int32_t on) { ((World*)h)->continuous = on != 0; }
+
 void orc_world_set_sleep(void* h, int32_t allow_sleep) {
   World* w = (World*)h;
   w->allowSleep = allow_sleep != 0;

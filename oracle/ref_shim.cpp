@@ -331,6 +331,7 @@ void* ref_scene_world(int32_t kind, uint32_t seed, int32_t n, float p0, float p1
   else if (kind == B2G_SCENE_JOINTS) c = b2scenes::JointZoo(rw->world, n, seed);
   else if (kind == B2G_SCENE_SLIDERS) c = b2scenes::SliderRigs(rw->world, n, seed);
   else if (kind == B2G_SCENE_GEARS) c = b2scenes::GearRigs(rw->world, n, seed);
+  else if (kind == B2G_SCENE_BULLETS) c = b2scenes::Bullets(rw->world, n, seed);
   if (counts) { counts[0] = c.bodies; counts[1] = c.fixtures; counts[2] = c.joints; }
   index_world(rw);
   return rw;
@@ -685,6 +686,7 @@ int ref_replay_step(void* h, float dt, int32_t vi, int32_t pi, const int32_t* co
     island.Solve(step, w->m_gravity, false);
     w->m_contactManager.FindNewContacts();
     w->RemoveDeadContacts();
+    if (w->m_continuousPhysics) w->SolveTOI(step);  // b2World::Step, src/dynamics/b2_world.cpp:1152-1156
     w->m_inv_dt0 = step.inv_dt;
   }
   if (w->m_clearForces) w->ClearForces();

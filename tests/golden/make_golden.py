@@ -207,10 +207,42 @@ def toi(ref, rng, n=1500):
                         t=np.array([o.t for o in out], np.float32))
 
 
+def replay_toi(ref, orc, seed=3, n=12, warm=5, steps=10, vi=8, pi=3):
+    """Consecutive steps of the bullets scene with continuous collision, each replayed by the
+    reference (b2Island::Solve in the oracle's order, then b2World::SolveTOI) from the state the
+    reference reached: per step the state before, the order and the bodies after."""
+    rw = ob.RefWorld(ref, G.SCENE_BULLETS, seed=seed, n=n, p0=0.0, p1=0.6, continuous=True)
+    rw.step(warm, vi=vi, pi=pi)
+    out = {"bodies": [], "contacts": [], "pairs": [], "after": [], "after_pairs": []}
+    fixtures = rw.fixtures()
+    orc.orc_set_libm_trig(1)
+    for _ in range(steps):
+        bodies, contacts = rw.bodies(), rw.contacts()
+        ow = ob.OracleWorld(orc, (0.0, -10.0), list(bodies), list(fixtures), [], list(contacts), inv_dt0=60.0,
+                            continuous=True)
+        ow.step(1, 1 / 60, vi, pi)
+        pairs, _ = ow.last_order()
+        arr = (C.c_int32 * max(len(pairs), 1))(*pairs)
+        assert ref.ref_replay_step(rw.h, 1 / 60, vi, pi, arr, len(pairs) // 2, (C.c_int32 * 1)(), 0) == 0
+        out["bodies"].append(rec_bytes(bodies))
+        out["contacts"].append(rec_bytes(contacts) if len(contacts) else np.zeros(0, np.uint8))
+        out["pairs"].append(np.array(pairs, np.int32))
+        out["after"].append(rec_bytes(rw.bodies()))
+        out["after_pairs"].append(np.array(sorted((min(c.fixture_a, c.fixture_b), max(c.fixture_a, c.fixture_b))
+                                                  for c in rw.contacts()), np.int32).reshape(-1))
+    orc.orc_set_libm_trig(0)
+    flat = {}
+    for k, v in out.items():
+        flat[k] = np.concatenate(v) if v else np.zeros(0)
+        flat[k + "_off"] = np.cumsum([0] + [len(x) for x in v]).astype(np.int64)
+    np.savez_compressed(HERE / "replay_bullets.npz", fixtures=rec_bytes(fixtures), vi=vi, pi=pi, **flat)
+
+
 def main():
     ref = ob.Ref()
-    if sys.argv[1:] == ["toi"]:  # the time-of-impact vectors alone
+    if sys.argv[1:] == ["toi"]:  # the continuous-collision vectors alone
         toi(ref, np.random.default_rng(20261204))
+        replay_toi(ref, ob.Oracle())
         return
     orc = ob.Oracle()
     rng = np.random.default_rng(20261203)
@@ -228,6 +260,7 @@ def main():
     measures(ref, orc, "mixed", G.SCENE_MIXED_DROP, 300, 3, 0.0, 256, 8, 3)
     measures(ref, orc, "chains", G.SCENE_CHAINS, 10, 2, 150.0, 256, 10, 4)
     toi(ref, np.random.default_rng(20261204))
+    replay_toi(ref, orc)
     print("golden vectors written to", HERE)
 
 

@@ -189,6 +189,7 @@ class Oracle:
             "orc_world_raycast": ([vp, P(f32), P(f32)], i32),
             "orc_world_query_aabb": ([vp, P(f32), P(i32), i32], i32),
             "orc_world_set_sleep": ([vp, i32], None),
+            "orc_world_set_continuous": ([vp, i32], None),
             "orc_world_flag_new_contacts": ([vp], None),
             "orc_world_sleep_times": ([vp, P(f32)], None),
             "orc_world_set_sleep_times": ([vp, P(f32)], None),
@@ -232,8 +233,9 @@ class OracleWorld:
     the oracle's own scene builder: scene = (kind, seed, n, p0, p1))."""
 
     def __init__(self, orc: Oracle, gravity, bodies=(), fixtures=(), joints=(), contacts=(),
-                 inv_dt0=0.0, scene=None):
+                 inv_dt0=0.0, scene=None, continuous=False):
         self.orc = orc
+        self._continuous = continuous
         self._raycast_fn, self._query_fn = orc.orc_world_raycast, orc.orc_world_query_aabb
         if scene is not None:
             kind, seed, n, p0, p1 = scene
@@ -242,6 +244,7 @@ class OracleWorld:
             if not self.h:
                 raise RuntimeError(f"orc_scene_world: unknown scene kind {kind}")
             self.counts = tuple(counts)
+            orc.orc_world_set_continuous(self.h, int(continuous))
             return
         self.h = orc.orc_world_new(gravity[0], gravity[1])
         nb, nf, nj, nc = len(bodies), len(fixtures), len(joints), len(contacts)
@@ -252,6 +255,7 @@ class OracleWorld:
         st = orc.orc_world_load(self.h, B, nb, F, nf, J, nj, Cc, nc, inv_dt0)
         if st != 0:
             raise RuntimeError(f"orc_world_load failed: {st}")
+        orc.orc_world_set_continuous(self.h, int(continuous))
         self._raycast_fn, self._query_fn = orc.orc_world_raycast, orc.orc_world_query_aabb
 
     def close(self):

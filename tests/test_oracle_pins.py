@@ -86,6 +86,77 @@ def test_oracle_toi_vs_golden(orc):
     assert (g["states"] == G.TOI_TOUCHING).sum() > 300 and ((g["t"] > 0) & (g["t"] < 1)).sum() > 300
 
 
+def _split(g, key, i):
+    off = g[key + "_off"]
+    return g[key][off[i]:off[i + 1]]
+
+
+def test_oracle_toi_replay_vs_golden(orc):
+    """Continuous collision: ten consecutive steps of the bullets scene, each replayed by the
+    reference (b2Island::Solve in the oracle's order, then b2World::SolveTOI); the oracle with
+    continuous collision reproduces the bodies bit for bit (libm trig like the reference) and the
+    contact set exactly, and without it differs (the impacts are resolved by SolveTOI)."""
+    g = np.load(GOLD / "replay_bullets.npz")
+    fixtures = recs(G.Fixture, g["fixtures"])
+    vi, pi = int(g["vi"]), int(g["pi"])
+    steps = len(g["bodies_off"]) - 1
+    changed = 0
+    orc.orc_set_libm_trig(1)
+    try:
+        for i in range(steps):
+            bodies, contacts = recs(G.Body, _split(g, "bodies", i)), recs(G.Contact, _split(g, "contacts", i))
+            after = bytes(np.asarray(_split(g, "after", i), np.uint8))
+            results = {}
+            for cont in (True, False):
+                ow = ob.OracleWorld(orc, (0.0, -10.0), bodies, fixtures, [], contacts, inv_dt0=60.0, continuous=cont)
+                ow.step(1, 1 / 60, vi, pi)
+                results[cont] = ow
+            ob_after = b"".join(bytes(b) for b in results[True].bodies())
+            assert [ob_after[k * C.sizeof(G.Body):k * C.sizeof(G.Body) + 40] for k in range(len(bodies))] == \
+                   [after[k * C.sizeof(G.Body):k * C.sizeof(G.Body) + 40] for k in range(len(bodies))], i
+            pairs = sorted((min(c.fixture_a, c.fixture_b), max(c.fixture_a, c.fixture_b)) for c in results[True].contacts())
+            assert np.array_equal(np.array(pairs, np.int32).reshape(-1), _split(g, "after_pairs", i)), i
+            plain = b"".join(bytes(b)[:40] for b in results[False].bodies())
+            changed += plain != b"".join(bytes(b)[:40] for b in results[True].bodies())
+    finally:
+        orc.orc_set_libm_trig(0)
+    assert changed >= 3
+
+
+@pytest.mark.parametrize("n,seed", [(12, 1), (12, 8), (30, 4)])
+def test_oracle_toi_replay_vs_reference_live(ref, orc, n, seed):
+    """b2World::SolveTOI against the oracle's restatement over 40 replayed steps of the bullets
+    scene (fired and thrown bullets, circles and squares), contacts exactly. The lanes of circle
+    bullets match bit for bit. In the lanes of square bullets a polygon-polygon contact made by
+    the pair update just before the impact takes its fixture order (which shape is A) from the
+    reference's broadphase tree, where the oracle's is canonical: the manifold's frame differs,
+    and those lanes agree to 1e-5."""
+    rw = ob.RefWorld(ref, G.SCENE_BULLETS, seed=seed, n=n, p0=0.0, p1=0.6, continuous=True)
+    fixtures = list(rw.fixtures())
+    orc.orc_set_libm_trig(1)
+    try:
+        for step in range(40):
+            ow = ob.OracleWorld(orc, (0.0, -10.0), list(rw.bodies()), fixtures, [], list(rw.contacts()),
+                                inv_dt0=60.0 if step else 0.0, continuous=True)
+            ow.step(1, 1 / 60, 8, 3)
+            pairs, _ = ow.last_order()
+            arr = (C.c_int32 * max(len(pairs), 1))(*pairs)
+            assert ref.ref_replay_step(rw.h, 1 / 60, 8, 3, arr, len(pairs) // 2, (C.c_int32 * 1)(), 0) == 0
+            rset = sorted((min(c.fixture_a, c.fixture_b), max(c.fixture_a, c.fixture_b)) for c in rw.contacts())
+            oset = sorted((min(c.fixture_a, c.fixture_b), max(c.fixture_a, c.fixture_b)) for c in ow.contacts())
+            assert rset == oset, step
+            rb, obs = list(rw.bodies()), list(ow.bodies())
+            for k in range(len(rb)):
+                circle_lane = k == 0 or ((k - 1) // 2) % 2 == 0
+                if circle_lane:
+                    assert bytes(rb[k])[:40] == bytes(obs[k])[:40], (step, k)
+                else:
+                    np.testing.assert_allclose(np.frombuffer(bytes(obs[k])[:40], np.float32),
+                                               np.frombuffer(bytes(rb[k])[:40], np.float32), rtol=1e-5, atol=1e-5)
+    finally:
+        orc.orc_set_libm_trig(0)
+
+
 @pytest.mark.parametrize("name", ["pyramid", "mixed", "chains", "sliders", "gears"])
 def test_oracle_replayed_step_vs_golden(orc, name):
     """One step from an exported reference state; the reference's b2Island solved the constraints
