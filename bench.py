@@ -291,6 +291,47 @@ def sleep_bench(lib, dev, seeds, settle, steps, cpu):
     return res
 
 
+def ccd_bench(lib, dev, n_worlds, lanes, steps, cpu):
+    """Continuous collision (b2World::SolveTOI on the device): `n_worlds` bullets worlds (`lanes`
+    bullets fired or thrown at boxes each, seeds 1..n) stepped `steps` steps from the start, when
+    the impacts happen, with continuous physics on and, for comparison, off; the TOI stage's share
+    of one more step; with `cpu`, the CPU oracle over the same worlds and window on all host
+    threads."""
+    out = {}
+    for cont in (True, False):
+        batch = G.Batch(lib, device=dev)
+        nb = 0
+        for i in range(n_worlds):
+            w = batch.add_world(0.0, -10.0)
+            batch.set_flags(w, allow_sleep=False, warm_starting=True, continuous=cont)
+            nb += batch.scene(w, G.SCENE_BULLETS, seed=i + 1, n=lanes, p0=0.0, p1=0.0)[0]
+        batch.step_timed(1, DT, VI, PI)  # upload and first contacts
+        ms = batch.step_timed(steps, DT, VI, PI)
+        batch.step(DT, VI, PI)
+        p = batch.profile()
+        out[cont] = {"ms": ms / steps, "toi_ms": p.solve_toi, "step_ms": p.step, "nb": nb}
+        batch.close()
+    nb = out[True]["nb"]
+    res = {"value": nb * steps / (out[True]["ms"] * steps / 1e3), "unit": "body-steps/s",
+           "ms_per_step": out[True]["ms"], "continuous_off_ms_per_step": out[False]["ms"],
+           "toi_stage_ms": out[True]["toi_ms"],
+           "workload": f"{n_worlds} bullets worlds of {lanes} lanes ({nb} bodies), steps 2-{steps + 1}, "
+                       "continuous physics on (eager steps: SolveTOI and a second pair update)"}
+    if cpu:
+        import oracle_bind as ob  # noqa: PLC0415 - CPU baseline leg only
+
+        threads = os.cpu_count() or 1
+        orc = ob.Oracle()
+        worlds = [ob.OracleWorld(orc, (0.0, -10.0), scene=(G.SCENE_BULLETS, i + 1, lanes, 0.0, 0.0), continuous=True)
+                  for i in range(n_worlds)]
+        hs = (C.c_void_p * len(worlds))(*[w.h for w in worlds])
+        orc.orc_worlds_step_parallel(hs, len(worlds), DT, VI, PI, 1, threads)
+        secs = orc.orc_worlds_step_parallel(hs, len(worlds), DT, VI, PI, steps, threads)
+        res["cpu_baseline"] = {"value": nb * steps / secs, "unit": "body-steps/s", "cores": threads, "kind": "port",
+                               "sample": "the same worlds and window, continuous physics on"}
+    return res
+
+
 # The single-world configurations: (name, scene kind, seed, n, p0, velocity / position
 # iterations, steps, workload).
 LARGE_CONFIGS = [
@@ -545,6 +586,11 @@ def run_ours(args, rank, world_size):
         sleep = sleep_bench(lib, dev, ss, args.sleep_settle, max(3, args.steps // 2),
                             rank == 0 and world_size == 1 and not args.no_cpu)
 
+    # continuous collision on its own workload (the batched worlds above run without it)
+    ccd = None
+    if args.ccd_worlds > 0:
+        ccd = ccd_bench(lib, dev, args.ccd_worlds, 12, 30, rank == 0 and world_size == 1 and not args.no_cpu)
+
     # per-phase breakdown: one eager (non-graph) step after the timed region
     lib.b2g_batch_set_graphs(batch.h, 0)
     batch.step(DT, VI, PI)
@@ -646,6 +692,7 @@ def run_ours(args, rank, world_size):
             "large_worlds": large,
             "queries": queries,
             "sleep": sleep,
+            "continuous": ccd,
             "clocks": clocks.summary(),
         }
     batch.close()
@@ -755,6 +802,7 @@ def main():
     ap.add_argument("--rays", type=int, default=1 << 20, help="rays of the world-query measurement (0: skip)")
     ap.add_argument("--sleep-worlds", type=int, default=256, help="worlds of the island-sleep measurement (0: skip)")
     ap.add_argument("--sleep-settle", type=int, default=480, help="steps before the island-sleep window")
+    ap.add_argument("--ccd-worlds", type=int, default=512, help="worlds of the continuous-collision measurement (0: skip)")
     ap.add_argument("--profile-window", action="store_true",
                     help="ncu case: settle --settle steps, then 2 steps inside the NVTX range 'profile'")
     ap.add_argument("--settle", type=int, default=250)

@@ -142,6 +142,10 @@ static KernelArgs make_args(Batch* b) {
   a.xf = b->xf.p; a.pos = b->pos.p; a.vel = b->vel.p; a.massd = b->massd.p; a.damp = b->damp.p;
   a.force = b->force.p; a.lc = b->lc.p; a.btype = b->btype.p; a.bworld = b->bworld.p;
   a.bstate = b->bstate.p; a.bwake = b->bwake.p; a.sl = b->sl.p; a.any_sleep = b->any_sleep ? 1 : 0;
+  if (b->step_ccd) {
+    a.sweep0 = b->sweep0.p; a.toi_hpos = b->toi_hpos.p; a.toi_cfl = b->toi_cfl.p; a.toi_heap = b->toi_heap.p;
+    a.toi_bfl = b->toi_bfl.p;
+  }
   a.any_sensor = b->any_sensor ? 1 : 0;
   a.shape = b->shape.p; a.fbody = b->fbody.p; a.fgroup = b->fgroup.p; a.fsensor = b->fsensor.p;
   a.fworld = b->fworld.p; a.frad = b->frad.p; a.ffilter = b->ffilter.p; a.fmat = b->fmat.p; a.aabb = b->aabb.p;
@@ -209,9 +213,18 @@ static void init_joint_dev(const b2g_joint_def& def, JointDev* d) {
 
 // Device world flags: the host flags without the per-step ones, plus the sleep bits.
 static int device_world_flags(const HostWorld& hw) {
-  int f = hw.flags & ~(B2G_WF_ACTIVE | B2G_WF_NEW_CONTACTS | B2G_WF_SLEEPMODE | B2G_WF_ALLOW_SLEEP);
+  int f = hw.flags & ~(B2G_WF_ACTIVE | B2G_WF_NEW_CONTACTS | B2G_WF_SLEEPMODE | B2G_WF_ALLOW_SLEEP | B2G_WF_CONTINUOUS);
   if (hw.allow_sleep || hw.sleepers) f |= B2G_WF_SLEEPMODE;
   if (hw.allow_sleep) f |= B2G_WF_ALLOW_SLEEP;
+  // SolveTOI finds times of impact only between two non-static bodies of which one is a bullet or
+  // kinematic (b2Contact::CalculateTOI, src/dynamics/b2_contact.cpp:222-246): without such a body
+  // it does nothing
+  if (hw.continuous)
+    for (const b2g_body& bd : hw.bodies)
+      if (bd.type == B2G_KINEMATIC || (bd.type == B2G_DYNAMIC && (bd.flags & B2G_BODY_BULLET))) {
+        f |= B2G_WF_CONTINUOUS;
+        break;
+      }
   return f;
 }
 
@@ -221,6 +234,7 @@ static int2 body_state(const HostWorld& hw, size_t i) {
   int fl = 0;
   if ((s.flags & B2G_BODY_AWAKE) && s.type != B2G_STATIC) fl |= B2G_BS_AWAKE;
   if (s.flags & B2G_BODY_AUTO_SLEEP) fl |= B2G_BS_AUTO_SLEEP;
+  if (s.flags & B2G_BODY_BULLET) fl |= B2G_BS_BULLET;
   float t = i < hw.body_sleep.size() ? hw.body_sleep[i] : 0.0f;
   int bits;
   memcpy(&bits, &t, sizeof(bits));
@@ -1106,6 +1120,34 @@ static double host_ms_since(std::chrono::steady_clock::time_point t0) {
 // The first half of one b2World::Step (src/dynamics/b2_world.cpp:1108-1171) for the worlds
 // selected by mask: uploads, flags, and the step's launches (or graph replay), without waiting
 // for the device; step_end waits and reads the step's counters.
+// Scratch of the SolveTOI kernel for the current layout and contact capacity.
+static int ensure_toi_scratch(Batch* b) {
+  TRY(ensure(b, b->sweep0, (size_t)std::max(b->NB, 1)));
+  TRY(ensure(b, b->toi_bfl, (size_t)std::max(b->NB, 1)));
+  TRY(ensure(b, b->toi_hpos, (size_t)std::max<int64_t>(b->ccap, 1)));
+  TRY(ensure(b, b->toi_cfl, (size_t)std::max<int64_t>(b->ccap, 1)));
+  TRY(ensure(b, b->toi_heap, (size_t)std::max<int64_t>(b->ccap, 1) + 32 * (size_t)b->NW));
+  return B2G_OK;
+}
+
+// The SolveTOI stage of a step (b2World::Step, src/dynamics/b2_world.cpp:1152-1156), after the
+// step's pair update has completed: the TOI kernel on the live list, then a second pair update
+// that moves the proxies of the bodies it moved and makes and drops their contacts (the
+// UpdateNoRebuild / Query / RemoveDeadContacts inside SolveTOI).
+static int toi_stage(Batch* b) {
+  NvtxRange range("b2g.solve_toi");
+  TRY(ensure_toi_scratch(b));  // the pair update may have grown the contact capacity
+  CUDA_TRY(b, cudaMemsetAsync(b->counters.p + 1, 0, 4 * sizeof(unsigned long long), b->stream));
+  KernelArgs a = step_args(b, b->last_dt, b->last_vi, b->last_pi);
+  cudaEventRecord(b->ev[6], b->stream);
+  launch_solve_toi(a, b->NW, b->stream);
+  CUDA_TRY(b, cudaGetLastError());
+  cudaEventRecord(b->ev[7], b->stream);
+  enqueue_broadphase(b, a, b->cur);
+  b->cur ^= 1;
+  return finish_step(b, b->cur ^ 1);
+}
+
 static int step_begin(Batch* b, float dt, int vi, int pi, const uint8_t* mask) {
   NvtxRange range("b2g.step");
   if (b->in_step) return locked(b);
@@ -1191,8 +1233,14 @@ static int step_begin(Batch* b, float dt, int vi, int pi, const uint8_t* mask) {
     b->profile.host_admit_broadphase = (float)host_ms_since(t0);
     CUDA_TRY(b, cudaMemsetAsync(b->counters.p + 1, 0, 4 * sizeof(unsigned long long), b->stream));
   }
+  // continuous collision (b2World::SolveTOI) runs eagerly after the step's pair update
+  b->step_ccd = false;
+  if (dt > 0.0f)
+    for (int w = 0; w < b->NW && !b->step_ccd; ++w)
+      b->step_ccd = (wflags[w] & B2G_WF_CONTINUOUS) && (wflags[w] & B2G_WF_ACTIVE) && !(wflags[w] & B2G_WF_RETIRED);
+  if (b->step_ccd) TRY(ensure_toi_scratch(b));
   int entry = b->cur;
-  bool graph = b->use_graphs && !need_bp && !b->events_on && all_active && dt > 0.0f;
+  bool graph = b->use_graphs && !need_bp && !b->events_on && all_active && dt > 0.0f && !b->step_ccd;
   if (graph && (!b->graph_exec[0][0] || b->graph_version != b->layout_version || b->graph_dt != dt ||
                 b->graph_vi != vi || b->graph_pi != pi))
     TRY(capture_graphs(b, dt, vi, pi));
@@ -1237,6 +1285,11 @@ static int step_end(Batch* b) {
   b->in_step = false;
   int live_before_last_bp = b->cur ^ 1;
   int st = finish_step(b, live_before_last_bp);
+  float t_toi = 0.0f;
+  if (st == B2G_OK && b->step_ccd) {
+    st = toi_stage(b);
+    cudaEventElapsedTime(&t_toi, b->ev[6], b->ev[7]);
+  }
   if (!b->step_graph) {
     float t_col = 0, t_sol = 0, t_bp = 0;
     cudaEventElapsedTime(&t_col, b->ev[0], b->ev[1]);
@@ -1249,7 +1302,7 @@ static int step_end(Batch* b) {
   float t_all = 0;
   cudaEventElapsedTime(&t_all, b->ev[0], b->ev[4]);
   b->profile.step = t_all;
-  b->profile.solve_toi = 0.0f;
+  b->profile.solve_toi = t_toi;
   b->profile.bodies = b->NB;
   b->profile.fixtures = b->NF;
   b->profile.contacts = b->NC;
@@ -1378,6 +1431,7 @@ B2G_API int b2g_batch_destroy(b2g_batch* b) {
   release(b, b->world_order); release(b, b->xf); release(b, b->pos); release(b, b->vel); release(b, b->massd);
   release(b, b->damp); release(b, b->force); release(b, b->lc); release(b, b->btype); release(b, b->bworld);
   release(b, b->bstate); release(b, b->bwake); release(b, b->sl);
+  release(b, b->sweep0); release(b, b->toi_hpos); release(b, b->toi_cfl); release(b, b->toi_heap); release(b, b->toi_bfl);
   release(b, b->shape); release(b, b->fbody); release(b, b->fgroup); release(b, b->fsensor); release(b, b->fworld);
   release(b, b->ffilter); release(b, b->fmat); release(b, b->aabb); release(b, b->joints); release(b, b->nocollide);
   for (int k = 0; k < 2; ++k) {
@@ -2705,12 +2759,18 @@ B2G_API int b2g_step_io(b2g_batch* b, float dt, int32_t vi, int32_t pi, const fl
     return st;
   }
   const int64_t n = std::min<int64_t>(cap_bodies, b->NB);
-  if (xf4_out && n > 0) {
-    // after the solve wrote the transforms; the closing broadphase only reads them
+  // after the solve wrote the transforms; the closing broadphase only reads them (a step with
+  // continuous collision moves bodies again after it: its transforms are read at the end)
+  const bool early = !b->step_ccd;
+  if (xf4_out && n > 0 && early) {
     CUDA_TRY(b, cudaStreamWaitEvent(b->io_stream, b->io_solved, 0));
     CUDA_TRY(b, cudaMemcpyAsync(xf4_out, b->xf.p, n * sizeof(float4), cudaMemcpyDeviceToHost, b->io_stream));
   }
   st = step_end(b);
+  if (xf4_out && n > 0 && !early && st == B2G_OK) {
+    CUDA_TRY(b, cudaMemcpyAsync(xf4_out, b->xf.p, n * sizeof(float4), cudaMemcpyDeviceToHost, b->stream));
+    CUDA_TRY(b, cudaStreamSynchronize(b->stream));
+  }
   CUDA_TRY(b, cudaStreamSynchronize(b->io_stream));
   if (n_out) *n_out = b->NB;
   return st;

@@ -94,10 +94,12 @@ struct VCDev {
 #define B2G_WF_FAULTED 32  // produced a non-finite state: frozen (retired) and reported
 #define B2G_WF_SLEEPMODE 64     // islands and awake flags are tracked (sleeping allowed or sleepers present)
 #define B2G_WF_ALLOW_SLEEP 128  // b2World::SetAllowSleeping(true): island sleep timers run
+#define B2G_WF_CONTINUOUS 256  // b2World::SetContinuousPhysics(true) with a bullet or kinematic body: SolveTOI runs
 
 // Body sleep state on the device (bstate.x) and island bits (sl.y).
 #define B2G_BS_AWAKE 1        // b2Body::e_awakeFlag
 #define B2G_BS_AUTO_SLEEP 2   // b2Body::e_autoSleepFlag
+#define B2G_BS_BULLET 4       // b2Body::e_bulletFlag
 #define B2G_ISL_AWAKE 1       // (at the island's root) some member was awake: the island is solved
 #define B2G_ISL_DONE 2        // (at the root) the island's position constraints were solved
 #define B2G_ISL_LINKED 4      // (own entry) the body has a contact or a joint: not an orphan
@@ -214,6 +216,13 @@ struct Batch {
   TailPack tail_pack;             // prepared upload of appended worlds
   bool in_step = false;           // between b2g_step_begin and b2g_step_end
   bool step_graph = false;        // the step in flight replays a graph
+  bool step_ccd = false;          // the step in flight runs SolveTOI (and a second pair update) in step_end
+  // continuous collision scratch (allocated once a world runs SolveTOI)
+  DBuf<float4> sweep0;            // per body: b2Sweep c0, a0, alpha0
+  DBuf<int> toi_hpos;             // per contact slot: TOI heap node
+  DBuf<uint8_t> toi_cfl;          // per contact slot: TOI island / persist flags
+  DBuf<int4> toi_heap;            // contact slots + 32 per world: TOI heap nodes
+  DBuf<uint8_t> toi_bfl;          // per body: TOI island flag
   std::chrono::steady_clock::time_point step_t0;  // host time the step in flight began
 
   DBuf<b2g_shape> shape;

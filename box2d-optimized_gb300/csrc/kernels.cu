@@ -15,6 +15,8 @@
 #include "engine.h"
 #include "dev_common.cuh"
 #include "kernels.h"
+#include "solver_dev.cuh"
+#include "toi.cuh"
 
 namespace b2g {
 
@@ -755,6 +757,526 @@ __global__ void k_commit_contacts(KernelArgs a) {
   unsigned long long total = (unsigned long long)a.poff[a.nf];
   if ((int64_t)total > a.ccap) a.counters[B2G_CNT_OVERFLOW] = total;
   else a.counters[B2G_CNT_CONTACTS] = total;
+}
+
+// ================================================================================ continuous collision
+// b2World::SolveTOI (src/dynamics/b2_world.cpp:859-1106) for one world per warp, after the
+// step's pair update: the times of impact of the world's contacts (b2Contact::CalculateTOI,
+// src/dynamics/b2_contact.cpp:212-280) in a min-heap (b2TOIMinHeap, b2_world.cpp:671-850); the
+// earliest impact advances its two bodies (b2Body::Advance), gathers the static, kinematic and
+// bullet bodies touching them into a small island that b2Island::SolveTOI
+// (src/dynamics/b2_island.cpp:486-619) solves over the rest of the step, moves the island's
+// fixture boxes, refreshes the TOIs of their contacts and queries the boxes for new contacts,
+// until no impact is left before the step's end. The lanes compute the first TOIs of all the
+// world's contacts; lane 0 runs the event loop. The heap is built in contact order, a body's
+// contacts are visited in contact order, and a moved fixture meets its partners in fixture order.
+// Contacts made inside the loop live in shared memory (at most TOI_MADE per world and step) and
+// are made again by the pair update that follows the kernel.
+#define TOI_MADE 32
+#define TOI_BODIES 64    // 2 * b2_maxTOIContacts
+#define TOI_CONTACTS 32  // b2_maxTOIContacts
+#define TOI_ISLAND 1u
+#define TOI_PERSIST 2u
+
+struct ToiMade {
+  b2g_manifold man;
+  float4 mat;
+  int2 fix;
+  uint32_t flags;
+  int hpos;
+  uint32_t fl;
+};
+struct ToiSmem {
+  VCDev vc[TOI_CONTACTS];
+  ToiMade made[TOI_MADE];
+  float4 P[TOI_BODIES], V[TOI_BODIES];
+  int ib[TOI_BODIES];
+  int ic[TOI_CONTACTS];
+};
+
+struct ToiWorld {
+  const KernelArgs& a;
+  ToiSmem& S;
+  int w, c0, nc, nmade, b0, nb, f0, nf, fo;
+  int4* heap;
+  int hn;
+  bool sleepMode;
+  int2 nocol;
+
+  __device__ ToiWorld(const KernelArgs& a_, ToiSmem& S_) : a(a_), S(S_) {}
+
+  // contact k of the world: its live slot below nc, else a contact made inside the loop
+  __device__ int2 fix(int k) const { return k < nc ? a.cfix[c0 + k] : S.made[k - nc].fix; }
+  __device__ uint32_t& flags(int k) { return k < nc ? a.cflags[c0 + k] : S.made[k - nc].flags; }
+  __device__ b2g_manifold* man(int k) { return k < nc ? &a.cman[c0 + k] : &S.made[k - nc].man; }
+  __device__ float4 mat(int k) const { return k < nc ? a.cmat[c0 + k] : S.made[k - nc].mat; }
+  __device__ int& hpos(int k) { return k < nc ? a.toi_hpos[c0 + k] : S.made[k - nc].hpos; }
+  __device__ uint32_t getFl(int k) const { return k < nc ? (uint32_t)a.toi_cfl[c0 + k] : S.made[k - nc].fl; }
+  __device__ void setFl(int k, uint32_t v) {
+    if (k < nc) a.toi_cfl[c0 + k] = (uint8_t)v;
+    else S.made[k - nc].fl = v;
+  }
+  __device__ int count() const { return nc + nmade; }
+
+  __device__ bool awake(int b) const { return (a.bstate[b].x & B2G_BS_AWAKE) != 0; }
+  __device__ bool bullet(int b) const { return (a.bstate[b].x & B2G_BS_BULLET) != 0; }
+  // SET_AWAKE_OR_NONE / b2Body::SetAwake(true): sleep-mode worlds only
+  __device__ void wake(int b) {
+    if (sleepMode && a.btype[b] != B2G_STATIC) a.bstate[b] = make_int2(a.bstate[b].x | B2G_BS_AWAKE, 0);
+  }
+
+  __device__ Sweep sweep(int b) const {
+    float4 s = a.sweep0[b], p = a.pos[b];
+    float2 l = a.lc[b];
+    Sweep o;
+    o.lc = mk(l.x, l.y);
+    o.c0 = mk(s.x, s.y);
+    o.c = mk(p.x, p.y);
+    o.a0 = s.z;
+    o.a = p.z;
+    o.alpha0 = s.w;
+    return o;
+  }
+  __device__ void advanceSweep(int b, float alpha) {
+    Sweep s = sweep(b);
+    sweepAdvance(s, alpha);
+    a.sweep0[b] = make_float4(s.c0.x, s.c0.y, s.a0, s.alpha0);
+  }
+  // b2Body::SynchronizeTransform
+  __device__ void syncXf(int b) {
+    float4 p = a.pos[b];
+    float2 l = a.lc[b];
+    Rot q = rotOf(p.z);
+    V2 o = mk(p.x, p.y) - mul(q, mk(l.x, l.y));
+    a.xf[b] = make_float4(o.x, o.y, q.s, q.c);
+  }
+  // b2Body::Advance (include/box2d/b2_body.h:963-971)
+  __device__ void advanceBody(int b, float alpha) {
+    advanceSweep(b, alpha);
+    float4 s = a.sweep0[b];
+    a.pos[b] = make_float4(s.x, s.y, s.z, 0.0f);
+    syncXf(b);
+  }
+
+  // b2Contact::CalculateTOI
+  __device__ __noinline__ float calcTOI(int k) {
+    const int2 f = fix(k);
+    if (a.fsensor[f.x] || a.fsensor[f.y] || !(flags(k) & B2G_CONTACT_ENABLED)) return 1.0f;
+    const int A = a.fbody[f.x], B = a.fbody[f.y];
+    const int tA = a.btype[A], tB = a.btype[B];
+    const bool active = sleepMode ? (awake(A) && tA != B2G_STATIC && awake(B) && tB != B2G_STATIC)
+                                  : (tA != B2G_STATIC && tB != B2G_STATIC);
+    if (!active) return 1.0f;
+    const bool collideA = bullet(A) || tA != B2G_DYNAMIC;
+    const bool collideB = bullet(B) || tB != B2G_DYNAMIC;
+    if (!collideA && !collideB) return 1.0f;
+    const float alA = a.sweep0[A].w, alB = a.sweep0[B].w;
+    float alpha0 = alA;
+    if (alA < alB) {
+      alpha0 = alB;
+      advanceSweep(A, alpha0);
+    } else if (alB < alA) {
+      alpha0 = alA;
+      advanceSweep(B, alpha0);
+    }
+    float t;
+    const int state = timeOfImpact(a.shape[f.x], a.shape[f.y], sweep(A), sweep(B), 1.0f, &t);
+    return state == B2G_TOI_TOUCHING ? fmin2(alpha0 + (1.0f - alpha0) * t, 1.0f) : 1.0f;
+  }
+
+  // b2TOIMinHeap
+  __device__ float key(int i) const { return __int_as_float(heap[i].x); }
+  __device__ void swapNodes(int i, int j) {
+    int4 x = heap[i], y = heap[j];
+    hpos(x.z) = j;
+    hpos(y.z) = i;
+    heap[i] = y;
+    heap[j] = x;
+  }
+  __device__ void down(int i) {
+    for (;;) {
+      int m = i, l = 2 * i + 1, r = 2 * i + 2;
+      if (l < hn && key(l) < key(m)) m = l;
+      if (r < hn && key(r) < key(m)) m = r;
+      if (m == i) return;
+      swapNodes(i, m);
+      i = m;
+    }
+  }
+  __device__ void up(int i) {
+    while (i > 0 && key(i) < key((i - 1) / 2)) {
+      swapNodes(i, (i - 1) / 2);
+      i = (i - 1) / 2;
+    }
+  }
+  __device__ void setKey(int i, float toi) {
+    const bool u = toi < key(i), d = toi > key(i);
+    heap[i].x = __float_as_int(toi);
+    if (u) up(i);
+    else if (d) down(i);
+  }
+  __device__ void update(int k) {
+    const int i = hpos(k);
+    setKey(i, heap[i].y > 8 ? 1.0f : calcTOI(k));  // b2_maxSubSteps
+  }
+  __device__ void insert(int k) {
+    const float toi = calcTOI(k);
+    if (toi < 1.0f) {
+      heap[hn] = make_int4(__float_as_int(toi), 0, k, 0);
+      hpos(k) = hn;
+      ++hn;
+      up(hn - 1);
+    }
+  }
+
+  // b2Contact::Update of a non-sensor contact at the bodies' current transforms; returns whether
+  // touching changed (which wakes both bodies in sleep-mode worlds)
+  __device__ bool updateContact(int k) {
+    const int2 f = fix(k);
+    uint32_t fl = flags(k);
+    const bool wasTouching = (fl & B2G_CONTACT_TOUCHING) != 0;
+    fl |= B2G_CONTACT_ENABLED;
+    b2g_manifold* mp = man(k);
+    const b2g_manifold old = *mp;
+    const int A = a.fbody[f.x], B = a.fbody[f.y];
+    Man m;
+    evaluate(&m, a.shape[f.x], ldXf(a.xf, A), a.shape[f.y], ldXf(a.xf, B));
+    const bool touching = m.pointCount > 0;
+    b2g_manifold nm;
+    nm.type = m.type;
+    nm.point_count = m.pointCount;
+    nm.local_normal[0] = m.localNormal.x; nm.local_normal[1] = m.localNormal.y;
+    nm.local_point[0] = m.localPoint.x; nm.local_point[1] = m.localPoint.y;
+    for (int j = 0; j < 2; ++j) {
+      nm.points[j].local_point[0] = m.lp[j].x;
+      nm.points[j].local_point[1] = m.lp[j].y;
+      nm.points[j].id = m.id[j];
+      nm.points[j].normal_impulse = 0.0f;
+      nm.points[j].tangent_impulse = 0.0f;
+    }
+    for (int j = 0; j < m.pointCount; ++j)
+      for (int q = 0; q < old.point_count; ++q)
+        if (old.points[q].id == nm.points[j].id) {
+          nm.points[j].normal_impulse = old.points[q].normal_impulse;
+          nm.points[j].tangent_impulse = old.points[q].tangent_impulse;
+          break;
+        }
+    *mp = nm;
+    if (touching) fl |= B2G_CONTACT_TOUCHING;
+    else fl &= ~B2G_CONTACT_TOUCHING;
+    flags(k) = fl;
+    if (a.events_on) {
+      if (!wasTouching && touching) record_event(a, B2G_EVENT_BEGIN, w, f.x - fo, f.y - fo, 0, 0, 0, 0);
+      if (wasTouching && !touching) record_event(a, B2G_EVENT_END, w, f.x - fo, f.y - fo, 0, 0, 0, 0);
+      if (touching) record_event(a, B2G_EVENT_PRESOLVE, w, f.x - fo, f.y - fo, 0, 0, 0, &old);
+    }
+    if (touching != wasTouching) {
+      a.isl_dirty[w] = 1;
+      wake(A);
+      wake(B);
+      return true;
+    }
+    return false;
+  }
+
+  __device__ int islandIndex(int b, int nbI) const {
+    for (int i = 0; i < nbI; ++i)
+      if (S.ib[i] == b) return i;
+    return 0;
+  }
+
+  // b2ContactSolver::SolveTOIPositionConstraints (src/dynamics/b2_contact_solver.cpp:790-878) for
+  // one constraint over island positions P: only island bodies 0 and 1 (the impact's) move.
+  __device__ float solveTOIPosition(const VCDev& vc) {
+    float minSeparation = 0.0f;
+    float mA = 0.0f, iA = 0.0f, mB = 0.0f, iB = 0.0f;
+    if (vc.indexA == 0 || vc.indexA == 1) { mA = vc.invMassA; iA = vc.invIA; }
+    if (vc.indexB == 0 || vc.indexB == 1) { mB = vc.invMassB; iB = vc.invIB; }
+    V2 lcA = ld2(vc.localCenterA), lcB = ld2(vc.localCenterB);
+    float4 pa = S.P[vc.indexA], pb = S.P[vc.indexB];
+    V2 cA = mk(pa.x, pa.y), cB = mk(pb.x, pb.y);
+    float aA = pa.z, aB = pb.z;
+    for (int j = 0; j < vc.pcPointCount; ++j) {
+      Xf xfA, xfB;
+      xfA.q = rotOf(aA);
+      xfB.q = rotOf(aB);
+      xfA.p = cA - mul(xfA.q, lcA);
+      xfB.p = cB - mul(xfB.q, lcB);
+      V2 normal, point;
+      float separation;
+      if (vc.type == B2G_MANIFOLD_CIRCLES) {
+        V2 pointA = mul(xfA, ld2(vc.localPoint));
+        V2 pointB = mul(xfB, ld2(vc.localPoints[0]));
+        normal = pointB - pointA;
+        normalize(normal);
+        point = 0.5f * (pointA + pointB);
+        separation = (dot(pointB - pointA, normal) - vc.radiusA) - vc.radiusB;
+      } else if (vc.type == B2G_MANIFOLD_FACE_A) {
+        normal = mul(xfA.q, ld2(vc.localNormal));
+        V2 clipPoint = mul(xfB, ld2(vc.localPoints[j]));
+        separation = (dot(clipPoint - mul(xfA, ld2(vc.localPoint)), normal) - vc.radiusA) - vc.radiusB;
+        point = clipPoint;
+      } else {
+        normal = mul(xfB.q, ld2(vc.localNormal));
+        V2 clipPoint = mul(xfA, ld2(vc.localPoints[j]));
+        separation = (dot(clipPoint - mul(xfB, ld2(vc.localPoint)), normal) - vc.radiusA) - vc.radiusB;
+        point = clipPoint;
+        normal = -normal;
+      }
+      V2 rA = point - cA, rB = point - cB;
+      minSeparation = fmin2(minSeparation, separation);
+      float C = fclamp(0.75f * (separation + B2G_LINEAR_SLOP), -B2G_MAX_LINEAR_CORRECTION, 0.0f);  // b2_toiBaumgarte
+      float rnA = cross(rA, normal), rnB = cross(rB, normal);
+      float K = mA + mB + iA * rnA * rnA + iB * rnB * rnB;
+      float impulse = K > 0.0f ? -C / K : 0.0f;
+      V2 P = impulse * normal;
+      subFrom(cA, mA * P);
+      aA -= iA * cross(rA, P);
+      addTo(cB, mB * P);
+      aB += iB * cross(rB, P);
+    }
+    S.P[vc.indexA] = make_float4(cA.x, cA.y, aA, 0.0f);
+    S.P[vc.indexB] = make_float4(cB.x, cB.y, aB, 0.0f);
+    return minSeparation;
+  }
+
+  __device__ void prepare(int nbI, int ncI) {
+    for (int j = 0; j < ncI; ++j) {
+      const int k = S.ic[j];
+      const int2 f = fix(k);
+      const int A = a.fbody[f.x], B = a.fbody[f.y];
+      const int ia = islandIndex(A, nbI), ib = islandIndex(B, nbI);
+      prepareContact(S.vc[j], *man(k), mat(k), a.frad[f.x], a.frad[f.y], ia, ib, a.massd[A], a.massd[B], a.lc[A],
+                     a.lc[B], S.P[ia], S.V[ia], S.P[ib], S.V[ib], 1.0f, false, k);
+    }
+  }
+
+  // b2Island::SolveTOI over the island's bodies S.ib[0, nbI) and contacts S.ic[0, ncI)
+  __device__ void solveIsland(int nbI, int ncI, float minAlpha) {
+    const float h = (1.0f - minAlpha) * a.dt;
+    for (int i = 0; i < nbI; ++i) {
+      S.P[i] = a.pos[S.ib[i]];
+      S.V[i] = a.vel[S.ib[i]];
+    }
+    prepare(nbI, ncI);
+    for (int it = 0; it < 20; ++it) {  // b2TimeStep::positionIterations of the sub-step
+      float minSep = 0.0f;
+      for (int j = 0; j < ncI; ++j) minSep = fmin2(minSep, solveTOIPosition(S.vc[j]));
+      if (minSep >= -1.5f * B2G_LINEAR_SLOP) break;
+    }
+    for (int k = 0; k < 2; ++k) {
+      float4 s = a.sweep0[S.ib[k]];
+      a.sweep0[S.ib[k]] = make_float4(S.P[k].x, S.P[k].y, S.P[k].z, s.w);
+    }
+    prepare(nbI, ncI);  // InitializeVelocityConstraints at the corrected positions
+    for (int it = 0; it < a.vi; ++it)
+      for (int j = 0; j < ncI; ++j) solveContactVelocity(S.vc[j], S.V);
+    for (int i = 0; i < nbI; ++i) {
+      V2 c = mk(S.P[i].x, S.P[i].y), v = mk(S.V[i].x, S.V[i].y);
+      float an = S.P[i].z, wv = S.V[i].z;
+      V2 translation = h * v;
+      if (dot(translation, translation) > B2G_MAX_TRANSLATION_SQ) {
+        float ratio = B2G_MAX_TRANSLATION / lengthOf(translation);
+        v.x *= ratio;
+        v.y *= ratio;
+      }
+      float rotation = h * wv;
+      if (rotation * rotation > B2G_MAX_ROTATION_SQ) {
+        float ratio = B2G_MAX_ROTATION / fabs2(rotation);
+        wv *= ratio;
+      }
+      addTo(c, h * v);
+      an += h * wv;
+      const int b = S.ib[i];
+      a.pos[b] = make_float4(c.x, c.y, an, 0.0f);
+      a.vel[b] = make_float4(v.x, v.y, wv, 0.0f);
+      syncXf(b);
+    }
+    if (a.events_on)  // b2Island::Report (src/dynamics/b2_island.cpp:621-647)
+      for (int j = 0; j < ncI; ++j) {
+        const VCDev& vc = S.vc[j];
+        const int2 f = fix(S.ic[j]);
+        float ni[2] = {vc.normalImpulse[0], vc.pointCount > 1 ? vc.normalImpulse[1] : 0.0f};
+        float ti[2] = {vc.tangentImpulse[0], vc.pointCount > 1 ? vc.tangentImpulse[1] : 0.0f};
+        record_event(a, B2G_EVENT_POSTSOLVE, w, f.x - fo, f.y - fo, vc.pointCount, ni, ti, 0);
+      }
+  }
+
+  __device__ void run() {
+    while (hn > 0) {
+      heap[0].y += 1;
+      const int mc = heap[0].z;
+      const float minAlpha = key(0);
+      if (1.0f - 10.0f * B2G_EPSILON < minAlpha) break;
+      const int2 mf = fix(mc);
+      const int ia = a.fbody[mf.x], ib = a.fbody[mf.y];
+      const float4 sA = a.sweep0[ia], pA = a.pos[ia], sB = a.sweep0[ib], pB = a.pos[ib];
+      advanceBody(ia, minAlpha);
+      advanceBody(ib, minAlpha);
+      updateContact(mc);
+      update(mc);
+      if (!(flags(mc) & B2G_CONTACT_ENABLED) || !(flags(mc) & B2G_CONTACT_TOUCHING)) {
+        flags(mc) &= ~B2G_CONTACT_ENABLED;
+        a.sweep0[ia] = sA; a.pos[ia] = pA;
+        a.sweep0[ib] = sB; a.pos[ib] = pB;
+        syncXf(ia);
+        syncXf(ib);
+        update(mc);
+        continue;
+      }
+      wake(ia);
+      wake(ib);
+      int nbI = 2, ncI = 1;
+      S.ib[0] = ia;
+      S.ib[1] = ib;
+      S.ic[0] = mc;
+      a.toi_bfl[ia] = 1;
+      a.toi_bfl[ib] = 1;
+      setFl(mc, getFl(mc) | TOI_ISLAND);
+      for (int side = 0; side < 2; ++side) {
+        const int body = side ? ib : ia;
+        if (a.btype[body] != B2G_DYNAMIC) continue;
+        for (int ci = 0; ci < count(); ++ci) {
+          const int2 f = fix(ci);
+          const int ca = a.fbody[f.x], cb = a.fbody[f.y];
+          if (ca != body && cb != body) continue;
+          if (nbI == TOI_BODIES || ncI == TOI_CONTACTS) break;
+          const uint32_t cf = getFl(ci);
+          if ((cf & TOI_ISLAND) || !(cf & TOI_PERSIST)) continue;
+          const int other = ca == body ? cb : ca;
+          if (a.btype[other] == B2G_DYNAMIC && !bullet(body) && !bullet(other)) continue;
+          if (a.fsensor[f.x] || a.fsensor[f.y]) continue;
+          const float4 so = a.sweep0[other], po = a.pos[other];
+          if (!a.toi_bfl[other]) advanceBody(other, minAlpha);
+          updateContact(ci);
+          const uint32_t fl = flags(ci);
+          if (!(fl & B2G_CONTACT_ENABLED) || !(fl & B2G_CONTACT_TOUCHING)) {
+            a.sweep0[other] = so;
+            a.pos[other] = po;
+            syncXf(other);
+            continue;
+          }
+          setFl(ci, cf | TOI_ISLAND);
+          S.ic[ncI++] = ci;
+          if (a.toi_bfl[other]) continue;
+          a.toi_bfl[other] = 1;
+          wake(other);
+          S.ib[nbI++] = other;
+        }
+      }
+      solveIsland(nbI, ncI, minAlpha);
+      // reset the island flags, move the dynamic bodies' fixture boxes, refresh their contacts' TOIs
+      for (int i = 0; i < nbI; ++i) {
+        const int b = S.ib[i];
+        a.toi_bfl[b] = 0;
+        if (a.btype[b] != B2G_DYNAMIC) continue;
+        for (int f = f0; f < f0 + nf; ++f)
+          if (a.fbody[f] == b) {
+            AABB bb = shapeAABB(a.shape[f], ldXf(a.xf, b));
+            a.aabb[f] = make_float4(bb.lo.x, bb.lo.y, bb.hi.x, bb.hi.y);
+          }
+        for (int ci = 0; ci < count(); ++ci) {
+          const int2 f = fix(ci);
+          if (a.fbody[f.x] != b && a.fbody[f.y] != b) continue;
+          if (getFl(ci) & TOI_PERSIST) {
+            if (hpos(ci) == -1) insert(ci);
+            else update(ci);
+          }
+          setFl(ci, 0);
+        }
+      }
+      // b2BroadPhase::Query with each moved fixture's box (b2ContactManager::QueryCallback)
+      for (int i = 0; i < nbI; ++i) {
+        const int b = S.ib[i];
+        if (a.btype[b] != B2G_DYNAMIC) continue;
+        for (int f = f0; f < f0 + nf; ++f) {
+          if (a.fbody[f] != b) continue;
+          const float4 fb = a.aabb[f];
+          for (int g = f0; g < f0 + nf; ++g) {
+            if (a.fbody[g] == b || !aabb_overlap4(fb, a.aabb[g])) continue;
+            int found = -1;
+            for (int ci = 0; ci < count() && found < 0; ++ci) {
+              const int2 cf = fix(ci);
+              if ((cf.x == f && cf.y == g) || (cf.x == g && cf.y == f)) found = ci;
+            }
+            if (found >= 0) {
+              setFl(found, getFl(found) | TOI_PERSIST);
+              if (hpos(found) == -1) insert(found);
+              continue;
+            }
+            const bool sg = a.btype[a.fbody[g]] == B2G_STATIC;
+            const int e = sg ? f : min(f, g), p = sg ? g : max(f, g);
+            if (!accept_leaves(a, leaf_attr(e, a.fattr[e]), leaf_attr(p, a.fattr[p]), nocol)) continue;
+            if (nmade == TOI_MADE) continue;
+            ToiMade& m = S.made[nmade];
+            int fa = e, fb2 = p;
+            if (!hasCollider(a.shape[e].type, a.shape[p].type)) { fa = p; fb2 = e; }
+            const float4 ma = a.fmat[fa], mb = a.fmat[fb2];
+            m.fix = make_int2(fa, fb2);
+            m.flags = B2G_CONTACT_ENABLED;
+            m.mat = make_float4(sqrtf(ma.x * mb.x), ma.y > mb.y ? ma.y : mb.y, ma.z < mb.z ? ma.z : mb.z, 0.0f);
+            memset(&m.man, 0, sizeof(m.man));
+            m.hpos = -1;
+            m.fl = TOI_PERSIST;
+            ++nmade;
+            insert(nc + nmade - 1);
+          }
+        }
+      }
+    }
+  }
+};
+
+__global__ void __launch_bounds__(32) k_solve_toi(KernelArgs a) {
+  __shared__ ToiSmem S;
+  const int w = blockIdx.x;
+  const int wf = a.wflags[w];
+  if (!(wf & B2G_WF_ACTIVE) || !(wf & B2G_WF_CONTINUOUS) || (wf & B2G_WF_RETIRED)) return;
+  if (a.counters[B2G_CNT_OVERFLOW]) return;  // the pair update was skipped: no live list to work on
+  const int lane = threadIdx.x;
+  ToiWorld T(a, S);
+  const int4 wb = a.wb[w];
+  const int2 wc = a.wc[w];
+  const int4 wj = a.wj[w];
+  T.w = w;
+  T.c0 = wc.x;
+  T.nc = wc.y;
+  T.nmade = 0;
+  T.b0 = wb.x;
+  T.nb = wb.y;
+  T.f0 = wb.z;
+  T.nf = wb.w;
+  T.fo = wb.z;
+  T.heap = a.toi_heap + wc.x + (int64_t)TOI_MADE * w;
+  T.hn = 0;
+  T.sleepMode = (wf & B2G_WF_SLEEPMODE) != 0;
+  T.nocol = make_int2(wj.z, wj.w);
+  if (T.nc == 0) return;
+  for (int i = lane; i < T.nb; i += 32) {
+    a.sweep0[T.b0 + i].w = 0.0f;
+    a.toi_bfl[T.b0 + i] = 0;
+  }
+  __syncwarp();
+  // the contacts' first TOIs (no sweep is advanced here: every alpha0 is 0)
+  for (int k = lane; k < T.nc; k += 32) {
+    a.toi_cfl[T.c0 + k] = (uint8_t)TOI_PERSIST;
+    const float toi = (a.cflags[T.c0 + k] & B2G_CONTACT_ENABLED) ? T.calcTOI(k) : 1.0f;
+    a.toi_hpos[T.c0 + k] = __float_as_int(toi);
+  }
+  __syncwarp();
+  if (lane != 0) return;
+  for (int k = 0; k < T.nc; ++k) {
+    const float toi = __int_as_float(a.toi_hpos[T.c0 + k]);
+    a.toi_hpos[T.c0 + k] = -1;
+    if (toi < 1.0f) T.heap[T.hn++] = make_int4(__float_as_int(toi), 0, k, 0);
+  }
+  for (int i = T.hn / 2 - 1; i >= 0; --i) T.down(i);
+  for (int i = 0; i < T.hn; ++i) a.toi_hpos[T.c0 + T.heap[i].z] = i;
+  T.run();
+}
+
+void launch_solve_toi(const KernelArgs& a, int nw, cudaStream_t s) {
+  if (nw > 0) k_solve_toi<<<nw, 32, 0, s>>>(a);
 }
 
 // ================================================================================ standalone

@@ -127,6 +127,13 @@ struct KernelArgs {
   uint8_t* jready;
   int* ncolors;                   // per world: contact colours, joint colours, solver contacts, slot base
 
+  // continuous collision (null unless a world runs SolveTOI)
+  float4* sweep0;                 // per body: b2Sweep c0.x, c0.y, a0, alpha0 (the solver writes the step's start)
+  int* toi_hpos;                  // per contact: its TOI heap node, -1 when not in the heap
+  uint8_t* toi_cfl;               // per contact: island and persist flags of the TOI loop
+  int4* toi_heap;                 // per world: TOI heap nodes {toi bits, sub-steps, contact, -} from wc.x + 32 w
+  uint8_t* toi_bfl;               // per body: island flag of the TOI loop
+
   // events, status
   EventDev* events;
   int64_t event_cap;
@@ -226,6 +233,8 @@ void launch_bp_tail(const KernelArgs& a, int f0, int nf, int w0, int nw, size_t 
 void launch_contact_diff(const KernelArgs& a, int src, int dst, cudaStream_t s);
 size_t cub_temp_bytes(int nf);
 void launch_time_of_impact(const b2g_toi_input* in, int n, b2g_toi_output* out, cudaStream_t s);
+// b2World::SolveTOI for the active worlds flagged B2G_WF_CONTINUOUS, on the live contact list.
+void launch_solve_toi(const KernelArgs& a, int nw, cudaStream_t s);
 void launch_collide_pairs(const b2g_shape* sa, const float* xa, const b2g_shape* sb, const float* xb, int n,
                           b2g_manifold* out, cudaStream_t s);
 

@@ -1331,10 +1331,13 @@ __device__ __forceinline__ void iterate_world(Team& tm, const KernelArgs& a, int
     if (pc > 1) { m->points[1].normal_impulse = im.y; m->points[1].tangent_impulse = im.w; }
   }
 
-  // 8. integrate positions (b2_island.cpp:349-385); the buffer switches to positions
+  // 8. integrate positions (b2_island.cpp:349-385); the buffer switches to positions. Worlds with
+  //    continuous collision keep every body's position at the step's start (b2Sweep c0, a0)
+  const bool sweeps = a.sweep0 != nullptr && (wfl & B2G_WF_CONTINUOUS);
   for (int i = tid; i < nb; i += NT) {
     int bi = b0 + i;
     float4 p4 = a.pos[bi];
+    if (sweeps) a.sweep0[bi] = make_float4(p4.x, p4.y, p4.z, 0.0f);
     if (a.btype[bi] == B2G_STATIC || (sleepMode && !(BS[i].x & B2G_BS_AWAKE))) {
       if (bsm) bs[i] = p4;
       continue;

@@ -3402,6 +3402,7 @@ static void solveTOI(World* w, const Step& step) {
           if (!hasCollider(w->fixtures[e].shape.type, w->fixtures[pp].shape.type) &&
               !hasCollider(w->fixtures[pp].shape.type, w->fixtures[e].shape.type))
             continue;
+          if ((int)w->contacts.size() - nc == 32) continue;  // at most 32 made in one step
           w->contacts.push_back(makeContact(*w, ((uint64_t)(uint32_t)e << 32) | (uint32_t)pp));
           contactIsland.push_back(0);
           persist.push_back(1);
@@ -3540,10 +3541,12 @@ static void stepWorld(World* w, float dt, int vi, int pi) {
     }
     // integrate positions (b2_island.cpp:349-385)
     for (int i = 0; i < nb; ++i) {
+      // every body's position at the step's start, for continuous collision (b2Island::Solve
+      // stores it for the bodies it solves; the others have not moved since)
+      w->bodies[i].c0 = sb[i].c;
+      w->bodies[i].a0 = sb[i].a;
       if (w->bodies[i].type == 0 || !solved(i)) continue;
       V2 c = sb[i].c; float a = sb[i].a; V2 v = sb[i].v; float wv = sb[i].w;
-      w->bodies[i].c0 = c;  // b2Island::Solve keeps the step's start for continuous collision
-      w->bodies[i].a0 = a;
       V2 translation = h * v;
       if (dot(translation, translation) > kMaxTranslationSquared) {
         float ratio = kMaxTranslation / lengthOf(translation);

@@ -51,12 +51,13 @@ def _contact_key(c):
             c.tangent_speed, m.point_count, geo, pts)
 
 
-def _rollout(lib, orc, kind, n, seed=1, p0=1.0, p1=0.6, steps=60, vi=8, pi=3, gravity=(0.0, -10.0)):
+def _rollout(lib, orc, kind, n, seed=1, p0=1.0, p1=0.6, steps=60, vi=8, pi=3, gravity=(0.0, -10.0),
+             continuous=False):
     batch = G.Batch(lib, device=0)
     w = batch.add_world(*gravity)
-    batch.set_flags(w, allow_sleep=False, warm_starting=True, continuous=False)
+    batch.set_flags(w, allow_sleep=False, warm_starting=True, continuous=continuous)
     batch.scene(w, kind, seed=seed, n=n, p0=p0, p1=p1)
-    ow = ob.OracleWorld(orc, gravity, batch.bodies(w), batch.fixtures(w), batch.joints(w))
+    ow = ob.OracleWorld(orc, gravity, batch.bodies(w), batch.fixtures(w), batch.joints(w), continuous=continuous)
     for s in range(steps):
         batch.step(1 / 60, vi, pi)
         ow.step(1, 1 / 60, vi, pi)
@@ -79,6 +80,60 @@ def test_pyramid_rollout_bit_exact(lib, orc):
     # its full 256 steps
     nc = _rollout(lib, orc, G.SCENE_PYRAMID, 20, steps=256)
     assert nc > 300
+
+
+@pytest.mark.parametrize("n,seed", [(12, 1), (40, 4)])
+def test_bullets_rollout_bit_exact(lib, orc, n, seed):
+    """Continuous collision (b2World::SolveTOI on the device, one warp per world): bullets fired
+    and thrown at boxes, 120 steps, bodies bit for bit every step and contacts at the end; the
+    impacts change the outcome (the same rollout without continuous collision differs)."""
+    _rollout(lib, orc, G.SCENE_BULLETS, n, seed=seed, steps=120, continuous=True)
+    plain = ob.OracleWorld(orc, (0.0, -10.0), scene=(G.SCENE_BULLETS, seed, n, 0.0, 0.6))
+    ccd = ob.OracleWorld(orc, (0.0, -10.0), scene=(G.SCENE_BULLETS, seed, n, 0.0, 0.6), continuous=True)
+    plain.step(120, 1 / 60, 8, 3)
+    ccd.step(120, 1 / 60, 8, 3)
+    assert _state_bytes(plain.bodies()) != _state_bytes(ccd.bodies())
+
+
+def test_bullets_batch_sleep_events_step_io(lib, orc):
+    """A batch of a bullets world with sleeping allowed, a bullets world without and a pyramid
+    without continuous collision, stepped through b2g_step_io (transforms read after SolveTOI)
+    with listener events on: every world bit for bit like the oracle every step, awake flags
+    included, and the events (those of the sub-step impacts among them) equal per world."""
+    from test_oracle_pins import event_key
+
+    batch = G.Batch(lib, device=0)
+    specs = [(G.SCENE_BULLETS, 15, 2, True, True), (G.SCENE_BULLETS, 9, 6, False, True),
+             (G.SCENE_PYRAMID, 8, 1, False, False)]
+    worlds, ows = [], []
+    for kind, n, seed, sleep, cont in specs:
+        w = batch.add_world(0.0, -10.0)
+        batch.set_flags(w, allow_sleep=sleep, warm_starting=True, continuous=cont)
+        batch.scene(w, kind, seed=seed, n=n, p0=1.0, p1=0.6)
+        ow = ob.OracleWorld(orc, (0.0, -10.0), batch.bodies(w), batch.fixtures(w), batch.joints(w), continuous=cont)
+        ow.set_sleep(sleep)
+        ow.events_enable(True)
+        worlds.append(w)
+        ows.append(ow)
+    batch.events(enable=True)
+    nb = sum(len(batch.bodies(w)) for w in worlds)
+    xf = np.zeros((nb, 4), np.float32)
+    for s in range(100):
+        got_n = batch.step_io(0, 0, xf.ctypes.data, nb, 1 / 60, 8, 3)
+        assert got_n == nb
+        off = 0
+        for w, ow in zip(worlds, ows):
+            ow.step(1, 1 / 60, 8, 3)
+            g, o = batch.bodies(w), ow.bodies()
+            assert _state_bytes(g) == _state_bytes(o), f"world {w} step {s + 1}: {_first_diff(g, o)}"
+            assert _awake_flags(g) == _awake_flags(o), (w, s)
+            got_xf = xf[off:off + len(g)]
+            assert np.array_equal(got_xf, np.array([list(r.xf) for r in g], np.float32)), (w, s)
+            off += len(g)
+            got = [event_key(e) for e in batch.world_events(w)]
+            exp = [event_key(e) for e in ow.events()]
+            assert sorted(got) == sorted(exp), f"world {w} step {s + 1}: {len(got)} events against {len(exp)}"
+    batch.close()
 
 
 @pytest.mark.parametrize("n,seed,vi,pi", [(3, 9, 8, 3), (2, 17, 10, 4)])
