@@ -802,7 +802,7 @@ def main():
     ap.add_argument("--rays", type=int, default=1 << 20, help="rays of the world-query measurement (0: skip)")
     ap.add_argument("--sleep-worlds", type=int, default=256, help="worlds of the island-sleep measurement (0: skip)")
     ap.add_argument("--sleep-settle", type=int, default=480, help="steps before the island-sleep window")
-    ap.add_argument("--ccd-worlds", type=int, default=512, help="worlds of the continuous-collision measurement (0: skip)")
+    ap.add_argument("--ccd-worlds", type=int, default=4096, help="worlds of the continuous-collision measurement (0: skip)")
     ap.add_argument("--profile-window", action="store_true",
                     help="ncu case: settle --settle steps, then 2 steps inside the NVTX range 'profile'")
     ap.add_argument("--settle", type=int, default=250)

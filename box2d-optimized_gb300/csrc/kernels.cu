@@ -8,6 +8,8 @@
 //                  bottom-up bounds, stack traversal emitting the sorted, filtered pair list, and the
 //                  sorted diff of that list against the live contacts (b2BroadPhase::UpdateAndQuery +
 //                  b2ContactManager::QueryCallback / RemoveDeadContacts).
+//   k_solve_toi    continuous collision: b2World::SolveTOI for the worlds that run it, one warp per
+//                  world (src/dynamics/b2_world.cpp:859-1106)
 #include <cub/cub.cuh>
 #include <cuda/atomic>
 
