@@ -257,7 +257,7 @@ class Lib:
         "b2g_batch_world_params", "b2g_server_create", "b2g_server_destroy", "b2g_server_submit",
         "b2g_server_tick", "b2g_server_poll", "b2g_server_stats", "b2g_status_string",
         "b2g_last_error", "b2g_device_count", "b2g_query_aabb", "b2g_raycast_closest", "b2g_world_status",
-        "b2g_world_snapshot", "b2g_world_restore", "b2g_server_cancel", "b2g_body_set_awake",
+        "b2g_world_snapshot", "b2g_world_restore", "b2g_server_cancel", "b2g_body_set_awake", "b2g_body_set_bullet",
         "b2g_bodies_sleep_time_read", "b2g_world_get_flags", "b2g_server_batch", "b2g_step_begin",
         "b2g_step_poll", "b2g_step_end", "b2g_batch_stage", "b2g_server_set_builders", "b2g_batch_set_solver_waves", "b2g_batch_set_tree_rebuild_period",
         "b2g_batch_set_cluster_solve", "b2g_batch_get_cluster_solve", "b2g_events_drain_world",
@@ -327,6 +327,7 @@ class Lib:
             "b2g_batch_set_tree_rebuild_period": ([vp, i32], C.c_int),
             "b2g_batch_set_debug_checks": ([vp, i32], C.c_int),
             "b2g_body_set_awake": ([vp, i32, i32, i32], C.c_int),
+            "b2g_body_set_bullet": ([vp, i32, i32, i32], C.c_int),
             "b2g_world_get_flags": ([vp, i32, P(i32), P(i32), P(i32), P(i32)], C.c_int),
             "b2g_bodies_sleep_time_read": ([vp, i32, i32, i32, P(f32)], C.c_int),
             "b2g_world_snapshot": ([vp, i32, vp, C.c_uint64, P(C.c_uint64)], C.c_int),
@@ -481,6 +482,10 @@ class Batch:
     def set_awake(self, world, body, awake=True):
         """b2Body::SetAwake."""
         self.lib.check(self.lib.b2g_body_set_awake(self.h, world, body, int(awake)), "b2g_body_set_awake")
+
+    def set_bullet(self, world, body, bullet=True):
+        """b2Body::SetBullet: continuous collision with other dynamic bodies."""
+        self.lib.check(self.lib.b2g_body_set_bullet(self.h, world, body, int(bullet)), "b2g_body_set_bullet")
 
     def sleep_times(self, world):
         """The bodies' sleep timers (b2Body::m_sleepTime) in creation order."""

@@ -144,7 +144,7 @@ static KernelArgs make_args(Batch* b) {
   a.bstate = b->bstate.p; a.bwake = b->bwake.p; a.sl = b->sl.p; a.any_sleep = b->any_sleep ? 1 : 0;
   if (b->step_ccd) {
     a.sweep0 = b->sweep0.p; a.toi_hpos = b->toi_hpos.p; a.toi_cfl = b->toi_cfl.p; a.toi_heap = b->toi_heap.p;
-    a.toi_bfl = b->toi_bfl.p;
+    a.toi_bfl = b->toi_bfl.p; a.toi_moved = b->toi_moved.p;
   }
   a.any_sensor = b->any_sensor ? 1 : 0;
   a.shape = b->shape.p; a.fbody = b->fbody.p; a.fgroup = b->fgroup.p; a.fsensor = b->fsensor.p;
@@ -1127,6 +1127,7 @@ static int ensure_toi_scratch(Batch* b) {
   TRY(ensure(b, b->toi_hpos, (size_t)std::max<int64_t>(b->ccap, 1)));
   TRY(ensure(b, b->toi_cfl, (size_t)std::max<int64_t>(b->ccap, 1)));
   TRY(ensure(b, b->toi_heap, (size_t)std::max<int64_t>(b->ccap, 1) + 32 * (size_t)b->NW));
+  TRY(ensure(b, b->toi_moved, 1));
   return B2G_OK;
 }
 
@@ -1138,14 +1139,26 @@ static int toi_stage(Batch* b) {
   NvtxRange range("b2g.solve_toi");
   TRY(ensure_toi_scratch(b));  // the pair update may have grown the contact capacity
   CUDA_TRY(b, cudaMemsetAsync(b->counters.p + 1, 0, 4 * sizeof(unsigned long long), b->stream));
+  CUDA_TRY(b, cudaMemsetAsync(b->toi_moved.p, 0, sizeof(int), b->stream));
   KernelArgs a = step_args(b, b->last_dt, b->last_vi, b->last_pi);
   cudaEventRecord(b->ev[6], b->stream);
   launch_solve_toi(a, b->NW, b->stream);
   CUDA_TRY(b, cudaGetLastError());
   cudaEventRecord(b->ev[7], b->stream);
-  enqueue_broadphase(b, a, b->cur);
-  b->cur ^= 1;
-  return finish_step(b, b->cur ^ 1);
+  // no impact solved in any world: the contacts' boxes are those of the step's pair update
+  int* moved = reinterpret_cast<int*>(b->h_readback + 6);
+  CUDA_TRY(b, cudaMemcpyAsync(moved, b->toi_moved.p, sizeof(int), cudaMemcpyDeviceToHost, b->stream));
+  CUDA_TRY(b, cudaStreamSynchronize(b->stream));
+  if (*moved) {
+    enqueue_broadphase(b, a, b->cur);
+    b->cur ^= 1;
+  }
+  // the step's solver counters were read by the first readback
+  const int64_t touching = b->profile.touching, colors = b->profile.colors_max;
+  const int st = finish_step(b, b->cur ^ 1);
+  b->profile.touching = touching;
+  b->profile.colors_max = colors;
+  return st;
 }
 
 static int step_begin(Batch* b, float dt, int vi, int pi, const uint8_t* mask) {
@@ -1431,7 +1444,7 @@ B2G_API int b2g_batch_destroy(b2g_batch* b) {
   release(b, b->world_order); release(b, b->xf); release(b, b->pos); release(b, b->vel); release(b, b->massd);
   release(b, b->damp); release(b, b->force); release(b, b->lc); release(b, b->btype); release(b, b->bworld);
   release(b, b->bstate); release(b, b->bwake); release(b, b->sl);
-  release(b, b->sweep0); release(b, b->toi_hpos); release(b, b->toi_cfl); release(b, b->toi_heap); release(b, b->toi_bfl);
+  release(b, b->sweep0); release(b, b->toi_hpos); release(b, b->toi_cfl); release(b, b->toi_heap); release(b, b->toi_bfl); release(b, b->toi_moved);
   release(b, b->shape); release(b, b->fbody); release(b, b->fgroup); release(b, b->fsensor); release(b, b->fworld);
   release(b, b->ffilter); release(b, b->fmat); release(b, b->aabb); release(b, b->joints); release(b, b->nocollide);
   for (int k = 0; k < 2; ++k) {
@@ -2706,6 +2719,17 @@ B2G_API int b2g_body_set_awake(b2g_batch* b, int32_t world, int32_t body, int32_
     r.force[0] = r.force[1] = r.torque = 0.0f;
     w.sleepers = true;
   }
+  return B2G_OK;
+}
+
+B2G_API int b2g_body_set_bullet(b2g_batch* b, int32_t world, int32_t body, int32_t bullet) {
+  if (!world_index_ok(b, world) || body < 0 || body >= (int32_t)b->worlds[world].bodies.size())
+    return B2G_E_INVALID_ARG;
+  if (world < b->NW) TRY(begin_edit(b));
+  else b->tail_pack.valid = false;
+  b2g_body& r = b->worlds[world].bodies[body];
+  if (bullet) r.flags |= B2G_BODY_BULLET;
+  else r.flags &= ~B2G_BODY_BULLET;
   return B2G_OK;
 }
 

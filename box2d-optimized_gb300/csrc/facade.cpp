@@ -706,6 +706,13 @@ void b2Body::SetAwake(bool flag) {
 
 bool b2Body::IsAwake() const { return (m_world->BodyRecord(m_index).flags & B2G_BODY_AWAKE) != 0; }
 
+void b2Body::SetBullet(bool flag) {
+  m_world->m_lastStatus = b2g_body_set_bullet(m_world->m_batch, m_world->m_index, m_index, flag ? 1 : 0);
+  m_world->InvalidateCaches();
+}
+
+bool b2Body::IsBullet() const { return (m_world->BodyRecord(m_index).flags & B2G_BODY_BULLET) != 0; }
+
 bool b2Body::IsSleepingAllowed() const { return (m_world->BodyRecord(m_index).flags & B2G_BODY_AUTO_SLEEP) != 0; }
 
 b2Joint* b2World::CreateJoint(const b2JointDef* def) {

@@ -1167,6 +1167,7 @@ struct ToiWorld {
         }
       }
       solveIsland(nbI, ncI, minAlpha);
+      *a.toi_moved = 1;
       // reset the island flags, move the dynamic bodies' fixture boxes, refresh their contacts' TOIs
       for (int i = 0; i < nbI; ++i) {
         const int b = S.ib[i];

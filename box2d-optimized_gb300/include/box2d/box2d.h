@@ -14,8 +14,10 @@
 //  * Custom b2ContactFilter subclasses cannot run on the GPU: SetContactFilter with one makes the
 //    next Step fail (LastStatus() = B2G_E_INVALID_ARG, the world does not advance); the default
 //    filter (group / category / mask) always applies.
-//  * TOI (bullets) and particle systems are not part of this engine. Sleeping is (the world
-//    allows it by default, like the reference).
+//  * Continuous collision (SolveTOI) runs on the GPU for bullets and kinematic bodies, as in the
+//    reference (on by default); contacts it makes inside its loop are remade by the pair update
+//    after it. Particle systems are not part of this engine. Sleeping is (the world allows it by
+//    default, like the reference).
 //  * Sine/cosine inside the step come from a portable routine (identical on host and GPU), so
 //    trajectories agree with the reference to rounding, not bit for bit.
 #pragma once
@@ -442,8 +444,10 @@ class b2Body {
     return GetLinearVelocity() + b2Cross(GetAngularVelocity(), worldPoint - GetWorldCenter());
   }
   b2BodyType GetType() const { return m_type; }
-  void SetBullet(bool flag) { B2_NOT_USED(flag); }
-  bool IsBullet() const { return false; }
+  // b2Body::SetBullet / IsBullet (include/box2d/b2_body.h:701-716): continuous collision with
+  // other dynamic bodies
+  void SetBullet(bool flag);
+  bool IsBullet() const;
   void SetSleepingAllowed(bool flag) { B2_NOT_USED(flag); }
   bool IsSleepingAllowed() const;
   // b2Body::SetAwake / IsAwake (include/box2d/b2_body.h:719-746)

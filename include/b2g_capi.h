@@ -492,6 +492,9 @@ B2G_API int b2g_bodies_write(b2g_batch* b, int32_t world, int32_t first, int32_t
 /* b2Body::SetAwake (include/box2d/b2_body.h:719-740): awake = 0 puts the body to sleep (velocity,
  * force and torque cleared); a static body ignores it. */
 B2G_API int b2g_body_set_awake(b2g_batch* b, int32_t world, int32_t body, int32_t awake);
+/* b2Body::SetBullet (include/box2d/b2_body.h:701-711): the body takes part in continuous
+ * collision with other dynamic bodies (B2G_BODY_BULLET in b2g_body.flags). */
+B2G_API int b2g_body_set_bullet(b2g_batch* b, int32_t world, int32_t body, int32_t bullet);
 /* The bodies' sleep timers (b2Body::m_sleepTime, which the reference keeps private): for
  * checkpoint tooling and tests. */
 B2G_API int b2g_bodies_sleep_time_read(b2g_batch* b, int32_t world, int32_t first, int32_t n, float* out);

@@ -95,6 +95,35 @@ def test_bullets_rollout_bit_exact(lib, orc, n, seed):
     assert _state_bytes(plain.bodies()) != _state_bytes(ccd.bodies())
 
 
+def test_set_bullet_mid_rollout(lib, orc):
+    """b2Body::SetBullet through the C ABI: half the bullets of a bullets world lose the flag
+    after 4 steps (their impacts then go through the discrete step only) and the world steps on
+    bit for bit like the oracle loaded with the edited state; clearing the rest turns
+    SolveTOI off for the world (no bullet or kinematic body left)."""
+    batch = G.Batch(lib, device=0)
+    w = batch.add_world(0.0, -10.0)
+    batch.set_flags(w, allow_sleep=False, warm_starting=True, continuous=True)
+    batch.scene(w, G.SCENE_BULLETS, seed=5, n=16, p0=0.0, p1=0.6)
+    batch.step_n(4, 1 / 60, 8, 3)
+    bullets = [i for i, r in enumerate(batch.bodies(w)) if r.flags & G.BODY_BULLET]
+    assert len(bullets) == 16
+    for i in bullets[::2]:
+        batch.set_bullet(w, i, False)
+    assert [bool(batch.bodies(w)[i].flags & G.BODY_BULLET) for i in bullets] == [k % 2 == 1 for k in range(16)]
+    ow = ob.OracleWorld(orc, (0.0, -10.0), batch.bodies(w), batch.fixtures(w), batch.joints(w), batch.contacts(w),
+                        inv_dt0=60.0, continuous=True)
+    for s in range(60):
+        batch.step(1 / 60, 8, 3)
+        ow.step(1, 1 / 60, 8, 3)
+        g, o = batch.bodies(w), ow.bodies()
+        assert _state_bytes(g) == _state_bytes(o), f"step {s + 1}: {_first_diff(g, o)}"
+    for i in bullets[1::2]:
+        batch.set_bullet(w, i, False)
+    batch.step(1 / 60, 8, 3)
+    assert batch.profile().solve_toi == 0.0
+    batch.close()
+
+
 def test_bullets_batch_sleep_events_step_io(lib, orc):
     """A batch of a bullets world with sleeping allowed, a bullets world without and a pyramid
     without continuous collision, stepped through b2g_step_io (transforms read after SolveTOI)
