@@ -219,12 +219,18 @@ static int device_world_flags(const HostWorld& hw) {
   // SolveTOI finds times of impact only between two non-static bodies of which one is a bullet or
   // kinematic (b2Contact::CalculateTOI, src/dynamics/b2_contact.cpp:222-246): without such a body
   // it does nothing
-  if (hw.continuous)
-    for (const b2g_body& bd : hw.bodies)
-      if (bd.type == B2G_KINEMATIC || (bd.type == B2G_DYNAMIC && (bd.flags & B2G_BODY_BULLET))) {
-        f |= B2G_WF_CONTINUOUS;
-        break;
-      }
+  // (found once per upload: every change to a body reaches the device through one)
+  if (hw.continuous) {
+    if (hw.toi_bodies < 0) {
+      hw.toi_bodies = 0;
+      for (const b2g_body& bd : hw.bodies)
+        if (bd.type == B2G_KINEMATIC || (bd.type == B2G_DYNAMIC && (bd.flags & B2G_BODY_BULLET))) {
+          hw.toi_bodies = 1;
+          break;
+        }
+    }
+    if (hw.toi_bodies) f |= B2G_WF_CONTINUOUS;
+  }
   return f;
 }
 
@@ -310,6 +316,7 @@ int upload_all(Batch* b) {
     wb[w] = make_int4(NB, (int)hw.bodies.size(), NF, (int)hw.fixtures.size());
     wj[w] = make_int4(NJ, (int)hw.joints.size(), 0, 0);
     wg[w] = make_float4(hw.gx, hw.gy, hw.inv_dt0, 0.0f);
+    hw.toi_bodies = -1;
     wflags[w] = device_world_flags(hw);
     NB += (int)hw.bodies.size();
     NF += (int)hw.fixtures.size();
@@ -632,6 +639,7 @@ static int flush_tail(Batch* b, TailPack& P) {
     const HostWorld& hw = b->worlds[w];
     wb[w] = make_int4(b->h_body_off[w], (int)hw.bodies.size(), b->h_fix_off[w], (int)hw.fixtures.size());
     wj[w] = make_int4(b->h_joint_off[w], (int)hw.joints.size(), 0, 0);
+    hw.toi_bodies = -1;
     wflags[w] = device_world_flags(hw);
   }
   std::vector<int> order(NW);

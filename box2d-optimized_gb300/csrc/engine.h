@@ -114,6 +114,8 @@ struct HostWorld {
   float inv_dt0 = 0.0f;
   int flags = B2G_WF_WARM | B2G_WF_CLEAR_FORCES;
   bool allow_sleep = false, continuous = false;
+  // a bullet or kinematic body is present (1), absent (0), not known since the last upload (-1)
+  mutable int toi_bodies = -1;
   bool sleepers = false;  // bodies may be asleep although sleeping is not allowed (created asleep)
   std::vector<b2g_body> bodies;
   std::vector<float> body_sleep;  // b2Body::m_sleepTime per body

@@ -985,7 +985,7 @@ extern "C" B2G_API int b2g_scene_build(b2g_batch* b, int32_t world, int32_t kind
   else if (kind == B2G_SCENE_JOINTS) c = b2scenes::JointZoo(&w, n, seed);
   else if (kind == B2G_SCENE_SLIDERS) c = b2scenes::SliderRigs(&w, n, seed);
   else if (kind == B2G_SCENE_GEARS) c = b2scenes::GearRigs(&w, n, seed);
-  else if (kind == B2G_SCENE_BULLETS) c = b2scenes::Bullets(&w, n, seed);
+  else if (kind == B2G_SCENE_BULLETS) c = b2scenes::Bullets(&w, n, seed, p0 > 0.5f);
   else return B2G_E_INVALID_ARG;
   if (counts) { counts[0] = c.bodies; counts[1] = c.fixtures; counts[2] = c.joints; }
   return B2G_OK;

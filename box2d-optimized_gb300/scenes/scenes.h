@@ -338,8 +338,9 @@ inline Counts BatchWorld(b2World* world, uint32_t seed, int n) {
 // rests on the ground and a bullet (b2BodyDef::bullet; a circle of radius 0.1-0.25 m in even
 // lanes, a square of half-extent 0.1-0.25 m in odd ones, density 3) flies at it: fired
 // horizontally at 25-70 m/s from 7 m away, or, in every third lane, thrown down at it at
-// 25-70 m/s from 7 m above. Continuous collision resolves the impacts.
-inline Counts Bullets(b2World* world, int n, uint32_t seed) {
+// 25-70 m/s from 7 m above. With `kinematic`, every fourth lane drives a kinematic bar (0.3 x 1.2 m)
+// at its box at 15-40 m/s instead of a bullet. Continuous collision resolves the impacts.
+inline Counts Bullets(b2World* world, int n, uint32_t seed, bool kinematic = false) {
   Counts c;
   Rng rng(seed);
   b2BodyDef gd;
@@ -365,6 +366,19 @@ inline Counts Bullets(b2World* world, int n, uint32_t seed) {
     const float lateral = rng.uni(-0.4f, 0.4f);
     const float spin = rng.uni(-5.0f, 5.0f);
     const float size = rng.uni(0.1f, 0.25f);
+    if (kinematic && i % 4 == 3) {
+      b2BodyDef kd;
+      kd.type = b2_kinematicBody;
+      kd.position.Set(x0, half + lateral);
+      kd.linearVelocity.Set(0.5f * speed + 2.5f, 0.0f);
+      kd.angularVelocity = 0.2f * spin;
+      b2Body* bar = MakeBody(world, &kd);
+      b2PolygonShape shape;
+      shape.SetAsBox(0.15f, 0.6f);
+      MakeFixture(bar, &shape, 1.0f);
+      c.fixtures++;
+      continue;
+    }
     b2BodyDef bd;
     bd.type = b2_dynamicBody;
     bd.bullet = true;

@@ -603,7 +603,7 @@ B2G_API int b2g_pairs_static(const float* d_aabbs, int32_t n, uint64_t* d_pairs,
 #define B2G_SCENE_JOINTS 4      /* rigs of weld, wheel, motor, friction, mouse and pulley joints */
 #define B2G_SCENE_SLIDERS 5     /* rigs of distance and prismatic joints (n rigs) */
 #define B2G_SCENE_GEARS 6       /* rigs of gear joints (n rigs) */
-#define B2G_SCENE_BULLETS 7     /* bullets fired at boxes (n lanes), for continuous collision */
+#define B2G_SCENE_BULLETS 7     /* bullets fired at boxes (n lanes; p0 = 1: kinematic bars in every fourth), for continuous collision */
 B2G_API int b2g_scene_build(b2g_batch* b, int32_t world, int32_t kind, uint32_t seed, int32_t n,
                             float p0, float p1, int32_t* counts);
 B2G_API int b2g_batch_world_params(uint32_t seed, int32_t* n_bodies, float* gx, float* gy);

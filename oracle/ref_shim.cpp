@@ -331,7 +331,7 @@ void* ref_scene_world(int32_t kind, uint32_t seed, int32_t n, float p0, float p1
   else if (kind == B2G_SCENE_JOINTS) c = b2scenes::JointZoo(rw->world, n, seed);
   else if (kind == B2G_SCENE_SLIDERS) c = b2scenes::SliderRigs(rw->world, n, seed);
   else if (kind == B2G_SCENE_GEARS) c = b2scenes::GearRigs(rw->world, n, seed);
-  else if (kind == B2G_SCENE_BULLETS) c = b2scenes::Bullets(rw->world, n, seed);
+  else if (kind == B2G_SCENE_BULLETS) c = b2scenes::Bullets(rw->world, n, seed, p0 > 0.5f);
   if (counts) { counts[0] = c.bodies; counts[1] = c.fixtures; counts[2] = c.joints; }
   index_world(rw);
   return rw;

@@ -234,7 +234,7 @@ static bool build_scene(b2World* w, int32_t kind, uint32_t seed, int32_t n, floa
   else if (kind == B2G_SCENE_MIXED_DROP) c = b2scenes::MixedDrop(w, n, seed);
   else if (kind == B2G_SCENE_CHAINS) c = b2scenes::ChainsOverPile(w, n, 20, (int)p0, seed);
   else if (kind == B2G_SCENE_BATCH_WORLD) c = b2scenes::BatchWorld(w, seed, n);
-  else if (kind == B2G_SCENE_BULLETS) c = b2scenes::Bullets(w, n, seed);
+  else if (kind == B2G_SCENE_BULLETS) c = b2scenes::Bullets(w, n, seed, p0 > 0.5f);
   else return false;
   if (counts) {
     counts[0] = c.bodies;

@@ -82,14 +82,15 @@ def test_pyramid_rollout_bit_exact(lib, orc):
     assert nc > 300
 
 
-@pytest.mark.parametrize("n,seed", [(12, 1), (40, 4)])
-def test_bullets_rollout_bit_exact(lib, orc, n, seed):
+@pytest.mark.parametrize("n,seed,p0", [(12, 1, 0.0), (40, 4, 0.0), (24, 7, 1.0)])
+def test_bullets_rollout_bit_exact(lib, orc, n, seed, p0):
     """Continuous collision (b2World::SolveTOI on the device, one warp per world): bullets fired
-    and thrown at boxes, 120 steps, bodies bit for bit every step and contacts at the end; the
-    impacts change the outcome (the same rollout without continuous collision differs)."""
-    _rollout(lib, orc, G.SCENE_BULLETS, n, seed=seed, steps=120, continuous=True)
-    plain = ob.OracleWorld(orc, (0.0, -10.0), scene=(G.SCENE_BULLETS, seed, n, 0.0, 0.6))
-    ccd = ob.OracleWorld(orc, (0.0, -10.0), scene=(G.SCENE_BULLETS, seed, n, 0.0, 0.6), continuous=True)
+    and thrown at boxes (with p0 = 1 also kinematic bars driven through boxes), 120 steps, bodies
+    bit for bit every step and contacts at the end; the impacts change the outcome (the same
+    rollout without continuous collision differs)."""
+    _rollout(lib, orc, G.SCENE_BULLETS, n, seed=seed, p0=p0, steps=120, continuous=True)
+    plain = ob.OracleWorld(orc, (0.0, -10.0), scene=(G.SCENE_BULLETS, seed, n, p0, 0.6))
+    ccd = ob.OracleWorld(orc, (0.0, -10.0), scene=(G.SCENE_BULLETS, seed, n, p0, 0.6), continuous=True)
     plain.step(120, 1 / 60, 8, 3)
     ccd.step(120, 1 / 60, 8, 3)
     assert _state_bytes(plain.bodies()) != _state_bytes(ccd.bodies())

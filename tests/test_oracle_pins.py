@@ -123,15 +123,16 @@ def test_oracle_toi_replay_vs_golden(orc):
     assert changed >= 3
 
 
-@pytest.mark.parametrize("n,seed", [(12, 1), (12, 8), (30, 4)])
-def test_oracle_toi_replay_vs_reference_live(ref, orc, n, seed):
+@pytest.mark.parametrize("n,seed,p0", [(12, 1, 0.0), (12, 8, 0.0), (30, 4, 0.0), (16, 3, 1.0), (24, 7, 1.0)])
+def test_oracle_toi_replay_vs_reference_live(ref, orc, n, seed, p0):
     """b2World::SolveTOI against the oracle's restatement over 40 replayed steps of the bullets
-    scene (fired and thrown bullets, circles and squares), contacts exactly. The lanes of circle
+    scene (fired and thrown bullets, circles and squares; with p0 = 1 kinematic bars driven at
+    boxes in every fourth lane), contacts exactly. The lanes of circle
     bullets match bit for bit. In the lanes of square bullets a polygon-polygon contact made by
     the pair update just before the impact takes its fixture order (which shape is A) from the
     reference's broadphase tree, where the oracle's is canonical: the manifold's frame differs,
     and those lanes agree to 1e-5."""
-    rw = ob.RefWorld(ref, G.SCENE_BULLETS, seed=seed, n=n, p0=0.0, p1=0.6, continuous=True)
+    rw = ob.RefWorld(ref, G.SCENE_BULLETS, seed=seed, n=n, p0=p0, p1=0.6, continuous=True)
     fixtures = list(rw.fixtures())
     orc.orc_set_libm_trig(1)
     try:
