@@ -307,16 +307,20 @@ def ccd_bench(lib, dev, n_worlds, lanes, steps, cpu):
             nb += batch.scene(w, G.SCENE_BULLETS, seed=i + 1, n=lanes, p0=0.0, p1=0.0)[0]
         batch.step_timed(1, DT, VI, PI)  # upload and first contacts
         ms = batch.step_timed(steps, DT, VI, PI)
-        batch.step(DT, VI, PI)
+        batch.set_graphs(False)
+        batch.step(DT, VI, PI)  # one eager step for the TOI kernel's time
         p = batch.profile()
-        out[cont] = {"ms": ms / steps, "toi_ms": p.solve_toi, "step_ms": p.step, "nb": nb}
+        out[cont] = {"ms": ms / steps, "toi_ms": p.solve_toi, "nb": nb,
+                     "breakdown": {"step": p.step, "collide": p.collide, "solve": p.solve,
+                                   "pair_updates_and_toi": p.broadphase, "toi_kernel": p.solve_toi}}
         batch.close()
     nb = out[True]["nb"]
     res = {"value": nb * steps / (out[True]["ms"] * steps / 1e3), "unit": "body-steps/s",
            "ms_per_step": out[True]["ms"], "continuous_off_ms_per_step": out[False]["ms"],
            "toi_stage_ms": out[True]["toi_ms"],
+           "breakdown_ms": out[True]["breakdown"], "continuous_off_breakdown_ms": out[False]["breakdown"],
            "workload": f"{n_worlds} bullets worlds of {lanes} lanes ({nb} bodies), steps 2-{steps + 1}, "
-                       "continuous physics on (eager steps: SolveTOI and a second pair update)"}
+                       "continuous physics on (the step's graph holds SolveTOI and a second pair update)"}
     if cpu:
         import oracle_bind as ob  # noqa: PLC0415 - CPU baseline leg only
 

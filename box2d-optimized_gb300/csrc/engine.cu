@@ -144,7 +144,7 @@ static KernelArgs make_args(Batch* b) {
   a.bstate = b->bstate.p; a.bwake = b->bwake.p; a.sl = b->sl.p; a.any_sleep = b->any_sleep ? 1 : 0;
   if (b->step_ccd) {
     a.sweep0 = b->sweep0.p; a.toi_hpos = b->toi_hpos.p; a.toi_cfl = b->toi_cfl.p; a.toi_heap = b->toi_heap.p;
-    a.toi_bfl = b->toi_bfl.p; a.toi_moved = b->toi_moved.p;
+    a.toi_bfl = b->toi_bfl.p; a.toi_flags = b->toi_flags.p;
   }
   a.any_sensor = b->any_sensor ? 1 : 0;
   a.shape = b->shape.p; a.fbody = b->fbody.p; a.fgroup = b->fgroup.p; a.fsensor = b->fsensor.p;
@@ -947,6 +947,19 @@ static void enqueue_step(Batch* b, float dt, int vi, int pi, bool initial_bp, in
     if (capture_mode >= 0) enqueue_broadphase(b, a, src, capture_mode, b->NF, b->NW);
     else enqueue_broadphase(b, a, src);
     src ^= 1;
+    if (b->step_ccd) {
+      // b2World::SolveTOI (src/dynamics/b2_world.cpp:1152-1156) on the list the pair update made,
+      // then a pair update over the moved bodies' boxes (a refit: the forest covers every fixture)
+      b->cur = src;
+      KernelArgs t = step_args(b, dt, vi, pi);
+      cudaMemsetAsync(b->toi_flags.p, 0, 2 * sizeof(int), b->stream);
+      if (!captured) cudaEventRecord(b->ev[6], b->stream);
+      launch_solve_toi(t, b->NW, b->stream);
+      if (!captured) cudaEventRecord(b->ev[7], b->stream);
+      enqueue_broadphase(b, t, src, BP_REFIT, b->NF, b->NW);
+      if (!captured) bp_done(b, BP_REFIT);
+      src ^= 1;
+    }
   } else if (record_profile) {
     cudaEventRecord(b->ev[2], b->stream);
   }
@@ -1116,6 +1129,7 @@ static int capture_graphs(Batch* b, float dt, int vi, int pi) {
   b->graph_dt = dt;
   b->graph_vi = vi;
   b->graph_pi = pi;
+  b->graph_ccd = b->step_ccd;
   b->graph_version = b->layout_version;
   return B2G_OK;
 }
@@ -1130,24 +1144,28 @@ static double host_ms_since(std::chrono::steady_clock::time_point t0) {
 // for the device; step_end waits and reads the step's counters.
 // Scratch of the SolveTOI kernel for the current layout and contact capacity.
 static int ensure_toi_scratch(Batch* b) {
+  const void* before[6] = {b->sweep0.p, b->toi_bfl.p, b->toi_hpos.p, b->toi_cfl.p, b->toi_heap.p, b->toi_flags.p};
   TRY(ensure(b, b->sweep0, (size_t)std::max(b->NB, 1)));
   TRY(ensure(b, b->toi_bfl, (size_t)std::max(b->NB, 1)));
   TRY(ensure(b, b->toi_hpos, (size_t)std::max<int64_t>(b->ccap, 1)));
   TRY(ensure(b, b->toi_cfl, (size_t)std::max<int64_t>(b->ccap, 1)));
   TRY(ensure(b, b->toi_heap, (size_t)std::max<int64_t>(b->ccap, 1) + 32 * (size_t)b->NW));
-  TRY(ensure(b, b->toi_moved, 1));
+  TRY(ensure(b, b->toi_flags, 2));
+  const void* after[6] = {b->sweep0.p, b->toi_bfl.p, b->toi_hpos.p, b->toi_cfl.p, b->toi_heap.p, b->toi_flags.p};
+  for (int i = 0; i < 6; ++i)
+    if (before[i] != after[i]) b->layout_version++;  // captured graphs hold the old addresses
   return B2G_OK;
 }
 
-// The SolveTOI stage of a step (b2World::Step, src/dynamics/b2_world.cpp:1152-1156), after the
-// step's pair update has completed: the TOI kernel on the live list, then a second pair update
-// that moves the proxies of the bodies it moved and makes and drops their contacts (the
-// UpdateNoRebuild / Query / RemoveDeadContacts inside SolveTOI).
+// The SolveTOI stage of a step run on its own, after a pair update that had overflowed was redone
+// (a step normally runs it inside enqueue_step): the TOI kernel on the live list, then, when an
+// island moved bodies, a second pair update that moves their proxies and makes and drops their
+// contacts (the UpdateNoRebuild / Query / RemoveDeadContacts inside SolveTOI).
 static int toi_stage(Batch* b) {
   NvtxRange range("b2g.solve_toi");
   TRY(ensure_toi_scratch(b));  // the pair update may have grown the contact capacity
   CUDA_TRY(b, cudaMemsetAsync(b->counters.p + 1, 0, 4 * sizeof(unsigned long long), b->stream));
-  CUDA_TRY(b, cudaMemsetAsync(b->toi_moved.p, 0, sizeof(int), b->stream));
+  CUDA_TRY(b, cudaMemsetAsync(b->toi_flags.p, 0, 2 * sizeof(int), b->stream));
   KernelArgs a = step_args(b, b->last_dt, b->last_vi, b->last_pi);
   cudaEventRecord(b->ev[6], b->stream);
   launch_solve_toi(a, b->NW, b->stream);
@@ -1155,7 +1173,7 @@ static int toi_stage(Batch* b) {
   cudaEventRecord(b->ev[7], b->stream);
   // no impact solved in any world: the contacts' boxes are those of the step's pair update
   int* moved = reinterpret_cast<int*>(b->h_readback + 6);
-  CUDA_TRY(b, cudaMemcpyAsync(moved, b->toi_moved.p, sizeof(int), cudaMemcpyDeviceToHost, b->stream));
+  CUDA_TRY(b, cudaMemcpyAsync(moved, b->toi_flags.p, sizeof(int), cudaMemcpyDeviceToHost, b->stream));
   CUDA_TRY(b, cudaStreamSynchronize(b->stream));
   if (*moved) {
     enqueue_broadphase(b, a, b->cur);
@@ -1261,9 +1279,9 @@ static int step_begin(Batch* b, float dt, int vi, int pi, const uint8_t* mask) {
       b->step_ccd = (wflags[w] & B2G_WF_CONTINUOUS) && (wflags[w] & B2G_WF_ACTIVE) && !(wflags[w] & B2G_WF_RETIRED);
   if (b->step_ccd) TRY(ensure_toi_scratch(b));
   int entry = b->cur;
-  bool graph = b->use_graphs && !need_bp && !b->events_on && all_active && dt > 0.0f && !b->step_ccd;
+  bool graph = b->use_graphs && !need_bp && !b->events_on && all_active && dt > 0.0f;
   if (graph && (!b->graph_exec[0][0] || b->graph_version != b->layout_version || b->graph_dt != dt ||
-                b->graph_vi != vi || b->graph_pi != pi))
+                b->graph_vi != vi || b->graph_pi != pi || b->graph_ccd != b->step_ccd))
     TRY(capture_graphs(b, dt, vi, pi));
   if (need_bp) {
     // fixtures were added or bodies moved: find contacts first (b2_world.cpp:1113-1122), and
@@ -1281,8 +1299,9 @@ static int step_begin(Batch* b, float dt, int vi, int pi, const uint8_t* mask) {
     cudaEventRecord(b->ev[0], b->stream);
     CUDA_TRY(b, cudaGraphLaunch(b->graph_exec[mode][entry], b->stream));
     bp_done(b, mode);
+    if (b->step_ccd) bp_done(b, BP_REFIT);
     cudaEventRecord(b->ev[4], b->stream);
-    b->cur = entry ^ 1;
+    b->cur = b->step_ccd ? entry : entry ^ 1;  // a step with SolveTOI has two pair updates
     b->last_solve_buf = entry;
   } else {
     enqueue_step(b, dt, vi, pi, false, entry, true);
@@ -1305,12 +1324,20 @@ static int step_end(Batch* b) {
   }
   b->in_step = false;
   int live_before_last_bp = b->cur ^ 1;
+  bool toi_ran = true;
+  if (b->step_ccd) {
+    // the TOI kernel found the first pair update overflowed: both pair updates skipped their
+    // lists, the live list is the step's first, and the TOI stage runs once it is redone
+    int* flags = reinterpret_cast<int*>(b->h_readback + 6);
+    CUDA_TRY(b, cudaMemcpyAsync(flags, b->toi_flags.p, 2 * sizeof(int), cudaMemcpyDeviceToHost, b->stream));
+    CUDA_TRY(b, cudaStreamSynchronize(b->stream));
+    toi_ran = flags[1] != 0;
+    if (!toi_ran) live_before_last_bp = b->cur;
+  }
   int st = finish_step(b, live_before_last_bp);
   float t_toi = 0.0f;
-  if (st == B2G_OK && b->step_ccd) {
-    st = toi_stage(b);
-    cudaEventElapsedTime(&t_toi, b->ev[6], b->ev[7]);
-  }
+  if (st == B2G_OK && b->step_ccd && !toi_ran) st = toi_stage(b);
+  if (b->step_ccd && (!b->step_graph || !toi_ran)) cudaEventElapsedTime(&t_toi, b->ev[6], b->ev[7]);
   if (!b->step_graph) {
     float t_col = 0, t_sol = 0, t_bp = 0;
     cudaEventElapsedTime(&t_col, b->ev[0], b->ev[1]);
@@ -1452,7 +1479,7 @@ B2G_API int b2g_batch_destroy(b2g_batch* b) {
   release(b, b->world_order); release(b, b->xf); release(b, b->pos); release(b, b->vel); release(b, b->massd);
   release(b, b->damp); release(b, b->force); release(b, b->lc); release(b, b->btype); release(b, b->bworld);
   release(b, b->bstate); release(b, b->bwake); release(b, b->sl);
-  release(b, b->sweep0); release(b, b->toi_hpos); release(b, b->toi_cfl); release(b, b->toi_heap); release(b, b->toi_bfl); release(b, b->toi_moved);
+  release(b, b->sweep0); release(b, b->toi_hpos); release(b, b->toi_cfl); release(b, b->toi_heap); release(b, b->toi_bfl); release(b, b->toi_flags);
   release(b, b->shape); release(b, b->fbody); release(b, b->fgroup); release(b, b->fsensor); release(b, b->fworld);
   release(b, b->ffilter); release(b, b->fmat); release(b, b->aabb); release(b, b->joints); release(b, b->nocollide);
   for (int k = 0; k < 2; ++k) {

@@ -225,7 +225,8 @@ struct Batch {
   DBuf<uint8_t> toi_cfl;          // per contact slot: TOI island / persist flags
   DBuf<int4> toi_heap;            // contact slots + 32 per world: TOI heap nodes
   DBuf<uint8_t> toi_bfl;          // per body: TOI island flag
-  DBuf<int> toi_moved;            // one flag: some TOI island moved bodies in the last TOI stage
+  DBuf<int> toi_flags;            // [0] some TOI island moved bodies, [1] the TOI kernel ran
+  bool graph_ccd = false;         // the captured graphs include the TOI stage
   std::chrono::steady_clock::time_point step_t0;  // host time the step in flight began
 
   DBuf<b2g_shape> shape;

@@ -589,6 +589,7 @@ __global__ void k_pairs_emit(KernelArgs a, int n) {
   if (idx >= n) return;
   int f = a.bp_f0 + idx;
   if ((int64_t)a.poff[a.nf] > a.ccap) return;  // overflow: the host grows the buffers and redoes this pass
+  if (a.counters[B2G_CNT_OVERFLOW]) return;    // an earlier pair update of the step overflowed
   int64_t off = a.poff[f];
   int cnt = (int)(a.poff[f + 1] - off);
   if (cnt == 0) return;
@@ -631,7 +632,7 @@ __global__ void k_pairs_emit(KernelArgs a, int n) {
 
 __global__ void k_world_contacts(KernelArgs a, int nw) {
   int idx = blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= nw) return;
+  if (idx >= nw || a.counters[B2G_CNT_OVERFLOW]) return;
   int w = a.bp_w0 + idx;
   int4 wb = a.wb[w];
   int s = a.poff[wb.z], e = a.poff[wb.z + wb.w];
@@ -670,7 +671,7 @@ __global__ void k_contact_diff(KernelArgs a, int src, int dst) {
   int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   int64_t nnew = a.poff[a.nf];
   int64_t nold = (int64_t)a.counters[B2G_CNT_CONTACTS];
-  if (nnew > a.ccap || k >= nnew) return;
+  if (nnew > a.ccap || k >= nnew || a.counters[B2G_CNT_OVERFLOW]) return;
   uint64_t key = a.pairs[k];
   int64_t o;
   if (a.poff_old) {  // the live list's entries of this emitter
@@ -733,7 +734,7 @@ __global__ void k_contact_dead(KernelArgs a, int src) {
   int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   int64_t nnew = a.poff[a.nf];
   int64_t nold = (int64_t)a.counters[B2G_CNT_CONTACTS];
-  if (nnew > a.ccap || k >= nold) return;
+  if (nnew > a.ccap || k >= nold || a.counters[B2G_CNT_OVERFLOW]) return;
   uint64_t key = a.ckeyB[src][k];
   int e = (int)(key >> 32);
   int64_t lo = a.poff[e];
@@ -756,6 +757,7 @@ __global__ void k_contact_dead(KernelArgs a, int src) {
 
 // The new list becomes the live one, or the needed capacity is recorded for the host.
 __global__ void k_commit_contacts(KernelArgs a) {
+  if (a.counters[B2G_CNT_OVERFLOW]) return;  // kept from an earlier pair update of the step
   unsigned long long total = (unsigned long long)a.poff[a.nf];
   if ((int64_t)total > a.ccap) a.counters[B2G_CNT_OVERFLOW] = total;
   else a.counters[B2G_CNT_CONTACTS] = total;
@@ -1167,7 +1169,7 @@ struct ToiWorld {
         }
       }
       solveIsland(nbI, ncI, minAlpha);
-      *a.toi_moved = 1;
+      a.toi_flags[0] = 1;
       // reset the island flags, move the dynamic bodies' fixture boxes, refresh their contacts' TOIs
       for (int i = 0; i < nbI; ++i) {
         const int b = S.ib[i];
@@ -1234,8 +1236,11 @@ __global__ void __launch_bounds__(32) k_solve_toi(KernelArgs a) {
   __shared__ ToiSmem S;
   const int w = blockIdx.x;
   const int wf = a.wflags[w];
-  if (!(wf & B2G_WF_ACTIVE) || !(wf & B2G_WF_CONTINUOUS) || (wf & B2G_WF_RETIRED)) return;
-  if (a.counters[B2G_CNT_OVERFLOW]) return;  // the pair update was skipped: no live list to work on
+  // the pair update before this kernel skipped its list when it overflowed: nothing to work on,
+  // and the host redoes both after growing the buffers
+  const bool overflowed = a.counters[B2G_CNT_OVERFLOW] != 0;
+  if (w == 0 && threadIdx.x == 0 && !overflowed) a.toi_flags[1] = 1;
+  if (!(wf & B2G_WF_ACTIVE) || !(wf & B2G_WF_CONTINUOUS) || (wf & B2G_WF_RETIRED) || overflowed) return;
   const int lane = threadIdx.x;
   ToiWorld T(a, S);
   const int4 wb = a.wb[w];

@@ -133,7 +133,7 @@ struct KernelArgs {
   uint8_t* toi_cfl;               // per contact: island and persist flags of the TOI loop
   int4* toi_heap;                 // per world: TOI heap nodes {toi bits, sub-steps, contact, -} from wc.x + 32 w
   uint8_t* toi_bfl;               // per body: island flag of the TOI loop
-  int* toi_moved;                 // set to 1 when a TOI island moved bodies (their contacts need a pair update)
+  int* toi_flags;                 // [0] a TOI island moved bodies, [1] the TOI kernel ran (its pair update had not overflowed)
 
   // events, status
   EventDev* events;

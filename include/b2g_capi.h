@@ -328,9 +328,8 @@ B2G_API int b2g_world_count(b2g_batch* b, int32_t* out_n);
 /* b2World::SetGravity / SetAllowSleeping / SetWarmStarting / SetContinuousPhysics /
  * SetAutoClearForces, include/box2d/b2_world.h:195-235. With continuous physics on and a bullet
  * or kinematic body in the world, each step ends with b2World::SolveTOI (src/dynamics/
- * b2_world.cpp:859-1106) on the device; such a step is launched eagerly, not from a graph. The
- * world's default (b2g_world_add) is off; the b2World facade turns it on, as the reference's
- * constructor does. */
+ * b2_world.cpp:859-1106) on the device, followed by a second pair update. The world's default
+ * (b2g_world_add) is off; the b2World facade turns it on, as the reference's constructor does. */
 B2G_API int b2g_world_set_gravity(b2g_batch* b, int32_t world, float gx, float gy);
 B2G_API int b2g_world_set_flags(b2g_batch* b, int32_t world, int32_t allow_sleep,
                                 int32_t warm_starting, int32_t continuous, int32_t auto_clear_forces);

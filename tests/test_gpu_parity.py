@@ -683,16 +683,19 @@ def test_graph_replay_equals_eager(lib):
     assert out[0] == out[1]
 
 
-def test_pair_overflow_recovery_bit_exact(lib, orc):
+@pytest.mark.parametrize("kind,n,every,continuous", [(G.SCENE_PYRAMID, 12, 10, False), (G.SCENE_BULLETS, 20, 3, True)])
+def test_pair_overflow_recovery_bit_exact(lib, orc, kind, n, every, continuous):
     """Contact buffers far too small: every overflowing broadphase is redone with larger buffers
-    and the rollout still matches the oracle bit for bit."""
+    and the rollout still matches the oracle bit for bit. With continuous collision a step has two
+    pair updates around SolveTOI: an overflow of the first makes the TOI kernel stand aside and
+    the stage rerun after the redone update; an overflow of the second redoes only that one."""
     b = G.Batch(lib, device=0)
     w = b.add_world(0.0, -10.0)
-    b.set_flags(w)
-    b.scene(w, G.SCENE_PYRAMID, n=12, p0=1.0, p1=0.6)
-    ow = ob.OracleWorld(orc, (0.0, -10.0), b.bodies(w), b.fixtures(w), b.joints(w))
+    b.set_flags(w, continuous=continuous)
+    b.scene(w, kind, n=n, p0=1.0, p1=0.6)
+    ow = ob.OracleWorld(orc, (0.0, -10.0), b.bodies(w), b.fixtures(w), b.joints(w), continuous=continuous)
     for s in range(40):
-        if s % 10 == 0:
+        if s % every == 0:
             nc = b.sizes(w)[3]
             assert lib.b2g_debug_set_contact_capacity(b.h, max(nc, 1)) == 0
         b.step(1 / 60, 8, 3)
