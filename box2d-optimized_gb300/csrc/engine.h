@@ -226,6 +226,7 @@ struct Batch {
   DBuf<int4> toi_heap;            // contact slots + 32 per world: TOI heap nodes
   DBuf<uint8_t> toi_bfl;          // per body: TOI island flag
   DBuf<int> toi_flags;            // [0] some TOI island moved bodies, [1] the TOI kernel ran
+  DBuf<int> toi_adj;              // per-body contact and fixture lists of the TOI loop (four sections)
   bool graph_ccd = false;         // the captured graphs include the TOI stage
   std::chrono::steady_clock::time_point step_t0;  // host time the step in flight began
 

@@ -806,8 +806,56 @@ struct ToiWorld {
   int hn;
   bool sleepMode;
   int2 nocol;
+  int *boff, *blist, *foff, *flist;  // per-body contact / fixture lists (valid once `adj`)
+  bool adj;
 
   __device__ ToiWorld(const KernelArgs& a_, ToiSmem& S_) : a(a_), S(S_) {}
+
+  // Per-body lists of the live contacts and of the fixtures, each in ascending order: counts at
+  // off[A + 1], prefix sums (off[A + 1] = end of A's list, off[nb + 1] = the total), then a
+  // descending fill that moves off[A + 1] to the start of A's list: list A = [off[A + 1], off[A + 2]).
+  __device__ void buildLists(int* off, int* list, int n, bool contacts) {
+    for (int i = 0; i < nb + 2; ++i) off[i] = 0;
+    for (int k = 0; k < n; ++k) {
+      if (contacts) {
+        const int2 f = fix(k);
+        ++off[a.fbody[f.x] - b0 + 1];
+        ++off[a.fbody[f.y] - b0 + 1];
+      } else {
+        ++off[a.fbody[f0 + k] - b0 + 1];
+      }
+    }
+    for (int i = 1; i <= nb; ++i) off[i] += off[i - 1];
+    off[nb + 1] = off[nb];
+    for (int k = n - 1; k >= 0; --k) {
+      if (contacts) {
+        const int2 f = fix(k);
+        list[--off[a.fbody[f.x] - b0 + 1]] = k;
+        list[--off[a.fbody[f.y] - b0 + 1]] = k;
+      } else {
+        list[--off[a.fbody[f0 + k] - b0 + 1]] = k;
+      }
+    }
+  }
+  __device__ void ensureLists() {
+    if (adj) return;
+    buildLists(boff, blist, nc, true);
+    buildLists(foff, flist, nf, false);
+    adj = true;
+  }
+  // Calls fn(k) for body b's contacts in contact order (the live list's, then those made in the
+  // loop) until fn returns false; returns whether it ran to the end.
+  template <class F>
+  __device__ bool forContacts(int b, F&& fn) {
+    const int A = b - b0;
+    for (int j = boff[A + 1]; j < boff[A + 2]; ++j)
+      if (!fn(blist[j])) return false;
+    for (int m = 0; m < nmade; ++m) {
+      const int2 f = S.made[m].fix;
+      if ((a.fbody[f.x] == b || a.fbody[f.y] == b) && !fn(nc + m)) return false;
+    }
+    return true;
+  }
 
   // contact k of the world: its live slot below nc, else a contact made inside the loop
   __device__ int2 fix(int k) const { return k < nc ? a.cfix[c0 + k] : S.made[k - nc].fix; }
@@ -1137,19 +1185,19 @@ struct ToiWorld {
       a.toi_bfl[ia] = 1;
       a.toi_bfl[ib] = 1;
       setFl(mc, getFl(mc) | TOI_ISLAND);
+      ensureLists();
       for (int side = 0; side < 2; ++side) {
         const int body = side ? ib : ia;
         if (a.btype[body] != B2G_DYNAMIC) continue;
-        for (int ci = 0; ci < count(); ++ci) {
+        forContacts(body, [&](int ci) {
+          if (nbI == TOI_BODIES || ncI == TOI_CONTACTS) return false;
           const int2 f = fix(ci);
           const int ca = a.fbody[f.x], cb = a.fbody[f.y];
-          if (ca != body && cb != body) continue;
-          if (nbI == TOI_BODIES || ncI == TOI_CONTACTS) break;
           const uint32_t cf = getFl(ci);
-          if ((cf & TOI_ISLAND) || !(cf & TOI_PERSIST)) continue;
+          if ((cf & TOI_ISLAND) || !(cf & TOI_PERSIST)) return true;
           const int other = ca == body ? cb : ca;
-          if (a.btype[other] == B2G_DYNAMIC && !bullet(body) && !bullet(other)) continue;
-          if (a.fsensor[f.x] || a.fsensor[f.y]) continue;
+          if (a.btype[other] == B2G_DYNAMIC && !bullet(body) && !bullet(other)) return true;
+          if (a.fsensor[f.x] || a.fsensor[f.y]) return true;
           const float4 so = a.sweep0[other], po = a.pos[other];
           if (!a.toi_bfl[other]) advanceBody(other, minAlpha);
           updateContact(ci);
@@ -1158,15 +1206,16 @@ struct ToiWorld {
             a.sweep0[other] = so;
             a.pos[other] = po;
             syncXf(other);
-            continue;
+            return true;
           }
           setFl(ci, cf | TOI_ISLAND);
           S.ic[ncI++] = ci;
-          if (a.toi_bfl[other]) continue;
+          if (a.toi_bfl[other]) return true;
           a.toi_bfl[other] = 1;
           wake(other);
           S.ib[nbI++] = other;
-        }
+          return true;
+        });
       }
       solveIsland(nbI, ncI, minAlpha);
       a.toi_flags[0] = 1;
@@ -1175,35 +1224,37 @@ struct ToiWorld {
         const int b = S.ib[i];
         a.toi_bfl[b] = 0;
         if (a.btype[b] != B2G_DYNAMIC) continue;
-        for (int f = f0; f < f0 + nf; ++f)
-          if (a.fbody[f] == b) {
-            AABB bb = shapeAABB(a.shape[f], ldXf(a.xf, b));
-            a.aabb[f] = make_float4(bb.lo.x, bb.lo.y, bb.hi.x, bb.hi.y);
-          }
-        for (int ci = 0; ci < count(); ++ci) {
-          const int2 f = fix(ci);
-          if (a.fbody[f.x] != b && a.fbody[f.y] != b) continue;
+        const int A = b - b0;
+        for (int j = foff[A + 1]; j < foff[A + 2]; ++j) {
+          const int f = f0 + flist[j];
+          AABB bb = shapeAABB(a.shape[f], ldXf(a.xf, b));
+          a.aabb[f] = make_float4(bb.lo.x, bb.lo.y, bb.hi.x, bb.hi.y);
+        }
+        forContacts(b, [&](int ci) {
           if (getFl(ci) & TOI_PERSIST) {
             if (hpos(ci) == -1) insert(ci);
             else update(ci);
           }
           setFl(ci, 0);
-        }
+          return true;
+        });
       }
       // b2BroadPhase::Query with each moved fixture's box (b2ContactManager::QueryCallback)
       for (int i = 0; i < nbI; ++i) {
         const int b = S.ib[i];
         if (a.btype[b] != B2G_DYNAMIC) continue;
-        for (int f = f0; f < f0 + nf; ++f) {
-          if (a.fbody[f] != b) continue;
+        const int A = b - b0;
+        for (int j = foff[A + 1]; j < foff[A + 2]; ++j) {
+          const int f = f0 + flist[j];
           const float4 fb = a.aabb[f];
           for (int g = f0; g < f0 + nf; ++g) {
             if (a.fbody[g] == b || !aabb_overlap4(fb, a.aabb[g])) continue;
             int found = -1;
-            for (int ci = 0; ci < count() && found < 0; ++ci) {
+            forContacts(b, [&](int ci) {
               const int2 cf = fix(ci);
               if ((cf.x == f && cf.y == g) || (cf.x == g && cf.y == f)) found = ci;
-            }
+              return found < 0;
+            });
             if (found >= 0) {
               setFl(found, getFl(found) | TOI_PERSIST);
               if (hpos(found) == -1) insert(found);
@@ -1259,6 +1310,11 @@ __global__ void __launch_bounds__(32) k_solve_toi(KernelArgs a) {
   T.hn = 0;
   T.sleepMode = (wf & B2G_WF_SLEEPMODE) != 0;
   T.nocol = make_int2(wj.z, wj.w);
+  T.boff = a.toi_boff + wb.x + 2 * w;
+  T.foff = a.toi_foff + wb.x + 2 * w;
+  T.blist = a.toi_blist + 2 * (int64_t)wc.x;
+  T.flist = a.toi_flist + wb.z;
+  T.adj = false;
   if (T.nc == 0) return;
   for (int i = lane; i < T.nb; i += 32) {
     a.sweep0[T.b0 + i].w = 0.0f;

@@ -134,6 +134,9 @@ struct KernelArgs {
   int4* toi_heap;                 // per world: TOI heap nodes {toi bits, sub-steps, contact, -} from wc.x + 32 w
   uint8_t* toi_bfl;               // per body: island flag of the TOI loop
   int* toi_flags;                 // [0] a TOI island moved bodies, [1] the TOI kernel ran (its pair update had not overflowed)
+  // per-body contact and fixture lists of the TOI loop (built at a world's first impact):
+  // offsets from b0 + 2 w (nb + 2 per world), lists from 2 c0 (contacts) and f0 (fixtures)
+  int *toi_boff, *toi_blist, *toi_foff, *toi_flist;
 
   // events, status
   EventDev* events;
