@@ -798,6 +798,49 @@ struct ToiSmem {
   int ic[TOI_CONTACTS];
 };
 
+// b2Contact::CalculateTOI (src/dynamics/b2_contact.cpp:212-280) of the contact between fixtures
+// f.x and f.y with flags `cflags`: 1 unless both bodies are non-static (and awake in sleep-mode
+// worlds) and one is a bullet or kinematic; the sweeps are first put on the same alpha0 (which
+// advances the earlier one). Out of line, so that the TOI loop's state stays in registers.
+__device__ __noinline__ float contactTOI(const KernelArgs& a, int2 f, uint32_t cflags, bool sleepMode) {
+  if (a.fsensor[f.x] || a.fsensor[f.y] || !(cflags & B2G_CONTACT_ENABLED)) return 1.0f;
+  const int A = a.fbody[f.x], B = a.fbody[f.y];
+  const int tA = a.btype[A], tB = a.btype[B];
+  const int sA = a.bstate[A].x, sB = a.bstate[B].x;
+  const bool active = sleepMode ? ((sA & B2G_BS_AWAKE) && tA != B2G_STATIC && (sB & B2G_BS_AWAKE) && tB != B2G_STATIC)
+                                : (tA != B2G_STATIC && tB != B2G_STATIC);
+  if (!active) return 1.0f;
+  const bool collideA = (sA & B2G_BS_BULLET) || tA != B2G_DYNAMIC;
+  const bool collideB = (sB & B2G_BS_BULLET) || tB != B2G_DYNAMIC;
+  if (!collideA && !collideB) return 1.0f;
+  auto sweepOfBody = [&](int b) {
+    float4 s = a.sweep0[b], p = a.pos[b];
+    float2 l = a.lc[b];
+    Sweep o;
+    o.lc = mk(l.x, l.y);
+    o.c0 = mk(s.x, s.y);
+    o.c = mk(p.x, p.y);
+    o.a0 = s.z;
+    o.a = p.z;
+    o.alpha0 = s.w;
+    return o;
+  };
+  Sweep swA = sweepOfBody(A), swB = sweepOfBody(B);
+  float alpha0 = swA.alpha0;
+  if (swA.alpha0 < swB.alpha0) {
+    alpha0 = swB.alpha0;
+    sweepAdvance(swA, alpha0);
+    a.sweep0[A] = make_float4(swA.c0.x, swA.c0.y, swA.a0, swA.alpha0);
+  } else if (swB.alpha0 < swA.alpha0) {
+    alpha0 = swA.alpha0;
+    sweepAdvance(swB, alpha0);
+    a.sweep0[B] = make_float4(swB.c0.x, swB.c0.y, swB.a0, swB.alpha0);
+  }
+  float t;
+  const int state = timeOfImpact(a.shape[f.x], a.shape[f.y], swA, swB, 1.0f, &t);
+  return state == B2G_TOI_TOUCHING ? fmin2(alpha0 + (1.0f - alpha0) * t, 1.0f) : 1.0f;
+}
+
 struct ToiWorld {
   const KernelArgs& a;
   ToiSmem& S;
@@ -911,30 +954,7 @@ struct ToiWorld {
   }
 
   // b2Contact::CalculateTOI
-  __device__ __noinline__ float calcTOI(int k) {
-    const int2 f = fix(k);
-    if (a.fsensor[f.x] || a.fsensor[f.y] || !(flags(k) & B2G_CONTACT_ENABLED)) return 1.0f;
-    const int A = a.fbody[f.x], B = a.fbody[f.y];
-    const int tA = a.btype[A], tB = a.btype[B];
-    const bool active = sleepMode ? (awake(A) && tA != B2G_STATIC && awake(B) && tB != B2G_STATIC)
-                                  : (tA != B2G_STATIC && tB != B2G_STATIC);
-    if (!active) return 1.0f;
-    const bool collideA = bullet(A) || tA != B2G_DYNAMIC;
-    const bool collideB = bullet(B) || tB != B2G_DYNAMIC;
-    if (!collideA && !collideB) return 1.0f;
-    const float alA = a.sweep0[A].w, alB = a.sweep0[B].w;
-    float alpha0 = alA;
-    if (alA < alB) {
-      alpha0 = alB;
-      advanceSweep(A, alpha0);
-    } else if (alB < alA) {
-      alpha0 = alA;
-      advanceSweep(B, alpha0);
-    }
-    float t;
-    const int state = timeOfImpact(a.shape[f.x], a.shape[f.y], sweep(A), sweep(B), 1.0f, &t);
-    return state == B2G_TOI_TOUCHING ? fmin2(alpha0 + (1.0f - alpha0) * t, 1.0f) : 1.0f;
-  }
+  __device__ float calcTOI(int k) { return contactTOI(a, fix(k), flags(k), sleepMode); }
 
   // b2TOIMinHeap
   __device__ float key(int i) const { return __int_as_float(heap[i].x); }

@@ -51,95 +51,178 @@ struct SimplexCache {
 };
 
 // b2Simplex::GetMetric (b2_distance.cpp:248-271)
-B2G_HD float simplexMetric(const SimplexVertex* v, int count) {
-  if (count == 2) return lengthOf(v[0].w - v[1].w);
-  if (count == 3) return cross(v[1].w - v[0].w, v[2].w - v[0].w);
+B2G_HD float simplexMetric3(const SimplexVertex& v0, const SimplexVertex& v1, const SimplexVertex& v2, int count) {
+  if (count == 2) return lengthOf(v0.w - v1.w);
+  if (count == 3) return cross(v1.w - v0.w, v2.w - v0.w);
   return 0.0f;
 }
 
+// b2Simplex::Solve2 (b2_distance.cpp:284-321) on named vertices (kept in registers)
+B2G_HD void simplexSolve2r(SimplexVertex& v0, SimplexVertex& v1, int& count) {
+  V2 w1 = v0.w, w2 = v1.w;
+  V2 e12 = w2 - w1;
+  float d12_2 = -dot(w1, e12);
+  if (d12_2 <= 0.0f) {
+    v0.a = 1.0f;
+    count = 1;
+    return;
+  }
+  float d12_1 = dot(w2, e12);
+  if (d12_1 <= 0.0f) {
+    v1.a = 1.0f;
+    count = 1;
+    v0 = v1;
+    return;
+  }
+  float inv_d12 = 1.0f / (d12_1 + d12_2);
+  v0.a = d12_1 * inv_d12;
+  v1.a = d12_2 * inv_d12;
+  count = 2;
+}
+// b2Simplex::Solve3 (b2_distance.cpp:323-430) on named vertices
+B2G_HD void simplexSolve3r(SimplexVertex& v0, SimplexVertex& v1, SimplexVertex& v2, int& count) {
+  V2 w1 = v0.w, w2 = v1.w, w3 = v2.w;
+  V2 e12 = w2 - w1;
+  float w1e12 = dot(w1, e12);
+  float w2e12 = dot(w2, e12);
+  float d12_1 = w2e12;
+  float d12_2 = -w1e12;
+  V2 e13 = w3 - w1;
+  float w1e13 = dot(w1, e13);
+  float w3e13 = dot(w3, e13);
+  float d13_1 = w3e13;
+  float d13_2 = -w1e13;
+  V2 e23 = w3 - w2;
+  float w2e23 = dot(w2, e23);
+  float w3e23 = dot(w3, e23);
+  float d23_1 = w3e23;
+  float d23_2 = -w2e23;
+  float n123 = cross(e12, e13);
+  float d123_1 = n123 * cross(w2, w3);
+  float d123_2 = n123 * cross(w3, w1);
+  float d123_3 = n123 * cross(w1, w2);
+  if (d12_2 <= 0.0f && d13_2 <= 0.0f) {
+    v0.a = 1.0f;
+    count = 1;
+    return;
+  }
+  if (d12_1 > 0.0f && d12_2 > 0.0f && d123_3 <= 0.0f) {
+    float inv_d12 = 1.0f / (d12_1 + d12_2);
+    v0.a = d12_1 * inv_d12;
+    v1.a = d12_2 * inv_d12;
+    count = 2;
+    return;
+  }
+  if (d13_1 > 0.0f && d13_2 > 0.0f && d123_2 <= 0.0f) {
+    float inv_d13 = 1.0f / (d13_1 + d13_2);
+    v0.a = d13_1 * inv_d13;
+    v2.a = d13_2 * inv_d13;
+    count = 2;
+    v1 = v2;
+    return;
+  }
+  if (d12_1 <= 0.0f && d23_2 <= 0.0f) {
+    v1.a = 1.0f;
+    count = 1;
+    v0 = v1;
+    return;
+  }
+  if (d13_1 <= 0.0f && d23_1 <= 0.0f) {
+    v2.a = 1.0f;
+    count = 1;
+    v0 = v2;
+    return;
+  }
+  if (d23_1 > 0.0f && d23_2 > 0.0f && d123_1 <= 0.0f) {
+    float inv_d23 = 1.0f / (d23_1 + d23_2);
+    v1.a = d23_1 * inv_d23;
+    v2.a = d23_2 * inv_d23;
+    count = 2;
+    v0 = v2;
+    return;
+  }
+  float inv_d123 = 1.0f / (d123_1 + d123_2 + d123_3);
+  v0.a = d123_1 * inv_d123;
+  v1.a = d123_2 * inv_d123;
+  v2.a = d123_3 * inv_d123;
+  count = 3;
+}
+
+B2G_HD void simplexVertexAt(SimplexVertex& v, int iA, int iB, const b2g_shape& A, const Xf& xfA, const b2g_shape& B,
+                            const Xf& xfB) {
+  v.indexA = iA;
+  v.indexB = iB;
+  v.wA = mul(xfA, proxyVertex(A, iA));
+  v.wB = mul(xfB, proxyVertex(B, iB));
+  v.w = v.wB - v.wA;
+}
+
 // b2Distance without radii (useRadii = false), warm-started from and written back to `cache`.
-// Returns the distance between the witness points pA and pB.
+// Returns the distance between the witness points. The simplex's three vertices are named
+// values, not an indexed array, so that they stay in registers.
 B2G_HD float distanceCached(const b2g_shape& A, const Xf& xfA, const b2g_shape& B, const Xf& xfB,
                             SimplexCache& cache, V2* pA_out, V2* pB_out) {
-  SimplexVertex v[3];
+  SimplexVertex v0 = {}, v1 = {}, v2 = {};
   // ReadCache
   int count = cache.count;
-  for (int i = 0; i < count; ++i) {
-    v[i].indexA = cache.indexA[i];
-    v[i].indexB = cache.indexB[i];
-    v[i].wA = mul(xfA, proxyVertex(A, v[i].indexA));
-    v[i].wB = mul(xfB, proxyVertex(B, v[i].indexB));
-    v[i].w = v[i].wB - v[i].wA;
-    v[i].a = 0.0f;
-  }
+  if (count > 0) { simplexVertexAt(v0, cache.indexA[0], cache.indexB[0], A, xfA, B, xfB); v0.a = 0.0f; }
+  if (count > 1) { simplexVertexAt(v1, cache.indexA[1], cache.indexB[1], A, xfA, B, xfB); v1.a = 0.0f; }
+  if (count > 2) { simplexVertexAt(v2, cache.indexA[2], cache.indexB[2], A, xfA, B, xfB); v2.a = 0.0f; }
   if (count > 1) {
     float metric1 = cache.metric;
-    float metric2 = simplexMetric(v, count);
+    float metric2 = simplexMetric3(v0, v1, v2, count);
     if (metric2 < 0.5f * metric1 || 2.0f * metric1 < metric2 || metric2 < B2G_EPSILON) count = 0;
   }
   if (count == 0) {
-    v[0].indexA = 0;
-    v[0].indexB = 0;
-    v[0].wA = mul(xfA, proxyVertex(A, 0));
-    v[0].wB = mul(xfB, proxyVertex(B, 0));
-    v[0].w = v[0].wB - v[0].wA;
-    v[0].a = 1.0f;
+    simplexVertexAt(v0, 0, 0, A, xfA, B, xfB);
+    v0.a = 1.0f;
     count = 1;
   }
-  int saveA[3], saveB[3];
+  int sA0 = 0, sB0 = 0, sA1 = 0, sB1 = 0, sA2 = 0, sB2 = 0;
   for (int iter = 0; iter < 20;) {
     const int saveCount = count;
-    for (int i = 0; i < saveCount; ++i) {
-      saveA[i] = v[i].indexA;
-      saveB[i] = v[i].indexB;
-    }
-    if (count == 2) simplexSolve2(v, count);
-    else if (count == 3) simplexSolve3(v, count);
+    sA0 = v0.indexA; sB0 = v0.indexB;
+    sA1 = v1.indexA; sB1 = v1.indexB;
+    sA2 = v2.indexA; sB2 = v2.indexB;
+    if (count == 2) simplexSolve2r(v0, v1, count);
+    else if (count == 3) simplexSolve3r(v0, v1, v2, count);
     if (count == 3) break;
     V2 d;
     if (count == 1) {
-      d = -v[0].w;
+      d = -v0.w;
     } else {
-      V2 e12 = v[1].w - v[0].w;
-      float sgn = cross(e12, -v[0].w);
+      V2 e12 = v1.w - v0.w;
+      float sgn = cross(e12, -v0.w);
       d = sgn > 0.0f ? cross(1.0f, e12) : cross(e12, 1.0f);
     }
     if (lengthSq(d) < B2G_EPSILON * B2G_EPSILON) break;
-    SimplexVertex& nv = v[count];
-    nv.indexA = proxySupport(A, mulT(xfA.q, -d));
-    nv.wA = mul(xfA, proxyVertex(A, nv.indexA));
-    nv.indexB = proxySupport(B, mulT(xfB.q, d));
-    nv.wB = mul(xfB, proxyVertex(B, nv.indexB));
-    nv.w = nv.wB - nv.wA;
+    const int iA = proxySupport(A, mulT(xfA.q, -d));
+    const int iB = proxySupport(B, mulT(xfB.q, d));
+    if (count == 1) simplexVertexAt(v1, iA, iB, A, xfA, B, xfB);
+    else simplexVertexAt(v2, iA, iB, A, xfA, B, xfB);
     ++iter;
-    bool duplicate = false;
-    for (int i = 0; i < saveCount; ++i) {
-      if (nv.indexA == saveA[i] && nv.indexB == saveB[i]) {
-        duplicate = true;
-        break;
-      }
-    }
+    const bool duplicate = (saveCount > 0 && iA == sA0 && iB == sB0) || (saveCount > 1 && iA == sA1 && iB == sB1) ||
+                           (saveCount > 2 && iA == sA2 && iB == sB2);
     if (duplicate) break;
     ++count;
   }
   V2 pA, pB;
   if (count == 1) {
-    pA = v[0].wA;
-    pB = v[0].wB;
+    pA = v0.wA;
+    pB = v0.wB;
   } else if (count == 2) {
-    pA = v[0].a * v[0].wA + v[1].a * v[1].wA;
-    pB = v[0].a * v[0].wB + v[1].a * v[1].wB;
+    pA = v0.a * v0.wA + v1.a * v1.wA;
+    pB = v0.a * v0.wB + v1.a * v1.wB;
   } else {
-    pA = (v[0].a * v[0].wA + v[1].a * v[1].wA) + v[2].a * v[2].wA;
+    pA = (v0.a * v0.wA + v1.a * v1.wA) + v2.a * v2.wA;
     pB = pA;
   }
   // WriteCache
-  cache.metric = simplexMetric(v, count);
+  cache.metric = simplexMetric3(v0, v1, v2, count);
   cache.count = count;
-  for (int i = 0; i < count; ++i) {
-    cache.indexA[i] = v[i].indexA;
-    cache.indexB[i] = v[i].indexB;
-  }
+  cache.indexA[0] = v0.indexA; cache.indexB[0] = v0.indexB;
+  if (count > 1) { cache.indexA[1] = v1.indexA; cache.indexB[1] = v1.indexB; }
+  if (count > 2) { cache.indexA[2] = v2.indexA; cache.indexB[2] = v2.indexB; }
   if (pA_out) *pA_out = pA;
   if (pB_out) *pB_out = pB;
   return lengthOf(pA - pB);
