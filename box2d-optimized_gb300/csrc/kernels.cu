@@ -1019,6 +1019,7 @@ struct ToiWorld {
     nm.point_count = m.pointCount;
     nm.local_normal[0] = m.localNormal.x; nm.local_normal[1] = m.localNormal.y;
     nm.local_point[0] = m.localPoint.x; nm.local_point[1] = m.localPoint.y;
+#pragma unroll
     for (int j = 0; j < 2; ++j) {
       nm.points[j].local_point[0] = m.lp[j].x;
       nm.points[j].local_point[1] = m.lp[j].y;
@@ -1026,13 +1027,19 @@ struct ToiWorld {
       nm.points[j].normal_impulse = 0.0f;
       nm.points[j].tangent_impulse = 0.0f;
     }
-    for (int j = 0; j < m.pointCount; ++j)
-      for (int q = 0; q < old.point_count; ++q)
+#pragma unroll
+    for (int j = 0; j < 2; ++j) {
+      if (j >= m.pointCount) break;
+#pragma unroll
+      for (int q = 0; q < 2; ++q) {
+        if (q >= old.point_count) break;
         if (old.points[q].id == nm.points[j].id) {
           nm.points[j].normal_impulse = old.points[q].normal_impulse;
           nm.points[j].tangent_impulse = old.points[q].tangent_impulse;
           break;
         }
+      }
+    }
     *mp = nm;
     if (touching) fl |= B2G_CONTACT_TOUCHING;
     else fl &= ~B2G_CONTACT_TOUCHING;
