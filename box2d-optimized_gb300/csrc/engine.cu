@@ -148,6 +148,7 @@ static KernelArgs make_args(Batch* b) {
     const int64_t nbw = (int64_t)b->NB + 2 * (int64_t)b->NW;
     a.toi_boff = b->toi_adj.p; a.toi_foff = b->toi_adj.p + nbw; a.toi_blist = b->toi_adj.p + 2 * nbw;
     a.toi_flist = a.toi_blist + 2 * b->ccap;
+    a.toi_vc = b->toi_vc.p;
   }
   a.any_sensor = b->any_sensor ? 1 : 0;
   a.shape = b->shape.p; a.fbody = b->fbody.p; a.fgroup = b->fgroup.p; a.fsensor = b->fsensor.p;
@@ -1147,8 +1148,8 @@ static double host_ms_since(std::chrono::steady_clock::time_point t0) {
 // for the device; step_end waits and reads the step's counters.
 // Scratch of the SolveTOI kernel for the current layout and contact capacity.
 static int ensure_toi_scratch(Batch* b) {
-  const void* before[7] = {b->sweep0.p, b->toi_bfl.p, b->toi_hpos.p, b->toi_cfl.p, b->toi_heap.p, b->toi_flags.p,
-                           b->toi_adj.p};
+  const void* before[8] = {b->sweep0.p, b->toi_bfl.p, b->toi_hpos.p, b->toi_cfl.p, b->toi_heap.p, b->toi_flags.p,
+                           b->toi_adj.p, b->toi_vc.p};
   TRY(ensure(b, b->sweep0, (size_t)std::max(b->NB, 1)));
   TRY(ensure(b, b->toi_bfl, (size_t)std::max(b->NB, 1)));
   TRY(ensure(b, b->toi_hpos, (size_t)std::max<int64_t>(b->ccap, 1)));
@@ -1157,9 +1158,10 @@ static int ensure_toi_scratch(Batch* b) {
   TRY(ensure(b, b->toi_flags, 2));
   TRY(ensure(b, b->toi_adj, 2 * ((size_t)b->NB + 2 * (size_t)b->NW) + 2 * (size_t)std::max<int64_t>(b->ccap, 1) +
                                 (size_t)b->NF + 1));
-  const void* after[7] = {b->sweep0.p, b->toi_bfl.p, b->toi_hpos.p, b->toi_cfl.p, b->toi_heap.p, b->toi_flags.p,
-                          b->toi_adj.p};
-  for (int i = 0; i < 7; ++i)
+  TRY(ensure(b, b->toi_vc, 32 * (size_t)std::max(b->NW, 1)));
+  const void* after[8] = {b->sweep0.p, b->toi_bfl.p, b->toi_hpos.p, b->toi_cfl.p, b->toi_heap.p, b->toi_flags.p,
+                          b->toi_adj.p, b->toi_vc.p};
+  for (int i = 0; i < 8; ++i)
     if (before[i] != after[i]) b->layout_version++;  // captured graphs hold the old addresses
   return B2G_OK;
 }
@@ -1486,7 +1488,7 @@ B2G_API int b2g_batch_destroy(b2g_batch* b) {
   release(b, b->world_order); release(b, b->xf); release(b, b->pos); release(b, b->vel); release(b, b->massd);
   release(b, b->damp); release(b, b->force); release(b, b->lc); release(b, b->btype); release(b, b->bworld);
   release(b, b->bstate); release(b, b->bwake); release(b, b->sl);
-  release(b, b->sweep0); release(b, b->toi_hpos); release(b, b->toi_cfl); release(b, b->toi_heap); release(b, b->toi_bfl); release(b, b->toi_flags); release(b, b->toi_adj);
+  release(b, b->sweep0); release(b, b->toi_hpos); release(b, b->toi_cfl); release(b, b->toi_heap); release(b, b->toi_bfl); release(b, b->toi_flags); release(b, b->toi_adj); release(b, b->toi_vc);
   release(b, b->shape); release(b, b->fbody); release(b, b->fgroup); release(b, b->fsensor); release(b, b->fworld);
   release(b, b->ffilter); release(b, b->fmat); release(b, b->aabb); release(b, b->joints); release(b, b->nocollide);
   for (int k = 0; k < 2; ++k) {

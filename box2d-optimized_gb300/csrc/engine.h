@@ -227,6 +227,7 @@ struct Batch {
   DBuf<uint8_t> toi_bfl;          // per body: TOI island flag
   DBuf<int> toi_flags;            // [0] some TOI island moved bodies, [1] the TOI kernel ran
   DBuf<int> toi_adj;              // per-body contact and fixture lists of the TOI loop (four sections)
+  DBuf<VCDev> toi_vc;             // per world: the TOI island's contact constraints (32)
   bool graph_ccd = false;         // the captured graphs include the TOI stage
   std::chrono::steady_clock::time_point step_t0;  // host time the step in flight began
 

@@ -791,7 +791,6 @@ struct ToiMade {
   uint32_t fl;
 };
 struct ToiSmem {
-  VCDev vc[TOI_CONTACTS];
   ToiMade made[TOI_MADE];
   float4 P[TOI_BODIES], V[TOI_BODIES];
   int ib[TOI_BODIES];
@@ -851,6 +850,7 @@ struct ToiWorld {
   int2 nocol;
   int *boff, *blist, *foff, *flist;  // per-body contact / fixture lists (valid once `adj`)
   bool adj;
+  VCDev* vcs;  // the island's contact constraints (global scratch: TOI_CONTACTS per world)
 
   __device__ ToiWorld(const KernelArgs& a_, ToiSmem& S_) : a(a_), S(S_) {}
 
@@ -1125,7 +1125,7 @@ struct ToiWorld {
       const int2 f = fix(k);
       const int A = a.fbody[f.x], B = a.fbody[f.y];
       const int ia = islandIndex(A, nbI), ib = islandIndex(B, nbI);
-      prepareContact(S.vc[j], *man(k), mat(k), a.frad[f.x], a.frad[f.y], ia, ib, a.massd[A], a.massd[B], a.lc[A],
+      prepareContact(vcs[j], *man(k), mat(k), a.frad[f.x], a.frad[f.y], ia, ib, a.massd[A], a.massd[B], a.lc[A],
                      a.lc[B], S.P[ia], S.V[ia], S.P[ib], S.V[ib], 1.0f, false, k);
     }
   }
@@ -1140,7 +1140,7 @@ struct ToiWorld {
     prepare(nbI, ncI);
     for (int it = 0; it < 20; ++it) {  // b2TimeStep::positionIterations of the sub-step
       float minSep = 0.0f;
-      for (int j = 0; j < ncI; ++j) minSep = fmin2(minSep, solveTOIPosition(S.vc[j]));
+      for (int j = 0; j < ncI; ++j) minSep = fmin2(minSep, solveTOIPosition(vcs[j]));
       if (minSep >= -1.5f * B2G_LINEAR_SLOP) break;
     }
     for (int k = 0; k < 2; ++k) {
@@ -1149,7 +1149,7 @@ struct ToiWorld {
     }
     prepare(nbI, ncI);  // InitializeVelocityConstraints at the corrected positions
     for (int it = 0; it < a.vi; ++it)
-      for (int j = 0; j < ncI; ++j) solveContactVelocity(S.vc[j], S.V);
+      for (int j = 0; j < ncI; ++j) solveContactVelocity(vcs[j], S.V);
     for (int i = 0; i < nbI; ++i) {
       V2 c = mk(S.P[i].x, S.P[i].y), v = mk(S.V[i].x, S.V[i].y);
       float an = S.P[i].z, wv = S.V[i].z;
@@ -1173,7 +1173,7 @@ struct ToiWorld {
     }
     if (a.events_on)  // b2Island::Report (src/dynamics/b2_island.cpp:621-647)
       for (int j = 0; j < ncI; ++j) {
-        const VCDev& vc = S.vc[j];
+        const VCDev& vc = vcs[j];
         const int2 f = fix(S.ic[j]);
         float ni[2] = {vc.normalImpulse[0], vc.pointCount > 1 ? vc.normalImpulse[1] : 0.0f};
         float ti[2] = {vc.tangentImpulse[0], vc.pointCount > 1 ? vc.tangentImpulse[1] : 0.0f};
@@ -1310,7 +1310,7 @@ struct ToiWorld {
   }
 };
 
-__global__ void __launch_bounds__(32) k_solve_toi(KernelArgs a) {
+__global__ void __launch_bounds__(32, 27) k_solve_toi(KernelArgs a) {
   __shared__ ToiSmem S;
   const int w = blockIdx.x;
   const int wf = a.wflags[w];
@@ -1342,6 +1342,7 @@ __global__ void __launch_bounds__(32) k_solve_toi(KernelArgs a) {
   T.blist = a.toi_blist + 2 * (int64_t)wc.x;
   T.flist = a.toi_flist + wb.z;
   T.adj = false;
+  T.vcs = a.toi_vc + (int64_t)TOI_CONTACTS * w;
   if (T.nc == 0) return;
   for (int i = lane; i < T.nb; i += 32) {
     a.sweep0[T.b0 + i].w = 0.0f;

@@ -137,6 +137,7 @@ struct KernelArgs {
   // per-body contact and fixture lists of the TOI loop (built at a world's first impact):
   // offsets from b0 + 2 w (nb + 2 per world), lists from 2 c0 (contacts) and f0 (fixtures)
   int *toi_boff, *toi_blist, *toi_foff, *toi_flist;
+  VCDev* toi_vc;                  // per world: the TOI island's contact constraints (32)
 
   // events, status
   EventDev* events;
