@@ -54,6 +54,32 @@ def test_host_only_batch_builds_and_reads_back():
     b.close()
 
 
+def test_bullets_scene_and_set_bullet_on_the_host():
+    """The bullets scene on a host-only batch: a box and a bullet (B2G_BODY_BULLET) per lane,
+    kinematic bars instead of bullets in every fourth lane with p0 = 1; b2g_body_set_bullet sets
+    and clears the flag (b2Body::SetBullet) and rejects bad indices; the world's continuous flag
+    reads back as set (b2World::GetContinuousPhysics)."""
+    lib = G.Lib()
+    b = G.Batch(lib, device=G.HOST_ONLY)
+    w = b.add_world(0.0, -10.0)
+    b.set_flags(w, continuous=True)
+    b.scene(w, G.SCENE_BULLETS, seed=4, n=8, p0=1.0, p1=0.6)
+    bodies = b.bodies(w)
+    assert len(bodies) == 1 + 2 * 8
+    bullets = [i for i, r in enumerate(bodies) if r.flags & G.BODY_BULLET]
+    kinematic = [i for i, r in enumerate(bodies) if r.type == 1]
+    assert len(bullets) == 6 and len(kinematic) == 2
+    b.set_bullet(w, bullets[0], False)
+    b.set_bullet(w, 1, True)
+    now = b.bodies(w)
+    assert not now[bullets[0]].flags & G.BODY_BULLET and now[1].flags & G.BODY_BULLET
+    assert lib.lib.b2g_body_set_bullet(b.h, w, len(bodies), 1) == 1  # B2G_E_INVALID_ARG
+    flags = [C.c_int32() for _ in range(4)]
+    assert lib.lib.b2g_world_get_flags(b.h, w, *[C.byref(x) for x in flags]) == 0
+    assert flags[2].value == 1
+    b.close()
+
+
 def test_snapshot_round_trip_on_the_host():
     """A world's snapshot restores into an equal world (host-only batch: no device involved),
     and malformed blobs are rejected with INVALID_ARG."""
